@@ -1,0 +1,208 @@
+"""cpvulkan_gb300 — GB300 (sm_103a) Vulkan ICD for the draw hot path.
+
+The product is the native library ``_build/libcpvulkan_gb300.so`` (a Vulkan
+ICD loaded through ``_build/CPVulkan.json``). This module only locates and
+builds the native libraries and wraps the headless harness
+(``libcpv_harness.so``), which drives the ICD through Vulkan calls the way an
+application behind the Vulkan loader does.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(_HERE, "_build")
+ICD_PATH = os.path.join(BUILD_DIR, "libcpvulkan_gb300.so")
+HARNESS_PATH = os.path.join(BUILD_DIR, "libcpv_harness.so")
+MANIFEST_PATH = os.path.join(BUILD_DIR, "CPVulkan.json")
+
+# Scene configurations (include/cpv_harness.h).
+CUBE, HEIGHTFIELD, BLEND, BATCH, PROGRAM, SERVE = 1, 2, 3, 4, 5, 6
+# Shader programs (include/cpv/scene.h).
+PROGRAM_CUBE, PROGRAM_TEXLIT, PROGRAM_FLATQUAD, PROGRAM_MESHPC, PROGRAM_DISCARD, PROGRAM_NOPERSP = range(6)
+
+VK_FORMAT_D16_UNORM = 124
+VK_FORMAT_D32_SFLOAT = 126
+VK_FORMAT_D32_SFLOAT_S8_UINT = 130
+VK_SUCCESS = 0
+
+
+def build():
+    """Compiles the native libraries (nvcc/g++, sm_103a) if sources changed."""
+    from . import build as _b
+    return _b.build()
+
+
+class SceneHeader(ctypes.Structure):
+    """Leading fields of cpv_scene (include/cpv/scene.h)."""
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("color_format", ctypes.c_uint32),
+                ("depth_format", ctypes.c_uint32)]
+
+
+def depth_texel_bytes(fmt):
+    return {0: 0, VK_FORMAT_D16_UNORM: 2, VK_FORMAT_D32_SFLOAT: 4, VK_FORMAT_D32_SFLOAT_S8_UINT: 8}[fmt]
+
+
+_harness = None
+
+
+def harness():
+    """Loads libcpv_harness.so (building it first when missing)."""
+    global _harness
+    if _harness is not None:
+        return _harness
+    if not os.path.exists(HARNESS_PATH):
+        build()
+    h = ctypes.CDLL(HARNESS_PATH)
+    vp, u32, u64, cp = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_char_p
+    h.cpvh_scene_create.restype = vp
+    h.cpvh_scene_create.argtypes = [u32, u64, ctypes.POINTER(u64), u32]
+    h.cpvh_scene_destroy.argtypes = [vp]
+    h.cpvh_scene_set_frame.argtypes = [vp, u32]
+    h.cpvh_scene_triangles.restype = u64
+    h.cpvh_scene_triangles.argtypes = [vp]
+    h.cpvh_open.restype = vp
+    h.cpvh_open.argtypes = [cp, cp, u32]
+    h.cpvh_close.argtypes = [vp]
+    h.cpvh_renderer_create.restype = vp
+    h.cpvh_renderer_create.argtypes = [vp, vp, cp, u32]
+    h.cpvh_renderer_destroy.argtypes = [vp]
+    h.cpvh_compile_pipelines.restype = ctypes.c_int
+    h.cpvh_compile_pipelines.argtypes = [vp, vp, cp, u32]
+    h.cpvh_render.restype = ctypes.c_int
+    h.cpvh_render.argtypes = [vp, u32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    h.cpvh_render_e2e.restype = ctypes.c_int
+    h.cpvh_render_e2e.argtypes = [vp, u32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(u64), ctypes.POINTER(u64)]
+    h.cpvh_renderer_update.restype = ctypes.c_int
+    h.cpvh_renderer_update.argtypes = [vp]
+    h.cpvh_readback.restype = ctypes.c_int
+    h.cpvh_readback.argtypes = [vp, vp, vp]
+    h.cpvh_queue.restype = vp
+    h.cpvh_queue.argtypes = [vp]
+    h.cpvh_last_error.restype = cp
+    _harness = h
+    return h
+
+
+class Scene:
+    """A seeded scene owned by the harness (plain-data cpv_scene)."""
+
+    def __init__(self, config, seed=1, params=()):
+        h = harness()
+        arr = (ctypes.c_uint64 * max(1, len(params)))(*[int(p) for p in params])
+        self.ptr = h.cpvh_scene_create(config, seed, arr, len(params))
+        if not self.ptr:
+            raise ValueError("unknown scene configuration %r" % config)
+        hdr = SceneHeader.from_address(self.ptr)
+        self.width, self.height = hdr.width, hdr.height
+        self.color_format, self.depth_format = hdr.color_format, hdr.depth_format
+        self.config = config
+
+    @property
+    def triangles(self):
+        return harness().cpvh_scene_triangles(self.ptr)
+
+    def set_frame(self, frame):
+        harness().cpvh_scene_set_frame(self.ptr, frame)
+
+    def close(self):
+        if self.ptr:
+            harness().cpvh_scene_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """An ICD loaded the loader's way, with one device and queue."""
+
+    def __init__(self, icd_path=ICD_PATH):
+        h = harness()
+        err = ctypes.create_string_buffer(1024)
+        self.ptr = h.cpvh_open(icd_path.encode(), err, len(err))
+        if not self.ptr:
+            raise RuntimeError("cannot open ICD: " + err.value.decode(errors="replace"))
+
+    def compile_pipelines(self, scene):
+        err = ctypes.create_string_buffer(4096)
+        r = harness().cpvh_compile_pipelines(self.ptr, scene.ptr, err, len(err))
+        if r != VK_SUCCESS:
+            raise RuntimeError("pipeline compilation failed (%d): %s" % (r, err.value.decode(errors="replace")))
+
+    @property
+    def queue(self):
+        return harness().cpvh_queue(self.ptr)
+
+    def close(self):
+        if self.ptr:
+            harness().cpvh_close(self.ptr)
+            self.ptr = None
+
+
+class Renderer:
+    """All Vulkan objects of one scene plus its recorded frame."""
+
+    def __init__(self, ctx, scene):
+        h = harness()
+        err = ctypes.create_string_buffer(4096)
+        self.scene = scene
+        self.ctx = ctx
+        self.ptr = h.cpvh_renderer_create(ctx.ptr, scene.ptr, err, len(err))
+        if not self.ptr:
+            raise RuntimeError("renderer creation failed: " + err.value.decode(errors="replace"))
+
+    def render(self, frames=1, latencies=False):
+        """Submits the frame `frames` times. Returns (device_ms, latencies_ms or None)."""
+        dev = ctypes.c_double(0.0)
+        lat = (ctypes.c_double * frames)() if latencies else None
+        r = harness().cpvh_render(self.ptr, frames, ctypes.byref(dev), lat)
+        if r != VK_SUCCESS:
+            raise RuntimeError("render failed (%d): %s" % (r, harness().cpvh_last_error().decode()))
+        return dev.value, (np.array(lat[:]) if latencies else None)
+
+    def render_e2e(self, frames=1):
+        total = ctypes.c_double(0.0)
+        h2d, d2h = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        r = harness().cpvh_render_e2e(self.ptr, frames, ctypes.byref(total), ctypes.byref(h2d), ctypes.byref(d2h))
+        if r != VK_SUCCESS:
+            raise RuntimeError("end-to-end render failed (%d)" % r)
+        return total.value, h2d.value, d2h.value
+
+    def update(self):
+        r = harness().cpvh_renderer_update(self.ptr)
+        if r != VK_SUCCESS:
+            raise RuntimeError("update failed (%d)" % r)
+
+    def readback(self):
+        s = self.scene
+        color = np.zeros((s.height, s.width, 4), np.uint8)
+        dsz = depth_texel_bytes(s.depth_format)
+        depth = np.zeros((s.height, s.width, dsz), np.uint8) if dsz else None
+        r = harness().cpvh_readback(self.ptr, color.ctypes.data, depth.ctypes.data if depth is not None else None)
+        if r != VK_SUCCESS:
+            raise RuntimeError("readback failed (%d)" % r)
+        return color, depth
+
+    def close(self):
+        if self.ptr:
+            harness().cpvh_renderer_destroy(self.ptr)
+            self.ptr = None
+
+
+def device_available():
+    """True when the ICD can create a CUDA context (a GB300 is present)."""
+    if not os.path.exists(ICD_PATH):
+        build()
+    lib = ctypes.CDLL(ICD_PATH)
+    return bool(lib.cpv_device_available())
+
+
+def kernel_launches():
+    lib = ctypes.CDLL(ICD_PATH)
+    lib.cpv_kernel_launches.restype = ctypes.c_uint64
+    return lib.cpv_kernel_launches()

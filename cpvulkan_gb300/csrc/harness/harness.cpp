@@ -1,0 +1,934 @@
+// harness.cpp — headless Vulkan application over an ICD shared object.
+//
+// Loads the ICD as the Khronos loader would (dlopen, interface negotiation,
+// vk_icdGetInstanceProcAddr, dispatch-word check and overwrite) and renders
+// cpv_scene descriptions through Vulkan calls only: the role the LunarG
+// samples play for the reference (Samples/15-draw_cube,
+// Samples/utils/util_init.cpp), without a window system.
+#include <dlfcn.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../../include/cpv/vk_subset.h"
+#include "../../../include/cpv_harness.h"
+
+extern "C" const uint32_t* cpvh_spirv(uint32_t program, uint32_t stage, size_t* bytes);
+
+namespace {
+
+thread_local std::string g_err;
+
+#define CPVH_FN(name) PFN_##name name = nullptr;
+struct Fns {
+    CPVH_FN(vkGetInstanceProcAddr)
+    CPVH_FN(vkGetDeviceProcAddr)
+    CPVH_FN(vkCreateInstance)
+    CPVH_FN(vkDestroyInstance)
+    CPVH_FN(vkEnumeratePhysicalDevices)
+    CPVH_FN(vkGetPhysicalDeviceMemoryProperties)
+    CPVH_FN(vkGetPhysicalDeviceQueueFamilyProperties)
+    CPVH_FN(vkCreateDevice)
+    CPVH_FN(vkDestroyDevice)
+    CPVH_FN(vkGetDeviceQueue)
+    CPVH_FN(vkDeviceWaitIdle)
+    CPVH_FN(vkAllocateMemory)
+    CPVH_FN(vkFreeMemory)
+    CPVH_FN(vkMapMemory)
+    CPVH_FN(vkUnmapMemory)
+    CPVH_FN(vkCreateBuffer)
+    CPVH_FN(vkDestroyBuffer)
+    CPVH_FN(vkGetBufferMemoryRequirements)
+    CPVH_FN(vkBindBufferMemory)
+    CPVH_FN(vkCreateImage)
+    CPVH_FN(vkDestroyImage)
+    CPVH_FN(vkGetImageMemoryRequirements)
+    CPVH_FN(vkBindImageMemory)
+    CPVH_FN(vkCreateImageView)
+    CPVH_FN(vkDestroyImageView)
+    CPVH_FN(vkCreateSampler)
+    CPVH_FN(vkDestroySampler)
+    CPVH_FN(vkCreateShaderModule)
+    CPVH_FN(vkDestroyShaderModule)
+    CPVH_FN(vkCreatePipelineCache)
+    CPVH_FN(vkDestroyPipelineCache)
+    CPVH_FN(vkCreateGraphicsPipelines)
+    CPVH_FN(vkDestroyPipeline)
+    CPVH_FN(vkCreatePipelineLayout)
+    CPVH_FN(vkDestroyPipelineLayout)
+    CPVH_FN(vkCreateDescriptorSetLayout)
+    CPVH_FN(vkDestroyDescriptorSetLayout)
+    CPVH_FN(vkCreateDescriptorPool)
+    CPVH_FN(vkDestroyDescriptorPool)
+    CPVH_FN(vkAllocateDescriptorSets)
+    CPVH_FN(vkUpdateDescriptorSets)
+    CPVH_FN(vkCreateRenderPass)
+    CPVH_FN(vkDestroyRenderPass)
+    CPVH_FN(vkCreateFramebuffer)
+    CPVH_FN(vkDestroyFramebuffer)
+    CPVH_FN(vkCreateCommandPool)
+    CPVH_FN(vkDestroyCommandPool)
+    CPVH_FN(vkAllocateCommandBuffers)
+    CPVH_FN(vkBeginCommandBuffer)
+    CPVH_FN(vkEndCommandBuffer)
+    CPVH_FN(vkCmdBindPipeline)
+    CPVH_FN(vkCmdBindDescriptorSets)
+    CPVH_FN(vkCmdBindIndexBuffer)
+    CPVH_FN(vkCmdBindVertexBuffers)
+    CPVH_FN(vkCmdDraw)
+    CPVH_FN(vkCmdDrawIndexed)
+    CPVH_FN(vkCmdCopyBuffer)
+    CPVH_FN(vkCmdCopyBufferToImage)
+    CPVH_FN(vkCmdCopyImageToBuffer)
+    CPVH_FN(vkCmdPipelineBarrier)
+    CPVH_FN(vkCmdPushConstants)
+    CPVH_FN(vkCmdBeginRenderPass)
+    CPVH_FN(vkCmdEndRenderPass)
+    CPVH_FN(vkQueueSubmit)
+    CPVH_FN(vkQueueWaitIdle)
+    CPVH_FN(vkCreateFence)
+    CPVH_FN(vkDestroyFence)
+    CPVH_FN(vkResetFences)
+    CPVH_FN(vkWaitForFences)
+};
+#undef CPVH_FN
+
+typedef int (*PFN_cpv_queue_record)(VkQueue, uint32_t);
+typedef double (*PFN_cpv_queue_elapsed_ms)(VkQueue, uint32_t, uint32_t);
+typedef const char* (*PFN_cpv_last_error)(void);
+
+// What a loader keeps in the first word of dispatchable objects.
+struct LoaderDispatch {
+    const void* table;
+} g_loader_dispatch{&g_loader_dispatch};
+
+}  // namespace
+
+struct cpvh_context {
+    void* lib = nullptr;
+    Fns f;
+    VkInstance instance = nullptr;
+    VkPhysicalDevice physical = nullptr;
+    VkDevice device = nullptr;
+    VkQueue queue = nullptr;
+    VkPhysicalDeviceMemoryProperties mem{};
+    VkPipelineCache cache = nullptr;
+    PFN_cpv_queue_record record = nullptr;
+    PFN_cpv_queue_elapsed_ms elapsed = nullptr;
+    PFN_cpv_last_error icd_error = nullptr;
+};
+
+namespace {
+
+std::string icd_error(cpvh_context* c) { return c && c->icd_error ? c->icd_error() : ""; }
+
+bool check_dispatch(void* handle) {
+    // Loader contract: the ICD's dispatchable object begins with
+    // ICD_LOADER_MAGIC; the loader then stores its dispatch table there.
+    uintptr_t* word = reinterpret_cast<uintptr_t*>(handle);
+    if (*word != ICD_LOADER_MAGIC) return false;
+    *word = reinterpret_cast<uintptr_t>(&g_loader_dispatch);
+    return true;
+}
+
+uint32_t find_memory_type(const cpvh_context* c, uint32_t bits, bool host_visible) {
+    for (uint32_t i = 0; i < c->mem.memoryTypeCount; i++) {
+        if (!(bits & (1u << i))) continue;
+        const bool hv = (c->mem.memoryTypes[i].propertyFlags & VK_MEMORY_PROPERTY_HOST_VISIBLE_BIT) != 0;
+        if (hv == host_visible) return i;
+    }
+    for (uint32_t i = 0; i < c->mem.memoryTypeCount; i++)
+        if (bits & (1u << i)) return i;
+    return 0;
+}
+
+struct BufferAlloc {
+    VkBuffer buffer = nullptr;
+    VkDeviceMemory memory = nullptr;
+    VkDeviceSize size = 0;
+};
+
+struct ImageAlloc {
+    VkImage image = nullptr;
+    VkDeviceMemory memory = nullptr;
+    VkImageView view = nullptr;
+};
+
+}  // namespace
+
+struct cpvh_renderer {
+    cpvh_context* ctx = nullptr;
+    const cpv_scene* scene = nullptr;
+    BufferAlloc vertex, index, uniform, staging, readback;
+    ImageAlloc colour, depth, texture;
+    VkSampler sampler = nullptr;
+    VkRenderPass pass = nullptr;
+    VkFramebuffer fb = nullptr;
+    VkDescriptorSetLayout set_layout = nullptr;
+    VkDescriptorPool pool = nullptr;
+    VkDescriptorSet set = nullptr;
+    VkPipelineLayout layout = nullptr;
+    std::vector<VkShaderModule> modules;
+    std::vector<VkPipeline> pipelines;
+    VkCommandPool cmd_pool = nullptr;
+    VkCommandBuffer frame_cmd = nullptr, e2e_cmd = nullptr, copy_cmd = nullptr;
+    VkFence fence = nullptr;
+    uint32_t depth_texel = 0;
+    uint64_t upload_bytes = 0;
+};
+
+namespace {
+
+VkResult make_buffer(cpvh_context* c, VkDeviceSize size, VkBufferUsageFlags usage, bool host_visible, BufferAlloc& out) {
+    VkBufferCreateInfo bi{};
+    bi.sType = VK_STRUCTURE_TYPE_BUFFER_CREATE_INFO;
+    bi.size = size ? size : 16;
+    bi.usage = usage;
+    VkResult r = c->f.vkCreateBuffer(c->device, &bi, nullptr, &out.buffer);
+    if (r != VK_SUCCESS) return r;
+    VkMemoryRequirements req;
+    c->f.vkGetBufferMemoryRequirements(c->device, out.buffer, &req);
+    VkMemoryAllocateInfo ai{};
+    ai.sType = VK_STRUCTURE_TYPE_MEMORY_ALLOCATE_INFO;
+    ai.allocationSize = req.size;
+    ai.memoryTypeIndex = find_memory_type(c, req.memoryTypeBits, host_visible);
+    r = c->f.vkAllocateMemory(c->device, &ai, nullptr, &out.memory);
+    if (r != VK_SUCCESS) return r;
+    out.size = bi.size;
+    return c->f.vkBindBufferMemory(c->device, out.buffer, out.memory, 0);
+}
+
+VkResult make_image(cpvh_context* c, VkFormat fmt, uint32_t w, uint32_t h, uint32_t levels, VkImageUsageFlags usage, VkImageAspectFlags aspect,
+                    ImageAlloc& out) {
+    VkImageCreateInfo ii{};
+    ii.sType = VK_STRUCTURE_TYPE_IMAGE_CREATE_INFO;
+    ii.imageType = VK_IMAGE_TYPE_2D;
+    ii.format = fmt;
+    ii.extent = {w, h, 1};
+    ii.mipLevels = levels;
+    ii.arrayLayers = 1;
+    ii.samples = VK_SAMPLE_COUNT_1_BIT;
+    ii.tiling = VK_IMAGE_TILING_OPTIMAL;
+    ii.usage = usage;
+    VkResult r = c->f.vkCreateImage(c->device, &ii, nullptr, &out.image);
+    if (r != VK_SUCCESS) return r;
+    VkMemoryRequirements req;
+    c->f.vkGetImageMemoryRequirements(c->device, out.image, &req);
+    VkMemoryAllocateInfo ai{};
+    ai.sType = VK_STRUCTURE_TYPE_MEMORY_ALLOCATE_INFO;
+    ai.allocationSize = req.size;
+    ai.memoryTypeIndex = find_memory_type(c, req.memoryTypeBits, false);
+    r = c->f.vkAllocateMemory(c->device, &ai, nullptr, &out.memory);
+    if (r != VK_SUCCESS) return r;
+    r = c->f.vkBindImageMemory(c->device, out.image, out.memory, 0);
+    if (r != VK_SUCCESS) return r;
+    VkImageViewCreateInfo vi{};
+    vi.sType = VK_STRUCTURE_TYPE_IMAGE_VIEW_CREATE_INFO;
+    vi.image = out.image;
+    vi.viewType = VK_IMAGE_VIEW_TYPE_2D;
+    vi.format = fmt;
+    vi.subresourceRange = {aspect, 0, levels, 0, 1};
+    return c->f.vkCreateImageView(c->device, &vi, nullptr, &out.view);
+}
+
+void destroy_buffer(cpvh_context* c, BufferAlloc& b) {
+    if (b.buffer) c->f.vkDestroyBuffer(c->device, b.buffer, nullptr);
+    if (b.memory) c->f.vkFreeMemory(c->device, b.memory, nullptr);
+    b = BufferAlloc{};
+}
+
+void destroy_image(cpvh_context* c, ImageAlloc& i) {
+    if (i.view) c->f.vkDestroyImageView(c->device, i.view, nullptr);
+    if (i.image) c->f.vkDestroyImage(c->device, i.image, nullptr);
+    if (i.memory) c->f.vkFreeMemory(c->device, i.memory, nullptr);
+    i = ImageAlloc{};
+}
+
+uint32_t depth_texel_size(uint32_t f) { return f == VK_FORMAT_D16_UNORM ? 2 : (f == VK_FORMAT_D32_SFLOAT ? 4 : (f == VK_FORMAT_D32_SFLOAT_S8_UINT ? 8 : 0)); }
+
+VkResult submit_and_wait(cpvh_renderer* r, VkCommandBuffer cmd) {
+    cpvh_context* c = r->ctx;
+    VkSubmitInfo si{};
+    si.sType = VK_STRUCTURE_TYPE_SUBMIT_INFO;
+    si.commandBufferCount = 1;
+    si.pCommandBuffers = &cmd;
+    VkResult res = c->f.vkQueueSubmit(c->queue, 1, &si, r->fence);
+    if (res != VK_SUCCESS) return res;
+    res = c->f.vkWaitForFences(c->device, 1, &r->fence, VK_TRUE, ~0ull);
+    c->f.vkResetFences(c->device, 1, &r->fence);
+    return res;
+}
+
+// Copies the staging buffer's regions into the device-local buffers (the
+// layout staging = [vertex | index | uniform]).
+void record_upload(cpvh_renderer* r, VkCommandBuffer cmd) {
+    cpvh_context* c = r->ctx;
+    const cpv_scene* s = r->scene;
+    VkDeviceSize off = 0;
+    auto copy = [&](BufferAlloc& dst, uint64_t bytes) {
+        if (!bytes) return;
+        VkBufferCopy bc{off, 0, bytes};
+        c->f.vkCmdCopyBuffer(cmd, r->staging.buffer, dst.buffer, 1, &bc);
+        off += (bytes + 255) & ~255ull;
+    };
+    copy(r->vertex, s->vertex_bytes);
+    copy(r->index, s->index_bytes);
+    copy(r->uniform, s->uniform_bytes);
+}
+
+void fill_staging(cpvh_renderer* r, void* map) {
+    const cpv_scene* s = r->scene;
+    uint8_t* p = static_cast<uint8_t*>(map);
+    VkDeviceSize off = 0;
+    auto put = [&](const uint8_t* src, uint64_t bytes) {
+        if (!bytes) return;
+        std::memcpy(p + off, src, bytes);
+        off += (bytes + 255) & ~255ull;
+    };
+    put(s->vertex_data, s->vertex_bytes);
+    put(s->index_data, s->index_bytes);
+    put(s->uniform_data, s->uniform_bytes);
+}
+
+void record_frame(cpvh_renderer* r, VkCommandBuffer cmd) {
+    cpvh_context* c = r->ctx;
+    const cpv_scene* s = r->scene;
+    VkClearValue clears[2];
+    std::memset(clears, 0, sizeof(clears));
+    for (int i = 0; i < 4; i++) clears[0].color.float32[i] = s->clear_color[i];
+    clears[1].depthStencil.depth = s->clear_depth;
+    clears[1].depthStencil.stencil = s->clear_stencil;
+    VkRenderPassBeginInfo rb{};
+    rb.sType = VK_STRUCTURE_TYPE_RENDER_PASS_BEGIN_INFO;
+    rb.renderPass = r->pass;
+    rb.framebuffer = r->fb;
+    rb.renderArea = {{0, 0}, {s->width, s->height}};
+    rb.clearValueCount = s->depth_format ? 2 : 1;
+    rb.pClearValues = clears;
+    c->f.vkCmdBeginRenderPass(cmd, &rb, VK_SUBPASS_CONTENTS_INLINE);
+    uint32_t bound = ~0u;
+    for (uint32_t i = 0; i < s->num_draws; i++) {
+        const cpv_scene_draw& d = s->draws[i];
+        const cpv_scene_pipeline& p = s->pipelines[d.pipeline];
+        if (bound != d.pipeline) {
+            c->f.vkCmdBindPipeline(cmd, VK_PIPELINE_BIND_POINT_GRAPHICS, r->pipelines[d.pipeline]);
+            if (r->set) c->f.vkCmdBindDescriptorSets(cmd, VK_PIPELINE_BIND_POINT_GRAPHICS, r->layout, 0, 1, &r->set, 0, nullptr);
+            bound = d.pipeline;
+        }
+        for (uint32_t b = 0; b < p.num_bindings; b++) {
+            const VkDeviceSize off = d.vertex_offsets[b];
+            c->f.vkCmdBindVertexBuffers(cmd, p.bindings[b].binding, 1, &r->vertex.buffer, &off);
+        }
+        if (d.push_size) c->f.vkCmdPushConstants(cmd, r->layout, VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, 0, d.push_size, d.push);
+        if (d.indexed) {
+            c->f.vkCmdBindIndexBuffer(cmd, r->index.buffer, d.index_offset, static_cast<VkIndexType>(s->index_type));
+            c->f.vkCmdDrawIndexed(cmd, d.count, d.instance_count, d.first, d.vertex_offset, d.first_instance);
+        } else {
+            c->f.vkCmdDraw(cmd, d.count, d.instance_count, d.first, d.first_instance);
+        }
+    }
+    c->f.vkCmdEndRenderPass(cmd);
+}
+
+void record_readback(cpvh_renderer* r, VkCommandBuffer cmd) {
+    cpvh_context* c = r->ctx;
+    const cpv_scene* s = r->scene;
+    VkBufferImageCopy bc{};
+    bc.imageSubresource = {VK_IMAGE_ASPECT_COLOR_BIT, 0, 0, 1};
+    bc.imageExtent = {s->width, s->height, 1};
+    c->f.vkCmdCopyImageToBuffer(cmd, r->colour.image, VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL, r->readback.buffer, 1, &bc);
+    if (s->depth_format) {
+        bc.bufferOffset = static_cast<VkDeviceSize>(s->width) * s->height * 4;
+        bc.imageSubresource.aspectMask = VK_IMAGE_ASPECT_DEPTH_BIT;
+        c->f.vkCmdCopyImageToBuffer(cmd, r->depth.image, VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL, r->readback.buffer, 1, &bc);
+    }
+}
+
+VkResult record_all(cpvh_renderer* r) {
+    cpvh_context* c = r->ctx;
+    VkCommandBufferBeginInfo bi{};
+    bi.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_BEGIN_INFO;
+    bi.flags = VK_COMMAND_BUFFER_USAGE_SIMULTANEOUS_USE_BIT;
+    c->f.vkBeginCommandBuffer(r->frame_cmd, &bi);
+    record_frame(r, r->frame_cmd);
+    c->f.vkEndCommandBuffer(r->frame_cmd);
+    c->f.vkBeginCommandBuffer(r->e2e_cmd, &bi);
+    record_upload(r, r->e2e_cmd);
+    record_frame(r, r->e2e_cmd);
+    record_readback(r, r->e2e_cmd);
+    c->f.vkEndCommandBuffer(r->e2e_cmd);
+    return VK_SUCCESS;
+}
+
+bool build_pipelines(cpvh_context* c, const cpv_scene* s, VkRenderPass pass, VkPipelineLayout layout, std::vector<VkShaderModule>& modules,
+                     std::vector<VkPipeline>& pipelines, std::string& err) {
+    const Fns& f = c->f;
+    for (uint32_t i = 0; i < s->num_pipelines; i++) {
+        const cpv_scene_pipeline& sp = s->pipelines[i];
+        VkShaderModule mods[2];
+        for (uint32_t st = 0; st < 2; st++) {
+            size_t bytes = 0;
+            const uint32_t* code = cpvh_spirv(sp.program, st, &bytes);
+            if (!code) { err = "no SPIR-V for program " + std::to_string(sp.program); return false; }
+            VkShaderModuleCreateInfo smi{};
+            smi.sType = VK_STRUCTURE_TYPE_SHADER_MODULE_CREATE_INFO;
+            smi.codeSize = bytes;
+            smi.pCode = code;
+            if (f.vkCreateShaderModule(c->device, &smi, nullptr, &mods[st]) != VK_SUCCESS) { err = "shader module"; return false; }
+            modules.push_back(mods[st]);
+        }
+        VkPipelineShaderStageCreateInfo stages[2]{};
+        stages[0].sType = stages[1].sType = VK_STRUCTURE_TYPE_PIPELINE_SHADER_STAGE_CREATE_INFO;
+        stages[0].stage = VK_SHADER_STAGE_VERTEX_BIT;
+        stages[0].module = mods[0];
+        stages[0].pName = "main";
+        stages[1].stage = VK_SHADER_STAGE_FRAGMENT_BIT;
+        stages[1].module = mods[1];
+        stages[1].pName = "main";
+        VkVertexInputBindingDescription vbd[CPV_SCENE_MAX_BINDINGS];
+        VkVertexInputAttributeDescription vad[CPV_SCENE_MAX_ATTRIBUTES];
+        for (uint32_t b = 0; b < sp.num_bindings; b++) vbd[b] = {sp.bindings[b].binding, sp.bindings[b].stride, static_cast<VkVertexInputRate>(sp.bindings[b].input_rate)};
+        for (uint32_t a = 0; a < sp.num_attributes; a++)
+            vad[a] = {sp.attributes[a].location, sp.attributes[a].binding, static_cast<VkFormat>(sp.attributes[a].format), sp.attributes[a].offset};
+        VkPipelineVertexInputStateCreateInfo vis{};
+        vis.sType = VK_STRUCTURE_TYPE_PIPELINE_VERTEX_INPUT_STATE_CREATE_INFO;
+        vis.vertexBindingDescriptionCount = sp.num_bindings;
+        vis.pVertexBindingDescriptions = vbd;
+        vis.vertexAttributeDescriptionCount = sp.num_attributes;
+        vis.pVertexAttributeDescriptions = vad;
+        VkPipelineInputAssemblyStateCreateInfo ias{};
+        ias.sType = VK_STRUCTURE_TYPE_PIPELINE_INPUT_ASSEMBLY_STATE_CREATE_INFO;
+        ias.topology = static_cast<VkPrimitiveTopology>(sp.topology);
+        VkViewport vp{s->viewport[0], s->viewport[1], s->viewport[2], s->viewport[3], s->viewport[4], s->viewport[5]};
+        VkRect2D sc{{0, 0}, {s->width, s->height}};
+        VkPipelineViewportStateCreateInfo vps{};
+        vps.sType = VK_STRUCTURE_TYPE_PIPELINE_VIEWPORT_STATE_CREATE_INFO;
+        vps.viewportCount = 1;
+        vps.pViewports = &vp;
+        vps.scissorCount = 1;
+        vps.pScissors = &sc;
+        VkPipelineRasterizationStateCreateInfo rs{};
+        rs.sType = VK_STRUCTURE_TYPE_PIPELINE_RASTERIZATION_STATE_CREATE_INFO;
+        rs.polygonMode = VK_POLYGON_MODE_FILL;
+        rs.cullMode = sp.cull_mode;
+        rs.frontFace = static_cast<VkFrontFace>(sp.front_face);
+        rs.lineWidth = 1.0f;
+        VkPipelineMultisampleStateCreateInfo ms{};
+        ms.sType = VK_STRUCTURE_TYPE_PIPELINE_MULTISAMPLE_STATE_CREATE_INFO;
+        ms.rasterizationSamples = VK_SAMPLE_COUNT_1_BIT;
+        VkPipelineDepthStencilStateCreateInfo ds{};
+        ds.sType = VK_STRUCTURE_TYPE_PIPELINE_DEPTH_STENCIL_STATE_CREATE_INFO;
+        ds.depthTestEnable = sp.depth_test;
+        ds.depthWriteEnable = sp.depth_write;
+        ds.depthCompareOp = static_cast<VkCompareOp>(sp.depth_compare);
+        ds.stencilTestEnable = sp.stencil_test;
+        const cpv_scene_stencil* so[2] = {&sp.stencil_front, &sp.stencil_back};
+        VkStencilOpState* dso[2] = {&ds.front, &ds.back};
+        for (int k = 0; k < 2; k++)
+            *dso[k] = {static_cast<VkStencilOp>(so[k]->fail_op), static_cast<VkStencilOp>(so[k]->pass_op), static_cast<VkStencilOp>(so[k]->depth_fail_op),
+                       static_cast<VkCompareOp>(so[k]->compare_op), so[k]->compare_mask, so[k]->write_mask, so[k]->reference};
+        VkPipelineColorBlendAttachmentState cba{};
+        cba.blendEnable = sp.blend_enable;
+        cba.srcColorBlendFactor = static_cast<VkBlendFactor>(sp.src_color);
+        cba.dstColorBlendFactor = static_cast<VkBlendFactor>(sp.dst_color);
+        cba.colorBlendOp = static_cast<VkBlendOp>(sp.color_op);
+        cba.srcAlphaBlendFactor = static_cast<VkBlendFactor>(sp.src_alpha);
+        cba.dstAlphaBlendFactor = static_cast<VkBlendFactor>(sp.dst_alpha);
+        cba.alphaBlendOp = static_cast<VkBlendOp>(sp.alpha_op);
+        cba.colorWriteMask = 0xF;
+        VkPipelineColorBlendStateCreateInfo cbs{};
+        cbs.sType = VK_STRUCTURE_TYPE_PIPELINE_COLOR_BLEND_STATE_CREATE_INFO;
+        cbs.attachmentCount = 1;
+        cbs.pAttachments = &cba;
+        for (int k = 0; k < 4; k++) cbs.blendConstants[k] = sp.blend_constants[k];
+        VkGraphicsPipelineCreateInfo gpi{};
+        gpi.sType = VK_STRUCTURE_TYPE_GRAPHICS_PIPELINE_CREATE_INFO;
+        gpi.stageCount = 2;
+        gpi.pStages = stages;
+        gpi.pVertexInputState = &vis;
+        gpi.pInputAssemblyState = &ias;
+        gpi.pViewportState = &vps;
+        gpi.pRasterizationState = &rs;
+        gpi.pMultisampleState = &ms;
+        gpi.pDepthStencilState = &ds;
+        gpi.pColorBlendState = &cbs;
+        gpi.layout = layout;
+        gpi.renderPass = pass;
+        VkPipeline pipe = nullptr;
+        if (f.vkCreateGraphicsPipelines(c->device, c->cache, 1, &gpi, nullptr, &pipe) != VK_SUCCESS) { err = "vkCreateGraphicsPipelines:"; return false; }
+        pipelines.push_back(pipe);
+    }
+    return true;
+}
+
+VkResult make_pass_and_layout(cpvh_context* c, const cpv_scene* s, bool with_sets, VkRenderPass& pass, VkDescriptorSetLayout& set_layout,
+                              VkPipelineLayout& layout) {
+    const Fns& f = c->f;
+    VkAttachmentDescription att[2]{};
+    att[0].format = static_cast<VkFormat>(s->color_format);
+    att[0].samples = VK_SAMPLE_COUNT_1_BIT;
+    att[0].loadOp = VK_ATTACHMENT_LOAD_OP_CLEAR;
+    att[0].storeOp = VK_ATTACHMENT_STORE_OP_STORE;
+    att[0].stencilLoadOp = VK_ATTACHMENT_LOAD_OP_DONT_CARE;
+    att[0].finalLayout = VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL;
+    att[1] = att[0];
+    att[1].format = static_cast<VkFormat>(s->depth_format);
+    att[1].stencilLoadOp = VK_ATTACHMENT_LOAD_OP_CLEAR;
+    VkAttachmentReference cref{0, VK_IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL}, dref{1, VK_IMAGE_LAYOUT_DEPTH_STENCIL_ATTACHMENT_OPTIMAL};
+    VkSubpassDescription sub{};
+    sub.colorAttachmentCount = 1;
+    sub.pColorAttachments = &cref;
+    sub.pDepthStencilAttachment = s->depth_format ? &dref : nullptr;
+    VkRenderPassCreateInfo rpi{};
+    rpi.sType = VK_STRUCTURE_TYPE_RENDER_PASS_CREATE_INFO;
+    rpi.attachmentCount = s->depth_format ? 2 : 1;
+    rpi.pAttachments = att;
+    rpi.subpassCount = 1;
+    rpi.pSubpasses = &sub;
+    VkResult res = f.vkCreateRenderPass(c->device, &rpi, nullptr, &pass);
+    if (res != VK_SUCCESS) return res;
+    std::vector<VkDescriptorSetLayoutBinding> lb;
+    if (with_sets && s->uniform_bytes) lb.push_back({0, VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER, 1, VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
+    if (with_sets && s->texture_data) lb.push_back({1, VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER, 1, VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
+    VkDescriptorSetLayoutCreateInfo dli{};
+    dli.sType = VK_STRUCTURE_TYPE_DESCRIPTOR_SET_LAYOUT_CREATE_INFO;
+    dli.bindingCount = static_cast<uint32_t>(lb.size());
+    dli.pBindings = lb.data();
+    res = f.vkCreateDescriptorSetLayout(c->device, &dli, nullptr, &set_layout);
+    if (res != VK_SUCCESS) return res;
+    VkPushConstantRange pcr{VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, 0, 128};
+    VkPipelineLayoutCreateInfo pli{};
+    pli.sType = VK_STRUCTURE_TYPE_PIPELINE_LAYOUT_CREATE_INFO;
+    pli.setLayoutCount = 1;
+    pli.pSetLayouts = &set_layout;
+    pli.pushConstantRangeCount = 1;
+    pli.pPushConstantRanges = &pcr;
+    return f.vkCreatePipelineLayout(c->device, &pli, nullptr, &layout);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* cpvh_last_error(void) { return g_err.c_str(); }
+
+cpvh_context* cpvh_open(const char* icd_path, char* err, uint32_t err_len) {
+    auto fail = [&](const std::string& e, cpvh_context* c) -> cpvh_context* {
+        g_err = e + (c ? " " + icd_error(c) : "");
+        if (err && err_len) std::snprintf(err, err_len, "%s", g_err.c_str());
+        if (c) cpvh_close(c);
+        return nullptr;
+    };
+    auto* c = new cpvh_context();
+    c->lib = dlopen(icd_path, RTLD_NOW | RTLD_LOCAL);
+    if (!c->lib) return fail(std::string("dlopen failed: ") + dlerror(), c);
+    auto negotiate = reinterpret_cast<PFN_vk_icdNegotiateLoaderICDInterfaceVersion>(dlsym(c->lib, "vk_icdNegotiateLoaderICDInterfaceVersion"));
+    auto gipa = reinterpret_cast<PFN_vk_icdGetInstanceProcAddr>(dlsym(c->lib, "vk_icdGetInstanceProcAddr"));
+    c->record = reinterpret_cast<PFN_cpv_queue_record>(dlsym(c->lib, "cpv_queue_record"));
+    c->elapsed = reinterpret_cast<PFN_cpv_queue_elapsed_ms>(dlsym(c->lib, "cpv_queue_elapsed_ms"));
+    c->icd_error = reinterpret_cast<PFN_cpv_last_error>(dlsym(c->lib, "cpv_last_error"));
+    if (!negotiate || !gipa) return fail("not a Vulkan ICD (missing vk_icd* exports)", c);
+    uint32_t version = 5;
+    if (negotiate(&version) != VK_SUCCESS || version < 1) return fail("interface negotiation failed", c);
+    Fns& f = c->f;
+    f.vkGetInstanceProcAddr = reinterpret_cast<PFN_vkGetInstanceProcAddr>(gipa(nullptr, "vkGetInstanceProcAddr"));
+    f.vkCreateInstance = reinterpret_cast<PFN_vkCreateInstance>(gipa(nullptr, "vkCreateInstance"));
+    if (!f.vkGetInstanceProcAddr || !f.vkCreateInstance) return fail("ICD lacks global entry points", c);
+    VkApplicationInfo app{};
+    app.sType = VK_STRUCTURE_TYPE_APPLICATION_INFO;
+    app.pApplicationName = "cpvh";
+    app.apiVersion = VK_API_VERSION_1_1;
+    VkInstanceCreateInfo ici{};
+    ici.sType = VK_STRUCTURE_TYPE_INSTANCE_CREATE_INFO;
+    ici.pApplicationInfo = &app;
+    if (f.vkCreateInstance(&ici, nullptr, &c->instance) != VK_SUCCESS) return fail("vkCreateInstance failed", c);
+    if (!check_dispatch(c->instance)) return fail("VkInstance lacks the loader magic", c);
+#define LOAD_I(name) f.name = reinterpret_cast<PFN_##name>(f.vkGetInstanceProcAddr(c->instance, #name))
+    LOAD_I(vkDestroyInstance);
+    LOAD_I(vkEnumeratePhysicalDevices);
+    LOAD_I(vkGetPhysicalDeviceMemoryProperties);
+    LOAD_I(vkGetPhysicalDeviceQueueFamilyProperties);
+    LOAD_I(vkCreateDevice);
+    LOAD_I(vkGetDeviceProcAddr);
+#undef LOAD_I
+    uint32_t n = 1;
+    if (f.vkEnumeratePhysicalDevices(c->instance, &n, &c->physical) != VK_SUCCESS || n < 1) return fail("no physical device", c);
+    if (!check_dispatch(c->physical)) return fail("VkPhysicalDevice lacks the loader magic", c);
+    f.vkGetPhysicalDeviceMemoryProperties(c->physical, &c->mem);
+    const float prio = 1.0f;
+    VkDeviceQueueCreateInfo qci{};
+    qci.sType = VK_STRUCTURE_TYPE_DEVICE_QUEUE_CREATE_INFO;
+    qci.queueCount = 1;
+    qci.pQueuePriorities = &prio;
+    VkDeviceCreateInfo dci{};
+    dci.sType = VK_STRUCTURE_TYPE_DEVICE_CREATE_INFO;
+    dci.queueCreateInfoCount = 1;
+    dci.pQueueCreateInfos = &qci;
+    if (f.vkCreateDevice(c->physical, &dci, nullptr, &c->device) != VK_SUCCESS) return fail("vkCreateDevice failed:", c);
+    if (!check_dispatch(c->device)) return fail("VkDevice lacks the loader magic", c);
+#define LOAD_D(name)                                                                     \
+    f.name = reinterpret_cast<PFN_##name>(f.vkGetDeviceProcAddr(c->device, #name));      \
+    if (!f.name) return fail("ICD lacks " #name, c)
+    LOAD_D(vkDestroyDevice); LOAD_D(vkGetDeviceQueue); LOAD_D(vkDeviceWaitIdle); LOAD_D(vkAllocateMemory); LOAD_D(vkFreeMemory);
+    LOAD_D(vkMapMemory); LOAD_D(vkUnmapMemory); LOAD_D(vkCreateBuffer); LOAD_D(vkDestroyBuffer); LOAD_D(vkGetBufferMemoryRequirements);
+    LOAD_D(vkBindBufferMemory); LOAD_D(vkCreateImage); LOAD_D(vkDestroyImage); LOAD_D(vkGetImageMemoryRequirements); LOAD_D(vkBindImageMemory);
+    LOAD_D(vkCreateImageView); LOAD_D(vkDestroyImageView); LOAD_D(vkCreateSampler); LOAD_D(vkDestroySampler); LOAD_D(vkCreateShaderModule);
+    LOAD_D(vkDestroyShaderModule); LOAD_D(vkCreatePipelineCache); LOAD_D(vkDestroyPipelineCache); LOAD_D(vkCreateGraphicsPipelines);
+    LOAD_D(vkDestroyPipeline); LOAD_D(vkCreatePipelineLayout); LOAD_D(vkDestroyPipelineLayout); LOAD_D(vkCreateDescriptorSetLayout);
+    LOAD_D(vkDestroyDescriptorSetLayout); LOAD_D(vkCreateDescriptorPool); LOAD_D(vkDestroyDescriptorPool); LOAD_D(vkAllocateDescriptorSets);
+    LOAD_D(vkUpdateDescriptorSets); LOAD_D(vkCreateRenderPass); LOAD_D(vkDestroyRenderPass); LOAD_D(vkCreateFramebuffer);
+    LOAD_D(vkDestroyFramebuffer); LOAD_D(vkCreateCommandPool); LOAD_D(vkDestroyCommandPool); LOAD_D(vkAllocateCommandBuffers);
+    LOAD_D(vkBeginCommandBuffer); LOAD_D(vkEndCommandBuffer); LOAD_D(vkCmdBindPipeline); LOAD_D(vkCmdBindDescriptorSets);
+    LOAD_D(vkCmdBindIndexBuffer); LOAD_D(vkCmdBindVertexBuffers); LOAD_D(vkCmdDraw); LOAD_D(vkCmdDrawIndexed); LOAD_D(vkCmdCopyBuffer);
+    LOAD_D(vkCmdCopyBufferToImage); LOAD_D(vkCmdCopyImageToBuffer); LOAD_D(vkCmdPipelineBarrier); LOAD_D(vkCmdPushConstants);
+    LOAD_D(vkCmdBeginRenderPass); LOAD_D(vkCmdEndRenderPass); LOAD_D(vkQueueSubmit); LOAD_D(vkQueueWaitIdle); LOAD_D(vkCreateFence);
+    LOAD_D(vkDestroyFence); LOAD_D(vkResetFences); LOAD_D(vkWaitForFences);
+#undef LOAD_D
+    f.vkGetDeviceQueue(c->device, 0, 0, &c->queue);
+    if (!check_dispatch(c->queue)) return fail("VkQueue lacks the loader magic", c);
+    VkPipelineCacheCreateInfo pci{};
+    pci.sType = VK_STRUCTURE_TYPE_PIPELINE_CACHE_CREATE_INFO;
+    f.vkCreatePipelineCache(c->device, &pci, nullptr, &c->cache);
+    return c;
+}
+
+void cpvh_close(cpvh_context* c) {
+    if (!c) return;
+    if (c->device) {
+        c->f.vkDeviceWaitIdle(c->device);
+        if (c->cache) c->f.vkDestroyPipelineCache(c->device, c->cache, nullptr);
+        c->f.vkDestroyDevice(c->device, nullptr);
+    }
+    if (c->instance && c->f.vkDestroyInstance) c->f.vkDestroyInstance(c->instance, nullptr);
+    // The ICD stays loaded: CUDA state it created lives until process exit.
+    delete c;
+}
+
+void* cpvh_queue(cpvh_context* c) { return c ? c->queue : nullptr; }
+
+cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* err, uint32_t err_len) {
+    auto* r = new cpvh_renderer();
+    r->ctx = c;
+    r->scene = s;
+    auto fail = [&](const std::string& e) -> cpvh_renderer* {
+        g_err = e + " " + icd_error(c);
+        if (err && err_len) std::snprintf(err, err_len, "%s", g_err.c_str());
+        cpvh_renderer_destroy(r);
+        return nullptr;
+    };
+    const Fns& f = c->f;
+    const VkBufferUsageFlags vb_usage = VK_BUFFER_USAGE_VERTEX_BUFFER_BIT | VK_BUFFER_USAGE_TRANSFER_DST_BIT;
+    if (make_buffer(c, s->vertex_bytes, vb_usage, false, r->vertex) != VK_SUCCESS) return fail("vertex buffer");
+    if (make_buffer(c, s->index_bytes, VK_BUFFER_USAGE_INDEX_BUFFER_BIT | VK_BUFFER_USAGE_TRANSFER_DST_BIT, false, r->index) != VK_SUCCESS)
+        return fail("index buffer");
+    if (s->uniform_bytes && make_buffer(c, s->uniform_bytes, VK_BUFFER_USAGE_UNIFORM_BUFFER_BIT | VK_BUFFER_USAGE_TRANSFER_DST_BIT, false, r->uniform) != VK_SUCCESS)
+        return fail("uniform buffer");
+    const uint64_t staging = ((s->vertex_bytes + 255) & ~255ull) + ((s->index_bytes + 255) & ~255ull) + ((s->uniform_bytes + 255) & ~255ull) +
+                             ((s->texture_bytes + 255) & ~255ull);
+    r->upload_bytes = s->vertex_bytes + s->index_bytes + s->uniform_bytes;
+    if (make_buffer(c, staging, VK_BUFFER_USAGE_TRANSFER_SRC_BIT, true, r->staging) != VK_SUCCESS) return fail("staging buffer");
+    r->depth_texel = depth_texel_size(s->depth_format);
+    const uint64_t rb_bytes = static_cast<uint64_t>(s->width) * s->height * (4 + r->depth_texel);
+    if (make_buffer(c, rb_bytes, VK_BUFFER_USAGE_TRANSFER_DST_BIT, true, r->readback) != VK_SUCCESS) return fail("readback buffer");
+    if (make_image(c, static_cast<VkFormat>(s->color_format), s->width, s->height, 1, VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT | VK_IMAGE_USAGE_TRANSFER_SRC_BIT,
+                   VK_IMAGE_ASPECT_COLOR_BIT, r->colour) != VK_SUCCESS)
+        return fail("colour image");
+    if (s->depth_format &&
+        make_image(c, static_cast<VkFormat>(s->depth_format), s->width, s->height, 1, VK_IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT_BIT | VK_IMAGE_USAGE_TRANSFER_SRC_BIT,
+                   VK_IMAGE_ASPECT_DEPTH_BIT, r->depth) != VK_SUCCESS)
+        return fail("depth image");
+    if (s->texture_data) {
+        if (make_image(c, static_cast<VkFormat>(s->texture_format), s->texture_width, s->texture_height, s->texture_levels,
+                       VK_IMAGE_USAGE_SAMPLED_BIT | VK_IMAGE_USAGE_TRANSFER_DST_BIT, VK_IMAGE_ASPECT_COLOR_BIT, r->texture) != VK_SUCCESS)
+            return fail("texture image");
+        VkSamplerCreateInfo sci{};
+        sci.sType = VK_STRUCTURE_TYPE_SAMPLER_CREATE_INFO;
+        sci.magFilter = static_cast<VkFilter>(s->sampler.mag_filter);
+        sci.minFilter = static_cast<VkFilter>(s->sampler.min_filter);
+        sci.mipmapMode = static_cast<VkSamplerMipmapMode>(s->sampler.mipmap_mode);
+        sci.addressModeU = static_cast<VkSamplerAddressMode>(s->sampler.address_u);
+        sci.addressModeV = static_cast<VkSamplerAddressMode>(s->sampler.address_v);
+        sci.addressModeW = static_cast<VkSamplerAddressMode>(s->sampler.address_w);
+        sci.mipLodBias = s->sampler.mip_lod_bias;
+        sci.minLod = s->sampler.min_lod;
+        sci.maxLod = s->sampler.max_lod;
+        sci.borderColor = static_cast<VkBorderColor>(s->sampler.border_color);
+        if (f.vkCreateSampler(c->device, &sci, nullptr, &r->sampler) != VK_SUCCESS) return fail("sampler");
+    }
+    // Render pass + framebuffer.
+    VkAttachmentDescription att[2]{};
+    att[0].format = static_cast<VkFormat>(s->color_format);
+    att[0].samples = VK_SAMPLE_COUNT_1_BIT;
+    att[0].loadOp = VK_ATTACHMENT_LOAD_OP_CLEAR;
+    att[0].storeOp = VK_ATTACHMENT_STORE_OP_STORE;
+    att[0].stencilLoadOp = VK_ATTACHMENT_LOAD_OP_DONT_CARE;
+    att[0].finalLayout = VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL;
+    att[1] = att[0];
+    att[1].format = static_cast<VkFormat>(s->depth_format);
+    att[1].stencilLoadOp = VK_ATTACHMENT_LOAD_OP_CLEAR;
+    VkAttachmentReference cref{0, VK_IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL}, dref{1, VK_IMAGE_LAYOUT_DEPTH_STENCIL_ATTACHMENT_OPTIMAL};
+    VkSubpassDescription sub{};
+    sub.colorAttachmentCount = 1;
+    sub.pColorAttachments = &cref;
+    sub.pDepthStencilAttachment = s->depth_format ? &dref : nullptr;
+    VkRenderPassCreateInfo rpi{};
+    rpi.sType = VK_STRUCTURE_TYPE_RENDER_PASS_CREATE_INFO;
+    rpi.attachmentCount = s->depth_format ? 2 : 1;
+    rpi.pAttachments = att;
+    rpi.subpassCount = 1;
+    rpi.pSubpasses = &sub;
+    if (f.vkCreateRenderPass(c->device, &rpi, nullptr, &r->pass) != VK_SUCCESS) return fail("render pass");
+    VkImageView views[2] = {r->colour.view, r->depth.view};
+    VkFramebufferCreateInfo fbi{};
+    fbi.sType = VK_STRUCTURE_TYPE_FRAMEBUFFER_CREATE_INFO;
+    fbi.renderPass = r->pass;
+    fbi.attachmentCount = s->depth_format ? 2 : 1;
+    fbi.pAttachments = views;
+    fbi.width = s->width;
+    fbi.height = s->height;
+    fbi.layers = 1;
+    if (f.vkCreateFramebuffer(c->device, &fbi, nullptr, &r->fb) != VK_SUCCESS) return fail("framebuffer");
+    // Descriptors: binding 0 uniform buffer, binding 1 combined image sampler.
+    std::vector<VkDescriptorSetLayoutBinding> lb;
+    if (s->uniform_bytes) lb.push_back({0, VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER, 1, VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
+    if (s->texture_data) lb.push_back({1, VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER, 1, VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
+    VkDescriptorSetLayoutCreateInfo dli{};
+    dli.sType = VK_STRUCTURE_TYPE_DESCRIPTOR_SET_LAYOUT_CREATE_INFO;
+    dli.bindingCount = static_cast<uint32_t>(lb.size());
+    dli.pBindings = lb.data();
+    if (f.vkCreateDescriptorSetLayout(c->device, &dli, nullptr, &r->set_layout) != VK_SUCCESS) return fail("set layout");
+    VkDescriptorPoolSize ps[2] = {{VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER, 1}, {VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER, 1}};
+    VkDescriptorPoolCreateInfo dpi{};
+    dpi.sType = VK_STRUCTURE_TYPE_DESCRIPTOR_POOL_CREATE_INFO;
+    dpi.maxSets = 1;
+    dpi.poolSizeCount = 2;
+    dpi.pPoolSizes = ps;
+    if (f.vkCreateDescriptorPool(c->device, &dpi, nullptr, &r->pool) != VK_SUCCESS) return fail("descriptor pool");
+    if (!lb.empty()) {
+        VkDescriptorSetAllocateInfo dai{};
+        dai.sType = VK_STRUCTURE_TYPE_DESCRIPTOR_SET_ALLOCATE_INFO;
+        dai.descriptorPool = r->pool;
+        dai.descriptorSetCount = 1;
+        dai.pSetLayouts = &r->set_layout;
+        if (f.vkAllocateDescriptorSets(c->device, &dai, &r->set) != VK_SUCCESS) return fail("descriptor set");
+        VkDescriptorBufferInfo dbi{r->uniform.buffer, 0, VK_WHOLE_SIZE};
+        VkDescriptorImageInfo dii{r->sampler, r->texture.view, VK_IMAGE_LAYOUT_SHADER_READ_ONLY_OPTIMAL};
+        VkWriteDescriptorSet w[2]{};
+        uint32_t nw = 0;
+        if (s->uniform_bytes) {
+            w[nw].sType = VK_STRUCTURE_TYPE_WRITE_DESCRIPTOR_SET;
+            w[nw].dstSet = r->set;
+            w[nw].dstBinding = 0;
+            w[nw].descriptorCount = 1;
+            w[nw].descriptorType = VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER;
+            w[nw].pBufferInfo = &dbi;
+            nw++;
+        }
+        if (s->texture_data) {
+            w[nw].sType = VK_STRUCTURE_TYPE_WRITE_DESCRIPTOR_SET;
+            w[nw].dstSet = r->set;
+            w[nw].dstBinding = 1;
+            w[nw].descriptorCount = 1;
+            w[nw].descriptorType = VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER;
+            w[nw].pImageInfo = &dii;
+            nw++;
+        }
+        f.vkUpdateDescriptorSets(c->device, nw, w, 0, nullptr);
+    }
+    VkPushConstantRange pcr{VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, 0, 128};
+    VkPipelineLayoutCreateInfo pli{};
+    pli.sType = VK_STRUCTURE_TYPE_PIPELINE_LAYOUT_CREATE_INFO;
+    pli.setLayoutCount = 1;
+    pli.pSetLayouts = &r->set_layout;
+    pli.pushConstantRangeCount = 1;
+    pli.pPushConstantRanges = &pcr;
+    if (f.vkCreatePipelineLayout(c->device, &pli, nullptr, &r->layout) != VK_SUCCESS) return fail("pipeline layout");
+    {
+        std::string perr;
+        if (!build_pipelines(c, s, r->pass, r->layout, r->modules, r->pipelines, perr)) return fail(perr);
+    }
+    // Command buffers and fence.
+    VkCommandPoolCreateInfo cpi{};
+    cpi.sType = VK_STRUCTURE_TYPE_COMMAND_POOL_CREATE_INFO;
+    cpi.flags = VK_COMMAND_POOL_CREATE_RESET_COMMAND_BUFFER_BIT;
+    if (f.vkCreateCommandPool(c->device, &cpi, nullptr, &r->cmd_pool) != VK_SUCCESS) return fail("command pool");
+    VkCommandBuffer cbs3[3];
+    VkCommandBufferAllocateInfo cai{};
+    cai.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_ALLOCATE_INFO;
+    cai.commandPool = r->cmd_pool;
+    cai.level = VK_COMMAND_BUFFER_LEVEL_PRIMARY;
+    cai.commandBufferCount = 3;
+    if (f.vkAllocateCommandBuffers(c->device, &cai, cbs3) != VK_SUCCESS) return fail("command buffers");
+    for (auto cb : cbs3)
+        if (!check_dispatch(cb)) return fail("VkCommandBuffer lacks the loader magic");
+    r->frame_cmd = cbs3[0];
+    r->e2e_cmd = cbs3[1];
+    r->copy_cmd = cbs3[2];
+    VkFenceCreateInfo fci{};
+    fci.sType = VK_STRUCTURE_TYPE_FENCE_CREATE_INFO;
+    if (f.vkCreateFence(c->device, &fci, nullptr, &r->fence) != VK_SUCCESS) return fail("fence");
+    // Upload vertex/index/uniform/texture once through the staging buffer.
+    void* map = nullptr;
+    if (f.vkMapMemory(c->device, r->staging.memory, 0, VK_WHOLE_SIZE, 0, &map) != VK_SUCCESS) return fail("map staging");
+    fill_staging(r, map);
+    const uint64_t tex_off = ((s->vertex_bytes + 255) & ~255ull) + ((s->index_bytes + 255) & ~255ull) + ((s->uniform_bytes + 255) & ~255ull);
+    if (s->texture_data) std::memcpy(static_cast<uint8_t*>(map) + tex_off, s->texture_data, s->texture_bytes);
+    f.vkUnmapMemory(c->device, r->staging.memory);
+    VkCommandBufferBeginInfo bi{};
+    bi.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_BEGIN_INFO;
+    f.vkBeginCommandBuffer(r->copy_cmd, &bi);
+    record_upload(r, r->copy_cmd);
+    if (s->texture_data) {
+        uint64_t off = tex_off;
+        uint32_t w = s->texture_width, h = s->texture_height;
+        for (uint32_t l = 0; l < s->texture_levels; l++) {
+            VkBufferImageCopy bc{};
+            bc.bufferOffset = off;
+            bc.imageSubresource = {VK_IMAGE_ASPECT_COLOR_BIT, l, 0, 1};
+            bc.imageExtent = {w, h, 1};
+            f.vkCmdCopyBufferToImage(r->copy_cmd, r->staging.buffer, r->texture.image, VK_IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL, 1, &bc);
+            off += static_cast<uint64_t>(w) * h * 4;
+            w = w > 1 ? w / 2 : 1;
+            h = h > 1 ? h / 2 : 1;
+        }
+    }
+    f.vkEndCommandBuffer(r->copy_cmd);
+    if (submit_and_wait(r, r->copy_cmd) != VK_SUCCESS) return fail("upload submit");
+    record_all(r);
+    return r;
+}
+
+int cpvh_compile_pipelines(cpvh_context* c, const cpv_scene* s, char* err, uint32_t err_len) {
+    VkRenderPass pass = nullptr;
+    VkDescriptorSetLayout set_layout = nullptr;
+    VkPipelineLayout layout = nullptr;
+    std::vector<VkShaderModule> modules;
+    std::vector<VkPipeline> pipelines;
+    std::string perr;
+    int result = make_pass_and_layout(c, s, true, pass, set_layout, layout);
+    if (result == VK_SUCCESS && !build_pipelines(c, s, pass, layout, modules, pipelines, perr)) result = VK_ERROR_INITIALIZATION_FAILED;
+    if (result != VK_SUCCESS) {
+        g_err = perr + " " + icd_error(c);
+        if (err && err_len) std::snprintf(err, err_len, "%s", g_err.c_str());
+    }
+    for (auto p : pipelines) c->f.vkDestroyPipeline(c->device, p, nullptr);
+    for (auto m : modules) c->f.vkDestroyShaderModule(c->device, m, nullptr);
+    if (layout) c->f.vkDestroyPipelineLayout(c->device, layout, nullptr);
+    if (set_layout) c->f.vkDestroyDescriptorSetLayout(c->device, set_layout, nullptr);
+    if (pass) c->f.vkDestroyRenderPass(c->device, pass, nullptr);
+    return result;
+}
+
+void cpvh_renderer_destroy(cpvh_renderer* r) {
+    if (!r) return;
+    cpvh_context* c = r->ctx;
+    const Fns& f = c->f;
+    f.vkDeviceWaitIdle(c->device);
+    if (r->fence) f.vkDestroyFence(c->device, r->fence, nullptr);
+    if (r->cmd_pool) f.vkDestroyCommandPool(c->device, r->cmd_pool, nullptr);
+    for (auto p : r->pipelines) f.vkDestroyPipeline(c->device, p, nullptr);
+    for (auto m : r->modules) f.vkDestroyShaderModule(c->device, m, nullptr);
+    if (r->layout) f.vkDestroyPipelineLayout(c->device, r->layout, nullptr);
+    if (r->pool) f.vkDestroyDescriptorPool(c->device, r->pool, nullptr);
+    if (r->set_layout) f.vkDestroyDescriptorSetLayout(c->device, r->set_layout, nullptr);
+    if (r->fb) f.vkDestroyFramebuffer(c->device, r->fb, nullptr);
+    if (r->pass) f.vkDestroyRenderPass(c->device, r->pass, nullptr);
+    if (r->sampler) f.vkDestroySampler(c->device, r->sampler, nullptr);
+    destroy_image(c, r->colour);
+    destroy_image(c, r->depth);
+    destroy_image(c, r->texture);
+    destroy_buffer(c, r->vertex);
+    destroy_buffer(c, r->index);
+    destroy_buffer(c, r->uniform);
+    destroy_buffer(c, r->staging);
+    destroy_buffer(c, r->readback);
+    delete r;
+}
+
+int cpvh_renderer_update(cpvh_renderer* r) {
+    cpvh_context* c = r->ctx;
+    void* map = nullptr;
+    if (c->f.vkMapMemory(c->device, r->staging.memory, 0, VK_WHOLE_SIZE, 0, &map) != VK_SUCCESS) return VK_ERROR_MEMORY_MAP_FAILED;
+    fill_staging(r, map);
+    c->f.vkUnmapMemory(c->device, r->staging.memory);
+    VkCommandBufferBeginInfo bi{};
+    bi.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_BEGIN_INFO;
+    c->f.vkBeginCommandBuffer(r->copy_cmd, &bi);
+    record_upload(r, r->copy_cmd);
+    c->f.vkEndCommandBuffer(r->copy_cmd);
+    const VkResult res = submit_and_wait(r, r->copy_cmd);
+    record_all(r);
+    return res;
+}
+
+int cpvh_render(cpvh_renderer* r, uint32_t frames, double* device_ms, double* latency_ms) {
+    cpvh_context* c = r->ctx;
+    VkSubmitInfo si{};
+    si.sType = VK_STRUCTURE_TYPE_SUBMIT_INFO;
+    si.commandBufferCount = 1;
+    si.pCommandBuffers = &r->frame_cmd;
+    if (c->record) c->record(c->queue, 0);
+    for (uint32_t i = 0; i < frames; i++) {
+        const bool wait = latency_ms != nullptr || i + 1 == frames;
+        const auto t0 = std::chrono::steady_clock::now();
+        VkResult res = c->f.vkQueueSubmit(c->queue, 1, &si, wait ? r->fence : nullptr);
+        if (res != VK_SUCCESS) return res;
+        if (wait) {
+            res = c->f.vkWaitForFences(c->device, 1, &r->fence, VK_TRUE, ~0ull);
+            c->f.vkResetFences(c->device, 1, &r->fence);
+            if (res != VK_SUCCESS) return res;
+        }
+        if (latency_ms) latency_ms[i] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    if (c->record) c->record(c->queue, 1);
+    if (device_ms) *device_ms = c->elapsed ? c->elapsed(c->queue, 0, 1) : -1.0;
+    return VK_SUCCESS;
+}
+
+int cpvh_render_e2e(cpvh_renderer* r, uint32_t frames, double* total_ms, uint64_t* h2d, uint64_t* d2h) {
+    cpvh_context* c = r->ctx;
+    const cpv_scene* s = r->scene;
+    const auto t0 = std::chrono::steady_clock::now();
+    const uint64_t out_bytes = static_cast<uint64_t>(s->width) * s->height * 4;
+    std::vector<uint8_t> host_out(out_bytes);
+    for (uint32_t i = 0; i < frames; i++) {
+        void* map = nullptr;
+        if (c->f.vkMapMemory(c->device, r->staging.memory, 0, VK_WHOLE_SIZE, 0, &map) != VK_SUCCESS) return VK_ERROR_MEMORY_MAP_FAILED;
+        fill_staging(r, map);
+        c->f.vkUnmapMemory(c->device, r->staging.memory);
+        const VkResult res = submit_and_wait(r, r->e2e_cmd);
+        if (res != VK_SUCCESS) return res;
+        if (c->f.vkMapMemory(c->device, r->readback.memory, 0, VK_WHOLE_SIZE, 0, &map) != VK_SUCCESS) return VK_ERROR_MEMORY_MAP_FAILED;
+        std::memcpy(host_out.data(), map, out_bytes);
+        c->f.vkUnmapMemory(c->device, r->readback.memory);
+    }
+    if (total_ms) *total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (h2d) *h2d = r->upload_bytes;
+    if (d2h) *d2h = out_bytes;
+    return VK_SUCCESS;
+}
+
+int cpvh_readback(cpvh_renderer* r, uint8_t* color, uint8_t* depth) {
+    cpvh_context* c = r->ctx;
+    const cpv_scene* s = r->scene;
+    VkCommandBufferBeginInfo bi{};
+    bi.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_BEGIN_INFO;
+    c->f.vkBeginCommandBuffer(r->copy_cmd, &bi);
+    record_readback(r, r->copy_cmd);
+    c->f.vkEndCommandBuffer(r->copy_cmd);
+    VkResult res = submit_and_wait(r, r->copy_cmd);
+    if (res != VK_SUCCESS) return res;
+    void* map = nullptr;
+    res = c->f.vkMapMemory(c->device, r->readback.memory, 0, VK_WHOLE_SIZE, 0, &map);
+    if (res != VK_SUCCESS) return res;
+    const uint64_t cb = static_cast<uint64_t>(s->width) * s->height * 4;
+    if (color) std::memcpy(color, map, cb);
+    if (depth && s->depth_format) std::memcpy(depth, static_cast<uint8_t*>(map) + cb, static_cast<uint64_t>(s->width) * s->height * r->depth_texel);
+    c->f.vkUnmapMemory(c->device, r->readback.memory);
+    return VK_SUCCESS;
+}
+
+}  // extern "C"

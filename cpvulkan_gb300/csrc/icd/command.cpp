@@ -1,0 +1,349 @@
+// command.cpp — replay of a recorded command buffer on a queue's CUDA stream.
+//
+// Reference counterpart: CommandBuffer::Submit / RunCommands
+// (CPVulkan/CommandBuffer.cpp:21-30, 964-968) and the Process() methods of
+// the recorded commands (CommandBuffer.Binding.cpp, CommandBuffer.Draw.cpp,
+// CommandBuffer.Copy.cpp). Where the reference executes each draw on the
+// calling thread, this enqueues the draw's kernels on the stream and returns;
+// the fence observes completion.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "icd.h"
+
+namespace cpv::icd {
+
+uint32_t encode_unorm_host(float x, float maxv) {
+    float v = x;
+    if (v != v) v = 0.0f;  // maxnum(NaN, 0) = 0
+    if (v < 0.0f) v = 0.0f;
+    if (v > 1.0f) v = 1.0f;
+    v = v * maxv;
+    return static_cast<uint32_t>(std::round(v));
+}
+
+namespace {
+
+struct BoundVertex {
+    Buffer* buffer = nullptr;
+    VkDeviceSize offset = 0;
+};
+
+struct State {
+    Pipeline* pipeline = nullptr;
+    BoundVertex vertex[8];
+    Buffer* index = nullptr;
+    VkDeviceSize index_offset = 0;
+    uint32_t index_size = 4;
+    DescriptorSet* sets[8] = {};
+    std::vector<uint32_t> dynamic_offsets[8];
+    uint8_t push[128] = {};
+    VkViewport viewport{};
+    bool viewport_set = false;
+    float blend_constants[4] = {0, 0, 0, 0};
+    bool blend_set = false;
+    RenderPass* pass = nullptr;
+    Framebuffer* fb = nullptr;
+};
+
+// Resolves the (set, binding) → dynamic offset index: dynamic descriptors are
+// numbered in binding order within the set (Vulkan rule).
+uint32_t dynamic_offset(const State& s, uint32_t set, uint32_t binding) {
+    const DescriptorSet* ds = s.sets[set];
+    if (!ds || !ds->layout) return 0;
+    uint32_t index = 0;
+    std::vector<VkDescriptorSetLayoutBinding> sorted = ds->layout->bindings;
+    std::sort(sorted.begin(), sorted.end(), [](auto& a, auto& b) { return a.binding < b.binding; });
+    for (const auto& b : sorted) {
+        const bool dyn = b.descriptorType == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC || b.descriptorType == VK_DESCRIPTOR_TYPE_STORAGE_BUFFER_DYNAMIC;
+        if (b.binding == binding) return dyn && index < s.dynamic_offsets[set].size() ? s.dynamic_offsets[set][index] : 0;
+        if (dyn) index += b.descriptorCount;
+    }
+    return 0;
+}
+
+void fill_texture(CpvTexture& t, const ImageView* view, const Sampler* sampler) {
+    std::memset(&t, 0, sizeof(t));
+    if (!view || !view->image || !view->image->memory) return;
+    const Image* img = view->image;
+    const uint32_t base = view->range.baseMipLevel;
+    uint32_t count = view->range.levelCount == VK_REMAINING_MIP_LEVELS ? img->levels - base : view->range.levelCount;
+    if (count > CPV_MAX_LEVELS) count = CPV_MAX_LEVELS;
+    const uint64_t layer_off = static_cast<uint64_t>(view->range.baseArrayLayer) * img->layer_size;
+    const uint64_t base_off = layer_off + img->level[base].offset;
+    t.data = img->device_ptr() + base_off;
+    t.bytes = img->total_size - base_off;
+    t.levels = count;
+    t.format = static_cast<uint32_t>(view->format);
+    for (uint32_t l = 0; l < count; l++) {
+        t.level_offset[l] = img->level[base + l].offset - img->level[base].offset;
+        t.level_w[l] = img->level[base + l].width;
+        t.level_h[l] = img->level[base + l].height;
+    }
+    if (sampler) {
+        const auto& s = sampler->info;
+        t.mag_filter = s.magFilter;
+        t.min_filter = s.minFilter;
+        t.mipmap_mode = s.mipmapMode;
+        t.address_u = s.addressModeU;
+        t.address_v = s.addressModeV;
+        t.border = s.borderColor;
+        t.lod_bias = s.mipLodBias;
+        t.min_lod = s.minLod;
+        t.max_lod = s.maxLod;
+    }
+}
+
+uint8_t* view_base(const ImageView* v, uint32_t& width, uint32_t& height) {
+    const Image* img = v->image;
+    const uint32_t level = v->range.baseMipLevel;
+    width = img->level[level].width;
+    height = img->level[level].height;
+    return img->device_ptr() + static_cast<uint64_t>(v->range.baseArrayLayer) * img->layer_size + img->level[level].offset;
+}
+
+VkResult begin_render_pass(Queue* q, State& s, const Cmd& c, std::vector<DeviceMemory*>& written) {
+    s.pass = static_cast<RenderPass*>(c.p[0]);
+    s.fb = static_cast<Framebuffer*>(c.p[1]);
+    if (!s.pass || !s.fb) return VK_ERROR_DEVICE_LOST;
+    for (size_t i = 0; i < s.pass->attachments.size() && i < s.fb->attachments.size(); i++) {
+        const auto& a = s.pass->attachments[i];
+        ImageView* v = s.fb->attachments[i];
+        if (!v || !v->image || !v->image->memory) continue;
+        written.push_back(v->image->memory);
+        const bool depth = format_is_depth(a.format);
+        const bool clear = a.loadOp == VK_ATTACHMENT_LOAD_OP_CLEAR || (depth && format_has_stencil(a.format) && a.stencilLoadOp == VK_ATTACHMENT_LOAD_OP_CLEAR);
+        if (!clear || i >= c.clears.size()) continue;
+        uint32_t w, h;
+        uint8_t* base = view_base(v, w, h);
+        const uint64_t texels = static_cast<uint64_t>(w) * h;
+        const VkClearValue& cv = c.clears[i];
+        int r = rt::kOk;
+        if (!depth) {
+            // ClearImage → SetPixel through the format encoder
+            // (CPVulkan/CommandBuffer.Draw.cpp:117-149).
+            uint32_t packed = 0;
+            const int shift_bgra[4] = {16, 8, 0, 24};
+            for (int ch = 0; ch < 4; ch++) {
+                const uint32_t b = encode_unorm_host(cv.color.float32[ch], 255.0f);
+                const int sh = a.format == VK_FORMAT_B8G8R8A8_UNORM ? shift_bgra[ch] : 8 * ch;
+                packed |= b << sh;
+            }
+            r = rt::fill(q->stream, base, texels, 4, packed, 0);
+        } else if (a.format == VK_FORMAT_D16_UNORM) {
+            r = rt::fill(q->stream, base, texels, 2, encode_unorm_host(cv.depthStencil.depth, 65535.0f), 0);
+        } else if (a.format == VK_FORMAT_D32_SFLOAT) {
+            uint32_t bits;
+            std::memcpy(&bits, &cv.depthStencil.depth, 4);
+            r = rt::fill(q->stream, base, texels, 4, bits, 0);
+        } else if (a.format == VK_FORMAT_D32_SFLOAT_S8_UINT) {
+            uint32_t bits;
+            std::memcpy(&bits, &cv.depthStencil.depth, 4);
+            r = rt::fill(q->stream, base, texels, 8, bits, cv.depthStencil.stencil & 0xFFu);
+        }
+        if (r != rt::kOk) return VK_ERROR_DEVICE_LOST;
+    }
+    return VK_SUCCESS;
+}
+
+VkResult draw(Queue* q, State& s, uint32_t count, uint32_t instances, uint32_t first, int32_t vertex_offset, uint32_t first_instance, bool indexed) {
+    Pipeline* p = s.pipeline;
+    if (!p || !s.pass || !s.fb) return VK_ERROR_DEVICE_LOST;
+    CpvDrawParams P;
+    std::memset(&P, 0, sizeof(P));
+    for (int b = 0; b < 8; b++) {
+        const BoundVertex& bv = s.vertex[b];
+        if (!bv.buffer || !bv.buffer->memory) continue;
+        P.vb[b] = bv.buffer->device_ptr(bv.offset);
+        P.vb_bytes[b] = bv.offset < bv.buffer->size ? bv.buffer->size - bv.offset : 0;
+    }
+    if (indexed) {
+        if (!s.index || !s.index->memory) return VK_ERROR_DEVICE_LOST;
+        P.ib = s.index->device_ptr(s.index_offset);
+        P.ib_bytes = s.index_offset < s.index->size ? s.index->size - s.index_offset : 0;
+        P.index_size = s.index_size;
+    }
+    P.count = count;
+    P.first = first;
+    P.vertex_offset = vertex_offset;
+    P.first_instance = first_instance;
+    P.instance_count = instances;
+    uint32_t ppi = 0;
+    if (p->topology == VK_PRIMITIVE_TOPOLOGY_TRIANGLE_LIST) ppi = count / 3;
+    else ppi = count > 2 ? count - 2 : 0;
+    P.prims_per_instance = ppi;
+    P.total_prims = static_cast<uint64_t>(ppi) * instances;
+    if (P.total_prims == 0) return VK_SUCCESS;
+    for (const auto& slot : p->slots) {
+        if (slot.set >= 8 || !s.sets[slot.set]) continue;
+        auto it = s.sets[slot.set]->bindings.find(slot.binding);
+        if (it == s.sets[slot.set]->bindings.end() || it->second.empty()) continue;
+        const Descriptor& d = it->second[0];
+        if (slot.is_texture) {
+            fill_texture(P.tex[slot.slot], d.view, d.sampler);
+        } else if (d.buffer && d.buffer->memory) {
+            const uint64_t dyn = (d.type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC) ? dynamic_offset(s, slot.set, slot.binding) : 0;
+            const uint64_t off = d.offset + dyn;
+            uint64_t range = d.range == VK_WHOLE_SIZE ? (d.buffer->size > off ? d.buffer->size - off : 0) : d.range;
+            if (off + range > d.buffer->size) range = d.buffer->size > off ? d.buffer->size - off : 0;
+            P.ubo[slot.slot] = d.buffer->device_ptr(off);
+            P.ubo_bytes[slot.slot] = range;
+        }
+    }
+    std::memcpy(P.push, s.push, sizeof(P.push));
+    // Attachments of subpass 0.
+    ImageView* cv = s.fb->attachments[s.pass->colour[0]];
+    uint32_t w = 0, h = 0;
+    P.color = view_base(cv, w, h);
+    P.fb_width = w < s.fb->width ? w : s.fb->width;
+    P.fb_height = h < s.fb->height ? h : s.fb->height;
+    // Attachment addressing uses the image row length.
+    P.fb_width = w;
+    P.fb_height = h;
+    if (s.pass->depth != VK_ATTACHMENT_UNUSED) {
+        uint32_t dw, dh;
+        P.depth = view_base(s.fb->attachments[s.pass->depth], dw, dh);
+        if (dw != w || dh != h) return VK_ERROR_DEVICE_LOST;
+    }
+    const VkViewport vp = p->dynamic_viewport ? s.viewport : p->viewport;
+    P.viewport[0] = vp.x;
+    P.viewport[1] = vp.y;
+    P.viewport[2] = vp.width;
+    P.viewport[3] = vp.height;
+    P.viewport[4] = vp.minDepth;
+    P.viewport[5] = vp.maxDepth;
+    for (int i = 0; i < 4; i++) P.blend_constants[i] = p->dynamic_blend_constants ? s.blend_constants[i] : p->blend_constants[i];
+    const int r = rt::draw_plain(q->stream, p->module, P, q->scratch);
+    return r == rt::kOk ? VK_SUCCESS : VK_ERROR_DEVICE_LOST;
+}
+
+}  // namespace
+
+VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& written) {
+    State s;
+    for (const Cmd& c : cb->cmds) {
+        VkResult r = VK_SUCCESS;
+        switch (c.type) {
+        case CmdType::BeginRenderPass: r = begin_render_pass(q, s, c, written); break;
+        case CmdType::EndRenderPass: s.pass = nullptr; s.fb = nullptr; break;
+        case CmdType::BindPipeline: s.pipeline = static_cast<Pipeline*>(c.p[0]); break;
+        case CmdType::BindVertexBuffers:
+            for (uint32_t i = 0; i < c.u[1]; i++) {
+                const uint32_t slot = c.u[0] + i;
+                if (slot < 8) {
+                    s.vertex[slot].buffer = reinterpret_cast<Buffer*>(c.list[2 * i]);
+                    s.vertex[slot].offset = c.list[2 * i + 1];
+                }
+            }
+            break;
+        case CmdType::BindIndexBuffer:
+            s.index = static_cast<Buffer*>(c.p[0]);
+            s.index_offset = c.q[0];
+            s.index_size = c.u[0] == VK_INDEX_TYPE_UINT16 ? 2 : 4;
+            break;
+        case CmdType::BindDescriptorSets: {
+            const uint32_t first = c.u[0], count = c.u[1];
+            uint32_t dyn_used = 0;
+            for (uint32_t i = 0; i < count && first + i < 8; i++) {
+                DescriptorSet* ds = reinterpret_cast<DescriptorSet*>(c.list[i]);
+                s.sets[first + i] = ds;
+                s.dynamic_offsets[first + i].clear();
+                if (!ds || !ds->layout) continue;
+                for (const auto& b : ds->layout->bindings)
+                    if (b.descriptorType == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC || b.descriptorType == VK_DESCRIPTOR_TYPE_STORAGE_BUFFER_DYNAMIC)
+                        for (uint32_t k = 0; k < b.descriptorCount && dyn_used < c.u[2]; k++)
+                            s.dynamic_offsets[first + i].push_back(static_cast<uint32_t>(c.list[count + dyn_used++]));
+            }
+            break;
+        }
+        case CmdType::PushConstants: {
+            const uint32_t off = c.u[0];
+            const size_t n = c.bytes.size();
+            if (off < 128) std::memcpy(s.push + off, c.bytes.data(), off + n <= 128 ? n : 128 - off);
+            break;
+        }
+        case CmdType::SetViewport: s.viewport = c.viewport; s.viewport_set = true; break;
+        case CmdType::SetScissor: break;
+        case CmdType::SetBlendConstants:
+            std::memcpy(s.blend_constants, c.bytes.data(), 16);
+            s.blend_set = true;
+            break;
+        case CmdType::Draw: r = draw(q, s, c.u[0], c.u[1], c.u[2], 0, c.u[3], false); break;
+        case CmdType::DrawIndexed: r = draw(q, s, c.u[0], c.u[1], c.u[2], c.i0, c.u[3], true); break;
+        case CmdType::CopyBuffer: {
+            Buffer* src = static_cast<Buffer*>(c.p[0]);
+            Buffer* dst = static_cast<Buffer*>(c.p[1]);
+            for (const auto& reg : c.buffer_regions) {
+                if (reg.srcOffset + reg.size > src->size || reg.dstOffset + reg.size > dst->size) return VK_ERROR_DEVICE_LOST;
+                if (cudaMemcpyAsync(dst->device_ptr(reg.dstOffset), src->device_ptr(reg.srcOffset), reg.size, cudaMemcpyDeviceToDevice, q->stream) != cudaSuccess)
+                    return VK_ERROR_DEVICE_LOST;
+            }
+            written.push_back(dst->memory);
+            break;
+        }
+        case CmdType::CopyBufferToImage:
+        case CmdType::CopyImageToBuffer: {
+            const bool to_image = c.type == CmdType::CopyBufferToImage;
+            Buffer* buf = static_cast<Buffer*>(c.p[0]);
+            Image* img = static_cast<Image*>(c.p[1]);
+            for (const auto& reg : c.image_regions) {
+                const uint32_t level = reg.imageSubresource.mipLevel;
+                if (level >= img->levels) return VK_ERROR_DEVICE_LOST;
+                const ImageLevel& L = img->level[level];
+                const uint32_t texel = img->texel;
+                const uint32_t row_len = reg.bufferRowLength ? reg.bufferRowLength : reg.imageExtent.width;
+                const uint32_t img_h = reg.bufferImageHeight ? reg.bufferImageHeight : reg.imageExtent.height;
+                for (uint32_t layer = 0; layer < reg.imageSubresource.layerCount; layer++) {
+                    for (uint32_t z = 0; z < reg.imageExtent.depth; z++) {
+                        const uint64_t img_off = static_cast<uint64_t>(reg.imageSubresource.baseArrayLayer + layer) * img->layer_size + L.offset +
+                                                 static_cast<uint64_t>(reg.imageOffset.z + z) * L.plane + static_cast<uint64_t>(reg.imageOffset.y) * L.stride +
+                                                 static_cast<uint64_t>(reg.imageOffset.x) * texel;
+                        const uint64_t buf_off = reg.bufferOffset + (static_cast<uint64_t>(layer) * reg.imageExtent.depth + z) * row_len * img_h * texel;
+                        const uint64_t width_bytes = static_cast<uint64_t>(reg.imageExtent.width) * texel;
+                        if (buf_off + static_cast<uint64_t>(row_len) * texel * (reg.imageExtent.height - 1) + width_bytes > buf->size) return VK_ERROR_DEVICE_LOST;
+                        if (img_off + L.stride * (reg.imageExtent.height - 1) + width_bytes > img->total_size) return VK_ERROR_DEVICE_LOST;
+                        uint8_t* ip = img->device_ptr() + img_off;
+                        uint8_t* bp = buf->device_ptr(buf_off);
+                        cudaError_t e;
+                        if (to_image)
+                            e = cudaMemcpy2DAsync(ip, L.stride, bp, static_cast<size_t>(row_len) * texel, width_bytes, reg.imageExtent.height, cudaMemcpyDeviceToDevice, q->stream);
+                        else
+                            e = cudaMemcpy2DAsync(bp, static_cast<size_t>(row_len) * texel, ip, L.stride, width_bytes, reg.imageExtent.height, cudaMemcpyDeviceToDevice, q->stream);
+                        if (e != cudaSuccess) return VK_ERROR_DEVICE_LOST;
+                    }
+                }
+            }
+            written.push_back(to_image ? img->memory : buf->memory);
+            break;
+        }
+        case CmdType::FillBuffer: {
+            Buffer* dst = static_cast<Buffer*>(c.p[0]);
+            uint64_t off = c.q[0], size = c.q[1];
+            if (size == VK_WHOLE_SIZE) size = (dst->size - off) & ~3ull;
+            if (off + size > dst->size) return VK_ERROR_DEVICE_LOST;
+            if (rt::fill(q->stream, dst->device_ptr(off), size / 4, 4, c.u[0], 0) != rt::kOk) return VK_ERROR_DEVICE_LOST;
+            written.push_back(dst->memory);
+            break;
+        }
+        case CmdType::UpdateBuffer: {
+            Buffer* dst = static_cast<Buffer*>(c.p[0]);
+            if (c.q[0] + c.bytes.size() > dst->size) return VK_ERROR_DEVICE_LOST;
+            // The command owns its bytes until the command buffer is reset;
+            // the copy is ordered on the stream.
+            if (cudaMemcpyAsync(dst->device_ptr(c.q[0]), c.bytes.data(), c.bytes.size(), cudaMemcpyHostToDevice, q->stream) != cudaSuccess)
+                return VK_ERROR_DEVICE_LOST;
+            written.push_back(dst->memory);
+            break;
+        }
+        case CmdType::Barrier:
+        case CmdType::DrawIndirect:
+        case CmdType::DrawIndexedIndirect:
+            break;
+        }
+        if (r != VK_SUCCESS) return r;
+    }
+    return VK_SUCCESS;
+}
+
+}  // namespace cpv::icd

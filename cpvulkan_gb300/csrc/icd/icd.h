@@ -1,0 +1,245 @@
+// icd.h — object model of the cpvulkan_gb300 Vulkan ICD.
+//
+// Mirrors the reference ICD's objects (CPVulkan/Instance.h, Device.h,
+// Buffer.h, Image.h, Pipeline.h, CommandBuffer.h, Queue.h ...) with GB300
+// storage: VkDeviceMemory is a cudaMalloc allocation in HBM (plus a pinned
+// host mirror for host-visible memory types), buffers and images are
+// sub-ranges of it, and a queue is a CUDA stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <array>
+#include <atomic>
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "../../../include/cpv/vk_subset.h"
+#include "../runtime/runtime.h"
+#include "../spirv/spirv.h"
+
+namespace cpv::icd {
+
+// Dispatchable objects start with the loader's word (ICD_LOADER_MAGIC until
+// the loader stores its dispatch table there).
+struct Dispatchable {
+    uintptr_t loader_data = ICD_LOADER_MAGIC;
+};
+
+struct PhysicalDevice;
+struct Device;
+struct Queue;
+
+struct Instance : Dispatchable {
+    PhysicalDevice* physical = nullptr;
+    uint32_t api_version = VK_API_VERSION_1_1;
+};
+
+struct PhysicalDevice : Dispatchable {
+    Instance* instance = nullptr;
+};
+
+struct DeviceMemory {
+    uint8_t* device = nullptr;     // HBM
+    uint8_t* host = nullptr;       // pinned mirror (host-visible types)
+    VkDeviceSize size = 0;
+    uint32_t type = 0;
+    bool mapped = false;
+    bool device_dirty = false;     // HBM newer than the mirror
+};
+
+struct Buffer {
+    VkDeviceSize size = 0;
+    VkBufferUsageFlags usage = 0;
+    DeviceMemory* memory = nullptr;
+    VkDeviceSize offset = 0;
+    uint8_t* device_ptr(VkDeviceSize at = 0) const { return memory ? memory->device + offset + at : nullptr; }
+};
+
+// Linear image layout of the reference (CPVulkanBase/Formats.cpp:453-484):
+// levels concatenated inside each layer, tightly packed rows.
+struct ImageLevel {
+    uint64_t offset = 0;
+    uint32_t width = 0, height = 0, depth = 0;
+    uint64_t stride = 0, plane = 0, size = 0;
+};
+
+struct Image {
+    VkFormat format = VK_FORMAT_UNDEFINED;
+    uint32_t texel = 0;
+    VkExtent3D extent{};
+    uint32_t levels = 1, layers = 1;
+    std::vector<ImageLevel> level;
+    uint64_t layer_size = 0, total_size = 0;
+    DeviceMemory* memory = nullptr;
+    VkDeviceSize offset = 0;
+    uint8_t* device_ptr() const { return memory ? memory->device + offset : nullptr; }
+};
+
+struct ImageView {
+    Image* image = nullptr;
+    VkFormat format = VK_FORMAT_UNDEFINED;
+    VkImageSubresourceRange range{};
+    VkComponentMapping components{};
+};
+
+struct Sampler {
+    VkSamplerCreateInfo info{};
+};
+
+struct ShaderModule {
+    std::vector<uint32_t> words;
+    spirv::Module module;
+};
+
+struct DescriptorSetLayout {
+    std::vector<VkDescriptorSetLayoutBinding> bindings;
+    std::vector<std::vector<Sampler*>> immutable;
+};
+
+struct Descriptor {
+    VkDescriptorType type = VK_DESCRIPTOR_TYPE_MAX_ENUM;
+    Buffer* buffer = nullptr;
+    VkDeviceSize offset = 0, range = 0;
+    ImageView* view = nullptr;
+    Sampler* sampler = nullptr;
+};
+
+struct DescriptorSet {
+    DescriptorSetLayout* layout = nullptr;
+    std::map<uint32_t, std::vector<Descriptor>> bindings;
+};
+
+struct DescriptorPool {
+    std::set<DescriptorSet*> sets;
+};
+
+struct PipelineLayout {
+    std::vector<DescriptorSetLayout*> sets;
+    std::vector<VkPushConstantRange> push;
+};
+
+struct RenderPass {
+    std::vector<VkAttachmentDescription> attachments;
+    std::vector<uint32_t> colour;     // subpass 0 colour attachment indices
+    uint32_t depth = VK_ATTACHMENT_UNUSED;
+};
+
+struct Framebuffer {
+    RenderPass* pass = nullptr;
+    std::vector<ImageView*> attachments;
+    uint32_t width = 0, height = 0, layers = 1;
+};
+
+struct PipelineCache {
+    std::mutex mutex;
+    std::map<std::array<uint8_t, 32>, std::vector<uint8_t>> entries;  // key → cubin
+};
+
+struct Pipeline {
+    rt::Module module;
+    std::array<uint8_t, 32> key{};
+    std::vector<spirv::ResourceSlot> slots;
+    VkPrimitiveTopology topology = VK_PRIMITIVE_TOPOLOGY_TRIANGLE_LIST;
+    VkViewport viewport{};
+    bool dynamic_viewport = false;
+    bool dynamic_blend_constants = false;
+    float blend_constants[4] = {0, 0, 0, 0};
+    PipelineLayout* layout = nullptr;
+    uint32_t colour_format = 0, depth_format = 0;
+    bool blend = false;
+    std::string source;  // generated CUDA translation unit (diagnostics)
+};
+
+// ---- command recording ----
+enum class CmdType : uint8_t {
+    BeginRenderPass, EndRenderPass, BindPipeline, BindVertexBuffers, BindIndexBuffer, BindDescriptorSets, PushConstants,
+    SetViewport, SetScissor, SetBlendConstants, Draw, DrawIndexed, DrawIndirect, DrawIndexedIndirect, CopyBuffer,
+    CopyBufferToImage, CopyImageToBuffer, FillBuffer, UpdateBuffer, Barrier,
+};
+
+struct Cmd {
+    CmdType type;
+    // generic fields (meaning depends on type)
+    uint32_t u[8] = {};
+    int32_t i0 = 0;
+    uint64_t q[4] = {};
+    void* p[4] = {};
+    std::vector<uint8_t> bytes;
+    std::vector<uint64_t> list;
+    std::vector<VkBufferImageCopy> image_regions;
+    std::vector<VkBufferCopy> buffer_regions;
+    std::vector<VkClearValue> clears;
+    VkViewport viewport{};
+};
+
+struct CommandBuffer : Dispatchable {
+    Device* device = nullptr;
+    std::vector<Cmd> cmds;
+    bool recording = false;
+};
+
+struct CommandPool {
+    std::set<CommandBuffer*> buffers;
+};
+
+struct Fence {
+    cudaEvent_t event = nullptr;
+    bool signalled = false;   // created signalled or completed and observed
+    bool pending = false;     // a submission will record the event
+    std::vector<DeviceMemory*> readback;  // host-visible memories written by the submission
+};
+
+struct Semaphore {
+    cudaEvent_t event = nullptr;
+    bool signalled = false;
+};
+
+struct Queue : Dispatchable {
+    Device* device = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t timing[16] = {};
+    rt::Scratch scratch;
+    std::vector<DeviceMemory*> pending_readback;
+    std::mutex mutex;
+};
+
+struct Device : Dispatchable {
+    PhysicalDevice* physical = nullptr;
+    // No CUDA device and CPV_COMPILE_ONLY=1: pipelines are translated and
+    // compiled with NVRTC but not loaded; memory is host memory; submissions
+    // fail with VK_ERROR_DEVICE_LOST. Used to check pipeline compilation on
+    // machines without a GPU.
+    bool compile_only = false;
+    Queue* queue = nullptr;
+    std::mutex cache_mutex;
+    std::map<std::array<uint8_t, 32>, std::vector<uint8_t>> module_cache;  // in-process NVRTC cubin cache
+    std::set<DeviceMemory*> memories;
+    std::mutex memory_mutex;
+};
+
+// Execution of a recorded command buffer on a queue (command.cpp).
+VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& written);
+
+// Pipeline creation (pipeline.cpp).
+VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGraphicsPipelineCreateInfo& info, Pipeline** out);
+
+// SHA3-256 (sha3.cpp), FIPS 202.
+std::array<uint8_t, 32> sha3_256(const void* data, size_t size);
+
+// Format helpers.
+uint32_t format_texel_size(VkFormat f);
+bool format_is_depth(VkFormat f);
+bool format_has_stencil(VkFormat f);
+void image_layout(Image& img);
+
+// Host-side encode of clear values with the reference's codecs
+// (LLVMRuntime/ImageCompiler.cpp:869-947, 1081-1095).
+uint32_t encode_unorm_host(float x, float maxv);
+
+}  // namespace cpv::icd

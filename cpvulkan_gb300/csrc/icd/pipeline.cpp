@@ -1,0 +1,283 @@
+// pipeline.cpp — vkCreateGraphicsPipelines: state validation, SPIR-V → CUDA
+// translation of both stages, the pipeline translation unit, the SHA3 cache
+// key, NVRTC compilation for sm_103a and module loading.
+//
+// Reference counterpart: GraphicsPipeline::Create / Parse
+// (CPVulkan/Pipeline.cpp:43-714), CompileBaseShaderModule / CalculateHash
+// (:540-597, :735-763), and the pipeline wrappers of
+// LLVMRuntime/PipelineCompiler.cpp, which bake the fixed-function state into
+// the JIT module exactly as the CPV_* constants below bake it into the
+// NVRTC module. Unsupported state is rejected with a VkResult instead of the
+// reference's abort.
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <sstream>
+
+#include "icd.h"
+
+namespace cpv::icd {
+
+namespace {
+
+const char* kTranslationVersion = "cpvulkan_gb300 pipeline v1";
+
+uint32_t tile_shift_for_pipeline() {
+    const char* v = std::getenv("CPV_TILE");
+    if (!v) return 4;
+    const int t = std::atoi(v);
+    if (t == 8) return 3;
+    if (t == 32) return 5;
+    return 4;
+}
+
+std::string cache_dir() {
+    const char* v = std::getenv("CPV_CACHE_DIR");
+    return v ? std::string(v) : std::string();
+}
+
+std::string hex(const std::array<uint8_t, 32>& k) {
+    static const char* d = "0123456789abcdef";
+    std::string s;
+    for (uint8_t b : k) {
+        s.push_back(d[b >> 4]);
+        s.push_back(d[b & 15]);
+    }
+    return s;
+}
+
+bool supported_colour(VkFormat f) { return f == VK_FORMAT_R8G8B8A8_UNORM || f == VK_FORMAT_B8G8R8A8_UNORM; }
+bool supported_depth(VkFormat f) { return f == VK_FORMAT_D16_UNORM || f == VK_FORMAT_D32_SFLOAT || f == VK_FORMAT_D32_SFLOAT_S8_UINT; }
+
+}  // namespace
+
+VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGraphicsPipelineCreateInfo& ci, Pipeline** out) {
+    auto reject = [&](const std::string& why) {
+        rt::set_last_error("vkCreateGraphicsPipelines: " + why);
+        return VK_ERROR_FEATURE_NOT_PRESENT;
+    };
+    const ShaderModule* vs = nullptr;
+    const ShaderModule* fs = nullptr;
+    std::string vs_entry, fs_entry;
+    std::vector<spirv::SpecConstant> vs_spec, fs_spec;
+    for (uint32_t i = 0; i < ci.stageCount; i++) {
+        const auto& st = ci.pStages[i];
+        std::vector<spirv::SpecConstant> spec;
+        if (st.pSpecializationInfo) {
+            const auto* si = st.pSpecializationInfo;
+            for (uint32_t k = 0; k < si->mapEntryCount; k++) {
+                spirv::SpecConstant sc;
+                sc.id = si->pMapEntries[k].constantID;
+                const uint8_t* b = static_cast<const uint8_t*>(si->pData) + si->pMapEntries[k].offset;
+                sc.bytes.assign(b, b + si->pMapEntries[k].size);
+                spec.push_back(sc);
+            }
+        }
+        if (st.stage == VK_SHADER_STAGE_VERTEX_BIT) {
+            vs = reinterpret_cast<const ShaderModule*>(st.module);
+            vs_entry = st.pName ? st.pName : "main";
+            vs_spec = spec;
+        } else if (st.stage == VK_SHADER_STAGE_FRAGMENT_BIT) {
+            fs = reinterpret_cast<const ShaderModule*>(st.module);
+            fs_entry = st.pName ? st.pName : "main";
+            fs_spec = spec;
+        } else {
+            return reject("only vertex and fragment stages are supported");
+        }
+    }
+    if (!vs || !fs) return reject("a vertex and a fragment stage are required");
+    if (!ci.pInputAssemblyState || !ci.pRasterizationState || !ci.pVertexInputState) return reject("missing fixed-function state");
+    const auto topo = ci.pInputAssemblyState->topology;
+    if (topo != VK_PRIMITIVE_TOPOLOGY_TRIANGLE_LIST && topo != VK_PRIMITIVE_TOPOLOGY_TRIANGLE_STRIP && topo != VK_PRIMITIVE_TOPOLOGY_TRIANGLE_FAN)
+        return reject("only triangle topologies are implemented");
+    if (ci.pInputAssemblyState->primitiveRestartEnable) return reject("primitive restart");
+    const auto& rs = *ci.pRasterizationState;
+    if (rs.rasterizerDiscardEnable) return reject("rasterizer discard");
+    if (rs.polygonMode != VK_POLYGON_MODE_FILL) return reject("non-fill polygon mode");
+    if (rs.depthClampEnable) return reject("depth clamp");
+    if (ci.pMultisampleState && ci.pMultisampleState->rasterizationSamples > 1) return reject("multisampling");
+
+    const RenderPass* pass = reinterpret_cast<const RenderPass*>(ci.renderPass);
+    if (!pass) return reject("no render pass");
+    if (pass->colour.size() != 1) return reject("exactly one colour attachment is supported");
+    const VkFormat cfmt = pass->attachments[pass->colour[0]].format;
+    if (!supported_colour(cfmt)) return reject("colour attachment format " + std::to_string(cfmt));
+    VkFormat dfmt = VK_FORMAT_UNDEFINED;
+    if (pass->depth != VK_ATTACHMENT_UNUSED) {
+        dfmt = pass->attachments[pass->depth].format;
+        if (!supported_depth(dfmt)) return reject("depth attachment format " + std::to_string(dfmt));
+    }
+
+    VkPipelineDepthStencilStateCreateInfo ds{};
+    if (ci.pDepthStencilState) ds = *ci.pDepthStencilState;
+    if (ds.depthBoundsTestEnable) return reject("depth bounds test");
+    const bool stencil = ds.stencilTestEnable && dfmt == VK_FORMAT_D32_SFLOAT_S8_UINT;
+
+    VkPipelineColorBlendAttachmentState blend{};
+    blend.colorWriteMask = 0xF;
+    float blend_constants[4] = {0, 0, 0, 0};
+    if (ci.pColorBlendState) {
+        if (ci.pColorBlendState->logicOpEnable) return reject("logic op");
+        if (ci.pColorBlendState->attachmentCount >= 1) blend = ci.pColorBlendState->pAttachments[0];
+        for (int i = 0; i < 4; i++) blend_constants[i] = ci.pColorBlendState->blendConstants[i];
+    }
+    if (blend.blendEnable) {
+        auto bad = [](VkBlendFactor f) { return f > VK_BLEND_FACTOR_SRC_ALPHA_SATURATE; };
+        if (bad(blend.srcColorBlendFactor) || bad(blend.dstColorBlendFactor) || bad(blend.srcAlphaBlendFactor) || bad(blend.dstAlphaBlendFactor))
+            return reject("dual-source blend factors");
+        if (blend.colorBlendOp > VK_BLEND_OP_MAX || blend.alphaBlendOp > VK_BLEND_OP_MAX) return reject("advanced blend ops");
+    }
+
+    bool dyn_viewport = false, dyn_blend = false;
+    if (ci.pDynamicState) {
+        for (uint32_t i = 0; i < ci.pDynamicState->dynamicStateCount; i++) {
+            const auto d = ci.pDynamicState->pDynamicStates[i];
+            if (d == VK_DYNAMIC_STATE_VIEWPORT) dyn_viewport = true;
+            else if (d == VK_DYNAMIC_STATE_BLEND_CONSTANTS) dyn_blend = true;
+            else if (d == VK_DYNAMIC_STATE_SCISSOR || d == VK_DYNAMIC_STATE_LINE_WIDTH || d == VK_DYNAMIC_STATE_DEPTH_BIAS) continue;
+            else return reject("dynamic state " + std::to_string(d));
+        }
+    }
+    VkViewport viewport{};
+    if (!dyn_viewport) {
+        if (!ci.pViewportState || ci.pViewportState->viewportCount != 1 || !ci.pViewportState->pViewports)
+            return reject("exactly one static viewport is required");
+        viewport = ci.pViewportState->pViewports[0];
+    }
+
+    // Vertex input state → translator view.
+    std::vector<spirv::VertexBinding> bindings;
+    std::vector<spirv::VertexAttribute> attributes;
+    for (uint32_t i = 0; i < ci.pVertexInputState->vertexBindingDescriptionCount; i++) {
+        const auto& b = ci.pVertexInputState->pVertexBindingDescriptions[i];
+        bindings.push_back({b.binding, b.stride, static_cast<uint32_t>(b.inputRate)});
+    }
+    for (uint32_t i = 0; i < ci.pVertexInputState->vertexAttributeDescriptionCount; i++) {
+        const auto& a = ci.pVertexInputState->pVertexAttributeDescriptions[i];
+        attributes.push_back({a.location, a.binding, static_cast<uint32_t>(a.format), a.offset});
+    }
+
+    // Translate both stages.
+    std::vector<spirv::ResourceSlot> slots;
+    spirv::StageResult vr, fr;
+    std::string err;
+    if (!spirv::translate_stage(vs->module, 0, vs_entry, vs_spec, bindings, attributes, slots, vr, err)) return reject("vertex shader: " + err);
+    if (!spirv::translate_stage(fs->module, 4, fs_entry, fs_spec, {}, {}, slots, fr, err)) return reject("fragment shader: " + err);
+
+    const uint32_t nv = vr.num_floats > fr.num_floats ? vr.num_floats : fr.num_floats;
+    const uint32_t tile_shift = tile_shift_for_pipeline();
+    std::ostringstream src;
+    src << "// " << kTranslationVersion << "\n";
+    src << "#define CPV_TILE_SHIFT " << tile_shift << "\n";
+    src << "#define CPV_NV " << nv << "\n";
+    src << "#define CPV_TOPOLOGY " << static_cast<uint32_t>(topo) << "\n";
+    src << "#define CPV_CULL_MODE " << rs.cullMode << "\n";
+    src << "#define CPV_FRONT_CW " << (rs.frontFace == VK_FRONT_FACE_CLOCKWISE ? 1 : 0) << "\n";
+    src << "#define CPV_DEPTH_TEST " << (ds.depthTestEnable ? 1 : 0) << "\n";
+    src << "#define CPV_DEPTH_WRITE " << (ds.depthWriteEnable ? 1 : 0) << "\n";
+    src << "#define CPV_DEPTH_OP " << static_cast<uint32_t>(ds.depthCompareOp) << "\n";
+    src << "#define CPV_STENCIL_TEST " << (stencil ? 1 : 0) << "\n";
+    const VkStencilOpState* so[2] = {&ds.front, &ds.back};
+    const char* sn[2] = {"F", "B"};
+    for (int k = 0; k < 2; k++) {
+        src << "#define CPV_ST_" << sn[k] << "_FAIL " << static_cast<uint32_t>(so[k]->failOp) << "\n";
+        src << "#define CPV_ST_" << sn[k] << "_PASS " << static_cast<uint32_t>(so[k]->passOp) << "\n";
+        src << "#define CPV_ST_" << sn[k] << "_DFAIL " << static_cast<uint32_t>(so[k]->depthFailOp) << "\n";
+        src << "#define CPV_ST_" << sn[k] << "_OP " << static_cast<uint32_t>(so[k]->compareOp) << "\n";
+        src << "#define CPV_ST_" << sn[k] << "_CMASK " << so[k]->compareMask << "u\n";
+        src << "#define CPV_ST_" << sn[k] << "_WMASK " << so[k]->writeMask << "u\n";
+        src << "#define CPV_ST_" << sn[k] << "_REF " << so[k]->reference << "u\n";
+    }
+    src << "#define CPV_BLEND " << (blend.blendEnable ? 1 : 0) << "\n";
+    src << "#define CPV_SRC_COLOR " << static_cast<uint32_t>(blend.srcColorBlendFactor) << "\n";
+    src << "#define CPV_DST_COLOR " << static_cast<uint32_t>(blend.dstColorBlendFactor) << "\n";
+    src << "#define CPV_COLOR_OP " << static_cast<uint32_t>(blend.colorBlendOp) << "\n";
+    src << "#define CPV_SRC_ALPHA " << static_cast<uint32_t>(blend.srcAlphaBlendFactor) << "\n";
+    src << "#define CPV_DST_ALPHA " << static_cast<uint32_t>(blend.dstAlphaBlendFactor) << "\n";
+    src << "#define CPV_ALPHA_OP " << static_cast<uint32_t>(blend.alphaBlendOp) << "\n";
+    src << "#define CPV_WRITE_MASK " << (blend.colorWriteMask & 0xF) << "u\n";
+    src << "#define CPV_COLOR_FORMAT " << static_cast<uint32_t>(cfmt) << "\n";
+    src << "#define CPV_DEPTH_FORMAT " << static_cast<uint32_t>(dfmt) << "\n";
+    src << "#define CPV_ORIGIN_UPPER " << (fr.origin_upper_left ? 1 : 0) << "\n";
+    src << "#include \"cpv_device.cuh\"\n";
+    src << vr.code << fr.code;
+    src << "__device__ __forceinline__ int cpv_interp(int c) {\n  switch (c) {\n";
+    for (size_t i = 0; i < fr.interp.size(); i++)
+        if (fr.interp[i] != 0) src << "  case " << i << ": return " << fr.interp[i] << ";\n";
+    src << "  default: return 0;\n  }\n}\n";
+    src << "#include \"cpv_pipeline.cuh\"\n";
+
+    auto p = std::make_unique<Pipeline>();
+    p->source = src.str();
+    p->key = sha3_256(p->source.data(), p->source.size());
+    p->slots = slots;
+    p->topology = topo;
+    p->viewport = viewport;
+    p->dynamic_viewport = dyn_viewport;
+    p->dynamic_blend_constants = dyn_blend;
+    for (int i = 0; i < 4; i++) p->blend_constants[i] = blend_constants[i];
+    p->layout = reinterpret_cast<PipelineLayout*>(ci.layout);
+    p->colour_format = cfmt;
+    p->depth_format = dfmt;
+    p->blend = blend.blendEnable != 0;
+
+    // Cubin: pipeline cache object → in-process cache → disk cache → NVRTC.
+    std::vector<uint8_t> cubin;
+    bool found = false;
+    if (cache) {
+        std::lock_guard<std::mutex> lock(cache->mutex);
+        auto it = cache->entries.find(p->key);
+        if (it != cache->entries.end()) {
+            cubin = it->second;
+            found = true;
+        }
+    }
+    if (!found) {
+        std::lock_guard<std::mutex> lock(dev->cache_mutex);
+        auto it = dev->module_cache.find(p->key);
+        if (it != dev->module_cache.end()) {
+            cubin = it->second;
+            found = true;
+        }
+    }
+    const std::string dir = cache_dir();
+    if (!found && !dir.empty()) {
+        std::ifstream f(dir + "/" + hex(p->key) + ".cubin", std::ios::binary);
+        if (f) {
+            cubin.assign(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
+            found = !cubin.empty();
+        }
+    }
+    if (!found) {
+        std::string log;
+        if (rt::compile(p->source, "pipeline_" + hex(p->key).substr(0, 12) + ".cu", cubin, log) != rt::kOk) {
+            rt::set_last_error("NVRTC failed: " + log);
+            if (std::getenv("CPV_DUMP_FAILED")) std::fprintf(stderr, "%s\n----\n%s\n", p->source.c_str(), log.c_str());
+            return VK_ERROR_INITIALIZATION_FAILED;
+        }
+        if (!dir.empty()) {
+            std::ofstream f(dir + "/" + hex(p->key) + ".cubin", std::ios::binary);
+            f.write(reinterpret_cast<const char*>(cubin.data()), static_cast<std::streamsize>(cubin.size()));
+        }
+    }
+    {
+        std::lock_guard<std::mutex> lock(dev->cache_mutex);
+        dev->module_cache[p->key] = cubin;
+    }
+    if (cache) {
+        std::lock_guard<std::mutex> lock(cache->mutex);
+        cache->entries[p->key] = cubin;
+    }
+    if (dev->compile_only) {
+        *out = p.release();
+        return VK_SUCCESS;
+    }
+    if (rt::load(cubin, tile_shift, p->module, err) != rt::kOk) {
+        rt::set_last_error("module load failed: " + err);
+        return VK_ERROR_INITIALIZATION_FAILED;
+    }
+    *out = p.release();
+    return VK_SUCCESS;
+}
+
+}  // namespace cpv::icd

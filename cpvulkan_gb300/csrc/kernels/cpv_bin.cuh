@@ -1,0 +1,220 @@
+/*
+ * cpv_bin.cuh — order-preserving sort-middle binning and the other generic
+ * device kernels (scan, fills).
+ *
+ * Binning builds, for every screen tile, the list of primitive ids that
+ * touch it, in API order — the per-pixel order the reference's serial loop
+ * (CPVulkan/CommandBuffer.Draw.cpp:1526-1593) produces. Primitives are split
+ * into S contiguous spans, one warp per span:
+ *
+ *   1. cpv_span_count: each warp counts, per tile, the primitives of its span
+ *      that touch the tile → counts[tile * S + span].
+ *   2. exclusive scan of counts in tile-major order → the write cursor of
+ *      every (tile, span) pair; tile t's list is the contiguous range
+ *      [cursor(t, 0), cursor(t + 1, 0)).
+ *   3. cpv_span_write: each warp walks its span again in order and appends
+ *      primitive ids at its cursors; within a warp, 32 (primitive, tile) pairs
+ *      are placed per step with a match-any rank, so the order inside a span
+ *      is the primitive order, and spans are laid out in span order.
+ *
+ * Everything is sized from host-known quantities (primitives, tiles, spans),
+ * so a draw needs no host round trip and the whole sequence can be captured
+ * in a CUDA graph. The list has a fixed capacity; a draw that would exceed
+ * it records the overflow and the raster kernel falls back to scanning the
+ * per-primitive rectangles (slower, same result).
+ */
+#ifndef CPV_BIN_CUH
+#define CPV_BIN_CUH
+
+#include "cpv_device.cuh"
+
+__device__ __forceinline__ void cpv_rect_unpack(const uint16_t* rects, uint64_t g, uint32_t& x0, uint32_t& y0, uint32_t& x1, uint32_t& y1) {
+    const uint2 r = reinterpret_cast<const uint2*>(rects)[g];
+    x0 = r.x & 0xFFFFu;
+    y0 = r.x >> 16;
+    x1 = r.y & 0xFFFFu;
+    y1 = r.y >> 16;
+}
+
+__device__ __forceinline__ void cpv_span_range(uint64_t total, uint32_t spans, uint32_t span, uint64_t& begin, uint64_t& end) {
+    const uint64_t per = (total + spans - 1u) / spans;
+    begin = per * span;
+    end = begin + per;
+    if (begin > total) begin = total;
+    if (end > total) end = total;
+}
+
+/* counts[tile * spans + span] += primitives of the span touching the tile. */
+extern "C" __global__ void __launch_bounds__(256) cpv_span_count(const uint16_t* __restrict__ rects, uint64_t total, uint32_t spans,
+                                                                 uint32_t tiles_x, uint32_t* __restrict__ counts) {
+    const uint32_t span = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31u;
+    if (span >= spans) return;
+    uint64_t begin, end;
+    cpv_span_range(total, spans, span, begin, end);
+    for (uint64_t g = begin + lane; g < end; g += 32u) {
+        uint32_t x0, y0, x1, y1;
+        cpv_rect_unpack(rects, g, x0, y0, x1, y1);
+        for (uint32_t y = y0; y < y1; y++)
+            for (uint32_t x = x0; x < x1; x++) atomicAdd(&counts[(static_cast<uint64_t>(y) * tiles_x + x) * spans + span], 1u);
+    }
+}
+
+/* Appends primitive ids in order. cursor = scanned counts (modified in place:
+ * afterwards cursor[t * spans + s] is the end of (t, s)). */
+extern "C" __global__ void __launch_bounds__(256) cpv_span_write(const uint16_t* __restrict__ rects, uint64_t total, uint32_t spans,
+                                                                 uint32_t tiles_x, uint32_t* __restrict__ cursor,
+                                                                 uint32_t* __restrict__ list, uint32_t capacity,
+                                                                 const uint32_t* __restrict__ pair_total) {
+    const uint32_t span = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31u;
+    if (span >= spans) return;
+    const bool overflow = *pair_total > capacity;
+    uint64_t begin, end;
+    cpv_span_range(total, spans, span, begin, end);
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    for (uint64_t base = begin; base < end; base += 32u) {
+        const uint64_t g = base + lane;
+        uint32_t x0 = 0, y0 = 0, x1 = 0, y1 = 0;
+        if (g < end) cpv_rect_unpack(rects, g, x0, y0, x1, y1);
+        const uint32_t w = x1 - x0;
+        const uint32_t n = w * (y1 - y0);
+        /* inclusive warp scan of pair counts → this lane's first pair */
+        uint32_t incl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= static_cast<uint32_t>(o)) incl += v;
+        }
+        const uint32_t total_pairs = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        const uint32_t excl = incl - n;
+        /* place the chunk's pairs 32 at a time, in (primitive, tile) order */
+        for (uint32_t p0 = 0; p0 < total_pairs; p0 += 32u) {
+            const uint32_t p = p0 + lane;
+            const bool valid = p < total_pairs;
+            /* owner lane: last lane whose exclusive start <= p */
+            uint32_t owner = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                const uint32_t cand = owner + static_cast<uint32_t>(step);
+                const uint32_t cand_excl = __shfl_sync(0xFFFFFFFFu, excl, cand);
+                if (cand_excl <= p) owner = cand;
+            }
+            /* excl is non-decreasing, so the last lane with excl <= p owns pair p
+             * (lanes with no pairs share the next lane's excl and are skipped) */
+            const uint32_t o_excl = __shfl_sync(0xFFFFFFFFu, excl, owner);
+            const uint32_t o_x0 = __shfl_sync(0xFFFFFFFFu, x0, owner);
+            const uint32_t o_y0 = __shfl_sync(0xFFFFFFFFu, y0, owner);
+            const uint32_t o_w = __shfl_sync(0xFFFFFFFFu, w, owner);
+            uint32_t tile = 0xFFFFFFFFu;
+            if (valid) {
+                const uint32_t local = p - o_excl;
+                tile = (o_y0 + local / o_w) * tiles_x + (o_x0 + local % o_w);
+            }
+            const uint32_t key = valid ? tile : (0x80000000u | lane);
+            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+            const uint32_t rank = __popc(peers & lt_mask);
+            const uint32_t leader = __ffs(peers) - 1u;
+            uint32_t pos = 0;
+            volatile uint32_t* cur = nullptr;
+            if (valid) {
+                cur = &cursor[static_cast<uint64_t>(tile) * spans + span];
+                pos = *cur + rank;
+                if (!overflow && pos < capacity) list[pos] = static_cast<uint32_t>(base + owner);
+            }
+            __syncwarp();
+            if (valid && lane == leader) *cur = *cur + __popc(peers);
+            __syncwarp();
+        }
+    }
+}
+
+/* ---- exclusive scan of u32 (three-level, 2048 elements per block) ---- */
+
+#define CPV_SCAN_THREADS 256
+#define CPV_SCAN_ITEMS 8
+#define CPV_SCAN_BLOCK (CPV_SCAN_THREADS * CPV_SCAN_ITEMS)
+
+__device__ __forceinline__ uint32_t cpv_block_exclusive_scan(uint32_t v, uint32_t& block_total) {
+    __shared__ uint32_t warp_sums[CPV_SCAN_THREADS / 32];
+    __shared__ uint32_t total_sh;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= static_cast<uint32_t>(o)) incl += t;
+    }
+    if (lane == 31u) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0u) {
+        const uint32_t s = lane < CPV_SCAN_THREADS / 32 ? warp_sums[lane] : 0u;
+        uint32_t si = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, si, o);
+            if (lane >= static_cast<uint32_t>(o)) si += t;
+        }
+        if (lane < CPV_SCAN_THREADS / 32) warp_sums[lane] = si - s;
+        if (lane == CPV_SCAN_THREADS / 32 - 1) total_sh = si;
+    }
+    __syncthreads();
+    const uint32_t r = warp_sums[warp] + incl - v;
+    block_total = total_sh;
+    __syncthreads();
+    return r;
+}
+
+/* Level scan: out[i] = exclusive prefix within the block; block_sums[b] = block total. */
+extern "C" __global__ void __launch_bounds__(CPV_SCAN_THREADS) cpv_scan_blocks(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                                                              uint64_t n, uint32_t* __restrict__ block_sums) {
+    const uint64_t base = static_cast<uint64_t>(blockIdx.x) * CPV_SCAN_BLOCK + static_cast<uint64_t>(threadIdx.x) * CPV_SCAN_ITEMS;
+    uint32_t v[CPV_SCAN_ITEMS];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int i = 0; i < CPV_SCAN_ITEMS; i++) {
+        v[i] = (base + i < n) ? in[base + i] : 0u;
+        sum += v[i];
+    }
+    uint32_t total = 0;
+    uint32_t run = cpv_block_exclusive_scan(sum, total);
+#pragma unroll
+    for (int i = 0; i < CPV_SCAN_ITEMS; i++) {
+        if (base + i < n) out[base + i] = run;
+        run += v[i];
+    }
+    if (threadIdx.x == 0 && block_sums) block_sums[blockIdx.x] = total;
+}
+
+/* out[i] += add[block(i)]; optionally writes the grand total. */
+extern "C" __global__ void __launch_bounds__(CPV_SCAN_THREADS) cpv_scan_add(uint32_t* __restrict__ out, uint64_t n, const uint32_t* __restrict__ add) {
+    const uint64_t base = static_cast<uint64_t>(blockIdx.x) * CPV_SCAN_BLOCK;
+    const uint32_t a = add[blockIdx.x];
+    for (uint32_t i = threadIdx.x; i < CPV_SCAN_BLOCK; i += CPV_SCAN_THREADS) {
+        if (base + i < n) out[base + i] += a;
+    }
+}
+
+/* total = last exclusive prefix + last input. */
+extern "C" __global__ void cpv_scan_total(const uint32_t* __restrict__ in, const uint32_t* __restrict__ out, uint64_t n, uint32_t* __restrict__ total) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *total = n ? out[n - 1] + in[n - 1] : 0u;
+}
+
+/* ---- fills ---- */
+
+extern "C" __global__ void __launch_bounds__(256) cpv_fill_u32(uint32_t* __restrict__ dst, uint64_t count, uint32_t value) {
+    for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        dst[i] = value;
+}
+
+extern "C" __global__ void __launch_bounds__(256) cpv_fill_u16(uint16_t* __restrict__ dst, uint64_t count, uint32_t value) {
+    for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        dst[i] = static_cast<uint16_t>(value);
+}
+
+extern "C" __global__ void __launch_bounds__(256) cpv_fill_u64(uint2* __restrict__ dst, uint64_t count, uint32_t lo, uint32_t hi) {
+    for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        dst[i] = make_uint2(lo, hi);
+}
+
+#endif /* CPV_BIN_CUH */

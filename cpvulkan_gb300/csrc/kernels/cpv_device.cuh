@@ -1,0 +1,378 @@
+/*
+ * cpv_device.cuh — device-side types and arithmetic shared by every kernel of
+ * the draw path: per-draw parameters, attachment codecs, the image sampler,
+ * the edge function and primitive set-up, plus the value types that
+ * translated SPIR-V shaders use.
+ *
+ * Compiled twice: by nvcc into libcpvulkan_gb300.so (the generic binning,
+ * scan and clear kernels) and by NVRTC at vkCreateGraphicsPipelines, where
+ * the translated shaders and the pipeline's fixed-function state are
+ * prepended and cpv_pipeline.cuh instantiates the pipeline's kernels.
+ *
+ * Every arithmetic step that decides a pixel follows the reference CPU path
+ * operation for operation (cited per function) and must be compiled with
+ * -fmad=false, IEEE division and square root, and no flush-to-zero, so that
+ * results are bit-identical to the reference's uncontracted binary32 code.
+ */
+#ifndef CPV_DEVICE_CUH
+#define CPV_DEVICE_CUH
+
+#include "cpv_params.h"
+
+/* ------------------------------------------------------------------------- */
+/* Scalar helpers                                                            */
+/* ------------------------------------------------------------------------- */
+
+/* static_cast<int32_t>(float) with the saturating semantics of the target
+ * (cvt.rzi.s32.f32): the reference's screen bounding box conversion
+ * (CPVulkan/CommandBuffer.Draw.cpp:1548-1563). */
+__device__ __forceinline__ int32_t cpv_f2i(float f) { return __float2int_rz(f); }
+
+/* std::max / std::min as the reference's GLSL helpers use them
+ * (CPVulkan/GlslFunctions.cpp:106-130). */
+__device__ __forceinline__ float cpv_std_max(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float cpv_std_min(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float cpv_std_clamp(float v, float lo, float hi) { return (v < lo) ? lo : ((hi < v) ? hi : v); }
+
+/* UNORM encode (LLVMRuntime/ImageCompiler.cpp:27-32, 1081-1095):
+ * minnum(maxnum(x,0),1) * (2^n-1), round half away from zero, to unsigned. */
+__device__ __forceinline__ uint32_t cpv_encode_unorm(float x, float maxv) {
+    float v = fminf(fmaxf(x, 0.0f), 1.0f);
+    v = __fmul_rn(v, maxv);
+    v = roundf(v);
+    return __float2uint_rz(v);
+}
+
+/* UNORM decode: uitofp then IEEE divide (LLVMRuntime/ImageCompiler.cpp:43-53). */
+__device__ __forceinline__ float cpv_decode_unorm8(uint32_t u) { return __fdiv_rn(__uint2float_rn(u), 255.0f); }
+__device__ __forceinline__ float cpv_decode_unorm16(uint32_t u) { return __fdiv_rn(__uint2float_rn(u), 65535.0f); }
+
+/* EdgeFunction (CPVulkan/CommandBuffer.Draw.cpp:410-418). */
+__device__ __forceinline__ float cpv_edge(float ax, float ay, float bx, float by, float cx, float cy) {
+    const float t0 = __fmul_rn(__fsub_rn(cx, ax), __fsub_rn(by, ay));
+    const float t1 = __fmul_rn(__fsub_rn(cy, ay), __fsub_rn(bx, ax));
+    return __fsub_rn(t0, t1);
+}
+
+/* Bounds-checked reads of application memory. Out-of-range reads return
+ * zero (the oracle defines the same), so no input can make a kernel read
+ * outside the buffers it was given. */
+__device__ __forceinline__ float cpv_ld_f32(const uint8_t* base, uint64_t bytes, uint64_t off) {
+    if (base == nullptr || off + 4u > bytes) return 0.0f;
+    return __ldg(reinterpret_cast<const float*>(base + off));
+}
+__device__ __forceinline__ uint32_t cpv_ld_u32(const uint8_t* base, uint64_t bytes, uint64_t off) {
+    if (base == nullptr || off + 4u > bytes) return 0u;
+    return __ldg(reinterpret_cast<const uint32_t*>(base + off));
+}
+__device__ __forceinline__ int32_t cpv_ld_i32(const uint8_t* base, uint64_t bytes, uint64_t off) {
+    return static_cast<int32_t>(cpv_ld_u32(base, bytes, off));
+}
+
+/* ------------------------------------------------------------------------- */
+/* Value types for translated shaders                                        */
+/* ------------------------------------------------------------------------- */
+
+template <typename T, int N>
+struct cvec {
+    T v[N];
+};
+
+template <int C, int R>
+struct cmat {
+    cvec<float, R> c[C];
+};
+
+/* Component-wise arithmetic, one IEEE operation per component. */
+#define CPV_VEC_BINOP(NAME, EXPR)                                                          \
+    __device__ __forceinline__ float NAME(float a, float b) { return EXPR; }               \
+    template <int N>                                                                       \
+    __device__ __forceinline__ cvec<float, N> NAME(const cvec<float, N>& a, const cvec<float, N>& b) { \
+        cvec<float, N> r;                                                                  \
+        _Pragma("unroll") for (int i = 0; i < N; i++) r.v[i] = NAME(a.v[i], b.v[i]);       \
+        return r;                                                                          \
+    }
+CPV_VEC_BINOP(cpv_fadd, __fadd_rn(a, b))
+CPV_VEC_BINOP(cpv_fsub, __fsub_rn(a, b))
+CPV_VEC_BINOP(cpv_fmul, __fmul_rn(a, b))
+CPV_VEC_BINOP(cpv_fdiv, __fdiv_rn(a, b))
+#undef CPV_VEC_BINOP
+
+__device__ __forceinline__ float cpv_fneg(float a) { return -a; }
+template <int N>
+__device__ __forceinline__ cvec<float, N> cpv_fneg(const cvec<float, N>& a) {
+    cvec<float, N> r;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.v[i] = -a.v[i];
+    return r;
+}
+
+template <int N>
+__device__ __forceinline__ cvec<float, N> cpv_vec_times_scalar(const cvec<float, N>& a, float s) {
+    cvec<float, N> r;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.v[i] = __fmul_rn(a.v[i], s);
+    return r;
+}
+
+template <int C, int R>
+__device__ __forceinline__ cmat<C, R> cpv_mat_times_scalar(const cmat<C, R>& m, float s) {
+    cmat<C, R> r;
+#pragma unroll
+    for (int c = 0; c < C; c++) r.c[c] = cpv_vec_times_scalar(m.c[c], s);
+    return r;
+}
+
+/* OpMatrixTimesVector for mat4 → glm operator*(mat4, vec4) order:
+ * (m0*v0 + m1*v1) + (m2*v2 + m3*v3) per row (LLVMRuntime/SpirvFunctions.cpp:34-45;
+ * glm 0.9.9 summation order, restated). */
+__device__ __forceinline__ cvec<float, 4> cpv_mat_times_vec(const cmat<4, 4>& m, const cvec<float, 4>& v) {
+    cvec<float, 4> r;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float mul0 = __fmul_rn(m.c[0].v[i], v.v[0]);
+        const float mul1 = __fmul_rn(m.c[1].v[i], v.v[1]);
+        const float add0 = __fadd_rn(mul0, mul1);
+        const float mul2 = __fmul_rn(m.c[2].v[i], v.v[2]);
+        const float mul3 = __fmul_rn(m.c[3].v[i], v.v[3]);
+        const float add1 = __fadd_rn(mul2, mul3);
+        r.v[i] = __fadd_rn(add0, add1);
+    }
+    return r;
+}
+
+/* mat3 * vec3 → glm order: (m0*v0 + m1*v1) + m2*v2. */
+__device__ __forceinline__ cvec<float, 3> cpv_mat_times_vec(const cmat<3, 3>& m, const cvec<float, 3>& v) {
+    cvec<float, 3> r;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const float mul0 = __fmul_rn(m.c[0].v[i], v.v[0]);
+        const float mul1 = __fmul_rn(m.c[1].v[i], v.v[1]);
+        const float mul2 = __fmul_rn(m.c[2].v[i], v.v[2]);
+        r.v[i] = __fadd_rn(__fadd_rn(mul0, mul1), mul2);
+    }
+    return r;
+}
+
+/* OpDot → glm::dot: vec2/vec3 left to right, vec4 pairwise. */
+__device__ __forceinline__ float cpv_dot(const cvec<float, 2>& a, const cvec<float, 2>& b) {
+    return __fadd_rn(__fmul_rn(a.v[0], b.v[0]), __fmul_rn(a.v[1], b.v[1]));
+}
+__device__ __forceinline__ float cpv_dot(const cvec<float, 3>& a, const cvec<float, 3>& b) {
+    const float t0 = __fmul_rn(a.v[0], b.v[0]);
+    const float t1 = __fmul_rn(a.v[1], b.v[1]);
+    const float t2 = __fmul_rn(a.v[2], b.v[2]);
+    return __fadd_rn(__fadd_rn(t0, t1), t2);
+}
+__device__ __forceinline__ float cpv_dot(const cvec<float, 4>& a, const cvec<float, 4>& b) {
+    const float t0 = __fmul_rn(a.v[0], b.v[0]);
+    const float t1 = __fmul_rn(a.v[1], b.v[1]);
+    const float t2 = __fmul_rn(a.v[2], b.v[2]);
+    const float t3 = __fmul_rn(a.v[3], b.v[3]);
+    return __fadd_rn(__fadd_rn(t0, t1), __fadd_rn(t2, t3));
+}
+
+/* GLSL.std.450 Normalize on vectors → glm::normalize: x * (1 / sqrt(dot(x, x)))
+ * (CPVulkan/GlslFunctions.cpp:178-182). The scalar form is the reference's
+ * sign-based variant (:172-176). */
+template <int N>
+__device__ __forceinline__ cvec<float, N> cpv_normalize(const cvec<float, N>& x) {
+    const float inv = __fdiv_rn(1.0f, __fsqrt_rn(cpv_dot(x, x)));
+    return cpv_vec_times_scalar(x, inv);
+}
+__device__ __forceinline__ float cpv_normalize(float x) { return signbit(x) ? 1.0f : -1.0f; }
+
+#define CPV_VEC_FUNC2(NAME, SCALAR)                                                        \
+    __device__ __forceinline__ float NAME(float a, float b) { return SCALAR(a, b); }       \
+    template <int N>                                                                       \
+    __device__ __forceinline__ cvec<float, N> NAME(const cvec<float, N>& a, const cvec<float, N>& b) { \
+        cvec<float, N> r;                                                                  \
+        _Pragma("unroll") for (int i = 0; i < N; i++) r.v[i] = SCALAR(a.v[i], b.v[i]);     \
+        return r;                                                                          \
+    }
+CPV_VEC_FUNC2(cpv_glsl_fmax, cpv_std_max)
+CPV_VEC_FUNC2(cpv_glsl_fmin, cpv_std_min)
+CPV_VEC_FUNC2(cpv_glsl_pow, powf)
+#undef CPV_VEC_FUNC2
+
+__device__ __forceinline__ float cpv_glsl_fclamp(float v, float lo, float hi) { return cpv_std_clamp(v, lo, hi); }
+template <int N>
+__device__ __forceinline__ cvec<float, N> cpv_glsl_fclamp(const cvec<float, N>& v, const cvec<float, N>& lo, const cvec<float, N>& hi) {
+    cvec<float, N> r;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.v[i] = cpv_std_clamp(v.v[i], lo.v[i], hi.v[i]);
+    return r;
+}
+/* FMix: x * (1 - a) + y * a (CPVulkan/GlslFunctions.cpp:155-159). */
+__device__ __forceinline__ float cpv_glsl_fmix(float x, float y, float a) {
+    return __fadd_rn(__fmul_rn(x, __fsub_rn(1.0f, a)), __fmul_rn(y, a));
+}
+template <int N>
+__device__ __forceinline__ cvec<float, N> cpv_glsl_fmix(const cvec<float, N>& x, const cvec<float, N>& y, const cvec<float, N>& a) {
+    cvec<float, N> r;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.v[i] = cpv_glsl_fmix(x.v[i], y.v[i], a.v[i]);
+    return r;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Image sampler (CPVulkan/ImageSampler.cpp, CPVulkan/GlslFunctions.cpp)     */
+/* ------------------------------------------------------------------------- */
+
+/* wrap (CPVulkan/ImageSampler.cpp:12-38). */
+__device__ __forceinline__ int32_t cpv_wrap(int32_t v, int32_t size, uint32_t mode) {
+    switch (mode) {
+    case 0: return (v % size + size) % size;
+    case 1: {
+        const int32_t two = 2 * size;
+        const int32_t n = (v % two + two) % two - size;
+        return size - 1 - (n >= 0 ? n : -(1 + n));
+    }
+    case 2: return v < 0 ? 0 : (v > size - 1 ? size - 1 : v);
+    case 3: return v < -1 ? -1 : (v > size ? size : v);
+    case 4: {
+        const int32_t m = v >= 0 ? v : -(1 + v);
+        return m < 0 ? 0 : (m > size - 1 ? size - 1 : m);
+    }
+    default: return 0;
+    }
+}
+
+/* GetPixel<fvec4> of an RGBA8 UNORM texel with the border check
+ * (CPVulkan/ImageSampler.cpp:133-160) and the border table (:409-417). */
+__device__ __forceinline__ void cpv_texel(const CpvTexture& t, uint32_t level, int32_t x, int32_t y, float out[4]) {
+    const int32_t w = static_cast<int32_t>(t.level_w[level]);
+    const int32_t h = static_cast<int32_t>(t.level_h[level]);
+    if (x < 0 || x >= w || y < 0 || y >= h) {
+        const uint32_t b = t.border < 6u ? t.border : 0u;
+        const float rgb = (b >= 4u) ? 1.0f : 0.0f;
+        const float a = (b >= 2u) ? 1.0f : 0.0f;
+        out[0] = rgb; out[1] = rgb; out[2] = rgb; out[3] = a;
+        return;
+    }
+    const uint64_t off = t.level_offset[level] + (static_cast<uint64_t>(y) * static_cast<uint64_t>(w) + static_cast<uint64_t>(x)) * 4u;
+    if (off + 4u > t.bytes) {
+        out[0] = out[1] = out[2] = out[3] = 0.0f;
+        return;
+    }
+    const uint32_t px = __ldg(reinterpret_cast<const uint32_t*>(t.data + off));
+#pragma unroll
+    for (int i = 0; i < 4; i++) out[i] = cpv_decode_unorm8((px >> (8 * i)) & 0xFFu);
+}
+
+/* lerp with a double-precision delta (CPVulkan/ImageSampler.cpp:51-55). */
+__device__ __forceinline__ void cpv_lerp4(const float a[4], const float b[4], double delta, float out[4]) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float diff = __fsub_rn(b[i], a[i]);
+        const double sum = __dadd_rn(static_cast<double>(a[i]), __dmul_rn(static_cast<double>(diff), delta));
+        out[i] = __double2float_rn(sum);
+    }
+}
+
+/* SampleImageOfLevel, 2D (CPVulkan/ImageSampler.cpp:403-531). */
+__device__ __forceinline__ void cpv_sample_level(const CpvTexture& t, uint32_t level, float u, float v, uint32_t filter, float out[4]) {
+    const float range_x = __uint2float_rn(t.level_w[level]);
+    const float range_y = __uint2float_rn(t.level_h[level]);
+    const int32_t wx = static_cast<int32_t>(t.level_w[level]);
+    const int32_t wy = static_cast<int32_t>(t.level_h[level]);
+    if (filter == 0u) {
+        int32_t cx = cpv_f2i(floorf(__fadd_rn(__fmul_rn(u, range_x), 0.0f)));
+        int32_t cy = cpv_f2i(floorf(__fadd_rn(__fmul_rn(v, range_y), 0.0f)));
+        cx = cpv_wrap(cx, wx, t.address_u);
+        cy = cpv_wrap(cy, wy, t.address_v);
+        cpv_texel(t, level, cx, cy, out);
+        return;
+    }
+    const float sx = __fsub_rn(__fmul_rn(u, range_x), 0.5f);
+    const float sy = __fsub_rn(__fmul_rn(v, range_y), 0.5f);
+    const float flx = floorf(sx), fly = floorf(sy);
+    const int32_t x0r = cpv_f2i(flx), y0r = cpv_f2i(fly);
+    const int32_t x1 = cpv_wrap(x0r + 1, wx, t.address_u);
+    const int32_t y1 = cpv_wrap(y0r + 1, wy, t.address_v);
+    const int32_t x0 = cpv_wrap(x0r, wx, t.address_u);
+    const int32_t y0 = cpv_wrap(y0r, wy, t.address_v);
+    const double fx = static_cast<double>(__fsub_rn(sx, flx));
+    const double fy = static_cast<double>(__fsub_rn(sy, fly));
+    float t00[4], t01[4], t10[4], t11[4];
+    cpv_texel(t, level, x0, y0, t00);
+    cpv_texel(t, level, x0, y1, t01);
+    cpv_texel(t, level, x1, y0, t10);
+    cpv_texel(t, level, x1, y1, t11);
+    float ij0[4], ij1[4];
+    cpv_lerp4(t00, t10, fx, ij0);
+    cpv_lerp4(t01, t11, fx, ij1);
+    cpv_lerp4(ij0, ij1, fy, out);
+}
+
+/* ImageSampleExplicitLod λ (CPVulkan/GlslFunctions.cpp:624-628) + SampleImage
+ * (CPVulkan/ImageSampler.cpp:562-673). Implicit-LOD sampling passes lod 0
+ * (CPVulkan/GlslFunctions.cpp:657-672). */
+__device__ __forceinline__ cvec<float, 4> cpv_sample(const CpvTexture& t, float u, float v, float lod) {
+    const float bias = cpv_std_clamp(__fadd_rn(t.lod_bias, 0.0f), -32.0f, 32.0f);
+    const float lambda = cpv_std_clamp(__fadd_rn(lod, bias), t.min_lod, t.max_lod);
+    float out[4];
+    if (t.levels == 0u || t.data == nullptr) {
+        out[0] = out[1] = out[2] = 0.0f;
+        out[3] = 1.0f;
+    } else if (lambda <= 0.0f) {
+        cpv_sample_level(t, 0u, u, v, t.mag_filter, out);
+    } else {
+        const float max_level = __uint2float_rn(t.levels - 1u);
+        const float mip = cpv_std_clamp(lambda, 0.0f, max_level);
+        if (t.mipmap_mode == 0u) {
+            const uint32_t real = __float2uint_rz(ceilf(__fadd_rn(mip, 0.5f))) - 1u;
+            cpv_sample_level(t, real, u, v, t.min_filter, out);
+        } else {
+            const uint32_t l1 = __float2uint_rz(floorf(mip));
+            const float delta = __fsub_rn(mip, __uint2float_rn(l1));
+            float p1[4];
+            cpv_sample_level(t, l1, u, v, t.min_filter, p1);
+            if (delta == 0.0f) {
+#pragma unroll
+                for (int i = 0; i < 4; i++) out[i] = p1[i];
+            } else {
+                float p2[4];
+                cpv_sample_level(t, l1 + 1u, u, v, t.min_filter, p2);
+                cpv_lerp4(p1, p2, static_cast<double>(delta), out);
+            }
+        }
+    }
+    cvec<float, 4> r;
+#pragma unroll
+    for (int i = 0; i < 4; i++) r.v[i] = out[i];
+    return r;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Input assembly                                                            */
+/* ------------------------------------------------------------------------- */
+
+/* Assembled-vertex slots of primitive p for the topology
+ * (CPVulkan/CommandBuffer.Draw.cpp:567-673): returns raw ids v[3] and the
+ * provoking raw id. */
+__device__ __forceinline__ void cpv_prim_vertices(uint32_t topology, uint32_t p, uint32_t v[3], uint32_t& provoking) {
+    if (topology == 4u) { /* strip */
+        v[0] = p; v[1] = p + 1u; v[2] = p + 2u; provoking = p;
+    } else if (topology == 5u) { /* fan */
+        v[0] = 0u; v[1] = p + 1u; v[2] = p + 2u; provoking = p + 1u;
+    } else { /* list */
+        v[0] = 3u * p; v[1] = 3u * p + 1u; v[2] = 3u * p + 2u; provoking = 3u * p;
+    }
+}
+
+/* Raw assembled vertex → vertex id (CPVulkan/CommandBuffer.Draw.cpp:675-760):
+ * firstVertex + i, or vertexOffset + index[firstIndex + i]; an index outside
+ * the bound index buffer reads as 0. */
+__device__ __forceinline__ uint32_t cpv_vertex_id(const CpvDrawParams& P, uint32_t raw) {
+    if (P.index_size == 0u) return P.first + raw;
+    const uint64_t off = (static_cast<uint64_t>(P.first) + raw) * P.index_size;
+    uint32_t index = 0u;
+    if (off + P.index_size <= P.ib_bytes) {
+        if (P.index_size == 2u) index = __ldg(reinterpret_cast<const uint16_t*>(P.ib + off));
+        else index = __ldg(reinterpret_cast<const uint32_t*>(P.ib + off));
+    }
+    return static_cast<uint32_t>(P.vertex_offset) + index;
+}
+
+#endif /* CPV_DEVICE_CUH */

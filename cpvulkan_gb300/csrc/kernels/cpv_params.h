@@ -1,0 +1,95 @@
+/*
+ * cpv_params.h — per-draw parameter block shared by the host runtime and
+ * every draw kernel (plain C++ layout, no device code). Included by
+ * cpv_device.cuh on the device side and by the runtime on the host side.
+ */
+#ifndef CPV_PARAMS_H
+#define CPV_PARAMS_H
+
+#ifdef __CUDACC_RTC__
+typedef unsigned char uint8_t;
+typedef signed char int8_t;
+typedef unsigned short uint16_t;
+typedef unsigned int uint32_t;
+typedef int int32_t;
+typedef unsigned long long uint64_t;
+typedef long long int64_t;
+#else
+#include <stdint.h>
+#endif
+
+#define CPV_MAX_VB 8
+#define CPV_MAX_UBO 8
+#define CPV_MAX_TEX 4
+#define CPV_MAX_VARYINGS 16
+#define CPV_MAX_LEVELS 16
+
+/* Status word bits written by kernels instead of trapping. */
+#define CPV_STATUS_LIST_OVERFLOW 0x1u
+#define CPV_STATUS_BAD_INPUT 0x2u
+#define CPV_STATUS_TIMEOUT 0x4u
+
+#define CPV_FMT_R8G8B8A8_UNORM 37u
+#define CPV_FMT_B8G8R8A8_UNORM 44u
+#define CPV_FMT_D16_UNORM 124u
+#define CPV_FMT_D32_SFLOAT 126u
+#define CPV_FMT_D32_SFLOAT_S8_UINT 130u
+
+/* One sampled image + its sampler, resolved from a descriptor at draw time.
+ * Levels follow the reference's linear layout: level after level, tightly
+ * packed rows (CPVulkanBase/Formats.cpp:453-484). */
+struct CpvTexture {
+    const uint8_t* data;
+    uint64_t bytes;
+    uint64_t level_offset[CPV_MAX_LEVELS];
+    uint32_t level_w[CPV_MAX_LEVELS];
+    uint32_t level_h[CPV_MAX_LEVELS];
+    uint32_t levels;
+    uint32_t format;
+    uint32_t mag_filter, min_filter, mipmap_mode;
+    uint32_t address_u, address_v, border;
+    float lod_bias, min_lod, max_lod;
+};
+
+/* Everything one draw's kernels read. Passed by value as a kernel argument. */
+struct CpvDrawParams {
+    /* geometry */
+    const uint8_t* vb[CPV_MAX_VB];
+    uint64_t vb_bytes[CPV_MAX_VB];
+    const uint8_t* ib;
+    uint64_t ib_bytes;
+    uint32_t index_size; /* 0 = non-indexed, 2 or 4 */
+    uint32_t count;      /* vertexCount or indexCount */
+    uint32_t first;      /* firstVertex or firstIndex */
+    int32_t vertex_offset;
+    uint32_t first_instance;
+    uint32_t instance_count;
+    uint32_t prims_per_instance;
+    uint32_t pad0;
+    uint64_t total_prims;
+    /* resources */
+    const uint8_t* ubo[CPV_MAX_UBO];
+    uint64_t ubo_bytes[CPV_MAX_UBO];
+    CpvTexture tex[CPV_MAX_TEX];
+    uint32_t push[32];
+    /* attachments */
+    uint8_t* color;
+    uint8_t* depth;
+    uint32_t fb_width, fb_height;
+    float viewport[6];
+    float blend_constants[4];
+    /* screen tiling */
+    uint32_t tile_shift;
+    uint32_t tiles_x, tiles_y;
+    uint32_t pad1;
+    /* binning scratch (null in direct mode) */
+    const uint32_t* tile_end;   /* tiles*spans cursor matrix after the write pass */
+    const uint32_t* bin_list;   /* primitive ids, tile-major, primitive order within a tile */
+    const uint32_t* pair_total; /* device word: pairs the draw needed */
+    const uint16_t* rects;      /* per primitive tile rectangle (x0,y0,x1,y1), exclusive ends */
+    uint32_t spans;
+    uint32_t list_capacity;
+    uint32_t* status;
+};
+
+#endif /* CPV_PARAMS_H */

@@ -1,0 +1,309 @@
+// runtime.cu — see runtime.h. Compiled by nvcc for sm_103a; the generic
+// binning/scan/fill kernels come from cpv_bin.cuh, the pipeline-specific
+// kernels from NVRTC modules built at pipeline creation.
+#include "runtime.h"
+
+#include <nvrtc.h>
+
+#include <atomic>
+#include <cstdlib>
+#include <cstring>
+
+#include "../kernels/cpv_bin.cuh"
+
+namespace cpv::rt {
+
+namespace {
+
+std::mutex g_init_mutex;
+bool g_initialised = false;
+bool g_available = false;
+std::atomic<uint64_t> g_launches{0};
+thread_local std::string g_last_error;
+
+int cuda_fail(cudaError_t e, const char* what) {
+    set_last_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return kErrCuda;
+}
+
+#define CPV_CUDA(call)                                              \
+    do {                                                            \
+        cudaError_t e_ = (call);                                    \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);         \
+    } while (0)
+
+template <typename T>
+int grow(T*& ptr, uint64_t& cap, uint64_t need) {
+    if (need <= cap && ptr) return kOk;
+    uint64_t n = cap ? cap : 1024;
+    while (n < need) n *= 2;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    if (cudaMalloc(reinterpret_cast<void**>(&ptr), n * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        set_last_error("cudaMalloc of binning scratch failed");
+        return kErrOutOfMemory;
+    }
+    cap = n;
+    return kOk;
+}
+
+uint32_t env_u32(const char* name, uint32_t dflt) {
+    const char* v = std::getenv(name);
+    if (!v || !*v) return dflt;
+    return static_cast<uint32_t>(std::strtoul(v, nullptr, 0));
+}
+
+}  // namespace
+
+const char* last_error() { return g_last_error.c_str(); }
+void set_last_error(const std::string& e) { g_last_error = e; }
+
+uint64_t launches() { return g_launches.load(); }
+void count_launch(uint64_t n) { g_launches += n; }
+
+int init(std::string& error) {
+    std::lock_guard<std::mutex> lock(g_init_mutex);
+    if (g_initialised) {
+        if (!g_available) error = "no CUDA device";
+        return g_available ? kOk : kErrCuda;
+    }
+    g_initialised = true;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        error = "no CUDA device";
+        return kErrCuda;
+    }
+    if (cudaSetDevice(0) != cudaSuccess || cudaFree(nullptr) != cudaSuccess) {
+        cudaGetLastError();
+        error = "cannot create a CUDA context on device 0";
+        return kErrCuda;
+    }
+    g_available = true;
+    return kOk;
+}
+
+bool available() { return g_available; }
+
+int compile(const std::string& source, const std::string& name, std::vector<uint8_t>& cubin, std::string& log) {
+    nvrtcProgram prog;
+    const char* headers[3] = {kDeviceHeaderSource, kPipelineHeaderSource, kParamsHeaderSource};
+    const char* names[3] = {kDeviceHeaderName, kPipelineHeaderName, kParamsHeaderName};
+    if (nvrtcCreateProgram(&prog, source.c_str(), name.c_str(), 3, headers, names) != NVRTC_SUCCESS) {
+        log = "nvrtcCreateProgram failed";
+        return kErrCompile;
+    }
+    // Exact binary32 semantics: no contraction, IEEE divide and square root,
+    // denormals preserved.
+    const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
+                          "-ftz=false", "-default-device", "-lineinfo", "-diag-suppress=177", "-diag-suppress=550"};
+    const nvrtcResult r = nvrtcCompileProgram(prog, static_cast<int>(sizeof(opts) / sizeof(opts[0])), opts);
+    size_t log_size = 0;
+    nvrtcGetProgramLogSize(prog, &log_size);
+    log.assign(log_size, '\0');
+    if (log_size) nvrtcGetProgramLog(prog, &log[0]);
+    if (r != NVRTC_SUCCESS) {
+        nvrtcDestroyProgram(&prog);
+        return kErrCompile;
+    }
+    size_t size = 0;
+    if (nvrtcGetCUBINSize(prog, &size) != NVRTC_SUCCESS || size == 0) {
+        nvrtcDestroyProgram(&prog);
+        log += "\nno cubin produced";
+        return kErrCompile;
+    }
+    cubin.resize(size);
+    nvrtcGetCUBIN(prog, reinterpret_cast<char*>(cubin.data()));
+    nvrtcDestroyProgram(&prog);
+    return kOk;
+}
+
+int load(const std::vector<uint8_t>& cubin, uint32_t tile_shift, Module& out, std::string& error) {
+    if (!g_available) {
+        error = "no CUDA device: pipeline modules cannot be loaded";
+        return kErrCuda;
+    }
+    cudaLibrary_t lib = nullptr;
+    cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+    if (e != cudaSuccess) {
+        error = std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        return kErrCuda;
+    }
+    out.library = lib;
+    if (cudaLibraryGetKernel(&out.setup_rects, lib, "cpv_setup_rects") != cudaSuccess ||
+        cudaLibraryGetKernel(&out.raster, lib, "cpv_raster") != cudaSuccess) {
+        cudaGetLastError();
+        cudaLibraryUnload(lib);
+        out.library = nullptr;
+        error = "pipeline module lacks its kernels";
+        return kErrCuda;
+    }
+    out.tile_shift = tile_shift;
+    const uint32_t tile = 1u << tile_shift;
+    out.raster_threads = tile * tile < 256 ? tile * tile : 256;
+    return kOk;
+}
+
+void unload(Module& m) {
+    if (m.library) cudaLibraryUnload(m.library);
+    m.library = nullptr;
+}
+
+Scratch::~Scratch() {
+    if (!available()) return;
+    cudaFree(rects_);
+    cudaFree(counts_);
+    cudaFree(cursor_);
+    cudaFree(list_);
+    for (auto* p : scan_) cudaFree(p);
+    cudaFree(words_);
+}
+
+int Scratch::reserve_rects(uint64_t prims) { return grow(rects_, rects_cap_, prims * 4); }
+
+int Scratch::reserve_bins(uint64_t entries) {
+    const int r = grow(counts_, counts_cap_, entries);
+    if (r != kOk) return r;
+    return grow(cursor_, cursor_cap_, entries);
+}
+
+int Scratch::reserve_list(uint64_t entries) { return grow(list_, list_cap_, entries); }
+
+int Scratch::reserve_scan(uint64_t n) {
+    int level = 0;
+    while (n > CPV_SCAN_BLOCK && level < 8) {
+        n = (n + CPV_SCAN_BLOCK - 1) / CPV_SCAN_BLOCK;
+        // two arrays per level (sums and scanned sums) share one allocation
+        const int r = grow(scan_[level], scan_cap_[level], 2 * n);
+        if (r != kOk) return r;
+        level++;
+    }
+    return kOk;
+}
+
+int Scratch::ensure_words() {
+    if (words_) return kOk;
+    if (cudaMalloc(reinterpret_cast<void**>(&words_), 64) != cudaSuccess) {
+        cudaGetLastError();
+        return kErrOutOfMemory;
+    }
+    cudaMemset(words_, 0, 64);
+    return kOk;
+}
+
+namespace {
+
+int scan_level(cudaStream_t stream, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total, Scratch& sc, int level) {
+    const uint64_t blocks = (n + CPV_SCAN_BLOCK - 1) / CPV_SCAN_BLOCK;
+    if (blocks <= 1) {
+        cpv_scan_blocks<<<1, CPV_SCAN_THREADS, 0, stream>>>(in, out, n, nullptr);
+        count_launch();
+    } else {
+        uint32_t* sums = sc.scan_level(level);
+        uint32_t* sums_scanned = sums + blocks;
+        cpv_scan_blocks<<<static_cast<unsigned>(blocks), CPV_SCAN_THREADS, 0, stream>>>(in, out, n, sums);
+        count_launch();
+        const int r = scan_level(stream, sums, sums_scanned, blocks, nullptr, sc, level + 1);
+        if (r != kOk) return r;
+        cpv_scan_add<<<static_cast<unsigned>(blocks), CPV_SCAN_THREADS, 0, stream>>>(out, n, sums_scanned);
+        count_launch();
+    }
+    if (total) {
+        cpv_scan_total<<<1, 32, 0, stream>>>(in, out, n, total);
+        count_launch();
+    }
+    return kOk;
+}
+
+}  // namespace
+
+int scan_u32(cudaStream_t stream, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total, Scratch& sc) {
+    int r = sc.reserve_scan(n);
+    if (r != kOk) return r;
+    r = scan_level(stream, in, out, n, total, sc, 0);
+    if (r != kOk) return r;
+    CPV_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, uint32_t lo, uint32_t hi) {
+    if (!dst || texels == 0) return kOk;
+    const unsigned grid = static_cast<unsigned>(texels / 256 + 1 < 152 * 16 ? texels / 256 + 1 : 152 * 16);
+    switch (texel_bytes) {
+    case 1:
+        CPV_CUDA(cudaMemsetAsync(dst, static_cast<int>(lo & 0xFF), texels, stream));
+        return kOk;
+    case 2:
+        cpv_fill_u16<<<grid, 256, 0, stream>>>(static_cast<uint16_t*>(dst), texels, lo);
+        break;
+    case 4:
+        cpv_fill_u32<<<grid, 256, 0, stream>>>(static_cast<uint32_t*>(dst), texels, lo);
+        break;
+    case 8:
+        cpv_fill_u64<<<grid, 256, 0, stream>>>(static_cast<uint2*>(dst), texels, lo, hi);
+        break;
+    default:
+        return kErrInvalid;
+    }
+    count_launch();
+    CPV_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& sc) {
+    if (P.total_prims == 0 || P.fb_width == 0 || P.fb_height == 0) return kOk;
+    const uint32_t shift = m.tile_shift;
+    const uint32_t tile = 1u << shift;
+    P.tile_shift = shift;
+    P.tiles_x = (P.fb_width + tile - 1) / tile;
+    P.tiles_y = (P.fb_height + tile - 1) / tile;
+    const uint64_t tiles = static_cast<uint64_t>(P.tiles_x) * P.tiles_y;
+    const uint64_t G = P.total_prims;
+    int r = sc.ensure_words();
+    if (r != kOk) return r;
+    P.status = sc.words() + 1;
+    const uint32_t direct_limit = env_u32("CPV_DIRECT_LIMIT", 1u << 18);
+    uint32_t direct = (G * tiles <= direct_limit) ? 1u : 0u;
+    if (G > 0xFFFFFFFFull) return kErrInvalid;
+    if (!direct) {
+        // Spans: one warp per ~256 primitives, at most 4096 spans.
+        uint64_t spans = (G + 255) / 256;
+        if (spans > 4096) spans = 4096;
+        if (spans < 1) spans = 1;
+        const uint64_t bins = tiles * spans;
+        const uint32_t cap = env_u32("CPV_LIST_CAPACITY", 1u << 26);
+        if ((r = sc.reserve_rects(G)) != kOk) return r;
+        if ((r = sc.reserve_bins(bins)) != kOk) return r;
+        if ((r = sc.reserve_list(cap)) != kOk) return r;
+        P.rects = sc.rects();
+        P.spans = static_cast<uint32_t>(spans);
+        P.list_capacity = sc.list_capacity();
+        P.pair_total = sc.words();
+        P.tile_end = sc.cursor();
+        P.bin_list = sc.list();
+        CPV_CUDA(cudaMemsetAsync(sc.counts(), 0, bins * sizeof(uint32_t), stream));
+        {
+            void* args[] = {&P};
+            CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.setup_rects), dim3(static_cast<unsigned>((G + 255) / 256)), dim3(256), args, 0, stream));
+            count_launch();
+        }
+        const unsigned warp_blocks = static_cast<unsigned>((spans * 32 + 255) / 256);
+        cpv_span_count<<<warp_blocks, 256, 0, stream>>>(sc.rects(), G, static_cast<uint32_t>(spans), P.tiles_x, sc.counts());
+        count_launch();
+        if ((r = scan_u32(stream, sc.counts(), sc.cursor(), bins, sc.words(), sc)) != kOk) return r;
+        cpv_span_write<<<warp_blocks, 256, 0, stream>>>(sc.rects(), G, static_cast<uint32_t>(spans), P.tiles_x, sc.cursor(), sc.list(),
+                                                        sc.list_capacity(), sc.words());
+        count_launch();
+    }
+    {
+        void* args[] = {&P, &direct};
+        CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.raster), dim3(static_cast<unsigned>(tiles)), dim3(m.raster_threads), args, 0, stream));
+        count_launch();
+    }
+    return kOk;
+}
+
+}  // namespace cpv::rt

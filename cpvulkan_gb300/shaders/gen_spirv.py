@@ -1,0 +1,405 @@
+#!/usr/bin/env python3
+"""Emit the SPIR-V modules of the shader programs the harness renders with.
+
+There is no GLSL compiler in this image, so the vertex/fragment modules are
+assembled directly from the SPIR-V 1.0 binary specification (word layout,
+opcode and enumerant numbers). Each program mirrors a GLSL shader given in its
+docstring; the instruction sequence is what the CPU oracle restates op for op.
+
+Usage: python gen_spirv.py [outdir]   (default: this directory)
+Writes <program>.vert.spv / <program>.frag.spv.
+"""
+import os
+import struct
+import sys
+
+# --- opcodes (SPIR-V 1.0) ---------------------------------------------------
+OP = dict(
+    Name=5, MemberName=6, ExtInstImport=11, ExtInst=12, MemoryModel=14, EntryPoint=15, ExecutionMode=16,
+    Capability=17, TypeVoid=19, TypeBool=20, TypeInt=21, TypeFloat=22, TypeVector=23, TypeMatrix=24,
+    TypeImage=25, TypeSampledImage=27, TypeArray=28, TypeStruct=30, TypePointer=32, TypeFunction=33,
+    Constant=43, ConstantComposite=44, Function=54, FunctionEnd=56, Variable=59, Load=61, Store=62,
+    AccessChain=65, Decorate=71, MemberDecorate=72, VectorShuffle=79, CompositeConstruct=80,
+    CompositeExtract=81, ImageSampleImplicitLod=87, FAdd=129, FSub=131, FMul=133, FDiv=136,
+    VectorTimesScalar=142, MatrixTimesVector=145, Dot=148, FOrdGreaterThan=186, SelectionMerge=247,
+    Label=248, Branch=249, BranchConditional=250, Kill=252, Return=253,
+)
+DEC = dict(Block=2, ColMajor=5, MatrixStride=7, BuiltIn=11, NoPerspective=13, Flat=14, Location=30, Binding=33,
+           DescriptorSet=34, Offset=35)
+SC = dict(UniformConstant=0, Input=1, Uniform=2, Output=3, Function=7, PushConstant=9)
+BUILTIN = dict(Position=0, PointSize=1, ClipDistance=3, CullDistance=4)
+GLSL = dict(FMax=40, Normalize=69)
+
+
+def _str_words(s):
+    b = s.encode() + b"\0"
+    b += b"\0" * ((4 - len(b) % 4) % 4)
+    return list(struct.unpack("<%dI" % (len(b) // 4), b))
+
+
+def _f32(x):
+    return struct.unpack("<I", struct.pack("<f", x))[0]
+
+
+class Module:
+    """Minimal SPIR-V module builder with type/constant de-duplication."""
+
+    def __init__(self, model):
+        self.model = model  # 0 vertex, 4 fragment
+        self.next_id = 1
+        self.caps, self.ext, self.mem, self.entry, self.modes = [], [], [], [], []
+        self.names, self.annot, self.types, self.body = [], [], [], []
+        self.cache = {}
+        self.interface = []
+        self.glsl = self.id()
+        self.ext.append(self._ins("ExtInstImport", [self.glsl] + _str_words("GLSL.std.450")))
+
+    def id(self):
+        i = self.next_id
+        self.next_id += 1
+        return i
+
+    @staticmethod
+    def _ins(op, words):
+        return [((len(words) + 1) << 16) | OP[op]] + list(words)
+
+    def _type(self, key, op, words_fn):
+        if key not in self.cache:
+            i = self.id()
+            self.types.append(self._ins(op, [i] + words_fn()))
+            self.cache[key] = i
+        return self.cache[key]
+
+    def _const(self, key, op, type_fn, words_fn):
+        """Constants put the result type before the result id."""
+        if key not in self.cache:
+            t = type_fn()
+            words = words_fn()
+            i = self.id()
+            self.types.append(self._ins(op, [t, i] + words))
+            self.cache[key] = i
+        return self.cache[key]
+
+    # types
+    def void(self): return self._type(("void",), "TypeVoid", lambda: [])
+    def bool(self): return self._type(("bool",), "TypeBool", lambda: [])
+    def int(self): return self._type(("int",), "TypeInt", lambda: [32, 1])
+    def float(self): return self._type(("float",), "TypeFloat", lambda: [32])
+    def vec(self, n): return self._type(("vec", n), "TypeVector", lambda: [self.float(), n])
+    def mat4(self): return self._type(("mat4",), "TypeMatrix", lambda: [self.vec(4), 4])
+    def ptr(self, sc, t): return self._type(("ptr", sc, t), "TypePointer", lambda: [SC[sc], t])
+    def fn_void(self): return self._type(("fnvoid",), "TypeFunction", lambda: [self.void()])
+
+    def array(self, t, n):
+        return self._type(("arr", t, n), "TypeArray", lambda: [t, self.const_int(n)])
+
+    def struct(self, key, members):
+        return self._type(("struct", key), "TypeStruct", lambda: list(members))
+
+    def sampled_image_2d(self):
+        img = self._type(("img2d",), "TypeImage", lambda: [self.float(), 1, 0, 0, 0, 1, 0])
+        return self._type(("simg2d",), "TypeSampledImage", lambda: [img])
+
+    # constants
+    def const_f(self, x):
+        return self._const(("cf", _f32(x)), "Constant", self.float, lambda: [_f32(x)])
+
+    def const_int(self, x):
+        return self._const(("ci", x), "Constant", self.int, lambda: [x & 0xFFFFFFFF])
+
+    # declarations
+    def decorate(self, target, dec, *lits):
+        self.annot.append(self._ins("Decorate", [target, DEC[dec]] + list(lits)))
+
+    def member_decorate(self, st, member, dec, *lits):
+        self.annot.append(self._ins("MemberDecorate", [st, member, DEC[dec]] + list(lits)))
+
+    def name(self, target, s):
+        self.names.append(self._ins("Name", [target] + _str_words(s)))
+
+    def variable(self, sc, t, name=None):
+        v = self.id()
+        self.types.append(self._ins("Variable", [self.ptr(sc, t), v, SC[sc]]))
+        if name:
+            self.name(v, name)
+        if sc in ("Input", "Output"):
+            self.interface.append(v)
+        return v
+
+    # instructions in the function body
+    def op(self, opname, rtype, *args):
+        r = self.id()
+        self.body.append(self._ins(opname, [rtype, r] + list(args)))
+        return r
+
+    def op_void(self, opname, *args):
+        self.body.append(self._ins(opname, list(args)))
+
+    def load(self, t, p): return self.op("Load", t, p)
+    def store(self, p, v): self.op_void("Store", p, v)
+    def access(self, sc, t, base, *idx): return self.op("AccessChain", self.ptr(sc, t), base, *idx)
+    def ext_inst(self, t, inst, *args): return self.op("ExtInst", t, self.glsl, GLSL[inst], *args)
+    def label(self):
+        lbl = self.id()
+        self.body.append(self._ins("Label", [lbl]))
+        return lbl
+
+    def per_vertex_block(self):
+        """gl_PerVertex { vec4 Position; float PointSize; float ClipDistance[1]; float CullDistance[1]; }"""
+        f = self.float()
+        arr = self.array(f, 1)
+        st = self.struct("gl_PerVertex", [self.vec(4), f, arr, arr])
+        self.member_decorate(st, 0, "BuiltIn", BUILTIN["Position"])
+        self.member_decorate(st, 1, "BuiltIn", BUILTIN["PointSize"])
+        self.member_decorate(st, 2, "BuiltIn", BUILTIN["ClipDistance"])
+        self.member_decorate(st, 3, "BuiltIn", BUILTIN["CullDistance"])
+        self.decorate(st, "Block")
+        return st, self.variable("Output", st, "gl_PerVertex")
+
+    def ubo_block(self, key, members, offsets, binding, set_=0, sc="Uniform"):
+        st = self.struct(key, members)
+        for i, off in enumerate(offsets):
+            self.member_decorate(st, i, "Offset", off)
+            if members[i] == self.mat4():
+                self.member_decorate(st, i, "ColMajor")
+                self.member_decorate(st, i, "MatrixStride", 16)
+        self.decorate(st, "Block")
+        v = self.variable(sc, st, key.lower())
+        if sc == "Uniform":
+            self.decorate(v, "DescriptorSet", set_)
+            self.decorate(v, "Binding", binding)
+        return v
+
+    def assemble(self, body_fn):
+        """body_fn(mod) emits the entry function body after its first label."""
+        fn = self.id()
+        self.body.append(self._ins("Function", [self.void(), fn, 0, self.fn_void()]))
+        self.label()
+        body_fn(self)
+        self.body.append(self._ins("FunctionEnd", []))
+        self.caps.append(self._ins("Capability", [1]))
+        self.mem.append(self._ins("MemoryModel", [0, 1]))
+        self.entry.append(self._ins("EntryPoint", [self.model, fn] + _str_words("main") + self.interface))
+        if self.model == 4:
+            self.modes.append(self._ins("ExecutionMode", [fn, 7]))  # OriginUpperLeft
+        words = [0x07230203, 0x00010000, 0, self.next_id, 0]
+        for sec in (self.caps, self.ext, self.mem, self.entry, self.modes, self.names, self.annot, self.types,
+                    self.body):
+            for ins in sec:
+                words += ins
+        return struct.pack("<%dI" % len(words), *words)
+
+
+# --- programs -----------------------------------------------------------------
+
+def cube_vert():
+    """layout(set=0,binding=0) uniform UBO { mat4 mvp; };
+    layout(location=0) in vec4 pos; layout(location=1) in vec4 inColor;
+    layout(location=0) out vec4 outColor;
+    void main() { outColor = inColor; gl_Position = mvp * pos; }"""
+    m = Module(0)
+    v4, mat = m.vec(4), m.mat4()
+    ubo = m.ubo_block("UBO", [mat], [0], binding=0)
+    pos = m.variable("Input", v4, "pos")
+    m.decorate(pos, "Location", 0)
+    col = m.variable("Input", v4, "inColor")
+    m.decorate(col, "Location", 1)
+    out = m.variable("Output", v4, "outColor")
+    m.decorate(out, "Location", 0)
+    pv_t, pv = m.per_vertex_block()
+
+    def body(m):
+        c = m.load(v4, col)
+        m.store(out, c)
+        mp = m.access("Uniform", mat, ubo, m.const_int(0))
+        mv = m.load(mat, mp)
+        p = m.load(v4, pos)
+        r = m.op("MatrixTimesVector", v4, mv, p)
+        dst = m.access("Output", v4, pv, m.const_int(0))
+        m.store(dst, r)
+        m.op_void("Return")
+    return m.assemble(body)
+
+
+def colour_frag(decoration=None, discard=False):
+    """layout(location=0) [flat|noperspective] in vec4 color; layout(location=0) out vec4 o;
+    void main() { [if (color.r > 0.5) discard;] o = color; }"""
+    m = Module(4)
+    v4, f = m.vec(4), m.float()
+    col = m.variable("Input", v4, "color")
+    m.decorate(col, "Location", 0)
+    if decoration:
+        m.decorate(col, decoration)
+    out = m.variable("Output", v4, "o")
+    m.decorate(out, "Location", 0)
+
+    def body(m):
+        c = m.load(v4, col)
+        if discard:
+            r = m.op("CompositeExtract", f, c, 0)
+            cond = m.op("FOrdGreaterThan", m.bool(), r, m.const_f(0.5))
+            kill_lbl, merge_lbl = m.id(), m.id()
+            m.op_void("SelectionMerge", merge_lbl, 0)
+            m.op_void("BranchConditional", cond, kill_lbl, merge_lbl)
+            m.body.append(m._ins("Label", [kill_lbl]))
+            m.op_void("Kill")
+            m.body.append(m._ins("Label", [merge_lbl]))
+        m.store(out, c)
+        m.op_void("Return")
+    return m.assemble(body)
+
+
+def texlit_vert():
+    """layout(set=0,binding=0) uniform UBO { mat4 mvp; vec4 light; };
+    layout(location=0) in vec3 pos; layout(location=1) in vec2 uv; layout(location=2) in vec3 normal;
+    layout(location=0) out vec2 vUV; layout(location=1) out vec3 vN;
+    void main() { vUV = uv; vN = normal; gl_Position = mvp * vec4(pos, 1.0); }"""
+    m = Module(0)
+    v2, v3, v4, mat, f = m.vec(2), m.vec(3), m.vec(4), m.mat4(), m.float()
+    ubo = m.ubo_block("UBO", [mat, v4], [0, 64], binding=0)
+    pos = m.variable("Input", v3, "pos"); m.decorate(pos, "Location", 0)
+    uv = m.variable("Input", v2, "uv"); m.decorate(uv, "Location", 1)
+    nrm = m.variable("Input", v3, "normal"); m.decorate(nrm, "Location", 2)
+    ouv = m.variable("Output", v2, "vUV"); m.decorate(ouv, "Location", 0)
+    on = m.variable("Output", v3, "vN"); m.decorate(on, "Location", 1)
+    pv_t, pv = m.per_vertex_block()
+
+    def body(m):
+        m.store(ouv, m.load(v2, uv))
+        m.store(on, m.load(v3, nrm))
+        mv = m.load(mat, m.access("Uniform", mat, ubo, m.const_int(0)))
+        p = m.load(v3, pos)
+        p4 = m.op("CompositeConstruct", v4, p, m.const_f(1.0))
+        r = m.op("MatrixTimesVector", v4, mv, p4)
+        m.store(m.access("Output", v4, pv, m.const_int(0)), r)
+        m.op_void("Return")
+    return m.assemble(body)
+
+
+def texlit_frag():
+    """layout(set=0,binding=0) uniform UBO { mat4 mvp; vec4 light; };
+    layout(set=0,binding=1) uniform sampler2D tex;
+    layout(location=0) in vec2 uv; layout(location=1) in vec3 n; layout(location=0) out vec4 o;
+    void main() { vec4 c = texture(tex, uv); float l = max(dot(normalize(n), light.xyz), 0.0);
+                  o = vec4(c.xyz * l, c.w); }"""
+    m = Module(4)
+    v2, v3, v4, mat, f = m.vec(2), m.vec(3), m.vec(4), m.mat4(), m.float()
+    ubo = m.ubo_block("UBO", [mat, v4], [0, 64], binding=0)
+    simg = m.sampled_image_2d()
+    tex = m.variable("UniformConstant", simg, "tex")
+    m.decorate(tex, "DescriptorSet", 0)
+    m.decorate(tex, "Binding", 1)
+    uv = m.variable("Input", v2, "uv"); m.decorate(uv, "Location", 0)
+    n = m.variable("Input", v3, "n"); m.decorate(n, "Location", 1)
+    out = m.variable("Output", v4, "o"); m.decorate(out, "Location", 0)
+
+    def body(m):
+        s = m.load(simg, tex)
+        c = m.op("ImageSampleImplicitLod", v4, s, m.load(v2, uv))
+        nn = m.ext_inst(v3, "Normalize", m.load(v3, n))
+        light = m.load(v4, m.access("Uniform", v4, ubo, m.const_int(1)))
+        lxyz = m.op("VectorShuffle", v3, light, light, 0, 1, 2)
+        d = m.op("Dot", f, nn, lxyz)
+        l = m.ext_inst(f, "FMax", d, m.const_f(0.0))
+        cxyz = m.op("VectorShuffle", v3, c, c, 0, 1, 2)
+        rgb = m.op("VectorTimesScalar", v3, cxyz, l)
+        cw = m.op("CompositeExtract", f, c, 3)
+        m.store(out, m.op("CompositeConstruct", v4, rgb, cw))
+        m.op_void("Return")
+    return m.assemble(body)
+
+
+def flatquad_vert():
+    """layout(location=0) in vec2 pos; layout(location=1) in vec4 color; layout(location=0) out vec4 vColor;
+    void main() { vColor = color; gl_Position = vec4(pos, 0.0, 1.0); }"""
+    m = Module(0)
+    v2, v4 = m.vec(2), m.vec(4)
+    pos = m.variable("Input", v2, "pos"); m.decorate(pos, "Location", 0)
+    col = m.variable("Input", v4, "color"); m.decorate(col, "Location", 1)
+    out = m.variable("Output", v4, "vColor"); m.decorate(out, "Location", 0)
+    pv_t, pv = m.per_vertex_block()
+
+    def body(m):
+        m.store(out, m.load(v4, col))
+        p = m.load(v2, pos)
+        p4 = m.op("CompositeConstruct", v4, p, m.const_f(0.0), m.const_f(1.0))
+        m.store(m.access("Output", v4, pv, m.const_int(0)), p4)
+        m.op_void("Return")
+    return m.assemble(body)
+
+
+def meshpc_vert():
+    """layout(push_constant) uniform PC { mat4 mvp; vec4 color; };
+    layout(location=0) in vec3 pos; layout(location=1) in vec3 normal; layout(location=2) in vec4 offset;
+    layout(location=0) out vec3 vN;
+    void main() { vN = normal; gl_Position = mvp * vec4(pos + offset.xyz, 1.0); }"""
+    m = Module(0)
+    v3, v4, mat = m.vec(3), m.vec(4), m.mat4()
+    pc = m.ubo_block("PC", [mat, v4], [0, 64], binding=0, sc="PushConstant")
+    pos = m.variable("Input", v3, "pos"); m.decorate(pos, "Location", 0)
+    nrm = m.variable("Input", v3, "normal"); m.decorate(nrm, "Location", 1)
+    off = m.variable("Input", v4, "offset"); m.decorate(off, "Location", 2)
+    on = m.variable("Output", v3, "vN"); m.decorate(on, "Location", 0)
+    pv_t, pv = m.per_vertex_block()
+
+    def body(m):
+        m.store(on, m.load(v3, nrm))
+        o = m.load(v4, off)
+        oxyz = m.op("VectorShuffle", v3, o, o, 0, 1, 2)
+        s = m.op("FAdd", v3, m.load(v3, pos), oxyz)
+        p4 = m.op("CompositeConstruct", v4, s, m.const_f(1.0))
+        mv = m.load(mat, m.access("PushConstant", mat, pc, m.const_int(0)))
+        r = m.op("MatrixTimesVector", v4, mv, p4)
+        m.store(m.access("Output", v4, pv, m.const_int(0)), r)
+        m.op_void("Return")
+    return m.assemble(body)
+
+
+def meshpc_frag():
+    """layout(push_constant) uniform PC { mat4 mvp; vec4 color; };
+    layout(location=0) in vec3 n; layout(location=0) out vec4 o;
+    void main() { float l = max(dot(normalize(n), vec3(0.48, 0.6, 0.64)), 0.0) * 0.8 + 0.2;
+                  o = vec4(color.xyz * l, color.w); }"""
+    m = Module(4)
+    v3, v4, mat, f = m.vec(3), m.vec(4), m.mat4(), m.float()
+    pc = m.ubo_block("PC", [mat, v4], [0, 64], binding=0, sc="PushConstant")
+    n = m.variable("Input", v3, "n"); m.decorate(n, "Location", 0)
+    out = m.variable("Output", v4, "o"); m.decorate(out, "Location", 0)
+    light = m._const(("cc_light",), "ConstantComposite", lambda: v3,
+                     lambda: [m.const_f(0.48), m.const_f(0.6), m.const_f(0.64)])
+
+    def body(m):
+        nn = m.ext_inst(v3, "Normalize", m.load(v3, n))
+        d = m.op("Dot", f, nn, light)
+        l0 = m.ext_inst(f, "FMax", d, m.const_f(0.0))
+        l1 = m.op("FMul", f, l0, m.const_f(0.8))
+        l = m.op("FAdd", f, l1, m.const_f(0.2))
+        col = m.load(v4, m.access("PushConstant", v4, pc, m.const_int(1)))
+        cxyz = m.op("VectorShuffle", v3, col, col, 0, 1, 2)
+        rgb = m.op("VectorTimesScalar", v3, cxyz, l)
+        cw = m.op("CompositeExtract", f, col, 3)
+        m.store(out, m.op("CompositeConstruct", v4, rgb, cw))
+        m.op_void("Return")
+    return m.assemble(body)
+
+
+PROGRAMS = {
+    "cube": (cube_vert, lambda: colour_frag()),
+    "texlit": (texlit_vert, texlit_frag),
+    "flatquad": (flatquad_vert, lambda: colour_frag("Flat")),
+    "meshpc": (meshpc_vert, meshpc_frag),
+    "discard": (cube_vert, lambda: colour_frag(discard=True)),
+    "nopersp": (cube_vert, lambda: colour_frag("NoPerspective")),
+}
+
+
+def main(outdir):
+    os.makedirs(outdir, exist_ok=True)
+    for name, (vert, frag) in PROGRAMS.items():
+        for stage, fn in (("vert", vert), ("frag", frag)):
+            with open(os.path.join(outdir, "%s.%s.spv" % (name, stage)), "wb") as fh:
+                fh.write(fn())
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else os.path.dirname(os.path.abspath(__file__)))

@@ -1,0 +1,135 @@
+/*
+ * scene.h — plain-data description of one frame of draws: the contract
+ * between the headless application harness (which turns it into Vulkan calls
+ * on the ICD) and the CPU oracle (which renders the same bytes with the
+ * reference's CPU draw semantics).
+ *
+ * Nothing here is a Vulkan object. Enumerants reuse the Vulkan values (see
+ * vk_subset.h) so that the harness passes them through unchanged.
+ *
+ * A frame = begin render pass (clear colour, clear depth) → draws in order →
+ * end render pass. Every draw binds one pipeline, its vertex buffer offsets,
+ * optional index buffer offset and push constants. One uniform block (set 0,
+ * binding 0) and at most one combined image sampler (set 0, binding 1) are
+ * shared by all draws of a scene.
+ */
+#ifndef CPV_SCENE_H
+#define CPV_SCENE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Shader programs (vertex + fragment pair). The harness maps each to the
+ * SPIR-V modules it ships; the oracle maps each to a hand-written C++
+ * restatement of the same arithmetic. */
+enum cpv_program {
+    CPV_PROGRAM_CUBE = 0,        /* pos vec4 + colour vec4 → UBO mat4 MVP; FS passes colour                      */
+    CPV_PROGRAM_TEXLIT = 1,      /* pos vec3 + uv vec2 + normal vec3 → UBO {MVP, light}; FS texture × Lambert  */
+    CPV_PROGRAM_FLATQUAD = 2,    /* pos vec2 (NDC) + flat colour vec4 → FS passes colour                         */
+    CPV_PROGRAM_MESHPC = 3,      /* pos vec3 + normal vec3 + per-instance offset vec4 → push {MVP, colour}; Lambert */
+    CPV_PROGRAM_DISCARD = 4,     /* CUBE with a fragment discard when colour.r > 0.5 (OpKill coverage)          */
+    CPV_PROGRAM_NOPERSP = 5,     /* CUBE with noperspective colour (InterpolationType::Linear coverage)         */
+    CPV_PROGRAM_COUNT = 6
+};
+
+#define CPV_SCENE_MAX_BINDINGS 4
+#define CPV_SCENE_MAX_ATTRIBUTES 8
+#define CPV_SCENE_MAX_PUSH 128
+
+typedef struct cpv_scene_binding {
+    uint32_t binding;
+    uint32_t stride;
+    uint32_t input_rate; /* VkVertexInputRate */
+} cpv_scene_binding;
+
+typedef struct cpv_scene_attribute {
+    uint32_t location;
+    uint32_t binding;
+    uint32_t format; /* VkFormat */
+    uint32_t offset;
+} cpv_scene_attribute;
+
+typedef struct cpv_scene_stencil {
+    uint32_t fail_op, pass_op, depth_fail_op, compare_op;
+    uint32_t compare_mask, write_mask, reference;
+} cpv_scene_stencil;
+
+typedef struct cpv_scene_pipeline {
+    uint32_t program;    /* cpv_program */
+    uint32_t topology;   /* VkPrimitiveTopology (triangle list / strip / fan) */
+    uint32_t cull_mode;  /* VkCullModeFlags */
+    uint32_t front_face; /* VkFrontFace */
+    uint32_t depth_test, depth_write, depth_compare;
+    uint32_t stencil_test;
+    cpv_scene_stencil stencil_front, stencil_back;
+    uint32_t blend_enable;
+    uint32_t src_color, dst_color, color_op;
+    uint32_t src_alpha, dst_alpha, alpha_op;
+    float blend_constants[4];
+    uint32_t num_bindings;
+    cpv_scene_binding bindings[CPV_SCENE_MAX_BINDINGS];
+    uint32_t num_attributes;
+    cpv_scene_attribute attributes[CPV_SCENE_MAX_ATTRIBUTES];
+} cpv_scene_pipeline;
+
+typedef struct cpv_scene_draw {
+    uint32_t pipeline;       /* index into pipelines */
+    uint32_t indexed;        /* vkCmdDrawIndexed when non-zero */
+    uint32_t count;          /* vertexCount or indexCount */
+    uint32_t instance_count;
+    uint32_t first;          /* firstVertex or firstIndex */
+    int32_t vertex_offset;   /* vertexOffset (indexed only) */
+    uint32_t first_instance;
+    uint32_t push_size;
+    uint64_t vertex_offsets[CPV_SCENE_MAX_BINDINGS]; /* byte offsets into vertex_data, per binding slot */
+    uint64_t index_offset;   /* byte offset into index_data */
+    uint8_t push[CPV_SCENE_MAX_PUSH];
+} cpv_scene_draw;
+
+typedef struct cpv_scene_sampler {
+    uint32_t mag_filter, min_filter, mipmap_mode;
+    uint32_t address_u, address_v, address_w;
+    float mip_lod_bias, min_lod, max_lod;
+    uint32_t border_color;
+} cpv_scene_sampler;
+
+typedef struct cpv_scene {
+    uint32_t width, height;
+    uint32_t color_format; /* VkFormat: R8G8B8A8_UNORM or B8G8R8A8_UNORM */
+    uint32_t depth_format; /* VkFormat: 0 (none), D16_UNORM, D32_SFLOAT, D32_SFLOAT_S8_UINT */
+    float clear_color[4];
+    float clear_depth;
+    uint32_t clear_stencil;
+    float viewport[6]; /* x, y, width, height, minDepth, maxDepth */
+
+    const uint8_t* vertex_data;
+    uint64_t vertex_bytes;
+    const uint8_t* index_data;
+    uint64_t index_bytes;
+    uint32_t index_type; /* VkIndexType */
+
+    const uint8_t* uniform_data; /* set 0 binding 0 (may be null) */
+    uint32_t uniform_bytes;
+
+    /* set 0 binding 1: one 2D texture with a full linear mip chain, levels
+     * concatenated level after level (the reference's linear image layout). */
+    const uint8_t* texture_data;
+    uint64_t texture_bytes;
+    uint32_t texture_width, texture_height, texture_levels;
+    uint32_t texture_format; /* VkFormat, R8G8B8A8_UNORM */
+    cpv_scene_sampler sampler;
+
+    uint32_t num_pipelines;
+    const cpv_scene_pipeline* pipelines;
+    uint32_t num_draws;
+    const cpv_scene_draw* draws;
+} cpv_scene;
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CPV_SCENE_H */

@@ -1,0 +1,85 @@
+/*
+ * cpv_harness.h — C ABI of libcpv_harness.so: a headless application that
+ * loads an ICD shared object the way the Vulkan loader does (dlopen,
+ * vk_icdNegotiateLoaderICDInterfaceVersion, vk_icdGetInstanceProcAddr,
+ * dispatch-word check) and renders plain-data scenes (cpv/scene.h) through
+ * the Vulkan API only. It stands in for the loader and the LunarG samples,
+ * neither of which exists on these machines.
+ *
+ * It also holds the seeded scene generators of the benchmark workloads.
+ */
+#ifndef CPV_HARNESS_H
+#define CPV_HARNESS_H
+
+#include <stdint.h>
+
+#include "cpv/scene.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Scene configurations. */
+enum cpvh_config {
+    CPVH_CUBE = 1,        /* spinning cube, 500x500 BGRA8 + D16 (param0 = frame index)                         */
+    CPVH_HEIGHTFIELD = 2, /* textured heightfield (param0 = grid side, default 1024; param1/2 = width/height)   */
+    CPVH_BLEND = 3,       /* blend-bound overdraw quads (param0 = quad count, default 200000; param1/2 = w/h)  */
+    CPVH_BATCH = 4,       /* 4096 icosphere draws (param0 = draw count, param1 = max triangles, param2/3 = w/h) */
+    CPVH_PROGRAM = 5,     /* small scene for one shader program (param0 = cpv_program, param1 = variant)       */
+    CPVH_SERVE = 6        /* one serving request (param0 = side px, param1 = triangles, param2 = client id)     */
+};
+
+/* Builds a scene; the harness owns every array it points to. */
+cpv_scene* cpvh_scene_create(uint32_t config, uint64_t seed, const uint64_t* params, uint32_t num_params);
+void cpvh_scene_destroy(cpv_scene* scene);
+/* Updates the per-frame data of a scene (the cube's rotation for frame f). */
+void cpvh_scene_set_frame(cpv_scene* scene, uint32_t frame);
+/* Total triangles of all draws × instances. */
+uint64_t cpvh_scene_triangles(const cpv_scene* scene);
+
+typedef struct cpvh_context cpvh_context;
+typedef struct cpvh_renderer cpvh_renderer;
+
+/* Loads the ICD at icd_path and creates instance, device and queue.
+ * Returns NULL and fills err on failure. */
+cpvh_context* cpvh_open(const char* icd_path, char* err, uint32_t err_len);
+void cpvh_close(cpvh_context* ctx);
+
+/* Creates every Vulkan object the scene needs and records one command
+ * buffer (clear + all draws). Vertex/index/uniform/texture data are uploaded
+ * once into device-local memory through a staging buffer. */
+cpvh_renderer* cpvh_renderer_create(cpvh_context* ctx, const cpv_scene* scene, char* err, uint32_t err_len);
+void cpvh_renderer_destroy(cpvh_renderer* r);
+
+/* Submits the recorded frame `frames` times, waiting on the fence after each
+ * submission. device_ms: device time of all frames (queue events) or NULL;
+ * latency_ms: per-frame host submit→fence times (array of `frames`) or NULL.
+ * Returns a VkResult. */
+int cpvh_render(cpvh_renderer* r, uint32_t frames, double* device_ms, double* latency_ms);
+
+/* End-to-end frame through the public API: uploads the scene's vertex,
+ * index and uniform bytes from host memory (map/copy/unmap + vkCmdCopyBuffer),
+ * renders, copies the colour attachment to a host-visible buffer and reads
+ * it back. Returns a VkResult; bytes moved are reported. */
+int cpvh_render_e2e(cpvh_renderer* r, uint32_t frames, double* total_ms, uint64_t* h2d_bytes, uint64_t* d2h_bytes);
+
+/* Creates (then destroys) only the scene's graphics pipelines: SPIR-V
+ * translation and NVRTC compilation, without rendering. Returns a VkResult. */
+int cpvh_compile_pipelines(cpvh_context* ctx, const cpv_scene* scene, char* err, uint32_t err_len);
+
+/* Re-uploads the scene's uniform buffer and push constants (e.g. after
+ * cpvh_scene_set_frame) and re-records the frame. */
+int cpvh_renderer_update(cpvh_renderer* r);
+
+/* Reads the attachments back (colour: width*height*4; depth: texel-sized). */
+int cpvh_readback(cpvh_renderer* r, uint8_t* color, uint8_t* depth);
+
+/* The ICD's vkQueue (for the ICD's timing helpers). */
+void* cpvh_queue(cpvh_context* ctx);
+const char* cpvh_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CPV_HARNESS_H */

@@ -1,0 +1,917 @@
+/*
+ * oracle.cpp — CPU oracle for the draw hot path. TEST INFRASTRUCTURE ONLY
+ * (see oracle.h for who may call it and its parity status).
+ *
+ * Build: g++ -O2 -std=c++17 -ffp-contract=off (oracle/Makefile). Contraction
+ * must stay off: the reference's arithmetic is plain IEEE single precision
+ * with no fused multiply-add (its JIT emits separate fmul/fadd,
+ * LLVMRuntime/Jit.cpp:44-71, and the ICD's own C++ was built for x86-64
+ * without FMA), and GCC on aarch64 contracts by default.
+ *
+ * Every function cites the reference lines it restates. Paths are relative
+ * to the reference project root.
+ */
+#include "oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+namespace {
+
+enum : uint32_t {
+    FMT_R8G8B8A8_UNORM = 37,
+    FMT_B8G8R8A8_UNORM = 44,
+    FMT_R32_SFLOAT = 100,
+    FMT_R32G32_SFLOAT = 103,
+    FMT_R32G32B32_SFLOAT = 106,
+    FMT_R32G32B32A32_SFLOAT = 109,
+    FMT_D16_UNORM = 124,
+    FMT_D32_SFLOAT = 126,
+    FMT_D32_SFLOAT_S8_UINT = 130,
+};
+
+enum : uint32_t { TOPO_TRIANGLE_LIST = 3, TOPO_TRIANGLE_STRIP = 4, TOPO_TRIANGLE_FAN = 5 };
+enum : uint32_t { CULL_FRONT = 1, CULL_BACK = 2 };
+enum : uint32_t { FRONT_FACE_CW = 1 };
+enum : uint32_t { RATE_VERTEX = 0, RATE_INSTANCE = 1 };
+
+constexpr int kMaxVaryings = 16;
+
+/* ---------------------------------------------------------------------- */
+/* Scalar helpers                                                          */
+/* ---------------------------------------------------------------------- */
+
+/* static_cast<int32_t>(float) as both target machines execute it
+ * (saturating, NaN → 0): the reference relies on this conversion for the
+ * screen bounding box (CPVulkan/CommandBuffer.Draw.cpp:1548-1563). */
+int32_t f2i(float f) {
+    if (f != f) return 0;
+    if (f >= 2147483648.0f) return std::numeric_limits<int32_t>::max();
+    if (f < -2147483648.0f) return std::numeric_limits<int32_t>::min();
+    return static_cast<int32_t>(f);
+}
+
+/* std::max / std::min / std::clamp as the reference's GLSL helpers call
+ * them (CPVulkan/GlslFunctions.cpp:106-140). */
+float fmax_std(float a, float b) { return (a < b) ? b : a; }
+float fmin_std(float a, float b) { return (b < a) ? b : a; }
+
+/* llvm.maxnum / llvm.minnum (NaN-ignoring), used by the pixel encoders
+ * (LLVMRuntime/ImageCompiler.cpp:540-560). */
+float maxnum(float a, float b) { if (a != a) return b; if (b != b) return a; return a > b ? a : b; }
+float minnum(float a, float b) { if (a != a) return b; if (b != b) return a; return a < b ? a : b; }
+
+/* UNORM encode: minnum(maxnum(x,0),1) * (2^n-1) → llvm.round (half away
+ * from zero) → fptoui (LLVMRuntime/ImageCompiler.cpp:27-32, 1081-1095). */
+uint32_t encode_unorm(float x, float maxv) {
+    float v = minnum(maxnum(x, 0.0f), 1.0f);
+    v = v * maxv;
+    v = std::round(v);
+    return static_cast<uint32_t>(v);
+}
+
+/* UNORM decode: uitofp / (2^n-1) (LLVMRuntime/ImageCompiler.cpp:43-53). */
+float decode_unorm8(uint8_t u) { return static_cast<float>(u) / 255.0f; }
+float decode_unorm16(uint16_t u) { return static_cast<float>(u) / 65535.0f; }
+
+/* EdgeFunction (CPVulkan/CommandBuffer.Draw.cpp:410-418). */
+float edge(float ax, float ay, float bx, float by, float cx, float cy) {
+    const float t0 = (cx - ax) * (by - ay);
+    const float t1 = (cy - ay) * (bx - ax);
+    return t0 - t1;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Vector helpers with the operand order the reference's glm calls give.   */
+/* glm is a third-party dependency absent from the mount; the order below  */
+/* restates glm 0.9.9's published operator*(mat4, vec4) (pairwise column   */
+/* sums), compute_dot (left-to-right for vec2/vec3, pairwise for vec4) and */
+/* normalize (x * (1 / sqrt(dot(x, x)))). Parity unpinned.                 */
+/* ---------------------------------------------------------------------- */
+
+struct V4 { float x, y, z, w; };
+
+V4 mat4_mul_vec4(const float* m /* column-major 16 */, const float v[4]) {
+    float r[4];
+    for (int i = 0; i < 4; i++) {
+        const float mul0 = m[0 * 4 + i] * v[0];
+        const float mul1 = m[1 * 4 + i] * v[1];
+        const float add0 = mul0 + mul1;
+        const float mul2 = m[2 * 4 + i] * v[2];
+        const float mul3 = m[3 * 4 + i] * v[3];
+        const float add1 = mul2 + mul3;
+        r[i] = add0 + add1;
+    }
+    return V4{r[0], r[1], r[2], r[3]};
+}
+
+float dot3(const float a[3], const float b[3]) {
+    const float t0 = a[0] * b[0];
+    const float t1 = a[1] * b[1];
+    const float t2 = a[2] * b[2];
+    return (t0 + t1) + t2;
+}
+
+void normalize3(const float v[3], float out[3]) {
+    const float d = dot3(v, v);
+    const float inv = 1.0f / std::sqrt(d);
+    out[0] = v[0] * inv;
+    out[1] = v[1] * inv;
+    out[2] = v[2] * inv;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Image sampler (CPVulkan/ImageSampler.cpp)                               */
+/* ---------------------------------------------------------------------- */
+
+struct Texture {
+    const uint8_t* data = nullptr;
+    uint64_t bytes = 0;
+    uint32_t width = 0, height = 0, levels = 0;
+    uint64_t level_offset[16] = {};
+    uint32_t level_w[16] = {}, level_h[16] = {};
+};
+
+/* wrap (CPVulkan/ImageSampler.cpp:12-38). */
+int32_t wrap(int32_t v, int32_t size, uint32_t mode) {
+    switch (mode) {
+    case 0: /* REPEAT */
+        return (v % size + size) % size;
+    case 1: { /* MIRRORED_REPEAT */
+        const int32_t two = 2 * size;
+        const int32_t n = (v % two + two) % two - size;
+        return size - 1 - (n >= 0 ? n : -(1 + n));
+    }
+    case 2: /* CLAMP_TO_EDGE */
+        return std::clamp(v, 0, size - 1);
+    case 3: /* CLAMP_TO_BORDER */
+        return std::clamp(v, -1, size);
+    case 4: /* MIRROR_CLAMP_TO_EDGE */
+        return std::clamp(v >= 0 ? v : -(1 + v), 0, size - 1);
+    default:
+        return 0;
+    }
+}
+
+/* Border colour table (CPVulkan/ImageSampler.cpp:409-417). */
+void border_colour(uint32_t border, float out[4]) {
+    static const float table[6][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 1}, {0, 0, 0, 1}, {1, 1, 1, 1}, {1, 1, 1, 1}};
+    const uint32_t b = border < 6 ? border : 0;
+    for (int i = 0; i < 4; i++) out[i] = table[b][i];
+}
+
+/* GetPixel<fvec4> for RGBA8 UNORM with the border check
+ * (CPVulkan/ImageSampler.cpp:133-160). */
+void get_texel(const Texture& t, uint32_t level, int32_t x, int32_t y, uint32_t border, float out[4]) {
+    const int32_t w = static_cast<int32_t>(t.level_w[level]);
+    const int32_t h = static_cast<int32_t>(t.level_h[level]);
+    if (x < 0 || x >= w || y < 0 || y >= h) {
+        border_colour(border, out);
+        return;
+    }
+    const uint64_t off = t.level_offset[level] + (static_cast<uint64_t>(y) * static_cast<uint64_t>(w) + static_cast<uint64_t>(x)) * 4u;
+    if (off + 4 > t.bytes) {
+        for (int i = 0; i < 4; i++) out[i] = 0.0f;
+        return;
+    }
+    for (int i = 0; i < 4; i++) out[i] = decode_unorm8(t.data[off + i]);
+}
+
+/* lerp with a double-precision delta (CPVulkan/ImageSampler.cpp:51-55):
+ * dvec4(min) + dvec4(max - min) * delta, converted back to float. */
+void lerp4(const float a[4], const float b[4], double delta, float out[4]) {
+    for (int i = 0; i < 4; i++) {
+        const float diff = b[i] - a[i];
+        const double prod = static_cast<double>(diff) * delta;
+        const double sum = static_cast<double>(a[i]) + prod;
+        out[i] = static_cast<float>(sum);
+    }
+}
+
+/* SampleImageOfLevel for 2D, NEAREST/LINEAR, weighted average
+ * (CPVulkan/ImageSampler.cpp:403-531). */
+void sample_level(const Texture& t, uint32_t level, float u, float v, uint32_t filter, const cpv_scene_sampler& s, float out[4]) {
+    const uint32_t range[2] = {t.level_w[level], t.level_h[level]};
+    const float coord[2] = {u, v};
+    const uint32_t modes[2] = {s.address_u, s.address_v};
+    if (filter == 0) {
+        int32_t c[2];
+        for (int i = 0; i < 2; i++) {
+            const float scaled = coord[i] * static_cast<float>(range[i]) + 0.0f;
+            c[i] = f2i(std::floor(scaled));
+            c[i] = wrap(c[i], static_cast<int32_t>(range[i]), modes[i]);
+        }
+        get_texel(t, level, c[0], c[1], s.border_color, out);
+        return;
+    }
+    int32_t c0[2], c1[2];
+    float frac[2];
+    for (int i = 0; i < 2; i++) {
+        const float scaled = coord[i] * static_cast<float>(range[i]) - 0.5f;
+        const float fl = std::floor(scaled);
+        c0[i] = f2i(fl);
+        c1[i] = wrap(c0[i] + 1, static_cast<int32_t>(range[i]), modes[i]);
+        c0[i] = wrap(c0[i], static_cast<int32_t>(range[i]), modes[i]);
+        frac[i] = scaled - fl;
+    }
+    float t00[4], t01[4], t10[4], t11[4];
+    get_texel(t, level, c0[0], c0[1], s.border_color, t00);
+    get_texel(t, level, c0[0], c1[1], s.border_color, t01);
+    get_texel(t, level, c1[0], c0[1], s.border_color, t10);
+    get_texel(t, level, c1[0], c1[1], s.border_color, t11);
+    float ij0[4], ij1[4];
+    lerp4(t00, t10, static_cast<double>(frac[0]), ij0);
+    lerp4(t01, t11, static_cast<double>(frac[0]), ij1);
+    lerp4(ij0, ij1, static_cast<double>(frac[1]), out);
+}
+
+/* SampleImage (CPVulkan/ImageSampler.cpp:562-673) after the λ computation of
+ * ImageSampleExplicitLod (CPVulkan/GlslFunctions.cpp:598-646). */
+void sample(const Texture& t, const cpv_scene_sampler& s, float u, float v, float lod_base, float out[4]) {
+    const float bias = std::clamp(s.mip_lod_bias + 0.0f, -32.0f, 32.0f);
+    const float lambda_prime = lod_base + bias;
+    const float lambda = std::clamp(lambda_prime, s.min_lod, s.max_lod);
+    if (lambda <= 0) {
+        sample_level(t, 0, u, v, s.mag_filter, s, out);
+    } else {
+        const float max_level = static_cast<float>(t.levels - 1);
+        const float mip = std::clamp(lambda, 0.0f, max_level);
+        if (s.mipmap_mode == 0) {
+            const uint32_t real = static_cast<uint32_t>(std::ceil(mip + 0.5f)) - 1;
+            sample_level(t, real, u, v, s.min_filter, s, out);
+        } else {
+            const uint32_t l1 = static_cast<uint32_t>(std::floor(mip));
+            const float delta = mip - static_cast<float>(l1);
+            float p1[4];
+            sample_level(t, l1, u, v, s.min_filter, s, p1);
+            if (delta == 0) {
+                for (int i = 0; i < 4; i++) out[i] = p1[i];
+            } else {
+                float p2[4];
+                sample_level(t, l1 + 1, u, v, s.min_filter, s, p2);
+                lerp4(p1, p2, static_cast<double>(delta), out);
+            }
+        }
+    }
+    /* RGBA8 carries all four channels: no channel forcing (:652-670). */
+}
+
+/* ---------------------------------------------------------------------- */
+/* Blend (CPVulkan/CommandBuffer.Draw.cpp:956-1262, ApplyBlendFactor and   */
+/* ApplyBlend). The reference never reaches these templates (blendEnable   */
+/* aborts in LLVMRuntime/PipelineCompiler.cpp:1674-1684); they are adopted */
+/* as its blend semantics.                                                 */
+/* ---------------------------------------------------------------------- */
+
+void blend_factor(const float s[4], const float d[4], const float c[4], uint32_t colour_factor, uint32_t alpha_factor, float out[4]) {
+    for (int i = 0; i < 4; i++) out[i] = 0.0f;
+    switch (colour_factor) {
+    case 0: break;
+    case 1: for (int i = 0; i < 4; i++) out[i] = 1.0f; break;
+    case 2: for (int i = 0; i < 4; i++) out[i] = s[i]; break;
+    case 3: for (int i = 0; i < 4; i++) out[i] = 1.0f - s[i]; break;
+    case 4: for (int i = 0; i < 4; i++) out[i] = d[i]; break;
+    case 5: for (int i = 0; i < 4; i++) out[i] = 1.0f - d[i]; break;
+    case 6: for (int i = 0; i < 4; i++) out[i] = s[3]; break;
+    case 7: { const float v = 1 - s[3]; for (int i = 0; i < 4; i++) out[i] = v; break; }
+    case 8: for (int i = 0; i < 4; i++) out[i] = d[3]; break;
+    case 9: { const float v = 1 - d[3]; for (int i = 0; i < 4; i++) out[i] = v; break; }
+    case 10: for (int i = 0; i < 4; i++) out[i] = c[i]; break;
+    case 11: for (int i = 0; i < 4; i++) out[i] = 1.0f - c[i]; break;
+    case 12: for (int i = 0; i < 4; i++) out[i] = c[3]; break;
+    case 13: { const float v = 1 - c[3]; for (int i = 0; i < 4; i++) out[i] = v; break; }
+    case 14: { const float f = fmin_std(s[3], 1 - d[3]); out[0] = f; out[1] = f; out[2] = f; out[3] = 1; break; }
+    default: break;
+    }
+    if (colour_factor != alpha_factor) {
+        switch (alpha_factor) {
+        case 0: out[3] = 0; break;
+        case 1: case 14: out[3] = 1; break;
+        case 2: case 6: out[3] = s[3]; break;
+        case 3: case 7: out[3] = 1 - s[3]; break;
+        case 4: case 8: out[3] = d[3]; break;
+        case 5: case 9: out[3] = 1 - d[3]; break;
+        case 10: case 12: out[3] = c[3]; break;
+        case 11: case 13: out[3] = 1 - c[3]; break;
+        default: break;
+        }
+    }
+}
+
+void blend(const float s[4], const float d[4], const float c[4], uint32_t src_color, uint32_t dst_color, uint32_t color_op,
+           uint32_t src_alpha, uint32_t dst_alpha, uint32_t alpha_op, float out[4]) {
+    float sf[4], df[4];
+    blend_factor(s, d, c, src_color, src_alpha, sf);
+    blend_factor(s, d, c, dst_color, dst_alpha, df);
+    for (int i = 0; i < 4; i++) {
+        const float a = s[i] * sf[i];
+        const float b = d[i] * df[i];
+        switch (color_op) {
+        case 0: out[i] = a + b; break;
+        case 1: out[i] = a - b; break;
+        case 2: out[i] = b - a; break;
+        case 3: out[i] = fmin_std(s[i], d[i]); break;
+        case 4: out[i] = fmax_std(s[i], d[i]); break;
+        default: out[i] = 0; break;
+        }
+    }
+    if (color_op != alpha_op) {
+        const float a = s[3] * sf[3];
+        const float b = d[3] * df[3];
+        switch (alpha_op) {
+        case 0: out[3] = a + b; break;
+        case 1: out[3] = a - b; break;
+        case 2: out[3] = b - a; break;
+        case 3: out[3] = fmin_std(s[3], d[3]); break;
+        case 4: out[3] = fmax_std(s[3], d[3]); break;
+        default: break;
+        }
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+/* Shader programs: C++ restatements of the SPIR-V modules the harness    */
+/* ships (cpvulkan_gb300/shaders/gen_spirv.py), one op per SPIR-V op.     */
+/* ---------------------------------------------------------------------- */
+
+enum Interp { INTERP_PERSPECTIVE = 0, INTERP_LINEAR = 1, INTERP_FLAT = 2 };
+
+struct ProgramInfo {
+    int num_inputs;           /* fragment shader inputs, declaration order */
+    int input_size[4];        /* components per input */
+    Interp input_interp[4];
+};
+
+ProgramInfo program_info(uint32_t program) {
+    switch (program) {
+    case CPV_PROGRAM_CUBE: return {1, {4}, {INTERP_PERSPECTIVE}};
+    case CPV_PROGRAM_TEXLIT: return {2, {2, 3}, {INTERP_PERSPECTIVE, INTERP_PERSPECTIVE}};
+    case CPV_PROGRAM_FLATQUAD: return {1, {4}, {INTERP_FLAT}};
+    case CPV_PROGRAM_MESHPC: return {1, {3}, {INTERP_PERSPECTIVE}};
+    case CPV_PROGRAM_DISCARD: return {1, {4}, {INTERP_PERSPECTIVE}};
+    case CPV_PROGRAM_NOPERSP: return {1, {4}, {INTERP_LINEAR}};
+    default: return {0, {0}, {INTERP_PERSPECTIVE}};
+    }
+}
+
+struct Resources {
+    const float* ubo = nullptr; /* set 0 binding 0 */
+    uint32_t ubo_floats = 0;
+    const Texture* texture = nullptr;
+    const cpv_scene_sampler* sampler = nullptr;
+    const float* push = nullptr; /* 32 floats */
+};
+
+float ubo_at(const Resources& r, uint32_t i) { return i < r.ubo_floats ? r.ubo[i] : 0.0f; }
+
+struct VsOut {
+    float pos[4];
+    float var[kMaxVaryings];
+};
+
+/* attr[location][4] holds each attribute as fetched (missing components
+ * default to 0,0,0,1). */
+void run_vs(uint32_t program, const float attr[8][4], const Resources& r, VsOut& out) {
+    switch (program) {
+    case CPV_PROGRAM_CUBE:
+    case CPV_PROGRAM_DISCARD:
+    case CPV_PROGRAM_NOPERSP: {
+        float m[16];
+        for (int i = 0; i < 16; i++) m[i] = ubo_at(r, i);
+        for (int i = 0; i < 4; i++) out.var[i] = attr[1][i];
+        const V4 p = mat4_mul_vec4(m, attr[0]);
+        out.pos[0] = p.x; out.pos[1] = p.y; out.pos[2] = p.z; out.pos[3] = p.w;
+        break;
+    }
+    case CPV_PROGRAM_TEXLIT: {
+        float m[16];
+        for (int i = 0; i < 16; i++) m[i] = ubo_at(r, i);
+        out.var[0] = attr[1][0]; out.var[1] = attr[1][1];
+        out.var[2] = attr[2][0]; out.var[3] = attr[2][1]; out.var[4] = attr[2][2];
+        const float v[4] = {attr[0][0], attr[0][1], attr[0][2], 1.0f};
+        const V4 p = mat4_mul_vec4(m, v);
+        out.pos[0] = p.x; out.pos[1] = p.y; out.pos[2] = p.z; out.pos[3] = p.w;
+        break;
+    }
+    case CPV_PROGRAM_FLATQUAD: {
+        for (int i = 0; i < 4; i++) out.var[i] = attr[1][i];
+        out.pos[0] = attr[0][0]; out.pos[1] = attr[0][1]; out.pos[2] = 0.0f; out.pos[3] = 1.0f;
+        break;
+    }
+    case CPV_PROGRAM_MESHPC: {
+        out.var[0] = attr[1][0]; out.var[1] = attr[1][1]; out.var[2] = attr[1][2];
+        const float sum[3] = {attr[0][0] + attr[2][0], attr[0][1] + attr[2][1], attr[0][2] + attr[2][2]};
+        const float v[4] = {sum[0], sum[1], sum[2], 1.0f};
+        const V4 p = mat4_mul_vec4(r.push, v);
+        out.pos[0] = p.x; out.pos[1] = p.y; out.pos[2] = p.z; out.pos[3] = p.w;
+        break;
+    }
+    default:
+        for (int i = 0; i < 4; i++) out.pos[i] = 0.0f;
+        break;
+    }
+}
+
+/* Returns true when the fragment is discarded (OpKill → return true,
+ * LLVMRuntime/SPIRVCompiler.cpp:3308-3310, 3642-3651). */
+bool run_fs(uint32_t program, const float* in, const Resources& r, float colour[4]) {
+    switch (program) {
+    case CPV_PROGRAM_CUBE:
+    case CPV_PROGRAM_NOPERSP:
+    case CPV_PROGRAM_FLATQUAD:
+        for (int i = 0; i < 4; i++) colour[i] = in[i];
+        return false;
+    case CPV_PROGRAM_DISCARD:
+        if (in[0] > 0.5f) return true;
+        for (int i = 0; i < 4; i++) colour[i] = in[i];
+        return false;
+    case CPV_PROGRAM_TEXLIT: {
+        float c[4] = {0, 0, 0, 1};
+        if (r.texture && r.sampler) sample(*r.texture, *r.sampler, in[0], in[1], 0.0f, c);
+        float n[3];
+        normalize3(in + 2, n);
+        const float light[3] = {ubo_at(r, 16), ubo_at(r, 17), ubo_at(r, 18)};
+        const float d = dot3(n, light);
+        const float l = fmax_std(d, 0.0f);
+        colour[0] = c[0] * l; colour[1] = c[1] * l; colour[2] = c[2] * l; colour[3] = c[3];
+        return false;
+    }
+    case CPV_PROGRAM_MESHPC: {
+        float n[3];
+        normalize3(in, n);
+        const float light[3] = {0.48f, 0.6f, 0.64f};
+        const float d = dot3(n, light);
+        const float l0 = fmax_std(d, 0.0f);
+        const float l1 = l0 * 0.8f;
+        const float l = l1 + 0.2f;
+        colour[0] = r.push[16] * l; colour[1] = r.push[17] * l; colour[2] = r.push[18] * l; colour[3] = r.push[19];
+        return false;
+    }
+    default:
+        for (int i = 0; i < 4; i++) colour[i] = 0.0f;
+        return false;
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+/* Attachments                                                             */
+/* ---------------------------------------------------------------------- */
+
+uint32_t depth_texel_size(uint32_t fmt) {
+    switch (fmt) {
+    case FMT_D16_UNORM: return 2;
+    case FMT_D32_SFLOAT: return 4;
+    case FMT_D32_SFLOAT_S8_UINT: return 8;
+    default: return 0;
+    }
+}
+
+bool has_stencil(uint32_t fmt) { return fmt == FMT_D32_SFLOAT_S8_UINT; }
+
+/* Depth decode (LLVMRuntime/ImageCompiler.cpp:541-565). */
+float get_depth(const uint8_t* texel, uint32_t fmt) {
+    if (fmt == FMT_D16_UNORM) {
+        uint16_t u;
+        std::memcpy(&u, texel, 2);
+        return decode_unorm16(u);
+    }
+    float f;
+    std::memcpy(&f, texel, 4);
+    return f;
+}
+
+/* Depth/stencil encode (LLVMRuntime/ImageCompiler.cpp:869-947). */
+void set_depth(uint8_t* texel, uint32_t fmt, float d) {
+    if (fmt == FMT_D16_UNORM) {
+        const uint16_t u = static_cast<uint16_t>(encode_unorm(d, 65535.0f));
+        std::memcpy(texel, &u, 2);
+    } else {
+        std::memcpy(texel, &d, 4);
+    }
+}
+
+/* Channel byte offsets (CPVulkanBase/Formats.cpp:248,255). */
+void colour_offsets(uint32_t fmt, int off[4]) {
+    if (fmt == FMT_B8G8R8A8_UNORM) { off[0] = 2; off[1] = 1; off[2] = 0; off[3] = 3; }
+    else { off[0] = 0; off[1] = 1; off[2] = 2; off[3] = 3; }
+}
+
+void set_colour(uint8_t* texel, uint32_t fmt, const float c[4]) {
+    int off[4];
+    colour_offsets(fmt, off);
+    for (int i = 0; i < 4; i++) texel[off[i]] = static_cast<uint8_t>(encode_unorm(c[i], 255.0f));
+}
+
+void get_colour(const uint8_t* texel, uint32_t fmt, float c[4]) {
+    int off[4];
+    colour_offsets(fmt, off);
+    for (int i = 0; i < 4; i++) c[i] = decode_unorm8(texel[off[i]]);
+}
+
+/* Stencil compare / ops (LLVMRuntime/PipelineCompiler.cpp:1194-1223,
+ * 1382-1413, 1492-1526). Increment/decrement-and-clamp use the reference's
+ * *signed* saturating i8 intrinsics. */
+bool icompare(uint32_t a, uint32_t b, uint32_t op) {
+    switch (op) {
+    case 0: return false;
+    case 1: return a < b;
+    case 2: return a == b;
+    case 3: return a <= b;
+    case 4: return a > b;
+    case 5: return a != b;
+    case 6: return a >= b;
+    default: return true;
+    }
+}
+
+bool fcompare(float a, float b, uint32_t op) {
+    switch (op) {
+    case 0: return false;
+    case 1: return a < b;
+    case 2: return a == b;
+    case 3: return a <= b;
+    case 4: return a > b;
+    case 5: return (a < b) || (a > b); /* FCmpONE: ordered and not equal */
+    case 6: return a >= b;
+    default: return true;
+    }
+}
+
+uint8_t stencil_op(uint32_t op, uint8_t current, uint8_t reference) {
+    const int8_t sc = static_cast<int8_t>(current);
+    switch (op) {
+    case 0: return current;
+    case 1: return 0;
+    case 2: return reference;
+    case 3: return static_cast<uint8_t>(sc == 127 ? 127 : sc + 1);
+    case 4: return static_cast<uint8_t>(sc == -128 ? -128 : sc - 1);
+    case 5: return static_cast<uint8_t>(~current);
+    case 6: return static_cast<uint8_t>(current + 1);
+    case 7: return static_cast<uint8_t>(current - 1);
+    default: return current;
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+/* Draw                                                                    */
+/* ---------------------------------------------------------------------- */
+
+struct Frame {
+    const cpv_scene* s;
+    uint8_t* colour;
+    uint8_t* depth;
+    uint32_t depth_size;
+    Resources res;
+    cpv_oracle_stats* stats;
+};
+
+/* Attribute fetch (LLVMRuntime/PipelineCompiler.cpp:821-896): address =
+ * binding base + stride * (vertex or instance id) + attribute offset; float
+ * formats copy straight; components absent from the format read 0,0,0,1.
+ * Reads outside the vertex blob return zeros. */
+void fetch_attributes(const Frame& f, const cpv_scene_pipeline& p, const cpv_scene_draw& d, uint32_t vertex_id, uint32_t instance_id, float attr[8][4]) {
+    for (int l = 0; l < 8; l++) { attr[l][0] = 0; attr[l][1] = 0; attr[l][2] = 0; attr[l][3] = 1; }
+    for (uint32_t a = 0; a < p.num_attributes; a++) {
+        const cpv_scene_attribute& at = p.attributes[a];
+        if (at.location >= 8) continue;
+        uint32_t slot = 0;
+        const cpv_scene_binding* b = nullptr;
+        for (uint32_t i = 0; i < p.num_bindings; i++) {
+            if (p.bindings[i].binding == at.binding) { b = &p.bindings[i]; slot = i; }
+        }
+        if (!b) continue;
+        int comps = 0;
+        switch (at.format) {
+        case FMT_R32_SFLOAT: comps = 1; break;
+        case FMT_R32G32_SFLOAT: comps = 2; break;
+        case FMT_R32G32B32_SFLOAT: comps = 3; break;
+        case FMT_R32G32B32A32_SFLOAT: comps = 4; break;
+        default: comps = 0; break;
+        }
+        const uint64_t index = (b->input_rate == RATE_VERTEX) ? vertex_id : instance_id;
+        const uint64_t off = d.vertex_offsets[slot] + static_cast<uint64_t>(b->stride) * index + at.offset;
+        if (off + static_cast<uint64_t>(comps) * 4u > f.s->vertex_bytes) continue;
+        for (int c = 0; c < comps; c++) std::memcpy(&attr[at.location][c], f.s->vertex_data + off + 4u * c, 4);
+    }
+}
+
+struct Assembled {
+    std::vector<uint32_t> vertex_id;   /* per assembled vertex (rawId order) */
+    std::vector<uint32_t> prims;       /* provoking, v0, v1, v2 per triangle */
+};
+
+/* Input assembly (CPVulkan/CommandBuffer.Draw.cpp:567-760). */
+void assemble(const Frame& f, const cpv_scene_pipeline& p, const cpv_scene_draw& d, Assembled& out) {
+    const uint32_t n = d.count;
+    out.vertex_id.resize(n);
+    if (d.indexed) {
+        const uint32_t isz = f.s->index_type == 0 ? 2 : 4;
+        for (uint32_t i = 0; i < n; i++) {
+            const uint64_t off = d.index_offset + (static_cast<uint64_t>(d.first) + i) * isz;
+            uint32_t index = 0;
+            if (off + isz <= f.s->index_bytes) {
+                if (isz == 2) { uint16_t v; std::memcpy(&v, f.s->index_data + off, 2); index = v; }
+                else std::memcpy(&index, f.s->index_data + off, 4);
+            }
+            out.vertex_id[i] = static_cast<uint32_t>(d.vertex_offset) + index;
+        }
+    } else {
+        for (uint32_t i = 0; i < n; i++) out.vertex_id[i] = d.first + i;
+    }
+    out.prims.clear();
+    if (p.topology == TOPO_TRIANGLE_LIST) {
+        for (uint32_t i = 0; i < n / 3; i++) { out.prims.push_back(i * 3); out.prims.push_back(i * 3); out.prims.push_back(i * 3 + 1); out.prims.push_back(i * 3 + 2); }
+    } else if (p.topology == TOPO_TRIANGLE_STRIP) {
+        for (uint32_t i = 0; i + 2 < n; i++) { out.prims.push_back(i); out.prims.push_back(i); out.prims.push_back(i + 1); out.prims.push_back(i + 2); }
+    } else if (p.topology == TOPO_TRIANGLE_FAN) {
+        for (uint32_t i = 0; i + 2 < n; i++) { out.prims.push_back(i + 1); out.prims.push_back(0); out.prims.push_back(i + 1); out.prims.push_back(i + 2); }
+    }
+}
+
+/* Interpolation (CPVulkan/CommandBuffer.Draw.cpp:816-871). */
+float interp_persp(const float pw[3], const float v[3], const float w[3]) {
+    float num = 0.0f, den = 0.0f;
+    for (int i = 0; i < 3; i++) {
+        const float wv = w[i] * v[i];
+        num = num + wv / pw[i];
+        den = den + w[i] / pw[i];
+    }
+    return num / den;
+}
+
+float interp_linear(const float v[3], const float w[3]) {
+    float r = 0.0f;
+    for (int i = 0; i < 3; i++) r = r + w[i] * v[i];
+    return r;
+}
+
+/* Per-fragment operations (LLVMRuntime/PipelineCompiler.cpp:1020-1429). */
+void fragment(Frame& f, const cpv_scene_pipeline& p, uint32_t x, uint32_t y, float depth_mapped, bool front, const float* inputs) {
+    const cpv_scene* s = f.s;
+    f.stats->fragments++;
+    float colour[4];
+    if (run_fs(p.program, inputs, f.res, colour)) return;
+
+    const uint64_t pix = static_cast<uint64_t>(y) * s->width + x;
+    uint8_t* ds = f.depth ? f.depth + pix * f.depth_size : nullptr;
+    const bool has_depth_att = ds != nullptr;
+
+    float current_depth = 0.0f;
+    if (p.depth_test && has_depth_att) current_depth = get_depth(ds, s->depth_format);
+    uint8_t current_stencil = 0;
+    const bool stencil_on = p.stencil_test && has_depth_att && has_stencil(s->depth_format);
+    if (stencil_on) current_stencil = ds[4];
+
+    bool stencil_result = true;
+    uint8_t stencil_ref = 0;
+    const cpv_scene_stencil& st = front ? p.stencil_front : p.stencil_back;
+    if (stencil_on) {
+        stencil_ref = static_cast<uint8_t>(st.reference);
+        const uint8_t mask = static_cast<uint8_t>(st.compare_mask);
+        stencil_result = icompare(stencil_ref & mask, current_stencil & mask, st.compare_op);
+    }
+    bool depth_result = true;
+    if (p.depth_test && has_depth_att) depth_result = fcompare(depth_mapped, current_depth, p.depth_compare);
+
+    const bool attempt_depth_write = p.depth_test && p.depth_write && has_depth_att;
+    if (stencil_on) {
+        /* CompileStencilWrite (:1382-1470): depth is written when the depth
+         * test passes, independent of the stencil result. */
+        const uint8_t fail = stencil_op(st.fail_op, current_stencil, stencil_ref);
+        const uint8_t dfail = stencil_op(st.depth_fail_op, current_stencil, stencil_ref);
+        const uint8_t pass = stencil_op(st.pass_op, current_stencil, stencil_ref);
+        uint8_t value = stencil_result ? (depth_result ? pass : dfail) : fail;
+        const uint8_t wmask = static_cast<uint8_t>(st.write_mask);
+        value = static_cast<uint8_t>((value & wmask) | (current_stencil & static_cast<uint8_t>(~wmask)));
+        if (depth_result && attempt_depth_write) set_depth(ds, s->depth_format, depth_mapped);
+        ds[4] = value;
+    } else if (attempt_depth_write && depth_result) {
+        set_depth(ds, s->depth_format, depth_mapped);
+    }
+
+    if (stencil_result && depth_result) {
+        uint8_t* texel = f.colour + pix * 4;
+        if (p.blend_enable) {
+            float dst[4], out[4];
+            get_colour(texel, s->color_format, dst);
+            blend(colour, dst, p.blend_constants, p.src_color, p.dst_color, p.color_op, p.src_alpha, p.dst_alpha, p.alpha_op, out);
+            set_colour(texel, s->color_format, out);
+        } else {
+            set_colour(texel, s->color_format, colour);
+        }
+        f.stats->fragments_written++;
+    }
+}
+
+/* ProcessTriangles + GetFragmentInput + DrawPixel
+ * (CPVulkan/CommandBuffer.Draw.cpp:874-954, 1300-1313, 1510-1594). */
+void rasterise(Frame& f, const cpv_scene_pipeline& p, const Assembled& as, const std::vector<VsOut>& vs) {
+    const cpv_scene* s = f.s;
+    const float vw = s->viewport[2], vh = s->viewport[3];
+    const float min_d = s->viewport[4], max_d = s->viewport[5];
+    const float half_x = (1.0f / vw) * 0.5f;
+    const float half_y = (1.0f / vh) * 0.5f;
+    const ProgramInfo info = program_info(p.program);
+    const int32_t iw = f2i(vw), ih = f2i(vh);
+    const int32_t fb_w = static_cast<int32_t>(s->width), fb_h = static_cast<int32_t>(s->height);
+
+    for (size_t t = 0; t + 4 <= as.prims.size(); t += 4) {
+        const uint32_t provoking = as.prims[t];
+        uint32_t i0 = as.prims[t + 1], i1 = as.prims[t + 2], i2 = as.prims[t + 3];
+        if (p.front_face == FRONT_FACE_CW) std::swap(i0, i2);
+        f.stats->triangles++;
+        const VsOut* v[3] = {&vs[i0], &vs[i1], &vs[i2]};
+        float P[3][4];
+        for (int k = 0; k < 3; k++) {
+            const float w = v[k]->pos[3];
+            P[k][0] = v[k]->pos[0] / w;
+            P[k][1] = v[k]->pos[1] / w;
+            P[k][2] = v[k]->pos[2] / w;
+            P[k][3] = w;
+        }
+        int32_t sx[3], sy[3];
+        for (int k = 0; k < 3; k++) {
+            sx[k] = f2i(((P[k][0] + 1.0f) * 0.5f) * vw);
+            sy[k] = f2i(((P[k][1] + 1.0f) * 0.5f) * vh);
+        }
+        const int64_t start_x = std::max<int64_t>(0, std::min({sx[0], sx[1], sx[2]}));
+        const int64_t start_y = std::max<int64_t>(0, std::min({sy[0], sy[1], sy[2]}));
+        int64_t end_x = std::min<int64_t>(iw, static_cast<int64_t>(std::max({sx[0], sx[1], sx[2]})) + 1);
+        int64_t end_y = std::min<int64_t>(ih, static_cast<int64_t>(std::max({sy[0], sy[1], sy[2]})) + 1);
+        /* Pixels outside the attachment are never written (the reference
+         * assumes viewport == framebuffer; this bound keeps the restatement
+         * memory safe). */
+        end_x = std::min<int64_t>(end_x, fb_w);
+        end_y = std::min<int64_t>(end_y, fb_h);
+
+        float area = edge(P[0][0], P[0][1], P[1][0], P[1][1], P[2][0], P[2][1]);
+        bool front;
+        int e[3][2];
+        if (area < 0) {
+            area = -area;
+            front = false;
+            e[0][0] = 2; e[0][1] = 1; e[1][0] = 0; e[1][1] = 2; e[2][0] = 1; e[2][1] = 0;
+        } else {
+            front = true;
+            e[0][0] = 1; e[0][1] = 2; e[1][0] = 2; e[1][1] = 0; e[2][0] = 0; e[2][1] = 1;
+        }
+        if ((p.cull_mode & CULL_BACK) && !front) continue;
+        if ((p.cull_mode & CULL_FRONT) && front) continue;
+
+        for (int64_t y = start_y; y < end_y; y++) {
+            const float yf = (static_cast<float>(y) / vh + half_y) * 2.0f - 1.0f;
+            for (int64_t x = start_x; x < end_x; x++) {
+                const float xf = (static_cast<float>(x) / vw + half_x) * 2.0f - 1.0f;
+                float w[3];
+                for (int k = 0; k < 3; k++) {
+                    const float* a = P[e[k][0]];
+                    const float* b = P[e[k][1]];
+                    w[k] = edge(a[0], a[1], b[0], b[1], xf, yf);
+                }
+                if (w[0] < 0 || w[1] < 0 || w[2] < 0) continue;
+                w[0] = w[0] / area;
+                w[1] = w[1] / area;
+                w[2] = w[2] / area;
+                const float depth = (P[0][2] * w[0] + P[1][2] * w[1]) + P[2][2] * w[2];
+
+                float inputs[kMaxVaryings];
+                int comp = 0;
+                const float pw[3] = {P[0][3], P[1][3], P[2][3]};
+                for (int in = 0; in < info.num_inputs; in++) {
+                    for (int c = 0; c < info.input_size[in]; c++, comp++) {
+                        const float val[3] = {v[0]->var[comp], v[1]->var[comp], v[2]->var[comp]};
+                        switch (info.input_interp[in]) {
+                        case INTERP_PERSPECTIVE: inputs[comp] = interp_persp(pw, val, w); break;
+                        case INTERP_LINEAR: inputs[comp] = interp_linear(val, w); break;
+                        case INTERP_FLAT: inputs[comp] = vs[provoking].var[comp]; break;
+                        }
+                    }
+                }
+                const float mapped = (max_d - min_d) * depth + min_d;
+                fragment(f, p, static_cast<uint32_t>(x), static_cast<uint32_t>(y), mapped, front, inputs);
+            }
+        }
+    }
+}
+
+void draw(Frame& f, const cpv_scene_draw& d) {
+    const cpv_scene* s = f.s;
+    if (d.pipeline >= s->num_pipelines) return;
+    const cpv_scene_pipeline& p = s->pipelines[d.pipeline];
+    float push[32] = {};
+    std::memcpy(push, d.push, std::min<uint32_t>(d.push_size, sizeof(push)));
+    f.res.push = push;
+    Assembled as;
+    std::vector<VsOut> vs;
+    for (uint32_t i = 0; i < d.instance_count; i++) {
+        const uint32_t instance = d.first_instance + i;
+        assemble(f, p, d, as);
+        vs.resize(as.vertex_id.size());
+        for (size_t k = 0; k < as.vertex_id.size(); k++) {
+            float attr[8][4];
+            fetch_attributes(f, p, d, as.vertex_id[k], instance, attr);
+            std::memset(&vs[k], 0, sizeof(VsOut));
+            run_vs(p.program, attr, f.res, vs[k]);
+        }
+        f.stats->vs_invocations += as.vertex_id.size();
+        rasterise(f, p, as, vs);
+    }
+    f.res.push = nullptr;
+}
+
+} // namespace
+
+extern "C" {
+
+int cpv_oracle_render(const cpv_scene* scene, uint8_t* color, uint8_t* depth, uint32_t do_clear, uint32_t draw_begin,
+                      uint32_t draw_end, cpv_oracle_stats* stats) {
+    if (!scene || !color) return -1;
+    if (scene->color_format != FMT_R8G8B8A8_UNORM && scene->color_format != FMT_B8G8R8A8_UNORM) return -2;
+    const uint32_t dsize = depth_texel_size(scene->depth_format);
+    if (scene->depth_format != 0 && (dsize == 0 || !depth)) return -3;
+    cpv_oracle_stats local{};
+    Frame f{};
+    f.s = scene;
+    f.colour = color;
+    f.depth = scene->depth_format ? depth : nullptr;
+    f.depth_size = dsize;
+    f.stats = stats ? stats : &local;
+
+    Texture tex;
+    if (scene->texture_data) {
+        tex.data = scene->texture_data;
+        tex.bytes = scene->texture_bytes;
+        tex.width = scene->texture_width;
+        tex.height = scene->texture_height;
+        tex.levels = std::min<uint32_t>(scene->texture_levels, 16);
+        uint64_t off = 0;
+        uint32_t w = tex.width, h = tex.height;
+        /* GetNormalImageSize (CPVulkanBase/Formats.cpp:453-484). */
+        for (uint32_t l = 0; l < tex.levels; l++) {
+            tex.level_offset[l] = off;
+            tex.level_w[l] = w;
+            tex.level_h[l] = h;
+            off += static_cast<uint64_t>(w) * h * 4u;
+            w = std::max(w / 2, 1u);
+            h = std::max(h / 2, 1u);
+        }
+        f.res.texture = &tex;
+        f.res.sampler = &scene->sampler;
+    }
+    f.res.ubo = reinterpret_cast<const float*>(scene->uniform_data);
+    f.res.ubo_floats = scene->uniform_bytes / 4;
+
+    const uint64_t pixels = static_cast<uint64_t>(scene->width) * scene->height;
+    if (do_clear) {
+        /* BeginRenderPassCommand + ClearImage (CPVulkan/CommandBuffer.cpp:591-646,
+         * CPVulkan/CommandBuffer.Draw.cpp:117-149): every texel goes through the
+         * format encoder. */
+        for (uint64_t i = 0; i < pixels; i++) set_colour(color + i * 4, scene->color_format, scene->clear_color);
+        if (f.depth) {
+            for (uint64_t i = 0; i < pixels; i++) {
+                uint8_t* t = f.depth + i * dsize;
+                set_depth(t, scene->depth_format, scene->clear_depth);
+                if (has_stencil(scene->depth_format)) { t[4] = static_cast<uint8_t>(scene->clear_stencil); t[5] = t[6] = t[7] = 0; }
+            }
+        }
+    }
+    const uint32_t end = std::min(draw_end, scene->num_draws);
+    for (uint32_t i = draw_begin; i < end; i++) draw(f, scene->draws[i]);
+    return 0;
+}
+
+float cpv_oracle_edge(float ax, float ay, float bx, float by, float cx, float cy) { return edge(ax, ay, bx, by, cx, cy); }
+uint8_t cpv_oracle_encode_unorm8(float value) { return static_cast<uint8_t>(encode_unorm(value, 255.0f)); }
+uint16_t cpv_oracle_encode_unorm16(float value) { return static_cast<uint16_t>(encode_unorm(value, 65535.0f)); }
+float cpv_oracle_decode_unorm8(uint8_t value) { return decode_unorm8(value); }
+
+void cpv_oracle_sample(const uint8_t* texels, uint32_t width, uint32_t height, uint32_t levels, const cpv_scene_sampler* sampler,
+                       float u, float v, float lod, float out[4]) {
+    Texture tex;
+    tex.data = texels;
+    tex.width = width;
+    tex.height = height;
+    tex.levels = std::min<uint32_t>(levels, 16);
+    uint64_t off = 0;
+    uint32_t w = width, h = height;
+    for (uint32_t l = 0; l < tex.levels; l++) {
+        tex.level_offset[l] = off;
+        tex.level_w[l] = w;
+        tex.level_h[l] = h;
+        off += static_cast<uint64_t>(w) * h * 4u;
+        w = std::max(w / 2, 1u);
+        h = std::max(h / 2, 1u);
+    }
+    tex.bytes = off;
+    sample(tex, *sampler, u, v, lod, out);
+}
+
+void cpv_oracle_blend(const float src[4], const float dst[4], const float constant[4], uint32_t src_color, uint32_t dst_color,
+                      uint32_t color_op, uint32_t src_alpha, uint32_t dst_alpha, uint32_t alpha_op, float out[4]) {
+    blend(src, dst, constant, src_color, dst_color, color_op, src_alpha, dst_alpha, alpha_op, out);
+}
+
+} // extern "C"

@@ -1,0 +1,66 @@
+/*
+ * oracle.h — CPU oracle for the draw hot path. TEST INFRASTRUCTURE ONLY.
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+ * load this library, and only as the checker / the timed CPU baseline. The
+ * product path (libcpvulkan_gb300.so) never calls it.
+ *
+ * What it is: a single-threaded C++ restatement of the reference ICD's CPU
+ * draw path (CPVulkan/CommandBuffer.Draw.cpp, LLVMRuntime/PipelineCompiler.cpp,
+ * LLVMRuntime/ImageCompiler.cpp, CPVulkan/ImageSampler.cpp,
+ * CPVulkan/GlslFunctions.cpp), operating on the plain-data scene description
+ * in include/cpv/scene.h. Shader programs are hand-written C++ restatements of
+ * the SPIR-V modules the harness ships (one per cpv_program).
+ *
+ * Parity status: the reference itself cannot be built in this image (it needs
+ * LLVM-C 8, the Khronos Vulkan headers, Microsoft GSL and glm >= 0.9.9, none
+ * of which are present) and ships no tests, golden images or fixtures. This
+ * restatement is therefore pinned only by hand-derived known-answer tests
+ * (tests/golden/) built from the cited reference lines: "parity unpinned"
+ * against a reference binary.
+ */
+#ifndef CPV_ORACLE_H
+#define CPV_ORACLE_H
+
+#include <stdint.h>
+
+#include "../include/cpv/scene.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cpv_oracle_stats {
+    uint64_t triangles;        /* assembled triangles (all instances) */
+    uint64_t vs_invocations;   /* vertex shader invocations (one per assembled vertex, as the reference) */
+    uint64_t fragments;        /* covered pixels that ran the fragment shader */
+    uint64_t fragments_written;/* fragments whose colour write happened */
+} cpv_oracle_stats;
+
+/* Renders draws [draw_begin, draw_end) of the scene (clear first when
+ * do_clear != 0). color: width*height*4 bytes; depth: width*height*texel bytes
+ * of depth_format (may be null when depth_format == 0). Both are read as the
+ * initial attachment contents when do_clear == 0. Returns 0 on success,
+ * negative on an unsupported scene. */
+int cpv_oracle_render(const cpv_scene* scene, uint8_t* color, uint8_t* depth, uint32_t do_clear,
+                      uint32_t draw_begin, uint32_t draw_end, cpv_oracle_stats* stats);
+
+/* Single-step helpers exposed for known-answer tests. */
+float cpv_oracle_edge(float ax, float ay, float bx, float by, float cx, float cy);
+uint8_t cpv_oracle_encode_unorm8(float value);
+uint16_t cpv_oracle_encode_unorm16(float value);
+float cpv_oracle_decode_unorm8(uint8_t value);
+/* Bilinear/nearest sample of level 0..levels-1 of an RGBA8 texture with the
+ * reference sampler semantics; out = RGBA float. */
+void cpv_oracle_sample(const uint8_t* texels, uint32_t width, uint32_t height, uint32_t levels,
+                       const cpv_scene_sampler* sampler, float u, float v, float lod, float out[4]);
+/* Blend one colour against a destination with the reference blend equations. */
+void cpv_oracle_blend(const float src[4], const float dst[4], const float constant[4],
+                      uint32_t src_color, uint32_t dst_color, uint32_t color_op,
+                      uint32_t src_alpha, uint32_t dst_alpha, uint32_t alpha_op, float out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,65 @@
+"""ctypes binding of the CPU oracle (oracle/), used only as the checker."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+LIB = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("triangles", ctypes.c_uint64), ("vs_invocations", ctypes.c_uint64), ("fragments", ctypes.c_uint64),
+                ("fragments_written", ctypes.c_uint64)]
+
+
+class SamplerDesc(ctypes.Structure):
+    _fields_ = [("mag_filter", ctypes.c_uint32), ("min_filter", ctypes.c_uint32), ("mipmap_mode", ctypes.c_uint32),
+                ("address_u", ctypes.c_uint32), ("address_v", ctypes.c_uint32), ("address_w", ctypes.c_uint32),
+                ("mip_lod_bias", ctypes.c_float), ("min_lod", ctypes.c_float), ("max_lod", ctypes.c_float),
+                ("border_color", ctypes.c_uint32)]
+
+
+class Oracle:
+    def __init__(self, lib):
+        self.lib = lib
+        f, u32, vp = ctypes.c_float, ctypes.c_uint32, ctypes.c_void_p
+        lib.cpv_oracle_render.restype = ctypes.c_int
+        lib.cpv_oracle_render.argtypes = [vp, vp, vp, u32, u32, u32, ctypes.POINTER(Stats)]
+        lib.cpv_oracle_edge.restype = f
+        lib.cpv_oracle_edge.argtypes = [f] * 6
+        lib.cpv_oracle_encode_unorm8.restype = ctypes.c_uint8
+        lib.cpv_oracle_encode_unorm8.argtypes = [f]
+        lib.cpv_oracle_encode_unorm16.restype = ctypes.c_uint16
+        lib.cpv_oracle_encode_unorm16.argtypes = [f]
+        lib.cpv_oracle_decode_unorm8.restype = f
+        lib.cpv_oracle_decode_unorm8.argtypes = [ctypes.c_uint8]
+        lib.cpv_oracle_sample.argtypes = [vp, u32, u32, u32, ctypes.POINTER(SamplerDesc), f, f, f, ctypes.POINTER(f * 4)]
+        lib.cpv_oracle_blend.argtypes = [ctypes.POINTER(f * 4)] * 3 + [u32] * 6 + [ctypes.POINTER(f * 4)]
+
+    def render(self, scene, draw_begin=0, draw_end=None, color=None, depth=None, clear=True):
+        """Renders a cpvulkan_gb300.Scene; returns (color HxWx4 u8, depth HxWxB u8 or None, stats dict)."""
+        from cpvulkan_gb300 import depth_texel_bytes
+        h, w = scene.height, scene.width
+        dsz = depth_texel_bytes(scene.depth_format)
+        color = np.zeros((h, w, 4), np.uint8) if color is None else color
+        if dsz and depth is None:
+            depth = np.zeros((h, w, dsz), np.uint8)
+        st = Stats()
+        end = 0xFFFFFFFF if draw_end is None else draw_end
+        r = self.lib.cpv_oracle_render(scene.ptr, color.ctypes.data, depth.ctypes.data if dsz else None, 1 if clear else 0,
+                                       draw_begin, end, ctypes.byref(st))
+        if r != 0:
+            raise RuntimeError("oracle rejected the scene (%d)" % r)
+        return color, (depth if dsz else None), {k: getattr(st, k) for k, _ in Stats._fields_}
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", ORACLE_DIR], stdout=subprocess.DEVNULL)
+
+
+def load():
+    build()
+    return Oracle(ctypes.CDLL(LIB))
