@@ -1,0 +1,324 @@
+"""Benchmark of the draw hot path (one JSON line on rank 0).
+
+Default workload: the textured heightfield (1024x1024 grid, 2,093,058
+triangles, 1920x1080 RGBA8 + D32, trilinear texture, Lambert), rendered through
+the Vulkan ICD. A step is one frame: one vkQueueSubmit of the recorded
+command buffer (render-pass clear + the draw) and its fence.
+
+  value  Mtri/s with scene data resident in HBM, device time of K frames
+         (queue events around each frame; a 256 MiB vkCmdFillBuffer before
+         every frame evicts the 129 MB L2 and is not timed).
+  e2e    the same metric through the public API with host buffers: every
+         step maps/copies/unmaps the vertex, index and uniform bytes, copies
+         them to device-local buffers, renders, copies the colour image to a
+         host-visible buffer and reads it back, wall-clock timed.
+
+--impl reference times the reference's CPU draw path (its C++ restatement in
+oracle/) on all host cores on the same scene. --gpus N under torchrun runs N
+independent replicas (the path does not shard a frame).
+"""
+import argparse
+import concurrent.futures as cf
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    # name: (harness config, params, description)
+    "cube": (1, [30], "spinning cube 500x500 BGRA8+D16, 12 triangles, 1 draw"),
+    "heightfield": (2, [], "textured heightfield 1024x1024 grid (2,093,058 tris, u32 indices), 1920x1080 RGBA8+D32, trilinear, Lambert"),
+    "blend": (3, [], "200k screen-space quads (400k tris), sides log-uniform 4-256 px, src-over blend, 1920x1080 RGBA8"),
+    "batch": (4, [], "4096 indexed icosphere draws (12-200k tris, 25% instanced 1-64x), 70/30 opaque/blended, 2560x1440 RGBA8+D32"),
+}
+FLUSH_BYTES = 256 << 20
+FALLBACK_HBM_GBS = 6800.0
+
+
+def algorithmic_bytes(name, scene, frag_written):
+    """Bytes the frame must move at least once (inputs read, attachments written/read)."""
+    w, h = scene.width, scene.height
+    px = w * h
+    if name == "heightfield":
+        verts, idx = 1024 * 1024 * 32, 1023 * 1023 * 6 * 4
+        tex = sum((1024 >> l) ** 2 * 4 for l in range(11))
+        return verts + idx + tex + px * 4 + 2 * px * 4  # colour store + depth read/write
+    if name == "blend":
+        return 8 * frag_written + 800000 * 24 + 1200000 * 4  # RGBA8 read+write per blended fragment + vertices + indices
+    if name == "cube":
+        return 36 * 32 + px * 4 + px * 2 * 2
+    return px * 4 + px * 4 * 2
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def committed_traffic(kernel, workload):
+    """DRAM bytes per launch of `kernel` on `workload` from the committed ncu summary, else None."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as fh:
+            return json.load(fh).get(workload, {}).get(kernel)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if not self.proc:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as fh:
+            for line in fh:
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+        return out
+
+
+def cpu_baseline(scene, seconds, threads=1):
+    """Times the oracle (the reference's CPU draw path restated) on this host."""
+    from tests import oracle_binding
+    oracle = oracle_binding.load()
+    oracle.render(scene)  # warm
+    t0 = time.time()
+    frames = 0
+
+    def one(_):
+        oracle.render(scene)
+        return 1
+
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        while time.time() - t0 < seconds or frames == 0:
+            frames += sum(ex.map(one, range(threads)))
+    dt = time.time() - t0
+    return frames, dt
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if backend == "nccl":
+            import torch
+            torch.cuda.set_device(0)
+        dist.init_process_group(backend)
+    return world, rank, dist
+
+
+def max_over_ranks(dist, value):
+    if dist is None:
+        return value
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def run_reference(args, world, rank, dist):
+    import cpvulkan_gb300 as c
+    c.build()
+    if rank != 0:
+        return
+    cfg, params, desc = CONFIGS[args.config]
+    scene = c.Scene(cfg, 1, params)
+    threads = os.cpu_count() or 1
+    per_step = []
+    for i in range(args.warmup + args.steps):
+        frames, dt = cpu_baseline(scene, 0.0, threads)
+        if i >= args.warmup:
+            per_step.append((frames, dt))
+    frames = sum(f for f, _ in per_step)
+    dt = sum(t for _, t in per_step)
+    value = scene.triangles * frames / dt / 1e6
+    line = {
+        "impl": "reference", "metric": "Mtri/s", "value": round(value, 3), "unit": "Mtri/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000 * dt / len(per_step), 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene)",
+        "config": {"workload": args.config, "description": desc, "triangles": scene.triangles, "frames_per_step": threads},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mtri/s", "cores": threads, "kind": "port",
+                         "sample": "%d whole frames per step, one per host thread" % threads},
+        "e2e": {"value": round(value, 3), "unit": "Mtri/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, dist):
+    import numpy as np
+    import cpvulkan_gb300 as c
+    c.build()
+    if not c.device_available():
+        raise SystemExit("bench.py: no CUDA device — the GB300 path needs a GPU (no CPU fallback exists)")
+    import ctypes
+    icd = ctypes.CDLL(c.ICD_PATH)
+    icd.cpv_kernel_launches.restype = ctypes.c_uint64
+    icd.cpv_profile_get.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_double)]
+    cfg, params, desc = CONFIGS[args.config]
+    scene = c.Scene(cfg, 1, params)
+    tris = scene.triangles
+    ctx = c.Context()
+    t0 = time.time()
+    r = c.Renderer(ctx, scene)
+    create_s = time.time() - t0
+    h = c.harness()
+    h.cpvh_render_timed.restype = ctypes.c_int
+    h.cpvh_render_timed.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)]
+
+    def timed(frames):
+        arr = (ctypes.c_double * frames)()
+        res = h.cpvh_render_timed(r.ptr, frames, FLUSH_BYTES, arr)
+        if res != 0:
+            raise RuntimeError("render failed: %d" % res)
+        return list(arr)
+
+    timed(args.warmup)
+    barrier(dist)
+    clocks = ClockSampler()
+    clocks.start()
+    launches0 = icd.cpv_kernel_launches()
+    frame_ms = timed(args.steps)
+    launches = icd.cpv_kernel_launches() - launches0
+    clock_info = clocks.stop()
+    barrier(dist)
+    total_ms = max_over_ranks(dist, sum(frame_ms))
+    ms_per_step = total_ms / args.steps
+    value = tris * args.steps * world / (total_ms / 1000.0) / 1e6
+    # Gaps between fenced frames removed: launch latency of back-to-back submits.
+    _, lat = r.render(args.steps, latencies=True)
+    # End to end through the API with host buffers.
+    r.render_e2e(2)
+    e2e_ms, h2d, d2h = r.render_e2e(args.steps)
+    e2e_ms = max_over_ranks(dist, e2e_ms)
+    e2e = tris * args.steps * world / (e2e_ms / 1000.0) / 1e6
+    # Per-kernel device time (CUDA events on the queue stream) for the roofline.
+    icd.cpv_profile_reset()
+    icd.cpv_profile_enable(1)
+    timed(args.steps)
+    icd.cpv_profile_enable(0)
+    kernels = {}
+    for k in ("cpv_raster", "cpv_setup_rects", "cpv_span_count", "cpv_scan", "cpv_span_write"):
+        n, ms = ctypes.c_uint64(0), ctypes.c_double(0.0)
+        icd.cpv_profile_get(k.encode(), ctypes.byref(n), ctypes.byref(ms))
+        if n.value:
+            kernels[k] = {"launches": n.value, "ms_per_launch": round(ms.value / n.value, 4)}
+    color, depth = r.readback()
+    r.close()
+    line = None
+    if rank == 0:
+        from tests import oracle_binding
+        oracle = oracle_binding.load()
+        _, _, st = oracle.render(scene)
+        frames_cpu, dt_cpu = cpu_baseline(scene, args.cpu_seconds, 1)
+        cpu_value = tris * frames_cpu / dt_cpu / 1e6
+        peak, peak_kind = measured_peak()
+        dom = "cpv_raster"
+        alg = algorithmic_bytes(args.config, scene, st["fragments_written"])
+        achieved = alg / (kernels[dom]["ms_per_launch"] / 1000.0) / 1e9 if dom in kernels else None
+        traffic = committed_traffic(dom, args.config)
+        line = {
+            "metric": "Mtri/s", "value": round(value, 3), "unit": "Mtri/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator, same bytes as the CPU oracle)",
+            "config": {"workload": args.config, "description": desc, "triangles": tris, "mode": "plain per-draw",
+                       "l2": "256 MiB fill between frames (untimed)", "pipeline_create_s": round(create_s, 3)},
+            "gfrag_s": round(st["fragments"] * args.steps * world / (total_ms / 1000.0) / 1e9, 4),
+            "frames_s": round(1000.0 * world / ms_per_step, 2),
+            "submit_to_fence_ms": {"p50": round(float(np.percentile(lat, 50)), 4), "p99": round(float(np.percentile(lat, 99)), 4)},
+            "e2e": {"value": round(e2e, 3), "unit": "Mtri/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": round(e2e_ms / args.steps, 3)},
+            "gpu_launches": int(launches),
+            "kernels": kernels,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": alg},
+            "cpu_baseline": {"value": round(cpu_value, 4), "unit": "Mtri/s", "cores": 1, "kind": "port",
+                             "sample": "%d whole frame(s) in %.1f s, single thread" % (frames_cpu, dt_cpu)},
+            "clocks": clock_info,
+            "image_checksum": int(np.asarray(color, dtype=np.uint64).sum() % (1 << 61)),
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", choices=sorted(CONFIGS), default="heightfield")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, dist = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank, dist)
+    else:
+        run_ours(args, world, rank, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -30,8 +30,8 @@ VK_SUCCESS = 0
 
 def build():
     """Compiles the native libraries (nvcc/g++, sm_103a) if sources changed."""
-    from . import build as _b
-    return _b.build()
+    from . import native_build
+    return native_build.build()
 
 
 class SceneHeader(ctypes.Structure):

@@ -888,6 +888,50 @@ int cpvh_render(cpvh_renderer* r, uint32_t frames, double* device_ms, double* la
     return VK_SUCCESS;
 }
 
+int cpvh_render_timed(cpvh_renderer* r, uint32_t frames, uint64_t flush_bytes, double* frame_ms) {
+    cpvh_context* c = r->ctx;
+    if (!c->record || !c->elapsed) return VK_ERROR_FEATURE_NOT_PRESENT;
+    BufferAlloc flush;
+    VkCommandBuffer flush_cmd = nullptr;
+    if (flush_bytes) {
+        if (make_buffer(c, flush_bytes, VK_BUFFER_USAGE_TRANSFER_DST_BIT, false, flush) != VK_SUCCESS) return VK_ERROR_OUT_OF_DEVICE_MEMORY;
+        VkCommandBufferAllocateInfo cai{};
+        cai.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_ALLOCATE_INFO;
+        cai.commandPool = r->cmd_pool;
+        cai.level = VK_COMMAND_BUFFER_LEVEL_PRIMARY;
+        cai.commandBufferCount = 1;
+        c->f.vkAllocateCommandBuffers(c->device, &cai, &flush_cmd);
+        auto fill = reinterpret_cast<PFN_vkCmdFillBuffer>(c->f.vkGetDeviceProcAddr(c->device, "vkCmdFillBuffer"));
+        VkCommandBufferBeginInfo bi{};
+        bi.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_BEGIN_INFO;
+        c->f.vkBeginCommandBuffer(flush_cmd, &bi);
+        fill(flush_cmd, flush.buffer, 0, VK_WHOLE_SIZE, 0x5A5A5A5Au);
+        c->f.vkEndCommandBuffer(flush_cmd);
+    }
+    VkSubmitInfo si{};
+    si.sType = VK_STRUCTURE_TYPE_SUBMIT_INFO;
+    si.commandBufferCount = 1;
+    VkResult res = VK_SUCCESS;
+    for (uint32_t i = 0; i < frames && res == VK_SUCCESS; i++) {
+        if (flush_cmd) {
+            si.pCommandBuffers = &flush_cmd;
+            res = c->f.vkQueueSubmit(c->queue, 1, &si, nullptr);
+            if (res != VK_SUCCESS) break;
+        }
+        c->record(c->queue, 2);
+        si.pCommandBuffers = &r->frame_cmd;
+        res = c->f.vkQueueSubmit(c->queue, 1, &si, r->fence);
+        if (res != VK_SUCCESS) break;
+        c->record(c->queue, 3);
+        res = c->f.vkWaitForFences(c->device, 1, &r->fence, VK_TRUE, ~0ull);
+        c->f.vkResetFences(c->device, 1, &r->fence);
+        if (frame_ms) frame_ms[i] = c->elapsed(c->queue, 2, 3);
+    }
+    c->f.vkDeviceWaitIdle(c->device);
+    destroy_buffer(c, flush);
+    return res;
+}
+
 int cpvh_render_e2e(cpvh_renderer* r, uint32_t frames, double* total_ms, uint64_t* h2d, uint64_t* d2h) {
     cpvh_context* c = r->ctx;
     const cpv_scene* s = r->scene;

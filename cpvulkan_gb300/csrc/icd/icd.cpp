@@ -1184,6 +1184,12 @@ CPV_EXPORT double cpv_queue_elapsed_ms(VkQueue queue, uint32_t a, uint32_t b) {
     return ms;
 }
 
+CPV_EXPORT void cpv_profile_enable(int on) { cpv::rt::profile_enable(on != 0); }
+
+CPV_EXPORT int cpv_profile_get(const char* kernel, uint64_t* launches, double* total_ms) { return cpv::rt::profile_get(kernel, launches, total_ms); }
+
+CPV_EXPORT void cpv_profile_reset(void) { cpv::rt::profile_reset(); }
+
 CPV_EXPORT int cpv_device_available(void) {
     std::string err;
     return cpv::rt::init(err) == cpv::rt::kOk ? 1 : 0;

@@ -56,14 +56,17 @@ __device__ __forceinline__ float cpv_edge(float ax, float ay, float bx, float by
 
 /* Bounds-checked reads of application memory. Out-of-range reads return
  * zero (the oracle defines the same), so no input can make a kernel read
- * outside the buffers it was given. */
+ * outside the buffers it was given. Plain (generic) loads: the same helpers
+ * read push constants, which live in the kernel's parameter block, not in
+ * global memory, so the global-only read-only path (ld.global.nc) must not
+ * be used here. */
 __device__ __forceinline__ float cpv_ld_f32(const uint8_t* base, uint64_t bytes, uint64_t off) {
     if (base == nullptr || off + 4u > bytes) return 0.0f;
-    return __ldg(reinterpret_cast<const float*>(base + off));
+    return *reinterpret_cast<const float*>(base + off);
 }
 __device__ __forceinline__ uint32_t cpv_ld_u32(const uint8_t* base, uint64_t bytes, uint64_t off) {
     if (base == nullptr || off + 4u > bytes) return 0u;
-    return __ldg(reinterpret_cast<const uint32_t*>(base + off));
+    return *reinterpret_cast<const uint32_t*>(base + off);
 }
 __device__ __forceinline__ int32_t cpv_ld_i32(const uint8_t* base, uint64_t bytes, uint64_t off) {
     return static_cast<int32_t>(cpv_ld_u32(base, bytes, off));

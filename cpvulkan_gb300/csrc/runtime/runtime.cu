@@ -63,6 +63,98 @@ void set_last_error(const std::string& e) { g_last_error = e; }
 uint64_t launches() { return g_launches.load(); }
 void count_launch(uint64_t n) { g_launches += n; }
 
+namespace {
+struct ProfileRecord {
+    std::string name;
+    cudaEvent_t start = nullptr, end = nullptr;
+};
+std::mutex g_prof_mutex;
+bool g_prof_on = false;
+std::vector<ProfileRecord> g_prof_records;
+std::vector<cudaEvent_t> g_prof_free;
+struct ProfileTotal {
+    uint64_t count = 0;
+    double ms = 0.0;
+};
+std::vector<std::pair<std::string, ProfileTotal>> g_prof_totals;
+
+cudaEvent_t prof_event() {
+    if (!g_prof_free.empty()) {
+        cudaEvent_t e = g_prof_free.back();
+        g_prof_free.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void prof_drain() {
+    for (auto& r : g_prof_records) {
+        if (!r.end) continue;
+        cudaEventSynchronize(r.end);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, r.start, r.end);
+        bool found = false;
+        for (auto& t : g_prof_totals)
+            if (t.first == r.name) {
+                t.second.count++;
+                t.second.ms += ms;
+                found = true;
+            }
+        if (!found) g_prof_totals.push_back({r.name, ProfileTotal{1, ms}});
+        g_prof_free.push_back(r.start);
+        g_prof_free.push_back(r.end);
+    }
+    g_prof_records.clear();
+}
+}  // namespace
+
+void profile_enable(bool on) {
+    std::lock_guard<std::mutex> lock(g_prof_mutex);
+    g_prof_on = on;
+}
+bool profile_enabled() { return g_prof_on; }
+
+void profile_begin(cudaStream_t s, const char* name) {
+    if (!g_prof_on) return;
+    std::lock_guard<std::mutex> lock(g_prof_mutex);
+    ProfileRecord r;
+    r.name = name;
+    r.start = prof_event();
+    cudaEventRecord(r.start, s);
+    g_prof_records.push_back(r);
+}
+
+void profile_end(cudaStream_t s) {
+    if (!g_prof_on) return;
+    std::lock_guard<std::mutex> lock(g_prof_mutex);
+    if (g_prof_records.empty() || g_prof_records.back().end) return;
+    g_prof_records.back().end = prof_event();
+    cudaEventRecord(g_prof_records.back().end, s);
+    if (g_prof_records.size() > 4096) prof_drain();
+}
+
+int profile_get(const char* name, uint64_t* count, double* ms) {
+    std::lock_guard<std::mutex> lock(g_prof_mutex);
+    prof_drain();
+    for (auto& t : g_prof_totals)
+        if (t.first == name) {
+            *count = t.second.count;
+            *ms = t.second.ms;
+            return kOk;
+        }
+    *count = 0;
+    *ms = 0.0;
+    return kOk;
+}
+
+void profile_reset() {
+    std::lock_guard<std::mutex> lock(g_prof_mutex);
+    prof_drain();
+    g_prof_totals.clear();
+}
+
 int init(std::string& error) {
     std::lock_guard<std::mutex> lock(g_init_mutex);
     if (g_initialised) {
@@ -287,20 +379,30 @@ int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& s
         CPV_CUDA(cudaMemsetAsync(sc.counts(), 0, bins * sizeof(uint32_t), stream));
         {
             void* args[] = {&P};
+            profile_begin(stream, "cpv_setup_rects");
             CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.setup_rects), dim3(static_cast<unsigned>((G + 255) / 256)), dim3(256), args, 0, stream));
+            profile_end(stream);
             count_launch();
         }
         const unsigned warp_blocks = static_cast<unsigned>((spans * 32 + 255) / 256);
+        profile_begin(stream, "cpv_span_count");
         cpv_span_count<<<warp_blocks, 256, 0, stream>>>(sc.rects(), G, static_cast<uint32_t>(spans), P.tiles_x, sc.counts());
+        profile_end(stream);
         count_launch();
+        profile_begin(stream, "cpv_scan");
         if ((r = scan_u32(stream, sc.counts(), sc.cursor(), bins, sc.words(), sc)) != kOk) return r;
+        profile_end(stream);
+        profile_begin(stream, "cpv_span_write");
         cpv_span_write<<<warp_blocks, 256, 0, stream>>>(sc.rects(), G, static_cast<uint32_t>(spans), P.tiles_x, sc.cursor(), sc.list(),
                                                         sc.list_capacity(), sc.words());
+        profile_end(stream);
         count_launch();
     }
     {
         void* args[] = {&P, &direct};
+        profile_begin(stream, "cpv_raster");
         CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.raster), dim3(static_cast<unsigned>(tiles)), dim3(m.raster_threads), args, 0, stream));
+        profile_end(stream);
         count_launch();
     }
     return kOk;

@@ -87,6 +87,16 @@ private:
 uint64_t launches();
 void count_launch(uint64_t n = 1);
 
+// Optional per-kernel device timing: when enabled, every kernel of the draw
+// path is bracketed by CUDA events on its launching stream; totals are
+// summed (after synchronising) per kernel name.
+void profile_enable(bool on);
+bool profile_enabled();
+void profile_begin(cudaStream_t s, const char* name);
+void profile_end(cudaStream_t s);
+int profile_get(const char* name, uint64_t* count, double* ms);
+void profile_reset();
+
 // Plain per-draw path: the full kernel sequence of one draw on `stream`.
 // `P` must have geometry, resources and attachments filled; tiling and
 // binning fields are filled here.

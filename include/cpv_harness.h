@@ -57,6 +57,11 @@ void cpvh_renderer_destroy(cpvh_renderer* r);
  * Returns a VkResult. */
 int cpvh_render(cpvh_renderer* r, uint32_t frames, double* device_ms, double* latency_ms);
 
+/* Device-timed frames: before each frame, a vkCmdFillBuffer over
+ * `flush_bytes` of scratch memory evicts the L2 (untimed); the frame itself
+ * is bracketed by queue events. frame_ms receives `frames` device times. */
+int cpvh_render_timed(cpvh_renderer* r, uint32_t frames, uint64_t flush_bytes, double* frame_ms);
+
 /* End-to-end frame through the public API: uploads the scene's vertex,
  * index and uniform bytes from host memory (map/copy/unmap + vkCmdCopyBuffer),
  * renders, copies the colour attachment to a host-visible buffer and reads
