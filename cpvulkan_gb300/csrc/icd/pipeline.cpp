@@ -168,7 +168,14 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     const uint32_t tile_shift = tile_shift_for_pipeline();
     std::ostringstream src;
     src << "// " << kTranslationVersion << "\n";
+    src << "#define CPV_PIPELINE_MODULE 1\n";
     src << "#define CPV_TILE_SHIFT " << tile_shift << "\n";
+    // Fragment schedule: deferred (dense shading) when the fragment shader
+    // samples images or is long; immediate otherwise. CPV_DEFERRED=0/1
+    // overrides (used by the autotuner and tests).
+    bool deferred = fr.samples > 0 || fr.instructions > 48;
+    if (const char* d = std::getenv("CPV_DEFERRED")) deferred = d[0] == '1';
+    src << "#define CPV_DEFERRED " << (deferred ? 1 : 0) << "\n";
     src << "#define CPV_NV " << nv << "\n";
     src << "#define CPV_TOPOLOGY " << static_cast<uint32_t>(topo) << "\n";
     src << "#define CPV_CULL_MODE " << rs.cullMode << "\n";
@@ -210,6 +217,10 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     auto p = std::make_unique<Pipeline>();
     p->source = src.str();
     p->key = sha3_256(p->source.data(), p->source.size());
+    if (const char* dump = std::getenv("CPV_DUMP_DIR")) {
+        std::ofstream f(std::string(dump) + "/pipeline_" + hex(p->key).substr(0, 12) + ".cu");
+        f << p->source;
+    }
     p->slots = slots;
     p->topology = topo;
     p->viewport = viewport;

@@ -47,6 +47,19 @@ __device__ __forceinline__ uint32_t cpv_encode_unorm(float x, float maxv) {
 __device__ __forceinline__ float cpv_decode_unorm8(uint32_t u) { return __fdiv_rn(__uint2float_rn(u), 255.0f); }
 __device__ __forceinline__ float cpv_decode_unorm16(uint32_t u) { return __fdiv_rn(__uint2float_rn(u), 65535.0f); }
 
+/* In pipeline modules the 256 UNORM8 decodes are a table in shared memory,
+ * filled with exactly cpv_decode_unorm8(0..255) by each kernel before use:
+ * one shared-memory read instead of an IEEE divide per channel. */
+#ifdef CPV_PIPELINE_MODULE
+__shared__ float cpv_lut8[256];
+#define CPV_DECODE8(u) cpv_lut8[(u)]
+__device__ __forceinline__ void cpv_lut8_init() {
+    for (uint32_t i = threadIdx.x; i < 256u; i += blockDim.x) cpv_lut8[i] = cpv_decode_unorm8(i);
+}
+#else
+#define CPV_DECODE8(u) cpv_decode_unorm8(u)
+#endif
+
 /* EdgeFunction (CPVulkan/CommandBuffer.Draw.cpp:410-418). */
 __device__ __forceinline__ float cpv_edge(float ax, float ay, float bx, float by, float cx, float cy) {
     const float t0 = __fmul_rn(__fsub_rn(cx, ax), __fsub_rn(by, ay));
@@ -260,15 +273,18 @@ __device__ __forceinline__ void cpv_texel(const CpvTexture& t, uint32_t level, i
     }
     const uint32_t px = __ldg(reinterpret_cast<const uint32_t*>(t.data + off));
 #pragma unroll
-    for (int i = 0; i < 4; i++) out[i] = cpv_decode_unorm8((px >> (8 * i)) & 0xFFu);
+    for (int i = 0; i < 4; i++) out[i] = CPV_DECODE8((px >> (8 * i)) & 0xFFu);
 }
 
-/* lerp with a double-precision delta (CPVulkan/ImageSampler.cpp:51-55). */
+/* lerp with a double-precision delta (CPVulkan/ImageSampler.cpp:51-55):
+ * float(double(a) + double(b - a) * delta). The product of two binary32
+ * values is exact in binary64 (48 significant bits), so the reference's
+ * multiply-then-add equals one binary64 fused multiply-add. */
 __device__ __forceinline__ void cpv_lerp4(const float a[4], const float b[4], double delta, float out[4]) {
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         const float diff = __fsub_rn(b[i], a[i]);
-        const double sum = __dadd_rn(static_cast<double>(a[i]), __dmul_rn(static_cast<double>(diff), delta));
+        const double sum = __fma_rn(static_cast<double>(diff), delta, static_cast<double>(a[i]));
         out[i] = __double2float_rn(sum);
     }
 }

@@ -21,6 +21,19 @@
  *                     colour/depth/stencil held in registers, and writes the
  *                     tile back once.
  *
+ * Two fragment schedules, chosen per pipeline (CPV_DEFERRED):
+ *   immediate — each pixel's thread shades its covered fragments as it finds
+ *               them (cheap shaders, large primitives);
+ *   deferred  — per batch of primitives, threads first record up to
+ *               CPV_SLOTS covered fragments each, the CTA then shades all
+ *               recorded fragments densely (full warps, whatever the
+ *               coverage pattern), and finally every pixel's thread applies
+ *               its own fragments' per-fragment operations in primitive
+ *               order. Used when the fragment shader is expensive and
+ *               primitives are small (sampling, many varyings).
+ * Both apply each pixel's fragments in API primitive order, as the
+ * reference's serial loop does.
+ *
  * Vertex shading is recomputed where it is needed (set-up and raster) instead
  * of being stored: a vertex shader is a pure function of its inputs, and the
  * reference itself shades every assembled vertex (one per index), so the
@@ -33,39 +46,47 @@
 #ifndef CPV_TILE_SHIFT
 #define CPV_TILE_SHIFT 4
 #endif
+#ifndef CPV_DEFERRED
+#define CPV_DEFERRED 0
+#endif
 #define CPV_TILE (1 << CPV_TILE_SHIFT)
 #define CPV_RT_THREADS ((CPV_TILE * CPV_TILE) < 256 ? (CPV_TILE * CPV_TILE) : 256)
 #define CPV_PPT ((CPV_TILE * CPV_TILE) / CPV_RT_THREADS)
 #define CPV_ROWS_PER_PASS (CPV_RT_THREADS / CPV_TILE)
 #define CPV_BATCH 128
 #define CPV_NV_ALLOC (CPV_NV > 0 ? CPV_NV : 1)
+#define CPV_NV_PAD ((CPV_NV_ALLOC + 3) & ~3)
+#define CPV_SLOTS 4
+#define CPV_NSLOT (CPV_RT_THREADS * CPV_SLOTS)
 
 /* One primitive after set-up, in the reference's terms
- * (CPVulkan/CommandBuffer.Draw.cpp:1510-1594, 874-954). */
-struct CpvTri {
-    float ax[3], ay[3];   /* start vertex of edge k (NDC) */
-    float dx[3], dy[3];   /* b - a of edge k */
-    float z[3], w[3];     /* NDC z and clip w of p0..p2 (after the CW swap) */
-    float area;           /* |EdgeFunction(p0, p1, p2)| */
-    int32_t x0, y0, x1, y1; /* pixel bounding box, end exclusive */
-    uint32_t flags;       /* 1 live, 2 front facing */
-    uint32_t pslot;       /* which of p0..p2 is the provoking vertex */
-    float var[3][CPV_NV_ALLOC];
+ * (CPVulkan/CommandBuffer.Draw.cpp:1510-1594, 874-954). 16-byte aligned
+ * groups so that the coverage loop reads them with 128-bit loads. */
+struct __align__(16) CpvTri {
+    float4 e[3];     /* edge k: start vertex (x, y) and b - a (dx, dy), NDC */
+    int4 box;        /* pixel bounding box x0, y0, x1, y1 (end exclusive) */
+    float4 za;       /* NDC z of p0..p2 (after the CW swap), |area| */
+    float4 wf;       /* clip w of p0..p2, flags (bits: 1 live, 2 front, pslot << 8) */
+    float var[3][CPV_NV_PAD];
 };
+
+__device__ __forceinline__ uint32_t cpv_tri_flags(const CpvTri& t) { return __float_as_uint(t.wf.w); }
 
 /* Primitive set-up: vertex shading of the three vertices, perspective divide,
  * screen bounding box, area, facing and cull. */
 template <bool WITH_VARYINGS>
 __device__ __forceinline__ void cpv_setup(const CpvDrawParams& P, uint64_t g, CpvTri& t) {
     const uint32_t ppi = P.prims_per_instance;
-    const uint32_t instance = P.first_instance + static_cast<uint32_t>(g / ppi);
-    const uint32_t p = static_cast<uint32_t>(g % ppi);
+    const uint32_t g32 = static_cast<uint32_t>(g);  /* draws hold < 2^32 primitives */
+    const uint32_t inst = P.instance_count > 1u ? g32 / ppi : 0u;
+    const uint32_t instance = P.first_instance + inst;
+    const uint32_t p = g32 - inst * ppi;
     uint32_t raw[3], provoking;
     cpv_prim_vertices(CPV_TOPOLOGY, p, raw, provoking);
 #if CPV_FRONT_CW
     { const uint32_t tmp = raw[0]; raw[0] = raw[2]; raw[2] = tmp; }
 #endif
-    t.pslot = raw[0] == provoking ? 0u : (raw[1] == provoking ? 1u : 2u);
+    const uint32_t pslot = raw[0] == provoking ? 0u : (raw[1] == provoking ? 1u : 2u);
     float Pn[3][4];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -100,36 +121,34 @@ __device__ __forceinline__ void cpv_setup(const CpvDrawParams& P, uint64_t g, Cp
     y1 = y1 < ih ? y1 : ih;
     x1 = x1 < static_cast<int64_t>(P.fb_width) ? x1 : static_cast<int64_t>(P.fb_width);
     y1 = y1 < static_cast<int64_t>(P.fb_height) ? y1 : static_cast<int64_t>(P.fb_height);
-    t.x0 = static_cast<int32_t>(x0);
-    t.y0 = static_cast<int32_t>(y0);
-    t.x1 = static_cast<int32_t>(x1 > x0 ? x1 : x0);
-    t.y1 = static_cast<int32_t>(y1 > y0 ? y1 : y0);
+    int4 box;
+    box.x = static_cast<int32_t>(x0);
+    box.y = static_cast<int32_t>(y0);
+    box.z = static_cast<int32_t>(x1 > x0 ? x1 : x0);
+    box.w = static_cast<int32_t>(y1 > y0 ? y1 : y0);
+    t.box = box;
 
     float area = cpv_edge(Pn[0][0], Pn[0][1], Pn[1][0], Pn[1][1], Pn[2][0], Pn[2][1]);
-    bool front;
-    int ea[3], eb[3];
-    if (area < 0.0f) {
-        area = -area;
-        front = false;
-        ea[0] = 2; eb[0] = 1; ea[1] = 0; eb[1] = 2; ea[2] = 1; eb[2] = 0;
-    } else {
-        front = true;
-        ea[0] = 1; eb[0] = 2; ea[1] = 2; eb[1] = 0; ea[2] = 0; eb[2] = 1;
-    }
-    t.area = area;
+    /* Edges (a → b): front (area >= 0) w0 = E(p1,p2), w1 = E(p2,p0), w2 = E(p0,p1);
+     * back: w0 = E(p2,p1), w1 = E(p0,p2), w2 = E(p1,p0) (Draw.cpp:882-898).
+     * Selected with constant indices so the vertices stay in registers. */
+    const bool front = !(area < 0.0f);
+    if (!front) area = -area;
+    const int fa[3] = {1, 2, 0}, fb[3] = {2, 0, 1};
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        t.ax[k] = Pn[ea[k]][0];
-        t.ay[k] = Pn[ea[k]][1];
-        t.dx[k] = __fsub_rn(Pn[eb[k]][0], Pn[ea[k]][0]);
-        t.dy[k] = __fsub_rn(Pn[eb[k]][1], Pn[ea[k]][1]);
-        t.z[k] = Pn[k][2];
-        t.w[k] = Pn[k][3];
+        const float ax = front ? Pn[fa[k]][0] : Pn[fb[k]][0];
+        const float ay = front ? Pn[fa[k]][1] : Pn[fb[k]][1];
+        const float bx = front ? Pn[fb[k]][0] : Pn[fa[k]][0];
+        const float by = front ? Pn[fb[k]][1] : Pn[fa[k]][1];
+        t.e[k] = make_float4(ax, ay, __fsub_rn(bx, ax), __fsub_rn(by, ay));
     }
-    bool live = t.x1 > t.x0 && t.y1 > t.y0;
+    t.za = make_float4(Pn[0][2], Pn[1][2], Pn[2][2], area);
+    bool live = box.z > box.x && box.w > box.y;
     if ((CPV_CULL_MODE & 2) && !front) live = false;
     if ((CPV_CULL_MODE & 1) && front) live = false;
-    t.flags = (live ? 1u : 0u) | (front ? 2u : 0u);
+    const uint32_t flags = (live ? 1u : 0u) | (front ? 2u : 0u) | (pslot << 8);
+    t.wf = make_float4(Pn[0][3], Pn[1][3], Pn[2][3], __uint_as_float(flags));
 }
 
 /* Pixel centre in NDC (CPVulkan/CommandBuffer.Draw.cpp:1524, 1573-1580):
@@ -139,11 +158,15 @@ __device__ __forceinline__ float cpv_pixel_ndc(int32_t x, float extent) {
     return __fsub_rn(__fmul_rn(__fadd_rn(__fdiv_rn(static_cast<float>(x), extent), half), 2.0f), 1.0f);
 }
 
+/* Edge functions at a pixel centre (CPVulkan/CommandBuffer.Draw.cpp:882-902):
+ * w_k = (p.x - a.x) * (b.y - a.y) - (p.y - a.y) * (b.x - a.x); covered when
+ * no w_k is negative (inclusive on every edge). */
 __device__ __forceinline__ bool cpv_covers(const CpvTri& t, float xf, float yf, float w[3]) {
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        const float t0 = __fmul_rn(__fsub_rn(xf, t.ax[k]), t.dy[k]);
-        const float t1 = __fmul_rn(__fsub_rn(yf, t.ay[k]), t.dx[k]);
+        const float4 e = t.e[k];
+        const float t0 = __fmul_rn(__fsub_rn(xf, e.x), e.w);
+        const float t1 = __fmul_rn(__fsub_rn(yf, e.y), e.z);
         w[k] = __fsub_rn(t0, t1);
     }
     return !(w[0] < 0.0f || w[1] < 0.0f || w[2] < 0.0f);
@@ -153,34 +176,37 @@ __device__ __forceinline__ bool cpv_covers(const CpvTri& t, float xf, float yf, 
  * screen, or when a bounding box of at most four pixels covers none of its
  * pixel centres — the raster would find no fragment there either). */
 extern "C" __global__ void __launch_bounds__(256) cpv_setup_rects(CpvDrawParams P) {
+    cpv_lut8_init();
+    __syncthreads();
     const uint64_t g = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (g >= P.total_prims) return;
     CpvTri t;
     cpv_setup<false>(P, g, t);
-    uint16_t r[4] = {0, 0, 0, 0};
-    if (t.flags & 1u) {
+    uint32_t r[4] = {0, 0, 0, 0};
+    if (cpv_tri_flags(t) & 1u) {
         bool any = true;
-        if ((t.x1 - t.x0) * (t.y1 - t.y0) <= 4) {
+        const int4 b = t.box;
+        if ((b.z - b.x) * (b.w - b.y) <= 4) {
             any = false;
             const float vw = P.viewport[2], vh = P.viewport[3];
-            for (int32_t y = t.y0; y < t.y1; y++) {
+            for (int32_t y = b.y; y < b.w; y++) {
                 const float yf = cpv_pixel_ndc(y, vh);
-                for (int32_t x = t.x0; x < t.x1; x++) {
+                for (int32_t x = b.x; x < b.z; x++) {
                     float w[3];
                     if (cpv_covers(t, cpv_pixel_ndc(x, vw), yf, w)) any = true;
                 }
             }
         }
         if (any) {
-            r[0] = static_cast<uint16_t>(t.x0 >> CPV_TILE_SHIFT);
-            r[1] = static_cast<uint16_t>(t.y0 >> CPV_TILE_SHIFT);
-            r[2] = static_cast<uint16_t>(((t.x1 - 1) >> CPV_TILE_SHIFT) + 1);
-            r[3] = static_cast<uint16_t>(((t.y1 - 1) >> CPV_TILE_SHIFT) + 1);
+            r[0] = static_cast<uint32_t>(b.x >> CPV_TILE_SHIFT);
+            r[1] = static_cast<uint32_t>(b.y >> CPV_TILE_SHIFT);
+            r[2] = static_cast<uint32_t>(((b.z - 1) >> CPV_TILE_SHIFT) + 1);
+            r[3] = static_cast<uint32_t>(((b.w - 1) >> CPV_TILE_SHIFT) + 1);
         }
     }
     uint2 packed;
-    packed.x = static_cast<uint32_t>(r[0]) | (static_cast<uint32_t>(r[1]) << 16);
-    packed.y = static_cast<uint32_t>(r[2]) | (static_cast<uint32_t>(r[3]) << 16);
+    packed.x = r[0] | (r[1] << 16);
+    packed.y = r[2] | (r[3] << 16);
     reinterpret_cast<uint2*>(const_cast<uint16_t*>(P.rects))[g] = packed;
 }
 
@@ -353,20 +379,27 @@ __device__ __forceinline__ void cpv_write_depth(CpvPixel& s, float mapped) {
 #endif
 }
 
-/* One covered pixel: barycentrics, depth, varyings, fragment shader, then
- * the reference's per-fragment operations. Returns 1 when the colour write
- * happened. */
-__device__ __forceinline__ void cpv_fragment(const CpvDrawParams& P, const CpvTri& t, float w[3], int32_t x, int32_t y, CpvPixel& s) {
-    w[0] = __fdiv_rn(w[0], t.area);
-    w[1] = __fdiv_rn(w[1], t.area);
-    w[2] = __fdiv_rn(w[2], t.area);
-    const float depth = __fadd_rn(__fadd_rn(__fmul_rn(t.z[0], w[0]), __fmul_rn(t.z[1], w[1])), __fmul_rn(t.z[2], w[2]));
+/* Shading of one covered pixel: barycentrics (w_k / area), screen-linear
+ * depth, varyings (perspective Σ w·v/p ÷ Σ w/p, linear Σ w·v, or flat from
+ * the provoking vertex; CPVulkan/CommandBuffer.Draw.cpp:816-954), viewport
+ * depth mapping (:1300-1313) and the fragment shader. Returns true when the
+ * shader discards. */
+__device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& t, const float wr[3], int32_t x, int32_t y, float colour[4],
+                                          float& mapped) {
+    const float area = t.za.w;
+    float w[3];
+    w[0] = __fdiv_rn(wr[0], area);
+    w[1] = __fdiv_rn(wr[1], area);
+    w[2] = __fdiv_rn(wr[2], area);
+    const float depth = __fadd_rn(__fadd_rn(__fmul_rn(t.za.x, w[0]), __fmul_rn(t.za.y, w[1])), __fmul_rn(t.za.z, w[2]));
+    const float pw[3] = {t.wf.x, t.wf.y, t.wf.z};
+    const uint32_t pslot = cpv_tri_flags(t) >> 8;
     float in[CPV_NV_ALLOC];
 #pragma unroll
     for (int c = 0; c < CPV_NV; c++) {
         const int kind = cpv_interp(c);
         if (kind == 2) {
-            in[c] = t.var[t.pslot][c];
+            in[c] = t.var[pslot][c];
         } else if (kind == 1) {
             float r = 0.0f;
 #pragma unroll
@@ -376,14 +409,14 @@ __device__ __forceinline__ void cpv_fragment(const CpvDrawParams& P, const CpvTr
             float num = 0.0f, den = 0.0f;
 #pragma unroll
             for (int k = 0; k < 3; k++) {
-                num = __fadd_rn(num, __fdiv_rn(__fmul_rn(w[k], t.var[k][c]), t.w[k]));
-                den = __fadd_rn(den, __fdiv_rn(w[k], t.w[k]));
+                num = __fadd_rn(num, __fdiv_rn(__fmul_rn(w[k], t.var[k][c]), pw[k]));
+                den = __fadd_rn(den, __fdiv_rn(w[k], pw[k]));
             }
             in[c] = __fdiv_rn(num, den);
         }
     }
     const float min_d = P.viewport[4], max_d = P.viewport[5];
-    const float mapped = __fadd_rn(__fmul_rn(__fsub_rn(max_d, min_d), depth), min_d);
+    mapped = __fadd_rn(__fmul_rn(__fsub_rn(max_d, min_d), depth), min_d);
     float frag_coord[4];
 #if CPV_ORIGIN_UPPER
     frag_coord[0] = static_cast<float>(x);
@@ -393,10 +426,14 @@ __device__ __forceinline__ void cpv_fragment(const CpvDrawParams& P, const CpvTr
     frag_coord[1] = static_cast<float>(y);
     frag_coord[2] = depth;
     frag_coord[3] = 1.0f;
-    const bool front = (t.flags & 2u) != 0u;
-    float colour[4];
-    if (cpv_fs_run(P, in, frag_coord, front, colour)) return;
+    const bool front = (cpv_tri_flags(t) & 2u) != 0u;
+    return cpv_fs_run(P, in, frag_coord, front, colour);
+}
 
+/* Depth bounds are rejected at pipeline creation; order as the reference's
+ * fragment wrapper: current values → stencil test → depth test → depth /
+ * stencil write → colour write (blend, write mask, encode). */
+__device__ __forceinline__ void cpv_rop(const CpvDrawParams& P, bool front, const float colour[4], float mapped, CpvPixel& s) {
     const bool has_depth = CPV_DEPTH_FORMAT != 0;
     const bool stencil_on = CPV_STENCIL_TEST && CPV_DEPTH_FORMAT == 130;
     const float current_depth = (CPV_DEPTH_TEST && has_depth) ? s.depth : 0.0f;
@@ -423,11 +460,11 @@ __device__ __forceinline__ void cpv_fragment(const CpvDrawParams& P, const CpvTr
         cpv_write_depth(s, mapped);
     }
     if (stencil_result && depth_result) {
-        float dst[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++) dst[i] = cpv_decode_unorm8((s.colour >> cpv_channel_shift(i)) & 0xFFu);
         float out[4];
 #if CPV_BLEND
+        float dst[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) dst[i] = CPV_DECODE8((s.colour >> cpv_channel_shift(i)) & 0xFFu);
         cpv_blend(colour, dst, P.blend_constants, out);
 #else
 #pragma unroll
@@ -443,13 +480,37 @@ __device__ __forceinline__ void cpv_fragment(const CpvDrawParams& P, const CpvTr
     }
 }
 
+/* Block-wide exclusive sum over CPV_RT_THREADS threads. */
+__device__ __forceinline__ uint32_t cpv_block_scan(uint32_t v, uint32_t& total, uint32_t* warp_sums) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= static_cast<uint32_t>(o)) incl += t;
+    }
+    if (lane == 31u) warp_sums[warp] = incl;
+    __syncthreads();
+    uint32_t base = 0, sum = 0;
+    for (uint32_t k = 0; k < CPV_RT_THREADS / 32; k++) {
+        const uint32_t s = warp_sums[k];
+        if (k < warp) base += s;
+        sum += s;
+    }
+    total = sum;
+    return base + incl - v;
+}
+
 /* Raster kernel: one CTA per screen tile (blockIdx.x = tile id).
  * direct != 0: the tile walks every primitive of the draw (small draws).
  * Otherwise it walks its bin: bin_list[start, end) in API order, or — when
  * the bin list overflowed its capacity — every primitive whose tile
- * rectangle overlaps the tile. */
+ * rectangle overlaps the tile. Dynamic shared memory: CPV_BATCH primitives,
+ * then (deferred schedule) the fragment slots. */
 extern "C" __global__ void __launch_bounds__(CPV_RT_THREADS) cpv_raster(CpvDrawParams P, uint32_t direct) {
-    __shared__ CpvTri tris[CPV_BATCH];
+    extern __shared__ float4 cpv_dyn_smem[];
+    CpvTri* tris = reinterpret_cast<CpvTri*>(cpv_dyn_smem);
+    __shared__ uint32_t warp_sums[CPV_RT_THREADS / 32];
     const uint32_t tile = blockIdx.x;
     const uint32_t tx = tile % P.tiles_x, ty = tile / P.tiles_x;
     uint64_t begin = 0, end = P.total_prims;
@@ -463,6 +524,7 @@ extern "C" __global__ void __launch_bounds__(CPV_RT_THREADS) cpv_raster(CpvDrawP
         }
     }
     if (begin >= end) return;
+    cpv_lut8_init();
 
     const float vw = P.viewport[2], vh = P.viewport[3];
     int32_t px[CPV_PPT], py[CPV_PPT];
@@ -478,6 +540,13 @@ extern "C" __global__ void __launch_bounds__(CPV_RT_THREADS) cpv_raster(CpvDrawP
         yf[k] = cpv_pixel_ndc(py[k], vh);
         if (inside[k]) cpv_load_pixel(P, static_cast<uint64_t>(py[k]) * P.fb_width + px[k], st[k]);
     }
+
+#if CPV_DEFERRED
+    uint8_t* slot_base = reinterpret_cast<uint8_t*>(tris + CPV_BATCH);
+    uint32_t* slot_jk = reinterpret_cast<uint32_t*>(slot_base);          /* batch index | pixel k << 8 | discard << 31 */
+    float* slot_f = reinterpret_cast<float*>(slot_jk + CPV_NSLOT);       /* 5 floats per slot: w0 w1 w2 → rgba + mapped */
+    uint16_t* dense = reinterpret_cast<uint16_t*>(slot_f + 5 * CPV_NSLOT);
+#endif
 
     for (uint64_t base = begin; base < end; base += CPV_BATCH) {
         const uint32_t n = static_cast<uint32_t>((end - base) < CPV_BATCH ? (end - base) : CPV_BATCH);
@@ -496,22 +565,92 @@ extern "C" __global__ void __launch_bounds__(CPV_RT_THREADS) cpv_raster(CpvDrawP
             } else {
                 g = P.bin_list[base + threadIdx.x];
             }
-            if (skip) t.flags = 0u;
+            if (skip) t.wf.w = __uint_as_float(0u);
             else cpv_setup<true>(P, g, t);
         }
         __syncthreads();
+#if !CPV_DEFERRED
         for (uint32_t j = 0; j < n; j++) {
             const CpvTri& t = tris[j];
-            if (!(t.flags & 1u)) continue;
+            const uint32_t flags = cpv_tri_flags(t);
+            if (!(flags & 1u)) continue;
+            const int4 box = t.box;
 #pragma unroll
             for (int k = 0; k < CPV_PPT; k++) {
                 if (!inside[k]) continue;
-                if (px[k] < t.x0 || px[k] >= t.x1 || py[k] < t.y0 || py[k] >= t.y1) continue;
+                if (px[k] < box.x || px[k] >= box.z || py[k] < box.y || py[k] >= box.w) continue;
                 float w[3];
                 if (!cpv_covers(t, xf[k], yf[k], w)) continue;
-                cpv_fragment(P, t, w, px[k], py[k], st[k]);
+                float colour[4], mapped;
+                if (cpv_shade(P, t, w, px[k], py[k], colour, mapped)) continue;
+                cpv_rop(P, (flags & 2u) != 0u, colour, mapped, st[k]);
             }
         }
+#else
+        const uint32_t limit = n * CPV_PPT;
+        uint32_t cursor = 0;
+        while (__syncthreads_or(cursor < limit)) {
+            /* 1. coverage: record up to CPV_SLOTS fragments, in primitive order */
+            uint32_t cnt = 0;
+            while (cursor < limit && cnt < CPV_SLOTS) {
+                const uint32_t j = cursor / CPV_PPT, k = cursor - j * CPV_PPT;
+                cursor++;
+                const CpvTri& t = tris[j];
+                if (!(cpv_tri_flags(t) & 1u)) continue;
+                int32_t pxk = px[0], pyk = py[0];
+                float xfk = xf[0], yfk = yf[0];
+                bool ink = inside[0];
+#pragma unroll
+                for (int kk = 1; kk < CPV_PPT; kk++)
+                    if (k == static_cast<uint32_t>(kk)) { pxk = px[kk]; pyk = py[kk]; xfk = xf[kk]; yfk = yf[kk]; ink = inside[kk]; }
+                const int4 box = t.box;
+                if (!ink || pxk < box.x || pxk >= box.z || pyk < box.y || pyk >= box.w) continue;
+                float w[3];
+                if (!cpv_covers(t, xfk, yfk, w)) continue;
+                const uint32_t s = threadIdx.x * CPV_SLOTS + cnt;
+                slot_jk[s] = j | (k << 8);
+                slot_f[5 * s + 0] = w[0];
+                slot_f[5 * s + 1] = w[1];
+                slot_f[5 * s + 2] = w[2];
+                cnt++;
+            }
+            /* 2. dense shading of every recorded fragment */
+            uint32_t total;
+            const uint32_t pos = cpv_block_scan(cnt, total, warp_sums);
+            for (uint32_t i = 0; i < cnt; i++) dense[pos + i] = static_cast<uint16_t>(threadIdx.x * CPV_SLOTS + i);
+            __syncthreads();
+            for (uint32_t d = threadIdx.x; d < total; d += CPV_RT_THREADS) {
+                const uint32_t s = dense[d];
+                const uint32_t owner = s / CPV_SLOTS;
+                const uint32_t jk = slot_jk[s];
+                const uint32_t j = jk & 0xFFu, k = (jk >> 8) & 0xFFu;
+                const int32_t x = static_cast<int32_t>(tx * CPV_TILE + (owner % CPV_TILE));
+                const int32_t y = static_cast<int32_t>(ty * CPV_TILE + (owner / CPV_TILE) + k * CPV_ROWS_PER_PASS);
+                const float w[3] = {slot_f[5 * s + 0], slot_f[5 * s + 1], slot_f[5 * s + 2]};
+                float colour[4], mapped;
+                const bool discard = cpv_shade(P, tris[j], w, x, y, colour, mapped);
+                slot_f[5 * s + 0] = colour[0];
+                slot_f[5 * s + 1] = colour[1];
+                slot_f[5 * s + 2] = colour[2];
+                slot_f[5 * s + 3] = colour[3];
+                slot_f[5 * s + 4] = mapped;
+                if (discard) slot_jk[s] = jk | 0x80000000u;
+            }
+            __syncthreads();
+            /* 3. per-fragment operations of this thread's pixels, in order */
+            for (uint32_t i = 0; i < cnt; i++) {
+                const uint32_t s = threadIdx.x * CPV_SLOTS + i;
+                const uint32_t jk = slot_jk[s];
+                if (jk >> 31) continue;
+                const uint32_t j = jk & 0xFFu, k = (jk >> 8) & 0xFFu;
+                const float colour[4] = {slot_f[5 * s + 0], slot_f[5 * s + 1], slot_f[5 * s + 2], slot_f[5 * s + 3]};
+                const bool front = (cpv_tri_flags(tris[j]) & 2u) != 0u;
+#pragma unroll
+                for (int kk = 0; kk < CPV_PPT; kk++)
+                    if (k == static_cast<uint32_t>(kk)) cpv_rop(P, front, colour, slot_f[5 * s + 4], st[kk]);
+            }
+        }
+#endif
     }
 #pragma unroll
     for (int k = 0; k < CPV_PPT; k++) {
@@ -520,3 +659,8 @@ extern "C" __global__ void __launch_bounds__(CPV_RT_THREADS) cpv_raster(CpvDrawP
 }
 
 #endif /* CPV_PIPELINE_CUH */
+
+/* Dynamic shared memory the raster kernel needs, read by the host at module
+ * load (cudaLibraryGetGlobal) to size the launch. */
+extern "C" __device__ const uint32_t cpv_raster_smem_bytes =
+    CPV_BATCH * sizeof(CpvTri) + (CPV_DEFERRED ? CPV_NSLOT * (4u + 20u + 2u) : 0u);

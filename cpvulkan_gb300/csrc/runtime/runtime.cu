@@ -236,6 +236,26 @@ int load(const std::vector<uint8_t>& cubin, uint32_t tile_shift, Module& out, st
     out.tile_shift = tile_shift;
     const uint32_t tile = 1u << tile_shift;
     out.raster_threads = tile * tile < 256 ? tile * tile : 256;
+    void* dptr = nullptr;
+    size_t dbytes = 0;
+    uint32_t smem = 0;
+    if (cudaLibraryGetGlobal(&dptr, &dbytes, lib, "cpv_raster_smem_bytes") != cudaSuccess || dbytes != 4 ||
+        cudaMemcpy(&smem, dptr, 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        cudaLibraryUnload(lib);
+        out.library = nullptr;
+        error = "pipeline module lacks cpv_raster_smem_bytes";
+        return kErrCuda;
+    }
+    out.raster_smem = smem;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(reinterpret_cast<const void*>(out.raster), cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaLibraryUnload(lib);
+        out.library = nullptr;
+        error = "raster kernel needs more shared memory than the device allows";
+        return kErrCuda;
+    }
     return kOk;
 }
 
@@ -401,7 +421,8 @@ int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& s
     {
         void* args[] = {&P, &direct};
         profile_begin(stream, "cpv_raster");
-        CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.raster), dim3(static_cast<unsigned>(tiles)), dim3(m.raster_threads), args, 0, stream));
+        CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.raster), dim3(static_cast<unsigned>(tiles)), dim3(m.raster_threads), args, m.raster_smem,
+                                  stream));
         profile_end(stream);
         count_launch();
     }

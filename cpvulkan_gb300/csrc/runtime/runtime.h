@@ -39,6 +39,7 @@ struct Module {
     cudaKernel_t raster = nullptr;
     uint32_t tile_shift = 4;
     uint32_t raster_threads = 256;
+    uint32_t raster_smem = 0;  // dynamic shared memory of cpv_raster (bytes)
 };
 
 // Initialises the CUDA context on device 0 (once per process).

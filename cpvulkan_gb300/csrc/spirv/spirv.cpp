@@ -415,6 +415,8 @@ private:
     std::map<uint32_t, uint32_t> handles_;     // SSA id holding a sampled image → slot
     std::string err_;
     bool has_kill_ = false;
+    uint32_t samples_ = 0;
+    uint32_t instructions_ = 0;
 
     bool fail(const std::string& e) {
         if (err_.empty()) err_ = e;
@@ -901,6 +903,7 @@ bool Translator::emit_globals(const EntryPoint& ep, StageResult& out) {
 }
 
 bool Translator::emit_function(const Function& f) {
+    for (const Block& b : f.blocks) instructions_ += static_cast<uint32_t>(b.body.size());
     // Result types of every instruction, and function-local variables.
     for (const Block& b : f.blocks) {
         for (const Instruction& ins : b.body) {
@@ -1288,6 +1291,7 @@ bool Translator::emit_instruction(const Instruction& ins, const std::map<uint32_
             if (w.size() < 6 || !(w[4] & 0x2u)) return fail("explicit-LOD sampling without a Lod operand");
             lod = value(w[5]);
         }
+        samples_++;
         body_ << "  " << R(w[1]) << " = cpv_sample(P.tex[" << h->second << "], " << comp(w[3], 0) << ", " << comp(w[3], 1) << ", " << lod << ");\n";
         return true;
     }
@@ -1353,6 +1357,8 @@ bool Translator::run(const std::string& entry_name, StageResult& out, std::strin
         return false;
     }
     out.has_kill = has_kill_;
+    out.samples = samples_;
+    out.instructions = instructions_;
     const std::string ns = model_ == 0 ? "cpv_vs_ns" : "cpv_fs_ns";
     std::ostringstream s;
     s << "namespace " << ns << " {\n" << types_.str() << loaders_.str() << "}\n";

@@ -128,6 +128,8 @@ struct StageResult {
     std::vector<int> interp;   // FS: per input float, 0 perspective / 1 linear / 2 flat
     bool origin_upper_left = true;
     bool has_kill = false;
+    uint32_t samples = 0;      // image sampling instructions emitted
+    uint32_t instructions = 0; // SPIR-V instructions of the entry function
 };
 
 // Translates the entry point of `m` for `model` (0 vertex, 4 fragment) into a
