@@ -216,7 +216,15 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
 
     auto p = std::make_unique<Pipeline>();
     p->source = src.str();
-    p->key = sha3_256(p->source.data(), p->source.size());
+    // The key covers the generated source and the embedded kernel headers it
+    // includes, so an on-disk cache never returns a cubin of older kernels.
+    {
+        std::string keyed = p->source;
+        keyed += rt::kDeviceHeaderSource;
+        keyed += rt::kPipelineHeaderSource;
+        keyed += rt::kParamsHeaderSource;
+        p->key = sha3_256(keyed.data(), keyed.size());
+    }
     if (const char* dump = std::getenv("CPV_DUMP_DIR")) {
         std::ofstream f(std::string(dump) + "/pipeline_" + hex(p->key).substr(0, 12) + ".cu");
         f << p->source;

@@ -551,19 +551,20 @@ extern "C" __global__ void __launch_bounds__(CPV_RT_THREADS) cpv_raster(CpvDrawP
     for (uint64_t base = begin; base < end; base += CPV_BATCH) {
         const uint32_t n = static_cast<uint32_t>((end - base) < CPV_BATCH ? (end - base) : CPV_BATCH);
         __syncthreads();
-        if (threadIdx.x < n) {
-            CpvTri& t = tris[threadIdx.x];
+        /* a tile of 8 × 8 has fewer threads than CPV_BATCH: stride the set-up */
+        for (uint32_t i = threadIdx.x; i < n; i += CPV_RT_THREADS) {
+            CpvTri& t = tris[i];
             uint64_t g;
             bool skip = false;
             if (direct || scan_rects) {
-                g = base + threadIdx.x;
+                g = base + i;
                 if (scan_rects) {
                     const uint2 r = reinterpret_cast<const uint2*>(P.rects)[g];
                     const uint32_t rx0 = r.x & 0xFFFFu, ry0 = r.x >> 16, rx1 = r.y & 0xFFFFu, ry1 = r.y >> 16;
                     skip = !(tx >= rx0 && tx < rx1 && ty >= ry0 && ty < ry1);
                 }
             } else {
-                g = P.bin_list[base + threadIdx.x];
+                g = P.bin_list[base + i];
             }
             if (skip) t.wf.w = __uint_as_float(0u);
             else cpv_setup<true>(P, g, t);
