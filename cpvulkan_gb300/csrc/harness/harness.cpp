@@ -9,6 +9,7 @@
 
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -587,6 +588,13 @@ cpvh_context* cpvh_open(const char* icd_path, char* err, uint32_t err_len) {
     LOAD_D(vkCmdBeginRenderPass); LOAD_D(vkCmdEndRenderPass); LOAD_D(vkQueueSubmit); LOAD_D(vkQueueWaitIdle); LOAD_D(vkCreateFence);
     LOAD_D(vkDestroyFence); LOAD_D(vkResetFences); LOAD_D(vkWaitForFences);
 #undef LOAD_D
+    // CPVH_SUBMIT=no_alloc: every submission of this context goes through the
+    // ICD's allocation-free submit export (same signature as vkQueueSubmit).
+    if (const char* mode = std::getenv("CPVH_SUBMIT"); mode && std::strcmp(mode, "no_alloc") == 0) {
+        auto fn = reinterpret_cast<PFN_vkQueueSubmit>(dlsym(c->lib, "cpv_queue_submit_no_alloc"));
+        if (!fn) return fail("CPVH_SUBMIT=no_alloc but the ICD lacks cpv_queue_submit_no_alloc", c);
+        f.vkQueueSubmit = fn;
+    }
     f.vkGetDeviceQueue(c->device, 0, 0, &c->queue);
     if (!check_dispatch(c->queue)) return fail("VkQueue lacks the loader magic", c);
     VkPipelineCacheCreateInfo pci{};

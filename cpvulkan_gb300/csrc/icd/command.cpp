@@ -147,7 +147,8 @@ VkResult begin_render_pass(Queue* q, State& s, const Cmd& c, std::vector<DeviceM
     return VK_SUCCESS;
 }
 
-VkResult draw(Queue* q, State& s, uint32_t count, uint32_t instances, uint32_t first, int32_t vertex_offset, uint32_t first_instance, bool indexed) {
+VkResult draw(Queue* q, State& s, uint32_t count, uint32_t instances, uint32_t first, int32_t vertex_offset, uint32_t first_instance, bool indexed,
+              bool no_alloc) {
     Pipeline* p = s.pipeline;
     if (!p || !s.pass || !s.fb) return VK_ERROR_DEVICE_LOST;
     CpvDrawParams P;
@@ -214,13 +215,13 @@ VkResult draw(Queue* q, State& s, uint32_t count, uint32_t instances, uint32_t f
     P.viewport[4] = vp.minDepth;
     P.viewport[5] = vp.maxDepth;
     for (int i = 0; i < 4; i++) P.blend_constants[i] = p->dynamic_blend_constants ? s.blend_constants[i] : p->blend_constants[i];
-    const int r = rt::draw_plain(q->stream, p->module, P, q->scratch);
+    const int r = no_alloc ? rt::draw_plain_static(q->stream, p->module, P) : rt::draw_plain(q->stream, p->module, P, q->scratch);
     return r == rt::kOk ? VK_SUCCESS : VK_ERROR_DEVICE_LOST;
 }
 
 }  // namespace
 
-VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& written) {
+VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& written, bool no_alloc) {
     State s;
     for (const Cmd& c : cb->cmds) {
         VkResult r = VK_SUCCESS;
@@ -269,8 +270,8 @@ VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& writte
             std::memcpy(s.blend_constants, c.bytes.data(), 16);
             s.blend_set = true;
             break;
-        case CmdType::Draw: r = draw(q, s, c.u[0], c.u[1], c.u[2], 0, c.u[3], false); break;
-        case CmdType::DrawIndexed: r = draw(q, s, c.u[0], c.u[1], c.u[2], c.i0, c.u[3], true); break;
+        case CmdType::Draw: r = draw(q, s, c.u[0], c.u[1], c.u[2], 0, c.u[3], false, no_alloc); break;
+        case CmdType::DrawIndexed: r = draw(q, s, c.u[0], c.u[1], c.u[2], c.i0, c.u[3], true, no_alloc); break;
         case CmdType::CopyBuffer: {
             Buffer* src = static_cast<Buffer*>(c.p[0]);
             Buffer* dst = static_cast<Buffer*>(c.p[1]);
@@ -342,6 +343,41 @@ VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& writte
             break;
         }
         if (r != VK_SUCCESS) return r;
+    }
+    return VK_SUCCESS;
+}
+
+VkResult check_no_alloc(CommandBuffer* cb) {
+    Pipeline* pipeline = nullptr;
+    RenderPass* pass = nullptr;
+    Framebuffer* fb = nullptr;
+    for (const Cmd& c : cb->cmds) {
+        switch (c.type) {
+        case CmdType::BeginRenderPass:
+            pass = static_cast<RenderPass*>(c.p[0]);
+            fb = static_cast<Framebuffer*>(c.p[1]);
+            break;
+        case CmdType::EndRenderPass: pass = nullptr; fb = nullptr; break;
+        case CmdType::BindPipeline: pipeline = static_cast<Pipeline*>(c.p[0]); break;
+        case CmdType::Draw:
+        case CmdType::DrawIndexed: {
+            if (!pipeline || !pass || !fb || pass->colour.empty()) break;  // execute() reports these
+            const uint32_t count = c.u[0], instances = c.u[1];
+            const uint32_t ppi = pipeline->topology == VK_PRIMITIVE_TOPOLOGY_TRIANGLE_LIST ? count / 3 : (count > 2 ? count - 2 : 0);
+            if (pass->colour[0] >= fb->attachments.size()) break;
+            const ImageView* cv = fb->attachments[pass->colour[0]];
+            uint32_t w = 0, h = 0;
+            if (!cv || !cv->image) break;
+            view_base(cv, w, h);
+            std::string err;
+            if (rt::static_scratch_check(static_cast<uint64_t>(ppi) * instances, pipeline->module.tile_shift, w, h, err) != rt::kOk) {
+                rt::set_last_error("cpv_queue_submit_no_alloc: " + err);
+                return VK_ERROR_OUT_OF_DEVICE_MEMORY;
+            }
+            break;
+        }
+        default: break;
+        }
     }
     return VK_SUCCESS;
 }

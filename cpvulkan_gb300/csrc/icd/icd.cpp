@@ -1042,8 +1042,8 @@ VKAPI_ATTR void VKAPI_CALL DestroySemaphore(VkDevice, VkSemaphore sem, const VkA
 
 // vkQueueSubmit (CPVulkan/Queue.cpp:11-77): waits, replays each command
 // buffer onto the queue's stream, signals semaphores and the fence. Returns
-// once the work is enqueued.
-VKAPI_ATTR VkResult VKAPI_CALL QueueSubmit(VkQueue queue, uint32_t n, const VkSubmitInfo* si, VkFence fence) {
+// once the work is enqueued. no_alloc selects the fixed binning scratch.
+VkResult submit(VkQueue queue, uint32_t n, const VkSubmitInfo* si, VkFence fence, bool no_alloc) {
     auto* q = reinterpret_cast<Queue*>(queue);
     Device* dev = q->device;
     if (dev->compile_only) {
@@ -1065,7 +1065,7 @@ VKAPI_ATTR VkResult VKAPI_CALL QueueSubmit(VkQueue queue, uint32_t n, const VkSu
             s->signalled = false;
         }
         for (uint32_t k = 0; k < si[i].commandBufferCount; k++) {
-            const VkResult r = execute(q, reinterpret_cast<CommandBuffer*>(si[i].pCommandBuffers[k]), written);
+            const VkResult r = execute(q, reinterpret_cast<CommandBuffer*>(si[i].pCommandBuffers[k]), written, no_alloc);
             if (r != VK_SUCCESS) return r;
         }
         for (uint32_t k = 0; k < si[i].signalSemaphoreCount; k++) {
@@ -1091,6 +1091,8 @@ VKAPI_ATTR VkResult VKAPI_CALL QueueSubmit(VkQueue queue, uint32_t n, const VkSu
     if (cudaGetLastError() != cudaSuccess) return VK_ERROR_DEVICE_LOST;
     return VK_SUCCESS;
 }
+
+VKAPI_ATTR VkResult VKAPI_CALL QueueSubmit(VkQueue queue, uint32_t n, const VkSubmitInfo* si, VkFence fence) { return submit(queue, n, si, fence, false); }
 
 // ------------------------------------------------------- dispatch tables --
 
@@ -1189,6 +1191,31 @@ CPV_EXPORT void cpv_profile_enable(int on) { cpv::rt::profile_enable(on != 0); }
 CPV_EXPORT int cpv_profile_get(const char* kernel, uint64_t* launches, double* total_ms) { return cpv::rt::profile_get(kernel, launches, total_ms); }
 
 CPV_EXPORT void cpv_profile_reset(void) { cpv::rt::profile_reset(); }
+
+CPV_EXPORT VkResult VKAPI_CALL cpv_queue_submit_no_alloc(VkQueue queue, uint32_t submitCount, const VkSubmitInfo* pSubmits, VkFence fence) {
+    using namespace cpv::icd;
+    if (!queue || (submitCount && !pSubmits)) {
+        cpv::rt::set_last_error("cpv_queue_submit_no_alloc: null queue or submit array");
+        return VK_ERROR_INITIALIZATION_FAILED;
+    }
+    auto* q = reinterpret_cast<Queue*>(queue);
+    if (q->device->compile_only) {
+        cpv::rt::set_last_error("cpv_queue_submit_no_alloc: compile-only device (no CUDA device)");
+        return VK_ERROR_DEVICE_LOST;
+    }
+    std::string err;
+    if (cpv::rt::static_scratch_setup(err) != cpv::rt::kOk) {
+        cpv::rt::set_last_error("cpv_queue_submit_no_alloc: " + err);
+        return VK_ERROR_INITIALIZATION_FAILED;
+    }
+    // Reject an oversized draw before any work of the submission is enqueued.
+    for (uint32_t i = 0; i < submitCount; i++)
+        for (uint32_t k = 0; k < pSubmits[i].commandBufferCount; k++) {
+            const VkResult r = check_no_alloc(reinterpret_cast<CommandBuffer*>(pSubmits[i].pCommandBuffers[k]));
+            if (r != VK_SUCCESS) return r;
+        }
+    return submit(queue, submitCount, pSubmits, fence, true);
+}
 
 CPV_EXPORT int cpv_device_available(void) {
     std::string err;

@@ -224,7 +224,12 @@ struct Device : Dispatchable {
 };
 
 // Execution of a recorded command buffer on a queue (command.cpp).
-VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& written);
+// no_alloc: draws bin through the fixed scratch array (rt::draw_plain_static)
+// instead of the queue's grow-only scratch.
+VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& written, bool no_alloc = false);
+// Checks, before any work is enqueued, that every draw of `cb` fits the fixed
+// scratch array (VK_ERROR_OUT_OF_DEVICE_MEMORY and a message otherwise).
+VkResult check_no_alloc(CommandBuffer* cb);
 
 // Pipeline creation (pipeline.cpp).
 VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGraphicsPipelineCreateInfo& info, Pipeline** out);

@@ -429,4 +429,209 @@ int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& s
     return kOk;
 }
 
+// ---------------------------------------------------------------------------
+// Fixed binning scratch for submissions that may not allocate.
+//
+// One file-scope device array per device holds every per-draw scratch buffer
+// of the binning path. It is carved per draw, 256-byte aligned:
+//   words  (256 B)            [0] pair total (written by the scan before the
+//                             raster reads it), [1] status word
+//   rects  (8 B / primitive)  tile rectangles, written by cpv_setup_rects
+//   counts (4 B / tile·span)  bin counters: MUST start at zero; zeroed on
+//                             the stream at the start of every draw
+//   cursor (4 B / tile·span)  scanned counts, then write cursors
+//   scan   (per level)        block sums of the multi-level scan
+//   list   (the rest)         bin list; when the draw produces more
+//                             (primitive, tile) pairs than fit, the raster
+//                             walks the tile rectangles instead (same
+//                             image, slower)
+// Nothing else in the array needs an initial value.
+// ---------------------------------------------------------------------------
+
+static __device__ __align__(256) uint8_t cpv_static_scratch[CPV_STATIC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kMaxStaticDevices = 64;
+std::mutex g_static_mutex;
+uint8_t* g_static_addr[kMaxStaticDevices] = {};
+
+uint64_t align256(uint64_t b) { return (b + 255u) & ~255ull; }
+
+struct StaticCarve {
+    uint64_t words = 0, rects = 0, counts = 0, cursor = 0, scan[8] = {}, list = 0, end = 0;
+};
+
+// Offsets of the binning buffers for `prims` primitives over `bins` tile·span
+// bins; end = first byte of the bin list.
+StaticCarve static_carve(uint64_t prims, uint64_t bins) {
+    StaticCarve c;
+    uint64_t o = 0;
+    c.words = o;
+    o += 256;
+    c.rects = o;
+    o += align256(prims * 8);
+    c.counts = o;
+    o += align256(bins * 4);
+    c.cursor = o;
+    o += align256(bins * 4);
+    uint64_t n = bins;
+    int level = 0;
+    while (n > CPV_SCAN_BLOCK && level < 8) {
+        n = (n + CPV_SCAN_BLOCK - 1) / CPV_SCAN_BLOCK;
+        c.scan[level++] = o;
+        o += align256(2 * n * 4);
+    }
+    c.list = o;
+    c.end = o;
+    return c;
+}
+
+// The binning decision of draw_plain: direct (no bins) or spans per tile.
+bool static_direct(uint64_t prims, uint64_t tiles) { return prims * tiles <= env_u32("CPV_DIRECT_LIMIT", 1u << 18); }
+
+// Spans for a draw in the fixed array: draw_plain's choice, halved until the
+// buffers leave at least a quarter of the array for the bin list (or one
+// span remains).
+uint64_t static_spans(uint64_t prims, uint64_t tiles) {
+    uint64_t spans = (prims + 255) / 256;
+    if (spans > 4096) spans = 4096;
+    if (spans < 1) spans = 1;
+    while (spans > 1 && static_carve(prims, tiles * spans).end + CPV_STATIC_SCRATCH_BYTES / 4 > CPV_STATIC_SCRATCH_BYTES) spans = (spans + 1) / 2;
+    return spans;
+}
+
+int scan_level_static(cudaStream_t stream, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total, uint32_t* const* levels, int level) {
+    const uint64_t blocks = (n + CPV_SCAN_BLOCK - 1) / CPV_SCAN_BLOCK;
+    if (blocks <= 1) {
+        cpv_scan_blocks<<<1, CPV_SCAN_THREADS, 0, stream>>>(in, out, n, nullptr);
+        count_launch();
+    } else {
+        if (level >= 8 || !levels[level]) return kErrInvalid;
+        uint32_t* sums = levels[level];
+        uint32_t* sums_scanned = sums + blocks;
+        cpv_scan_blocks<<<static_cast<unsigned>(blocks), CPV_SCAN_THREADS, 0, stream>>>(in, out, n, sums);
+        count_launch();
+        const int r = scan_level_static(stream, sums, sums_scanned, blocks, nullptr, levels, level + 1);
+        if (r != kOk) return r;
+        cpv_scan_add<<<static_cast<unsigned>(blocks), CPV_SCAN_THREADS, 0, stream>>>(out, n, sums_scanned);
+        count_launch();
+    }
+    if (total) {
+        cpv_scan_total<<<1, 32, 0, stream>>>(in, out, n, total);
+        count_launch();
+    }
+    return kOk;
+}
+
+}  // namespace
+
+int static_scratch_setup(std::string& error) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= kMaxStaticDevices) {
+        cudaGetLastError();
+        error = "static scratch set-up: no current CUDA device";
+        return kErrCuda;
+    }
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (g_static_addr[dev]) return kOk;
+    uint8_t* ptr = nullptr;
+    e = cudaGetSymbolAddress((void**)&ptr, cpv_static_scratch);
+    if (e != cudaSuccess || !ptr) {
+        cudaGetLastError();
+        error = std::string("cudaGetSymbolAddress(cpv_static_scratch) failed: ") + cudaGetErrorString(e);
+        return kErrCuda;
+    }
+    g_static_addr[dev] = ptr;
+    return kOk;
+}
+
+int static_scratch_check(uint64_t prims, uint32_t tile_shift, uint32_t width, uint32_t height, std::string& error) {
+    if (prims == 0 || width == 0 || height == 0) return kOk;
+    const uint64_t tile = 1ull << tile_shift;
+    const uint64_t tiles = ((width + tile - 1) / tile) * ((height + tile - 1) / tile);
+    if (prims > 0xFFFFFFFFull) {
+        error = "draw of " + std::to_string(prims) + " primitives exceeds 2^32 - 1";
+        return kErrInvalid;
+    }
+    if (static_direct(prims, tiles)) return kOk;
+    const uint64_t need = static_carve(prims, tiles * static_spans(prims, tiles)).end;
+    if (need > CPV_STATIC_SCRATCH_BYTES) {
+        error = "draw of " + std::to_string(prims) + " primitives over " + std::to_string(tiles) + " tiles needs " + std::to_string(need) +
+                " bytes of binning scratch; the fixed scratch holds " + std::to_string(static_cast<uint64_t>(CPV_STATIC_SCRATCH_BYTES));
+        return kErrOutOfMemory;
+    }
+    return kOk;
+}
+
+int draw_plain_static(cudaStream_t stream, const Module& m, CpvDrawParams P) {
+    if (P.total_prims == 0 || P.fb_width == 0 || P.fb_height == 0) return kOk;
+    int dev = -1;
+    CPV_CUDA(cudaGetDevice(&dev));
+    uint8_t* base = (dev >= 0 && dev < kMaxStaticDevices) ? g_static_addr[dev] : nullptr;
+    if (!base) {
+        set_last_error("static scratch used before its set-up on this device");
+        return kErrInvalid;
+    }
+    const uint32_t shift = m.tile_shift;
+    const uint32_t tile = 1u << shift;
+    P.tile_shift = shift;
+    P.tiles_x = (P.fb_width + tile - 1) / tile;
+    P.tiles_y = (P.fb_height + tile - 1) / tile;
+    const uint64_t tiles = static_cast<uint64_t>(P.tiles_x) * P.tiles_y;
+    const uint64_t G = P.total_prims;
+    std::string err;
+    int r = static_scratch_check(G, shift, P.fb_width, P.fb_height, err);
+    if (r != kOk) {
+        set_last_error(err);
+        return r;
+    }
+    uint32_t* words = reinterpret_cast<uint32_t*>(base);
+    P.status = words + 1;
+    uint32_t direct = static_direct(G, tiles) ? 1u : 0u;
+    if (!direct) {
+        const uint64_t spans = static_spans(G, tiles);
+        const uint64_t bins = tiles * spans;
+        const StaticCarve c = static_carve(G, bins);
+        uint64_t cap = (CPV_STATIC_SCRATCH_BYTES - c.end) / 4;
+        if (cap > 0xFFFFFFFFull) cap = 0xFFFFFFFFull;
+        uint16_t* rects = reinterpret_cast<uint16_t*>(base + c.rects);
+        uint32_t* counts = reinterpret_cast<uint32_t*>(base + c.counts);
+        uint32_t* cursor = reinterpret_cast<uint32_t*>(base + c.cursor);
+        uint32_t* list = reinterpret_cast<uint32_t*>(base + c.list);
+        uint32_t* levels[8] = {};
+        for (int l = 0; l < 8; l++) levels[l] = c.scan[l] ? reinterpret_cast<uint32_t*>(base + c.scan[l]) : nullptr;
+        P.rects = rects;
+        P.spans = static_cast<uint32_t>(spans);
+        P.list_capacity = static_cast<uint32_t>(cap);
+        P.pair_total = words;
+        P.tile_end = cursor;
+        P.bin_list = list;
+        CPV_CUDA(cudaMemsetAsync(counts, 0, bins * sizeof(uint32_t), stream));
+        {
+            void* args[] = {&P};
+            CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.setup_rects), dim3(static_cast<unsigned>((G + 255) / 256)), dim3(256), args, 0, stream));
+            count_launch();
+        }
+        const unsigned warp_blocks = static_cast<unsigned>((spans * 32 + 255) / 256);
+        cpv_span_count<<<warp_blocks, 256, 0, stream>>>(rects, G, static_cast<uint32_t>(spans), P.tiles_x, counts);
+        count_launch();
+        if ((r = scan_level_static(stream, counts, cursor, bins, words, levels, 0)) != kOk) {
+            set_last_error("static scratch scan levels exhausted");
+            return r;
+        }
+        cpv_span_write<<<warp_blocks, 256, 0, stream>>>(rects, G, static_cast<uint32_t>(spans), P.tiles_x, cursor, list, P.list_capacity, words);
+        count_launch();
+    }
+    {
+        void* args[] = {&P, &direct};
+        CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.raster), dim3(static_cast<unsigned>(tiles)), dim3(m.raster_threads), args, m.raster_smem,
+                                  stream));
+        count_launch();
+    }
+    CPV_CUDA(cudaGetLastError());
+    return kOk;
+}
+
 }  // namespace cpv::rt

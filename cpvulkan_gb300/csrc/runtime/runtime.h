@@ -103,6 +103,22 @@ void profile_reset();
 // binning fields are filled here.
 int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& scratch);
 
+// Fixed binning scratch for submissions that may not allocate: one
+// 32 MiB file-scope device array per device. A draw needs 8 bytes per
+// primitive for its tile rectangles plus its bins; one that does not fit even
+// with one span per tile is rejected (kErrOutOfMemory, message in
+// last_error()). The array is shared by every queue of the process on that
+// device, so draw_plain_static calls whose work overlaps on the GPU race.
+#define CPV_STATIC_SCRATCH_BYTES (32ull << 20)
+// Resolves the array's device address for the current device
+// (cudaGetSymbolAddress, once per device). Call outside any stream capture.
+int static_scratch_setup(std::string& error);
+// kOk when a draw of `prims` primitives on a width × height attachment fits.
+int static_scratch_check(uint64_t prims, uint32_t tile_shift, uint32_t width, uint32_t height, std::string& error);
+// draw_plain with every scratch buffer carved from the fixed array: launches
+// the same kernels, allocates nothing, creates no CUDA objects.
+int draw_plain_static(cudaStream_t stream, const Module& m, CpvDrawParams P);
+
 // Attachment fill with an encoded texel (1, 2, 4 or 8 bytes).
 int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, uint32_t lo, uint32_t hi);
 

@@ -65,6 +65,34 @@ CPV_EXPORT int cpv_device_available(void);
 CPV_EXPORT int cpv_queue_record(VkQueue queue, uint32_t slot);
 CPV_EXPORT double cpv_queue_elapsed_ms(VkQueue queue, uint32_t slot_begin, uint32_t slot_end);
 
+/* ---- submission without allocation (no counterpart in the reference) ----
+ *
+ * Same signature and results as vkQueueSubmit, for callers that cannot
+ * allocate device memory while submitting: a renderer working inside a fixed
+ * device-memory budget that must not grow, or a submit thread that must not
+ * stall, as cudaMalloc / cudaFree may synchronise the device. vkQueueSubmit
+ * grows each queue's binning scratch with cudaMalloc the first time a draw
+ * needs more of it; this variant bins every draw through one file-scope
+ * 32 MiB device array instead, and allocates no device or pinned memory and
+ * creates no CUDA objects (host-side bookkeeping of the submission is as in
+ * vkQueueSubmit).
+ *
+ * - The first call on a device resolves the array's address
+ *   (cudaGetSymbolAddress) with that device current; make that first call
+ *   outside any stream capture, before relying on it.
+ * - A draw needs 8 bytes per primitive for its tile rectangles plus its bins;
+ *   a submission holding a draw that does not fit is rejected before any of
+ *   its work is enqueued: VK_ERROR_OUT_OF_DEVICE_MEMORY, reason in
+ *   cpv_last_error(). Draws of up to about 4 million primitives fit.
+ * - The bin counters must start at zero for every draw; the call zeroes
+ *   them on the queue's stream itself. Nothing else needs an initial value.
+ * - The array is shared by every queue of the process on a device: calls
+ *   whose work overlaps on the GPU (two queues, or two devices' queues on
+ *   one GPU) race on it. Serialise them, e.g. wait for the fence of one
+ *   before submitting on another queue. Successive calls on one queue are
+ *   ordered by its stream and do not race. */
+CPV_EXPORT VkResult VKAPI_CALL cpv_queue_submit_no_alloc(VkQueue queue, uint32_t submitCount, const VkSubmitInfo* pSubmits, VkFence fence);
+
 #ifdef __cplusplus
 }
 #endif
