@@ -34,10 +34,21 @@ def build():
     return native_build.build()
 
 
+class SamplerDesc(ctypes.Structure):
+    """cpv_scene_sampler (include/cpv/scene.h)."""
+    _fields_ = [(n, ctypes.c_uint32) for n in ("mag_filter", "min_filter", "mipmap_mode", "address_u", "address_v", "address_w")] + \
+               [(n, ctypes.c_float) for n in ("mip_lod_bias", "min_lod", "max_lod")] + [("border_color", ctypes.c_uint32)]
+
+
 class SceneHeader(ctypes.Structure):
-    """Leading fields of cpv_scene (include/cpv/scene.h)."""
-    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("color_format", ctypes.c_uint32),
-                ("depth_format", ctypes.c_uint32)]
+    """cpv_scene (include/cpv/scene.h)."""
+    u32, f32, u64, vp = ctypes.c_uint32, ctypes.c_float, ctypes.c_uint64, ctypes.c_void_p
+    _fields_ = [("width", u32), ("height", u32), ("color_format", u32), ("depth_format", u32), ("clear_color", f32 * 4),
+                ("clear_depth", f32), ("clear_stencil", u32), ("viewport", f32 * 6), ("vertex_data", vp), ("vertex_bytes", u64),
+                ("index_data", vp), ("index_bytes", u64), ("index_type", u32), ("uniform_data", vp), ("uniform_bytes", u32),
+                ("texture_data", vp), ("texture_bytes", u64), ("texture_width", u32), ("texture_height", u32),
+                ("texture_levels", u32), ("texture_format", u32), ("sampler", SamplerDesc), ("num_pipelines", u32),
+                ("pipelines", vp), ("num_draws", u32), ("draws", vp)]
 
 
 def depth_texel_bytes(fmt):
@@ -98,6 +109,16 @@ class Scene:
         self.width, self.height = hdr.width, hdr.height
         self.color_format, self.depth_format = hdr.color_format, hdr.depth_format
         self.config = config
+
+    @property
+    def draws(self):
+        return SceneHeader.from_address(self.ptr).num_draws
+
+    @property
+    def input_bytes(self):
+        """Vertex, index, uniform and texture bytes of the scene."""
+        h = SceneHeader.from_address(self.ptr)
+        return h.vertex_bytes + h.index_bytes + h.uniform_bytes + h.texture_bytes
 
     @property
     def triangles(self):

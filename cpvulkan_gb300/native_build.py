@@ -105,6 +105,18 @@ def _check_arch():
 
 
 def build(verbose=False):
+    """Builds what is out of date. Processes that build at the same time (one
+    per rank under torchrun) take turns on a lock file."""
+    import fcntl
+    with open(os.path.join(HERE, ".build.lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            return _build(verbose)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
+
+
+def _build(verbose):
     _check_arch()
     _embed_sources()
     _embed_spirv()

@@ -1,0 +1,105 @@
+"""The C ABI boundary on a machine without a GPU: the libraries load, export
+every function their public headers declare, and the ICD answers the loader
+interface (negotiation, proc-address lookup, manifest) without a device."""
+import ctypes
+import json
+import os
+import re
+
+import pytest
+
+import cpvulkan_gb300 as c
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared(header, prefix_re):
+    text = open(os.path.join(ROOT, header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = "\n".join(l for l in text.splitlines() if not l.lstrip().startswith("#"))
+    return sorted(set(re.findall(prefix_re, text)))
+
+
+def test_icd_exports_every_declared_symbol(native):
+    names = declared("include/cpvulkan_gb300.h", r"CPV_EXPORT[^;(]*?\b(\w+)\s*\(")
+    assert "vk_icdGetInstanceProcAddr" in names and "cpv_queue_submit_no_alloc" in names
+    lib = ctypes.CDLL(c.ICD_PATH)
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_harness_exports_every_declared_symbol(native):
+    names = declared("include/cpv_harness.h", r"\b(cpvh_\w+)\s*\(")
+    assert len(names) >= 10
+    lib = c.harness()
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_oracle_exports_every_declared_symbol(oracle):
+    names = declared("oracle/oracle.h", r"\b(cpv_oracle_\w+)\s*\(")
+    missing = [n for n in names if not hasattr(oracle.lib, n)]
+    assert not missing, missing
+
+
+def test_loader_negotiation_and_proc_addr(native):
+    lib = ctypes.CDLL(c.ICD_PATH)
+    ver = ctypes.c_uint32(7)
+    assert lib.vk_icdNegotiateLoaderICDInterfaceVersion(ctypes.byref(ver)) == 0
+    assert 1 <= ver.value <= 7
+    gipa = lib.vk_icdGetInstanceProcAddr
+    gipa.restype = ctypes.c_void_p
+    gipa.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+    for name in (b"vkCreateInstance", b"vkEnumerateInstanceExtensionProperties", b"vkEnumerateInstanceVersion"):
+        assert gipa(None, name), name
+    assert not gipa(None, b"vkNotAFunction")
+    gpa = lib.vk_icdGetPhysicalDeviceProcAddr
+    gpa.restype = ctypes.c_void_p
+    gpa.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+    assert not gpa(None, b"vkGetPhysicalDeviceProperties")
+
+
+def test_manifest_names_the_library(native):
+    path = os.path.join(os.path.dirname(c.ICD_PATH), "CPVulkan.json")
+    with open(path) as f:
+        m = json.load(f)
+    assert m["file_format_version"]
+    lib = m["ICD"]["library_path"]
+    lib = lib if os.path.isabs(lib) else os.path.join(os.path.dirname(path), lib)
+    assert os.path.samefile(lib, c.ICD_PATH)
+    assert m["ICD"]["api_version"].startswith("1.")
+
+
+def test_diagnostics_without_device(native):
+    lib = ctypes.CDLL(c.ICD_PATH)
+    lib.cpv_last_error.restype = ctypes.c_char_p
+    assert lib.cpv_last_error() is not None
+    lib.cpv_kernel_launches.restype = ctypes.c_uint64
+    assert lib.cpv_kernel_launches() >= 0
+    assert lib.cpv_device_available() in (0, 1)
+
+
+def test_no_alloc_submit_rejects_null(native):
+    lib = ctypes.CDLL(c.ICD_PATH)
+    f = lib.cpv_queue_submit_no_alloc
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p]
+    assert f(None, 0, None, None) != 0
+    lib.cpv_last_error.restype = ctypes.c_char_p
+    assert b"cpv_queue_submit_no_alloc" in lib.cpv_last_error()
+
+
+def test_gpu_path_has_no_cpu_fallback(native):
+    """Without a device, submissions fail loudly instead of rendering on the CPU."""
+    if c.device_available():
+        pytest.skip("a CUDA device is present")
+    os.environ["CPV_COMPILE_ONLY"] = "1"
+    try:
+        ctx = c.Context()
+        scene = c.Scene(c.CUBE, 1, [0])
+        with pytest.raises(RuntimeError):
+            r = c.Renderer(ctx, scene)
+            r.render(1)
+        ctx.close()
+    finally:
+        del os.environ["CPV_COMPILE_ONLY"]

@@ -1,0 +1,78 @@
+"""Pipeline creation on a machine without a GPU (compile-only device):
+SPIR-V translation and NVRTC compilation for sm_103a of every shipped shader
+program under its fixed-function variants, the pipeline key (SHA3-256 of the
+generated source and the kernel headers it includes), and the disk cache."""
+import glob
+import hashlib
+import os
+
+import pytest
+
+import cpvulkan_gb300 as c
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+KERNELS = os.path.join(ROOT, "cpvulkan_gb300", "csrc", "kernels")
+
+# (program, variant bits) — bits: 0-1 cull, 2 front CW, 3-4 depth format,
+# 5 blend, 6-7 depth op, 8 stencil, 9 BGRA, 10-11 topology, 12 u16 indices,
+# 13 depth write off, 14 nearest + mirror/border sampler, 15 LOD bias
+PROGRAMS = [
+    (c.PROGRAM_CUBE, 0x0), (c.PROGRAM_CUBE, 0x18 | 0x100), (c.PROGRAM_CUBE, 0x20 | 0x200 | 0x400),
+    (c.PROGRAM_TEXLIT, 0x10 | 0x4000), (c.PROGRAM_FLATQUAD, 0x20), (c.PROGRAM_MESHPC, 0x10 | 0x2 | 0x4),
+    (c.PROGRAM_DISCARD, 0x10), (c.PROGRAM_NOPERSP, 0x8 | 0x800),
+]
+
+
+@pytest.fixture
+def compile_ctx(native, monkeypatch, tmp_path):
+    monkeypatch.setenv("CPV_COMPILE_ONLY", "1")
+    monkeypatch.setenv("CPV_DUMP_DIR", str(tmp_path))
+    ctx = c.Context()
+    yield ctx, tmp_path
+    ctx.close()
+
+
+@pytest.mark.parametrize("program,variant", PROGRAMS)
+def test_program_compiles(compile_ctx, program, variant):
+    ctx, dump = compile_ctx
+    ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [program, variant, 32, 32, 4]))
+    sources = glob.glob(str(dump / "pipeline_*.cu"))
+    assert sources
+    text = open(sources[0]).read()
+    assert "cpv_vs_run" in text and "cpv_fs_run" in text
+
+
+def test_pipeline_key_is_sha3_of_source_and_kernels(compile_ctx):
+    ctx, dump = compile_ctx
+    ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [c.PROGRAM_TEXLIT, 0x10, 32, 32, 4]))
+    (path,) = glob.glob(str(dump / "pipeline_*.cu"))
+    keyed = open(path, "rb").read()
+    for h in ("cpv_device.cuh", "cpv_pipeline.cuh", "cpv_params.h"):
+        keyed += open(os.path.join(KERNELS, h), "rb").read()
+    assert os.path.basename(path) == "pipeline_%s.cu" % hashlib.sha3_256(keyed).hexdigest()[:12]
+
+
+def test_disk_cache_round_trip(native, monkeypatch, tmp_path):
+    monkeypatch.setenv("CPV_COMPILE_ONLY", "1")
+    monkeypatch.setenv("CPV_CACHE_DIR", str(tmp_path))
+    scene = c.Scene(c.PROGRAM, 1, [c.PROGRAM_FLATQUAD, 0x20, 32, 32, 4])
+    ctx = c.Context()
+    ctx.compile_pipelines(scene)
+    ctx.close()
+    cubins = glob.glob(str(tmp_path / "*.cubin"))
+    assert len(cubins) == 1 and os.path.getsize(cubins[0]) > 1000
+    mtime = os.path.getmtime(cubins[0])
+    ctx = c.Context()  # a new device: the cubin comes from the disk cache
+    ctx.compile_pipelines(scene)
+    ctx.close()
+    assert os.path.getmtime(cubins[0]) == mtime
+
+
+@pytest.mark.parametrize("tile", ["8", "32"])
+def test_tile_sizes_compile(native, monkeypatch, tile):
+    monkeypatch.setenv("CPV_COMPILE_ONLY", "1")
+    monkeypatch.setenv("CPV_TILE", tile)
+    ctx = c.Context()
+    ctx.compile_pipelines(c.Scene(c.HEIGHTFIELD, 1, [16, 64, 64]))
+    ctx.close()
+
