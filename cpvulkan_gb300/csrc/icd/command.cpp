@@ -8,6 +8,7 @@
 // the fence observes completion.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "icd.h"
@@ -147,11 +148,14 @@ VkResult begin_render_pass(Queue* q, State& s, const Cmd& c, std::vector<DeviceM
     return VK_SUCCESS;
 }
 
-VkResult draw(Queue* q, State& s, uint32_t count, uint32_t instances, uint32_t first, int32_t vertex_offset, uint32_t first_instance, bool indexed,
-              bool no_alloc) {
+// Parameters of one draw from the current state: the per-draw path launches
+// them, the batched path collects them. `empty` when the draw has no
+// primitive.
+VkResult build_draw(State& s, uint32_t count, uint32_t instances, uint32_t first, int32_t vertex_offset, uint32_t first_instance, bool indexed,
+                    CpvDrawParams& P, bool& empty) {
     Pipeline* p = s.pipeline;
+    empty = true;
     if (!p || !s.pass || !s.fb) return VK_ERROR_DEVICE_LOST;
-    CpvDrawParams P;
     std::memset(&P, 0, sizeof(P));
     for (int b = 0; b < 8; b++) {
         const BoundVertex& bv = s.vertex[b];
@@ -215,61 +219,167 @@ VkResult draw(Queue* q, State& s, uint32_t count, uint32_t instances, uint32_t f
     P.viewport[4] = vp.minDepth;
     P.viewport[5] = vp.maxDepth;
     for (int i = 0; i < 4; i++) P.blend_constants[i] = p->dynamic_blend_constants ? s.blend_constants[i] : p->blend_constants[i];
+    empty = false;
+    return VK_SUCCESS;
+}
+
+VkResult draw(Queue* q, State& s, uint32_t count, uint32_t instances, uint32_t first, int32_t vertex_offset, uint32_t first_instance, bool indexed,
+              bool no_alloc) {
+    CpvDrawParams P;
+    bool empty = true;
+    const VkResult vr = build_draw(s, count, instances, first, vertex_offset, first_instance, indexed, P, empty);
+    if (vr != VK_SUCCESS || empty) return vr;
+    Pipeline* p = s.pipeline;
     const int r = no_alloc ? rt::draw_plain_static(q->stream, p->module, P) : rt::draw_plain(q->stream, p->module, P, q->scratch);
     return r == rt::kOk ? VK_SUCCESS : VK_ERROR_DEVICE_LOST;
+}
+
+// Applies a binding / dynamic-state command to `s`; false for any other.
+bool apply_state(State& s, const Cmd& c) {
+    switch (c.type) {
+    case CmdType::BindPipeline: s.pipeline = static_cast<Pipeline*>(c.p[0]); return true;
+    case CmdType::BindVertexBuffers:
+        for (uint32_t i = 0; i < c.u[1]; i++) {
+            const uint32_t slot = c.u[0] + i;
+            if (slot < 8) {
+                s.vertex[slot].buffer = reinterpret_cast<Buffer*>(c.list[2 * i]);
+                s.vertex[slot].offset = c.list[2 * i + 1];
+            }
+        }
+        return true;
+    case CmdType::BindIndexBuffer:
+        s.index = static_cast<Buffer*>(c.p[0]);
+        s.index_offset = c.q[0];
+        s.index_size = c.u[0] == VK_INDEX_TYPE_UINT16 ? 2 : 4;
+        return true;
+    case CmdType::BindDescriptorSets: {
+        const uint32_t first = c.u[0], count = c.u[1];
+        uint32_t dyn_used = 0;
+        for (uint32_t i = 0; i < count && first + i < 8; i++) {
+            DescriptorSet* ds = reinterpret_cast<DescriptorSet*>(c.list[i]);
+            s.sets[first + i] = ds;
+            s.dynamic_offsets[first + i].clear();
+            if (!ds || !ds->layout) continue;
+            for (const auto& b : ds->layout->bindings)
+                if (b.descriptorType == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC || b.descriptorType == VK_DESCRIPTOR_TYPE_STORAGE_BUFFER_DYNAMIC)
+                    for (uint32_t k = 0; k < b.descriptorCount && dyn_used < c.u[2]; k++)
+                        s.dynamic_offsets[first + i].push_back(static_cast<uint32_t>(c.list[count + dyn_used++]));
+        }
+        return true;
+    }
+    case CmdType::PushConstants: {
+        const uint32_t off = c.u[0];
+        const size_t n = c.bytes.size();
+        if (off < 128) std::memcpy(s.push + off, c.bytes.data(), off + n <= 128 ? n : 128 - off);
+        return true;
+    }
+    case CmdType::SetViewport: s.viewport = c.viewport; s.viewport_set = true; return true;
+    case CmdType::SetScissor: return true;
+    case CmdType::SetBlendConstants:
+        std::memcpy(s.blend_constants, c.bytes.data(), 16);
+        s.blend_set = true;
+        return true;
+    default: return false;
+    }
+}
+
+uint32_t env_u32(const char* name, uint32_t dflt) {
+    const char* v = std::getenv(name);
+    return v && *v ? static_cast<uint32_t>(std::strtoul(v, nullptr, 0)) : dflt;
+}
+
+// Builds the batch of the render pass whose commands are (begin, end): the
+// draws' parameters, the pipeline set, the batched module and the plan.
+// Leaves state->plain set when the pass does not batch.
+void build_batch(Queue* q, const CommandBuffer* cb, size_t begin, size_t end, const State& entry, BatchState& state) {
+    state.plain = true;
+    State s = entry;
+    rt::BatchDraws in;
+    std::vector<Pipeline*> pipelines;
+    float vw = 0.0f, vh = 0.0f;
+    for (size_t i = begin + 1; i < end; i++) {
+        const Cmd& c = cb->cmds[i];
+        if (apply_state(s, c)) continue;
+        if (c.type != CmdType::Draw && c.type != CmdType::DrawIndexed) return;  // indirect draws: per-draw path
+        CpvDrawParams P;
+        bool empty = true;
+        const bool indexed = c.type == CmdType::DrawIndexed;
+        if (build_draw(s, c.u[0], c.u[1], c.u[2], indexed ? c.i0 : 0, c.u[3], indexed, P, empty) != VK_SUCCESS) return;
+        if (empty) continue;
+        auto it = std::find(pipelines.begin(), pipelines.end(), s.pipeline);
+        if (it == pipelines.end()) {
+            if (pipelines.size() == 16) return;  // 4-bit pipeline index
+            pipelines.push_back(s.pipeline);
+            it = pipelines.end() - 1;
+        }
+        if (in.draws.empty()) {
+            vw = P.viewport[2];
+            vh = P.viewport[3];
+            in.color = P.color;
+            in.depth = P.depth;
+            in.fb_width = P.fb_width;
+            in.fb_height = P.fb_height;
+        } else if (P.viewport[2] != vw || P.viewport[3] != vh) {
+            return;  // pixel centres depend on the viewport extent
+        }
+        in.draws.push_back(P);
+        in.pipeline.push_back(static_cast<uint32_t>(it - pipelines.begin()));
+    }
+    if (in.draws.empty()) return;
+    in.vw = vw;
+    in.vh = vh;
+    ModuleConfig mc;
+    mc.tile_shift = pipelines[0]->tile_shift;
+    for (const Pipeline* p : pipelines) mc.deferred = mc.deferred || p->prefers_deferred;
+    if (const char* d = std::getenv("CPV_DEFERRED")) mc.deferred = d[0] == '1';
+    rt::Module* m = batch_module(cb->device, pipelines, mc);
+    if (!m) return;
+    auto plan = std::make_unique<rt::BatchPlan>();
+    if (plan->build(*m, in, q->stream) != rt::kOk) return;
+    state.module = m;
+    state.plan = std::move(plan);
+    state.plain = false;
+}
+
+// Runs the render pass (begin, end) batched when it batches: returns true
+// after enqueuing it, with `s` advanced past its commands; false leaves the
+// pass to the per-draw path.
+bool run_batched(Queue* q, CommandBuffer* cb, size_t begin, size_t end, State& s, VkResult& result) {
+    size_t draws = 0;
+    for (size_t i = begin + 1; i < end; i++)
+        if (cb->cmds[i].type == CmdType::Draw || cb->cmds[i].type == CmdType::DrawIndexed) draws++;
+    if (draws < env_u32("CPV_BATCH_MIN_DRAWS", 16u) || env_u32("CPV_BATCH", 1u) == 0u) return false;
+    auto& slot = cb->batches[begin];
+    if (!slot) {
+        slot = std::make_unique<BatchState>();
+        build_batch(q, cb, begin, end, s, *slot);
+    }
+    if (slot->plain) return false;
+    for (size_t i = begin + 1; i < end; i++) apply_state(s, cb->cmds[i]);
+    rt::profile_begin(q->stream, "cpv_batch");
+    result = slot->plan->launch(*slot->module, q->stream) == rt::kOk ? VK_SUCCESS : VK_ERROR_DEVICE_LOST;
+    rt::profile_end(q->stream);
+    return true;
 }
 
 }  // namespace
 
 VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& written, bool no_alloc) {
     State s;
-    for (const Cmd& c : cb->cmds) {
+    for (size_t idx = 0; idx < cb->cmds.size(); idx++) {
+        const Cmd& c = cb->cmds[idx];
+        if (apply_state(s, c)) continue;
         VkResult r = VK_SUCCESS;
         switch (c.type) {
-        case CmdType::BeginRenderPass: r = begin_render_pass(q, s, c, written); break;
+        case CmdType::BeginRenderPass: {
+            r = begin_render_pass(q, s, c, written);
+            if (r != VK_SUCCESS || no_alloc) break;
+            size_t end = idx + 1;
+            while (end < cb->cmds.size() && cb->cmds[end].type != CmdType::EndRenderPass) end++;
+            if (end < cb->cmds.size() && run_batched(q, cb, idx, end, s, r)) idx = end - 1;  // continue at EndRenderPass
+            break;
+        }
         case CmdType::EndRenderPass: s.pass = nullptr; s.fb = nullptr; break;
-        case CmdType::BindPipeline: s.pipeline = static_cast<Pipeline*>(c.p[0]); break;
-        case CmdType::BindVertexBuffers:
-            for (uint32_t i = 0; i < c.u[1]; i++) {
-                const uint32_t slot = c.u[0] + i;
-                if (slot < 8) {
-                    s.vertex[slot].buffer = reinterpret_cast<Buffer*>(c.list[2 * i]);
-                    s.vertex[slot].offset = c.list[2 * i + 1];
-                }
-            }
-            break;
-        case CmdType::BindIndexBuffer:
-            s.index = static_cast<Buffer*>(c.p[0]);
-            s.index_offset = c.q[0];
-            s.index_size = c.u[0] == VK_INDEX_TYPE_UINT16 ? 2 : 4;
-            break;
-        case CmdType::BindDescriptorSets: {
-            const uint32_t first = c.u[0], count = c.u[1];
-            uint32_t dyn_used = 0;
-            for (uint32_t i = 0; i < count && first + i < 8; i++) {
-                DescriptorSet* ds = reinterpret_cast<DescriptorSet*>(c.list[i]);
-                s.sets[first + i] = ds;
-                s.dynamic_offsets[first + i].clear();
-                if (!ds || !ds->layout) continue;
-                for (const auto& b : ds->layout->bindings)
-                    if (b.descriptorType == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC || b.descriptorType == VK_DESCRIPTOR_TYPE_STORAGE_BUFFER_DYNAMIC)
-                        for (uint32_t k = 0; k < b.descriptorCount && dyn_used < c.u[2]; k++)
-                            s.dynamic_offsets[first + i].push_back(static_cast<uint32_t>(c.list[count + dyn_used++]));
-            }
-            break;
-        }
-        case CmdType::PushConstants: {
-            const uint32_t off = c.u[0];
-            const size_t n = c.bytes.size();
-            if (off < 128) std::memcpy(s.push + off, c.bytes.data(), off + n <= 128 ? n : 128 - off);
-            break;
-        }
-        case CmdType::SetViewport: s.viewport = c.viewport; s.viewport_set = true; break;
-        case CmdType::SetScissor: break;
-        case CmdType::SetBlendConstants:
-            std::memcpy(s.blend_constants, c.bytes.data(), 16);
-            s.blend_set = true;
-            break;
         case CmdType::Draw: r = draw(q, s, c.u[0], c.u[1], c.u[2], 0, c.u[3], false, no_alloc); break;
         case CmdType::DrawIndexed: r = draw(q, s, c.u[0], c.u[1], c.u[2], c.i0, c.u[3], true, no_alloc); break;
         case CmdType::CopyBuffer: {
@@ -340,11 +450,48 @@ VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& writte
         case CmdType::Barrier:
         case CmdType::DrawIndirect:
         case CmdType::DrawIndexedIndirect:
+        default:
             break;
         }
         if (r != VK_SUCCESS) return r;
     }
     return VK_SUCCESS;
+}
+
+void precompile_batches(CommandBuffer* cb) {
+    if (env_u32("CPV_BATCH", 1u) == 0u) return;
+    const uint32_t min_draws = env_u32("CPV_BATCH_MIN_DRAWS", 16u);
+    Pipeline* bound = nullptr;
+    std::vector<Pipeline*> pipelines;
+    size_t draws = 0;
+    bool in_pass = false;
+    for (const Cmd& c : cb->cmds) {
+        switch (c.type) {
+        case CmdType::BeginRenderPass:
+            in_pass = true;
+            pipelines.clear();
+            draws = 0;
+            break;
+        case CmdType::BindPipeline: bound = static_cast<Pipeline*>(c.p[0]); break;
+        case CmdType::Draw:
+        case CmdType::DrawIndexed:
+            if (!in_pass || !bound) break;
+            draws++;
+            if (std::find(pipelines.begin(), pipelines.end(), bound) == pipelines.end()) pipelines.push_back(bound);
+            break;
+        case CmdType::EndRenderPass:
+            if (in_pass && draws >= min_draws && !pipelines.empty() && pipelines.size() <= 16) {
+                ModuleConfig mc;
+                mc.tile_shift = pipelines[0]->tile_shift;
+                for (const Pipeline* p : pipelines) mc.deferred = mc.deferred || p->prefers_deferred;
+                if (const char* d = std::getenv("CPV_DEFERRED")) mc.deferred = d[0] == '1';
+                batch_module(cb->device, pipelines, mc);  // compiled and cached; errors surface at submit
+            }
+            in_pass = false;
+            break;
+        default: break;
+        }
+    }
 }
 
 VkResult check_no_alloc(CommandBuffer* cb) {

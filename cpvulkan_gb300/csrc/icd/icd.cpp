@@ -301,6 +301,7 @@ VKAPI_ATTR void VKAPI_CALL DestroyDevice(VkDevice device, const VkAllocationCall
     }
     cudaStreamSynchronize(dev->queue->stream);
     cudaStreamDestroy(dev->queue->stream);
+    for (auto& kv : dev->batch_modules) rt::unload(*kv.second);
     delete dev->queue;
     delete dev;
 }
@@ -787,7 +788,7 @@ VKAPI_ATTR void VKAPI_CALL DestroyCommandPool(VkDevice, VkCommandPool pool, cons
     delete p;
 }
 VKAPI_ATTR VkResult VKAPI_CALL ResetCommandPool(VkDevice, VkCommandPool pool, VkCommandPoolResetFlags) {
-    for (auto* cb : reinterpret_cast<CommandPool*>(pool)->buffers) cb->cmds.clear();
+    for (auto* cb : reinterpret_cast<CommandPool*>(pool)->buffers) cb->reset();
     return VK_SUCCESS;
 }
 VKAPI_ATTR VkResult VKAPI_CALL AllocateCommandBuffers(VkDevice device, const VkCommandBufferAllocateInfo* ai, VkCommandBuffer* out) {
@@ -811,16 +812,18 @@ VKAPI_ATTR void VKAPI_CALL FreeCommandBuffers(VkDevice, VkCommandPool pool, uint
 }
 VKAPI_ATTR VkResult VKAPI_CALL BeginCommandBuffer(VkCommandBuffer cmd, const VkCommandBufferBeginInfo*) {
     auto* cb = reinterpret_cast<CommandBuffer*>(cmd);
-    cb->cmds.clear();
+    cb->reset();
     cb->recording = true;
     return VK_SUCCESS;
 }
 VKAPI_ATTR VkResult VKAPI_CALL EndCommandBuffer(VkCommandBuffer cmd) {
-    reinterpret_cast<CommandBuffer*>(cmd)->recording = false;
+    auto* cb = reinterpret_cast<CommandBuffer*>(cmd);
+    cb->recording = false;
+    precompile_batches(cb);
     return VK_SUCCESS;
 }
 VKAPI_ATTR VkResult VKAPI_CALL ResetCommandBuffer(VkCommandBuffer cmd, VkCommandBufferResetFlags) {
-    reinterpret_cast<CommandBuffer*>(cmd)->cmds.clear();
+    reinterpret_cast<CommandBuffer*>(cmd)->reset();
     return VK_SUCCESS;
 }
 

@@ -153,8 +153,25 @@ struct Pipeline {
     PipelineLayout* layout = nullptr;
     uint32_t colour_format = 0, depth_format = 0;
     bool blend = false;
-    std::string source;  // generated CUDA translation unit (diagnostics)
+    std::string stage;   // stage block: fixed-function macros + translated shaders (see compose_module)
+    uint32_t nv = 0;     // varying floats
+    bool prefers_deferred = false;  // fragment shader samples images or is long
+    uint32_t tile_shift = 4;        // screen tile of the pipeline's modules
+    std::string source;  // generated CUDA translation unit of the per-draw module
 };
+
+// Tunables of a raster module, fixed at NVRTC time.
+struct ModuleConfig {
+    uint32_t tile_shift = 4;  // 8, 16 or 32 px tiles
+    bool deferred = false;    // fragment schedule
+    uint32_t warps = 8;       // warps per tile CTA (capped by the tile's pixels)
+    uint32_t batch = 128;     // primitives set up per shared-memory batch
+};
+
+// The CUDA translation unit of a module over one pipeline's stage block
+// (per-draw kernels) or several (batched kernels, pipeline i in namespace
+// cpv_p<i>).
+std::string compose_module(const std::vector<std::string>& stages, const std::vector<uint32_t>& nvs, const ModuleConfig& mc, bool batched);
 
 // ---- command recording ----
 enum class CmdType : uint8_t {
@@ -178,10 +195,23 @@ struct Cmd {
     VkViewport viewport{};
 };
 
+// Batched execution state of one render pass of a recorded command buffer
+// (built on its first execution, reused until the command buffer is reset).
+struct BatchState {
+    rt::Module* module = nullptr;  // owned by Device::batch_modules
+    std::unique_ptr<rt::BatchPlan> plan;
+    bool plain = false;            // not batchable: the per-draw path runs
+};
+
 struct CommandBuffer : Dispatchable {
     Device* device = nullptr;
     std::vector<Cmd> cmds;
     bool recording = false;
+    std::map<size_t, std::unique_ptr<BatchState>> batches;  // by BeginRenderPass command index
+    void reset() {
+        cmds.clear();
+        batches.clear();
+    }
 };
 
 struct CommandPool {
@@ -221,12 +251,23 @@ struct Device : Dispatchable {
     std::map<std::array<uint8_t, 32>, std::vector<uint8_t>> module_cache;  // in-process NVRTC cubin cache
     std::set<DeviceMemory*> memories;
     std::mutex memory_mutex;
+    // Batched modules by (pipeline keys, module configuration).
+    std::mutex batch_mutex;
+    std::map<std::string, std::unique_ptr<rt::Module>> batch_modules;
 };
+
+// The batched module over `pipelines` (module pipeline i = pipelines[i]),
+// compiled with NVRTC on first use and cached on the device. Null on error
+// (message in rt::last_error()).
+rt::Module* batch_module(Device* dev, const std::vector<Pipeline*>& pipelines, const ModuleConfig& mc);
 
 // Execution of a recorded command buffer on a queue (command.cpp).
 // no_alloc: draws bin through the fixed scratch array (rt::draw_plain_static)
 // instead of the queue's grow-only scratch.
 VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& written, bool no_alloc = false);
+// At vkEndCommandBuffer: compiles (NVRTC) and caches the batched module of
+// every render pass that will run batched, so its first submission does not.
+void precompile_batches(CommandBuffer* cb);
 // Checks, before any work is enqueued, that every draw of `cb` fits the fixed
 // scratch array (VK_ERROR_OUT_OF_DEVICE_MEMORY and a message otherwise).
 VkResult check_no_alloc(CommandBuffer* cb);

@@ -49,7 +49,125 @@ std::string hex(const std::array<uint8_t, 32>& k) {
 bool supported_colour(VkFormat f) { return f == VK_FORMAT_R8G8B8A8_UNORM || f == VK_FORMAT_B8G8R8A8_UNORM; }
 bool supported_depth(VkFormat f) { return f == VK_FORMAT_D16_UNORM || f == VK_FORMAT_D32_SFLOAT || f == VK_FORMAT_D32_SFLOAT_S8_UINT; }
 
+// Per-pipeline macros of a stage block, undefined after its namespace so the
+// next pipeline of a module can define its own.
+const char* const kStageMacros[] = {
+    "CPV_NV", "CPV_TOPOLOGY", "CPV_CULL_MODE", "CPV_FRONT_CW", "CPV_DEPTH_TEST", "CPV_DEPTH_WRITE", "CPV_DEPTH_OP", "CPV_STENCIL_TEST",
+    "CPV_ST_F_FAIL", "CPV_ST_F_PASS", "CPV_ST_F_DFAIL", "CPV_ST_F_OP", "CPV_ST_F_CMASK", "CPV_ST_F_WMASK", "CPV_ST_F_REF",
+    "CPV_ST_B_FAIL", "CPV_ST_B_PASS", "CPV_ST_B_DFAIL", "CPV_ST_B_OP", "CPV_ST_B_CMASK", "CPV_ST_B_WMASK", "CPV_ST_B_REF",
+    "CPV_BLEND", "CPV_SRC_COLOR", "CPV_DST_COLOR", "CPV_COLOR_OP", "CPV_SRC_ALPHA", "CPV_DST_ALPHA", "CPV_ALPHA_OP", "CPV_WRITE_MASK",
+    "CPV_COLOR_FORMAT", "CPV_DEPTH_FORMAT", "CPV_ORIGIN_UPPER",
+};
+
 }  // namespace
+
+std::string compose_module(const std::vector<std::string>& stages, const std::vector<uint32_t>& nvs, const ModuleConfig& mc, bool batched) {
+    uint32_t nv_max = 0;
+    for (uint32_t nv : nvs) nv_max = nv > nv_max ? nv : nv_max;
+    std::ostringstream src;
+    src << "// " << kTranslationVersion << (batched ? " (batched)" : "") << "\n";
+    src << "#define CPV_PIPELINE_MODULE 1\n";
+    src << "#define CPV_TILE_SHIFT " << mc.tile_shift << "\n";
+    src << "#define CPV_DEFERRED " << (mc.deferred ? 1 : 0) << "\n";
+    src << "#define CPV_RT_WARPS " << mc.warps << "\n";
+    src << "#define CPV_BATCH " << mc.batch << "\n";
+    src << "#define CPV_NV_MAX " << nv_max << "\n";
+    src << "#include \"cpv_device.cuh\"\n#include \"cpv_raster.cuh\"\n";
+    for (size_t i = 0; i < stages.size(); i++) {
+        src << "namespace cpv_p" << i << " {\n" << stages[i] << "#include \"cpv_stage.cuh\"\n";
+        for (const char* m : kStageMacros) src << "#undef " << m << "\n";
+        src << "}  // namespace cpv_p" << i << "\n";
+    }
+    if (!batched) {
+        src << "#include \"cpv_pipeline.cuh\"\n";
+    } else {
+        // Routes a primitive to its pipeline's stage functions.
+        src << "#define CPV_NUM_PIPELINES " << stages.size() << "\n";
+        src << "template <typename F> __device__ __forceinline__ void cpv_dispatch(uint32_t pid, F&& f) {\n  switch (pid) {\n";
+        for (size_t i = 1; i < stages.size(); i++) src << "  case " << i << ": f(cpv_p" << i << "::Stage()); break;\n";
+        src << "  default: f(cpv_p0::Stage()); break;\n  }\n}\n";
+        src << "#include \"cpv_batch.cuh\"\n";
+    }
+    return src.str();
+}
+
+namespace {
+
+// Cubin for a module source: device cache → disk cache (CPV_CACHE_DIR) →
+// NVRTC. The key hashes the source and the kernel headers it includes.
+bool module_cubin(Device* dev, const std::string& source, std::array<uint8_t, 32>& key, std::vector<uint8_t>& cubin) {
+    std::string keyed = source;
+    for (int i = 0; i < rt::kKernelHeaderCount; i++) keyed += rt::kKernelHeaderSources[i];
+    key = sha3_256(keyed.data(), keyed.size());
+    {
+        std::lock_guard<std::mutex> lock(dev->cache_mutex);
+        auto it = dev->module_cache.find(key);
+        if (it != dev->module_cache.end()) {
+            cubin = it->second;
+            return true;
+        }
+    }
+    const std::string dir = cache_dir();
+    bool found = false;
+    if (!dir.empty()) {
+        std::ifstream f(dir + "/" + hex(key) + ".cubin", std::ios::binary);
+        if (f) {
+            cubin.assign(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
+            found = !cubin.empty();
+        }
+    }
+    if (!found) {
+        std::string log;
+        if (rt::compile(source, "module_" + hex(key).substr(0, 12) + ".cu", cubin, log) != rt::kOk) {
+            rt::set_last_error("NVRTC failed: " + log);
+            return false;
+        }
+        if (!dir.empty()) {
+            std::ofstream f(dir + "/" + hex(key) + ".cubin", std::ios::binary);
+            f.write(reinterpret_cast<const char*>(cubin.data()), static_cast<std::streamsize>(cubin.size()));
+        }
+    }
+    std::lock_guard<std::mutex> lock(dev->cache_mutex);
+    dev->module_cache[key] = cubin;
+    return true;
+}
+
+}  // namespace
+
+rt::Module* batch_module(Device* dev, const std::vector<Pipeline*>& pipelines, const ModuleConfig& mc) {
+    std::string id = std::to_string(mc.tile_shift) + "/" + std::to_string(mc.deferred) + "/" + std::to_string(mc.warps) + "/" + std::to_string(mc.batch);
+    for (const Pipeline* p : pipelines) id += "/" + hex(p->key);
+    std::lock_guard<std::mutex> lock(dev->batch_mutex);
+    auto it = dev->batch_modules.find(id);
+    if (it != dev->batch_modules.end()) return it->second.get();
+    std::vector<std::string> stages;
+    std::vector<uint32_t> nvs;
+    for (const Pipeline* p : pipelines) {
+        stages.push_back(p->stage);
+        nvs.push_back(p->nv);
+    }
+    const std::string source = compose_module(stages, nvs, mc, true);
+    if (const char* dump = std::getenv("CPV_DUMP_DIR")) {
+        std::ofstream f(std::string(dump) + "/batch_" + std::to_string(pipelines.size()) + "_" + std::to_string(mc.tile_shift) + ".cu");
+        f << source;
+    }
+    std::array<uint8_t, 32> key{};
+    std::vector<uint8_t> cubin;
+    if (!module_cubin(dev, source, key, cubin)) return nullptr;
+    auto m = std::make_unique<rt::Module>();
+    std::string err;
+    if (dev->compile_only) {
+        rt::set_last_error("batched module compiled; no device to load it on");
+        return nullptr;
+    }
+    if (rt::load(cubin, mc.tile_shift, true, *m, err) != rt::kOk) {
+        rt::set_last_error("batched module load failed: " + err);
+        return nullptr;
+    }
+    rt::Module* out = m.get();
+    dev->batch_modules[id] = std::move(m);
+    return out;
+}
 
 VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGraphicsPipelineCreateInfo& ci, Pipeline** out) {
     auto reject = [&](const std::string& why) {
@@ -166,16 +284,15 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
 
     const uint32_t nv = vr.num_floats > fr.num_floats ? vr.num_floats : fr.num_floats;
     const uint32_t tile_shift = tile_shift_for_pipeline();
-    std::ostringstream src;
-    src << "// " << kTranslationVersion << "\n";
-    src << "#define CPV_PIPELINE_MODULE 1\n";
-    src << "#define CPV_TILE_SHIFT " << tile_shift << "\n";
     // Fragment schedule: deferred (dense shading) when the fragment shader
     // samples images or is long; immediate otherwise. CPV_DEFERRED=0/1
     // overrides (used by the autotuner and tests).
-    bool deferred = fr.samples > 0 || fr.instructions > 48;
+    const bool prefers_deferred = fr.samples > 0 || fr.instructions > 48;
+    bool deferred = prefers_deferred;
     if (const char* d = std::getenv("CPV_DEFERRED")) deferred = d[0] == '1';
-    src << "#define CPV_DEFERRED " << (deferred ? 1 : 0) << "\n";
+    // The pipeline's stage block: fixed-function macros, translated shaders
+    // and the interpolation table. compose_module() wraps it in a namespace.
+    std::ostringstream src;
     src << "#define CPV_NV " << nv << "\n";
     src << "#define CPV_TOPOLOGY " << static_cast<uint32_t>(topo) << "\n";
     src << "#define CPV_CULL_MODE " << rs.cullMode << "\n";
@@ -206,23 +323,26 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     src << "#define CPV_COLOR_FORMAT " << static_cast<uint32_t>(cfmt) << "\n";
     src << "#define CPV_DEPTH_FORMAT " << static_cast<uint32_t>(dfmt) << "\n";
     src << "#define CPV_ORIGIN_UPPER " << (fr.origin_upper_left ? 1 : 0) << "\n";
-    src << "#include \"cpv_device.cuh\"\n";
     src << vr.code << fr.code;
     src << "__device__ __forceinline__ int cpv_interp(int c) {\n  switch (c) {\n";
     for (size_t i = 0; i < fr.interp.size(); i++)
         if (fr.interp[i] != 0) src << "  case " << i << ": return " << fr.interp[i] << ";\n";
     src << "  default: return 0;\n  }\n}\n";
-    src << "#include \"cpv_pipeline.cuh\"\n";
 
     auto p = std::make_unique<Pipeline>();
-    p->source = src.str();
+    p->stage = src.str();
+    p->nv = nv;
+    p->prefers_deferred = prefers_deferred;
+    p->tile_shift = tile_shift;
+    ModuleConfig mc;
+    mc.tile_shift = tile_shift;
+    mc.deferred = deferred;
+    p->source = compose_module({p->stage}, {nv}, mc, false);
     // The key covers the generated source and the embedded kernel headers it
     // includes, so an on-disk cache never returns a cubin of older kernels.
     {
         std::string keyed = p->source;
-        keyed += rt::kDeviceHeaderSource;
-        keyed += rt::kPipelineHeaderSource;
-        keyed += rt::kParamsHeaderSource;
+        for (int i = 0; i < rt::kKernelHeaderCount; i++) keyed += rt::kKernelHeaderSources[i];
         p->key = sha3_256(keyed.data(), keyed.size());
     }
     if (const char* dump = std::getenv("CPV_DUMP_DIR")) {
@@ -291,7 +411,7 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
         *out = p.release();
         return VK_SUCCESS;
     }
-    if (rt::load(cubin, tile_shift, p->module, err) != rt::kOk) {
+    if (rt::load(cubin, tile_shift, false, p->module, err) != rt::kOk) {
         rt::set_last_error("module load failed: " + err);
         return VK_ERROR_INITIALIZATION_FAILED;
     }

@@ -200,6 +200,143 @@ extern "C" __global__ void cpv_scan_total(const uint32_t* __restrict__ in, const
     if (threadIdx.x == 0 && blockIdx.x == 0) *total = n ? out[n - 1] + in[n - 1] : 0u;
 }
 
+/* ---- batched binning: pairs, stable radix sort by tile, tile ranges ----
+ *
+ * The batched path bins every draw of a render pass at once. Set-up writes
+ * one tile rectangle per primitive and the pair count of each 256-primitive
+ * block; after an exclusive scan of the block counts, cpv_batch_emit writes
+ * the (tile, primitive) pairs in primitive order; a stable LSD radix sort by
+ * tile (8-bit digits, one or two passes) groups them by tile while keeping
+ * primitive (API) order inside each tile; cpv_tile_ranges records where each
+ * tile's run starts and ends. Sizes that depend on the data (the pair count)
+ * are read on the device, so the sequence has fixed launch shapes and can be
+ * captured in a CUDA graph. Pairs beyond the capacity are not written; the
+ * raster then scans the rectangles instead (same image). */
+
+#define CPV_RADIX_THREADS 256
+#define CPV_RADIX_DIGITS 256
+
+__device__ __forceinline__ uint32_t cpv_pairs_in_bounds(const uint32_t* pair_total, uint32_t capacity) {
+    const uint32_t p = *pair_total;
+    return p <= capacity ? p : 0u;
+}
+
+/* Block-wide exclusive sum over 256 threads. */
+__device__ __forceinline__ uint32_t cpv_block256_exclusive(uint32_t v, uint32_t* warp_sums /* [8] */) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= static_cast<uint32_t>(o)) incl += t;
+    }
+    if (lane == 31u) warp_sums[warp] = incl;
+    __syncthreads();
+    uint32_t base = 0;
+    for (uint32_t k = 0; k < warp; k++) base += warp_sums[k];
+    return base + incl - v;
+}
+
+/* One block per 256-primitive set-up block: the block's pairs at
+ * block_offsets[block] + (pairs of the block's earlier primitives). */
+extern "C" __global__ void __launch_bounds__(256) cpv_batch_emit(const uint2* __restrict__ rects, const uint32_t* __restrict__ block_offsets,
+                                                                 uint32_t tiles_x, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                                 uint32_t capacity, const uint32_t* __restrict__ pair_total) {
+    __shared__ uint32_t warp_sums[8];
+    const uint64_t g = static_cast<uint64_t>(blockIdx.x) * 256u + threadIdx.x;
+    const uint2 r = rects[g];
+    const uint32_t x0 = r.x & 0xFFFFu, y0 = r.x >> 16, x1 = r.y & 0xFFFFu, y1 = r.y >> 16;
+    const uint32_t w = x1 - x0;
+    const uint32_t n = w * (y1 - y0);
+    const uint32_t excl = cpv_block256_exclusive(n, warp_sums);
+    if (*pair_total > capacity) return;
+    const uint32_t base = block_offsets[blockIdx.x] + excl;
+    for (uint32_t k = 0; k < n; k++) {
+        const uint64_t pos = static_cast<uint64_t>(base) + k;
+        if (pos >= capacity) break;  /* only reachable if the pair total wrapped 32 bits */
+        const uint32_t ty = y0 + k / w, tx = x0 + k % w;
+        keys[pos] = ty * tiles_x + tx;
+        vals[pos] = static_cast<uint32_t>(g);
+    }
+}
+
+/* Contiguous item range of CTA c of `ctas` over n items. */
+__device__ __forceinline__ void cpv_cta_range(uint32_t n, uint32_t c, uint32_t ctas, uint32_t& begin, uint32_t& end) {
+    const uint32_t per = (n + ctas - 1u) / ctas;
+    const uint64_t b = static_cast<uint64_t>(per) * c, e = b + per;
+    begin = static_cast<uint32_t>(b < n ? b : n);
+    end = static_cast<uint32_t>(e < n ? e : n);
+}
+
+/* hist[digit * gridDim.x + cta] = items of the CTA's range with that digit. */
+extern "C" __global__ void __launch_bounds__(CPV_RADIX_THREADS) cpv_radix_hist(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ pair_total,
+                                                                               uint32_t capacity, uint32_t shift, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t counts[CPV_RADIX_DIGITS];
+    counts[threadIdx.x] = 0u;
+    __syncthreads();
+    uint32_t begin, end;
+    cpv_cta_range(cpv_pairs_in_bounds(pair_total, capacity), blockIdx.x, gridDim.x, begin, end);
+    for (uint32_t i = begin + threadIdx.x; i < end; i += CPV_RADIX_THREADS) atomicAdd(&counts[(keys[i] >> shift) & 0xFFu], 1u);
+    __syncthreads();
+    hist[threadIdx.x * gridDim.x + blockIdx.x] = counts[threadIdx.x];
+}
+
+/* Stable scatter: offsets = exclusive scan of hist (digit-major). Each CTA
+ * walks its range in order, 256 items at a time; an item's position is its
+ * digit's running offset plus the number of earlier items of the sub-chunk
+ * with the same digit (earlier warps, then earlier lanes). */
+extern "C" __global__ void __launch_bounds__(CPV_RADIX_THREADS) cpv_radix_scatter(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                                                                                  uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+                                                                                  const uint32_t* __restrict__ pair_total, uint32_t capacity, uint32_t shift,
+                                                                                  const uint32_t* __restrict__ offsets) {
+    __shared__ uint32_t running[CPV_RADIX_DIGITS];
+    __shared__ uint32_t warp_count[CPV_RADIX_THREADS / 32][CPV_RADIX_DIGITS];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    running[threadIdx.x] = offsets[threadIdx.x * gridDim.x + blockIdx.x];
+    uint32_t begin, end;
+    cpv_cta_range(cpv_pairs_in_bounds(pair_total, capacity), blockIdx.x, gridDim.x, begin, end);
+    for (uint32_t base = begin; base < end; base += CPV_RADIX_THREADS) {
+#pragma unroll
+        for (uint32_t w = 0; w < CPV_RADIX_THREADS / 32; w++) warp_count[w][threadIdx.x] = 0u;
+        __syncthreads();
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < end;
+        uint32_t key = 0, val = 0, digit = CPV_RADIX_DIGITS + lane;  /* invalid lanes never match a digit */
+        if (valid) {
+            key = keys_in[i];
+            val = vals_in[i];
+            digit = (key >> shift) & 0xFFu;
+        }
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, digit);
+        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && rank == 0u) warp_count[warp][digit] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = running[digit] + rank;
+            for (uint32_t w = 0; w < warp; w++) pos += warp_count[w][digit];
+            keys_out[pos] = key;
+            vals_out[pos] = val;
+        }
+        __syncthreads();
+        uint32_t add = 0;
+#pragma unroll
+        for (uint32_t w = 0; w < CPV_RADIX_THREADS / 32; w++) add += warp_count[w][threadIdx.x];
+        running[threadIdx.x] += add;
+        __syncthreads();
+    }
+}
+
+/* tile_begin / tile_end (zeroed beforehand) from the sorted keys. */
+extern "C" __global__ void __launch_bounds__(256) cpv_tile_ranges(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ pair_total,
+                                                                  uint32_t capacity, uint32_t* __restrict__ tile_begin, uint32_t* __restrict__ tile_end) {
+    const uint32_t n = cpv_pairs_in_bounds(pair_total, capacity);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = keys[i];
+        if (i == 0u || keys[i - 1u] != k) tile_begin[k] = i;
+        if (i + 1u == n || keys[i + 1u] != k) tile_end[k] = i + 1u;
+    }
+}
+
 /* ---- fills ---- */
 
 extern "C" __global__ void __launch_bounds__(256) cpv_fill_u32(uint32_t* __restrict__ dst, uint64_t count, uint32_t value) {

@@ -92,4 +92,39 @@ struct CpvDrawParams {
     uint32_t* status;
 };
 
+/* Primitives per set-up block of the batched path: every draw of a batch
+ * starts at a multiple of this in the batch's primitive index space, so a
+ * primitive index g belongs to block g / CPV_BATCH_BLOCK and that block to
+ * exactly one draw. */
+#define CPV_BATCH_BLOCK 256u
+
+/* Everything the batched kernels read: the draws of one render pass, their
+ * tables and the binning buffers. Passed by value as a kernel argument. */
+struct CpvBatchParams {
+    const struct CpvDrawParams* draws; /* per draw (device array) */
+    const uint32_t* draw_pipeline;     /* per draw: pipeline index in the module */
+    const uint32_t* draw_block;        /* per draw + 1: first set-up block */
+    const uint32_t* block_draw;        /* per set-up block: its draw */
+    uint32_t num_draws;
+    uint32_t total_blocks;
+    /* shared attachments and pixel-centre grid of the render pass */
+    uint8_t* color;
+    uint8_t* depth;
+    uint32_t fb_width, fb_height;
+    float vw, vh;
+    uint32_t tiles_x, tiles_y;
+    /* binning */
+    uint2* rects;                 /* per primitive tile rectangle, packed */
+    uint32_t* block_pairs;        /* per set-up block: (primitive, tile) pairs */
+    const uint32_t* block_offsets;/* exclusive scan of block_pairs */
+    const uint32_t* pair_total;   /* device word: pairs of the batch */
+    uint32_t pair_capacity;
+    uint32_t pad0;
+    const uint32_t* sorted_prims; /* pair primitives sorted by tile, API order within a tile */
+    const uint32_t* tile_begin;   /* per tile: range in sorted_prims */
+    const uint32_t* tile_end;
+    uint32_t* tile_counter;       /* persistent raster work queue */
+    uint32_t* status;
+};
+
 #endif /* CPV_PARAMS_H */

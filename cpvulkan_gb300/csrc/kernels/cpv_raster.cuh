@@ -1,0 +1,385 @@
+/*
+ * cpv_raster.cuh — the pipeline-independent part of the tile rasteriser,
+ * shared by the per-draw module (cpv_pipeline.cuh) and the batched module
+ * (cpv_batch.cuh). Compiled by NVRTC after cpv_device.cuh; the module prefix
+ * defines CPV_TILE_SHIFT, CPV_DEFERRED and CPV_NV_MAX (the largest varying
+ * count over the module's pipelines).
+ *
+ * The per-pipeline part (primitive set-up, fragment shading and the
+ * per-fragment operations, which depend on the pipeline's shaders and
+ * fixed-function state) is cpv_stage.cuh, instantiated once per pipeline in
+ * its own namespace. cpv_raster_tile() walks one screen tile's primitives
+ * through a Source object that supplies the primitives in API order and
+ * routes each to its pipeline's stage functions.
+ */
+#ifndef CPV_RASTER_CUH
+#define CPV_RASTER_CUH
+
+#ifndef CPV_TILE_SHIFT
+#define CPV_TILE_SHIFT 4
+#endif
+#ifndef CPV_DEFERRED
+#define CPV_DEFERRED 0
+#endif
+#ifndef CPV_RT_WARPS
+#define CPV_RT_WARPS 8
+#endif
+#ifndef CPV_BATCH
+#define CPV_BATCH 128
+#endif
+#define CPV_TILE (1 << CPV_TILE_SHIFT)
+#define CPV_RT_THREADS ((CPV_TILE * CPV_TILE) < (32 * CPV_RT_WARPS) ? (CPV_TILE * CPV_TILE) : (32 * CPV_RT_WARPS))
+#define CPV_PPT ((CPV_TILE * CPV_TILE) / CPV_RT_THREADS)
+#define CPV_ROWS_PER_PASS (CPV_RT_THREADS / CPV_TILE)
+#define CPV_NV_ALLOC (CPV_NV_MAX > 0 ? CPV_NV_MAX : 1)
+#define CPV_NV_PAD ((CPV_NV_ALLOC + 3) & ~3)
+#define CPV_SLOTS 4
+#define CPV_NSLOT (CPV_RT_THREADS * CPV_SLOTS)
+
+/* One primitive after set-up, in the reference's terms
+ * (CPVulkan/CommandBuffer.Draw.cpp:1510-1594, 874-954). 16-byte aligned
+ * groups so that the coverage loop reads them with 128-bit loads. */
+struct __align__(16) CpvTri {
+    float4 e[3];     /* edge k: start vertex (x, y) and b - a (dx, dy), NDC */
+    int4 box;        /* pixel bounding box x0, y0, x1, y1 (end exclusive) */
+    float4 za;       /* NDC z of p0..p2 (after the CW swap), |area| */
+    float4 wf;       /* clip w of p0..p2, flags (see below) */
+    float var[3][CPV_NV_PAD];
+};
+
+/* Flag word (wf.w bits): 1 live, 2 front facing, bits 2-5 pipeline index in
+ * the module, bits 6-7 provoking-vertex slot, bits 8-31 draw index in the
+ * batch (0 for a per-draw module). */
+__device__ __forceinline__ uint32_t cpv_tri_flags(const CpvTri& t) { return __float_as_uint(t.wf.w); }
+__device__ __forceinline__ bool cpv_tri_live(const CpvTri& t) { return (cpv_tri_flags(t) & 1u) != 0u; }
+__device__ __forceinline__ bool cpv_tri_front(const CpvTri& t) { return (cpv_tri_flags(t) & 2u) != 0u; }
+__device__ __forceinline__ uint32_t cpv_tri_pipeline(const CpvTri& t) { return (cpv_tri_flags(t) >> 2) & 15u; }
+__device__ __forceinline__ uint32_t cpv_tri_pslot(const CpvTri& t) { return (cpv_tri_flags(t) >> 6) & 3u; }
+__device__ __forceinline__ uint32_t cpv_tri_draw(const CpvTri& t) { return cpv_tri_flags(t) >> 8; }
+__device__ __forceinline__ void cpv_tri_tag(CpvTri& t, uint32_t pipeline, uint32_t draw) {
+    t.wf.w = __uint_as_float((cpv_tri_flags(t) & 0xC3u) | (pipeline << 2) | (draw << 8));
+}
+
+/* Pixel centre in NDC (CPVulkan/CommandBuffer.Draw.cpp:1524, 1573-1580):
+ * (x / width + halfPixel) * 2 - 1, halfPixel = (1 / width) * 0.5. */
+__device__ __forceinline__ float cpv_pixel_ndc(int32_t x, float extent) {
+    const float half = __fmul_rn(__fdiv_rn(1.0f, extent), 0.5f);
+    return __fsub_rn(__fmul_rn(__fadd_rn(__fdiv_rn(static_cast<float>(x), extent), half), 2.0f), 1.0f);
+}
+
+/* Edge functions at a pixel centre (CPVulkan/CommandBuffer.Draw.cpp:882-902):
+ * w_k = (p.x - a.x) * (b.y - a.y) - (p.y - a.y) * (b.x - a.x); covered when
+ * no w_k is negative (inclusive on every edge). */
+__device__ __forceinline__ bool cpv_covers(const CpvTri& t, float xf, float yf, float w[3]) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float4 e = t.e[k];
+        const float t0 = __fmul_rn(__fsub_rn(xf, e.x), e.w);
+        const float t1 = __fmul_rn(__fsub_rn(yf, e.y), e.z);
+        w[k] = __fsub_rn(t0, t1);
+    }
+    return !(w[0] < 0.0f || w[1] < 0.0f || w[2] < 0.0f);
+}
+
+/* Tile rectangle of a set-up primitive (empty when culled, off screen, or
+ * when a bounding box of at most four pixels covers none of its pixel
+ * centres — the raster would find no fragment there either). Packed as
+ * x0 | y0 << 16, x1 | y1 << 16 in tile units, end exclusive. */
+__device__ __forceinline__ uint2 cpv_tile_rect(const CpvTri& t, float vw, float vh) {
+    uint32_t r[4] = {0, 0, 0, 0};
+    if (cpv_tri_live(t)) {
+        bool any = true;
+        const int4 b = t.box;
+        if ((b.z - b.x) * (b.w - b.y) <= 4) {
+            any = false;
+            for (int32_t y = b.y; y < b.w; y++) {
+                const float yf = cpv_pixel_ndc(y, vh);
+                for (int32_t x = b.x; x < b.z; x++) {
+                    float w[3];
+                    if (cpv_covers(t, cpv_pixel_ndc(x, vw), yf, w)) any = true;
+                }
+            }
+        }
+        if (any) {
+            r[0] = static_cast<uint32_t>(b.x >> CPV_TILE_SHIFT);
+            r[1] = static_cast<uint32_t>(b.y >> CPV_TILE_SHIFT);
+            r[2] = static_cast<uint32_t>(((b.z - 1) >> CPV_TILE_SHIFT) + 1);
+            r[3] = static_cast<uint32_t>(((b.w - 1) >> CPV_TILE_SHIFT) + 1);
+        }
+    }
+    return make_uint2(r[0] | (r[1] << 16), r[2] | (r[3] << 16));
+}
+
+/* ---- per-fragment operation helpers (LLVMRuntime/PipelineCompiler.cpp:1020-1429) ---- */
+
+__device__ __forceinline__ bool cpv_fcompare(float a, float b, uint32_t op) {
+    switch (op) {
+    case 0: return false;
+    case 1: return a < b;
+    case 2: return a == b;
+    case 3: return a <= b;
+    case 4: return a > b;
+    case 5: return (a < b) || (a > b);
+    case 6: return a >= b;
+    default: return true;
+    }
+}
+
+__device__ __forceinline__ bool cpv_icompare(uint32_t a, uint32_t b, uint32_t op) {
+    switch (op) {
+    case 0: return false;
+    case 1: return a < b;
+    case 2: return a == b;
+    case 3: return a <= b;
+    case 4: return a > b;
+    case 5: return a != b;
+    case 6: return a >= b;
+    default: return true;
+    }
+}
+
+/* Stencil ops; increment/decrement-and-clamp saturate as signed i8
+ * (LLVMRuntime/PipelineCompiler.cpp:1382-1413). */
+__device__ __forceinline__ uint32_t cpv_stencil_op(uint32_t op, uint32_t cur, uint32_t ref) {
+    const int32_t sc = static_cast<int8_t>(cur);
+    switch (op) {
+    case 0: return cur;
+    case 1: return 0u;
+    case 2: return ref & 0xFFu;
+    case 3: return static_cast<uint32_t>(static_cast<uint8_t>(sc == 127 ? 127 : sc + 1));
+    case 4: return static_cast<uint32_t>(static_cast<uint8_t>(sc == -128 ? -128 : sc - 1));
+    case 5: return (~cur) & 0xFFu;
+    case 6: return (cur + 1u) & 0xFFu;
+    case 7: return (cur - 1u) & 0xFFu;
+    default: return cur;
+    }
+}
+
+/* ApplyBlendFactor / ApplyBlend (CPVulkan/CommandBuffer.Draw.cpp:956-1262). */
+__device__ __forceinline__ void cpv_blend_factor(const float s[4], const float d[4], const float c[4], uint32_t cf, uint32_t af, float o[4]) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) o[i] = 0.0f;
+    switch (cf) {
+    case 0: break;
+    case 1: for (int i = 0; i < 4; i++) o[i] = 1.0f; break;
+    case 2: for (int i = 0; i < 4; i++) o[i] = s[i]; break;
+    case 3: for (int i = 0; i < 4; i++) o[i] = __fsub_rn(1.0f, s[i]); break;
+    case 4: for (int i = 0; i < 4; i++) o[i] = d[i]; break;
+    case 5: for (int i = 0; i < 4; i++) o[i] = __fsub_rn(1.0f, d[i]); break;
+    case 6: for (int i = 0; i < 4; i++) o[i] = s[3]; break;
+    case 7: { const float v = __fsub_rn(1.0f, s[3]); for (int i = 0; i < 4; i++) o[i] = v; break; }
+    case 8: for (int i = 0; i < 4; i++) o[i] = d[3]; break;
+    case 9: { const float v = __fsub_rn(1.0f, d[3]); for (int i = 0; i < 4; i++) o[i] = v; break; }
+    case 10: for (int i = 0; i < 4; i++) o[i] = c[i]; break;
+    case 11: for (int i = 0; i < 4; i++) o[i] = __fsub_rn(1.0f, c[i]); break;
+    case 12: for (int i = 0; i < 4; i++) o[i] = c[3]; break;
+    case 13: { const float v = __fsub_rn(1.0f, c[3]); for (int i = 0; i < 4; i++) o[i] = v; break; }
+    case 14: { const float f = cpv_std_min(s[3], __fsub_rn(1.0f, d[3])); o[0] = f; o[1] = f; o[2] = f; o[3] = 1.0f; break; }
+    default: break;
+    }
+    if (cf != af) {
+        switch (af) {
+        case 0: o[3] = 0.0f; break;
+        case 1: case 14: o[3] = 1.0f; break;
+        case 2: case 6: o[3] = s[3]; break;
+        case 3: case 7: o[3] = __fsub_rn(1.0f, s[3]); break;
+        case 4: case 8: o[3] = d[3]; break;
+        case 5: case 9: o[3] = __fsub_rn(1.0f, d[3]); break;
+        case 10: case 12: o[3] = c[3]; break;
+        case 11: case 13: o[3] = __fsub_rn(1.0f, c[3]); break;
+        default: break;
+        }
+    }
+}
+
+__device__ __forceinline__ float cpv_blend_op(float s, float sf, float d, float df, uint32_t op) {
+    const float a = __fmul_rn(s, sf);
+    const float b = __fmul_rn(d, df);
+    switch (op) {
+    case 0: return __fadd_rn(a, b);
+    case 1: return __fsub_rn(a, b);
+    case 2: return __fsub_rn(b, a);
+    case 3: return cpv_std_min(s, d);
+    case 4: return cpv_std_max(s, d);
+    default: return 0.0f;
+    }
+}
+
+/* Register-resident attachment state of one pixel. */
+struct CpvPixel {
+    uint32_t colour;
+    float depth;        /* decoded depth (D16: u16 / 65535) */
+    uint32_t depth_raw; /* stored bits */
+    uint32_t stencil;
+};
+
+/* Block-wide exclusive sum over CPV_RT_THREADS threads. */
+__device__ __forceinline__ uint32_t cpv_block_scan(uint32_t v, uint32_t& total, uint32_t* warp_sums) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= static_cast<uint32_t>(o)) incl += t;
+    }
+    if (lane == 31u) warp_sums[warp] = incl;
+    __syncthreads();
+    uint32_t base = 0, sum = 0;
+    for (uint32_t k = 0; k < CPV_RT_THREADS / 32; k++) {
+        const uint32_t s = warp_sums[k];
+        if (k < warp) base += s;
+        sum += s;
+    }
+    total = sum;
+    return base + incl - v;
+}
+
+/* Dynamic shared memory of the raster kernels: CPV_BATCH primitives, then
+ * (deferred schedule) the fragment slots. */
+#define CPV_RASTER_SMEM_BYTES (CPV_BATCH * sizeof(CpvTri) + (CPV_DEFERRED ? CPV_NSLOT * (4u + 20u + 2u) : 0u))
+
+/* One screen tile (tx, ty): loads the tile's attachment texels into
+ * registers, walks the tile's primitives from `src` in API order in batches
+ * of CPV_BATCH (set-up into shared memory, then coverage, shading and the
+ * per-fragment operations of each pixel in primitive order) and stores the
+ * texels back once.
+ *
+ * Source supplies:
+ *   uint64_t count()                         primitives of this tile
+ *   void setup(uint64_t i, CpvTri& t)        set up the i-th (or mark it dead)
+ *   bool shade(const CpvTri&, const float w[3], int x, int y, float colour[4], float& mapped)
+ *   void rop(const CpvTri&, const float colour[4], float mapped, CpvPixel&)
+ *   void load_pixel(uint64_t pix, CpvPixel&) / store_pixel(uint64_t pix, const CpvPixel&)
+ *   float vw, vh                             viewport extent (pixel centres)
+ *   uint32_t fb_width, fb_height
+ *
+ * Two fragment schedules (CPV_DEFERRED):
+ *   immediate — each pixel's thread shades its covered fragments as it finds
+ *               them (cheap shaders, large primitives);
+ *   deferred  — per batch of primitives, threads first record up to
+ *               CPV_SLOTS covered fragments each, the CTA then shades all
+ *               recorded fragments densely (full warps, whatever the
+ *               coverage pattern), and finally every pixel's thread applies
+ *               its own fragments' per-fragment operations in primitive
+ *               order (expensive shaders, small primitives).
+ * Both apply each pixel's fragments in API primitive order, as the
+ * reference's serial loop does. */
+template <class Source>
+__device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32_t ty, CpvTri* tris, uint32_t* warp_sums) {
+    const uint64_t end = src.count();
+    if (end == 0) return;
+    int32_t px[CPV_PPT], py[CPV_PPT];
+    float xf[CPV_PPT], yf[CPV_PPT];
+    bool inside[CPV_PPT];
+    CpvPixel st[CPV_PPT];
+#pragma unroll
+    for (int k = 0; k < CPV_PPT; k++) {
+        px[k] = static_cast<int32_t>(tx * CPV_TILE + (threadIdx.x % CPV_TILE));
+        py[k] = static_cast<int32_t>(ty * CPV_TILE + (threadIdx.x / CPV_TILE) + k * CPV_ROWS_PER_PASS);
+        inside[k] = px[k] < static_cast<int32_t>(src.fb_width) && py[k] < static_cast<int32_t>(src.fb_height);
+        xf[k] = cpv_pixel_ndc(px[k], src.vw);
+        yf[k] = cpv_pixel_ndc(py[k], src.vh);
+        if (inside[k]) src.load_pixel(static_cast<uint64_t>(py[k]) * src.fb_width + px[k], st[k]);
+    }
+
+#if CPV_DEFERRED
+    uint8_t* slot_base = reinterpret_cast<uint8_t*>(tris + CPV_BATCH);
+    uint32_t* slot_jk = reinterpret_cast<uint32_t*>(slot_base);          /* batch index | pixel k << 8 | discard << 31 */
+    float* slot_f = reinterpret_cast<float*>(slot_jk + CPV_NSLOT);       /* 5 floats per slot: w0 w1 w2 → rgba + mapped */
+    uint16_t* dense = reinterpret_cast<uint16_t*>(slot_f + 5 * CPV_NSLOT);
+#endif
+
+    for (uint64_t base = 0; base < end; base += CPV_BATCH) {
+        const uint32_t n = static_cast<uint32_t>((end - base) < CPV_BATCH ? (end - base) : CPV_BATCH);
+        __syncthreads();
+        /* a tile of 8 × 8 has fewer threads than CPV_BATCH: stride the set-up */
+        for (uint32_t i = threadIdx.x; i < n; i += CPV_RT_THREADS) src.setup(base + i, tris[i]);
+        __syncthreads();
+#if !CPV_DEFERRED
+        for (uint32_t j = 0; j < n; j++) {
+            const CpvTri& t = tris[j];
+            if (!cpv_tri_live(t)) continue;
+            const int4 box = t.box;
+#pragma unroll
+            for (int k = 0; k < CPV_PPT; k++) {
+                if (!inside[k]) continue;
+                if (px[k] < box.x || px[k] >= box.z || py[k] < box.y || py[k] >= box.w) continue;
+                float w[3];
+                if (!cpv_covers(t, xf[k], yf[k], w)) continue;
+                float colour[4], mapped;
+                if (src.shade(t, w, px[k], py[k], colour, mapped)) continue;
+                src.rop(t, colour, mapped, st[k]);
+            }
+        }
+#else
+        const uint32_t limit = n * CPV_PPT;
+        uint32_t cursor = 0;
+        while (__syncthreads_or(cursor < limit)) {
+            /* 1. coverage: record up to CPV_SLOTS fragments, in primitive order */
+            uint32_t cnt = 0;
+            while (cursor < limit && cnt < CPV_SLOTS) {
+                const uint32_t j = cursor / CPV_PPT, k = cursor - j * CPV_PPT;
+                cursor++;
+                const CpvTri& t = tris[j];
+                if (!cpv_tri_live(t)) continue;
+                int32_t pxk = px[0], pyk = py[0];
+                float xfk = xf[0], yfk = yf[0];
+                bool ink = inside[0];
+#pragma unroll
+                for (int kk = 1; kk < CPV_PPT; kk++)
+                    if (k == static_cast<uint32_t>(kk)) { pxk = px[kk]; pyk = py[kk]; xfk = xf[kk]; yfk = yf[kk]; ink = inside[kk]; }
+                const int4 box = t.box;
+                if (!ink || pxk < box.x || pxk >= box.z || pyk < box.y || pyk >= box.w) continue;
+                float w[3];
+                if (!cpv_covers(t, xfk, yfk, w)) continue;
+                const uint32_t s = threadIdx.x * CPV_SLOTS + cnt;
+                slot_jk[s] = j | (k << 8);
+                slot_f[5 * s + 0] = w[0];
+                slot_f[5 * s + 1] = w[1];
+                slot_f[5 * s + 2] = w[2];
+                cnt++;
+            }
+            /* 2. dense shading of every recorded fragment */
+            uint32_t total;
+            const uint32_t pos = cpv_block_scan(cnt, total, warp_sums);
+            for (uint32_t i = 0; i < cnt; i++) dense[pos + i] = static_cast<uint16_t>(threadIdx.x * CPV_SLOTS + i);
+            __syncthreads();
+            for (uint32_t d = threadIdx.x; d < total; d += CPV_RT_THREADS) {
+                const uint32_t s = dense[d];
+                const uint32_t owner = s / CPV_SLOTS;
+                const uint32_t jk = slot_jk[s];
+                const uint32_t j = jk & 0xFFu, k = (jk >> 8) & 0xFFu;
+                const int32_t x = static_cast<int32_t>(tx * CPV_TILE + (owner % CPV_TILE));
+                const int32_t y = static_cast<int32_t>(ty * CPV_TILE + (owner / CPV_TILE) + k * CPV_ROWS_PER_PASS);
+                const float w[3] = {slot_f[5 * s + 0], slot_f[5 * s + 1], slot_f[5 * s + 2]};
+                float colour[4], mapped;
+                const bool discard = src.shade(tris[j], w, x, y, colour, mapped);
+                slot_f[5 * s + 0] = colour[0];
+                slot_f[5 * s + 1] = colour[1];
+                slot_f[5 * s + 2] = colour[2];
+                slot_f[5 * s + 3] = colour[3];
+                slot_f[5 * s + 4] = mapped;
+                if (discard) slot_jk[s] = jk | 0x80000000u;
+            }
+            __syncthreads();
+            /* 3. per-fragment operations of this thread's pixels, in order */
+            for (uint32_t i = 0; i < cnt; i++) {
+                const uint32_t s = threadIdx.x * CPV_SLOTS + i;
+                const uint32_t jk = slot_jk[s];
+                if (jk >> 31) continue;
+                const uint32_t j = jk & 0xFFu, k = (jk >> 8) & 0xFFu;
+                const float colour[4] = {slot_f[5 * s + 0], slot_f[5 * s + 1], slot_f[5 * s + 2], slot_f[5 * s + 3]};
+#pragma unroll
+                for (int kk = 0; kk < CPV_PPT; kk++)
+                    if (k == static_cast<uint32_t>(kk)) src.rop(tris[j], colour, slot_f[5 * s + 4], st[kk]);
+            }
+        }
+#endif
+    }
+#pragma unroll
+    for (int k = 0; k < CPV_PPT; k++) {
+        if (inside[k]) src.store_pixel(static_cast<uint64_t>(py[k]) * src.fb_width + px[k], st[k]);
+    }
+}
+
+#endif /* CPV_RASTER_CUH */

@@ -1,0 +1,287 @@
+/*
+ * cpv_stage.cuh — the per-pipeline stage functions. Deliberately without an
+ * include guard: the module source includes it once per pipeline, inside
+ * that pipeline's namespace (cpv_p0, cpv_p1, …), after the pipeline's
+ * fixed-function macros (CPV_TOPOLOGY, CPV_CULL_MODE, CPV_FRONT_CW,
+ * CPV_DEPTH_*, CPV_STENCIL_TEST, CPV_ST_*, CPV_BLEND, CPV_SRC_* / CPV_DST_*,
+ * CPV_*_OP, CPV_WRITE_MASK, CPV_COLOR_FORMAT, CPV_DEPTH_FORMAT,
+ * CPV_ORIGIN_UPPER, CPV_NV) and its translated shaders:
+ *
+ *   __device__ void cpv_vs_run(const CpvDrawParams&, uint32_t vertex_index,
+ *                              uint32_t instance_index, float pos[4], float var[CPV_NV]);
+ *   __device__ bool cpv_fs_run(const CpvDrawParams&, const float in[CPV_NV],
+ *                              const float frag_coord[4], bool front, float colour[4]);
+ *   __device__ int  cpv_interp(int component);  // 0 perspective, 1 linear, 2 flat
+ *
+ * Vertex shading is recomputed where it is needed (set-up and raster) instead
+ * of being stored: a vertex shader is a pure function of its inputs, and the
+ * reference itself shades every assembled vertex (one per index), so the
+ * recomputation is arithmetic the reference also performs and costs no HBM
+ * traffic for a vertex-output buffer.
+ */
+
+/* Primitive set-up: vertex shading of the three vertices, perspective divide,
+ * screen bounding box, area, facing and cull. `g` is the primitive index
+ * within the draw (all instances). */
+template <bool WITH_VARYINGS>
+__device__ __forceinline__ void cpv_setup(const CpvDrawParams& P, uint64_t g, CpvTri& t) {
+    const uint32_t ppi = P.prims_per_instance;
+    const uint32_t g32 = static_cast<uint32_t>(g);  /* draws hold < 2^32 primitives */
+    const uint32_t inst = P.instance_count > 1u ? g32 / ppi : 0u;
+    const uint32_t instance = P.first_instance + inst;
+    const uint32_t p = g32 - inst * ppi;
+    uint32_t raw[3], provoking;
+    cpv_prim_vertices(CPV_TOPOLOGY, p, raw, provoking);
+#if CPV_FRONT_CW
+    { const uint32_t tmp = raw[0]; raw[0] = raw[2]; raw[2] = tmp; }
+#endif
+    const uint32_t pslot = raw[0] == provoking ? 0u : (raw[1] == provoking ? 1u : 2u);
+    float Pn[3][4];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float pos[4];
+        float var[CPV_NV_ALLOC];
+        cpv_vs_run(P, cpv_vertex_id(P, raw[k]), instance, pos, var);
+        const float w = pos[3];
+        Pn[k][0] = __fdiv_rn(pos[0], w);
+        Pn[k][1] = __fdiv_rn(pos[1], w);
+        Pn[k][2] = __fdiv_rn(pos[2], w);
+        Pn[k][3] = w;
+        if (WITH_VARYINGS) {
+#pragma unroll
+            for (int c = 0; c < CPV_NV; c++) t.var[k][c] = var[c];
+        }
+    }
+    const float vw = P.viewport[2], vh = P.viewport[3];
+    int32_t sx[3], sy[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        sx[k] = cpv_f2i(__fmul_rn(__fmul_rn(__fadd_rn(Pn[k][0], 1.0f), 0.5f), vw));
+        sy[k] = cpv_f2i(__fmul_rn(__fmul_rn(__fadd_rn(Pn[k][1], 1.0f), 0.5f), vh));
+    }
+    const int64_t minx = min(sx[0], min(sx[1], sx[2]));
+    const int64_t miny = min(sy[0], min(sy[1], sy[2]));
+    const int64_t maxx = max(sx[0], max(sx[1], sx[2]));
+    const int64_t maxy = max(sy[0], max(sy[1], sy[2]));
+    int64_t x0 = minx > 0 ? minx : 0, y0 = miny > 0 ? miny : 0;
+    int64_t x1 = maxx + 1, y1 = maxy + 1;
+    const int64_t iw = cpv_f2i(vw), ih = cpv_f2i(vh);
+    x1 = x1 < iw ? x1 : iw;
+    y1 = y1 < ih ? y1 : ih;
+    x1 = x1 < static_cast<int64_t>(P.fb_width) ? x1 : static_cast<int64_t>(P.fb_width);
+    y1 = y1 < static_cast<int64_t>(P.fb_height) ? y1 : static_cast<int64_t>(P.fb_height);
+    int4 box;
+    box.x = static_cast<int32_t>(x0);
+    box.y = static_cast<int32_t>(y0);
+    box.z = static_cast<int32_t>(x1 > x0 ? x1 : x0);
+    box.w = static_cast<int32_t>(y1 > y0 ? y1 : y0);
+    t.box = box;
+
+    float area = cpv_edge(Pn[0][0], Pn[0][1], Pn[1][0], Pn[1][1], Pn[2][0], Pn[2][1]);
+    /* Edges (a → b): front (area >= 0) w0 = E(p1,p2), w1 = E(p2,p0), w2 = E(p0,p1);
+     * back: w0 = E(p2,p1), w1 = E(p0,p2), w2 = E(p1,p0) (Draw.cpp:882-898).
+     * Selected with constant indices so the vertices stay in registers. */
+    const bool front = !(area < 0.0f);
+    if (!front) area = -area;
+    const int fa[3] = {1, 2, 0}, fb[3] = {2, 0, 1};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float ax = front ? Pn[fa[k]][0] : Pn[fb[k]][0];
+        const float ay = front ? Pn[fa[k]][1] : Pn[fb[k]][1];
+        const float bx = front ? Pn[fb[k]][0] : Pn[fa[k]][0];
+        const float by = front ? Pn[fb[k]][1] : Pn[fa[k]][1];
+        t.e[k] = make_float4(ax, ay, __fsub_rn(bx, ax), __fsub_rn(by, ay));
+    }
+    t.za = make_float4(Pn[0][2], Pn[1][2], Pn[2][2], area);
+    bool live = box.z > box.x && box.w > box.y;
+    if ((CPV_CULL_MODE & 2) && !front) live = false;
+    if ((CPV_CULL_MODE & 1) && front) live = false;
+    const uint32_t flags = (live ? 1u : 0u) | (front ? 2u : 0u) | (pslot << 6);
+    t.wf = make_float4(Pn[0][3], Pn[1][3], Pn[2][3], __uint_as_float(flags));
+}
+
+/* Byte offset of channel i in the colour attachment texel
+ * (CPVulkanBase/Formats.cpp:248,255). */
+__device__ __forceinline__ int cpv_channel_shift(int i) {
+#if CPV_COLOR_FORMAT == 44
+    return i == 0 ? 16 : (i == 1 ? 8 : (i == 2 ? 0 : 24));
+#else
+    return 8 * i;
+#endif
+}
+
+__device__ __forceinline__ void cpv_load_pixel(const uint8_t* color, const uint8_t* depth, uint64_t pix, CpvPixel& s) {
+    s.colour = reinterpret_cast<const uint32_t*>(color)[pix];
+#if CPV_DEPTH_FORMAT == 124
+    s.depth_raw = reinterpret_cast<const uint16_t*>(depth)[pix];
+    s.depth = cpv_decode_unorm16(s.depth_raw);
+    s.stencil = 0u;
+#elif CPV_DEPTH_FORMAT == 126
+    s.depth_raw = reinterpret_cast<const uint32_t*>(depth)[pix];
+    s.depth = __uint_as_float(s.depth_raw);
+    s.stencil = 0u;
+#elif CPV_DEPTH_FORMAT == 130
+    const uint2 v = reinterpret_cast<const uint2*>(depth)[pix];
+    s.depth_raw = v.x;
+    s.depth = __uint_as_float(v.x);
+    s.stencil = v.y & 0xFFu;
+#else
+    (void)depth;
+    s.depth_raw = 0u;
+    s.depth = 0.0f;
+    s.stencil = 0u;
+#endif
+}
+
+__device__ __forceinline__ void cpv_store_pixel(uint8_t* color, uint8_t* depth, uint64_t pix, const CpvPixel& s) {
+    reinterpret_cast<uint32_t*>(color)[pix] = s.colour;
+#if CPV_DEPTH_FORMAT == 124
+    reinterpret_cast<uint16_t*>(depth)[pix] = static_cast<uint16_t>(s.depth_raw);
+#elif CPV_DEPTH_FORMAT == 126
+    reinterpret_cast<uint32_t*>(depth)[pix] = s.depth_raw;
+#elif CPV_DEPTH_FORMAT == 130
+    uint2* p = reinterpret_cast<uint2*>(depth) + pix;
+    uint2 v = *p;
+    v.x = s.depth_raw;
+    v.y = (v.y & ~0xFFu) | (s.stencil & 0xFFu);
+    *p = v;
+#else
+    (void)depth;
+#endif
+}
+
+__device__ __forceinline__ void cpv_write_depth(CpvPixel& s, float mapped) {
+#if CPV_DEPTH_FORMAT == 124
+    s.depth_raw = cpv_encode_unorm(mapped, 65535.0f);
+    s.depth = cpv_decode_unorm16(s.depth_raw);
+#else
+    s.depth_raw = __float_as_uint(mapped);
+    s.depth = mapped;
+#endif
+}
+
+__device__ __forceinline__ void cpv_blend(const float s[4], const float d[4], const float c[4], float out[4]) {
+    float sf[4], df[4];
+    cpv_blend_factor(s, d, c, CPV_SRC_COLOR, CPV_SRC_ALPHA, sf);
+    cpv_blend_factor(s, d, c, CPV_DST_COLOR, CPV_DST_ALPHA, df);
+#pragma unroll
+    for (int i = 0; i < 4; i++) out[i] = cpv_blend_op(s[i], sf[i], d[i], df[i], CPV_COLOR_OP);
+    if (CPV_COLOR_OP != CPV_ALPHA_OP) out[3] = cpv_blend_op(s[3], sf[3], d[3], df[3], CPV_ALPHA_OP);
+}
+
+/* Shading of one covered pixel: barycentrics (w_k / area), screen-linear
+ * depth, varyings (perspective Σ w·v/p ÷ Σ w/p, linear Σ w·v, or flat from
+ * the provoking vertex; CPVulkan/CommandBuffer.Draw.cpp:816-954), viewport
+ * depth mapping (:1300-1313) and the fragment shader. Returns true when the
+ * shader discards. */
+__device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& t, const float wr[3], int32_t x, int32_t y, float colour[4],
+                                          float& mapped) {
+    const float area = t.za.w;
+    float w[3];
+    w[0] = __fdiv_rn(wr[0], area);
+    w[1] = __fdiv_rn(wr[1], area);
+    w[2] = __fdiv_rn(wr[2], area);
+    const float depth = __fadd_rn(__fadd_rn(__fmul_rn(t.za.x, w[0]), __fmul_rn(t.za.y, w[1])), __fmul_rn(t.za.z, w[2]));
+    const float pw[3] = {t.wf.x, t.wf.y, t.wf.z};
+    const uint32_t pslot = cpv_tri_pslot(t);
+    float in[CPV_NV_ALLOC];
+#pragma unroll
+    for (int c = 0; c < CPV_NV; c++) {
+        const int kind = cpv_interp(c);
+        if (kind == 2) {
+            in[c] = t.var[pslot][c];
+        } else if (kind == 1) {
+            float r = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 3; k++) r = __fadd_rn(r, __fmul_rn(w[k], t.var[k][c]));
+            in[c] = r;
+        } else {
+            float num = 0.0f, den = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                num = __fadd_rn(num, __fdiv_rn(__fmul_rn(w[k], t.var[k][c]), pw[k]));
+                den = __fadd_rn(den, __fdiv_rn(w[k], pw[k]));
+            }
+            in[c] = __fdiv_rn(num, den);
+        }
+    }
+    const float min_d = P.viewport[4], max_d = P.viewport[5];
+    mapped = __fadd_rn(__fmul_rn(__fsub_rn(max_d, min_d), depth), min_d);
+    float frag_coord[4];
+#if CPV_ORIGIN_UPPER
+    frag_coord[0] = static_cast<float>(x);
+#else
+    frag_coord[0] = __fsub_rn(__fsub_rn(P.viewport[2], static_cast<float>(x)), 1.0f);
+#endif
+    frag_coord[1] = static_cast<float>(y);
+    frag_coord[2] = depth;
+    frag_coord[3] = 1.0f;
+    return cpv_fs_run(P, in, frag_coord, cpv_tri_front(t), colour);
+}
+
+/* Depth bounds are rejected at pipeline creation; order as the reference's
+ * fragment wrapper: current values → stencil test → depth test → depth /
+ * stencil write → colour write (blend, write mask, encode). */
+__device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool front, const float colour[4], float mapped, CpvPixel& s) {
+    const bool has_depth = CPV_DEPTH_FORMAT != 0;
+    const bool stencil_on = CPV_STENCIL_TEST && CPV_DEPTH_FORMAT == 130;
+    const float current_depth = (CPV_DEPTH_TEST && has_depth) ? s.depth : 0.0f;
+    const uint32_t current_stencil = stencil_on ? s.stencil : 0u;
+    bool stencil_result = true;
+    uint32_t ref = 0u;
+    if (stencil_on) {
+        ref = (front ? CPV_ST_F_REF : CPV_ST_B_REF) & 0xFFu;
+        const uint32_t mask = (front ? CPV_ST_F_CMASK : CPV_ST_B_CMASK) & 0xFFu;
+        stencil_result = cpv_icompare(ref & mask, current_stencil & mask, front ? CPV_ST_F_OP : CPV_ST_B_OP);
+    }
+    const bool depth_result = (CPV_DEPTH_TEST && has_depth) ? cpv_fcompare(mapped, current_depth, CPV_DEPTH_OP) : true;
+    const bool attempt_depth_write = CPV_DEPTH_TEST && CPV_DEPTH_WRITE && has_depth;
+    if (stencil_on) {
+        const uint32_t fail = cpv_stencil_op(front ? CPV_ST_F_FAIL : CPV_ST_B_FAIL, current_stencil, ref);
+        const uint32_t dfail = cpv_stencil_op(front ? CPV_ST_F_DFAIL : CPV_ST_B_DFAIL, current_stencil, ref);
+        const uint32_t pass = cpv_stencil_op(front ? CPV_ST_F_PASS : CPV_ST_B_PASS, current_stencil, ref);
+        uint32_t value = stencil_result ? (depth_result ? pass : dfail) : fail;
+        const uint32_t wmask = (front ? CPV_ST_F_WMASK : CPV_ST_B_WMASK) & 0xFFu;
+        value = ((value & wmask) | (current_stencil & ~wmask)) & 0xFFu;
+        if (depth_result && attempt_depth_write) cpv_write_depth(s, mapped);
+        s.stencil = value;
+    } else if (attempt_depth_write && depth_result) {
+        cpv_write_depth(s, mapped);
+    }
+    if (stencil_result && depth_result) {
+        float out[4];
+#if CPV_BLEND
+        float dst[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) dst[i] = CPV_DECODE8((s.colour >> cpv_channel_shift(i)) & 0xFFu);
+        cpv_blend(colour, dst, blend_constants, out);
+#else
+        (void)blend_constants;
+#pragma unroll
+        for (int i = 0; i < 4; i++) out[i] = colour[i];
+#endif
+        uint32_t packed = 0u;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint32_t byte = ((CPV_WRITE_MASK >> i) & 1u) ? cpv_encode_unorm(out[i], 255.0f) : ((s.colour >> cpv_channel_shift(i)) & 0xFFu);
+            packed |= byte << cpv_channel_shift(i);
+        }
+        s.colour = packed;
+    }
+}
+
+/* The stage functions of this pipeline, as one type the module's
+ * dispatcher (cpv_dispatch) hands to generic code. */
+struct Stage {
+    template <bool WITH_VARYINGS>
+    static __device__ __forceinline__ void setup(const CpvDrawParams& P, uint64_t g, CpvTri& t) { cpv_setup<WITH_VARYINGS>(P, g, t); }
+    static __device__ __forceinline__ bool shade(const CpvDrawParams& P, const CpvTri& t, const float w[3], int32_t x, int32_t y, float colour[4],
+                                                 float& mapped) {
+        return cpv_shade(P, t, w, x, y, colour, mapped);
+    }
+    static __device__ __forceinline__ void rop(const float blend_constants[4], bool front, const float colour[4], float mapped, CpvPixel& s) {
+        cpv_rop(blend_constants, front, colour, mapped, s);
+    }
+    static __device__ __forceinline__ void load_pixel(const uint8_t* c, const uint8_t* d, uint64_t pix, CpvPixel& s) { cpv_load_pixel(c, d, pix, s); }
+    static __device__ __forceinline__ void store_pixel(uint8_t* c, uint8_t* d, uint64_t pix, const CpvPixel& s) { cpv_store_pixel(c, d, pix, s); }
+};

@@ -181,9 +181,7 @@ bool available() { return g_available; }
 
 int compile(const std::string& source, const std::string& name, std::vector<uint8_t>& cubin, std::string& log) {
     nvrtcProgram prog;
-    const char* headers[3] = {kDeviceHeaderSource, kPipelineHeaderSource, kParamsHeaderSource};
-    const char* names[3] = {kDeviceHeaderName, kPipelineHeaderName, kParamsHeaderName};
-    if (nvrtcCreateProgram(&prog, source.c_str(), name.c_str(), 3, headers, names) != NVRTC_SUCCESS) {
+    if (nvrtcCreateProgram(&prog, source.c_str(), name.c_str(), kKernelHeaderCount, kKernelHeaderSources, kKernelHeaderNames) != NVRTC_SUCCESS) {
         log = "nvrtcCreateProgram failed";
         return kErrCompile;
     }
@@ -212,7 +210,21 @@ int compile(const std::string& source, const std::string& name, std::vector<uint
     return kOk;
 }
 
-int load(const std::vector<uint8_t>& cubin, uint32_t tile_shift, Module& out, std::string& error) {
+namespace {
+
+bool module_u32(cudaLibrary_t lib, const char* name, uint32_t& value) {
+    void* dptr = nullptr;
+    size_t bytes = 0;
+    if (cudaLibraryGetGlobal(&dptr, &bytes, lib, name) != cudaSuccess || bytes != 4 || cudaMemcpy(&value, dptr, 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return true;
+}
+
+}  // namespace
+
+int load(const std::vector<uint8_t>& cubin, uint32_t tile_shift, bool batched, Module& out, std::string& error) {
     if (!g_available) {
         error = "no CUDA device: pipeline modules cannot be loaded";
         return kErrCuda;
@@ -225,37 +237,29 @@ int load(const std::vector<uint8_t>& cubin, uint32_t tile_shift, Module& out, st
         return kErrCuda;
     }
     out.library = lib;
-    if (cudaLibraryGetKernel(&out.setup_rects, lib, "cpv_setup_rects") != cudaSuccess ||
-        cudaLibraryGetKernel(&out.raster, lib, "cpv_raster") != cudaSuccess) {
+    auto fail = [&](const std::string& why) {
         cudaGetLastError();
         cudaLibraryUnload(lib);
         out.library = nullptr;
-        error = "pipeline module lacks its kernels";
+        error = why;
         return kErrCuda;
-    }
+    };
+    bool ok;
+    if (batched)
+        ok = cudaLibraryGetKernel(&out.setup_rects, lib, "cpv_batch_setup") == cudaSuccess &&
+             cudaLibraryGetKernel(&out.raster, lib, "cpv_batch_raster") == cudaSuccess;
+    else
+        ok = cudaLibraryGetKernel(&out.setup_rects, lib, "cpv_setup_rects") == cudaSuccess &&
+             cudaLibraryGetKernel(&out.raster, lib, "cpv_raster") == cudaSuccess;
+    if (!ok) return fail("pipeline module lacks its kernels");
+    out.batched = batched;
     out.tile_shift = tile_shift;
-    const uint32_t tile = 1u << tile_shift;
-    out.raster_threads = tile * tile < 256 ? tile * tile : 256;
-    void* dptr = nullptr;
-    size_t dbytes = 0;
-    uint32_t smem = 0;
-    if (cudaLibraryGetGlobal(&dptr, &dbytes, lib, "cpv_raster_smem_bytes") != cudaSuccess || dbytes != 4 ||
-        cudaMemcpy(&smem, dptr, 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
-        cudaGetLastError();
-        cudaLibraryUnload(lib);
-        out.library = nullptr;
-        error = "pipeline module lacks cpv_raster_smem_bytes";
-        return kErrCuda;
-    }
-    out.raster_smem = smem;
-    if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(reinterpret_cast<const void*>(out.raster), cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess) {
-        cudaGetLastError();
-        cudaLibraryUnload(lib);
-        out.library = nullptr;
-        error = "raster kernel needs more shared memory than the device allows";
-        return kErrCuda;
-    }
+    if (!module_u32(lib, "cpv_raster_smem_bytes", out.raster_smem) || !module_u32(lib, "cpv_raster_threads", out.raster_threads))
+        return fail("pipeline module lacks its launch-shape globals");
+    if (out.raster_smem > 48 * 1024 &&
+        cudaFuncSetAttribute(reinterpret_cast<const void*>(out.raster), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(out.raster_smem)) != cudaSuccess)
+        return fail("raster kernel needs more shared memory than the device allows");
     return kOk;
 }
 
@@ -426,6 +430,268 @@ int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& s
         profile_end(stream);
         count_launch();
     }
+    return kOk;
+}
+
+// ---------------------------------------------------------------------------
+// Batched path.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+template <typename T>
+int dev_alloc(T*& ptr, uint64_t count) {
+    ptr = nullptr;
+    if (count == 0) count = 1;
+    if (cudaMalloc(reinterpret_cast<void**>(&ptr), count * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        ptr = nullptr;
+        set_last_error("cudaMalloc of batch buffers failed (" + std::to_string(count * sizeof(T)) + " bytes)");
+        return kErrOutOfMemory;
+    }
+    return kOk;
+}
+
+template <typename T>
+void dev_free(T*& ptr) {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+}
+
+}  // namespace
+
+BatchPlan::~BatchPlan() {
+    if (!available()) return;
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (done_) cudaEventDestroy(done_);
+    dev_free(draws_);
+    dev_free(pipeline_);
+    dev_free(draw_block_);
+    dev_free(block_draw_);
+    dev_free(rects_);
+    dev_free(block_pairs_);
+    dev_free(block_offsets_);
+    free_pairs();
+    dev_free(hist_);
+    dev_free(hist_offsets_);
+    dev_free(tile_begin_);
+    dev_free(tile_end_);
+    dev_free(words_);
+    if (pinned_pairs_) cudaFreeHost(pinned_pairs_);
+}
+
+void BatchPlan::free_pairs() {
+    for (int i = 0; i < 2; i++) {
+        dev_free(keys_[i]);
+        dev_free(vals_[i]);
+    }
+    cap_ = 0;
+}
+
+int BatchPlan::alloc_pairs(uint32_t capacity) {
+    free_pairs();
+    for (int i = 0; i < 2; i++) {
+        int r;
+        if ((r = dev_alloc(keys_[i], capacity)) != kOk || (r = dev_alloc(vals_[i], capacity)) != kOk) {
+            free_pairs();
+            return r;
+        }
+    }
+    cap_ = capacity;
+    P_.pair_capacity = capacity;
+    return kOk;
+}
+
+int BatchPlan::build(const Module& m, const BatchDraws& in, cudaStream_t stream) {
+    const uint32_t n = static_cast<uint32_t>(in.draws.size());
+    if (n == 0 || in.pipeline.size() != n || !m.batched) {
+        set_last_error("batch plan: empty batch or module without batched kernels");
+        return kErrInvalid;
+    }
+    // Block layout: draw d owns blocks [draw_block[d], draw_block[d+1]).
+    std::vector<uint32_t> draw_block(n + 1);
+    uint64_t blocks = 0;
+    prims_ = 0;
+    for (uint32_t d = 0; d < n; d++) {
+        draw_block[d] = static_cast<uint32_t>(blocks);
+        blocks += (in.draws[d].total_prims + CPV_BATCH_BLOCK - 1) / CPV_BATCH_BLOCK;
+        prims_ += in.draws[d].total_prims;
+        if (blocks * CPV_BATCH_BLOCK >= (1ull << 32)) {
+            set_last_error("batch plan: more than 2^32 primitives in one batch");
+            return kErrInvalid;
+        }
+    }
+    draw_block[n] = static_cast<uint32_t>(blocks);
+    std::vector<uint32_t> block_draw(blocks ? blocks : 1, 0);
+    for (uint32_t d = 0; d < n; d++)
+        for (uint32_t b = draw_block[d]; b < draw_block[d + 1]; b++) block_draw[b] = d;
+    const uint32_t tile = 1u << m.tile_shift;
+    const uint32_t tiles_x = (in.fb_width + tile - 1) / tile, tiles_y = (in.fb_height + tile - 1) / tile;
+    tiles_ = tiles_x * tiles_y;
+    if (tiles_ == 0 || tiles_ > 65536u) {
+        set_last_error("batch plan: attachment needs more than 65536 tiles");
+        return kErrInvalid;
+    }
+    passes_ = tiles_ > 256u ? 2u : 1u;
+    int r;
+    if ((r = dev_alloc(draws_, n)) != kOk || (r = dev_alloc(pipeline_, n)) != kOk || (r = dev_alloc(draw_block_, n + 1)) != kOk ||
+        (r = dev_alloc(block_draw_, block_draw.size())) != kOk || (r = dev_alloc(rects_, blocks * CPV_BATCH_BLOCK)) != kOk ||
+        (r = dev_alloc(block_pairs_, blocks)) != kOk || (r = dev_alloc(block_offsets_, blocks)) != kOk ||
+        (r = dev_alloc(tile_begin_, tiles_)) != kOk || (r = dev_alloc(tile_end_, tiles_)) != kOk || (r = dev_alloc(words_, 64)) != kOk)
+        return r;
+    if (cudaMallocHost(reinterpret_cast<void**>(&pinned_pairs_), 64) != cudaSuccess) {
+        cudaGetLastError();
+        set_last_error("batch plan: pinned word allocation failed");
+        return kErrOutOfMemory;
+    }
+    CPV_CUDA(cudaEventCreateWithFlags(&done_, cudaEventDisableTiming));
+    CPV_CUDA(cudaMemcpy(draws_, in.draws.data(), n * sizeof(CpvDrawParams), cudaMemcpyHostToDevice));
+    CPV_CUDA(cudaMemcpy(pipeline_, in.pipeline.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    CPV_CUDA(cudaMemcpy(draw_block_, draw_block.data(), (n + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    CPV_CUDA(cudaMemcpy(block_draw_, block_draw.data(), block_draw.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    CPV_CUDA(cudaMemset(words_, 0, 64 * sizeof(uint32_t)));
+
+    int sms = 0, per_sm = 0;
+    CPV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+    CPV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(m.raster), static_cast<int>(m.raster_threads),
+                                                           m.raster_smem));
+    if (per_sm < 1) per_sm = 1;
+    raster_ctas_ = static_cast<uint32_t>(sms * per_sm);
+    if (raster_ctas_ > tiles_) raster_ctas_ = tiles_;
+    radix_ctas_ = static_cast<uint32_t>(sms * 4);
+    if ((r = dev_alloc(hist_, static_cast<uint64_t>(CPV_RADIX_DIGITS) * radix_ctas_)) != kOk ||
+        (r = dev_alloc(hist_offsets_, static_cast<uint64_t>(CPV_RADIX_DIGITS) * radix_ctas_)) != kOk)
+        return r;
+    // Scan levels for both scans, reserved now so that no launch allocates.
+    if ((r = scan_.reserve_scan(blocks)) != kOk || (r = scan_.reserve_scan(static_cast<uint64_t>(CPV_RADIX_DIGITS) * radix_ctas_)) != kOk) return r;
+
+    P_ = CpvBatchParams{};
+    P_.draws = draws_;
+    P_.draw_pipeline = pipeline_;
+    P_.draw_block = draw_block_;
+    P_.block_draw = block_draw_;
+    P_.num_draws = n;
+    P_.total_blocks = static_cast<uint32_t>(blocks);
+    P_.color = in.color;
+    P_.depth = in.depth;
+    P_.fb_width = in.fb_width;
+    P_.fb_height = in.fb_height;
+    P_.vw = in.vw;
+    P_.vh = in.vh;
+    P_.tiles_x = tiles_x;
+    P_.tiles_y = tiles_y;
+    P_.rects = rects_;
+    P_.block_pairs = block_pairs_;
+    P_.block_offsets = block_offsets_;
+    P_.pair_total = words_;
+    P_.tile_begin = tile_begin_;
+    P_.tile_end = tile_end_;
+    P_.tile_counter = words_ + 2;
+    P_.status = words_ + 1;
+
+    // One set-up run to size the pair buffers.
+    if (blocks) {
+        void* args[] = {&P_};
+        CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.setup_rects), dim3(static_cast<unsigned>(blocks)), dim3(CPV_BATCH_BLOCK), args, 0, stream));
+        count_launch();
+        if ((r = scan_u32(stream, block_pairs_, block_offsets_, blocks, words_, scan_)) != kOk) return r;
+    }
+    CPV_CUDA(cudaMemcpyAsync(pinned_pairs_, words_, 4, cudaMemcpyDeviceToHost, stream));
+    CPV_CUDA(cudaStreamSynchronize(stream));
+    const uint64_t pairs = *pinned_pairs_;
+    uint64_t cap = pairs + pairs / 4 + (1u << 20);
+    if (cap > 0xFFFFFFFFull) cap = 0xFFFFFFFFull;
+    // CPV_BATCH_PAIR_CAPACITY forces a capacity (tests of the overflow path).
+    if (const uint32_t forced = env_u32("CPV_BATCH_PAIR_CAPACITY", 0u)) cap = forced;
+    return alloc_pairs(static_cast<uint32_t>(cap));
+}
+
+int BatchPlan::enqueue(const Module& m, cudaStream_t stream) {
+    const uint32_t blocks = P_.total_blocks;
+    const uint64_t before = launches();
+    if (blocks == 0) {
+        kernels_ = 0;
+        return kOk;  // no primitive: nothing to draw
+    }
+    {
+        void* args[] = {&P_};
+        CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.setup_rects), dim3(blocks), dim3(CPV_BATCH_BLOCK), args, 0, stream));
+        count_launch();
+    }
+    int r = scan_u32(stream, block_pairs_, block_offsets_, blocks, words_, scan_);
+    if (r != kOk) return r;
+    cpv_batch_emit<<<blocks, 256, 0, stream>>>(rects_, block_offsets_, P_.tiles_x, keys_[0], vals_[0], cap_, words_);
+    count_launch();
+    for (uint32_t pass = 0; pass < passes_; pass++) {
+        const uint32_t src = pass & 1u, dst = src ^ 1u;
+        cpv_radix_hist<<<radix_ctas_, CPV_RADIX_THREADS, 0, stream>>>(keys_[src], words_, cap_, 8u * pass, hist_);
+        count_launch();
+        r = scan_u32(stream, hist_, hist_offsets_, static_cast<uint64_t>(CPV_RADIX_DIGITS) * radix_ctas_, nullptr, scan_);
+        if (r != kOk) return r;
+        cpv_radix_scatter<<<radix_ctas_, CPV_RADIX_THREADS, 0, stream>>>(keys_[src], vals_[src], keys_[dst], vals_[dst], words_, cap_, 8u * pass,
+                                                                       hist_offsets_);
+        count_launch();
+    }
+    const uint32_t fin = passes_ & 1u;
+    P_.sorted_prims = vals_[fin];
+    CPV_CUDA(cudaMemsetAsync(tile_begin_, 0, tiles_ * sizeof(uint32_t), stream));
+    CPV_CUDA(cudaMemsetAsync(tile_end_, 0, tiles_ * sizeof(uint32_t), stream));
+    cpv_tile_ranges<<<radix_ctas_, 256, 0, stream>>>(keys_[fin], words_, cap_, tile_begin_, tile_end_);
+    count_launch();
+    CPV_CUDA(cudaMemsetAsync(words_ + 2, 0, sizeof(uint32_t), stream));
+    {
+        void* args[] = {&P_};
+        CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.raster), dim3(raster_ctas_), dim3(m.raster_threads), args, m.raster_smem, stream));
+        count_launch();
+    }
+    CPV_CUDA(cudaMemcpyAsync(pinned_pairs_, words_, 4, cudaMemcpyDeviceToHost, stream));
+    CPV_CUDA(cudaGetLastError());
+    kernels_ = static_cast<uint32_t>(launches() - before);
+    return kOk;
+}
+
+int BatchPlan::launch(const Module& m, cudaStream_t stream) {
+    // An earlier launch that needed more pairs than the buffers hold rendered
+    // correctly through the rectangle scan; grow the buffers for the next.
+    if (exec_ && cudaEventQuery(done_) == cudaSuccess && *pinned_pairs_ > cap_) {
+        const uint64_t pairs = *pinned_pairs_;
+        uint64_t cap = pairs + pairs / 4 + (1u << 20);
+        if (cap > 0xFFFFFFFFull) cap = 0xFFFFFFFFull;
+        cudaGraphExecDestroy(exec_);
+        exec_ = nullptr;
+        const int r = alloc_pairs(static_cast<uint32_t>(cap));
+        if (r != kOk) return r;
+    }
+    cudaGetLastError();
+    if (!exec_ && env_u32("CPV_BATCH_GRAPH", 1u)) {
+        // Capture the sequence once; later launches replay the graph.
+        cudaGraph_t graph = nullptr;
+        const uint64_t before = launches();
+        CPV_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        const int r = enqueue(m, stream);
+        const cudaError_t e = cudaStreamEndCapture(stream, &graph);
+        g_launches -= launches() - before;  // captured, not launched yet
+        if (r != kOk || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            if (r != kOk) return r;
+            return cuda_fail(e, "cudaStreamEndCapture");
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&exec_, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            exec_ = nullptr;
+            return cuda_fail(ie, "cudaGraphInstantiate");
+        }
+    }
+    if (exec_) {
+        CPV_CUDA(cudaGraphLaunch(exec_, stream));
+        count_launch(kernels_);
+    } else {
+        const int r = enqueue(m, stream);
+        if (r != kOk) return r;
+    }
+    CPV_CUDA(cudaEventRecord(done_, stream));
     return kOk;
 }
 

@@ -25,21 +25,23 @@ enum Status : int {
     kErrDeviceLost = -6,
 };
 
-// Embedded device sources (generated at build time from csrc/kernels/*.cuh).
-extern const char* const kDeviceHeaderName;
-extern const char* const kDeviceHeaderSource;
-extern const char* const kPipelineHeaderName;
-extern const char* const kPipelineHeaderSource;
-extern const char* const kParamsHeaderName;
-extern const char* const kParamsHeaderSource;
+// Embedded kernel headers for NVRTC (generated at build time from
+// csrc/kernels/: names and sources, in a fixed order).
+extern const int kKernelHeaderCount;
+extern const char* const kKernelHeaderNames[];
+extern const char* const kKernelHeaderSources[];
 
+// A loaded raster module: the per-draw kernels of one pipeline
+// (cpv_setup_rects, cpv_raster) or the batched kernels of a set of pipelines
+// (cpv_batch_setup, cpv_batch_raster).
 struct Module {
     cudaLibrary_t library = nullptr;
     cudaKernel_t setup_rects = nullptr;
     cudaKernel_t raster = nullptr;
+    bool batched = false;
     uint32_t tile_shift = 4;
     uint32_t raster_threads = 256;
-    uint32_t raster_smem = 0;  // dynamic shared memory of cpv_raster (bytes)
+    uint32_t raster_smem = 0;  // dynamic shared memory of the raster kernel (bytes)
 };
 
 // Initialises the CUDA context on device 0 (once per process).
@@ -49,7 +51,7 @@ bool available();
 // Compiles a pipeline translation unit with NVRTC for sm_103a.
 int compile(const std::string& source, const std::string& name, std::vector<uint8_t>& cubin, std::string& log);
 // Loads a cubin and resolves the pipeline kernels.
-int load(const std::vector<uint8_t>& cubin, uint32_t tile_shift, Module& out, std::string& error);
+int load(const std::vector<uint8_t>& cubin, uint32_t tile_shift, bool batched, Module& out, std::string& error);
 void unload(Module& m);
 
 // Grow-only device scratch owned by one queue. Draws on that queue's stream
@@ -102,6 +104,68 @@ void profile_reset();
 // `P` must have geometry, resources and attachments filled; tiling and
 // binning fields are filled here.
 int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& scratch);
+
+// ---- batched path: every draw of a render pass in one kernel sequence ----
+
+// Host description of one batch: the draws' parameters (as the per-draw path
+// builds them) and each draw's pipeline index in the batched module. All
+// draws share the render pass's attachments and viewport extent.
+struct BatchDraws {
+    std::vector<CpvDrawParams> draws;
+    std::vector<uint32_t> pipeline;
+    uint8_t* color = nullptr;
+    uint8_t* depth = nullptr;
+    uint32_t fb_width = 0, fb_height = 0;
+    float vw = 0.0f, vh = 0.0f;
+};
+
+// Device state of one batched render pass of a recorded command buffer:
+// the uploaded draw tables, the binning buffers (sized on the first run) and,
+// after the first launch, a CUDA graph of the whole kernel sequence.
+class BatchPlan {
+public:
+    BatchPlan() = default;
+    BatchPlan(const BatchPlan&) = delete;
+    BatchPlan& operator=(const BatchPlan&) = delete;
+    ~BatchPlan();
+    // Uploads the tables, allocates every buffer and measures the pair count
+    // of the batch with one synchronous set-up run.
+    int build(const Module& m, const BatchDraws& in, cudaStream_t stream);
+    // Enqueues the batch on `stream`: the captured graph when there is one
+    // (captured on the first call), else the kernel sequence. Grows the pair
+    // buffers first when an earlier launch needed more than they hold.
+    int launch(const Module& m, cudaStream_t stream);
+    uint64_t primitives() const { return prims_; }
+    uint32_t kernels_per_launch() const { return kernels_; }
+
+private:
+    int enqueue(const Module& m, cudaStream_t stream);
+    int alloc_pairs(uint32_t capacity);
+    void free_pairs();
+
+    CpvBatchParams P_{};
+    Scratch scan_;
+    CpvDrawParams* draws_ = nullptr;
+    uint32_t* pipeline_ = nullptr;
+    uint32_t* draw_block_ = nullptr;
+    uint32_t* block_draw_ = nullptr;
+    uint2* rects_ = nullptr;
+    uint32_t* block_pairs_ = nullptr;
+    uint32_t* block_offsets_ = nullptr;
+    uint32_t* keys_[2] = {};
+    uint32_t* vals_[2] = {};
+    uint32_t cap_ = 0;
+    uint32_t* hist_ = nullptr;
+    uint32_t* hist_offsets_ = nullptr;
+    uint32_t* tile_begin_ = nullptr;
+    uint32_t* tile_end_ = nullptr;
+    uint32_t* words_ = nullptr;         // [0] pair total, [1] status, [2] tile counter
+    uint32_t* pinned_pairs_ = nullptr;  // pair total of the last launch (host)
+    cudaEvent_t done_ = nullptr;
+    uint64_t prims_ = 0;
+    uint32_t tiles_ = 0, radix_ctas_ = 0, raster_ctas_ = 0, passes_ = 1, kernels_ = 0;
+    cudaGraphExec_t exec_ = nullptr;
+};
 
 // Fixed binning scratch for submissions that may not allocate: one
 // 32 MiB file-scope device array per device. A draw needs 8 bytes per

@@ -39,16 +39,25 @@ def _write_if_changed(path, text):
         fh.write(text)
 
 
+# Kernel headers NVRTC compiles pipeline modules from, in this order (the
+# pipeline key hashes them in the same order).
+KERNEL_HEADERS = ["cpv_params.h", "cpv_device.cuh", "cpv_raster.cuh", "cpv_stage.cuh", "cpv_pipeline.cuh", "cpv_batch.cuh"]
+
+
 def _embed_sources():
     kdir = os.path.join(HERE, "csrc", "kernels")
     out = ['#include "../../csrc/runtime/runtime.h"', "namespace cpv::rt {"]
-    for var, name in (("kDeviceHeader", "cpv_device.cuh"), ("kPipelineHeader", "cpv_pipeline.cuh"), ("kParamsHeader", "cpv_params.h")):
+    names, sources = [], []
+    for name in KERNEL_HEADERS:
         with open(os.path.join(kdir, name)) as fh:
             src = fh.read()
         if ")CPVSRC" in src:
             raise RuntimeError("delimiter clash in " + name)
-        out.append('extern const char* const %sName = "%s";' % (var, name))
-        out.append('extern const char* const %sSource = R"CPVSRC(%s)CPVSRC";' % (var, src))
+        names.append('"%s"' % name)
+        sources.append('R"CPVSRC(%s)CPVSRC"' % src)
+    out.append("extern const int kKernelHeaderCount = %d;" % len(names))
+    out.append("extern const char* const kKernelHeaderNames[] = {%s};" % ", ".join(names))
+    out.append("extern const char* const kKernelHeaderSources[] = {\n%s};" % ",\n".join(sources))
     out.append("}")
     _write_if_changed(os.path.join(GEN, "embedded_sources.cpp"), "\n".join(out) + "\n")
 
@@ -121,7 +130,7 @@ def _build(verbose):
     _embed_sources()
     _embed_spirv()
     csrc = os.path.join(HERE, "csrc")
-    kernels = [os.path.join(csrc, "kernels", f) for f in ("cpv_params.h", "cpv_device.cuh", "cpv_bin.cuh", "cpv_pipeline.cuh")]
+    kernels = [os.path.join(csrc, "kernels", f) for f in KERNEL_HEADERS + ["cpv_bin.cuh"]]
     headers = [os.path.join(csrc, "icd", "icd.h"), os.path.join(csrc, "runtime", "runtime.h"), os.path.join(csrc, "spirv", "spirv.h"),
                os.path.join(ROOT, "include", "cpvulkan_gb300.h"), os.path.join(ROOT, "include", "cpv", "vk_subset.h")]
     jobs = []

@@ -1,0 +1,93 @@
+"""Batched render passes (one kernel sequence, captured in a CUDA graph, for
+every draw of a render pass) against the per-draw path and the oracle.
+
+Batching changes no draw's arithmetic: its images must equal the per-draw
+images bit for bit, on every frame (the first eager run and the graph
+replays), for every tile size and fragment schedule, and when the pair
+buffers overflow (the raster then scans the tile rectangles).
+"""
+import numpy as np
+import pytest
+
+import cpvulkan_gb300 as c
+from tests.parity import compare
+
+pytestmark = pytest.mark.gpu
+
+
+def frames(ctx, scene, n=1):
+    r = c.Renderer(ctx, scene)
+    try:
+        out = []
+        for _ in range(n):
+            r.render(1)
+            out.append(r.readback())
+        return out
+    finally:
+        r.close()
+
+
+def same(a, b):
+    (ca, da), (cb, db) = a, b
+    assert np.count_nonzero(np.any(ca != cb, axis=-1)) == 0
+    if da is not None:
+        assert np.count_nonzero(np.any(da != db, axis=-1)) == 0
+
+
+@pytest.fixture
+def plain(monkeypatch):
+    def run(ctx, scene, n=1):
+        monkeypatch.setenv("CPV_BATCH", "0")
+        out = frames(ctx, scene, n)
+        monkeypatch.setenv("CPV_BATCH", "1")
+        return out
+    return run
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_batched_equals_plain_and_oracle(gpu_ctx, oracle, plain, seed):
+    scene = c.Scene(c.BATCH, seed, [64, 4000, 640, 360])
+    ref = plain(gpu_ctx, scene)[0]
+    before = c.kernel_launches()
+    runs = frames(gpu_ctx, scene, 3)  # eager first run, then graph replays
+    assert c.kernel_launches() > before
+    for got in runs:
+        same(got, ref)
+    ocol, odep, _ = oracle.render(scene)
+    report = compare(scene, runs[-1][0], runs[-1][1], ocol, odep)
+    assert report["color_pixels_differing"] == 0, report
+
+
+@pytest.mark.parametrize("tile", ["8", "16", "32"])
+@pytest.mark.parametrize("deferred", ["0", "1"])
+def test_batched_schedules(gpu_ctx, plain, monkeypatch, tile, deferred):
+    monkeypatch.setenv("CPV_TILE", tile)
+    monkeypatch.setenv("CPV_DEFERRED", deferred)
+    scene = c.Scene(c.BATCH, 3, [40, 3000, 400, 272])
+    ref = plain(gpu_ctx, scene)[0]
+    same(frames(gpu_ctx, scene)[0], ref)
+
+
+def test_batched_pair_overflow_scans_rectangles(gpu_ctx, plain, monkeypatch):
+    scene = c.Scene(c.BATCH, 4, [24, 2000, 320, 200])
+    ref = plain(gpu_ctx, scene)[0]
+    monkeypatch.setenv("CPV_BATCH_PAIR_CAPACITY", "100")
+    for got in frames(gpu_ctx, scene, 3):  # overflowing launch, then regrown buffers
+        same(got, ref)
+
+
+def test_batched_blend_scene(gpu_ctx, plain, monkeypatch):
+    monkeypatch.setenv("CPV_BATCH_MIN_DRAWS", "1")
+    scene = c.Scene(c.BLEND, 5, [1500, 480, 270])  # one draw: a batch of one
+    ref = plain(gpu_ctx, scene)[0]
+    same(frames(gpu_ctx, scene, 2)[1], ref)
+
+
+def test_batched_program_variants(gpu_ctx, plain, monkeypatch):
+    """Stencil, D16, CW, strips and discard through the batched kernels."""
+    monkeypatch.setenv("CPV_BATCH_MIN_DRAWS", "1")
+    for program, variant in [(c.PROGRAM_CUBE, 0x18 | 0x100), (c.PROGRAM_CUBE, 0x8 | 0x4 | 0x1), (c.PROGRAM_CUBE, 0x400 | 0x10),
+                             (c.PROGRAM_DISCARD, 0x10), (c.PROGRAM_TEXLIT, 0x10 | 0x4000), (c.PROGRAM_MESHPC, 0x10 | 0x20)]:
+        scene = c.Scene(c.PROGRAM, 2, [program, variant, 64, 48, 24])
+        ref = plain(gpu_ctx, scene)[0]
+        same(frames(gpu_ctx, scene)[0], ref)

@@ -47,7 +47,8 @@ def test_pipeline_key_is_sha3_of_source_and_kernels(compile_ctx):
     ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [c.PROGRAM_TEXLIT, 0x10, 32, 32, 4]))
     (path,) = glob.glob(str(dump / "pipeline_*.cu"))
     keyed = open(path, "rb").read()
-    for h in ("cpv_device.cuh", "cpv_pipeline.cuh", "cpv_params.h"):
+    from cpvulkan_gb300.native_build import KERNEL_HEADERS
+    for h in KERNEL_HEADERS:
         keyed += open(os.path.join(KERNELS, h), "rb").read()
     assert os.path.basename(path) == "pipeline_%s.cu" % hashlib.sha3_256(keyed).hexdigest()[:12]
 
