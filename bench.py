@@ -229,6 +229,10 @@ def run_reference(args, world, rank, dist):
     print(json.dumps(line), flush=True)
 
 
+PLAIN_KERNELS = ("cpv_raster", "cpv_setup_rects", "cpv_span_count", "cpv_scan", "cpv_span_write")
+BATCH_KERNELS = ("cpv_batch", "cpv_batch_setup", "cpv_batch_bin", "cpv_batch_raster")
+
+
 def run_ours(args, world, rank, dist):
     import numpy as np
     import cpvulkan_gb300 as c
@@ -242,6 +246,12 @@ def run_ours(args, world, rank, dist):
     cfg, params, desc = CONFIGS[args.config]
     scene = c.Scene(cfg, 1, params)
     tris = scene.triangles
+    # Batching applies to render passes with many draws; one-draw scenes
+    # measure the per-draw path only.
+    modes = ["plain", "batched"] if scene.draws >= 16 and args.mode == "auto" else ["plain"]
+    if args.mode == "batched":
+        os.environ["CPV_BATCH_MIN_DRAWS"] = "1"  # a one-draw pass runs as a batch of one
+        modes = ["batched"]
     ctx = c.Context()
     t0 = time.time()
     r = c.Renderer(ctx, scene)
@@ -257,74 +267,124 @@ def run_ours(args, world, rank, dist):
             raise RuntimeError("render failed: %d" % res)
         return list(arr)
 
-    timed(args.warmup)
-    barrier(dist)
-    clocks = ClockSampler()
-    clocks.start()
-    launches0 = icd.cpv_kernel_launches()
-    frame_ms = timed(args.steps)
-    launches = icd.cpv_kernel_launches() - launches0
-    clock_info = clocks.stop()
-    barrier(dist)
-    total_ms = max_over_ranks(dist, sum(frame_ms))
+    def profile(names, frames):
+        icd.cpv_profile_reset()
+        icd.cpv_profile_enable(1)
+        timed(frames)
+        icd.cpv_profile_enable(0)
+        out = {}
+        for k in names:
+            n, ms = ctypes.c_uint64(0), ctypes.c_double(0.0)
+            icd.cpv_profile_get(k.encode(), ctypes.byref(n), ctypes.byref(ms))
+            if n.value:
+                out[k] = {"launches": n.value, "ms_per_launch": round(ms.value / n.value, 4), "ms_per_frame": round(ms.value / frames, 4)}
+        return out
+
+    results = {}
+    for mode in modes:
+        os.environ["CPV_BATCH"] = "1" if mode == "batched" else "0"
+        timed(args.warmup)
+        barrier(dist)
+        clocks = ClockSampler()
+        clocks.start()
+        launches0 = icd.cpv_kernel_launches()
+        frame_ms = timed(args.steps)
+        launches = icd.cpv_kernel_launches() - launches0
+        clock_info = clocks.stop()
+        barrier(dist)
+        total_ms = max_over_ranks(dist, sum(frame_ms))
+        kernels = profile(BATCH_KERNELS if mode == "batched" else PLAIN_KERNELS, min(args.steps, 5))
+        results[mode] = {"total_ms": total_ms, "launches": int(launches), "clocks": clock_info, "kernels": kernels}
+    head = modes[-1]
+    total_ms = results[head]["total_ms"]
     ms_per_step = total_ms / args.steps
     value = tris * args.steps * world / (total_ms / 1000.0) / 1e6
-    # Gaps between fenced frames removed: launch latency of back-to-back submits.
+    # Submit-to-fence latency of fenced frames, one at a time.
     _, lat = r.render(args.steps, latencies=True)
     # End to end through the API with host buffers.
     r.render_e2e(2)
     e2e_ms, h2d, d2h = r.render_e2e(args.steps)
     e2e_ms = max_over_ranks(dist, e2e_ms)
     e2e = tris * args.steps * world / (e2e_ms / 1000.0) / 1e6
-    # Per-kernel device time (CUDA events on the queue stream) for the roofline.
-    icd.cpv_profile_reset()
-    icd.cpv_profile_enable(1)
-    timed(args.steps)
-    icd.cpv_profile_enable(0)
-    kernels = {}
-    for k in ("cpv_raster", "cpv_setup_rects", "cpv_span_count", "cpv_scan", "cpv_span_write"):
-        n, ms = ctypes.c_uint64(0), ctypes.c_double(0.0)
-        icd.cpv_profile_get(k.encode(), ctypes.byref(n), ctypes.byref(ms))
-        if n.value:
-            kernels[k] = {"launches": n.value, "ms_per_launch": round(ms.value / n.value, 4)}
     color, depth = r.readback()
     r.close()
     line = None
     if rank == 0:
         from tests import oracle_binding
         oracle = oracle_binding.load()
-        _, _, st = oracle.render(scene)
+        st = oracle_stats(oracle, scene, args.config)
         tris_cpu, dt_cpu, cpu_desc = cpu_baseline(scene, args.cpu_seconds, 1)
         cpu_value = tris_cpu / dt_cpu / 1e6
         peak, peak_kind = measured_peak()
-        dom = "cpv_raster"
-        alg = algorithmic_bytes(args.config, scene, st["fragments_written"])
+        kernels = results[head]["kernels"]
+        dom = "cpv_batch_raster" if head == "batched" else "cpv_raster"
+        alg = algorithmic_bytes(args.config, scene, st.get("fragments_written"))
         achieved = alg / (kernels[dom]["ms_per_launch"] / 1000.0) / 1e9 if dom in kernels else None
         traffic = committed_traffic(dom, args.config)
+        frags = st.get("fragments")
         line = {
             "metric": "Mtri/s", "value": round(value, 3), "unit": "Mtri/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator, same bytes as the CPU oracle)",
-            "config": {"workload": args.config, "description": desc, "triangles": tris, "mode": "plain per-draw",
+            "config": {"workload": args.config, "description": desc, "triangles": tris, "draws": scene.draws, "mode": head,
                        "l2": "256 MiB fill between frames (untimed)", "pipeline_create_s": round(create_s, 3)},
-            "gfrag_s": round(st["fragments"] * args.steps * world / (total_ms / 1000.0) / 1e9, 4),
-            "frames_s": round(1000.0 * world / ms_per_step, 2),
+            "gfrag_s": round(frags * args.steps * world / (total_ms / 1000.0) / 1e9, 4) if frags else None,
+            "frames_s": round(1000.0 * world / ms_per_step, 3),
             "submit_to_fence_ms": {"p50": round(float(np.percentile(lat, 50)), 4), "p99": round(float(np.percentile(lat, 99)), 4)},
             "e2e": {"value": round(e2e, 3), "unit": "Mtri/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": round(e2e_ms / args.steps, 3)},
-            "gpu_launches": int(launches),
+            "gpu_launches": results[head]["launches"],
             "kernels": kernels,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
                          "traffic": traffic, "algorithmic_bytes_per_launch": alg},
-            "cpu_baseline": {"value": round(cpu_value, 4), "unit": "Mtri/s", "cores": 1, "kind": "port",
-                             "sample": cpu_desc},
-            "clocks": clock_info,
+            "cpu_baseline": {"value": round(cpu_value, 4), "unit": "Mtri/s", "cores": 1, "kind": "port", "sample": cpu_desc},
+            "clocks": results[head]["clocks"],
             "image_checksum": int(np.asarray(color, dtype=np.uint64).sum() % (1 << 61)),
         }
+        if "plain" in results and head != "plain":
+            pm = results["plain"]["total_ms"] / args.steps
+            line["plain"] = {"value": round(tris * world / (pm / 1000.0) / 1e6, 3), "unit": "Mtri/s", "ms_per_step": round(pm, 4),
+                             "frames_s": round(1000.0 * world / pm, 3), "gpu_launches": results["plain"]["launches"],
+                             "kernels": results["plain"]["kernels"], "clocks": results["plain"]["clocks"]}
+            line["batched_over_plain_frames"] = round(pm / ms_per_step, 3)
         print(json.dumps(line), flush=True)
     ctx.close()
     return line
+
+
+def oracle_stats(oracle, scene, workload):
+    """Fragment statistics of one frame from the oracle. The fragment count
+    (covered pixels that ran the fragment shader, before the depth test) of
+    a draw does not depend on the attachments, so a many-draw frame is
+    counted draw by draw on all host cores, each thread with its own
+    attachments."""
+    if scene.draws <= 1:
+        _, _, st = oracle.render(scene)
+        return st
+    import threading
+    lock = threading.Lock()
+    total = {"fragments": 0, "triangles": 0}
+    nxt = [0]
+
+    def worker(_):
+        color = depth = None
+        first = True
+        while True:
+            with lock:
+                i = nxt[0]
+                nxt[0] += 1
+            if i >= scene.draws:
+                return
+            color, depth, st = oracle.render(scene, i, i + 1, color=color, depth=depth, clear=first)
+            first = False
+            with lock:
+                total["fragments"] += st["fragments"]
+                total["triangles"] += st["triangles"]
+
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        list(ex.map(worker, range(os.cpu_count() or 1)))
+    return total
 
 
 def main():
@@ -333,7 +393,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=sorted(CONFIGS), default="heightfield")
+    ap.add_argument("--config", choices=sorted(CONFIGS), default="batch")
+    ap.add_argument("--mode", choices=["auto", "plain", "batched"], default="auto",
+                    help="auto: per-draw and batched where batching applies (render passes of 16+ draws)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="oracle time for the cpu_baseline figure")
     ap.add_argument("--ref-seconds", type=float, default=3.0, help="oracle time per step of --impl reference")
     args = ap.parse_args()

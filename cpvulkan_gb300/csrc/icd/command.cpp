@@ -288,6 +288,16 @@ uint32_t env_u32(const char* name, uint32_t dflt) {
     return v && *v ? static_cast<uint32_t>(std::strtoul(v, nullptr, 0)) : dflt;
 }
 
+// Module configuration of a batch over `pipelines`.
+ModuleConfig batch_config(const std::vector<Pipeline*>& pipelines) {
+    ModuleConfig mc;
+    mc.tile_shift = pipelines[0]->tile_shift;
+    bool dense = false;
+    for (const Pipeline* p : pipelines) dense = dense || p->prefers_deferred;
+    mc.schedule = schedule_for(dense);
+    return mc;
+}
+
 // Builds the batch of the render pass whose commands are (begin, end): the
 // draws' parameters, the pipeline set, the batched module and the plan.
 // Leaves state->plain set when the pass does not batch.
@@ -328,11 +338,7 @@ void build_batch(Queue* q, const CommandBuffer* cb, size_t begin, size_t end, co
     if (in.draws.empty()) return;
     in.vw = vw;
     in.vh = vh;
-    ModuleConfig mc;
-    mc.tile_shift = pipelines[0]->tile_shift;
-    for (const Pipeline* p : pipelines) mc.deferred = mc.deferred || p->prefers_deferred;
-    if (const char* d = std::getenv("CPV_DEFERRED")) mc.deferred = d[0] == '1';
-    rt::Module* m = batch_module(cb->device, pipelines, mc);
+    rt::Module* m = batch_module(cb->device, pipelines, batch_config(pipelines));
     if (!m) return;
     auto plan = std::make_unique<rt::BatchPlan>();
     if (plan->build(*m, in, q->stream) != rt::kOk) return;
@@ -481,11 +487,7 @@ void precompile_batches(CommandBuffer* cb) {
             break;
         case CmdType::EndRenderPass:
             if (in_pass && draws >= min_draws && !pipelines.empty() && pipelines.size() <= 16) {
-                ModuleConfig mc;
-                mc.tile_shift = pipelines[0]->tile_shift;
-                for (const Pipeline* p : pipelines) mc.deferred = mc.deferred || p->prefers_deferred;
-                if (const char* d = std::getenv("CPV_DEFERRED")) mc.deferred = d[0] == '1';
-                batch_module(cb->device, pipelines, mc);  // compiled and cached; errors surface at submit
+                batch_module(cb->device, pipelines, batch_config(pipelines));  // compiled and cached; errors surface at submit
             }
             in_pass = false;
             break;

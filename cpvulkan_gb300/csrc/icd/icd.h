@@ -163,10 +163,14 @@ struct Pipeline {
 // Tunables of a raster module, fixed at NVRTC time.
 struct ModuleConfig {
     uint32_t tile_shift = 4;  // 8, 16 or 32 px tiles
-    bool deferred = false;    // fragment schedule
+    uint32_t schedule = 0;    // fragment schedule: 0 immediate, 1 deferred, 2 sparse
     uint32_t warps = 8;       // warps per tile CTA (capped by the tile's pixels)
     uint32_t batch = 128;     // primitives set up per shared-memory batch
 };
+
+// Fragment schedule of a module whose pipelines prefer (or not) dense
+// shading; CPV_SCHEDULE=0/1/2 overrides.
+uint32_t schedule_for(bool prefers_deferred);
 
 // The CUDA translation unit of a module over one pipeline's stage block
 // (per-draw kernels) or several (batched kernels, pipeline i in namespace

@@ -61,6 +61,18 @@ const char* const kStageMacros[] = {
 
 }  // namespace
 
+uint32_t schedule_for(bool prefers_deferred) {
+    if (const char* v = std::getenv("CPV_SCHEDULE")) {
+        const int s = std::atoi(v);
+        if (s >= 0 && s <= 2) return static_cast<uint32_t>(s);
+    }
+    // The sparse schedule falls back to the immediate one batch by batch where
+    // primitives are large, so it serves every pipeline; dense shading
+    // (deferred) stays available through CPV_SCHEDULE=1.
+    (void)prefers_deferred;
+    return 2u;
+}
+
 std::string compose_module(const std::vector<std::string>& stages, const std::vector<uint32_t>& nvs, const ModuleConfig& mc, bool batched) {
     uint32_t nv_max = 0;
     for (uint32_t nv : nvs) nv_max = nv > nv_max ? nv : nv_max;
@@ -68,7 +80,7 @@ std::string compose_module(const std::vector<std::string>& stages, const std::ve
     src << "// " << kTranslationVersion << (batched ? " (batched)" : "") << "\n";
     src << "#define CPV_PIPELINE_MODULE 1\n";
     src << "#define CPV_TILE_SHIFT " << mc.tile_shift << "\n";
-    src << "#define CPV_DEFERRED " << (mc.deferred ? 1 : 0) << "\n";
+    src << "#define CPV_SCHEDULE " << mc.schedule << "\n";
     src << "#define CPV_RT_WARPS " << mc.warps << "\n";
     src << "#define CPV_BATCH " << mc.batch << "\n";
     src << "#define CPV_NV_MAX " << nv_max << "\n";
@@ -135,7 +147,7 @@ bool module_cubin(Device* dev, const std::string& source, std::array<uint8_t, 32
 }  // namespace
 
 rt::Module* batch_module(Device* dev, const std::vector<Pipeline*>& pipelines, const ModuleConfig& mc) {
-    std::string id = std::to_string(mc.tile_shift) + "/" + std::to_string(mc.deferred) + "/" + std::to_string(mc.warps) + "/" + std::to_string(mc.batch);
+    std::string id = std::to_string(mc.tile_shift) + "/" + std::to_string(mc.schedule) + "/" + std::to_string(mc.warps) + "/" + std::to_string(mc.batch);
     for (const Pipeline* p : pipelines) id += "/" + hex(p->key);
     std::lock_guard<std::mutex> lock(dev->batch_mutex);
     auto it = dev->batch_modules.find(id);
@@ -284,12 +296,8 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
 
     const uint32_t nv = vr.num_floats > fr.num_floats ? vr.num_floats : fr.num_floats;
     const uint32_t tile_shift = tile_shift_for_pipeline();
-    // Fragment schedule: deferred (dense shading) when the fragment shader
-    // samples images or is long; immediate otherwise. CPV_DEFERRED=0/1
-    // overrides (used by the autotuner and tests).
+    // Dense shading pays off when the fragment shader samples images or is long.
     const bool prefers_deferred = fr.samples > 0 || fr.instructions > 48;
-    bool deferred = prefers_deferred;
-    if (const char* d = std::getenv("CPV_DEFERRED")) deferred = d[0] == '1';
     // The pipeline's stage block: fixed-function macros, translated shaders
     // and the interpolation table. compose_module() wraps it in a namespace.
     std::ostringstream src;
@@ -336,7 +344,7 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     p->tile_shift = tile_shift;
     ModuleConfig mc;
     mc.tile_shift = tile_shift;
-    mc.deferred = deferred;
+    mc.schedule = schedule_for(prefers_deferred);
     p->source = compose_module({p->stage}, {nv}, mc, false);
     // The key covers the generated source and the embedded kernel headers it
     // includes, so an on-disk cache never returns a cubin of older kernels.

@@ -2,8 +2,8 @@
  * cpv_raster.cuh — the pipeline-independent part of the tile rasteriser,
  * shared by the per-draw module (cpv_pipeline.cuh) and the batched module
  * (cpv_batch.cuh). Compiled by NVRTC after cpv_device.cuh; the module prefix
- * defines CPV_TILE_SHIFT, CPV_DEFERRED and CPV_NV_MAX (the largest varying
- * count over the module's pipelines).
+ * defines CPV_TILE_SHIFT, CPV_SCHEDULE, CPV_RT_WARPS, CPV_BATCH and
+ * CPV_NV_MAX (the largest varying count over the module's pipelines).
  *
  * The per-pipeline part (primitive set-up, fragment shading and the
  * per-fragment operations, which depend on the pipeline's shaders and
@@ -18,8 +18,16 @@
 #ifndef CPV_TILE_SHIFT
 #define CPV_TILE_SHIFT 4
 #endif
-#ifndef CPV_DEFERRED
-#define CPV_DEFERRED 0
+#ifndef CPV_SCHEDULE
+#define CPV_SCHEDULE 0 /* 0 immediate, 1 deferred, 2 sparse (see cpv_raster_tile) */
+#endif
+#define CPV_DEFERRED (CPV_SCHEDULE == 1)
+#define CPV_SPARSE (CPV_SCHEDULE == 2)
+#ifndef CPV_SLOT_DEPTH
+#define CPV_SLOT_DEPTH 16 /* sparse: fragments a pixel takes per batch before its fallback */
+#endif
+#ifndef CPV_SMALL_PX
+#define CPV_SMALL_PX 32 /* sparse: largest in-tile bounding box one thread rasterises */
 #endif
 #ifndef CPV_RT_WARPS
 #define CPV_RT_WARPS 8
@@ -234,9 +242,47 @@ __device__ __forceinline__ uint32_t cpv_block_scan(uint32_t v, uint32_t& total, 
     return base + incl - v;
 }
 
+/* Sparse schedule: class of a primitive in the tile — 0 dead or outside the
+ * tile, 1 small (its bounding box covers at most CPV_SMALL_PX pixels of the
+ * tile), 2 large. */
+__device__ __forceinline__ uint32_t cpv_tile_class(const CpvTri& t, int32_t tile_x0, int32_t tile_y0) {
+    if (!cpv_tri_live(t)) return 0u;
+    const int4 box = t.box;
+    const int32_t x0 = max(box.x, tile_x0), x1 = min(box.z, tile_x0 + CPV_TILE);
+    const int32_t y0 = max(box.y, tile_y0), y1 = min(box.w, tile_y0 + CPV_TILE);
+    if (x1 <= x0 || y1 <= y0) return 0u;
+    return (x1 - x0) * (y1 - y0) > CPV_SMALL_PX ? 2u : 1u;
+}
+
+/* Sparse schedule: a small primitive j of the batch tests the pixels of its
+ * box inside the tile and appends j to the list of each covered one. A live
+ * primitive's box lies inside the attachment, so every listed pixel is
+ * inside it. */
+__device__ __forceinline__ void cpv_list_small(const CpvTri& t, uint32_t j, int32_t tile_x0, int32_t tile_y0, const float* col_ndc,
+                                               const float* row_ndc, uint32_t* list_count, uint8_t* list_j) {
+    if (cpv_tile_class(t, tile_x0, tile_y0) != 1u) return;
+    const int4 box = t.box;
+    const int32_t x0 = max(box.x, tile_x0), x1 = min(box.z, tile_x0 + CPV_TILE);
+    const int32_t y0 = max(box.y, tile_y0), y1 = min(box.w, tile_y0 + CPV_TILE);
+    for (int32_t y = y0; y < y1; y++) {
+        const float yf = row_ndc[y - tile_y0];
+        for (int32_t x = x0; x < x1; x++) {
+            float w[3];
+            if (!cpv_covers(t, col_ndc[x - tile_x0], yf, w)) continue;
+            const uint32_t p = static_cast<uint32_t>((y - tile_y0) * CPV_TILE + (x - tile_x0));
+            const uint32_t s = atomicAdd(&list_count[p], 1u);
+            if (s < CPV_SLOT_DEPTH) list_j[p * CPV_SLOT_DEPTH + s] = static_cast<uint8_t>(j);
+        }
+    }
+}
+
 /* Dynamic shared memory of the raster kernels: CPV_BATCH primitives, then
- * (deferred schedule) the fragment slots. */
-#define CPV_RASTER_SMEM_BYTES (CPV_BATCH * sizeof(CpvTri) + (CPV_DEFERRED ? CPV_NSLOT * (4u + 20u + 2u) : 0u))
+ * the schedule's buffers (deferred: fragment slots; sparse: per-pixel
+ * primitive lists, pixel-centre tables, the large-primitive list). */
+#define CPV_TILE_PX (CPV_TILE * CPV_TILE)
+#define CPV_SPARSE_BYTES (4u * CPV_TILE_PX + 8u * CPV_TILE + CPV_TILE_PX * CPV_SLOT_DEPTH + CPV_BATCH)
+#define CPV_RASTER_SMEM_BYTES \
+    (CPV_BATCH * sizeof(CpvTri) + (CPV_DEFERRED ? CPV_NSLOT * (4u + 20u + 2u) : 0u) + (CPV_SPARSE ? CPV_SPARSE_BYTES : 0u))
 
 /* One screen tile (tx, ty): loads the tile's attachment texels into
  * registers, walks the tile's primitives from `src` in API order in batches
@@ -253,16 +299,26 @@ __device__ __forceinline__ uint32_t cpv_block_scan(uint32_t v, uint32_t& total, 
  *   float vw, vh                             viewport extent (pixel centres)
  *   uint32_t fb_width, fb_height
  *
- * Two fragment schedules (CPV_DEFERRED):
- *   immediate — each pixel's thread shades its covered fragments as it finds
- *               them (cheap shaders, large primitives);
- *   deferred  — per batch of primitives, threads first record up to
+ * Three fragment schedules (CPV_SCHEDULE):
+ *   0 immediate — each pixel's thread tests every primitive of the batch and
+ *               shades its covered fragments as it finds them (cheap
+ *               shaders, large primitives);
+ *   1 deferred — per batch of primitives, threads first record up to
  *               CPV_SLOTS covered fragments each, the CTA then shades all
  *               recorded fragments densely (full warps, whatever the
  *               coverage pattern), and finally every pixel's thread applies
  *               its own fragments' per-fragment operations in primitive
- *               order (expensive shaders, small primitives).
- * Both apply each pixel's fragments in API primitive order, as the
+ *               order (expensive shaders);
+ *   2 sparse  — coverage is found per primitive instead of per pixel: a
+ *               primitive whose bounding box covers at most CPV_SMALL_PX
+ *               pixels of the tile is rasterised by one thread, which tests
+ *               only those pixels; larger ones are tested by the pixels'
+ *               threads. Either appends the primitive's batch index to each
+ *               covered pixel's list (up to CPV_SLOT_DEPTH per batch); each
+ *               pixel's thread then shades and applies its list in
+ *               primitive order (tiny primitives, heavy overdraw). A pixel
+ *               whose list overflowed walks the whole batch instead.
+ * All apply each pixel's fragments in API primitive order, as the
  * reference's serial loop does. */
 template <class Source>
 __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32_t ty, CpvTri* tris, uint32_t* warp_sums) {
@@ -288,6 +344,23 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
     float* slot_f = reinterpret_cast<float*>(slot_jk + CPV_NSLOT);       /* 5 floats per slot: w0 w1 w2 → rgba + mapped */
     uint16_t* dense = reinterpret_cast<uint16_t*>(slot_f + 5 * CPV_NSLOT);
 #endif
+#if CPV_SPARSE
+    static_assert(CPV_BATCH <= 256, "batch indices are stored in bytes");
+    uint32_t* list_count = reinterpret_cast<uint32_t*>(tris + CPV_BATCH);  /* per tile pixel: fragments listed this batch */
+    float* col_ndc = reinterpret_cast<float*>(list_count + CPV_TILE_PX);    /* pixel-centre NDC of the tile's columns … */
+    float* row_ndc = col_ndc + CPV_TILE;                                     /* … and rows (the values of cpv_pixel_ndc) */
+    uint8_t* list_j = reinterpret_cast<uint8_t*>(row_ndc + CPV_TILE);       /* per tile pixel: CPV_SLOT_DEPTH batch indices */
+    uint8_t* large = list_j + CPV_TILE_PX * CPV_SLOT_DEPTH;                  /* batch indices of large primitives, in order */
+    const int32_t tile_x0 = static_cast<int32_t>(tx * CPV_TILE), tile_y0 = static_cast<int32_t>(ty * CPV_TILE);
+    for (uint32_t i = threadIdx.x; i < CPV_TILE_PX; i += CPV_RT_THREADS) list_count[i] = 0u;
+    for (uint32_t i = threadIdx.x; i < CPV_TILE; i += CPV_RT_THREADS) {
+        col_ndc[i] = cpv_pixel_ndc(tile_x0 + static_cast<int32_t>(i), src.vw);
+        row_ndc[i] = cpv_pixel_ndc(tile_y0 + static_cast<int32_t>(i), src.vh);
+    }
+    uint32_t lp[CPV_PPT]; /* this thread's pixels, as tile pixel indices */
+#pragma unroll
+    for (int k = 0; k < CPV_PPT; k++) lp[k] = static_cast<uint32_t>((py[k] - tile_y0) * CPV_TILE + (px[k] - tile_x0));
+#endif
 
     for (uint64_t base = 0; base < end; base += CPV_BATCH) {
         const uint32_t n = static_cast<uint32_t>((end - base) < CPV_BATCH ? (end - base) : CPV_BATCH);
@@ -295,20 +368,102 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
         /* a tile of 8 × 8 has fewer threads than CPV_BATCH: stride the set-up */
         for (uint32_t i = threadIdx.x; i < n; i += CPV_RT_THREADS) src.setup(base + i, tris[i]);
         __syncthreads();
-#if !CPV_DEFERRED
-        for (uint32_t j = 0; j < n; j++) {
-            const CpvTri& t = tris[j];
-            if (!cpv_tri_live(t)) continue;
-            const int4 box = t.box;
+#if CPV_SPARSE
+        /* 1. classify: large primitives (box covering more than CPV_SMALL_PX
+         *    pixels of the tile) are collected in batch order, in rounds of
+         *    one primitive per thread */
+        uint32_t nlarge = 0u;
+        for (uint32_t round = 0; round < n; round += CPV_RT_THREADS) {
+            const uint32_t j = round + threadIdx.x;
+            const uint32_t is_large = j < n && cpv_tile_class(tris[j], tile_x0, tile_y0) == 2u ? 1u : 0u;
+            uint32_t round_large;
+            const uint32_t lpos = cpv_block_scan(is_large, round_large, warp_sums);
+            if (is_large) large[nlarge + lpos] = static_cast<uint8_t>(j);
+            nlarge += round_large;
+            __syncthreads();
+        }
+        /* mostly large primitives: this batch runs the immediate schedule */
+        const bool immediate_batch = nlarge * 4u >= 3u * n;
+        if (!immediate_batch) {
+            /* 2. small primitives: one thread each lists the pixels it covers */
+            for (uint32_t j = threadIdx.x; j < n; j += CPV_RT_THREADS)
+                cpv_list_small(tris[j], j, tile_x0, tile_y0, col_ndc, row_ndc, list_count, list_j);
+            /* 3. large primitives, in order: every pixel's thread tests its pixels */
+            for (uint32_t m = 0; m < nlarge; m++) {
+                const uint32_t j = large[m];
+                const CpvTri& t = tris[j];
+                const int4 box = t.box;
+#pragma unroll
+                for (int k = 0; k < CPV_PPT; k++) {
+                    if (!inside[k]) continue;
+                    if (px[k] < box.x || px[k] >= box.z || py[k] < box.y || py[k] >= box.w) continue;
+                    float w[3];
+                    if (!cpv_covers(t, xf[k], yf[k], w)) continue;
+                    const uint32_t s = atomicAdd(&list_count[lp[k]], 1u);
+                    if (s < CPV_SLOT_DEPTH) list_j[lp[k] * CPV_SLOT_DEPTH + s] = static_cast<uint8_t>(j);
+                }
+            }
+            __syncthreads();
+            /* 4. each pixel shades and applies its list in batch (API) order */
 #pragma unroll
             for (int k = 0; k < CPV_PPT; k++) {
-                if (!inside[k]) continue;
-                if (px[k] < box.x || px[k] >= box.z || py[k] < box.y || py[k] >= box.w) continue;
-                float w[3];
-                if (!cpv_covers(t, xf[k], yf[k], w)) continue;
-                float colour[4], mapped;
-                if (src.shade(t, w, px[k], py[k], colour, mapped)) continue;
-                src.rop(t, colour, mapped, st[k]);
+                const uint32_t c = list_count[lp[k]];
+                if (c == 0u) continue;
+                if (c <= CPV_SLOT_DEPTH) {
+                    const uint8_t* lj = list_j + lp[k] * CPV_SLOT_DEPTH;
+                    int32_t last = -1;
+                    for (uint32_t it = 0; it < c; it++) {
+                        /* next batch index after `last` (a primitive covers a pixel once) */
+                        int32_t j = 0x7FFFFFFF;
+                        for (uint32_t e = 0; e < c; e++) {
+                            const int32_t v = lj[e];
+                            if (v > last && v < j) j = v;
+                        }
+                        last = j;
+                        const CpvTri& t = tris[j];
+                        float w[3], colour[4], mapped;
+                        cpv_covers(t, xf[k], yf[k], w);
+                        if (src.shade(t, w, px[k], py[k], colour, mapped)) continue;
+                        src.rop(t, colour, mapped, st[k]);
+                    }
+                } else {
+                    /* list overflow: walk the whole batch for this pixel */
+                    for (uint32_t j = 0; j < n; j++) {
+                        const CpvTri& t = tris[j];
+                        if (!cpv_tri_live(t)) continue;
+                        const int4 box = t.box;
+                        if (px[k] < box.x || px[k] >= box.z || py[k] < box.y || py[k] >= box.w) continue;
+                        float w[3], colour[4], mapped;
+                        if (!cpv_covers(t, xf[k], yf[k], w)) continue;
+                        if (src.shade(t, w, px[k], py[k], colour, mapped)) continue;
+                        src.rop(t, colour, mapped, st[k]);
+                    }
+                }
+                list_count[lp[k]] = 0u;
+            }
+        }
+#else
+        const bool immediate_batch = true;
+        (void)immediate_batch;
+#endif
+#if !CPV_DEFERRED
+        /* immediate: every pixel's thread tests each primitive in order,
+         * shading and applying what it covers */
+        if (immediate_batch) {
+            for (uint32_t j = 0; j < n; j++) {
+                const CpvTri& t = tris[j];
+                if (!cpv_tri_live(t)) continue;
+                const int4 box = t.box;
+#pragma unroll
+                for (int k = 0; k < CPV_PPT; k++) {
+                    if (!inside[k]) continue;
+                    if (px[k] < box.x || px[k] >= box.z || py[k] < box.y || py[k] >= box.w) continue;
+                    float w[3];
+                    if (!cpv_covers(t, xf[k], yf[k], w)) continue;
+                    float colour[4], mapped;
+                    if (src.shade(t, w, px[k], py[k], colour, mapped)) continue;
+                    src.rop(t, colour, mapped, st[k]);
+                }
             }
         }
 #else

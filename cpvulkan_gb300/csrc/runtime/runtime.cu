@@ -72,6 +72,7 @@ std::mutex g_prof_mutex;
 bool g_prof_on = false;
 std::vector<ProfileRecord> g_prof_records;
 std::vector<cudaEvent_t> g_prof_free;
+size_t g_prof_open = 0;  // markers begun and not yet ended
 struct ProfileTotal {
     uint64_t count = 0;
     double ms = 0.0;
@@ -124,15 +125,21 @@ void profile_begin(cudaStream_t s, const char* name) {
     r.start = prof_event();
     cudaEventRecord(r.start, s);
     g_prof_records.push_back(r);
+    g_prof_open++;
 }
 
 void profile_end(cudaStream_t s) {
     if (!g_prof_on) return;
     std::lock_guard<std::mutex> lock(g_prof_mutex);
-    if (g_prof_records.empty() || g_prof_records.back().end) return;
-    g_prof_records.back().end = prof_event();
-    cudaEventRecord(g_prof_records.back().end, s);
-    if (g_prof_records.size() > 4096) prof_drain();
+    // Close the innermost open marker (markers nest).
+    for (size_t i = g_prof_records.size(); i-- > 0;) {
+        if (g_prof_records[i].end) continue;
+        g_prof_records[i].end = prof_event();
+        cudaEventRecord(g_prof_records[i].end, s);
+        g_prof_open--;
+        break;
+    }
+    if (g_prof_open == 0 && g_prof_records.size() > 4096) prof_drain();
 }
 
 int profile_get(const char* name, uint64_t* count, double* ms) {
@@ -613,11 +620,15 @@ int BatchPlan::enqueue(const Module& m, cudaStream_t stream) {
         kernels_ = 0;
         return kOk;  // no primitive: nothing to draw
     }
+    // Profile markers (only when profiling, which also bypasses the graph).
     {
         void* args[] = {&P_};
+        profile_begin(stream, "cpv_batch_setup");
         CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.setup_rects), dim3(blocks), dim3(CPV_BATCH_BLOCK), args, 0, stream));
+        profile_end(stream);
         count_launch();
     }
+    profile_begin(stream, "cpv_batch_bin");
     int r = scan_u32(stream, block_pairs_, block_offsets_, blocks, words_, scan_);
     if (r != kOk) return r;
     cpv_batch_emit<<<blocks, 256, 0, stream>>>(rects_, block_offsets_, P_.tiles_x, keys_[0], vals_[0], cap_, words_);
@@ -639,9 +650,12 @@ int BatchPlan::enqueue(const Module& m, cudaStream_t stream) {
     cpv_tile_ranges<<<radix_ctas_, 256, 0, stream>>>(keys_[fin], words_, cap_, tile_begin_, tile_end_);
     count_launch();
     CPV_CUDA(cudaMemsetAsync(words_ + 2, 0, sizeof(uint32_t), stream));
+    profile_end(stream);
     {
         void* args[] = {&P_};
+        profile_begin(stream, "cpv_batch_raster");
         CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.raster), dim3(raster_ctas_), dim3(m.raster_threads), args, m.raster_smem, stream));
+        profile_end(stream);
         count_launch();
     }
     CPV_CUDA(cudaMemcpyAsync(pinned_pairs_, words_, 4, cudaMemcpyDeviceToHost, stream));
@@ -663,6 +677,13 @@ int BatchPlan::launch(const Module& m, cudaStream_t stream) {
         if (r != kOk) return r;
     }
     cudaGetLastError();
+    if (profile_enabled()) {
+        // Per-kernel timing needs the events between the kernels: run eagerly.
+        const int r = enqueue(m, stream);
+        if (r != kOk) return r;
+        CPV_CUDA(cudaEventRecord(done_, stream));
+        return kOk;
+    }
     if (!exec_ && env_u32("CPV_BATCH_GRAPH", 1u)) {
         // Capture the sequence once; later launches replay the graph.
         cudaGraph_t graph = nullptr;

@@ -59,10 +59,10 @@ def test_batched_equals_plain_and_oracle(gpu_ctx, oracle, plain, seed):
 
 
 @pytest.mark.parametrize("tile", ["8", "16", "32"])
-@pytest.mark.parametrize("deferred", ["0", "1"])
-def test_batched_schedules(gpu_ctx, plain, monkeypatch, tile, deferred):
+@pytest.mark.parametrize("schedule", ["0", "1", "2"])
+def test_batched_schedules(gpu_ctx, plain, monkeypatch, tile, schedule):
     monkeypatch.setenv("CPV_TILE", tile)
-    monkeypatch.setenv("CPV_DEFERRED", deferred)
+    monkeypatch.setenv("CPV_SCHEDULE", schedule)
     scene = c.Scene(c.BATCH, 3, [40, 3000, 400, 272])
     ref = plain(gpu_ctx, scene)[0]
     same(frames(gpu_ctx, scene)[0], ref)

@@ -80,13 +80,13 @@ def test_serve_request(gpu_ctx, oracle):
 
 
 @pytest.mark.parametrize("tile", ["8", "16", "32"])
-@pytest.mark.parametrize("deferred", ["0", "1"])
+@pytest.mark.parametrize("schedule", ["0", "1", "2"])
 @pytest.mark.parametrize("config,params", [(c.HEIGHTFIELD, [96, 320, 200]), (c.BLEND, [600, 320, 200]), (c.BATCH, [24, 2000, 320, 200])])
-def test_schedule_invariance(gpu_ctx, oracle, monkeypatch, tile, deferred, config, params):
+def test_schedule_invariance(gpu_ctx, oracle, monkeypatch, tile, schedule, config, params):
     """Tile size and fragment schedule change only the work distribution:
     every combination must reproduce the oracle's image exactly."""
     monkeypatch.setenv("CPV_TILE", tile)
-    monkeypatch.setenv("CPV_DEFERRED", deferred)
+    monkeypatch.setenv("CPV_SCHEDULE", schedule)
     scene = c.Scene(config, 7, params)
     report, _ = check(gpu_ctx, oracle, scene)
     assert report["color_pixels_differing"] == 0, report
