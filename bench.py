@@ -41,6 +41,16 @@ FLUSH_BYTES = 256 << 20
 FALLBACK_HBM_GBS = 6800.0
 
 
+def workload(args):
+    """(harness config, scene parameters, description) of the run; --params
+    replaces the scene parameters (smaller cases for profiling)."""
+    cfg, params, desc = CONFIGS[args.config]
+    if args.params:
+        params = [int(v) for v in args.params.split(",")]
+        desc += " [params %s]" % args.params
+    return cfg, params, desc
+
+
 def algorithmic_bytes(name, scene, frag_written):
     """Bytes the frame must move at least once (inputs read, attachments written/read)."""
     w, h = scene.width, scene.height
@@ -206,7 +216,7 @@ def run_reference(args, world, rank, dist):
     c.build()
     if rank != 0:
         return
-    cfg, params, cfg_desc = CONFIGS[args.config]
+    cfg, params, cfg_desc = workload(args)
     scene = c.Scene(cfg, 1, params)
     threads = os.cpu_count() or 1
     per_step = []
@@ -243,7 +253,7 @@ def run_ours(args, world, rank, dist):
     icd = ctypes.CDLL(c.ICD_PATH)
     icd.cpv_kernel_launches.restype = ctypes.c_uint64
     icd.cpv_profile_get.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_double)]
-    cfg, params, desc = CONFIGS[args.config]
+    cfg, params, desc = workload(args)
     scene = c.Scene(cfg, 1, params)
     tris = scene.triangles
     # Batching applies to render passes with many draws; one-draw scenes
@@ -394,6 +404,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", choices=sorted(CONFIGS), default="batch")
+    ap.add_argument("--params", default="", help="comma-separated scene parameters replacing the workload's (profiling cases)")
     ap.add_argument("--mode", choices=["auto", "plain", "batched"], default="auto",
                     help="auto: per-draw and batched where batching applies (render passes of 16+ draws)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="oracle time for the cpu_baseline figure")

@@ -290,12 +290,9 @@ uint32_t env_u32(const char* name, uint32_t dflt) {
 
 // Module configuration of a batch over `pipelines`.
 ModuleConfig batch_config(const std::vector<Pipeline*>& pipelines) {
-    ModuleConfig mc;
-    mc.tile_shift = pipelines[0]->tile_shift;
     bool dense = false;
     for (const Pipeline* p : pipelines) dense = dense || p->prefers_deferred;
-    mc.schedule = schedule_for(dense);
-    return mc;
+    return module_config(pipelines[0]->tile_shift, dense);
 }
 
 // Builds the batch of the render pass whose commands are (begin, end): the

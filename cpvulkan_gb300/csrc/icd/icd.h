@@ -171,6 +171,9 @@ struct ModuleConfig {
 // Fragment schedule of a module whose pipelines prefer (or not) dense
 // shading; CPV_SCHEDULE=0/1/2 overrides.
 uint32_t schedule_for(bool prefers_deferred);
+// Module configuration for a tile size and shading preference, with the
+// environment's tunables applied.
+ModuleConfig module_config(uint32_t tile_shift, bool prefers_deferred);
 
 // The CUDA translation unit of a module over one pipeline's stage block
 // (per-draw kernels) or several (batched kernels, pipeline i in namespace

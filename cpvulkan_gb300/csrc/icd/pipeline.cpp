@@ -61,6 +61,23 @@ const char* const kStageMacros[] = {
 
 }  // namespace
 
+ModuleConfig module_config(uint32_t tile_shift, bool prefers_deferred) {
+    ModuleConfig mc;
+    mc.tile_shift = tile_shift;
+    mc.schedule = schedule_for(prefers_deferred);
+    // Tunables (CPV_RT_WARPS 1-32 warps per tile CTA, CPV_BATCH_PRIMS 32-256
+    // primitives per shared-memory batch).
+    if (const char* v = std::getenv("CPV_RT_WARPS")) {
+        const int w = std::atoi(v);
+        if (w >= 1 && w <= 32) mc.warps = static_cast<uint32_t>(w);
+    }
+    if (const char* v = std::getenv("CPV_BATCH_PRIMS")) {
+        const int b = std::atoi(v);
+        if (b >= 32 && b <= 256) mc.batch = static_cast<uint32_t>(b);
+    }
+    return mc;
+}
+
 uint32_t schedule_for(bool prefers_deferred) {
     if (const char* v = std::getenv("CPV_SCHEDULE")) {
         const int s = std::atoi(v);
@@ -342,10 +359,7 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     p->nv = nv;
     p->prefers_deferred = prefers_deferred;
     p->tile_shift = tile_shift;
-    ModuleConfig mc;
-    mc.tile_shift = tile_shift;
-    mc.schedule = schedule_for(prefers_deferred);
-    p->source = compose_module({p->stage}, {nv}, mc, false);
+    p->source = compose_module({p->stage}, {nv}, module_config(tile_shift, prefers_deferred), false);
     // The key covers the generated source and the embedded kernel headers it
     // includes, so an on-disk cache never returns a cubin of older kernels.
     {

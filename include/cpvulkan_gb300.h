@@ -65,6 +65,15 @@ CPV_EXPORT int cpv_device_available(void);
 CPV_EXPORT int cpv_queue_record(VkQueue queue, uint32_t slot);
 CPV_EXPORT double cpv_queue_elapsed_ms(VkQueue queue, uint32_t slot_begin, uint32_t slot_end);
 
+/* Per-kernel device timing: while enabled, every kernel of the draw paths is
+ * bracketed by CUDA events on its stream (batched render passes then run
+ * without their CUDA graph). cpv_profile_get returns the launches and the
+ * summed milliseconds recorded under `kernel` (e.g. "cpv_raster",
+ * "cpv_batch_raster"); cpv_profile_reset clears the totals. */
+CPV_EXPORT void cpv_profile_enable(int on);
+CPV_EXPORT int cpv_profile_get(const char* kernel, uint64_t* launches, double* total_ms);
+CPV_EXPORT void cpv_profile_reset(void);
+
 /* ---- submission without allocation (no counterpart in the reference) ----
  *
  * Same signature and results as vkQueueSubmit, for callers that cannot
