@@ -1,13 +1,17 @@
 """Benchmark of the draw hot path (one JSON line on rank 0).
 
-Default workload: the textured heightfield (1024x1024 grid, 2,093,058
-triangles, 1920x1080 RGBA8 + D32, trilinear texture, Lambert), rendered through
-the Vulkan ICD. A step is one frame: one vkQueueSubmit of the recorded
-command buffer (render-pass clear + the draw) and its fence.
+Default workload: 4096 indexed icosphere draws in one render pass (755 M
+triangles with instancing, 2560x1440 RGBA8 + D32, opaque and src-over
+pipelines), rendered through the Vulkan ICD per draw and batched (the
+metric is batched vs per-draw). Other workloads: cube, heightfield (1024x1024
+grid, trilinear texture), blend (200k quads), serve (64 clients). A step is
+one frame: one vkQueueSubmit of the recorded command buffer (render-pass
+clear + the draws) and its fence.
 
   value  Mtri/s with scene data resident in HBM, device time of K frames
          (queue events around each frame; a 256 MiB vkCmdFillBuffer before
          every frame evicts the 129 MB L2 and is not timed).
+  plain  the same frames through the per-draw path (many-draw workloads).
   e2e    the same metric through the public API with host buffers: every
          step maps/copies/unmaps the vertex, index and uniform bytes, copies
          them to device-local buffers, renders, copies the colour image to a
@@ -36,6 +40,8 @@ CONFIGS = {
     "heightfield": (2, [], "textured heightfield 1024x1024 grid (2,093,058 tris, u32 indices), 1920x1080 RGBA8+D32, trilinear, Lambert"),
     "blend": (3, [], "200k screen-space quads (400k tris), sides log-uniform 4-256 px, src-over blend, 1920x1080 RGBA8"),
     "batch": (4, [], "4096 indexed icosphere draws (12-200k tris, 25% instanced 1-64x), 70/30 opaque/blended, 2560x1440 RGBA8+D32"),
+    "serve": (6, [], "64 offscreen clients, Poisson arrivals (mean 2 ms each), 256-2048 px RGBA8+D32 images of 1k-500k textured "
+                     "triangles, resident pipelines and attachments, 16 queues"),
 }
 FLUSH_BYTES = 256 << 20
 FALLBACK_HBM_GBS = 6800.0
@@ -363,6 +369,60 @@ def run_ours(args, world, rank, dist):
     return line
 
 
+def run_serve(args, world, rank, dist):
+    """Serving: the arrivals of args.serve_seconds per client, admitted into
+    16 queues as slots free up, through vkQueueSubmit and fences."""
+    import cpvulkan_gb300 as c
+    c.build()
+    if not c.device_available():
+        raise SystemExit("bench.py: no CUDA device — the GB300 path needs a GPU (no CPU fallback exists)")
+    import ctypes
+    icd = ctypes.CDLL(c.ICD_PATH)
+    icd.cpv_kernel_launches.restype = ctypes.c_uint64
+    ctx = c.Context()
+    t0 = time.time()
+    server = c.Server(ctx, clients=64, slots=16, mean_interarrival_ms=2.0, duration_s=args.serve_seconds, seed=5 + rank)
+    create_s = time.time() - t0
+    barrier(dist)
+    clocks = ClockSampler()
+    clocks.start()
+    launches0 = icd.cpv_kernel_launches()
+    st = server.run()
+    launches = icd.cpv_kernel_launches() - launches0
+    clock_info = clocks.stop()
+    barrier(dist)
+    wall_ms = max_over_ranks(dist, st["wall_s"] * 1000.0)
+    tris = st["triangles"] * world  # replicas: every rank serves its own clients
+    value = tris / (wall_ms / 1000.0) / 1e6
+    line = None
+    if rank == 0:
+        scene = c.Scene(6, 5, [512, 20000, 0])
+        tris_cpu, dt_cpu, cpu_desc = cpu_baseline(scene, args.cpu_seconds, 1)
+        line = {
+            "metric": "Mtri/s", "value": round(value, 3), "unit": "Mtri/s", "n_gpus": world, "steps": int(st["completed"]),
+            "warmup": 16, "ms_per_step": round(wall_ms / max(1, st["completed"]), 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded client scenes and arrivals)",
+            "config": {"workload": "serve", "description": CONFIGS["serve"][2], "clients": 64, "queues": 16,
+                       "arrival_window_s": args.serve_seconds, "resident_clients": st["resident_clients"],
+                       "resident_bytes": st["resident_bytes"], "client_create_s": round(create_s, 2)},
+            "requests": st["requests"], "completed": st["completed"], "max_in_flight": st["max_in_flight"],
+            "latency_ms": {"p50": round(st["latency_p50_ms"], 3), "p99": round(st["latency_p99_ms"], 3), "from": "arrival"},
+            "submit_to_fence_ms": {"p50": round(st["submit_p50_ms"], 3), "p99": round(st["submit_p99_ms"], 3)},
+            "queue_wait_ms": {"p50": round(st["queue_p50_ms"], 3), "p99": round(st["queue_p99_ms"], 3)},
+            "e2e": {"value": round(value, 3), "unit": "Mtri/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                    "note": "clients' data are resident by design; requests go through vkQueueSubmit and fences, wall-clock timed"},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": "cpv_raster", "achieved": None, "peak": measured_peak()[0], "unit": "GB/s",
+                         "frac": None, "traffic": None, "note": "many small launches; see the per-draw workloads"},
+            "cpu_baseline": {"value": round(tris_cpu / dt_cpu / 1e6, 4), "unit": "Mtri/s", "cores": 1, "kind": "port", "sample": cpu_desc},
+            "clocks": clock_info,
+        }
+        print(json.dumps(line), flush=True)
+    server.close()
+    ctx.close()
+    return line
+
+
 def oracle_stats(oracle, scene, workload):
     """Fragment statistics of one frame from the oracle. The fragment count
     (covered pixels that ran the fragment shader, before the depth test) of
@@ -404,6 +464,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", choices=sorted(CONFIGS), default="batch")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the serving workload")
     ap.add_argument("--params", default="", help="comma-separated scene parameters replacing the workload's (profiling cases)")
     ap.add_argument("--mode", choices=["auto", "plain", "batched"], default="auto",
                     help="auto: per-draw and batched where batching applies (render passes of 16+ draws)")
@@ -414,6 +475,8 @@ def main():
     world, rank, dist = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank, dist)
+    elif args.config == "serve":
+        run_serve(args, world, rank, dist)
     else:
         run_ours(args, world, rank, dist)
     if dist is not None:

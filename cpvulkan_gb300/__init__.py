@@ -92,6 +92,17 @@ def harness():
     h.cpvh_queue.restype = vp
     h.cpvh_queue.argtypes = [vp]
     h.cpvh_last_error.restype = cp
+    h.cpvh_server_create.restype = vp
+    h.cpvh_server_create.argtypes = [vp, ctypes.POINTER(ServeConfig), cp, u32]
+    h.cpvh_server_run.restype = ctypes.c_int
+    h.cpvh_server_run.argtypes = [vp, ctypes.POINTER(ServeResult)]
+    h.cpvh_server_clients.restype = u32
+    h.cpvh_server_clients.argtypes = [vp]
+    h.cpvh_server_client.restype = vp
+    h.cpvh_server_client.argtypes = [vp, u32]
+    h.cpvh_server_scene.restype = vp
+    h.cpvh_server_scene.argtypes = [vp, u32]
+    h.cpvh_server_destroy.argtypes = [vp]
     _harness = h
     return h
 
@@ -183,7 +194,7 @@ class Renderer:
         lat = (ctypes.c_double * frames)() if latencies else None
         r = harness().cpvh_render(self.ptr, frames, ctypes.byref(dev), lat)
         if r != VK_SUCCESS:
-            raise RuntimeError("render failed (%d): %s" % (r, harness().cpvh_last_error().decode()))
+            raise RuntimeError("render failed (%d): %s %s" % (r, harness().cpvh_last_error().decode(), icd_last_error()))
         return dev.value, (np.array(lat[:]) if latencies else None)
 
     def render_e2e(self, frames=1):
@@ -210,9 +221,83 @@ class Renderer:
         return color, depth
 
     def close(self):
-        if self.ptr:
+        if self.ptr and getattr(self, "owned", True):  # server client views belong to their server
             harness().cpvh_renderer_destroy(self.ptr)
+        self.ptr = None
+
+
+class ServeConfig(ctypes.Structure):
+    """cpvh_serve_config (include/cpv_harness.h)."""
+    _fields_ = [("clients", ctypes.c_uint32), ("slots", ctypes.c_uint32), ("mean_interarrival_ms", ctypes.c_double),
+                ("duration_s", ctypes.c_double), ("seed", ctypes.c_uint64), ("hbm_budget_bytes", ctypes.c_uint64),
+                ("min_tris", ctypes.c_uint32), ("max_tris", ctypes.c_uint32), ("max_side", ctypes.c_uint32)]
+
+
+class ServeResult(ctypes.Structure):
+    """cpvh_serve_result (include/cpv_harness.h)."""
+    _fields_ = [("requests", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("triangles", ctypes.c_uint64),
+                ("resident_clients", ctypes.c_uint32), ("max_in_flight", ctypes.c_uint32), ("resident_bytes", ctypes.c_uint64),
+                ("wall_s", ctypes.c_double), ("mtri_s", ctypes.c_double),
+                ("latency_p50_ms", ctypes.c_double), ("latency_p99_ms", ctypes.c_double),
+                ("submit_p50_ms", ctypes.c_double), ("submit_p99_ms", ctypes.c_double),
+                ("queue_p50_ms", ctypes.c_double), ("queue_p99_ms", ctypes.c_double)]
+
+
+class _ClientScene:
+    """Dimensions of a server client's scene (for readback buffers)."""
+
+    def __init__(self, ptr):
+        hdr = SceneHeader.from_address(ptr)
+        self.ptr = ptr
+        self.width, self.height = hdr.width, hdr.height
+        self.color_format, self.depth_format = hdr.color_format, hdr.depth_format
+
+
+class Server:
+    """Continuous-batching serving loop over resident offscreen clients."""
+
+    def __init__(self, ctx, clients=64, slots=16, mean_interarrival_ms=2.0, duration_s=10.0, seed=5, hbm_budget_bytes=64 << 30,
+                 min_tris=1000, max_tris=500000, max_side=0):
+        cfg = ServeConfig(clients, slots, mean_interarrival_ms, duration_s, seed, hbm_budget_bytes, min_tris, max_tris, max_side)
+        err = ctypes.create_string_buffer(4096)
+        self.ptr = harness().cpvh_server_create(ctx.ptr, ctypes.byref(cfg), err, len(err))
+        if not self.ptr:
+            raise RuntimeError("server creation failed: " + err.value.decode(errors="replace"))
+
+    @property
+    def clients(self):
+        return harness().cpvh_server_clients(self.ptr)
+
+    def run(self):
+        res = ServeResult()
+        r = harness().cpvh_server_run(self.ptr, ctypes.byref(res))
+        if r != VK_SUCCESS:
+            raise RuntimeError("serving loop failed (%d)" % r)
+        return {k: getattr(res, k) for k, _ in ServeResult._fields_}
+
+    def client(self, i):
+        """A Renderer view of client i (readback, render alone)."""
+        ptr = harness().cpvh_server_client(self.ptr, i)
+        if not ptr:
+            return None
+        view = Renderer.__new__(Renderer)
+        view.ptr = ptr
+        view.ctx = None
+        view.scene = _ClientScene(harness().cpvh_server_scene(self.ptr, i))
+        view.owned = False
+        return view
+
+    def close(self):
+        if self.ptr:
+            harness().cpvh_server_destroy(self.ptr)
             self.ptr = None
+
+
+def icd_last_error():
+    """The ICD's last error message on this thread (cpv_last_error)."""
+    lib = ctypes.CDLL(ICD_PATH)
+    lib.cpv_last_error.restype = ctypes.c_char_p
+    return lib.cpv_last_error().decode(errors="replace")
 
 
 def device_available():

@@ -7,10 +7,13 @@
 // Samples/utils/util_init.cpp), without a window system.
 #include <dlfcn.h>
 
+#include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <string>
 #include <vector>
 
@@ -94,6 +97,7 @@ struct Fns {
     CPVH_FN(vkDestroyFence)
     CPVH_FN(vkResetFences)
     CPVH_FN(vkWaitForFences)
+    CPVH_FN(vkGetFenceStatus)
 };
 #undef CPVH_FN
 
@@ -114,7 +118,8 @@ struct cpvh_context {
     VkInstance instance = nullptr;
     VkPhysicalDevice physical = nullptr;
     VkDevice device = nullptr;
-    VkQueue queue = nullptr;
+    VkQueue queue = nullptr;          // queues[0]
+    std::vector<VkQueue> queues;      // every queue of the device's queue family
     VkPhysicalDeviceMemoryProperties mem{};
     VkPipelineCache cache = nullptr;
     PFN_cpv_queue_record record = nullptr;
@@ -559,11 +564,16 @@ cpvh_context* cpvh_open(const char* icd_path, char* err, uint32_t err_len) {
     if (f.vkEnumeratePhysicalDevices(c->instance, &n, &c->physical) != VK_SUCCESS || n < 1) return fail("no physical device", c);
     if (!check_dispatch(c->physical)) return fail("VkPhysicalDevice lacks the loader magic", c);
     f.vkGetPhysicalDeviceMemoryProperties(c->physical, &c->mem);
-    const float prio = 1.0f;
+    // All queues of family 0: the serving loop runs requests on several.
+    VkQueueFamilyProperties family{};
+    uint32_t families = 1;
+    f.vkGetPhysicalDeviceQueueFamilyProperties(c->physical, &families, &family);
+    const uint32_t nqueues = families >= 1 && family.queueCount >= 1 ? family.queueCount : 1;
+    const std::vector<float> prio(nqueues, 1.0f);
     VkDeviceQueueCreateInfo qci{};
     qci.sType = VK_STRUCTURE_TYPE_DEVICE_QUEUE_CREATE_INFO;
-    qci.queueCount = 1;
-    qci.pQueuePriorities = &prio;
+    qci.queueCount = nqueues;
+    qci.pQueuePriorities = prio.data();
     VkDeviceCreateInfo dci{};
     dci.sType = VK_STRUCTURE_TYPE_DEVICE_CREATE_INFO;
     dci.queueCreateInfoCount = 1;
@@ -586,7 +596,7 @@ cpvh_context* cpvh_open(const char* icd_path, char* err, uint32_t err_len) {
     LOAD_D(vkCmdBindIndexBuffer); LOAD_D(vkCmdBindVertexBuffers); LOAD_D(vkCmdDraw); LOAD_D(vkCmdDrawIndexed); LOAD_D(vkCmdCopyBuffer);
     LOAD_D(vkCmdCopyBufferToImage); LOAD_D(vkCmdCopyImageToBuffer); LOAD_D(vkCmdPipelineBarrier); LOAD_D(vkCmdPushConstants);
     LOAD_D(vkCmdBeginRenderPass); LOAD_D(vkCmdEndRenderPass); LOAD_D(vkQueueSubmit); LOAD_D(vkQueueWaitIdle); LOAD_D(vkCreateFence);
-    LOAD_D(vkDestroyFence); LOAD_D(vkResetFences); LOAD_D(vkWaitForFences);
+    LOAD_D(vkDestroyFence); LOAD_D(vkResetFences); LOAD_D(vkWaitForFences); LOAD_D(vkGetFenceStatus);
 #undef LOAD_D
     // CPVH_SUBMIT=no_alloc: every submission of this context goes through the
     // ICD's allocation-free submit export (same signature as vkQueueSubmit).
@@ -595,8 +605,13 @@ cpvh_context* cpvh_open(const char* icd_path, char* err, uint32_t err_len) {
         if (!fn) return fail("CPVH_SUBMIT=no_alloc but the ICD lacks cpv_queue_submit_no_alloc", c);
         f.vkQueueSubmit = fn;
     }
-    f.vkGetDeviceQueue(c->device, 0, 0, &c->queue);
-    if (!check_dispatch(c->queue)) return fail("VkQueue lacks the loader magic", c);
+    for (uint32_t i = 0; i < nqueues; i++) {
+        VkQueue q = nullptr;
+        f.vkGetDeviceQueue(c->device, 0, i, &q);
+        if (!q || !check_dispatch(q)) return fail("VkQueue lacks the loader magic", c);
+        c->queues.push_back(q);
+    }
+    c->queue = c->queues[0];
     VkPipelineCacheCreateInfo pci{};
     pci.sType = VK_STRUCTURE_TYPE_PIPELINE_CACHE_CREATE_INFO;
     f.vkCreatePipelineCache(c->device, &pci, nullptr, &c->cache);
@@ -981,6 +996,242 @@ int cpvh_readback(cpvh_renderer* r, uint8_t* color, uint8_t* depth) {
     if (depth && s->depth_format) std::memcpy(depth, static_cast<uint8_t*>(map) + cb, static_cast<uint64_t>(s->width) * s->height * r->depth_texel);
     c->f.vkUnmapMemory(c->device, r->readback.memory);
     return VK_SUCCESS;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ serving loop --
+//
+// Continuous batching of offscreen clients: every client owns a scene, its
+// pipelines, buffers and attachments, kept resident; requests arrive with
+// Poisson inter-arrival times per client; the loop admits a waiting request
+// whenever a slot (a queue) is free, its client has no request in flight and
+// the in-flight footprint stays within the HBM budget, and retires requests
+// as their fences signal. Work on different queues overlaps on the device.
+
+struct cpvh_server {
+    cpvh_context* ctx = nullptr;
+    cpvh_serve_config cfg{};
+    std::vector<cpv_scene*> scenes;
+    std::vector<cpvh_renderer*> clients;  // null: not resident (budget)
+    std::vector<uint64_t> footprint;
+    std::vector<uint64_t> triangles;
+    uint64_t resident_bytes = 0;
+};
+
+namespace {
+
+uint64_t splitmix(uint64_t& s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+double uniform01(uint64_t& s) { return static_cast<double>(splitmix(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+double percentile(std::vector<double> v, double p) {
+    if (v.empty()) return 0.0;
+    std::sort(v.begin(), v.end());
+    const double pos = p * static_cast<double>(v.size() - 1);
+    const size_t i = static_cast<size_t>(pos);
+    const double f = pos - static_cast<double>(i);
+    return i + 1 < v.size() ? v[i] * (1.0 - f) + v[i + 1] * f : v[i];
+}
+
+}  // namespace
+
+extern "C" {
+
+cpvh_server* cpvh_server_create(cpvh_context* ctx, const cpvh_serve_config* cfg, char* err, uint32_t err_len) {
+    auto fail = [&](const std::string& why, cpvh_server* s) -> cpvh_server* {
+        g_err = why;
+        if (err && err_len) std::snprintf(err, err_len, "%s", why.c_str());
+        cpvh_server_destroy(s);
+        return nullptr;
+    };
+    if (!ctx || !cfg || cfg->clients == 0 || cfg->min_tris == 0 || cfg->max_tris < cfg->min_tris) return fail("bad serving configuration", nullptr);
+    auto* s = new cpvh_server();
+    s->ctx = ctx;
+    s->cfg = *cfg;
+    if (s->cfg.slots == 0) s->cfg.slots = 1;
+    uint64_t rng = cfg->seed * 0x2545F4914F6CDD1Dull + 7;
+    static const uint64_t sides[4] = {256, 512, 1024, 2048};
+    for (uint32_t i = 0; i < cfg->clients; i++) {
+        // Image side uniform over {256, 512, 1024, 2048}; triangles
+        // log-uniform in [min_tris, max_tris].
+        const uint64_t side = cfg->max_side ? std::min<uint64_t>(sides[splitmix(rng) & 3u], cfg->max_side) : sides[splitmix(rng) & 3u];
+        const double lt = std::log(static_cast<double>(cfg->min_tris)) +
+                          uniform01(rng) * (std::log(static_cast<double>(cfg->max_tris)) - std::log(static_cast<double>(cfg->min_tris)));
+        const uint64_t params[3] = {side, static_cast<uint64_t>(std::llround(std::exp(lt))), i};
+        cpv_scene* scene = cpvh_scene_create(CPVH_SERVE, cfg->seed + i, params, 3);
+        if (!scene) return fail("client scene creation failed", s);
+        s->scenes.push_back(scene);
+        const uint64_t px = static_cast<uint64_t>(scene->width) * scene->height;
+        const uint64_t bytes = px * (4 + depth_texel_size(scene->depth_format)) * 2 /* attachments + readback */ +
+                               2 * (scene->vertex_bytes + scene->index_bytes + scene->uniform_bytes) /* buffers + staging */ + scene->texture_bytes;
+        s->footprint.push_back(bytes);
+        s->triangles.push_back(cpvh_scene_triangles(scene));
+        cpvh_renderer* r = nullptr;
+        if (s->resident_bytes + bytes <= cfg->hbm_budget_bytes) {
+            char e[512] = {0};
+            r = cpvh_renderer_create(ctx, scene, e, sizeof(e));
+            if (!r) return fail(std::string("client renderer creation failed: ") + e, s);
+            s->resident_bytes += bytes;
+        }
+        s->clients.push_back(r);
+    }
+    return s;
+}
+
+int cpvh_server_run(cpvh_server* s, cpvh_serve_result* out) {
+    cpvh_context* c = s->ctx;
+    const cpvh_serve_config& cfg = s->cfg;
+    struct Request {
+        double arrival_ms;
+        uint32_t client;
+    };
+    // Poisson arrivals per client over the window, merged in time order.
+    std::vector<Request> arrivals;
+    uint64_t rng = cfg.seed * 0x9E3779B97F4A7C15ull + 11;
+    for (uint32_t i = 0; i < cfg.clients; i++) {
+        if (!s->clients[i]) continue;
+        double t = 0.0;
+        for (;;) {
+            t += -std::log(1.0 - uniform01(rng)) * cfg.mean_interarrival_ms;
+            if (t >= cfg.duration_s * 1000.0) break;
+            arrivals.push_back({t, i});
+        }
+    }
+    std::sort(arrivals.begin(), arrivals.end(), [](const Request& a, const Request& b) { return a.arrival_ms < b.arrival_ms; });
+    const uint32_t slots = std::min<uint32_t>(cfg.slots, static_cast<uint32_t>(c->queues.size()));
+    // Warm-up (untimed): the largest resident client once on every queue,
+    // so that each queue's binning scratch has grown before the clock starts.
+    {
+        int big = -1;
+        for (uint32_t i = 0; i < cfg.clients; i++)
+            if (s->clients[i] && (big < 0 || s->triangles[i] > s->triangles[static_cast<uint32_t>(big)])) big = static_cast<int>(i);
+        if (big >= 0) {
+            cpvh_renderer* r = s->clients[static_cast<uint32_t>(big)];
+            VkSubmitInfo si{};
+            si.sType = VK_STRUCTURE_TYPE_SUBMIT_INFO;
+            si.commandBufferCount = 1;
+            si.pCommandBuffers = &r->frame_cmd;
+            for (uint32_t k = 0; k < slots; k++) {
+                VkResult res = c->f.vkQueueSubmit(c->queues[k], 1, &si, r->fence);
+                if (res == VK_SUCCESS) res = c->f.vkWaitForFences(c->device, 1, &r->fence, VK_TRUE, ~0ull);
+                c->f.vkResetFences(c->device, 1, &r->fence);
+                if (res != VK_SUCCESS) return res;
+            }
+        }
+    }
+    struct Slot {
+        bool busy = false;
+        uint32_t client = 0;
+        double arrival_ms = 0.0, submit_ms = 0.0;
+    };
+    std::vector<Slot> slot(slots);
+    std::vector<std::deque<double>> waiting(cfg.clients);  // arrival times per client
+    std::vector<bool> in_flight(cfg.clients, false);
+    std::vector<double> latency, submit_latency, queue_delay;
+    latency.reserve(arrivals.size());
+    uint64_t triangles = 0, inflight_bytes = 0;
+    uint32_t max_in_flight = 0, busy = 0;
+    size_t next = 0, done = 0;
+    const auto t0 = std::chrono::steady_clock::now();
+    auto now_ms = [&]() { return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(); };
+    double last_done = 0.0;
+    while (done < arrivals.size()) {
+        const double now = now_ms();
+        while (next < arrivals.size() && arrivals[next].arrival_ms <= now) {
+            waiting[arrivals[next].client].push_back(arrivals[next].arrival_ms);
+            next++;
+        }
+        // Retire finished requests.
+        for (uint32_t k = 0; k < slots; k++) {
+            if (!slot[k].busy) continue;
+            cpvh_renderer* r = s->clients[slot[k].client];
+            const VkResult st = c->f.vkGetFenceStatus(c->device, r->fence);
+            if (st == VK_NOT_READY) continue;
+            if (st != VK_SUCCESS) return st;
+            const double t = now_ms();
+            c->f.vkResetFences(c->device, 1, &r->fence);
+            latency.push_back(t - slot[k].arrival_ms);
+            submit_latency.push_back(t - slot[k].submit_ms);
+            triangles += s->triangles[slot[k].client];
+            inflight_bytes -= s->footprint[slot[k].client];
+            in_flight[slot[k].client] = false;
+            slot[k].busy = false;
+            busy--;
+            done++;
+            last_done = t;
+        }
+        // Admit: the oldest waiting request whose client is idle, while a slot
+        // is free and the in-flight footprint fits the budget.
+        for (uint32_t k = 0; k < slots; k++) {
+            if (slot[k].busy) continue;
+            int best = -1;
+            for (uint32_t i = 0; i < cfg.clients; i++) {
+                if (waiting[i].empty() || in_flight[i]) continue;
+                if (inflight_bytes + s->footprint[i] > cfg.hbm_budget_bytes && busy > 0) continue;
+                if (best < 0 || waiting[i].front() < waiting[static_cast<uint32_t>(best)].front()) best = static_cast<int>(i);
+            }
+            if (best < 0) break;
+            const uint32_t i = static_cast<uint32_t>(best);
+            cpvh_renderer* r = s->clients[i];
+            VkSubmitInfo si{};
+            si.sType = VK_STRUCTURE_TYPE_SUBMIT_INFO;
+            si.commandBufferCount = 1;
+            si.pCommandBuffers = &r->frame_cmd;
+            slot[k].submit_ms = now_ms();
+            const VkResult res = c->f.vkQueueSubmit(c->queues[k], 1, &si, r->fence);
+            if (res != VK_SUCCESS) return res;
+            slot[k].busy = true;
+            slot[k].client = i;
+            slot[k].arrival_ms = waiting[i].front();
+            queue_delay.push_back(slot[k].submit_ms - slot[k].arrival_ms);
+            waiting[i].pop_front();
+            in_flight[i] = true;
+            inflight_bytes += s->footprint[i];
+            busy++;
+            max_in_flight = std::max(max_in_flight, busy);
+        }
+    }
+    c->f.vkDeviceWaitIdle(c->device);
+    if (out) {
+        std::memset(out, 0, sizeof(*out));
+        out->requests = arrivals.size();
+        out->completed = done;
+        out->triangles = triangles;
+        out->wall_s = last_done / 1000.0;
+        out->mtri_s = last_done > 0.0 ? static_cast<double>(triangles) / (last_done / 1000.0) / 1e6 : 0.0;
+        out->latency_p50_ms = percentile(latency, 0.50);
+        out->latency_p99_ms = percentile(latency, 0.99);
+        out->submit_p50_ms = percentile(submit_latency, 0.50);
+        out->submit_p99_ms = percentile(submit_latency, 0.99);
+        out->queue_p50_ms = percentile(queue_delay, 0.50);
+        out->queue_p99_ms = percentile(queue_delay, 0.99);
+        out->max_in_flight = max_in_flight;
+        out->resident_bytes = s->resident_bytes;
+        uint32_t resident = 0;
+        for (auto* r : s->clients) resident += r ? 1u : 0u;
+        out->resident_clients = resident;
+    }
+    return VK_SUCCESS;
+}
+
+uint32_t cpvh_server_clients(const cpvh_server* s) { return s ? static_cast<uint32_t>(s->clients.size()) : 0u; }
+
+cpvh_renderer* cpvh_server_client(cpvh_server* s, uint32_t i) { return s && i < s->clients.size() ? s->clients[i] : nullptr; }
+
+const cpv_scene* cpvh_server_scene(cpvh_server* s, uint32_t i) { return s && i < s->scenes.size() ? s->scenes[i] : nullptr; }
+
+void cpvh_server_destroy(cpvh_server* s) {
+    if (!s) return;
+    for (auto* r : s->clients)
+        if (r) cpvh_renderer_destroy(r);
+    for (auto* sc : s->scenes) cpvh_scene_destroy(sc);
+    delete s;
 }
 
 }  // extern "C"

@@ -461,6 +461,75 @@ VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& writte
     return VK_SUCCESS;
 }
 
+void CommandBuffer::reset() {
+    for (auto& kv : graphs)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    graphs.clear();
+    cmds.clear();
+    batches.clear();
+    written.clear();
+    graphable = -1;
+}
+
+VkResult run_command_buffer(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& written, bool no_alloc) {
+    if (no_alloc || rt::profile_enabled() || env_u32("CPV_CB_GRAPH", 1u) == 0u || cb->graphable == 0) return execute(q, cb, written, no_alloc);
+    if (cb->graphable < 0) {
+        // First execution: eager. It decides whether the buffer can be a graph
+        // (its commands read no host memory and no pass runs batched, whose
+        // plans keep graphs of their own) and records what it writes.
+        const size_t before = written.size();
+        const VkResult r = execute(q, cb, written, false);
+        if (r != VK_SUCCESS) return r;
+        bool ok = true;
+        for (const Cmd& c : cb->cmds) ok = ok && c.type != CmdType::UpdateBuffer;
+        for (const auto& kv : cb->batches) ok = ok && kv.second->plain;
+        cb->graphable = ok ? 1 : 0;
+        cb->written.assign(written.begin() + static_cast<std::ptrdiff_t>(before), written.end());
+        cb->graphs[q].warm = true;
+        return VK_SUCCESS;
+    }
+    QueueGraph& g = cb->graphs[q];
+    if (g.exec && g.generation != q->scratch.generation()) {
+        cudaGraphExecDestroy(g.exec);  // the queue's scratch moved since the capture
+        g.exec = nullptr;
+    }
+    if (!g.exec) {
+        if (!g.warm) {
+            // First run on this queue sizes its scratch; capture on the next.
+            g.warm = true;
+            return execute(q, cb, written, false);
+        }
+        cudaGraph_t graph = nullptr;
+        std::vector<DeviceMemory*> w;
+        const uint64_t before = rt::launches();
+        if (cudaStreamBeginCapture(q->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            cb->graphable = 0;
+            return execute(q, cb, written, false);
+        }
+        const VkResult r = execute(q, cb, w, false);
+        const cudaError_t e = cudaStreamEndCapture(q->stream, &graph);
+        g.kernels = rt::launches() - before;
+        rt::count_launch(0 - g.kernels);  // captured, not launched yet
+        if (r != VK_SUCCESS || e != cudaSuccess || cudaGraphInstantiate(&g.exec, graph, 0) != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            g.exec = nullptr;
+            cb->graphable = 0;  // fall back to eager execution for good
+            return execute(q, cb, written, false);
+        }
+        cudaGraphDestroy(graph);
+        g.generation = q->scratch.generation();
+    }
+    if (cudaGraphLaunch(g.exec, q->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return VK_ERROR_DEVICE_LOST;
+    }
+    rt::count_launch(g.kernels);
+    written.insert(written.end(), cb->written.begin(), cb->written.end());
+    return VK_SUCCESS;
+}
+
 void precompile_batches(CommandBuffer* cb) {
     if (env_u32("CPV_BATCH", 1u) == 0u) return;
     const uint32_t min_draws = env_u32("CPV_BATCH_MIN_DRAWS", 16u);

@@ -228,7 +228,7 @@ VKAPI_ATTR void VKAPI_CALL GetPhysicalDeviceQueueFamilyProperties(VkPhysicalDevi
     if (*count < 1) return;
     std::memset(p, 0, sizeof(*p));
     p[0].queueFlags = VK_QUEUE_GRAPHICS_BIT | VK_QUEUE_TRANSFER_BIT;
-    p[0].queueCount = 1;
+    p[0].queueCount = kMaxQueues;
     p[0].timestampValidBits = 0;
     p[0].minImageTransferGranularity = {1, 1, 1};
     *count = 1;
@@ -272,21 +272,29 @@ VKAPI_ATTR VkResult VKAPI_CALL CreateDevice(VkPhysicalDevice pd, const VkDeviceC
         rt::set_last_error("vkCreateDevice: " + err);
         return VK_ERROR_INITIALIZATION_FAILED;
     }
+    // One queue family; each queue is its own CUDA stream with its own
+    // binning scratch, so work submitted to different queues overlaps.
+    uint32_t queues = 1;
+    if (ci->queueCreateInfoCount >= 1 && ci->pQueueCreateInfos) queues = ci->pQueueCreateInfos[0].queueCount;
+    if (queues < 1 || queues > kMaxQueues) return VK_ERROR_INITIALIZATION_FAILED;
     auto* dev = new Device();
     dev->physical = reinterpret_cast<PhysicalDevice*>(pd);
-    dev->queue = new Queue();
-    dev->queue->device = dev;
     dev->compile_only = !rt::available();
-    if (dev->compile_only) {
-        *out = to_handle<VkDevice>(dev);
-        return VK_SUCCESS;
+    for (uint32_t i = 0; i < queues; i++) {
+        auto* q = new Queue();
+        q->device = dev;
+        dev->queues.push_back(q);
+        if (!dev->compile_only && cudaStreamCreateWithFlags(&q->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            for (Queue* x : dev->queues) {
+                if (x->stream) cudaStreamDestroy(x->stream);
+                delete x;
+            }
+            delete dev;
+            return VK_ERROR_INITIALIZATION_FAILED;
+        }
     }
-    if (cudaStreamCreateWithFlags(&dev->queue->stream, cudaStreamNonBlocking) != cudaSuccess) {
-        cudaGetLastError();
-        delete dev->queue;
-        delete dev;
-        return VK_ERROR_INITIALIZATION_FAILED;
-    }
+    dev->queue = dev->queues[0];
     *out = to_handle<VkDevice>(dev);
     return VK_SUCCESS;
 }
@@ -294,20 +302,25 @@ VKAPI_ATTR VkResult VKAPI_CALL CreateDevice(VkPhysicalDevice pd, const VkDeviceC
 VKAPI_ATTR void VKAPI_CALL DestroyDevice(VkDevice device, const VkAllocationCallbacks*) {
     auto* dev = reinterpret_cast<Device*>(device);
     if (!dev) return;
-    if (dev->compile_only) {
-        delete dev->queue;
-        delete dev;
-        return;
+    if (!dev->compile_only) {
+        for (Queue* q : dev->queues) {
+            cudaStreamSynchronize(q->stream);
+            cudaStreamDestroy(q->stream);
+        }
+        for (auto& kv : dev->batch_modules) rt::unload(*kv.second);
     }
-    cudaStreamSynchronize(dev->queue->stream);
-    cudaStreamDestroy(dev->queue->stream);
-    for (auto& kv : dev->batch_modules) rt::unload(*kv.second);
-    delete dev->queue;
+    for (Queue* q : dev->queues) delete q;
     delete dev;
 }
 
-VKAPI_ATTR void VKAPI_CALL GetDeviceQueue(VkDevice device, uint32_t, uint32_t, VkQueue* q) {
-    *q = to_handle<VkQueue>(reinterpret_cast<Device*>(device)->queue);
+VKAPI_ATTR void VKAPI_CALL GetDeviceQueue(VkDevice device, uint32_t, uint32_t index, VkQueue* q) {
+    auto* dev = reinterpret_cast<Device*>(device);
+    *q = to_handle<VkQueue>(dev->queues[index < dev->queues.size() ? index : 0]);
+}
+
+// Waits for the work of every queue of the device (memory coherence points).
+void sync_queues(Device* dev) {
+    for (Queue* q : dev->queues) cudaStreamSynchronize(q->stream);
 }
 
 // Completion of a submission: host-visible memories the GPU wrote and that
@@ -327,9 +340,11 @@ void complete_readback(std::vector<DeviceMemory*>& mems) {
 VKAPI_ATTR VkResult VKAPI_CALL DeviceWaitIdle(VkDevice device) {
     auto* dev = reinterpret_cast<Device*>(device);
     if (dev->compile_only) return VK_SUCCESS;
-    std::lock_guard<std::mutex> lock(dev->queue->mutex);
-    if (cudaStreamSynchronize(dev->queue->stream) != cudaSuccess) return VK_ERROR_DEVICE_LOST;
-    complete_readback(dev->queue->pending_readback);
+    for (Queue* q : dev->queues) {
+        std::lock_guard<std::mutex> lock(q->mutex);
+        if (cudaStreamSynchronize(q->stream) != cudaSuccess) return VK_ERROR_DEVICE_LOST;
+        complete_readback(q->pending_readback);
+    }
     return VK_SUCCESS;
 }
 
@@ -384,13 +399,15 @@ VKAPI_ATTR void VKAPI_CALL FreeMemory(VkDevice device, VkDeviceMemory memory, co
     auto* dev = reinterpret_cast<Device*>(device);
     auto* m = reinterpret_cast<DeviceMemory*>(memory);
     if (!m) return;
-    if (!dev->compile_only) cudaStreamSynchronize(dev->queue->stream);
+    if (!dev->compile_only) sync_queues(dev);
     {
         std::lock_guard<std::mutex> lock(dev->memory_mutex);
         dev->memories.erase(m);
     }
-    auto& pr = dev->queue->pending_readback;
-    pr.erase(std::remove(pr.begin(), pr.end(), m), pr.end());
+    for (Queue* q : dev->queues) {
+        auto& pr = q->pending_readback;
+        pr.erase(std::remove(pr.begin(), pr.end(), m), pr.end());
+    }
     if (dev->compile_only) {
         std::free(m->device);
         std::free(m->host);
@@ -412,7 +429,7 @@ VKAPI_ATTR VkResult VKAPI_CALL MapMemory(VkDevice device, VkDeviceMemory memory,
         return VK_SUCCESS;
     }
     if (m->device_dirty) {
-        cudaStreamSynchronize(dev->queue->stream);
+        sync_queues(dev);
         if (cudaMemcpy(m->host, m->device, m->size, cudaMemcpyDeviceToHost) != cudaSuccess) return VK_ERROR_MEMORY_MAP_FAILED;
         m->device_dirty = false;
     }
@@ -429,14 +446,14 @@ VKAPI_ATTR void VKAPI_CALL UnmapMemory(VkDevice device, VkDeviceMemory memory) {
         m->mapped = false;
         return;
     }
-    cudaStreamSynchronize(dev->queue->stream);
+    sync_queues(dev);
     cudaMemcpy(m->device, m->host, m->size, cudaMemcpyHostToDevice);
     m->mapped = false;
 }
 
 VKAPI_ATTR VkResult VKAPI_CALL FlushMappedMemoryRanges(VkDevice device, uint32_t n, const VkMappedMemoryRange* r) {
     auto* dev = reinterpret_cast<Device*>(device);
-    cudaStreamSynchronize(dev->queue->stream);
+    if (!dev->compile_only) sync_queues(dev);
     for (uint32_t i = 0; i < n; i++) {
         auto* m = reinterpret_cast<DeviceMemory*>(r[i].memory);
         if (!m->host) continue;
@@ -448,7 +465,7 @@ VKAPI_ATTR VkResult VKAPI_CALL FlushMappedMemoryRanges(VkDevice device, uint32_t
 
 VKAPI_ATTR VkResult VKAPI_CALL InvalidateMappedMemoryRanges(VkDevice device, uint32_t n, const VkMappedMemoryRange* r) {
     auto* dev = reinterpret_cast<Device*>(device);
-    cudaStreamSynchronize(dev->queue->stream);
+    if (!dev->compile_only) sync_queues(dev);
     for (uint32_t i = 0; i < n; i++) {
         auto* m = reinterpret_cast<DeviceMemory*>(r[i].memory);
         if (!m->host) continue;
@@ -1068,7 +1085,7 @@ VkResult submit(VkQueue queue, uint32_t n, const VkSubmitInfo* si, VkFence fence
             s->signalled = false;
         }
         for (uint32_t k = 0; k < si[i].commandBufferCount; k++) {
-            const VkResult r = execute(q, reinterpret_cast<CommandBuffer*>(si[i].pCommandBuffers[k]), written, no_alloc);
+            const VkResult r = run_command_buffer(q, reinterpret_cast<CommandBuffer*>(si[i].pCommandBuffers[k]), written, no_alloc);
             if (r != VK_SUCCESS) return r;
         }
         for (uint32_t k = 0; k < si[i].signalSemaphoreCount; k++) {

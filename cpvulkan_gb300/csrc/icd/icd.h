@@ -165,7 +165,7 @@ struct ModuleConfig {
     uint32_t tile_shift = 4;  // 8, 16 or 32 px tiles
     uint32_t schedule = 0;    // fragment schedule: 0 immediate, 1 deferred, 2 sparse
     uint32_t warps = 8;       // warps per tile CTA (capped by the tile's pixels)
-    uint32_t batch = 128;     // primitives set up per shared-memory batch
+    uint32_t batch = 256;     // primitives set up per shared-memory batch (measured: 256 beats 128 on C2 and C4)
 };
 
 // Fragment schedule of a module whose pipelines prefer (or not) dense
@@ -210,15 +210,27 @@ struct BatchState {
     bool plain = false;            // not batchable: the per-draw path runs
 };
 
+// A command buffer's work captured as a CUDA graph for one queue (its
+// binning scratch is per queue).
+struct QueueGraph {
+    bool warm = false;               // ran once eagerly on this queue (scratch sized)
+    cudaGraphExec_t exec = nullptr;
+    uint64_t generation = 0;         // the queue's scratch generation at capture
+    uint64_t kernels = 0;
+};
+
 struct CommandBuffer : Dispatchable {
     Device* device = nullptr;
     std::vector<Cmd> cmds;
     bool recording = false;
     std::map<size_t, std::unique_ptr<BatchState>> batches;  // by BeginRenderPass command index
-    void reset() {
-        cmds.clear();
-        batches.clear();
-    }
+    // Replay as a CUDA graph per queue: decided after the first execution
+    // (no host-memory sources, no batched pass).
+    int graphable = -1;  // -1 unknown, 0 no, 1 yes
+    std::vector<DeviceMemory*> written;  // memories its execution writes
+    std::map<Queue*, QueueGraph> graphs;
+    void reset();
+    ~CommandBuffer() { reset(); }
 };
 
 struct CommandPool {
@@ -246,6 +258,9 @@ struct Queue : Dispatchable {
     std::mutex mutex;
 };
 
+// Queues a device may create in its one queue family.
+constexpr uint32_t kMaxQueues = 16;
+
 struct Device : Dispatchable {
     PhysicalDevice* physical = nullptr;
     // No CUDA device and CPV_COMPILE_ONLY=1: pipelines are translated and
@@ -253,7 +268,8 @@ struct Device : Dispatchable {
     // fail with VK_ERROR_DEVICE_LOST. Used to check pipeline compilation on
     // machines without a GPU.
     bool compile_only = false;
-    Queue* queue = nullptr;
+    std::vector<Queue*> queues;  // the queues of the one queue family
+    Queue* queue = nullptr;      // queues[0]
     std::mutex cache_mutex;
     std::map<std::array<uint8_t, 32>, std::vector<uint8_t>> module_cache;  // in-process NVRTC cubin cache
     std::set<DeviceMemory*> memories;
@@ -268,6 +284,10 @@ struct Device : Dispatchable {
 // (message in rt::last_error()).
 rt::Module* batch_module(Device* dev, const std::vector<Pipeline*>& pipelines, const ModuleConfig& mc);
 
+// Runs a command buffer on a queue: replays its CUDA graph for that queue
+// when it has one, captures one on its second run there, else executes
+// eagerly (command.cpp). CPV_CB_GRAPH=0 always executes eagerly.
+VkResult run_command_buffer(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& written, bool no_alloc);
 // Execution of a recorded command buffer on a queue (command.cpp).
 // no_alloc: draws bin through the fixed scratch array (rt::draw_plain_static)
 // instead of the queue's grow-only scratch.

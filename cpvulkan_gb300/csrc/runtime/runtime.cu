@@ -263,7 +263,9 @@ int load(const std::vector<uint8_t>& cubin, uint32_t tile_shift, bool batched, M
     out.tile_shift = tile_shift;
     if (!module_u32(lib, "cpv_raster_smem_bytes", out.raster_smem) || !module_u32(lib, "cpv_raster_threads", out.raster_threads))
         return fail("pipeline module lacks its launch-shape globals");
-    if (out.raster_smem > 48 * 1024 &&
+    // Opt in to the dynamic shared memory even below 48 KB: the kernel's
+    // static shared memory counts against the same default limit.
+    if (out.raster_smem > 0 &&
         cudaFuncSetAttribute(reinterpret_cast<const void*>(out.raster), cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(out.raster_smem)) != cudaSuccess)
         return fail("raster kernel needs more shared memory than the device allows");
@@ -285,22 +287,30 @@ Scratch::~Scratch() {
     cudaFree(words_);
 }
 
-int Scratch::reserve_rects(uint64_t prims) { return grow(rects_, rects_cap_, prims * 4); }
-
-int Scratch::reserve_bins(uint64_t entries) {
-    const int r = grow(counts_, counts_cap_, entries);
-    if (r != kOk) return r;
-    return grow(cursor_, cursor_cap_, entries);
+template <typename T>
+int Scratch::grow_tracked(T*& ptr, uint64_t& cap, uint64_t need) {
+    const T* before = ptr;
+    const int r = grow(ptr, cap, need);
+    if (ptr != before) generation_++;
+    return r;
 }
 
-int Scratch::reserve_list(uint64_t entries) { return grow(list_, list_cap_, entries); }
+int Scratch::reserve_rects(uint64_t prims) { return grow_tracked(rects_, rects_cap_, prims * 4); }
+
+int Scratch::reserve_bins(uint64_t entries) {
+    const int r = grow_tracked(counts_, counts_cap_, entries);
+    if (r != kOk) return r;
+    return grow_tracked(cursor_, cursor_cap_, entries);
+}
+
+int Scratch::reserve_list(uint64_t entries) { return grow_tracked(list_, list_cap_, entries); }
 
 int Scratch::reserve_scan(uint64_t n) {
     int level = 0;
     while (n > CPV_SCAN_BLOCK && level < 8) {
         n = (n + CPV_SCAN_BLOCK - 1) / CPV_SCAN_BLOCK;
         // two arrays per level (sums and scanned sums) share one allocation
-        const int r = grow(scan_[level], scan_cap_[level], 2 * n);
+        const int r = grow_tracked(scan_[level], scan_cap_[level], 2 * n);
         if (r != kOk) return r;
         level++;
     }
@@ -314,6 +324,7 @@ int Scratch::ensure_words() {
         return kErrOutOfMemory;
     }
     cudaMemset(words_, 0, 64);
+    generation_++;
     return kOk;
 }
 

@@ -71,8 +71,14 @@ public:
     uint32_t* words() const { return words_; }  // [0] pair total, [1] status
     uint32_t* scan_level(int level) const { return scan_[level]; }
     int ensure_words();
+    // Incremented whenever a buffer is (re)allocated: work captured in a CUDA
+    // graph against older pointers must be captured again.
+    uint64_t generation() const { return generation_; }
 
 private:
+    template <typename T>
+    int grow_tracked(T*& ptr, uint64_t& cap, uint64_t need);
+    uint64_t generation_ = 0;
     uint16_t* rects_ = nullptr;
     uint64_t rects_cap_ = 0;
     uint32_t* counts_ = nullptr;

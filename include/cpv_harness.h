@@ -83,6 +83,49 @@ int cpvh_readback(cpvh_renderer* r, uint8_t* color, uint8_t* depth);
 void* cpvh_queue(cpvh_context* ctx);
 const char* cpvh_last_error(void);
 
+/* ---- serving: continuous batching of offscreen clients ----
+ *
+ * Each client owns a seeded textured-icosphere scene (image side uniform over
+ * {256, 512, 1024, 2048}, at most max_side when non-zero; triangles
+ * log-uniform in [min_tris, max_tris]) whose pipelines, buffers, texture and
+ * attachments are created once and stay resident while the resident total
+ * fits hbm_budget_bytes. Requests arrive per client with exponential
+ * inter-arrival times (mean mean_interarrival_ms) during duration_s; a
+ * request renders one frame of its client. The loop admits the oldest
+ * waiting request whose client is idle whenever one of `slots` queues is
+ * free and the footprint of the requests in flight stays within the budget,
+ * and retires requests as their fences signal. */
+typedef struct cpvh_serve_config {
+    uint32_t clients;
+    uint32_t slots;
+    double mean_interarrival_ms;
+    double duration_s;
+    uint64_t seed;
+    uint64_t hbm_budget_bytes;
+    uint32_t min_tris, max_tris;
+    uint32_t max_side;
+} cpvh_serve_config;
+
+typedef struct cpvh_serve_result {
+    uint64_t requests, completed, triangles;
+    uint32_t resident_clients, max_in_flight;
+    uint64_t resident_bytes;
+    double wall_s, mtri_s;
+    double latency_p50_ms, latency_p99_ms; /* arrival → fence signalled */
+    double submit_p50_ms, submit_p99_ms;   /* vkQueueSubmit → fence signalled */
+    double queue_p50_ms, queue_p99_ms;     /* arrival → vkQueueSubmit */
+} cpvh_serve_result;
+
+typedef struct cpvh_server cpvh_server;
+cpvh_server* cpvh_server_create(cpvh_context* ctx, const cpvh_serve_config* cfg, char* err, uint32_t err_len);
+int cpvh_server_run(cpvh_server* server, cpvh_serve_result* out);
+uint32_t cpvh_server_clients(const cpvh_server* server);
+/* The client's renderer (readback, or a frame rendered alone with
+ * cpvh_render), or NULL when the client is not resident. */
+cpvh_renderer* cpvh_server_client(cpvh_server* server, uint32_t client);
+const cpv_scene* cpvh_server_scene(cpvh_server* server, uint32_t client);
+void cpvh_server_destroy(cpvh_server* server);
+
 #ifdef __cplusplus
 }
 #endif
