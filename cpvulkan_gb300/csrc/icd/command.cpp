@@ -290,9 +290,12 @@ uint32_t env_u32(const char* name, uint32_t dflt) {
 
 // Module configuration of a batch over `pipelines`.
 ModuleConfig batch_config(const std::vector<Pipeline*>& pipelines) {
-    bool dense = false;
-    for (const Pipeline* p : pipelines) dense = dense || p->prefers_deferred;
-    return module_config(pipelines[0]->tile_shift, dense);
+    bool dense = false, constant = true;
+    for (const Pipeline* p : pipelines) {
+        dense = dense || p->prefers_deferred;
+        constant = constant && p->fs_constant;
+    }
+    return module_config(pipelines[0]->tile_shift, dense, constant);
 }
 
 // Builds the batch of the render pass whose commands are (begin, end): the

@@ -157,6 +157,8 @@ struct Pipeline {
     uint32_t nv = 0;     // varying floats
     bool prefers_deferred = false;  // fragment shader samples images or is long
     uint32_t tile_shift = 4;        // screen tile of the pipeline's modules
+    bool blend_table = false;       // per-primitive blend tables (constant colour, per-channel blend)
+    bool fs_constant = false;       // fragment shader shaded once per primitive
     std::string source;  // generated CUDA translation unit of the per-draw module
 };
 
@@ -170,10 +172,10 @@ struct ModuleConfig {
 
 // Fragment schedule of a module whose pipelines prefer (or not) dense
 // shading; CPV_SCHEDULE=0/1/2 overrides.
-uint32_t schedule_for(bool prefers_deferred);
+uint32_t schedule_for(bool prefers_deferred, bool fs_constant);
 // Module configuration for a tile size and shading preference, with the
 // environment's tunables applied.
-ModuleConfig module_config(uint32_t tile_shift, bool prefers_deferred);
+ModuleConfig module_config(uint32_t tile_shift, bool prefers_deferred, bool fs_constant);
 
 // The CUDA translation unit of a module over one pipeline's stage block
 // (per-draw kernels) or several (batched kernels, pipeline i in namespace

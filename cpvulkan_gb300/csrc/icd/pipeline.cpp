@@ -56,15 +56,15 @@ const char* const kStageMacros[] = {
     "CPV_ST_F_FAIL", "CPV_ST_F_PASS", "CPV_ST_F_DFAIL", "CPV_ST_F_OP", "CPV_ST_F_CMASK", "CPV_ST_F_WMASK", "CPV_ST_F_REF",
     "CPV_ST_B_FAIL", "CPV_ST_B_PASS", "CPV_ST_B_DFAIL", "CPV_ST_B_OP", "CPV_ST_B_CMASK", "CPV_ST_B_WMASK", "CPV_ST_B_REF",
     "CPV_BLEND", "CPV_SRC_COLOR", "CPV_DST_COLOR", "CPV_COLOR_OP", "CPV_SRC_ALPHA", "CPV_DST_ALPHA", "CPV_ALPHA_OP", "CPV_WRITE_MASK",
-    "CPV_COLOR_FORMAT", "CPV_DEPTH_FORMAT", "CPV_ORIGIN_UPPER",
+    "CPV_COLOR_FORMAT", "CPV_DEPTH_FORMAT", "CPV_ORIGIN_UPPER", "CPV_FS_CONSTANT", "CPV_BLEND_TABLE",
 };
 
 }  // namespace
 
-ModuleConfig module_config(uint32_t tile_shift, bool prefers_deferred) {
+ModuleConfig module_config(uint32_t tile_shift, bool prefers_deferred, bool fs_constant) {
     ModuleConfig mc;
     mc.tile_shift = tile_shift;
-    mc.schedule = schedule_for(prefers_deferred);
+    mc.schedule = schedule_for(prefers_deferred, fs_constant);
     // Tunables (CPV_RT_WARPS 1-32 warps per tile CTA, CPV_BATCH_PRIMS 32-256
     // primitives per shared-memory batch).
     if (const char* v = std::getenv("CPV_RT_WARPS")) {
@@ -78,16 +78,18 @@ ModuleConfig module_config(uint32_t tile_shift, bool prefers_deferred) {
     return mc;
 }
 
-uint32_t schedule_for(bool prefers_deferred) {
+uint32_t schedule_for(bool prefers_deferred, bool fs_constant) {
     if (const char* v = std::getenv("CPV_SCHEDULE")) {
         const int s = std::atoi(v);
         if (s >= 0 && s <= 2) return static_cast<uint32_t>(s);
     }
-    // The sparse schedule falls back to the immediate one batch by batch where
-    // primitives are large, so it serves every pipeline; dense shading
-    // (deferred) stays available through CPV_SCHEDULE=1.
+    // Shading once per primitive (flat-shaded geometry: overlays, quads)
+    // goes with the immediate schedule and its per-warp primitive lists.
+    // Otherwise the sparse schedule, which falls back to the immediate one
+    // batch by batch where primitives are large; dense shading (deferred)
+    // stays available through CPV_SCHEDULE=1.
     (void)prefers_deferred;
-    return 2u;
+    return fs_constant ? 0u : 2u;
 }
 
 std::string compose_module(const std::vector<std::string>& stages, const std::vector<uint32_t>& nvs, const ModuleConfig& mc, bool batched) {
@@ -101,6 +103,9 @@ std::string compose_module(const std::vector<std::string>& stages, const std::ve
     src << "#define CPV_RT_WARPS " << mc.warps << "\n";
     src << "#define CPV_BATCH " << mc.batch << "\n";
     src << "#define CPV_NV_MAX " << nv_max << "\n";
+    bool any_constant = false;
+    for (const std::string& st : stages) any_constant = any_constant || st.find("#define CPV_FS_CONSTANT 1\n") != std::string::npos;
+    src << "#define CPV_ANY_FS_CONSTANT " << (any_constant ? 1 : 0) << "\n";
     src << "#include \"cpv_device.cuh\"\n#include \"cpv_raster.cuh\"\n";
     for (size_t i = 0; i < stages.size(); i++) {
         src << "namespace cpv_p" << i << " {\n" << stages[i] << "#include \"cpv_stage.cuh\"\n";
@@ -348,6 +353,22 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     src << "#define CPV_COLOR_FORMAT " << static_cast<uint32_t>(cfmt) << "\n";
     src << "#define CPV_DEPTH_FORMAT " << static_cast<uint32_t>(dfmt) << "\n";
     src << "#define CPV_ORIGIN_UPPER " << (fr.origin_upper_left ? 1 : 0) << "\n";
+    // A fragment shader that reads neither FragCoord nor FrontFacing and only
+    // flat inputs computes the same result for every fragment of a primitive:
+    // it runs once per primitive at set-up.
+    bool fs_constant = !fr.reads_frag_coord && !fr.reads_front_facing;
+    for (int k : fr.interp) fs_constant = fs_constant && k == 2;
+    src << "#define CPV_FS_CONSTANT " << (fs_constant ? 1 : 0) << "\n";
+    // Blending a per-primitive constant colour where each channel's result
+    // depends only on that channel of the destination (no DST_ALPHA,
+    // ONE_MINUS_DST_ALPHA or SRC_ALPHA_SATURATE colour factors): the result
+    // is a byte → byte table per channel, built once per primitive.
+    auto dst_alpha_factor = [](VkBlendFactor f) {
+        return f == VK_BLEND_FACTOR_DST_ALPHA || f == VK_BLEND_FACTOR_ONE_MINUS_DST_ALPHA || f == VK_BLEND_FACTOR_SRC_ALPHA_SATURATE;
+    };
+    const bool blend_table = fs_constant && blend.blendEnable && !dst_alpha_factor(blend.srcColorBlendFactor) &&
+                             !dst_alpha_factor(blend.dstColorBlendFactor);
+    src << "#define CPV_BLEND_TABLE " << (blend_table ? 1 : 0) << "\n";
     src << vr.code << fr.code;
     src << "__device__ __forceinline__ int cpv_interp(int c) {\n  switch (c) {\n";
     for (size_t i = 0; i < fr.interp.size(); i++)
@@ -359,7 +380,9 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     p->nv = nv;
     p->prefers_deferred = prefers_deferred;
     p->tile_shift = tile_shift;
-    p->source = compose_module({p->stage}, {nv}, module_config(tile_shift, prefers_deferred), false);
+    p->blend_table = blend_table;
+    p->fs_constant = fs_constant;
+    p->source = compose_module({p->stage}, {nv}, module_config(tile_shift, prefers_deferred, fs_constant), false);
     // The key covers the generated source and the embedded kernel headers it
     // includes, so an on-disk cache never returns a cubin of older kernels.
     {
@@ -437,6 +460,7 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
         rt::set_last_error("module load failed: " + err);
         return VK_ERROR_INITIALIZATION_FAILED;
     }
+    p->module.blend_table = blend_table;
     *out = p.release();
     return VK_SUCCESS;
 }

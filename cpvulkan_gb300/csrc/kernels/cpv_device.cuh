@@ -39,7 +39,7 @@ __device__ __forceinline__ float cpv_std_clamp(float v, float lo, float hi) { re
 __device__ __forceinline__ uint32_t cpv_encode_unorm(float x, float maxv) {
     float v = fminf(fmaxf(x, 0.0f), 1.0f);
     v = __fmul_rn(v, maxv);
-    v = roundf(v);
+    v = roundf(v); /* half away from zero, as llvm.round */
     return __float2uint_rz(v);
 }
 

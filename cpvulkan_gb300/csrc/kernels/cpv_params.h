@@ -90,6 +90,9 @@ struct CpvDrawParams {
     uint32_t spans;
     uint32_t list_capacity;
     uint32_t* status;
+    /* per primitive 4 x 256 bytes: the blend result of each channel for each
+     * destination byte (pipelines blending a constant colour; null: compute) */
+    uint8_t* tables;
 };
 
 /* Primitives per set-up block of the batched path: every draw of a batch

@@ -31,6 +31,45 @@ extern "C" __global__ void __launch_bounds__(256) cpv_setup_rects(const __grid_c
     reinterpret_cast<uint2*>(const_cast<uint16_t*>(P.rects))[g] = cpv_tile_rect(t, P.viewport[2], P.viewport[3]);
 }
 
+/* Blend tables (pipelines that blend a per-primitive constant colour): one
+ * thread per primitive shades it (vertex shader, flat inputs, fragment
+ * shader), then the CTA fills the 4 × 256-byte table of each live primitive
+ * of its 256, one destination byte per thread. Primitives whose tile
+ * rectangle is empty are skipped (the raster never reads their tables). */
+extern "C" __global__ void __launch_bounds__(256) cpv_blend_tables(const __grid_constant__ CpvDrawParams P) {
+    __shared__ float colours[256][4];
+    __shared__ uint32_t live[256];
+    cpv_lut8_init();
+    const uint64_t g = static_cast<uint64_t>(blockIdx.x) * 256u + threadIdx.x;
+    uint32_t ok = 0u;
+    if (cpv_p0::kBlendTable && g < P.total_prims) {
+        bool drawn = true;
+        if (P.rects) {
+            const uint2 r = reinterpret_cast<const uint2*>(P.rects)[g];
+            drawn = r.x != r.y;  /* empty rectangles are all-zero */
+        }
+        if (drawn) {
+            CpvTri t;
+            cpv_p0::Stage::setup<true>(P, g, t);
+            ok = cpv_tri_live(t) ? 1u : 0u;
+#pragma unroll
+            for (int c = 0; c < 4; c++) colours[threadIdx.x][c] = t.var[0][c];
+        }
+    }
+    live[threadIdx.x] = ok;
+    __syncthreads();
+    const uint64_t first = static_cast<uint64_t>(blockIdx.x) * 256u;
+    for (uint32_t k = 0; k < 256u; k++) {
+        if (!live[k]) continue;
+        const float colour[4] = {colours[k][0], colours[k][1], colours[k][2], colours[k][3]};
+        uint8_t bytes[4];
+        cpv_p0::cpv_blend_table_column(colour, P.blend_constants, threadIdx.x, bytes);
+        uint8_t* table = P.tables + (first + k) * 1024u;
+#pragma unroll
+        for (int c = 0; c < 4; c++) table[c * 256 + threadIdx.x] = bytes[c];
+    }
+}
+
 /* Primitives of one tile of a single draw: every primitive (direct mode), the
  * tile's bin list[begin, end) in API order, or — when the bin list overflowed
  * its capacity — every primitive whose tile rectangle covers the tile. */
@@ -64,7 +103,7 @@ struct CpvPlainSource {
         return cpv_p0::Stage::shade(P, t, w, x, y, colour, mapped);
     }
     __device__ __forceinline__ void rop(const CpvTri& t, const float colour[4], float mapped, CpvPixel& s) const {
-        cpv_p0::Stage::rop(P.blend_constants, cpv_tri_front(t), colour, mapped, s);
+        cpv_p0::Stage::rop(P.blend_constants, cpv_tri_front(t), colour, mapped, s, cpv_p0::Stage::table(P, t));
     }
     __device__ __forceinline__ void load_pixel(uint64_t pix, CpvPixel& s) const { cpv_p0::Stage::load_pixel(P.color, P.depth, pix, s); }
     __device__ __forceinline__ void store_pixel(uint64_t pix, const CpvPixel& s) const { cpv_p0::Stage::store_pixel(P.color, P.depth, pix, s); }

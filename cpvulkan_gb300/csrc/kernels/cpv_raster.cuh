@@ -23,6 +23,7 @@
 #endif
 #define CPV_DEFERRED (CPV_SCHEDULE == 1)
 #define CPV_SPARSE (CPV_SCHEDULE == 2)
+#define CPV_WARP_LISTS (CPV_SCHEDULE == 0) /* immediate: each warp walks only the primitives reaching its rows */
 #ifndef CPV_SLOT_DEPTH
 #define CPV_SLOT_DEPTH 16 /* sparse: fragments a pixel takes per batch before its fallback */
 #endif
@@ -35,12 +36,17 @@
 #ifndef CPV_BATCH
 #define CPV_BATCH 128
 #endif
+#ifndef CPV_ANY_FS_CONSTANT
+#define CPV_ANY_FS_CONSTANT 0 /* some pipeline of the module shades once per primitive */
+#endif
 #define CPV_TILE (1 << CPV_TILE_SHIFT)
 #define CPV_RT_THREADS ((CPV_TILE * CPV_TILE) < (32 * CPV_RT_WARPS) ? (CPV_TILE * CPV_TILE) : (32 * CPV_RT_WARPS))
 #define CPV_PPT ((CPV_TILE * CPV_TILE) / CPV_RT_THREADS)
 #define CPV_ROWS_PER_PASS (CPV_RT_THREADS / CPV_TILE)
+#define CPV_WARP_ROWS (32 / CPV_TILE > 0 ? 32 / CPV_TILE : 1) /* tile rows one warp covers per pass */
 #define CPV_NV_ALLOC (CPV_NV_MAX > 0 ? CPV_NV_MAX : 1)
-#define CPV_NV_PAD ((CPV_NV_ALLOC + 3) & ~3)
+#define CPV_NV_ROOM (CPV_ANY_FS_CONSTANT && CPV_NV_ALLOC < 4 ? 4 : CPV_NV_ALLOC)
+#define CPV_NV_PAD ((CPV_NV_ROOM + 3) & ~3)
 #define CPV_SLOTS 4
 #define CPV_NSLOT (CPV_RT_THREADS * CPV_SLOTS)
 
@@ -52,7 +58,9 @@ struct __align__(16) CpvTri {
     int4 box;        /* pixel bounding box x0, y0, x1, y1 (end exclusive) */
     float4 za;       /* NDC z of p0..p2 (after the CW swap), |area| */
     float4 wf;       /* clip w of p0..p2, flags (see below) */
-    float var[3][CPV_NV_PAD];
+    float var[3][CPV_NV_PAD]; /* varyings per vertex; for a pipeline whose fragment
+                                 shader is constant per primitive, var[0][0..3]
+                                 holds the shaded colour instead */
 };
 
 /* Flag word (wf.w bits): 1 live, 2 front facing, bits 2-5 pipeline index in
@@ -362,6 +370,12 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
     for (int k = 0; k < CPV_PPT; k++) lp[k] = static_cast<uint32_t>((py[k] - tile_y0) * CPV_TILE + (px[k] - tile_x0));
 #endif
 
+#if CPV_WARP_LISTS
+    /* immediate schedule: per warp, the batch's primitives reaching its rows */
+    __shared__ uint8_t warp_list[(CPV_RT_THREADS / 32) * CPV_BATCH];
+    const int32_t warp_y0 = static_cast<int32_t>(ty * CPV_TILE + ((threadIdx.x & ~31u) / CPV_TILE));
+#endif
+
     for (uint64_t base = 0; base < end; base += CPV_BATCH) {
         const uint32_t n = static_cast<uint32_t>((end - base) < CPV_BATCH ? (end - base) : CPV_BATCH);
         __syncthreads();
@@ -448,11 +462,38 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
 #endif
 #if !CPV_DEFERRED
         /* immediate: every pixel's thread tests each primitive in order,
-         * shading and applying what it covers */
+         * shading and applying what it covers. Each warp first lists, in
+         * order, the batch's live primitives whose box reaches its rows, and
+         * walks only those. */
         if (immediate_batch) {
-            for (uint32_t j = 0; j < n; j++) {
+#if CPV_WARP_LISTS
+            const uint32_t lane = threadIdx.x & 31u;
+            uint8_t* mine = warp_list + (threadIdx.x >> 5) * CPV_BATCH;
+            uint32_t count = 0;
+            for (uint32_t b = 0; b < n; b += 32u) {
+                const uint32_t j = b + lane;
+                bool hit = false;
+                if (j < n && cpv_tri_live(tris[j])) {
+                    const int4 box = tris[j].box;
+#pragma unroll
+                    for (int k = 0; k < CPV_PPT; k++) hit = hit || (box.y < warp_y0 + k * CPV_ROWS_PER_PASS + CPV_WARP_ROWS && box.w > warp_y0 + k * CPV_ROWS_PER_PASS);
+                }
+                const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, hit);
+                if (hit) mine[count + __popc(ballot & ((1u << lane) - 1u))] = static_cast<uint8_t>(j);
+                count += __popc(ballot);
+            }
+            __syncwarp();
+#else
+            const uint32_t count = n;
+#endif
+            for (uint32_t m = 0; m < count; m++) {
+#if CPV_WARP_LISTS
+                const uint32_t j = mine[m];
+#else
+                const uint32_t j = m;
+                if (!cpv_tri_live(tris[j])) continue;
+#endif
                 const CpvTri& t = tris[j];
-                if (!cpv_tri_live(t)) continue;
                 const int4 box = t.box;
 #pragma unroll
                 for (int k = 0; k < CPV_PPT; k++) {

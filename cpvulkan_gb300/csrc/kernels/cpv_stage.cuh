@@ -96,6 +96,24 @@ __device__ __forceinline__ void cpv_setup(const CpvDrawParams& P, uint64_t g, Cp
     bool live = box.z > box.x && box.w > box.y;
     if ((CPV_CULL_MODE & 2) && !front) live = false;
     if ((CPV_CULL_MODE & 1) && front) live = false;
+#if CPV_FS_CONSTANT
+    /* The fragment shader reads only flat inputs (the provoking vertex's):
+     * every fragment of the primitive gets this colour, and a discard
+     * discards them all. */
+    if (WITH_VARYINGS && live) {
+        float in[CPV_NV_ALLOC];
+#pragma unroll
+        for (int c = 0; c < CPV_NV_ALLOC; c++) in[c] = c < CPV_NV ? t.var[pslot][c] : 0.0f;
+        const float frag_coord[4] = {0.0f, 0.0f, 0.0f, 1.0f};  /* not read by this shader */
+        float colour[4];
+        if (cpv_fs_run(P, in, frag_coord, front, colour)) live = false;
+#pragma unroll
+        for (int c = 0; c < 4; c++) t.var[0][c] = colour[c];
+#if CPV_BLEND_TABLE
+        t.var[1][0] = __uint_as_float(g32);  /* the primitive's blend table */
+#endif
+    }
+#endif
     const uint32_t flags = (live ? 1u : 0u) | (front ? 2u : 0u) | (pslot << 6);
     t.wf = make_float4(Pn[0][3], Pn[1][3], Pn[2][3], __uint_as_float(flags));
 }
@@ -216,13 +234,23 @@ __device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& 
     frag_coord[1] = static_cast<float>(y);
     frag_coord[2] = depth;
     frag_coord[3] = 1.0f;
+#if CPV_FS_CONSTANT
+    /* shaded once at set-up (a discarding primitive is not live) */
+    (void)in;
+    (void)frag_coord;
+#pragma unroll
+    for (int c = 0; c < 4; c++) colour[c] = t.var[0][c];
+    return false;
+#else
     return cpv_fs_run(P, in, frag_coord, cpv_tri_front(t), colour);
+#endif
 }
 
 /* Depth bounds are rejected at pipeline creation; order as the reference's
  * fragment wrapper: current values → stencil test → depth test → depth /
  * stencil write → colour write (blend, write mask, encode). */
-__device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool front, const float colour[4], float mapped, CpvPixel& s) {
+__device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool front, const float colour[4], float mapped, CpvPixel& s,
+                                        const uint8_t* table = nullptr) {
     const bool has_depth = CPV_DEPTH_FORMAT != 0;
     const bool stencil_on = CPV_STENCIL_TEST && CPV_DEPTH_FORMAT == 130;
     const float current_depth = (CPV_DEPTH_TEST && has_depth) ? s.depth : 0.0f;
@@ -249,6 +277,21 @@ __device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool fro
         cpv_write_depth(s, mapped);
     }
     if (stencil_result && depth_result) {
+#if CPV_BLEND_TABLE
+        if (table) {
+            /* the primitive's blend result for this destination byte, per channel */
+            uint32_t packed = 0u;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const uint32_t d = (s.colour >> cpv_channel_shift(i)) & 0xFFu;
+                packed |= static_cast<uint32_t>(table[i * 256 + d]) << cpv_channel_shift(i);
+            }
+            s.colour = packed;
+            return;
+        }
+#else
+        (void)table;
+#endif
         float out[4];
 #if CPV_BLEND
         float dst[4];
@@ -270,6 +313,29 @@ __device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool fro
     }
 }
 
+/* One destination byte b of a blend table: the colour write of `colour`
+ * (constant over the primitive) over a destination whose channels all hold
+ * byte b, for each of the 4 channels (the same arithmetic as cpv_rop; with
+ * no DST_ALPHA-based colour factor, channel i's result depends only on
+ * destination channel i). */
+__device__ __forceinline__ void cpv_blend_table_column(const float colour[4], const float blend_constants[4], uint32_t b, uint8_t out_bytes[4]) {
+    const float d = CPV_DECODE8(b);
+    const float dst[4] = {d, d, d, d};
+    float out[4];
+#if CPV_BLEND
+    cpv_blend(colour, dst, blend_constants, out);
+#else
+    (void)dst;
+    (void)blend_constants;
+#pragma unroll
+    for (int i = 0; i < 4; i++) out[i] = colour[i];
+#endif
+#pragma unroll
+    for (int i = 0; i < 4; i++) out_bytes[i] = static_cast<uint8_t>(((CPV_WRITE_MASK >> i) & 1u) ? cpv_encode_unorm(out[i], 255.0f) : b);
+}
+
+constexpr bool kBlendTable = CPV_BLEND_TABLE != 0;
+
 /* The stage functions of this pipeline, as one type the module's
  * dispatcher (cpv_dispatch) hands to generic code. */
 struct Stage {
@@ -279,8 +345,19 @@ struct Stage {
                                                  float& mapped) {
         return cpv_shade(P, t, w, x, y, colour, mapped);
     }
-    static __device__ __forceinline__ void rop(const float blend_constants[4], bool front, const float colour[4], float mapped, CpvPixel& s) {
-        cpv_rop(blend_constants, front, colour, mapped, s);
+    static __device__ __forceinline__ void rop(const float blend_constants[4], bool front, const float colour[4], float mapped, CpvPixel& s,
+                                               const uint8_t* table = nullptr) {
+        cpv_rop(blend_constants, front, colour, mapped, s, table);
+    }
+    /* the primitive's blend table in P.tables, or null */
+    static __device__ __forceinline__ const uint8_t* table(const CpvDrawParams& P, const CpvTri& t) {
+#if CPV_BLEND_TABLE
+        return P.tables ? P.tables + static_cast<uint64_t>(__float_as_uint(t.var[1][0])) * 1024u : nullptr;
+#else
+        (void)P;
+        (void)t;
+        return nullptr;
+#endif
     }
     static __device__ __forceinline__ void load_pixel(const uint8_t* c, const uint8_t* d, uint64_t pix, CpvPixel& s) { cpv_load_pixel(c, d, pix, s); }
     static __device__ __forceinline__ void store_pixel(uint8_t* c, uint8_t* d, uint64_t pix, const CpvPixel& s) { cpv_store_pixel(c, d, pix, s); }

@@ -257,7 +257,8 @@ int load(const std::vector<uint8_t>& cubin, uint32_t tile_shift, bool batched, M
              cudaLibraryGetKernel(&out.raster, lib, "cpv_batch_raster") == cudaSuccess;
     else
         ok = cudaLibraryGetKernel(&out.setup_rects, lib, "cpv_setup_rects") == cudaSuccess &&
-             cudaLibraryGetKernel(&out.raster, lib, "cpv_raster") == cudaSuccess;
+             cudaLibraryGetKernel(&out.raster, lib, "cpv_raster") == cudaSuccess &&
+             cudaLibraryGetKernel(&out.blend_tables, lib, "cpv_blend_tables") == cudaSuccess;
     if (!ok) return fail("pipeline module lacks its kernels");
     out.batched = batched;
     out.tile_shift = tile_shift;
@@ -285,6 +286,7 @@ Scratch::~Scratch() {
     cudaFree(list_);
     for (auto* p : scan_) cudaFree(p);
     cudaFree(words_);
+    cudaFree(tables_);
 }
 
 template <typename T>
@@ -304,6 +306,8 @@ int Scratch::reserve_bins(uint64_t entries) {
 }
 
 int Scratch::reserve_list(uint64_t entries) { return grow_tracked(list_, list_cap_, entries); }
+
+int Scratch::reserve_tables(uint64_t bytes) { return grow_tracked(tables_, tables_cap_, bytes); }
 
 int Scratch::reserve_scan(uint64_t n) {
     int level = 0;
@@ -437,6 +441,19 @@ int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& s
         profile_begin(stream, "cpv_span_write");
         cpv_span_write<<<warp_blocks, 256, 0, stream>>>(sc.rects(), G, static_cast<uint32_t>(spans), P.tiles_x, sc.cursor(), sc.list(),
                                                         sc.list_capacity(), sc.words());
+        profile_end(stream);
+        count_launch();
+    }
+    // Blend tables: 1 KiB per primitive, built once per draw, when the
+    // pipeline blends a per-primitive constant colour (up to 4 GiB of them;
+    // beyond, or with CPV_BLEND_TABLES=0, the raster computes the blend).
+    if (m.blend_table && m.blend_tables && env_u32("CPV_BLEND_TABLES", 1u) != 0u && G * 1024u <= (4ull << 30)) {
+        if ((r = sc.reserve_tables(G * 1024u)) != kOk) return r;
+        P.tables = sc.tables();
+        void* args[] = {&P};
+        profile_begin(stream, "cpv_blend_tables");
+        CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.blend_tables), dim3(static_cast<unsigned>((G + 255) / 256)), dim3(256), args, 0,
+                                  stream));
         profile_end(stream);
         count_launch();
     }

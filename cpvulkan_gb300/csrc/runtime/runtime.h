@@ -38,6 +38,8 @@ struct Module {
     cudaLibrary_t library = nullptr;
     cudaKernel_t setup_rects = nullptr;
     cudaKernel_t raster = nullptr;
+    cudaKernel_t blend_tables = nullptr;  // per-draw modules
+    bool blend_table = false;             // the pipeline blends a per-primitive constant colour
     bool batched = false;
     uint32_t tile_shift = 4;
     uint32_t raster_threads = 256;
@@ -63,6 +65,8 @@ public:
     int reserve_bins(uint64_t entries);  // tiles * spans
     int reserve_list(uint64_t entries);
     int reserve_scan(uint64_t n);
+    int reserve_tables(uint64_t bytes);
+    uint8_t* tables() const { return tables_; }
     uint16_t* rects() const { return rects_; }
     uint32_t* counts() const { return counts_; }
     uint32_t* cursor() const { return cursor_; }
@@ -90,6 +94,8 @@ private:
     uint32_t* scan_[8] = {};
     uint64_t scan_cap_[8] = {};
     uint32_t* words_ = nullptr;
+    uint8_t* tables_ = nullptr;
+    uint64_t tables_cap_ = 0;
 };
 
 // Launch-count accounting (kernels this library launched), for benchmarks.

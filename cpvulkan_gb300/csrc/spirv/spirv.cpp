@@ -802,8 +802,10 @@ bool Translator::emit_globals(const EntryPoint& ep, StageResult& out) {
                     if (is_builtin) {
                         if (builtin == BIFragCoord) {
                             for (int i = 0; i < 4; i++) pro_ << "  " << var << ".v[" << i << "] = cpv_frag_coord[" << i << "];\n";
+                            out.reads_frag_coord = true;
                         } else if (builtin == BIFrontFacing) {
                             pro_ << "  " << var << " = cpv_front;\n";
+                            out.reads_front_facing = true;
                         } else {
                             return fail("unsupported fragment input builtin " + std::to_string(builtin));
                         }

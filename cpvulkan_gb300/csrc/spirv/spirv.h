@@ -130,6 +130,8 @@ struct StageResult {
     bool has_kill = false;
     uint32_t samples = 0;      // image sampling instructions emitted
     uint32_t instructions = 0; // SPIR-V instructions of the entry function
+    bool reads_frag_coord = false;    // FS: FragCoord is an input
+    bool reads_front_facing = false;  // FS: FrontFacing is an input
 };
 
 // Translates the entry point of `m` for `model` (0 vertex, 4 fragment) into a
