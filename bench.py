@@ -358,6 +358,8 @@ def run_ours(args, world, rank, dist):
             "clocks": results[head]["clocks"],
             "image_checksum": int(np.asarray(color, dtype=np.uint64).sum() % (1 << 61)),
         }
+        if head == "batched":
+            line["config"]["tuning"] = c.batch_tuning() or "default configuration (pass below the tuning threshold)"
         if "plain" in results and head != "plain":
             pm = results["plain"]["total_ms"] / args.steps
             line["plain"] = {"value": round(tris * world / (pm / 1000.0) / 1e6, 3), "unit": "Mtri/s", "ms_per_step": round(pm, 4),

@@ -92,6 +92,8 @@ def harness():
     h.cpvh_queue.restype = vp
     h.cpvh_queue.argtypes = [vp]
     h.cpvh_last_error.restype = cp
+    h.cpvh_blit.restype = ctypes.c_int
+    h.cpvh_blit.argtypes = [vp, vp, u32, u32, u32, u32, vp, u32, u32, u32, u32, vp, u32, u32, cp, u32]
     h.cpvh_server_create.restype = vp
     h.cpvh_server_create.argtypes = [vp, ctypes.POINTER(ServeConfig), cp, u32]
     h.cpvh_server_run.restype = ctypes.c_int
@@ -165,6 +167,25 @@ class Context:
         r = harness().cpvh_compile_pipelines(self.ptr, scene.ptr, err, len(err))
         if r != VK_SUCCESS:
             raise RuntimeError("pipeline compilation failed (%d): %s" % (r, err.value.decode(errors="replace")))
+
+    def blit(self, src, src_size, src_levels, src_format, regions, filter, dst=None, dst_size=None, dst_levels=1,
+             dst_format=None):
+        """vkCmdBlitImage between RGBA8/BGRA8 images given as packed mip
+        chains (uint8 numpy arrays). regions: sequence of
+        (src_level, sx0, sy0, sx1, sy1, dst_level, dx0, dy0, dx1, dy1).
+        Updates dst in place, or src when dst is None (blits within one
+        image)."""
+        import numpy as np
+
+        reg = np.ascontiguousarray(np.asarray(regions, dtype=np.int32).reshape(-1, 10))
+        err = ctypes.create_string_buffer(1024)
+        dw, dh = dst_size if dst is not None else (0, 0)
+        r = harness().cpvh_blit(self.ptr, src.ctypes.data, src_size[0], src_size[1], src_levels, src_format,
+                                dst.ctypes.data if dst is not None else None, dw, dh, dst_levels,
+                                dst_format if dst_format is not None else src_format, reg.ctypes.data, reg.shape[0],
+                                filter, err, len(err))
+        if r != VK_SUCCESS:
+            raise RuntimeError("blit failed (%d): %s" % (r, err.value.decode(errors="replace")))
 
     @property
     def queue(self):
@@ -298,6 +319,13 @@ def icd_last_error():
     lib = ctypes.CDLL(ICD_PATH)
     lib.cpv_last_error.restype = ctypes.c_char_p
     return lib.cpv_last_error().decode(errors="replace")
+
+
+def batch_tuning():
+    """The ICD's report of this thread's last batch tuning (cpv_batch_tuning)."""
+    lib = ctypes.CDLL(ICD_PATH)
+    lib.cpv_batch_tuning.restype = ctypes.c_char_p
+    return lib.cpv_batch_tuning().decode(errors="replace")
 
 
 def device_available():

@@ -84,9 +84,12 @@ struct Fns {
     CPVH_FN(vkCmdBindVertexBuffers)
     CPVH_FN(vkCmdDraw)
     CPVH_FN(vkCmdDrawIndexed)
+    CPVH_FN(vkCmdDrawIndirect)
+    CPVH_FN(vkCmdDrawIndexedIndirect)
     CPVH_FN(vkCmdCopyBuffer)
     CPVH_FN(vkCmdCopyBufferToImage)
     CPVH_FN(vkCmdCopyImageToBuffer)
+    CPVH_FN(vkCmdBlitImage)
     CPVH_FN(vkCmdPipelineBarrier)
     CPVH_FN(vkCmdPushConstants)
     CPVH_FN(vkCmdBeginRenderPass)
@@ -168,7 +171,7 @@ struct ImageAlloc {
 struct cpvh_renderer {
     cpvh_context* ctx = nullptr;
     const cpv_scene* scene = nullptr;
-    BufferAlloc vertex, index, uniform, staging, readback;
+    BufferAlloc vertex, index, uniform, staging, readback, indirect;
     ImageAlloc colour, depth, texture;
     VkSampler sampler = nullptr;
     VkRenderPass pass = nullptr;
@@ -329,8 +332,12 @@ void record_frame(cpvh_renderer* r, VkCommandBuffer cmd) {
             c->f.vkCmdBindVertexBuffers(cmd, p.bindings[b].binding, 1, &r->vertex.buffer, &off);
         }
         if (d.push_size) c->f.vkCmdPushConstants(cmd, r->layout, VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, 0, d.push_size, d.push);
-        if (d.indexed) {
-            c->f.vkCmdBindIndexBuffer(cmd, r->index.buffer, d.index_offset, static_cast<VkIndexType>(s->index_type));
+        if (d.indexed) c->f.vkCmdBindIndexBuffer(cmd, r->index.buffer, d.index_offset, static_cast<VkIndexType>(s->index_type));
+        if (r->indirect.buffer) {
+            const VkDeviceSize at = static_cast<VkDeviceSize>(i) * 20;
+            if (d.indexed) c->f.vkCmdDrawIndexedIndirect(cmd, r->indirect.buffer, at, 1, 20);
+            else c->f.vkCmdDrawIndirect(cmd, r->indirect.buffer, at, 1, 20);
+        } else if (d.indexed) {
             c->f.vkCmdDrawIndexed(cmd, d.count, d.instance_count, d.first, d.vertex_offset, d.first_instance);
         } else {
             c->f.vkCmdDraw(cmd, d.count, d.instance_count, d.first, d.first_instance);
@@ -594,7 +601,9 @@ cpvh_context* cpvh_open(const char* icd_path, char* err, uint32_t err_len) {
     LOAD_D(vkDestroyFramebuffer); LOAD_D(vkCreateCommandPool); LOAD_D(vkDestroyCommandPool); LOAD_D(vkAllocateCommandBuffers);
     LOAD_D(vkBeginCommandBuffer); LOAD_D(vkEndCommandBuffer); LOAD_D(vkCmdBindPipeline); LOAD_D(vkCmdBindDescriptorSets);
     LOAD_D(vkCmdBindIndexBuffer); LOAD_D(vkCmdBindVertexBuffers); LOAD_D(vkCmdDraw); LOAD_D(vkCmdDrawIndexed); LOAD_D(vkCmdCopyBuffer);
+    LOAD_D(vkCmdDrawIndirect); LOAD_D(vkCmdDrawIndexedIndirect);
     LOAD_D(vkCmdCopyBufferToImage); LOAD_D(vkCmdCopyImageToBuffer); LOAD_D(vkCmdPipelineBarrier); LOAD_D(vkCmdPushConstants);
+    LOAD_D(vkCmdBlitImage);
     LOAD_D(vkCmdBeginRenderPass); LOAD_D(vkCmdEndRenderPass); LOAD_D(vkQueueSubmit); LOAD_D(vkQueueWaitIdle); LOAD_D(vkCreateFence);
     LOAD_D(vkDestroyFence); LOAD_D(vkResetFences); LOAD_D(vkWaitForFences); LOAD_D(vkGetFenceStatus);
 #undef LOAD_D
@@ -656,6 +665,26 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
     r->depth_texel = depth_texel_size(s->depth_format);
     const uint64_t rb_bytes = static_cast<uint64_t>(s->width) * s->height * (4 + r->depth_texel);
     if (make_buffer(c, rb_bytes, VK_BUFFER_USAGE_TRANSFER_DST_BIT, true, r->readback) != VK_SUCCESS) return fail("readback buffer");
+    // CPVH_INDIRECT=1: the frame issues every draw as an indirect draw whose
+    // record (VkDrawIndexedIndirectCommand / VkDrawIndirectCommand, 20-byte
+    // stride) lives in a host-visible buffer.
+    if (const char* ind = std::getenv("CPVH_INDIRECT"); ind && ind[0] == '1' && s->num_draws) {
+        if (make_buffer(c, static_cast<VkDeviceSize>(s->num_draws) * 20, VK_BUFFER_USAGE_INDIRECT_BUFFER_BIT, true, r->indirect) != VK_SUCCESS)
+            return fail("indirect buffer");
+        void* map = nullptr;
+        if (c->f.vkMapMemory(c->device, r->indirect.memory, 0, VK_WHOLE_SIZE, 0, &map) != VK_SUCCESS) return fail("indirect map");
+        for (uint32_t i = 0; i < s->num_draws; i++) {
+            const cpv_scene_draw& d = s->draws[i];
+            uint32_t rec[5];
+            if (d.indexed) {
+                rec[0] = d.count, rec[1] = d.instance_count, rec[2] = d.first, rec[3] = static_cast<uint32_t>(d.vertex_offset), rec[4] = d.first_instance;
+            } else {
+                rec[0] = d.count, rec[1] = d.instance_count, rec[2] = d.first, rec[3] = d.first_instance, rec[4] = 0;
+            }
+            std::memcpy(static_cast<uint8_t*>(map) + static_cast<size_t>(i) * 20, rec, 20);
+        }
+        c->f.vkUnmapMemory(c->device, r->indirect.memory);
+    }
     if (make_image(c, static_cast<VkFormat>(s->color_format), s->width, s->height, 1, VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT | VK_IMAGE_USAGE_TRANSFER_SRC_BIT,
                    VK_IMAGE_ASPECT_COLOR_BIT, r->colour) != VK_SUCCESS)
         return fail("colour image");
@@ -868,6 +897,7 @@ void cpvh_renderer_destroy(cpvh_renderer* r) {
     destroy_buffer(c, r->uniform);
     destroy_buffer(c, r->staging);
     destroy_buffer(c, r->readback);
+    destroy_buffer(c, r->indirect);
     delete r;
 }
 
@@ -996,6 +1026,139 @@ int cpvh_readback(cpvh_renderer* r, uint8_t* color, uint8_t* depth) {
     if (depth && s->depth_format) std::memcpy(depth, static_cast<uint8_t*>(map) + cb, static_cast<uint64_t>(s->width) * s->height * r->depth_texel);
     c->f.vkUnmapMemory(c->device, r->readback.memory);
     return VK_SUCCESS;
+}
+
+int cpvh_blit(cpvh_context* c, uint8_t* src, uint32_t src_w, uint32_t src_h, uint32_t src_levels, uint32_t src_format, uint8_t* dst,
+              uint32_t dst_w, uint32_t dst_h, uint32_t dst_levels, uint32_t dst_format, const int32_t* regions, uint32_t region_count,
+              uint32_t filter, char* err, uint32_t err_len) {
+    const Fns& f = c->f;
+    struct Packed {
+        uint64_t offset[16] = {};
+        uint32_t w[16] = {}, h[16] = {};
+        uint64_t bytes = 0;
+    };
+    auto pack = [](uint32_t w, uint32_t h, uint32_t levels, Packed& p) {
+        for (uint32_t l = 0; l < levels; l++) {
+            p.offset[l] = p.bytes;
+            p.w[l] = w;
+            p.h[l] = h;
+            p.bytes += static_cast<uint64_t>(w) * h * 4;
+            w = w > 1 ? w / 2 : 1;
+            h = h > 1 ? h / 2 : 1;
+        }
+    };
+    ImageAlloc src_img, dst_img;
+    BufferAlloc staging;
+    VkCommandPool pool = nullptr;
+    VkFence fence = nullptr;
+    int rc = VK_SUCCESS;
+    auto cleanup = [&]() {
+        if (fence) f.vkDestroyFence(c->device, fence, nullptr);
+        if (pool) f.vkDestroyCommandPool(c->device, pool, nullptr);
+        destroy_buffer(c, staging);
+        destroy_image(c, dst_img);
+        destroy_image(c, src_img);
+    };
+    auto fail = [&](const std::string& e, int code) {
+        g_err = e + " " + icd_error(c);
+        if (err && err_len) std::snprintf(err, err_len, "%s", g_err.c_str());
+        cleanup();
+        return code;
+    };
+    if (!src || src_levels == 0 || src_levels > 16 || (dst && (dst_levels == 0 || dst_levels > 16)))
+        return fail("blit: bad image description", VK_ERROR_INITIALIZATION_FAILED);
+    Packed sp, dp;
+    pack(src_w, src_h, src_levels, sp);
+    if (dst) pack(dst_w, dst_h, dst_levels, dp);
+    const VkImageUsageFlags usage = VK_IMAGE_USAGE_TRANSFER_SRC_BIT | VK_IMAGE_USAGE_TRANSFER_DST_BIT | VK_IMAGE_USAGE_SAMPLED_BIT;
+    if (make_image(c, static_cast<VkFormat>(src_format), src_w, src_h, src_levels, usage, VK_IMAGE_ASPECT_COLOR_BIT, src_img) != VK_SUCCESS)
+        return fail("blit: source image", VK_ERROR_OUT_OF_DEVICE_MEMORY);
+    if (dst && make_image(c, static_cast<VkFormat>(dst_format), dst_w, dst_h, dst_levels, usage, VK_IMAGE_ASPECT_COLOR_BIT, dst_img) != VK_SUCCESS)
+        return fail("blit: destination image", VK_ERROR_OUT_OF_DEVICE_MEMORY);
+    if (make_buffer(c, sp.bytes + dp.bytes, VK_BUFFER_USAGE_TRANSFER_SRC_BIT | VK_BUFFER_USAGE_TRANSFER_DST_BIT, true, staging) != VK_SUCCESS)
+        return fail("blit: staging buffer", VK_ERROR_OUT_OF_DEVICE_MEMORY);
+    void* map = nullptr;
+    if (f.vkMapMemory(c->device, staging.memory, 0, VK_WHOLE_SIZE, 0, &map) != VK_SUCCESS) return fail("blit: map", VK_ERROR_MEMORY_MAP_FAILED);
+    std::memcpy(map, src, sp.bytes);
+    if (dst) std::memcpy(static_cast<uint8_t*>(map) + sp.bytes, dst, dp.bytes);
+    f.vkUnmapMemory(c->device, staging.memory);
+
+    VkCommandPoolCreateInfo cpi{};
+    cpi.sType = VK_STRUCTURE_TYPE_COMMAND_POOL_CREATE_INFO;
+    if (f.vkCreateCommandPool(c->device, &cpi, nullptr, &pool) != VK_SUCCESS) return fail("blit: command pool", VK_ERROR_INITIALIZATION_FAILED);
+    VkCommandBufferAllocateInfo cai{};
+    cai.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_ALLOCATE_INFO;
+    cai.commandPool = pool;
+    cai.level = VK_COMMAND_BUFFER_LEVEL_PRIMARY;
+    cai.commandBufferCount = 1;
+    VkCommandBuffer cmd = nullptr;
+    if (f.vkAllocateCommandBuffers(c->device, &cai, &cmd) != VK_SUCCESS || !check_dispatch(cmd))
+        return fail("blit: command buffer", VK_ERROR_INITIALIZATION_FAILED);
+    VkFenceCreateInfo fci{};
+    fci.sType = VK_STRUCTURE_TYPE_FENCE_CREATE_INFO;
+    if (f.vkCreateFence(c->device, &fci, nullptr, &fence) != VK_SUCCESS) return fail("blit: fence", VK_ERROR_INITIALIZATION_FAILED);
+
+    VkImage target = dst ? dst_img.image : src_img.image;
+    const Packed& tp = dst ? dp : sp;
+    const uint32_t target_levels = dst ? dst_levels : src_levels;
+    auto level_copy = [](const Packed& p, uint64_t base, uint32_t l) {
+        VkBufferImageCopy bc{};
+        bc.bufferOffset = base + p.offset[l];
+        bc.imageSubresource = {VK_IMAGE_ASPECT_COLOR_BIT, l, 0, 1};
+        bc.imageExtent = {p.w[l], p.h[l], 1};
+        return bc;
+    };
+    VkMemoryBarrier mb{};
+    mb.sType = VK_STRUCTURE_TYPE_MEMORY_BARRIER;
+    mb.srcAccessMask = VK_ACCESS_TRANSFER_WRITE_BIT;
+    mb.dstAccessMask = VK_ACCESS_TRANSFER_READ_BIT | VK_ACCESS_TRANSFER_WRITE_BIT;
+    auto barrier = [&]() {
+        f.vkCmdPipelineBarrier(cmd, VK_PIPELINE_STAGE_TRANSFER_BIT, VK_PIPELINE_STAGE_TRANSFER_BIT, 0, 1, &mb, 0, nullptr, 0, nullptr);
+    };
+    VkCommandBufferBeginInfo bi{};
+    bi.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_BEGIN_INFO;
+    f.vkBeginCommandBuffer(cmd, &bi);
+    for (uint32_t l = 0; l < src_levels; l++) {
+        const VkBufferImageCopy bc = level_copy(sp, 0, l);
+        f.vkCmdCopyBufferToImage(cmd, staging.buffer, src_img.image, VK_IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL, 1, &bc);
+    }
+    if (dst)
+        for (uint32_t l = 0; l < dst_levels; l++) {
+            const VkBufferImageCopy bc = level_copy(dp, sp.bytes, l);
+            f.vkCmdCopyBufferToImage(cmd, staging.buffer, dst_img.image, VK_IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL, 1, &bc);
+        }
+    barrier();
+    for (uint32_t i = 0; i < region_count; i++) {
+        const int32_t* g = regions + i * 10;
+        VkImageBlit b{};
+        b.srcSubresource = {VK_IMAGE_ASPECT_COLOR_BIT, static_cast<uint32_t>(g[0]), 0, 1};
+        b.srcOffsets[0] = {g[1], g[2], 0};
+        b.srcOffsets[1] = {g[3], g[4], 1};
+        b.dstSubresource = {VK_IMAGE_ASPECT_COLOR_BIT, static_cast<uint32_t>(g[5]), 0, 1};
+        b.dstOffsets[0] = {g[6], g[7], 0};
+        b.dstOffsets[1] = {g[8], g[9], 1};
+        f.vkCmdBlitImage(cmd, src_img.image, VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL, target, VK_IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL, 1, &b,
+                         filter ? VK_FILTER_LINEAR : VK_FILTER_NEAREST);
+        barrier();
+    }
+    const uint64_t out_base = dst ? sp.bytes : 0;
+    for (uint32_t l = 0; l < target_levels; l++) {
+        const VkBufferImageCopy bc = level_copy(tp, out_base, l);
+        f.vkCmdCopyImageToBuffer(cmd, target, VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL, staging.buffer, 1, &bc);
+    }
+    f.vkEndCommandBuffer(cmd);
+    VkSubmitInfo si{};
+    si.sType = VK_STRUCTURE_TYPE_SUBMIT_INFO;
+    si.commandBufferCount = 1;
+    si.pCommandBuffers = &cmd;
+    VkResult res = f.vkQueueSubmit(c->queue, 1, &si, fence);
+    if (res == VK_SUCCESS) res = f.vkWaitForFences(c->device, 1, &fence, VK_TRUE, ~0ull);
+    if (res != VK_SUCCESS) return fail("blit: submit", res);
+    if (f.vkMapMemory(c->device, staging.memory, 0, VK_WHOLE_SIZE, 0, &map) != VK_SUCCESS) return fail("blit: map", VK_ERROR_MEMORY_MAP_FAILED);
+    std::memcpy(dst ? dst : src, static_cast<uint8_t*>(map) + out_base, tp.bytes);
+    f.vkUnmapMemory(c->device, staging.memory);
+    cleanup();
+    return rc;
 }
 
 }  // extern "C"

@@ -9,7 +9,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstdio>
 #include <cstring>
+#include <thread>
 
 #include "icd.h"
 
@@ -234,6 +236,42 @@ VkResult draw(Queue* q, State& s, uint32_t count, uint32_t instances, uint32_t f
     return r == rt::kOk ? VK_SUCCESS : VK_ERROR_DEVICE_LOST;
 }
 
+// vkCmdDrawIndirect / vkCmdDrawIndexedIndirect (CPVulkan/CommandBuffer.Draw.cpp:1874-2348):
+// the reference reads each VkDraw(Indexed)IndirectCommand from the buffer on
+// the CPU and runs the draw. Here too the records are read on the host at
+// replay: from the pinned mirror of host-visible memory the device has not
+// written, else from HBM after the queue's earlier work has finished.
+VkResult draw_indirect(Queue* q, State& s, const Cmd& c, const std::vector<DeviceMemory*>& written, bool no_alloc) {
+    const Buffer* b = static_cast<const Buffer*>(c.p[0]);
+    const bool indexed = c.type == CmdType::DrawIndexedIndirect;
+    const uint32_t n = c.u[0], stride = c.u[1], record = indexed ? 20u : 16u;
+    if (n == 0) return VK_SUCCESS;
+    if (!b || !b->memory) return VK_ERROR_DEVICE_LOST;
+    const uint64_t span = static_cast<uint64_t>(n - 1) * stride + record;
+    if (c.q[0] + span > b->size) return VK_ERROR_DEVICE_LOST;
+    std::vector<uint8_t> bytes(span);
+    DeviceMemory* m = b->memory;
+    const uint64_t at = b->offset + c.q[0];
+    const bool device_newer = !m->host || m->device_dirty || std::find(written.begin(), written.end(), m) != written.end();
+    if (!device_newer) {
+        std::memcpy(bytes.data(), m->host + at, span);
+    } else if (cudaStreamSynchronize(q->stream) != cudaSuccess || cudaMemcpy(bytes.data(), m->device + at, span, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return VK_ERROR_DEVICE_LOST;
+    }
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t v[5] = {0, 0, 0, 0, 0};
+        std::memcpy(v, bytes.data() + static_cast<uint64_t>(i) * stride, record);
+        VkResult r;
+        if (indexed)  // indexCount, instanceCount, firstIndex, vertexOffset, firstInstance
+            r = draw(q, s, v[0], v[1], v[2], static_cast<int32_t>(v[3]), v[4], true, no_alloc);
+        else  // vertexCount, instanceCount, firstVertex, firstInstance
+            r = draw(q, s, v[0], v[1], v[2], 0, v[3], false, no_alloc);
+        if (r != VK_SUCCESS) return r;
+    }
+    return VK_SUCCESS;
+}
+
 // Applies a binding / dynamic-state command to `s`; false for any other.
 bool apply_state(State& s, const Cmd& c) {
     switch (c.type) {
@@ -298,6 +336,113 @@ ModuleConfig batch_config(const std::vector<Pipeline*>& pipelines) {
     return module_config(pipelines[0]->tile_shift, dense, constant);
 }
 
+// ---- batch tuner ----
+//
+// The tile size and the warps per tile CTA change only the speed of a batch,
+// never its image: every configuration applies each pixel's fragments in API
+// order. The tuner therefore times the pass itself under each candidate and
+// keeps the fastest (CPV_AUTOTUNE: 0 off, 1 every batched pass, default
+// passes of at least CPV_AUTOTUNE_MIN_DRAWS = 256 draws; an explicit
+// CPV_TILE or CPV_RT_WARPS turns it off).
+
+thread_local std::string g_last_tuning;
+
+bool tuning_enabled(size_t draws) {
+    const uint32_t mode = env_u32("CPV_AUTOTUNE", 2u);
+    if (mode == 0u || std::getenv("CPV_TILE") || std::getenv("CPV_RT_WARPS")) return false;
+    return mode == 1u || draws >= env_u32("CPV_AUTOTUNE_MIN_DRAWS", 256u);
+}
+
+// Tile 8, 16 and 32 px, each with the warp counts that suit its pixels.
+std::vector<ModuleConfig> tune_candidates(const ModuleConfig& base) {
+    static const uint32_t shapes[][2] = {{3, 2}, {4, 4}, {4, 8}, {5, 8}, {5, 16}};
+    std::vector<ModuleConfig> out;
+    for (const auto& s : shapes) {
+        ModuleConfig mc = base;
+        mc.tile_shift = s[0];
+        mc.warps = s[1];
+        out.push_back(mc);
+    }
+    return out;
+}
+
+// Compiles (NVRTC, one thread per candidate) and loads the candidates'
+// modules; null where a candidate failed.
+std::vector<rt::Module*> candidate_modules(Device* dev, const std::vector<Pipeline*>& pipelines, const std::vector<ModuleConfig>& cands) {
+    std::vector<rt::Module*> out(cands.size(), nullptr);
+    std::vector<std::thread> workers;
+    for (size_t i = 0; i < cands.size(); i++)
+        workers.emplace_back([&, i]() { out[i] = batch_module(dev, pipelines, cands[i]); });
+    for (auto& w : workers) w.join();
+    return out;
+}
+
+std::string batch_signature(const std::vector<Pipeline*>& pipelines, const rt::BatchDraws& in) {
+    uint64_t prims = 0;
+    for (const CpvDrawParams& P : in.draws) prims += P.total_prims;
+    std::string sig = std::to_string(in.draws.size()) + "/" + std::to_string(prims) + "/" + std::to_string(in.fb_width) + "x" +
+                      std::to_string(in.fb_height);
+    for (const Pipeline* p : pipelines)
+        for (uint8_t b : p->key) sig += static_cast<char>('a' + (b & 15)), sig += static_cast<char>('a' + (b >> 4));
+    return sig;
+}
+
+// Times every candidate on the pass and returns the fastest module and plan.
+// The attachments are saved first and restored before each run and at the
+// end, so the pass still renders once from its initial contents.
+bool tune_batch(Queue* q, Device* dev, const std::vector<Pipeline*>& pipelines, const rt::BatchDraws& in, uint64_t color_bytes,
+                uint64_t depth_bytes, ModuleConfig& chosen, rt::Module*& best_m, std::unique_ptr<rt::BatchPlan>& best_plan) {
+    const std::vector<ModuleConfig> cands = tune_candidates(batch_config(pipelines));
+    const std::vector<rt::Module*> mods = candidate_modules(dev, pipelines, cands);
+    uint8_t* saved = nullptr;
+    if (cudaMalloc(&saved, color_bytes + depth_bytes) != cudaSuccess) return false;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    bool ok = cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+    auto copy = [&](bool restore) {
+        bool good = cudaMemcpyAsync(restore ? in.color : saved, restore ? saved : in.color, color_bytes, cudaMemcpyDeviceToDevice, q->stream) == cudaSuccess;
+        if (depth_bytes)
+            good = good && cudaMemcpyAsync(restore ? in.depth : saved + color_bytes, restore ? saved + color_bytes : in.depth, depth_bytes,
+                                           cudaMemcpyDeviceToDevice, q->stream) == cudaSuccess;
+        return good;
+    };
+    ok = ok && copy(false);
+    float best_ms = 0.0f;
+    std::string report;
+    for (size_t i = 0; ok && i < cands.size(); i++) {
+        if (!mods[i]) continue;
+        auto plan = std::make_unique<rt::BatchPlan>();
+        if (plan->build(*mods[i], in, q->stream) != rt::kOk) continue;
+        // One warm run (graph capture, pair-buffer growth), one timed run.
+        if (!copy(true) || plan->launch(*mods[i], q->stream) != rt::kOk || !copy(true)) continue;
+        if (cudaEventRecord(e0, q->stream) != cudaSuccess || plan->launch(*mods[i], q->stream) != rt::kOk ||
+            cudaEventRecord(e1, q->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+            continue;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        char line[96];
+        std::snprintf(line, sizeof(line), "%stile %u warps %u schedule %u: %.3f ms", report.empty() ? "" : "; ", 1u << cands[i].tile_shift,
+                      cands[i].warps, cands[i].schedule, ms);
+        report += line;
+        if (!best_plan || ms < best_ms) {
+            best_ms = ms;
+            chosen = cands[i];
+            best_m = mods[i];
+            best_plan = std::move(plan);
+        }
+    }
+    ok = copy(true) && ok;
+    cudaStreamSynchronize(q->stream);
+    cudaFree(saved);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (best_plan) {
+        char line[64];
+        std::snprintf(line, sizeof(line), "; chosen tile %u warps %u", 1u << chosen.tile_shift, chosen.warps);
+        g_last_tuning = report + line;
+    }
+    return ok && best_plan != nullptr;
+}
+
 // Builds the batch of the render pass whose commands are (begin, end): the
 // draws' parameters, the pipeline set, the batched module and the plan.
 // Leaves state->plain set when the pass does not batch.
@@ -338,7 +483,42 @@ void build_batch(Queue* q, const CommandBuffer* cb, size_t begin, size_t end, co
     if (in.draws.empty()) return;
     in.vw = vw;
     in.vh = vh;
-    rt::Module* m = batch_module(cb->device, pipelines, batch_config(pipelines));
+    Device* dev = cb->device;
+    ModuleConfig mc = batch_config(pipelines);
+    if (tuning_enabled(in.draws.size())) {
+        const std::string sig = batch_signature(pipelines, in);
+        bool known = false;
+        {
+            std::lock_guard<std::mutex> lock(dev->batch_mutex);
+            auto it = dev->tuned.find(sig);
+            if (it != dev->tuned.end()) {
+                mc = it->second;
+                known = true;
+            }
+        }
+        if (!known) {
+            uint32_t w = 0, h = 0;
+            view_base(s.fb->attachments[s.pass->colour[0]], w, h);
+            const uint64_t color_bytes = static_cast<uint64_t>(w) * h * 4u;
+            uint64_t depth_bytes = 0;
+            if (s.pass->depth != VK_ATTACHMENT_UNUSED) {
+                const ImageView* dv = s.fb->attachments[s.pass->depth];
+                depth_bytes = static_cast<uint64_t>(w) * h * dv->image->texel;
+            }
+            rt::Module* m = nullptr;
+            std::unique_ptr<rt::BatchPlan> plan;
+            if (tune_batch(q, dev, pipelines, in, color_bytes, depth_bytes, mc, m, plan)) {
+                std::lock_guard<std::mutex> lock(dev->batch_mutex);
+                dev->tuned[sig] = mc;
+                state.module = m;
+                state.plan = std::move(plan);
+                state.plain = false;
+                return;
+            }
+            mc = batch_config(pipelines);
+        }
+    }
+    rt::Module* m = batch_module(dev, pipelines, mc);
     if (!m) return;
     auto plan = std::make_unique<rt::BatchPlan>();
     if (plan->build(*m, in, q->stream) != rt::kOk) return;
@@ -434,6 +614,42 @@ VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& writte
             written.push_back(to_image ? img->memory : buf->memory);
             break;
         }
+        case CmdType::BlitImage: {
+            // Colour regions between RGBA8/BGRA8 2D images (depth/stencil
+            // blits, other formats and 3D regions are not implemented).
+            Image* src = static_cast<Image*>(c.p[0]);
+            Image* dst = static_cast<Image*>(c.p[1]);
+            auto colour8 = [](VkFormat f) { return f == VK_FORMAT_R8G8B8A8_UNORM || f == VK_FORMAT_B8G8R8A8_UNORM; };
+            if (!src || !dst || !src->memory || !dst->memory || !colour8(src->format) || !colour8(dst->format)) return VK_ERROR_DEVICE_LOST;
+            for (const VkImageBlit& b : c.blit_regions) {
+                const auto& ss = b.srcSubresource;
+                const auto& ds = b.dstSubresource;
+                if (ss.aspectMask != VK_IMAGE_ASPECT_COLOR_BIT || ss.mipLevel >= src->levels || ds.mipLevel >= dst->levels ||
+                    ss.layerCount != ds.layerCount || b.srcOffsets[1].z - b.srcOffsets[0].z != 1 || b.dstOffsets[1].z - b.dstOffsets[0].z != 1)
+                    return VK_ERROR_DEVICE_LOST;
+                const ImageLevel& sl = src->level[ss.mipLevel];
+                const ImageLevel& dl = dst->level[ds.mipLevel];
+                for (uint32_t layer = 0; layer < ss.layerCount; layer++) {
+                    if (ss.baseArrayLayer + layer >= src->layers || ds.baseArrayLayer + layer >= dst->layers) return VK_ERROR_DEVICE_LOST;
+                    CpvTexture t;
+                    std::memset(&t, 0, sizeof(t));
+                    t.data = src->device_ptr() + static_cast<uint64_t>(ss.baseArrayLayer + layer) * src->layer_size + sl.offset;
+                    t.bytes = sl.size;
+                    t.levels = 1;
+                    t.level_w[0] = sl.width;
+                    t.level_h[0] = sl.height;
+                    t.format = static_cast<uint32_t>(src->format);
+                    t.address_u = t.address_v = VK_SAMPLER_ADDRESS_MODE_CLAMP_TO_EDGE;
+                    uint8_t* out = dst->device_ptr() + static_cast<uint64_t>(ds.baseArrayLayer + layer) * dst->layer_size + dl.offset;
+                    const int32_t sr[4] = {b.srcOffsets[0].x, b.srcOffsets[0].y, b.srcOffsets[1].x, b.srcOffsets[1].y};
+                    const int32_t dr[4] = {b.dstOffsets[0].x, b.dstOffsets[0].y, b.dstOffsets[1].x, b.dstOffsets[1].y};
+                    if (rt::blit(q->stream, t, out, dl.width, dl.height, static_cast<uint32_t>(dst->format), sr, dr, c.u[0]) != rt::kOk)
+                        return VK_ERROR_DEVICE_LOST;
+                }
+            }
+            written.push_back(dst->memory);
+            break;
+        }
         case CmdType::FillBuffer: {
             Buffer* dst = static_cast<Buffer*>(c.p[0]);
             uint64_t off = c.q[0], size = c.q[1];
@@ -453,9 +669,9 @@ VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& writte
             written.push_back(dst->memory);
             break;
         }
-        case CmdType::Barrier:
         case CmdType::DrawIndirect:
-        case CmdType::DrawIndexedIndirect:
+        case CmdType::DrawIndexedIndirect: r = draw_indirect(q, s, c, written, no_alloc); break;
+        case CmdType::Barrier:
         default:
             break;
         }
@@ -483,8 +699,9 @@ VkResult run_command_buffer(Queue* q, CommandBuffer* cb, std::vector<DeviceMemor
         const size_t before = written.size();
         const VkResult r = execute(q, cb, written, false);
         if (r != VK_SUCCESS) return r;
-        bool ok = true;
-        for (const Cmd& c : cb->cmds) ok = ok && c.type != CmdType::UpdateBuffer;
+        bool ok = true;  // indirect draws read their arguments on the host at every replay
+        for (const Cmd& c : cb->cmds)
+            ok = ok && c.type != CmdType::UpdateBuffer && c.type != CmdType::DrawIndirect && c.type != CmdType::DrawIndexedIndirect;
         for (const auto& kv : cb->batches) ok = ok && kv.second->plain;
         cb->graphable = ok ? 1 : 0;
         cb->written.assign(written.begin() + static_cast<std::ptrdiff_t>(before), written.end());
@@ -555,8 +772,13 @@ void precompile_batches(CommandBuffer* cb) {
             if (std::find(pipelines.begin(), pipelines.end(), bound) == pipelines.end()) pipelines.push_back(bound);
             break;
         case CmdType::EndRenderPass:
+            // Compiled and cached; errors surface at submit. A pass the tuner
+            // will time gets every candidate compiled now, in parallel.
             if (in_pass && draws >= min_draws && !pipelines.empty() && pipelines.size() <= 16) {
-                batch_module(cb->device, pipelines, batch_config(pipelines));  // compiled and cached; errors surface at submit
+                if (tuning_enabled(draws))
+                    candidate_modules(cb->device, pipelines, tune_candidates(batch_config(pipelines)));
+                else
+                    batch_module(cb->device, pipelines, batch_config(pipelines));
             }
             in_pass = false;
             break;
@@ -564,6 +786,8 @@ void precompile_batches(CommandBuffer* cb) {
         }
     }
 }
+
+const char* last_tuning() { return g_last_tuning.c_str(); }
 
 VkResult check_no_alloc(CommandBuffer* cb) {
     Pipeline* pipeline = nullptr;

@@ -934,6 +934,15 @@ VKAPI_ATTR void VKAPI_CALL CmdCopyImageToBuffer(VkCommandBuffer cmd, VkImage src
     c.p[1] = reinterpret_cast<void*>(src);
     c.image_regions.assign(r, r + n);
 }
+// vkCmdBlitImage (CPVulkan/CommandBuffer.cpp:822-826).
+VKAPI_ATTR void VKAPI_CALL CmdBlitImage(VkCommandBuffer cmd, VkImage src, VkImageLayout, VkImage dst, VkImageLayout, uint32_t n, const VkImageBlit* r,
+                                        VkFilter filter) {
+    auto& c = push(cmd, CmdType::BlitImage);
+    c.p[0] = reinterpret_cast<void*>(src);
+    c.p[1] = reinterpret_cast<void*>(dst);
+    c.u[0] = static_cast<uint32_t>(filter);
+    c.blit_regions.assign(r, r + n);
+}
 VKAPI_ATTR void VKAPI_CALL CmdFillBuffer(VkCommandBuffer cmd, VkBuffer dst, VkDeviceSize off, VkDeviceSize size, uint32_t data) {
     auto& c = push(cmd, CmdType::FillBuffer);
     c.p[0] = reinterpret_cast<void*>(dst);
@@ -1139,7 +1148,7 @@ const Entry kDevice[] = {
     E(DestroyRenderPass), E(CreateFramebuffer), E(DestroyFramebuffer), E(CreateCommandPool), E(DestroyCommandPool), E(ResetCommandPool),
     E(AllocateCommandBuffers), E(FreeCommandBuffers), E(BeginCommandBuffer), E(EndCommandBuffer), E(ResetCommandBuffer), E(CmdBindPipeline),
     E(CmdSetViewport), E(CmdSetScissor), E(CmdSetBlendConstants), E(CmdBindDescriptorSets), E(CmdBindIndexBuffer), E(CmdBindVertexBuffers),
-    E(CmdDraw), E(CmdDrawIndexed), E(CmdDrawIndirect), E(CmdDrawIndexedIndirect), E(CmdCopyBuffer), E(CmdCopyBufferToImage),
+    E(CmdDraw), E(CmdDrawIndexed), E(CmdDrawIndirect), E(CmdDrawIndexedIndirect), E(CmdCopyBuffer), E(CmdCopyBufferToImage), E(CmdBlitImage),
     E(CmdCopyImageToBuffer), E(CmdFillBuffer), E(CmdUpdateBuffer), E(CmdPipelineBarrier), E(CmdPushConstants), E(CmdBeginRenderPass),
     E(CmdEndRenderPass), E(QueueSubmit), E(CreateFence), E(DestroyFence), E(ResetFences), E(GetFenceStatus), E(WaitForFences),
     E(CreateSemaphore), E(DestroySemaphore),
@@ -1189,6 +1198,8 @@ CPV_EXPORT PFN_vkVoidFunction VKAPI_CALL vk_icdGetPhysicalDeviceProcAddr(VkInsta
 CPV_EXPORT const char* cpv_last_error(void) { return cpv::rt::last_error(); }
 
 CPV_EXPORT uint64_t cpv_kernel_launches(void) { return cpv::rt::launches(); }
+
+CPV_EXPORT const char* cpv_batch_tuning(void) { return cpv::icd::last_tuning(); }
 
 CPV_EXPORT int cpv_queue_record(VkQueue queue, uint32_t slot) {
     auto* q = reinterpret_cast<cpv::icd::Queue*>(queue);

@@ -186,7 +186,7 @@ std::string compose_module(const std::vector<std::string>& stages, const std::ve
 enum class CmdType : uint8_t {
     BeginRenderPass, EndRenderPass, BindPipeline, BindVertexBuffers, BindIndexBuffer, BindDescriptorSets, PushConstants,
     SetViewport, SetScissor, SetBlendConstants, Draw, DrawIndexed, DrawIndirect, DrawIndexedIndirect, CopyBuffer,
-    CopyBufferToImage, CopyImageToBuffer, FillBuffer, UpdateBuffer, Barrier,
+    CopyBufferToImage, CopyImageToBuffer, FillBuffer, UpdateBuffer, Barrier, BlitImage,
 };
 
 struct Cmd {
@@ -200,6 +200,7 @@ struct Cmd {
     std::vector<uint64_t> list;
     std::vector<VkBufferImageCopy> image_regions;
     std::vector<VkBufferCopy> buffer_regions;
+    std::vector<VkImageBlit> blit_regions;
     std::vector<VkClearValue> clears;
     VkViewport viewport{};
 };
@@ -279,6 +280,9 @@ struct Device : Dispatchable {
     // Batched modules by (pipeline keys, module configuration).
     std::mutex batch_mutex;
     std::map<std::string, std::unique_ptr<rt::Module>> batch_modules;
+    // Module configuration the tuner chose, by batch signature (pipeline
+    // keys, draw and primitive counts, target size); guarded by batch_mutex.
+    std::map<std::string, ModuleConfig> tuned;
 };
 
 // The batched module over `pipelines` (module pipeline i = pipelines[i]),
@@ -297,6 +301,9 @@ VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& writte
 // At vkEndCommandBuffer: compiles (NVRTC) and caches the batched module of
 // every render pass that will run batched, so its first submission does not.
 void precompile_batches(CommandBuffer* cb);
+// Report of the calling thread's last batch tuning: one "tile/warps/schedule
+// ms" entry per candidate and the choice ("" when none ran).
+const char* last_tuning();
 // Checks, before any work is enqueued, that every draw of `cb` fits the fixed
 // scratch array (VK_ERROR_OUT_OF_DEVICE_MEMORY and a message otherwise).
 VkResult check_no_alloc(CommandBuffer* cb);

@@ -171,9 +171,13 @@ bool module_cubin(Device* dev, const std::string& source, std::array<uint8_t, 32
 rt::Module* batch_module(Device* dev, const std::vector<Pipeline*>& pipelines, const ModuleConfig& mc) {
     std::string id = std::to_string(mc.tile_shift) + "/" + std::to_string(mc.schedule) + "/" + std::to_string(mc.warps) + "/" + std::to_string(mc.batch);
     for (const Pipeline* p : pipelines) id += "/" + hex(p->key);
-    std::lock_guard<std::mutex> lock(dev->batch_mutex);
-    auto it = dev->batch_modules.find(id);
-    if (it != dev->batch_modules.end()) return it->second.get();
+    {
+        std::lock_guard<std::mutex> lock(dev->batch_mutex);
+        auto it = dev->batch_modules.find(id);
+        if (it != dev->batch_modules.end()) return it->second.get();
+    }
+    // Compiled and loaded outside the lock, so that several configurations
+    // (the tuner's candidates) compile at once; the first one stored wins.
     std::vector<std::string> stages;
     std::vector<uint32_t> nvs;
     for (const Pipeline* p : pipelines) {
@@ -197,6 +201,12 @@ rt::Module* batch_module(Device* dev, const std::vector<Pipeline*>& pipelines, c
     if (rt::load(cubin, mc.tile_shift, true, *m, err) != rt::kOk) {
         rt::set_last_error("batched module load failed: " + err);
         return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(dev->batch_mutex);
+    auto it = dev->batch_modules.find(id);
+    if (it != dev->batch_modules.end()) {
+        rt::unload(*m);
+        return it->second.get();
     }
     rt::Module* out = m.get();
     dev->batch_modules[id] = std::move(m);

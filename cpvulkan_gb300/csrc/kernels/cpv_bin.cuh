@@ -337,6 +337,48 @@ extern "C" __global__ void __launch_bounds__(256) cpv_tile_ranges(const uint32_t
     }
 }
 
+/* ---- vkCmdBlitImage (CPVulkan/CommandBuffer.cpp:32-240), colour aspect ----
+ *
+ * One thread per destination texel of a region (2D; the reference's third
+ * axis has depth 1 and contributes an exact lerp by 0). Its source position
+ * is the reference's: u = (dstX + 0.5 - dst0.x) * ((src1.x - src0.x) / (dst1.x
+ * - dst0.x)) + src0.x in binary32, normalised by the source level's width,
+ * and the source level is sampled as SampleImage samples it for a blit
+ * (level 0 of a one-level image, the blit's filter, CLAMP_TO_EDGE). The
+ * result is written through the UNORM8 encoder. `src` describes the source
+ * level as level 0. */
+struct CpvBlitRegion {
+    int32_t src[4]; /* x0, y0, x1, y1 */
+    int32_t dst[4];
+};
+
+extern "C" __global__ void __launch_bounds__(256) cpv_blit(CpvTexture src, uint8_t* __restrict__ dst, uint32_t dst_w, uint32_t dst_h,
+                                                           uint32_t dst_format, CpvBlitRegion r, uint32_t filter) {
+    const int32_t dw = abs(r.dst[2] - r.dst[0]), dh = abs(r.dst[3] - r.dst[1]);
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (dw == 0 || dh == 0 || i >= static_cast<uint64_t>(dw) * dh) return;
+    const int32_t x = static_cast<int32_t>(i % static_cast<uint64_t>(dw)), y = static_cast<int32_t>(i / static_cast<uint64_t>(dw));
+    const int32_t dst_x = r.dst[2] < r.dst[0] ? x + r.dst[2] : x + r.dst[0];
+    const int32_t dst_y = r.dst[3] < r.dst[1] ? y + r.dst[3] : y + r.dst[1];
+    if (dst_x < 0 || dst_y < 0 || dst_x >= static_cast<int32_t>(dst_w) || dst_y >= static_cast<int32_t>(dst_h)) return;
+    const float sx = __fdiv_rn(static_cast<float>(r.src[2] - r.src[0]), static_cast<float>(r.dst[2] - r.dst[0]));
+    const float sy = __fdiv_rn(static_cast<float>(r.src[3] - r.src[1]), static_cast<float>(r.dst[3] - r.dst[1]));
+    const float u = __fadd_rn(__fmul_rn(__fsub_rn(__fadd_rn(static_cast<float>(dst_x), 0.5f), static_cast<float>(r.dst[0])), sx),
+                              static_cast<float>(r.src[0]));
+    const float v = __fadd_rn(__fmul_rn(__fsub_rn(__fadd_rn(static_cast<float>(dst_y), 0.5f), static_cast<float>(r.dst[1])), sy),
+                              static_cast<float>(r.src[1]));
+    float value[4];
+    cpv_sample_level(src, 0u, __fdiv_rn(u, __uint2float_rn(src.level_w[0])), __fdiv_rn(v, __uint2float_rn(src.level_h[0])), filter, value);
+    uint32_t packed = 0u;
+    const bool bgra = dst_format == CPV_FMT_B8G8R8A8_UNORM;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const int byte = (bgra && c < 3) ? 2 - c : c;
+        packed |= cpv_encode_unorm(value[c], 255.0f) << (8 * byte);
+    }
+    reinterpret_cast<uint32_t*>(dst)[static_cast<uint64_t>(dst_y) * dst_w + dst_x] = packed;
+}
+
 /* ---- fills ---- */
 
 extern "C" __global__ void __launch_bounds__(256) cpv_fill_u32(uint32_t* __restrict__ dst, uint64_t count, uint32_t value) {

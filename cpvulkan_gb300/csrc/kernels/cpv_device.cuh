@@ -272,8 +272,13 @@ __device__ __forceinline__ void cpv_texel(const CpvTexture& t, uint32_t level, i
         return;
     }
     const uint32_t px = __ldg(reinterpret_cast<const uint32_t*>(t.data + off));
+    /* B8G8R8A8 stores red in byte 2 (CPVulkanBase/Formats.cpp:255) */
+    const bool bgra = t.format == CPV_FMT_B8G8R8A8_UNORM;
 #pragma unroll
-    for (int i = 0; i < 4; i++) out[i] = CPV_DECODE8((px >> (8 * i)) & 0xFFu);
+    for (int i = 0; i < 4; i++) {
+        const int byte = (bgra && i < 3) ? 2 - i : i;
+        out[i] = CPV_DECODE8((px >> (8 * byte)) & 0xFFu);
+    }
 }
 
 /* lerp with a double-precision delta (CPVulkan/ImageSampler.cpp:51-55):

@@ -391,6 +391,22 @@ int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, 
     return kOk;
 }
 
+int blit(cudaStream_t stream, const CpvTexture& src, uint8_t* dst, uint32_t dst_w, uint32_t dst_h, uint32_t dst_format, const int32_t src_region[4],
+         const int32_t dst_region[4], uint32_t filter) {
+    CpvBlitRegion r;
+    for (int i = 0; i < 4; i++) {
+        r.src[i] = src_region[i];
+        r.dst[i] = dst_region[i];
+    }
+    const uint64_t texels = static_cast<uint64_t>(std::abs(r.dst[2] - r.dst[0])) * static_cast<uint64_t>(std::abs(r.dst[3] - r.dst[1]));
+    if (texels == 0) return kOk;
+    if (texels > (1ull << 38)) return kErrInvalid;  // keeps the grid within 2^30 blocks
+    cpv_blit<<<static_cast<unsigned>((texels + 255) / 256), 256, 0, stream>>>(src, dst, dst_w, dst_h, dst_format, r, filter);
+    count_launch();
+    CPV_CUDA(cudaGetLastError());
+    return kOk;
+}
+
 int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& sc) {
     if (P.total_prims == 0 || P.fb_width == 0 || P.fb_height == 0) return kOk;
     const uint32_t shift = m.tile_shift;

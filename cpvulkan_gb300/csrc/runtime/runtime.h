@@ -195,6 +195,13 @@ int static_scratch_check(uint64_t prims, uint32_t tile_shift, uint32_t width, ui
 // the same kernels, allocates nothing, creates no CUDA objects.
 int draw_plain_static(cudaStream_t stream, const Module& m, CpvDrawParams P);
 
+// vkCmdBlitImage of one 2D colour region between RGBA8/BGRA8 levels: `src`
+// describes the source level (as level 0), `dst` points at the destination
+// level's first texel. Regions are {x0, y0, x1, y1} (end exclusive, may be
+// reversed); filter 0 NEAREST, 1 LINEAR.
+int blit(cudaStream_t stream, const CpvTexture& src, uint8_t* dst, uint32_t dst_w, uint32_t dst_h, uint32_t dst_format, const int32_t src_region[4],
+         const int32_t dst_region[4], uint32_t filter);
+
 // Attachment fill with an encoded texel (1, 2, 4 or 8 bytes).
 int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, uint32_t lo, uint32_t hi);
 

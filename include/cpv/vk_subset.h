@@ -328,6 +328,8 @@ enum {
     VK_PIPELINE_STAGE_TRANSFER_BIT = 0x1000,
     VK_PIPELINE_STAGE_BOTTOM_OF_PIPE_BIT = 0x2000,
     VK_PIPELINE_STAGE_ALL_COMMANDS_BIT = 0x10000,
+    VK_ACCESS_TRANSFER_READ_BIT = 0x800,
+    VK_ACCESS_TRANSFER_WRITE_BIT = 0x1000,
     VK_FORMAT_FEATURE_SAMPLED_IMAGE_BIT = 0x1,
     VK_FORMAT_FEATURE_VERTEX_BUFFER_BIT = 0x40,
     VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BIT = 0x80,

@@ -79,6 +79,19 @@ int cpvh_renderer_update(cpvh_renderer* r);
 /* Reads the attachments back (colour: width*height*4; depth: texel-sized). */
 int cpvh_readback(cpvh_renderer* r, uint8_t* color, uint8_t* depth);
 
+/* vkCmdBlitImage through the ICD. src (and dst when not null) hold every mip
+ * level of an RGBA8 (37) / BGRA8 (44) image, level l being
+ * max(w >> l, 1) x max(h >> l, 1) texels, packed one after another. Both
+ * images are uploaded, one vkCmdBlitImage per region is recorded (each 10
+ * ints: src level, src x0, y0, x1, y1, dst level, dst x0, y0, x1, y1) with a
+ * barrier between regions, and the destination is read back into dst, or
+ * into src when dst is null (the regions then blit within the source image,
+ * as a mip chain is generated). filter: 0 NEAREST, 1 LINEAR. Returns a
+ * VkResult. */
+int cpvh_blit(cpvh_context* ctx, uint8_t* src, uint32_t src_w, uint32_t src_h, uint32_t src_levels, uint32_t src_format, uint8_t* dst,
+              uint32_t dst_w, uint32_t dst_h, uint32_t dst_levels, uint32_t dst_format, const int32_t* regions, uint32_t region_count,
+              uint32_t filter, char* err, uint32_t err_len);
+
 /* The ICD's vkQueue (for the ICD's timing helpers). */
 void* cpvh_queue(cpvh_context* ctx);
 const char* cpvh_last_error(void);

@@ -133,6 +133,7 @@ struct Texture {
     uint32_t width = 0, height = 0, levels = 0;
     uint64_t level_offset[16] = {};
     uint32_t level_w[16] = {}, level_h[16] = {};
+    uint32_t format = 37;  /* VkFormat: R8G8B8A8 (37) or B8G8R8A8 (44) UNORM */
 };
 
 /* wrap (CPVulkan/ImageSampler.cpp:12-38). */
@@ -177,7 +178,8 @@ void get_texel(const Texture& t, uint32_t level, int32_t x, int32_t y, uint32_t 
         for (int i = 0; i < 4; i++) out[i] = 0.0f;
         return;
     }
-    for (int i = 0; i < 4; i++) out[i] = decode_unorm8(t.data[off + i]);
+    /* B8G8R8A8 keeps red in byte 2 (CPVulkanBase/Formats.cpp:255) */
+    for (int i = 0; i < 4; i++) out[i] = decode_unorm8(t.data[off + ((t.format == 44 && i < 3) ? 2 - i : i)]);
 }
 
 /* lerp with a double-precision delta (CPVulkan/ImageSampler.cpp:51-55):
@@ -912,6 +914,50 @@ void cpv_oracle_sample(const uint8_t* texels, uint32_t width, uint32_t height, u
 void cpv_oracle_blend(const float src[4], const float dst[4], const float constant[4], uint32_t src_color, uint32_t dst_color,
                       uint32_t color_op, uint32_t src_alpha, uint32_t dst_alpha, uint32_t alpha_op, float out[4]) {
     blend(src, dst, constant, src_color, dst_color, color_op, src_alpha, dst_alpha, alpha_op, out);
+}
+
+/* BlitImageCommand::Process for one 2D colour region between RGBA8/BGRA8
+ * levels (CPVulkan/CommandBuffer.cpp:57-232): for each destination texel of
+ * the region (negative extents walk from offset 1), the source position
+ * u = (dstX + 0.5 - dst0.x) * ((src1.x - src0.x) / (dst1.x - dst0.x)) + src0.x
+ * (and v) is normalised by the level size and sampled as SampleImage does
+ * for a blit (the level as a one-level image, CLAMP_TO_EDGE, the blit's
+ * filter); SetPixel encodes the result. The third axis of the reference has
+ * depth 1: its lerp by 0 changes nothing. */
+void cpv_oracle_blit(const uint8_t* src, uint32_t src_w, uint32_t src_h, uint32_t src_format, uint8_t* dst, uint32_t dst_w, uint32_t dst_h,
+                     uint32_t dst_format, const int32_t region[8], uint32_t filter) {
+    Texture tex;
+    tex.data = src;
+    tex.width = src_w;
+    tex.height = src_h;
+    tex.levels = 1;
+    tex.level_w[0] = src_w;
+    tex.level_h[0] = src_h;
+    tex.bytes = static_cast<uint64_t>(src_w) * src_h * 4u;
+    tex.format = src_format;
+    cpv_scene_sampler s{};
+    s.address_u = s.address_v = s.address_w = 2; /* CLAMP_TO_EDGE */
+    const int32_t* r0 = region;      /* src x0, y0, x1, y1 */
+    const int32_t* d0 = region + 4;  /* dst x0, y0, x1, y1 */
+    int32_t dw = d0[2] - d0[0], dh = d0[3] - d0[1];
+    const bool neg_w = dw < 0, neg_h = dh < 0;
+    dw = neg_w ? -dw : dw;
+    dh = neg_h ? -dh : dh;
+    for (int32_t y = 0; y < dh; y++) {
+        for (int32_t x = 0; x < dw; x++) {
+            const int32_t dst_x = neg_w ? x + d0[2] : x + d0[0];
+            const int32_t dst_y = neg_h ? y + d0[3] : y + d0[1];
+            if (dst_x < 0 || dst_y < 0 || dst_x >= static_cast<int32_t>(dst_w) || dst_y >= static_cast<int32_t>(dst_h)) continue;
+            const float u = (static_cast<float>(dst_x) + 0.5f - static_cast<float>(d0[0])) *
+                                (static_cast<float>(r0[2] - r0[0]) / static_cast<float>(d0[2] - d0[0])) + static_cast<float>(r0[0]);
+            const float v = (static_cast<float>(dst_y) + 0.5f - static_cast<float>(d0[1])) *
+                                (static_cast<float>(r0[3] - r0[1]) / static_cast<float>(d0[3] - d0[1])) + static_cast<float>(r0[1]);
+            float value[4];
+            sample_level(tex, 0, u / static_cast<float>(src_w), v / static_cast<float>(src_h), filter, s, value);
+            uint8_t* texel = dst + (static_cast<uint64_t>(dst_y) * dst_w + dst_x) * 4u;
+            for (int c = 0; c < 4; c++) texel[(dst_format == 44 && c < 3) ? 2 - c : c] = static_cast<uint8_t>(encode_unorm(value[c], 255.0f));
+        }
+    }
 }
 
 } // extern "C"

@@ -54,6 +54,11 @@ float cpv_oracle_decode_unorm8(uint8_t value);
  * reference sampler semantics; out = RGBA float. */
 void cpv_oracle_sample(const uint8_t* texels, uint32_t width, uint32_t height, uint32_t levels,
                        const cpv_scene_sampler* sampler, float u, float v, float lod, float out[4]);
+/* vkCmdBlitImage of one 2D colour region between RGBA8 (37) / BGRA8 (44)
+ * images: region = src x0, y0, x1, y1, dst x0, y0, x1, y1; filter 0 NEAREST,
+ * 1 LINEAR; dst is updated in place. */
+void cpv_oracle_blit(const uint8_t* src, uint32_t src_w, uint32_t src_h, uint32_t src_format, uint8_t* dst, uint32_t dst_w, uint32_t dst_h,
+                     uint32_t dst_format, const int32_t region[8], uint32_t filter);
 /* Blend one colour against a destination with the reference blend equations. */
 void cpv_oracle_blend(const float src[4], const float dst[4], const float constant[4],
                       uint32_t src_color, uint32_t dst_color, uint32_t color_op,

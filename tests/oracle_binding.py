@@ -38,6 +38,15 @@ class Oracle:
         lib.cpv_oracle_decode_unorm8.argtypes = [ctypes.c_uint8]
         lib.cpv_oracle_sample.argtypes = [vp, u32, u32, u32, ctypes.POINTER(SamplerDesc), f, f, f, ctypes.POINTER(f * 4)]
         lib.cpv_oracle_blend.argtypes = [ctypes.POINTER(f * 4)] * 3 + [u32] * 6 + [ctypes.POINTER(f * 4)]
+        lib.cpv_oracle_blit.argtypes = [vp, u32, u32, u32, vp, u32, u32, u32, vp, u32]
+
+    def blit(self, src, src_format, dst, dst_format, region, filter):
+        """One blit region between single levels (HxWx4 uint8 arrays, dst
+        updated in place); region = (sx0, sy0, sx1, sy1, dx0, dy0, dx1, dy1)."""
+        assert src.flags.c_contiguous and dst.flags.c_contiguous
+        reg = np.ascontiguousarray(np.asarray(region, dtype=np.int32))
+        self.lib.cpv_oracle_blit(src.ctypes.data, src.shape[1], src.shape[0], src_format, dst.ctypes.data, dst.shape[1],
+                                 dst.shape[0], dst_format, reg.ctypes.data, filter)
 
     def render(self, scene, draw_begin=0, draw_end=None, color=None, depth=None, clear=True):
         """Renders a cpvulkan_gb300.Scene; returns (color HxWx4 u8, depth HxWxB u8 or None, stats dict)."""

@@ -91,3 +91,19 @@ def test_batched_program_variants(gpu_ctx, plain, monkeypatch):
         scene = c.Scene(c.PROGRAM, 2, [program, variant, 64, 48, 24])
         ref = plain(gpu_ctx, scene)[0]
         same(frames(gpu_ctx, scene)[0], ref)
+
+
+@pytest.mark.parametrize("seed", [6, 7])
+def test_tuned_batch_equals_plain(gpu_ctx, plain, monkeypatch, seed):
+    """The tuner runs the pass once per candidate (tile 8/16/32, warps per
+    tile) on its first submission, restoring the attachments around each
+    run: the frames must still equal the per-draw path's, and the report
+    must name every candidate and the choice."""
+    monkeypatch.setenv("CPV_AUTOTUNE", "1")
+    scene = c.Scene(c.BATCH, seed, [32, 3000, 352, 208])
+    ref = plain(gpu_ctx, scene)[0]
+    runs = frames(gpu_ctx, scene, 3)
+    report = c.batch_tuning()
+    assert report.count(" ms") == 5 and "chosen tile" in report, report
+    for got in runs:
+        same(got, ref)
