@@ -428,7 +428,7 @@ bool build_pipelines(cpvh_context* c, const cpv_scene* s, VkRenderPass pass, VkP
         rs.polygonMode = VK_POLYGON_MODE_FILL;
         rs.cullMode = sp.cull_mode;
         rs.frontFace = static_cast<VkFrontFace>(sp.front_face);
-        rs.lineWidth = 1.0f;
+        rs.lineWidth = sp.line_width;
         VkPipelineMultisampleStateCreateInfo ms{};
         ms.sType = VK_STRUCTURE_TYPE_PIPELINE_MULTISAMPLE_STATE_CREATE_INFO;
         ms.rasterizationSamples = VK_SAMPLE_COUNT_1_BIT;

@@ -169,6 +169,7 @@ cpv_scene_pipeline base_pipeline(uint32_t program) {
     p.stencil_front.write_mask = p.stencil_back.write_mask = 0xFF;
     p.src_color = p.src_alpha = VK_BLEND_FACTOR_ONE;
     p.dst_color = p.dst_alpha = VK_BLEND_FACTOR_ZERO;
+    p.line_width = 1.0f;
     return p;
 }
 
@@ -609,7 +610,9 @@ void build_serve(Store& st, uint64_t seed, uint32_t side, uint32_t tris, uint32_
 // variant. variant bits: 0-1 cull mode, 2 front CW, 3-4 depth format
 // (0 none, 1 D16, 2 D32, 3 D32S8), 5 blend, 6-7 depth op (LESS, LEQUAL,
 // GREATER, ALWAYS), 8 stencil test, 9 BGRA target, 10-11 topology
-// (list, strip, fan), 12 uint16 indices, 13 depth write off.
+// (list, strip, fan; with bit 16: points, lines, line strip), 12 uint16
+// indices, 13 depth write off, 16 point/line topologies (line width 1 + 2.5
+// × bit 17).
 void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant, uint32_t width, uint32_t height, uint32_t tris) {
     cpv_scene& s = st.scene;
     s.width = width;
@@ -645,10 +648,14 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
     }
     const uint32_t topo_sel = (variant >> 10) & 3;
     p.topology = topo_sel == 1 ? VK_PRIMITIVE_TOPOLOGY_TRIANGLE_STRIP : (topo_sel == 2 ? VK_PRIMITIVE_TOPOLOGY_TRIANGLE_FAN : VK_PRIMITIVE_TOPOLOGY_TRIANGLE_LIST);
+    if (variant & 0x10000) {
+        p.topology = topo_sel == 1 ? VK_PRIMITIVE_TOPOLOGY_LINE_LIST : (topo_sel == 2 ? VK_PRIMITIVE_TOPOLOGY_LINE_STRIP : VK_PRIMITIVE_TOPOLOGY_POINT_LIST);
+        p.line_width = (variant & 0x20000) ? 3.5f : 1.0f;
+    }
     const bool u16 = (variant & 0x1000) != 0;
 
     uint32_t vcount = 0;
-    if (program == CPV_PROGRAM_CUBE || program == CPV_PROGRAM_DISCARD || program == CPV_PROGRAM_NOPERSP) {
+    if (program == CPV_PROGRAM_CUBE || program == CPV_PROGRAM_DISCARD || program == CPV_PROGRAM_NOPERSP || program == CPV_PROGRAM_POINTS) {
         // Clip-space vertices with w in [0.5, 2] (positive, as the reference
         // requires), a shared-edge pair, and a zero-area triangle.
         st.uniform.resize(64);
@@ -720,6 +727,7 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
         t.depth_write = p.depth_write;
         t.depth_compare = p.depth_compare;
         t.topology = p.topology;
+        t.line_width = p.line_width;
         t.blend_enable = p.blend_enable;
         t.src_color = p.src_color; t.dst_color = p.dst_color; t.color_op = p.color_op;
         t.src_alpha = p.src_alpha; t.dst_alpha = p.dst_alpha; t.alpha_op = p.alpha_op;
@@ -834,7 +842,14 @@ uint64_t cpvh_scene_triangles(const cpv_scene* s) {
     for (uint32_t i = 0; i < s->num_draws; i++) {
         const auto& d = s->draws[i];
         const auto& p = s->pipelines[d.pipeline];
-        const uint64_t per = p.topology == VK_PRIMITIVE_TOPOLOGY_TRIANGLE_LIST ? d.count / 3 : (d.count > 2 ? d.count - 2 : 0);
+        uint64_t per;
+        switch (p.topology) {
+        case VK_PRIMITIVE_TOPOLOGY_POINT_LIST: per = d.count; break;
+        case VK_PRIMITIVE_TOPOLOGY_LINE_LIST: per = d.count / 2; break;
+        case VK_PRIMITIVE_TOPOLOGY_LINE_STRIP: per = d.count > 1 ? d.count - 1 : 0; break;
+        case VK_PRIMITIVE_TOPOLOGY_TRIANGLE_LIST: per = d.count / 3; break;
+        default: per = d.count > 2 ? d.count - 2 : 0; break;
+        }
         total += per * d.instance_count;
     }
     return total;

@@ -28,6 +28,18 @@ uint32_t encode_unorm_host(float x, float maxv) {
 
 namespace {
 
+// Primitives of one instance of `count` assembled vertices
+// (CPVulkan/CommandBuffer.Draw.cpp:567-673).
+uint32_t primitives_per_instance(VkPrimitiveTopology topology, uint32_t count) {
+    switch (topology) {
+    case VK_PRIMITIVE_TOPOLOGY_POINT_LIST: return count;
+    case VK_PRIMITIVE_TOPOLOGY_LINE_LIST: return count / 2;
+    case VK_PRIMITIVE_TOPOLOGY_LINE_STRIP: return count > 1 ? count - 1 : 0;
+    case VK_PRIMITIVE_TOPOLOGY_TRIANGLE_LIST: return count / 3;
+    default: return count > 2 ? count - 2 : 0;  // strips and fans
+    }
+}
+
 struct BoundVertex {
     Buffer* buffer = nullptr;
     VkDeviceSize offset = 0;
@@ -176,9 +188,7 @@ VkResult build_draw(State& s, uint32_t count, uint32_t instances, uint32_t first
     P.vertex_offset = vertex_offset;
     P.first_instance = first_instance;
     P.instance_count = instances;
-    uint32_t ppi = 0;
-    if (p->topology == VK_PRIMITIVE_TOPOLOGY_TRIANGLE_LIST) ppi = count / 3;
-    else ppi = count > 2 ? count - 2 : 0;
+    const uint32_t ppi = primitives_per_instance(p->topology, count);
     P.prims_per_instance = ppi;
     P.total_prims = static_cast<uint64_t>(ppi) * instances;
     if (P.total_prims == 0) return VK_SUCCESS;
@@ -805,7 +815,7 @@ VkResult check_no_alloc(CommandBuffer* cb) {
         case CmdType::DrawIndexed: {
             if (!pipeline || !pass || !fb || pass->colour.empty()) break;  // execute() reports these
             const uint32_t count = c.u[0], instances = c.u[1];
-            const uint32_t ppi = pipeline->topology == VK_PRIMITIVE_TOPOLOGY_TRIANGLE_LIST ? count / 3 : (count > 2 ? count - 2 : 0);
+            const uint32_t ppi = primitives_per_instance(pipeline->topology, count);
             if (pass->colour[0] >= fb->attachments.size()) break;
             const ImageView* cv = fb->attachments[pass->colour[0]];
             uint32_t w = 0, h = 0;

@@ -11,6 +11,7 @@
 // reference's abort.
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
 #include <sstream>
 
@@ -56,7 +57,7 @@ const char* const kStageMacros[] = {
     "CPV_ST_F_FAIL", "CPV_ST_F_PASS", "CPV_ST_F_DFAIL", "CPV_ST_F_OP", "CPV_ST_F_CMASK", "CPV_ST_F_WMASK", "CPV_ST_F_REF",
     "CPV_ST_B_FAIL", "CPV_ST_B_PASS", "CPV_ST_B_DFAIL", "CPV_ST_B_OP", "CPV_ST_B_CMASK", "CPV_ST_B_WMASK", "CPV_ST_B_REF",
     "CPV_BLEND", "CPV_SRC_COLOR", "CPV_DST_COLOR", "CPV_COLOR_OP", "CPV_SRC_ALPHA", "CPV_DST_ALPHA", "CPV_ALPHA_OP", "CPV_WRITE_MASK",
-    "CPV_COLOR_FORMAT", "CPV_DEPTH_FORMAT", "CPV_ORIGIN_UPPER", "CPV_FS_CONSTANT", "CPV_BLEND_TABLE",
+    "CPV_COLOR_FORMAT", "CPV_DEPTH_FORMAT", "CPV_ORIGIN_UPPER", "CPV_FS_CONSTANT", "CPV_BLEND_TABLE", "CPV_LINE_WIDTH", "CPV_PRIM_KIND",
 };
 
 }  // namespace
@@ -106,6 +107,10 @@ std::string compose_module(const std::vector<std::string>& stages, const std::ve
     bool any_constant = false;
     for (const std::string& st : stages) any_constant = any_constant || st.find("#define CPV_FS_CONSTANT 1\n") != std::string::npos;
     src << "#define CPV_ANY_FS_CONSTANT " << (any_constant ? 1 : 0) << "\n";
+    bool any_lines = false;
+    for (const std::string& st : stages)
+        any_lines = any_lines || st.find("#define CPV_TOPOLOGY 1\n") != std::string::npos || st.find("#define CPV_TOPOLOGY 2\n") != std::string::npos;
+    src << "#define CPV_ANY_LINES " << (any_lines ? 1 : 0) << "\n";
     src << "#include \"cpv_device.cuh\"\n#include \"cpv_raster.cuh\"\n";
     for (size_t i = 0; i < stages.size(); i++) {
         src << "namespace cpv_p" << i << " {\n" << stages[i] << "#include \"cpv_stage.cuh\"\n";
@@ -250,8 +255,7 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     if (!vs || !fs) return reject("a vertex and a fragment stage are required");
     if (!ci.pInputAssemblyState || !ci.pRasterizationState || !ci.pVertexInputState) return reject("missing fixed-function state");
     const auto topo = ci.pInputAssemblyState->topology;
-    if (topo != VK_PRIMITIVE_TOPOLOGY_TRIANGLE_LIST && topo != VK_PRIMITIVE_TOPOLOGY_TRIANGLE_STRIP && topo != VK_PRIMITIVE_TOPOLOGY_TRIANGLE_FAN)
-        return reject("only triangle topologies are implemented");
+    if (topo > VK_PRIMITIVE_TOPOLOGY_TRIANGLE_FAN) return reject("topologies with adjacency and patch lists are not implemented");
     if (ci.pInputAssemblyState->primitiveRestartEnable) return reject("primitive restart");
     const auto& rs = *ci.pRasterizationState;
     if (rs.rasterizerDiscardEnable) return reject("rasterizer discard");
@@ -336,6 +340,13 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     src << "#define CPV_NV " << nv << "\n";
     src << "#define CPV_TOPOLOGY " << static_cast<uint32_t>(topo) << "\n";
     src << "#define CPV_CULL_MODE " << rs.cullMode << "\n";
+    {
+        // The pipeline's (static) line width, bit-exact; the reference reads
+        // it from the pipeline even when the width is dynamic state.
+        uint32_t bits;
+        std::memcpy(&bits, &rs.lineWidth, 4);
+        src << "#define CPV_LINE_WIDTH __uint_as_float(" << bits << "u)\n";
+    }
     src << "#define CPV_FRONT_CW " << (rs.frontFace == VK_FRONT_FACE_CLOCKWISE ? 1 : 0) << "\n";
     src << "#define CPV_DEPTH_TEST " << (ds.depthTestEnable ? 1 : 0) << "\n";
     src << "#define CPV_DEPTH_WRITE " << (ds.depthWriteEnable ? 1 : 0) << "\n";

@@ -374,9 +374,15 @@ __device__ __forceinline__ cvec<float, 4> cpv_sample(const CpvTexture& t, float 
 
 /* Assembled-vertex slots of primitive p for the topology
  * (CPVulkan/CommandBuffer.Draw.cpp:567-673): returns raw ids v[3] and the
- * provoking raw id. */
+ * provoking raw id. Points use v[0], lines v[0..1]. */
 __device__ __forceinline__ void cpv_prim_vertices(uint32_t topology, uint32_t p, uint32_t v[3], uint32_t& provoking) {
-    if (topology == 4u) { /* strip */
+    if (topology == 0u) { /* point list */
+        v[0] = v[1] = v[2] = p; provoking = p;
+    } else if (topology == 1u) { /* line list */
+        v[0] = 2u * p; v[1] = 2u * p + 1u; v[2] = v[1]; provoking = 2u * p;
+    } else if (topology == 2u) { /* line strip */
+        v[0] = p; v[1] = p + 1u; v[2] = v[1]; provoking = p;
+    } else if (topology == 4u) { /* strip */
         v[0] = p; v[1] = p + 1u; v[2] = p + 2u; provoking = p;
     } else if (topology == 5u) { /* fan */
         v[0] = 0u; v[1] = p + 1u; v[2] = p + 2u; provoking = p + 1u;

@@ -44,15 +44,29 @@
 #define CPV_PPT ((CPV_TILE * CPV_TILE) / CPV_RT_THREADS)
 #define CPV_ROWS_PER_PASS (CPV_RT_THREADS / CPV_TILE)
 #define CPV_WARP_ROWS (32 / CPV_TILE > 0 ? 32 / CPV_TILE : 1) /* tile rows one warp covers per pass */
+#ifndef CPV_ANY_LINES
+#define CPV_ANY_LINES 0 /* some pipeline of the module draws lines */
+#endif
 #define CPV_NV_ALLOC (CPV_NV_MAX > 0 ? CPV_NV_MAX : 1)
-#define CPV_NV_ROOM (CPV_ANY_FS_CONSTANT && CPV_NV_ALLOC < 4 ? 4 : CPV_NV_ALLOC)
+#define CPV_NV_ROOM0 (CPV_ANY_FS_CONSTANT && CPV_NV_ALLOC < 4 ? 4 : CPV_NV_ALLOC)
+#define CPV_NV_ROOM (CPV_ANY_LINES && CPV_NV_ROOM0 < 7 ? 7 : CPV_NV_ROOM0)
 #define CPV_NV_PAD ((CPV_NV_ROOM + 3) & ~3)
 #define CPV_SLOTS 4
 #define CPV_NSLOT (CPV_RT_THREADS * CPV_SLOTS)
 
 /* One primitive after set-up, in the reference's terms
  * (CPVulkan/CommandBuffer.Draw.cpp:1510-1594, 874-954). 16-byte aligned
- * groups so that the coverage loop reads them with 128-bit loads. */
+ * groups so that the coverage loop reads them with 128-bit loads.
+ *
+ * Points and lines reuse the record (Draw.cpp:1315-1508):
+ *   point — box is exactly the set of pixels the reference covers and the
+ *           edges are zero (every pixel of the box passes); za.x = NDC z,
+ *           wf.x = clip w, var[0] = the vertex's outputs;
+ *   line  — e[0..2] and za are the four edges of the line's quad, wf.x/y
+ *           the two clip w, var[0..1] the vertices' outputs, var[2][0..6] =
+ *           p0.x, p0.y, (p1 - p0).x, (p1 - p0).y, |p1 - p0|², z0, z1; the
+ *           provoking slot field holds 3 (a line's provoking vertex is its
+ *           first). */
 struct __align__(16) CpvTri {
     float4 e[3];     /* edge k: start vertex (x, y) and b - a (dx, dy), NDC */
     int4 box;        /* pixel bounding box x0, y0, x1, y1 (end exclusive) */
@@ -64,8 +78,8 @@ struct __align__(16) CpvTri {
 };
 
 /* Flag word (wf.w bits): 1 live, 2 front facing, bits 2-5 pipeline index in
- * the module, bits 6-7 provoking-vertex slot, bits 8-31 draw index in the
- * batch (0 for a per-draw module). */
+ * the module, bits 6-7 provoking-vertex slot (3: a line), bits 8-31 draw
+ * index in the batch (0 for a per-draw module). */
 __device__ __forceinline__ uint32_t cpv_tri_flags(const CpvTri& t) { return __float_as_uint(t.wf.w); }
 __device__ __forceinline__ bool cpv_tri_live(const CpvTri& t) { return (cpv_tri_flags(t) & 1u) != 0u; }
 __device__ __forceinline__ bool cpv_tri_front(const CpvTri& t) { return (cpv_tri_flags(t) & 2u) != 0u; }
@@ -94,6 +108,15 @@ __device__ __forceinline__ bool cpv_covers(const CpvTri& t, float xf, float yf, 
         const float t1 = __fmul_rn(__fsub_rn(yf, e.y), e.z);
         w[k] = __fsub_rn(t0, t1);
     }
+#if CPV_ANY_LINES
+    /* a line's quad has a fourth edge (CPVulkan/CommandBuffer.Draw.cpp:1437):
+     * every edge must be >= 0, which also rejects NaN */
+    if (((__float_as_uint(t.wf.w) >> 6) & 3u) == 3u) {
+        const float4 e = t.za;
+        const float w3 = __fsub_rn(__fmul_rn(__fsub_rn(xf, e.x), e.w), __fmul_rn(__fsub_rn(yf, e.y), e.z));
+        return w[0] >= 0.0f && w[1] >= 0.0f && w[2] >= 0.0f && w3 >= 0.0f;
+    }
+#endif
     return !(w[0] < 0.0f || w[1] < 0.0f || w[2] < 0.0f);
 }
 

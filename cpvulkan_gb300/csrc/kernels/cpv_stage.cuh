@@ -20,6 +20,183 @@
  * traffic for a vertex-output buffer.
  */
 
+/* Primitive class of the pipeline's topology: 0 triangles, 1 lines (list,
+ * strip), 2 points. */
+#if CPV_TOPOLOGY == 0
+#define CPV_PRIM_KIND 2
+#elif CPV_TOPOLOGY == 1 || CPV_TOPOLOGY == 2
+#define CPV_PRIM_KIND 1
+#else
+#define CPV_PRIM_KIND 0
+#endif
+#ifndef CPV_LINE_WIDTH
+#define CPV_LINE_WIDTH 1.0f
+#endif
+
+/* The fragment shader of a primitive whose shader is constant over it
+ * (CPV_FS_CONSTANT): shaded once from the provoking vertex's outputs; the
+ * colour goes to var[0][0..3] (a discard kills the primitive) and, with
+ * blend tables, the primitive index to var[1][0]. */
+template <bool WITH_VARYINGS>
+__device__ __forceinline__ void cpv_shade_constant(const CpvDrawParams& P, const float* provoking, bool front, uint32_t g32, CpvTri& t, bool& live) {
+#if CPV_FS_CONSTANT
+    if (WITH_VARYINGS && live) {
+        float in[CPV_NV_ALLOC];
+#pragma unroll
+        for (int c = 0; c < CPV_NV_ALLOC; c++) in[c] = c < CPV_NV ? provoking[c] : 0.0f;
+        const float frag_coord[4] = {0.0f, 0.0f, 0.0f, 1.0f};  /* not read by this shader */
+        float colour[4];
+        if (cpv_fs_run(P, in, frag_coord, front, colour)) live = false;
+#pragma unroll
+        for (int c = 0; c < 4; c++) t.var[0][c] = colour[c];
+#if CPV_BLEND_TABLE
+        t.var[1][0] = __uint_as_float(g32);  /* the primitive's blend table */
+#endif
+    }
+#else
+    (void)P; (void)provoking; (void)front; (void)g32; (void)t; (void)live;
+#endif
+}
+
+#if CPV_PRIM_KIND == 2
+/* Point set-up (CPVulkan/CommandBuffer.Draw.cpp:1315-1380): screen position
+ * (int)((ndc + 1) * 0.5 * (extent - 1)), half size ceil(size / 2), and the
+ * pixels whose s = 0.5 + (x - sx) / size and t (likewise in y) lie in
+ * [0, 1]. s is monotonic in x, so those pixels form a rectangle, found by
+ * evaluating the reference's expression at the candidate range's ends; it
+ * becomes the box, and the zero edges cover every pixel in it. */
+template <bool WITH_VARYINGS>
+__device__ __forceinline__ void cpv_setup(const CpvDrawParams& P, uint64_t g, CpvTri& t) {
+    const uint32_t ppi = P.prims_per_instance;
+    const uint32_t g32 = static_cast<uint32_t>(g);
+    const uint32_t inst = P.instance_count > 1u ? g32 / ppi : 0u;
+    const uint32_t p = g32 - inst * ppi;
+    float pos[4], var[CPV_NV_ALLOC], size = 1.0f;
+    cpv_vs_run(P, cpv_vertex_id(P, p), P.first_instance + inst, pos, var, &size);
+    const float w = pos[3];
+    const float nx = __fdiv_rn(pos[0], w), ny = __fdiv_rn(pos[1], w), nz = __fdiv_rn(pos[2], w);
+    const float vw = P.viewport[2], vh = P.viewport[3];
+    const int64_t sx = cpv_f2i(__fmul_rn(__fmul_rn(__fadd_rn(nx, 1.0f), 0.5f), __fsub_rn(vw, 1.0f)));
+    const int64_t sy = cpv_f2i(__fmul_rn(__fmul_rn(__fadd_rn(ny, 1.0f), 0.5f), __fsub_rn(vh, 1.0f)));
+    const int64_t half = cpv_f2i(ceilf(__fdiv_rn(size, 2.0f)));
+    int64_t xe = min(static_cast<int64_t>(cpv_f2i(vw)), sx + half + 1), ye = min(static_cast<int64_t>(cpv_f2i(vh)), sy + half + 1);
+    xe = min(xe, static_cast<int64_t>(P.fb_width));
+    ye = min(ye, static_cast<int64_t>(P.fb_height));
+    int64_t xb = max(static_cast<int64_t>(0), sx - half), yb = max(static_cast<int64_t>(0), sy - half);
+    auto inside = [&](int64_t d) {
+        const float s = __fadd_rn(0.5f, __fdiv_rn(static_cast<float>(static_cast<int32_t>(d)), size));
+        return s >= 0.0f && s <= 1.0f;
+    };
+    /* the reference's loops cover at most a size-wide square plus one
+     * pixel: shrink each end to its first covered pixel */
+    while (xb < xe && !inside(xb - sx)) xb++;
+    while (xe > xb && !inside(xe - 1 - sx)) xe--;
+    while (yb < ye && !inside(yb - sy)) yb++;
+    while (ye > yb && !inside(ye - 1 - sy)) ye--;
+    bool live = xe > xb && ye > yb && size == size;
+    t.box = make_int4(static_cast<int32_t>(xb), static_cast<int32_t>(yb), static_cast<int32_t>(live ? xe : xb), static_cast<int32_t>(live ? ye : yb));
+#pragma unroll
+    for (int k = 0; k < 3; k++) t.e[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    t.za = make_float4(nz, 0.0f, 0.0f, 1.0f);
+    if (WITH_VARYINGS) {
+#pragma unroll
+        for (int c = 0; c < CPV_NV; c++) t.var[0][c] = var[c];
+    }
+    cpv_shade_constant<WITH_VARYINGS>(P, var, true, g32, t, live);
+    t.wf = make_float4(w, w, w, __uint_as_float((live ? 1u : 0u) | 2u));
+}
+#elif CPV_PRIM_KIND == 1
+/* Line set-up (CPVulkan/CommandBuffer.Draw.cpp:1382-1449): the quad around
+ * p0 → p1 offset by ±(dir.y, -dir.x) * lineWidth / extent, dir the
+ * normalised 4-component difference of the two (NDC xyz, clip w) points;
+ * its four edges; a box around the quad's corners with a two-pixel margin
+ * (the edge tests decide coverage; the reference tests every viewport
+ * pixel, and pixels that far outside the quad fail an edge). */
+template <bool WITH_VARYINGS>
+__device__ __forceinline__ void cpv_setup(const CpvDrawParams& P, uint64_t g, CpvTri& t) {
+    static_assert(CPV_ANY_LINES && CPV_NV_PAD >= 7, "a module with line pipelines defines CPV_ANY_LINES");
+    const uint32_t ppi = P.prims_per_instance;
+    const uint32_t g32 = static_cast<uint32_t>(g);
+    const uint32_t inst = P.instance_count > 1u ? g32 / ppi : 0u;
+    const uint32_t instance = P.first_instance + inst;
+    const uint32_t p = g32 - inst * ppi;
+    uint32_t raw[3], provoking;
+    cpv_prim_vertices(CPV_TOPOLOGY, p, raw, provoking);
+    (void)provoking;
+    float Pn[2][4];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        float pos[4];
+        float var[CPV_NV_ALLOC];
+        cpv_vs_run(P, cpv_vertex_id(P, raw[k]), instance, pos, var);
+        const float w = pos[3];
+        Pn[k][0] = __fdiv_rn(pos[0], w);
+        Pn[k][1] = __fdiv_rn(pos[1], w);
+        Pn[k][2] = __fdiv_rn(pos[2], w);
+        Pn[k][3] = w;
+        if (WITH_VARYINGS) {
+#pragma unroll
+            for (int c = 0; c < CPV_NV; c++) t.var[k][c] = var[c];
+        }
+    }
+    const float vw = P.viewport[2], vh = P.viewport[3];
+    const float lwx = __fdiv_rn(CPV_LINE_WIDTH, vw), lwy = __fdiv_rn(CPV_LINE_WIDTH, vh);
+    /* glm::normalize: v * (1 / sqrt(dot(v, v))), dot4 = (x + y) + (z + w) */
+    float dv[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) dv[i] = __fsub_rn(Pn[1][i], Pn[0][i]);
+    const float dot = __fadd_rn(__fadd_rn(__fmul_rn(dv[0], dv[0]), __fmul_rn(dv[1], dv[1])),
+                                __fadd_rn(__fmul_rn(dv[2], dv[2]), __fmul_rn(dv[3], dv[3])));
+    const float inv = __fdiv_rn(1.0f, __fsqrt_rn(dot));
+    const float dir_x = __fmul_rn(dv[0], inv), dir_y = __fmul_rn(dv[1], inv);
+    const float ox = __fmul_rn(dir_y, lwx), oy = __fmul_rn(-dir_x, lwy);
+    const float c00x = __fadd_rn(Pn[0][0], ox), c00y = __fadd_rn(Pn[0][1], oy);
+    const float c01x = __fsub_rn(Pn[0][0], ox), c01y = __fsub_rn(Pn[0][1], oy);
+    const float c10x = __fadd_rn(Pn[1][0], ox), c10y = __fadd_rn(Pn[1][1], oy);
+    const float c11x = __fsub_rn(Pn[1][0], ox), c11y = __fsub_rn(Pn[1][1], oy);
+    /* edges (a, b): (p00, p01), (p11, p10), (p10, p00), (p01, p11) */
+    t.e[0] = make_float4(c00x, c00y, __fsub_rn(c01x, c00x), __fsub_rn(c01y, c00y));
+    t.e[1] = make_float4(c11x, c11y, __fsub_rn(c10x, c11x), __fsub_rn(c10y, c11y));
+    t.e[2] = make_float4(c10x, c10y, __fsub_rn(c00x, c10x), __fsub_rn(c00y, c10y));
+    t.za = make_float4(c01x, c01y, __fsub_rn(c11x, c01x), __fsub_rn(c11y, c01y));
+    const float cx[4] = {c00x, c01x, c10x, c11x}, cy[4] = {c00y, c01y, c10y, c11y};
+    bool nan = false, finite = true;
+    float minx = cx[0], maxx = cx[0], miny = cy[0], maxy = cy[0];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        nan = nan || cx[i] != cx[i] || cy[i] != cy[i];
+        finite = finite && fabsf(cx[i]) <= 3.0e38f && fabsf(cy[i]) <= 3.0e38f;
+        minx = fminf(minx, cx[i]); maxx = fmaxf(maxx, cx[i]);
+        miny = fminf(miny, cy[i]); maxy = fmaxf(maxy, cy[i]);
+    }
+    /* the reference loops x < viewport.width (a float): ceil */
+    const int64_t iw = min(static_cast<int64_t>(cpv_f2i(ceilf(vw))), static_cast<int64_t>(P.fb_width));
+    const int64_t ih = min(static_cast<int64_t>(cpv_f2i(ceilf(vh))), static_cast<int64_t>(P.fb_height));
+    int64_t x0 = 0, y0 = 0, x1 = iw, y1 = ih;
+    if (finite) {
+        /* pixel x has its centre at NDC (2x + 1) / W - 1 */
+        auto lo = [](float v, float e) { return static_cast<int64_t>(floorf(fminf(fmaxf((v + 1.0f) * e * 0.5f - 0.5f, -4.0f), e + 4.0f))) - 2; };
+        auto hi = [](float v, float e) { return static_cast<int64_t>(ceilf(fminf(fmaxf((v + 1.0f) * e * 0.5f - 0.5f, -4.0f), e + 4.0f))) + 3; };
+        x0 = max(x0, lo(minx, vw));
+        y0 = max(y0, lo(miny, vh));
+        x1 = min(x1, hi(maxx, vw));
+        y1 = min(y1, hi(maxy, vh));
+    }
+    bool live = !nan && x1 > x0 && y1 > y0;
+    t.box = make_int4(static_cast<int32_t>(x0), static_cast<int32_t>(y0), static_cast<int32_t>(live ? x1 : x0), static_cast<int32_t>(live ? y1 : y0));
+    const float dx = __fsub_rn(Pn[1][0], Pn[0][0]), dy = __fsub_rn(Pn[1][1], Pn[0][1]);
+    const float len = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+    if (WITH_VARYINGS) cpv_shade_constant<WITH_VARYINGS>(P, t.var[0], true, g32, t, live);
+    t.var[2][0] = Pn[0][0];
+    t.var[2][1] = Pn[0][1];
+    t.var[2][2] = dx;
+    t.var[2][3] = dy;
+    t.var[2][4] = __fmul_rn(len, len);
+    t.var[2][5] = Pn[0][2];
+    t.var[2][6] = Pn[1][2];
+    t.wf = make_float4(Pn[0][3], Pn[1][3], 0.0f, __uint_as_float((live ? 1u : 0u) | 2u | (3u << 6)));
+}
+#else
 /* Primitive set-up: vertex shading of the three vertices, perspective divide,
  * screen bounding box, area, facing and cull. `g` is the primitive index
  * within the draw (all instances). */
@@ -96,27 +273,14 @@ __device__ __forceinline__ void cpv_setup(const CpvDrawParams& P, uint64_t g, Cp
     bool live = box.z > box.x && box.w > box.y;
     if ((CPV_CULL_MODE & 2) && !front) live = false;
     if ((CPV_CULL_MODE & 1) && front) live = false;
-#if CPV_FS_CONSTANT
-    /* The fragment shader reads only flat inputs (the provoking vertex's):
-     * every fragment of the primitive gets this colour, and a discard
-     * discards them all. */
-    if (WITH_VARYINGS && live) {
-        float in[CPV_NV_ALLOC];
-#pragma unroll
-        for (int c = 0; c < CPV_NV_ALLOC; c++) in[c] = c < CPV_NV ? t.var[pslot][c] : 0.0f;
-        const float frag_coord[4] = {0.0f, 0.0f, 0.0f, 1.0f};  /* not read by this shader */
-        float colour[4];
-        if (cpv_fs_run(P, in, frag_coord, front, colour)) live = false;
-#pragma unroll
-        for (int c = 0; c < 4; c++) t.var[0][c] = colour[c];
-#if CPV_BLEND_TABLE
-        t.var[1][0] = __uint_as_float(g32);  /* the primitive's blend table */
-#endif
-    }
-#endif
+    /* a fragment shader reading only flat inputs (the provoking vertex's)
+     * gives every fragment of the primitive one colour; a discard discards
+     * them all */
+    if (WITH_VARYINGS) cpv_shade_constant<WITH_VARYINGS>(P, t.var[pslot], front, g32, t, live);
     const uint32_t flags = (live ? 1u : 0u) | (front ? 2u : 0u) | (pslot << 6);
     t.wf = make_float4(Pn[0][3], Pn[1][3], Pn[2][3], __uint_as_float(flags));
 }
+#endif /* CPV_PRIM_KIND */
 
 /* Byte offset of channel i in the colour attachment texel
  * (CPVulkanBase/Formats.cpp:248,255). */
@@ -194,6 +358,43 @@ __device__ __forceinline__ void cpv_blend(const float s[4], const float d[4], co
  * shader discards. */
 __device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& t, const float wr[3], int32_t x, int32_t y, float colour[4],
                                           float& mapped) {
+    float in[CPV_NV_ALLOC];
+#if CPV_PRIM_KIND == 2
+    /* a point's fragments take its vertex's outputs as they are and its NDC z
+     * (CPVulkan/CommandBuffer.Draw.cpp:1364-1374) */
+    (void)wr;
+    const float depth = t.za.x;
+#pragma unroll
+    for (int c = 0; c < CPV_NV; c++) in[c] = t.var[0][c];
+#elif CPV_PRIM_KIND == 1
+    /* line parameter t = dot(p - p0, d) / (|d| |d|) at the pixel centre,
+     * weights (1 - t, t), depth p0.z * t + p1.z * (1 - t) as the reference
+     * writes it (CPVulkan/CommandBuffer.Draw.cpp:1441-1486) */
+    (void)wr;
+    const float xf = cpv_pixel_ndc(x, P.viewport[2]), yf = cpv_pixel_ndc(y, P.viewport[3]);
+    const float num = __fadd_rn(__fmul_rn(__fsub_rn(xf, t.var[2][0]), t.var[2][2]), __fmul_rn(__fsub_rn(yf, t.var[2][1]), t.var[2][3]));
+    const float lt = __fdiv_rn(num, t.var[2][4]);
+    const float w[2] = {__fsub_rn(1.0f, lt), lt};
+    const float depth = __fadd_rn(__fmul_rn(t.var[2][5], lt), __fmul_rn(t.var[2][6], w[0]));
+    const float pw[2] = {t.wf.x, t.wf.y};
+#pragma unroll
+    for (int c = 0; c < CPV_NV; c++) {
+        const int kind = cpv_interp(c);
+        if (kind == 2) {
+            in[c] = t.var[0][c];
+        } else if (kind == 1) {
+            in[c] = __fadd_rn(__fadd_rn(0.0f, __fmul_rn(w[0], t.var[0][c])), __fmul_rn(w[1], t.var[1][c]));
+        } else {
+            float n = 0.0f, d = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                n = __fadd_rn(n, __fdiv_rn(__fmul_rn(w[k], t.var[k][c]), pw[k]));
+                d = __fadd_rn(d, __fdiv_rn(w[k], pw[k]));
+            }
+            in[c] = __fdiv_rn(n, d);
+        }
+    }
+#else
     const float area = t.za.w;
     float w[3];
     w[0] = __fdiv_rn(wr[0], area);
@@ -202,7 +403,6 @@ __device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& 
     const float depth = __fadd_rn(__fadd_rn(__fmul_rn(t.za.x, w[0]), __fmul_rn(t.za.y, w[1])), __fmul_rn(t.za.z, w[2]));
     const float pw[3] = {t.wf.x, t.wf.y, t.wf.z};
     const uint32_t pslot = cpv_tri_pslot(t);
-    float in[CPV_NV_ALLOC];
 #pragma unroll
     for (int c = 0; c < CPV_NV; c++) {
         const int kind = cpv_interp(c);
@@ -223,6 +423,7 @@ __device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& 
             in[c] = __fdiv_rn(num, den);
         }
     }
+#endif /* CPV_PRIM_KIND */
     const float min_d = P.viewport[4], max_d = P.viewport[5];
     mapped = __fadd_rn(__fmul_rn(__fsub_rn(max_d, min_d), depth), min_d);
     float frag_coord[4];

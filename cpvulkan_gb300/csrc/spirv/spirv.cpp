@@ -832,12 +832,22 @@ bool Translator::emit_globals(const EntryPoint& ep, StageResult& out) {
                     if (is_builtin) {
                         if (builtin == BIPosition)
                             for (int i = 0; i < 4; i++) epi_ << "  cpv_pos[" << i << "] = " << var << ".v[" << i << "];\n";
+                        else if (builtin == BIPointSize) {
+                            // A shader that never writes gl_PointSize gives points of size 1.
+                            pro_ << "  " << var << " = 1.0f;\n";
+                            epi_ << "  if (cpv_point_size) *cpv_point_size = " << var << ";\n";
+                        }
                     } else if (type(tid)->kind == TypeKind::Struct && m_.has_decoration(tid, DecBlock)) {
                         const Type* st = type(tid);
                         for (size_t k = 0; k < st->members.size(); k++) {
                             uint32_t bi = 0;
-                            if (m_.member_decoration(tid, static_cast<uint32_t>(k), DecBuiltIn, bi) && bi == BIPosition)
+                            if (!m_.member_decoration(tid, static_cast<uint32_t>(k), DecBuiltIn, bi)) continue;
+                            if (bi == BIPosition)
                                 for (int i = 0; i < 4; i++) epi_ << "  cpv_pos[" << i << "] = " << var << ".m" << k << ".v[" << i << "];\n";
+                            else if (bi == BIPointSize) {
+                                pro_ << "  " << var << ".m" << k << " = 1.0f;\n";
+                                epi_ << "  if (cpv_point_size) *cpv_point_size = " << var << ".m" << k << ";\n";
+                            }
                         }
                     } else if (has_location) {
                         // PipelineCompiler.cpp:957-980: outputs stored in declaration order.
@@ -1366,7 +1376,7 @@ bool Translator::run(const std::string& entry_name, StageResult& out, std::strin
     s << "namespace " << ns << " {\n" << types_.str() << loaders_.str() << "}\n";
     if (model_ == 0) {
         s << "__device__ __forceinline__ void cpv_vs_run(const CpvDrawParams& P, uint32_t cpv_vertex_index, uint32_t cpv_instance_index, "
-             "float* cpv_pos, float* cpv_var) {\n";
+             "float* cpv_pos, float* cpv_var, float* cpv_point_size = nullptr) {\n";
         s << "  using namespace " << ns << ";\n";
         s << "  for (int i = 0; i < CPV_NV; i++) cpv_var[i] = 0.0f;\n";
         s << "  cpv_pos[0] = cpv_pos[1] = cpv_pos[2] = 0.0f; cpv_pos[3] = 1.0f;\n";

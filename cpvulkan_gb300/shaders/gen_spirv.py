@@ -221,6 +221,34 @@ def cube_vert():
     return m.assemble(body)
 
 
+def points_vert():
+    """cube_vert plus gl_PointSize = inColor.a * 16.0 (the gl_PerVertex member)."""
+    m = Module(0)
+    v4, mat, f = m.vec(4), m.mat4(), m.float()
+    ubo = m.ubo_block("UBO", [mat], [0], binding=0)
+    pos = m.variable("Input", v4, "pos")
+    m.decorate(pos, "Location", 0)
+    col = m.variable("Input", v4, "inColor")
+    m.decorate(col, "Location", 1)
+    out = m.variable("Output", v4, "outColor")
+    m.decorate(out, "Location", 0)
+    pv_t, pv = m.per_vertex_block()
+
+    def body(m):
+        c = m.load(v4, col)
+        m.store(out, c)
+        mp = m.access("Uniform", mat, ubo, m.const_int(0))
+        mv = m.load(mat, mp)
+        p = m.load(v4, pos)
+        r = m.op("MatrixTimesVector", v4, mv, p)
+        m.store(m.access("Output", v4, pv, m.const_int(0)), r)
+        a = m.op("CompositeExtract", f, c, 3)
+        size = m.op("FMul", f, a, m.const_f(16.0))
+        m.store(m.access("Output", f, pv, m.const_int(1)), size)
+        m.op_void("Return")
+    return m.assemble(body)
+
+
 def colour_frag(decoration=None, discard=False):
     """layout(location=0) [flat|noperspective] in vec4 color; layout(location=0) out vec4 o;
     void main() { [if (color.r > 0.5) discard;] o = color; }"""
@@ -390,6 +418,7 @@ PROGRAMS = {
     "meshpc": (meshpc_vert, meshpc_frag),
     "discard": (cube_vert, lambda: colour_frag(discard=True)),
     "nopersp": (cube_vert, lambda: colour_frag("NoPerspective")),
+    "points": (points_vert, colour_frag),
 }
 
 

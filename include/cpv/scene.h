@@ -32,7 +32,8 @@ enum cpv_program {
     CPV_PROGRAM_MESHPC = 3,      /* pos vec3 + normal vec3 + per-instance offset vec4 → push {MVP, colour}; Lambert */
     CPV_PROGRAM_DISCARD = 4,     /* CUBE with a fragment discard when colour.r > 0.5 (OpKill coverage)          */
     CPV_PROGRAM_NOPERSP = 5,     /* CUBE with noperspective colour (InterpolationType::Linear coverage)         */
-    CPV_PROGRAM_COUNT = 6
+    CPV_PROGRAM_POINTS = 6,      /* CUBE that also writes gl_PointSize = colour.a * 16                          */
+    CPV_PROGRAM_COUNT = 7
 };
 
 #define CPV_SCENE_MAX_BINDINGS 4
@@ -59,7 +60,7 @@ typedef struct cpv_scene_stencil {
 
 typedef struct cpv_scene_pipeline {
     uint32_t program;    /* cpv_program */
-    uint32_t topology;   /* VkPrimitiveTopology (triangle list / strip / fan) */
+    uint32_t topology;   /* VkPrimitiveTopology (point list, line list / strip, triangle list / strip / fan) */
     uint32_t cull_mode;  /* VkCullModeFlags */
     uint32_t front_face; /* VkFrontFace */
     uint32_t depth_test, depth_write, depth_compare;
@@ -73,6 +74,7 @@ typedef struct cpv_scene_pipeline {
     cpv_scene_binding bindings[CPV_SCENE_MAX_BINDINGS];
     uint32_t num_attributes;
     cpv_scene_attribute attributes[CPV_SCENE_MAX_ATTRIBUTES];
+    float line_width;    /* VkPipelineRasterizationStateCreateInfo::lineWidth */
 } cpv_scene_pipeline;
 
 typedef struct cpv_scene_draw {

@@ -33,7 +33,7 @@ enum : uint32_t {
     FMT_D32_SFLOAT_S8_UINT = 130,
 };
 
-enum : uint32_t { TOPO_TRIANGLE_LIST = 3, TOPO_TRIANGLE_STRIP = 4, TOPO_TRIANGLE_FAN = 5 };
+enum : uint32_t { TOPO_POINT_LIST = 0, TOPO_LINE_LIST = 1, TOPO_LINE_STRIP = 2, TOPO_TRIANGLE_LIST = 3, TOPO_TRIANGLE_STRIP = 4, TOPO_TRIANGLE_FAN = 5 };
 enum : uint32_t { CULL_FRONT = 1, CULL_BACK = 2 };
 enum : uint32_t { FRONT_FACE_CW = 1 };
 enum : uint32_t { RATE_VERTEX = 0, RATE_INSTANCE = 1 };
@@ -355,6 +355,7 @@ ProgramInfo program_info(uint32_t program) {
     case CPV_PROGRAM_MESHPC: return {1, {3}, {INTERP_PERSPECTIVE}};
     case CPV_PROGRAM_DISCARD: return {1, {4}, {INTERP_PERSPECTIVE}};
     case CPV_PROGRAM_NOPERSP: return {1, {4}, {INTERP_LINEAR}};
+    case CPV_PROGRAM_POINTS: return {1, {4}, {INTERP_PERSPECTIVE}};
     default: return {0, {0}, {INTERP_PERSPECTIVE}};
     }
 }
@@ -372,20 +373,24 @@ float ubo_at(const Resources& r, uint32_t i) { return i < r.ubo_floats ? r.ubo[i
 struct VsOut {
     float pos[4];
     float var[kMaxVaryings];
+    float point_size; /* gl_PointSize (1 when the shader does not write it) */
 };
 
 /* attr[location][4] holds each attribute as fetched (missing components
  * default to 0,0,0,1). */
 void run_vs(uint32_t program, const float attr[8][4], const Resources& r, VsOut& out) {
+    out.point_size = 1.0f;
     switch (program) {
     case CPV_PROGRAM_CUBE:
     case CPV_PROGRAM_DISCARD:
-    case CPV_PROGRAM_NOPERSP: {
+    case CPV_PROGRAM_NOPERSP:
+    case CPV_PROGRAM_POINTS: {
         float m[16];
         for (int i = 0; i < 16; i++) m[i] = ubo_at(r, i);
         for (int i = 0; i < 4; i++) out.var[i] = attr[1][i];
         const V4 p = mat4_mul_vec4(m, attr[0]);
         out.pos[0] = p.x; out.pos[1] = p.y; out.pos[2] = p.z; out.pos[3] = p.w;
+        if (program == CPV_PROGRAM_POINTS) out.point_size = attr[1][3] * 16.0f;
         break;
     }
     case CPV_PROGRAM_TEXLIT: {
@@ -424,6 +429,7 @@ bool run_fs(uint32_t program, const float* in, const Resources& r, float colour[
     case CPV_PROGRAM_CUBE:
     case CPV_PROGRAM_NOPERSP:
     case CPV_PROGRAM_FLATQUAD:
+    case CPV_PROGRAM_POINTS:
         for (int i = 0; i < 4; i++) colour[i] = in[i];
         return false;
     case CPV_PROGRAM_DISCARD:
@@ -624,7 +630,13 @@ void assemble(const Frame& f, const cpv_scene_pipeline& p, const cpv_scene_draw&
         for (uint32_t i = 0; i < n; i++) out.vertex_id[i] = d.first + i;
     }
     out.prims.clear();
-    if (p.topology == TOPO_TRIANGLE_LIST) {
+    if (p.topology == TOPO_POINT_LIST) {
+        for (uint32_t i = 0; i < n; i++) { out.prims.push_back(i); out.prims.push_back(i); out.prims.push_back(i); out.prims.push_back(i); }
+    } else if (p.topology == TOPO_LINE_LIST) {
+        for (uint32_t i = 0; i < n / 2; i++) { out.prims.push_back(i * 2); out.prims.push_back(i * 2); out.prims.push_back(i * 2 + 1); out.prims.push_back(i * 2 + 1); }
+    } else if (p.topology == TOPO_LINE_STRIP) {
+        for (uint32_t i = 0; i + 1 < n; i++) { out.prims.push_back(i); out.prims.push_back(i); out.prims.push_back(i + 1); out.prims.push_back(i + 1); }
+    } else if (p.topology == TOPO_TRIANGLE_LIST) {
         for (uint32_t i = 0; i < n / 3; i++) { out.prims.push_back(i * 3); out.prims.push_back(i * 3); out.prims.push_back(i * 3 + 1); out.prims.push_back(i * 3 + 2); }
     } else if (p.topology == TOPO_TRIANGLE_STRIP) {
         for (uint32_t i = 0; i + 2 < n; i++) { out.prims.push_back(i); out.prims.push_back(i); out.prims.push_back(i + 1); out.prims.push_back(i + 2); }
@@ -799,6 +811,118 @@ void rasterise(Frame& f, const cpv_scene_pipeline& p, const Assembled& as, const
     }
 }
 
+/* ProcessPoints (CPVulkan/CommandBuffer.Draw.cpp:1315-1380): the point's
+ * screen position (int)((ndc + 1) * 0.5 * (extent - 1)), a square of
+ * ceil(size / 2) around it, and the pixels whose s = 0.5 + (x - sx) / size
+ * and t (likewise) lie in [0, 1]; every fragment takes the vertex's outputs
+ * unchanged and its NDC z, facing front. */
+void rasterise_points(Frame& f, const cpv_scene_pipeline& p, const Assembled& as, const std::vector<VsOut>& vs) {
+    const cpv_scene* s = f.s;
+    const float vw = s->viewport[2], vh = s->viewport[3];
+    const float min_d = s->viewport[4], max_d = s->viewport[5];
+    for (size_t t = 0; t + 4 <= as.prims.size(); t += 4) {
+        const VsOut& v = vs[as.prims[t + 1]];
+        f.stats->triangles++;
+        const float w = v.pos[3];
+        const float p0[3] = {v.pos[0] / w, v.pos[1] / w, v.pos[2] / w};
+        const int64_t sx = f2i(((p0[0] + 1.0f) * 0.5f) * (vw - 1.0f));
+        const int64_t sy = f2i(((p0[1] + 1.0f) * 0.5f) * (vh - 1.0f));
+        const float size = v.point_size;
+        const int64_t half = f2i(std::ceil(size / 2.0f));
+        const int64_t start_x = std::max<int64_t>(0, sx - half), start_y = std::max<int64_t>(0, sy - half);
+        int64_t end_x = std::min<int64_t>(f2i(vw), sx + half + 1), end_y = std::min<int64_t>(f2i(vh), sy + half + 1);
+        end_x = std::min<int64_t>(end_x, s->width);
+        end_y = std::min<int64_t>(end_y, s->height);
+        for (int64_t y = start_y; y < end_y; y++) {
+            for (int64_t x = start_x; x < end_x; x++) {
+                const float ps = 0.5f + static_cast<float>(static_cast<int32_t>(x - sx)) / size;
+                const float pt = 0.5f + static_cast<float>(static_cast<int32_t>(y - sy)) / size;
+                if (!(ps >= 0 && pt >= 0 && ps <= 1 && pt <= 1)) continue;
+                const float mapped = (max_d - min_d) * p0[2] + min_d;
+                fragment(f, p, static_cast<uint32_t>(x), static_cast<uint32_t>(y), mapped, true, v.var);
+            }
+        }
+    }
+}
+
+/* ProcessLines, rectangular mode (CPVulkan/CommandBuffer.Draw.cpp:1382-1508):
+ * the quad p0 ± o, p1 ± o with o = (dir.y, -dir.x) * lineWidth / extent and
+ * dir = normalize(p1 - p0) over (NDC x, y, z, clip w); every viewport pixel
+ * centre inside all four edges is a fragment, its line parameter
+ * t = dot(p - p0, p1 - p0) / (|p1 - p0| |p1 - p0|) weighting the two
+ * vertices (1 - t, t) and its depth p0.z * t + p1.z * (1 - t). */
+void rasterise_lines(Frame& f, const cpv_scene_pipeline& p, const Assembled& as, const std::vector<VsOut>& vs) {
+    const cpv_scene* s = f.s;
+    const float vw = s->viewport[2], vh = s->viewport[3];
+    const float min_d = s->viewport[4], max_d = s->viewport[5];
+    const float half_x = (1.0f / vw) * 0.5f;
+    const float half_y = (1.0f / vh) * 0.5f;
+    const float lw_x = p.line_width / vw, lw_y = p.line_width / vh;
+    const ProgramInfo info = program_info(p.program);
+    for (size_t t = 0; t + 4 <= as.prims.size(); t += 4) {
+        const uint32_t provoking = as.prims[t];
+        const VsOut* v[2] = {&vs[as.prims[t + 1]], &vs[as.prims[t + 2]]};
+        f.stats->triangles++;
+        float P[2][4];
+        for (int k = 0; k < 2; k++) {
+            const float w = v[k]->pos[3];
+            P[k][0] = v[k]->pos[0] / w;
+            P[k][1] = v[k]->pos[1] / w;
+            P[k][2] = v[k]->pos[2] / w;
+            P[k][3] = w;
+        }
+        float dv[4];
+        for (int i = 0; i < 4; i++) dv[i] = P[1][i] - P[0][i];
+        const float dot4 = (dv[0] * dv[0] + dv[1] * dv[1]) + (dv[2] * dv[2] + dv[3] * dv[3]);
+        const float inv = 1.0f / std::sqrt(dot4);
+        const float dir_x = dv[0] * inv, dir_y = dv[1] * inv;
+        const float ox = dir_y * lw_x, oy = -dir_x * lw_y;
+        const float c00[2] = {P[0][0] + ox, P[0][1] + oy}, c01[2] = {P[0][0] - ox, P[0][1] - oy};
+        const float c10[2] = {P[1][0] + ox, P[1][1] + oy}, c11[2] = {P[1][0] - ox, P[1][1] - oy};
+        const float dx = P[1][0] - P[0][0], dy = P[1][1] - P[0][1];
+        for (uint32_t y = 0; static_cast<float>(y) < vh && y < s->height; y++) {
+            const float yf = (static_cast<float>(y) / vh + half_y) * 2.0f - 1.0f;
+            for (uint32_t x = 0; static_cast<float>(x) < vw && x < s->width; x++) {
+                const float xf = (static_cast<float>(x) / vw + half_x) * 2.0f - 1.0f;
+                if (!(edge(c00[0], c00[1], c01[0], c01[1], xf, yf) >= 0 && edge(c11[0], c11[1], c10[0], c10[1], xf, yf) >= 0 &&
+                      edge(c10[0], c10[1], c00[0], c00[1], xf, yf) >= 0 && edge(c01[0], c01[1], c11[0], c11[1], xf, yf) >= 0))
+                    continue;
+                const float num = (xf - P[0][0]) * dx + (yf - P[0][1]) * dy;
+                const float len = std::sqrt(dx * dx + dy * dy);
+                const float lt = num / (len * len);
+                const float wts[2] = {1.0f - lt, lt};
+                float inputs[kMaxVaryings];
+                int comp = 0;
+                for (int in = 0; in < info.num_inputs; in++) {
+                    for (int c = 0; c < info.input_size[in]; c++, comp++) {
+                        switch (info.input_interp[in]) {
+                        case INTERP_PERSPECTIVE: {
+                            float n = 0.0f, d = 0.0f;
+                            for (int k = 0; k < 2; k++) {
+                                n = n + wts[k] * v[k]->var[comp] / P[k][3];
+                                d = d + wts[k] / P[k][3];
+                            }
+                            inputs[comp] = n / d;
+                            break;
+                        }
+                        case INTERP_LINEAR: {
+                            float r = 0.0f;
+                            for (int k = 0; k < 2; k++) r = r + wts[k] * v[k]->var[comp];
+                            inputs[comp] = r;
+                            break;
+                        }
+                        case INTERP_FLAT: inputs[comp] = vs[provoking].var[comp]; break;
+                        }
+                    }
+                }
+                const float depth = P[0][2] * lt + P[1][2] * (1.0f - lt);
+                const float mapped = (max_d - min_d) * depth + min_d;
+                fragment(f, p, x, y, mapped, true, inputs);
+            }
+        }
+    }
+}
+
 void draw(Frame& f, const cpv_scene_draw& d) {
     const cpv_scene* s = f.s;
     if (d.pipeline >= s->num_pipelines) return;
@@ -819,7 +943,9 @@ void draw(Frame& f, const cpv_scene_draw& d) {
             run_vs(p.program, attr, f.res, vs[k]);
         }
         f.stats->vs_invocations += as.vertex_id.size();
-        rasterise(f, p, as, vs);
+        if (p.topology == TOPO_POINT_LIST) rasterise_points(f, p, as, vs);
+        else if (p.topology == TOPO_LINE_LIST || p.topology == TOPO_LINE_STRIP) rasterise_lines(f, p, as, vs);
+        else rasterise(f, p, as, vs);
     }
     f.res.push = nullptr;
 }

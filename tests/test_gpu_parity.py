@@ -39,7 +39,20 @@ VARIANTS = [
 ]
 
 
-@pytest.mark.parametrize("program,variant", VARIANTS)
+# Points and lines (variant bit 16; bits 10-11 then pick points, line list,
+# line strip; bit 17 a 3.5 px line width): sizes from the POINTS program's
+# gl_PointSize (0-16 px) or the default 1, perspective / linear / flat
+# varyings, depth, blending, BGRA, discard and a sampled texture.
+POINTS_LINES = [
+    (c.PROGRAM_POINTS, 0x10000 | 0x10), (c.PROGRAM_POINTS, 0x10000 | 0x20 | 0x8), (c.PROGRAM_POINTS, 0x10000 | 0x200 | 0x18 | 0x100),
+    (c.PROGRAM_FLATQUAD, 0x10000 | 0x20), (c.PROGRAM_CUBE, 0x10000 | 0x400), (c.PROGRAM_CUBE, 0x10000 | 0x400 | 0x20000 | 0x10),
+    (c.PROGRAM_CUBE, 0x10000 | 0x800 | 0x20 | 0x20000), (c.PROGRAM_NOPERSP, 0x10000 | 0x400 | 0x20000),
+    (c.PROGRAM_FLATQUAD, 0x10000 | 0x400 | 0x20000 | 0x20), (c.PROGRAM_DISCARD, 0x10000 | 0x20000 | 0x400),
+    (c.PROGRAM_TEXLIT, 0x10000 | 0x800 | 0x10 | 0x20000), (c.PROGRAM_POINTS, 0x10000 | 0x400 | 0x20000 | 0x1000),
+]
+
+
+@pytest.mark.parametrize("program,variant", VARIANTS + POINTS_LINES)
 @pytest.mark.parametrize("seed", [1, 2, 3])
 def test_program_variants(gpu_ctx, oracle, program, variant, seed):
     scene = c.Scene(c.PROGRAM, seed, [program, variant, 64, 48, 24])
@@ -89,4 +102,16 @@ def test_schedule_invariance(gpu_ctx, oracle, monkeypatch, tile, schedule, confi
     monkeypatch.setenv("CPV_SCHEDULE", schedule)
     scene = c.Scene(config, 7, params)
     report, _ = check(gpu_ctx, oracle, scene)
+    assert report["color_pixels_differing"] == 0, report
+
+
+@pytest.mark.parametrize("tile", ["8", "16", "32"])
+@pytest.mark.parametrize("schedule", ["0", "1", "2"])
+@pytest.mark.parametrize("program,variant", [(c.PROGRAM_POINTS, 0x10000 | 0x20), (c.PROGRAM_CUBE, 0x10000 | 0x800 | 0x20000 | 0x20)])
+def test_points_lines_schedule_invariance(gpu_ctx, oracle, monkeypatch, tile, schedule, program, variant):
+    monkeypatch.setenv("CPV_TILE", tile)
+    monkeypatch.setenv("CPV_SCHEDULE", schedule)
+    scene = c.Scene(c.PROGRAM, 4, [program, variant, 96, 64, 120])
+    report, stats = check(gpu_ctx, oracle, scene)
+    assert stats["fragments"] > 0
     assert report["color_pixels_differing"] == 0, report

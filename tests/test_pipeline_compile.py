@@ -15,11 +15,13 @@ KERNELS = os.path.join(ROOT, "cpvulkan_gb300", "csrc", "kernels")
 
 # (program, variant bits) — bits: 0-1 cull, 2 front CW, 3-4 depth format,
 # 5 blend, 6-7 depth op, 8 stencil, 9 BGRA, 10-11 topology, 12 u16 indices,
-# 13 depth write off, 14 nearest + mirror/border sampler, 15 LOD bias
+# 13 depth write off, 14 nearest + mirror/border sampler, 15 LOD bias,
+# 16 point/line topologies (10-11 then: points, lines, line strip), 17 wide lines
 PROGRAMS = [
     (c.PROGRAM_CUBE, 0x0), (c.PROGRAM_CUBE, 0x18 | 0x100), (c.PROGRAM_CUBE, 0x20 | 0x200 | 0x400),
     (c.PROGRAM_TEXLIT, 0x10 | 0x4000), (c.PROGRAM_FLATQUAD, 0x20), (c.PROGRAM_MESHPC, 0x10 | 0x2 | 0x4),
     (c.PROGRAM_DISCARD, 0x10), (c.PROGRAM_NOPERSP, 0x8 | 0x800),
+    (c.PROGRAM_POINTS, 0x10000 | 0x10), (c.PROGRAM_CUBE, 0x10000 | 0x400 | 0x20000), (c.PROGRAM_NOPERSP, 0x10000 | 0x800 | 0x8),
 ]
 
 
