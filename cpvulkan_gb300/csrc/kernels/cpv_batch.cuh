@@ -39,7 +39,7 @@ extern "C" __global__ void __launch_bounds__(CPV_BATCH_BLOCK) cpv_batch_setup(co
     if (local < P.total_prims) {
         CpvTri t;
         cpv_dispatch(B.draw_pipeline[d], [&](auto S) { decltype(S)::template setup<false>(P, local, t); });
-        rect = cpv_tile_rect(t, B.vw, B.vh);
+        rect = cpv_tile_rect(t, B.vw, B.vh, B.ndc_x, B.ndc_y);
     }
     const uint64_t g = static_cast<uint64_t>(block) * CPV_BATCH_BLOCK + threadIdx.x;
     B.rects[g] = rect;
@@ -105,7 +105,7 @@ struct CpvBatchSource {
 
 /* Persistent raster: CTAs take tiles from B.tile_counter (reset to zero
  * before the launch) until every tile is done. */
-extern "C" __global__ void __launch_bounds__(CPV_RT_THREADS) cpv_batch_raster(const __grid_constant__ CpvBatchParams B) {
+extern "C" __global__ void __launch_bounds__(CPV_RT_THREADS, CPV_RT_MIN_BLOCKS) cpv_batch_raster(const __grid_constant__ CpvBatchParams B) {
     extern __shared__ float4 cpv_dyn_smem[];
     __shared__ uint32_t warp_sums[CPV_RT_THREADS / 32];
     __shared__ uint32_t next_tile;

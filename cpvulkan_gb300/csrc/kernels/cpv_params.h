@@ -128,6 +128,10 @@ struct CpvBatchParams {
     const uint32_t* tile_end;
     uint32_t* tile_counter;       /* persistent raster work queue */
     uint32_t* status;
+    /* pixel-centre NDC of every column (fb_width) and row (fb_height):
+     * (x / vw + (1 / vw) * 0.5) * 2 - 1, each operation rounded once */
+    const float* ndc_x;
+    const float* ndc_y;
 };
 
 #endif /* CPV_PARAMS_H */

@@ -42,6 +42,10 @@
 #define CPV_TILE (1 << CPV_TILE_SHIFT)
 #define CPV_RT_THREADS ((CPV_TILE * CPV_TILE) < (32 * CPV_RT_WARPS) ? (CPV_TILE * CPV_TILE) : (32 * CPV_RT_WARPS))
 #define CPV_PPT ((CPV_TILE * CPV_TILE) / CPV_RT_THREADS)
+/* register budget of the persistent batched raster: 40 resident warps per
+ * SM (48 registers a thread at 256 threads a CTA, the five CTAs shared
+ * memory allows) */
+#define CPV_RT_MIN_BLOCKS (1280 / CPV_RT_THREADS)
 #define CPV_ROWS_PER_PASS (CPV_RT_THREADS / CPV_TILE)
 #define CPV_WARP_ROWS (32 / CPV_TILE > 0 ? 32 / CPV_TILE : 1) /* tile rows one warp covers per pass */
 #ifndef CPV_ANY_LINES
@@ -124,18 +128,20 @@ __device__ __forceinline__ bool cpv_covers(const CpvTri& t, float xf, float yf, 
  * when a bounding box of at most four pixels covers none of its pixel
  * centres — the raster would find no fragment there either). Packed as
  * x0 | y0 << 16, x1 | y1 << 16 in tile units, end exclusive. */
-__device__ __forceinline__ uint2 cpv_tile_rect(const CpvTri& t, float vw, float vh) {
+__device__ __forceinline__ uint2 cpv_tile_rect(const CpvTri& t, float vw, float vh, const float* ndc_x = nullptr, const float* ndc_y = nullptr) {
     uint32_t r[4] = {0, 0, 0, 0};
     if (cpv_tri_live(t)) {
         bool any = true;
         const int4 b = t.box;
         if ((b.z - b.x) * (b.w - b.y) <= 4) {
+            /* pixel centres from the tables when given (the box lies inside
+             * the attachment), else computed */
             any = false;
             for (int32_t y = b.y; y < b.w; y++) {
-                const float yf = cpv_pixel_ndc(y, vh);
+                const float yf = ndc_y ? __ldg(ndc_y + y) : cpv_pixel_ndc(y, vh);
                 for (int32_t x = b.x; x < b.z; x++) {
                     float w[3];
-                    if (cpv_covers(t, cpv_pixel_ndc(x, vw), yf, w)) any = true;
+                    if (cpv_covers(t, ndc_x ? __ldg(ndc_x + x) : cpv_pixel_ndc(x, vw), yf, w)) any = true;
                 }
             }
         }
@@ -147,6 +153,48 @@ __device__ __forceinline__ uint2 cpv_tile_rect(const CpvTri& t, float vw, float 
         }
     }
     return make_uint2(r[0] | (r[1] << 16), r[2] | (r[3] << 16));
+}
+
+/* Whether primitive t may cover a pixel of the rectangle [rx0, rx1) x
+ * [ry0, ry1) (inside its box). Each rounded edge function
+ * w = fl(fl(xf - a.x) * dy) - fl(fl(yf - a.y) * dx) is monotonic along a
+ * row and along a column (the pixel-centre values are monotonic in the
+ * pixel index, and IEEE subtraction and multiplication by a fixed value are
+ * monotonic), so its largest value over the rectangle is at the corner
+ * picked by the signs of dy and dx; if that value is negative, every pixel
+ * of the rectangle fails the edge and none is covered. Exact: it only
+ * drops pixels the coverage test rejects. Edges with a non-finite
+ * coefficient keep the primitive (NaN counts as covered). col/row hold the
+ * tile's pixel-centre NDC values, indexed from (tile_x0, tile_y0). */
+__device__ __forceinline__ bool cpv_may_cover(const CpvTri& t, int32_t rx0, int32_t ry0, int32_t rx1, int32_t ry1, const float* col,
+                                              const float* row, int32_t tile_x0, int32_t tile_y0) {
+    /* the pixel-centre sequences are monotonic (in either direction for a
+     * negative extent): their extremes over a range are its ends */
+    const float c0 = col[rx0 - tile_x0], c1 = col[rx1 - 1 - tile_x0];
+    const float r0 = row[ry0 - tile_y0], r1 = row[ry1 - 1 - tile_y0];
+    const float xa = fminf(c0, c1), xb = fmaxf(c0, c1), ya = fminf(r0, r1), yb = fmaxf(r0, r1);
+    if (!(fabsf(c0) <= 3.4e38f && fabsf(c1) <= 3.4e38f && fabsf(r0) <= 3.4e38f && fabsf(r1) <= 3.4e38f)) return true;
+    bool may = true;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        float4 e;
+        if (k < 3) {
+            e = t.e[k];
+        } else {
+#if CPV_ANY_LINES
+            if (((__float_as_uint(t.wf.w) >> 6) & 3u) != 3u) break;
+            e = t.za; /* a line's fourth edge */
+#else
+            break;
+#endif
+        }
+        if (!(fabsf(e.x) <= 3.4e38f && fabsf(e.y) <= 3.4e38f && fabsf(e.z) <= 3.4e38f && fabsf(e.w) <= 3.4e38f)) continue;
+        const float xf = e.w > 0.0f ? xb : xa;
+        const float yf = e.z > 0.0f ? ya : yb;
+        const float w = __fsub_rn(__fmul_rn(__fsub_rn(xf, e.x), e.w), __fmul_rn(__fsub_rn(yf, e.y), e.z));
+        may = may && !(w < 0.0f);
+    }
+    return may;
 }
 
 /* ---- per-fragment operation helpers (LLVMRuntime/PipelineCompiler.cpp:1020-1429) ---- */
@@ -311,7 +359,7 @@ __device__ __forceinline__ void cpv_list_small(const CpvTri& t, uint32_t j, int3
  * the schedule's buffers (deferred: fragment slots; sparse: per-pixel
  * primitive lists, pixel-centre tables, the large-primitive list). */
 #define CPV_TILE_PX (CPV_TILE * CPV_TILE)
-#define CPV_SPARSE_BYTES (4u * CPV_TILE_PX + 8u * CPV_TILE + CPV_TILE_PX * CPV_SLOT_DEPTH + CPV_BATCH)
+#define CPV_SPARSE_BYTES (4u * CPV_TILE_PX + CPV_TILE_PX * CPV_SLOT_DEPTH + CPV_BATCH)
 #define CPV_RASTER_SMEM_BYTES \
     (CPV_BATCH * sizeof(CpvTri) + (CPV_DEFERRED ? CPV_NSLOT * (4u + 20u + 2u) : 0u) + (CPV_SPARSE ? CPV_SPARSE_BYTES : 0u))
 
@@ -355,6 +403,16 @@ template <class Source>
 __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32_t ty, CpvTri* tris, uint32_t* warp_sums) {
     const uint64_t end = src.count();
     if (end == 0) return;
+    /* pixel-centre NDC of the tile's columns and rows (the values of
+     * cpv_pixel_ndc); the barrier keeps the previous tile's readers of a
+     * persistent CTA ahead of the rewrite */
+    __shared__ float col_ndc[CPV_TILE], row_ndc[CPV_TILE];
+    const int32_t tile_x0 = static_cast<int32_t>(tx * CPV_TILE), tile_y0 = static_cast<int32_t>(ty * CPV_TILE);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < CPV_TILE; i += CPV_RT_THREADS) {
+        col_ndc[i] = cpv_pixel_ndc(tile_x0 + static_cast<int32_t>(i), src.vw);
+        row_ndc[i] = cpv_pixel_ndc(tile_y0 + static_cast<int32_t>(i), src.vh);
+    }
     int32_t px[CPV_PPT], py[CPV_PPT];
     float xf[CPV_PPT], yf[CPV_PPT];
     bool inside[CPV_PPT];
@@ -378,16 +436,9 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
 #if CPV_SPARSE
     static_assert(CPV_BATCH <= 256, "batch indices are stored in bytes");
     uint32_t* list_count = reinterpret_cast<uint32_t*>(tris + CPV_BATCH);  /* per tile pixel: fragments listed this batch */
-    float* col_ndc = reinterpret_cast<float*>(list_count + CPV_TILE_PX);    /* pixel-centre NDC of the tile's columns … */
-    float* row_ndc = col_ndc + CPV_TILE;                                     /* … and rows (the values of cpv_pixel_ndc) */
-    uint8_t* list_j = reinterpret_cast<uint8_t*>(row_ndc + CPV_TILE);       /* per tile pixel: CPV_SLOT_DEPTH batch indices */
+    uint8_t* list_j = reinterpret_cast<uint8_t*>(list_count + CPV_TILE_PX);  /* per tile pixel: CPV_SLOT_DEPTH batch indices */
     uint8_t* large = list_j + CPV_TILE_PX * CPV_SLOT_DEPTH;                  /* batch indices of large primitives, in order */
-    const int32_t tile_x0 = static_cast<int32_t>(tx * CPV_TILE), tile_y0 = static_cast<int32_t>(ty * CPV_TILE);
     for (uint32_t i = threadIdx.x; i < CPV_TILE_PX; i += CPV_RT_THREADS) list_count[i] = 0u;
-    for (uint32_t i = threadIdx.x; i < CPV_TILE; i += CPV_RT_THREADS) {
-        col_ndc[i] = cpv_pixel_ndc(tile_x0 + static_cast<int32_t>(i), src.vw);
-        row_ndc[i] = cpv_pixel_ndc(tile_y0 + static_cast<int32_t>(i), src.vh);
-    }
     uint32_t lp[CPV_PPT]; /* this thread's pixels, as tile pixel indices */
 #pragma unroll
     for (int k = 0; k < CPV_PPT; k++) lp[k] = static_cast<uint32_t>((py[k] - tile_y0) * CPV_TILE + (px[k] - tile_x0));
@@ -402,8 +453,23 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
     for (uint64_t base = 0; base < end; base += CPV_BATCH) {
         const uint32_t n = static_cast<uint32_t>((end - base) < CPV_BATCH ? (end - base) : CPV_BATCH);
         __syncthreads();
-        /* a tile of 8 × 8 has fewer threads than CPV_BATCH: stride the set-up */
-        for (uint32_t i = threadIdx.x; i < n; i += CPV_RT_THREADS) src.setup(base + i, tris[i]);
+        /* a tile of 8 × 8 has fewer threads than CPV_BATCH: stride the set-up;
+         * a primitive reaching beyond the tile that covers no pixel of it
+         * (its box ∩ the tile) is dropped for this tile; one inside the tile
+         * is left to the pixel tests, which is cheaper for small primitives */
+        for (uint32_t i = threadIdx.x; i < n; i += CPV_RT_THREADS) {
+            CpvTri& t = tris[i];
+            src.setup(base + i, t);
+            const int4 b = t.box;
+            if (cpv_tri_live(t) && (b.x < tile_x0 || b.y < tile_y0 || b.z > tile_x0 + CPV_TILE || b.w > tile_y0 + CPV_TILE)) {
+                const int32_t rx0 = max(b.x, tile_x0), ry0 = max(b.y, tile_y0);
+                const int32_t rx1 = min(b.z, tile_x0 + CPV_TILE), ry1 = min(b.w, tile_y0 + CPV_TILE);
+                /* worth a test when the primitive spans much of the tile */
+                if (rx1 <= rx0 || ry1 <= ry0 ||
+                    ((rx1 - rx0) * (ry1 - ry0) >= CPV_TILE_PX / 8 && !cpv_may_cover(t, rx0, ry0, rx1, ry1, col_ndc, row_ndc, tile_x0, tile_y0)))
+                    t.wf.w = __uint_as_float(__float_as_uint(t.wf.w) & ~1u);
+            }
+        }
         __syncthreads();
 #if CPV_SPARSE
         /* 1. classify: large primitives (box covering more than CPV_SMALL_PX
@@ -497,9 +563,16 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
                 const uint32_t j = b + lane;
                 bool hit = false;
                 if (j < n && cpv_tri_live(tris[j])) {
-                    const int4 box = tris[j].box;
+                    const CpvTri& t = tris[j];
+                    const int4 box = t.box;
+                    const int32_t rx0 = max(box.x, tile_x0), rx1 = min(box.z, tile_x0 + CPV_TILE);
 #pragma unroll
-                    for (int k = 0; k < CPV_PPT; k++) hit = hit || (box.y < warp_y0 + k * CPV_ROWS_PER_PASS + CPV_WARP_ROWS && box.w > warp_y0 + k * CPV_ROWS_PER_PASS);
+                    for (int k = 0; k < CPV_PPT; k++) {
+                        /* the warp's rows of pass k, within the box */
+                        const int32_t ry0 = max(box.y, warp_y0 + k * CPV_ROWS_PER_PASS);
+                        const int32_t ry1 = min(box.w, warp_y0 + k * CPV_ROWS_PER_PASS + CPV_WARP_ROWS);
+                        hit = hit || (ry1 > ry0 && cpv_may_cover(t, rx0, ry0, rx1, ry1, col_ndc, row_ndc, tile_x0, tile_y0));
+                    }
                 }
                 const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, hit);
                 if (hit) mine[count + __popc(ballot & ((1u << lane) - 1u))] = static_cast<uint8_t>(j);

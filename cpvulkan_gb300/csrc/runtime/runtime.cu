@@ -528,6 +528,7 @@ BatchPlan::~BatchPlan() {
     dev_free(tile_begin_);
     dev_free(tile_end_);
     dev_free(words_);
+    dev_free(ndc_);
     if (pinned_pairs_) cudaFreeHost(pinned_pairs_);
 }
 
@@ -601,6 +602,22 @@ int BatchPlan::build(const Module& m, const BatchDraws& in, cudaStream_t stream)
     CPV_CUDA(cudaMemcpy(draw_block_, draw_block.data(), (n + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CPV_CUDA(cudaMemcpy(block_draw_, block_draw.data(), block_draw.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CPV_CUDA(cudaMemset(words_, 0, 64 * sizeof(uint32_t)));
+    // Pixel-centre tables for the set-up's coverage pretest, with the same
+    // rounded operations as cpv_pixel_ndc (IEEE binary32; the product by 2
+    // is exact, so contraction cannot change a value).
+    {
+        std::vector<float> ndc(static_cast<size_t>(in.fb_width) + in.fb_height);
+        auto centre = [](uint32_t i, float extent) {
+            const float half = (1.0f / extent) * 0.5f;
+            const float q = static_cast<float>(i) / extent;
+            const float s = q + half;
+            return s * 2.0f - 1.0f;
+        };
+        for (uint32_t x = 0; x < in.fb_width; x++) ndc[x] = centre(x, in.vw);
+        for (uint32_t y = 0; y < in.fb_height; y++) ndc[in.fb_width + y] = centre(y, in.vh);
+        if ((r = dev_alloc(ndc_, ndc.size())) != kOk) return r;
+        CPV_CUDA(cudaMemcpy(ndc_, ndc.data(), ndc.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
 
     int sms = 0, per_sm = 0;
     CPV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
@@ -639,6 +656,8 @@ int BatchPlan::build(const Module& m, const BatchDraws& in, cudaStream_t stream)
     P_.tile_end = tile_end_;
     P_.tile_counter = words_ + 2;
     P_.status = words_ + 1;
+    P_.ndc_x = ndc_;
+    P_.ndc_y = ndc_ + in.fb_width;
 
     // One set-up run to size the pair buffers.
     if (blocks) {

@@ -172,6 +172,7 @@ private:
     uint32_t* tile_begin_ = nullptr;
     uint32_t* tile_end_ = nullptr;
     uint32_t* words_ = nullptr;         // [0] pair total, [1] status, [2] tile counter
+    float* ndc_ = nullptr;              // pixel-centre NDC of the columns, then the rows
     uint32_t* pinned_pairs_ = nullptr;  // pair total of the last launch (host)
     cudaEvent_t done_ = nullptr;
     uint64_t prims_ = 0;
