@@ -396,4 +396,22 @@ extern "C" __global__ void __launch_bounds__(256) cpv_fill_u64(uint2* __restrict
         dst[i] = make_uint2(lo, hi);
 }
 
+/* ---- host → HBM copy read by the SMs ----
+ * Copies `words` 16-byte words from pinned host memory (device-accessible)
+ * to HBM with every SM issuing loads across the chip-to-chip link. Both
+ * pointers are 16-byte aligned; the caller copies any tail. */
+extern "C" __global__ void __launch_bounds__(256) cpv_copy_words(uint4* __restrict__ dst, const uint4* __restrict__ src, uint64_t words) {
+    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    /* four independent loads in flight per thread */
+    for (; i + 3 * stride < words; i += 4 * stride) {
+        const uint4 a = src[i], b = src[i + stride], c = src[i + 2 * stride], d = src[i + 3 * stride];
+        dst[i] = a;
+        dst[i + stride] = b;
+        dst[i + 2 * stride] = c;
+        dst[i + 3 * stride] = d;
+    }
+    for (; i < words; i += stride) dst[i] = src[i];
+}
+
 #endif /* CPV_BIN_CUH */

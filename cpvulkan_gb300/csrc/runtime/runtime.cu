@@ -391,6 +391,24 @@ int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, 
     return kOk;
 }
 
+int copy_host_to_device(cudaStream_t stream, uint8_t* dst, const uint8_t* host, uint64_t bytes) {
+    if (bytes == 0) return kOk;
+    const bool aligned = (reinterpret_cast<uintptr_t>(dst) % 16u) == 0 && (reinterpret_cast<uintptr_t>(host) % 16u) == 0;
+    uint64_t words = aligned && env_u32("CPV_H2D_KERNEL", 1u) ? bytes / 16u : 0;
+    if (words) {
+        int sms = 0;
+        CPV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+        uint64_t grid = static_cast<uint64_t>(sms) * 8u;
+        if (grid > (words + 255) / 256) grid = (words + 255) / 256;
+        cpv_copy_words<<<static_cast<unsigned>(grid), 256, 0, stream>>>(reinterpret_cast<uint4*>(dst), reinterpret_cast<const uint4*>(host), words);
+        count_launch();
+        CPV_CUDA(cudaGetLastError());
+    }
+    const uint64_t done = words * 16u;
+    if (done < bytes) CPV_CUDA(cudaMemcpyAsync(dst + done, host + done, bytes - done, cudaMemcpyHostToDevice, stream));
+    return kOk;
+}
+
 int blit(cudaStream_t stream, const CpvTexture& src, uint8_t* dst, uint32_t dst_w, uint32_t dst_h, uint32_t dst_format, const int32_t src_region[4],
          const int32_t dst_region[4], uint32_t filter) {
     CpvBlitRegion r;

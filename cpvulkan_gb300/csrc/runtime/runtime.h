@@ -205,6 +205,11 @@ int blit(cudaStream_t stream, const CpvTexture& src, uint8_t* dst, uint32_t dst_
 
 // Attachment fill with an encoded texel (1, 2, 4 or 8 bytes).
 int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, uint32_t lo, uint32_t hi);
+// Copies `bytes` from pinned host memory to HBM on `stream`: a kernel whose
+// SMs read the host memory directly (16-byte words, both pointers 16-byte
+// aligned), the unaligned remainder by cudaMemcpyAsync. CPV_H2D_KERNEL=0
+// uses cudaMemcpyAsync for everything.
+int copy_host_to_device(cudaStream_t stream, uint8_t* dst, const uint8_t* host, uint64_t bytes);
 
 // Exclusive scan helper (exposed for tests through the C ABI).
 int scan_u32(cudaStream_t stream, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total, Scratch& scratch);
