@@ -167,7 +167,7 @@ struct ModuleConfig {
     uint32_t tile_shift = 4;  // 8, 16 or 32 px tiles
     uint32_t schedule = 0;    // fragment schedule: 0 immediate, 1 deferred, 2 sparse
     uint32_t warps = 8;       // warps per tile CTA (capped by the tile's pixels)
-    uint32_t batch = 256;     // primitives set up per shared-memory batch (measured: 256 beats 128 on C2 and C4)
+    uint32_t batch = 256;     // primitives set up per shared-memory batch (set per schedule by module_config)
 };
 
 // Fragment schedule of a module whose pipelines prefer (or not) dense

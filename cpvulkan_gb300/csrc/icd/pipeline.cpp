@@ -66,6 +66,11 @@ ModuleConfig module_config(uint32_t tile_shift, bool prefers_deferred, bool fs_c
     ModuleConfig mc;
     mc.tile_shift = tile_shift;
     mc.schedule = schedule_for(prefers_deferred, fs_constant);
+    // Measured on GB300: the immediate schedule runs best with batches of 128
+    // primitives (C3: 2.64 against 2.87 ms; the smaller batch leaves room
+    // for a sixth CTA per SM), the sparse one with 256 (C2: 0.39 against
+    // 0.54 ms).
+    mc.batch = mc.schedule == 0 ? 128u : 256u;
     // Tunables (CPV_RT_WARPS 1-32 warps per tile CTA, CPV_BATCH_PRIMS 32-256
     // primitives per shared-memory batch).
     if (const char* v = std::getenv("CPV_RT_WARPS")) {
@@ -103,6 +108,12 @@ std::string compose_module(const std::vector<std::string>& stages, const std::ve
     src << "#define CPV_SCHEDULE " << mc.schedule << "\n";
     src << "#define CPV_RT_WARPS " << mc.warps << "\n";
     src << "#define CPV_BATCH " << mc.batch << "\n";
+    // Register budget of the per-draw raster: the immediate schedule gains
+    // from a seventh resident CTA (C3: 2.53 against 2.64 ms), the others
+    // keep the compiler's choice. CPV_PLAIN_MIN_BLOCKS overrides.
+    int min_blocks = mc.schedule == 0 ? 7 : 0;
+    if (const char* v = std::getenv("CPV_PLAIN_MIN_BLOCKS")) min_blocks = std::atoi(v);
+    if (min_blocks >= 1 && min_blocks <= 32) src << "#define CPV_PLAIN_MIN_BLOCKS " << min_blocks << "\n";
     src << "#define CPV_NV_MAX " << nv_max << "\n";
     bool any_constant = false;
     for (const std::string& st : stages) any_constant = any_constant || st.find("#define CPV_FS_CONSTANT 1\n") != std::string::npos;

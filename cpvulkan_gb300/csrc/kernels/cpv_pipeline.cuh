@@ -112,7 +112,13 @@ struct CpvPlainSource {
 /* Raster kernel: one CTA per screen tile (blockIdx.x = tile id).
  * direct != 0: the tile walks every primitive of the draw (small draws).
  * Otherwise it walks its bin. Dynamic shared memory: CPV_RASTER_SMEM_BYTES. */
-extern "C" __global__ void __launch_bounds__(CPV_RT_THREADS) cpv_raster(const __grid_constant__ CpvDrawParams P, uint32_t direct) {
+#ifdef CPV_PLAIN_MIN_BLOCKS
+/* a register budget for CPV_PLAIN_MIN_BLOCKS resident CTAs per SM */
+#define CPV_PLAIN_BOUNDS __launch_bounds__(CPV_RT_THREADS, CPV_PLAIN_MIN_BLOCKS)
+#else
+#define CPV_PLAIN_BOUNDS __launch_bounds__(CPV_RT_THREADS)
+#endif
+extern "C" __global__ void CPV_PLAIN_BOUNDS cpv_raster(const __grid_constant__ CpvDrawParams P, uint32_t direct) {
     extern __shared__ float4 cpv_dyn_smem[];
     __shared__ uint32_t warp_sums[CPV_RT_THREADS / 32];
     const uint32_t tile = blockIdx.x;

@@ -46,6 +46,7 @@
  * SM (48 registers a thread at 256 threads a CTA, the five CTAs shared
  * memory allows) */
 #define CPV_RT_MIN_BLOCKS (1280 / CPV_RT_THREADS)
+
 #define CPV_ROWS_PER_PASS (CPV_RT_THREADS / CPV_TILE)
 #define CPV_WARP_ROWS (32 / CPV_TILE > 0 ? 32 / CPV_TILE : 1) /* tile rows one warp covers per pass */
 #ifndef CPV_ANY_LINES
