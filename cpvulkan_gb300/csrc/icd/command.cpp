@@ -363,7 +363,9 @@ bool tuning_enabled(size_t draws) {
     return mode == 1u || draws >= env_u32("CPV_AUTOTUNE_MIN_DRAWS", 256u);
 }
 
-// Tile 8, 16 and 32 px, each with the warp counts that suit its pixels.
+// Tile 8, 16 and 32 px, each with the warp counts that suit its pixels, and
+// for 16 px tiles also 128-primitive batches and the other fast schedule
+// (immediate for a sparse module, sparse for an immediate one).
 std::vector<ModuleConfig> tune_candidates(const ModuleConfig& base) {
     static const uint32_t shapes[][2] = {{3, 2}, {4, 4}, {4, 8}, {5, 8}, {5, 16}};
     std::vector<ModuleConfig> out;
@@ -373,6 +375,17 @@ std::vector<ModuleConfig> tune_candidates(const ModuleConfig& base) {
         mc.warps = s[1];
         out.push_back(mc);
     }
+    ModuleConfig half = base;
+    half.tile_shift = 4;
+    half.warps = 8;
+    half.batch = base.batch == 256u ? 128u : 256u;
+    out.push_back(half);
+    ModuleConfig other = base;
+    other.tile_shift = 4;
+    other.warps = 8;
+    other.schedule = base.schedule == 0u ? 2u : 0u;
+    other.batch = other.schedule == 0u ? 128u : 256u;
+    out.push_back(other);
     return out;
 }
 
@@ -430,8 +443,8 @@ bool tune_batch(Queue* q, Device* dev, const std::vector<Pipeline*>& pipelines, 
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, e0, e1);
         char line[96];
-        std::snprintf(line, sizeof(line), "%stile %u warps %u schedule %u: %.3f ms", report.empty() ? "" : "; ", 1u << cands[i].tile_shift,
-                      cands[i].warps, cands[i].schedule, ms);
+        std::snprintf(line, sizeof(line), "%stile %u warps %u schedule %u batch %u: %.3f ms", report.empty() ? "" : "; ",
+                      1u << cands[i].tile_shift, cands[i].warps, cands[i].schedule, cands[i].batch, ms);
         report += line;
         if (!best_plan || ms < best_ms) {
             best_ms = ms;
@@ -447,7 +460,8 @@ bool tune_batch(Queue* q, Device* dev, const std::vector<Pipeline*>& pipelines, 
     if (e1) cudaEventDestroy(e1);
     if (best_plan) {
         char line[64];
-        std::snprintf(line, sizeof(line), "; chosen tile %u warps %u", 1u << chosen.tile_shift, chosen.warps);
+        std::snprintf(line, sizeof(line), "; chosen tile %u warps %u schedule %u batch %u", 1u << chosen.tile_shift, chosen.warps,
+                      chosen.schedule, chosen.batch);
         g_last_tuning = report + line;
     }
     return ok && best_plan != nullptr;

@@ -57,10 +57,11 @@ CPV_EXPORT const char* cpv_last_error(void);
 CPV_EXPORT uint64_t cpv_kernel_launches(void);
 
 /* The calling thread's last batch tuning (a render pass of many draws timed
- * under each tile size / warps-per-tile candidate on its first submission):
- * each candidate's time and the choice, e.g. "tile 16 warps 8 schedule 2:
- * 61.2 ms; ...; chosen tile 16 warps 8". Empty when no tuning ran. No
- * reference counterpart. */
+ * under each tile size / warps-per-tile / batch / schedule candidate on its
+ * first submission): each candidate's time and the choice, e.g. "tile 16
+ * warps 8 schedule 2 batch 256: 65.4 ms; ...; chosen tile 16 warps 8
+ * schedule 2 batch 256". Empty when no tuning ran. No reference
+ * counterpart. */
 CPV_EXPORT const char* cpv_batch_tuning(void);
 
 /* 1 when a CUDA device can be used (creates the context), else 0. */

@@ -105,6 +105,6 @@ def test_tuned_batch_equals_plain(gpu_ctx, plain, monkeypatch, seed):
     ref = plain(gpu_ctx, scene)[0]
     runs = frames(gpu_ctx, scene, 3)
     report = c.batch_tuning()
-    assert report.count(" ms") == 5 and "chosen tile" in report, report
+    assert report.count(" ms") == 7 and "chosen tile" in report, report
     for got in runs:
         same(got, ref)
