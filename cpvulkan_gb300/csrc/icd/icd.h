@@ -301,8 +301,8 @@ VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& writte
 // At vkEndCommandBuffer: compiles (NVRTC) and caches the batched module of
 // every render pass that will run batched, so its first submission does not.
 void precompile_batches(CommandBuffer* cb);
-// Report of the calling thread's last batch tuning: one "tile/warps/schedule
-// ms" entry per candidate and the choice ("" when none ran).
+// Report of the calling thread's last batch tuning: each candidate's
+// configuration and time, then the choice ("" when none ran).
 const char* last_tuning();
 // Checks, before any work is enqueued, that every draw of `cb` fits the fixed
 // scratch array (VK_ERROR_OUT_OF_DEVICE_MEMORY and a message otherwise).

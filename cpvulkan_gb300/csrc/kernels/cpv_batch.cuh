@@ -99,6 +99,8 @@ struct CpvBatchSource {
         const bool front = cpv_tri_front(t);
         cpv_dispatch(cpv_tri_pipeline(t), [&](auto S) { decltype(S)::rop(bc, front, colour, mapped, s); });
     }
+    /* batched passes build no blend tables */
+    __device__ __forceinline__ bool table_fragment(const CpvTri&, CpvPixel&) const { return false; }
     __device__ __forceinline__ void load_pixel(uint64_t pix, CpvPixel& s) const { cpv_p0::Stage::load_pixel(B.color, B.depth, pix, s); }
     __device__ __forceinline__ void store_pixel(uint64_t pix, const CpvPixel& s) const { cpv_p0::Stage::store_pixel(B.color, B.depth, pix, s); }
 };

@@ -105,6 +105,19 @@ struct CpvPlainSource {
     __device__ __forceinline__ void rop(const CpvTri& t, const float colour[4], float mapped, CpvPixel& s) const {
         cpv_p0::Stage::rop(P.blend_constants, cpv_tri_front(t), colour, mapped, s, cpv_p0::Stage::table(P, t));
     }
+    /* A covered fragment of a table-only pipeline: the table lookup is the
+     * whole of shade + rop (the colour is constant and nothing discards a
+     * live primitive). Returns false when the general path must run. */
+    __device__ __forceinline__ bool table_fragment(const CpvTri& t, CpvPixel& s) const {
+        if (cpv_p0::kTableOnly) {
+            const uint8_t* table = cpv_p0::Stage::table(P, t);
+            if (table) {
+                cpv_p0::cpv_apply_table(table, s);
+                return true;
+            }
+        }
+        return false;
+    }
     __device__ __forceinline__ void load_pixel(uint64_t pix, CpvPixel& s) const { cpv_p0::Stage::load_pixel(P.color, P.depth, pix, s); }
     __device__ __forceinline__ void store_pixel(uint64_t pix, const CpvPixel& s) const { cpv_p0::Stage::store_pixel(P.color, P.depth, pix, s); }
 };

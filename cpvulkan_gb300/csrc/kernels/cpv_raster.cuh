@@ -375,6 +375,8 @@ __device__ __forceinline__ void cpv_list_small(const CpvTri& t, uint32_t j, int3
  *   void setup(uint64_t i, CpvTri& t)        set up the i-th (or mark it dead)
  *   bool shade(const CpvTri&, const float w[3], int x, int y, float colour[4], float& mapped)
  *   void rop(const CpvTri&, const float colour[4], float mapped, CpvPixel&)
+ *   bool table_fragment(const CpvTri&, CpvPixel&)  a covered fragment applied by a
+ *                                            blend-table lookup alone (false: use shade + rop)
  *   void load_pixel(uint64_t pix, CpvPixel&) / store_pixel(uint64_t pix, const CpvPixel&)
  *   float vw, vh                             viewport extent (pixel centres)
  *   uint32_t fb_width, fb_height
@@ -598,6 +600,7 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
                     if (px[k] < box.x || px[k] >= box.z || py[k] < box.y || py[k] >= box.w) continue;
                     float w[3];
                     if (!cpv_covers(t, xf[k], yf[k], w)) continue;
+                    if (src.table_fragment(t, st[k])) continue;
                     float colour[4], mapped;
                     if (src.shade(t, w, px[k], py[k], colour, mapped)) continue;
                     src.rop(t, colour, mapped, st[k]);

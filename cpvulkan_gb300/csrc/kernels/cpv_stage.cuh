@@ -536,6 +536,20 @@ __device__ __forceinline__ void cpv_blend_table_column(const float colour[4], co
 }
 
 constexpr bool kBlendTable = CPV_BLEND_TABLE != 0;
+/* a blend-table pipeline without depth or stencil operations: a covered
+ * fragment's whole effect is its table lookup */
+constexpr bool kTableOnly = kBlendTable && !(CPV_DEPTH_TEST && CPV_DEPTH_FORMAT != 0) && !(CPV_STENCIL_TEST && CPV_DEPTH_FORMAT == 130);
+
+/* cpv_rop's colour write through a blend table, when every test passes */
+__device__ __forceinline__ void cpv_apply_table(const uint8_t* table, CpvPixel& s) {
+    uint32_t packed = 0u;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const uint32_t d = (s.colour >> cpv_channel_shift(i)) & 0xFFu;
+        packed |= static_cast<uint32_t>(table[i * 256 + d]) << cpv_channel_shift(i);
+    }
+    s.colour = packed;
+}
 
 /* The stage functions of this pipeline, as one type the module's
  * dispatcher (cpv_dispatch) hands to generic code. */
