@@ -464,7 +464,13 @@ VKAPI_ATTR VkResult VKAPI_CALL FlushMappedMemoryRanges(VkDevice device, uint32_t
         auto* m = reinterpret_cast<DeviceMemory*>(r[i].memory);
         if (!m->host) continue;
         const VkDeviceSize size = r[i].size == VK_WHOLE_SIZE ? m->size - r[i].offset : r[i].size;
-        if (cudaMemcpy(m->device + r[i].offset, m->host + r[i].offset, size, cudaMemcpyHostToDevice) != cudaSuccess) return VK_ERROR_OUT_OF_DEVICE_MEMORY;
+        if (dev->compile_only || dev->queues.empty()) {
+            if (cudaMemcpy(m->device + r[i].offset, m->host + r[i].offset, size, cudaMemcpyHostToDevice) != cudaSuccess) return VK_ERROR_OUT_OF_DEVICE_MEMORY;
+            continue;
+        }
+        cudaStream_t s = dev->queues[0]->stream;
+        if (rt::copy_host_to_device(s, m->device + r[i].offset, m->host + r[i].offset, size) != rt::kOk || cudaStreamSynchronize(s) != cudaSuccess)
+            return VK_ERROR_OUT_OF_DEVICE_MEMORY;
     }
     return VK_SUCCESS;
 }
