@@ -49,6 +49,12 @@
 
 #define CPV_ROWS_PER_PASS (CPV_RT_THREADS / CPV_TILE)
 #define CPV_WARP_ROWS (32 / CPV_TILE > 0 ? 32 / CPV_TILE : 1) /* tile rows one warp covers per pass */
+/* immediate schedule with one pixel a thread: each warp owns an 8 x 4 block
+ * of the tile instead of whole rows (a compact block is more often wholly
+ * inside or outside a primitive, so fewer visits cover few lanes) */
+#define CPV_WARP_BLOCKS (CPV_WARP_LISTS && CPV_PPT == 1 && CPV_TILE >= 8)
+#define CPV_BLOCK_W 8
+#define CPV_BLOCK_H 4
 #ifndef CPV_ANY_LINES
 #define CPV_ANY_LINES 0 /* some pipeline of the module draws lines */
 #endif
@@ -422,8 +428,15 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
     CpvPixel st[CPV_PPT];
 #pragma unroll
     for (int k = 0; k < CPV_PPT; k++) {
+#if CPV_WARP_BLOCKS
+        /* warp w: block (w % blocks a row, w / blocks a row); lane: x = lane % 8, y = lane / 8 */
+        const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+        px[k] = static_cast<int32_t>(tx * CPV_TILE + (warp % (CPV_TILE / CPV_BLOCK_W)) * CPV_BLOCK_W + (lane % CPV_BLOCK_W));
+        py[k] = static_cast<int32_t>(ty * CPV_TILE + (warp / (CPV_TILE / CPV_BLOCK_W)) * CPV_BLOCK_H + (lane / CPV_BLOCK_W));
+#else
         px[k] = static_cast<int32_t>(tx * CPV_TILE + (threadIdx.x % CPV_TILE));
         py[k] = static_cast<int32_t>(ty * CPV_TILE + (threadIdx.x / CPV_TILE) + k * CPV_ROWS_PER_PASS);
+#endif
         inside[k] = px[k] < static_cast<int32_t>(src.fb_width) && py[k] < static_cast<int32_t>(src.fb_height);
         xf[k] = cpv_pixel_ndc(px[k], src.vw);
         yf[k] = cpv_pixel_ndc(py[k], src.vh);
@@ -450,7 +463,12 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
 #if CPV_WARP_LISTS
     /* immediate schedule: per warp, the batch's primitives reaching its rows */
     __shared__ uint8_t warp_list[(CPV_RT_THREADS / 32) * CPV_BATCH];
+#if CPV_WARP_BLOCKS
+    const int32_t warp_x0 = static_cast<int32_t>(tx * CPV_TILE + ((threadIdx.x >> 5) % (CPV_TILE / CPV_BLOCK_W)) * CPV_BLOCK_W);
+    const int32_t warp_y0 = static_cast<int32_t>(ty * CPV_TILE + ((threadIdx.x >> 5) / (CPV_TILE / CPV_BLOCK_W)) * CPV_BLOCK_H);
+#else
     const int32_t warp_y0 = static_cast<int32_t>(ty * CPV_TILE + ((threadIdx.x & ~31u) / CPV_TILE));
+#endif
 #endif
 
     for (uint64_t base = 0; base < end; base += CPV_BATCH) {
@@ -568,6 +586,12 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
                 if (j < n && cpv_tri_live(tris[j])) {
                     const CpvTri& t = tris[j];
                     const int4 box = t.box;
+#if CPV_WARP_BLOCKS
+                    /* the warp's block, within the box */
+                    const int32_t rx0 = max(box.x, warp_x0), rx1 = min(box.z, warp_x0 + CPV_BLOCK_W);
+                    const int32_t ry0 = max(box.y, warp_y0), ry1 = min(box.w, warp_y0 + CPV_BLOCK_H);
+                    hit = rx1 > rx0 && ry1 > ry0 && cpv_may_cover(t, rx0, ry0, rx1, ry1, col_ndc, row_ndc, tile_x0, tile_y0);
+#else
                     const int32_t rx0 = max(box.x, tile_x0), rx1 = min(box.z, tile_x0 + CPV_TILE);
 #pragma unroll
                     for (int k = 0; k < CPV_PPT; k++) {
@@ -576,6 +600,7 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
                         const int32_t ry1 = min(box.w, warp_y0 + k * CPV_ROWS_PER_PASS + CPV_WARP_ROWS);
                         hit = hit || (ry1 > ry0 && cpv_may_cover(t, rx0, ry0, rx1, ry1, col_ndc, row_ndc, tile_x0, tile_y0));
                     }
+#endif
                 }
                 const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, hit);
                 if (hit) mine[count + __popc(ballot & ((1u << lane) - 1u))] = static_cast<uint8_t>(j);
