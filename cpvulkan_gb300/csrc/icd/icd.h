@@ -159,6 +159,7 @@ struct Pipeline {
     uint32_t tile_shift = 4;        // screen tile of the pipeline's modules
     bool blend_table = false;       // per-primitive blend tables (constant colour, per-channel blend)
     bool fs_constant = false;       // fragment shader shaded once per primitive
+    bool samples = false;           // fragment shader samples images
     std::string source;  // generated CUDA translation unit of the per-draw module
 };
 
@@ -168,6 +169,7 @@ struct ModuleConfig {
     uint32_t schedule = 0;    // fragment schedule: 0 immediate, 1 deferred, 2 sparse
     uint32_t warps = 8;       // warps per tile CTA (capped by the tile's pixels)
     uint32_t batch = 256;     // primitives set up per shared-memory batch (set per schedule by module_config)
+    bool samples = false;     // a fragment shader samples images (register budget of the batched raster)
 };
 
 // Fragment schedule of a module whose pipelines prefer (or not) dense
@@ -175,7 +177,7 @@ struct ModuleConfig {
 uint32_t schedule_for(bool prefers_deferred, bool fs_constant);
 // Module configuration for a tile size and shading preference, with the
 // environment's tunables applied.
-ModuleConfig module_config(uint32_t tile_shift, bool prefers_deferred, bool fs_constant);
+ModuleConfig module_config(uint32_t tile_shift, bool prefers_deferred, bool fs_constant, bool samples);
 
 // The CUDA translation unit of a module over one pipeline's stage block
 // (per-draw kernels) or several (batched kernels, pipeline i in namespace

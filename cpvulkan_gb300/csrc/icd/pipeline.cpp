@@ -9,6 +9,7 @@
 // the JIT module exactly as the CPV_* constants below bake it into the
 // NVRTC module. Unsupported state is rejected with a VkResult instead of the
 // reference's abort.
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -62,9 +63,10 @@ const char* const kStageMacros[] = {
 
 }  // namespace
 
-ModuleConfig module_config(uint32_t tile_shift, bool prefers_deferred, bool fs_constant) {
+ModuleConfig module_config(uint32_t tile_shift, bool prefers_deferred, bool fs_constant, bool samples) {
     ModuleConfig mc;
     mc.tile_shift = tile_shift;
+    mc.samples = samples;
     mc.schedule = schedule_for(prefers_deferred, fs_constant);
     // Measured on GB300: the immediate schedule runs best with batches of 128
     // primitives (C3: 2.64 against 2.87 ms; the smaller batch leaves room
@@ -114,6 +116,18 @@ std::string compose_module(const std::vector<std::string>& stages, const std::ve
     int min_blocks = mc.schedule == 0 ? 7 : 0;
     if (const char* v = std::getenv("CPV_PLAIN_MIN_BLOCKS")) min_blocks = std::atoi(v);
     if (min_blocks >= 1 && min_blocks <= 32) src << "#define CPV_PLAIN_MIN_BLOCKS " << min_blocks << "\n";
+    // Register budget of the persistent batched raster, in resident CTAs of
+    // 256 threads: 5 (48 registers a thread) for flat or lit shading, 4 (64)
+    // when a fragment shader samples images (C4: 39.4 ms at 5 against 40.2
+    // at 4; the textured heightfield: 0.41 ms at 4 against 0.43 at 5).
+    // CPV_BATCH_MIN_BLOCKS overrides.
+    {
+        const uint32_t threads = std::min(1u << (2 * mc.tile_shift), 32u * mc.warps);
+        int b = static_cast<int>((mc.samples ? 1024u : 1280u) / threads);
+        if (b < 1) b = 1;
+        if (const char* v = std::getenv("CPV_BATCH_MIN_BLOCKS")) b = std::atoi(v);
+        if (b >= 1 && b <= 32) src << "#define CPV_RT_MIN_BLOCKS " << b << "\n";
+    }
     src << "#define CPV_NV_MAX " << nv_max << "\n";
     bool any_constant = false;
     for (const std::string& st : stages) any_constant = any_constant || st.find("#define CPV_FS_CONSTANT 1\n") != std::string::npos;
@@ -411,10 +425,11 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     p->stage = src.str();
     p->nv = nv;
     p->prefers_deferred = prefers_deferred;
+    p->samples = fr.samples > 0;
     p->tile_shift = tile_shift;
     p->blend_table = blend_table;
     p->fs_constant = fs_constant;
-    p->source = compose_module({p->stage}, {nv}, module_config(tile_shift, prefers_deferred, fs_constant), false);
+    p->source = compose_module({p->stage}, {nv}, module_config(tile_shift, prefers_deferred, fs_constant, fr.samples > 0), false);
     // The key covers the generated source and the embedded kernel headers it
     // includes, so an on-disk cache never returns a cubin of older kernels.
     {

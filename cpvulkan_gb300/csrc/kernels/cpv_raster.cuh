@@ -45,7 +45,9 @@
 /* register budget of the persistent batched raster: 40 resident warps per
  * SM (48 registers a thread at 256 threads a CTA, the five CTAs shared
  * memory allows) */
+#ifndef CPV_RT_MIN_BLOCKS
 #define CPV_RT_MIN_BLOCKS (1280 / CPV_RT_THREADS)
+#endif
 
 #define CPV_ROWS_PER_PASS (CPV_RT_THREADS / CPV_TILE)
 #define CPV_WARP_ROWS (32 / CPV_TILE > 0 ? 32 / CPV_TILE : 1) /* tile rows one warp covers per pass */

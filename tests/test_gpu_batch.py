@@ -108,3 +108,28 @@ def test_tuned_batch_equals_plain(gpu_ctx, plain, monkeypatch, seed):
     assert report.count(" ms") == 7 and "chosen tile" in report, report
     for got in runs:
         same(got, ref)
+
+
+def test_large_single_draw_runs_batched(gpu_ctx, oracle, plain, monkeypatch):
+    """A pass of one draw with at least CPV_BATCH_MIN_PRIMS primitives (and no
+    blend tables) runs batched: its image equals the per-draw image and the
+    oracle's, and the batched raster is what ran."""
+    import ctypes
+    monkeypatch.setenv("CPV_BATCH_MIN_PRIMS", "20000")
+    scene = c.Scene(c.HEIGHTFIELD, 3, [128, 480, 270])  # 32,258 triangles in one draw
+    ref = plain(gpu_ctx, scene)[0]
+    icd = ctypes.CDLL(c.ICD_PATH)
+    icd.cpv_profile_get.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_double)]
+    icd.cpv_profile_reset()
+    icd.cpv_profile_enable(1)
+    try:
+        got = frames(gpu_ctx, scene, 2)
+    finally:
+        icd.cpv_profile_enable(0)
+    n, ms = ctypes.c_uint64(0), ctypes.c_double(0.0)
+    icd.cpv_profile_get(b"cpv_batch_raster", ctypes.byref(n), ctypes.byref(ms))
+    assert n.value >= 2
+    for g in got:
+        same(g, ref)
+    ocol, odep, _ = oracle.render(scene)
+    assert compare(scene, got[-1][0], got[-1][1], ocol, odep)["color_pixels_differing"] == 0
