@@ -393,8 +393,15 @@ int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, 
 
 int copy_host_to_device(cudaStream_t stream, uint8_t* dst, const uint8_t* host, uint64_t bytes) {
     if (bytes == 0) return kOk;
-    const bool aligned = (reinterpret_cast<uintptr_t>(dst) % 16u) == 0 && (reinterpret_cast<uintptr_t>(host) % 16u) == 0;
-    uint64_t words = aligned && env_u32("CPV_H2D_KERNEL", 1u) ? bytes / 16u : 0;
+    // The kernel reads the host memory through its device mapping: only
+    // page-locked host memory the device can address qualifies.
+    const uint8_t* mapped = nullptr;
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, host) == cudaSuccess && attr.type == cudaMemoryTypeHost && attr.devicePointer)
+        mapped = static_cast<const uint8_t*>(attr.devicePointer);
+    cudaGetLastError();
+    const bool aligned = (reinterpret_cast<uintptr_t>(dst) % 16u) == 0 && (reinterpret_cast<uintptr_t>(mapped) % 16u) == 0;
+    uint64_t words = mapped && aligned && env_u32("CPV_H2D_KERNEL", 1u) ? bytes / 16u : 0;
     if (words) {
         int sms = 0;
         CPV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
@@ -402,7 +409,7 @@ int copy_host_to_device(cudaStream_t stream, uint8_t* dst, const uint8_t* host, 
         // link, not the SMs, sets the rate.
         uint64_t grid = static_cast<uint64_t>(sms) * 8u;
         if (grid > (words + 255) / 256) grid = (words + 255) / 256;
-        cpv_copy_words<<<static_cast<unsigned>(grid), 256, 0, stream>>>(reinterpret_cast<uint4*>(dst), reinterpret_cast<const uint4*>(host), words);
+        cpv_copy_words<<<static_cast<unsigned>(grid), 256, 0, stream>>>(reinterpret_cast<uint4*>(dst), reinterpret_cast<const uint4*>(mapped), words);
         count_launch();
         CPV_CUDA(cudaGetLastError());
     }
