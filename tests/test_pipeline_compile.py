@@ -79,3 +79,29 @@ def test_tile_sizes_compile(native, monkeypatch, tile):
     ctx.compile_pipelines(c.Scene(c.HEIGHTFIELD, 1, [16, 64, 64]))
     ctx.close()
 
+
+
+def _module_source(compile_ctx, program, variant):
+    ctx, dump = compile_ctx
+    ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [program, variant, 32, 32, 4]))
+    (path,) = glob.glob(str(dump / "pipeline_*.cu"))
+    return open(path).read()
+
+
+@pytest.mark.parametrize("program,variant,expect", [
+    # lines need the fourth edge in every coverage test of their module
+    (c.PROGRAM_CUBE, 0x10000 | 0x400, {"CPV_ANY_LINES": "1", "CPV_TOPOLOGY": "1"}),
+    (c.PROGRAM_POINTS, 0x10000, {"CPV_ANY_LINES": "0", "CPV_TOPOLOGY": "0"}),
+    # flat shading: the immediate schedule, 128-primitive batches, a 7-CTA register budget
+    (c.PROGRAM_FLATQUAD, 0x20, {"CPV_FS_CONSTANT": "1", "CPV_SCHEDULE": "0", "CPV_BATCH": "128", "CPV_PLAIN_MIN_BLOCKS": "7",
+                                "CPV_BLEND_TABLE": "1"}),
+    # interpolated colour: sparse schedule, 256-primitive batches, 24 fragments a pixel
+    (c.PROGRAM_CUBE, 0x10, {"CPV_SCHEDULE": "2", "CPV_BATCH": "256", "CPV_SLOT_DEPTH": "24", "CPV_RT_MIN_BLOCKS": "5"}),
+    # texture sampling: 16 fragments a pixel, a 4-CTA budget for the batched raster
+    (c.PROGRAM_TEXLIT, 0x10, {"CPV_SCHEDULE": "2", "CPV_SLOT_DEPTH": "16", "CPV_RT_MIN_BLOCKS": "4"}),
+])
+def test_module_configuration(compile_ctx, program, variant, expect):
+    """The fixed-function and schedule macros a pipeline's module is compiled with."""
+    text = _module_source(compile_ctx, program, variant)
+    for name, value in expect.items():
+        assert "#define %s %s\n" % (name, value) in text, (name, value)
