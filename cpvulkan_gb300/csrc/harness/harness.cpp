@@ -451,9 +451,11 @@ bool build_pipelines(cpvh_context* c, const cpv_scene* s, VkRenderPass pass, VkP
         cba.srcAlphaBlendFactor = static_cast<VkBlendFactor>(sp.src_alpha);
         cba.dstAlphaBlendFactor = static_cast<VkBlendFactor>(sp.dst_alpha);
         cba.alphaBlendOp = static_cast<VkBlendOp>(sp.alpha_op);
-        cba.colorWriteMask = 0xF;
+        cba.colorWriteMask = sp.color_write_mask;
         VkPipelineColorBlendStateCreateInfo cbs{};
         cbs.sType = VK_STRUCTURE_TYPE_PIPELINE_COLOR_BLEND_STATE_CREATE_INFO;
+        cbs.logicOpEnable = sp.logic_op_enable;
+        cbs.logicOp = static_cast<VkLogicOp>(sp.logic_op);
         cbs.attachmentCount = 1;
         cbs.pAttachments = &cba;
         for (int k = 0; k < 4; k++) cbs.blendConstants[k] = sp.blend_constants[k];

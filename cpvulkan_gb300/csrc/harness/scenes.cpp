@@ -170,6 +170,7 @@ cpv_scene_pipeline base_pipeline(uint32_t program) {
     p.src_color = p.src_alpha = VK_BLEND_FACTOR_ONE;
     p.dst_color = p.dst_alpha = VK_BLEND_FACTOR_ZERO;
     p.line_width = 1.0f;
+    p.color_write_mask = 0xF;
     return p;
 }
 
@@ -652,6 +653,11 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
         p.topology = topo_sel == 1 ? VK_PRIMITIVE_TOPOLOGY_LINE_LIST : (topo_sel == 2 ? VK_PRIMITIVE_TOPOLOGY_LINE_STRIP : VK_PRIMITIVE_TOPOLOGY_POINT_LIST);
         p.line_width = (variant & 0x20000) ? 3.5f : 1.0f;
     }
+    if (variant & 0x40000) {  // logic op (bits 20-23) instead of blending
+        p.logic_op_enable = 1;
+        p.logic_op = (variant >> 20) & 0xF;
+    }
+    if (variant & 0x80000) p.color_write_mask = (variant >> 24) & 0xF;  // partial colour write mask (bits 24-27)
     const bool u16 = (variant & 0x1000) != 0;
 
     uint32_t vcount = 0;

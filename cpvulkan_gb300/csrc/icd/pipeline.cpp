@@ -57,7 +57,7 @@ const char* const kStageMacros[] = {
     "CPV_NV", "CPV_TOPOLOGY", "CPV_CULL_MODE", "CPV_FRONT_CW", "CPV_DEPTH_TEST", "CPV_DEPTH_WRITE", "CPV_DEPTH_OP", "CPV_STENCIL_TEST",
     "CPV_ST_F_FAIL", "CPV_ST_F_PASS", "CPV_ST_F_DFAIL", "CPV_ST_F_OP", "CPV_ST_F_CMASK", "CPV_ST_F_WMASK", "CPV_ST_F_REF",
     "CPV_ST_B_FAIL", "CPV_ST_B_PASS", "CPV_ST_B_DFAIL", "CPV_ST_B_OP", "CPV_ST_B_CMASK", "CPV_ST_B_WMASK", "CPV_ST_B_REF",
-    "CPV_BLEND", "CPV_SRC_COLOR", "CPV_DST_COLOR", "CPV_COLOR_OP", "CPV_SRC_ALPHA", "CPV_DST_ALPHA", "CPV_ALPHA_OP", "CPV_WRITE_MASK",
+    "CPV_BLEND", "CPV_SRC_COLOR", "CPV_DST_COLOR", "CPV_COLOR_OP", "CPV_SRC_ALPHA", "CPV_DST_ALPHA", "CPV_ALPHA_OP", "CPV_WRITE_MASK", "CPV_LOGIC", "CPV_LOGIC_OP",
     "CPV_COLOR_FORMAT", "CPV_DEPTH_FORMAT", "CPV_ORIGIN_UPPER", "CPV_FS_CONSTANT", "CPV_BLEND_TABLE", "CPV_LINE_WIDTH", "CPV_PRIM_KIND",
 };
 
@@ -322,10 +322,21 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     VkPipelineColorBlendAttachmentState blend{};
     blend.colorWriteMask = 0xF;
     float blend_constants[4] = {0, 0, 0, 0};
+    bool logic = false;
+    uint32_t logic_op = VK_LOGIC_OP_COPY;
     if (ci.pColorBlendState) {
-        if (ci.pColorBlendState->logicOpEnable) return reject("logic op");
         if (ci.pColorBlendState->attachmentCount >= 1) blend = ci.pColorBlendState->pAttachments[0];
         for (int i = 0; i < 4; i++) blend_constants[i] = ci.pColorBlendState->blendConstants[i];
+        if (ci.pColorBlendState->logicOpEnable) {
+            // Both colour formats are UNORM, where a logic op applies; blending
+            // of the attachment is then treated as disabled (Vulkan 1.1,
+            // "Logical Operations"). The reference aborts here
+            // (LLVMRuntime/PipelineCompiler.cpp:1687-1690).
+            if (static_cast<uint32_t>(ci.pColorBlendState->logicOp) > VK_LOGIC_OP_SET) return reject("logic op " + std::to_string(ci.pColorBlendState->logicOp));
+            logic = true;
+            logic_op = static_cast<uint32_t>(ci.pColorBlendState->logicOp);
+            blend.blendEnable = VK_FALSE;
+        }
     }
     if (blend.blendEnable) {
         auto bad = [](VkBlendFactor f) { return f > VK_BLEND_FACTOR_SRC_ALPHA_SATURATE; };
@@ -411,6 +422,8 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     src << "#define CPV_DST_ALPHA " << static_cast<uint32_t>(blend.dstAlphaBlendFactor) << "\n";
     src << "#define CPV_ALPHA_OP " << static_cast<uint32_t>(blend.alphaBlendOp) << "\n";
     src << "#define CPV_WRITE_MASK " << (blend.colorWriteMask & 0xF) << "u\n";
+    src << "#define CPV_LOGIC " << (logic ? 1 : 0) << "\n";
+    src << "#define CPV_LOGIC_OP " << logic_op << "\n";
     src << "#define CPV_COLOR_FORMAT " << static_cast<uint32_t>(cfmt) << "\n";
     src << "#define CPV_DEPTH_FORMAT " << static_cast<uint32_t>(dfmt) << "\n";
     src << "#define CPV_ORIGIN_UPPER " << (fr.origin_upper_left ? 1 : 0) << "\n";

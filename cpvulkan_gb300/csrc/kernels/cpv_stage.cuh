@@ -4,7 +4,7 @@
  * that pipeline's namespace (cpv_p0, cpv_p1, …), after the pipeline's
  * fixed-function macros (CPV_TOPOLOGY, CPV_CULL_MODE, CPV_FRONT_CW,
  * CPV_DEPTH_*, CPV_STENCIL_TEST, CPV_ST_*, CPV_BLEND, CPV_SRC_* / CPV_DST_*,
- * CPV_*_OP, CPV_WRITE_MASK, CPV_COLOR_FORMAT, CPV_DEPTH_FORMAT,
+ * CPV_*_OP, CPV_WRITE_MASK, CPV_LOGIC, CPV_LOGIC_OP, CPV_COLOR_FORMAT, CPV_DEPTH_FORMAT,
  * CPV_ORIGIN_UPPER, CPV_NV) and its translated shaders:
  *
  *   __device__ void cpv_vs_run(const CpvDrawParams&, uint32_t vertex_index,
@@ -31,6 +31,11 @@
 #endif
 #ifndef CPV_LINE_WIDTH
 #define CPV_LINE_WIDTH 1.0f
+#endif
+/* logicOpEnable (blending is then off) and its VkLogicOp */
+#ifndef CPV_LOGIC
+#define CPV_LOGIC 0
+#define CPV_LOGIC_OP 3
 #endif
 
 /* The fragment shader of a primitive whose shader is constant over it
@@ -447,9 +452,35 @@ __device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& 
 #endif
 }
 
+/* VkLogicOp CPV_LOGIC_OP of an encoded fragment channel s and the stored
+ * channel d (Vulkan 1.1, "Logical Operations"); the switch folds to one
+ * expression at compile time. */
+__device__ __forceinline__ uint32_t cpv_logic(uint32_t s, uint32_t d) {
+    uint32_t r;
+    switch (CPV_LOGIC_OP) {
+    case 0: r = 0u; break;
+    case 1: r = s & d; break;
+    case 2: r = s & ~d; break;
+    case 3: r = s; break;
+    case 4: r = ~s & d; break;
+    case 5: r = d; break;
+    case 6: r = s ^ d; break;
+    case 7: r = s | d; break;
+    case 8: r = ~(s | d); break;
+    case 9: r = ~(s ^ d); break;
+    case 10: r = ~d; break;
+    case 11: r = s | ~d; break;
+    case 12: r = ~s; break;
+    case 13: r = ~s | d; break;
+    case 14: r = ~(s & d); break;
+    default: r = 0xFFu; break;
+    }
+    return r & 0xFFu;
+}
+
 /* Depth bounds are rejected at pipeline creation; order as the reference's
  * fragment wrapper: current values → stencil test → depth test → depth /
- * stencil write → colour write (blend, write mask, encode). */
+ * stencil write → colour write (logic op or blend, write mask, encode). */
 __device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool front, const float colour[4], float mapped, CpvPixel& s,
                                         const uint8_t* table = nullptr) {
     const bool has_depth = CPV_DEPTH_FORMAT != 0;
@@ -492,6 +523,18 @@ __device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool fro
         }
 #else
         (void)table;
+#endif
+#if CPV_LOGIC
+        (void)blend_constants;
+        uint32_t logic = 0u;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint32_t d = (s.colour >> cpv_channel_shift(i)) & 0xFFu;
+            const uint32_t byte = ((CPV_WRITE_MASK >> i) & 1u) ? cpv_logic(cpv_encode_unorm(colour[i], 255.0f), d) : d;
+            logic |= byte << cpv_channel_shift(i);
+        }
+        s.colour = logic;
+        return;
 #endif
         float out[4];
 #if CPV_BLEND

@@ -75,6 +75,9 @@ typedef struct cpv_scene_pipeline {
     uint32_t num_attributes;
     cpv_scene_attribute attributes[CPV_SCENE_MAX_ATTRIBUTES];
     float line_width;    /* VkPipelineRasterizationStateCreateInfo::lineWidth */
+    uint32_t color_write_mask; /* VkColorComponentFlags: R 1, G 2, B 4, A 8 (0xF writes every channel) */
+    uint32_t logic_op_enable;  /* VkPipelineColorBlendStateCreateInfo::logicOpEnable (blending then off) */
+    uint32_t logic_op;         /* VkLogicOp, CLEAR (0) .. SET (15) */
 } cpv_scene_pipeline;
 
 typedef struct cpv_scene_draw {

@@ -645,6 +645,60 @@ void assemble(const Frame& f, const cpv_scene_pipeline& p, const cpv_scene_draw&
     }
 }
 
+/* The 16 logical operations on one UNORM8 channel (Vulkan 1.1, "Logical
+ * Operations"): s is the fragment's encoded value, d the stored one. The
+ * reference aborts on logicOpEnable (LLVMRuntime/PipelineCompiler.cpp:1687-1690). */
+uint8_t logic_op(uint32_t op, uint8_t s, uint8_t d) {
+    uint32_t r = 0;
+    switch (op) {
+    case 0: r = 0; break;                  // CLEAR
+    case 1: r = s & d; break;              // AND
+    case 2: r = s & ~d; break;             // AND_REVERSE
+    case 3: r = s; break;                  // COPY
+    case 4: r = ~s & d; break;             // AND_INVERTED
+    case 5: r = d; break;                  // NO_OP
+    case 6: r = s ^ d; break;              // XOR
+    case 7: r = s | d; break;              // OR
+    case 8: r = ~(s | d); break;           // NOR
+    case 9: r = ~(s ^ d); break;           // EQUIVALENT
+    case 10: r = ~d; break;                // INVERT
+    case 11: r = s | ~d; break;            // OR_REVERSE
+    case 12: r = ~s; break;                // COPY_INVERTED
+    case 13: r = ~s | d; break;            // OR_INVERTED
+    case 14: r = ~(s & d); break;          // NAND
+    default: r = 0xFF; break;              // SET
+    }
+    return static_cast<uint8_t>(r);
+}
+
+/* Colour write of a fragment that passed its tests
+ * (LLVMRuntime/PipelineCompiler.cpp:1415-1429, 1528-1727): a logic op on the
+ * encoded channels, else the blend (the reference's ApplyBlend,
+ * CPVulkan/CommandBuffer.Draw.cpp:956-1262), else the colour itself; then the
+ * colour write mask keeps the stored byte of every channel it leaves out
+ * (the reference aborts on a partial mask, PipelineCompiler.cpp:1693-1700;
+ * this follows Vulkan 1.1, "Color Write Mask"). */
+void write_colour(uint8_t* texel, uint32_t fmt, const cpv_scene_pipeline& p, const float colour[4]) {
+    int off[4];
+    colour_offsets(fmt, off);
+    uint8_t bytes[4];
+    if (p.logic_op_enable) {
+        for (int i = 0; i < 4; i++) bytes[i] = logic_op(p.logic_op, static_cast<uint8_t>(encode_unorm(colour[i], 255.0f)), texel[off[i]]);
+    } else {
+        float out[4];
+        if (p.blend_enable) {
+            float dst[4];
+            get_colour(texel, fmt, dst);
+            blend(colour, dst, p.blend_constants, p.src_color, p.dst_color, p.color_op, p.src_alpha, p.dst_alpha, p.alpha_op, out);
+        } else {
+            for (int i = 0; i < 4; i++) out[i] = colour[i];
+        }
+        for (int i = 0; i < 4; i++) bytes[i] = static_cast<uint8_t>(encode_unorm(out[i], 255.0f));
+    }
+    for (int i = 0; i < 4; i++)
+        if ((p.color_write_mask >> i) & 1u) texel[off[i]] = bytes[i];
+}
+
 /* Interpolation (CPVulkan/CommandBuffer.Draw.cpp:816-871). */
 float interp_persp(const float pw[3], const float v[3], const float w[3]) {
     float num = 0.0f, den = 0.0f;
@@ -707,15 +761,7 @@ void fragment(Frame& f, const cpv_scene_pipeline& p, uint32_t x, uint32_t y, flo
     }
 
     if (stencil_result && depth_result) {
-        uint8_t* texel = f.colour + pix * 4;
-        if (p.blend_enable) {
-            float dst[4], out[4];
-            get_colour(texel, s->color_format, dst);
-            blend(colour, dst, p.blend_constants, p.src_color, p.dst_color, p.color_op, p.src_alpha, p.dst_alpha, p.alpha_op, out);
-            set_colour(texel, s->color_format, out);
-        } else {
-            set_colour(texel, s->color_format, colour);
-        }
+        write_colour(f.colour + pix * 4, s->color_format, p, colour);
         f.stats->fragments_written++;
     }
 }
@@ -1013,6 +1059,7 @@ int cpv_oracle_render(const cpv_scene* scene, uint8_t* color, uint8_t* depth, ui
 
 float cpv_oracle_edge(float ax, float ay, float bx, float by, float cx, float cy) { return edge(ax, ay, bx, by, cx, cy); }
 uint8_t cpv_oracle_encode_unorm8(float value) { return static_cast<uint8_t>(encode_unorm(value, 255.0f)); }
+uint8_t cpv_oracle_logic_op(uint32_t op, uint8_t src, uint8_t dst) { return logic_op(op, src, dst); }
 uint16_t cpv_oracle_encode_unorm16(float value) { return static_cast<uint16_t>(encode_unorm(value, 65535.0f)); }
 float cpv_oracle_decode_unorm8(uint8_t value) { return decode_unorm8(value); }
 

@@ -48,6 +48,8 @@ int cpv_oracle_render(const cpv_scene* scene, uint8_t* color, uint8_t* depth, ui
 /* Single-step helpers exposed for known-answer tests. */
 float cpv_oracle_edge(float ax, float ay, float bx, float by, float cx, float cy);
 uint8_t cpv_oracle_encode_unorm8(float value);
+/* VkLogicOp `op` (0 CLEAR .. 15 SET) of an encoded source and destination byte. */
+uint8_t cpv_oracle_logic_op(uint32_t op, uint8_t src, uint8_t dst);
 uint16_t cpv_oracle_encode_unorm16(float value);
 float cpv_oracle_decode_unorm8(uint8_t value);
 /* Bilinear/nearest sample of level 0..levels-1 of an RGBA8 texture with the

@@ -36,6 +36,8 @@ class Oracle:
         lib.cpv_oracle_encode_unorm16.argtypes = [f]
         lib.cpv_oracle_decode_unorm8.restype = f
         lib.cpv_oracle_decode_unorm8.argtypes = [ctypes.c_uint8]
+        lib.cpv_oracle_logic_op.restype = ctypes.c_uint8
+        lib.cpv_oracle_logic_op.argtypes = [ctypes.c_uint32, ctypes.c_uint8, ctypes.c_uint8]
         lib.cpv_oracle_sample.argtypes = [vp, u32, u32, u32, ctypes.POINTER(SamplerDesc), f, f, f, ctypes.POINTER(f * 4)]
         lib.cpv_oracle_blend.argtypes = [ctypes.POINTER(f * 4)] * 3 + [u32] * 6 + [ctypes.POINTER(f * 4)]
         lib.cpv_oracle_blit.argtypes = [vp, u32, u32, u32, vp, u32, u32, u32, vp, u32]

@@ -52,7 +52,19 @@ POINTS_LINES = [
 ]
 
 
-@pytest.mark.parametrize("program,variant", VARIANTS + POINTS_LINES)
+# Logic ops (bit 18, VkLogicOp in bits 20-23; blending is then off) and
+# partial colour write masks (bit 19, mask in bits 24-27), on interpolated,
+# flat-shaded (blend-table candidates), textured, line and BGRA pipelines.
+LOGIC_MASK = [
+    (c.PROGRAM_CUBE, 0x10 | 0x40000 | (6 << 20)), (c.PROGRAM_FLATQUAD, 0x20 | 0x40000 | (7 << 20)),
+    (c.PROGRAM_FLATQUAD, 0x20 | 0x200 | 0x40000 | (2 << 20)), (c.PROGRAM_TEXLIT, 0x10 | 0x40000 | (12 << 20) | 0x80000 | (0x7 << 24)),
+    (c.PROGRAM_CUBE, 0x10000 | 0x400 | 0x20000 | 0x40000 | (9 << 20)), (c.PROGRAM_FLATQUAD, 0x40000 | (14 << 20)),
+    (c.PROGRAM_FLATQUAD, 0x20 | 0x80000 | (0x9 << 24)), (c.PROGRAM_CUBE, 0x18 | 0x100 | 0x200 | 0x80000 | (0x6 << 24)),
+    (c.PROGRAM_POINTS, 0x10000 | 0x20 | 0x80000 | (0x3 << 24)),
+]
+
+
+@pytest.mark.parametrize("program,variant", VARIANTS + POINTS_LINES + LOGIC_MASK)
 @pytest.mark.parametrize("seed", [1, 2, 3])
 def test_program_variants(gpu_ctx, oracle, program, variant, seed):
     scene = c.Scene(c.PROGRAM, seed, [program, variant, 64, 48, 24])
