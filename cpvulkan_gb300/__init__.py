@@ -51,6 +51,14 @@ class SceneHeader(ctypes.Structure):
                 ("pipelines", vp), ("num_draws", u32), ("draws", vp)]
 
 
+class SceneDraw(ctypes.Structure):
+    """cpv_scene_draw (include/cpv/scene.h)."""
+    u32 = ctypes.c_uint32
+    _fields_ = [("pipeline", u32), ("indexed", u32), ("count", u32), ("instance_count", u32), ("first", u32),
+                ("vertex_offset", ctypes.c_int32), ("first_instance", u32), ("push_size", u32),
+                ("vertex_offsets", ctypes.c_uint64 * 4), ("index_offset", ctypes.c_uint64), ("push", ctypes.c_uint8 * 128)]
+
+
 def depth_texel_bytes(fmt):
     return {0: 0, VK_FORMAT_D16_UNORM: 2, VK_FORMAT_D32_SFLOAT: 4, VK_FORMAT_D32_SFLOAT_S8_UINT: 8}[fmt]
 
@@ -87,6 +95,8 @@ def harness():
     h.cpvh_render_e2e.argtypes = [vp, u32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(u64), ctypes.POINTER(u64)]
     h.cpvh_renderer_update.restype = ctypes.c_int
     h.cpvh_renderer_update.argtypes = [vp]
+    h.cpvh_renderer_set_indirect.restype = ctypes.c_int
+    h.cpvh_renderer_set_indirect.argtypes = [vp, u32, vp]
     h.cpvh_readback.restype = ctypes.c_int
     h.cpvh_readback.argtypes = [vp, vp, vp]
     h.cpvh_queue.restype = vp
@@ -126,6 +136,20 @@ class Scene:
     @property
     def draws(self):
         return SceneHeader.from_address(self.ptr).num_draws
+
+    def draw(self, i):
+        """Draw i of the scene (a view of the harness's cpv_scene_draw)."""
+        h = SceneHeader.from_address(self.ptr)
+        if not 0 <= i < h.num_draws:
+            raise IndexError(i)
+        return SceneDraw.from_address(h.draws + i * ctypes.sizeof(SceneDraw))
+
+    def indirect_record(self, i):
+        """Draw i as its VkDrawIndexedIndirectCommand / VkDrawIndirectCommand words."""
+        d = self.draw(i)
+        if d.indexed:
+            return [d.count, d.instance_count, d.first, d.vertex_offset & 0xFFFFFFFF, d.first_instance]
+        return [d.count, d.instance_count, d.first, d.first_instance, 0]
 
     @property
     def input_bytes(self):
@@ -230,6 +254,15 @@ class Renderer:
         r = harness().cpvh_renderer_update(self.ptr)
         if r != VK_SUCCESS:
             raise RuntimeError("update failed (%d)" % r)
+
+    def set_indirect(self, draw, record):
+        """Overwrites draw `draw`'s indirect record (renderers created with
+        CPVH_INDIRECT=1): [count, instances, first, vertex offset or first
+        instance, first instance or 0]."""
+        rec = (ctypes.c_uint32 * 5)(*[int(v) & 0xFFFFFFFF for v in (list(record) + [0] * 5)[:5]])
+        r = harness().cpvh_renderer_set_indirect(self.ptr, draw, rec)
+        if r != VK_SUCCESS:
+            raise RuntimeError("set_indirect failed (%d)" % r)
 
     def readback(self):
         s = self.scene

@@ -919,6 +919,16 @@ int cpvh_renderer_update(cpvh_renderer* r) {
     return res;
 }
 
+int cpvh_renderer_set_indirect(cpvh_renderer* r, uint32_t draw, const uint32_t record[5]) {
+    cpvh_context* c = r->ctx;
+    if (!r->indirect.buffer || draw >= r->scene->num_draws) return VK_ERROR_INITIALIZATION_FAILED;
+    void* map = nullptr;
+    if (c->f.vkMapMemory(c->device, r->indirect.memory, static_cast<VkDeviceSize>(draw) * 20, 20, 0, &map) != VK_SUCCESS) return VK_ERROR_MEMORY_MAP_FAILED;
+    std::memcpy(map, record, 20);
+    c->f.vkUnmapMemory(c->device, r->indirect.memory);
+    return VK_SUCCESS;
+}
+
 int cpvh_render(cpvh_renderer* r, uint32_t frames, double* device_ms, double* latency_ms) {
     cpvh_context* c = r->ctx;
     VkSubmitInfo si{};

@@ -251,7 +251,8 @@ VkResult draw(Queue* q, State& s, uint32_t count, uint32_t instances, uint32_t f
 // the CPU and runs the draw. Here too the records are read on the host at
 // replay: from the pinned mirror of host-visible memory the device has not
 // written, else from HBM after the queue's earlier work has finished.
-VkResult draw_indirect(Queue* q, State& s, const Cmd& c, const std::vector<DeviceMemory*>& written, bool no_alloc) {
+VkResult read_indirect(Queue* q, const Cmd& c, const std::vector<DeviceMemory*>& written, std::vector<IndirectDraw>& out) {
+    out.clear();
     const Buffer* b = static_cast<const Buffer*>(c.p[0]);
     const bool indexed = c.type == CmdType::DrawIndexedIndirect;
     const uint32_t n = c.u[0], stride = c.u[1], record = indexed ? 20u : 16u;
@@ -269,18 +270,32 @@ VkResult draw_indirect(Queue* q, State& s, const Cmd& c, const std::vector<Devic
         cudaGetLastError();
         return VK_ERROR_DEVICE_LOST;
     }
+    out.resize(n);
     for (uint32_t i = 0; i < n; i++) {
         uint32_t v[5] = {0, 0, 0, 0, 0};
         std::memcpy(v, bytes.data() + static_cast<uint64_t>(i) * stride, record);
-        VkResult r;
         if (indexed)  // indexCount, instanceCount, firstIndex, vertexOffset, firstInstance
-            r = draw(q, s, v[0], v[1], v[2], static_cast<int32_t>(v[3]), v[4], true, no_alloc);
+            out[i] = {v[0], v[1], v[2], static_cast<int32_t>(v[3]), v[4]};
         else  // vertexCount, instanceCount, firstVertex, firstInstance
-            r = draw(q, s, v[0], v[1], v[2], 0, v[3], false, no_alloc);
+            out[i] = {v[0], v[1], v[2], 0, v[3]};
+    }
+    return VK_SUCCESS;
+}
+
+VkResult draw_indirect(Queue* q, State& s, const Cmd& c, const std::vector<DeviceMemory*>& written, bool no_alloc) {
+    std::vector<IndirectDraw> records;
+    const VkResult rr = read_indirect(q, c, written, records);
+    if (rr != VK_SUCCESS) return rr;
+    const bool indexed = c.type == CmdType::DrawIndexedIndirect;
+    for (const IndirectDraw& d : records) {
+        const VkResult r = draw(q, s, d.count, d.instances, d.first, d.vertex_offset, d.first_instance, indexed, no_alloc);
         if (r != VK_SUCCESS) return r;
     }
     return VK_SUCCESS;
 }
+
+bool is_indirect(const Cmd& c) { return c.type == CmdType::DrawIndirect || c.type == CmdType::DrawIndexedIndirect; }
+
 
 // Applies a binding / dynamic-state command to `s`; false for any other.
 bool apply_state(State& s, const Cmd& c) {
@@ -358,13 +373,23 @@ ModuleConfig batch_config(const std::vector<Pipeline*>& pipelines) {
 // 0.59 ms batched against 0.74 ms per draw. Blend-table pipelines stay per
 // draw, where their tables exist (the 400k-triangle blend scene: 2.84 ms per
 // draw, 3.28 ms batched).
+// Indirect draws count as the draws their records hold (at recording, where
+// the records are not read yet, their primitives count as none).
 struct PassCensus {
     Pipeline* bound = nullptr;
     size_t draws = 0;
     uint64_t prims = 0;
     bool blend_tables = false;
-    void add(const Cmd& c) {
+    void add(const Cmd& c, const std::vector<IndirectDraw>* records = nullptr) {
         if (c.type == CmdType::BindPipeline) bound = static_cast<Pipeline*>(c.p[0]);
+        if (is_indirect(c)) {
+            draws += c.u[0];
+            if (!bound) return;
+            if (records)
+                for (const IndirectDraw& d : *records) prims += static_cast<uint64_t>(primitives_per_instance(bound->topology, d.count)) * d.instances;
+            blend_tables = blend_tables || (c.u[0] > 0 && bound->blend_table);
+            return;
+        }
         if (c.type != CmdType::Draw && c.type != CmdType::DrawIndexed) return;
         draws++;
         if (!bound) return;
@@ -502,24 +527,21 @@ bool tune_batch(Queue* q, Device* dev, const std::vector<Pipeline*>& pipelines, 
 // Builds the batch of the render pass whose commands are (begin, end): the
 // draws' parameters, the pipeline set, the batched module and the plan.
 // Leaves state->plain set when the pass does not batch.
-void build_batch(Queue* q, const CommandBuffer* cb, size_t begin, size_t end, const State& entry, BatchState& state) {
+void build_batch(Queue* q, const CommandBuffer* cb, size_t begin, size_t end, const State& entry, const PassIndirect& indirect, BatchState& state) {
     state.plain = true;
     State s = entry;
     rt::BatchDraws in;
     std::vector<Pipeline*> pipelines;
     float vw = 0.0f, vh = 0.0f;
-    for (size_t i = begin + 1; i < end; i++) {
-        const Cmd& c = cb->cmds[i];
-        if (apply_state(s, c)) continue;
-        if (c.type != CmdType::Draw && c.type != CmdType::DrawIndexed) return;  // indirect draws: per-draw path
+    // false when the draw cannot join the batch
+    auto add = [&](uint32_t count, uint32_t instances, uint32_t first, int32_t vertex_offset, uint32_t first_instance, bool indexed) {
         CpvDrawParams P;
         bool empty = true;
-        const bool indexed = c.type == CmdType::DrawIndexed;
-        if (build_draw(s, c.u[0], c.u[1], c.u[2], indexed ? c.i0 : 0, c.u[3], indexed, P, empty) != VK_SUCCESS) return;
-        if (empty) continue;
+        if (build_draw(s, count, instances, first, vertex_offset, first_instance, indexed, P, empty) != VK_SUCCESS) return false;
+        if (empty) return true;
         auto it = std::find(pipelines.begin(), pipelines.end(), s.pipeline);
         if (it == pipelines.end()) {
-            if (pipelines.size() == 16) return;  // 4-bit pipeline index
+            if (pipelines.size() == 16) return false;  // 4-bit pipeline index
             pipelines.push_back(s.pipeline);
             it = pipelines.end() - 1;
         }
@@ -531,10 +553,27 @@ void build_batch(Queue* q, const CommandBuffer* cb, size_t begin, size_t end, co
             in.fb_width = P.fb_width;
             in.fb_height = P.fb_height;
         } else if (P.viewport[2] != vw || P.viewport[3] != vh) {
-            return;  // pixel centres depend on the viewport extent
+            return false;  // pixel centres depend on the viewport extent
         }
         in.draws.push_back(P);
         in.pipeline.push_back(static_cast<uint32_t>(it - pipelines.begin()));
+        return true;
+    };
+    size_t next_indirect = 0;
+    for (size_t i = begin + 1; i < end; i++) {
+        const Cmd& c = cb->cmds[i];
+        if (apply_state(s, c)) continue;
+        if (is_indirect(c)) {
+            if (next_indirect >= indirect.size() || indirect[next_indirect].first != i) return;
+            const bool indexed = c.type == CmdType::DrawIndexedIndirect;
+            for (const IndirectDraw& d : indirect[next_indirect].second)
+                if (!add(d.count, d.instances, d.first, d.vertex_offset, d.first_instance, indexed)) return;
+            next_indirect++;
+            continue;
+        }
+        if (c.type != CmdType::Draw && c.type != CmdType::DrawIndexed) return;
+        const bool indexed = c.type == CmdType::DrawIndexed;
+        if (!add(c.u[0], c.u[1], c.u[2], indexed ? c.i0 : 0, c.u[3], indexed)) return;
     }
     if (in.draws.empty()) return;
     in.vw = vw;
@@ -586,15 +625,37 @@ void build_batch(Queue* q, const CommandBuffer* cb, size_t begin, size_t end, co
 // Runs the render pass (begin, end) batched when it batches: returns true
 // after enqueuing it, with `s` advanced past its commands; false leaves the
 // pass to the per-draw path.
-bool run_batched(Queue* q, CommandBuffer* cb, size_t begin, size_t end, State& s, VkResult& result) {
+// A pass with indirect draws reads their records at every submission; its
+// batch is rebuilt when they differ from the records it was built from.
+bool run_batched(Queue* q, CommandBuffer* cb, size_t begin, size_t end, State& s, const std::vector<DeviceMemory*>& written, VkResult& result) {
+    PassIndirect indirect;
+    for (size_t i = begin + 1; i < end; i++) {
+        if (!is_indirect(cb->cmds[i])) continue;
+        indirect.emplace_back(i, std::vector<IndirectDraw>());
+        if (read_indirect(q, cb->cmds[i], written, indirect.back().second) != VK_SUCCESS) return false;  // the per-draw path reports it
+    }
     PassCensus census;
     census.bound = s.pipeline;
-    for (size_t i = begin + 1; i < end; i++) census.add(cb->cmds[i]);
+    size_t next_indirect = 0;
+    for (size_t i = begin + 1; i < end; i++) {
+        const Cmd& c = cb->cmds[i];
+        census.add(c, is_indirect(c) ? &indirect[next_indirect++].second : nullptr);
+    }
     if (!census.batches()) return false;
     auto& slot = cb->batches[begin];
+    if (slot && slot->indirect != indirect) {
+        // the old plan's buffers may still be in use by this queue's work
+        if (cudaStreamSynchronize(q->stream) != cudaSuccess) {
+            cudaGetLastError();
+            result = VK_ERROR_DEVICE_LOST;
+            return true;
+        }
+        slot.reset();
+    }
     if (!slot) {
         slot = std::make_unique<BatchState>();
-        build_batch(q, cb, begin, end, s, *slot);
+        slot->indirect = indirect;
+        build_batch(q, cb, begin, end, s, indirect, *slot);
     }
     if (slot->plain) return false;
     for (size_t i = begin + 1; i < end; i++) apply_state(s, cb->cmds[i]);
@@ -618,7 +679,7 @@ VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& writte
             if (r != VK_SUCCESS || no_alloc) break;
             size_t end = idx + 1;
             while (end < cb->cmds.size() && cb->cmds[end].type != CmdType::EndRenderPass) end++;
-            if (end < cb->cmds.size() && run_batched(q, cb, idx, end, s, r)) idx = end - 1;  // continue at EndRenderPass
+            if (end < cb->cmds.size() && run_batched(q, cb, idx, end, s, written, r)) idx = end - 1;  // continue at EndRenderPass
             break;
         }
         case CmdType::EndRenderPass: s.pass = nullptr; s.fb = nullptr; break;
@@ -826,6 +887,8 @@ void precompile_batches(CommandBuffer* cb) {
             break;
         case CmdType::Draw:
         case CmdType::DrawIndexed:
+        case CmdType::DrawIndirect:
+        case CmdType::DrawIndexedIndirect:
             if (!in_pass || !bound) break;
             census.add(c);
             if (std::find(pipelines.begin(), pipelines.end(), bound) == pipelines.end()) pipelines.push_back(bound);

@@ -209,10 +209,25 @@ struct Cmd {
 
 // Batched execution state of one render pass of a recorded command buffer
 // (built on its first execution, reused until the command buffer is reset).
+// One VkDrawIndirectCommand / VkDrawIndexedIndirectCommand as a direct
+// draw's arguments.
+struct IndirectDraw {
+    uint32_t count, instances, first;
+    int32_t vertex_offset;
+    uint32_t first_instance;
+    bool operator==(const IndirectDraw& o) const {
+        return count == o.count && instances == o.instances && first == o.first && vertex_offset == o.vertex_offset && first_instance == o.first_instance;
+    }
+};
+
+// The records of a render pass's indirect draws, by command index.
+using PassIndirect = std::vector<std::pair<size_t, std::vector<IndirectDraw>>>;
+
 struct BatchState {
     rt::Module* module = nullptr;  // owned by Device::batch_modules
     std::unique_ptr<rt::BatchPlan> plan;
     bool plain = false;            // not batchable: the per-draw path runs
+    PassIndirect indirect;         // the indirect draws' records the batch was built from
 };
 
 // A command buffer's work captured as a CUDA graph for one queue (its

@@ -1,6 +1,9 @@
 """vkCmdDrawIndirect / vkCmdDrawIndexedIndirect: the same draws issued
 through indirect argument records give the same images as direct draws
-(the records are read from a host-visible buffer at replay)."""
+(the records are read from a host-visible buffer at replay), per draw and
+batched, also when the records change between submissions."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -29,3 +32,59 @@ def test_indirect_equals_direct(gpu_ctx, monkeypatch, config, params):
     assert np.array_equal(direct[0], indirect[0])
     if direct[1] is not None:
         assert np.array_equal(direct[1], indirect[1])
+
+
+def batch_raster_launches():
+    icd = ctypes.CDLL(c.ICD_PATH)
+    icd.cpv_profile_get.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_double)]
+    n, ms = ctypes.c_uint64(0), ctypes.c_double(0.0)
+    icd.cpv_profile_get(b"cpv_batch_raster", ctypes.byref(n), ctypes.byref(ms))
+    return n.value
+
+
+def test_batched_indirect_follows_record_changes(gpu_ctx, monkeypatch):
+    """A pass of 24 indirect draws runs batched, its records read at every
+    submission. Records rewritten between submissions (half the draws without
+    instances, one drawn from a later first index with fewer indices) rebuild
+    the batch: every image equals the per-draw path's under the same records,
+    and restoring the records restores the first image."""
+    monkeypatch.setenv("CPVH_INDIRECT", "1")
+    scene = c.Scene(c.BATCH, 6, [24, 3000, 320, 200])
+    original = [scene.indirect_record(i) for i in range(scene.draws)]
+    changed = [list(r) for r in original]
+    for k in range(0, scene.draws, 2):
+        changed[k][1] = 0
+    d = scene.draw(1)
+    changed[1][0] = (d.count // 3 // 2) * 3
+    changed[1][2] = d.first + (d.count // 3 - d.count // 3 // 2) * 3
+
+    def run(batched):
+        if batched:
+            monkeypatch.delenv("CPV_BATCH", raising=False)
+        else:
+            monkeypatch.setenv("CPV_BATCH", "0")
+        r = c.Renderer(gpu_ctx, scene)
+        try:
+            images = []
+            for records in (original, changed, original):
+                for i, rec in enumerate(records):
+                    r.set_indirect(i, rec)
+                r.render(2)
+                images.append(r.readback())
+            return images
+        finally:
+            r.close()
+
+    icd = ctypes.CDLL(c.ICD_PATH)
+    icd.cpv_profile_reset()
+    icd.cpv_profile_enable(1)
+    try:
+        batched = run(True)
+    finally:
+        icd.cpv_profile_enable(0)
+    assert batch_raster_launches() >= 6
+    plain = run(False)
+    for (bc, bd), (pc, pd) in zip(batched, plain):
+        assert np.array_equal(bc, pc) and np.array_equal(bd, pd)
+    assert not np.array_equal(batched[0][0], batched[1][0])
+    assert np.array_equal(batched[0][0], batched[2][0]) and np.array_equal(batched[0][1], batched[2][1])
