@@ -97,6 +97,8 @@ def harness():
     h.cpvh_renderer_update.argtypes = [vp]
     h.cpvh_renderer_set_indirect.restype = ctypes.c_int
     h.cpvh_renderer_set_indirect.argtypes = [vp, u32, vp]
+    h.cpvh_renderer_set_indirect_count.restype = ctypes.c_int
+    h.cpvh_renderer_set_indirect_count.argtypes = [vp, u32, u32]
     h.cpvh_readback.restype = ctypes.c_int
     h.cpvh_readback.argtypes = [vp, vp, vp]
     h.cpvh_queue.restype = vp
@@ -257,12 +259,20 @@ class Renderer:
 
     def set_indirect(self, draw, record):
         """Overwrites draw `draw`'s indirect record (renderers created with
-        CPVH_INDIRECT=1): [count, instances, first, vertex offset or first
+        CPVH_INDIRECT=1 or 2): [count, instances, first, vertex offset or first
         instance, first instance or 0]."""
         rec = (ctypes.c_uint32 * 5)(*[int(v) & 0xFFFFFFFF for v in (list(record) + [0] * 5)[:5]])
         r = harness().cpvh_renderer_set_indirect(self.ptr, draw, rec)
         if r != VK_SUCCESS:
             raise RuntimeError("set_indirect failed (%d)" % r)
+
+    def set_indirect_count(self, draw, count):
+        """Overwrites draw `draw`'s count word (renderers created with
+        CPVH_INDIRECT=2, where each draw is an indirect-count draw of at most
+        one record)."""
+        r = harness().cpvh_renderer_set_indirect_count(self.ptr, draw, count)
+        if r != VK_SUCCESS:
+            raise RuntimeError("set_indirect_count failed (%d)" % r)
 
     def readback(self):
         s = self.scene

@@ -86,6 +86,8 @@ struct Fns {
     CPVH_FN(vkCmdDrawIndexed)
     CPVH_FN(vkCmdDrawIndirect)
     CPVH_FN(vkCmdDrawIndexedIndirect)
+    CPVH_FN(vkCmdDrawIndirectCountKHR)
+    CPVH_FN(vkCmdDrawIndexedIndirectCountKHR)
     CPVH_FN(vkCmdCopyBuffer)
     CPVH_FN(vkCmdCopyBufferToImage)
     CPVH_FN(vkCmdCopyImageToBuffer)
@@ -171,7 +173,7 @@ struct ImageAlloc {
 struct cpvh_renderer {
     cpvh_context* ctx = nullptr;
     const cpv_scene* scene = nullptr;
-    BufferAlloc vertex, index, uniform, staging, readback, indirect;
+    BufferAlloc vertex, index, uniform, staging, readback, indirect, indirect_count;
     ImageAlloc colour, depth, texture;
     VkSampler sampler = nullptr;
     VkRenderPass pass = nullptr;
@@ -333,7 +335,11 @@ void record_frame(cpvh_renderer* r, VkCommandBuffer cmd) {
         }
         if (d.push_size) c->f.vkCmdPushConstants(cmd, r->layout, VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, 0, d.push_size, d.push);
         if (d.indexed) c->f.vkCmdBindIndexBuffer(cmd, r->index.buffer, d.index_offset, static_cast<VkIndexType>(s->index_type));
-        if (r->indirect.buffer) {
+        if (r->indirect_count.buffer) {
+            const VkDeviceSize at = static_cast<VkDeviceSize>(i) * 20, count_at = static_cast<VkDeviceSize>(i) * 4;
+            if (d.indexed) c->f.vkCmdDrawIndexedIndirectCountKHR(cmd, r->indirect.buffer, at, r->indirect_count.buffer, count_at, 1, 20);
+            else c->f.vkCmdDrawIndirectCountKHR(cmd, r->indirect.buffer, at, r->indirect_count.buffer, count_at, 1, 20);
+        } else if (r->indirect.buffer) {
             const VkDeviceSize at = static_cast<VkDeviceSize>(i) * 20;
             if (d.indexed) c->f.vkCmdDrawIndexedIndirect(cmd, r->indirect.buffer, at, 1, 20);
             else c->f.vkCmdDrawIndirect(cmd, r->indirect.buffer, at, 1, 20);
@@ -587,6 +593,9 @@ cpvh_context* cpvh_open(const char* icd_path, char* err, uint32_t err_len) {
     dci.sType = VK_STRUCTURE_TYPE_DEVICE_CREATE_INFO;
     dci.queueCreateInfoCount = 1;
     dci.pQueueCreateInfos = &qci;
+    const char* const device_extensions[] = {"VK_KHR_draw_indirect_count"};
+    dci.enabledExtensionCount = 1;
+    dci.ppEnabledExtensionNames = device_extensions;
     if (f.vkCreateDevice(c->physical, &dci, nullptr, &c->device) != VK_SUCCESS) return fail("vkCreateDevice failed:", c);
     if (!check_dispatch(c->device)) return fail("VkDevice lacks the loader magic", c);
 #define LOAD_D(name)                                                                     \
@@ -603,7 +612,7 @@ cpvh_context* cpvh_open(const char* icd_path, char* err, uint32_t err_len) {
     LOAD_D(vkDestroyFramebuffer); LOAD_D(vkCreateCommandPool); LOAD_D(vkDestroyCommandPool); LOAD_D(vkAllocateCommandBuffers);
     LOAD_D(vkBeginCommandBuffer); LOAD_D(vkEndCommandBuffer); LOAD_D(vkCmdBindPipeline); LOAD_D(vkCmdBindDescriptorSets);
     LOAD_D(vkCmdBindIndexBuffer); LOAD_D(vkCmdBindVertexBuffers); LOAD_D(vkCmdDraw); LOAD_D(vkCmdDrawIndexed); LOAD_D(vkCmdCopyBuffer);
-    LOAD_D(vkCmdDrawIndirect); LOAD_D(vkCmdDrawIndexedIndirect);
+    LOAD_D(vkCmdDrawIndirect); LOAD_D(vkCmdDrawIndexedIndirect); LOAD_D(vkCmdDrawIndirectCountKHR); LOAD_D(vkCmdDrawIndexedIndirectCountKHR);
     LOAD_D(vkCmdCopyBufferToImage); LOAD_D(vkCmdCopyImageToBuffer); LOAD_D(vkCmdPipelineBarrier); LOAD_D(vkCmdPushConstants);
     LOAD_D(vkCmdBlitImage);
     LOAD_D(vkCmdBeginRenderPass); LOAD_D(vkCmdEndRenderPass); LOAD_D(vkQueueSubmit); LOAD_D(vkQueueWaitIdle); LOAD_D(vkCreateFence);
@@ -669,8 +678,19 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
     if (make_buffer(c, rb_bytes, VK_BUFFER_USAGE_TRANSFER_DST_BIT, true, r->readback) != VK_SUCCESS) return fail("readback buffer");
     // CPVH_INDIRECT=1: the frame issues every draw as an indirect draw whose
     // record (VkDrawIndexedIndirectCommand / VkDrawIndirectCommand, 20-byte
-    // stride) lives in a host-visible buffer.
-    if (const char* ind = std::getenv("CPVH_INDIRECT"); ind && ind[0] == '1' && s->num_draws) {
+    // stride) lives in a host-visible buffer. CPVH_INDIRECT=2: as an
+    // indirect-count draw of at most one record, whose count word (one per
+    // draw, initially 1) lives in a second host-visible buffer.
+    const char* ind = std::getenv("CPVH_INDIRECT");
+    if (ind && ind[0] == '2' && s->num_draws) {
+        if (make_buffer(c, static_cast<VkDeviceSize>(s->num_draws) * 4, VK_BUFFER_USAGE_INDIRECT_BUFFER_BIT, true, r->indirect_count) != VK_SUCCESS)
+            return fail("indirect count buffer");
+        void* map = nullptr;
+        if (c->f.vkMapMemory(c->device, r->indirect_count.memory, 0, VK_WHOLE_SIZE, 0, &map) != VK_SUCCESS) return fail("indirect count map");
+        for (uint32_t i = 0; i < s->num_draws; i++) static_cast<uint32_t*>(map)[i] = 1u;
+        c->f.vkUnmapMemory(c->device, r->indirect_count.memory);
+    }
+    if (ind && (ind[0] == '1' || ind[0] == '2') && s->num_draws) {
         if (make_buffer(c, static_cast<VkDeviceSize>(s->num_draws) * 20, VK_BUFFER_USAGE_INDIRECT_BUFFER_BIT, true, r->indirect) != VK_SUCCESS)
             return fail("indirect buffer");
         void* map = nullptr;
@@ -900,6 +920,7 @@ void cpvh_renderer_destroy(cpvh_renderer* r) {
     destroy_buffer(c, r->staging);
     destroy_buffer(c, r->readback);
     destroy_buffer(c, r->indirect);
+    destroy_buffer(c, r->indirect_count);
     delete r;
 }
 
@@ -926,6 +947,16 @@ int cpvh_renderer_set_indirect(cpvh_renderer* r, uint32_t draw, const uint32_t r
     if (c->f.vkMapMemory(c->device, r->indirect.memory, static_cast<VkDeviceSize>(draw) * 20, 20, 0, &map) != VK_SUCCESS) return VK_ERROR_MEMORY_MAP_FAILED;
     std::memcpy(map, record, 20);
     c->f.vkUnmapMemory(c->device, r->indirect.memory);
+    return VK_SUCCESS;
+}
+
+int cpvh_renderer_set_indirect_count(cpvh_renderer* r, uint32_t draw, uint32_t count) {
+    cpvh_context* c = r->ctx;
+    if (!r->indirect_count.buffer || draw >= r->scene->num_draws) return VK_ERROR_INITIALIZATION_FAILED;
+    void* map = nullptr;
+    if (c->f.vkMapMemory(c->device, r->indirect_count.memory, static_cast<VkDeviceSize>(draw) * 4, 4, 0, &map) != VK_SUCCESS) return VK_ERROR_MEMORY_MAP_FAILED;
+    std::memcpy(map, &count, 4);
+    c->f.vkUnmapMemory(c->device, r->indirect_count.memory);
     return VK_SUCCESS;
 }
 

@@ -251,25 +251,39 @@ VkResult draw(Queue* q, State& s, uint32_t count, uint32_t instances, uint32_t f
 // the CPU and runs the draw. Here too the records are read on the host at
 // replay: from the pinned mirror of host-visible memory the device has not
 // written, else from HBM after the queue's earlier work has finished.
-VkResult read_indirect(Queue* q, const Cmd& c, const std::vector<DeviceMemory*>& written, std::vector<IndirectDraw>& out) {
-    out.clear();
-    const Buffer* b = static_cast<const Buffer*>(c.p[0]);
-    const bool indexed = c.type == CmdType::DrawIndexedIndirect;
-    const uint32_t n = c.u[0], stride = c.u[1], record = indexed ? 20u : 16u;
-    if (n == 0) return VK_SUCCESS;
-    if (!b || !b->memory) return VK_ERROR_DEVICE_LOST;
-    const uint64_t span = static_cast<uint64_t>(n - 1) * stride + record;
-    if (c.q[0] + span > b->size) return VK_ERROR_DEVICE_LOST;
-    std::vector<uint8_t> bytes(span);
+// `size` bytes of buffer `b` at `offset` as the queue's work up to now
+// leaves them: from the pinned mirror of host-visible memory the device has
+// not written, else from HBM after the queue's earlier work has finished.
+VkResult read_buffer(Queue* q, const Buffer* b, uint64_t offset, uint64_t size, const std::vector<DeviceMemory*>& written, uint8_t* out) {
+    if (!b || !b->memory || offset + size > b->size) return VK_ERROR_DEVICE_LOST;
     DeviceMemory* m = b->memory;
-    const uint64_t at = b->offset + c.q[0];
+    const uint64_t at = b->offset + offset;
     const bool device_newer = !m->host || m->device_dirty || std::find(written.begin(), written.end(), m) != written.end();
     if (!device_newer) {
-        std::memcpy(bytes.data(), m->host + at, span);
-    } else if (cudaStreamSynchronize(q->stream) != cudaSuccess || cudaMemcpy(bytes.data(), m->device + at, span, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        std::memcpy(out, m->host + at, size);
+    } else if (cudaStreamSynchronize(q->stream) != cudaSuccess || cudaMemcpy(out, m->device + at, size, cudaMemcpyDeviceToHost) != cudaSuccess) {
         cudaGetLastError();
         return VK_ERROR_DEVICE_LOST;
     }
+    return VK_SUCCESS;
+}
+
+VkResult read_indirect(Queue* q, const Cmd& c, const std::vector<DeviceMemory*>& written, std::vector<IndirectDraw>& out) {
+    out.clear();
+    const bool indexed = c.type == CmdType::DrawIndexedIndirect;
+    uint32_t n = c.u[0];
+    const uint32_t stride = c.u[1], record = indexed ? 20u : 16u;
+    if (c.p[1]) {  // an indirect-count draw: min(maxDrawCount, the count word)
+        uint32_t count = 0;
+        const VkResult r = read_buffer(q, static_cast<const Buffer*>(c.p[1]), c.q[1], 4, written, reinterpret_cast<uint8_t*>(&count));
+        if (r != VK_SUCCESS) return r;
+        n = std::min(n, count);
+    }
+    if (n == 0) return VK_SUCCESS;
+    const uint64_t span = static_cast<uint64_t>(n - 1) * stride + record;
+    std::vector<uint8_t> bytes(span);
+    const VkResult r = read_buffer(q, static_cast<const Buffer*>(c.p[0]), c.q[0], span, written, bytes.data());
+    if (r != VK_SUCCESS) return r;
     out.resize(n);
     for (uint32_t i = 0; i < n; i++) {
         uint32_t v[5] = {0, 0, 0, 0, 0};
@@ -374,7 +388,8 @@ ModuleConfig batch_config(const std::vector<Pipeline*>& pipelines) {
 // draw, where their tables exist (the 400k-triangle blend scene: 2.84 ms per
 // draw, 3.28 ms batched).
 // Indirect draws count as the draws their records hold (at recording, where
-// the records are not read yet, their primitives count as none).
+// the records are not read yet, as their maximum draw count, with no
+// primitives).
 struct PassCensus {
     Pipeline* bound = nullptr;
     size_t draws = 0;
@@ -383,11 +398,11 @@ struct PassCensus {
     void add(const Cmd& c, const std::vector<IndirectDraw>* records = nullptr) {
         if (c.type == CmdType::BindPipeline) bound = static_cast<Pipeline*>(c.p[0]);
         if (is_indirect(c)) {
-            draws += c.u[0];
+            draws += records ? records->size() : c.u[0];
             if (!bound) return;
             if (records)
                 for (const IndirectDraw& d : *records) prims += static_cast<uint64_t>(primitives_per_instance(bound->topology, d.count)) * d.instances;
-            blend_tables = blend_tables || (c.u[0] > 0 && bound->blend_table);
+            blend_tables = blend_tables || ((records ? !records->empty() : c.u[0] > 0) && bound->blend_table);
             return;
         }
         if (c.type != CmdType::Draw && c.type != CmdType::DrawIndexed) return;

@@ -255,16 +255,40 @@ VKAPI_ATTR void VKAPI_CALL GetPhysicalDeviceFormatProperties(VkPhysicalDevice, V
     }
 }
 
-VKAPI_ATTR VkResult VKAPI_CALL EnumerateDeviceExtensionProperties(VkPhysicalDevice, const char*, uint32_t* count, VkExtensionProperties*) {
-    *count = 0;
-    return VK_SUCCESS;
+// The device extensions (with their specification versions): the
+// indirect-count draws, as the reference registers them
+// (CPVulkan/Extensions.cpp:764-773, 1030-1038).
+const struct {
+    const char* name;
+    uint32_t version;
+} kDeviceExtensions[] = {{"VK_KHR_draw_indirect_count", 1}, {"VK_AMD_draw_indirect_count", 2}};
+
+VKAPI_ATTR VkResult VKAPI_CALL EnumerateDeviceExtensionProperties(VkPhysicalDevice, const char* layer, uint32_t* count, VkExtensionProperties* props) {
+    if (!count) return VK_INCOMPLETE;
+    const uint32_t n = layer ? 0u : static_cast<uint32_t>(sizeof(kDeviceExtensions) / sizeof(kDeviceExtensions[0]));
+    if (!props) {
+        *count = n;
+        return VK_SUCCESS;
+    }
+    const uint32_t written = std::min(*count, n);
+    for (uint32_t i = 0; i < written; i++) {
+        std::memset(&props[i], 0, sizeof(props[i]));
+        std::strncpy(props[i].extensionName, kDeviceExtensions[i].name, VK_MAX_EXTENSION_NAME_SIZE - 1);
+        props[i].specVersion = kDeviceExtensions[i].version;
+    }
+    *count = written;
+    return written < n ? VK_INCOMPLETE : VK_SUCCESS;
 }
 
 // ------------------------------------------------------------------ device --
 
 VKAPI_ATTR VkResult VKAPI_CALL CreateDevice(VkPhysicalDevice pd, const VkDeviceCreateInfo* ci, const VkAllocationCallbacks*, VkDevice* out) {
     if (!ci || !out) return VK_ERROR_INITIALIZATION_FAILED;
-    if (ci->enabledExtensionCount) return VK_ERROR_EXTENSION_NOT_PRESENT;
+    for (uint32_t i = 0; i < ci->enabledExtensionCount; i++) {
+        bool known = false;
+        for (const auto& e : kDeviceExtensions) known = known || (ci->ppEnabledExtensionNames[i] && std::strcmp(ci->ppEnabledExtensionNames[i], e.name) == 0);
+        if (!known) return VK_ERROR_EXTENSION_NOT_PRESENT;
+    }
     std::string err;
     const char* co = std::getenv("CPV_COMPILE_ONLY");
     const bool compile_only = co && co[0] == '1';
@@ -928,6 +952,23 @@ VKAPI_ATTR void VKAPI_CALL CmdDrawIndexedIndirect(VkCommandBuffer cmd, VkBuffer 
     c.u[0] = n;
     c.u[1] = stride;
 }
+// vkCmdDraw(Indexed)IndirectCountKHR / vkCmdDrawIndirectCountAMD
+// (CPVulkan/CommandBuffer.Draw.cpp:2226-2348, 2421-2433): the draw count is
+// min(maxDrawCount, the 32-bit word at countBufferOffset), read at replay.
+VKAPI_ATTR void VKAPI_CALL CmdDrawIndirectCount(VkCommandBuffer cmd, VkBuffer b, VkDeviceSize off, VkBuffer count_buffer, VkDeviceSize count_off,
+                                                uint32_t max_draws, uint32_t stride) {
+    CmdDrawIndirect(cmd, b, off, max_draws, stride);
+    auto& c = reinterpret_cast<CommandBuffer*>(cmd)->cmds.back();
+    c.p[1] = reinterpret_cast<void*>(count_buffer);
+    c.q[1] = count_off;
+}
+VKAPI_ATTR void VKAPI_CALL CmdDrawIndexedIndirectCount(VkCommandBuffer cmd, VkBuffer b, VkDeviceSize off, VkBuffer count_buffer, VkDeviceSize count_off,
+                                                       uint32_t max_draws, uint32_t stride) {
+    CmdDrawIndexedIndirect(cmd, b, off, max_draws, stride);
+    auto& c = reinterpret_cast<CommandBuffer*>(cmd)->cmds.back();
+    c.p[1] = reinterpret_cast<void*>(count_buffer);
+    c.q[1] = count_off;
+}
 VKAPI_ATTR void VKAPI_CALL CmdCopyBuffer(VkCommandBuffer cmd, VkBuffer src, VkBuffer dst, uint32_t n, const VkBufferCopy* r) {
     auto& c = push(cmd, CmdType::CopyBuffer);
     c.p[0] = reinterpret_cast<void*>(src);
@@ -1160,7 +1201,10 @@ const Entry kDevice[] = {
     E(DestroyRenderPass), E(CreateFramebuffer), E(DestroyFramebuffer), E(CreateCommandPool), E(DestroyCommandPool), E(ResetCommandPool),
     E(AllocateCommandBuffers), E(FreeCommandBuffers), E(BeginCommandBuffer), E(EndCommandBuffer), E(ResetCommandBuffer), E(CmdBindPipeline),
     E(CmdSetViewport), E(CmdSetScissor), E(CmdSetBlendConstants), E(CmdBindDescriptorSets), E(CmdBindIndexBuffer), E(CmdBindVertexBuffers),
-    E(CmdDraw), E(CmdDrawIndexed), E(CmdDrawIndirect), E(CmdDrawIndexedIndirect), E(CmdCopyBuffer), E(CmdCopyBufferToImage), E(CmdBlitImage),
+    E(CmdDraw), E(CmdDrawIndexed), E(CmdDrawIndirect), E(CmdDrawIndexedIndirect),
+    {"vkCmdDrawIndirectCountKHR", reinterpret_cast<PFN_vkVoidFunction>(CmdDrawIndirectCount)},
+    {"vkCmdDrawIndexedIndirectCountKHR", reinterpret_cast<PFN_vkVoidFunction>(CmdDrawIndexedIndirectCount)},
+    {"vkCmdDrawIndirectCountAMD", reinterpret_cast<PFN_vkVoidFunction>(CmdDrawIndirectCount)}, E(CmdCopyBuffer), E(CmdCopyBufferToImage), E(CmdBlitImage),
     E(CmdCopyImageToBuffer), E(CmdFillBuffer), E(CmdUpdateBuffer), E(CmdPipelineBarrier), E(CmdPushConstants), E(CmdBeginRenderPass),
     E(CmdEndRenderPass), E(QueueSubmit), E(CreateFence), E(DestroyFence), E(ResetFences), E(GetFenceStatus), E(WaitForFences),
     E(CreateSemaphore), E(DestroySemaphore),

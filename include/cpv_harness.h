@@ -76,11 +76,16 @@ int cpvh_compile_pipelines(cpvh_context* ctx, const cpv_scene* scene, char* err,
  * cpvh_scene_set_frame) and re-records the frame. */
 int cpvh_renderer_update(cpvh_renderer* r);
 
-/* With CPVH_INDIRECT=1 at creation: overwrites draw `draw`'s indirect record
+/* With CPVH_INDIRECT=1 or 2 at creation: overwrites draw `draw`'s indirect record
  * (5 words; a non-indexed draw uses the first 4) through vkMapMemory /
  * vkUnmapMemory, without re-recording; the next frame reads it. Returns a
  * VkResult (VK_ERROR_INITIALIZATION_FAILED without indirect records). */
 int cpvh_renderer_set_indirect(cpvh_renderer* r, uint32_t draw, const uint32_t record[5]);
+
+/* With CPVH_INDIRECT=2 at creation (each draw an indirect-count draw of at
+ * most one record): overwrites draw `draw`'s count word; 0 skips the draw,
+ * any larger value draws its one record. Returns a VkResult. */
+int cpvh_renderer_set_indirect_count(cpvh_renderer* r, uint32_t draw, uint32_t count);
 
 /* Reads the attachments back (colour: width*height*4; depth: texel-sized). */
 int cpvh_readback(cpvh_renderer* r, uint8_t* color, uint8_t* depth);

@@ -103,3 +103,30 @@ def test_gpu_path_has_no_cpu_fallback(native):
         ctx.close()
     finally:
         del os.environ["CPV_COMPILE_ONLY"]
+
+
+def test_indirect_count_extension(native):
+    """VK_KHR_draw_indirect_count and VK_AMD_draw_indirect_count are listed
+    and their draw commands resolve under the reference's names
+    (CPVulkan/Extensions.cpp:764-773, 1030-1038). Instance-level lookups take
+    a non-null instance; the ICD's tables do not dereference it."""
+    lib = ctypes.CDLL(c.ICD_PATH)
+    gipa = lib.vk_icdGetInstanceProcAddr
+    gipa.restype = ctypes.c_void_p
+    gipa.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+    instance = ctypes.c_void_p(16)
+    for name in (b"vkCmdDrawIndirectCountKHR", b"vkCmdDrawIndexedIndirectCountKHR", b"vkCmdDrawIndirectCountAMD"):
+        assert gipa(instance, name), name
+    enum = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint32), ctypes.c_void_p)(
+        gipa(instance, b"vkEnumerateDeviceExtensionProperties"))
+    n = ctypes.c_uint32(0)
+    assert enum(None, None, ctypes.byref(n), None) == 0 and n.value == 2
+
+    class Props(ctypes.Structure):
+        _fields_ = [("name", ctypes.c_char * 256), ("version", ctypes.c_uint32)]
+
+    props = (Props * 2)()
+    one = ctypes.c_uint32(1)
+    assert enum(None, None, ctypes.byref(one), props) == 5 and one.value == 1  # VK_INCOMPLETE
+    assert enum(None, None, ctypes.byref(n), props) == 0
+    assert {(p.name, p.version) for p in props} == {(b"VK_KHR_draw_indirect_count", 1), (b"VK_AMD_draw_indirect_count", 2)}

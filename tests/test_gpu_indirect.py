@@ -21,13 +21,14 @@ def render(ctx, scene, frames=2):
         r.close()
 
 
+@pytest.mark.parametrize("mode", ["1", "2"])  # indirect, indirect-count draws
 @pytest.mark.parametrize("config,params", [(c.CUBE, [20]), (c.BATCH, [24, 3000, 320, 200]), (c.HEIGHTFIELD, [64, 256, 160]),
                                            (c.PROGRAM, [c.PROGRAM_CUBE, 0x400 | 0x10, 64, 48, 24]),
                                            (c.PROGRAM, [c.PROGRAM_MESHPC, 0x10 | 0x20, 64, 48, 24])])
-def test_indirect_equals_direct(gpu_ctx, monkeypatch, config, params):
+def test_indirect_equals_direct(gpu_ctx, monkeypatch, config, params, mode):
     scene = c.Scene(config, 6, params)
     direct = render(gpu_ctx, scene)
-    monkeypatch.setenv("CPVH_INDIRECT", "1")
+    monkeypatch.setenv("CPVH_INDIRECT", mode)
     indirect = render(gpu_ctx, scene)
     assert np.array_equal(direct[0], indirect[0])
     if direct[1] is not None:
@@ -88,3 +89,43 @@ def test_batched_indirect_follows_record_changes(gpu_ctx, monkeypatch):
         assert np.array_equal(bc, pc) and np.array_equal(bd, pd)
     assert not np.array_equal(batched[0][0], batched[1][0])
     assert np.array_equal(batched[0][0], batched[2][0]) and np.array_equal(batched[0][1], batched[2][1])
+
+
+@pytest.mark.parametrize("batched", [True, False])
+def test_indirect_count_words(gpu_ctx, monkeypatch, batched):
+    """vkCmdDraw(Indexed)IndirectCountKHR (CPVulkan/CommandBuffer.Draw.cpp:
+    2226-2348): each draw is at most one record, drawn min(maxDrawCount = 1,
+    count word) times. Count words of 0 skip their draws, words above 1 are
+    clamped to 1: the image equals the indirect path's with those draws
+    given no instances, batched and per draw."""
+    if not batched:
+        monkeypatch.setenv("CPV_BATCH", "0")
+    scene = c.Scene(c.BATCH, 7, [30, 3000, 320, 200])
+    skip = set(range(1, scene.draws, 3))  # 20 draws remain: the pass still batches
+    monkeypatch.setenv("CPVH_INDIRECT", "2")
+    r = c.Renderer(gpu_ctx, scene)
+    icd = ctypes.CDLL(c.ICD_PATH)
+    icd.cpv_profile_reset()
+    icd.cpv_profile_enable(1)
+    try:
+        for i in range(scene.draws):
+            r.set_indirect_count(i, 0 if i in skip else (7 if i % 2 else 1))
+        r.render(2)
+        got = r.readback()
+    finally:
+        icd.cpv_profile_enable(0)
+        r.close()
+    assert (batch_raster_launches() >= 2) == batched
+    monkeypatch.setenv("CPVH_INDIRECT", "1")
+    r = c.Renderer(gpu_ctx, scene)
+    try:
+        for i in skip:
+            rec = scene.indirect_record(i)
+            rec[1] = 0
+            r.set_indirect(i, rec)
+        r.render(2)
+        want = r.readback()
+    finally:
+        r.close()
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+    assert not np.array_equal(got[0], render(gpu_ctx, scene)[0])
