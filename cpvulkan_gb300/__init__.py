@@ -104,6 +104,8 @@ def harness():
     h.cpvh_queue.restype = vp
     h.cpvh_queue.argtypes = [vp]
     h.cpvh_last_error.restype = cp
+    h.cpvh_image_ops.restype = ctypes.c_int
+    h.cpvh_image_ops.argtypes = [vp, u32, u32, u32, u32, vp, vp, vp, u32, vp, cp, u32]
     h.cpvh_blit.restype = ctypes.c_int
     h.cpvh_blit.argtypes = [vp, vp, u32, u32, u32, u32, vp, u32, u32, u32, u32, vp, u32, u32, cp, u32]
     h.cpvh_server_create.restype = vp
@@ -178,6 +180,17 @@ class Scene:
             pass
 
 
+OP_CLEAR_COLOR_IMAGE, OP_CLEAR_DEPTH_STENCIL_IMAGE, OP_COPY_IMAGE, OP_CLEAR_ATTACHMENTS = 0, 1, 2, 3
+
+
+class ImageOp(ctypes.Structure):
+    """cpvh_image_op (include/cpv_harness.h)."""
+    u32, i32 = ctypes.c_uint32, ctypes.c_int32
+    _fields_ = [("kind", u32), ("aspect", u32), ("level", u32), ("level_count", u32), ("src_level", u32), ("x", i32), ("y", i32),
+                ("src_x", i32), ("src_y", i32), ("w", u32), ("h", u32), ("colour", ctypes.c_float * 4), ("depth", ctypes.c_float),
+                ("stencil", u32)]
+
+
 class Context:
     """An ICD loaded the loader's way, with one device and queue."""
 
@@ -212,6 +225,30 @@ class Context:
                                 filter, err, len(err))
         if r != VK_SUCCESS:
             raise RuntimeError("blit failed (%d): %s" % (r, err.value.decode(errors="replace")))
+
+    def image_ops(self, format, size, levels, init0, ops, init1=None):
+        """vkCmdClearColorImage / vkCmdClearDepthStencilImage /
+        vkCmdCopyImage / vkCmdClearAttachments on image 0 of two images of
+        `format` given as packed mip chains (uint8 numpy arrays in the ICD's
+        texel layout); ops: dicts of ImageOp fields. Returns image 0's bytes."""
+        import numpy as np
+
+        arr = (ImageOp * max(1, len(ops)))()
+        for i, op in enumerate(ops):
+            for k, v in op.items():
+                if k == "colour":
+                    arr[i].colour[:] = list(v)
+                else:
+                    setattr(arr[i], k, v)
+        init0 = np.ascontiguousarray(init0, dtype=np.uint8)
+        init1 = None if init1 is None else np.ascontiguousarray(init1, dtype=np.uint8)
+        out = np.zeros_like(init0)
+        err = ctypes.create_string_buffer(1024)
+        r = harness().cpvh_image_ops(self.ptr, format, size[0], size[1], levels, init0.ctypes.data,
+                                     init1.ctypes.data if init1 is not None else None, arr, len(ops), out.ctypes.data, err, len(err))
+        if r != VK_SUCCESS:
+            raise RuntimeError("image ops failed (%d): %s" % (r, err.value.decode(errors="replace")))
+        return out
 
     @property
     def queue(self):

@@ -92,6 +92,10 @@ struct Fns {
     CPVH_FN(vkCmdCopyBufferToImage)
     CPVH_FN(vkCmdCopyImageToBuffer)
     CPVH_FN(vkCmdBlitImage)
+    CPVH_FN(vkCmdCopyImage)
+    CPVH_FN(vkCmdClearColorImage)
+    CPVH_FN(vkCmdClearDepthStencilImage)
+    CPVH_FN(vkCmdClearAttachments)
     CPVH_FN(vkCmdPipelineBarrier)
     CPVH_FN(vkCmdPushConstants)
     CPVH_FN(vkCmdBeginRenderPass)
@@ -614,7 +618,7 @@ cpvh_context* cpvh_open(const char* icd_path, char* err, uint32_t err_len) {
     LOAD_D(vkCmdBindIndexBuffer); LOAD_D(vkCmdBindVertexBuffers); LOAD_D(vkCmdDraw); LOAD_D(vkCmdDrawIndexed); LOAD_D(vkCmdCopyBuffer);
     LOAD_D(vkCmdDrawIndirect); LOAD_D(vkCmdDrawIndexedIndirect); LOAD_D(vkCmdDrawIndirectCountKHR); LOAD_D(vkCmdDrawIndexedIndirectCountKHR);
     LOAD_D(vkCmdCopyBufferToImage); LOAD_D(vkCmdCopyImageToBuffer); LOAD_D(vkCmdPipelineBarrier); LOAD_D(vkCmdPushConstants);
-    LOAD_D(vkCmdBlitImage);
+    LOAD_D(vkCmdBlitImage); LOAD_D(vkCmdCopyImage); LOAD_D(vkCmdClearColorImage); LOAD_D(vkCmdClearDepthStencilImage); LOAD_D(vkCmdClearAttachments);
     LOAD_D(vkCmdBeginRenderPass); LOAD_D(vkCmdEndRenderPass); LOAD_D(vkQueueSubmit); LOAD_D(vkQueueWaitIdle); LOAD_D(vkCreateFence);
     LOAD_D(vkDestroyFence); LOAD_D(vkResetFences); LOAD_D(vkWaitForFences); LOAD_D(vkGetFenceStatus);
 #undef LOAD_D
@@ -1204,6 +1208,206 @@ int cpvh_blit(cpvh_context* c, uint8_t* src, uint32_t src_w, uint32_t src_h, uin
     f.vkUnmapMemory(c->device, staging.memory);
     cleanup();
     return rc;
+}
+
+int cpvh_image_ops(cpvh_context* c, uint32_t format, uint32_t width, uint32_t height, uint32_t levels, const uint8_t* init0, const uint8_t* init1,
+                   const cpvh_image_op* ops, uint32_t op_count, uint8_t* out, char* err, uint32_t err_len) {
+    const Fns& f = c->f;
+    const bool depth = depth_texel_size(format) != 0;
+    const uint32_t texel = depth ? depth_texel_size(format) : 4u;
+    const VkImageAspectFlags view_aspect = depth ? (format == VK_FORMAT_D32_SFLOAT_S8_UINT ? VK_IMAGE_ASPECT_DEPTH_BIT | VK_IMAGE_ASPECT_STENCIL_BIT
+                                                                                             : VK_IMAGE_ASPECT_DEPTH_BIT)
+                                                 : VK_IMAGE_ASPECT_COLOR_BIT;
+    uint64_t offset[16] = {}, bytes = 0;
+    uint32_t lw[16] = {}, lh[16] = {};
+    ImageAlloc img[2];
+    BufferAlloc staging;
+    std::vector<VkImageView> views;
+    std::vector<VkFramebuffer> fbs;
+    VkRenderPass pass = nullptr;
+    VkCommandPool pool = nullptr;
+    VkFence fence = nullptr;
+    auto cleanup = [&]() {
+        if (fence) f.vkDestroyFence(c->device, fence, nullptr);
+        if (pool) f.vkDestroyCommandPool(c->device, pool, nullptr);
+        for (VkFramebuffer fb : fbs) f.vkDestroyFramebuffer(c->device, fb, nullptr);
+        for (VkImageView v : views) f.vkDestroyImageView(c->device, v, nullptr);
+        if (pass) f.vkDestroyRenderPass(c->device, pass, nullptr);
+        destroy_buffer(c, staging);
+        destroy_image(c, img[1]);
+        destroy_image(c, img[0]);
+    };
+    auto fail = [&](const std::string& e, int code) {
+        g_err = e + " " + icd_error(c);
+        if (err && err_len) std::snprintf(err, err_len, "%s", g_err.c_str());
+        cleanup();
+        return code;
+    };
+    if (!init0 || !out || levels == 0 || levels > 16 || width == 0 || height == 0) return fail("image_ops: bad image description", VK_ERROR_INITIALIZATION_FAILED);
+    for (uint32_t l = 0, w = width, h = height; l < levels; l++) {
+        offset[l] = bytes;
+        lw[l] = w;
+        lh[l] = h;
+        bytes += static_cast<uint64_t>(w) * h * texel;
+        w = w > 1 ? w / 2 : 1;
+        h = h > 1 ? h / 2 : 1;
+    }
+    const VkImageUsageFlags usage = VK_IMAGE_USAGE_TRANSFER_SRC_BIT | VK_IMAGE_USAGE_TRANSFER_DST_BIT |
+                                    (depth ? VK_IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT_BIT : VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT);
+    for (int k = 0; k < 2; k++)
+        if (make_image(c, static_cast<VkFormat>(format), width, height, levels, usage, view_aspect, img[k]) != VK_SUCCESS)
+            return fail("image_ops: image", VK_ERROR_OUT_OF_DEVICE_MEMORY);
+    if (make_buffer(c, 2 * bytes, VK_BUFFER_USAGE_TRANSFER_SRC_BIT | VK_BUFFER_USAGE_TRANSFER_DST_BIT, true, staging) != VK_SUCCESS)
+        return fail("image_ops: staging buffer", VK_ERROR_OUT_OF_DEVICE_MEMORY);
+    void* map = nullptr;
+    if (f.vkMapMemory(c->device, staging.memory, 0, VK_WHOLE_SIZE, 0, &map) != VK_SUCCESS) return fail("image_ops: map", VK_ERROR_MEMORY_MAP_FAILED);
+    std::memcpy(map, init0, bytes);
+    if (init1) std::memcpy(static_cast<uint8_t*>(map) + bytes, init1, bytes);
+    else std::memset(static_cast<uint8_t*>(map) + bytes, 0, bytes);
+    f.vkUnmapMemory(c->device, staging.memory);
+
+    // a LOAD / STORE render pass over one attachment, for vkCmdClearAttachments
+    VkAttachmentDescription att{};
+    att.format = static_cast<VkFormat>(format);
+    att.samples = VK_SAMPLE_COUNT_1_BIT;
+    att.loadOp = VK_ATTACHMENT_LOAD_OP_LOAD;
+    att.storeOp = VK_ATTACHMENT_STORE_OP_STORE;
+    att.stencilLoadOp = VK_ATTACHMENT_LOAD_OP_LOAD;
+    att.stencilStoreOp = VK_ATTACHMENT_STORE_OP_STORE;
+    att.finalLayout = VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL;
+    VkAttachmentReference ref{0, depth ? VK_IMAGE_LAYOUT_DEPTH_STENCIL_ATTACHMENT_OPTIMAL : VK_IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL};
+    VkSubpassDescription sub{};
+    sub.colorAttachmentCount = depth ? 0 : 1;
+    sub.pColorAttachments = depth ? nullptr : &ref;
+    sub.pDepthStencilAttachment = depth ? &ref : nullptr;
+    VkRenderPassCreateInfo rpi{};
+    rpi.sType = VK_STRUCTURE_TYPE_RENDER_PASS_CREATE_INFO;
+    rpi.attachmentCount = 1;
+    rpi.pAttachments = &att;
+    rpi.subpassCount = 1;
+    rpi.pSubpasses = &sub;
+    if (f.vkCreateRenderPass(c->device, &rpi, nullptr, &pass) != VK_SUCCESS) return fail("image_ops: render pass", VK_ERROR_INITIALIZATION_FAILED);
+
+    VkCommandPoolCreateInfo cpi{};
+    cpi.sType = VK_STRUCTURE_TYPE_COMMAND_POOL_CREATE_INFO;
+    if (f.vkCreateCommandPool(c->device, &cpi, nullptr, &pool) != VK_SUCCESS) return fail("image_ops: command pool", VK_ERROR_INITIALIZATION_FAILED);
+    VkCommandBufferAllocateInfo cai{};
+    cai.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_ALLOCATE_INFO;
+    cai.commandPool = pool;
+    cai.level = VK_COMMAND_BUFFER_LEVEL_PRIMARY;
+    cai.commandBufferCount = 1;
+    VkCommandBuffer cmd = nullptr;
+    if (f.vkAllocateCommandBuffers(c->device, &cai, &cmd) != VK_SUCCESS || !check_dispatch(cmd))
+        return fail("image_ops: command buffer", VK_ERROR_INITIALIZATION_FAILED);
+    VkFenceCreateInfo fci{};
+    fci.sType = VK_STRUCTURE_TYPE_FENCE_CREATE_INFO;
+    if (f.vkCreateFence(c->device, &fci, nullptr, &fence) != VK_SUCCESS) return fail("image_ops: fence", VK_ERROR_INITIALIZATION_FAILED);
+
+    VkMemoryBarrier mb{};
+    mb.sType = VK_STRUCTURE_TYPE_MEMORY_BARRIER;
+    mb.srcAccessMask = VK_ACCESS_TRANSFER_WRITE_BIT;
+    mb.dstAccessMask = VK_ACCESS_TRANSFER_READ_BIT | VK_ACCESS_TRANSFER_WRITE_BIT;
+    auto barrier = [&]() { f.vkCmdPipelineBarrier(cmd, VK_PIPELINE_STAGE_ALL_COMMANDS_BIT, VK_PIPELINE_STAGE_ALL_COMMANDS_BIT, 0, 1, &mb, 0, nullptr, 0, nullptr); };
+    auto level_copy = [&](uint64_t base, uint32_t l) {
+        VkBufferImageCopy bc{};
+        bc.bufferOffset = base + offset[l];
+        bc.imageSubresource = {view_aspect, l, 0, 1};
+        bc.imageExtent = {lw[l], lh[l], 1};
+        return bc;
+    };
+    VkCommandBufferBeginInfo bi{};
+    bi.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_BEGIN_INFO;
+    f.vkBeginCommandBuffer(cmd, &bi);
+    for (int k = 0; k < 2; k++)
+        for (uint32_t l = 0; l < levels; l++) {
+            const VkBufferImageCopy bc = level_copy(k * bytes, l);
+            f.vkCmdCopyBufferToImage(cmd, staging.buffer, img[k].image, VK_IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL, 1, &bc);
+        }
+    barrier();
+    for (uint32_t i = 0; i < op_count; i++) {
+        const cpvh_image_op& op = ops[i];
+        const VkImageSubresourceRange range{op.aspect, op.level, op.level_count, 0, 1};
+        switch (op.kind) {
+        case CPVH_OP_CLEAR_COLOR_IMAGE: {
+            VkClearColorValue v;
+            std::memcpy(v.float32, op.colour, sizeof(v.float32));
+            f.vkCmdClearColorImage(cmd, img[0].image, VK_IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL, &v, 1, &range);
+            break;
+        }
+        case CPVH_OP_CLEAR_DEPTH_STENCIL_IMAGE: {
+            const VkClearDepthStencilValue v{op.depth, op.stencil};
+            f.vkCmdClearDepthStencilImage(cmd, img[0].image, VK_IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL, &v, 1, &range);
+            break;
+        }
+        case CPVH_OP_COPY_IMAGE: {
+            VkImageCopy rc{};
+            rc.srcSubresource = {view_aspect, op.src_level, 0, 1};
+            rc.srcOffset = {op.src_x, op.src_y, 0};
+            rc.dstSubresource = {view_aspect, op.level, 0, 1};
+            rc.dstOffset = {op.x, op.y, 0};
+            rc.extent = {op.w, op.h, 1};
+            f.vkCmdCopyImage(cmd, img[1].image, VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL, img[0].image, VK_IMAGE_LAYOUT_TRANSFER_DST_OPTIMAL, 1, &rc);
+            break;
+        }
+        case CPVH_OP_CLEAR_ATTACHMENTS: {
+            if (op.level >= levels) return fail("image_ops: level", VK_ERROR_INITIALIZATION_FAILED);
+            VkImageViewCreateInfo vi{};
+            vi.sType = VK_STRUCTURE_TYPE_IMAGE_VIEW_CREATE_INFO;
+            vi.image = img[0].image;
+            vi.viewType = VK_IMAGE_VIEW_TYPE_2D;
+            vi.format = static_cast<VkFormat>(format);
+            vi.subresourceRange = {view_aspect, op.level, 1, 0, 1};
+            VkImageView view = nullptr;
+            if (f.vkCreateImageView(c->device, &vi, nullptr, &view) != VK_SUCCESS) return fail("image_ops: view", VK_ERROR_INITIALIZATION_FAILED);
+            views.push_back(view);
+            VkFramebufferCreateInfo fbi{};
+            fbi.sType = VK_STRUCTURE_TYPE_FRAMEBUFFER_CREATE_INFO;
+            fbi.renderPass = pass;
+            fbi.attachmentCount = 1;
+            fbi.pAttachments = &view;
+            fbi.width = lw[op.level];
+            fbi.height = lh[op.level];
+            fbi.layers = 1;
+            VkFramebuffer fb = nullptr;
+            if (f.vkCreateFramebuffer(c->device, &fbi, nullptr, &fb) != VK_SUCCESS) return fail("image_ops: framebuffer", VK_ERROR_INITIALIZATION_FAILED);
+            fbs.push_back(fb);
+            VkRenderPassBeginInfo rb{};
+            rb.sType = VK_STRUCTURE_TYPE_RENDER_PASS_BEGIN_INFO;
+            rb.renderPass = pass;
+            rb.framebuffer = fb;
+            rb.renderArea = {{0, 0}, {lw[op.level], lh[op.level]}};
+            f.vkCmdBeginRenderPass(cmd, &rb, VK_SUBPASS_CONTENTS_INLINE);
+            VkClearAttachment ca{};
+            ca.aspectMask = op.aspect;
+            ca.colorAttachment = 0;
+            if (depth) ca.clearValue.depthStencil = {op.depth, op.stencil};
+            else std::memcpy(ca.clearValue.color.float32, op.colour, sizeof(op.colour));
+            const VkClearRect rect{{{op.x, op.y}, {op.w, op.h}}, 0, 1};
+            f.vkCmdClearAttachments(cmd, 1, &ca, 1, &rect);
+            f.vkCmdEndRenderPass(cmd);
+            break;
+        }
+        default: return fail("image_ops: unknown operation", VK_ERROR_INITIALIZATION_FAILED);
+        }
+        barrier();
+    }
+    for (uint32_t l = 0; l < levels; l++) {
+        const VkBufferImageCopy bc = level_copy(0, l);
+        f.vkCmdCopyImageToBuffer(cmd, img[0].image, VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL, staging.buffer, 1, &bc);
+    }
+    f.vkEndCommandBuffer(cmd);
+    VkSubmitInfo si{};
+    si.sType = VK_STRUCTURE_TYPE_SUBMIT_INFO;
+    si.commandBufferCount = 1;
+    si.pCommandBuffers = &cmd;
+    VkResult res = f.vkQueueSubmit(c->queue, 1, &si, fence);
+    if (res == VK_SUCCESS) res = f.vkWaitForFences(c->device, 1, &fence, VK_TRUE, ~0ull);
+    if (res != VK_SUCCESS) return fail("image_ops: submit", res);
+    if (f.vkMapMemory(c->device, staging.memory, 0, VK_WHOLE_SIZE, 0, &map) != VK_SUCCESS) return fail("image_ops: map", VK_ERROR_MEMORY_MAP_FAILED);
+    std::memcpy(out, map, bytes);
+    f.vkUnmapMemory(c->device, staging.memory);
+    cleanup();
+    return VK_SUCCESS;
 }
 
 }  // extern "C"

@@ -118,6 +118,58 @@ uint8_t* view_base(const ImageView* v, uint32_t& width, uint32_t& height) {
     return img->device_ptr() + static_cast<uint64_t>(v->range.baseArrayLayer) * img->layer_size + img->level[level].offset;
 }
 
+// The texel a clear value encodes to in `fmt`: colour through the UNORM8
+// encoder in the format's byte order, D16 quantised, D32 as its bits, the
+// stencil byte in the second word of a D32S8 texel (ClearImage → SetPixel,
+// CPVulkan/CommandBuffer.Draw.cpp:117-149, 2398-2419). False for a format
+// without a clear encoding here.
+bool clear_texel(VkFormat fmt, const VkClearValue& cv, uint32_t& lo, uint32_t& hi) {
+    lo = hi = 0;
+    switch (fmt) {
+    case VK_FORMAT_R8G8B8A8_UNORM:
+    case VK_FORMAT_B8G8R8A8_UNORM: {
+        const int shift_bgra[4] = {16, 8, 0, 24};
+        for (int ch = 0; ch < 4; ch++) {
+            const uint32_t b = encode_unorm_host(cv.color.float32[ch], 255.0f);
+            lo |= b << (fmt == VK_FORMAT_B8G8R8A8_UNORM ? shift_bgra[ch] : 8 * ch);
+        }
+        return true;
+    }
+    case VK_FORMAT_D16_UNORM: lo = encode_unorm_host(cv.depthStencil.depth, 65535.0f); return true;
+    case VK_FORMAT_D32_SFLOAT: std::memcpy(&lo, &cv.depthStencil.depth, 4); return true;
+    case VK_FORMAT_D32_SFLOAT_S8_UINT:
+        std::memcpy(&lo, &cv.depthStencil.depth, 4);
+        hi = cv.depthStencil.stencil & 0xFFu;
+        return true;
+    default: return false;
+    }
+}
+
+// Fills a rectangle of one layer and level of `img` with a clear value, in
+// the aspects `aspects` selects (Vulkan: a clear writes only the aspects it
+// names; the reference writes both, CPVulkan/CommandBuffer.Draw.cpp:2201-2203).
+VkResult clear_rect(Queue* q, Image* img, uint32_t layer, uint32_t level, VkImageAspectFlags aspects, const VkClearValue& cv, int32_t x0, int32_t y0,
+                    uint32_t w, uint32_t h) {
+    if (!img || !img->memory || level >= img->levels || layer >= img->layers) return VK_ERROR_DEVICE_LOST;
+    const ImageLevel& L = img->level[level];
+    // the rectangle within the level
+    const int64_t x1 = std::min<int64_t>(static_cast<int64_t>(x0) + w, L.width), y1 = std::min<int64_t>(static_cast<int64_t>(y0) + h, static_cast<int64_t>(L.height) * std::max(1u, L.depth));
+    x0 = std::max(x0, 0);
+    y0 = std::max(y0, 0);
+    if (x1 <= x0 || y1 <= y0) return VK_SUCCESS;
+    uint32_t lo, hi;
+    if (!clear_texel(img->format, cv, lo, hi)) return VK_ERROR_DEVICE_LOST;
+    const bool depth = format_is_depth(img->format);
+    const bool write_lo = !depth || (aspects & VK_IMAGE_ASPECT_DEPTH_BIT) != 0;
+    const bool write_hi = depth && (aspects & VK_IMAGE_ASPECT_STENCIL_BIT) != 0;
+    if (!write_lo && (img->texel != 8 || !write_hi)) return VK_SUCCESS;
+    uint8_t* base = img->device_ptr() + static_cast<uint64_t>(layer) * img->layer_size + L.offset + static_cast<uint64_t>(y0) * L.stride +
+                    static_cast<uint64_t>(x0) * img->texel;
+    return rt::fill_rect(q->stream, base, L.stride, static_cast<uint32_t>(x1 - x0), static_cast<uint32_t>(y1 - y0), img->texel, lo, hi, write_lo, write_hi) == rt::kOk
+               ? VK_SUCCESS
+               : VK_ERROR_DEVICE_LOST;
+}
+
 VkResult begin_render_pass(Queue* q, State& s, const Cmd& c, std::vector<DeviceMemory*>& written) {
     s.pass = static_cast<RenderPass*>(c.p[0]);
     s.fb = static_cast<Framebuffer*>(c.p[1]);
@@ -127,37 +179,17 @@ VkResult begin_render_pass(Queue* q, State& s, const Cmd& c, std::vector<DeviceM
         ImageView* v = s.fb->attachments[i];
         if (!v || !v->image || !v->image->memory) continue;
         written.push_back(v->image->memory);
+        // loadOp CLEAR clears colour or depth, stencilLoadOp CLEAR the
+        // stencil (ClearImage → SetPixel through the format encoder,
+        // CPVulkan/CommandBuffer.Draw.cpp:117-149)
         const bool depth = format_is_depth(a.format);
-        const bool clear = a.loadOp == VK_ATTACHMENT_LOAD_OP_CLEAR || (depth && format_has_stencil(a.format) && a.stencilLoadOp == VK_ATTACHMENT_LOAD_OP_CLEAR);
-        if (!clear || i >= c.clears.size()) continue;
-        uint32_t w, h;
-        uint8_t* base = view_base(v, w, h);
-        const uint64_t texels = static_cast<uint64_t>(w) * h;
-        const VkClearValue& cv = c.clears[i];
-        int r = rt::kOk;
-        if (!depth) {
-            // ClearImage → SetPixel through the format encoder
-            // (CPVulkan/CommandBuffer.Draw.cpp:117-149).
-            uint32_t packed = 0;
-            const int shift_bgra[4] = {16, 8, 0, 24};
-            for (int ch = 0; ch < 4; ch++) {
-                const uint32_t b = encode_unorm_host(cv.color.float32[ch], 255.0f);
-                const int sh = a.format == VK_FORMAT_B8G8R8A8_UNORM ? shift_bgra[ch] : 8 * ch;
-                packed |= b << sh;
-            }
-            r = rt::fill(q->stream, base, texels, 4, packed, 0);
-        } else if (a.format == VK_FORMAT_D16_UNORM) {
-            r = rt::fill(q->stream, base, texels, 2, encode_unorm_host(cv.depthStencil.depth, 65535.0f), 0);
-        } else if (a.format == VK_FORMAT_D32_SFLOAT) {
-            uint32_t bits;
-            std::memcpy(&bits, &cv.depthStencil.depth, 4);
-            r = rt::fill(q->stream, base, texels, 4, bits, 0);
-        } else if (a.format == VK_FORMAT_D32_SFLOAT_S8_UINT) {
-            uint32_t bits;
-            std::memcpy(&bits, &cv.depthStencil.depth, 4);
-            r = rt::fill(q->stream, base, texels, 8, bits, cv.depthStencil.stencil & 0xFFu);
-        }
-        if (r != rt::kOk) return VK_ERROR_DEVICE_LOST;
+        VkImageAspectFlags aspects = 0;
+        if (a.loadOp == VK_ATTACHMENT_LOAD_OP_CLEAR) aspects |= depth ? VK_IMAGE_ASPECT_DEPTH_BIT : VK_IMAGE_ASPECT_COLOR_BIT;
+        if (depth && format_has_stencil(a.format) && a.stencilLoadOp == VK_ATTACHMENT_LOAD_OP_CLEAR) aspects |= VK_IMAGE_ASPECT_STENCIL_BIT;
+        if (!aspects || i >= c.clears.size()) continue;
+        const ImageLevel& L = v->image->level[v->range.baseMipLevel];
+        const VkResult r = clear_rect(q, v->image, v->range.baseArrayLayer, v->range.baseMipLevel, aspects, c.clears[i], 0, 0, L.width, L.height);
+        if (r != VK_SUCCESS) return r;
     }
     return VK_SUCCESS;
 }
@@ -780,6 +812,86 @@ VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& writte
                 }
             }
             written.push_back(dst->memory);
+            break;
+        }
+        case CmdType::CopyImage: {
+            // Regions between images of one texel size, row by row
+            // (CPVulkan/CommandBuffer.Copy.cpp:1091-1095).
+            Image* src = static_cast<Image*>(c.p[0]);
+            Image* dst = static_cast<Image*>(c.p[1]);
+            if (!src || !dst || !src->memory || !dst->memory || src->texel != dst->texel) return VK_ERROR_DEVICE_LOST;
+            const uint32_t texel = src->texel;
+            for (const VkImageCopy& rg : c.image_copies) {
+                const auto& ss = rg.srcSubresource;
+                const auto& ds = rg.dstSubresource;
+                if (ss.mipLevel >= src->levels || ds.mipLevel >= dst->levels || ss.layerCount != ds.layerCount) return VK_ERROR_DEVICE_LOST;
+                const ImageLevel& sl = src->level[ss.mipLevel];
+                const ImageLevel& dl = dst->level[ds.mipLevel];
+                auto inside = [](const ImageLevel& L, const VkOffset3D& o, const VkExtent3D& e) {
+                    return o.x >= 0 && o.y >= 0 && o.z >= 0 && static_cast<uint64_t>(o.x) + e.width <= L.width && static_cast<uint64_t>(o.y) + e.height <= L.height &&
+                           static_cast<uint64_t>(o.z) + e.depth <= std::max(1u, L.depth);
+                };
+                if (!inside(sl, rg.srcOffset, rg.extent) || !inside(dl, rg.dstOffset, rg.extent)) return VK_ERROR_DEVICE_LOST;
+                if (ss.baseArrayLayer + ss.layerCount > src->layers || ds.baseArrayLayer + ds.layerCount > dst->layers) return VK_ERROR_DEVICE_LOST;
+                if (rg.extent.width == 0 || rg.extent.height == 0) continue;
+                for (uint32_t layer = 0; layer < ss.layerCount; layer++) {
+                    for (uint32_t z = 0; z < std::max(1u, rg.extent.depth); z++) {
+                        const uint8_t* sp = src->device_ptr() + static_cast<uint64_t>(ss.baseArrayLayer + layer) * src->layer_size + sl.offset +
+                                            static_cast<uint64_t>(rg.srcOffset.z + z) * sl.plane + static_cast<uint64_t>(rg.srcOffset.y) * sl.stride +
+                                            static_cast<uint64_t>(rg.srcOffset.x) * texel;
+                        uint8_t* dp = dst->device_ptr() + static_cast<uint64_t>(ds.baseArrayLayer + layer) * dst->layer_size + dl.offset +
+                                      static_cast<uint64_t>(rg.dstOffset.z + z) * dl.plane + static_cast<uint64_t>(rg.dstOffset.y) * dl.stride +
+                                      static_cast<uint64_t>(rg.dstOffset.x) * texel;
+                        if (cudaMemcpy2DAsync(dp, dl.stride, sp, sl.stride, static_cast<size_t>(rg.extent.width) * texel, rg.extent.height, cudaMemcpyDeviceToDevice,
+                                              q->stream) != cudaSuccess)
+                            return VK_ERROR_DEVICE_LOST;
+                    }
+                }
+            }
+            written.push_back(dst->memory);
+            break;
+        }
+        case CmdType::ClearImage: {
+            Image* img = static_cast<Image*>(c.p[0]);
+            if (!img || !img->memory || c.clears.empty()) return VK_ERROR_DEVICE_LOST;
+            for (const VkImageSubresourceRange& rg : c.ranges) {
+                const uint32_t levels = rg.levelCount == VK_REMAINING_MIP_LEVELS ? img->levels - std::min(rg.baseMipLevel, img->levels) : rg.levelCount;
+                const uint32_t layers = rg.layerCount == VK_REMAINING_ARRAY_LAYERS ? img->layers - std::min(rg.baseArrayLayer, img->layers) : rg.layerCount;
+                if (static_cast<uint64_t>(rg.baseMipLevel) + levels > img->levels || static_cast<uint64_t>(rg.baseArrayLayer) + layers > img->layers)
+                    return VK_ERROR_DEVICE_LOST;
+                for (uint32_t layer = 0; layer < layers; layer++)
+                    for (uint32_t level = 0; level < levels; level++) {
+                        const ImageLevel& L = img->level[rg.baseMipLevel + level];
+                        const VkResult r = clear_rect(q, img, rg.baseArrayLayer + layer, rg.baseMipLevel + level, rg.aspectMask, c.clears[0], 0, 0, L.width,
+                                                      L.height * std::max(1u, L.depth));
+                        if (r != VK_SUCCESS) return r;
+                    }
+            }
+            written.push_back(img->memory);
+            break;
+        }
+        case CmdType::ClearAttachments: {
+            // Rectangles of the current subpass's attachments
+            // (CPVulkan/CommandBuffer.Draw.cpp:2142-2224); a colour index or
+            // depth attachment the subpass does not use is not cleared.
+            if (!s.pass || !s.fb) return VK_ERROR_DEVICE_LOST;
+            for (const VkClearAttachment& a : c.clear_attachments) {
+                uint32_t index = VK_ATTACHMENT_UNUSED;
+                if (a.aspectMask & VK_IMAGE_ASPECT_COLOR_BIT) {
+                    if (a.colorAttachment < s.pass->colour.size()) index = s.pass->colour[a.colorAttachment];
+                } else {
+                    index = s.pass->depth;
+                }
+                if (index == VK_ATTACHMENT_UNUSED || index >= s.fb->attachments.size() || !s.fb->attachments[index]) continue;
+                const ImageView* v = s.fb->attachments[index];
+                for (const VkClearRect& rect : c.clear_rects)
+                    for (uint32_t layer = 0; layer < rect.layerCount; layer++) {
+                        const VkResult r = clear_rect(q, v->image, v->range.baseArrayLayer + rect.baseArrayLayer + layer, v->range.baseMipLevel, a.aspectMask,
+                                                      a.clearValue, rect.rect.offset.x, rect.rect.offset.y, rect.rect.extent.width, rect.rect.extent.height);
+                        if (r != VK_SUCCESS) return r;
+                    }
+                written.push_back(v->image->memory);
+            }
             break;
         }
         case CmdType::FillBuffer: {

@@ -996,6 +996,38 @@ VKAPI_ATTR void VKAPI_CALL CmdBlitImage(VkCommandBuffer cmd, VkImage src, VkImag
     c.u[0] = static_cast<uint32_t>(filter);
     c.blit_regions.assign(r, r + n);
 }
+// vkCmdCopyImage (CPVulkan/CommandBuffer.Copy.cpp:1091-1095).
+VKAPI_ATTR void VKAPI_CALL CmdCopyImage(VkCommandBuffer cmd, VkImage src, VkImageLayout, VkImage dst, VkImageLayout, uint32_t n, const VkImageCopy* r) {
+    auto& c = push(cmd, CmdType::CopyImage);
+    c.p[0] = reinterpret_cast<void*>(src);
+    c.p[1] = reinterpret_cast<void*>(dst);
+    c.image_copies.assign(r, r + n);
+}
+// vkCmdClearColorImage / vkCmdClearDepthStencilImage / vkCmdClearAttachments
+// (CPVulkan/CommandBuffer.Draw.cpp:2380-2396).
+VKAPI_ATTR void VKAPI_CALL CmdClearColorImage(VkCommandBuffer cmd, VkImage image, VkImageLayout, const VkClearColorValue* colour, uint32_t n,
+                                              const VkImageSubresourceRange* ranges) {
+    auto& c = push(cmd, CmdType::ClearImage);
+    c.p[0] = reinterpret_cast<void*>(image);
+    VkClearValue v{};
+    v.color = *colour;
+    c.clears.push_back(v);
+    c.ranges.assign(ranges, ranges + n);
+}
+VKAPI_ATTR void VKAPI_CALL CmdClearDepthStencilImage(VkCommandBuffer cmd, VkImage image, VkImageLayout, const VkClearDepthStencilValue* ds, uint32_t n,
+                                                     const VkImageSubresourceRange* ranges) {
+    auto& c = push(cmd, CmdType::ClearImage);
+    c.p[0] = reinterpret_cast<void*>(image);
+    VkClearValue v{};
+    v.depthStencil = *ds;
+    c.clears.push_back(v);
+    c.ranges.assign(ranges, ranges + n);
+}
+VKAPI_ATTR void VKAPI_CALL CmdClearAttachments(VkCommandBuffer cmd, uint32_t n, const VkClearAttachment* a, uint32_t rects, const VkClearRect* r) {
+    auto& c = push(cmd, CmdType::ClearAttachments);
+    c.clear_attachments.assign(a, a + n);
+    c.clear_rects.assign(r, r + rects);
+}
 VKAPI_ATTR void VKAPI_CALL CmdFillBuffer(VkCommandBuffer cmd, VkBuffer dst, VkDeviceSize off, VkDeviceSize size, uint32_t data) {
     auto& c = push(cmd, CmdType::FillBuffer);
     c.p[0] = reinterpret_cast<void*>(dst);
@@ -1204,7 +1236,8 @@ const Entry kDevice[] = {
     E(CmdDraw), E(CmdDrawIndexed), E(CmdDrawIndirect), E(CmdDrawIndexedIndirect),
     {"vkCmdDrawIndirectCountKHR", reinterpret_cast<PFN_vkVoidFunction>(CmdDrawIndirectCount)},
     {"vkCmdDrawIndexedIndirectCountKHR", reinterpret_cast<PFN_vkVoidFunction>(CmdDrawIndexedIndirectCount)},
-    {"vkCmdDrawIndirectCountAMD", reinterpret_cast<PFN_vkVoidFunction>(CmdDrawIndirectCount)}, E(CmdCopyBuffer), E(CmdCopyBufferToImage), E(CmdBlitImage),
+    {"vkCmdDrawIndirectCountAMD", reinterpret_cast<PFN_vkVoidFunction>(CmdDrawIndirectCount)}, E(CmdCopyBuffer), E(CmdCopyImage),
+    E(CmdClearColorImage), E(CmdClearDepthStencilImage), E(CmdClearAttachments), E(CmdCopyBufferToImage), E(CmdBlitImage),
     E(CmdCopyImageToBuffer), E(CmdFillBuffer), E(CmdUpdateBuffer), E(CmdPipelineBarrier), E(CmdPushConstants), E(CmdBeginRenderPass),
     E(CmdEndRenderPass), E(QueueSubmit), E(CreateFence), E(DestroyFence), E(ResetFences), E(GetFenceStatus), E(WaitForFences),
     E(CreateSemaphore), E(DestroySemaphore),

@@ -188,7 +188,7 @@ std::string compose_module(const std::vector<std::string>& stages, const std::ve
 enum class CmdType : uint8_t {
     BeginRenderPass, EndRenderPass, BindPipeline, BindVertexBuffers, BindIndexBuffer, BindDescriptorSets, PushConstants,
     SetViewport, SetScissor, SetBlendConstants, Draw, DrawIndexed, DrawIndirect, DrawIndexedIndirect, CopyBuffer,
-    CopyBufferToImage, CopyImageToBuffer, FillBuffer, UpdateBuffer, Barrier, BlitImage,
+    CopyBufferToImage, CopyImageToBuffer, FillBuffer, UpdateBuffer, Barrier, BlitImage, CopyImage, ClearImage, ClearAttachments,
 };
 
 struct Cmd {
@@ -203,6 +203,10 @@ struct Cmd {
     std::vector<VkBufferImageCopy> image_regions;
     std::vector<VkBufferCopy> buffer_regions;
     std::vector<VkImageBlit> blit_regions;
+    std::vector<VkImageCopy> image_copies;
+    std::vector<VkImageSubresourceRange> ranges;
+    std::vector<VkClearAttachment> clear_attachments;
+    std::vector<VkClearRect> clear_rects;
     std::vector<VkClearValue> clears;
     VkViewport viewport{};
 };

@@ -396,6 +396,27 @@ extern "C" __global__ void __launch_bounds__(256) cpv_fill_u64(uint2* __restrict
         dst[i] = make_uint2(lo, hi);
 }
 
+/* Fill of a w x h texel rectangle whose rows start `pitch` bytes apart: a
+ * 2-byte texel takes the low half of lo; 4- and 8-byte texels take lo in
+ * their first word when write_lo, and an 8-byte (D32 + stencil) texel takes
+ * hi in its second word when write_hi. */
+extern "C" __global__ void __launch_bounds__(256) cpv_fill_rect(uint8_t* __restrict__ base, uint64_t pitch, uint32_t w, uint32_t h, uint32_t texel_bytes,
+                                                                uint32_t lo, uint32_t hi, uint32_t write_lo, uint32_t write_hi) {
+    /* rows over blockIdx.y, texels of a row over x */
+    for (uint32_t y = blockIdx.y; y < h; y += gridDim.y) {
+        uint8_t* row = base + static_cast<uint64_t>(y) * pitch;
+        for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < w; x += gridDim.x * blockDim.x) {
+            uint8_t* p = row + static_cast<uint64_t>(x) * texel_bytes;
+            if (texel_bytes == 2) {
+                *reinterpret_cast<uint16_t*>(p) = static_cast<uint16_t>(lo);
+            } else {
+                if (write_lo) *reinterpret_cast<uint32_t*>(p) = lo;
+                if (texel_bytes == 8 && write_hi) *reinterpret_cast<uint32_t*>(p + 4) = hi;
+            }
+        }
+    }
+}
+
 /* ---- host → HBM copy read by the SMs ----
  * Copies `words` 16-byte words from pinned host memory (device-accessible)
  * to HBM with every SM issuing loads across the chip-to-chip link. Both

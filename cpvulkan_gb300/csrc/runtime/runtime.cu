@@ -391,6 +391,21 @@ int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, 
     return kOk;
 }
 
+int fill_rect(cudaStream_t stream, uint8_t* base, uint64_t pitch, uint32_t w, uint32_t h, uint32_t texel_bytes, uint32_t lo, uint32_t hi, bool write_lo,
+              bool write_hi) {
+    if (!base || w == 0 || h == 0) return kOk;
+    if (texel_bytes != 2 && texel_bytes != 4 && texel_bytes != 8) return kErrInvalid;
+    if (reinterpret_cast<uintptr_t>(base) % texel_bytes != 0 || pitch % texel_bytes != 0 || pitch < static_cast<uint64_t>(w) * texel_bytes) return kErrInvalid;
+    if (!write_lo && !(texel_bytes == 8 && write_hi)) return kOk;
+    if (pitch == static_cast<uint64_t>(w) * texel_bytes && write_lo && (texel_bytes != 8 || write_hi))
+        return fill(stream, base, static_cast<uint64_t>(w) * h, texel_bytes, lo, hi);  // contiguous: one span
+    const dim3 grid((w + 255) / 256 < 8 ? (w + 255) / 256 : 8, h < 2048 ? h : 2048);
+    cpv_fill_rect<<<grid, 256, 0, stream>>>(base, pitch, w, h, texel_bytes, lo, hi, write_lo ? 1u : 0u, write_hi ? 1u : 0u);
+    count_launch();
+    CPV_CUDA(cudaGetLastError());
+    return kOk;
+}
+
 int copy_host_to_device(cudaStream_t stream, uint8_t* dst, const uint8_t* host, uint64_t bytes) {
     if (bytes == 0) return kOk;
     // The kernel reads the host memory through its device mapping: only

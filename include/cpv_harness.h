@@ -90,6 +90,34 @@ int cpvh_renderer_set_indirect_count(cpvh_renderer* r, uint32_t draw, uint32_t c
 /* Reads the attachments back (colour: width*height*4; depth: texel-sized). */
 int cpvh_readback(cpvh_renderer* r, uint8_t* color, uint8_t* depth);
 
+/* One transfer / clear command of cpvh_image_ops on image 0 (image 1 is a
+ * copy source). */
+enum {
+    CPVH_OP_CLEAR_COLOR_IMAGE = 0,         /* vkCmdClearColorImage of levels level .. level+level_count-1 */
+    CPVH_OP_CLEAR_DEPTH_STENCIL_IMAGE = 1, /* vkCmdClearDepthStencilImage of those levels, aspects `aspect` */
+    CPVH_OP_COPY_IMAGE = 2,                /* vkCmdCopyImage: image 1 level src_level at (src_x, src_y) → image 0 level `level` at (x, y), w x h */
+    CPVH_OP_CLEAR_ATTACHMENTS = 3          /* vkCmdClearAttachments in a LOAD/STORE render pass over level `level`: rectangle (x, y, w, h) */
+};
+typedef struct cpvh_image_op {
+    uint32_t kind;
+    uint32_t aspect; /* VkImageAspectFlags of the range, region or clear */
+    uint32_t level, level_count, src_level;
+    int32_t x, y, src_x, src_y;
+    uint32_t w, h;
+    float colour[4];
+    float depth;
+    uint32_t stencil;
+} cpvh_image_op;
+
+/* Runs `ops` in order through the ICD on two 2D images of `format` (one
+ * layer, `levels` mips of width x height halving), initialised from init0 /
+ * init1 (every level packed in order, in the ICD's texel layout: 4 bytes for
+ * colour, 2 for D16, 4 for D32, 8 for D32S8 with the stencil in byte 4;
+ * init1 may be null: zeros), then reads image 0 back into `out` in the same
+ * layout. Returns a VkResult. */
+int cpvh_image_ops(cpvh_context* ctx, uint32_t format, uint32_t width, uint32_t height, uint32_t levels, const uint8_t* init0, const uint8_t* init1,
+                   const cpvh_image_op* ops, uint32_t op_count, uint8_t* out, char* err, uint32_t err_len);
+
 /* vkCmdBlitImage through the ICD. src (and dst when not null) hold every mip
  * level of an RGBA8 (37) / BGRA8 (44) image, level l being
  * max(w >> l, 1) x max(h >> l, 1) texels, packed one after another. Both
