@@ -448,6 +448,9 @@ bool build_pipelines(cpvh_context* c, const cpv_scene* s, VkRenderPass pass, VkP
         ds.depthWriteEnable = sp.depth_write;
         ds.depthCompareOp = static_cast<VkCompareOp>(sp.depth_compare);
         ds.stencilTestEnable = sp.stencil_test;
+        ds.depthBoundsTestEnable = sp.depth_bounds_test;
+        ds.minDepthBounds = sp.min_depth_bounds;
+        ds.maxDepthBounds = sp.max_depth_bounds;
         const cpv_scene_stencil* so[2] = {&sp.stencil_front, &sp.stencil_back};
         VkStencilOpState* dso[2] = {&ds.front, &ds.back};
         for (int k = 0; k < 2; k++)

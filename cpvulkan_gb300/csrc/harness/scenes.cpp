@@ -658,6 +658,13 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
         p.logic_op = (variant >> 20) & 0xF;
     }
     if (variant & 0x80000) p.color_write_mask = (variant >> 24) & 0xF;  // partial colour write mask (bits 24-27)
+    if (const uint32_t bounds = (variant >> 28) & 3u) {  // depth bounds test (bits 28-29) against the stored depth (cleared to 0.75)
+        // 1: the whole range; 2: stored depth from 0.3 up; 3: above the clear depth, so nothing passes
+        static const float range[4][2] = {{0.0f, 1.0f}, {0.0f, 1.0f}, {0.3f, 1.0f}, {0.8f, 1.0f}};
+        p.depth_bounds_test = 1;
+        p.min_depth_bounds = range[bounds][0];
+        p.max_depth_bounds = range[bounds][1];
+    }
     const bool u16 = (variant & 0x1000) != 0;
 
     uint32_t vcount = 0;

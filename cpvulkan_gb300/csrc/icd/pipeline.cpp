@@ -58,6 +58,7 @@ const char* const kStageMacros[] = {
     "CPV_ST_F_FAIL", "CPV_ST_F_PASS", "CPV_ST_F_DFAIL", "CPV_ST_F_OP", "CPV_ST_F_CMASK", "CPV_ST_F_WMASK", "CPV_ST_F_REF",
     "CPV_ST_B_FAIL", "CPV_ST_B_PASS", "CPV_ST_B_DFAIL", "CPV_ST_B_OP", "CPV_ST_B_CMASK", "CPV_ST_B_WMASK", "CPV_ST_B_REF",
     "CPV_BLEND", "CPV_SRC_COLOR", "CPV_DST_COLOR", "CPV_COLOR_OP", "CPV_SRC_ALPHA", "CPV_DST_ALPHA", "CPV_ALPHA_OP", "CPV_WRITE_MASK", "CPV_LOGIC", "CPV_LOGIC_OP",
+    "CPV_DEPTH_BOUNDS", "CPV_MIN_DEPTH_BOUNDS", "CPV_MAX_DEPTH_BOUNDS",
     "CPV_COLOR_FORMAT", "CPV_DEPTH_FORMAT", "CPV_ORIGIN_UPPER", "CPV_FS_CONSTANT", "CPV_BLEND_TABLE", "CPV_LINE_WIDTH", "CPV_PRIM_KIND",
 };
 
@@ -316,7 +317,6 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
 
     VkPipelineDepthStencilStateCreateInfo ds{};
     if (ci.pDepthStencilState) ds = *ci.pDepthStencilState;
-    if (ds.depthBoundsTestEnable) return reject("depth bounds test");
     const bool stencil = ds.stencilTestEnable && dfmt == VK_FORMAT_D32_SFLOAT_S8_UINT;
 
     VkPipelineColorBlendAttachmentState blend{};
@@ -402,6 +402,17 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     src << "#define CPV_DEPTH_TEST " << (ds.depthTestEnable ? 1 : 0) << "\n";
     src << "#define CPV_DEPTH_WRITE " << (ds.depthWriteEnable ? 1 : 0) << "\n";
     src << "#define CPV_DEPTH_OP " << static_cast<uint32_t>(ds.depthCompareOp) << "\n";
+    // Depth bounds test (LLVMRuntime/PipelineCompiler.cpp:1128-1166): static
+    // bounds only (the reference aborts on dynamic ones, and so
+    // VK_DYNAMIC_STATE_DEPTH_BOUNDS is rejected above); without a depth
+    // attachment there is no test.
+    const bool depth_bounds = ds.depthBoundsTestEnable && dfmt != VK_FORMAT_UNDEFINED;
+    uint32_t min_bits, max_bits;
+    std::memcpy(&min_bits, &ds.minDepthBounds, 4);
+    std::memcpy(&max_bits, &ds.maxDepthBounds, 4);
+    src << "#define CPV_DEPTH_BOUNDS " << (depth_bounds ? 1 : 0) << "\n";
+    src << "#define CPV_MIN_DEPTH_BOUNDS __uint_as_float(" << min_bits << "u)\n";
+    src << "#define CPV_MAX_DEPTH_BOUNDS __uint_as_float(" << max_bits << "u)\n";
     src << "#define CPV_STENCIL_TEST " << (stencil ? 1 : 0) << "\n";
     const VkStencilOpState* so[2] = {&ds.front, &ds.back};
     const char* sn[2] = {"F", "B"};

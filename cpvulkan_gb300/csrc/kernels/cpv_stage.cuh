@@ -4,7 +4,8 @@
  * that pipeline's namespace (cpv_p0, cpv_p1, …), after the pipeline's
  * fixed-function macros (CPV_TOPOLOGY, CPV_CULL_MODE, CPV_FRONT_CW,
  * CPV_DEPTH_*, CPV_STENCIL_TEST, CPV_ST_*, CPV_BLEND, CPV_SRC_* / CPV_DST_*,
- * CPV_*_OP, CPV_WRITE_MASK, CPV_LOGIC, CPV_LOGIC_OP, CPV_COLOR_FORMAT, CPV_DEPTH_FORMAT,
+ * CPV_*_OP, CPV_WRITE_MASK, CPV_LOGIC, CPV_LOGIC_OP, CPV_DEPTH_BOUNDS,
+ * CPV_MIN_DEPTH_BOUNDS, CPV_MAX_DEPTH_BOUNDS, CPV_COLOR_FORMAT, CPV_DEPTH_FORMAT,
  * CPV_ORIGIN_UPPER, CPV_NV) and its translated shaders:
  *
  *   __device__ void cpv_vs_run(const CpvDrawParams&, uint32_t vertex_index,
@@ -36,6 +37,12 @@
 #ifndef CPV_LOGIC
 #define CPV_LOGIC 0
 #define CPV_LOGIC_OP 3
+#endif
+/* depthBoundsTestEnable with a depth attachment, and the static bounds */
+#ifndef CPV_DEPTH_BOUNDS
+#define CPV_DEPTH_BOUNDS 0
+#define CPV_MIN_DEPTH_BOUNDS 0.0f
+#define CPV_MAX_DEPTH_BOUNDS 1.0f
 #endif
 
 /* The fragment shader of a primitive whose shader is constant over it
@@ -478,12 +485,17 @@ __device__ __forceinline__ uint32_t cpv_logic(uint32_t s, uint32_t d) {
     return r & 0xFFu;
 }
 
-/* Depth bounds are rejected at pipeline creation; order as the reference's
- * fragment wrapper: current values → stencil test → depth test → depth /
- * stencil write → colour write (logic op or blend, write mask, encode). */
+/* Order as the reference's fragment wrapper: current values → depth bounds
+ * test → stencil test → depth test → depth / stencil write → colour write
+ * (logic op or blend, write mask, encode). */
 __device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool front, const float colour[4], float mapped, CpvPixel& s,
                                         const uint8_t* table = nullptr) {
     const bool has_depth = CPV_DEPTH_FORMAT != 0;
+#if CPV_DEPTH_BOUNDS && CPV_DEPTH_FORMAT != 0
+    /* the stored depth outside the bounds (unordered compares: NaN is
+     * outside) ends the fragment with no write of any kind */
+    if (!(s.depth >= CPV_MIN_DEPTH_BOUNDS) || !(s.depth <= CPV_MAX_DEPTH_BOUNDS)) return;
+#endif
     const bool stencil_on = CPV_STENCIL_TEST && CPV_DEPTH_FORMAT == 130;
     const float current_depth = (CPV_DEPTH_TEST && has_depth) ? s.depth : 0.0f;
     const uint32_t current_stencil = stencil_on ? s.stencil : 0u;
@@ -581,7 +593,8 @@ __device__ __forceinline__ void cpv_blend_table_column(const float colour[4], co
 constexpr bool kBlendTable = CPV_BLEND_TABLE != 0;
 /* a blend-table pipeline without depth or stencil operations: a covered
  * fragment's whole effect is its table lookup */
-constexpr bool kTableOnly = kBlendTable && !(CPV_DEPTH_TEST && CPV_DEPTH_FORMAT != 0) && !(CPV_STENCIL_TEST && CPV_DEPTH_FORMAT == 130);
+constexpr bool kTableOnly = kBlendTable && !(CPV_DEPTH_TEST && CPV_DEPTH_FORMAT != 0) && !(CPV_STENCIL_TEST && CPV_DEPTH_FORMAT == 130) &&
+                            !(CPV_DEPTH_BOUNDS && CPV_DEPTH_FORMAT != 0);
 
 /* cpv_rop's colour write through a blend table, when every test passes */
 __device__ __forceinline__ void cpv_apply_table(const uint8_t* table, CpvPixel& s) {

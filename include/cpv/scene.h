@@ -78,6 +78,8 @@ typedef struct cpv_scene_pipeline {
     uint32_t color_write_mask; /* VkColorComponentFlags: R 1, G 2, B 4, A 8 (0xF writes every channel) */
     uint32_t logic_op_enable;  /* VkPipelineColorBlendStateCreateInfo::logicOpEnable (blending then off) */
     uint32_t logic_op;         /* VkLogicOp, CLEAR (0) .. SET (15) */
+    uint32_t depth_bounds_test;              /* VkPipelineDepthStencilStateCreateInfo::depthBoundsTestEnable */
+    float min_depth_bounds, max_depth_bounds;
 } cpv_scene_pipeline;
 
 typedef struct cpv_scene_draw {

@@ -728,7 +728,11 @@ void fragment(Frame& f, const cpv_scene_pipeline& p, uint32_t x, uint32_t y, flo
     const bool has_depth_att = ds != nullptr;
 
     float current_depth = 0.0f;
-    if (p.depth_test && has_depth_att) current_depth = get_depth(ds, s->depth_format);
+    if ((p.depth_test || p.depth_bounds_test) && has_depth_att) current_depth = get_depth(ds, s->depth_format);
+    /* Depth bounds test (CompileDepthBoundsTest, :1128-1166): the stored
+     * depth outside [min, max] (unordered compares: NaN is outside) ends the
+     * fragment before the stencil test, with no write of any kind. */
+    if (p.depth_bounds_test && has_depth_att && (!(current_depth >= p.min_depth_bounds) || !(current_depth <= p.max_depth_bounds))) return;
     uint8_t current_stencil = 0;
     const bool stencil_on = p.stencil_test && has_depth_att && has_stencil(s->depth_format);
     if (stencil_on) current_stencil = ds[4];

@@ -63,8 +63,16 @@ LOGIC_MASK = [
     (c.PROGRAM_POINTS, 0x10000 | 0x20 | 0x80000 | (0x3 << 24)),
 ]
 
+# The depth bounds test (bits 28-29: [0, 1], [0.3, 1], [0.8, 1] against a
+# depth cleared to 0.75) with D32, D32S8 + stencil, D16, blending and lines.
+DEPTH_BOUNDS = [
+    (c.PROGRAM_CUBE, 0x10 | (2 << 28)), (c.PROGRAM_CUBE, 0x18 | 0x100 | (2 << 28)), (c.PROGRAM_CUBE, 0x18 | 0x100 | (3 << 28)),
+    (c.PROGRAM_FLATQUAD, 0x8 | 0x20 | (2 << 28)), (c.PROGRAM_MESHPC, 0x10 | 0x20 | (1 << 28)),
+    (c.PROGRAM_CUBE, 0x10000 | 0x400 | 0x20000 | 0x10 | (2 << 28)),
+]
 
-@pytest.mark.parametrize("program,variant", VARIANTS + POINTS_LINES + LOGIC_MASK)
+
+@pytest.mark.parametrize("program,variant", VARIANTS + POINTS_LINES + LOGIC_MASK + DEPTH_BOUNDS)
 @pytest.mark.parametrize("seed", [1, 2, 3])
 def test_program_variants(gpu_ctx, oracle, program, variant, seed):
     scene = c.Scene(c.PROGRAM, seed, [program, variant, 64, 48, 24])

@@ -78,3 +78,32 @@ def test_logic_op_relations(native, oracle, program, variant):
     for comp in range(4):
         ref = res[COPY_INVERTED] if (0x5 >> comp) & 1 else clear
         assert np.array_equal(part[..., offsets[comp]], ref[..., offsets[comp]])
+
+
+def bounds(mode):
+    return mode << 28
+
+
+@pytest.mark.parametrize("program,variant", [(c.PROGRAM_CUBE, 0x10), (c.PROGRAM_CUBE, 0x18 | 0x100), (c.PROGRAM_FLATQUAD, 0x8 | 0x20)])
+def test_depth_bounds_relations(native, oracle, program, variant):
+    """The depth bounds test (LLVMRuntime/PipelineCompiler.cpp:1128-1166)
+    compares the stored depth: bounds [0, 1] change nothing; bounds [0.8, 1]
+    reject every fragment of a target cleared to depth 0.75, which then keeps
+    its clear colour, depth and stencil; bounds [0.3, 1] stop a pixel from
+    changing once its stored depth falls below 0.3."""
+    off_c, off_d = render(oracle, program, variant)
+    full_c, full_d = render(oracle, program, variant | bounds(1))
+    assert np.array_equal(off_c, full_c) and np.array_equal(off_d, full_d)
+    none_c, none_d = render(oracle, program, variant | bounds(3))
+    clear_c, clear_d = render(oracle, program, variant | bounds(3) | mask(0))
+    assert np.array_equal(none_c, clear_c) and np.array_equal(none_d, clear_d)
+    assert not np.array_equal(off_c, none_c)
+    # bounds [0.3, 1]: a pixel that ends unlike the unbounded render was
+    # frozen by a stored depth below 0.3
+    part_c, part_d = render(oracle, program, variant | bounds(2))
+    if part_d.shape[-1] == 2:
+        stored = part_d.view(np.uint16)[..., 0] / np.float32(65535)
+    else:
+        stored = np.ascontiguousarray(part_d[..., :4]).view(np.float32)[..., 0]
+    changed = (part_c != off_c).any(axis=-1) | (part_d != off_d).any(axis=-1)
+    assert (stored[changed] < 0.3).all()

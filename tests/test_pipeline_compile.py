@@ -17,13 +17,15 @@ KERNELS = os.path.join(ROOT, "cpvulkan_gb300", "csrc", "kernels")
 # 5 blend, 6-7 depth op, 8 stencil, 9 BGRA, 10-11 topology, 12 u16 indices,
 # 13 depth write off, 14 nearest + mirror/border sampler, 15 LOD bias,
 # 16 point/line topologies (10-11 then: points, lines, line strip), 17 wide lines,
-# 18 logic op (op in bits 20-23), 19 colour write mask (mask in bits 24-27)
+# 18 logic op (op in bits 20-23), 19 colour write mask (mask in bits 24-27),
+# 28-29 depth bounds
 PROGRAMS = [
     (c.PROGRAM_CUBE, 0x0), (c.PROGRAM_CUBE, 0x18 | 0x100), (c.PROGRAM_CUBE, 0x20 | 0x200 | 0x400),
     (c.PROGRAM_TEXLIT, 0x10 | 0x4000), (c.PROGRAM_FLATQUAD, 0x20), (c.PROGRAM_MESHPC, 0x10 | 0x2 | 0x4),
     (c.PROGRAM_DISCARD, 0x10), (c.PROGRAM_NOPERSP, 0x8 | 0x800),
     (c.PROGRAM_POINTS, 0x10000 | 0x10), (c.PROGRAM_CUBE, 0x10000 | 0x400 | 0x20000), (c.PROGRAM_NOPERSP, 0x10000 | 0x800 | 0x8),
     (c.PROGRAM_CUBE, 0x40000 | (6 << 20) | 0x10), (c.PROGRAM_FLATQUAD, 0x20 | 0x80000 | (0x5 << 24)),
+    (c.PROGRAM_CUBE, 0x18 | 0x100 | (2 << 28)),
 ]
 
 
@@ -104,6 +106,11 @@ def _module_source(compile_ctx, program, variant):
     # a logic op turns blending (and so the blend tables) off
     (c.PROGRAM_FLATQUAD, 0x20 | 0x40000 | (9 << 20), {"CPV_LOGIC": "1", "CPV_LOGIC_OP": "9", "CPV_BLEND": "0", "CPV_BLEND_TABLE": "0"}),
     (c.PROGRAM_CUBE, 0x80000 | (0xA << 24), {"CPV_LOGIC": "0", "CPV_WRITE_MASK": "10u"}),
+    # static depth bounds as float bit patterns (0.3f, 1.0f)
+    (c.PROGRAM_CUBE, 0x10 | (2 << 28), {"CPV_DEPTH_BOUNDS": "1", "CPV_MIN_DEPTH_BOUNDS": "__uint_as_float(1050253722u)",
+                                       "CPV_MAX_DEPTH_BOUNDS": "__uint_as_float(1065353216u)"}),
+    # no depth attachment: no test
+    (c.PROGRAM_FLATQUAD, 0x20 | (2 << 28), {"CPV_DEPTH_BOUNDS": "0"}),
 ])
 def test_module_configuration(compile_ctx, program, variant, expect):
     """The fixed-function and schedule macros a pipeline's module is compiled with."""
