@@ -135,3 +135,20 @@ def test_points_lines_schedule_invariance(gpu_ctx, oracle, monkeypatch, tile, sc
     report, stats = check(gpu_ctx, oracle, scene)
     assert stats["fragments"] > 0
     assert report["color_pixels_differing"] == 0, report
+
+
+@pytest.mark.parametrize("schedule", ["0", "2"])
+@pytest.mark.parametrize("tile", ["8", "16"])
+def test_coverage_kats(gpu_ctx, oracle, monkeypatch, tile, schedule):
+    """The hand-placed coverage cases (pixel centres on edges, a shared edge,
+    both windings under every cull mode, a sliver, a degenerate and an
+    off-screen triangle) through the device: images equal to the oracle's,
+    whose coverage the numpy restatement pins, under two tile sizes and
+    both the immediate and the sparse schedule."""
+    from tests import coverage_kat as kat
+    monkeypatch.setenv("CPV_TILE", tile)
+    monkeypatch.setenv("CPV_SCHEDULE", schedule)
+    for case in kat.CASES:
+        report, stats = check(gpu_ctx, oracle, kat.scene(case))
+        assert stats["fragments"] == int(kat.coverage(case).sum())
+        assert report["color_pixels_differing"] == 0, (case[0], report)
