@@ -104,6 +104,8 @@ def harness():
     h.cpvh_queue.restype = vp
     h.cpvh_queue.argtypes = [vp]
     h.cpvh_last_error.restype = cp
+    h.cpvh_allocator_check.restype = ctypes.c_int
+    h.cpvh_allocator_check.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(u64), ctypes.POINTER(u64)]
     h.cpvh_image_ops.restype = ctypes.c_int
     h.cpvh_image_ops.argtypes = [vp, u32, u32, u32, u32, vp, vp, vp, u32, vp, cp, u32]
     h.cpvh_blit.restype = ctypes.c_int
@@ -249,6 +251,14 @@ class Context:
         if r != VK_SUCCESS:
             raise RuntimeError("image ops failed (%d): %s" % (r, err.value.decode(errors="replace")))
         return out
+
+    def allocator_check(self):
+        """(objects, allocations, frees) of cpvh_allocator_check."""
+        o, a, f = ctypes.c_uint64(0), ctypes.c_uint64(0), ctypes.c_uint64(0)
+        r = harness().cpvh_allocator_check(self.ptr, ctypes.byref(o), ctypes.byref(a), ctypes.byref(f))
+        if r != VK_SUCCESS:
+            raise RuntimeError("allocator check failed (%d)" % r)
+        return o.value, a.value, f.value
 
     @property
     def queue(self):

@@ -1213,6 +1213,146 @@ int cpvh_blit(cpvh_context* c, uint8_t* src, uint32_t src_w, uint32_t src_h, uin
     return rc;
 }
 
+namespace {
+// Counting allocator for cpvh_allocator_check: every block carries a
+// 16-byte header so that frees can be matched to allocations.
+struct CountingAllocator {
+    uint64_t allocations = 0, frees = 0, live = 0;
+};
+void* VKAPI_CALL counting_alloc(void* user, size_t size, size_t align, int) {
+    if (align > 16) return nullptr;
+    auto* c = static_cast<CountingAllocator*>(user);
+    auto* p = static_cast<uint8_t*>(std::malloc(size + 16));
+    if (!p) return nullptr;
+    std::memcpy(p, &size, sizeof(size));
+    c->allocations++;
+    c->live++;
+    return p + 16;
+}
+void VKAPI_CALL counting_free(void* user, void* mem) {
+    if (!mem) return;
+    auto* c = static_cast<CountingAllocator*>(user);
+    c->frees++;
+    c->live--;
+    std::free(static_cast<uint8_t*>(mem) - 16);
+}
+}  // namespace
+
+int cpvh_allocator_check(cpvh_context* c, uint64_t* objects, uint64_t* allocations, uint64_t* frees) {
+    const Fns& f = c->f;
+    CountingAllocator counts;
+    VkAllocationCallbacks cb{};
+    cb.pUserData = &counts;
+    cb.pfnAllocation = counting_alloc;
+    cb.pfnFree = counting_free;
+    const VkAllocationCallbacks* a = &cb;
+    uint64_t n = 0;
+    VkResult r = VK_SUCCESS;
+    auto ok = [&](VkResult x) {
+        if (x != VK_SUCCESS && r == VK_SUCCESS) r = x;
+        if (x == VK_SUCCESS) n++;
+        return x == VK_SUCCESS;
+    };
+    VkBufferCreateInfo bi{};
+    bi.sType = VK_STRUCTURE_TYPE_BUFFER_CREATE_INFO;
+    bi.size = 4096;
+    bi.usage = VK_BUFFER_USAGE_TRANSFER_SRC_BIT;
+    VkBuffer buffer = nullptr;
+    if (ok(f.vkCreateBuffer(c->device, &bi, a, &buffer))) f.vkDestroyBuffer(c->device, buffer, a);
+    VkMemoryAllocateInfo ai{};
+    ai.sType = VK_STRUCTURE_TYPE_MEMORY_ALLOCATE_INFO;
+    ai.allocationSize = 4096;
+    ai.memoryTypeIndex = find_memory_type(c, ~0u, true);
+    VkDeviceMemory memory = nullptr;
+    if (ok(f.vkAllocateMemory(c->device, &ai, a, &memory))) f.vkFreeMemory(c->device, memory, a);
+    VkImageCreateInfo ii{};
+    ii.sType = VK_STRUCTURE_TYPE_IMAGE_CREATE_INFO;
+    ii.imageType = VK_IMAGE_TYPE_2D;
+    ii.format = VK_FORMAT_R8G8B8A8_UNORM;
+    ii.extent = {16, 16, 1};
+    ii.mipLevels = 1;
+    ii.arrayLayers = 1;
+    ii.samples = VK_SAMPLE_COUNT_1_BIT;
+    ii.usage = VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT;
+    VkImage image = nullptr;
+    if (ok(f.vkCreateImage(c->device, &ii, a, &image))) {
+        VkImageViewCreateInfo vi{};
+        vi.sType = VK_STRUCTURE_TYPE_IMAGE_VIEW_CREATE_INFO;
+        vi.image = image;
+        vi.viewType = VK_IMAGE_VIEW_TYPE_2D;
+        vi.format = ii.format;
+        vi.subresourceRange = {VK_IMAGE_ASPECT_COLOR_BIT, 0, 1, 0, 1};
+        VkImageView view = nullptr;
+        if (ok(f.vkCreateImageView(c->device, &vi, a, &view))) {
+            VkAttachmentDescription att{};
+            att.format = ii.format;
+            att.samples = VK_SAMPLE_COUNT_1_BIT;
+            VkAttachmentReference ref{0, VK_IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL};
+            VkSubpassDescription sub{};
+            sub.colorAttachmentCount = 1;
+            sub.pColorAttachments = &ref;
+            VkRenderPassCreateInfo rpi{};
+            rpi.sType = VK_STRUCTURE_TYPE_RENDER_PASS_CREATE_INFO;
+            rpi.attachmentCount = 1;
+            rpi.pAttachments = &att;
+            rpi.subpassCount = 1;
+            rpi.pSubpasses = &sub;
+            VkRenderPass pass = nullptr;
+            if (ok(f.vkCreateRenderPass(c->device, &rpi, a, &pass))) {
+                VkFramebufferCreateInfo fbi{};
+                fbi.sType = VK_STRUCTURE_TYPE_FRAMEBUFFER_CREATE_INFO;
+                fbi.renderPass = pass;
+                fbi.attachmentCount = 1;
+                fbi.pAttachments = &view;
+                fbi.width = fbi.height = 16;
+                fbi.layers = 1;
+                VkFramebuffer fb = nullptr;
+                if (ok(f.vkCreateFramebuffer(c->device, &fbi, a, &fb))) f.vkDestroyFramebuffer(c->device, fb, a);
+                f.vkDestroyRenderPass(c->device, pass, a);
+            }
+            f.vkDestroyImageView(c->device, view, a);
+        }
+        f.vkDestroyImage(c->device, image, a);
+    }
+    VkSamplerCreateInfo si{};
+    si.sType = VK_STRUCTURE_TYPE_SAMPLER_CREATE_INFO;
+    VkSampler sampler = nullptr;
+    if (ok(f.vkCreateSampler(c->device, &si, a, &sampler))) f.vkDestroySampler(c->device, sampler, a);
+    VkPipelineCacheCreateInfo pci{};
+    pci.sType = VK_STRUCTURE_TYPE_PIPELINE_CACHE_CREATE_INFO;
+    VkPipelineCache cache = nullptr;
+    if (ok(f.vkCreatePipelineCache(c->device, &pci, a, &cache))) f.vkDestroyPipelineCache(c->device, cache, a);
+    VkDescriptorSetLayoutCreateInfo dli{};
+    dli.sType = VK_STRUCTURE_TYPE_DESCRIPTOR_SET_LAYOUT_CREATE_INFO;
+    VkDescriptorSetLayout dsl = nullptr;
+    if (ok(f.vkCreateDescriptorSetLayout(c->device, &dli, a, &dsl))) {
+        VkPipelineLayoutCreateInfo pli{};
+        pli.sType = VK_STRUCTURE_TYPE_PIPELINE_LAYOUT_CREATE_INFO;
+        pli.setLayoutCount = 1;
+        pli.pSetLayouts = &dsl;
+        VkPipelineLayout layout = nullptr;
+        if (ok(f.vkCreatePipelineLayout(c->device, &pli, a, &layout))) f.vkDestroyPipelineLayout(c->device, layout, a);
+        f.vkDestroyDescriptorSetLayout(c->device, dsl, a);
+    }
+    VkDescriptorPoolCreateInfo dpi{};
+    dpi.sType = VK_STRUCTURE_TYPE_DESCRIPTOR_POOL_CREATE_INFO;
+    dpi.maxSets = 1;
+    VkDescriptorPool dpool = nullptr;
+    if (ok(f.vkCreateDescriptorPool(c->device, &dpi, a, &dpool))) f.vkDestroyDescriptorPool(c->device, dpool, a);
+    VkCommandPoolCreateInfo cpi{};
+    cpi.sType = VK_STRUCTURE_TYPE_COMMAND_POOL_CREATE_INFO;
+    VkCommandPool cpool = nullptr;
+    if (ok(f.vkCreateCommandPool(c->device, &cpi, a, &cpool))) f.vkDestroyCommandPool(c->device, cpool, a);
+    VkFenceCreateInfo fci{};
+    fci.sType = VK_STRUCTURE_TYPE_FENCE_CREATE_INFO;
+    VkFence fence = nullptr;
+    if (ok(f.vkCreateFence(c->device, &fci, a, &fence))) f.vkDestroyFence(c->device, fence, a);
+    *objects = n;
+    *allocations = counts.allocations;
+    *frees = counts.frees;
+    return r;
+}
+
 int cpvh_image_ops(cpvh_context* c, uint32_t format, uint32_t width, uint32_t height, uint32_t levels, const uint8_t* init0, const uint8_t* init1,
                    const cpvh_image_op* ops, uint32_t op_count, uint8_t* out, char* err, uint32_t err_len) {
     const Fns& f = c->f;

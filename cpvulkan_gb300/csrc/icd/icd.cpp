@@ -14,6 +14,7 @@
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
+#include <new>
 #include <thread>
 #include <unordered_map>
 
@@ -84,12 +85,36 @@ constexpr uint32_t kMemoryTypeDeviceOnly = 1;   // DEVICE_LOCAL
 
 std::mutex g_instance_mutex;
 
+// Host objects live in the application's allocator when it passes one, as
+// the reference's Allocate / Free do (CPVulkanBase/Base.h:256-294), else on
+// the ICD's heap; a destroy call passes the allocator its create call did.
+// (Pipelines, queues, command buffers and descriptor sets always use the
+// ICD's heap: the latter three belong to their device or pool.)
+template <typename T>
+T* host_new(const VkAllocationCallbacks* alloc, int scope) {
+    if (!alloc || !alloc->pfnAllocation) return new T();
+    void* p = alloc->pfnAllocation(alloc->pUserData, sizeof(T), alignof(T) < 16 ? 16 : alignof(T), scope);
+    return p ? new (p) T() : nullptr;
+}
+template <typename T>
+void host_delete(T* t, const VkAllocationCallbacks* alloc) {
+    if (!t) return;
+    if (!alloc || !alloc->pfnFree) {
+        delete t;
+        return;
+    }
+    t->~T();
+    alloc->pfnFree(alloc->pUserData, t);
+}
+constexpr int kScopeObject = 1, kScopeDevice = 3, kScopeInstance = 4;  // VkSystemAllocationScope
+
 // ---------------------------------------------------------------- instance --
 
-VKAPI_ATTR VkResult VKAPI_CALL CreateInstance(const VkInstanceCreateInfo* ci, const VkAllocationCallbacks*, VkInstance* out) {
+VKAPI_ATTR VkResult VKAPI_CALL CreateInstance(const VkInstanceCreateInfo* ci, const VkAllocationCallbacks* alloc, VkInstance* out) {
     if (!ci || !out) return VK_ERROR_INITIALIZATION_FAILED;
     for (uint32_t i = 0; i < ci->enabledExtensionCount; i++) return VK_ERROR_EXTENSION_NOT_PRESENT;
-    auto* inst = new Instance();
+    auto* inst = host_new<Instance>(alloc, kScopeInstance);
+    if (!inst) return VK_ERROR_OUT_OF_HOST_MEMORY;
     inst->physical = new PhysicalDevice();
     inst->physical->instance = inst;
     if (ci->pApplicationInfo && ci->pApplicationInfo->apiVersion) inst->api_version = ci->pApplicationInfo->apiVersion;
@@ -97,11 +122,11 @@ VKAPI_ATTR VkResult VKAPI_CALL CreateInstance(const VkInstanceCreateInfo* ci, co
     return VK_SUCCESS;
 }
 
-VKAPI_ATTR void VKAPI_CALL DestroyInstance(VkInstance instance, const VkAllocationCallbacks*) {
+VKAPI_ATTR void VKAPI_CALL DestroyInstance(VkInstance instance, const VkAllocationCallbacks* alloc) {
     auto* inst = reinterpret_cast<Instance*>(instance);
     if (!inst) return;
     delete inst->physical;
-    delete inst;
+    host_delete(inst, alloc);
 }
 
 VKAPI_ATTR VkResult VKAPI_CALL EnumerateInstanceExtensionProperties(const char*, uint32_t* count, VkExtensionProperties*) {
@@ -282,7 +307,7 @@ VKAPI_ATTR VkResult VKAPI_CALL EnumerateDeviceExtensionProperties(VkPhysicalDevi
 
 // ------------------------------------------------------------------ device --
 
-VKAPI_ATTR VkResult VKAPI_CALL CreateDevice(VkPhysicalDevice pd, const VkDeviceCreateInfo* ci, const VkAllocationCallbacks*, VkDevice* out) {
+VKAPI_ATTR VkResult VKAPI_CALL CreateDevice(VkPhysicalDevice pd, const VkDeviceCreateInfo* ci, const VkAllocationCallbacks* alloc, VkDevice* out) {
     if (!ci || !out) return VK_ERROR_INITIALIZATION_FAILED;
     for (uint32_t i = 0; i < ci->enabledExtensionCount; i++) {
         bool known = false;
@@ -301,7 +326,8 @@ VKAPI_ATTR VkResult VKAPI_CALL CreateDevice(VkPhysicalDevice pd, const VkDeviceC
     uint32_t queues = 1;
     if (ci->queueCreateInfoCount >= 1 && ci->pQueueCreateInfos) queues = ci->pQueueCreateInfos[0].queueCount;
     if (queues < 1 || queues > kMaxQueues) return VK_ERROR_INITIALIZATION_FAILED;
-    auto* dev = new Device();
+    auto* dev = host_new<Device>(alloc, kScopeDevice);
+    if (!dev) return VK_ERROR_OUT_OF_HOST_MEMORY;
     dev->physical = reinterpret_cast<PhysicalDevice*>(pd);
     dev->compile_only = !rt::available();
     for (uint32_t i = 0; i < queues; i++) {
@@ -314,7 +340,7 @@ VKAPI_ATTR VkResult VKAPI_CALL CreateDevice(VkPhysicalDevice pd, const VkDeviceC
                 if (x->stream) cudaStreamDestroy(x->stream);
                 delete x;
             }
-            delete dev;
+            host_delete(dev, alloc);
             return VK_ERROR_INITIALIZATION_FAILED;
         }
     }
@@ -323,7 +349,7 @@ VKAPI_ATTR VkResult VKAPI_CALL CreateDevice(VkPhysicalDevice pd, const VkDeviceC
     return VK_SUCCESS;
 }
 
-VKAPI_ATTR void VKAPI_CALL DestroyDevice(VkDevice device, const VkAllocationCallbacks*) {
+VKAPI_ATTR void VKAPI_CALL DestroyDevice(VkDevice device, const VkAllocationCallbacks* alloc) {
     auto* dev = reinterpret_cast<Device*>(device);
     if (!dev) return;
     if (!dev->compile_only) {
@@ -334,7 +360,7 @@ VKAPI_ATTR void VKAPI_CALL DestroyDevice(VkDevice device, const VkAllocationCall
         for (auto& kv : dev->batch_modules) rt::unload(*kv.second);
     }
     for (Queue* q : dev->queues) delete q;
-    delete dev;
+    host_delete(dev, alloc);
 }
 
 VKAPI_ATTR void VKAPI_CALL GetDeviceQueue(VkDevice device, uint32_t, uint32_t index, VkQueue* q) {
@@ -382,10 +408,11 @@ VKAPI_ATTR VkResult VKAPI_CALL QueueWaitIdle(VkQueue queue) {
 
 // ------------------------------------------------------------------ memory --
 
-VKAPI_ATTR VkResult VKAPI_CALL AllocateMemory(VkDevice device, const VkMemoryAllocateInfo* ai, const VkAllocationCallbacks*, VkDeviceMemory* out) {
+VKAPI_ATTR VkResult VKAPI_CALL AllocateMemory(VkDevice device, const VkMemoryAllocateInfo* ai, const VkAllocationCallbacks* alloc, VkDeviceMemory* out) {
     auto* dev = reinterpret_cast<Device*>(device);
     if (ai->memoryTypeIndex > kMemoryTypeDeviceOnly) return VK_ERROR_OUT_OF_DEVICE_MEMORY;
-    auto* m = new DeviceMemory();
+    auto* m = host_new<DeviceMemory>(alloc, kScopeObject);
+    if (!m) return VK_ERROR_OUT_OF_HOST_MEMORY;
     m->size = ai->allocationSize;
     m->type = ai->memoryTypeIndex;
     const size_t bytes = m->size ? m->size : 1;
@@ -399,14 +426,14 @@ VKAPI_ATTR VkResult VKAPI_CALL AllocateMemory(VkDevice device, const VkMemoryAll
     }
     if (cudaMalloc(reinterpret_cast<void**>(&m->device), bytes) != cudaSuccess) {
         cudaGetLastError();
-        delete m;
+        host_delete(m, alloc);
         return VK_ERROR_OUT_OF_DEVICE_MEMORY;
     }
     if (m->type == kMemoryTypeHostVisible) {
         if (cudaMallocHost(reinterpret_cast<void**>(&m->host), bytes) != cudaSuccess) {
             cudaGetLastError();
             cudaFree(m->device);
-            delete m;
+            host_delete(m, alloc);
             return VK_ERROR_OUT_OF_HOST_MEMORY;
         }
         std::memset(m->host, 0, bytes);
@@ -419,7 +446,7 @@ VKAPI_ATTR VkResult VKAPI_CALL AllocateMemory(VkDevice device, const VkMemoryAll
     return VK_SUCCESS;
 }
 
-VKAPI_ATTR void VKAPI_CALL FreeMemory(VkDevice device, VkDeviceMemory memory, const VkAllocationCallbacks*) {
+VKAPI_ATTR void VKAPI_CALL FreeMemory(VkDevice device, VkDeviceMemory memory, const VkAllocationCallbacks* alloc) {
     auto* dev = reinterpret_cast<Device*>(device);
     auto* m = reinterpret_cast<DeviceMemory*>(memory);
     if (!m) return;
@@ -435,12 +462,12 @@ VKAPI_ATTR void VKAPI_CALL FreeMemory(VkDevice device, VkDeviceMemory memory, co
     if (dev->compile_only) {
         std::free(m->device);
         std::free(m->host);
-        delete m;
+        host_delete(m, alloc);
         return;
     }
     cudaFree(m->device);
     if (m->host) cudaFreeHost(m->host);
-    delete m;
+    host_delete(m, alloc);
 }
 
 VKAPI_ATTR VkResult VKAPI_CALL MapMemory(VkDevice device, VkDeviceMemory memory, VkDeviceSize offset, VkDeviceSize, VkMemoryMapFlags, void** data) {
@@ -513,14 +540,15 @@ VKAPI_ATTR VkResult VKAPI_CALL InvalidateMappedMemoryRanges(VkDevice device, uin
 
 // --------------------------------------------------------- buffers, images --
 
-VKAPI_ATTR VkResult VKAPI_CALL CreateBuffer(VkDevice, const VkBufferCreateInfo* ci, const VkAllocationCallbacks*, VkBuffer* out) {
-    auto* b = new Buffer();
+VKAPI_ATTR VkResult VKAPI_CALL CreateBuffer(VkDevice, const VkBufferCreateInfo* ci, const VkAllocationCallbacks* alloc, VkBuffer* out) {
+    auto* b = host_new<Buffer>(alloc, kScopeObject);
+    if (!b) return VK_ERROR_OUT_OF_HOST_MEMORY;
     b->size = ci->size;
     b->usage = ci->usage;
     *out = to_handle<VkBuffer>(b);
     return VK_SUCCESS;
 }
-VKAPI_ATTR void VKAPI_CALL DestroyBuffer(VkDevice, VkBuffer b, const VkAllocationCallbacks*) { delete reinterpret_cast<Buffer*>(b); }
+VKAPI_ATTR void VKAPI_CALL DestroyBuffer(VkDevice, VkBuffer b, const VkAllocationCallbacks* alloc) { host_delete(reinterpret_cast<Buffer*>(b), alloc); }
 VKAPI_ATTR void VKAPI_CALL GetBufferMemoryRequirements(VkDevice, VkBuffer buffer, VkMemoryRequirements* r) {
     auto* b = reinterpret_cast<Buffer*>(buffer);
     r->size = (b->size + 255) & ~255ull;
@@ -536,10 +564,11 @@ VKAPI_ATTR VkResult VKAPI_CALL BindBufferMemory(VkDevice, VkBuffer buffer, VkDev
     return VK_SUCCESS;
 }
 
-VKAPI_ATTR VkResult VKAPI_CALL CreateImage(VkDevice, const VkImageCreateInfo* ci, const VkAllocationCallbacks*, VkImage* out) {
+VKAPI_ATTR VkResult VKAPI_CALL CreateImage(VkDevice, const VkImageCreateInfo* ci, const VkAllocationCallbacks* alloc, VkImage* out) {
     const uint32_t texel = format_texel_size(ci->format);
     if (!texel || ci->samples > 1) return VK_ERROR_FORMAT_NOT_SUPPORTED;
-    auto* img = new Image();
+    auto* img = host_new<Image>(alloc, kScopeObject);
+    if (!img) return VK_ERROR_OUT_OF_HOST_MEMORY;
     img->format = ci->format;
     img->texel = texel;
     img->extent = ci->extent;
@@ -549,7 +578,7 @@ VKAPI_ATTR VkResult VKAPI_CALL CreateImage(VkDevice, const VkImageCreateInfo* ci
     *out = to_handle<VkImage>(img);
     return VK_SUCCESS;
 }
-VKAPI_ATTR void VKAPI_CALL DestroyImage(VkDevice, VkImage i, const VkAllocationCallbacks*) { delete reinterpret_cast<Image*>(i); }
+VKAPI_ATTR void VKAPI_CALL DestroyImage(VkDevice, VkImage i, const VkAllocationCallbacks* alloc) { host_delete(reinterpret_cast<Image*>(i), alloc); }
 VKAPI_ATTR void VKAPI_CALL GetImageMemoryRequirements(VkDevice, VkImage image, VkMemoryRequirements* r) {
     auto* img = reinterpret_cast<Image*>(image);
     r->size = (img->total_size + 255) & ~255ull;
@@ -574,8 +603,9 @@ VKAPI_ATTR void VKAPI_CALL GetImageSubresourceLayout(VkDevice, VkImage image, co
     out->depthPitch = L.plane;
 }
 
-VKAPI_ATTR VkResult VKAPI_CALL CreateImageView(VkDevice, const VkImageViewCreateInfo* ci, const VkAllocationCallbacks*, VkImageView* out) {
-    auto* v = new ImageView();
+VKAPI_ATTR VkResult VKAPI_CALL CreateImageView(VkDevice, const VkImageViewCreateInfo* ci, const VkAllocationCallbacks* alloc, VkImageView* out) {
+    auto* v = host_new<ImageView>(alloc, kScopeObject);
+    if (!v) return VK_ERROR_OUT_OF_HOST_MEMORY;
     v->image = reinterpret_cast<Image*>(ci->image);
     v->format = ci->format;
     v->range = ci->subresourceRange;
@@ -585,39 +615,42 @@ VKAPI_ATTR VkResult VKAPI_CALL CreateImageView(VkDevice, const VkImageViewCreate
     *out = to_handle<VkImageView>(v);
     return VK_SUCCESS;
 }
-VKAPI_ATTR void VKAPI_CALL DestroyImageView(VkDevice, VkImageView v, const VkAllocationCallbacks*) { delete reinterpret_cast<ImageView*>(v); }
+VKAPI_ATTR void VKAPI_CALL DestroyImageView(VkDevice, VkImageView v, const VkAllocationCallbacks* alloc) { host_delete(reinterpret_cast<ImageView*>(v), alloc); }
 
-VKAPI_ATTR VkResult VKAPI_CALL CreateSampler(VkDevice, const VkSamplerCreateInfo* ci, const VkAllocationCallbacks*, VkSampler* out) {
+VKAPI_ATTR VkResult VKAPI_CALL CreateSampler(VkDevice, const VkSamplerCreateInfo* ci, const VkAllocationCallbacks* alloc, VkSampler* out) {
     if (ci->anisotropyEnable || ci->compareEnable || ci->unnormalizedCoordinates) return VK_ERROR_FEATURE_NOT_PRESENT;
-    auto* s = new Sampler();
+    auto* s = host_new<Sampler>(alloc, kScopeObject);
+    if (!s) return VK_ERROR_OUT_OF_HOST_MEMORY;
     s->info = *ci;
     s->info.pNext = nullptr;
     *out = to_handle<VkSampler>(s);
     return VK_SUCCESS;
 }
-VKAPI_ATTR void VKAPI_CALL DestroySampler(VkDevice, VkSampler s, const VkAllocationCallbacks*) { delete reinterpret_cast<Sampler*>(s); }
+VKAPI_ATTR void VKAPI_CALL DestroySampler(VkDevice, VkSampler s, const VkAllocationCallbacks* alloc) { host_delete(reinterpret_cast<Sampler*>(s), alloc); }
 
 // --------------------------------------------------------------- shaders --
 
-VKAPI_ATTR VkResult VKAPI_CALL CreateShaderModule(VkDevice, const VkShaderModuleCreateInfo* ci, const VkAllocationCallbacks*, VkShaderModule* out) {
-    auto* sm = new ShaderModule();
+VKAPI_ATTR VkResult VKAPI_CALL CreateShaderModule(VkDevice, const VkShaderModuleCreateInfo* ci, const VkAllocationCallbacks* alloc, VkShaderModule* out) {
+    auto* sm = host_new<ShaderModule>(alloc, kScopeObject);
+    if (!sm) return VK_ERROR_OUT_OF_HOST_MEMORY;
     sm->words.assign(ci->pCode, ci->pCode + ci->codeSize / 4);
     std::string err;
     if (!spirv::parse(sm->words.data(), sm->words.size(), sm->module, err)) {
         rt::set_last_error("vkCreateShaderModule: " + err);
-        delete sm;
+        host_delete(sm, alloc);
         return VK_ERROR_INITIALIZATION_FAILED;
     }
     *out = to_handle<VkShaderModule>(sm);
     return VK_SUCCESS;
 }
-VKAPI_ATTR void VKAPI_CALL DestroyShaderModule(VkDevice, VkShaderModule s, const VkAllocationCallbacks*) { delete reinterpret_cast<ShaderModule*>(s); }
+VKAPI_ATTR void VKAPI_CALL DestroyShaderModule(VkDevice, VkShaderModule s, const VkAllocationCallbacks* alloc) { host_delete(reinterpret_cast<ShaderModule*>(s), alloc); }
 
 // Pipeline cache blob: 32-byte header {size, version 1, vendor, device,
 // UUID[16]} + u32 count + {key[32], u32 size, cubin} entries — the layout of
 // CPVulkan/PipelineCache.cpp:5-120 with a cubin payload.
-VKAPI_ATTR VkResult VKAPI_CALL CreatePipelineCache(VkDevice, const VkPipelineCacheCreateInfo* ci, const VkAllocationCallbacks*, VkPipelineCache* out) {
-    auto* c = new PipelineCache();
+VKAPI_ATTR VkResult VKAPI_CALL CreatePipelineCache(VkDevice, const VkPipelineCacheCreateInfo* ci, const VkAllocationCallbacks* alloc, VkPipelineCache* out) {
+    auto* c = host_new<PipelineCache>(alloc, kScopeObject);
+    if (!c) return VK_ERROR_OUT_OF_HOST_MEMORY;
     const uint8_t* d = static_cast<const uint8_t*>(ci->pInitialData);
     size_t n = ci->initialDataSize;
     if (d && n >= 36) {
@@ -638,7 +671,7 @@ VKAPI_ATTR VkResult VKAPI_CALL CreatePipelineCache(VkDevice, const VkPipelineCac
     *out = to_handle<VkPipelineCache>(c);
     return VK_SUCCESS;
 }
-VKAPI_ATTR void VKAPI_CALL DestroyPipelineCache(VkDevice, VkPipelineCache c, const VkAllocationCallbacks*) { delete reinterpret_cast<PipelineCache*>(c); }
+VKAPI_ATTR void VKAPI_CALL DestroyPipelineCache(VkDevice, VkPipelineCache c, const VkAllocationCallbacks* alloc) { host_delete(reinterpret_cast<PipelineCache*>(c), alloc); }
 VKAPI_ATTR VkResult VKAPI_CALL GetPipelineCacheData(VkDevice, VkPipelineCache cache, size_t* size, void* data) {
     auto* c = reinterpret_cast<PipelineCache*>(cache);
     std::lock_guard<std::mutex> lock(c->mutex);
@@ -691,20 +724,22 @@ VKAPI_ATTR void VKAPI_CALL DestroyPipeline(VkDevice, VkPipeline pipeline, const 
     delete p;
 }
 
-VKAPI_ATTR VkResult VKAPI_CALL CreatePipelineLayout(VkDevice, const VkPipelineLayoutCreateInfo* ci, const VkAllocationCallbacks*, VkPipelineLayout* out) {
-    auto* l = new PipelineLayout();
+VKAPI_ATTR VkResult VKAPI_CALL CreatePipelineLayout(VkDevice, const VkPipelineLayoutCreateInfo* ci, const VkAllocationCallbacks* alloc, VkPipelineLayout* out) {
+    auto* l = host_new<PipelineLayout>(alloc, kScopeObject);
+    if (!l) return VK_ERROR_OUT_OF_HOST_MEMORY;
     for (uint32_t i = 0; i < ci->setLayoutCount; i++) l->sets.push_back(reinterpret_cast<DescriptorSetLayout*>(ci->pSetLayouts[i]));
     for (uint32_t i = 0; i < ci->pushConstantRangeCount; i++) l->push.push_back(ci->pPushConstantRanges[i]);
     *out = to_handle<VkPipelineLayout>(l);
     return VK_SUCCESS;
 }
-VKAPI_ATTR void VKAPI_CALL DestroyPipelineLayout(VkDevice, VkPipelineLayout l, const VkAllocationCallbacks*) { delete reinterpret_cast<PipelineLayout*>(l); }
+VKAPI_ATTR void VKAPI_CALL DestroyPipelineLayout(VkDevice, VkPipelineLayout l, const VkAllocationCallbacks* alloc) { host_delete(reinterpret_cast<PipelineLayout*>(l), alloc); }
 
 // ------------------------------------------------------------ descriptors --
 
-VKAPI_ATTR VkResult VKAPI_CALL CreateDescriptorSetLayout(VkDevice, const VkDescriptorSetLayoutCreateInfo* ci, const VkAllocationCallbacks*,
+VKAPI_ATTR VkResult VKAPI_CALL CreateDescriptorSetLayout(VkDevice, const VkDescriptorSetLayoutCreateInfo* ci, const VkAllocationCallbacks* alloc,
                                                          VkDescriptorSetLayout* out) {
-    auto* l = new DescriptorSetLayout();
+    auto* l = host_new<DescriptorSetLayout>(alloc, kScopeObject);
+    if (!l) return VK_ERROR_OUT_OF_HOST_MEMORY;
     for (uint32_t i = 0; i < ci->bindingCount; i++) {
         VkDescriptorSetLayoutBinding b = ci->pBindings[i];
         std::vector<Sampler*> imm;
@@ -717,18 +752,20 @@ VKAPI_ATTR VkResult VKAPI_CALL CreateDescriptorSetLayout(VkDevice, const VkDescr
     *out = to_handle<VkDescriptorSetLayout>(l);
     return VK_SUCCESS;
 }
-VKAPI_ATTR void VKAPI_CALL DestroyDescriptorSetLayout(VkDevice, VkDescriptorSetLayout l, const VkAllocationCallbacks*) {
-    delete reinterpret_cast<DescriptorSetLayout*>(l);
+VKAPI_ATTR void VKAPI_CALL DestroyDescriptorSetLayout(VkDevice, VkDescriptorSetLayout l, const VkAllocationCallbacks* alloc) {
+    host_delete(reinterpret_cast<DescriptorSetLayout*>(l), alloc);
 }
-VKAPI_ATTR VkResult VKAPI_CALL CreateDescriptorPool(VkDevice, const VkDescriptorPoolCreateInfo*, const VkAllocationCallbacks*, VkDescriptorPool* out) {
-    *out = to_handle<VkDescriptorPool>(new DescriptorPool());
+VKAPI_ATTR VkResult VKAPI_CALL CreateDescriptorPool(VkDevice, const VkDescriptorPoolCreateInfo*, const VkAllocationCallbacks* alloc, VkDescriptorPool* out) {
+    auto* p = host_new<DescriptorPool>(alloc, kScopeObject);
+    if (!p) return VK_ERROR_OUT_OF_HOST_MEMORY;
+    *out = to_handle<VkDescriptorPool>(p);
     return VK_SUCCESS;
 }
-VKAPI_ATTR void VKAPI_CALL DestroyDescriptorPool(VkDevice, VkDescriptorPool pool, const VkAllocationCallbacks*) {
+VKAPI_ATTR void VKAPI_CALL DestroyDescriptorPool(VkDevice, VkDescriptorPool pool, const VkAllocationCallbacks* alloc) {
     auto* p = reinterpret_cast<DescriptorPool*>(pool);
     if (!p) return;
     for (auto* s : p->sets) delete s;
-    delete p;
+    host_delete(p, alloc);
 }
 VKAPI_ATTR VkResult VKAPI_CALL AllocateDescriptorSets(VkDevice, const VkDescriptorSetAllocateInfo* ai, VkDescriptorSet* out) {
     auto* pool = reinterpret_cast<DescriptorPool*>(ai->descriptorPool);
@@ -800,12 +837,13 @@ VKAPI_ATTR void VKAPI_CALL UpdateDescriptorSets(VkDevice, uint32_t nw, const VkW
 
 // ------------------------------------------------- render pass, framebuffer --
 
-VKAPI_ATTR VkResult VKAPI_CALL CreateRenderPass(VkDevice, const VkRenderPassCreateInfo* ci, const VkAllocationCallbacks*, VkRenderPass* out) {
+VKAPI_ATTR VkResult VKAPI_CALL CreateRenderPass(VkDevice, const VkRenderPassCreateInfo* ci, const VkAllocationCallbacks* alloc, VkRenderPass* out) {
     if (ci->subpassCount != 1) {
         rt::set_last_error("vkCreateRenderPass: only single-subpass render passes are supported");
         return VK_ERROR_FEATURE_NOT_PRESENT;
     }
-    auto* rp = new RenderPass();
+    auto* rp = host_new<RenderPass>(alloc, kScopeObject);
+    if (!rp) return VK_ERROR_OUT_OF_HOST_MEMORY;
     rp->attachments.assign(ci->pAttachments, ci->pAttachments + ci->attachmentCount);
     const auto& sp = ci->pSubpasses[0];
     for (uint32_t i = 0; i < sp.colorAttachmentCount; i++)
@@ -814,10 +852,11 @@ VKAPI_ATTR VkResult VKAPI_CALL CreateRenderPass(VkDevice, const VkRenderPassCrea
     *out = to_handle<VkRenderPass>(rp);
     return VK_SUCCESS;
 }
-VKAPI_ATTR void VKAPI_CALL DestroyRenderPass(VkDevice, VkRenderPass rp, const VkAllocationCallbacks*) { delete reinterpret_cast<RenderPass*>(rp); }
+VKAPI_ATTR void VKAPI_CALL DestroyRenderPass(VkDevice, VkRenderPass rp, const VkAllocationCallbacks* alloc) { host_delete(reinterpret_cast<RenderPass*>(rp), alloc); }
 
-VKAPI_ATTR VkResult VKAPI_CALL CreateFramebuffer(VkDevice, const VkFramebufferCreateInfo* ci, const VkAllocationCallbacks*, VkFramebuffer* out) {
-    auto* fb = new Framebuffer();
+VKAPI_ATTR VkResult VKAPI_CALL CreateFramebuffer(VkDevice, const VkFramebufferCreateInfo* ci, const VkAllocationCallbacks* alloc, VkFramebuffer* out) {
+    auto* fb = host_new<Framebuffer>(alloc, kScopeObject);
+    if (!fb) return VK_ERROR_OUT_OF_HOST_MEMORY;
     fb->pass = reinterpret_cast<RenderPass*>(ci->renderPass);
     for (uint32_t i = 0; i < ci->attachmentCount; i++) fb->attachments.push_back(reinterpret_cast<ImageView*>(ci->pAttachments[i]));
     fb->width = ci->width;
@@ -826,19 +865,21 @@ VKAPI_ATTR VkResult VKAPI_CALL CreateFramebuffer(VkDevice, const VkFramebufferCr
     *out = to_handle<VkFramebuffer>(fb);
     return VK_SUCCESS;
 }
-VKAPI_ATTR void VKAPI_CALL DestroyFramebuffer(VkDevice, VkFramebuffer fb, const VkAllocationCallbacks*) { delete reinterpret_cast<Framebuffer*>(fb); }
+VKAPI_ATTR void VKAPI_CALL DestroyFramebuffer(VkDevice, VkFramebuffer fb, const VkAllocationCallbacks* alloc) { host_delete(reinterpret_cast<Framebuffer*>(fb), alloc); }
 
 // ------------------------------------------------------- command buffers --
 
-VKAPI_ATTR VkResult VKAPI_CALL CreateCommandPool(VkDevice, const VkCommandPoolCreateInfo*, const VkAllocationCallbacks*, VkCommandPool* out) {
-    *out = to_handle<VkCommandPool>(new CommandPool());
+VKAPI_ATTR VkResult VKAPI_CALL CreateCommandPool(VkDevice, const VkCommandPoolCreateInfo*, const VkAllocationCallbacks* alloc, VkCommandPool* out) {
+    auto* p = host_new<CommandPool>(alloc, kScopeObject);
+    if (!p) return VK_ERROR_OUT_OF_HOST_MEMORY;
+    *out = to_handle<VkCommandPool>(p);
     return VK_SUCCESS;
 }
-VKAPI_ATTR void VKAPI_CALL DestroyCommandPool(VkDevice, VkCommandPool pool, const VkAllocationCallbacks*) {
+VKAPI_ATTR void VKAPI_CALL DestroyCommandPool(VkDevice, VkCommandPool pool, const VkAllocationCallbacks* alloc) {
     auto* p = reinterpret_cast<CommandPool*>(pool);
     if (!p) return;
     for (auto* cb : p->buffers) delete cb;
-    delete p;
+    host_delete(p, alloc);
 }
 VKAPI_ATTR VkResult VKAPI_CALL ResetCommandPool(VkDevice, VkCommandPool pool, VkCommandPoolResetFlags) {
     for (auto* cb : reinterpret_cast<CommandPool*>(pool)->buffers) cb->reset();
@@ -1060,22 +1101,23 @@ VKAPI_ATTR void VKAPI_CALL CmdEndRenderPass(VkCommandBuffer cmd) { push(cmd, Cmd
 
 // ------------------------------------------------------ sync and submit --
 
-VKAPI_ATTR VkResult VKAPI_CALL CreateFence(VkDevice, const VkFenceCreateInfo* ci, const VkAllocationCallbacks*, VkFence* out) {
-    auto* f = new Fence();
+VKAPI_ATTR VkResult VKAPI_CALL CreateFence(VkDevice, const VkFenceCreateInfo* ci, const VkAllocationCallbacks* alloc, VkFence* out) {
+    auto* f = host_new<Fence>(alloc, kScopeObject);
+    if (!f) return VK_ERROR_OUT_OF_HOST_MEMORY;
     if (rt::available() && cudaEventCreateWithFlags(&f->event, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
-        delete f;
+        host_delete(f, alloc);
         return VK_ERROR_OUT_OF_DEVICE_MEMORY;
     }
     f->signalled = (ci->flags & VK_FENCE_CREATE_SIGNALED_BIT) != 0;
     *out = to_handle<VkFence>(f);
     return VK_SUCCESS;
 }
-VKAPI_ATTR void VKAPI_CALL DestroyFence(VkDevice, VkFence fence, const VkAllocationCallbacks*) {
+VKAPI_ATTR void VKAPI_CALL DestroyFence(VkDevice, VkFence fence, const VkAllocationCallbacks* alloc) {
     auto* f = reinterpret_cast<Fence*>(fence);
     if (!f) return;
     if (f->event) cudaEventDestroy(f->event);
-    delete f;
+    host_delete(f, alloc);
 }
 VKAPI_ATTR VkResult VKAPI_CALL ResetFences(VkDevice, uint32_t n, const VkFence* fences) {
     for (uint32_t i = 0; i < n; i++) {
@@ -1137,21 +1179,22 @@ VKAPI_ATTR VkResult VKAPI_CALL WaitForFences(VkDevice device, uint32_t n, const 
     }
 }
 
-VKAPI_ATTR VkResult VKAPI_CALL CreateSemaphore(VkDevice, const VkSemaphoreCreateInfo*, const VkAllocationCallbacks*, VkSemaphore* out) {
-    auto* s = new Semaphore();
+VKAPI_ATTR VkResult VKAPI_CALL CreateSemaphore(VkDevice, const VkSemaphoreCreateInfo*, const VkAllocationCallbacks* alloc, VkSemaphore* out) {
+    auto* s = host_new<Semaphore>(alloc, kScopeObject);
+    if (!s) return VK_ERROR_OUT_OF_HOST_MEMORY;
     if (rt::available() && cudaEventCreateWithFlags(&s->event, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
-        delete s;
+        host_delete(s, alloc);
         return VK_ERROR_OUT_OF_DEVICE_MEMORY;
     }
     *out = to_handle<VkSemaphore>(s);
     return VK_SUCCESS;
 }
-VKAPI_ATTR void VKAPI_CALL DestroySemaphore(VkDevice, VkSemaphore sem, const VkAllocationCallbacks*) {
+VKAPI_ATTR void VKAPI_CALL DestroySemaphore(VkDevice, VkSemaphore sem, const VkAllocationCallbacks* alloc) {
     auto* s = reinterpret_cast<Semaphore*>(sem);
     if (!s) return;
     if (s->event) cudaEventDestroy(s->event);
-    delete s;
+    host_delete(s, alloc);
 }
 
 // vkQueueSubmit (CPVulkan/Queue.cpp:11-77): waits, replays each command

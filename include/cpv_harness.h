@@ -90,6 +90,14 @@ int cpvh_renderer_set_indirect_count(cpvh_renderer* r, uint32_t draw, uint32_t c
 /* Reads the attachments back (colour: width*height*4; depth: texel-sized). */
 int cpvh_readback(cpvh_renderer* r, uint8_t* color, uint8_t* depth);
 
+/* Creates and destroys one of each host object kind the ICD places in an
+ * application allocator (buffer, device memory, image, image view, render
+ * pass, framebuffer, sampler, pipeline cache, descriptor set layout,
+ * pipeline layout, descriptor pool, command pool, fence), passing a counting
+ * VkAllocationCallbacks to every call; reports the objects created and the
+ * allocator's allocations and frees. Returns the first failing VkResult. */
+int cpvh_allocator_check(cpvh_context* ctx, uint64_t* objects, uint64_t* allocations, uint64_t* frees);
+
 /* One transfer / clear command of cpvh_image_ops on image 0 (image 1 is a
  * copy source). */
 enum {

@@ -130,3 +130,18 @@ def test_indirect_count_extension(native):
     assert enum(None, None, ctypes.byref(one), props) == 5 and one.value == 1  # VK_INCOMPLETE
     assert enum(None, None, ctypes.byref(n), props) == 0
     assert {(p.name, p.version) for p in props} == {(b"VK_KHR_draw_indirect_count", 1), (b"VK_AMD_draw_indirect_count", 2)}
+
+
+def test_host_objects_use_the_application_allocator(native, monkeypatch):
+    """Objects created with VkAllocationCallbacks live in the application's
+    allocator and go back to it on destruction (the reference's Allocate /
+    Free, CPVulkanBase/Base.h:256-294): one allocation and one free per
+    object, none outstanding. Runs on the compile-only device."""
+    monkeypatch.setenv("CPV_COMPILE_ONLY", "1")
+    ctx = c.Context()
+    try:
+        objects, allocations, frees = ctx.allocator_check()
+    finally:
+        ctx.close()
+    assert objects == 13
+    assert allocations == objects and frees == allocations
