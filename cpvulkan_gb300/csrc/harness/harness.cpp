@@ -313,15 +313,23 @@ void record_frame(cpvh_renderer* r, VkCommandBuffer cmd) {
     const cpv_scene* s = r->scene;
     VkClearValue clears[2];
     std::memset(clears, 0, sizeof(clears));
-    for (int i = 0; i < 4; i++) clears[0].color.float32[i] = s->clear_color[i];
-    clears[1].depthStencil.depth = s->clear_depth;
-    clears[1].depthStencil.stencil = s->clear_stencil;
+    // in attachment order: colour (absent in a depth-only pass), depth
+    uint32_t nclears = 0;
+    if (s->color_format) {
+        for (int i = 0; i < 4; i++) clears[nclears].color.float32[i] = s->clear_color[i];
+        nclears++;
+    }
+    if (s->depth_format) {
+        clears[nclears].depthStencil.depth = s->clear_depth;
+        clears[nclears].depthStencil.stencil = s->clear_stencil;
+        nclears++;
+    }
     VkRenderPassBeginInfo rb{};
     rb.sType = VK_STRUCTURE_TYPE_RENDER_PASS_BEGIN_INFO;
     rb.renderPass = r->pass;
     rb.framebuffer = r->fb;
     rb.renderArea = {{0, 0}, {s->width, s->height}};
-    rb.clearValueCount = s->depth_format ? 2 : 1;
+    rb.clearValueCount = nclears;
     rb.pClearValues = clears;
     c->f.vkCmdBeginRenderPass(cmd, &rb, VK_SUBPASS_CONTENTS_INLINE);
     uint32_t bound = ~0u;
@@ -362,7 +370,7 @@ void record_readback(cpvh_renderer* r, VkCommandBuffer cmd) {
     VkBufferImageCopy bc{};
     bc.imageSubresource = {VK_IMAGE_ASPECT_COLOR_BIT, 0, 0, 1};
     bc.imageExtent = {s->width, s->height, 1};
-    c->f.vkCmdCopyImageToBuffer(cmd, r->colour.image, VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL, r->readback.buffer, 1, &bc);
+    if (s->color_format) c->f.vkCmdCopyImageToBuffer(cmd, r->colour.image, VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL, r->readback.buffer, 1, &bc);
     if (s->depth_format) {
         bc.bufferOffset = static_cast<VkDeviceSize>(s->width) * s->height * 4;
         bc.imageSubresource.aspectMask = VK_IMAGE_ASPECT_DEPTH_BIT;
@@ -469,7 +477,7 @@ bool build_pipelines(cpvh_context* c, const cpv_scene* s, VkRenderPass pass, VkP
         cbs.sType = VK_STRUCTURE_TYPE_PIPELINE_COLOR_BLEND_STATE_CREATE_INFO;
         cbs.logicOpEnable = sp.logic_op_enable;
         cbs.logicOp = static_cast<VkLogicOp>(sp.logic_op);
-        cbs.attachmentCount = 1;
+        cbs.attachmentCount = s->color_format ? 1 : 0;
         cbs.pAttachments = &cba;
         for (int k = 0; k < 4; k++) cbs.blendConstants[k] = sp.blend_constants[k];
         VkGraphicsPipelineCreateInfo gpi{};
@@ -492,31 +500,47 @@ bool build_pipelines(cpvh_context* c, const cpv_scene* s, VkRenderPass pass, VkP
     return true;
 }
 
-VkResult make_pass_and_layout(cpvh_context* c, const cpv_scene* s, bool with_sets, VkRenderPass& pass, VkDescriptorSetLayout& set_layout,
-                              VkPipelineLayout& layout) {
-    const Fns& f = c->f;
+// The scene's render pass: a cleared colour attachment (none in a
+// depth-only pass) then a cleared depth/stencil attachment (when the scene
+// has a depth format), both stored.
+VkResult create_scene_pass(cpvh_context* c, const cpv_scene* s, VkRenderPass* out) {
     VkAttachmentDescription att[2]{};
-    att[0].format = static_cast<VkFormat>(s->color_format);
-    att[0].samples = VK_SAMPLE_COUNT_1_BIT;
-    att[0].loadOp = VK_ATTACHMENT_LOAD_OP_CLEAR;
-    att[0].storeOp = VK_ATTACHMENT_STORE_OP_STORE;
-    att[0].stencilLoadOp = VK_ATTACHMENT_LOAD_OP_DONT_CARE;
-    att[0].finalLayout = VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL;
-    att[1] = att[0];
-    att[1].format = static_cast<VkFormat>(s->depth_format);
-    att[1].stencilLoadOp = VK_ATTACHMENT_LOAD_OP_CLEAR;
-    VkAttachmentReference cref{0, VK_IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL}, dref{1, VK_IMAGE_LAYOUT_DEPTH_STENCIL_ATTACHMENT_OPTIMAL};
+    VkAttachmentReference cref{0, VK_IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL}, dref{0, VK_IMAGE_LAYOUT_DEPTH_STENCIL_ATTACHMENT_OPTIMAL};
+    uint32_t n = 0;
     VkSubpassDescription sub{};
-    sub.colorAttachmentCount = 1;
-    sub.pColorAttachments = &cref;
-    sub.pDepthStencilAttachment = s->depth_format ? &dref : nullptr;
+    for (uint32_t k = 0; k < 2; k++) {
+        const uint32_t fmt = k == 0 ? s->color_format : s->depth_format;
+        if (!fmt) continue;
+        VkAttachmentDescription& a = att[n];
+        a.format = static_cast<VkFormat>(fmt);
+        a.samples = VK_SAMPLE_COUNT_1_BIT;
+        a.loadOp = VK_ATTACHMENT_LOAD_OP_CLEAR;
+        a.storeOp = VK_ATTACHMENT_STORE_OP_STORE;
+        a.stencilLoadOp = k == 0 ? VK_ATTACHMENT_LOAD_OP_DONT_CARE : VK_ATTACHMENT_LOAD_OP_CLEAR;
+        a.finalLayout = VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL;
+        if (k == 0) {
+            cref.attachment = n;
+            sub.colorAttachmentCount = 1;
+            sub.pColorAttachments = &cref;
+        } else {
+            dref.attachment = n;
+            sub.pDepthStencilAttachment = &dref;
+        }
+        n++;
+    }
     VkRenderPassCreateInfo rpi{};
     rpi.sType = VK_STRUCTURE_TYPE_RENDER_PASS_CREATE_INFO;
-    rpi.attachmentCount = s->depth_format ? 2 : 1;
+    rpi.attachmentCount = n;
     rpi.pAttachments = att;
     rpi.subpassCount = 1;
     rpi.pSubpasses = &sub;
-    VkResult res = f.vkCreateRenderPass(c->device, &rpi, nullptr, &pass);
+    return c->f.vkCreateRenderPass(c->device, &rpi, nullptr, out);
+}
+
+VkResult make_pass_and_layout(cpvh_context* c, const cpv_scene* s, bool with_sets, VkRenderPass& pass, VkDescriptorSetLayout& set_layout,
+                              VkPipelineLayout& layout) {
+    const Fns& f = c->f;
+    VkResult res = create_scene_pass(c, s, &pass);
     if (res != VK_SUCCESS) return res;
     std::vector<VkDescriptorSetLayoutBinding> lb;
     if (with_sets && s->uniform_bytes) lb.push_back({0, VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER, 1, VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
@@ -714,7 +738,8 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
         }
         c->f.vkUnmapMemory(c->device, r->indirect.memory);
     }
-    if (make_image(c, static_cast<VkFormat>(s->color_format), s->width, s->height, 1, VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT | VK_IMAGE_USAGE_TRANSFER_SRC_BIT,
+    if (s->color_format &&
+        make_image(c, static_cast<VkFormat>(s->color_format), s->width, s->height, 1, VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT | VK_IMAGE_USAGE_TRANSFER_SRC_BIT,
                    VK_IMAGE_ASPECT_COLOR_BIT, r->colour) != VK_SUCCESS)
         return fail("colour image");
     if (s->depth_format &&
@@ -740,33 +765,16 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
         if (f.vkCreateSampler(c->device, &sci, nullptr, &r->sampler) != VK_SUCCESS) return fail("sampler");
     }
     // Render pass + framebuffer.
-    VkAttachmentDescription att[2]{};
-    att[0].format = static_cast<VkFormat>(s->color_format);
-    att[0].samples = VK_SAMPLE_COUNT_1_BIT;
-    att[0].loadOp = VK_ATTACHMENT_LOAD_OP_CLEAR;
-    att[0].storeOp = VK_ATTACHMENT_STORE_OP_STORE;
-    att[0].stencilLoadOp = VK_ATTACHMENT_LOAD_OP_DONT_CARE;
-    att[0].finalLayout = VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL;
-    att[1] = att[0];
-    att[1].format = static_cast<VkFormat>(s->depth_format);
-    att[1].stencilLoadOp = VK_ATTACHMENT_LOAD_OP_CLEAR;
-    VkAttachmentReference cref{0, VK_IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL}, dref{1, VK_IMAGE_LAYOUT_DEPTH_STENCIL_ATTACHMENT_OPTIMAL};
-    VkSubpassDescription sub{};
-    sub.colorAttachmentCount = 1;
-    sub.pColorAttachments = &cref;
-    sub.pDepthStencilAttachment = s->depth_format ? &dref : nullptr;
-    VkRenderPassCreateInfo rpi{};
-    rpi.sType = VK_STRUCTURE_TYPE_RENDER_PASS_CREATE_INFO;
-    rpi.attachmentCount = s->depth_format ? 2 : 1;
-    rpi.pAttachments = att;
-    rpi.subpassCount = 1;
-    rpi.pSubpasses = &sub;
-    if (f.vkCreateRenderPass(c->device, &rpi, nullptr, &r->pass) != VK_SUCCESS) return fail("render pass");
-    VkImageView views[2] = {r->colour.view, r->depth.view};
+    if (create_scene_pass(c, s, &r->pass) != VK_SUCCESS) return fail("render pass");
+    // attachments in order: colour (absent in a depth-only pass), depth
+    VkImageView views[2];
+    uint32_t nviews = 0;
+    if (s->color_format) views[nviews++] = r->colour.view;
+    if (s->depth_format) views[nviews++] = r->depth.view;
     VkFramebufferCreateInfo fbi{};
     fbi.sType = VK_STRUCTURE_TYPE_FRAMEBUFFER_CREATE_INFO;
     fbi.renderPass = r->pass;
-    fbi.attachmentCount = s->depth_format ? 2 : 1;
+    fbi.attachmentCount = nviews;
     fbi.pAttachments = views;
     fbi.width = s->width;
     fbi.height = s->height;
@@ -1074,7 +1082,8 @@ int cpvh_readback(cpvh_renderer* r, uint8_t* color, uint8_t* depth) {
     res = c->f.vkMapMemory(c->device, r->readback.memory, 0, VK_WHOLE_SIZE, 0, &map);
     if (res != VK_SUCCESS) return res;
     const uint64_t cb = static_cast<uint64_t>(s->width) * s->height * 4;
-    if (color) std::memcpy(color, map, cb);
+    if (color && s->color_format) std::memcpy(color, map, cb);
+    else if (color) std::memset(color, 0, cb);  // a depth-only pass
     if (depth && s->depth_format) std::memcpy(depth, static_cast<uint8_t*>(map) + cb, static_cast<uint64_t>(s->width) * s->height * r->depth_texel);
     c->f.vkUnmapMemory(c->device, r->readback.memory);
     return VK_SUCCESS;

@@ -613,13 +613,17 @@ void build_serve(Store& st, uint64_t seed, uint32_t side, uint32_t tris, uint32_
 // GREATER, ALWAYS), 8 stencil test, 9 BGRA target, 10-11 topology
 // (list, strip, fan; with bit 16: points, lines, line strip), 12 uint16
 // indices, 13 depth write off, 16 point/line topologies (line width 1 + 2.5
-// × bit 17).
+// × bit 17), 18 logic op (op in 20-23), 19 colour write mask (mask in
+// 24-27), 28-29 depth bounds, 30 no colour attachment (a depth-only pass;
+// D32 when bits 3-4 pick no depth format).
 void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant, uint32_t width, uint32_t height, uint32_t tris) {
     cpv_scene& s = st.scene;
     s.width = width;
     s.height = height;
     s.color_format = (variant & 0x200) ? VK_FORMAT_B8G8R8A8_UNORM : VK_FORMAT_R8G8B8A8_UNORM;
-    const uint32_t dsel = (variant >> 3) & 3;
+    const bool depth_only = (variant & 0x40000000u) != 0;
+    if (depth_only) s.color_format = 0;
+    const uint32_t dsel = depth_only && ((variant >> 3) & 3) == 0 ? 2u : (variant >> 3) & 3;
     const uint32_t dfmts[4] = {0, VK_FORMAT_D16_UNORM, VK_FORMAT_D32_SFLOAT, VK_FORMAT_D32_SFLOAT_S8_UINT};
     s.depth_format = dfmts[dsel];
     s.clear_color[0] = 0.25f; s.clear_color[1] = 0.5f; s.clear_color[2] = 0.75f; s.clear_color[3] = 1.0f;

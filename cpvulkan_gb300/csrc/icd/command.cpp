@@ -241,20 +241,23 @@ VkResult build_draw(State& s, uint32_t count, uint32_t instances, uint32_t first
         }
     }
     std::memcpy(P.push, s.push, sizeof(P.push));
-    // Attachments of subpass 0.
-    ImageView* cv = s.fb->attachments[s.pass->colour[0]];
+    // Attachments of subpass 0 (no colour attachment in a depth-only pass);
+    // attachment addressing uses the image row length.
     uint32_t w = 0, h = 0;
-    P.color = view_base(cv, w, h);
-    P.fb_width = w < s.fb->width ? w : s.fb->width;
-    P.fb_height = h < s.fb->height ? h : s.fb->height;
-    // Attachment addressing uses the image row length.
-    P.fb_width = w;
-    P.fb_height = h;
+    if (!s.pass->colour.empty()) P.color = view_base(s.fb->attachments[s.pass->colour[0]], w, h);
     if (s.pass->depth != VK_ATTACHMENT_UNUSED) {
         uint32_t dw, dh;
         P.depth = view_base(s.fb->attachments[s.pass->depth], dw, dh);
-        if (dw != w || dh != h) return VK_ERROR_DEVICE_LOST;
+        if (!P.color) {
+            w = dw;
+            h = dh;
+        } else if (dw != w || dh != h) {
+            return VK_ERROR_DEVICE_LOST;
+        }
     }
+    if (!P.color && !P.depth) return VK_ERROR_DEVICE_LOST;
+    P.fb_width = w;
+    P.fb_height = h;
     const VkViewport vp = p->dynamic_viewport ? s.viewport : p->viewport;
     P.viewport[0] = vp.x;
     P.viewport[1] = vp.y;
@@ -526,7 +529,9 @@ bool tune_batch(Queue* q, Device* dev, const std::vector<Pipeline*>& pipelines, 
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     bool ok = cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
     auto copy = [&](bool restore) {
-        bool good = cudaMemcpyAsync(restore ? in.color : saved, restore ? saved : in.color, color_bytes, cudaMemcpyDeviceToDevice, q->stream) == cudaSuccess;
+        bool good = true;
+        if (color_bytes)
+            good = cudaMemcpyAsync(restore ? in.color : saved, restore ? saved : in.color, color_bytes, cudaMemcpyDeviceToDevice, q->stream) == cudaSuccess;
         if (depth_bytes)
             good = good && cudaMemcpyAsync(restore ? in.depth : saved + color_bytes, restore ? saved + color_bytes : in.depth, depth_bytes,
                                            cudaMemcpyDeviceToDevice, q->stream) == cudaSuccess;
@@ -639,9 +644,8 @@ void build_batch(Queue* q, const CommandBuffer* cb, size_t begin, size_t end, co
             }
         }
         if (!known) {
-            uint32_t w = 0, h = 0;
-            view_base(s.fb->attachments[s.pass->colour[0]], w, h);
-            const uint64_t color_bytes = static_cast<uint64_t>(w) * h * 4u;
+            const uint32_t w = in.fb_width, h = in.fb_height;
+            const uint64_t color_bytes = in.color ? static_cast<uint64_t>(w) * h * 4u : 0u;
             uint64_t depth_bytes = 0;
             if (s.pass->depth != VK_ATTACHMENT_UNUSED) {
                 const ImageView* dv = s.fb->attachments[s.pass->depth];
@@ -1052,11 +1056,13 @@ VkResult check_no_alloc(CommandBuffer* cb) {
         case CmdType::BindPipeline: pipeline = static_cast<Pipeline*>(c.p[0]); break;
         case CmdType::Draw:
         case CmdType::DrawIndexed: {
-            if (!pipeline || !pass || !fb || pass->colour.empty()) break;  // execute() reports these
+            if (!pipeline || !pass || !fb) break;  // execute() reports these
             const uint32_t count = c.u[0], instances = c.u[1];
             const uint32_t ppi = primitives_per_instance(pipeline->topology, count);
-            if (pass->colour[0] >= fb->attachments.size()) break;
-            const ImageView* cv = fb->attachments[pass->colour[0]];
+            // the attachment that sizes the draw: colour, else depth
+            const uint32_t index = !pass->colour.empty() ? pass->colour[0] : pass->depth;
+            if (index == VK_ATTACHMENT_UNUSED || index >= fb->attachments.size()) break;
+            const ImageView* cv = fb->attachments[index];
             uint32_t w = 0, h = 0;
             if (!cv || !cv->image) break;
             view_base(cv, w, h);

@@ -306,9 +306,11 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
 
     const RenderPass* pass = reinterpret_cast<const RenderPass*>(ci.renderPass);
     if (!pass) return reject("no render pass");
-    if (pass->colour.size() != 1) return reject("exactly one colour attachment is supported");
-    const VkFormat cfmt = pass->attachments[pass->colour[0]].format;
-    if (!supported_colour(cfmt)) return reject("colour attachment format " + std::to_string(cfmt));
+    // one colour attachment, or none (a depth-only pass)
+    if (pass->colour.size() > 1) return reject("at most one colour attachment is supported");
+    const VkFormat cfmt = pass->colour.empty() ? VK_FORMAT_UNDEFINED : pass->attachments[pass->colour[0]].format;
+    if (!pass->colour.empty() && !supported_colour(cfmt)) return reject("colour attachment format " + std::to_string(cfmt));
+    if (pass->colour.empty() && pass->depth == VK_ATTACHMENT_UNUSED) return reject("a colour or a depth attachment is required");
     VkFormat dfmt = VK_FORMAT_UNDEFINED;
     if (pass->depth != VK_ATTACHMENT_UNUSED) {
         dfmt = pass->attachments[pass->depth].format;
@@ -324,7 +326,7 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     float blend_constants[4] = {0, 0, 0, 0};
     bool logic = false;
     uint32_t logic_op = VK_LOGIC_OP_COPY;
-    if (ci.pColorBlendState) {
+    if (ci.pColorBlendState && cfmt != VK_FORMAT_UNDEFINED) {
         if (ci.pColorBlendState->attachmentCount >= 1) blend = ci.pColorBlendState->pAttachments[0];
         for (int i = 0; i < 4; i++) blend_constants[i] = ci.pColorBlendState->blendConstants[i];
         if (ci.pColorBlendState->logicOpEnable) {

@@ -305,7 +305,12 @@ __device__ __forceinline__ int cpv_channel_shift(int i) {
 }
 
 __device__ __forceinline__ void cpv_load_pixel(const uint8_t* color, const uint8_t* depth, uint64_t pix, CpvPixel& s) {
+#if CPV_COLOR_FORMAT != 0
     s.colour = reinterpret_cast<const uint32_t*>(color)[pix];
+#else
+    (void)color; /* a depth-only pass */
+    s.colour = 0u;
+#endif
 #if CPV_DEPTH_FORMAT == 124
     s.depth_raw = reinterpret_cast<const uint16_t*>(depth)[pix];
     s.depth = cpv_decode_unorm16(s.depth_raw);
@@ -328,7 +333,11 @@ __device__ __forceinline__ void cpv_load_pixel(const uint8_t* color, const uint8
 }
 
 __device__ __forceinline__ void cpv_store_pixel(uint8_t* color, uint8_t* depth, uint64_t pix, const CpvPixel& s) {
+#if CPV_COLOR_FORMAT != 0
     reinterpret_cast<uint32_t*>(color)[pix] = s.colour;
+#else
+    (void)color;
+#endif
 #if CPV_DEPTH_FORMAT == 124
     reinterpret_cast<uint16_t*>(depth)[pix] = static_cast<uint16_t>(s.depth_raw);
 #elif CPV_DEPTH_FORMAT == 126
@@ -520,6 +529,7 @@ __device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool fro
     } else if (attempt_depth_write && depth_result) {
         cpv_write_depth(s, mapped);
     }
+    if (CPV_COLOR_FORMAT == 0) return; /* a depth-only pass: no colour write */
     if (stencil_result && depth_result) {
 #if CPV_BLEND_TABLE
         if (table) {

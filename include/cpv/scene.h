@@ -105,7 +105,7 @@ typedef struct cpv_scene_sampler {
 
 typedef struct cpv_scene {
     uint32_t width, height;
-    uint32_t color_format; /* VkFormat: R8G8B8A8_UNORM or B8G8R8A8_UNORM */
+    uint32_t color_format; /* VkFormat: R8G8B8A8_UNORM or B8G8R8A8_UNORM; 0: no colour attachment (depth-only) */
     uint32_t depth_format; /* VkFormat: 0 (none), D16_UNORM, D32_SFLOAT, D32_SFLOAT_S8_UINT */
     float clear_color[4];
     float clear_depth;

@@ -765,7 +765,7 @@ void fragment(Frame& f, const cpv_scene_pipeline& p, uint32_t x, uint32_t y, flo
     }
 
     if (stencil_result && depth_result) {
-        write_colour(f.colour + pix * 4, s->color_format, p, colour);
+        if (s->color_format) write_colour(f.colour + pix * 4, s->color_format, p, colour);
         f.stats->fragments_written++;
     }
 }
@@ -1007,7 +1007,8 @@ extern "C" {
 int cpv_oracle_render(const cpv_scene* scene, uint8_t* color, uint8_t* depth, uint32_t do_clear, uint32_t draw_begin,
                       uint32_t draw_end, cpv_oracle_stats* stats) {
     if (!scene || !color) return -1;
-    if (scene->color_format != FMT_R8G8B8A8_UNORM && scene->color_format != FMT_B8G8R8A8_UNORM) return -2;
+    if (scene->color_format != FMT_R8G8B8A8_UNORM && scene->color_format != FMT_B8G8R8A8_UNORM && scene->color_format != 0) return -2;
+    if (scene->color_format == 0 && scene->depth_format == 0) return -2;
     const uint32_t dsize = depth_texel_size(scene->depth_format);
     if (scene->depth_format != 0 && (dsize == 0 || !depth)) return -3;
     cpv_oracle_stats local{};
@@ -1047,7 +1048,8 @@ int cpv_oracle_render(const cpv_scene* scene, uint8_t* color, uint8_t* depth, ui
         /* BeginRenderPassCommand + ClearImage (CPVulkan/CommandBuffer.cpp:591-646,
          * CPVulkan/CommandBuffer.Draw.cpp:117-149): every texel goes through the
          * format encoder. */
-        for (uint64_t i = 0; i < pixels; i++) set_colour(color + i * 4, scene->color_format, scene->clear_color);
+        if (scene->color_format)  // a depth-only pass leaves `color` untouched
+            for (uint64_t i = 0; i < pixels; i++) set_colour(color + i * 4, scene->color_format, scene->clear_color);
         if (f.depth) {
             for (uint64_t i = 0; i < pixels; i++) {
                 uint8_t* t = f.depth + i * dsize;

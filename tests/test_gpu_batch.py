@@ -85,13 +85,14 @@ def test_batched_blend_scene(gpu_ctx, plain, monkeypatch):
 
 def test_batched_program_variants(gpu_ctx, plain, monkeypatch):
     """Stencil, D16, CW, strips, discard, points, lines, a logic op, a
-    colour write mask and the depth bounds test through the batched kernels."""
+    colour write mask, the depth bounds test and a depth-only pass through
+    the batched kernels."""
     monkeypatch.setenv("CPV_BATCH_MIN_DRAWS", "1")
     for program, variant in [(c.PROGRAM_CUBE, 0x18 | 0x100), (c.PROGRAM_CUBE, 0x8 | 0x4 | 0x1), (c.PROGRAM_CUBE, 0x400 | 0x10),
                              (c.PROGRAM_DISCARD, 0x10), (c.PROGRAM_TEXLIT, 0x10 | 0x4000), (c.PROGRAM_MESHPC, 0x10 | 0x20),
                              (c.PROGRAM_POINTS, 0x10000 | 0x20), (c.PROGRAM_CUBE, 0x10000 | 0x800 | 0x20000 | 0x10),
                              (c.PROGRAM_FLATQUAD, 0x20 | 0x40000 | (6 << 20)), (c.PROGRAM_CUBE, 0x10 | 0x80000 | (0xB << 24)),
-                             (c.PROGRAM_CUBE, 0x18 | 0x100 | (2 << 28))]:
+                             (c.PROGRAM_CUBE, 0x18 | 0x100 | (2 << 28)), (c.PROGRAM_CUBE, 0x40000000 | 0x18 | 0x100)]:
         scene = c.Scene(c.PROGRAM, 2, [program, variant, 64, 48, 24])
         ref = plain(gpu_ctx, scene)[0]
         same(frames(gpu_ctx, scene)[0], ref)

@@ -71,8 +71,17 @@ DEPTH_BOUNDS = [
     (c.PROGRAM_CUBE, 0x10000 | 0x400 | 0x20000 | 0x10 | (2 << 28)),
 ]
 
+# Depth-only passes (bit 30: no colour attachment): depth and stencil
+# against the oracle, with D32, D32S8 + stencil, D16 + discard, a sampled
+# texture, lines and the depth bounds test.
+DEPTH_ONLY = [
+    (c.PROGRAM_CUBE, 0x40000000 | 0x10), (c.PROGRAM_CUBE, 0x40000000 | 0x18 | 0x100), (c.PROGRAM_DISCARD, 0x40000000 | 0x8),
+    (c.PROGRAM_TEXLIT, 0x40000000 | 0x10), (c.PROGRAM_CUBE, 0x40000000 | 0x10000 | 0x800 | 0x20000 | 0x10),
+    (c.PROGRAM_FLATQUAD, 0x40000000 | 0x8 | 0x20 | (2 << 28)),
+]
 
-@pytest.mark.parametrize("program,variant", VARIANTS + POINTS_LINES + LOGIC_MASK + DEPTH_BOUNDS)
+
+@pytest.mark.parametrize("program,variant", VARIANTS + POINTS_LINES + LOGIC_MASK + DEPTH_BOUNDS + DEPTH_ONLY)
 @pytest.mark.parametrize("seed", [1, 2, 3])
 def test_program_variants(gpu_ctx, oracle, program, variant, seed):
     scene = c.Scene(c.PROGRAM, seed, [program, variant, 64, 48, 24])

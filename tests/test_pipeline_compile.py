@@ -18,14 +18,14 @@ KERNELS = os.path.join(ROOT, "cpvulkan_gb300", "csrc", "kernels")
 # 13 depth write off, 14 nearest + mirror/border sampler, 15 LOD bias,
 # 16 point/line topologies (10-11 then: points, lines, line strip), 17 wide lines,
 # 18 logic op (op in bits 20-23), 19 colour write mask (mask in bits 24-27),
-# 28-29 depth bounds
+# 28-29 depth bounds, 30 depth-only pass
 PROGRAMS = [
     (c.PROGRAM_CUBE, 0x0), (c.PROGRAM_CUBE, 0x18 | 0x100), (c.PROGRAM_CUBE, 0x20 | 0x200 | 0x400),
     (c.PROGRAM_TEXLIT, 0x10 | 0x4000), (c.PROGRAM_FLATQUAD, 0x20), (c.PROGRAM_MESHPC, 0x10 | 0x2 | 0x4),
     (c.PROGRAM_DISCARD, 0x10), (c.PROGRAM_NOPERSP, 0x8 | 0x800),
     (c.PROGRAM_POINTS, 0x10000 | 0x10), (c.PROGRAM_CUBE, 0x10000 | 0x400 | 0x20000), (c.PROGRAM_NOPERSP, 0x10000 | 0x800 | 0x8),
     (c.PROGRAM_CUBE, 0x40000 | (6 << 20) | 0x10), (c.PROGRAM_FLATQUAD, 0x20 | 0x80000 | (0x5 << 24)),
-    (c.PROGRAM_CUBE, 0x18 | 0x100 | (2 << 28)),
+    (c.PROGRAM_CUBE, 0x18 | 0x100 | (2 << 28)), (c.PROGRAM_TEXLIT, 0x40000000 | 0x10),
 ]
 
 
@@ -111,6 +111,8 @@ def _module_source(compile_ctx, program, variant):
                                        "CPV_MAX_DEPTH_BOUNDS": "__uint_as_float(1065353216u)"}),
     # no depth attachment: no test
     (c.PROGRAM_FLATQUAD, 0x20 | (2 << 28), {"CPV_DEPTH_BOUNDS": "0"}),
+    # a depth-only pass: no colour format, blending off
+    (c.PROGRAM_FLATQUAD, 0x40000000 | 0x8 | 0x20, {"CPV_COLOR_FORMAT": "0", "CPV_DEPTH_FORMAT": "124", "CPV_BLEND": "0"}),
 ])
 def test_module_configuration(compile_ctx, program, variant, expect):
     """The fixed-function and schedule macros a pipeline's module is compiled with."""
