@@ -936,6 +936,19 @@ VKAPI_ATTR void VKAPI_CALL CmdSetBlendConstants(VkCommandBuffer cmd, const float
     auto& x = push(cmd, CmdType::SetBlendConstants);
     x.bytes.assign(reinterpret_cast<const uint8_t*>(c), reinterpret_cast<const uint8_t*>(c) + 16);
 }
+// Dynamic state a pipeline here never takes from the command buffer: dynamic
+// line width (on line topologies), depth bounds and the stencil masks and
+// reference are rejected at pipeline creation (the reference aborts on
+// them: CPVulkan/CommandBuffer.h:37-43, LLVMRuntime/PipelineCompiler.cpp:
+// 1137-1146, 1196-1203), and depth bias is not applied, as in the reference.
+// Setting state a bound pipeline does not declare dynamic has no effect, so
+// these record nothing.
+VKAPI_ATTR void VKAPI_CALL CmdSetLineWidth(VkCommandBuffer, float) {}
+VKAPI_ATTR void VKAPI_CALL CmdSetDepthBias(VkCommandBuffer, float, float, float) {}
+VKAPI_ATTR void VKAPI_CALL CmdSetDepthBounds(VkCommandBuffer, float, float) {}
+VKAPI_ATTR void VKAPI_CALL CmdSetStencilCompareMask(VkCommandBuffer, VkStencilFaceFlags, uint32_t) {}
+VKAPI_ATTR void VKAPI_CALL CmdSetStencilWriteMask(VkCommandBuffer, VkStencilFaceFlags, uint32_t) {}
+VKAPI_ATTR void VKAPI_CALL CmdSetStencilReference(VkCommandBuffer, VkStencilFaceFlags, uint32_t) {}
 VKAPI_ATTR void VKAPI_CALL CmdBindDescriptorSets(VkCommandBuffer cmd, VkPipelineBindPoint, VkPipelineLayout, uint32_t first, uint32_t n,
                                                  const VkDescriptorSet* sets, uint32_t ndyn, const uint32_t* dyn) {
     auto& c = push(cmd, CmdType::BindDescriptorSets);
@@ -1275,7 +1288,8 @@ const Entry kDevice[] = {
     E(DestroyDescriptorPool), E(AllocateDescriptorSets), E(FreeDescriptorSets), E(UpdateDescriptorSets), E(CreateRenderPass),
     E(DestroyRenderPass), E(CreateFramebuffer), E(DestroyFramebuffer), E(CreateCommandPool), E(DestroyCommandPool), E(ResetCommandPool),
     E(AllocateCommandBuffers), E(FreeCommandBuffers), E(BeginCommandBuffer), E(EndCommandBuffer), E(ResetCommandBuffer), E(CmdBindPipeline),
-    E(CmdSetViewport), E(CmdSetScissor), E(CmdSetBlendConstants), E(CmdBindDescriptorSets), E(CmdBindIndexBuffer), E(CmdBindVertexBuffers),
+    E(CmdSetViewport), E(CmdSetScissor), E(CmdSetBlendConstants), E(CmdSetLineWidth), E(CmdSetDepthBias), E(CmdSetDepthBounds),
+    E(CmdSetStencilCompareMask), E(CmdSetStencilWriteMask), E(CmdSetStencilReference), E(CmdBindDescriptorSets), E(CmdBindIndexBuffer), E(CmdBindVertexBuffers),
     E(CmdDraw), E(CmdDrawIndexed), E(CmdDrawIndirect), E(CmdDrawIndexedIndirect),
     {"vkCmdDrawIndirectCountKHR", reinterpret_cast<PFN_vkVoidFunction>(CmdDrawIndirectCount)},
     {"vkCmdDrawIndexedIndirectCountKHR", reinterpret_cast<PFN_vkVoidFunction>(CmdDrawIndexedIndirectCount)},

@@ -353,6 +353,8 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
             const auto d = ci.pDynamicState->pDynamicStates[i];
             if (d == VK_DYNAMIC_STATE_VIEWPORT) dyn_viewport = true;
             else if (d == VK_DYNAMIC_STATE_BLEND_CONSTANTS) dyn_blend = true;
+            else if (d == VK_DYNAMIC_STATE_LINE_WIDTH && (topo == VK_PRIMITIVE_TOPOLOGY_LINE_LIST || topo == VK_PRIMITIVE_TOPOLOGY_LINE_STRIP))
+                return reject("dynamic line width on a line topology");
             else if (d == VK_DYNAMIC_STATE_SCISSOR || d == VK_DYNAMIC_STATE_LINE_WIDTH || d == VK_DYNAMIC_STATE_DEPTH_BIAS) continue;
             else return reject("dynamic state " + std::to_string(d));
         }

@@ -105,6 +105,21 @@ def test_gpu_path_has_no_cpu_fallback(native):
         del os.environ["CPV_COMPILE_ONLY"]
 
 
+def test_dynamic_state_commands_resolve(native):
+    """Every vkCmdSet* of the reference's command buffer resolves (those for
+    state a pipeline here never makes dynamic record nothing), so a loader's
+    dispatch table has no null entry for them."""
+    lib = ctypes.CDLL(c.ICD_PATH)
+    gipa = lib.vk_icdGetInstanceProcAddr
+    gipa.restype = ctypes.c_void_p
+    gipa.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+    instance = ctypes.c_void_p(16)  # the lookup does not dereference it
+    for name in (b"vkCmdSetViewport", b"vkCmdSetScissor", b"vkCmdSetBlendConstants", b"vkCmdSetLineWidth", b"vkCmdSetDepthBias",
+                 b"vkCmdSetDepthBounds", b"vkCmdSetStencilCompareMask", b"vkCmdSetStencilWriteMask", b"vkCmdSetStencilReference",
+                 b"vkCmdCopyImage", b"vkCmdClearColorImage", b"vkCmdClearDepthStencilImage", b"vkCmdClearAttachments"):
+        assert gipa(instance, name), name
+
+
 def test_indirect_count_extension(native):
     """VK_KHR_draw_indirect_count and VK_AMD_draw_indirect_count are listed
     and their draw commands resolve under the reference's names
