@@ -260,6 +260,12 @@ SCENES = [
     ("serve_small", 6, 6, [96, 2000, 2]),
     ("program_texlit_mirror", 5, 7, [1, 0x10 | 0x4000, 48, 40, 12]),
     ("program_cube_stencil", 5, 8, [0, 0x18 | 0x100, 48, 40, 12]),
+    ("program_points", 5, 9, [6, 0x10000 | 0x10, 48, 40, 12]),
+    ("program_wide_line_strip", 5, 10, [0, 0x10000 | 0x800 | 0x20000 | 0x10, 48, 40, 12]),
+    ("program_flatquad_logic_xor", 5, 11, [2, 0x20 | 0x40000 | (6 << 20), 48, 40, 12]),
+    ("program_cube_write_mask", 5, 12, [0, 0x10 | 0x80000 | (0x5 << 24), 48, 40, 12]),
+    ("program_cube_depth_bounds", 5, 13, [0, 0x18 | 0x100 | (2 << 28), 48, 40, 12]),
+    ("program_cube_depth_only", 5, 14, [0, 0x40000000 | 0x18 | 0x100, 48, 40, 12]),
 ]
 
 
@@ -283,9 +289,11 @@ def scene_pins():
 
 
 def main():
-    rng = np.random.default_rng(20261203)
-    kat = make_kat(rng)
-    np.savez_compressed(os.path.join(HERE, "kat.npz"), **kat)
+    # --scenes-only rewrites the scene pins and leaves kat.npz as it is
+    if "--scenes-only" not in sys.argv:
+        rng = np.random.default_rng(20261203)
+        kat = make_kat(rng)
+        np.savez_compressed(os.path.join(HERE, "kat.npz"), **kat)
     with open(os.path.join(HERE, "oracle_scenes.json"), "w") as f:
         json.dump(scene_pins(), f, indent=1, sort_keys=True)
         f.write("\n")
