@@ -153,7 +153,9 @@ VkResult clear_rect(Queue* q, Image* img, uint32_t layer, uint32_t level, VkImag
     if (!img || !img->memory || level >= img->levels || layer >= img->layers) return VK_ERROR_DEVICE_LOST;
     const ImageLevel& L = img->level[level];
     // the rectangle within the level
-    const int64_t x1 = std::min<int64_t>(static_cast<int64_t>(x0) + w, L.width), y1 = std::min<int64_t>(static_cast<int64_t>(y0) + h, static_cast<int64_t>(L.height) * std::max(1u, L.depth));
+    const int64_t rows = static_cast<int64_t>(L.height) * std::max(1u, L.depth);
+    const int64_t x1 = std::min<int64_t>(static_cast<int64_t>(x0) + w, L.width);
+    const int64_t y1 = std::min<int64_t>(static_cast<int64_t>(y0) + h, rows);
     x0 = std::max(x0, 0);
     y0 = std::max(y0, 0);
     if (x1 <= x0 || y1 <= y0) return VK_SUCCESS;
