@@ -99,6 +99,7 @@ struct Fns {
     CPVH_FN(vkCmdPipelineBarrier)
     CPVH_FN(vkCmdPushConstants)
     CPVH_FN(vkCmdBeginRenderPass)
+    CPVH_FN(vkCmdNextSubpass)
     CPVH_FN(vkCmdEndRenderPass)
     CPVH_FN(vkQueueSubmit)
     CPVH_FN(vkQueueWaitIdle)
@@ -178,6 +179,7 @@ struct cpvh_renderer {
     cpvh_context* ctx = nullptr;
     const cpv_scene* scene = nullptr;
     BufferAlloc vertex, index, uniform, staging, readback, indirect, indirect_count;
+    uint32_t subpass = 0;  // the subpass the frame draws in (CPVH_SUBPASSES=2: 1)
     ImageAlloc colour, depth, texture;
     VkSampler sampler = nullptr;
     VkRenderPass pass = nullptr;
@@ -332,6 +334,7 @@ void record_frame(cpvh_renderer* r, VkCommandBuffer cmd) {
     rb.clearValueCount = nclears;
     rb.pClearValues = clears;
     c->f.vkCmdBeginRenderPass(cmd, &rb, VK_SUBPASS_CONTENTS_INLINE);
+    if (r->subpass == 1) c->f.vkCmdNextSubpass(cmd, VK_SUBPASS_CONTENTS_INLINE);
     uint32_t bound = ~0u;
     for (uint32_t i = 0; i < s->num_draws; i++) {
         const cpv_scene_draw& d = s->draws[i];
@@ -395,7 +398,7 @@ VkResult record_all(cpvh_renderer* r) {
 }
 
 bool build_pipelines(cpvh_context* c, const cpv_scene* s, VkRenderPass pass, VkPipelineLayout layout, std::vector<VkShaderModule>& modules,
-                     std::vector<VkPipeline>& pipelines, std::string& err) {
+                     std::vector<VkPipeline>& pipelines, std::string& err, uint32_t subpass = 0) {
     const Fns& f = c->f;
     for (uint32_t i = 0; i < s->num_pipelines; i++) {
         const cpv_scene_pipeline& sp = s->pipelines[i];
@@ -493,6 +496,7 @@ bool build_pipelines(cpvh_context* c, const cpv_scene* s, VkRenderPass pass, VkP
         gpi.pColorBlendState = &cbs;
         gpi.layout = layout;
         gpi.renderPass = pass;
+        gpi.subpass = subpass;
         VkPipeline pipe = nullptr;
         if (f.vkCreateGraphicsPipelines(c->device, c->cache, 1, &gpi, nullptr, &pipe) != VK_SUCCESS) { err = "vkCreateGraphicsPipelines:"; return false; }
         pipelines.push_back(pipe);
@@ -502,8 +506,10 @@ bool build_pipelines(cpvh_context* c, const cpv_scene* s, VkRenderPass pass, VkP
 
 // The scene's render pass: a cleared colour attachment (none in a
 // depth-only pass) then a cleared depth/stencil attachment (when the scene
-// has a depth format), both stored.
-VkResult create_scene_pass(cpvh_context* c, const cpv_scene* s, VkRenderPass* out) {
+// has a depth format), both stored. With two_subpasses the scene draws in
+// subpass 1 (these attachments), after a subpass 0 that references only the
+// depth attachment (only the colour one when there is no depth).
+VkResult create_scene_pass(cpvh_context* c, const cpv_scene* s, VkRenderPass* out, bool two_subpasses = false) {
     VkAttachmentDescription att[2]{};
     VkAttachmentReference cref{0, VK_IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL}, dref{0, VK_IMAGE_LAYOUT_DEPTH_STENCIL_ATTACHMENT_OPTIMAL};
     uint32_t n = 0;
@@ -528,12 +534,21 @@ VkResult create_scene_pass(cpvh_context* c, const cpv_scene* s, VkRenderPass* ou
         }
         n++;
     }
+    VkSubpassDescription subs[2] = {sub, sub};
+    if (two_subpasses) {
+        if (sub.pDepthStencilAttachment) {
+            subs[0].colorAttachmentCount = 0;
+            subs[0].pColorAttachments = nullptr;
+        } else {
+            subs[0].pDepthStencilAttachment = nullptr;
+        }
+    }
     VkRenderPassCreateInfo rpi{};
     rpi.sType = VK_STRUCTURE_TYPE_RENDER_PASS_CREATE_INFO;
     rpi.attachmentCount = n;
     rpi.pAttachments = att;
-    rpi.subpassCount = 1;
-    rpi.pSubpasses = &sub;
+    rpi.subpassCount = two_subpasses ? 2 : 1;
+    rpi.pSubpasses = subs;
     return c->f.vkCreateRenderPass(c->device, &rpi, nullptr, out);
 }
 
@@ -646,7 +661,7 @@ cpvh_context* cpvh_open(const char* icd_path, char* err, uint32_t err_len) {
     LOAD_D(vkCmdDrawIndirect); LOAD_D(vkCmdDrawIndexedIndirect); LOAD_D(vkCmdDrawIndirectCountKHR); LOAD_D(vkCmdDrawIndexedIndirectCountKHR);
     LOAD_D(vkCmdCopyBufferToImage); LOAD_D(vkCmdCopyImageToBuffer); LOAD_D(vkCmdPipelineBarrier); LOAD_D(vkCmdPushConstants);
     LOAD_D(vkCmdBlitImage); LOAD_D(vkCmdCopyImage); LOAD_D(vkCmdClearColorImage); LOAD_D(vkCmdClearDepthStencilImage); LOAD_D(vkCmdClearAttachments);
-    LOAD_D(vkCmdBeginRenderPass); LOAD_D(vkCmdEndRenderPass); LOAD_D(vkQueueSubmit); LOAD_D(vkQueueWaitIdle); LOAD_D(vkCreateFence);
+    LOAD_D(vkCmdBeginRenderPass); LOAD_D(vkCmdNextSubpass); LOAD_D(vkCmdEndRenderPass); LOAD_D(vkQueueSubmit); LOAD_D(vkQueueWaitIdle); LOAD_D(vkCreateFence);
     LOAD_D(vkDestroyFence); LOAD_D(vkResetFences); LOAD_D(vkWaitForFences); LOAD_D(vkGetFenceStatus);
 #undef LOAD_D
     // CPVH_SUBMIT=no_alloc: every submission of this context goes through the
@@ -765,7 +780,11 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
         if (f.vkCreateSampler(c->device, &sci, nullptr, &r->sampler) != VK_SUCCESS) return fail("sampler");
     }
     // Render pass + framebuffer.
-    if (create_scene_pass(c, s, &r->pass) != VK_SUCCESS) return fail("render pass");
+    // CPVH_SUBPASSES=2: the frame draws in subpass 1 of a two-subpass render
+    // pass (its pipelines are created for subpass 1)
+    const char* subpasses = std::getenv("CPVH_SUBPASSES");
+    r->subpass = subpasses && subpasses[0] == '2' ? 1u : 0u;
+    if (create_scene_pass(c, s, &r->pass, r->subpass == 1) != VK_SUCCESS) return fail("render pass");
     // attachments in order: colour (absent in a depth-only pass), depth
     VkImageView views[2];
     uint32_t nviews = 0;
@@ -837,7 +856,7 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
     if (f.vkCreatePipelineLayout(c->device, &pli, nullptr, &r->layout) != VK_SUCCESS) return fail("pipeline layout");
     {
         std::string perr;
-        if (!build_pipelines(c, s, r->pass, r->layout, r->modules, r->pipelines, perr)) return fail(perr);
+        if (!build_pipelines(c, s, r->pass, r->layout, r->modules, r->pipelines, perr, r->subpass)) return fail(perr);
     }
     // Command buffers and fence.
     VkCommandPoolCreateInfo cpi{};

@@ -60,6 +60,8 @@ struct State {
     bool blend_set = false;
     RenderPass* pass = nullptr;
     Framebuffer* fb = nullptr;
+    uint32_t subpass = 0;  // index into pass->subpasses
+    const Subpass& sub() const { return pass->subpasses[subpass]; }
 };
 
 // Resolves the (set, binding) → dynamic offset index: dynamic descriptors are
@@ -175,7 +177,8 @@ VkResult clear_rect(Queue* q, Image* img, uint32_t layer, uint32_t level, VkImag
 VkResult begin_render_pass(Queue* q, State& s, const Cmd& c, std::vector<DeviceMemory*>& written) {
     s.pass = static_cast<RenderPass*>(c.p[0]);
     s.fb = static_cast<Framebuffer*>(c.p[1]);
-    if (!s.pass || !s.fb) return VK_ERROR_DEVICE_LOST;
+    s.subpass = 0;
+    if (!s.pass || !s.fb || s.pass->subpasses.empty()) return VK_ERROR_DEVICE_LOST;
     for (size_t i = 0; i < s.pass->attachments.size() && i < s.fb->attachments.size(); i++) {
         const auto& a = s.pass->attachments[i];
         ImageView* v = s.fb->attachments[i];
@@ -243,13 +246,14 @@ VkResult build_draw(State& s, uint32_t count, uint32_t instances, uint32_t first
         }
     }
     std::memcpy(P.push, s.push, sizeof(P.push));
-    // Attachments of subpass 0 (no colour attachment in a depth-only pass);
-    // attachment addressing uses the image row length.
+    // Attachments of the current subpass (no colour attachment in a
+    // depth-only one); attachment addressing uses the image row length.
     uint32_t w = 0, h = 0;
-    if (!s.pass->colour.empty()) P.color = view_base(s.fb->attachments[s.pass->colour[0]], w, h);
-    if (s.pass->depth != VK_ATTACHMENT_UNUSED) {
+    const Subpass& sub = s.sub();
+    if (!sub.colour.empty()) P.color = view_base(s.fb->attachments[sub.colour[0]], w, h);
+    if (sub.depth != VK_ATTACHMENT_UNUSED) {
         uint32_t dw, dh;
-        P.depth = view_base(s.fb->attachments[s.pass->depth], dw, dh);
+        P.depth = view_base(s.fb->attachments[sub.depth], dw, dh);
         if (!P.color) {
             w = dw;
             h = dh;
@@ -351,6 +355,10 @@ bool is_indirect(const Cmd& c) { return c.type == CmdType::DrawIndirect || c.typ
 // Applies a binding / dynamic-state command to `s`; false for any other.
 bool apply_state(State& s, const Cmd& c) {
     switch (c.type) {
+    case CmdType::NextSubpass:
+        // the next subpass's attachments (CPVulkan/CommandBuffer.cpp:649-664)
+        if (s.pass && s.subpass + 1 < s.pass->subpasses.size()) s.subpass++;
+        return true;
     case CmdType::BindPipeline: s.pipeline = static_cast<Pipeline*>(c.p[0]); return true;
     case CmdType::BindVertexBuffers:
         for (uint32_t i = 0; i < c.u[1]; i++) {
@@ -432,8 +440,10 @@ struct PassCensus {
     size_t draws = 0;
     uint64_t prims = 0;
     bool blend_tables = false;
+    bool subpasses = false;  // a pass of several subpasses runs per draw
     void add(const Cmd& c, const std::vector<IndirectDraw>* records = nullptr) {
         if (c.type == CmdType::BindPipeline) bound = static_cast<Pipeline*>(c.p[0]);
+        if (c.type == CmdType::NextSubpass) subpasses = true;
         if (is_indirect(c)) {
             draws += records ? records->size() : c.u[0];
             if (!bound) return;
@@ -449,7 +459,7 @@ struct PassCensus {
         blend_tables = blend_tables || bound->blend_table;
     }
     bool batches() const {
-        if (env_u32("CPV_BATCH", 1u) == 0u || draws == 0) return false;
+        if (env_u32("CPV_BATCH", 1u) == 0u || draws == 0 || subpasses) return false;
         if (draws >= env_u32("CPV_BATCH_MIN_DRAWS", 16u)) return true;
         return !blend_tables && prims >= env_u32("CPV_BATCH_MIN_PRIMS", 1u << 20);
     }
@@ -649,8 +659,8 @@ void build_batch(Queue* q, const CommandBuffer* cb, size_t begin, size_t end, co
             const uint32_t w = in.fb_width, h = in.fb_height;
             const uint64_t color_bytes = in.color ? static_cast<uint64_t>(w) * h * 4u : 0u;
             uint64_t depth_bytes = 0;
-            if (s.pass->depth != VK_ATTACHMENT_UNUSED) {
-                const ImageView* dv = s.fb->attachments[s.pass->depth];
+            if (s.sub().depth != VK_ATTACHMENT_UNUSED) {
+                const ImageView* dv = s.fb->attachments[s.sub().depth];
                 depth_bytes = static_cast<uint64_t>(w) * h * dv->image->texel;
             }
             rt::Module* m = nullptr;
@@ -884,9 +894,9 @@ VkResult execute(Queue* q, CommandBuffer* cb, std::vector<DeviceMemory*>& writte
             for (const VkClearAttachment& a : c.clear_attachments) {
                 uint32_t index = VK_ATTACHMENT_UNUSED;
                 if (a.aspectMask & VK_IMAGE_ASPECT_COLOR_BIT) {
-                    if (a.colorAttachment < s.pass->colour.size()) index = s.pass->colour[a.colorAttachment];
+                    if (a.colorAttachment < s.sub().colour.size()) index = s.sub().colour[a.colorAttachment];
                 } else {
-                    index = s.pass->depth;
+                    index = s.sub().depth;
                 }
                 if (index == VK_ATTACHMENT_UNUSED || index >= s.fb->attachments.size() || !s.fb->attachments[index]) continue;
                 const ImageView* v = s.fb->attachments[index];
@@ -1016,6 +1026,7 @@ void precompile_batches(CommandBuffer* cb) {
             census.bound = bound;
             break;
         case CmdType::BindPipeline:
+        case CmdType::NextSubpass:
             if (in_pass) census.add(c);
             break;
         case CmdType::Draw:
@@ -1048,12 +1059,15 @@ VkResult check_no_alloc(CommandBuffer* cb) {
     Pipeline* pipeline = nullptr;
     RenderPass* pass = nullptr;
     Framebuffer* fb = nullptr;
+    uint32_t subpass = 0;
     for (const Cmd& c : cb->cmds) {
         switch (c.type) {
         case CmdType::BeginRenderPass:
             pass = static_cast<RenderPass*>(c.p[0]);
             fb = static_cast<Framebuffer*>(c.p[1]);
+            subpass = 0;
             break;
+        case CmdType::NextSubpass: subpass++; break;
         case CmdType::EndRenderPass: pass = nullptr; fb = nullptr; break;
         case CmdType::BindPipeline: pipeline = static_cast<Pipeline*>(c.p[0]); break;
         case CmdType::Draw:
@@ -1062,7 +1076,9 @@ VkResult check_no_alloc(CommandBuffer* cb) {
             const uint32_t count = c.u[0], instances = c.u[1];
             const uint32_t ppi = primitives_per_instance(pipeline->topology, count);
             // the attachment that sizes the draw: colour, else depth
-            const uint32_t index = !pass->colour.empty() ? pass->colour[0] : pass->depth;
+            if (subpass >= pass->subpasses.size()) break;
+            const Subpass& sub = pass->subpasses[subpass];
+            const uint32_t index = !sub.colour.empty() ? sub.colour[0] : sub.depth;
             if (index == VK_ATTACHMENT_UNUSED || index >= fb->attachments.size()) break;
             const ImageView* cv = fb->attachments[index];
             uint32_t w = 0, h = 0;

@@ -838,17 +838,23 @@ VKAPI_ATTR void VKAPI_CALL UpdateDescriptorSets(VkDevice, uint32_t nw, const VkW
 // ------------------------------------------------- render pass, framebuffer --
 
 VKAPI_ATTR VkResult VKAPI_CALL CreateRenderPass(VkDevice, const VkRenderPassCreateInfo* ci, const VkAllocationCallbacks* alloc, VkRenderPass* out) {
-    if (ci->subpassCount != 1) {
-        rt::set_last_error("vkCreateRenderPass: only single-subpass render passes are supported");
-        return VK_ERROR_FEATURE_NOT_PRESENT;
+    if (ci->subpassCount == 0 || !ci->pSubpasses) {
+        rt::set_last_error("vkCreateRenderPass: a render pass needs a subpass");
+        return VK_ERROR_INITIALIZATION_FAILED;
     }
     auto* rp = host_new<RenderPass>(alloc, kScopeObject);
     if (!rp) return VK_ERROR_OUT_OF_HOST_MEMORY;
     rp->attachments.assign(ci->pAttachments, ci->pAttachments + ci->attachmentCount);
-    const auto& sp = ci->pSubpasses[0];
-    for (uint32_t i = 0; i < sp.colorAttachmentCount; i++)
-        if (sp.pColorAttachments[i].attachment != VK_ATTACHMENT_UNUSED) rp->colour.push_back(sp.pColorAttachments[i].attachment);
-    if (sp.pDepthStencilAttachment) rp->depth = sp.pDepthStencilAttachment->attachment;
+    // each subpass's colour and depth references (input attachments and
+    // dependencies need nothing: subpasses run in order on one stream)
+    for (uint32_t k = 0; k < ci->subpassCount; k++) {
+        const auto& sp = ci->pSubpasses[k];
+        Subpass sub;
+        for (uint32_t i = 0; i < sp.colorAttachmentCount; i++)
+            if (sp.pColorAttachments[i].attachment != VK_ATTACHMENT_UNUSED) sub.colour.push_back(sp.pColorAttachments[i].attachment);
+        if (sp.pDepthStencilAttachment) sub.depth = sp.pDepthStencilAttachment->attachment;
+        rp->subpasses.push_back(sub);
+    }
     *out = to_handle<VkRenderPass>(rp);
     return VK_SUCCESS;
 }
@@ -949,6 +955,8 @@ VKAPI_ATTR void VKAPI_CALL CmdSetDepthBounds(VkCommandBuffer, float, float) {}
 VKAPI_ATTR void VKAPI_CALL CmdSetStencilCompareMask(VkCommandBuffer, VkStencilFaceFlags, uint32_t) {}
 VKAPI_ATTR void VKAPI_CALL CmdSetStencilWriteMask(VkCommandBuffer, VkStencilFaceFlags, uint32_t) {}
 VKAPI_ATTR void VKAPI_CALL CmdSetStencilReference(VkCommandBuffer, VkStencilFaceFlags, uint32_t) {}
+// vkCmdNextSubpass (CPVulkan/CommandBuffer.cpp:649-664, 931-935).
+VKAPI_ATTR void VKAPI_CALL CmdNextSubpass(VkCommandBuffer cmd, VkSubpassContents) { push(cmd, CmdType::NextSubpass); }
 VKAPI_ATTR void VKAPI_CALL CmdBindDescriptorSets(VkCommandBuffer cmd, VkPipelineBindPoint, VkPipelineLayout, uint32_t first, uint32_t n,
                                                  const VkDescriptorSet* sets, uint32_t ndyn, const uint32_t* dyn) {
     auto& c = push(cmd, CmdType::BindDescriptorSets);
@@ -1296,7 +1304,7 @@ const Entry kDevice[] = {
     {"vkCmdDrawIndirectCountAMD", reinterpret_cast<PFN_vkVoidFunction>(CmdDrawIndirectCount)}, E(CmdCopyBuffer), E(CmdCopyImage),
     E(CmdClearColorImage), E(CmdClearDepthStencilImage), E(CmdClearAttachments), E(CmdCopyBufferToImage), E(CmdBlitImage),
     E(CmdCopyImageToBuffer), E(CmdFillBuffer), E(CmdUpdateBuffer), E(CmdPipelineBarrier), E(CmdPushConstants), E(CmdBeginRenderPass),
-    E(CmdEndRenderPass), E(QueueSubmit), E(CreateFence), E(DestroyFence), E(ResetFences), E(GetFenceStatus), E(WaitForFences),
+    E(CmdNextSubpass), E(CmdEndRenderPass), E(QueueSubmit), E(CreateFence), E(DestroyFence), E(ResetFences), E(GetFenceStatus), E(WaitForFences),
     E(CreateSemaphore), E(DestroySemaphore),
 };
 #undef E

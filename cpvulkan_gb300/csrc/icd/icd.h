@@ -124,10 +124,15 @@ struct PipelineLayout {
     std::vector<VkPushConstantRange> push;
 };
 
+// The attachments one subpass draws to.
+struct Subpass {
+    std::vector<uint32_t> colour;     // colour attachment indices
+    uint32_t depth = VK_ATTACHMENT_UNUSED;
+};
+
 struct RenderPass {
     std::vector<VkAttachmentDescription> attachments;
-    std::vector<uint32_t> colour;     // subpass 0 colour attachment indices
-    uint32_t depth = VK_ATTACHMENT_UNUSED;
+    std::vector<Subpass> subpasses;   // at least one
 };
 
 struct Framebuffer {
@@ -188,7 +193,7 @@ std::string compose_module(const std::vector<std::string>& stages, const std::ve
 enum class CmdType : uint8_t {
     BeginRenderPass, EndRenderPass, BindPipeline, BindVertexBuffers, BindIndexBuffer, BindDescriptorSets, PushConstants,
     SetViewport, SetScissor, SetBlendConstants, Draw, DrawIndexed, DrawIndirect, DrawIndexedIndirect, CopyBuffer,
-    CopyBufferToImage, CopyImageToBuffer, FillBuffer, UpdateBuffer, Barrier, BlitImage, CopyImage, ClearImage, ClearAttachments,
+    CopyBufferToImage, CopyImageToBuffer, FillBuffer, UpdateBuffer, Barrier, BlitImage, CopyImage, ClearImage, ClearAttachments, NextSubpass,
 };
 
 struct Cmd {

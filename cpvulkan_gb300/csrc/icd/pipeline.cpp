@@ -307,13 +307,15 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     const RenderPass* pass = reinterpret_cast<const RenderPass*>(ci.renderPass);
     if (!pass) return reject("no render pass");
     // one colour attachment, or none (a depth-only pass)
-    if (pass->colour.size() > 1) return reject("at most one colour attachment is supported");
-    const VkFormat cfmt = pass->colour.empty() ? VK_FORMAT_UNDEFINED : pass->attachments[pass->colour[0]].format;
-    if (!pass->colour.empty() && !supported_colour(cfmt)) return reject("colour attachment format " + std::to_string(cfmt));
-    if (pass->colour.empty() && pass->depth == VK_ATTACHMENT_UNUSED) return reject("a colour or a depth attachment is required");
+    if (ci.subpass >= pass->subpasses.size()) return reject("subpass " + std::to_string(ci.subpass) + " of the render pass");
+    const Subpass& sub = pass->subpasses[ci.subpass];
+    if (sub.colour.size() > 1) return reject("at most one colour attachment is supported");
+    const VkFormat cfmt = sub.colour.empty() ? VK_FORMAT_UNDEFINED : pass->attachments[sub.colour[0]].format;
+    if (!sub.colour.empty() && !supported_colour(cfmt)) return reject("colour attachment format " + std::to_string(cfmt));
+    if (sub.colour.empty() && sub.depth == VK_ATTACHMENT_UNUSED) return reject("a colour or a depth attachment is required");
     VkFormat dfmt = VK_FORMAT_UNDEFINED;
-    if (pass->depth != VK_ATTACHMENT_UNUSED) {
-        dfmt = pass->attachments[pass->depth].format;
+    if (sub.depth != VK_ATTACHMENT_UNUSED) {
+        dfmt = pass->attachments[sub.depth].format;
         if (!supported_depth(dfmt)) return reject("depth attachment format " + std::to_string(dfmt));
     }
 

@@ -1271,6 +1271,7 @@ typedef void (VKAPI_PTR* PFN_vkCmdPipelineBarrier)(VkCommandBuffer, VkPipelineSt
 typedef void (VKAPI_PTR* PFN_vkCmdPushConstants)(VkCommandBuffer, VkPipelineLayout, VkShaderStageFlags, uint32_t, uint32_t, const void*);
 typedef void (VKAPI_PTR* PFN_vkCmdBeginRenderPass)(VkCommandBuffer, const VkRenderPassBeginInfo*, VkSubpassContents);
 typedef void (VKAPI_PTR* PFN_vkCmdEndRenderPass)(VkCommandBuffer);
+typedef void (VKAPI_PTR* PFN_vkCmdNextSubpass)(VkCommandBuffer, VkSubpassContents);
 typedef VkResult (VKAPI_PTR* PFN_vkQueueSubmit)(VkQueue, uint32_t, const VkSubmitInfo*, VkFence);
 typedef VkResult (VKAPI_PTR* PFN_vkQueueWaitIdle)(VkQueue);
 typedef VkResult (VKAPI_PTR* PFN_vkCreateFence)(VkDevice, const VkFenceCreateInfo*, const VkAllocationCallbacks*, VkFence*);

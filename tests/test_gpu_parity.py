@@ -161,3 +161,18 @@ def test_coverage_kats(gpu_ctx, oracle, monkeypatch, tile, schedule):
         report, stats = check(gpu_ctx, oracle, kat.scene(case))
         assert stats["fragments"] == int(kat.coverage(case).sum())
         assert report["color_pixels_differing"] == 0, (case[0], report)
+
+
+@pytest.mark.parametrize("config,params", [(c.PROGRAM, [c.PROGRAM_CUBE, 0x18 | 0x100, 64, 48, 24]), (c.HEIGHTFIELD, [64, 256, 160]),
+                                           (c.PROGRAM, [c.PROGRAM_FLATQUAD, 0x20, 64, 48, 24]), (c.BATCH, [24, 3000, 320, 200]),
+                                           (c.CUBE, [45])])
+def test_second_subpass(gpu_ctx, oracle, monkeypatch, config, params):
+    """vkCmdNextSubpass (CPVulkan/CommandBuffer.cpp:649-664): the frame draws
+    in subpass 1 of a two-subpass render pass whose subpass 0 references only
+    the depth attachment, with pipelines created for subpass 1; the image
+    equals the oracle's (a pass of several subpasses runs per draw)."""
+    monkeypatch.setenv("CPVH_SUBPASSES", "2")
+    scene = c.Scene(config, 3, params)
+    report, stats = check(gpu_ctx, oracle, scene)
+    assert stats["fragments_written"] > 0
+    assert report["color_pixels_differing"] == 0, report
