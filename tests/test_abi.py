@@ -116,7 +116,7 @@ def test_dynamic_state_commands_resolve(native):
     instance = ctypes.c_void_p(16)  # the lookup does not dereference it
     for name in (b"vkCmdSetViewport", b"vkCmdSetScissor", b"vkCmdSetBlendConstants", b"vkCmdSetLineWidth", b"vkCmdSetDepthBias",
                  b"vkCmdSetDepthBounds", b"vkCmdSetStencilCompareMask", b"vkCmdSetStencilWriteMask", b"vkCmdSetStencilReference",
-                 b"vkCmdCopyImage", b"vkCmdClearColorImage", b"vkCmdClearDepthStencilImage", b"vkCmdClearAttachments"):
+                 b"vkCmdCopyImage", b"vkCmdClearColorImage", b"vkCmdClearDepthStencilImage", b"vkCmdClearAttachments", b"vkCmdNextSubpass"):
         assert gipa(instance, name), name
 
 
