@@ -553,9 +553,9 @@ VkResult create_scene_pass(cpvh_context* c, const cpv_scene* s, VkRenderPass* ou
 }
 
 VkResult make_pass_and_layout(cpvh_context* c, const cpv_scene* s, bool with_sets, VkRenderPass& pass, VkDescriptorSetLayout& set_layout,
-                              VkPipelineLayout& layout) {
+                              VkPipelineLayout& layout, bool two_subpasses = false) {
     const Fns& f = c->f;
-    VkResult res = create_scene_pass(c, s, &pass);
+    VkResult res = create_scene_pass(c, s, &pass, two_subpasses);
     if (res != VK_SUCCESS) return res;
     std::vector<VkDescriptorSetLayoutBinding> lb;
     if (with_sets && s->uniform_bytes) lb.push_back({0, VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER, 1, VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
@@ -916,8 +916,13 @@ int cpvh_compile_pipelines(cpvh_context* c, const cpv_scene* s, char* err, uint3
     std::vector<VkShaderModule> modules;
     std::vector<VkPipeline> pipelines;
     std::string perr;
-    int result = make_pass_and_layout(c, s, true, pass, set_layout, layout);
-    if (result == VK_SUCCESS && !build_pipelines(c, s, pass, layout, modules, pipelines, perr)) result = VK_ERROR_INITIALIZATION_FAILED;
+    // CPVH_SUBPASSES=2: pipelines for subpass 1 of the two-subpass pass the
+    // renderer uses; "2:0": for its subpass 0 (depth attachment only)
+    const char* sp = std::getenv("CPVH_SUBPASSES");
+    const bool two = sp && sp[0] == '2';
+    const uint32_t subpass = two && std::strcmp(sp, "2:0") != 0 ? 1u : 0u;
+    int result = make_pass_and_layout(c, s, true, pass, set_layout, layout, two);
+    if (result == VK_SUCCESS && !build_pipelines(c, s, pass, layout, modules, pipelines, perr, subpass)) result = VK_ERROR_INITIALIZATION_FAILED;
     if (result != VK_SUCCESS) {
         g_err = perr + " " + icd_error(c);
         if (err && err_len) std::snprintf(err, err_len, "%s", g_err.c_str());

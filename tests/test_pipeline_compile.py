@@ -119,3 +119,15 @@ def test_module_configuration(compile_ctx, program, variant, expect):
     text = _module_source(compile_ctx, program, variant)
     for name, value in expect.items():
         assert "#define %s %s\n" % (name, value) in text, (name, value)
+
+
+@pytest.mark.parametrize("subpasses,colour", [("2", "37"), ("2:0", "0")])
+def test_pipeline_takes_its_subpass_formats(compile_ctx, monkeypatch, subpasses, colour):
+    """A pipeline is compiled for the attachments of the subpass it is created
+    for: in a render pass whose subpass 0 references only the depth
+    attachment and subpass 1 colour and depth, a subpass-1 pipeline writes
+    RGBA8 colour and a subpass-0 pipeline none."""
+    monkeypatch.setenv("CPVH_SUBPASSES", subpasses)
+    text = _module_source(compile_ctx, c.PROGRAM_CUBE, 0x18 | 0x100)
+    assert "#define CPV_COLOR_FORMAT %s\n" % colour in text
+    assert "#define CPV_DEPTH_FORMAT 130\n" in text
