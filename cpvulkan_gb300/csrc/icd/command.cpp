@@ -284,6 +284,7 @@ VkResult draw(Queue* q, State& s, uint32_t count, uint32_t instances, uint32_t f
     if (vr != VK_SUCCESS || empty) return vr;
     Pipeline* p = s.pipeline;
     const int r = no_alloc ? rt::draw_plain_static(q->stream, p->module, P) : rt::draw_plain(q->stream, p->module, P, q->scratch);
+    if (r == rt::kErrOutOfMemory) return VK_ERROR_OUT_OF_DEVICE_MEMORY;
     return r == rt::kOk ? VK_SUCCESS : VK_ERROR_DEVICE_LOST;
 }
 
@@ -1055,11 +1056,33 @@ void precompile_batches(CommandBuffer* cb) {
 
 const char* last_tuning() { return g_last_tuning.c_str(); }
 
-VkResult check_no_alloc(CommandBuffer* cb) {
+VkResult check_no_alloc(Queue* q, CommandBuffer* cb) {
     Pipeline* pipeline = nullptr;
     RenderPass* pass = nullptr;
     Framebuffer* fb = nullptr;
     uint32_t subpass = 0;
+    // The attachment that sizes a draw of the current subpass: colour, else
+    // depth. False when there is none (execute() reports that).
+    auto target = [&](uint32_t& w, uint32_t& h) {
+        if (!pipeline || !pass || !fb || subpass >= pass->subpasses.size()) return false;
+        const Subpass& sub = pass->subpasses[subpass];
+        const uint32_t index = !sub.colour.empty() ? sub.colour[0] : sub.depth;
+        if (index == VK_ATTACHMENT_UNUSED || index >= fb->attachments.size()) return false;
+        const ImageView* cv = fb->attachments[index];
+        if (!cv || !cv->image) return false;
+        view_base(cv, w, h);
+        return true;
+    };
+    auto fits = [&](uint32_t count, uint32_t instances, uint32_t w, uint32_t h) {
+        const uint32_t ppi = primitives_per_instance(pipeline->topology, count);
+        std::string err;
+        if (rt::static_scratch_check(static_cast<uint64_t>(ppi) * instances, pipeline->module.tile_shift, w, h, err) != rt::kOk) {
+            rt::set_last_error("cpv_queue_submit_no_alloc: " + err);
+            return false;
+        }
+        return true;
+    };
+    const std::vector<DeviceMemory*> none;
     for (const Cmd& c : cb->cmds) {
         switch (c.type) {
         case CmdType::BeginRenderPass:
@@ -1072,23 +1095,21 @@ VkResult check_no_alloc(CommandBuffer* cb) {
         case CmdType::BindPipeline: pipeline = static_cast<Pipeline*>(c.p[0]); break;
         case CmdType::Draw:
         case CmdType::DrawIndexed: {
-            if (!pipeline || !pass || !fb) break;  // execute() reports these
-            const uint32_t count = c.u[0], instances = c.u[1];
-            const uint32_t ppi = primitives_per_instance(pipeline->topology, count);
-            // the attachment that sizes the draw: colour, else depth
-            if (subpass >= pass->subpasses.size()) break;
-            const Subpass& sub = pass->subpasses[subpass];
-            const uint32_t index = !sub.colour.empty() ? sub.colour[0] : sub.depth;
-            if (index == VK_ATTACHMENT_UNUSED || index >= fb->attachments.size()) break;
-            const ImageView* cv = fb->attachments[index];
             uint32_t w = 0, h = 0;
-            if (!cv || !cv->image) break;
-            view_base(cv, w, h);
-            std::string err;
-            if (rt::static_scratch_check(static_cast<uint64_t>(ppi) * instances, pipeline->module.tile_shift, w, h, err) != rt::kOk) {
-                rt::set_last_error("cpv_queue_submit_no_alloc: " + err);
-                return VK_ERROR_OUT_OF_DEVICE_MEMORY;
-            }
+            if (target(w, h) && !fits(c.u[0], c.u[1], w, h)) return VK_ERROR_OUT_OF_DEVICE_MEMORY;
+            break;
+        }
+        case CmdType::DrawIndirect:
+        case CmdType::DrawIndexedIndirect: {
+            // The records as they stand at submission (the host mirror, or
+            // HBM after the queue's earlier work). Records that commands of
+            // this same submission rewrite are checked again at replay.
+            uint32_t w = 0, h = 0;
+            if (!target(w, h)) break;
+            std::vector<IndirectDraw> records;
+            if (read_indirect(q, c, none, records) != VK_SUCCESS) break;  // execute() reports it
+            for (const IndirectDraw& d : records)
+                if (!fits(d.count, d.instances, w, h)) return VK_ERROR_OUT_OF_DEVICE_MEMORY;
             break;
         }
         default: break;

@@ -1371,6 +1371,11 @@ CPV_EXPORT double cpv_queue_elapsed_ms(VkQueue queue, uint32_t a, uint32_t b) {
     return ms;
 }
 
+CPV_EXPORT uint64_t cpv_queue_scratch_generation(VkQueue queue) {
+    auto* q = reinterpret_cast<cpv::icd::Queue*>(queue);
+    return q ? q->scratch.generation() : 0;
+}
+
 CPV_EXPORT void cpv_profile_enable(int on) { cpv::rt::profile_enable(on != 0); }
 
 CPV_EXPORT int cpv_profile_get(const char* kernel, uint64_t* launches, double* total_ms) { return cpv::rt::profile_get(kernel, launches, total_ms); }
@@ -1396,7 +1401,7 @@ CPV_EXPORT VkResult VKAPI_CALL cpv_queue_submit_no_alloc(VkQueue queue, uint32_t
     // Reject an oversized draw before any work of the submission is enqueued.
     for (uint32_t i = 0; i < submitCount; i++)
         for (uint32_t k = 0; k < pSubmits[i].commandBufferCount; k++) {
-            const VkResult r = check_no_alloc(reinterpret_cast<CommandBuffer*>(pSubmits[i].pCommandBuffers[k]));
+            const VkResult r = check_no_alloc(q, reinterpret_cast<CommandBuffer*>(pSubmits[i].pCommandBuffers[k]));
             if (r != VK_SUCCESS) return r;
         }
     return submit(queue, submitCount, pSubmits, fence, true);

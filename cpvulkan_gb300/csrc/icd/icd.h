@@ -332,7 +332,7 @@ void precompile_batches(CommandBuffer* cb);
 const char* last_tuning();
 // Checks, before any work is enqueued, that every draw of `cb` fits the fixed
 // scratch array (VK_ERROR_OUT_OF_DEVICE_MEMORY and a message otherwise).
-VkResult check_no_alloc(CommandBuffer* cb);
+VkResult check_no_alloc(Queue* q, CommandBuffer* cb);
 
 // Pipeline creation (pipeline.cpp).
 VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGraphicsPipelineCreateInfo& info, Pipeline** out);

@@ -880,7 +880,12 @@ StaticCarve static_carve(uint64_t prims, uint64_t bins) {
 }
 
 // The binning decision of draw_plain: direct (no bins) or spans per tile.
-bool static_direct(uint64_t prims, uint64_t tiles) { return prims * tiles <= env_u32("CPV_DIRECT_LIMIT", 1u << 18); }
+// CPV_DIRECT_LIMIT is read once per process, so the pre-check and the draw
+// always take the same path.
+bool static_direct(uint64_t prims, uint64_t tiles) {
+    static const uint32_t limit = env_u32("CPV_DIRECT_LIMIT", 1u << 18);
+    return prims * tiles <= limit;
+}
 
 // Spans for a draw in the fixed array: draw_plain's choice, halved until the
 // buffers leave at least a quarter of the array for the bin list (or one

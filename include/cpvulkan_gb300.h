@@ -73,6 +73,11 @@ CPV_EXPORT int cpv_device_available(void);
 CPV_EXPORT int cpv_queue_record(VkQueue queue, uint32_t slot);
 CPV_EXPORT double cpv_queue_elapsed_ms(VkQueue queue, uint32_t slot_begin, uint32_t slot_end);
 
+/* How many times the queue's grow-only binning scratch has been allocated
+ * or regrown (cudaMalloc) since the queue was created; 0 for a queue that
+ * only ever ran cpv_queue_submit_no_alloc. */
+CPV_EXPORT uint64_t cpv_queue_scratch_generation(VkQueue queue);
+
 /* Per-kernel device timing: while enabled, every kernel of the draw paths is
  * bracketed by CUDA events on its stream (batched render passes then run
  * without their CUDA graph). cpv_profile_get returns the launches and the
@@ -101,6 +106,12 @@ CPV_EXPORT void cpv_profile_reset(void);
  *   a submission holding a draw that does not fit is rejected before any of
  *   its work is enqueued: VK_ERROR_OUT_OF_DEVICE_MEMORY, reason in
  *   cpv_last_error(). Draws of up to about 4 million primitives fit.
+ *   Indirect draws are checked through their records as they stand at the
+ *   call (read from host-visible memory, or from device memory after the
+ *   queue's earlier work); a record that a command of the same submission
+ *   rewrites is checked again when its draw runs, and one that no longer
+ *   fits then ends the submission with VK_ERROR_OUT_OF_DEVICE_MEMORY after
+ *   the commands before it were enqueued.
  * - The bin counters must start at zero for every draw; the call zeroes
  *   them on the queue's stream itself. Nothing else needs an initial value.
  * - The array is shared by every queue of the process on a device: calls
