@@ -386,7 +386,10 @@ void build_heightfield(Store& st, uint64_t seed, uint32_t n, uint32_t width, uin
 
 // ---------------------------------------------------------------- blend --
 
-void build_blend(Store& st, uint64_t seed, uint32_t quads, uint32_t width, uint32_t height) {
+// smooth = 0: flat colour per quad (FLATQUAD program). smooth = 1: the same
+// quads drawn with the CUBE program (identity MVP, w = 1) and a colour per
+// corner, so the fragment shader's input is interpolated per pixel.
+void build_blend(Store& st, uint64_t seed, uint32_t quads, uint32_t width, uint32_t height, uint32_t smooth) {
     cpv_scene& s = st.scene;
     s.width = width;
     s.height = height;
@@ -407,20 +410,37 @@ void build_blend(Store& st, uint64_t seed, uint32_t quads, uint32_t width, uint3
             const double px = xs[k & 1], py = ys[k >> 1];
             append_f(st.vertex, static_cast<float>(px / width * 2.0 - 1.0));
             append_f(st.vertex, static_cast<float>(py / height * 2.0 - 1.0));
-            for (float c : col) append_f(st.vertex, c);
+            if (smooth) {
+                append_f(st.vertex, 0.0f);
+                append_f(st.vertex, 1.0f);
+                // each corner's colour: the quad's, channels scaled by [0.5, 1)
+                for (int c = 0; c < 3; c++) append_f(st.vertex, col[c] * static_cast<float>(rng.range(0.5, 1.0)));
+                append_f(st.vertex, col[3]);
+            } else {
+                for (float c : col) append_f(st.vertex, c);
+            }
         }
         const uint32_t b = q * 4;
         const uint32_t idx[6] = {b, b + 1, b + 2, b + 2, b + 1, b + 3};
         for (uint32_t x : idx) append(st.index, x);
     }
     s.index_type = VK_INDEX_TYPE_UINT32;
-    cpv_scene_pipeline p = base_pipeline(CPV_PROGRAM_FLATQUAD);
+    cpv_scene_pipeline p = base_pipeline(smooth ? CPV_PROGRAM_CUBE : CPV_PROGRAM_FLATQUAD);
     set_src_over(p);
     p.num_bindings = 1;
-    p.bindings[0] = {0, 24, VK_VERTEX_INPUT_RATE_VERTEX};
     p.num_attributes = 2;
-    p.attributes[0] = {0, 0, VK_FORMAT_R32G32_SFLOAT, 0};
-    p.attributes[1] = {1, 0, VK_FORMAT_R32G32B32A32_SFLOAT, 8};
+    if (smooth) {
+        p.bindings[0] = {0, 32, VK_VERTEX_INPUT_RATE_VERTEX};
+        p.attributes[0] = {0, 0, VK_FORMAT_R32G32B32A32_SFLOAT, 0};
+        p.attributes[1] = {1, 0, VK_FORMAT_R32G32B32A32_SFLOAT, 16};
+        st.uniform.assign(64, 0);
+        float* m = reinterpret_cast<float*>(st.uniform.data());
+        m[0] = m[5] = m[10] = m[15] = 1.0f;  // identity MVP
+    } else {
+        p.bindings[0] = {0, 24, VK_VERTEX_INPUT_RATE_VERTEX};
+        p.attributes[0] = {0, 0, VK_FORMAT_R32G32_SFLOAT, 0};
+        p.attributes[1] = {1, 0, VK_FORMAT_R32G32B32A32_SFLOAT, 8};
+    }
     st.pipelines.push_back(p);
     cpv_scene_draw d{};
     d.pipeline = 0;
@@ -831,7 +851,10 @@ cpv_scene* cpvh_scene_create(uint32_t config, uint64_t seed, const uint64_t* par
     switch (config) {
     case CPVH_CUBE: build_cube(*st, static_cast<uint32_t>(param(0, 0))); break;
     case CPVH_HEIGHTFIELD: build_heightfield(*st, seed, static_cast<uint32_t>(param(0, 1024)), static_cast<uint32_t>(param(1, 1920)), static_cast<uint32_t>(param(2, 1080))); break;
-    case CPVH_BLEND: build_blend(*st, seed, static_cast<uint32_t>(param(0, 200000)), static_cast<uint32_t>(param(1, 1920)), static_cast<uint32_t>(param(2, 1080))); break;
+    case CPVH_BLEND:
+        build_blend(*st, seed, static_cast<uint32_t>(param(0, 200000)), static_cast<uint32_t>(param(1, 1920)), static_cast<uint32_t>(param(2, 1080)),
+                    static_cast<uint32_t>(param(3, 0)));
+        break;
     case CPVH_BATCH:
         build_batch(*st, seed, static_cast<uint32_t>(param(0, 4096)), static_cast<uint32_t>(param(1, 200000)), static_cast<uint32_t>(param(2, 2560)),
                     static_cast<uint32_t>(param(3, 1440)));

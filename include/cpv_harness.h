@@ -23,7 +23,7 @@ extern "C" {
 enum cpvh_config {
     CPVH_CUBE = 1,        /* spinning cube, 500x500 BGRA8 + D16 (param0 = frame index)                         */
     CPVH_HEIGHTFIELD = 2, /* textured heightfield (param0 = grid side, default 1024; param1/2 = width/height)   */
-    CPVH_BLEND = 3,       /* blend-bound overdraw quads (param0 = quad count, default 200000; param1/2 = w/h)  */
+    CPVH_BLEND = 3,       /* blend-bound overdraw quads (param0 = quad count, default 200000; param1/2 = w/h; param3 = 1: colour per corner, interpolated) */
     CPVH_BATCH = 4,       /* 4096 icosphere draws (param0 = draw count, param1 = max triangles, param2/3 = w/h) */
     CPVH_PROGRAM = 5,     /* small scene for one shader program (param0 = cpv_program, param1 = variant)       */
     CPVH_SERVE = 6        /* one serving request (param0 = side px, param1 = triangles, param2 = client id)     */

@@ -15,8 +15,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <limits>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -574,7 +577,18 @@ struct Frame {
     uint32_t depth_size;
     Resources res;
     cpv_oracle_stats* stats;
+    /* Rows this frame writes: y % row_stride == row_index (1, 0: all rows).
+     * The threaded entry gives each thread its own interleaved rows; every
+     * pixel is then written by one thread, in API order. */
+    uint32_t row_stride = 1, row_index = 0;
+    bool count_prims = true;  /* count primitives (one thread of several) */
 };
+
+/* The first row >= start that the frame writes. */
+int64_t first_row(const Frame& f, int64_t start) {
+    const int64_t r = start % f.row_stride;
+    return start + (static_cast<int64_t>(f.row_index) + f.row_stride - r) % f.row_stride;
+}
 
 /* Attribute fetch (LLVMRuntime/PipelineCompiler.cpp:821-896): address =
  * binding base + stride * (vertex or instance id) + attribute offset; float
@@ -770,94 +784,143 @@ void fragment(Frame& f, const cpv_scene_pipeline& p, uint32_t x, uint32_t y, flo
     }
 }
 
-/* ProcessTriangles + GetFragmentInput + DrawPixel
- * (CPVulkan/CommandBuffer.Draw.cpp:874-954, 1300-1313, 1510-1594). */
-void rasterise(Frame& f, const cpv_scene_pipeline& p, const Assembled& as, const std::vector<VsOut>& vs) {
+/* One triangle after set-up (CPVulkan/CommandBuffer.Draw.cpp:1510-1569,
+ * 874-897): NDC positions with clip w, the screen box, |area|, facing. */
+struct TriSetup {
+    float P[3][4];
+    float area;
+    uint32_t provoking, v[3];
+    int32_t start_x, start_y, end_x, end_y;
+    bool front, culled;
+};
+
+/* The area, facing and cull test of GetFragmentInput
+ * (CPVulkan/CommandBuffer.Draw.cpp:879-900), once per triangle. */
+void setup_facing(TriSetup& ts, uint32_t cull_mode) {
+    const float (&P)[3][4] = ts.P;
+    float area = edge(P[0][0], P[0][1], P[1][0], P[1][1], P[2][0], P[2][1]);
+    if (area < 0) {
+        area = -area;
+        ts.front = false;
+    } else {
+        ts.front = true;
+    }
+    ts.area = area;
+    ts.culled = ((cull_mode & CULL_BACK) && !ts.front) || ((cull_mode & CULL_FRONT) && ts.front);
+}
+
+/* ProcessTriangles up to the pixel loop (CPVulkan/CommandBuffer.Draw.cpp:1510-1569)
+ * and the area / facing / cull part of GetFragmentInput (:874-897), for the
+ * triangle at as.prims[t]. */
+void setup_triangle(const Frame& f, const cpv_scene_pipeline& p, const Assembled& as, const std::vector<VsOut>& vs, size_t t, TriSetup& ts) {
+    const cpv_scene* s = f.s;
+    const float vw = s->viewport[2], vh = s->viewport[3];
+    const int32_t iw = f2i(vw), ih = f2i(vh);
+    const int32_t fb_w = static_cast<int32_t>(s->width), fb_h = static_cast<int32_t>(s->height);
+    ts.provoking = as.prims[t];
+    uint32_t i0 = as.prims[t + 1], i1 = as.prims[t + 2], i2 = as.prims[t + 3];
+    if (p.front_face == FRONT_FACE_CW) std::swap(i0, i2);
+    ts.v[0] = i0, ts.v[1] = i1, ts.v[2] = i2;
+    float (&P)[3][4] = ts.P;
+    for (int k = 0; k < 3; k++) {
+        const VsOut& v = vs[ts.v[k]];
+        const float w = v.pos[3];
+        P[k][0] = v.pos[0] / w;
+        P[k][1] = v.pos[1] / w;
+        P[k][2] = v.pos[2] / w;
+        P[k][3] = w;
+    }
+    int32_t sx[3], sy[3];
+    for (int k = 0; k < 3; k++) {
+        sx[k] = f2i(((P[k][0] + 1.0f) * 0.5f) * vw);
+        sy[k] = f2i(((P[k][1] + 1.0f) * 0.5f) * vh);
+    }
+    ts.start_x = std::max<int32_t>(0, std::min({sx[0], sx[1], sx[2]}));
+    ts.start_y = std::max<int32_t>(0, std::min({sy[0], sy[1], sy[2]}));
+    int64_t end_x = std::min<int64_t>(iw, static_cast<int64_t>(std::max({sx[0], sx[1], sx[2]})) + 1);
+    int64_t end_y = std::min<int64_t>(ih, static_cast<int64_t>(std::max({sy[0], sy[1], sy[2]})) + 1);
+    /* Pixels outside the attachment are never written (the reference
+     * assumes viewport == framebuffer; this bound keeps the restatement
+     * memory safe). */
+    ts.end_x = static_cast<int32_t>(std::min<int64_t>(end_x, fb_w));
+    ts.end_y = static_cast<int32_t>(std::min<int64_t>(end_y, fb_h));
+
+    setup_facing(ts, p.cull_mode);
+}
+
+/* GetFragmentInput up to the varyings (CPVulkan/CommandBuffer.Draw.cpp:874-909)
+ * at the pixel centre (xf, yf) of a set-up, uncull triangle: the three edge
+ * functions in the facing's order, rejection when any is negative, the
+ * weights divided by |area| and the screen-linear NDC depth. */
+bool fragment_weights(const TriSetup& ts, float xf, float yf, float w[3], float& depth) {
+    static const int kFront[3][2] = {{1, 2}, {2, 0}, {0, 1}};
+    static const int kBack[3][2] = {{2, 1}, {0, 2}, {1, 0}};
+    const int (*e)[2] = ts.front ? kFront : kBack;
+    const float (&P)[3][4] = ts.P;
+    for (int k = 0; k < 3; k++) {
+        const float* a = P[e[k][0]];
+        const float* b = P[e[k][1]];
+        w[k] = edge(a[0], a[1], b[0], b[1], xf, yf);
+    }
+    if (w[0] < 0 || w[1] < 0 || w[2] < 0) return false;
+    w[0] = w[0] / ts.area;
+    w[1] = w[1] / ts.area;
+    w[2] = w[2] / ts.area;
+    depth = (P[0][2] * w[0] + P[1][2] * w[1]) + P[2][2] * w[2];
+    return true;
+}
+
+/* The varyings of GetFragmentInput (SetDatum, CPVulkan/CommandBuffer.Draw.cpp:816-869,
+ * 911-951): perspective, linear or the provoking vertex's value, per float
+ * component in declaration order. */
+void fragment_inputs(const ProgramInfo& info, const TriSetup& ts, const std::vector<VsOut>& vs, const float w[3], float* inputs) {
+    const VsOut* v[3] = {&vs[ts.v[0]], &vs[ts.v[1]], &vs[ts.v[2]]};
+    const float pw[3] = {ts.P[0][3], ts.P[1][3], ts.P[2][3]};
+    int comp = 0;
+    for (int in = 0; in < info.num_inputs; in++) {
+        for (int c = 0; c < info.input_size[in]; c++, comp++) {
+            const float val[3] = {v[0]->var[comp], v[1]->var[comp], v[2]->var[comp]};
+            switch (info.input_interp[in]) {
+            case INTERP_PERSPECTIVE: inputs[comp] = interp_persp(pw, val, w); break;
+            case INTERP_LINEAR: inputs[comp] = interp_linear(val, w); break;
+            case INTERP_FLAT: inputs[comp] = vs[ts.provoking].var[comp]; break;
+            }
+        }
+    }
+}
+
+/* The pixel loop of ProcessTriangles (CPVulkan/CommandBuffer.Draw.cpp:1571-1594)
+ * with GetFragmentInput (:874-954) and DrawPixel's depth map (:1300-1313),
+ * over the frame's rows. */
+void raster_triangle(Frame& f, const cpv_scene_pipeline& p, const ProgramInfo& info, const TriSetup& ts, const std::vector<VsOut>& vs) {
     const cpv_scene* s = f.s;
     const float vw = s->viewport[2], vh = s->viewport[3];
     const float min_d = s->viewport[4], max_d = s->viewport[5];
     const float half_x = (1.0f / vw) * 0.5f;
     const float half_y = (1.0f / vh) * 0.5f;
+    for (int64_t y = first_row(f, ts.start_y); y < ts.end_y; y += f.row_stride) {
+        const float yf = (static_cast<float>(y) / vh + half_y) * 2.0f - 1.0f;
+        for (int64_t x = ts.start_x; x < ts.end_x; x++) {
+            const float xf = (static_cast<float>(x) / vw + half_x) * 2.0f - 1.0f;
+            float w[3], depth;
+            if (!fragment_weights(ts, xf, yf, w, depth)) continue;
+            float inputs[kMaxVaryings];
+            fragment_inputs(info, ts, vs, w, inputs);
+            const float mapped = (max_d - min_d) * depth + min_d;
+            fragment(f, p, static_cast<uint32_t>(x), static_cast<uint32_t>(y), mapped, ts.front, inputs);
+        }
+    }
+}
+
+/* ProcessTriangles + GetFragmentInput + DrawPixel
+ * (CPVulkan/CommandBuffer.Draw.cpp:874-954, 1300-1313, 1510-1594). */
+void rasterise(Frame& f, const cpv_scene_pipeline& p, const Assembled& as, const std::vector<VsOut>& vs) {
     const ProgramInfo info = program_info(p.program);
-    const int32_t iw = f2i(vw), ih = f2i(vh);
-    const int32_t fb_w = static_cast<int32_t>(s->width), fb_h = static_cast<int32_t>(s->height);
-
+    TriSetup ts;
     for (size_t t = 0; t + 4 <= as.prims.size(); t += 4) {
-        const uint32_t provoking = as.prims[t];
-        uint32_t i0 = as.prims[t + 1], i1 = as.prims[t + 2], i2 = as.prims[t + 3];
-        if (p.front_face == FRONT_FACE_CW) std::swap(i0, i2);
-        f.stats->triangles++;
-        const VsOut* v[3] = {&vs[i0], &vs[i1], &vs[i2]};
-        float P[3][4];
-        for (int k = 0; k < 3; k++) {
-            const float w = v[k]->pos[3];
-            P[k][0] = v[k]->pos[0] / w;
-            P[k][1] = v[k]->pos[1] / w;
-            P[k][2] = v[k]->pos[2] / w;
-            P[k][3] = w;
-        }
-        int32_t sx[3], sy[3];
-        for (int k = 0; k < 3; k++) {
-            sx[k] = f2i(((P[k][0] + 1.0f) * 0.5f) * vw);
-            sy[k] = f2i(((P[k][1] + 1.0f) * 0.5f) * vh);
-        }
-        const int64_t start_x = std::max<int64_t>(0, std::min({sx[0], sx[1], sx[2]}));
-        const int64_t start_y = std::max<int64_t>(0, std::min({sy[0], sy[1], sy[2]}));
-        int64_t end_x = std::min<int64_t>(iw, static_cast<int64_t>(std::max({sx[0], sx[1], sx[2]})) + 1);
-        int64_t end_y = std::min<int64_t>(ih, static_cast<int64_t>(std::max({sy[0], sy[1], sy[2]})) + 1);
-        /* Pixels outside the attachment are never written (the reference
-         * assumes viewport == framebuffer; this bound keeps the restatement
-         * memory safe). */
-        end_x = std::min<int64_t>(end_x, fb_w);
-        end_y = std::min<int64_t>(end_y, fb_h);
-
-        float area = edge(P[0][0], P[0][1], P[1][0], P[1][1], P[2][0], P[2][1]);
-        bool front;
-        int e[3][2];
-        if (area < 0) {
-            area = -area;
-            front = false;
-            e[0][0] = 2; e[0][1] = 1; e[1][0] = 0; e[1][1] = 2; e[2][0] = 1; e[2][1] = 0;
-        } else {
-            front = true;
-            e[0][0] = 1; e[0][1] = 2; e[1][0] = 2; e[1][1] = 0; e[2][0] = 0; e[2][1] = 1;
-        }
-        if ((p.cull_mode & CULL_BACK) && !front) continue;
-        if ((p.cull_mode & CULL_FRONT) && front) continue;
-
-        for (int64_t y = start_y; y < end_y; y++) {
-            const float yf = (static_cast<float>(y) / vh + half_y) * 2.0f - 1.0f;
-            for (int64_t x = start_x; x < end_x; x++) {
-                const float xf = (static_cast<float>(x) / vw + half_x) * 2.0f - 1.0f;
-                float w[3];
-                for (int k = 0; k < 3; k++) {
-                    const float* a = P[e[k][0]];
-                    const float* b = P[e[k][1]];
-                    w[k] = edge(a[0], a[1], b[0], b[1], xf, yf);
-                }
-                if (w[0] < 0 || w[1] < 0 || w[2] < 0) continue;
-                w[0] = w[0] / area;
-                w[1] = w[1] / area;
-                w[2] = w[2] / area;
-                const float depth = (P[0][2] * w[0] + P[1][2] * w[1]) + P[2][2] * w[2];
-
-                float inputs[kMaxVaryings];
-                int comp = 0;
-                const float pw[3] = {P[0][3], P[1][3], P[2][3]};
-                for (int in = 0; in < info.num_inputs; in++) {
-                    for (int c = 0; c < info.input_size[in]; c++, comp++) {
-                        const float val[3] = {v[0]->var[comp], v[1]->var[comp], v[2]->var[comp]};
-                        switch (info.input_interp[in]) {
-                        case INTERP_PERSPECTIVE: inputs[comp] = interp_persp(pw, val, w); break;
-                        case INTERP_LINEAR: inputs[comp] = interp_linear(val, w); break;
-                        case INTERP_FLAT: inputs[comp] = vs[provoking].var[comp]; break;
-                        }
-                    }
-                }
-                const float mapped = (max_d - min_d) * depth + min_d;
-                fragment(f, p, static_cast<uint32_t>(x), static_cast<uint32_t>(y), mapped, front, inputs);
-            }
-        }
+        if (f.count_prims) f.stats->triangles++;
+        setup_triangle(f, p, as, vs, t, ts);
+        if (!ts.culled) raster_triangle(f, p, info, ts, vs);
     }
 }
 
@@ -872,7 +935,7 @@ void rasterise_points(Frame& f, const cpv_scene_pipeline& p, const Assembled& as
     const float min_d = s->viewport[4], max_d = s->viewport[5];
     for (size_t t = 0; t + 4 <= as.prims.size(); t += 4) {
         const VsOut& v = vs[as.prims[t + 1]];
-        f.stats->triangles++;
+        if (f.count_prims) f.stats->triangles++;
         const float w = v.pos[3];
         const float p0[3] = {v.pos[0] / w, v.pos[1] / w, v.pos[2] / w};
         const int64_t sx = f2i(((p0[0] + 1.0f) * 0.5f) * (vw - 1.0f));
@@ -883,7 +946,7 @@ void rasterise_points(Frame& f, const cpv_scene_pipeline& p, const Assembled& as
         int64_t end_x = std::min<int64_t>(f2i(vw), sx + half + 1), end_y = std::min<int64_t>(f2i(vh), sy + half + 1);
         end_x = std::min<int64_t>(end_x, s->width);
         end_y = std::min<int64_t>(end_y, s->height);
-        for (int64_t y = start_y; y < end_y; y++) {
+        for (int64_t y = first_row(f, start_y); y < end_y; y += f.row_stride) {
             for (int64_t x = start_x; x < end_x; x++) {
                 const float ps = 0.5f + static_cast<float>(static_cast<int32_t>(x - sx)) / size;
                 const float pt = 0.5f + static_cast<float>(static_cast<int32_t>(y - sy)) / size;
@@ -912,7 +975,7 @@ void rasterise_lines(Frame& f, const cpv_scene_pipeline& p, const Assembled& as,
     for (size_t t = 0; t + 4 <= as.prims.size(); t += 4) {
         const uint32_t provoking = as.prims[t];
         const VsOut* v[2] = {&vs[as.prims[t + 1]], &vs[as.prims[t + 2]]};
-        f.stats->triangles++;
+        if (f.count_prims) f.stats->triangles++;
         float P[2][4];
         for (int k = 0; k < 2; k++) {
             const float w = v[k]->pos[3];
@@ -930,7 +993,7 @@ void rasterise_lines(Frame& f, const cpv_scene_pipeline& p, const Assembled& as,
         const float c00[2] = {P[0][0] + ox, P[0][1] + oy}, c01[2] = {P[0][0] - ox, P[0][1] - oy};
         const float c10[2] = {P[1][0] + ox, P[1][1] + oy}, c11[2] = {P[1][0] - ox, P[1][1] - oy};
         const float dx = P[1][0] - P[0][0], dy = P[1][1] - P[0][1];
-        for (uint32_t y = 0; static_cast<float>(y) < vh && y < s->height; y++) {
+        for (uint32_t y = f.row_index; static_cast<float>(y) < vh && y < s->height; y += f.row_stride) {
             const float yf = (static_cast<float>(y) / vh + half_y) * 2.0f - 1.0f;
             for (uint32_t x = 0; static_cast<float>(x) < vw && x < s->width; x++) {
                 const float xf = (static_cast<float>(x) / vw + half_x) * 2.0f - 1.0f;
@@ -1000,26 +1063,107 @@ void draw(Frame& f, const cpv_scene_draw& d) {
     f.res.push = nullptr;
 }
 
-} // namespace
+/* A reusable barrier for the threads of one threaded render. */
+class Barrier {
+public:
+    explicit Barrier(uint32_t n) : n_(n) {}
+    void wait() {
+        std::unique_lock<std::mutex> lock(m_);
+        const uint64_t gen = generation_;
+        if (++waiting_ == n_) {
+            waiting_ = 0;
+            generation_++;
+            cv_.notify_all();
+        } else {
+            cv_.wait(lock, [&] { return generation_ != gen; });
+        }
+    }
 
-extern "C" {
+private:
+    std::mutex m_;
+    std::condition_variable cv_;
+    uint32_t n_, waiting_ = 0;
+    uint64_t generation_ = 0;
+};
 
-int cpv_oracle_render(const cpv_scene* scene, uint8_t* color, uint8_t* depth, uint32_t do_clear, uint32_t draw_begin,
-                      uint32_t draw_end, cpv_oracle_stats* stats) {
+/* What the threads of one threaded render share for the current draw and
+ * instance: its assembly, vertex outputs and triangle set-ups. */
+struct Shared {
+    explicit Shared(uint32_t n) : bar(n) {}
+    Assembled as;
+    std::vector<VsOut> vs;
+    std::vector<TriSetup> tri;
+    std::vector<uint32_t> rows;  /* start_y << 16 | end_y per triangle, 0 if culled */
+    Barrier bar;
+};
+
+/* draw() for thread `tid` of `n`: the assembly is made once, vertex shading
+ * and triangle set-up are split into contiguous ranges, and every thread
+ * then walks all triangles of the instance in order over its own rows. */
+void draw_threaded(Frame& f, const cpv_scene_draw& d, Shared& sh, uint32_t tid, uint32_t n) {
+    const cpv_scene* s = f.s;
+    if (d.pipeline >= s->num_pipelines) return;
+    const cpv_scene_pipeline& p = s->pipelines[d.pipeline];
+    const bool triangles = p.topology != TOPO_POINT_LIST && p.topology != TOPO_LINE_LIST && p.topology != TOPO_LINE_STRIP;
+    const ProgramInfo info = program_info(p.program);
+    float push[32] = {};
+    std::memcpy(push, d.push, std::min<uint32_t>(d.push_size, sizeof(push)));
+    f.res.push = push;
+    for (uint32_t i = 0; i < d.instance_count; i++) {
+        const uint32_t instance = d.first_instance + i;
+        if (tid == 0) {
+            assemble(f, p, d, sh.as);
+            sh.vs.resize(sh.as.vertex_id.size());
+            sh.tri.resize(triangles ? sh.as.prims.size() / 4 : 0);
+            sh.rows.resize(sh.tri.size());
+            f.stats->vs_invocations += sh.as.vertex_id.size();
+        }
+        sh.bar.wait();
+        const size_t nv = sh.as.vertex_id.size();
+        for (size_t k = nv * tid / n; k < nv * (tid + 1) / n; k++) {
+            float attr[8][4];
+            fetch_attributes(f, p, d, sh.as.vertex_id[k], instance, attr);
+            std::memset(&sh.vs[k], 0, sizeof(VsOut));
+            run_vs(p.program, attr, f.res, sh.vs[k]);
+        }
+        sh.bar.wait();
+        if (triangles) {
+            const size_t nt = sh.tri.size();
+            for (size_t j = nt * tid / n; j < nt * (tid + 1) / n; j++) {
+                TriSetup& ts = sh.tri[j];
+                setup_triangle(f, p, sh.as, sh.vs, j * 4, ts);
+                f.stats->triangles++;
+                sh.rows[j] = (ts.culled || ts.end_y <= ts.start_y) ? 0u : (static_cast<uint32_t>(ts.start_y) << 16 | static_cast<uint32_t>(ts.end_y));
+            }
+            sh.bar.wait();
+            for (size_t j = 0; j < nt; j++) {
+                const uint32_t r = sh.rows[j];
+                if (!r || first_row(f, r >> 16) >= static_cast<int64_t>(r & 0xFFFFu)) continue;
+                raster_triangle(f, p, info, sh.tri[j], sh.vs);
+            }
+        } else {
+            f.count_prims = tid == 0;
+            if (p.topology == TOPO_POINT_LIST) rasterise_points(f, p, sh.as, sh.vs);
+            else rasterise_lines(f, p, sh.as, sh.vs);
+            f.count_prims = true;
+        }
+        sh.bar.wait();  /* before thread 0 assembles the next instance */
+    }
+    f.res.push = nullptr;
+}
+
+/* Checks a scene and fills the parts of `f` and `tex` every render needs. */
+int prepare(const cpv_scene* scene, uint8_t* color, uint8_t* depth, Frame& f, Texture& tex) {
     if (!scene || !color) return -1;
     if (scene->color_format != FMT_R8G8B8A8_UNORM && scene->color_format != FMT_B8G8R8A8_UNORM && scene->color_format != 0) return -2;
     if (scene->color_format == 0 && scene->depth_format == 0) return -2;
     const uint32_t dsize = depth_texel_size(scene->depth_format);
     if (scene->depth_format != 0 && (dsize == 0 || !depth)) return -3;
-    cpv_oracle_stats local{};
-    Frame f{};
+    if (scene->height > 0xFFFFu) return -2;
     f.s = scene;
     f.colour = color;
     f.depth = scene->depth_format ? depth : nullptr;
     f.depth_size = dsize;
-    f.stats = stats ? stats : &local;
-
-    Texture tex;
     if (scene->texture_data) {
         tex.data = scene->texture_data;
         tex.bytes = scene->texture_bytes;
@@ -1042,28 +1186,144 @@ int cpv_oracle_render(const cpv_scene* scene, uint8_t* color, uint8_t* depth, ui
     }
     f.res.ubo = reinterpret_cast<const float*>(scene->uniform_data);
     f.res.ubo_floats = scene->uniform_bytes / 4;
+    return 0;
+}
 
+/* BeginRenderPassCommand + ClearImage (CPVulkan/CommandBuffer.cpp:591-646,
+ * CPVulkan/CommandBuffer.Draw.cpp:117-149): every texel goes through the
+ * format encoder. */
+void clear(const Frame& f) {
+    const cpv_scene* scene = f.s;
     const uint64_t pixels = static_cast<uint64_t>(scene->width) * scene->height;
-    if (do_clear) {
-        /* BeginRenderPassCommand + ClearImage (CPVulkan/CommandBuffer.cpp:591-646,
-         * CPVulkan/CommandBuffer.Draw.cpp:117-149): every texel goes through the
-         * format encoder. */
-        if (scene->color_format)  // a depth-only pass leaves `color` untouched
-            for (uint64_t i = 0; i < pixels; i++) set_colour(color + i * 4, scene->color_format, scene->clear_color);
-        if (f.depth) {
-            for (uint64_t i = 0; i < pixels; i++) {
-                uint8_t* t = f.depth + i * dsize;
-                set_depth(t, scene->depth_format, scene->clear_depth);
-                if (has_stencil(scene->depth_format)) { t[4] = static_cast<uint8_t>(scene->clear_stencil); t[5] = t[6] = t[7] = 0; }
-            }
+    if (scene->color_format)  // a depth-only pass leaves `color` untouched
+        for (uint64_t i = 0; i < pixels; i++) set_colour(f.colour + i * 4, scene->color_format, scene->clear_color);
+    if (f.depth) {
+        for (uint64_t i = 0; i < pixels; i++) {
+            uint8_t* t = f.depth + i * f.depth_size;
+            set_depth(t, scene->depth_format, scene->clear_depth);
+            if (has_stencil(scene->depth_format)) { t[4] = static_cast<uint8_t>(scene->clear_stencil); t[5] = t[6] = t[7] = 0; }
         }
     }
+}
+
+} // namespace
+
+extern "C" {
+
+int cpv_oracle_render(const cpv_scene* scene, uint8_t* color, uint8_t* depth, uint32_t do_clear, uint32_t draw_begin,
+                      uint32_t draw_end, cpv_oracle_stats* stats) {
+    cpv_oracle_stats local{};
+    Frame f{};
+    Texture tex;
+    const int r = prepare(scene, color, depth, f, tex);
+    if (r != 0) return r;
+    f.stats = stats ? stats : &local;
+    if (do_clear) clear(f);
     const uint32_t end = std::min(draw_end, scene->num_draws);
     for (uint32_t i = draw_begin; i < end; i++) draw(f, scene->draws[i]);
     return 0;
 }
 
+int cpv_oracle_render_threaded(const cpv_scene* scene, uint8_t* color, uint8_t* depth, uint32_t do_clear, uint32_t draw_begin,
+                               uint32_t draw_end, uint32_t threads, cpv_oracle_stats* stats) {
+    Frame base{};
+    Texture tex;
+    const int r = prepare(scene, color, depth, base, tex);
+    if (r != 0) return r;
+    cpv_oracle_stats dummy{};
+    base.stats = &dummy;
+    if (do_clear) clear(base);
+    const uint32_t n = std::max(1u, std::min(threads, 256u));
+    const uint32_t end = std::min(draw_end, scene->num_draws);
+    Shared sh(n);
+    std::vector<cpv_oracle_stats> per(n);
+    std::vector<std::thread> pool;
+    for (uint32_t t = 0; t < n; t++) {
+        pool.emplace_back([&, t] {
+            Frame f = base;
+            if (f.res.texture) f.res.texture = &tex;
+            f.stats = &per[t];
+            f.row_stride = n;
+            f.row_index = t;
+            for (uint32_t i = draw_begin; i < end; i++) draw_threaded(f, scene->draws[i], sh, t, n);
+        });
+    }
+    for (std::thread& th : pool) th.join();
+    if (stats) {
+        *stats = cpv_oracle_stats{};
+        for (const cpv_oracle_stats& st : per) {
+            stats->triangles += st.triangles;
+            stats->vs_invocations += st.vs_invocations;
+            stats->fragments += st.fragments;
+            stats->fragments_written += st.fragments_written;
+        }
+    }
+    return 0;
+}
+
 float cpv_oracle_edge(float ax, float ay, float bx, float by, float cx, float cy) { return edge(ax, ay, bx, by, cx, cy); }
+
+void cpv_oracle_edge_n(const float* in, float* out, uint64_t n) {
+    for (uint64_t i = 0; i < n; i++) {
+        const float* p = in + 6 * i;
+        out[i] = edge(p[0], p[1], p[2], p[3], p[4], p[5]);
+    }
+}
+
+void cpv_oracle_wrap_n(const int32_t* v, const int32_t* size, const uint32_t* mode, int32_t* out, uint64_t n) {
+    for (uint64_t i = 0; i < n; i++) out[i] = wrap(v[i], size[i], mode[i]);
+}
+
+void cpv_oracle_blend_n(const float* src, const float* dst, const float* constant, const uint32_t* modes, float* out, uint64_t n) {
+    for (uint64_t i = 0; i < n; i++) {
+        const uint32_t* m = modes + 6 * i;
+        blend(src + 4 * i, dst + 4 * i, constant + 4 * i, m[0], m[1], m[2], m[3], m[4], m[5], out + 4 * i);
+    }
+}
+
+void cpv_oracle_fragment_input_n(const float* pts, const float* vars, const uint32_t* cull, const uint32_t* provoking, float* out, uint64_t n) {
+    const ProgramInfo info{3, {4, 4, 1}, {INTERP_PERSPECTIVE, INTERP_LINEAR, INTERP_FLAT}};
+    std::vector<VsOut> vs(3);
+    for (uint64_t i = 0; i < n; i++) {
+        const float* p = pts + 14 * i;
+        TriSetup ts{};
+        for (int k = 0; k < 3; k++) {
+            for (int c = 0; c < 4; c++) ts.P[k][c] = p[4 * k + c];
+            ts.v[k] = static_cast<uint32_t>(k);
+            std::memset(&vs[k], 0, sizeof(VsOut));
+            for (int c = 0; c < 9; c++) vs[k].var[c] = vars[27 * i + 9 * k + c];
+        }
+        ts.provoking = provoking[i];
+        setup_facing(ts, cull[i]);
+        float w[3], depth = 0.0f, inputs[kMaxVaryings] = {};
+        const bool covered = !ts.culled && fragment_weights(ts, p[12], p[13], w, depth);
+        if (covered) fragment_inputs(info, ts, vs, w, inputs);
+        float* o = out + 12 * i;
+        o[0] = covered ? 1.0f : 0.0f;
+        o[1] = ts.front ? 1.0f : 0.0f;
+        o[2] = covered ? depth : 0.0f;
+        for (int k = 0; k < 9; k++) o[3 + k] = covered ? inputs[k] : 0.0f;
+    }
+}
+
+void cpv_oracle_sample_n(const uint8_t* texels, uint32_t width, uint32_t height, uint32_t levels, const uint32_t* modes, const float* uvl, float* out,
+                         uint64_t n) {
+    for (uint64_t i = 0; i < n; i++) {
+        const uint32_t* m = modes + 6 * i;
+        cpv_scene_sampler s{};
+        s.mag_filter = m[0];
+        s.min_filter = m[1];
+        s.mipmap_mode = m[2];
+        s.address_u = m[3];
+        s.address_v = m[4];
+        s.address_w = m[3];
+        s.border_color = m[5];
+        s.mip_lod_bias = 0.0f;
+        s.min_lod = -1000.0f;
+        s.max_lod = 1000.0f;
+        cpv_oracle_sample(texels, width, height, levels, &s, uvl[3 * i], uvl[3 * i + 1], uvl[3 * i + 2], out + 4 * i);
+    }
+}
 uint8_t cpv_oracle_encode_unorm8(float value) { return static_cast<uint8_t>(encode_unorm(value, 255.0f)); }
 uint8_t cpv_oracle_logic_op(uint32_t op, uint8_t src, uint8_t dst) { return logic_op(op, src, dst); }
 uint16_t cpv_oracle_encode_unorm16(float value) { return static_cast<uint16_t>(encode_unorm(value, 65535.0f)); }

@@ -45,6 +45,16 @@ typedef struct cpv_oracle_stats {
 int cpv_oracle_render(const cpv_scene* scene, uint8_t* color, uint8_t* depth, uint32_t do_clear,
                       uint32_t draw_begin, uint32_t draw_end, cpv_oracle_stats* stats);
 
+/* The same render on `threads` host threads (the reference renders on one;
+ * this is the oracle's own parallel form, for full-size checks): the
+ * assembly of each draw instance is made once, vertex shading and triangle
+ * set-up are split among the threads, and thread t writes the rows y with
+ * y % threads == t, walking every triangle of every draw in API order, so
+ * each pixel receives its fragments in the order of cpv_oracle_render and
+ * the image is identical to it. */
+int cpv_oracle_render_threaded(const cpv_scene* scene, uint8_t* color, uint8_t* depth, uint32_t do_clear,
+                               uint32_t draw_begin, uint32_t draw_end, uint32_t threads, cpv_oracle_stats* stats);
+
 /* Single-step helpers exposed for known-answer tests. */
 float cpv_oracle_edge(float ax, float ay, float bx, float by, float cx, float cy);
 uint8_t cpv_oracle_encode_unorm8(float value);
@@ -61,6 +71,22 @@ void cpv_oracle_sample(const uint8_t* texels, uint32_t width, uint32_t height, u
  * 1 LINEAR; dst is updated in place. */
 void cpv_oracle_blit(const uint8_t* src, uint32_t src_w, uint32_t src_h, uint32_t src_format, uint8_t* dst, uint32_t dst_w, uint32_t dst_h,
                      uint32_t dst_format, const int32_t region[8], uint32_t filter);
+/* Batch forms for the comparison with the reference's own functions
+ * (oracle/refpin, tests/test_oracle_pinned.py); layouts as cpv_ref_*_n:
+ * edge: 6 floats in, 1 out per case; wrap: value, size, address mode;
+ * blend: 4 + 4 + 4 floats and 6 modes (src/dst colour factor, colour op,
+ * src/dst alpha factor, alpha op) per case; fragment input: p0, p1, p2
+ * (NDC x, y, z, clip w) and the pixel centre (14 floats), 27 vertex floats
+ * (perspective vec4, linear vec4, flat float per vertex), cull mode and
+ * provoking vertex in, covered, front, depth and 9 components out;
+ * sample: 6 modes (mag, min, mipmap, address u, address v, border) and
+ * u, v, λ in (no bias, no λ clamp), 4 floats out. */
+void cpv_oracle_edge_n(const float* in, float* out, uint64_t n);
+void cpv_oracle_wrap_n(const int32_t* v, const int32_t* size, const uint32_t* mode, int32_t* out, uint64_t n);
+void cpv_oracle_blend_n(const float* src, const float* dst, const float* constant, const uint32_t* modes, float* out, uint64_t n);
+void cpv_oracle_fragment_input_n(const float* pts, const float* vars, const uint32_t* cull, const uint32_t* provoking, float* out, uint64_t n);
+void cpv_oracle_sample_n(const uint8_t* texels, uint32_t width, uint32_t height, uint32_t levels, const uint32_t* modes, const float* uvl,
+                         float* out, uint64_t n);
 /* Blend one colour against a destination with the reference blend equations. */
 void cpv_oracle_blend(const float src[4], const float dst[4], const float constant[4],
                       uint32_t src_color, uint32_t dst_color, uint32_t color_op,

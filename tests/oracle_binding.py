@@ -28,6 +28,8 @@ class Oracle:
         f, u32, vp = ctypes.c_float, ctypes.c_uint32, ctypes.c_void_p
         lib.cpv_oracle_render.restype = ctypes.c_int
         lib.cpv_oracle_render.argtypes = [vp, vp, vp, u32, u32, u32, ctypes.POINTER(Stats)]
+        lib.cpv_oracle_render_threaded.restype = ctypes.c_int
+        lib.cpv_oracle_render_threaded.argtypes = [vp, vp, vp, u32, u32, u32, u32, ctypes.POINTER(Stats)]
         lib.cpv_oracle_edge.restype = f
         lib.cpv_oracle_edge.argtypes = [f] * 6
         lib.cpv_oracle_encode_unorm8.restype = ctypes.c_uint8
@@ -65,6 +67,25 @@ class Oracle:
         if r != 0:
             raise RuntimeError("oracle rejected the scene (%d)" % r)
         return color, (depth if dsz else None), {k: getattr(st, k) for k, _ in Stats._fields_}
+
+
+    def render_threaded(self, scene, threads=None, draw_begin=0, draw_end=None):
+        """render() on `threads` host threads (default: every usable core);
+        the image is identical to render()'s."""
+        from cpvulkan_gb300 import depth_texel_bytes
+        if threads is None:
+            threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+        h, w = scene.height, scene.width
+        dsz = depth_texel_bytes(scene.depth_format)
+        color = np.zeros((h, w, 4), np.uint8)
+        depth = np.zeros((h, w, dsz), np.uint8) if dsz else None
+        st = Stats()
+        end = 0xFFFFFFFF if draw_end is None else draw_end
+        r = self.lib.cpv_oracle_render_threaded(scene.ptr, color.ctypes.data, depth.ctypes.data if dsz else None, 1, draw_begin, end,
+                                                threads, ctypes.byref(st))
+        if r != 0:
+            raise RuntimeError("oracle rejected the scene (%d)" % r)
+        return color, depth, {k: getattr(st, k) for k, _ in Stats._fields_}
 
 
 def build():
