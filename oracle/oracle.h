@@ -12,12 +12,16 @@
  * in include/cpv/scene.h. Shader programs are hand-written C++ restatements of
  * the SPIR-V modules the harness ships (one per cpv_program).
  *
- * Parity status: the reference itself cannot be built in this image (it needs
- * LLVM-C 8, the Khronos Vulkan headers, Microsoft GSL and glm >= 0.9.9, none
- * of which are present) and ships no tests, golden images or fixtures. This
- * restatement is therefore pinned only by hand-derived known-answer tests
- * (tests/golden/) built from the cited reference lines: "parity unpinned"
- * against a reference binary.
+ * Parity status: the reference as a whole cannot be built in this image (it
+ * needs LLVM-C 8, the Khronos Vulkan headers, Microsoft GSL and glm >= 0.9.9,
+ * none of which are present) and ships no tests, golden images or fixtures.
+ * Its plain C++ parts of the path (edge function, fragment inputs, blend,
+ * wrap / lerp / image sampling) are compiled from the reference's own files
+ * by oracle/refpin and this restatement matches them bit for bit
+ * (tests/test_oracle_pinned.py). The parts the reference generates as LLVM
+ * IR at run time (pixel codecs, per-fragment operations, vertex fetch) and
+ * glm's operand order in shaders are "parity unpinned": they are checked
+ * against hand-derived known-answer tests (tests/golden/) only.
  */
 #ifndef CPV_ORACLE_H
 #define CPV_ORACLE_H
