@@ -904,7 +904,11 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
         }
     }
     f.vkEndCommandBuffer(r->copy_cmd);
-    if (submit_and_wait(r, r->copy_cmd) != VK_SUCCESS) return fail("upload submit");
+    // CPVH_RECORD_ONLY=1: record the frame without uploading (on a device
+    // that compiles but cannot execute, recording still compiles the
+    // batched modules at vkEndCommandBuffer)
+    const char* record_only = std::getenv("CPVH_RECORD_ONLY");
+    if (!(record_only && record_only[0] == '1') && submit_and_wait(r, r->copy_cmd) != VK_SUCCESS) return fail("upload submit");
     record_all(r);
     return r;
 }

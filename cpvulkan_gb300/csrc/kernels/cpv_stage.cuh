@@ -209,38 +209,25 @@ __device__ __forceinline__ void cpv_setup(const CpvDrawParams& P, uint64_t g, Cp
     t.wf = make_float4(Pn[0][3], Pn[1][3], 0.0f, __uint_as_float((live ? 1u : 0u) | 2u | (3u << 6)));
 }
 #else
-/* Primitive set-up: vertex shading of the three vertices, perspective divide,
- * screen bounding box, area, facing and cull. `g` is the primitive index
- * within the draw (all instances). */
+/* The per-vertex part of the set-up: the vertex shader and the perspective
+ * divide of its position (CPVulkan/CommandBuffer.Draw.cpp:1541-1546), NDC
+ * x, y, z and clip w. `var` receives the shader's outputs. */
+__device__ __forceinline__ void cpv_vertex_ndc(const CpvDrawParams& P, uint32_t vertex_id, uint32_t instance, float Pn[4], float var[CPV_NV_ALLOC]) {
+    float pos[4];
+    cpv_vs_run(P, vertex_id, instance, pos, var);
+    const float w = pos[3];
+    Pn[0] = __fdiv_rn(pos[0], w);
+    Pn[1] = __fdiv_rn(pos[1], w);
+    Pn[2] = __fdiv_rn(pos[2], w);
+    Pn[3] = w;
+}
+
+/* The per-triangle part of the set-up from its three vertices (after the CW
+ * swap): screen bounding box, area, facing and cull, and with varyings the
+ * constant fragment colour. t.var must hold the vertices' outputs when
+ * WITH_VARYINGS. */
 template <bool WITH_VARYINGS>
-__device__ __forceinline__ void cpv_setup(const CpvDrawParams& P, uint64_t g, CpvTri& t) {
-    const uint32_t ppi = P.prims_per_instance;
-    const uint32_t g32 = static_cast<uint32_t>(g);  /* draws hold < 2^32 primitives */
-    const uint32_t inst = P.instance_count > 1u ? g32 / ppi : 0u;
-    const uint32_t instance = P.first_instance + inst;
-    const uint32_t p = g32 - inst * ppi;
-    uint32_t raw[3], provoking;
-    cpv_prim_vertices(CPV_TOPOLOGY, p, raw, provoking);
-#if CPV_FRONT_CW
-    { const uint32_t tmp = raw[0]; raw[0] = raw[2]; raw[2] = tmp; }
-#endif
-    const uint32_t pslot = raw[0] == provoking ? 0u : (raw[1] == provoking ? 1u : 2u);
-    float Pn[3][4];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        float pos[4];
-        float var[CPV_NV_ALLOC];
-        cpv_vs_run(P, cpv_vertex_id(P, raw[k]), instance, pos, var);
-        const float w = pos[3];
-        Pn[k][0] = __fdiv_rn(pos[0], w);
-        Pn[k][1] = __fdiv_rn(pos[1], w);
-        Pn[k][2] = __fdiv_rn(pos[2], w);
-        Pn[k][3] = w;
-        if (WITH_VARYINGS) {
-#pragma unroll
-            for (int c = 0; c < CPV_NV; c++) t.var[k][c] = var[c];
-        }
-    }
+__device__ __forceinline__ void cpv_setup_tri(const CpvDrawParams& P, const float Pn[3][4], uint32_t pslot, uint32_t g32, CpvTri& t) {
     const float vw = P.viewport[2], vh = P.viewport[3];
     int32_t sx[3], sy[3];
 #pragma unroll
@@ -292,6 +279,44 @@ __device__ __forceinline__ void cpv_setup(const CpvDrawParams& P, uint64_t g, Cp
     const uint32_t flags = (live ? 1u : 0u) | (front ? 2u : 0u) | (pslot << 6);
     t.wf = make_float4(Pn[0][3], Pn[1][3], Pn[2][3], __uint_as_float(flags));
 }
+
+/* A triangle's instance and its three raw assembled vertices after the CW
+ * swap (CPVulkan/CommandBuffer.Draw.cpp:567-760, 1532-1535), and the slot of
+ * the provoking vertex among them. */
+__device__ __forceinline__ void cpv_tri_vertices(const CpvDrawParams& P, uint32_t g32, uint32_t raw[3], uint32_t& instance, uint32_t& pslot) {
+    const uint32_t ppi = P.prims_per_instance;
+    const uint32_t inst = P.instance_count > 1u ? g32 / ppi : 0u;
+    instance = P.first_instance + inst;
+    const uint32_t p = g32 - inst * ppi;
+    uint32_t provoking;
+    cpv_prim_vertices(CPV_TOPOLOGY, p, raw, provoking);
+#if CPV_FRONT_CW
+    { const uint32_t tmp = raw[0]; raw[0] = raw[2]; raw[2] = tmp; }
+#endif
+    pslot = raw[0] == provoking ? 0u : (raw[1] == provoking ? 1u : 2u);
+}
+
+/* Primitive set-up: vertex shading of the three vertices, perspective divide,
+ * screen bounding box, area, facing and cull. `g` is the primitive index
+ * within the draw (all instances). */
+template <bool WITH_VARYINGS>
+__device__ __forceinline__ void cpv_setup(const CpvDrawParams& P, uint64_t g, CpvTri& t) {
+    const uint32_t g32 = static_cast<uint32_t>(g);  /* draws hold < 2^32 primitives */
+    uint32_t raw[3], instance, pslot;
+    cpv_tri_vertices(P, g32, raw, instance, pslot);
+    float Pn[3][4];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float var[CPV_NV_ALLOC];
+        cpv_vertex_ndc(P, cpv_vertex_id(P, raw[k]), instance, Pn[k], var);
+        if (WITH_VARYINGS) {
+#pragma unroll
+            for (int c = 0; c < CPV_NV; c++) t.var[k][c] = var[c];
+        }
+    }
+    cpv_setup_tri<WITH_VARYINGS>(P, Pn, pslot, g32, t);
+}
+
 #endif /* CPV_PRIM_KIND */
 
 /* Byte offset of channel i in the colour attachment texel

@@ -131,3 +131,36 @@ def test_pipeline_takes_its_subpass_formats(compile_ctx, monkeypatch, subpasses,
     text = _module_source(compile_ctx, c.PROGRAM_CUBE, 0x18 | 0x100)
     assert "#define CPV_COLOR_FORMAT %s\n" % colour in text
     assert "#define CPV_DEPTH_FORMAT 130\n" in text
+
+
+@pytest.mark.parametrize("config,params", [
+    (c.BATCH, [24, 2000, 320, 200]),
+    (c.PROGRAM, [c.PROGRAM_POINTS, 0x10000 | 0x20, 32, 32, 4]),
+    (c.PROGRAM, [c.PROGRAM_CUBE, 0x10000 | 0x400 | 0x20000, 32, 32, 4]),
+    (c.PROGRAM, [c.PROGRAM_TEXLIT, 0x10, 32, 32, 4]),
+])
+def test_batched_module_compiles(native, monkeypatch, tmp_path, config, params):
+    """Recording a render pass that runs batched compiles its batched module
+    (every pipeline of the pass in one NVRTC module) at vkEndCommandBuffer;
+    on the compile-only device that must succeed for triangle, point and
+    line pipelines. Each compiled module leaves a cubin in the disk cache."""
+    dump, cache = tmp_path / "dump", tmp_path / "cache"
+    dump.mkdir()
+    cache.mkdir()
+    monkeypatch.setenv("CPV_COMPILE_ONLY", "1")
+    monkeypatch.setenv("CPV_DUMP_DIR", str(dump))
+    monkeypatch.setenv("CPV_CACHE_DIR", str(cache))
+    monkeypatch.setenv("CPVH_RECORD_ONLY", "1")
+    monkeypatch.setenv("CPV_BATCH_MIN_DRAWS", "1")
+    monkeypatch.setenv("CPV_AUTOTUNE", "0")
+    ctx = c.Context()
+    try:
+        r = c.Renderer(ctx, c.Scene(config, 1, params))
+        r.close()
+    finally:
+        ctx.close()
+    batch = glob.glob(str(dump / "batch_*.cu"))
+    assert batch, "no batched module was composed"
+    assert "#include \"cpv_batch.cuh\"" in open(batch[0]).read()
+    sources = glob.glob(str(dump / "*.cu"))
+    assert len(glob.glob(str(cache / "*.cubin"))) >= len(sources), c.icd_last_error()
