@@ -60,20 +60,15 @@ def workload(args):
 
 
 def algorithmic_bytes(name, scene, frag_written):
-    """Bytes the frame must move at least once (inputs read, attachments written/read)."""
-    w, h = scene.width, scene.height
-    px = w * h
-    if name == "heightfield":
-        verts, idx = 1024 * 1024 * 32, 1023 * 1023 * 6 * 4
-        tex = sum((1024 >> l) ** 2 * 4 for l in range(11))
-        return verts + idx + tex + px * 4 + 2 * px * 4  # colour store + depth read/write
-    if name == "blend":
-        return 8 * frag_written + 800000 * 24 + 1200000 * 4  # RGBA8 read+write per blended fragment + vertices + indices
-    if name == "cube":
-        return 36 * 32 + px * 4 + px * 2 * 2
-    # many-draw frames: every mesh and index byte read once, colour stored,
-    # depth read and written
-    return scene.input_bytes + px * 4 + px * 4 * 2
+    """Bytes the frame must move at least once: every vertex, index, uniform
+    and texture byte read once, plus the attachments — colour stored and
+    depth read and written per pixel, or for the blend workloads an RGBA8
+    read and write per blended fragment (the immediate-mode blend traffic)."""
+    px = scene.width * scene.height
+    if name.startswith("blend"):
+        return 8 * frag_written + scene.input_bytes
+    depth = 2 if name == "cube" else 4  # D16 / D32
+    return scene.input_bytes + px * 4 + px * depth * 2
 
 
 def measured_peak():
@@ -101,15 +96,17 @@ class ClockSampler:
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self):
+    def __init__(self, interval_ms=100):
         self.proc = None
         self.path = None
+        self.interval_ms = interval_ms
 
     def start(self):
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
-            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits", "-lms", "200"],
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits", "-lms",
+                                          str(self.interval_ms)],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -189,6 +186,39 @@ def cpu_baseline(scene, seconds, threads=1):
     return state["tris"], dt, desc
 
 
+def reference_frame(scene):
+    """The CPU-baseline leg's whole frame: the oracle (the reference's CPU
+    draw path restated) renders the full image on every host core, which
+    also gives the frame's fragment counts and the image the GPU's is
+    compared with. Returns (colour, depth, stats, seconds, threads)."""
+    from tests import oracle_binding
+    oracle = oracle_binding.load()
+    threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    t0 = time.time()
+    color, depth, st = oracle.render_threaded(scene, threads)
+    return color, depth, st, time.time() - t0, threads
+
+
+def image_diff(gpu_color, gpu_depth, ref_color, ref_depth):
+    """Differing pixels of two renders (colour: any channel; depth: any
+    byte of the texel), and the largest colour difference in LSB."""
+    import numpy as np
+    d = np.abs(gpu_color.astype(np.int16) - ref_color.astype(np.int16))
+    out = {"color_pixels_differing": int(np.count_nonzero(d.max(axis=2))), "color_max_lsb": int(d.max()) if d.size else 0}
+    if ref_depth is not None and gpu_depth is not None:
+        out["depth_pixels_differing"] = int(np.count_nonzero(np.any(gpu_depth != ref_depth, axis=-1)))
+    return out
+
+
+def limiter(workload):
+    """Compute-side utilisation of the workload's raster from the committed ncu capture, else None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "limiters.json")) as fh:
+            return json.load(fh).get(workload)
+    except Exception:
+        return None
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -222,28 +252,56 @@ def barrier(dist):
 
 
 def run_reference(args, world, rank, dist):
+    """The reference arm: the reference's CPU draw path (the oracle, its
+    line-cited restatement: the reference itself cannot be built here) on
+    every host core, rendering the workload's own frame — its draws in API
+    order into the frame's attachments — a chunk of draws per step of about
+    --ref-seconds, continuing where the previous step stopped (a one-draw
+    frame is rendered whole every step)."""
     import cpvulkan_gb300 as c
     c.build()
     if rank != 0:
         return
+    from tests import oracle_binding
+    oracle = oracle_binding.load()
     cfg, params, cfg_desc = workload(args)
     scene = c.Scene(cfg, 1, params)
-    threads = os.cpu_count() or 1
+    threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    color = depth = None
+    cursor, chunk = 0, 8
     per_step = []
     for i in range(args.warmup + args.steps):
-        tris, dt, desc = cpu_baseline(scene, args.ref_seconds, threads)
+        t0 = time.time()
+        tris = draws = 0
+        while True:
+            if scene.draws <= 1 or cursor >= scene.draws:
+                cursor = 0
+            end = scene.draws if scene.draws <= 1 else min(scene.draws, cursor + chunk)
+            c0 = time.time()
+            color, depth, st = oracle.render_threaded(scene, threads, cursor, end, color=color, depth=depth, clear=cursor == 0)
+            dt_chunk = time.time() - c0
+            tris += st["triangles"]
+            draws += end - cursor
+            cursor = end
+            if scene.draws > 1 and dt_chunk < 0.5:
+                chunk = min(chunk * 2, 512)
+            if time.time() - t0 >= args.ref_seconds or scene.draws <= 1:
+                break
         if i >= args.warmup:
-            per_step.append((tris, dt))
-    tris = sum(f for f, _ in per_step)
-    dt = sum(t for _, t in per_step)
+            per_step.append((tris, time.time() - t0, draws))
+    tris = sum(f for f, _, _ in per_step)
+    dt = sum(t for _, t, _ in per_step)
+    draws = sum(d for _, _, d in per_step)
     value = tris / dt / 1e6
+    sample = ("whole frame (%d triangles) per step" % scene.triangles if scene.draws <= 1 else
+              "the frame's draws in API order into its attachments, continuing across steps: %d draws (%d triangles) in %d timed steps "
+              "of about %.0f s" % (draws, tris, len(per_step), args.ref_seconds))
     line = {
         "impl": "reference", "metric": "Mtri/s", "value": round(value, 3), "unit": "Mtri/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(1000 * dt / len(per_step), 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene)",
         "config": {"workload": args.config, "description": cfg_desc, "triangles": scene.triangles},
-        "cpu_baseline": {"value": round(value, 3), "unit": "Mtri/s", "cores": threads, "kind": "port",
-                         "sample": "per step about %.0f s of oracle work; last step: %s" % (args.ref_seconds, desc)},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mtri/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 3), "unit": "Mtri/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -251,6 +309,137 @@ def run_reference(args, world, rank, dist):
 
 PLAIN_KERNELS = ("cpv_raster", "cpv_setup_rects", "cpv_span_count", "cpv_scan", "cpv_span_write", "cpv_blend_tables")
 BATCH_KERNELS = ("cpv_batch", "cpv_batch_setup", "cpv_batch_bin", "cpv_batch_raster")
+
+# Workloads measured beside the headline frame in the default run:
+# (name, harness config, scene parameters, environment, description).
+SIDE_WORKLOADS = [
+    ("cube", 1, [30], {}, CONFIGS["cube"][2]),
+    ("heightfield", 2, [], {}, CONFIGS["heightfield"][2]),
+    ("blend", 3, [], {}, CONFIGS["blend"][2] + "; flat colour: per-primitive blend tables"),
+    ("blend_general", 3, [], {"CPV_BLEND_TABLES": "0"}, CONFIGS["blend"][2] + "; blend computed per fragment (no tables)"),
+    ("blend_interpolated", 3, [200000, 1920, 1080, 1], {}, CONFIGS["blend"][2] + "; a colour per corner, interpolated per fragment"),
+]
+
+
+def timed_frames(h, r, frames):
+    """Device milliseconds of `frames` frames (queue events around each
+    submission; a 256 MiB fill before each evicts the L2, untimed)."""
+    import ctypes
+    arr = (ctypes.c_double * frames)()
+    res = h.cpvh_render_timed(r.ptr, frames, FLUSH_BYTES, arr)
+    if res != 0:
+        raise RuntimeError("render failed: %d" % res)
+    return list(arr)
+
+
+def kernel_profile(h, icd, r, names, frames):
+    """Per-kernel device time of `frames` eager frames (CUDA events around each kernel)."""
+    import ctypes
+    icd.cpv_profile_reset()
+    icd.cpv_profile_enable(1)
+    timed_frames(h, r, frames)
+    icd.cpv_profile_enable(0)
+    out = {}
+    for k in names:
+        n, ms = ctypes.c_uint64(0), ctypes.c_double(0.0)
+        icd.cpv_profile_get(k.encode(), ctypes.byref(n), ctypes.byref(ms))
+        if n.value:
+            out[k] = {"launches": n.value, "ms_per_launch": round(ms.value / n.value, 4), "ms_per_frame": round(ms.value / frames, 4)}
+    return out
+
+
+def roofline_of(name, scene, kernels, frag_written):
+    """HBM roofline of the frame's dominant raster kernel: algorithmic bytes
+    per launch over its CUDA-event time, against the measured copy
+    bandwidth; with the compute-side utilisation of the committed capture."""
+    dom = "cpv_batch_raster" if "cpv_batch_raster" in kernels else "cpv_raster"
+    peak, peak_kind = measured_peak()
+    alg = algorithmic_bytes(name, scene, frag_written)
+    achieved = alg / (kernels[dom]["ms_per_launch"] / 1000.0) / 1e9 if dom in kernels else None
+    base = name.split("_")[0]
+    return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None, "peak": peak, "peak_kind": peak_kind,
+            "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None, "traffic": committed_traffic(dom, base),
+            "algorithmic_bytes_per_launch": alg, "compute_side": limiter(base) if base != "cube" else
+            {"limiter": "launch and submission latency (one 12-triangle draw)"}}
+
+
+def measure_workload(ctx, h, icd, name, cfg, params, env, desc, min_seconds=1.2):
+    """One side workload at its full size: device-timed frames (at least
+    `min_seconds` of them, clocks sampled meanwhile), per-kernel times, the
+    roofline, and the image against the oracle's whole frame."""
+    import math
+    import cpvulkan_gb300 as c
+    saved = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
+    try:
+        scene = c.Scene(cfg, 1, params)
+        r = c.Renderer(ctx, scene)
+        try:
+            timed_frames(h, r, 3)
+            probe = sum(timed_frames(h, r, 3)) / 3.0
+            frames = int(min(20000, max(10, math.ceil(min_seconds * 1000.0 / (probe + 0.1)))))
+            clocks = ClockSampler(100)
+            clocks.start()
+            l0 = icd.cpv_kernel_launches()
+            ms = timed_frames(h, r, frames)
+            launches = icd.cpv_kernel_launches() - l0
+            clock_info = clocks.stop()
+            kernels = kernel_profile(h, icd, r, BATCH_KERNELS + PLAIN_KERNELS, 3)
+            color, depth = r.readback()
+        finally:
+            r.close()
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    ref_color, ref_depth, st, ref_s, threads = reference_frame(scene)
+    mpf = sum(ms) / frames
+    tris = scene.triangles
+    return {
+        "description": desc, "triangles": tris, "draws": scene.draws, "frames": frames,
+        "ms_per_frame": round(mpf, 5), "mtri_s": round(tris / (mpf / 1000.0) / 1e6, 3),
+        "gfrag_s": round(st["fragments"] / (mpf / 1000.0) / 1e9, 4), "frames_s": round(1000.0 / mpf, 2),
+        "fragments": st["fragments"], "fragments_written": st["fragments_written"],
+        "mode": "batched" if "cpv_batch_raster" in kernels else "plain", "gpu_launches_per_frame": round(launches / frames, 2),
+        "kernels": kernels, "roofline": roofline_of(name, scene, kernels, st["fragments_written"]), "clocks": clock_info,
+        "parity": dict(image_diff(color, depth, ref_color, ref_depth), against="oracle whole frame"),
+        "cpu_baseline": {"full_frame": {"seconds": round(ref_s, 3), "threads": threads, "kind": "port",
+                                        "mtri_s": round(tris / ref_s / 1e6, 4)}},
+        "env": env or None,
+    }
+
+
+def serve_sweep(ctx, seconds, seed=5, fractions=(0.25, 0.5, 0.8)):
+    """The serving workload at its configured load (64 clients, mean 2 ms
+    between one client's requests: above what one GPU serves, so it
+    measures capacity) and then at fractions of the measured capacity."""
+    import cpvulkan_gb300 as c
+    server = c.Server(ctx, clients=64, slots=16, mean_interarrival_ms=2.0, duration_s=seconds, seed=seed)
+
+    def point(label, ia, st):
+        return {"offered": label, "mean_interarrival_ms_per_client": round(ia, 3),
+                "offered_requests_s": round(64 * 1000.0 / ia, 1), "requests": st["requests"], "completed": st["completed"],
+                "served_requests_s": round(st["completed"] / st["wall_s"], 1) if st["wall_s"] else None,
+                "mtri_s": round(st["mtri_s"], 2), "max_in_flight": st["max_in_flight"],
+                "latency_ms": {"p50": round(st["latency_p50_ms"], 3), "p99": round(st["latency_p99_ms"], 3), "from": "arrival"},
+                "submit_to_fence_ms": {"p50": round(st["submit_p50_ms"], 3), "p99": round(st["submit_p99_ms"], 3)},
+                "queue_wait_ms": {"p50": round(st["queue_p50_ms"], 3), "p99": round(st["queue_p99_ms"], 3)},
+                "residencies": st["residencies"], "evictions": st["evictions"]}
+
+    try:
+        first = server.run()
+        capacity = first["completed"] / first["wall_s"]
+        out = {"resident_clients": first["resident_clients"], "resident_bytes": first["resident_bytes"],
+               "capacity_requests_s": round(capacity, 1), "points": [point("configured", 2.0, first)]}
+        for f in fractions:
+            ia = 64 / (f * capacity) * 1000.0
+            server.set_load(ia, seconds)
+            out["points"].append(point("%.2f of capacity" % f, ia, server.run()))
+        return out, first
+    finally:
+        server.close()
 
 
 def run_ours(args, world, rank, dist):
@@ -275,30 +464,17 @@ def run_ours(args, world, rank, dist):
     if args.mode == "batched":
         os.environ["CPV_BATCH_MIN_DRAWS"] = "1"  # a one-draw pass runs as a batch of one
         modes = ["default"]
+    icd.cpv_kernel_launches.restype = ctypes.c_uint64
     ctx = c.Context()
     h = c.harness()
     h.cpvh_render_timed.restype = ctypes.c_int
     h.cpvh_render_timed.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)]
 
     def timed(frames):
-        arr = (ctypes.c_double * frames)()
-        res = h.cpvh_render_timed(r.ptr, frames, FLUSH_BYTES, arr)
-        if res != 0:
-            raise RuntimeError("render failed: %d" % res)
-        return list(arr)
+        return timed_frames(h, r, frames)
 
     def profile(names, frames):
-        icd.cpv_profile_reset()
-        icd.cpv_profile_enable(1)
-        timed(frames)
-        icd.cpv_profile_enable(0)
-        out = {}
-        for k in names:
-            n, ms = ctypes.c_uint64(0), ctypes.c_double(0.0)
-            icd.cpv_profile_get(k.encode(), ctypes.byref(n), ctypes.byref(ms))
-            if n.value:
-                out[k] = {"launches": n.value, "ms_per_launch": round(ms.value / n.value, 4), "ms_per_frame": round(ms.value / frames, 4)}
-        return out
+        return kernel_profile(h, icd, r, names, frames)
 
     results = {}
     r = None
@@ -341,17 +517,13 @@ def run_ours(args, world, rank, dist):
     r.close()
     line = None
     if rank == 0:
-        from tests import oracle_binding
-        oracle = oracle_binding.load()
-        st = oracle_stats(oracle, scene, args.config)
+        # the CPU-baseline leg: the oracle's whole frame on every host core
+        # (its fragment counts and the image this frame is compared with),
+        # then a single-thread sample for the baseline rate
+        ref_color, ref_depth, st, ref_s, ref_threads = reference_frame(scene)
         tris_cpu, dt_cpu, cpu_desc = cpu_baseline(scene, args.cpu_seconds, 1)
         cpu_value = tris_cpu / dt_cpu / 1e6
-        peak, peak_kind = measured_peak()
         kernels = results[head]["kernels"]
-        dom = "cpv_batch_raster" if head == "batched" else "cpv_raster"
-        alg = algorithmic_bytes(args.config, scene, st.get("fragments_written"))
-        achieved = alg / (kernels[dom]["ms_per_launch"] / 1000.0) / 1e9 if dom in kernels else None
-        traffic = committed_traffic(dom, args.config)
         frags = st.get("fragments")
         line = {
             "metric": "Mtri/s", "value": round(value, 3), "unit": "Mtri/s", "n_gpus": world, "steps": args.steps,
@@ -366,12 +538,12 @@ def run_ours(args, world, rank, dist):
                     "ms_per_step": round(e2e_ms / args.steps, 3)},
             "gpu_launches": results[head]["launches"],
             "kernels": kernels,
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None, "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
-                         "traffic": traffic, "algorithmic_bytes_per_launch": alg},
-            "cpu_baseline": {"value": round(cpu_value, 4), "unit": "Mtri/s", "cores": 1, "kind": "port", "sample": cpu_desc},
+            "roofline": roofline_of(args.config, scene, kernels, st.get("fragments_written")),
+            "cpu_baseline": {"value": round(cpu_value, 4), "unit": "Mtri/s", "cores": 1, "kind": "port", "sample": cpu_desc,
+                             "full_frame": {"seconds": round(ref_s, 3), "threads": ref_threads, "kind": "port",
+                                            "mtri_s": round(tris / ref_s / 1e6, 4)}},
+            "parity": dict(image_diff(color, depth, ref_color, ref_depth), against="oracle whole frame"),
             "clocks": results[head]["clocks"],
-            "image_checksum": int(np.asarray(color, dtype=np.uint64).sum() % (1 << 61)),
         }
         if head == "batched":
             line["config"]["tuning"] = c.batch_tuning() or "default configuration (pass below the tuning threshold)"
@@ -381,6 +553,14 @@ def run_ours(args, world, rank, dist):
                              "frames_s": round(1000.0 * world / pm, 3), "gpu_launches": results["plain"]["launches"],
                              "kernels": results["plain"]["kernels"], "clocks": results["plain"]["clocks"]}
             line["batched_over_plain_frames"] = round(pm / ms_per_step, 3)
+        if args.configs:
+            # the other workloads at full size, and the serving sweep
+            configs = {}
+            for name, cfg_i, params_i, env_i, desc_i in SIDE_WORKLOADS:
+                configs[name] = measure_workload(ctx, h, icd, name, cfg_i, params_i, env_i, desc_i)
+            sweep, _ = serve_sweep(ctx, args.side_serve_seconds)
+            configs["serve"] = dict(sweep, description=CONFIGS["serve"][2], arrival_window_s=args.side_serve_seconds)
+            line["configs"] = configs
         print(json.dumps(line), flush=True)
     ctx.close()
     return line
@@ -388,7 +568,9 @@ def run_ours(args, world, rank, dist):
 
 def run_serve(args, world, rank, dist):
     """Serving: the arrivals of args.serve_seconds per client, admitted into
-    16 queues as slots free up, through vkQueueSubmit and fences."""
+    16 queues as slots free up, through vkQueueSubmit and fences; first at
+    the configured load (above capacity), then at fractions of the measured
+    capacity."""
     import cpvulkan_gb300 as c
     c.build()
     if not c.device_available():
@@ -397,14 +579,13 @@ def run_serve(args, world, rank, dist):
     icd = ctypes.CDLL(c.ICD_PATH)
     icd.cpv_kernel_launches.restype = ctypes.c_uint64
     ctx = c.Context()
-    t0 = time.time()
-    server = c.Server(ctx, clients=64, slots=16, mean_interarrival_ms=2.0, duration_s=args.serve_seconds, seed=5 + rank)
-    create_s = time.time() - t0
     barrier(dist)
     clocks = ClockSampler()
     clocks.start()
     launches0 = icd.cpv_kernel_launches()
-    st = server.run()
+    t0 = time.time()
+    sweep, st = serve_sweep(ctx, args.serve_seconds, seed=5 + rank)
+    sweep_s = time.time() - t0
     launches = icd.cpv_kernel_launches() - launches0
     clock_info = clocks.stop()
     barrier(dist)
@@ -421,57 +602,23 @@ def run_serve(args, world, rank, dist):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded client scenes and arrivals)",
             "config": {"workload": "serve", "description": CONFIGS["serve"][2], "clients": 64, "queues": 16,
                        "arrival_window_s": args.serve_seconds, "resident_clients": st["resident_clients"],
-                       "resident_bytes": st["resident_bytes"], "client_create_s": round(create_s, 2)},
+                       "resident_bytes": st["resident_bytes"], "value_at": "the configured load (above capacity)"},
             "requests": st["requests"], "completed": st["completed"], "max_in_flight": st["max_in_flight"],
             "latency_ms": {"p50": round(st["latency_p50_ms"], 3), "p99": round(st["latency_p99_ms"], 3), "from": "arrival"},
             "submit_to_fence_ms": {"p50": round(st["submit_p50_ms"], 3), "p99": round(st["submit_p99_ms"], 3)},
             "queue_wait_ms": {"p50": round(st["queue_p50_ms"], 3), "p99": round(st["queue_p99_ms"], 3)},
+            "sweep": sweep,
             "e2e": {"value": round(value, 3), "unit": "Mtri/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
                     "note": "clients' data are resident by design; requests go through vkQueueSubmit and fences, wall-clock timed"},
-            "gpu_launches": int(launches),
+            "gpu_launches": int(launches), "sweep_wall_s": round(sweep_s, 2),
             "roofline": {"bound": "hbm", "kernel": "cpv_raster", "achieved": None, "peak": measured_peak()[0], "unit": "GB/s",
                          "frac": None, "traffic": None, "note": "many small launches; see the per-draw workloads"},
             "cpu_baseline": {"value": round(tris_cpu / dt_cpu / 1e6, 4), "unit": "Mtri/s", "cores": 1, "kind": "port", "sample": cpu_desc},
             "clocks": clock_info,
         }
         print(json.dumps(line), flush=True)
-    server.close()
     ctx.close()
     return line
-
-
-def oracle_stats(oracle, scene, workload):
-    """Fragment statistics of one frame from the oracle. The fragment count
-    (covered pixels that ran the fragment shader, before the depth test) of
-    a draw does not depend on the attachments, so a many-draw frame is
-    counted draw by draw on all host cores, each thread with its own
-    attachments."""
-    if scene.draws <= 1:
-        _, _, st = oracle.render(scene)
-        return st
-    import threading
-    lock = threading.Lock()
-    total = {"fragments": 0, "triangles": 0}
-    nxt = [0]
-
-    def worker(_):
-        color = depth = None
-        first = True
-        while True:
-            with lock:
-                i = nxt[0]
-                nxt[0] += 1
-            if i >= scene.draws:
-                return
-            color, depth, st = oracle.render(scene, i, i + 1, color=color, depth=depth, clear=first)
-            first = False
-            with lock:
-                total["fragments"] += st["fragments"]
-                total["triangles"] += st["triangles"]
-
-    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
-        list(ex.map(worker, range(os.cpu_count() or 1)))
-    return total
 
 
 def main():
@@ -487,8 +634,13 @@ def main():
                     help="auto: per-draw and batched where batching applies (render passes of 16+ draws)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="oracle time for the cpu_baseline figure")
     ap.add_argument("--ref-seconds", type=float, default=3.0, help="oracle time per step of --impl reference")
+    ap.add_argument("--no-configs", dest="configs", action="store_false",
+                    help="skip the other workloads the default run measures beside the headline frame")
+    ap.add_argument("--side-serve-seconds", type=float, default=2.0, help="arrival window of each serving point in the default run")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.config != "batch" or args.params or args.mode != "auto":
+        args.configs = False  # side workloads only beside the default headline frame
     world, rank, dist = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank, dist)

@@ -114,6 +114,8 @@ def harness():
     h.cpvh_server_create.argtypes = [vp, ctypes.POINTER(ServeConfig), cp, u32]
     h.cpvh_server_run.restype = ctypes.c_int
     h.cpvh_server_run.argtypes = [vp, ctypes.POINTER(ServeResult)]
+    h.cpvh_server_set_load.restype = None
+    h.cpvh_server_set_load.argtypes = [vp, ctypes.c_double, ctypes.c_double]
     h.cpvh_server_clients.restype = u32
     h.cpvh_server_clients.argtypes = [vp]
     h.cpvh_server_client.restype = vp
@@ -341,7 +343,8 @@ class ServeConfig(ctypes.Structure):
     """cpvh_serve_config (include/cpv_harness.h)."""
     _fields_ = [("clients", ctypes.c_uint32), ("slots", ctypes.c_uint32), ("mean_interarrival_ms", ctypes.c_double),
                 ("duration_s", ctypes.c_double), ("seed", ctypes.c_uint64), ("hbm_budget_bytes", ctypes.c_uint64),
-                ("min_tris", ctypes.c_uint32), ("max_tris", ctypes.c_uint32), ("max_side", ctypes.c_uint32)]
+                ("min_tris", ctypes.c_uint32), ("max_tris", ctypes.c_uint32), ("max_side", ctypes.c_uint32),
+                ("admit_on_demand", ctypes.c_uint32)]
 
 
 class ServeResult(ctypes.Structure):
@@ -351,7 +354,9 @@ class ServeResult(ctypes.Structure):
                 ("wall_s", ctypes.c_double), ("mtri_s", ctypes.c_double),
                 ("latency_p50_ms", ctypes.c_double), ("latency_p99_ms", ctypes.c_double),
                 ("submit_p50_ms", ctypes.c_double), ("submit_p99_ms", ctypes.c_double),
-                ("queue_p50_ms", ctypes.c_double), ("queue_p99_ms", ctypes.c_double)]
+                ("queue_p50_ms", ctypes.c_double), ("queue_p99_ms", ctypes.c_double),
+                ("residencies", ctypes.c_uint64), ("evictions", ctypes.c_uint64),
+                ("residency_p50_ms", ctypes.c_double), ("residency_p99_ms", ctypes.c_double)]
 
 
 class _ClientScene:
@@ -368,8 +373,10 @@ class Server:
     """Continuous-batching serving loop over resident offscreen clients."""
 
     def __init__(self, ctx, clients=64, slots=16, mean_interarrival_ms=2.0, duration_s=10.0, seed=5, hbm_budget_bytes=64 << 30,
-                 min_tris=1000, max_tris=500000, max_side=0):
-        cfg = ServeConfig(clients, slots, mean_interarrival_ms, duration_s, seed, hbm_budget_bytes, min_tris, max_tris, max_side)
+                 min_tris=1000, max_tris=500000, max_side=0, admit_on_demand=True):
+        cfg = ServeConfig(clients, slots, mean_interarrival_ms, duration_s, seed, hbm_budget_bytes, min_tris, max_tris, max_side,
+                          1 if admit_on_demand else 0)
+        self.ctx = ctx
         err = ctypes.create_string_buffer(4096)
         self.ptr = harness().cpvh_server_create(ctx.ptr, ctypes.byref(cfg), err, len(err))
         if not self.ptr:
@@ -378,6 +385,10 @@ class Server:
     @property
     def clients(self):
         return harness().cpvh_server_clients(self.ptr)
+
+    def set_load(self, mean_interarrival_ms, duration_s):
+        """Arrival rate and window of the next run (load sweeps)."""
+        harness().cpvh_server_set_load(self.ptr, ctypes.c_double(mean_interarrival_ms), ctypes.c_double(duration_s))
 
     def run(self):
         res = ServeResult()

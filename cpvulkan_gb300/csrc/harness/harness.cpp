@@ -14,6 +14,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -939,11 +940,18 @@ int cpvh_compile_pipelines(cpvh_context* c, const cpv_scene* s, char* err, uint3
     return result;
 }
 
-void cpvh_renderer_destroy(cpvh_renderer* r) {
+}  // extern "C"
+
+namespace {
+
+// Destroys a renderer's objects. wait_idle: after the device has gone idle
+// (any queue may still use them); without it the caller knows that all of
+// the renderer's submissions have finished (their fences signalled).
+void renderer_destroy(cpvh_renderer* r, bool wait_idle) {
     if (!r) return;
     cpvh_context* c = r->ctx;
     const Fns& f = c->f;
-    f.vkDeviceWaitIdle(c->device);
+    if (wait_idle) f.vkDeviceWaitIdle(c->device);
     if (r->fence) f.vkDestroyFence(c->device, r->fence, nullptr);
     if (r->cmd_pool) f.vkDestroyCommandPool(c->device, r->cmd_pool, nullptr);
     for (auto p : r->pipelines) f.vkDestroyPipeline(c->device, p, nullptr);
@@ -966,6 +974,12 @@ void cpvh_renderer_destroy(cpvh_renderer* r) {
     destroy_buffer(c, r->indirect_count);
     delete r;
 }
+
+}  // namespace
+
+extern "C" {
+
+void cpvh_renderer_destroy(cpvh_renderer* r) { renderer_destroy(r, true); }
 
 int cpvh_renderer_update(cpvh_renderer* r) {
     cpvh_context* c = r->ctx;
@@ -1595,19 +1609,23 @@ int cpvh_image_ops(cpvh_context* c, uint32_t format, uint32_t width, uint32_t he
 // ------------------------------------------------------------ serving loop --
 //
 // Continuous batching of offscreen clients: every client owns a scene, its
-// pipelines, buffers and attachments, kept resident; requests arrive with
-// Poisson inter-arrival times per client; the loop admits a waiting request
-// whenever a slot (a queue) is free, its client has no request in flight and
-// the in-flight footprint stays within the HBM budget, and retires requests
-// as their fences signal. Work on different queues overlaps on the device.
+// pipelines, buffers and attachments; requests arrive with Poisson
+// inter-arrival times per client; the loop admits a waiting request whenever
+// a slot (a queue) is free and its client has no request in flight, and
+// retires requests as their fences signal. Work on different queues overlaps
+// on the device. Residency is by HBM footprint: clients are made resident at
+// creation while they fit the budget; a request of a client that is not
+// resident is admitted by making it resident, evicting idle resident clients
+// (least recently used first) until it fits.
 
 struct cpvh_server {
     cpvh_context* ctx = nullptr;
     cpvh_serve_config cfg{};
     std::vector<cpv_scene*> scenes;
-    std::vector<cpvh_renderer*> clients;  // null: not resident (budget)
+    std::vector<cpvh_renderer*> clients;  // null: not resident
     std::vector<uint64_t> footprint;
     std::vector<uint64_t> triangles;
+    std::vector<uint64_t> last_use;       // admission counter value of the client's last request
     uint64_t resident_bytes = 0;
 };
 
@@ -1664,6 +1682,7 @@ cpvh_server* cpvh_server_create(cpvh_context* ctx, const cpvh_serve_config* cfg,
                                2 * (scene->vertex_bytes + scene->index_bytes + scene->uniform_bytes) /* buffers + staging */ + scene->texture_bytes;
         s->footprint.push_back(bytes);
         s->triangles.push_back(cpvh_scene_triangles(scene));
+        s->last_use.push_back(0);
         cpvh_renderer* r = nullptr;
         if (s->resident_bytes + bytes <= cfg->hbm_budget_bytes) {
             char e[512] = {0};
@@ -1676,6 +1695,12 @@ cpvh_server* cpvh_server_create(cpvh_context* ctx, const cpvh_serve_config* cfg,
     return s;
 }
 
+void cpvh_server_set_load(cpvh_server* s, double mean_interarrival_ms, double duration_s) {
+    if (!s) return;
+    s->cfg.mean_interarrival_ms = mean_interarrival_ms;
+    s->cfg.duration_s = duration_s;
+}
+
 int cpvh_server_run(cpvh_server* s, cpvh_serve_result* out) {
     cpvh_context* c = s->ctx;
     const cpvh_serve_config& cfg = s->cfg;
@@ -1684,10 +1709,12 @@ int cpvh_server_run(cpvh_server* s, cpvh_serve_result* out) {
         uint32_t client;
     };
     // Poisson arrivals per client over the window, merged in time order.
+    // Without admission on demand, clients that are not resident send none.
     std::vector<Request> arrivals;
     uint64_t rng = cfg.seed * 0x9E3779B97F4A7C15ull + 11;
     for (uint32_t i = 0; i < cfg.clients; i++) {
-        if (!s->clients[i]) continue;
+        if (!s->clients[i] && !cfg.admit_on_demand) continue;
+        if (s->footprint[i] > cfg.hbm_budget_bytes) continue;  // can never be resident
         double t = 0.0;
         for (;;) {
             t += -std::log(1.0 - uniform01(rng)) * cfg.mean_interarrival_ms;
@@ -1725,14 +1752,47 @@ int cpvh_server_run(cpvh_server* s, cpvh_serve_result* out) {
     std::vector<Slot> slot(slots);
     std::vector<std::deque<double>> waiting(cfg.clients);  // arrival times per client
     std::vector<bool> in_flight(cfg.clients, false);
-    std::vector<double> latency, submit_latency, queue_delay;
+    std::vector<double> latency, submit_latency, queue_delay, residency_ms;
     latency.reserve(arrivals.size());
-    uint64_t triangles = 0, inflight_bytes = 0;
+    uint64_t triangles = 0, uses = 0, evictions = 0;
     uint32_t max_in_flight = 0, busy = 0;
     size_t next = 0, done = 0;
     const auto t0 = std::chrono::steady_clock::now();
     auto now_ms = [&]() { return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(); };
     double last_done = 0.0;
+    // Makes client i resident: evicts idle resident clients, least recently
+    // used first, until it fits the budget. False when the clients holding
+    // the budget are all busy (the request waits for one to retire).
+    auto make_resident = [&](uint32_t i, VkResult& res) {
+        res = VK_SUCCESS;
+        if (s->clients[i]) return true;
+        uint64_t idle_bytes = 0;
+        for (uint32_t j = 0; j < cfg.clients; j++)
+            if (s->clients[j] && !in_flight[j]) idle_bytes += s->footprint[j];
+        if (s->resident_bytes - idle_bytes + s->footprint[i] > cfg.hbm_budget_bytes) return false;
+        while (s->resident_bytes + s->footprint[i] > cfg.hbm_budget_bytes) {
+            int victim = -1;
+            for (uint32_t j = 0; j < cfg.clients; j++)
+                if (s->clients[j] && !in_flight[j] && (victim < 0 || s->last_use[j] < s->last_use[static_cast<uint32_t>(victim)])) victim = static_cast<int>(j);
+            if (victim < 0) return false;
+            renderer_destroy(s->clients[static_cast<uint32_t>(victim)], false);  // idle: its last fence has signalled
+            s->clients[static_cast<uint32_t>(victim)] = nullptr;
+            s->resident_bytes -= s->footprint[static_cast<uint32_t>(victim)];
+            evictions++;
+        }
+        const double t = now_ms();
+        char e[512] = {0};
+        s->clients[i] = cpvh_renderer_create(c, s->scenes[i], e, sizeof(e));
+        if (!s->clients[i]) {
+            g_err = std::string("client residency: ") + e;
+            res = VK_ERROR_OUT_OF_DEVICE_MEMORY;
+            return false;
+        }
+        s->resident_bytes += s->footprint[i];
+        residency_ms.push_back(now_ms() - t);
+        return true;
+    };
+    std::vector<VkFence> pending;
     while (done < arrivals.size()) {
         const double now = now_ms();
         while (next < arrivals.size() && arrivals[next].arrival_ms <= now) {
@@ -1751,32 +1811,36 @@ int cpvh_server_run(cpvh_server* s, cpvh_serve_result* out) {
             latency.push_back(t - slot[k].arrival_ms);
             submit_latency.push_back(t - slot[k].submit_ms);
             triangles += s->triangles[slot[k].client];
-            inflight_bytes -= s->footprint[slot[k].client];
             in_flight[slot[k].client] = false;
             slot[k].busy = false;
             busy--;
             done++;
             last_done = t;
         }
-        // Admit: the oldest waiting request whose client is idle, while a slot
-        // is free and the in-flight footprint fits the budget.
+        // Admit: the oldest waiting request whose client is idle (and
+        // resident, or can be made resident), while a slot is free.
+        bool admitted = false;
         for (uint32_t k = 0; k < slots; k++) {
             if (slot[k].busy) continue;
             int best = -1;
             for (uint32_t i = 0; i < cfg.clients; i++) {
                 if (waiting[i].empty() || in_flight[i]) continue;
-                if (inflight_bytes + s->footprint[i] > cfg.hbm_budget_bytes && busy > 0) continue;
                 if (best < 0 || waiting[i].front() < waiting[static_cast<uint32_t>(best)].front()) best = static_cast<int>(i);
             }
             if (best < 0) break;
             const uint32_t i = static_cast<uint32_t>(best);
+            VkResult res;
+            if (!make_resident(i, res)) {
+                if (res != VK_SUCCESS) return res;
+                break;  // the budget is held by busy clients: wait for a retirement
+            }
             cpvh_renderer* r = s->clients[i];
             VkSubmitInfo si{};
             si.sType = VK_STRUCTURE_TYPE_SUBMIT_INFO;
             si.commandBufferCount = 1;
             si.pCommandBuffers = &r->frame_cmd;
             slot[k].submit_ms = now_ms();
-            const VkResult res = c->f.vkQueueSubmit(c->queues[k], 1, &si, r->fence);
+            res = c->f.vkQueueSubmit(c->queues[k], 1, &si, r->fence);
             if (res != VK_SUCCESS) return res;
             slot[k].busy = true;
             slot[k].client = i;
@@ -1784,9 +1848,25 @@ int cpvh_server_run(cpvh_server* s, cpvh_serve_result* out) {
             queue_delay.push_back(slot[k].submit_ms - slot[k].arrival_ms);
             waiting[i].pop_front();
             in_flight[i] = true;
-            inflight_bytes += s->footprint[i];
+            s->last_use[i] = ++uses;
             busy++;
             max_in_flight = std::max(max_in_flight, busy);
+            admitted = true;
+        }
+        if (admitted) continue;
+        // Nothing to admit: wait for a retirement or the next arrival,
+        // whichever comes first, instead of polling.
+        const double until = next < arrivals.size() ? arrivals[next].arrival_ms - now_ms() : 1.0;
+        if (until <= 0.0) continue;
+        const uint64_t timeout_ns = static_cast<uint64_t>(std::min(until, 1.0) * 1e6);
+        pending.clear();
+        for (uint32_t k = 0; k < slots; k++)
+            if (slot[k].busy) pending.push_back(s->clients[slot[k].client]->fence);
+        if (!pending.empty()) {
+            const VkResult w = c->f.vkWaitForFences(c->device, static_cast<uint32_t>(pending.size()), pending.data(), VK_FALSE, timeout_ns);
+            if (w != VK_SUCCESS && w != VK_TIMEOUT) return w;
+        } else {
+            std::this_thread::sleep_for(std::chrono::nanoseconds(timeout_ns));
         }
     }
     c->f.vkDeviceWaitIdle(c->device);
@@ -1808,6 +1888,10 @@ int cpvh_server_run(cpvh_server* s, cpvh_serve_result* out) {
         uint32_t resident = 0;
         for (auto* r : s->clients) resident += r ? 1u : 0u;
         out->resident_clients = resident;
+        out->residencies = residency_ms.size();
+        out->evictions = evictions;
+        out->residency_p50_ms = percentile(residency_ms, 0.50);
+        out->residency_p99_ms = percentile(residency_ms, 0.99);
     }
     return VK_SUCCESS;
 }

@@ -161,9 +161,14 @@ typedef struct cpvh_serve_config {
     double mean_interarrival_ms;
     double duration_s;
     uint64_t seed;
-    uint64_t hbm_budget_bytes;
+    uint64_t hbm_budget_bytes;   /* resident clients' footprint (attachments, buffers, texture) */
     uint32_t min_tris, max_tris;
     uint32_t max_side;
+    /* 1: a request of a client that is not resident is admitted by making
+     * the client resident, evicting idle resident clients (least recently
+     * used first) until it fits the budget; 0: such clients are never made
+     * resident and their requests are not generated */
+    uint32_t admit_on_demand;
 } cpvh_serve_config;
 
 typedef struct cpvh_serve_result {
@@ -174,11 +179,15 @@ typedef struct cpvh_serve_result {
     double latency_p50_ms, latency_p99_ms; /* arrival → fence signalled */
     double submit_p50_ms, submit_p99_ms;   /* vkQueueSubmit → fence signalled */
     double queue_p50_ms, queue_p99_ms;     /* arrival → vkQueueSubmit */
+    uint64_t residencies, evictions;       /* clients made resident / evicted during the run */
+    double residency_p50_ms, residency_p99_ms; /* time to make a client resident (objects, upload, recording) */
 } cpvh_serve_result;
 
 typedef struct cpvh_server cpvh_server;
 cpvh_server* cpvh_server_create(cpvh_context* ctx, const cpvh_serve_config* cfg, char* err, uint32_t err_len);
 int cpvh_server_run(cpvh_server* server, cpvh_serve_result* out);
+/* Sets the mean inter-arrival time and the arrival window of later runs. */
+void cpvh_server_set_load(cpvh_server* server, double mean_interarrival_ms, double duration_s);
 uint32_t cpvh_server_clients(const cpvh_server* server);
 /* The client's renderer (readback, or a frame rendered alone with
  * cpvh_render), or NULL when the client is not resident. */

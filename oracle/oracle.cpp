@@ -625,13 +625,26 @@ struct Assembled {
     std::vector<uint32_t> prims;       /* provoking, v0, v1, v2 per triangle */
 };
 
-/* Input assembly (CPVulkan/CommandBuffer.Draw.cpp:567-760). */
-void assemble(const Frame& f, const cpv_scene_pipeline& p, const cpv_scene_draw& d, Assembled& out) {
-    const uint32_t n = d.count;
-    out.vertex_id.resize(n);
+/* Primitives assemble() makes from `n` vertices. */
+size_t primitive_count(uint32_t topology, uint32_t n) {
+    switch (topology) {
+    case TOPO_POINT_LIST: return n;
+    case TOPO_LINE_LIST: return n / 2;
+    case TOPO_LINE_STRIP: return n > 0 ? n - 1 : 0;
+    case TOPO_TRIANGLE_LIST: return n / 3;
+    default: return n > 1 ? n - 2 : 0;  /* strip, fan */
+    }
+}
+
+/* Input assembly (CPVulkan/CommandBuffer.Draw.cpp:567-760) of vertices
+ * [v0, v1) and primitives [p0, p1) into `out`, whose arrays are already
+ * sized (d.count vertex ids, 4 entries per primitive); `base` is added to
+ * every primitive entry. */
+void assemble_range(const Frame& f, const cpv_scene_pipeline& p, const cpv_scene_draw& d, Assembled& out, size_t v0, size_t v1, size_t p0,
+                    size_t p1, uint32_t base) {
     if (d.indexed) {
         const uint32_t isz = f.s->index_type == 0 ? 2 : 4;
-        for (uint32_t i = 0; i < n; i++) {
+        for (size_t i = v0; i < v1; i++) {
             const uint64_t off = d.index_offset + (static_cast<uint64_t>(d.first) + i) * isz;
             uint32_t index = 0;
             if (off + isz <= f.s->index_bytes) {
@@ -641,22 +654,30 @@ void assemble(const Frame& f, const cpv_scene_pipeline& p, const cpv_scene_draw&
             out.vertex_id[i] = static_cast<uint32_t>(d.vertex_offset) + index;
         }
     } else {
-        for (uint32_t i = 0; i < n; i++) out.vertex_id[i] = d.first + i;
+        for (size_t i = v0; i < v1; i++) out.vertex_id[i] = d.first + static_cast<uint32_t>(i);
     }
-    out.prims.clear();
-    if (p.topology == TOPO_POINT_LIST) {
-        for (uint32_t i = 0; i < n; i++) { out.prims.push_back(i); out.prims.push_back(i); out.prims.push_back(i); out.prims.push_back(i); }
-    } else if (p.topology == TOPO_LINE_LIST) {
-        for (uint32_t i = 0; i < n / 2; i++) { out.prims.push_back(i * 2); out.prims.push_back(i * 2); out.prims.push_back(i * 2 + 1); out.prims.push_back(i * 2 + 1); }
-    } else if (p.topology == TOPO_LINE_STRIP) {
-        for (uint32_t i = 0; i + 1 < n; i++) { out.prims.push_back(i); out.prims.push_back(i); out.prims.push_back(i + 1); out.prims.push_back(i + 1); }
-    } else if (p.topology == TOPO_TRIANGLE_LIST) {
-        for (uint32_t i = 0; i < n / 3; i++) { out.prims.push_back(i * 3); out.prims.push_back(i * 3); out.prims.push_back(i * 3 + 1); out.prims.push_back(i * 3 + 2); }
-    } else if (p.topology == TOPO_TRIANGLE_STRIP) {
-        for (uint32_t i = 0; i + 2 < n; i++) { out.prims.push_back(i); out.prims.push_back(i); out.prims.push_back(i + 1); out.prims.push_back(i + 2); }
-    } else if (p.topology == TOPO_TRIANGLE_FAN) {
-        for (uint32_t i = 0; i + 2 < n; i++) { out.prims.push_back(i + 1); out.prims.push_back(0); out.prims.push_back(i + 1); out.prims.push_back(i + 2); }
+    for (size_t i = p0; i < p1; i++) {
+        uint32_t* e = out.prims.data() + 4 * i;
+        const uint32_t k = static_cast<uint32_t>(i);
+        switch (p.topology) {
+        case TOPO_POINT_LIST: e[0] = e[1] = e[2] = e[3] = k; break;
+        case TOPO_LINE_LIST: e[0] = e[1] = 2 * k; e[2] = e[3] = 2 * k + 1; break;
+        case TOPO_LINE_STRIP: e[0] = e[1] = k; e[2] = e[3] = k + 1; break;
+        case TOPO_TRIANGLE_LIST: e[0] = e[1] = 3 * k; e[2] = 3 * k + 1; e[3] = 3 * k + 2; break;
+        case TOPO_TRIANGLE_STRIP: e[0] = e[1] = k; e[2] = k + 1; e[3] = k + 2; break;
+        default: /* fan */ e[0] = k + 1; e[1] = 0; e[2] = k + 1; e[3] = k + 2; break;
+        }
+        for (int j = 0; j < 4; j++) e[j] += base;
     }
+}
+
+/* Input assembly (CPVulkan/CommandBuffer.Draw.cpp:567-760): vertex ids per
+ * assembled vertex and (provoking, v0, v1, v2) per primitive. */
+void assemble(const Frame& f, const cpv_scene_pipeline& p, const cpv_scene_draw& d, Assembled& out) {
+    const size_t prims = primitive_count(p.topology, d.count);
+    out.vertex_id.resize(d.count);
+    out.prims.resize(4 * prims);
+    assemble_range(f, p, d, out, 0, d.count, 0, prims, 0);
 }
 
 /* The 16 logical operations on one UNORM8 channel (Vulkan 1.1, "Logical
@@ -1086,70 +1107,182 @@ private:
     uint64_t generation_ = 0;
 };
 
-/* What the threads of one threaded render share for the current draw and
- * instance: its assembly, vertex outputs and triangle set-ups. */
+/* One draw instance of a batch of the threaded render: its assembly (with
+ * primitive entries offset to index the batch's vertex outputs), push
+ * constants, and its ranges in the batch's vertex and triangle arrays. */
+struct Unit {
+    uint32_t draw = 0, instance = 0;
+    bool triangles = true;
+    size_t vs_base = 0, tri_base = 0, tri_count = 0, prim_base = 0, prim_count = 0;
+    float push[32] = {};
+    Assembled as;
+};
+
+/* What the threads of one threaded render share: the current batch of draw
+ * instances (consecutive in API order) and their vertex outputs and
+ * triangle set-ups. */
 struct Shared {
     explicit Shared(uint32_t n) : bar(n) {}
-    Assembled as;
+    std::vector<Unit> units;
+    size_t used = 0;            /* units of the current batch */
+    size_t prims = 0;           /* primitives of the current batch */
     std::vector<VsOut> vs;
     std::vector<TriSetup> tri;
     std::vector<uint32_t> rows;  /* start_y << 16 | end_y per triangle, 0 if culled */
+    std::vector<uint16_t> owner; /* per row: the thread that writes it (y % threads) */
+    uint32_t next_draw = 0, next_instance = 0;
     Barrier bar;
 };
 
-/* draw() for thread `tid` of `n`: the assembly is made once, vertex shading
- * and triangle set-up are split into contiguous ranges, and every thread
- * then walks all triangles of the instance in order over its own rows. */
-void draw_threaded(Frame& f, const cpv_scene_draw& d, Shared& sh, uint32_t tid, uint32_t n) {
+/* Fills the next batch: draw instances in API order from the cursor until
+ * about 64k triangles (one large instance forms a batch of its own). */
+void build_batch(Frame& f, Shared& sh, uint32_t end) {
     const cpv_scene* s = f.s;
-    if (d.pipeline >= s->num_pipelines) return;
-    const cpv_scene_pipeline& p = s->pipelines[d.pipeline];
-    const bool triangles = p.topology != TOPO_POINT_LIST && p.topology != TOPO_LINE_LIST && p.topology != TOPO_LINE_STRIP;
-    const ProgramInfo info = program_info(p.program);
-    float push[32] = {};
-    std::memcpy(push, d.push, std::min<uint32_t>(d.push_size, sizeof(push)));
-    f.res.push = push;
-    for (uint32_t i = 0; i < d.instance_count; i++) {
-        const uint32_t instance = d.first_instance + i;
-        if (tid == 0) {
-            assemble(f, p, d, sh.as);
-            sh.vs.resize(sh.as.vertex_id.size());
-            sh.tri.resize(triangles ? sh.as.prims.size() / 4 : 0);
-            sh.rows.resize(sh.tri.size());
-            f.stats->vs_invocations += sh.as.vertex_id.size();
+    sh.used = 0;
+    size_t nv = 0, nt = 0, np = 0;
+    while (sh.next_draw < end && nt < 65536 && nv < 3 * 65536) {
+        const cpv_scene_draw& d = s->draws[sh.next_draw];
+        if (d.pipeline >= s->num_pipelines || sh.next_instance >= d.instance_count) {
+            sh.next_draw++;
+            sh.next_instance = 0;
+            continue;
+        }
+        const cpv_scene_pipeline& p = s->pipelines[d.pipeline];
+        if (sh.used == sh.units.size()) sh.units.emplace_back();
+        Unit& u = sh.units[sh.used++];
+        u.draw = sh.next_draw;
+        u.instance = d.first_instance + sh.next_instance;
+        u.triangles = p.topology != TOPO_POINT_LIST && p.topology != TOPO_LINE_LIST && p.topology != TOPO_LINE_STRIP;
+        std::memset(u.push, 0, sizeof(u.push));
+        std::memcpy(u.push, d.push, std::min<uint32_t>(d.push_size, sizeof(u.push)));
+        /* assembly makes d.count vertices and primitive_count() primitives */
+        const uint32_t c = d.count;
+        u.vs_base = nv;
+        u.tri_base = nt;
+        u.prim_base = np;
+        u.prim_count = primitive_count(p.topology, c);
+        u.tri_count = u.triangles ? u.prim_count : 0;
+        nv += c;
+        nt += u.tri_count;
+        np += u.prim_count;
+        f.stats->vs_invocations += c;
+        if (++sh.next_instance >= d.instance_count) {
+            sh.next_draw++;
+            sh.next_instance = 0;
+        }
+    }
+    sh.vs.resize(nv);
+    sh.tri.resize(nt);
+    sh.rows.resize(nt);
+    sh.prims = np;
+}
+
+/* The unit of the current batch holding element k of a per-unit range:
+ * vertex outputs (0), triangles (1) or primitives (2). */
+size_t unit_of(const Shared& sh, size_t k, int kind) {
+    size_t lo = 0, hi = sh.used;
+    while (hi - lo > 1) {
+        const size_t mid = (lo + hi) / 2;
+        const Unit& u = sh.units[mid];
+        if ((kind == 0 ? u.vs_base : (kind == 1 ? u.tri_base : u.prim_base)) <= k) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+/* The render of draws [begin, end) by thread `tid` of `n`: per batch, vertex
+ * shading and triangle set-up split into contiguous ranges, then every
+ * thread walks all primitives of the batch in API order over its own rows. */
+void render_threaded(Frame& f, Shared& sh, uint32_t tid, uint32_t n, uint32_t end) {
+    const cpv_scene* s = f.s;
+    for (;;) {
+        if (tid == 0) build_batch(f, sh, end);
+        sh.bar.wait();
+        if (sh.used == 0) break;
+        const size_t nv = sh.vs.size(), nt = sh.tri.size();
+        /* assembly: the units' arrays sized a unit per thread in turn, then
+         * every thread fills its share of the batch's vertices and
+         * primitives, the entries offset to index the batch's outputs */
+        for (size_t u = tid; u < sh.used; u += n) {
+            Unit& unit = sh.units[u];
+            unit.as.vertex_id.resize(s->draws[unit.draw].count);
+            unit.as.prims.resize(4 * unit.prim_count);
         }
         sh.bar.wait();
-        const size_t nv = sh.as.vertex_id.size();
-        for (size_t k = nv * tid / n; k < nv * (tid + 1) / n; k++) {
-            float attr[8][4];
-            fetch_attributes(f, p, d, sh.as.vertex_id[k], instance, attr);
-            std::memset(&sh.vs[k], 0, sizeof(VsOut));
-            run_vs(p.program, attr, f.res, sh.vs[k]);
+        {
+            const size_t v0 = nv * tid / n, v1 = nv * (tid + 1) / n;
+            const size_t q0 = sh.prims * tid / n, q1 = sh.prims * (tid + 1) / n;
+            for (size_t u = v0 < v1 ? unit_of(sh, v0, 0) : sh.used; u < sh.used && sh.units[u].vs_base < v1; u++) {
+                Unit& unit = sh.units[u];
+                const cpv_scene_draw& d = s->draws[unit.draw];
+                const size_t a = std::max(v0, unit.vs_base) - unit.vs_base, b = std::min(v1, unit.vs_base + d.count) - unit.vs_base;
+                assemble_range(f, s->pipelines[d.pipeline], d, unit.as, a, b, 0, 0, 0);
+            }
+            for (size_t u = q0 < q1 ? unit_of(sh, q0, 2) : sh.used; u < sh.used && sh.units[u].prim_base < q1; u++) {
+                Unit& unit = sh.units[u];
+                const cpv_scene_draw& d = s->draws[unit.draw];
+                const size_t a = std::max(q0, unit.prim_base) - unit.prim_base, b = std::min(q1, unit.prim_base + unit.prim_count) - unit.prim_base;
+                assemble_range(f, s->pipelines[d.pipeline], d, unit.as, 0, 0, a, b, static_cast<uint32_t>(unit.vs_base));
+            }
         }
         sh.bar.wait();
-        if (triangles) {
-            const size_t nt = sh.tri.size();
-            for (size_t j = nt * tid / n; j < nt * (tid + 1) / n; j++) {
+        /* vertex shading */
+        size_t k = nv * tid / n;
+        const size_t k1 = nv * (tid + 1) / n;
+        for (size_t u = k < k1 ? unit_of(sh, k, 0) : sh.used; u < sh.used && k < k1; u++) {
+            const Unit& unit = sh.units[u];
+            const cpv_scene_draw& d = s->draws[unit.draw];
+            const cpv_scene_pipeline& p = s->pipelines[d.pipeline];
+            f.res.push = unit.push;
+            const size_t stop = std::min(k1, unit.vs_base + unit.as.vertex_id.size());
+            for (; k < stop; k++) {
+                float attr[8][4];
+                fetch_attributes(f, p, d, unit.as.vertex_id[k - unit.vs_base], unit.instance, attr);
+                std::memset(&sh.vs[k], 0, sizeof(VsOut));
+                run_vs(p.program, attr, f.res, sh.vs[k]);
+            }
+        }
+        sh.bar.wait();
+        /* triangle set-up */
+        size_t j = nt * tid / n;
+        const size_t j1 = nt * (tid + 1) / n;
+        for (size_t u = j < j1 ? unit_of(sh, j, 1) : sh.used; u < sh.used && j < j1; u++) {
+            const Unit& unit = sh.units[u];
+            const cpv_scene_pipeline& p = s->pipelines[s->draws[unit.draw].pipeline];
+            const size_t stop = std::min(j1, unit.tri_base + unit.tri_count);
+            for (; j < stop; j++) {
                 TriSetup& ts = sh.tri[j];
-                setup_triangle(f, p, sh.as, sh.vs, j * 4, ts);
+                setup_triangle(f, p, unit.as, sh.vs, (j - unit.tri_base) * 4, ts);
                 f.stats->triangles++;
                 sh.rows[j] = (ts.culled || ts.end_y <= ts.start_y) ? 0u : (static_cast<uint32_t>(ts.start_y) << 16 | static_cast<uint32_t>(ts.end_y));
             }
-            sh.bar.wait();
-            for (size_t j = 0; j < nt; j++) {
-                const uint32_t r = sh.rows[j];
-                if (!r || first_row(f, r >> 16) >= static_cast<int64_t>(r & 0xFFFFu)) continue;
-                raster_triangle(f, p, info, sh.tri[j], sh.vs);
-            }
-        } else {
-            f.count_prims = tid == 0;
-            if (p.topology == TOPO_POINT_LIST) rasterise_points(f, p, sh.as, sh.vs);
-            else rasterise_lines(f, p, sh.as, sh.vs);
-            f.count_prims = true;
         }
-        sh.bar.wait();  /* before thread 0 assembles the next instance */
+        sh.bar.wait();
+        /* raster, in API order, over this thread's rows */
+        for (size_t u = 0; u < sh.used; u++) {
+            const Unit& unit = sh.units[u];
+            const cpv_scene_pipeline& p = s->pipelines[s->draws[unit.draw].pipeline];
+            f.res.push = unit.push;
+            if (unit.triangles) {
+                const ProgramInfo info = program_info(p.program);
+                for (size_t t = unit.tri_base; t < unit.tri_base + unit.tri_count; t++) {
+                    const uint32_t r = sh.rows[t];
+                    if (!r) continue;
+                    const uint32_t y0 = r >> 16, y1 = r & 0xFFFFu;
+                    bool mine = y1 - y0 >= n;
+                    for (uint32_t y = y0; !mine && y < y1; y++) mine = sh.owner[y] == tid;
+                    if (mine) raster_triangle(f, p, info, sh.tri[t], sh.vs);
+                }
+            } else {
+                f.count_prims = tid == 0;
+                if (p.topology == TOPO_POINT_LIST) rasterise_points(f, p, unit.as, sh.vs);
+                else rasterise_lines(f, p, unit.as, sh.vs);
+                f.count_prims = true;
+            }
+        }
+        f.res.push = nullptr;
+        sh.bar.wait();  /* before thread 0 builds the next batch */
     }
-    f.res.push = nullptr;
 }
 
 /* Checks a scene and fills the parts of `f` and `tex` every render needs. */
@@ -1236,16 +1369,21 @@ int cpv_oracle_render_threaded(const cpv_scene* scene, uint8_t* color, uint8_t* 
     const uint32_t n = std::max(1u, std::min(threads, 256u));
     const uint32_t end = std::min(draw_end, scene->num_draws);
     Shared sh(n);
+    sh.next_draw = draw_begin;
+    sh.owner.resize(scene->height);
+    for (uint32_t y = 0; y < scene->height; y++) sh.owner[y] = static_cast<uint16_t>(y % n);
     std::vector<cpv_oracle_stats> per(n);
     std::vector<std::thread> pool;
     for (uint32_t t = 0; t < n; t++) {
         pool.emplace_back([&, t] {
             Frame f = base;
             if (f.res.texture) f.res.texture = &tex;
-            f.stats = &per[t];
+            cpv_oracle_stats local{};  /* counted per fragment: kept off the other threads' cache lines */
+            f.stats = &local;
             f.row_stride = n;
             f.row_index = t;
-            for (uint32_t i = draw_begin; i < end; i++) draw_threaded(f, scene->draws[i], sh, t, n);
+            render_threaded(f, sh, t, n, end);
+            per[t] = local;
         });
     }
     for (std::thread& th : pool) th.join();

@@ -69,7 +69,7 @@ class Oracle:
         return color, (depth if dsz else None), {k: getattr(st, k) for k, _ in Stats._fields_}
 
 
-    def render_threaded(self, scene, threads=None, draw_begin=0, draw_end=None):
+    def render_threaded(self, scene, threads=None, draw_begin=0, draw_end=None, color=None, depth=None, clear=True):
         """render() on `threads` host threads (default: every usable core);
         the image is identical to render()'s."""
         from cpvulkan_gb300 import depth_texel_bytes
@@ -77,15 +77,16 @@ class Oracle:
             threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
         h, w = scene.height, scene.width
         dsz = depth_texel_bytes(scene.depth_format)
-        color = np.zeros((h, w, 4), np.uint8)
-        depth = np.zeros((h, w, dsz), np.uint8) if dsz else None
+        color = np.zeros((h, w, 4), np.uint8) if color is None else color
+        if dsz and depth is None:
+            depth = np.zeros((h, w, dsz), np.uint8)
         st = Stats()
         end = 0xFFFFFFFF if draw_end is None else draw_end
-        r = self.lib.cpv_oracle_render_threaded(scene.ptr, color.ctypes.data, depth.ctypes.data if dsz else None, 1, draw_begin, end,
-                                                threads, ctypes.byref(st))
+        r = self.lib.cpv_oracle_render_threaded(scene.ptr, color.ctypes.data, depth.ctypes.data if dsz else None, 1 if clear else 0,
+                                                draw_begin, end, threads, ctypes.byref(st))
         if r != 0:
             raise RuntimeError("oracle rejected the scene (%d)" % r)
-        return color, depth, {k: getattr(st, k) for k, _ in Stats._fields_}
+        return color, (depth if dsz else None), {k: getattr(st, k) for k, _ in Stats._fields_}
 
 
 def build():
