@@ -363,7 +363,7 @@ def roofline_of(name, scene, kernels, frag_written):
             {"limiter": "launch and submission latency (one 12-triangle draw)"}}
 
 
-def measure_workload(ctx, h, icd, name, cfg, params, env, desc, min_seconds=1.2):
+def measure_workload(ctx, h, icd, name, cfg, params, env, desc, min_seconds=1.5):
     """One side workload at its full size: device-timed frames (at least
     `min_seconds` of them, clocks sampled meanwhile), per-kernel times, the
     roofline, and the image against the oracle's whole frame."""
@@ -376,8 +376,10 @@ def measure_workload(ctx, h, icd, name, cfg, params, env, desc, min_seconds=1.2)
         r = c.Renderer(ctx, scene)
         try:
             timed_frames(h, r, 3)
-            probe = sum(timed_frames(h, r, 3)) / 3.0
-            frames = int(min(20000, max(10, math.ceil(min_seconds * 1000.0 / (probe + 0.1)))))
+            t0 = time.time()
+            timed_frames(h, r, 5)
+            probe = (time.time() - t0) * 1000.0 / 5  # wall ms per frame, L2 flush and submission included
+            frames = int(min(50000, max(10, math.ceil(min_seconds * 1000.0 / probe))))
             clocks = ClockSampler(100)
             clocks.start()
             l0 = icd.cpv_kernel_launches()
