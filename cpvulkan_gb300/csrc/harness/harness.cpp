@@ -102,6 +102,7 @@ struct Fns {
     CPVH_FN(vkCmdBeginRenderPass)
     CPVH_FN(vkCmdNextSubpass)
     CPVH_FN(vkCmdEndRenderPass)
+    CPVH_FN(vkCmdExecuteCommands)
     CPVH_FN(vkQueueSubmit)
     CPVH_FN(vkQueueWaitIdle)
     CPVH_FN(vkCreateFence)
@@ -181,6 +182,7 @@ struct cpvh_renderer {
     const cpv_scene* scene = nullptr;
     BufferAlloc vertex, index, uniform, staging, readback, indirect, indirect_count;
     uint32_t subpass = 0;  // the subpass the frame draws in (CPVH_SUBPASSES=2: 1)
+    bool use_secondary = false;  // CPVH_SECONDARY=1: draws through secondary command buffers
     ImageAlloc colour, depth, texture;
     VkSampler sampler = nullptr;
     VkRenderPass pass = nullptr;
@@ -311,33 +313,12 @@ void fill_staging(cpvh_renderer* r, void* map) {
     put(s->uniform_data, s->uniform_bytes);
 }
 
-void record_frame(cpvh_renderer* r, VkCommandBuffer cmd) {
+// Binds and draws scene draws [begin, end) into `cmd` (inside a render pass).
+void record_draws(cpvh_renderer* r, VkCommandBuffer cmd, uint32_t begin, uint32_t end) {
     cpvh_context* c = r->ctx;
     const cpv_scene* s = r->scene;
-    VkClearValue clears[2];
-    std::memset(clears, 0, sizeof(clears));
-    // in attachment order: colour (absent in a depth-only pass), depth
-    uint32_t nclears = 0;
-    if (s->color_format) {
-        for (int i = 0; i < 4; i++) clears[nclears].color.float32[i] = s->clear_color[i];
-        nclears++;
-    }
-    if (s->depth_format) {
-        clears[nclears].depthStencil.depth = s->clear_depth;
-        clears[nclears].depthStencil.stencil = s->clear_stencil;
-        nclears++;
-    }
-    VkRenderPassBeginInfo rb{};
-    rb.sType = VK_STRUCTURE_TYPE_RENDER_PASS_BEGIN_INFO;
-    rb.renderPass = r->pass;
-    rb.framebuffer = r->fb;
-    rb.renderArea = {{0, 0}, {s->width, s->height}};
-    rb.clearValueCount = nclears;
-    rb.pClearValues = clears;
-    c->f.vkCmdBeginRenderPass(cmd, &rb, VK_SUBPASS_CONTENTS_INLINE);
-    if (r->subpass == 1) c->f.vkCmdNextSubpass(cmd, VK_SUBPASS_CONTENTS_INLINE);
     uint32_t bound = ~0u;
-    for (uint32_t i = 0; i < s->num_draws; i++) {
+    for (uint32_t i = begin; i < end; i++) {
         const cpv_scene_draw& d = s->draws[i];
         const cpv_scene_pipeline& p = s->pipelines[d.pipeline];
         if (bound != d.pipeline) {
@@ -364,6 +345,63 @@ void record_frame(cpvh_renderer* r, VkCommandBuffer cmd) {
         } else {
             c->f.vkCmdDraw(cmd, d.count, d.instance_count, d.first, d.first_instance);
         }
+    }
+}
+
+void record_frame(cpvh_renderer* r, VkCommandBuffer cmd) {
+    cpvh_context* c = r->ctx;
+    const cpv_scene* s = r->scene;
+    VkClearValue clears[2];
+    std::memset(clears, 0, sizeof(clears));
+    // in attachment order: colour (absent in a depth-only pass), depth
+    uint32_t nclears = 0;
+    if (s->color_format) {
+        for (int i = 0; i < 4; i++) clears[nclears].color.float32[i] = s->clear_color[i];
+        nclears++;
+    }
+    if (s->depth_format) {
+        clears[nclears].depthStencil.depth = s->clear_depth;
+        clears[nclears].depthStencil.stencil = s->clear_stencil;
+        nclears++;
+    }
+    VkRenderPassBeginInfo rb{};
+    rb.sType = VK_STRUCTURE_TYPE_RENDER_PASS_BEGIN_INFO;
+    rb.renderPass = r->pass;
+    rb.framebuffer = r->fb;
+    rb.renderArea = {{0, 0}, {s->width, s->height}};
+    rb.clearValueCount = nclears;
+    rb.pClearValues = clears;
+    // CPVH_SECONDARY=1: the draws are recorded into two secondary command
+    // buffers (the first and second half), executed in the render pass
+    if (r->use_secondary && r->subpass == 0) {
+        c->f.vkCmdBeginRenderPass(cmd, &rb, VK_SUBPASS_CONTENTS_SECONDARY_COMMAND_BUFFERS);
+        VkCommandBuffer secs[2] = {nullptr, nullptr};
+        VkCommandBufferAllocateInfo cai{};
+        cai.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_ALLOCATE_INFO;
+        cai.commandPool = r->cmd_pool;
+        cai.level = VK_COMMAND_BUFFER_LEVEL_SECONDARY;
+        cai.commandBufferCount = 2;
+        if (c->f.vkAllocateCommandBuffers(c->device, &cai, secs) != VK_SUCCESS) return;
+        VkCommandBufferInheritanceInfo inh{};
+        inh.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_INHERITANCE_INFO;
+        inh.renderPass = r->pass;
+        inh.subpass = 0;
+        inh.framebuffer = r->fb;
+        VkCommandBufferBeginInfo bi{};
+        bi.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_BEGIN_INFO;
+        bi.flags = VK_COMMAND_BUFFER_USAGE_RENDER_PASS_CONTINUE_BIT | VK_COMMAND_BUFFER_USAGE_SIMULTANEOUS_USE_BIT;
+        bi.pInheritanceInfo = &inh;
+        const uint32_t half = s->num_draws / 2;
+        for (uint32_t k = 0; k < 2; k++) {
+            c->f.vkBeginCommandBuffer(secs[k], &bi);
+            record_draws(r, secs[k], k == 0 ? 0 : half, k == 0 ? half : s->num_draws);
+            c->f.vkEndCommandBuffer(secs[k]);
+        }
+        c->f.vkCmdExecuteCommands(cmd, 2, secs);
+    } else {
+        c->f.vkCmdBeginRenderPass(cmd, &rb, VK_SUBPASS_CONTENTS_INLINE);
+        if (r->subpass == 1) c->f.vkCmdNextSubpass(cmd, VK_SUBPASS_CONTENTS_INLINE);
+        record_draws(r, cmd, 0, s->num_draws);
     }
     c->f.vkCmdEndRenderPass(cmd);
 }
@@ -423,6 +461,16 @@ bool build_pipelines(cpvh_context* c, const cpv_scene* s, VkRenderPass pass, VkP
         stages[1].stage = VK_SHADER_STAGE_FRAGMENT_BIT;
         stages[1].module = mods[1];
         stages[1].pName = "main";
+        // the fragment shader's specialisation constant 0, when the scene sets one
+        const VkSpecializationMapEntry spec_entry{0, 0, 4};
+        VkSpecializationInfo spec{};
+        if (sp.spec_k) {
+            spec.mapEntryCount = 1;
+            spec.pMapEntries = &spec_entry;
+            spec.dataSize = 4;
+            spec.pData = &sp.spec_k;
+            stages[1].pSpecializationInfo = &spec;
+        }
         VkVertexInputBindingDescription vbd[CPV_SCENE_MAX_BINDINGS];
         VkVertexInputAttributeDescription vad[CPV_SCENE_MAX_ATTRIBUTES];
         for (uint32_t b = 0; b < sp.num_bindings; b++) vbd[b] = {sp.bindings[b].binding, sp.bindings[b].stride, static_cast<VkVertexInputRate>(sp.bindings[b].input_rate)};
@@ -662,7 +710,7 @@ cpvh_context* cpvh_open(const char* icd_path, char* err, uint32_t err_len) {
     LOAD_D(vkCmdDrawIndirect); LOAD_D(vkCmdDrawIndexedIndirect); LOAD_D(vkCmdDrawIndirectCountKHR); LOAD_D(vkCmdDrawIndexedIndirectCountKHR);
     LOAD_D(vkCmdCopyBufferToImage); LOAD_D(vkCmdCopyImageToBuffer); LOAD_D(vkCmdPipelineBarrier); LOAD_D(vkCmdPushConstants);
     LOAD_D(vkCmdBlitImage); LOAD_D(vkCmdCopyImage); LOAD_D(vkCmdClearColorImage); LOAD_D(vkCmdClearDepthStencilImage); LOAD_D(vkCmdClearAttachments);
-    LOAD_D(vkCmdBeginRenderPass); LOAD_D(vkCmdNextSubpass); LOAD_D(vkCmdEndRenderPass); LOAD_D(vkQueueSubmit); LOAD_D(vkQueueWaitIdle); LOAD_D(vkCreateFence);
+    LOAD_D(vkCmdBeginRenderPass); LOAD_D(vkCmdNextSubpass); LOAD_D(vkCmdEndRenderPass); LOAD_D(vkCmdExecuteCommands); LOAD_D(vkQueueSubmit); LOAD_D(vkQueueWaitIdle); LOAD_D(vkCreateFence);
     LOAD_D(vkDestroyFence); LOAD_D(vkResetFences); LOAD_D(vkWaitForFences); LOAD_D(vkGetFenceStatus);
 #undef LOAD_D
     // CPVH_SUBMIT=no_alloc: every submission of this context goes through the
@@ -728,6 +776,7 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
     // stride) lives in a host-visible buffer. CPVH_INDIRECT=2: as an
     // indirect-count draw of at most one record, whose count word (one per
     // draw, initially 1) lives in a second host-visible buffer.
+    if (const char* sec = std::getenv("CPVH_SECONDARY")) r->use_secondary = sec[0] == '1';
     const char* ind = std::getenv("CPVH_INDIRECT");
     if (ind && ind[0] == '2' && s->num_draws) {
         if (make_buffer(c, static_cast<VkDeviceSize>(s->num_draws) * 4, VK_BUFFER_USAGE_INDIRECT_BUFFER_BIT, true, r->indirect_count) != VK_SUCCESS)

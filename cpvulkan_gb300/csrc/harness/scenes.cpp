@@ -636,7 +636,27 @@ void build_serve(Store& st, uint64_t seed, uint32_t side, uint32_t tris, uint32_
 // × bit 17), 18 logic op (op in 20-23), 19 colour write mask (mask in
 // 24-27), 28-29 depth bounds, 30 no colour attachment (a depth-only pass;
 // D32 when bits 3-4 pick no depth format).
-void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant, uint32_t width, uint32_t height, uint32_t tris) {
+// Bytes per vertex of the colour attribute in `format` (the normalised
+// 8/16-bit and 16-bit float formats the translator converts), 0 otherwise.
+uint32_t colour_attribute_bytes(uint32_t format) {
+    switch (format) {
+    case 9: case 10: return 1;                         // R8
+    case 16: case 17: case 70: case 71: case 76: return 2;  // R8G8, R16
+    case 23: case 24: return 3;                        // R8G8B8
+    case 37: case 38: case 44: case 77: case 78: case 83: return 4;
+    case 84: case 85: case 90: return 6;               // R16G16B16
+    case 91: case 92: case 97: return 8;               // R16G16B16A16
+    default: return 0;
+    }
+}
+
+// colour_format != 0 (CUBE-family programs): the colour attribute comes
+// from a second binding in that format, its bytes seeded at random over the
+// whole code range (half floats: any sign, exponents 0-15, so subnormals
+// and values up to 2). For the FETCH program the same parameter is the
+// value of the fragment shader's specialisation constant (0: none).
+void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant, uint32_t width, uint32_t height, uint32_t tris,
+                   uint32_t colour_format) {
     cpv_scene& s = st.scene;
     s.width = width;
     s.height = height;
@@ -692,6 +712,7 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
     const bool u16 = (variant & 0x1000) != 0;
 
     uint32_t vcount = 0;
+    uint64_t colour_offset = 0;
     if (program == CPV_PROGRAM_CUBE || program == CPV_PROGRAM_DISCARD || program == CPV_PROGRAM_NOPERSP || program == CPV_PROGRAM_POINTS) {
         // Clip-space vertices with w in [0.5, 2] (positive, as the reference
         // requires), a shared-edge pair, and a zero-area triangle.
@@ -715,6 +736,25 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
         p.num_attributes = 2;
         p.attributes[0] = {0, 0, VK_FORMAT_R32G32B32A32_SFLOAT, 0};
         p.attributes[1] = {1, 0, VK_FORMAT_R32G32B32A32_SFLOAT, 16};
+        if (const uint32_t cb = colour_attribute_bytes(colour_format)) {
+            while (st.vertex.size() % 16) st.vertex.push_back(0);
+            colour_offset = st.vertex.size();
+            const bool half = colour_format == 76 || colour_format == 83 || colour_format == 90 || colour_format == 97;
+            for (uint32_t v = 0; v < vcount; v++) {
+                for (uint32_t b = 0; b < cb; b += half ? 2 : 1) {
+                    if (half) {
+                        const uint32_t h = (static_cast<uint32_t>(rng.below(2)) << 15) | (static_cast<uint32_t>(rng.below(16)) << 10) |
+                                           static_cast<uint32_t>(rng.below(1024));
+                        append(st.vertex, static_cast<uint16_t>(h));
+                    } else {
+                        st.vertex.push_back(static_cast<uint8_t>(rng.below(256)));
+                    }
+                }
+            }
+            p.num_bindings = 2;
+            p.bindings[1] = {1, cb, VK_VERTEX_INPUT_RATE_VERTEX};
+            p.attributes[1] = {1, 1, colour_format, 0};
+        }
     } else if (program == CPV_PROGRAM_FLATQUAD) {
         vcount = tris * 3;
         for (uint32_t v = 0; v < vcount; v++) {
@@ -728,7 +768,7 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
         p.num_attributes = 2;
         p.attributes[0] = {0, 0, VK_FORMAT_R32G32_SFLOAT, 0};
         p.attributes[1] = {1, 0, VK_FORMAT_R32G32B32A32_SFLOAT, 8};
-    } else if (program == CPV_PROGRAM_TEXLIT) {
+    } else if (program == CPV_PROGRAM_TEXLIT || program == CPV_PROGRAM_FETCH) {
         const Mat4 proj = perspective(60.0 * M_PI / 180.0, static_cast<double>(width) / height, 0.1, 10.0);
         const Mat4 view = look_at({0, 1.2, -1.8}, {0, 0, 0.1}, {0, -1, 0});
         st.uniform.resize(80);
@@ -771,6 +811,8 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
         t.stencil_test = p.stencil_test;
         t.stencil_front = p.stencil_front;
         t.stencil_back = p.stencil_back;
+        t.program = program;
+        if (program == CPV_PROGRAM_FETCH) t.spec_k = colour_format;  // parameter 5: the specialisation constant (0: none)
         p = t;
     } else if (program == CPV_PROGRAM_MESHPC) {
         const double phase[3] = {1.0, 2.0, 3.0};
@@ -815,6 +857,7 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
     cpv_scene_draw d{};
     d.pipeline = 0;
     d.instance_count = 1;
+    d.vertex_offsets[1] = colour_offset;
     if (variant & 0x1000 || seed % 3 == 0) {
         d.indexed = 1;
         s.index_type = u16 ? VK_INDEX_TYPE_UINT16 : VK_INDEX_TYPE_UINT32;
@@ -861,7 +904,8 @@ cpv_scene* cpvh_scene_create(uint32_t config, uint64_t seed, const uint64_t* par
         break;
     case CPVH_PROGRAM:
         build_program(*st, seed, static_cast<uint32_t>(params && np > 0 ? params[0] : 0), static_cast<uint32_t>(params && np > 1 ? params[1] : 0),
-                      static_cast<uint32_t>(param(2, 64)), static_cast<uint32_t>(param(3, 48)), static_cast<uint32_t>(param(4, 12)));
+                      static_cast<uint32_t>(param(2, 64)), static_cast<uint32_t>(param(3, 48)), static_cast<uint32_t>(param(4, 12)),
+                      static_cast<uint32_t>(param(5, 0)));
         break;
     case CPVH_SERVE: build_serve(*st, seed, static_cast<uint32_t>(param(0, 512)), static_cast<uint32_t>(param(1, 20000)), static_cast<uint32_t>(params && np > 2 ? params[2] : 0)); break;
     default: return nullptr;

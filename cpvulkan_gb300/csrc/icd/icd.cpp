@@ -893,10 +893,11 @@ VKAPI_ATTR VkResult VKAPI_CALL ResetCommandPool(VkDevice, VkCommandPool pool, Vk
 }
 VKAPI_ATTR VkResult VKAPI_CALL AllocateCommandBuffers(VkDevice device, const VkCommandBufferAllocateInfo* ai, VkCommandBuffer* out) {
     auto* pool = reinterpret_cast<CommandPool*>(ai->commandPool);
-    if (ai->level != VK_COMMAND_BUFFER_LEVEL_PRIMARY) return VK_ERROR_FEATURE_NOT_PRESENT;
+    if (ai->level != VK_COMMAND_BUFFER_LEVEL_PRIMARY && ai->level != VK_COMMAND_BUFFER_LEVEL_SECONDARY) return VK_ERROR_FEATURE_NOT_PRESENT;
     for (uint32_t i = 0; i < ai->commandBufferCount; i++) {
         auto* cb = new CommandBuffer();
         cb->device = reinterpret_cast<Device*>(device);
+        cb->secondary = ai->level == VK_COMMAND_BUFFER_LEVEL_SECONDARY;
         pool->buffers.insert(cb);
         out[i] = to_handle<VkCommandBuffer>(cb);
     }
@@ -919,7 +920,7 @@ VKAPI_ATTR VkResult VKAPI_CALL BeginCommandBuffer(VkCommandBuffer cmd, const VkC
 VKAPI_ATTR VkResult VKAPI_CALL EndCommandBuffer(VkCommandBuffer cmd) {
     auto* cb = reinterpret_cast<CommandBuffer*>(cmd);
     cb->recording = false;
-    precompile_batches(cb);
+    if (!cb->secondary) precompile_batches(cb);  // a secondary's draws are compiled with the primary that executes them
     return VK_SUCCESS;
 }
 VKAPI_ATTR VkResult VKAPI_CALL ResetCommandBuffer(VkCommandBuffer cmd, VkCommandBufferResetFlags) {
@@ -1120,6 +1121,19 @@ VKAPI_ATTR void VKAPI_CALL CmdBeginRenderPass(VkCommandBuffer cmd, const VkRende
 }
 VKAPI_ATTR void VKAPI_CALL CmdEndRenderPass(VkCommandBuffer cmd) { push(cmd, CmdType::EndRenderPass); }
 
+// vkCmdExecuteCommands (CPVulkan/CommandBuffer.cpp:704-730): the reference
+// replays each secondary's commands in place, with the primary's state. A
+// secondary re-recorded after this call invalidates the primary (Vulkan's
+// rule), so its commands are copied into the primary now; the primary then
+// batches, captures and replays them like its own.
+VKAPI_ATTR void VKAPI_CALL CmdExecuteCommands(VkCommandBuffer cmd, uint32_t n, const VkCommandBuffer* cbs) {
+    auto* primary = reinterpret_cast<CommandBuffer*>(cmd);
+    for (uint32_t i = 0; i < n; i++) {
+        const auto* sec = reinterpret_cast<const CommandBuffer*>(cbs[i]);
+        if (sec && sec != primary) primary->cmds.insert(primary->cmds.end(), sec->cmds.begin(), sec->cmds.end());
+    }
+}
+
 // ------------------------------------------------------ sync and submit --
 
 VKAPI_ATTR VkResult VKAPI_CALL CreateFence(VkDevice, const VkFenceCreateInfo* ci, const VkAllocationCallbacks* alloc, VkFence* out) {
@@ -1304,7 +1318,7 @@ const Entry kDevice[] = {
     {"vkCmdDrawIndirectCountAMD", reinterpret_cast<PFN_vkVoidFunction>(CmdDrawIndirectCount)}, E(CmdCopyBuffer), E(CmdCopyImage),
     E(CmdClearColorImage), E(CmdClearDepthStencilImage), E(CmdClearAttachments), E(CmdCopyBufferToImage), E(CmdBlitImage),
     E(CmdCopyImageToBuffer), E(CmdFillBuffer), E(CmdUpdateBuffer), E(CmdPipelineBarrier), E(CmdPushConstants), E(CmdBeginRenderPass),
-    E(CmdNextSubpass), E(CmdEndRenderPass), E(QueueSubmit), E(CreateFence), E(DestroyFence), E(ResetFences), E(GetFenceStatus), E(WaitForFences),
+    E(CmdNextSubpass), E(CmdEndRenderPass), E(CmdExecuteCommands), E(QueueSubmit), E(CreateFence), E(DestroyFence), E(ResetFences), E(GetFenceStatus), E(WaitForFences),
     E(CreateSemaphore), E(DestroySemaphore),
 };
 #undef E

@@ -252,6 +252,7 @@ struct CommandBuffer : Dispatchable {
     Device* device = nullptr;
     std::vector<Cmd> cmds;
     bool recording = false;
+    bool secondary = false;  // VK_COMMAND_BUFFER_LEVEL_SECONDARY: executed through vkCmdExecuteCommands
     std::map<size_t, std::unique_ptr<BatchState>> batches;  // by BeginRenderPass command index
     // Replay as a CUDA graph per queue: decided after the first execution
     // (no host-memory sources, no batched pass).

@@ -84,6 +84,49 @@ __device__ __forceinline__ uint32_t cpv_ld_u32(const uint8_t* base, uint64_t byt
 __device__ __forceinline__ int32_t cpv_ld_i32(const uint8_t* base, uint64_t bytes, uint64_t off) {
     return static_cast<int32_t>(cpv_ld_u32(base, bytes, off));
 }
+/* One element of `size` bytes (1 or 2), little endian, read byte by byte
+ * (vertex attributes of 8- and 16-bit formats need no 4-byte alignment). */
+__device__ __forceinline__ uint32_t cpv_ld_elem(const uint8_t* base, uint64_t bytes, uint64_t off, uint32_t size) {
+    if (base == nullptr || off + size > bytes) return 0u;
+    uint32_t v = base[off];
+    if (size == 2u) v |= static_cast<uint32_t>(base[off + 1]) << 8;
+    return v;
+}
+
+/* A vertex attribute channel of a normalised 8/16-bit format as the
+ * reference's pixel decoder returns it (LLVMRuntime/ImageCompiler.cpp:15-101,
+ * 161-230): the unsigned or signed integer converted to float and divided by
+ * the type's maximum (255, 65535, 127, 32767) — for signed formats without
+ * a clamp, so the most negative code reads slightly below -1. */
+__device__ __forceinline__ float cpv_decode_norm(uint32_t raw, uint32_t size, bool is_signed) {
+    if (!is_signed) return __fdiv_rn(__uint2float_rn(raw), size == 1u ? 255.0f : 65535.0f);
+    const int32_t v = size == 1u ? static_cast<int32_t>(static_cast<int8_t>(raw)) : static_cast<int32_t>(static_cast<int16_t>(raw));
+    return __fdiv_rn(__int2float_rn(v), size == 1u ? 127.0f : 32767.0f);
+}
+
+/* IEEE binary16 → binary32, exact (the reference widens half attributes
+ * with fpext): zero, subnormal, normal, infinity; a NaN keeps its payload
+ * and becomes quiet. */
+__device__ __forceinline__ float cpv_half_to_float(uint32_t h) {
+    const uint32_t sign = (h & 0x8000u) << 16, exp = (h >> 10) & 0x1Fu, man = h & 0x3FFu;
+    uint32_t bits;
+    if (exp == 0x1Fu) {
+        bits = sign | 0x7F800000u | (man << 13) | (man ? 0x00400000u : 0u);
+    } else if (exp != 0u) {
+        bits = sign | ((exp + 112u) << 23) | (man << 13);
+    } else if (man == 0u) {
+        bits = sign;
+    } else {
+        /* subnormal: man x 2^-24, normalised */
+        uint32_t e = 113u, m = man;
+        while ((m & 0x400u) == 0u) {
+            m <<= 1;
+            e--;
+        }
+        bits = sign | (e << 23) | ((m & 0x3FFu) << 13);
+    }
+    return __uint_as_float(bits);
+}
 
 /* ------------------------------------------------------------------------- */
 /* Value types for translated shaders                                        */
@@ -332,6 +375,19 @@ __device__ __forceinline__ void cpv_sample_level(const CpvTexture& t, uint32_t l
 /* ImageSampleExplicitLod λ (CPVulkan/GlslFunctions.cpp:624-628) + SampleImage
  * (CPVulkan/ImageSampler.cpp:562-673). Implicit-LOD sampling passes lod 0
  * (CPVulkan/GlslFunctions.cpp:657-672). */
+/* ImageFetch (CPVulkan/GlslFunctions.cpp:674-742): the texel at integer
+ * coordinates of level 0 (the reference ignores the Lod operand), zeros
+ * outside it (GetPixel's border argument is ReturnType{}). */
+__device__ __forceinline__ cvec<float, 4> cpv_fetch(const CpvTexture& t, int32_t x, int32_t y) {
+    cvec<float, 4> r;
+    if (t.levels == 0u || x < 0 || y < 0 || x >= static_cast<int32_t>(t.level_w[0]) || y >= static_cast<int32_t>(t.level_h[0])) {
+        r.v[0] = r.v[1] = r.v[2] = r.v[3] = 0.0f;
+        return r;
+    }
+    cpv_texel(t, 0u, x, y, r.v);
+    return r;
+}
+
 __device__ __forceinline__ cvec<float, 4> cpv_sample(const CpvTexture& t, float u, float v, float lod) {
     const float bias = cpv_std_clamp(__fadd_rn(t.lod_bias, 0.0f), -32.0f, 32.0f);
     const float lambda = cpv_std_clamp(__fadd_rn(lod, bias), t.min_lod, t.max_lod);

@@ -53,7 +53,7 @@ enum Op : uint16_t {
     OpShiftRightArithmetic = 195, OpShiftLeftLogical = 196, OpBitwiseOr = 197, OpBitwiseXor = 198,
     OpBitwiseAnd = 199, OpNot = 200, OpPhi = 245, OpLoopMerge = 246, OpSelectionMerge = 247, OpLabel = 248,
     OpBranch = 249, OpBranchConditional = 250, OpSwitch = 251, OpKill = 252, OpReturn = 253, OpReturnValue = 254,
-    OpUnreachable = 255,
+    OpUnreachable = 255, OpCopyMemory = 63, OpImageFetch = 95, OpImage = 100, OpBitCount = 205, OpSpecConstantOp = 52,
 };
 
 enum Dec : uint32_t {
@@ -311,6 +311,16 @@ bool parse(const uint32_t* words, size_t n, Module& m, std::string& error) {
             c.null = true;
             break;
         }
+        case OpSpecConstantOp: {
+            // (result type, id, opcode, operands...): folded when the
+            // module is translated (LLVMRuntime/SPIRVCompiler.cpp:938-1052)
+            if (!need(4)) return false;
+            Constant& c = m.constants[w[1]];
+            c.type = w[0];
+            c.spec_op = w[2];
+            c.constituents.assign(w.begin() + 3, w.end());
+            break;
+        }
         case OpUndef:
             if (!need(2)) return false;
             m.undefs[w[1]] = w[0];
@@ -456,7 +466,8 @@ private:
         case TypeKind::Struct:
             emit_aggregate(id);
             return "S" + std::to_string(id);
-        case TypeKind::SampledImage: return "uint32_t";
+        case TypeKind::SampledImage:
+        case TypeKind::Image: return "uint32_t";  /* handles: resolved at translation, never read */
         default:
             fail("unsupported type kind in shader");
             return "int";
@@ -519,6 +530,7 @@ private:
         const Type* t = type(c.type);
         if (!t) { fail("constant of unknown type"); return "0"; }
         if (c.null) return tn(c.type) + "{}";
+        if (c.spec_op) return spec_op_expr(c);
         if (c.composite) {
             // cvec/cmat/array wrappers hold one array member: double braces;
             // structs list their members: single braces.
@@ -554,6 +566,51 @@ private:
             return buf;
         default:
             fail("unsupported constant type");
+            return "0";
+        }
+    }
+
+    // A specialisation-constant operation as a constant C++ expression of
+    // its operands, with the arithmetic of the corresponding instruction
+    // (integers wrap modulo 2^32; a zero divisor gives 0, as the
+    // instructions here do).
+    std::string spec_op_expr(const Constant& c) {
+        const auto& o = c.constituents;
+        auto a = [&](size_t i) { return i < o.size() ? "(" + value(o[i]) + ")" : std::string("0"); };
+        const std::string rt = tn(c.type);
+        auto u = [&](size_t i) { return "(uint32_t)" + a(i); };
+        auto si = [&](size_t i) { return "(int32_t)" + a(i); };
+        switch (c.spec_op) {
+        case OpIAdd: return rt + "(" + u(0) + " + " + u(1) + ")";
+        case OpISub: return rt + "(" + u(0) + " - " + u(1) + ")";
+        case OpIMul: return rt + "(" + u(0) + " * " + u(1) + ")";
+        case OpUDiv: return rt + "(" + u(1) + " == 0u ? 0u : " + u(0) + " / " + u(1) + ")";
+        case OpSDiv: return rt + "(" + si(1) + " == 0 ? 0 : " + si(0) + " / " + si(1) + ")";
+        case OpUMod: return rt + "(" + u(1) + " == 0u ? 0u : " + u(0) + " % " + u(1) + ")";
+        case OpShiftLeftLogical: return rt + "(" + u(0) + " << (" + u(1) + " & 31u))";
+        case OpShiftRightLogical: return rt + "(" + u(0) + " >> (" + u(1) + " & 31u))";
+        case OpShiftRightArithmetic: return rt + "(" + si(0) + " >> (" + u(1) + " & 31u))";
+        case OpBitwiseOr: return rt + "(" + u(0) + " | " + u(1) + ")";
+        case OpBitwiseAnd: return rt + "(" + u(0) + " & " + u(1) + ")";
+        case OpBitwiseXor: return rt + "(" + u(0) + " ^ " + u(1) + ")";
+        case OpNot: return rt + "(~" + u(0) + ")";
+        case OpSNegate: return rt + "(0u - " + u(0) + ")";
+        case OpIEqual: return "(" + a(0) + " == " + a(1) + ")";
+        case OpINotEqual: return "(" + a(0) + " != " + a(1) + ")";
+        case OpULessThan: return "(" + u(0) + " < " + u(1) + ")";
+        case OpSLessThan: return "(" + si(0) + " < " + si(1) + ")";
+        case OpUGreaterThan: return "(" + u(0) + " > " + u(1) + ")";
+        case OpSGreaterThan: return "(" + si(0) + " > " + si(1) + ")";
+        case OpLogicalAnd: return "(" + a(0) + " && " + a(1) + ")";
+        case OpLogicalOr: return "(" + a(0) + " || " + a(1) + ")";
+        case OpLogicalNot: return "(!" + a(0) + ")";
+        case OpSelect: return "(" + a(0) + " ? " + a(1) + " : " + a(2) + ")";
+        case OpUConvert: case OpSConvert: return rt + "(" + a(0) + ")";
+        case OpCompositeExtract:
+            if (o.size() != 2) { fail("specialisation-constant extract of nested composites"); return "0"; }
+            return a(0) + ".v[" + std::to_string(o[1]) + "]";
+        default:
+            fail("unsupported specialisation-constant operation " + std::to_string(c.spec_op));
             return "0";
         }
     }
@@ -728,8 +785,9 @@ bool Translator::emit_attribute_fetch(const Variable& v, uint32_t location) {
     const VertexBinding* b = find_binding(a->binding);
     if (!b) return fail("vertex attribute references an undeclared binding");
     if (a->binding >= 8) return fail("vertex binding index above 7");
-    uint32_t fcomps = 0;
-    int kind = 0;  // 0 float32, 1 uint32, 2 sint32, 3 unorm8
+    uint32_t fcomps = 0, esize = 0;
+    bool sgn = false, bgra = false;
+    int kind = 0;  // 0 float32, 1 uint32, 2 sint32, 3 normalised 8/16-bit, 4 float16
     switch (a->format) {
     case 100: fcomps = 1; break;
     case 103: fcomps = 2; break;
@@ -743,17 +801,47 @@ bool Translator::emit_attribute_fetch(const Variable& v, uint32_t location) {
     case 102: fcomps = 2; kind = 2; break;
     case 105: fcomps = 3; kind = 2; break;
     case 108: fcomps = 4; kind = 2; break;
-    case 37: fcomps = 4; kind = 3; break;
+    // UNORM / SNORM through the reference's pixel decoder
+    // (LLVMRuntime/PipelineCompiler.cpp:855-889, CPVulkanBase/Formats.cpp)
+    case 9: fcomps = 1; kind = 3; esize = 1; break;                // R8_UNORM
+    case 10: fcomps = 1; kind = 3; esize = 1; sgn = true; break;   // R8_SNORM
+    case 16: fcomps = 2; kind = 3; esize = 1; break;               // R8G8_UNORM
+    case 17: fcomps = 2; kind = 3; esize = 1; sgn = true; break;   // R8G8_SNORM
+    case 23: fcomps = 3; kind = 3; esize = 1; break;               // R8G8B8_UNORM
+    case 24: fcomps = 3; kind = 3; esize = 1; sgn = true; break;   // R8G8B8_SNORM
+    case 37: fcomps = 4; kind = 3; esize = 1; break;               // R8G8B8A8_UNORM
+    case 38: fcomps = 4; kind = 3; esize = 1; sgn = true; break;   // R8G8B8A8_SNORM
+    case 44: fcomps = 4; kind = 3; esize = 1; bgra = true; break;  // B8G8R8A8_UNORM (red in byte 2)
+    case 70: fcomps = 1; kind = 3; esize = 2; break;               // R16_UNORM
+    case 71: fcomps = 1; kind = 3; esize = 2; sgn = true; break;   // R16_SNORM
+    case 77: fcomps = 2; kind = 3; esize = 2; break;               // R16G16_UNORM
+    case 78: fcomps = 2; kind = 3; esize = 2; sgn = true; break;   // R16G16_SNORM
+    case 84: fcomps = 3; kind = 3; esize = 2; break;               // R16G16B16_UNORM
+    case 85: fcomps = 3; kind = 3; esize = 2; sgn = true; break;   // R16G16B16_SNORM
+    case 91: fcomps = 4; kind = 3; esize = 2; break;               // R16G16B16A16_UNORM
+    case 92: fcomps = 4; kind = 3; esize = 2; sgn = true; break;   // R16G16B16A16_SNORM
+    // half floats: loaded as the type itself and widened (fpext), which the
+    // reference does only for an input of the same width (:845-851, 711-764)
+    case 76: fcomps = 1; kind = 4; esize = 2; break;   // R16_SFLOAT
+    case 83: fcomps = 2; kind = 4; esize = 2; break;   // R16G16_SFLOAT
+    case 90: fcomps = 3; kind = 4; esize = 2; break;   // R16G16B16_SFLOAT
+    case 97: fcomps = 4; kind = 4; esize = 2; break;   // R16G16B16A16_SFLOAT
     default: return fail("unsupported vertex attribute format " + std::to_string(a->format));
     }
+    if (kind == 3 && !is_float) return fail("normalised vertex attribute into an integer input (the reference aborts on it)");
+    if (kind == 4 && (!is_float || fcomps != comps))
+        return fail("half-float vertex attribute into an input of another type or width (the reference aborts on it)");
     const std::string index = b->input_rate == 0 ? "cpv_vertex_index" : "cpv_instance_index";
     pro_ << "  { const uint64_t off = (uint64_t)" << b->stride << "u * (uint64_t)" << index << " + " << a->offset << "u;\n";
     for (uint32_t i = 0; i < comps && i < fcomps; i++) {
         std::string e;
         const std::string vb = "P.vb[" + std::to_string(a->binding) + "], P.vb_bytes[" + std::to_string(a->binding) + "]";
         if (kind == 3) {
-            e = "cpv_decode_unorm8((cpv_ld_u32(" + vb + ", off) >> " + std::to_string(8 * i) + ") & 0xFFu)";
-            if (!is_float) return fail("UNORM attribute into an integer input");
+            const uint32_t ch = bgra && i < 3 ? 2 - i : i;
+            e = "cpv_decode_norm(cpv_ld_elem(" + vb + ", off + " + std::to_string(ch * esize) + "u, " + std::to_string(esize) + "u), " +
+                std::to_string(esize) + "u, " + (sgn ? "true" : "false") + ")";
+        } else if (kind == 4) {
+            e = "cpv_half_to_float(cpv_ld_elem(" + vb + ", off + " + std::to_string(2 * i) + "u, 2u))";
         } else if (kind == 0) {
             e = "cpv_ld_f32(" + vb + ", off + " + std::to_string(4 * i) + "u)";
             if (!is_float) e = "(" + tn(elem) + ")__float_as_uint(" + e + ")";
@@ -1294,6 +1382,38 @@ bool Translator::emit_instruction(const Instruction& ins, const std::map<uint32_
     // ---- images ----
     case OpSampledImage:
         return fail("separate images and samplers are not supported");
+    case OpImage: {
+        // the image of a sampled image (LLVMRuntime/SPIRVCompiler.cpp:2480-2519)
+        auto h = handles_.find(w[2]);
+        if (h == handles_.end()) return fail("OpImage of an unknown sampled image");
+        handles_[w[1]] = h->second;
+        return true;
+    }
+    case OpImageFetch: {
+        // texelFetch (CPVulkan/GlslFunctions.cpp:674-742): level 0 whatever
+        // the Lod operand, integer texel coordinates, zero outside the level
+        auto h = handles_.find(w[2]);
+        if (h == handles_.end()) return fail("fetching from an unknown image");
+        samples_++;
+        body_ << "  " << R(w[1]) << " = cpv_fetch(P.tex[" << h->second << "], (int32_t)" << comp(w[3], 0) << ", (int32_t)" << comp(w[3], 1) << ");\n";
+        return true;
+    }
+    case OpBitCount:
+        cw(w[1], w[0], {w[2]}, [](auto& c) { return "__popc((uint32_t)" + c[0] + ")"; });
+        return true;
+    case OpCopyMemory: {
+        // a copy of the source object into the target (:2008-2019)
+        auto dst = ptrs_.find(w[0]);
+        auto src = ptrs_.find(w[1]);
+        if (dst == ptrs_.end() || src == ptrs_.end()) return fail("copy through an unknown pointer");
+        if (dst->second.kind != PtrInfo::Lvalue) return fail("copy to read-only memory");
+        const PtrInfo& p = src->second;
+        if (p.kind == PtrInfo::Lvalue) body_ << "  " << dst->second.lvalue << " = " << p.lvalue << ";\n";
+        else if (p.kind == PtrInfo::Explicit)
+            body_ << "  " << dst->second.lvalue << " = " << loader(p.type) << "(" << p.base << ", " << p.bytes << ", " << p.offset << ", " << p.mstride << "u);\n";
+        else return fail("copy of an image handle");
+        return true;
+    }
     case OpImageSampleImplicitLod:
     case OpImageSampleExplicitLod: {
         auto h = handles_.find(w[2]);

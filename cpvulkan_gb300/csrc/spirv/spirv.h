@@ -40,6 +40,7 @@ struct Constant {
     bool null = false;
     bool spec = false;
     uint32_t spec_id = 0xFFFFFFFFu;
+    uint32_t spec_op = 0;              // OpSpecConstantOp: the operation (operands in constituents)
 };
 
 struct Variable {

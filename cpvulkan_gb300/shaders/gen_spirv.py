@@ -22,9 +22,11 @@ OP = dict(
     AccessChain=65, Decorate=71, MemberDecorate=72, VectorShuffle=79, CompositeConstruct=80,
     CompositeExtract=81, ImageSampleImplicitLod=87, FAdd=129, FSub=131, FMul=133, FDiv=136,
     VectorTimesScalar=142, MatrixTimesVector=145, Dot=148, FOrdGreaterThan=186, SelectionMerge=247,
-    Label=248, Branch=249, BranchConditional=250, Kill=252, Return=253,
+    Label=248, Branch=249, BranchConditional=250, Kill=252, Return=253, SpecConstant=50, SpecConstantOp=52,
+    CopyMemory=63, ImageFetch=95, Image=100, ConvertFToS=110, ConvertSToF=111, IAdd=128, IMul=132, BitwiseXor=198,
+    BitCount=205,
 )
-DEC = dict(Block=2, ColMajor=5, MatrixStride=7, BuiltIn=11, NoPerspective=13, Flat=14, Location=30, Binding=33,
+DEC = dict(SpecId=1, Block=2, ColMajor=5, MatrixStride=7, BuiltIn=11, NoPerspective=13, Flat=14, Location=30, Binding=33,
            DescriptorSet=34, Offset=35)
 SC = dict(UniformConstant=0, Input=1, Uniform=2, Output=3, Function=7, PushConstant=9)
 BUILTIN = dict(Position=0, PointSize=1, ClipDistance=3, CullDistance=4)
@@ -96,9 +98,26 @@ class Module:
     def struct(self, key, members):
         return self._type(("struct", key), "TypeStruct", lambda: list(members))
 
+    def ivec(self, n): return self._type(("ivec", n), "TypeVector", lambda: [self.int(), n])
+
+    def image_2d(self):
+        return self._type(("img2d",), "TypeImage", lambda: [self.float(), 1, 0, 0, 0, 1, 0])
+
     def sampled_image_2d(self):
-        img = self._type(("img2d",), "TypeImage", lambda: [self.float(), 1, 0, 0, 0, 1, 0])
+        img = self.image_2d()
         return self._type(("simg2d",), "TypeSampledImage", lambda: [img])
+
+    def spec_const_int(self, default, spec_id):
+        c = self._const(("sci", spec_id), "SpecConstant", self.int, lambda: [default & 0xFFFFFFFF])
+        self.decorate(c, "SpecId", spec_id)
+        return c
+
+    def spec_op(self, t, opname, *operands):
+        return self._const(("sop", t, opname) + tuple(operands), "SpecConstantOp", lambda: t, lambda: [OP[opname]] + list(operands))
+
+    def local(self, t):
+        """A Function-storage variable: call first in the entry block."""
+        return self.op("Variable", self.ptr("Function", t), SC["Function"])
 
     # constants
     def const_f(self, x):
@@ -411,6 +430,44 @@ def meshpc_frag():
     return m.assemble(body)
 
 
+def fetch_frag():
+    """layout(constant_id = 0) const int K = 3; const int S = K * 8 + 8;
+    layout(set=0,binding=1) uniform sampler2D tex;
+    layout(location=0) in vec2 uv; layout(location=1) in vec3 n; layout(location=0) out vec4 o;
+    void main() { vec4 a, b; ivec2 p = ivec2(uv * float(S));
+                  a = texelFetch(tex, p, 0);       // OpImage + OpImageFetch
+                  b = a;                           // OpCopyMemory
+                  o = vec4(b.rgb, float(bitCount(p.x ^ p.y)) / 16.0); }"""
+    m = Module(4)
+    v2, v3, v4, f, i = m.vec(2), m.vec(3), m.vec(4), m.float(), m.int()
+    iv2 = m.ivec(2)
+    simg, img = m.sampled_image_2d(), m.image_2d()
+    tex = m.variable("UniformConstant", simg, "tex")
+    m.decorate(tex, "DescriptorSet", 0)
+    m.decorate(tex, "Binding", 1)
+    uv = m.variable("Input", v2, "uv"); m.decorate(uv, "Location", 0)
+    n = m.variable("Input", v3, "n"); m.decorate(n, "Location", 1)
+    out = m.variable("Output", v4, "o"); m.decorate(out, "Location", 0)
+    k = m.spec_const_int(3, 0)
+    scale = m.spec_op(i, "IAdd", m.spec_op(i, "IMul", k, m.const_int(8)), m.const_int(8))
+
+    def body(m):
+        a = m.local(v4)
+        b = m.local(v4)
+        sf = m.op("ConvertSToF", f, scale)
+        p = m.op("ConvertFToS", iv2, m.op("VectorTimesScalar", v2, m.load(v2, uv), sf))
+        im = m.op("Image", img, m.load(simg, tex))
+        m.store(a, m.op("ImageFetch", v4, im, p, 0x2, m.const_int(0)))
+        m.op_void("CopyMemory", b, a)
+        g = m.load(v4, b)
+        x = m.op("BitwiseXor", i, m.op("CompositeExtract", i, p, 0), m.op("CompositeExtract", i, p, 1))
+        alpha = m.op("FDiv", f, m.op("ConvertSToF", f, m.op("BitCount", i, x)), m.const_f(16.0))
+        rgb = m.op("VectorShuffle", v3, g, g, 0, 1, 2)
+        m.store(out, m.op("CompositeConstruct", v4, rgb, alpha))
+        m.op_void("Return")
+    return m.assemble(body)
+
+
 PROGRAMS = {
     "cube": (cube_vert, lambda: colour_frag()),
     "texlit": (texlit_vert, texlit_frag),
@@ -419,6 +476,7 @@ PROGRAMS = {
     "discard": (cube_vert, lambda: colour_frag(discard=True)),
     "nopersp": (cube_vert, lambda: colour_frag("NoPerspective")),
     "points": (points_vert, colour_frag),
+    "fetch": (texlit_vert, fetch_frag),
 }
 
 

@@ -33,7 +33,9 @@ enum cpv_program {
     CPV_PROGRAM_DISCARD = 4,     /* CUBE with a fragment discard when colour.r > 0.5 (OpKill coverage)          */
     CPV_PROGRAM_NOPERSP = 5,     /* CUBE with noperspective colour (InterpolationType::Linear coverage)         */
     CPV_PROGRAM_POINTS = 6,      /* CUBE that also writes gl_PointSize = colour.a * 16                          */
-    CPV_PROGRAM_COUNT = 7
+    CPV_PROGRAM_FETCH = 7,       /* TEXLIT's vertex shader; FS: texelFetch at uv * (K * 8 + 8) with K a
+                                    specialisation constant (default 3), bitCount, a copy between variables */
+    CPV_PROGRAM_COUNT = 8
 };
 
 #define CPV_SCENE_MAX_BINDINGS 4
@@ -80,6 +82,7 @@ typedef struct cpv_scene_pipeline {
     uint32_t logic_op;         /* VkLogicOp, CLEAR (0) .. SET (15) */
     uint32_t depth_bounds_test;              /* VkPipelineDepthStencilStateCreateInfo::depthBoundsTestEnable */
     float min_depth_bounds, max_depth_bounds;
+    uint32_t spec_k;           /* non-zero: the fragment shader's specialisation constant 0 (a 32-bit int) */
 } cpv_scene_pipeline;
 
 typedef struct cpv_scene_draw {

@@ -326,6 +326,7 @@ enum {
     VK_IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT_BIT = 0x20,
     VK_COMMAND_POOL_CREATE_RESET_COMMAND_BUFFER_BIT = 0x2,
     VK_COMMAND_BUFFER_USAGE_ONE_TIME_SUBMIT_BIT = 0x1,
+    VK_COMMAND_BUFFER_USAGE_RENDER_PASS_CONTINUE_BIT = 0x2,
     VK_COMMAND_BUFFER_USAGE_SIMULTANEOUS_USE_BIT = 0x4,
     VK_DESCRIPTOR_POOL_CREATE_FREE_DESCRIPTOR_SET_BIT = 0x1,
     VK_PIPELINE_STAGE_TOP_OF_PIPE_BIT = 0x1,
@@ -1271,6 +1272,7 @@ typedef void (VKAPI_PTR* PFN_vkCmdPipelineBarrier)(VkCommandBuffer, VkPipelineSt
 typedef void (VKAPI_PTR* PFN_vkCmdPushConstants)(VkCommandBuffer, VkPipelineLayout, VkShaderStageFlags, uint32_t, uint32_t, const void*);
 typedef void (VKAPI_PTR* PFN_vkCmdBeginRenderPass)(VkCommandBuffer, const VkRenderPassBeginInfo*, VkSubpassContents);
 typedef void (VKAPI_PTR* PFN_vkCmdEndRenderPass)(VkCommandBuffer);
+typedef void (VKAPI_PTR* PFN_vkCmdExecuteCommands)(VkCommandBuffer, uint32_t, const VkCommandBuffer*);
 typedef void (VKAPI_PTR* PFN_vkCmdNextSubpass)(VkCommandBuffer, VkSubpassContents);
 typedef VkResult (VKAPI_PTR* PFN_vkQueueSubmit)(VkQueue, uint32_t, const VkSubmitInfo*, VkFence);
 typedef VkResult (VKAPI_PTR* PFN_vkQueueWaitIdle)(VkQueue);

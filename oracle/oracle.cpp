@@ -353,7 +353,8 @@ struct ProgramInfo {
 ProgramInfo program_info(uint32_t program) {
     switch (program) {
     case CPV_PROGRAM_CUBE: return {1, {4}, {INTERP_PERSPECTIVE}};
-    case CPV_PROGRAM_TEXLIT: return {2, {2, 3}, {INTERP_PERSPECTIVE, INTERP_PERSPECTIVE}};
+    case CPV_PROGRAM_TEXLIT:
+    case CPV_PROGRAM_FETCH: return {2, {2, 3}, {INTERP_PERSPECTIVE, INTERP_PERSPECTIVE}};
     case CPV_PROGRAM_FLATQUAD: return {1, {4}, {INTERP_FLAT}};
     case CPV_PROGRAM_MESHPC: return {1, {3}, {INTERP_PERSPECTIVE}};
     case CPV_PROGRAM_DISCARD: return {1, {4}, {INTERP_PERSPECTIVE}};
@@ -396,7 +397,8 @@ void run_vs(uint32_t program, const float attr[8][4], const Resources& r, VsOut&
         if (program == CPV_PROGRAM_POINTS) out.point_size = attr[1][3] * 16.0f;
         break;
     }
-    case CPV_PROGRAM_TEXLIT: {
+    case CPV_PROGRAM_TEXLIT:
+    case CPV_PROGRAM_FETCH: {
         float m[16];
         for (int i = 0; i < 16; i++) m[i] = ubo_at(r, i);
         out.var[0] = attr[1][0]; out.var[1] = attr[1][1];
@@ -427,7 +429,7 @@ void run_vs(uint32_t program, const float attr[8][4], const Resources& r, VsOut&
 
 /* Returns true when the fragment is discarded (OpKill → return true,
  * LLVMRuntime/SPIRVCompiler.cpp:3308-3310, 3642-3651). */
-bool run_fs(uint32_t program, const float* in, const Resources& r, float colour[4]) {
+bool run_fs(uint32_t program, const float* in, const Resources& r, float colour[4], uint32_t spec_k) {
     switch (program) {
     case CPV_PROGRAM_CUBE:
     case CPV_PROGRAM_NOPERSP:
@@ -448,6 +450,25 @@ bool run_fs(uint32_t program, const float* in, const Resources& r, float colour[
         const float d = dot3(n, light);
         const float l = fmax_std(d, 0.0f);
         colour[0] = c[0] * l; colour[1] = c[1] * l; colour[2] = c[2] * l; colour[3] = c[3];
+        return false;
+    }
+    case CPV_PROGRAM_FETCH: {
+        /* K: specialisation constant 0 (default 3); S = K * 8 + 8 folded in
+         * 32-bit integers (OpSpecConstantOp IMul, IAdd). */
+        const uint32_t k = spec_k ? spec_k : 3u;
+        const int32_t scale = static_cast<int32_t>(k * 8u + 8u);
+        const float sf = static_cast<float>(scale);                 /* OpConvertSToF */
+        const int32_t px = static_cast<int32_t>(in[0] * sf);        /* OpVectorTimesScalar, OpConvertFToS */
+        const int32_t py = static_cast<int32_t>(in[1] * sf);
+        /* ImageFetch (CPVulkan/GlslFunctions.cpp:674-742): level 0 whatever
+         * the Lod operand, zeros outside it; OpCopyMemory copies it as is */
+        float t[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (r.texture && r.texture->levels > 0 && px >= 0 && py >= 0 && px < static_cast<int32_t>(r.texture->level_w[0]) &&
+            py < static_cast<int32_t>(r.texture->level_h[0]))
+            get_texel(*r.texture, 0, px, py, 0, t);
+        const uint32_t bits = static_cast<uint32_t>(__builtin_popcount(static_cast<uint32_t>(px ^ py)));  /* OpBitCount */
+        colour[0] = t[0]; colour[1] = t[1]; colour[2] = t[2];
+        colour[3] = static_cast<float>(static_cast<int32_t>(bits)) / 16.0f;
         return false;
     }
     case CPV_PROGRAM_MESHPC: {
@@ -590,10 +611,88 @@ int64_t first_row(const Frame& f, int64_t start) {
     return start + (static_cast<int64_t>(f.row_index) + f.row_stride - r) % f.row_stride;
 }
 
+/* Layout of a vertex attribute format: components, bytes per component,
+ * kind (0 float32, 1 normalised 8/16-bit, 2 float16), signedness and
+ * the B8G8R8A8 channel order (CPVulkanBase/Formats.cpp). False for formats
+ * the oracle does not convert. */
+bool attribute_layout(uint32_t format, int& comps, int& esize, int& kind, bool& sgn, bool& bgra) {
+    sgn = bgra = false;
+    kind = 1;
+    switch (format) {
+    case FMT_R32_SFLOAT: comps = 1; esize = 4; kind = 0; return true;
+    case FMT_R32G32_SFLOAT: comps = 2; esize = 4; kind = 0; return true;
+    case FMT_R32G32B32_SFLOAT: comps = 3; esize = 4; kind = 0; return true;
+    case FMT_R32G32B32A32_SFLOAT: comps = 4; esize = 4; kind = 0; return true;
+    case 9: comps = 1; esize = 1; return true;
+    case 10: comps = 1; esize = 1; sgn = true; return true;
+    case 16: comps = 2; esize = 1; return true;
+    case 17: comps = 2; esize = 1; sgn = true; return true;
+    case 23: comps = 3; esize = 1; return true;
+    case 24: comps = 3; esize = 1; sgn = true; return true;
+    case 37: comps = 4; esize = 1; return true;
+    case 38: comps = 4; esize = 1; sgn = true; return true;
+    case 44: comps = 4; esize = 1; bgra = true; return true;
+    case 70: comps = 1; esize = 2; return true;
+    case 71: comps = 1; esize = 2; sgn = true; return true;
+    case 77: comps = 2; esize = 2; return true;
+    case 78: comps = 2; esize = 2; sgn = true; return true;
+    case 84: comps = 3; esize = 2; return true;
+    case 85: comps = 3; esize = 2; sgn = true; return true;
+    case 91: comps = 4; esize = 2; return true;
+    case 92: comps = 4; esize = 2; sgn = true; return true;
+    case 76: comps = 1; esize = 2; kind = 2; return true;
+    case 83: comps = 2; esize = 2; kind = 2; return true;
+    case 90: comps = 3; esize = 2; kind = 2; return true;
+    case 97: comps = 4; esize = 2; kind = 2; return true;
+    default: return false;
+    }
+}
+
+/* IEEE binary16 → binary32 (exact; fpext of the reference's half loads). */
+float half_to_float(uint16_t h) {
+    const uint32_t sign = static_cast<uint32_t>(h & 0x8000u) << 16;
+    const int exp = (h >> 10) & 0x1F;
+    const uint32_t man = h & 0x3FFu;
+    float f;
+    if (exp == 0x1F) {
+        const uint32_t bits = sign | 0x7F800000u | (man << 13) | (man ? 0x00400000u : 0u);
+        std::memcpy(&f, &bits, 4);
+        return f;
+    }
+    if (exp == 0) f = std::ldexp(static_cast<float>(man), -24);           /* zero or subnormal: man x 2^-24 */
+    else f = std::ldexp(static_cast<float>(man | 0x400u), exp - 25);       /* (1024 + man) x 2^(exp - 25) */
+    return sign ? -f : f;
+}
+
+/* One channel of a normalised 8/16-bit attribute as the reference's pixel
+ * decoder returns it (LLVMRuntime/ImageCompiler.cpp:15-101, 161-230): the
+ * integer converted to float and divided by its type's maximum; signed
+ * values are not clamped, so the most negative code reads below -1. */
+float decode_norm(uint32_t raw, int esize, bool sgn) {
+    if (!sgn) return static_cast<float>(raw) / (esize == 1 ? 255.0f : 65535.0f);
+    const int32_t v = esize == 1 ? static_cast<int8_t>(raw) : static_cast<int16_t>(raw);
+    return static_cast<float>(v) / (esize == 1 ? 127.0f : 32767.0f);
+}
+
+/* An attribute's components from its bytes, into out[0..comps). */
+void decode_attribute(const uint8_t* p, int comps, int esize, int kind, bool sgn, bool bgra, float out[4]) {
+    for (int c = 0; c < comps; c++) {
+        const int ch = (bgra && c < 3) ? 2 - c : c;
+        const uint8_t* e = p + ch * esize;
+        if (kind == 0) {
+            std::memcpy(&out[c], e, 4);
+        } else {
+            const uint32_t raw = esize == 1 ? e[0] : static_cast<uint32_t>(e[0] | (e[1] << 8));
+            out[c] = kind == 2 ? half_to_float(static_cast<uint16_t>(raw)) : decode_norm(raw, esize, sgn);
+        }
+    }
+}
+
 /* Attribute fetch (LLVMRuntime/PipelineCompiler.cpp:821-896): address =
  * binding base + stride * (vertex or instance id) + attribute offset; float
- * formats copy straight; components absent from the format read 0,0,0,1.
- * Reads outside the vertex blob return zeros. */
+ * formats copy straight, normalised 8/16-bit formats go through the pixel
+ * decoder, half floats are widened; components absent from the format read
+ * 0,0,0,1. Reads outside the vertex blob return zeros. */
 void fetch_attributes(const Frame& f, const cpv_scene_pipeline& p, const cpv_scene_draw& d, uint32_t vertex_id, uint32_t instance_id, float attr[8][4]) {
     for (int l = 0; l < 8; l++) { attr[l][0] = 0; attr[l][1] = 0; attr[l][2] = 0; attr[l][3] = 1; }
     for (uint32_t a = 0; a < p.num_attributes; a++) {
@@ -605,18 +704,13 @@ void fetch_attributes(const Frame& f, const cpv_scene_pipeline& p, const cpv_sce
             if (p.bindings[i].binding == at.binding) { b = &p.bindings[i]; slot = i; }
         }
         if (!b) continue;
-        int comps = 0;
-        switch (at.format) {
-        case FMT_R32_SFLOAT: comps = 1; break;
-        case FMT_R32G32_SFLOAT: comps = 2; break;
-        case FMT_R32G32B32_SFLOAT: comps = 3; break;
-        case FMT_R32G32B32A32_SFLOAT: comps = 4; break;
-        default: comps = 0; break;
-        }
+        int comps = 0, esize = 4, kind = 0;
+        bool sgn = false, bgra = false;
+        if (!attribute_layout(at.format, comps, esize, kind, sgn, bgra)) continue;
         const uint64_t index = (b->input_rate == RATE_VERTEX) ? vertex_id : instance_id;
         const uint64_t off = d.vertex_offsets[slot] + static_cast<uint64_t>(b->stride) * index + at.offset;
-        if (off + static_cast<uint64_t>(comps) * 4u > f.s->vertex_bytes) continue;
-        for (int c = 0; c < comps; c++) std::memcpy(&attr[at.location][c], f.s->vertex_data + off + 4u * c, 4);
+        if (off + static_cast<uint64_t>(comps) * esize > f.s->vertex_bytes) continue;
+        decode_attribute(f.s->vertex_data + off, comps, esize, kind, sgn, bgra, attr[at.location]);
     }
 }
 
@@ -756,7 +850,7 @@ void fragment(Frame& f, const cpv_scene_pipeline& p, uint32_t x, uint32_t y, flo
     const cpv_scene* s = f.s;
     f.stats->fragments++;
     float colour[4];
-    if (run_fs(p.program, inputs, f.res, colour)) return;
+    if (run_fs(p.program, inputs, f.res, colour, p.spec_k)) return;
 
     const uint64_t pix = static_cast<uint64_t>(y) * s->width + x;
     uint8_t* ds = f.depth ? f.depth + pix * f.depth_size : nullptr;
@@ -1400,6 +1494,16 @@ int cpv_oracle_render_threaded(const cpv_scene* scene, uint8_t* color, uint8_t* 
 }
 
 float cpv_oracle_edge(float ax, float ay, float bx, float by, float cx, float cy) { return edge(ax, ay, bx, by, cx, cy); }
+
+int cpv_oracle_decode_attribute(uint32_t format, const uint8_t* bytes, float out[4]) {
+    int comps = 0, esize = 4, kind = 0;
+    bool sgn = false, bgra = false;
+    if (!attribute_layout(format, comps, esize, kind, sgn, bgra)) return -1;
+    out[0] = out[1] = out[2] = 0.0f;
+    out[3] = 1.0f;
+    decode_attribute(bytes, comps, esize, kind, sgn, bgra, out);
+    return comps;
+}
 
 void cpv_oracle_edge_n(const float* in, float* out, uint64_t n) {
     for (uint64_t i = 0; i < n; i++) {

@@ -60,6 +60,10 @@ int cpv_oracle_render_threaded(const cpv_scene* scene, uint8_t* color, uint8_t* 
                                uint32_t draw_begin, uint32_t draw_end, uint32_t threads, cpv_oracle_stats* stats);
 
 /* Single-step helpers exposed for known-answer tests. */
+/* A vertex attribute of `format` (32-bit float, normalised 8/16-bit, 16-bit
+ * float, B8G8R8A8) decoded from its bytes into out (absent components
+ * 0, 0, 0, 1); returns its component count, or -1 for another format. */
+int cpv_oracle_decode_attribute(uint32_t format, const uint8_t* bytes, float out[4]);
 float cpv_oracle_edge(float ax, float ay, float bx, float by, float cx, float cy);
 uint8_t cpv_oracle_encode_unorm8(float value);
 /* VkLogicOp `op` (0 CLEAR .. 15 SET) of an encoded source and destination byte. */

@@ -176,3 +176,47 @@ def test_second_subpass(gpu_ctx, oracle, monkeypatch, config, params):
     report, stats = check(gpu_ctx, oracle, scene)
     assert stats["fragments_written"] > 0
     assert report["color_pixels_differing"] == 0, report
+
+
+# Vertex attribute formats (scene parameter 5): the CUBE program's colour
+# attribute read from a second binding in normalised 8/16-bit formats (1-4
+# channels, B8G8R8A8) and half floats, raw bytes over the whole code range.
+VERTEX_FORMATS = [9, 10, 16, 17, 23, 24, 37, 38, 44, 70, 71, 77, 78, 84, 85, 91, 92, 97]
+
+
+@pytest.mark.parametrize("fmt", VERTEX_FORMATS)
+@pytest.mark.parametrize("seed", [1, 2])
+def test_vertex_attribute_formats(gpu_ctx, oracle, fmt, seed):
+    scene = c.Scene(c.PROGRAM, seed, [c.PROGRAM_CUBE, 0x10, 64, 48, 24, fmt])
+    report, stats = check(gpu_ctx, oracle, scene)
+    assert stats["fragments_written"] > 0
+    assert report["color_pixels_differing"] == 0, report
+
+
+@pytest.mark.parametrize("fmt", [38, 97])
+def test_vertex_attribute_formats_batched(gpu_ctx, oracle, monkeypatch, fmt):
+    monkeypatch.setenv("CPV_BATCH_MIN_DRAWS", "1")
+    scene = c.Scene(c.PROGRAM, 3, [c.PROGRAM_CUBE, 0x10, 64, 48, 24, fmt])
+    report, _ = check(gpu_ctx, oracle, scene)
+    assert report["color_pixels_differing"] == 0, report
+
+
+# The FETCH program: OpImage + OpImageFetch (level 0, zeros outside),
+# OpBitCount, OpCopyMemory and a specialisation constant folded through
+# OpSpecConstantOp, with the constant's default (parameter 5 = 0) and two
+# VkSpecializationInfo values; opaque and blended.
+@pytest.mark.parametrize("variant", [0x0, 0x20, 0x4])
+@pytest.mark.parametrize("k", [0, 1, 9])
+@pytest.mark.parametrize("seed", [1, 2])
+def test_fetch_program(gpu_ctx, oracle, variant, k, seed):
+    scene = c.Scene(c.PROGRAM, seed, [c.PROGRAM_FETCH, variant, 64, 48, 24, k])
+    report, stats = check(gpu_ctx, oracle, scene)
+    assert stats["fragments_written"] > 1000
+    assert report["color_pixels_differing"] == 0, report
+
+
+def test_fetch_program_batched(gpu_ctx, oracle, monkeypatch):
+    monkeypatch.setenv("CPV_BATCH_MIN_DRAWS", "1")
+    scene = c.Scene(c.PROGRAM, 3, [c.PROGRAM_FETCH, 0x20, 64, 48, 24, 9])
+    report, _ = check(gpu_ctx, oracle, scene)
+    assert report["color_pixels_differing"] == 0, report

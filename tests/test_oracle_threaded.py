@@ -22,6 +22,8 @@ SCENES = [
     (c.PROGRAM, 2, [c.PROGRAM_POINTS, 0x10000 | 0x20 | 0x8, 64, 48, 24]),
     (c.PROGRAM, 3, [c.PROGRAM_CUBE, 0x10000 | 0x800 | 0x20 | 0x20000, 64, 48, 24]),
     (c.PROGRAM, 1, [c.PROGRAM_TEXLIT, 0x10 | 0x8000 | 0x20, 64, 48, 24]),
+    (c.PROGRAM, 2, [c.PROGRAM_FETCH, 0x20, 64, 48, 24, 9]),
+    (c.PROGRAM, 2, [c.PROGRAM_CUBE, 0x10, 64, 48, 24, 92]),
 ]
 
 

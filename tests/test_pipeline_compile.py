@@ -25,7 +25,7 @@ PROGRAMS = [
     (c.PROGRAM_DISCARD, 0x10), (c.PROGRAM_NOPERSP, 0x8 | 0x800),
     (c.PROGRAM_POINTS, 0x10000 | 0x10), (c.PROGRAM_CUBE, 0x10000 | 0x400 | 0x20000), (c.PROGRAM_NOPERSP, 0x10000 | 0x800 | 0x8),
     (c.PROGRAM_CUBE, 0x40000 | (6 << 20) | 0x10), (c.PROGRAM_FLATQUAD, 0x20 | 0x80000 | (0x5 << 24)),
-    (c.PROGRAM_CUBE, 0x18 | 0x100 | (2 << 28)), (c.PROGRAM_TEXLIT, 0x40000000 | 0x10),
+    (c.PROGRAM_CUBE, 0x18 | 0x100 | (2 << 28)), (c.PROGRAM_TEXLIT, 0x40000000 | 0x10), (c.PROGRAM_FETCH, 0x0),
 ]
 
 
@@ -164,3 +164,36 @@ def test_batched_module_compiles(native, monkeypatch, tmp_path, config, params):
     assert "#include \"cpv_batch.cuh\"" in open(batch[0]).read()
     sources = glob.glob(str(dump / "*.cu"))
     assert len(glob.glob(str(cache / "*.cubin"))) >= len(sources), c.icd_last_error()
+
+
+@pytest.mark.parametrize("fmt,expect", [(38, "cpv_decode_norm"), (92, "cpv_decode_norm"), (44, "cpv_decode_norm"), (97, "cpv_half_to_float")])
+def test_vertex_attribute_formats_translate(compile_ctx, fmt, expect):
+    """Normalised 8/16-bit and half-float colour attributes compile to the
+    decoder the reference's vertex fetch uses for them."""
+    ctx, dump = compile_ctx
+    ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [c.PROGRAM_CUBE, 0x10, 32, 32, 4, fmt]))
+    (path,) = glob.glob(str(dump / "pipeline_*.cu"))
+    assert expect in open(path).read()
+
+
+@pytest.mark.parametrize("fmt", [76, 83])
+def test_half_attribute_of_other_width_rejected(compile_ctx, fmt):
+    """A half-float attribute narrower than its vec4 input is rejected at
+    pipeline creation (the reference aborts on the width mismatch)."""
+    ctx, _ = compile_ctx
+    with pytest.raises(RuntimeError, match="half-float vertex attribute"):
+        ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [c.PROGRAM_CUBE, 0x10, 32, 32, 4, fmt]))
+
+
+@pytest.mark.parametrize("k,scale", [(0, "int32_t(3)"), (5, "int32_t(5)")])
+def test_fetch_program_translation(compile_ctx, k, scale):
+    """OpImage / OpImageFetch become a level-0 fetch, OpBitCount a population
+    count, OpCopyMemory a copy of the variable, and the specialisation
+    constant (overridden by VkSpecializationInfo when given) feeds the
+    folded OpSpecConstantOp expression."""
+    ctx, dump = compile_ctx
+    ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [c.PROGRAM_FETCH, 0x0, 32, 32, 4, k]))
+    (path,) = glob.glob(str(dump / "pipeline_*.cu"))
+    text = open(path).read()
+    assert "cpv_fetch(P.tex[" in text and "__popc(" in text
+    assert scale in text and "(uint32_t)(int32_t(8))" in text
