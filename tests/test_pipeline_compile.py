@@ -197,3 +197,21 @@ def test_fetch_program_translation(compile_ctx, k, scale):
     text = open(path).read()
     assert "cpv_fetch(P.tex[" in text and "__popc(" in text
     assert scale in text and "(uint32_t)(int32_t(8))" in text
+
+
+def test_secondary_command_buffers_record_batched_pass(native, monkeypatch, tmp_path):
+    """Draws recorded in secondary command buffers and run by
+    vkCmdExecuteCommands become the primary's own commands: a pass of many
+    draws composed that way is compiled as one batched module when the
+    primary is ended."""
+    dump = tmp_path / "dump"
+    dump.mkdir()
+    for k, v in {"CPV_COMPILE_ONLY": "1", "CPV_DUMP_DIR": str(dump), "CPVH_RECORD_ONLY": "1", "CPVH_SECONDARY": "1",
+                 "CPV_AUTOTUNE": "0"}.items():
+        monkeypatch.setenv(k, v)
+    ctx = c.Context()
+    try:
+        c.Renderer(ctx, c.Scene(c.BATCH, 1, [24, 2000, 320, 200])).close()
+    finally:
+        ctx.close()
+    assert glob.glob(str(dump / "batch_*.cu"))
