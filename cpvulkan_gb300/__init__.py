@@ -63,6 +63,13 @@ def depth_texel_bytes(fmt):
     return {0: 0, VK_FORMAT_D16_UNORM: 2, VK_FORMAT_D32_SFLOAT: 4, VK_FORMAT_D32_SFLOAT_S8_UINT: 8}[fmt]
 
 
+def colour_texel_bytes(fmt):
+    """Bytes per texel of a colour attachment format (R8_UNORM 1; R8G8_UNORM
+    and R16_UNORM 2; the 4-byte formats otherwise); a depth-only pass reads
+    back zeros in the 4-byte layout."""
+    return {9: 1, 16: 2, 70: 2}.get(fmt, 4)
+
+
 _harness = None
 
 
@@ -325,7 +332,7 @@ class Renderer:
 
     def readback(self):
         s = self.scene
-        color = np.zeros((s.height, s.width, 4), np.uint8)
+        color = np.zeros((s.height, s.width, colour_texel_bytes(s.color_format)), np.uint8)
         dsz = depth_texel_bytes(s.depth_format)
         depth = np.zeros((s.height, s.width, dsz), np.uint8) if dsz else None
         r = harness().cpvh_readback(self.ptr, color.ctypes.data, depth.ctypes.data if depth is not None else None)

@@ -197,6 +197,7 @@ struct cpvh_renderer {
     VkCommandBuffer frame_cmd = nullptr, e2e_cmd = nullptr, copy_cmd = nullptr;
     VkFence fence = nullptr;
     uint32_t depth_texel = 0;
+    uint32_t colour_texel = 4;
     uint64_t upload_bytes = 0;
 };
 
@@ -267,6 +268,9 @@ void destroy_image(cpvh_context* c, ImageAlloc& i) {
     i = ImageAlloc{};
 }
 
+// Bytes per texel of a colour attachment format; 4 for a depth-only pass,
+// whose readback holds zeros in the RGBA8 layout.
+uint32_t colour_texel_size(uint32_t f) { return f == VK_FORMAT_R8_UNORM ? 1 : ((f == VK_FORMAT_R8G8_UNORM || f == VK_FORMAT_R16_UNORM) ? 2 : 4); }
 uint32_t depth_texel_size(uint32_t f) { return f == VK_FORMAT_D16_UNORM ? 2 : (f == VK_FORMAT_D32_SFLOAT ? 4 : (f == VK_FORMAT_D32_SFLOAT_S8_UINT ? 8 : 0)); }
 
 VkResult submit_and_wait(cpvh_renderer* r, VkCommandBuffer cmd) {
@@ -414,7 +418,7 @@ void record_readback(cpvh_renderer* r, VkCommandBuffer cmd) {
     bc.imageExtent = {s->width, s->height, 1};
     if (s->color_format) c->f.vkCmdCopyImageToBuffer(cmd, r->colour.image, VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL, r->readback.buffer, 1, &bc);
     if (s->depth_format) {
-        bc.bufferOffset = static_cast<VkDeviceSize>(s->width) * s->height * 4;
+        bc.bufferOffset = static_cast<VkDeviceSize>(s->width) * s->height * r->colour_texel;
         bc.imageSubresource.aspectMask = VK_IMAGE_ASPECT_DEPTH_BIT;
         c->f.vkCmdCopyImageToBuffer(cmd, r->depth.image, VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL, r->readback.buffer, 1, &bc);
     }
@@ -769,7 +773,8 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
     r->upload_bytes = s->vertex_bytes + s->index_bytes + s->uniform_bytes;
     if (make_buffer(c, staging, VK_BUFFER_USAGE_TRANSFER_SRC_BIT, true, r->staging) != VK_SUCCESS) return fail("staging buffer");
     r->depth_texel = depth_texel_size(s->depth_format);
-    const uint64_t rb_bytes = static_cast<uint64_t>(s->width) * s->height * (4 + r->depth_texel);
+    r->colour_texel = colour_texel_size(s->color_format);
+    const uint64_t rb_bytes = static_cast<uint64_t>(s->width) * s->height * (r->colour_texel + r->depth_texel);
     if (make_buffer(c, rb_bytes, VK_BUFFER_USAGE_TRANSFER_DST_BIT, true, r->readback) != VK_SUCCESS) return fail("readback buffer");
     // CPVH_INDIRECT=1: the frame issues every draw as an indirect draw whose
     // record (VkDrawIndexedIndirectCommand / VkDrawIndirectCommand, 20-byte
@@ -1138,7 +1143,7 @@ int cpvh_render_e2e(cpvh_renderer* r, uint32_t frames, double* total_ms, uint64_
     cpvh_context* c = r->ctx;
     const cpv_scene* s = r->scene;
     const auto t0 = std::chrono::steady_clock::now();
-    const uint64_t out_bytes = static_cast<uint64_t>(s->width) * s->height * 4;
+    const uint64_t out_bytes = static_cast<uint64_t>(s->width) * s->height * r->colour_texel;
     std::vector<uint8_t> host_out(out_bytes);
     for (uint32_t i = 0; i < frames; i++) {
         // The inputs live in the staging buffer's host-visible (pinned)
@@ -1172,7 +1177,7 @@ int cpvh_readback(cpvh_renderer* r, uint8_t* color, uint8_t* depth) {
     void* map = nullptr;
     res = c->f.vkMapMemory(c->device, r->readback.memory, 0, VK_WHOLE_SIZE, 0, &map);
     if (res != VK_SUCCESS) return res;
-    const uint64_t cb = static_cast<uint64_t>(s->width) * s->height * 4;
+    const uint64_t cb = static_cast<uint64_t>(s->width) * s->height * r->colour_texel;
     if (color && s->color_format) std::memcpy(color, map, cb);
     else if (color) std::memset(color, 0, cb);  // a depth-only pass
     if (depth && s->depth_format) std::memcpy(depth, static_cast<uint8_t*>(map) + cb, static_cast<uint64_t>(s->width) * s->height * r->depth_texel);
@@ -1457,7 +1462,7 @@ int cpvh_image_ops(cpvh_context* c, uint32_t format, uint32_t width, uint32_t he
                    const cpvh_image_op* ops, uint32_t op_count, uint8_t* out, char* err, uint32_t err_len) {
     const Fns& f = c->f;
     const bool depth = depth_texel_size(format) != 0;
-    const uint32_t texel = depth ? depth_texel_size(format) : 4u;
+    const uint32_t texel = depth ? depth_texel_size(format) : colour_texel_size(format);
     const VkImageAspectFlags view_aspect = depth ? (format == VK_FORMAT_D32_SFLOAT_S8_UINT ? VK_IMAGE_ASPECT_DEPTH_BIT | VK_IMAGE_ASPECT_STENCIL_BIT
                                                                                              : VK_IMAGE_ASPECT_DEPTH_BIT)
                                                  : VK_IMAGE_ASPECT_COLOR_BIT;

@@ -655,18 +655,23 @@ uint32_t colour_attribute_bytes(uint32_t format) {
 // whole code range (half floats: any sign, exponents 0-15, so subnormals
 // and values up to 2). For the FETCH program the same parameter is the
 // value of the fragment shader's specialisation constant (0: none).
+// attachment_format != 0: the colour attachment's format (R8, R8G8, R16,
+// R16G16 UNORM, R8G8B8A8 SNORM, R16G16 or R32 SFLOAT), cleared to a colour
+// with channels outside [0, 1].
 void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant, uint32_t width, uint32_t height, uint32_t tris,
-                   uint32_t colour_format) {
+                   uint32_t colour_format, uint32_t attachment_format) {
     cpv_scene& s = st.scene;
     s.width = width;
     s.height = height;
     s.color_format = (variant & 0x200) ? VK_FORMAT_B8G8R8A8_UNORM : VK_FORMAT_R8G8B8A8_UNORM;
+    if (attachment_format) s.color_format = attachment_format;
     const bool depth_only = (variant & 0x40000000u) != 0;
     if (depth_only) s.color_format = 0;
     const uint32_t dsel = depth_only && ((variant >> 3) & 3) == 0 ? 2u : (variant >> 3) & 3;
     const uint32_t dfmts[4] = {0, VK_FORMAT_D16_UNORM, VK_FORMAT_D32_SFLOAT, VK_FORMAT_D32_SFLOAT_S8_UINT};
     s.depth_format = dfmts[dsel];
     s.clear_color[0] = 0.25f; s.clear_color[1] = 0.5f; s.clear_color[2] = 0.75f; s.clear_color[3] = 1.0f;
+    if (attachment_format) { s.clear_color[0] = -0.3f; s.clear_color[1] = 0.6f; s.clear_color[2] = 1.7f; s.clear_color[3] = 0.45f; }
     s.clear_depth = 0.75f;
     s.clear_stencil = 3;
     viewport_full(s);
@@ -905,7 +910,7 @@ cpv_scene* cpvh_scene_create(uint32_t config, uint64_t seed, const uint64_t* par
     case CPVH_PROGRAM:
         build_program(*st, seed, static_cast<uint32_t>(params && np > 0 ? params[0] : 0), static_cast<uint32_t>(params && np > 1 ? params[1] : 0),
                       static_cast<uint32_t>(param(2, 64)), static_cast<uint32_t>(param(3, 48)), static_cast<uint32_t>(param(4, 12)),
-                      static_cast<uint32_t>(param(5, 0)));
+                      static_cast<uint32_t>(param(5, 0)), static_cast<uint32_t>(param(6, 0)));
         break;
     case CPVH_SERVE: build_serve(*st, seed, static_cast<uint32_t>(param(0, 512)), static_cast<uint32_t>(param(1, 20000)), static_cast<uint32_t>(params && np > 2 ? params[2] : 0)); break;
     default: return nullptr;

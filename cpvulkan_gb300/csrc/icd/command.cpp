@@ -17,6 +17,50 @@
 
 namespace cpv::icd {
 
+// IEEE binary32 → binary16, round to nearest even (the encoder of half
+// colour channels; the device code restates the same steps).
+uint32_t float_to_half_host(float f) {
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    const uint32_t sign = (x >> 16) & 0x8000u;
+    const uint32_t e = (x >> 23) & 0xFFu, m = x & 0x7FFFFFu;
+    if (e == 0xFFu) return sign | 0x7C00u | (m ? (0x200u | (m >> 13)) : 0u);
+    const int32_t he = static_cast<int32_t>(e) - 112;
+    if (he >= 31) return sign | 0x7C00u;
+    if (he <= 0) {
+        if (he < -10) return sign;
+        const uint32_t mi = m | 0x800000u;
+        const uint32_t shift = static_cast<uint32_t>(14 - he);
+        uint32_t hm = mi >> shift;
+        const uint32_t rem = mi & ((1u << shift) - 1u), half = 1u << (shift - 1u);
+        if (rem > half || (rem == half && (hm & 1u))) hm++;
+        return sign | hm;
+    }
+    uint32_t r = sign | (static_cast<uint32_t>(he) << 10) | (m >> 13);
+    const uint32_t rem = m & 0x1FFFu;
+    if (rem > 0x1000u || (rem == 0x1000u && (r & 1u))) r++;
+    return r;
+}
+
+// One colour channel through the reference's encoder for the format's kind
+// (LLVMRuntime/ImageCompiler.cpp:1077-1185).
+uint32_t encode_channel_host(float x, const ColourLayout& cl) {
+    const uint32_t mask = cl.bits >= 32 ? 0xFFFFFFFFu : ((1u << cl.bits) - 1u);
+    switch (cl.kind) {
+    case 0: return encode_unorm_host(x, cl.bits == 8 ? 255.0f : 65535.0f);
+    case 1: {
+        float v = std::fmin(std::fmax(x, -1.0f), 1.0f) * (cl.bits == 8 ? 127.0f : 32767.0f);
+        v = std::round(v);
+        return static_cast<uint32_t>(static_cast<int32_t>(v)) & mask;
+    }
+    default:
+        if (cl.bits == 16) return float_to_half_host(x);
+        uint32_t b;
+        std::memcpy(&b, &x, 4);
+        return b;
+    }
+}
+
 uint32_t encode_unorm_host(float x, float maxv) {
     float v = x;
     if (v != v) v = 0.0f;  // maxnum(NaN, 0) = 0
@@ -127,16 +171,18 @@ uint8_t* view_base(const ImageView* v, uint32_t& width, uint32_t& height) {
 // without a clear encoding here.
 bool clear_texel(VkFormat fmt, const VkClearValue& cv, uint32_t& lo, uint32_t& hi) {
     lo = hi = 0;
-    switch (fmt) {
-    case VK_FORMAT_R8G8B8A8_UNORM:
-    case VK_FORMAT_B8G8R8A8_UNORM: {
+    ColourLayout cl;
+    if (colour_layout(fmt, cl)) {
+        // each channel through the format's encoder (UNORM, SNORM, half,
+        // float), at its bit offset; red in byte 2 for B8G8R8A8
         const int shift_bgra[4] = {16, 8, 0, 24};
-        for (int ch = 0; ch < 4; ch++) {
-            const uint32_t b = encode_unorm_host(cv.color.float32[ch], 255.0f);
-            lo |= b << (fmt == VK_FORMAT_B8G8R8A8_UNORM ? shift_bgra[ch] : 8 * ch);
+        for (uint32_t ch = 0; ch < cl.channels; ch++) {
+            const uint32_t field = encode_channel_host(cv.color.float32[ch], cl);
+            lo |= field << (cl.bgra ? shift_bgra[ch] : static_cast<int>(cl.bits * ch));
         }
         return true;
     }
+    switch (fmt) {
     case VK_FORMAT_D16_UNORM: lo = encode_unorm_host(cv.depthStencil.depth, 65535.0f); return true;
     case VK_FORMAT_D32_SFLOAT: std::memcpy(&lo, &cv.depthStencil.depth, 4); return true;
     case VK_FORMAT_D32_SFLOAT_S8_UINT:

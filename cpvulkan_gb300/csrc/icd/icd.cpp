@@ -26,17 +26,32 @@ namespace cpv::icd {
 uint32_t format_texel_size(VkFormat f) {
     switch (f) {
     case VK_FORMAT_R8_UNORM: case VK_FORMAT_R8_UINT: case VK_FORMAT_S8_UINT: return 1;
-    case VK_FORMAT_R8G8_UNORM: case VK_FORMAT_D16_UNORM: case VK_FORMAT_R16_UNORM: return 2;
+    case VK_FORMAT_R8G8_UNORM: case VK_FORMAT_D16_UNORM: case VK_FORMAT_R16_UNORM: case VK_FORMAT_R16_SFLOAT: return 2;
     case VK_FORMAT_D16_UNORM_S8_UINT: return 3;
     case VK_FORMAT_R8G8B8A8_UNORM: case VK_FORMAT_R8G8B8A8_SNORM: case VK_FORMAT_R8G8B8A8_UINT: case VK_FORMAT_R8G8B8A8_SINT:
     case VK_FORMAT_R8G8B8A8_SRGB: case VK_FORMAT_B8G8R8A8_UNORM: case VK_FORMAT_B8G8R8A8_SRGB: case VK_FORMAT_R32_UINT:
     case VK_FORMAT_R32_SINT: case VK_FORMAT_R32_SFLOAT: case VK_FORMAT_D32_SFLOAT: case VK_FORMAT_X8_D24_UNORM_PACK32:
-    case VK_FORMAT_D24_UNORM_S8_UINT:
+    case VK_FORMAT_D24_UNORM_S8_UINT: case VK_FORMAT_R16G16_UNORM: case VK_FORMAT_R16G16_SFLOAT:
         return 4;
     case VK_FORMAT_R32G32_UINT: case VK_FORMAT_R32G32_SINT: case VK_FORMAT_R32G32_SFLOAT: case VK_FORMAT_D32_SFLOAT_S8_UINT: return 8;
     case VK_FORMAT_R32G32B32_UINT: case VK_FORMAT_R32G32B32_SINT: case VK_FORMAT_R32G32B32_SFLOAT: return 12;
     case VK_FORMAT_R32G32B32A32_UINT: case VK_FORMAT_R32G32B32A32_SINT: case VK_FORMAT_R32G32B32A32_SFLOAT: return 16;
     default: return 0;
+    }
+}
+
+bool colour_layout(VkFormat f, ColourLayout& out) {
+    switch (f) {
+    case VK_FORMAT_R8G8B8A8_UNORM: out = {4, 4, 8, 0, false}; return true;
+    case VK_FORMAT_B8G8R8A8_UNORM: out = {4, 4, 8, 0, true}; return true;
+    case VK_FORMAT_R8_UNORM: out = {1, 1, 8, 0, false}; return true;
+    case VK_FORMAT_R8G8_UNORM: out = {2, 2, 8, 0, false}; return true;
+    case VK_FORMAT_R8G8B8A8_SNORM: out = {4, 4, 8, 1, false}; return true;
+    case VK_FORMAT_R16_UNORM: out = {2, 1, 16, 0, false}; return true;
+    case VK_FORMAT_R16G16_UNORM: out = {4, 2, 16, 0, false}; return true;
+    case VK_FORMAT_R16G16_SFLOAT: out = {4, 2, 16, 2, false}; return true;
+    case VK_FORMAT_R32_SFLOAT: out = {4, 1, 32, 2, false}; return true;
+    default: return false;
     }
 }
 
@@ -262,6 +277,13 @@ VKAPI_ATTR void VKAPI_CALL GetPhysicalDeviceQueueFamilyProperties(VkPhysicalDevi
 VKAPI_ATTR void VKAPI_CALL GetPhysicalDeviceFormatProperties(VkPhysicalDevice, VkFormat f, VkFormatProperties* p) {
     std::memset(p, 0, sizeof(*p));
     const uint32_t size = format_texel_size(f);
+    ColourLayout cl;
+    if (f != VK_FORMAT_R8G8B8A8_UNORM && f != VK_FORMAT_B8G8R8A8_UNORM && colour_layout(f, cl)) {
+        // colour attachments of the draw path (blending too: the blend is
+        // computed in float and encoded to the format)
+        p->linearTilingFeatures = p->optimalTilingFeatures = VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BIT | VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BLEND_BIT |
+                                                             VK_FORMAT_FEATURE_TRANSFER_SRC_BIT | VK_FORMAT_FEATURE_TRANSFER_DST_BIT;
+    }
     if (f == VK_FORMAT_R8G8B8A8_UNORM || f == VK_FORMAT_B8G8R8A8_UNORM) {
         p->linearTilingFeatures = p->optimalTilingFeatures = VK_FORMAT_FEATURE_SAMPLED_IMAGE_BIT | VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BIT |
                                                              VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BLEND_BIT | VK_FORMAT_FEATURE_TRANSFER_SRC_BIT |

@@ -343,6 +343,15 @@ std::array<uint8_t, 32> sha3_256(const void* data, size_t size);
 
 // Format helpers.
 uint32_t format_texel_size(VkFormat f);
+// Layout of a colour attachment format the draw path writes: bytes per
+// texel, channels, bits per channel, kind (0 UNORM, 1 SNORM, 2 SFLOAT) and
+// red in byte 2 (B8G8R8A8) — from the reference's format table
+// (CPVulkanBase/Formats.cpp). False for any other format.
+struct ColourLayout {
+    uint32_t bytes = 0, channels = 0, bits = 0, kind = 0;
+    bool bgra = false;
+};
+bool colour_layout(VkFormat f, ColourLayout& out);
 bool format_is_depth(VkFormat f);
 bool format_has_stencil(VkFormat f);
 void image_layout(Image& img);

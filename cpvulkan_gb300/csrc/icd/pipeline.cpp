@@ -48,7 +48,10 @@ std::string hex(const std::array<uint8_t, 32>& k) {
     return s;
 }
 
-bool supported_colour(VkFormat f) { return f == VK_FORMAT_R8G8B8A8_UNORM || f == VK_FORMAT_B8G8R8A8_UNORM; }
+bool supported_colour(VkFormat f) {
+    ColourLayout cl;
+    return colour_layout(f, cl);
+}
 bool supported_depth(VkFormat f) { return f == VK_FORMAT_D16_UNORM || f == VK_FORMAT_D32_SFLOAT || f == VK_FORMAT_D32_SFLOAT_S8_UINT; }
 
 // Per-pipeline macros of a stage block, undefined after its namespace so the
@@ -332,10 +335,13 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
         if (ci.pColorBlendState->attachmentCount >= 1) blend = ci.pColorBlendState->pAttachments[0];
         for (int i = 0; i < 4; i++) blend_constants[i] = ci.pColorBlendState->blendConstants[i];
         if (ci.pColorBlendState->logicOpEnable) {
-            // Both colour formats are UNORM, where a logic op applies; blending
-            // of the attachment is then treated as disabled (Vulkan 1.1,
-            // "Logical Operations"). The reference aborts here
-            // (LLVMRuntime/PipelineCompiler.cpp:1687-1690).
+            // A logic op applies to the encoded bits of a normalised 8-bit
+            // format; blending of the attachment is then treated as disabled
+            // (Vulkan 1.1, "Logical Operations"). The reference aborts here
+            // (LLVMRuntime/PipelineCompiler.cpp:1687-1690); formats of other
+            // widths and float formats are rejected.
+            ColourLayout cl;
+            if (!colour_layout(cfmt, cl) || cl.bits != 8 || cl.kind == 2) return reject("logic op on colour format " + std::to_string(cfmt));
             if (static_cast<uint32_t>(ci.pColorBlendState->logicOp) > VK_LOGIC_OP_SET) return reject("logic op " + std::to_string(ci.pColorBlendState->logicOp));
             logic = true;
             logic_op = static_cast<uint32_t>(ci.pColorBlendState->logicOp);
@@ -442,6 +448,14 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     src << "#define CPV_LOGIC " << (logic ? 1 : 0) << "\n";
     src << "#define CPV_LOGIC_OP " << logic_op << "\n";
     src << "#define CPV_COLOR_FORMAT " << static_cast<uint32_t>(cfmt) << "\n";
+    {
+        // the colour attachment's layout: texel bytes, channels, bits per
+        // channel, kind (0 UNORM, 1 SNORM, 2 SFLOAT), red in byte 2
+        ColourLayout cl;
+        if (cfmt != VK_FORMAT_UNDEFINED) colour_layout(cfmt, cl);
+        src << "#define CPV_CF_BYTES " << cl.bytes << "\n#define CPV_CF_CHANNELS " << cl.channels << "\n#define CPV_CF_BITS " << cl.bits
+            << "\n#define CPV_CF_KIND " << cl.kind << "\n#define CPV_CF_BGRA " << (cl.bgra ? 1 : 0) << "\n";
+    }
     src << "#define CPV_DEPTH_FORMAT " << static_cast<uint32_t>(dfmt) << "\n";
     src << "#define CPV_ORIGIN_UPPER " << (fr.origin_upper_left ? 1 : 0) << "\n";
     // A fragment shader that reads neither FragCoord nor FrontFacing and only
@@ -458,7 +472,8 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
         return f == VK_BLEND_FACTOR_DST_ALPHA || f == VK_BLEND_FACTOR_ONE_MINUS_DST_ALPHA || f == VK_BLEND_FACTOR_SRC_ALPHA_SATURATE;
     };
     const bool blend_table = fs_constant && blend.blendEnable && !dst_alpha_factor(blend.srcColorBlendFactor) &&
-                             !dst_alpha_factor(blend.dstColorBlendFactor);
+                             !dst_alpha_factor(blend.dstColorBlendFactor) &&
+                             (cfmt == VK_FORMAT_R8G8B8A8_UNORM || cfmt == VK_FORMAT_B8G8R8A8_UNORM);  // tables map RGBA8 bytes
     src << "#define CPV_BLEND_TABLE " << (blend_table ? 1 : 0) << "\n";
     src << vr.code << fr.code;
     src << "__device__ __forceinline__ int cpv_interp(int c) {\n  switch (c) {\n";

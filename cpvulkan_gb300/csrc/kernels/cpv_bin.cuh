@@ -407,7 +407,9 @@ extern "C" __global__ void __launch_bounds__(256) cpv_fill_rect(uint8_t* __restr
         uint8_t* row = base + static_cast<uint64_t>(y) * pitch;
         for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < w; x += gridDim.x * blockDim.x) {
             uint8_t* p = row + static_cast<uint64_t>(x) * texel_bytes;
-            if (texel_bytes == 2) {
+            if (texel_bytes == 1) {
+                *p = static_cast<uint8_t>(lo);
+            } else if (texel_bytes == 2) {
                 *reinterpret_cast<uint16_t*>(p) = static_cast<uint16_t>(lo);
             } else {
                 if (write_lo) *reinterpret_cast<uint32_t*>(p) = lo;

@@ -104,6 +104,32 @@ __device__ __forceinline__ float cpv_decode_norm(uint32_t raw, uint32_t size, bo
     return __fdiv_rn(__int2float_rn(v), size == 1u ? 127.0f : 32767.0f);
 }
 
+/* IEEE binary32 → binary16 rounded to nearest, ties to even (the
+ * reference's fptrunc of half attachments): overflow to infinity, gradual
+ * underflow through the subnormals, NaN kept quiet with its top payload
+ * bits. */
+__device__ __forceinline__ uint32_t cpv_float_to_half(float f) {
+    const uint32_t x = __float_as_uint(f);
+    const uint32_t sign = (x >> 16) & 0x8000u;
+    const uint32_t e = (x >> 23) & 0xFFu, m = x & 0x7FFFFFu;
+    if (e == 0xFFu) return sign | 0x7C00u | (m ? (0x200u | (m >> 13)) : 0u);
+    const int32_t he = static_cast<int32_t>(e) - 112;  /* the half's biased exponent */
+    if (he >= 31) return sign | 0x7C00u;
+    if (he <= 0) {
+        if (he < -10) return sign;  /* below half the smallest subnormal */
+        const uint32_t mi = m | 0x800000u;
+        const uint32_t shift = static_cast<uint32_t>(14 - he);
+        uint32_t hm = mi >> shift;
+        const uint32_t rem = mi & ((1u << shift) - 1u), half = 1u << (shift - 1u);
+        if (rem > half || (rem == half && (hm & 1u))) hm++;
+        return sign | hm;
+    }
+    uint32_t r = sign | (static_cast<uint32_t>(he) << 10) | (m >> 13);
+    const uint32_t rem = m & 0x1FFFu;
+    if (rem > 0x1000u || (rem == 0x1000u && (r & 1u))) r++;  /* a carry into the exponent is the correct rounding */
+    return r;
+}
+
 /* IEEE binary16 → binary32, exact (the reference widens half attributes
  * with fpext): zero, subnormal, normal, infinity; a NaN keeps its payload
  * and becomes quiet. */

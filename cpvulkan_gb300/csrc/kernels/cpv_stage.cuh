@@ -319,18 +319,69 @@ __device__ __forceinline__ void cpv_setup(const CpvDrawParams& P, uint64_t g, Cp
 
 #endif /* CPV_PRIM_KIND */
 
-/* Byte offset of channel i in the colour attachment texel
+/* The colour attachment's layout (from the reference's format table,
+ * CPVulkanBase/Formats.cpp): texel bytes, channels, bits per channel, kind
+ * (0 UNORM, 1 SNORM, 2 SFLOAT), red in byte 2. */
+#ifndef CPV_CF_BYTES
+#define CPV_CF_BYTES 4
+#define CPV_CF_CHANNELS 4
+#define CPV_CF_BITS 8
+#define CPV_CF_KIND 0
+#define CPV_CF_BGRA (CPV_COLOR_FORMAT == 44)
+#endif
+#define CPV_CF_MASK (CPV_CF_BITS >= 32 ? 0xFFFFFFFFu : ((1u << (CPV_CF_BITS & 31)) - 1u))
+
+/* Bit offset of channel i in the colour attachment texel
  * (CPVulkanBase/Formats.cpp:248,255). */
 __device__ __forceinline__ int cpv_channel_shift(int i) {
-#if CPV_COLOR_FORMAT == 44
+#if CPV_CF_BGRA
     return i == 0 ? 16 : (i == 1 ? 8 : (i == 2 ? 0 : 24));
 #else
-    return 8 * i;
+    return CPV_CF_BITS * i;
+#endif
+}
+
+/* Stored channel bits → float, the reference's pixel decoder
+ * (LLVMRuntime/ImageCompiler.cpp:161-230): UNORM and SNORM over their
+ * maximum (signed codes not clamped), half floats widened, 32-bit floats
+ * as stored. */
+__device__ __forceinline__ float cpv_cf_decode(uint32_t raw) {
+#if CPV_CF_KIND == 0 && CPV_CF_BITS == 8
+    return CPV_DECODE8(raw);
+#elif CPV_CF_KIND == 0
+    return cpv_decode_unorm16(raw);
+#elif CPV_CF_KIND == 1
+    return cpv_decode_norm(raw, CPV_CF_BITS / 8, true);
+#elif CPV_CF_BITS == 16
+    return cpv_half_to_float(raw);
+#else
+    return __uint_as_float(raw);
+#endif
+}
+
+/* Float → stored channel bits, the reference's colour encoder
+ * (LLVMRuntime/ImageCompiler.cpp:1077-1185): UNORM clamped to [0, 1] and
+ * SNORM to [-1, 1] (minnum / maxnum), scaled, rounded half away from zero;
+ * half floats rounded to nearest even; 32-bit floats as they are. */
+__device__ __forceinline__ uint32_t cpv_cf_encode(float x) {
+#if CPV_CF_KIND == 0
+    return cpv_encode_unorm(x, CPV_CF_BITS == 8 ? 255.0f : 65535.0f);
+#elif CPV_CF_KIND == 1
+    const float v = roundf(__fmul_rn(fminf(fmaxf(x, -1.0f), 1.0f), CPV_CF_BITS == 8 ? 127.0f : 32767.0f));
+    return static_cast<uint32_t>(static_cast<int32_t>(v)) & CPV_CF_MASK;
+#elif CPV_CF_BITS == 16
+    return cpv_float_to_half(x);
+#else
+    return __float_as_uint(x);
 #endif
 }
 
 __device__ __forceinline__ void cpv_load_pixel(const uint8_t* color, const uint8_t* depth, uint64_t pix, CpvPixel& s) {
-#if CPV_COLOR_FORMAT != 0
+#if CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 1
+    s.colour = color[pix];
+#elif CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 2
+    s.colour = reinterpret_cast<const uint16_t*>(color)[pix];
+#elif CPV_COLOR_FORMAT != 0
     s.colour = reinterpret_cast<const uint32_t*>(color)[pix];
 #else
     (void)color; /* a depth-only pass */
@@ -358,7 +409,11 @@ __device__ __forceinline__ void cpv_load_pixel(const uint8_t* color, const uint8
 }
 
 __device__ __forceinline__ void cpv_store_pixel(uint8_t* color, uint8_t* depth, uint64_t pix, const CpvPixel& s) {
-#if CPV_COLOR_FORMAT != 0
+#if CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 1
+    color[pix] = static_cast<uint8_t>(s.colour);
+#elif CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 2
+    reinterpret_cast<uint16_t*>(color)[pix] = static_cast<uint16_t>(s.colour);
+#elif CPV_COLOR_FORMAT != 0
     reinterpret_cast<uint32_t*>(color)[pix] = s.colour;
 #else
     (void)color;
@@ -572,12 +627,13 @@ __device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool fro
         (void)table;
 #endif
 #if CPV_LOGIC
+        /* 8-bit normalised formats only (pipeline creation rejects others) */
         (void)blend_constants;
         uint32_t logic = 0u;
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
+        for (int i = 0; i < CPV_CF_CHANNELS; i++) {
             const uint32_t d = (s.colour >> cpv_channel_shift(i)) & 0xFFu;
-            const uint32_t byte = ((CPV_WRITE_MASK >> i) & 1u) ? cpv_logic(cpv_encode_unorm(colour[i], 255.0f), d) : d;
+            const uint32_t byte = ((CPV_WRITE_MASK >> i) & 1u) ? (cpv_logic(cpv_cf_encode(colour[i]), d) & 0xFFu) : d;
             logic |= byte << cpv_channel_shift(i);
         }
         s.colour = logic;
@@ -585,20 +641,24 @@ __device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool fro
 #endif
         float out[4];
 #if CPV_BLEND
+        /* the destination as the reference's decoder returns it: absent
+         * channels read (0, 0, 0, 1) */
         float dst[4];
 #pragma unroll
-        for (int i = 0; i < 4; i++) dst[i] = CPV_DECODE8((s.colour >> cpv_channel_shift(i)) & 0xFFu);
+        for (int i = 0; i < 4; i++)
+            dst[i] = i < CPV_CF_CHANNELS ? cpv_cf_decode((s.colour >> cpv_channel_shift(i)) & CPV_CF_MASK) : (i == 3 ? 1.0f : 0.0f);
         cpv_blend(colour, dst, blend_constants, out);
 #else
         (void)blend_constants;
 #pragma unroll
         for (int i = 0; i < 4; i++) out[i] = colour[i];
 #endif
+        /* the format's channels, each encoded or, outside the write mask, kept */
         uint32_t packed = 0u;
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const uint32_t byte = ((CPV_WRITE_MASK >> i) & 1u) ? cpv_encode_unorm(out[i], 255.0f) : ((s.colour >> cpv_channel_shift(i)) & 0xFFu);
-            packed |= byte << cpv_channel_shift(i);
+        for (int i = 0; i < CPV_CF_CHANNELS; i++) {
+            const uint32_t field = ((CPV_WRITE_MASK >> i) & 1u) ? cpv_cf_encode(out[i]) : ((s.colour >> cpv_channel_shift(i)) & CPV_CF_MASK);
+            packed |= field << cpv_channel_shift(i);
         }
         s.colour = packed;
     }

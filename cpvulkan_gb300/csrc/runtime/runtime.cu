@@ -394,7 +394,7 @@ int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, 
 int fill_rect(cudaStream_t stream, uint8_t* base, uint64_t pitch, uint32_t w, uint32_t h, uint32_t texel_bytes, uint32_t lo, uint32_t hi, bool write_lo,
               bool write_hi) {
     if (!base || w == 0 || h == 0) return kOk;
-    if (texel_bytes != 2 && texel_bytes != 4 && texel_bytes != 8) return kErrInvalid;
+    if (texel_bytes != 1 && texel_bytes != 2 && texel_bytes != 4 && texel_bytes != 8) return kErrInvalid;
     if (reinterpret_cast<uintptr_t>(base) % texel_bytes != 0 || pitch % texel_bytes != 0 || pitch < static_cast<uint64_t>(w) * texel_bytes) return kErrInvalid;
     if (!write_lo && !(texel_bytes == 8 && write_hi)) return kOk;
     if (pitch == static_cast<uint64_t>(w) * texel_bytes && write_lo && (texel_bytes != 8 || write_hi))

@@ -25,7 +25,7 @@ enum cpvh_config {
     CPVH_HEIGHTFIELD = 2, /* textured heightfield (param0 = grid side, default 1024; param1/2 = width/height)   */
     CPVH_BLEND = 3,       /* blend-bound overdraw quads (param0 = quad count, default 200000; param1/2 = w/h; param3 = 1: colour per corner, interpolated) */
     CPVH_BATCH = 4,       /* 4096 icosphere draws (param0 = draw count, param1 = max triangles, param2/3 = w/h) */
-    CPVH_PROGRAM = 5,     /* small scene for one shader program (param0 = cpv_program, param1 = variant, param2/3 = w/h, param4 = triangles, param5 = colour attribute VkFormat of CUBE-family programs, or FETCH's specialisation constant) */
+    CPVH_PROGRAM = 5,     /* small scene for one shader program (param0 = cpv_program, param1 = variant, param2/3 = w/h, param4 = triangles, param5 = colour attribute VkFormat of CUBE-family programs, or FETCH's specialisation constant, param6 = colour attachment VkFormat, 0 for RGBA8/BGRA8 by variant) */
     CPVH_SERVE = 6        /* one serving request (param0 = side px, param1 = triangles, param2 = client id)     */
 };
 

@@ -525,22 +525,89 @@ void set_depth(uint8_t* texel, uint32_t fmt, float d) {
     }
 }
 
-/* Channel byte offsets (CPVulkanBase/Formats.cpp:248,255). */
-void colour_offsets(uint32_t fmt, int off[4]) {
-    if (fmt == FMT_B8G8R8A8_UNORM) { off[0] = 2; off[1] = 1; off[2] = 0; off[3] = 3; }
-    else { off[0] = 0; off[1] = 1; off[2] = 2; off[3] = 3; }
+/* A colour attachment format (CPVulkanBase/Formats.cpp): bytes per texel,
+ * channels, bytes per channel, kind (0 UNORM, 1 SNORM, 2 SFLOAT) and the
+ * byte offset of each channel (B8G8R8A8: Formats.cpp:248,255). False for
+ * formats the oracle does not write. */
+struct ColourFormat {
+    uint32_t bytes, channels, esize, kind;
+    int off[4];
+};
+bool colour_format(uint32_t fmt, ColourFormat& cf) {
+    switch (fmt) {
+    case FMT_R8G8B8A8_UNORM: cf = {4, 4, 1, 0, {0, 1, 2, 3}}; return true;
+    case FMT_B8G8R8A8_UNORM: cf = {4, 4, 1, 0, {2, 1, 0, 3}}; return true;
+    case 9: cf = {1, 1, 1, 0, {0, 0, 0, 0}}; return true;    /* R8_UNORM */
+    case 16: cf = {2, 2, 1, 0, {0, 1, 0, 0}}; return true;   /* R8G8_UNORM */
+    case 38: cf = {4, 4, 1, 1, {0, 1, 2, 3}}; return true;   /* R8G8B8A8_SNORM */
+    case 70: cf = {2, 1, 2, 0, {0, 0, 0, 0}}; return true;   /* R16_UNORM */
+    case 77: cf = {4, 2, 2, 0, {0, 2, 0, 0}}; return true;   /* R16G16_UNORM */
+    case 83: cf = {4, 2, 2, 2, {0, 2, 0, 0}}; return true;   /* R16G16_SFLOAT */
+    case 100: cf = {4, 1, 4, 2, {0, 0, 0, 0}}; return true;  /* R32_SFLOAT */
+    default: return false;
+    }
+}
+
+/* One stored channel → float: the reference's pixel decoder
+ * (LLVMRuntime/ImageCompiler.cpp:161-230): UNORM and SNORM divided by
+ * their type's maximum (SNORM not clamped), half floats widened through
+ * the compiler's own binary16 type, 32-bit floats as stored. */
+float decode_channel(const uint8_t* p, const ColourFormat& cf) {
+    uint32_t raw = 0;
+    std::memcpy(&raw, p, cf.esize);
+    if (cf.kind == 2) {
+        if (cf.esize == 2) {
+            _Float16 h;
+            const uint16_t r16 = static_cast<uint16_t>(raw);
+            std::memcpy(&h, &r16, 2);
+            return static_cast<float>(h);
+        }
+        float f;
+        std::memcpy(&f, &raw, 4);
+        return f;
+    }
+    if (cf.kind == 1) {
+        const int32_t v = cf.esize == 1 ? static_cast<int8_t>(raw) : static_cast<int16_t>(raw);
+        return static_cast<float>(v) / (cf.esize == 1 ? 127.0f : 32767.0f);
+    }
+    return cf.esize == 1 ? decode_unorm8(static_cast<uint8_t>(raw)) : decode_unorm16(static_cast<uint16_t>(raw));
+}
+
+/* float → stored channel: the reference's colour encoder
+ * (LLVMRuntime/ImageCompiler.cpp:1077-1185): UNORM and SNORM clamped with
+ * minnum / maxnum, scaled and rounded half away from zero; half floats by a
+ * round-to-nearest-even narrowing; 32-bit floats unchanged. */
+void encode_channel(float x, const ColourFormat& cf, uint8_t* p) {
+    uint32_t raw;
+    if (cf.kind == 0) {
+        raw = encode_unorm(x, cf.esize == 1 ? 255.0f : 65535.0f);
+    } else if (cf.kind == 1) {
+        const float v = std::round(minnum(maxnum(x, -1.0f), 1.0f) * (cf.esize == 1 ? 127.0f : 32767.0f));
+        raw = static_cast<uint32_t>(static_cast<int32_t>(v));
+    } else if (cf.esize == 2) {
+        const _Float16 h = static_cast<_Float16>(x);
+        uint16_t r16;
+        std::memcpy(&r16, &h, 2);
+        raw = r16;
+    } else {
+        std::memcpy(&raw, &x, 4);
+    }
+    std::memcpy(p, &raw, cf.esize);
 }
 
 void set_colour(uint8_t* texel, uint32_t fmt, const float c[4]) {
-    int off[4];
-    colour_offsets(fmt, off);
-    for (int i = 0; i < 4; i++) texel[off[i]] = static_cast<uint8_t>(encode_unorm(c[i], 255.0f));
+    ColourFormat cf;
+    if (!colour_format(fmt, cf)) return;
+    for (uint32_t i = 0; i < cf.channels; i++) encode_channel(c[i], cf, texel + cf.off[i]);
 }
 
+/* The texel as the reference decodes it; absent channels read 0, 0, 0, 1. */
 void get_colour(const uint8_t* texel, uint32_t fmt, float c[4]) {
-    int off[4];
-    colour_offsets(fmt, off);
-    for (int i = 0; i < 4; i++) c[i] = decode_unorm8(texel[off[i]]);
+    ColourFormat cf;
+    c[0] = c[1] = c[2] = 0.0f;
+    c[3] = 1.0f;
+    if (!colour_format(fmt, cf)) return;
+    for (uint32_t i = 0; i < cf.channels; i++) c[i] = decode_channel(texel + cf.off[i], cf);
 }
 
 /* Stencil compare / ops (LLVMRuntime/PipelineCompiler.cpp:1194-1223,
@@ -596,6 +663,7 @@ struct Frame {
     uint8_t* colour;
     uint8_t* depth;
     uint32_t depth_size;
+    uint32_t colour_size;  /* bytes per colour texel */
     Resources res;
     cpv_oracle_stats* stats;
     /* Rows this frame writes: y % row_stride == row_index (1, 0: all rows).
@@ -808,11 +876,15 @@ uint8_t logic_op(uint32_t op, uint8_t s, uint8_t d) {
  * (the reference aborts on a partial mask, PipelineCompiler.cpp:1693-1700;
  * this follows Vulkan 1.1, "Color Write Mask"). */
 void write_colour(uint8_t* texel, uint32_t fmt, const cpv_scene_pipeline& p, const float colour[4]) {
-    int off[4];
-    colour_offsets(fmt, off);
-    uint8_t bytes[4];
+    ColourFormat cf;
+    if (!colour_format(fmt, cf)) return;
+    uint8_t enc[4][4];
     if (p.logic_op_enable) {
-        for (int i = 0; i < 4; i++) bytes[i] = logic_op(p.logic_op, static_cast<uint8_t>(encode_unorm(colour[i], 255.0f)), texel[off[i]]);
+        /* 8-bit normalised formats only: the op on the encoded bytes */
+        for (uint32_t i = 0; i < cf.channels; i++) {
+            encode_channel(colour[i], cf, enc[i]);
+            enc[i][0] = logic_op(p.logic_op, enc[i][0], texel[cf.off[i]]);
+        }
     } else {
         float out[4];
         if (p.blend_enable) {
@@ -822,10 +894,10 @@ void write_colour(uint8_t* texel, uint32_t fmt, const cpv_scene_pipeline& p, con
         } else {
             for (int i = 0; i < 4; i++) out[i] = colour[i];
         }
-        for (int i = 0; i < 4; i++) bytes[i] = static_cast<uint8_t>(encode_unorm(out[i], 255.0f));
+        for (uint32_t i = 0; i < cf.channels; i++) encode_channel(out[i], cf, enc[i]);
     }
-    for (int i = 0; i < 4; i++)
-        if ((p.color_write_mask >> i) & 1u) texel[off[i]] = bytes[i];
+    for (uint32_t i = 0; i < cf.channels; i++)
+        if ((p.color_write_mask >> i) & 1u) std::memcpy(texel + cf.off[i], enc[i], cf.esize);
 }
 
 /* Interpolation (CPVulkan/CommandBuffer.Draw.cpp:816-871). */
@@ -894,7 +966,7 @@ void fragment(Frame& f, const cpv_scene_pipeline& p, uint32_t x, uint32_t y, flo
     }
 
     if (stencil_result && depth_result) {
-        if (s->color_format) write_colour(f.colour + pix * 4, s->color_format, p, colour);
+        if (s->color_format) write_colour(f.colour + pix * f.colour_size, s->color_format, p, colour);
         f.stats->fragments_written++;
     }
 }
@@ -1382,7 +1454,8 @@ void render_threaded(Frame& f, Shared& sh, uint32_t tid, uint32_t n, uint32_t en
 /* Checks a scene and fills the parts of `f` and `tex` every render needs. */
 int prepare(const cpv_scene* scene, uint8_t* color, uint8_t* depth, Frame& f, Texture& tex) {
     if (!scene || !color) return -1;
-    if (scene->color_format != FMT_R8G8B8A8_UNORM && scene->color_format != FMT_B8G8R8A8_UNORM && scene->color_format != 0) return -2;
+    ColourFormat cf{};
+    if (scene->color_format != 0 && !colour_format(scene->color_format, cf)) return -2;
     if (scene->color_format == 0 && scene->depth_format == 0) return -2;
     const uint32_t dsize = depth_texel_size(scene->depth_format);
     if (scene->depth_format != 0 && (dsize == 0 || !depth)) return -3;
@@ -1391,6 +1464,7 @@ int prepare(const cpv_scene* scene, uint8_t* color, uint8_t* depth, Frame& f, Te
     f.colour = color;
     f.depth = scene->depth_format ? depth : nullptr;
     f.depth_size = dsize;
+    f.colour_size = cf.bytes;
     if (scene->texture_data) {
         tex.data = scene->texture_data;
         tex.bytes = scene->texture_bytes;
@@ -1423,7 +1497,7 @@ void clear(const Frame& f) {
     const cpv_scene* scene = f.s;
     const uint64_t pixels = static_cast<uint64_t>(scene->width) * scene->height;
     if (scene->color_format)  // a depth-only pass leaves `color` untouched
-        for (uint64_t i = 0; i < pixels; i++) set_colour(f.colour + i * 4, scene->color_format, scene->clear_color);
+        for (uint64_t i = 0; i < pixels; i++) set_colour(f.colour + i * f.colour_size, scene->color_format, scene->clear_color);
     if (f.depth) {
         for (uint64_t i = 0; i < pixels; i++) {
             uint8_t* t = f.depth + i * f.depth_size;

@@ -54,10 +54,10 @@ class Oracle:
 
     def render(self, scene, draw_begin=0, draw_end=None, color=None, depth=None, clear=True):
         """Renders a cpvulkan_gb300.Scene; returns (color HxWx4 u8, depth HxWxB u8 or None, stats dict)."""
-        from cpvulkan_gb300 import depth_texel_bytes
+        from cpvulkan_gb300 import colour_texel_bytes, depth_texel_bytes
         h, w = scene.height, scene.width
         dsz = depth_texel_bytes(scene.depth_format)
-        color = np.zeros((h, w, 4), np.uint8) if color is None else color
+        color = np.zeros((h, w, colour_texel_bytes(scene.color_format)), np.uint8) if color is None else color
         if dsz and depth is None:
             depth = np.zeros((h, w, dsz), np.uint8)
         st = Stats()
@@ -72,12 +72,12 @@ class Oracle:
     def render_threaded(self, scene, threads=None, draw_begin=0, draw_end=None, color=None, depth=None, clear=True):
         """render() on `threads` host threads (default: every usable core);
         the image is identical to render()'s."""
-        from cpvulkan_gb300 import depth_texel_bytes
+        from cpvulkan_gb300 import colour_texel_bytes, depth_texel_bytes
         if threads is None:
             threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
         h, w = scene.height, scene.width
         dsz = depth_texel_bytes(scene.depth_format)
-        color = np.zeros((h, w, 4), np.uint8) if color is None else color
+        color = np.zeros((h, w, colour_texel_bytes(scene.color_format)), np.uint8) if color is None else color
         if dsz and depth is None:
             depth = np.zeros((h, w, dsz), np.uint8)
         st = Stats()

@@ -42,3 +42,34 @@ def compare(scene, gpu_color, gpu_depth, ref_color, ref_depth):
         assert report["depth_max_ulp"] <= depth_tol, report
     assert report["color_max_lsb"] <= COLOR_LSB, report
     return report
+
+
+def unorm(x, bits):
+    """numpy restatement of the UNORM encoder: clamp to [0, 1] (NaN → 0),
+    scale in float32, round half away from zero."""
+    m = np.float32(2 ** bits - 1)
+    v = np.clip(np.nan_to_num(np.asarray(x, np.float32), nan=0.0), 0, 1).astype(np.float32) * m
+    return np.floor(v + np.float32(0.5)).astype(np.int64)
+
+
+def snorm(x, bits):
+    """numpy restatement of the SNORM encoder: clamp to [-1, 1], scale in
+    float32, round half away from zero."""
+    m = np.float32(2 ** (bits - 1) - 1)
+    v = np.clip(np.asarray(x, np.float32), -1, 1).astype(np.float32) * m
+    return (np.sign(v) * np.floor(np.abs(v) + np.float32(0.5))).astype(np.int64)
+
+
+def encode_colour(fmt, colour):
+    """The texel bytes of an RGBA float colour in a colour attachment format."""
+    x = np.asarray(colour, np.float32)
+    if fmt in (37, 44):
+        b = unorm(x, 8).astype(np.uint8)
+        return b[[2, 1, 0, 3]] if fmt == 44 else b
+    return np.frombuffer({9: lambda: unorm(x[:1], 8).astype(np.uint8).tobytes(),
+                          16: lambda: unorm(x[:2], 8).astype(np.uint8).tobytes(),
+                          38: lambda: snorm(x, 8).astype(np.int8).tobytes(),
+                          70: lambda: unorm(x[:1], 16).astype(np.uint16).tobytes(),
+                          77: lambda: unorm(x[:2], 16).astype(np.uint16).tobytes(),
+                          83: lambda: x[:2].astype(np.float16).tobytes(),
+                          100: lambda: x[:1].tobytes()}[fmt](), np.uint8)

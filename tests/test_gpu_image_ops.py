@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 import cpvulkan_gb300 as c
+from tests.parity import encode_colour
 
 pytestmark = pytest.mark.gpu
 
@@ -126,4 +127,27 @@ def test_clear_attachments(gpu_ctx, oracle, fmt):
             level_view(want, lv[0], texel)[0:20, 40:48, 4:] = ds_texel(oracle, fmt, 0.5, 77)[4:]
         else:
             level_view(want, lv[0], texel)[0:20, 40:48] = ds_texel(oracle, fmt, 0.5, 77)
+    assert np.array_equal(out, want)
+
+
+# Colour formats beyond RGBA8/BGRA8: 1-, 2- and 4-byte texels, UNORM, SNORM
+# and float channels, each through the format's own encoder.
+OTHER_COLOUR = [9, 16, 38, 70, 77, 83, 100]
+
+
+@pytest.mark.parametrize("fmt", OTHER_COLOUR)
+def test_clear_other_colour_formats(gpu_ctx, fmt):
+    texel = c.colour_texel_bytes(fmt)
+    rng = np.random.default_rng(6)
+    levels, (w, h) = 3, (37, 23)
+    lv, total = chain(w, h, levels, texel)
+    init = rng.integers(0, 256, total, dtype=np.uint8)
+    a, b = (-0.3, 0.6, 1.7, 0.45), (0.1234, -1.5, 0.5, 0.25)
+    out = gpu_ctx.image_ops(fmt, (w, h), levels, init, [
+        dict(kind=c.OP_CLEAR_COLOR_IMAGE, aspect=COLOR, level=1, level_count=REMAINING, colour=a),
+        dict(kind=c.OP_CLEAR_ATTACHMENTS, aspect=COLOR, level=0, x=3, y=2, w=9, h=5, colour=b)])
+    want = init.copy()
+    for l in (1, 2):
+        level_view(want, lv[l], texel)[:] = encode_colour(fmt, a)
+    level_view(want, lv[0], texel)[2:7, 3:12] = encode_colour(fmt, b)
     assert np.array_equal(out, want)

@@ -220,3 +220,39 @@ def test_fetch_program_batched(gpu_ctx, oracle, monkeypatch):
     scene = c.Scene(c.PROGRAM, 3, [c.PROGRAM_FETCH, 0x20, 64, 48, 24, 9])
     report, _ = check(gpu_ctx, oracle, scene)
     assert report["color_pixels_differing"] == 0, report
+
+
+# Colour attachments beyond RGBA8/BGRA8 (parameter 6): R8, R8G8, R16, R16G16
+# UNORM, R8G8B8A8 SNORM, R16G16 and R32 SFLOAT, cleared to a colour outside
+# [0, 1]; opaque, blended (destination alpha 1 where the format has none),
+# blended under a partial write mask, wide lines and flat quads. The colour
+# attribute is half-float with channels in [-2, 2], so the encoders clamp.
+COLOUR_ATTACHMENTS = [9, 16, 38, 70, 77, 83, 100]
+COLOUR_VARIANTS = [(c.PROGRAM_CUBE, 0x10), (c.PROGRAM_CUBE, 0x10 | 0x20), (c.PROGRAM_CUBE, 0x10 | 0x20 | 0x80000 | (0x5 << 24)),
+                   (c.PROGRAM_CUBE, 0x10000 | 0x400 | 0x20000 | 0x20), (c.PROGRAM_FLATQUAD, 0x20)]
+
+
+@pytest.mark.parametrize("fmt", COLOUR_ATTACHMENTS)
+@pytest.mark.parametrize("program,variant", COLOUR_VARIANTS)
+@pytest.mark.parametrize("seed", [1, 2])
+def test_colour_attachment_formats(gpu_ctx, oracle, fmt, program, variant, seed):
+    scene = c.Scene(c.PROGRAM, seed, [program, variant, 64, 48, 24, 97, fmt])
+    report, stats = check(gpu_ctx, oracle, scene)
+    assert stats["fragments_written"] > 0
+    assert report["color_pixels_differing"] == 0, report
+
+
+@pytest.mark.parametrize("fmt", [9, 16, 38])
+@pytest.mark.parametrize("op", [3, 6, 12])
+def test_colour_attachment_logic_ops(gpu_ctx, oracle, fmt, op):
+    scene = c.Scene(c.PROGRAM, 4, [c.PROGRAM_CUBE, 0x10 | 0x40000 | (op << 20) | 0x80000 | (0xB << 24), 64, 48, 24, 97, fmt])
+    report, _ = check(gpu_ctx, oracle, scene)
+    assert report["color_pixels_differing"] == 0, report
+
+
+@pytest.mark.parametrize("fmt", [9, 38, 83, 100])
+def test_colour_attachment_formats_batched(gpu_ctx, oracle, monkeypatch, fmt):
+    monkeypatch.setenv("CPV_BATCH_MIN_DRAWS", "1")
+    scene = c.Scene(c.PROGRAM, 3, [c.PROGRAM_CUBE, 0x10 | 0x20, 64, 48, 24, 97, fmt])
+    report, _ = check(gpu_ctx, oracle, scene)
+    assert report["color_pixels_differing"] == 0, report

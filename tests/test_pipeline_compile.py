@@ -215,3 +215,37 @@ def test_secondary_command_buffers_record_batched_pass(native, monkeypatch, tmp_
     finally:
         ctx.close()
     assert glob.glob(str(dump / "batch_*.cu"))
+
+
+COLOUR_ATTACHMENTS = [(9, 1, 1, 8, 0), (16, 2, 2, 8, 0), (38, 4, 4, 8, 1), (70, 2, 1, 16, 0), (77, 4, 2, 16, 0), (83, 4, 2, 16, 2),
+                      (100, 4, 1, 32, 2)]
+
+
+@pytest.mark.parametrize("fmt,nbytes,channels,bits,kind", COLOUR_ATTACHMENTS)
+@pytest.mark.parametrize("variant", [0x10, 0x20 | 0x80000 | (0x5 << 24)])
+def test_colour_attachment_formats_compile(compile_ctx, fmt, nbytes, channels, bits, kind, variant):
+    """A colour attachment in any of the draw path's formats compiles with
+    the format's layout: texel bytes, channels, bits per channel and kind
+    (0 UNORM, 1 SNORM, 2 SFLOAT); blending never takes the RGBA8 tables."""
+    ctx, dump = compile_ctx
+    ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [c.PROGRAM_FLATQUAD, variant, 32, 32, 4, 0, fmt]))
+    (path,) = glob.glob(str(dump / "pipeline_*.cu"))
+    text = open(path).read()
+    for name, value in (("BYTES", nbytes), ("CHANNELS", channels), ("BITS", bits), ("KIND", kind)):
+        assert "#define CPV_CF_%s %d\n" % (name, value) in text
+    assert "#define CPV_BLEND_TABLE 0\n" in text
+
+
+@pytest.mark.parametrize("fmt", [70, 77, 83, 100])
+def test_logic_op_on_wide_colour_format_rejected(compile_ctx, fmt):
+    """A logic op is accepted on 8-bit normalised colour attachments only."""
+    ctx, _ = compile_ctx
+    with pytest.raises(RuntimeError, match="logic op on colour format"):
+        ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [c.PROGRAM_CUBE, 0x40000 | (6 << 20), 32, 32, 4, 0, fmt]))
+
+
+def test_logic_op_on_8bit_colour_formats_compiles(compile_ctx):
+    ctx, dump = compile_ctx
+    for fmt in (9, 16, 38):
+        ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [c.PROGRAM_CUBE, 0x40000 | (6 << 20), 32, 32, 4, 0, fmt]))
+    assert len(glob.glob(str(dump / "pipeline_*.cu"))) == 3
