@@ -63,6 +63,7 @@ const char* const kStageMacros[] = {
     "CPV_BLEND", "CPV_SRC_COLOR", "CPV_DST_COLOR", "CPV_COLOR_OP", "CPV_SRC_ALPHA", "CPV_DST_ALPHA", "CPV_ALPHA_OP", "CPV_WRITE_MASK", "CPV_LOGIC", "CPV_LOGIC_OP",
     "CPV_DEPTH_BOUNDS", "CPV_MIN_DEPTH_BOUNDS", "CPV_MAX_DEPTH_BOUNDS",
     "CPV_COLOR_FORMAT", "CPV_DEPTH_FORMAT", "CPV_ORIGIN_UPPER", "CPV_FS_CONSTANT", "CPV_BLEND_TABLE", "CPV_LINE_WIDTH", "CPV_PRIM_KIND",
+    "CPV_CF_BYTES", "CPV_CF_CHANNELS", "CPV_CF_BITS", "CPV_CF_KIND", "CPV_CF_BGRA", "CPV_FS_KILL", "CPV_EARLY_DEPTH",
 };
 
 }  // namespace
@@ -464,6 +465,7 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     bool fs_constant = !fr.reads_frag_coord && !fr.reads_front_facing;
     for (int k : fr.interp) fs_constant = fs_constant && k == 2;
     src << "#define CPV_FS_CONSTANT " << (fs_constant ? 1 : 0) << "\n";
+    src << "#define CPV_FS_KILL " << (fr.has_kill ? 1 : 0) << "\n";
     // Blending a per-primitive constant colour where each channel's result
     // depends only on that channel of the destination (no DST_ALPHA,
     // ONE_MINUS_DST_ALPHA or SRC_ALPHA_SATURATE colour factors): the result

@@ -88,10 +88,11 @@ struct CpvBatchSource {
         cpv_dispatch(pid, [&](auto S) { decltype(S)::template setup<true>(B.draws[d], local, t); });
         cpv_tri_tag(t, pid, d);
     }
-    __device__ __forceinline__ bool shade(const CpvTri& t, const float w[3], int32_t x, int32_t y, float colour[4], float& mapped) const {
+    __device__ __forceinline__ bool shade(const CpvTri& t, const float w[3], int32_t x, int32_t y, float colour[4], float& mapped,
+                                          const CpvPixel* early = nullptr) const {
         bool discard = false;
         const CpvDrawParams& P = B.draws[cpv_tri_draw(t)];
-        cpv_dispatch(cpv_tri_pipeline(t), [&](auto S) { discard = decltype(S)::shade(P, t, w, x, y, colour, mapped); });
+        cpv_dispatch(cpv_tri_pipeline(t), [&](auto S) { discard = decltype(S)::shade(P, t, w, x, y, colour, mapped, early); });
         return discard;
     }
     __device__ __forceinline__ void rop(const CpvTri& t, const float colour[4], float mapped, CpvPixel& s) const {

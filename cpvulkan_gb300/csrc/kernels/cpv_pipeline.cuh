@@ -99,8 +99,9 @@ struct CpvPlainSource {
         }
         cpv_p0::Stage::setup<true>(P, g, t);
     }
-    __device__ __forceinline__ bool shade(const CpvTri& t, const float w[3], int32_t x, int32_t y, float colour[4], float& mapped) const {
-        return cpv_p0::Stage::shade(P, t, w, x, y, colour, mapped);
+    __device__ __forceinline__ bool shade(const CpvTri& t, const float w[3], int32_t x, int32_t y, float colour[4], float& mapped,
+                                          const CpvPixel* early = nullptr) const {
+        return cpv_p0::Stage::shade(P, t, w, x, y, colour, mapped, early);
     }
     __device__ __forceinline__ void rop(const CpvTri& t, const float colour[4], float mapped, CpvPixel& s) const {
         cpv_p0::Stage::rop(P.blend_constants, cpv_tri_front(t), colour, mapped, s, cpv_p0::Stage::table(P, t));

@@ -206,6 +206,35 @@ __device__ __forceinline__ bool cpv_may_cover(const CpvTri& t, int32_t rx0, int3
     return may;
 }
 
+/* Whether triangle t covers every pixel of the rectangle [rx0, rx1) x
+ * [ry0, ry1): by the monotonicity cpv_may_cover uses, each edge function's
+ * smallest value over the rectangle is at the corner picked by the signs of
+ * dy and dx, and a pixel whose value is not negative passes that edge.
+ * Exact in the other direction: true only when the coverage test passes at
+ * every pixel (a NaN corner value, a non-finite coefficient or a line's
+ * fourth edge gives false, and the pixels are then tested one by one). */
+__device__ __forceinline__ bool cpv_must_cover(const CpvTri& t, int32_t rx0, int32_t ry0, int32_t rx1, int32_t ry1, const float* col,
+                                               const float* row, int32_t tile_x0, int32_t tile_y0) {
+#if CPV_ANY_LINES
+    if (((__float_as_uint(t.wf.w) >> 6) & 3u) == 3u) return false;
+#endif
+    const float c0 = col[rx0 - tile_x0], c1 = col[rx1 - 1 - tile_x0];
+    const float r0 = row[ry0 - tile_y0], r1 = row[ry1 - 1 - tile_y0];
+    const float xa = fminf(c0, c1), xb = fmaxf(c0, c1), ya = fminf(r0, r1), yb = fmaxf(r0, r1);
+    if (!(fabsf(c0) <= 3.4e38f && fabsf(c1) <= 3.4e38f && fabsf(r0) <= 3.4e38f && fabsf(r1) <= 3.4e38f)) return false;
+    bool must = true;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float4 e = t.e[k];
+        if (!(fabsf(e.x) <= 3.4e38f && fabsf(e.y) <= 3.4e38f && fabsf(e.z) <= 3.4e38f && fabsf(e.w) <= 3.4e38f)) return false;
+        const float xf = e.w > 0.0f ? xa : xb;
+        const float yf = e.z > 0.0f ? yb : ya;
+        const float w = __fsub_rn(__fmul_rn(__fsub_rn(xf, e.x), e.w), __fmul_rn(__fsub_rn(yf, e.y), e.z));
+        must = must && w >= 0.0f;
+    }
+    return must;
+}
+
 /* ---- per-fragment operation helpers (LLVMRuntime/PipelineCompiler.cpp:1020-1429) ---- */
 
 __device__ __forceinline__ bool cpv_fcompare(float a, float b, uint32_t op) {
@@ -381,7 +410,9 @@ __device__ __forceinline__ void cpv_list_small(const CpvTri& t, uint32_t j, int3
  * Source supplies:
  *   uint64_t count()                         primitives of this tile
  *   void setup(uint64_t i, CpvTri& t)        set up the i-th (or mark it dead)
- *   bool shade(const CpvTri&, const float w[3], int x, int y, float colour[4], float& mapped)
+ *   bool shade(const CpvTri&, const float w[3], int x, int y, float colour[4], float& mapped, const CpvPixel* early)
+ *                                            (true: discarded, or failed the early depth
+ *                                            test against *early when given)
  *   void rop(const CpvTri&, const float colour[4], float mapped, CpvPixel&)
  *   bool table_fragment(const CpvTri&, CpvPixel&)  a covered fragment applied by a
  *                                            blend-table lookup alone (false: use shade + rop)
@@ -463,8 +494,9 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
 #endif
 
 #if CPV_WARP_LISTS
-    /* immediate schedule: per warp, the batch's primitives reaching its rows */
-    __shared__ uint8_t warp_list[(CPV_RT_THREADS / 32) * CPV_BATCH];
+    /* immediate schedule: per warp, the batch's primitives reaching its rows
+     * (batch index; bit 15: the primitive covers the warp's whole block) */
+    __shared__ uint16_t warp_list[(CPV_RT_THREADS / 32) * CPV_BATCH];
 #if CPV_WARP_BLOCKS
     const int32_t warp_x0 = static_cast<int32_t>(tx * CPV_TILE + ((threadIdx.x >> 5) % (CPV_TILE / CPV_BLOCK_W)) * CPV_BLOCK_W);
     const int32_t warp_y0 = static_cast<int32_t>(ty * CPV_TILE + ((threadIdx.x >> 5) / (CPV_TILE / CPV_BLOCK_W)) * CPV_BLOCK_H);
@@ -549,7 +581,7 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
                         const CpvTri& t = tris[j];
                         float w[3], colour[4], mapped;
                         cpv_covers(t, xf[k], yf[k], w);
-                        if (src.shade(t, w, px[k], py[k], colour, mapped)) continue;
+                        if (src.shade(t, w, px[k], py[k], colour, mapped, &st[k])) continue;
                         src.rop(t, colour, mapped, st[k]);
                     }
                 } else {
@@ -561,7 +593,7 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
                         if (px[k] < box.x || px[k] >= box.z || py[k] < box.y || py[k] >= box.w) continue;
                         float w[3], colour[4], mapped;
                         if (!cpv_covers(t, xf[k], yf[k], w)) continue;
-                        if (src.shade(t, w, px[k], py[k], colour, mapped)) continue;
+                        if (src.shade(t, w, px[k], py[k], colour, mapped, &st[k])) continue;
                         src.rop(t, colour, mapped, st[k]);
                     }
                 }
@@ -580,11 +612,12 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
         if (immediate_batch) {
 #if CPV_WARP_LISTS
             const uint32_t lane = threadIdx.x & 31u;
-            uint8_t* mine = warp_list + (threadIdx.x >> 5) * CPV_BATCH;
+            uint16_t* mine = warp_list + (threadIdx.x >> 5) * CPV_BATCH;
             uint32_t count = 0;
             for (uint32_t b = 0; b < n; b += 32u) {
                 const uint32_t j = b + lane;
                 bool hit = false;
+                uint32_t full = 0u;
                 if (j < n && cpv_tri_live(tris[j])) {
                     const CpvTri& t = tris[j];
                     const int4 box = t.box;
@@ -593,6 +626,11 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
                     const int32_t rx0 = max(box.x, warp_x0), rx1 = min(box.z, warp_x0 + CPV_BLOCK_W);
                     const int32_t ry0 = max(box.y, warp_y0), ry1 = min(box.w, warp_y0 + CPV_BLOCK_H);
                     hit = rx1 > rx0 && ry1 > ry0 && cpv_may_cover(t, rx0, ry0, rx1, ry1, col_ndc, row_ndc, tile_x0, tile_y0);
+                    /* a block inside the box (so inside the attachment) and
+                     * inside every edge: its pixels skip the box and edge tests */
+                    if (hit && rx0 == warp_x0 && rx1 == warp_x0 + CPV_BLOCK_W && ry0 == warp_y0 && ry1 == warp_y0 + CPV_BLOCK_H &&
+                        cpv_must_cover(t, rx0, ry0, rx1, ry1, col_ndc, row_ndc, tile_x0, tile_y0))
+                        full = 0x8000u;
 #else
                     const int32_t rx0 = max(box.x, tile_x0), rx1 = min(box.z, tile_x0 + CPV_TILE);
 #pragma unroll
@@ -605,7 +643,7 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
 #endif
                 }
                 const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, hit);
-                if (hit) mine[count + __popc(ballot & ((1u << lane) - 1u))] = static_cast<uint8_t>(j);
+                if (hit) mine[count + __popc(ballot & ((1u << lane) - 1u))] = static_cast<uint16_t>(j | full);
                 count += __popc(ballot);
             }
             __syncwarp();
@@ -614,7 +652,20 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
 #endif
             for (uint32_t m = 0; m < count; m++) {
 #if CPV_WARP_LISTS
-                const uint32_t j = mine[m];
+                const uint32_t entry = mine[m];
+                const uint32_t j = entry & 0x7FFFu;
+#if CPV_WARP_BLOCKS
+                if (entry & 0x8000u) {
+                    /* the whole block is covered (one pixel a thread, all inside) */
+                    const CpvTri& t = tris[j];
+                    if (src.table_fragment(t, st[0])) continue;
+                    float w[3], colour[4], mapped;
+                    cpv_covers(t, xf[0], yf[0], w);
+                    if (src.shade(t, w, px[0], py[0], colour, mapped, &st[0])) continue;
+                    src.rop(t, colour, mapped, st[0]);
+                    continue;
+                }
+#endif
 #else
                 const uint32_t j = m;
                 if (!cpv_tri_live(tris[j])) continue;
@@ -629,7 +680,7 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
                     if (!cpv_covers(t, xf[k], yf[k], w)) continue;
                     if (src.table_fragment(t, st[k])) continue;
                     float colour[4], mapped;
-                    if (src.shade(t, w, px[k], py[k], colour, mapped)) continue;
+                    if (src.shade(t, w, px[k], py[k], colour, mapped, &st[k])) continue;
                     src.rop(t, colour, mapped, st[k]);
                 }
             }

@@ -452,13 +452,26 @@ __device__ __forceinline__ void cpv_blend(const float s[4], const float d[4], co
     if (CPV_COLOR_OP != CPV_ALPHA_OP) out[3] = cpv_blend_op(s[3], sf[3], d[3], df[3], CPV_ALPHA_OP);
 }
 
+/* Early depth test. The fragment shader has no effect but its colour and
+ * its discard (no storage writes, no FragDepth), so when it cannot discard
+ * and no stencil test runs, a triangle fragment that fails the depth test
+ * against the pixel's current depth changes nothing whatever its colour:
+ * with the depth (the same arithmetic as below) known, the varyings and the
+ * shader are skipped for it. The depth test, depth write and colour write
+ * then run unchanged in cpv_rop for the fragments that pass. */
+#ifndef CPV_FS_KILL
+#define CPV_FS_KILL 1
+#endif
+#define CPV_EARLY_DEPTH (CPV_PRIM_KIND == 0 && CPV_DEPTH_TEST && CPV_DEPTH_FORMAT != 0 && !(CPV_STENCIL_TEST && CPV_DEPTH_FORMAT == 130) && !CPV_FS_KILL)
+
 /* Shading of one covered pixel: barycentrics (w_k / area), screen-linear
  * depth, varyings (perspective Σ w·v/p ÷ Σ w/p, linear Σ w·v, or flat from
  * the provoking vertex; CPVulkan/CommandBuffer.Draw.cpp:816-954), viewport
  * depth mapping (:1300-1313) and the fragment shader. Returns true when the
- * shader discards. */
+ * shader discards, or when `early` (the pixel's current state) is given and
+ * the fragment fails the early depth test. */
 __device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& t, const float wr[3], int32_t x, int32_t y, float colour[4],
-                                          float& mapped) {
+                                          float& mapped, const CpvPixel* early = nullptr) {
     float in[CPV_NV_ALLOC];
 #if CPV_PRIM_KIND == 2
     /* a point's fragments take its vertex's outputs as they are and its NDC z
@@ -502,6 +515,14 @@ __device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& 
     w[1] = __fdiv_rn(wr[1], area);
     w[2] = __fdiv_rn(wr[2], area);
     const float depth = __fadd_rn(__fadd_rn(__fmul_rn(t.za.x, w[0]), __fmul_rn(t.za.y, w[1])), __fmul_rn(t.za.z, w[2]));
+#if CPV_EARLY_DEPTH
+    if (early) {
+        const float early_mapped = __fadd_rn(__fmul_rn(__fsub_rn(P.viewport[5], P.viewport[4]), depth), P.viewport[4]);
+        if (!cpv_fcompare(early_mapped, early->depth, CPV_DEPTH_OP)) return true;
+    }
+#else
+    (void)early;
+#endif
     const float pw[3] = {t.wf.x, t.wf.y, t.wf.z};
     const uint32_t pslot = cpv_tri_pslot(t);
 #pragma unroll
@@ -708,8 +729,8 @@ struct Stage {
     template <bool WITH_VARYINGS>
     static __device__ __forceinline__ void setup(const CpvDrawParams& P, uint64_t g, CpvTri& t) { cpv_setup<WITH_VARYINGS>(P, g, t); }
     static __device__ __forceinline__ bool shade(const CpvDrawParams& P, const CpvTri& t, const float w[3], int32_t x, int32_t y, float colour[4],
-                                                 float& mapped) {
-        return cpv_shade(P, t, w, x, y, colour, mapped);
+                                                 float& mapped, const CpvPixel* early = nullptr) {
+        return cpv_shade(P, t, w, x, y, colour, mapped, early);
     }
     static __device__ __forceinline__ void rop(const float blend_constants[4], bool front, const float colour[4], float mapped, CpvPixel& s,
                                                const uint8_t* table = nullptr) {
