@@ -308,7 +308,7 @@ def run_reference(args, world, rank, dist):
 
 
 PLAIN_KERNELS = ("cpv_raster", "cpv_setup_rects", "cpv_span_count", "cpv_scan", "cpv_span_write", "cpv_blend_tables")
-BATCH_KERNELS = ("cpv_batch", "cpv_batch_setup", "cpv_batch_bin", "cpv_batch_raster")
+BATCH_KERNELS = ("cpv_batch", "cpv_batch_vs", "cpv_batch_setup", "cpv_batch_bin", "cpv_batch_raster")
 
 # Workloads measured beside the headline frame in the default run:
 # (name, harness config, scene parameters, environment, description).

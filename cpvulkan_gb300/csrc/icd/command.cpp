@@ -668,6 +668,9 @@ void build_batch(Queue* q, const CommandBuffer* cb, size_t begin, size_t end, co
         }
         in.draws.push_back(P);
         in.pipeline.push_back(static_cast<uint32_t>(it - pipelines.begin()));
+        const VkPrimitiveTopology topo = s.pipeline->topology;
+        in.triangles.push_back(topo == VK_PRIMITIVE_TOPOLOGY_TRIANGLE_LIST || topo == VK_PRIMITIVE_TOPOLOGY_TRIANGLE_STRIP ||
+                               topo == VK_PRIMITIVE_TOPOLOGY_TRIANGLE_FAN);
         return true;
     };
     size_t next_indirect = 0;

@@ -27,6 +27,30 @@
 #ifndef CPV_BATCH_CUH
 #define CPV_BATCH_CUH
 
+/* Floats of vertex outputs per vertex slot (a multiple of 4, so that every
+ * slot's outputs start on a 16-byte boundary). */
+#define CPV_VS_STRIDE (((CPV_NV_MAX) + 3) & ~3)
+
+/* Vertex stage: one thread per vertex slot of every draw that has slots —
+ * vertex id vs_lo + v of local instance i, shaded once per frame for the
+ * set-up and raster kernels that follow (cpv_setup reads the slot instead of
+ * shading the vertex again for each triangle and tile that uses it). */
+extern "C" __global__ void __launch_bounds__(CPV_BATCH_BLOCK) cpv_batch_vs(const __grid_constant__ CpvBatchParams B) {
+    cpv_lut8_init();  /* a vertex shader may sample images */
+    __syncthreads();
+    const uint32_t block = blockIdx.x;
+    const uint32_t d = B.vs_block_draw[block];
+    const CpvDrawParams& P = B.draws[d];
+    /* the host gives a draw slots only when vs_count * instances < 2^32 */
+    const uint32_t local = (block - B.vs_draw_block[d]) * CPV_BATCH_BLOCK + threadIdx.x;
+    const uint32_t count = P.vs_count;
+    const uint32_t instances = P.instance_count > 1u ? P.instance_count : 1u;
+    if (count == 0u || local >= count * instances) return;
+    const uint32_t inst = local / count;
+    const uint32_t v = local - inst * count;
+    cpv_dispatch(B.draw_pipeline[d], [&](auto S) { decltype(S)::vertex(P, P.vs_lo + v, P.first_instance + inst, local); });
+}
+
 extern "C" __global__ void __launch_bounds__(CPV_BATCH_BLOCK) cpv_batch_setup(const __grid_constant__ CpvBatchParams B) {
     __shared__ uint32_t warp_pairs[CPV_BATCH_BLOCK / 32];
     cpv_lut8_init();  /* a vertex shader may sample images */
@@ -136,3 +160,4 @@ extern "C" __global__ void __launch_bounds__(CPV_RT_THREADS, CPV_RT_MIN_BLOCKS) 
 
 extern "C" __device__ const uint32_t cpv_raster_smem_bytes = CPV_RASTER_SMEM_BYTES;
 extern "C" __device__ const uint32_t cpv_raster_threads = CPV_RT_THREADS;
+extern "C" __device__ const uint32_t cpv_vs_stride = CPV_VS_STRIDE;

@@ -260,6 +260,48 @@ extern "C" __global__ void __launch_bounds__(256) cpv_batch_emit(const uint2* __
     }
 }
 
+/* Vertex-stage sizing: one CTA per draw d with want[d] set finds the
+ * smallest and largest index value the draw reads inside its bound index
+ * buffer (indices outside the buffer read as 0 and are not counted; the
+ * set-up shades any vertex outside the found range itself). Writes
+ * range[d] = (min, max), or (0xFFFFFFFF, 0) when there is none. */
+extern "C" __global__ void __launch_bounds__(256) cpv_index_range(const CpvDrawParams* __restrict__ draws, const uint8_t* __restrict__ want,
+                                                                  uint2* __restrict__ range) {
+    __shared__ uint32_t smin[8], smax[8];
+    const uint32_t d = blockIdx.x;
+    uint32_t lo = 0xFFFFFFFFu, hi = 0u;
+    if (want[d]) {
+        const CpvDrawParams& P = draws[d];
+        const uint32_t size = P.index_size;
+        for (uint32_t i = threadIdx.x; i < P.count; i += 256u) {
+            const uint64_t off = (static_cast<uint64_t>(P.first) + i) * size;
+            if (size == 0u || off + size > P.ib_bytes) continue;
+            const uint32_t v = size == 2u ? static_cast<uint32_t>(__ldg(reinterpret_cast<const uint16_t*>(P.ib + off)))
+                                          : __ldg(reinterpret_cast<const uint32_t*>(P.ib + off));
+            lo = v < lo ? v : lo;
+            hi = v > hi ? v : hi;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint32_t a = __shfl_xor_sync(0xFFFFFFFFu, lo, o), b = __shfl_xor_sync(0xFFFFFFFFu, hi, o);
+        lo = a < lo ? a : lo;
+        hi = b > hi ? b : hi;
+    }
+    if ((threadIdx.x & 31u) == 0u) {
+        smin[threadIdx.x >> 5] = lo;
+        smax[threadIdx.x >> 5] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < 8; w++) {
+            lo = smin[w] < lo ? smin[w] : lo;
+            hi = smax[w] > hi ? smax[w] : hi;
+        }
+        range[d] = make_uint2(lo, hi);
+    }
+}
+
 /* Contiguous item range of CTA c of `ctas` over n items. */
 __device__ __forceinline__ void cpv_cta_range(uint32_t n, uint32_t c, uint32_t ctas, uint32_t& begin, uint32_t& end) {
     const uint32_t per = (n + ctas - 1u) / ctas;

@@ -94,6 +94,17 @@ struct CpvDrawParams {
     /* per primitive 4 x 256 bytes: the blend result of each channel for each
      * destination byte (pipelines blending a constant colour; null: compute) */
     uint8_t* tables;
+    /* vertex slots of the batched path's vertex stage: vertex ids
+     * [vs_lo, vs_lo + vs_count) of every instance, shaded once per frame
+     * (slot = local instance * vs_count + id - vs_lo). vs_pos holds NDC x, y,
+     * z and clip w per slot, vs_var vs_stride floats of outputs per slot.
+     * vs_count 0: no slots, the set-up shades its vertices itself. */
+    float* vs_pos;
+    float* vs_var;
+    uint32_t vs_lo;
+    uint32_t vs_count;
+    uint32_t vs_stride;
+    uint32_t pad2;
 };
 
 /* Primitives per set-up block of the batched path: every draw of a batch
@@ -133,6 +144,12 @@ struct CpvBatchParams {
      * (x / vw + (1 / vw) * 0.5) * 2 - 1, each operation rounded once */
     const float* ndc_x;
     const float* ndc_y;
+    /* vertex stage: draw d owns vertex blocks [vs_draw_block[d],
+     * vs_draw_block[d+1]) of CPV_BATCH_BLOCK slots each */
+    const uint32_t* vs_draw_block;
+    const uint32_t* vs_block_draw;
+    uint32_t vs_blocks;
+    uint32_t pad1;
 };
 
 #endif /* CPV_PARAMS_H */

@@ -283,9 +283,10 @@ __device__ __forceinline__ void cpv_setup_tri(const CpvDrawParams& P, const floa
 /* A triangle's instance and its three raw assembled vertices after the CW
  * swap (CPVulkan/CommandBuffer.Draw.cpp:567-760, 1532-1535), and the slot of
  * the provoking vertex among them. */
-__device__ __forceinline__ void cpv_tri_vertices(const CpvDrawParams& P, uint32_t g32, uint32_t raw[3], uint32_t& instance, uint32_t& pslot) {
+__device__ __forceinline__ void cpv_tri_vertices(const CpvDrawParams& P, uint32_t g32, uint32_t raw[3], uint32_t& instance, uint32_t& pslot,
+                                                 uint32_t& inst) {
     const uint32_t ppi = P.prims_per_instance;
-    const uint32_t inst = P.instance_count > 1u ? g32 / ppi : 0u;
+    inst = P.instance_count > 1u ? g32 / ppi : 0u;
     instance = P.first_instance + inst;
     const uint32_t p = g32 - inst * ppi;
     uint32_t provoking;
@@ -298,23 +299,63 @@ __device__ __forceinline__ void cpv_tri_vertices(const CpvDrawParams& P, uint32_
 
 /* Primitive set-up: vertex shading of the three vertices, perspective divide,
  * screen bounding box, area, facing and cull. `g` is the primitive index
- * within the draw (all instances). */
+ * within the draw (all instances). A vertex with a slot of the vertex stage
+ * (cpv_vertex_slot) is read from it instead of being shaded again: the slot
+ * holds what cpv_vertex_ndc returns for the same vertex id and instance,
+ * computed by the same function, so the bits are the same. */
 template <bool WITH_VARYINGS>
 __device__ __forceinline__ void cpv_setup(const CpvDrawParams& P, uint64_t g, CpvTri& t) {
     const uint32_t g32 = static_cast<uint32_t>(g);  /* draws hold < 2^32 primitives */
-    uint32_t raw[3], instance, pslot;
-    cpv_tri_vertices(P, g32, raw, instance, pslot);
+    uint32_t raw[3], instance, pslot, inst;
+    cpv_tri_vertices(P, g32, raw, instance, pslot, inst);
+    const uint32_t vs_count = P.vs_count;
     float Pn[3][4];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        float var[CPV_NV_ALLOC];
-        cpv_vertex_ndc(P, cpv_vertex_id(P, raw[k]), instance, Pn[k], var);
-        if (WITH_VARYINGS) {
+        const uint32_t vid = cpv_vertex_id(P, raw[k]);
+        const uint32_t rel = vid - P.vs_lo;
+        if (rel < vs_count) {
+            const uint64_t slot = static_cast<uint64_t>(inst) * vs_count + rel;
+            const float4 p = __ldg(reinterpret_cast<const float4*>(P.vs_pos) + slot);
+            Pn[k][0] = p.x;
+            Pn[k][1] = p.y;
+            Pn[k][2] = p.z;
+            Pn[k][3] = p.w;
+            if (WITH_VARYINGS) {
+                const float4* v = reinterpret_cast<const float4*>(P.vs_var + slot * P.vs_stride);
 #pragma unroll
-            for (int c = 0; c < CPV_NV; c++) t.var[k][c] = var[c];
+                for (int q = 0; q < (CPV_NV + 3) / 4; q++) {
+                    const float4 f = __ldg(v + q);
+                    const float fs[4] = {f.x, f.y, f.z, f.w};
+#pragma unroll
+                    for (int c = 0; c < 4; c++)
+                        if (4 * q + c < CPV_NV) t.var[k][4 * q + c] = fs[c];
+                }
+            }
+        } else {
+            float var[CPV_NV_ALLOC];
+            cpv_vertex_ndc(P, vid, instance, Pn[k], var);
+            if (WITH_VARYINGS) {
+#pragma unroll
+                for (int c = 0; c < CPV_NV; c++) t.var[k][c] = var[c];
+            }
         }
     }
     cpv_setup_tri<WITH_VARYINGS>(P, Pn, pslot, g32, t);
+}
+
+/* The vertex stage of the batched path: shades vertex id `vid` of
+ * `instance` once and stores its NDC position and clip w, and its outputs,
+ * in slot `slot` of P's vertex slots. */
+__device__ __forceinline__ void cpv_vertex_slot(const CpvDrawParams& P, uint32_t vid, uint32_t instance, uint64_t slot) {
+    float Pn[4], var[((CPV_NV_ALLOC + 3) / 4) * 4];
+    cpv_vertex_ndc(P, vid, instance, Pn, var);
+    reinterpret_cast<float4*>(P.vs_pos)[slot] = make_float4(Pn[0], Pn[1], Pn[2], Pn[3]);
+    float4* v = reinterpret_cast<float4*>(P.vs_var + slot * P.vs_stride);
+#pragma unroll
+    for (int q = 0; q < (CPV_NV + 3) / 4; q++)
+        v[q] = make_float4(var[4 * q], 4 * q + 1 < CPV_NV ? var[4 * q + 1] : 0.0f, 4 * q + 2 < CPV_NV ? var[4 * q + 2] : 0.0f,
+                           4 * q + 3 < CPV_NV ? var[4 * q + 3] : 0.0f);
 }
 
 #endif /* CPV_PRIM_KIND */
@@ -728,6 +769,15 @@ __device__ __forceinline__ void cpv_apply_table(const uint8_t* table, CpvPixel& 
 struct Stage {
     template <bool WITH_VARYINGS>
     static __device__ __forceinline__ void setup(const CpvDrawParams& P, uint64_t g, CpvTri& t) { cpv_setup<WITH_VARYINGS>(P, g, t); }
+    /* the vertex stage (triangle topologies only; the host gives other
+     * draws no slots) */
+    static __device__ __forceinline__ void vertex(const CpvDrawParams& P, uint32_t vid, uint32_t instance, uint64_t slot) {
+#if CPV_PRIM_KIND == 0
+        cpv_vertex_slot(P, vid, instance, slot);
+#else
+        (void)P; (void)vid; (void)instance; (void)slot;
+#endif
+    }
     static __device__ __forceinline__ bool shade(const CpvDrawParams& P, const CpvTri& t, const float w[3], int32_t x, int32_t y, float colour[4],
                                                  float& mapped, const CpvPixel* early = nullptr) {
         return cpv_shade(P, t, w, x, y, colour, mapped, early);

@@ -254,7 +254,8 @@ int load(const std::vector<uint8_t>& cubin, uint32_t tile_shift, bool batched, M
     bool ok;
     if (batched)
         ok = cudaLibraryGetKernel(&out.setup_rects, lib, "cpv_batch_setup") == cudaSuccess &&
-             cudaLibraryGetKernel(&out.raster, lib, "cpv_batch_raster") == cudaSuccess;
+             cudaLibraryGetKernel(&out.raster, lib, "cpv_batch_raster") == cudaSuccess &&
+             cudaLibraryGetKernel(&out.vertex, lib, "cpv_batch_vs") == cudaSuccess && module_u32(lib, "cpv_vs_stride", out.vs_stride);
     else
         ok = cudaLibraryGetKernel(&out.setup_rects, lib, "cpv_setup_rects") == cudaSuccess &&
              cudaLibraryGetKernel(&out.raster, lib, "cpv_raster") == cudaSuccess &&
@@ -571,6 +572,10 @@ BatchPlan::~BatchPlan() {
     dev_free(tile_end_);
     dev_free(words_);
     dev_free(ndc_);
+    dev_free(vs_pos_);
+    dev_free(vs_var_);
+    dev_free(vs_draw_block_);
+    dev_free(vs_block_draw_);
     if (pinned_pairs_) cudaFreeHost(pinned_pairs_);
 }
 
@@ -701,9 +706,15 @@ int BatchPlan::build(const Module& m, const BatchDraws& in, cudaStream_t stream)
     P_.ndc_x = ndc_;
     P_.ndc_y = ndc_ + in.fb_width;
 
-    // One set-up run to size the pair buffers.
+    if ((r = build_vertex_stage(m, in, stream)) != kOk) return r;
+
+    // One set-up run (after the vertex stage it reads) to size the pair buffers.
     if (blocks) {
         void* args[] = {&P_};
+        if (P_.vs_blocks) {
+            CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.vertex), dim3(P_.vs_blocks), dim3(CPV_BATCH_BLOCK), args, 0, stream));
+            count_launch();
+        }
         CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.setup_rects), dim3(static_cast<unsigned>(blocks)), dim3(CPV_BATCH_BLOCK), args, 0, stream));
         count_launch();
         if ((r = scan_u32(stream, block_pairs_, block_offsets_, blocks, words_, scan_)) != kOk) return r;
@@ -718,6 +729,131 @@ int BatchPlan::build(const Module& m, const BatchDraws& in, cudaStream_t stream)
     return alloc_pairs(static_cast<uint32_t>(cap));
 }
 
+// The vertex stage: every vertex id of a triangle draw's range, of every
+// instance, is shaded once per frame into a slot (NDC position and clip w,
+// then the outputs), which the set-up and raster kernels read instead of
+// shading the vertex for each triangle and each tile that uses it. A draw
+// gets slots when its pipeline assembles triangles and its vertex ids form a
+// range no wider than twice its primitives per instance plus 2 (an icosphere
+// or a grid uses each vertex in about six triangles; a non-indexed triangle
+// list uses each once and is left to the set-up). For an indexed draw the
+// range is that of the index values it reads now; a vertex outside it (the
+// indices rewritten later) is shaded by the set-up itself, so slots change
+// no result. CPV_VERTEX_STAGE=0 turns the stage off.
+int BatchPlan::build_vertex_stage(const Module& m, const BatchDraws& in, cudaStream_t stream) {
+    const uint32_t n = static_cast<uint32_t>(in.draws.size());
+    vs_slots_ = 0;
+    P_.vs_blocks = 0;
+    if (!m.vertex || !env_u32("CPV_VERTEX_STAGE", 1u) || in.triangles.size() != n) return kOk;
+    std::vector<uint8_t> want(n, 0);
+    bool any_indexed = false;
+    for (uint32_t d = 0; d < n; d++) {
+        if (in.triangles[d] && in.draws[d].total_prims && in.draws[d].index_size) {
+            want[d] = 1;
+            any_indexed = true;
+        }
+    }
+    std::vector<uint2> range(n, make_uint2(0xFFFFFFFFu, 0u));
+    if (any_indexed) {
+        uint8_t* want_d = nullptr;
+        uint2* range_d = nullptr;
+        int r;
+        if ((r = dev_alloc(want_d, n)) != kOk) return r;
+        if ((r = dev_alloc(range_d, n)) != kOk) {
+            dev_free(want_d);
+            return r;
+        }
+        bool ok = cudaMemcpyAsync(want_d, want.data(), n, cudaMemcpyHostToDevice, stream) == cudaSuccess;
+        if (ok) {
+            cpv_index_range<<<n, 256, 0, stream>>>(draws_, want_d, range_d);
+            count_launch();
+            ok = cudaGetLastError() == cudaSuccess &&
+                 cudaMemcpyAsync(range.data(), range_d, n * sizeof(uint2), cudaMemcpyDeviceToHost, stream) == cudaSuccess &&
+                 cudaStreamSynchronize(stream) == cudaSuccess;
+        }
+        dev_free(want_d);
+        dev_free(range_d);
+        if (!ok) {
+            cudaGetLastError();
+            set_last_error("batch plan: index range pass failed");
+            return kErrCuda;
+        }
+    }
+    const uint32_t trim = env_u32("CPV_VS_TRIM", 0u);
+    std::vector<uint32_t> lo(n, 0), count(n, 0);
+    std::vector<uint64_t> base(n, 0);
+    uint64_t total = 0, blocks = 0;
+    std::vector<uint32_t> draw_block(n + 1, 0);
+    for (uint32_t d = 0; d < n; d++) {
+        const CpvDrawParams& P = in.draws[d];
+        uint64_t c = 0;
+        uint32_t l = 0;
+        if (in.triangles[d] && P.total_prims) {
+            if (P.index_size == 0u) {
+                l = P.first;
+                c = P.count;
+            } else if (range[d].x <= range[d].y) {
+                l = static_cast<uint32_t>(P.vertex_offset) + range[d].x;
+                c = static_cast<uint64_t>(range[d].y) - range[d].x + 1u;
+            }
+        }
+        // CPV_VS_TRIM narrows every range by that many ids at each end
+        // (tests of the set-up shading the vertices outside a range).
+        if (trim) {
+            if (c > 2ull * trim) {
+                l += trim;
+                c -= 2ull * trim;
+            } else {
+                c = 0;
+            }
+        }
+        const uint64_t inst = P.instance_count > 1u ? P.instance_count : 1u;
+        if (c > 2ull * P.prims_per_instance + 2u || c * inst >= (1ull << 32)) c = 0;
+        lo[d] = l;
+        count[d] = static_cast<uint32_t>(c);
+        base[d] = total;
+        total += c * inst;
+        draw_block[d] = static_cast<uint32_t>(blocks);
+        blocks += (c * inst + CPV_BATCH_BLOCK - 1) / CPV_BATCH_BLOCK;
+    }
+    draw_block[n] = static_cast<uint32_t>(blocks);
+    const uint64_t stride = m.vs_stride;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return kOk;
+    }
+    if (total == 0 || blocks >= (1ull << 31) || total * (16u + 4u * stride) > free_b / 2) return kOk;  // no slots: the set-up shades
+    std::vector<uint32_t> block_draw(blocks);
+    for (uint32_t d = 0; d < n; d++)
+        for (uint32_t b = draw_block[d]; b < draw_block[d + 1]; b++) block_draw[b] = d;
+    if (dev_alloc(vs_pos_, total * 4u) != kOk || (stride && dev_alloc(vs_var_, total * stride) != kOk) ||
+        dev_alloc(vs_draw_block_, n + 1) != kOk || dev_alloc(vs_block_draw_, blocks) != kOk) {
+        dev_free(vs_pos_);
+        dev_free(vs_var_);
+        dev_free(vs_draw_block_);
+        dev_free(vs_block_draw_);
+        return kOk;  // no slots: the set-up shades
+    }
+    std::vector<CpvDrawParams> draws = in.draws;
+    for (uint32_t d = 0; d < n; d++) {
+        if (!count[d]) continue;
+        draws[d].vs_pos = vs_pos_ + 4u * base[d];
+        draws[d].vs_var = stride ? vs_var_ + stride * base[d] : nullptr;
+        draws[d].vs_lo = lo[d];
+        draws[d].vs_count = count[d];
+        draws[d].vs_stride = static_cast<uint32_t>(stride);
+    }
+    CPV_CUDA(cudaMemcpy(draws_, draws.data(), n * sizeof(CpvDrawParams), cudaMemcpyHostToDevice));
+    CPV_CUDA(cudaMemcpy(vs_draw_block_, draw_block.data(), (n + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    CPV_CUDA(cudaMemcpy(vs_block_draw_, block_draw.data(), blocks * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    P_.vs_draw_block = vs_draw_block_;
+    P_.vs_block_draw = vs_block_draw_;
+    P_.vs_blocks = static_cast<uint32_t>(blocks);
+    vs_slots_ = total;
+    return kOk;
+}
+
 int BatchPlan::enqueue(const Module& m, cudaStream_t stream) {
     const uint32_t blocks = P_.total_blocks;
     const uint64_t before = launches();
@@ -728,6 +864,12 @@ int BatchPlan::enqueue(const Module& m, cudaStream_t stream) {
     // Profile markers (only when profiling, which also bypasses the graph).
     {
         void* args[] = {&P_};
+        if (P_.vs_blocks) {
+            profile_begin(stream, "cpv_batch_vs");
+            CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.vertex), dim3(P_.vs_blocks), dim3(CPV_BATCH_BLOCK), args, 0, stream));
+            profile_end(stream);
+            count_launch();
+        }
         profile_begin(stream, "cpv_batch_setup");
         CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.setup_rects), dim3(blocks), dim3(CPV_BATCH_BLOCK), args, 0, stream));
         profile_end(stream);

@@ -39,6 +39,8 @@ struct Module {
     cudaKernel_t setup_rects = nullptr;
     cudaKernel_t raster = nullptr;
     cudaKernel_t blend_tables = nullptr;  // per-draw modules
+    cudaKernel_t vertex = nullptr;        // batched modules: the vertex stage
+    uint32_t vs_stride = 0;               // batched modules: output floats per vertex slot
     bool blend_table = false;             // the pipeline blends a per-primitive constant colour
     bool batched = false;
     uint32_t tile_shift = 4;
@@ -125,6 +127,7 @@ int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& s
 struct BatchDraws {
     std::vector<CpvDrawParams> draws;
     std::vector<uint32_t> pipeline;
+    std::vector<uint8_t> triangles;  // per draw: the pipeline assembles triangles (the vertex stage applies)
     uint8_t* color = nullptr;
     uint8_t* depth = nullptr;
     uint32_t fb_width = 0, fb_height = 0;
@@ -149,11 +152,14 @@ public:
     int launch(const Module& m, cudaStream_t stream);
     uint64_t primitives() const { return prims_; }
     uint32_t kernels_per_launch() const { return kernels_; }
+    // Vertex slots of the vertex stage (0 when no draw has any).
+    uint64_t vertex_slots() const { return vs_slots_; }
 
 private:
     int enqueue(const Module& m, cudaStream_t stream);
     int alloc_pairs(uint32_t capacity);
     void free_pairs();
+    int build_vertex_stage(const Module& m, const BatchDraws& in, cudaStream_t stream);
 
     CpvBatchParams P_{};
     Scratch scan_;
@@ -173,6 +179,11 @@ private:
     uint32_t* tile_end_ = nullptr;
     uint32_t* words_ = nullptr;         // [0] pair total, [1] status, [2] tile counter
     float* ndc_ = nullptr;              // pixel-centre NDC of the columns, then the rows
+    float* vs_pos_ = nullptr;           // vertex stage: NDC position and clip w per slot
+    float* vs_var_ = nullptr;           // vertex stage: outputs per slot
+    uint32_t* vs_draw_block_ = nullptr;
+    uint32_t* vs_block_draw_ = nullptr;
+    uint64_t vs_slots_ = 0;
     uint32_t* pinned_pairs_ = nullptr;  // pair total of the last launch (host)
     cudaEvent_t done_ = nullptr;
     uint64_t prims_ = 0;

@@ -137,3 +137,56 @@ def test_large_single_draw_runs_batched(gpu_ctx, oracle, plain, monkeypatch):
         same(g, ref)
     ocol, odep, _ = oracle.render(scene)
     assert compare(scene, got[-1][0], got[-1][1], ocol, odep)["color_pixels_differing"] == 0
+
+
+def _profiled_launches(name, fn):
+    import ctypes
+    icd = ctypes.CDLL(c.ICD_PATH)
+    icd.cpv_profile_get.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_double)]
+    icd.cpv_profile_reset()
+    icd.cpv_profile_enable(1)
+    try:
+        out = fn()
+    finally:
+        icd.cpv_profile_enable(0)
+    n, ms = ctypes.c_uint64(0), ctypes.c_double(0.0)
+    icd.cpv_profile_get(name.encode(), ctypes.byref(n), ctypes.byref(ms))
+    return out, n.value
+
+
+@pytest.mark.parametrize("trim", ["0", "1", "7"])
+def test_vertex_stage(gpu_ctx, plain, monkeypatch, trim):
+    """The vertex stage shades each vertex of an indexed triangle draw once
+    per frame into slots that the set-up and raster kernels read. With the
+    ranges narrowed (CPV_VS_TRIM), the vertices outside them are shaded by
+    the set-up itself, in the same triangles as slot vertices: every frame
+    must still equal the per-draw path's, and the stage must have run."""
+    monkeypatch.setenv("CPV_VS_TRIM", trim)
+    scene = c.Scene(c.BATCH, 8, [48, 3000, 400, 240])
+    ref = plain(gpu_ctx, scene)[0]
+    runs, n = _profiled_launches("cpv_batch_vs", lambda: frames(gpu_ctx, scene, 2))
+    assert n >= 2
+    for got in runs:
+        same(got, ref)
+
+
+def test_vertex_stage_off_and_textured_grid(gpu_ctx, plain, monkeypatch):
+    """CPV_VERTEX_STAGE=0 gives the same frames without the stage; a
+    textured heightfield grid (each vertex in six triangles, texture
+    coordinates and normals as outputs) through the stage equals the
+    per-draw path."""
+    scene = c.Scene(c.BATCH, 9, [24, 2000, 320, 200])
+    ref = plain(gpu_ctx, scene)[0]
+    monkeypatch.setenv("CPV_VERTEX_STAGE", "0")
+    runs, n = _profiled_launches("cpv_batch_vs", lambda: frames(gpu_ctx, scene, 2))
+    assert n == 0
+    for got in runs:
+        same(got, ref)
+    monkeypatch.setenv("CPV_VERTEX_STAGE", "1")
+    monkeypatch.setenv("CPV_BATCH_MIN_PRIMS", "20000")
+    grid = c.Scene(c.HEIGHTFIELD, 4, [160, 480, 270])
+    ref = plain(gpu_ctx, grid)[0]
+    runs, n = _profiled_launches("cpv_batch_vs", lambda: frames(gpu_ctx, grid, 2))
+    assert n >= 2
+    for got in runs:
+        same(got, ref)
