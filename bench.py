@@ -348,6 +348,15 @@ def kernel_profile(h, icd, r, names, frames):
     return out
 
 
+def batch_stats(icd):
+    """Primitives, vertex-stage slots and (primitive, tile) pairs of the
+    last completed batched frame (cpv_batch_stats)."""
+    import ctypes
+    out = (ctypes.c_uint64 * 3)()
+    icd.cpv_batch_stats(out)
+    return {"primitives": out[0], "vertex_slots": out[1], "pairs": out[2]}
+
+
 def roofline_of(name, scene, kernels, frag_written):
     """HBM roofline of the frame's dominant raster kernel: algorithmic bytes
     per launch over its CUDA-event time, against the measured copy
@@ -387,6 +396,7 @@ def measure_workload(ctx, h, icd, name, cfg, params, env, desc, min_seconds=1.5)
             launches = icd.cpv_kernel_launches() - l0
             clock_info = clocks.stop()
             kernels = kernel_profile(h, icd, r, BATCH_KERNELS + PLAIN_KERNELS, 3)
+            stats = batch_stats(icd) if "cpv_batch_raster" in kernels else None
             color, depth = r.readback()
         finally:
             r.close()
@@ -405,6 +415,7 @@ def measure_workload(ctx, h, icd, name, cfg, params, env, desc, min_seconds=1.5)
         "gfrag_s": round(st["fragments"] / (mpf / 1000.0) / 1e9, 4), "frames_s": round(1000.0 / mpf, 2),
         "fragments": st["fragments"], "fragments_written": st["fragments_written"],
         "mode": "batched" if "cpv_batch_raster" in kernels else "plain", "gpu_launches_per_frame": round(launches / frames, 2),
+        "batch_stats": stats,
         "kernels": kernels, "roofline": roofline_of(name, scene, kernels, st["fragments_written"]), "clocks": clock_info,
         "parity": dict(image_diff(color, depth, ref_color, ref_depth), against="oracle whole frame"),
         "cpu_baseline": {"full_frame": {"seconds": round(ref_s, 3), "threads": threads, "kind": "port",
@@ -503,7 +514,8 @@ def run_ours(args, world, rank, dist):
         kernels = profile(PLAIN_KERNELS if mode == "plain" else BATCH_KERNELS + PLAIN_KERNELS, min(args.steps, 5))
         if mode == "default":
             mode = "batched" if "cpv_batch_raster" in kernels else "plain"  # what the ICD ran
-        results[mode] = {"total_ms": total_ms, "launches": int(launches), "clocks": clock_info, "kernels": kernels}
+        results[mode] = {"total_ms": total_ms, "launches": int(launches), "clocks": clock_info, "kernels": kernels,
+                         "stats": batch_stats(icd)}
         head = mode
     total_ms = results[head]["total_ms"]
     ms_per_step = total_ms / args.steps
@@ -549,6 +561,7 @@ def run_ours(args, world, rank, dist):
         }
         if head == "batched":
             line["config"]["tuning"] = c.batch_tuning() or "default configuration (pass below the tuning threshold)"
+            line["batch_stats"] = results[head].get("stats")
         if "plain" in results and head != "plain":
             pm = results["plain"]["total_ms"] / args.steps
             line["plain"] = {"value": round(tris * world / (pm / 1000.0) / 1e6, 3), "unit": "Mtri/s", "ms_per_step": round(pm, 4),

@@ -1390,6 +1390,7 @@ CPV_EXPORT const char* cpv_last_error(void) { return cpv::rt::last_error(); }
 CPV_EXPORT uint64_t cpv_kernel_launches(void) { return cpv::rt::launches(); }
 
 CPV_EXPORT const char* cpv_batch_tuning(void) { return cpv::icd::last_tuning(); }
+CPV_EXPORT void cpv_batch_stats(uint64_t out[3]) { cpv::rt::batch_stats(out); }
 
 CPV_EXPORT int cpv_queue_record(VkQueue queue, uint32_t slot) {
     auto* q = reinterpret_cast<cpv::icd::Queue*>(queue);

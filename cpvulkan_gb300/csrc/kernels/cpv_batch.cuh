@@ -66,17 +66,18 @@ extern "C" __global__ void __launch_bounds__(CPV_BATCH_BLOCK) cpv_batch_setup(co
         rect = cpv_tile_rect(t, B.vw, B.vh, B.ndc_x, B.ndc_y);
     }
     const uint64_t g = static_cast<uint64_t>(block) * CPV_BATCH_BLOCK + threadIdx.x;
-    B.rects[g] = rect;
     uint32_t pairs = ((rect.y & 0xFFFFu) - (rect.x & 0xFFFFu)) * ((rect.y >> 16) - (rect.x >> 16));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(0xFFFFFFFFu, pairs, o);
     if ((threadIdx.x & 31u) == 0u) warp_pairs[threadIdx.x >> 5] = pairs;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t s = 0;
-        for (uint32_t w = 0; w < CPV_BATCH_BLOCK / 32; w++) s += warp_pairs[w];
-        B.block_pairs[block] = s;
-    }
+    uint32_t s = 0;
+    for (uint32_t w = 0; w < CPV_BATCH_BLOCK / 32; w++) s += warp_pairs[w];
+    /* a block without pairs (all culled or off screen) leaves its
+     * rectangles unwritten: the emit kernel and the raster's rectangle scan
+     * skip such blocks by their pair count */
+    if (s != 0u) B.rects[g] = rect;
+    if (threadIdx.x == 0) B.block_pairs[block] = s;
 }
 
 /* Primitives of one tile of the batch: the tile's range of the sorted pair
@@ -96,6 +97,10 @@ struct CpvBatchSource {
         uint64_t g;
         if (scan_rects) {
             g = begin + i;
+            if (B.block_pairs[g / CPV_BATCH_BLOCK] == 0u) {  /* its rectangles were not written */
+                t.wf.w = __uint_as_float(0u);
+                return;
+            }
             const uint2 r = B.rects[g];
             const uint32_t rx0 = r.x & 0xFFFFu, ry0 = r.x >> 16, rx1 = r.y & 0xFFFFu, ry1 = r.y >> 16;
             if (!(tx >= rx0 && tx < rx1 && ty >= ry0 && ty < ry1)) {

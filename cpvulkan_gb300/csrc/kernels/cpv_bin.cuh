@@ -238,11 +238,14 @@ __device__ __forceinline__ uint32_t cpv_block256_exclusive(uint32_t v, uint32_t*
 }
 
 /* One block per 256-primitive set-up block: the block's pairs at
- * block_offsets[block] + (pairs of the block's earlier primitives). */
-extern "C" __global__ void __launch_bounds__(256) cpv_batch_emit(const uint2* __restrict__ rects, const uint32_t* __restrict__ block_offsets,
-                                                                 uint32_t tiles_x, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                                                                 uint32_t capacity, const uint32_t* __restrict__ pair_total) {
+ * block_offsets[block] + (pairs of the block's earlier primitives). A block
+ * without pairs has no rectangles written this frame and emits nothing. */
+extern "C" __global__ void __launch_bounds__(256) cpv_batch_emit(const uint2* __restrict__ rects, const uint32_t* __restrict__ block_pairs,
+                                                                 const uint32_t* __restrict__ block_offsets, uint32_t tiles_x,
+                                                                 uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, uint32_t capacity,
+                                                                 const uint32_t* __restrict__ pair_total) {
     __shared__ uint32_t warp_sums[8];
+    if (block_pairs[blockIdx.x] == 0u) return;
     const uint64_t g = static_cast<uint64_t>(blockIdx.x) * 256u + threadIdx.x;
     const uint2 r = rects[g];
     const uint32_t x0 = r.x & 0xFFFFu, y0 = r.x >> 16, x1 = r.y & 0xFFFFu, y1 = r.y >> 16;

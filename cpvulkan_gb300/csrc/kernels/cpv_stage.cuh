@@ -341,6 +341,21 @@ __device__ __forceinline__ void cpv_setup(const CpvDrawParams& P, uint64_t g, Cp
             }
         }
     }
+#if CPV_CULL_MODE != 0
+    /* a culled triangle is dead whatever its box and edges: its facing is
+     * the sign of the area cpv_setup_tri computes (the same expression),
+     * so those are skipped for it. Nothing reads a dead primitive's other
+     * fields. */
+    {
+        const float area = cpv_edge(Pn[0][0], Pn[0][1], Pn[1][0], Pn[1][1], Pn[2][0], Pn[2][1]);
+        const bool front = !(area < 0.0f);
+        if (((CPV_CULL_MODE & 2) && !front) || ((CPV_CULL_MODE & 1) && front)) {
+            t.box = make_int4(0, 0, 0, 0);
+            t.wf.w = __uint_as_float(0u);
+            return;
+        }
+    }
+#endif
     cpv_setup_tri<WITH_VARYINGS>(P, Pn, pslot, g32, t);
 }
 

@@ -878,7 +878,7 @@ int BatchPlan::enqueue(const Module& m, cudaStream_t stream) {
     profile_begin(stream, "cpv_batch_bin");
     int r = scan_u32(stream, block_pairs_, block_offsets_, blocks, words_, scan_);
     if (r != kOk) return r;
-    cpv_batch_emit<<<blocks, 256, 0, stream>>>(rects_, block_offsets_, P_.tiles_x, keys_[0], vals_[0], cap_, words_);
+    cpv_batch_emit<<<blocks, 256, 0, stream>>>(rects_, block_pairs_, block_offsets_, P_.tiles_x, keys_[0], vals_[0], cap_, words_);
     count_launch();
     for (uint32_t pass = 0; pass < passes_; pass++) {
         const uint32_t src = pass & 1u, dst = src ^ 1u;
@@ -911,7 +911,24 @@ int BatchPlan::enqueue(const Module& m, cudaStream_t stream) {
     return kOk;
 }
 
+namespace {
+std::atomic<uint64_t> g_stat_prims{0}, g_stat_slots{0}, g_stat_pairs{0};
+}
+
+void batch_stats(uint64_t out[3]) {
+    out[0] = g_stat_prims.load();
+    out[1] = g_stat_slots.load();
+    out[2] = g_stat_pairs.load();
+}
+
 int BatchPlan::launch(const Module& m, cudaStream_t stream) {
+    // Statistics of the last completed launch (cpv_batch_stats).
+    if (cudaEventQuery(done_) == cudaSuccess) {
+        g_stat_prims = prims_;
+        g_stat_slots = vs_slots_;
+        g_stat_pairs = *pinned_pairs_;
+    }
+    cudaGetLastError();
     // An earlier launch that needed more pairs than the buffers hold rendered
     // correctly through the rectangle scan; grow the buffers for the next.
     if (exec_ && cudaEventQuery(done_) == cudaSuccess && *pinned_pairs_ > cap_) {

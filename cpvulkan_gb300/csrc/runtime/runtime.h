@@ -191,6 +191,10 @@ private:
     cudaGraphExec_t exec_ = nullptr;
 };
 
+// Primitives, vertex slots and (primitive, tile) pairs of the most recent
+// batched launch that had completed when the next one was enqueued.
+void batch_stats(uint64_t out[3]);
+
 // Fixed binning scratch for submissions that may not allocate: one
 // 32 MiB file-scope device array per device. A draw needs 8 bytes per
 // primitive for its tile rectangles plus its bins; one that does not fit even

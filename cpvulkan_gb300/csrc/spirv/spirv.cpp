@@ -833,6 +833,22 @@ bool Translator::emit_attribute_fetch(const Variable& v, uint32_t location) {
         return fail("half-float vertex attribute into an input of another type or width (the reference aborts on it)");
     const std::string index = b->input_rate == 0 ? "cpv_vertex_index" : "cpv_instance_index";
     pro_ << "  { const uint64_t off = (uint64_t)" << b->stride << "u * (uint64_t)" << index << " + " << a->offset << "u;\n";
+    const uint32_t nload = comps < fcomps ? comps : fcomps;
+    if (kind <= 2 && nload > 1) {
+        // 32-bit channels: one bounds check for all of them (each channel's
+        // own check passes exactly when the last one's does), then plain
+        // loads; otherwise the per-channel checked loads below
+        const std::string bs = std::to_string(a->binding);
+        pro_ << "    if (P.vb[" << bs << "] != nullptr && off + " << 4 * nload << "u <= P.vb_bytes[" << bs << "]) {\n";
+        pro_ << "      const uint32_t* cpv_q = reinterpret_cast<const uint32_t*>(P.vb[" << bs << "] + off);\n";
+        for (uint32_t i = 0; i < nload; i++) {
+            std::string e = "cpv_q[" + std::to_string(i) + "]";
+            if (kind == 0) e = is_float ? "__uint_as_float(" + e + ")" : "(" + tn(elem) + ")" + e;
+            else e = is_float ? "__uint_as_float(" + e + ")" : "(" + tn(elem) + ")(" + e + ")";
+            pro_ << "      " << path(i) << " = " << e << ";\n";
+        }
+        pro_ << "    } else {\n";
+    }
     for (uint32_t i = 0; i < comps && i < fcomps; i++) {
         std::string e;
         const std::string vb = "P.vb[" + std::to_string(a->binding) + "], P.vb_bytes[" + std::to_string(a->binding) + "]";
@@ -851,6 +867,7 @@ bool Translator::emit_attribute_fetch(const Variable& v, uint32_t location) {
         }
         pro_ << "    " << path(i) << " = " << e << ";\n";
     }
+    if (kind <= 2 && nload > 1) pro_ << "    }\n";
     pro_ << "  }\n";
     return true;
 }

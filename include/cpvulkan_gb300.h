@@ -64,6 +64,12 @@ CPV_EXPORT uint64_t cpv_kernel_launches(void);
  * counterpart. */
 CPV_EXPORT const char* cpv_batch_tuning(void);
 
+/* Statistics of the most recent batched render pass that had completed when
+ * the next batched pass was submitted: out[0] primitives, out[1] vertex
+ * slots shaded by the vertex stage, out[2] (primitive, screen tile) pairs
+ * binned. No reference counterpart. */
+CPV_EXPORT void cpv_batch_stats(uint64_t out[3]);
+
 /* 1 when a CUDA device can be used (creates the context), else 0. */
 CPV_EXPORT int cpv_device_available(void);
 
