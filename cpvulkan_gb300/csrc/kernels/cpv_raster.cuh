@@ -371,25 +371,65 @@ __device__ __forceinline__ uint32_t cpv_tile_class(const CpvTri& t, int32_t tile
     return (x1 - x0) * (y1 - y0) > CPV_SMALL_PX ? 2u : 1u;
 }
 
-/* Sparse schedule: a small primitive j of the batch tests the pixels of its
- * box inside the tile and appends j to the list of each covered one. A live
- * primitive's box lies inside the attachment, so every listed pixel is
- * inside it. */
-__device__ __forceinline__ void cpv_list_small(const CpvTri& t, uint32_t j, int32_t tile_x0, int32_t tile_y0, const float* col_ndc,
-                                               const float* row_ndc, uint32_t* list_count, uint8_t* list_j) {
-    if (cpv_tile_class(t, tile_x0, tile_y0) != 1u) return;
-    const int4 box = t.box;
-    const int32_t x0 = max(box.x, tile_x0), x1 = min(box.z, tile_x0 + CPV_TILE);
-    const int32_t y0 = max(box.y, tile_y0), y1 = min(box.w, tile_y0 + CPV_TILE);
-    for (int32_t y = y0; y < y1; y++) {
-        const float yf = row_ndc[y - tile_y0];
-        for (int32_t x = x0; x < x1; x++) {
-            float w[3];
-            if (!cpv_covers(t, col_ndc[x - tile_x0], yf, w)) continue;
-            const uint32_t p = static_cast<uint32_t>((y - tile_y0) * CPV_TILE + (x - tile_x0));
-            const uint32_t s = atomicAdd(&list_count[p], 1u);
-            if (s < CPV_SLOT_DEPTH) list_j[p * CPV_SLOT_DEPTH + s] = static_cast<uint8_t>(j);
+/* Sparse schedule: the small primitives j0 .. j0 + 31 of a batch (one per
+ * lane of the calling warp) test the pixels of their boxes inside the tile
+ * and append each covered pixel's primitive to its list — as one list of
+ * (primitive, pixel) tests spread evenly over the warp's lanes, so that a
+ * lane's large box does not hold the other 31 lanes. Test i of the warp
+ * belongs to the first lane whose inclusive box-size sum exceeds i (a
+ * binary search over the lanes' sums) and is pixel i - (that lane's
+ * exclusive sum) of its box, row-major. A pixel's list is applied in batch
+ * order whatever the order of its appends. */
+__device__ __forceinline__ void cpv_list_small_warp(const CpvTri* tris, uint32_t j0, uint32_t n, int32_t tile_x0, int32_t tile_y0,
+                                                    const float* col_ndc, const float* row_ndc, uint32_t* list_count, uint8_t* list_j) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t j = j0 + lane;
+    uint32_t size = 0u, geo = 0u, magic = 0u;
+    if (j < n && cpv_tile_class(tris[j], tile_x0, tile_y0) == 1u) {
+        const int4 box = tris[j].box;
+        const int32_t x0 = max(box.x, tile_x0), x1 = min(box.z, tile_x0 + CPV_TILE);
+        const int32_t y0 = max(box.y, tile_y0), y1 = min(box.w, tile_y0 + CPV_TILE);
+        const uint32_t bw = static_cast<uint32_t>(x1 - x0);
+        size = bw * static_cast<uint32_t>(y1 - y0);
+        geo = static_cast<uint32_t>(x0 - tile_x0) | (static_cast<uint32_t>(y0 - tile_y0) << 8) | (bw << 16);
+        /* row = (k * magic) >> 16 = floor(k / bw) for every k < 1024 and bw
+         * <= 32: magic = ceil(2^16 / bw) exceeds 2^16 / bw by less than 1,
+         * so the product exceeds k * 2^16 / bw by less than k < 2^16 / 64,
+         * under the 2^16 / bw gap from a non-integer k / bw to the next
+         * integer */
+        magic = (65536u + bw - 1u) / bw;
+    }
+    uint32_t incl = size;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= static_cast<uint32_t>(o)) incl += t;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    for (uint32_t base = 0; base < total; base += 32u) {
+        const uint32_t i = base + lane;
+        /* owner: the number of lanes whose inclusive sum is <= i */
+        uint32_t owner = 0u;
+#pragma unroll
+        for (uint32_t s = 16u; s > 0u; s >>= 1) {
+            const uint32_t v = __shfl_sync(0xFFFFFFFFu, incl, owner + s - 1u);
+            if (v <= i) owner += s;
         }
+        owner &= 31u;
+        const uint32_t o_incl = __shfl_sync(0xFFFFFFFFu, incl, owner);
+        const uint32_t o_size = __shfl_sync(0xFFFFFFFFu, size, owner);
+        const uint32_t o_geo = __shfl_sync(0xFFFFFFFFu, geo, owner);
+        const uint32_t o_magic = __shfl_sync(0xFFFFFFFFu, magic, owner);
+        if (i >= total) continue;
+        const uint32_t k = i - (o_incl - o_size);
+        const uint32_t row = (k * o_magic) >> 16;
+        const uint32_t col = k - row * (o_geo >> 16);
+        const uint32_t lx = (o_geo & 0xFFu) + col, ly = ((o_geo >> 8) & 0xFFu) + row;
+        float w[3];
+        if (!cpv_covers(tris[j0 + owner], col_ndc[lx], row_ndc[ly], w)) continue;
+        const uint32_t p = ly * CPV_TILE + lx;
+        const uint32_t s = atomicAdd(&list_count[p], 1u);
+        if (s < CPV_SLOT_DEPTH) list_j[p * CPV_SLOT_DEPTH + s] = static_cast<uint8_t>(j0 + owner);
     }
 }
 
@@ -543,9 +583,9 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
         /* mostly large primitives: this batch runs the immediate schedule */
         const bool immediate_batch = nlarge * 4u >= 3u * n;
         if (!immediate_batch) {
-            /* 2. small primitives: one thread each lists the pixels it covers */
-            for (uint32_t j = threadIdx.x; j < n; j += CPV_RT_THREADS)
-                cpv_list_small(tris[j], j, tile_x0, tile_y0, col_ndc, row_ndc, list_count, list_j);
+            /* 2. small primitives: each warp lists the pixels its 32 cover */
+            for (uint32_t j0 = threadIdx.x & ~31u; j0 < n; j0 += CPV_RT_THREADS)
+                cpv_list_small_warp(tris, j0, n, tile_x0, tile_y0, col_ndc, row_ndc, list_count, list_j);
             /* 3. large primitives, in order: every pixel's thread tests its pixels */
             for (uint32_t m = 0; m < nlarge; m++) {
                 const uint32_t j = large[m];
