@@ -20,7 +20,7 @@ MANIFEST_PATH = os.path.join(BUILD_DIR, "CPVulkan.json")
 # Scene configurations (include/cpv_harness.h).
 CUBE, HEIGHTFIELD, BLEND, BATCH, PROGRAM, SERVE = 1, 2, 3, 4, 5, 6
 # Shader programs (include/cpv/scene.h).
-PROGRAM_CUBE, PROGRAM_TEXLIT, PROGRAM_FLATQUAD, PROGRAM_MESHPC, PROGRAM_DISCARD, PROGRAM_NOPERSP, PROGRAM_POINTS, PROGRAM_FETCH = range(8)
+PROGRAM_CUBE, PROGRAM_TEXLIT, PROGRAM_FLATQUAD, PROGRAM_MESHPC, PROGRAM_DISCARD, PROGRAM_NOPERSP, PROGRAM_POINTS, PROGRAM_FETCH, PROGRAM_MRT = range(9)
 
 VK_FORMAT_D16_UNORM = 124
 VK_FORMAT_D32_SFLOAT = 126
@@ -48,7 +48,7 @@ class SceneHeader(ctypes.Structure):
                 ("index_data", vp), ("index_bytes", u64), ("index_type", u32), ("uniform_data", vp), ("uniform_bytes", u32),
                 ("texture_data", vp), ("texture_bytes", u64), ("texture_width", u32), ("texture_height", u32),
                 ("texture_levels", u32), ("texture_format", u32), ("sampler", SamplerDesc), ("num_pipelines", u32),
-                ("pipelines", vp), ("num_draws", u32), ("draws", vp)]
+                ("pipelines", vp), ("num_draws", u32), ("draws", vp), ("extra_color_count", u32), ("extra_color_formats", u32 * 7)]
 
 
 class SceneDraw(ctypes.Structure):
@@ -67,7 +67,7 @@ def colour_texel_bytes(fmt):
     """Bytes per texel of a colour attachment format (R8_UNORM 1; R8G8_UNORM
     and R16_UNORM 2; the 4-byte formats otherwise); a depth-only pass reads
     back zeros in the 4-byte layout."""
-    return {9: 1, 16: 2, 70: 2}.get(fmt, 4)
+    return {0: 4, 9: 1, 16: 2, 70: 2}.get(fmt, 4)
 
 
 _harness = None
@@ -108,6 +108,8 @@ def harness():
     h.cpvh_renderer_set_indirect_count.argtypes = [vp, u32, u32]
     h.cpvh_readback.restype = ctypes.c_int
     h.cpvh_readback.argtypes = [vp, vp, vp]
+    h.cpvh_readback_extra.restype = ctypes.c_int
+    h.cpvh_readback_extra.argtypes = [vp, u32, vp]
     h.cpvh_queue.restype = vp
     h.cpvh_queue.argtypes = [vp]
     h.cpvh_last_error.restype = cp
@@ -146,6 +148,8 @@ class Scene:
         hdr = SceneHeader.from_address(self.ptr)
         self.width, self.height = hdr.width, hdr.height
         self.color_format, self.depth_format = hdr.color_format, hdr.depth_format
+        # formats of the colour attachments after the first (0: unused reference)
+        self.extra_color_formats = [hdr.extra_color_formats[k] for k in range(hdr.extra_color_count)]
         self.config = config
 
     @property
@@ -339,6 +343,16 @@ class Renderer:
         if r != VK_SUCCESS:
             raise RuntimeError("readback failed (%d)" % r)
         return color, depth
+
+    def readback_extra(self, k):
+        """Colour attachment k (1 .. 7) of the scene's subpass, as bytes per texel."""
+        s = self.scene
+        fmt = s.extra_color_formats[k - 1]
+        out = np.zeros((s.height, s.width, colour_texel_bytes(fmt)), np.uint8)
+        r = harness().cpvh_readback_extra(self.ptr, k, out.ctypes.data)
+        if r != VK_SUCCESS:
+            raise RuntimeError("readback of colour attachment %d failed (%d)" % (k, r))
+        return out
 
     def close(self):
         if self.ptr and getattr(self, "owned", True):  # server client views belong to their server

@@ -184,6 +184,7 @@ struct cpvh_renderer {
     uint32_t subpass = 0;  // the subpass the frame draws in (CPVH_SUBPASSES=2: 1)
     bool use_secondary = false;  // CPVH_SECONDARY=1: draws through secondary command buffers
     ImageAlloc colour, depth, texture;
+    std::vector<ImageAlloc> extra;  // colour attachments after the first (an unused reference: no image)
     VkSampler sampler = nullptr;
     VkRenderPass pass = nullptr;
     VkFramebuffer fb = nullptr;
@@ -355,13 +356,19 @@ void record_draws(cpvh_renderer* r, VkCommandBuffer cmd, uint32_t begin, uint32_
 void record_frame(cpvh_renderer* r, VkCommandBuffer cmd) {
     cpvh_context* c = r->ctx;
     const cpv_scene* s = r->scene;
-    VkClearValue clears[2];
+    VkClearValue clears[2 + CPV_SCENE_MAX_EXTRA_COLOR];
     std::memset(clears, 0, sizeof(clears));
-    // in attachment order: colour (absent in a depth-only pass), depth
+    // in attachment order: colour (absent in a depth-only pass), the further
+    // colour attachments (the same clear colour), depth
     uint32_t nclears = 0;
     if (s->color_format) {
         for (int i = 0; i < 4; i++) clears[nclears].color.float32[i] = s->clear_color[i];
         nclears++;
+        for (uint32_t k = 0; k < s->extra_color_count; k++) {
+            if (!s->extra_color_formats[k]) continue;
+            for (int i = 0; i < 4; i++) clears[nclears].color.float32[i] = s->clear_color[i];
+            nclears++;
+        }
     }
     if (s->depth_format) {
         clears[nclears].depthStencil.depth = s->clear_depth;
@@ -529,12 +536,28 @@ bool build_pipelines(cpvh_context* c, const cpv_scene* s, VkRenderPass pass, VkP
         cba.dstAlphaBlendFactor = static_cast<VkBlendFactor>(sp.dst_alpha);
         cba.alphaBlendOp = static_cast<VkBlendOp>(sp.alpha_op);
         cba.colorWriteMask = sp.color_write_mask;
+        // one state per colour reference of the subpass
+        VkPipelineColorBlendAttachmentState cbas[1 + CPV_SCENE_MAX_EXTRA_COLOR];
+        cbas[0] = cba;
+        for (uint32_t k = 0; k < s->extra_color_count; k++) {
+            const cpv_scene_attachment_blend& eb = sp.extra_blend[k];
+            VkPipelineColorBlendAttachmentState& e = cbas[k + 1];
+            e = VkPipelineColorBlendAttachmentState{};
+            e.blendEnable = eb.blend_enable;
+            e.srcColorBlendFactor = static_cast<VkBlendFactor>(eb.src_color);
+            e.dstColorBlendFactor = static_cast<VkBlendFactor>(eb.dst_color);
+            e.colorBlendOp = static_cast<VkBlendOp>(eb.color_op);
+            e.srcAlphaBlendFactor = static_cast<VkBlendFactor>(eb.src_alpha);
+            e.dstAlphaBlendFactor = static_cast<VkBlendFactor>(eb.dst_alpha);
+            e.alphaBlendOp = static_cast<VkBlendOp>(eb.alpha_op);
+            e.colorWriteMask = eb.color_write_mask;
+        }
         VkPipelineColorBlendStateCreateInfo cbs{};
         cbs.sType = VK_STRUCTURE_TYPE_PIPELINE_COLOR_BLEND_STATE_CREATE_INFO;
         cbs.logicOpEnable = sp.logic_op_enable;
         cbs.logicOp = static_cast<VkLogicOp>(sp.logic_op);
-        cbs.attachmentCount = s->color_format ? 1 : 0;
-        cbs.pAttachments = &cba;
+        cbs.attachmentCount = s->color_format ? 1 + s->extra_color_count : 0;
+        cbs.pAttachments = cbas;
         for (int k = 0; k < 4; k++) cbs.blendConstants[k] = sp.blend_constants[k];
         VkGraphicsPipelineCreateInfo gpi{};
         gpi.sType = VK_STRUCTURE_TYPE_GRAPHICS_PIPELINE_CREATE_INFO;
@@ -563,29 +586,33 @@ bool build_pipelines(cpvh_context* c, const cpv_scene* s, VkRenderPass pass, VkP
 // subpass 1 (these attachments), after a subpass 0 that references only the
 // depth attachment (only the colour one when there is no depth).
 VkResult create_scene_pass(cpvh_context* c, const cpv_scene* s, VkRenderPass* out, bool two_subpasses = false) {
-    VkAttachmentDescription att[2]{};
-    VkAttachmentReference cref{0, VK_IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL}, dref{0, VK_IMAGE_LAYOUT_DEPTH_STENCIL_ATTACHMENT_OPTIMAL};
+    VkAttachmentDescription att[2 + CPV_SCENE_MAX_EXTRA_COLOR]{};
+    VkAttachmentReference crefs[1 + CPV_SCENE_MAX_EXTRA_COLOR], dref{0, VK_IMAGE_LAYOUT_DEPTH_STENCIL_ATTACHMENT_OPTIMAL};
     uint32_t n = 0;
     VkSubpassDescription sub{};
-    for (uint32_t k = 0; k < 2; k++) {
-        const uint32_t fmt = k == 0 ? s->color_format : s->depth_format;
-        if (!fmt) continue;
+    auto describe = [&](uint32_t fmt, bool depth) {
         VkAttachmentDescription& a = att[n];
         a.format = static_cast<VkFormat>(fmt);
         a.samples = VK_SAMPLE_COUNT_1_BIT;
         a.loadOp = VK_ATTACHMENT_LOAD_OP_CLEAR;
         a.storeOp = VK_ATTACHMENT_STORE_OP_STORE;
-        a.stencilLoadOp = k == 0 ? VK_ATTACHMENT_LOAD_OP_DONT_CARE : VK_ATTACHMENT_LOAD_OP_CLEAR;
+        a.stencilLoadOp = depth ? VK_ATTACHMENT_LOAD_OP_CLEAR : VK_ATTACHMENT_LOAD_OP_DONT_CARE;
         a.finalLayout = VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL;
-        if (k == 0) {
-            cref.attachment = n;
-            sub.colorAttachmentCount = 1;
-            sub.pColorAttachments = &cref;
-        } else {
-            dref.attachment = n;
-            sub.pDepthStencilAttachment = &dref;
+        return n++;
+    };
+    // colour references in order (an unused one keeps its position), then depth
+    if (s->color_format) {
+        crefs[0] = {describe(s->color_format, false), VK_IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL};
+        for (uint32_t k = 0; k < s->extra_color_count; k++) {
+            const uint32_t f = s->extra_color_formats[k];
+            crefs[k + 1] = {f ? describe(f, false) : VK_ATTACHMENT_UNUSED, VK_IMAGE_LAYOUT_COLOR_ATTACHMENT_OPTIMAL};
         }
-        n++;
+        sub.colorAttachmentCount = 1 + s->extra_color_count;
+        sub.pColorAttachments = crefs;
+    }
+    if (s->depth_format) {
+        dref.attachment = describe(s->depth_format, true);
+        sub.pDepthStencilAttachment = &dref;
     }
     VkSubpassDescription subs[2] = {sub, sub};
     if (two_subpasses) {
@@ -774,7 +801,7 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
     if (make_buffer(c, staging, VK_BUFFER_USAGE_TRANSFER_SRC_BIT, true, r->staging) != VK_SUCCESS) return fail("staging buffer");
     r->depth_texel = depth_texel_size(s->depth_format);
     r->colour_texel = colour_texel_size(s->color_format);
-    const uint64_t rb_bytes = static_cast<uint64_t>(s->width) * s->height * (r->colour_texel + r->depth_texel);
+    const uint64_t rb_bytes = static_cast<uint64_t>(s->width) * s->height * (std::max<uint32_t>(r->colour_texel, 4u) + r->depth_texel);
     if (make_buffer(c, rb_bytes, VK_BUFFER_USAGE_TRANSFER_DST_BIT, true, r->readback) != VK_SUCCESS) return fail("readback buffer");
     // CPVH_INDIRECT=1: the frame issues every draw as an indirect draw whose
     // record (VkDrawIndexedIndirectCommand / VkDrawIndirectCommand, 20-byte
@@ -816,6 +843,12 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
         make_image(c, static_cast<VkFormat>(s->depth_format), s->width, s->height, 1, VK_IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT_BIT | VK_IMAGE_USAGE_TRANSFER_SRC_BIT,
                    VK_IMAGE_ASPECT_DEPTH_BIT, r->depth) != VK_SUCCESS)
         return fail("depth image");
+    r->extra.resize(s->color_format ? s->extra_color_count : 0);
+    for (uint32_t k = 0; k < r->extra.size(); k++)
+        if (s->extra_color_formats[k] &&
+            make_image(c, static_cast<VkFormat>(s->extra_color_formats[k]), s->width, s->height, 1,
+                       VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT | VK_IMAGE_USAGE_TRANSFER_SRC_BIT, VK_IMAGE_ASPECT_COLOR_BIT, r->extra[k]) != VK_SUCCESS)
+            return fail("colour image " + std::to_string(k + 1));
     if (s->texture_data) {
         if (make_image(c, static_cast<VkFormat>(s->texture_format), s->texture_width, s->texture_height, s->texture_levels,
                        VK_IMAGE_USAGE_SAMPLED_BIT | VK_IMAGE_USAGE_TRANSFER_DST_BIT, VK_IMAGE_ASPECT_COLOR_BIT, r->texture) != VK_SUCCESS)
@@ -840,10 +873,15 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
     const char* subpasses = std::getenv("CPVH_SUBPASSES");
     r->subpass = subpasses && subpasses[0] == '2' ? 1u : 0u;
     if (create_scene_pass(c, s, &r->pass, r->subpass == 1) != VK_SUCCESS) return fail("render pass");
-    // attachments in order: colour (absent in a depth-only pass), depth
-    VkImageView views[2];
+    // attachments in order: colour (absent in a depth-only pass), the
+    // further colour attachments, depth
+    VkImageView views[2 + CPV_SCENE_MAX_EXTRA_COLOR];
     uint32_t nviews = 0;
-    if (s->color_format) views[nviews++] = r->colour.view;
+    if (s->color_format) {
+        views[nviews++] = r->colour.view;
+        for (const ImageAlloc& e : r->extra)
+            if (e.view) views[nviews++] = e.view;
+    }
     if (s->depth_format) views[nviews++] = r->depth.view;
     VkFramebufferCreateInfo fbi{};
     fbi.sType = VK_STRUCTURE_TYPE_FRAMEBUFFER_CREATE_INFO;
@@ -1017,6 +1055,7 @@ void renderer_destroy(cpvh_renderer* r, bool wait_idle) {
     if (r->pass) f.vkDestroyRenderPass(c->device, r->pass, nullptr);
     if (r->sampler) f.vkDestroySampler(c->device, r->sampler, nullptr);
     destroy_image(c, r->colour);
+    for (ImageAlloc& e : r->extra) destroy_image(c, e);
     destroy_image(c, r->depth);
     destroy_image(c, r->texture);
     destroy_buffer(c, r->vertex);
@@ -1181,6 +1220,35 @@ int cpvh_readback(cpvh_renderer* r, uint8_t* color, uint8_t* depth) {
     if (color && s->color_format) std::memcpy(color, map, cb);
     else if (color) std::memset(color, 0, cb);  // a depth-only pass
     if (depth && s->depth_format) std::memcpy(depth, static_cast<uint8_t*>(map) + cb, static_cast<uint64_t>(s->width) * s->height * r->depth_texel);
+    c->f.vkUnmapMemory(c->device, r->readback.memory);
+    return VK_SUCCESS;
+}
+
+int cpvh_readback_extra(cpvh_renderer* r, uint32_t k, uint8_t* out) {
+    cpvh_context* c = r->ctx;
+    const cpv_scene* s = r->scene;
+    if (k < 1 || k > r->extra.size() || !out) return VK_ERROR_INITIALIZATION_FAILED;
+    const uint32_t fmt = s->extra_color_formats[k - 1];
+    const uint64_t bytes = static_cast<uint64_t>(s->width) * s->height * colour_texel_size(fmt);
+    if (!fmt) {  // an unused reference has no image
+        std::memset(out, 0, bytes);
+        return VK_SUCCESS;
+    }
+    // the readback buffer holds a 4-byte colour texel per pixel at least
+    VkCommandBufferBeginInfo bi{};
+    bi.sType = VK_STRUCTURE_TYPE_COMMAND_BUFFER_BEGIN_INFO;
+    c->f.vkBeginCommandBuffer(r->copy_cmd, &bi);
+    VkBufferImageCopy bc{};
+    bc.imageSubresource = {VK_IMAGE_ASPECT_COLOR_BIT, 0, 0, 1};
+    bc.imageExtent = {s->width, s->height, 1};
+    c->f.vkCmdCopyImageToBuffer(r->copy_cmd, r->extra[k - 1].image, VK_IMAGE_LAYOUT_TRANSFER_SRC_OPTIMAL, r->readback.buffer, 1, &bc);
+    c->f.vkEndCommandBuffer(r->copy_cmd);
+    VkResult res = submit_and_wait(r, r->copy_cmd);
+    if (res != VK_SUCCESS) return res;
+    void* map = nullptr;
+    res = c->f.vkMapMemory(c->device, r->readback.memory, 0, VK_WHOLE_SIZE, 0, &map);
+    if (res != VK_SUCCESS) return res;
+    std::memcpy(out, map, bytes);
     c->f.vkUnmapMemory(c->device, r->readback.memory);
     return VK_SUCCESS;
 }

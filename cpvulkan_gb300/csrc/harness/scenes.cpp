@@ -169,6 +169,11 @@ cpv_scene_pipeline base_pipeline(uint32_t program) {
     p.stencil_front.write_mask = p.stencil_back.write_mask = 0xFF;
     p.src_color = p.src_alpha = VK_BLEND_FACTOR_ONE;
     p.dst_color = p.dst_alpha = VK_BLEND_FACTOR_ZERO;
+    for (auto& b : p.extra_blend) {
+        b.src_color = b.src_alpha = VK_BLEND_FACTOR_ONE;
+        b.dst_color = b.dst_alpha = VK_BLEND_FACTOR_ZERO;
+        b.color_write_mask = 0xF;
+    }
     p.line_width = 1.0f;
     p.color_write_mask = 0xF;
     return p;
@@ -659,7 +664,7 @@ uint32_t colour_attribute_bytes(uint32_t format) {
 // R16G16 UNORM, R8G8B8A8 SNORM, R16G16 or R32 SFLOAT), cleared to a colour
 // with channels outside [0, 1].
 void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant, uint32_t width, uint32_t height, uint32_t tris,
-                   uint32_t colour_format, uint32_t attachment_format) {
+                   uint32_t colour_format, uint32_t attachment_format, uint64_t extra_formats, uint64_t extra_blend) {
     cpv_scene& s = st.scene;
     s.width = width;
     s.height = height;
@@ -707,6 +712,30 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
         p.logic_op = (variant >> 20) & 0xF;
     }
     if (variant & 0x80000) p.color_write_mask = (variant >> 24) & 0xF;  // partial colour write mask (bits 24-27)
+    // Colour attachments after the first: byte k of extra_formats is the
+    // VkFormat of attachment k + 1 (0: an unused reference), byte k of
+    // extra_blend its blend state: bit 0 src-over, bit 1 additive colour
+    // with a MAX alpha, bits 4-7 a write mask (0: every channel).
+    for (uint32_t k = 0; k < CPV_SCENE_MAX_EXTRA_COLOR; k++) {
+        const uint32_t f = static_cast<uint32_t>((extra_formats >> (8 * k)) & 0xFFu);
+        if (f) s.extra_color_count = k + 1;
+        s.extra_color_formats[k] = f;
+        const uint32_t b = static_cast<uint32_t>((extra_blend >> (8 * k)) & 0xFFu);
+        cpv_scene_attachment_blend& eb = p.extra_blend[k];
+        if (b & 1u) {
+            eb.blend_enable = 1;
+            eb.src_color = VK_BLEND_FACTOR_SRC_ALPHA;
+            eb.dst_color = VK_BLEND_FACTOR_ONE_MINUS_SRC_ALPHA;
+            eb.src_alpha = VK_BLEND_FACTOR_ONE;
+            eb.dst_alpha = VK_BLEND_FACTOR_ONE_MINUS_SRC_ALPHA;
+        } else if (b & 2u) {
+            eb.blend_enable = 1;
+            eb.src_color = eb.dst_color = VK_BLEND_FACTOR_ONE;
+            eb.src_alpha = eb.dst_alpha = VK_BLEND_FACTOR_ONE;
+            eb.alpha_op = VK_BLEND_OP_MAX;
+        }
+        if (b >> 4) eb.color_write_mask = b >> 4;
+    }
     if (const uint32_t bounds = (variant >> 28) & 3u) {  // depth bounds test (bits 28-29) against the stored depth (cleared to 0.75)
         // 1: the whole range; 2: stored depth from 0.3 up; 3: above the clear depth, so nothing passes
         static const float range[4][2] = {{0.0f, 1.0f}, {0.0f, 1.0f}, {0.3f, 1.0f}, {0.8f, 1.0f}};
@@ -718,7 +747,8 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
 
     uint32_t vcount = 0;
     uint64_t colour_offset = 0;
-    if (program == CPV_PROGRAM_CUBE || program == CPV_PROGRAM_DISCARD || program == CPV_PROGRAM_NOPERSP || program == CPV_PROGRAM_POINTS) {
+    if (program == CPV_PROGRAM_CUBE || program == CPV_PROGRAM_DISCARD || program == CPV_PROGRAM_NOPERSP || program == CPV_PROGRAM_POINTS ||
+        program == CPV_PROGRAM_MRT) {
         // Clip-space vertices with w in [0.5, 2] (positive, as the reference
         // requires), a shared-edge pair, and a zero-area triangle.
         st.uniform.resize(64);
@@ -910,7 +940,7 @@ cpv_scene* cpvh_scene_create(uint32_t config, uint64_t seed, const uint64_t* par
     case CPVH_PROGRAM:
         build_program(*st, seed, static_cast<uint32_t>(params && np > 0 ? params[0] : 0), static_cast<uint32_t>(params && np > 1 ? params[1] : 0),
                       static_cast<uint32_t>(param(2, 64)), static_cast<uint32_t>(param(3, 48)), static_cast<uint32_t>(param(4, 12)),
-                      static_cast<uint32_t>(param(5, 0)), static_cast<uint32_t>(param(6, 0)));
+                      static_cast<uint32_t>(param(5, 0)), static_cast<uint32_t>(param(6, 0)), param(7, 0), param(8, 0));
         break;
     case CPVH_SERVE: build_serve(*st, seed, static_cast<uint32_t>(param(0, 512)), static_cast<uint32_t>(param(1, 20000)), static_cast<uint32_t>(params && np > 2 ? params[2] : 0)); break;
     default: return nullptr;

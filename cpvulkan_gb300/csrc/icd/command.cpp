@@ -296,7 +296,14 @@ VkResult build_draw(State& s, uint32_t count, uint32_t instances, uint32_t first
     // depth-only one); attachment addressing uses the image row length.
     uint32_t w = 0, h = 0;
     const Subpass& sub = s.sub();
-    if (!sub.colour.empty()) P.color = view_base(s.fb->attachments[sub.colour[0]], w, h);
+    if (!sub.colour.empty() && sub.colour[0] != VK_ATTACHMENT_UNUSED) P.color = view_base(s.fb->attachments[sub.colour[0]], w, h);
+    // the further colour attachments, each the size of the first
+    for (size_t k = 1; k < sub.colour.size() && k < CPV_MAX_CA; k++) {
+        if (sub.colour[k] == VK_ATTACHMENT_UNUSED) continue;
+        uint32_t ew, eh;
+        P.color_extra[k - 1] = view_base(s.fb->attachments[sub.colour[k]], ew, eh);
+        if (!P.color || ew != w || eh != h) return VK_ERROR_DEVICE_LOST;
+    }
     if (sub.depth != VK_ATTACHMENT_UNUSED) {
         uint32_t dw, dh;
         P.depth = view_base(s.fb->attachments[sub.depth], dw, dh);
@@ -552,6 +559,19 @@ std::vector<ModuleConfig> tune_candidates(const ModuleConfig& base) {
     other.schedule = base.schedule == 0u ? 2u : 0u;
     other.batch = other.schedule == 0u ? 128u : 256u;
     out.push_back(other);
+    // the sparse schedule's fragment-list depth per pixel and batch (the
+    // bin-queue depth): the default (24, or 16 when a fragment shader
+    // samples) and one shallower and one deeper
+    if (base.schedule == 2u) {
+        const uint32_t d = base.samples ? 16u : 24u;
+        for (uint32_t depth : {d - 8u, d + 8u}) {
+            ModuleConfig q = base;
+            q.tile_shift = 4;
+            q.warps = 8;
+            q.depth = depth;
+            out.push_back(q);
+        }
+    }
     return out;
 }
 
@@ -611,8 +631,8 @@ bool tune_batch(Queue* q, Device* dev, const std::vector<Pipeline*>& pipelines, 
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, e0, e1);
         char line[96];
-        std::snprintf(line, sizeof(line), "%stile %u warps %u schedule %u batch %u: %.3f ms", report.empty() ? "" : "; ",
-                      1u << cands[i].tile_shift, cands[i].warps, cands[i].schedule, cands[i].batch, ms);
+        std::snprintf(line, sizeof(line), "%stile %u warps %u schedule %u batch %u depth %u: %.3f ms", report.empty() ? "" : "; ",
+                      1u << cands[i].tile_shift, cands[i].warps, cands[i].schedule, cands[i].batch, cands[i].depth, ms);
         report += line;
         if (!best_plan || ms < best_ms) {
             best_ms = ms;
@@ -627,9 +647,9 @@ bool tune_batch(Queue* q, Device* dev, const std::vector<Pipeline*>& pipelines, 
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     if (best_plan) {
-        char line[64];
-        std::snprintf(line, sizeof(line), "; chosen tile %u warps %u schedule %u batch %u", 1u << chosen.tile_shift, chosen.warps,
-                      chosen.schedule, chosen.batch);
+        char line[96];
+        std::snprintf(line, sizeof(line), "; chosen tile %u warps %u schedule %u batch %u depth %u", 1u << chosen.tile_shift, chosen.warps,
+                      chosen.schedule, chosen.batch, chosen.depth);
         g_last_tuning = report + line;
     }
     return ok && best_plan != nullptr;
@@ -661,6 +681,7 @@ void build_batch(Queue* q, const CommandBuffer* cb, size_t begin, size_t end, co
             vh = P.viewport[3];
             in.color = P.color;
             in.depth = P.depth;
+            for (int k = 0; k < CPV_MAX_CA - 1; k++) in.color_extra[k] = P.color_extra[k];
             in.fb_width = P.fb_width;
             in.fb_height = P.fb_height;
         } else if (P.viewport[2] != vw || P.viewport[3] != vh) {
@@ -1115,7 +1136,7 @@ VkResult check_no_alloc(Queue* q, CommandBuffer* cb) {
     auto target = [&](uint32_t& w, uint32_t& h) {
         if (!pipeline || !pass || !fb || subpass >= pass->subpasses.size()) return false;
         const Subpass& sub = pass->subpasses[subpass];
-        const uint32_t index = !sub.colour.empty() ? sub.colour[0] : sub.depth;
+        const uint32_t index = !sub.colour.empty() && sub.colour[0] != VK_ATTACHMENT_UNUSED ? sub.colour[0] : sub.depth;
         if (index == VK_ATTACHMENT_UNUSED || index >= fb->attachments.size()) return false;
         const ImageView* cv = fb->attachments[index];
         if (!cv || !cv->image) return false;

@@ -872,8 +872,11 @@ VKAPI_ATTR VkResult VKAPI_CALL CreateRenderPass(VkDevice, const VkRenderPassCrea
     for (uint32_t k = 0; k < ci->subpassCount; k++) {
         const auto& sp = ci->pSubpasses[k];
         Subpass sub;
-        for (uint32_t i = 0; i < sp.colorAttachmentCount; i++)
-            if (sp.pColorAttachments[i].attachment != VK_ATTACHMENT_UNUSED) sub.colour.push_back(sp.pColorAttachments[i].attachment);
+        // colour references keep their positions (location L of the
+        // fragment shader writes reference L); trailing unused ones are
+        // dropped, so a subpass whose only reference is unused has none
+        for (uint32_t i = 0; i < sp.colorAttachmentCount; i++) sub.colour.push_back(sp.pColorAttachments[i].attachment);
+        while (!sub.colour.empty() && sub.colour.back() == VK_ATTACHMENT_UNUSED) sub.colour.pop_back();
         if (sp.pDepthStencilAttachment) sub.depth = sp.pDepthStencilAttachment->attachment;
         rp->subpasses.push_back(sub);
     }

@@ -126,7 +126,7 @@ struct PipelineLayout {
 
 // The attachments one subpass draws to.
 struct Subpass {
-    std::vector<uint32_t> colour;     // colour attachment indices
+    std::vector<uint32_t> colour;     // colour attachment indices by position (VK_ATTACHMENT_UNUSED kept, none trailing)
     uint32_t depth = VK_ATTACHMENT_UNUSED;
 };
 
@@ -159,6 +159,7 @@ struct Pipeline {
     uint32_t colour_format = 0, depth_format = 0;
     bool blend = false;
     std::string stage;   // stage block: fixed-function macros + translated shaders (see compose_module)
+    std::string stage_after;  // after the stage functions: the colour attachments after the first
     uint32_t nv = 0;     // varying floats
     bool prefers_deferred = false;  // fragment shader samples images or is long
     uint32_t tile_shift = 4;        // screen tile of the pipeline's modules
@@ -174,6 +175,7 @@ struct ModuleConfig {
     uint32_t schedule = 0;    // fragment schedule: 0 immediate, 1 deferred, 2 sparse
     uint32_t warps = 8;       // warps per tile CTA (capped by the tile's pixels)
     uint32_t batch = 256;     // primitives set up per shared-memory batch (set per schedule by module_config)
+    uint32_t depth = 0;       // sparse schedule: fragments a pixel lists per batch (0: 24, or 16 when sampling)
     bool samples = false;     // a fragment shader samples images (register budget of the batched raster)
 };
 
@@ -187,7 +189,8 @@ ModuleConfig module_config(uint32_t tile_shift, bool prefers_deferred, bool fs_c
 // The CUDA translation unit of a module over one pipeline's stage block
 // (per-draw kernels) or several (batched kernels, pipeline i in namespace
 // cpv_p<i>).
-std::string compose_module(const std::vector<std::string>& stages, const std::vector<uint32_t>& nvs, const ModuleConfig& mc, bool batched);
+std::string compose_module(const std::vector<std::string>& stages, const std::vector<uint32_t>& nvs, const ModuleConfig& mc, bool batched,
+                           const std::vector<std::string>& afters = {});
 
 // ---- command recording ----
 enum class CmdType : uint8_t {

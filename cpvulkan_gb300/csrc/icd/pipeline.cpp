@@ -63,7 +63,7 @@ const char* const kStageMacros[] = {
     "CPV_BLEND", "CPV_SRC_COLOR", "CPV_DST_COLOR", "CPV_COLOR_OP", "CPV_SRC_ALPHA", "CPV_DST_ALPHA", "CPV_ALPHA_OP", "CPV_WRITE_MASK", "CPV_LOGIC", "CPV_LOGIC_OP",
     "CPV_DEPTH_BOUNDS", "CPV_MIN_DEPTH_BOUNDS", "CPV_MAX_DEPTH_BOUNDS",
     "CPV_COLOR_FORMAT", "CPV_DEPTH_FORMAT", "CPV_ORIGIN_UPPER", "CPV_FS_CONSTANT", "CPV_BLEND_TABLE", "CPV_LINE_WIDTH", "CPV_PRIM_KIND",
-    "CPV_CF_BYTES", "CPV_CF_CHANNELS", "CPV_CF_BITS", "CPV_CF_KIND", "CPV_CF_BGRA", "CPV_FS_KILL", "CPV_EARLY_DEPTH",
+    "CPV_CF_BYTES", "CPV_CF_CHANNELS", "CPV_CF_BITS", "CPV_CF_KIND", "CPV_CF_BGRA", "CPV_FS_KILL", "CPV_EARLY_DEPTH", "CPV_VS_SAMPLES", "CPV_EXTRA_CA",
 };
 
 }  // namespace
@@ -105,14 +105,25 @@ uint32_t schedule_for(bool prefers_deferred, bool fs_constant) {
     return fs_constant ? 0u : 2u;
 }
 
-std::string compose_module(const std::vector<std::string>& stages, const std::vector<uint32_t>& nvs, const ModuleConfig& mc, bool batched) {
+std::string compose_module(const std::vector<std::string>& stages, const std::vector<uint32_t>& nvs, const ModuleConfig& mc, bool batched,
+                           const std::vector<std::string>& afters) {
     uint32_t nv_max = 0;
     for (uint32_t nv : nvs) nv_max = nv > nv_max ? nv : nv_max;
+    // colour attachments of the pipelines' subpass (the pipelines of one
+    // module share it)
+    uint32_t num_ca = 1;
+    for (const std::string& st : stages) {
+        const size_t at = st.find("#define CPV_EXTRA_CA ");
+        if (at != std::string::npos) num_ca = std::max<uint32_t>(num_ca, 1u + static_cast<uint32_t>(std::atoi(st.c_str() + at + 21)));
+    }
+    // the deferred schedule records one colour per fragment
+    const uint32_t schedule = num_ca > 1 && mc.schedule == 1 ? 2u : mc.schedule;
     std::ostringstream src;
     src << "// " << kTranslationVersion << (batched ? " (batched)" : "") << "\n";
     src << "#define CPV_PIPELINE_MODULE 1\n";
     src << "#define CPV_TILE_SHIFT " << mc.tile_shift << "\n";
-    src << "#define CPV_SCHEDULE " << mc.schedule << "\n";
+    src << "#define CPV_SCHEDULE " << schedule << "\n";
+    src << "#define CPV_NUM_CA " << num_ca << "\n";
     src << "#define CPV_RT_WARPS " << mc.warps << "\n";
     src << "#define CPV_BATCH " << mc.batch << "\n";
     // Sparse schedule: fragments a pixel lists per batch before its
@@ -122,7 +133,7 @@ std::string compose_module(const std::vector<std::string>& stages, const std::ve
     // CPV_SLOT_DEPTH overrides; CPV_SMALL_PX sets the largest in-tile box one
     // thread rasterises (default 32).
     {
-        int depth = mc.samples ? 16 : 24;
+        int depth = mc.depth ? static_cast<int>(mc.depth) : (mc.samples ? 16 : 24);
         if (const char* v = std::getenv("CPV_SLOT_DEPTH")) depth = std::atoi(v);
         if (depth >= 1 && depth <= 255) src << "#define CPV_SLOT_DEPTH " << depth << "\n";
         if (const char* v = std::getenv("CPV_SMALL_PX")) {
@@ -148,6 +159,12 @@ std::string compose_module(const std::vector<std::string>& stages, const std::ve
         if (const char* v = std::getenv("CPV_BATCH_MIN_BLOCKS")) b = std::atoi(v);
         if (b >= 1 && b <= 32) src << "#define CPV_RT_MIN_BLOCKS " << b << "\n";
     }
+    // Register budget of the batched set-up in resident CTAs of 256
+    // threads (CPV_SETUP_MIN_BLOCKS overrides the kernel's default).
+    if (const char* v = std::getenv("CPV_SETUP_MIN_BLOCKS")) {
+        const int k = std::atoi(v);
+        if (k >= 1 && k <= 8) src << "#define CPV_SETUP_MIN_BLOCKS " << k << "\n";
+    }
     src << "#define CPV_NV_MAX " << nv_max << "\n";
     bool any_constant = false;
     for (const std::string& st : stages) any_constant = any_constant || st.find("#define CPV_FS_CONSTANT 1\n") != std::string::npos;
@@ -156,9 +173,15 @@ std::string compose_module(const std::vector<std::string>& stages, const std::ve
     for (const std::string& st : stages)
         any_lines = any_lines || st.find("#define CPV_TOPOLOGY 1\n") != std::string::npos || st.find("#define CPV_TOPOLOGY 2\n") != std::string::npos;
     src << "#define CPV_ANY_LINES " << (any_lines ? 1 : 0) << "\n";
+    // Vertex-side kernels fill the UNORM8 decode table only when a vertex
+    // shader samples an image.
+    bool any_vs_samples = false;
+    for (const std::string& st : stages) any_vs_samples = any_vs_samples || st.find("#define CPV_VS_SAMPLES 1\n") != std::string::npos;
+    src << "#define CPV_ANY_VS_SAMPLES " << (any_vs_samples ? 1 : 0) << "\n";
     src << "#include \"cpv_device.cuh\"\n#include \"cpv_raster.cuh\"\n";
     for (size_t i = 0; i < stages.size(); i++) {
         src << "namespace cpv_p" << i << " {\n" << stages[i] << "#include \"cpv_stage.cuh\"\n";
+        if (i < afters.size()) src << afters[i];
         for (const char* m : kStageMacros) src << "#undef " << m << "\n";
         src << "}  // namespace cpv_p" << i << "\n";
     }
@@ -219,7 +242,8 @@ bool module_cubin(Device* dev, const std::string& source, std::array<uint8_t, 32
 }  // namespace
 
 rt::Module* batch_module(Device* dev, const std::vector<Pipeline*>& pipelines, const ModuleConfig& mc) {
-    std::string id = std::to_string(mc.tile_shift) + "/" + std::to_string(mc.schedule) + "/" + std::to_string(mc.warps) + "/" + std::to_string(mc.batch);
+    std::string id = std::to_string(mc.tile_shift) + "/" + std::to_string(mc.schedule) + "/" + std::to_string(mc.warps) + "/" + std::to_string(mc.batch) +
+                     "/" + std::to_string(mc.depth);
     for (const Pipeline* p : pipelines) id += "/" + hex(p->key);
     {
         std::lock_guard<std::mutex> lock(dev->batch_mutex);
@@ -228,13 +252,14 @@ rt::Module* batch_module(Device* dev, const std::vector<Pipeline*>& pipelines, c
     }
     // Compiled and loaded outside the lock, so that several configurations
     // (the tuner's candidates) compile at once; the first one stored wins.
-    std::vector<std::string> stages;
+    std::vector<std::string> stages, afters;
     std::vector<uint32_t> nvs;
     for (const Pipeline* p : pipelines) {
         stages.push_back(p->stage);
+        afters.push_back(p->stage_after);
         nvs.push_back(p->nv);
     }
-    const std::string source = compose_module(stages, nvs, mc, true);
+    const std::string source = compose_module(stages, nvs, mc, true, afters);
     if (const char* dump = std::getenv("CPV_DUMP_DIR")) {
         std::ofstream f(std::string(dump) + "/batch_" + std::to_string(pipelines.size()) + "_" + std::to_string(mc.tile_shift) + ".cu");
         f << source;
@@ -310,12 +335,22 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
 
     const RenderPass* pass = reinterpret_cast<const RenderPass*>(ci.renderPass);
     if (!pass) return reject("no render pass");
-    // one colour attachment, or none (a depth-only pass)
+    // up to eight colour attachments (the reference's
+    // MAX_FRAGMENT_OUTPUT_ATTACHMENTS), or none (a depth-only pass); with
+    // several, the first must be used
     if (ci.subpass >= pass->subpasses.size()) return reject("subpass " + std::to_string(ci.subpass) + " of the render pass");
     const Subpass& sub = pass->subpasses[ci.subpass];
-    if (sub.colour.size() > 1) return reject("at most one colour attachment is supported");
+    const uint32_t nca = static_cast<uint32_t>(sub.colour.size());
+    if (nca > CPV_MAX_CA) return reject("more than 8 colour attachments");
+    if (nca > 1 && sub.colour[0] == VK_ATTACHMENT_UNUSED) return reject("an unused first colour attachment with others after it");
     const VkFormat cfmt = sub.colour.empty() ? VK_FORMAT_UNDEFINED : pass->attachments[sub.colour[0]].format;
     if (!sub.colour.empty() && !supported_colour(cfmt)) return reject("colour attachment format " + std::to_string(cfmt));
+    std::vector<VkFormat> extra_fmt;  // attachments 1 .. nca - 1 (UNDEFINED: unused)
+    for (uint32_t k = 1; k < nca; k++) {
+        const VkFormat f = sub.colour[k] == VK_ATTACHMENT_UNUSED ? VK_FORMAT_UNDEFINED : pass->attachments[sub.colour[k]].format;
+        if (f != VK_FORMAT_UNDEFINED && !supported_colour(f)) return reject("colour attachment format " + std::to_string(f));
+        extra_fmt.push_back(f);
+    }
     if (sub.colour.empty() && sub.depth == VK_ATTACHMENT_UNUSED) return reject("a colour or a depth attachment is required");
     VkFormat dfmt = VK_FORMAT_UNDEFINED;
     if (sub.depth != VK_ATTACHMENT_UNUSED) {
@@ -343,18 +378,35 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
             // widths and float formats are rejected.
             ColourLayout cl;
             if (!colour_layout(cfmt, cl) || cl.bits != 8 || cl.kind == 2) return reject("logic op on colour format " + std::to_string(cfmt));
+            for (VkFormat f : extra_fmt)
+                if (f != VK_FORMAT_UNDEFINED && (!colour_layout(f, cl) || cl.bits != 8 || cl.kind == 2))
+                    return reject("logic op on colour format " + std::to_string(f));
             if (static_cast<uint32_t>(ci.pColorBlendState->logicOp) > VK_LOGIC_OP_SET) return reject("logic op " + std::to_string(ci.pColorBlendState->logicOp));
             logic = true;
             logic_op = static_cast<uint32_t>(ci.pColorBlendState->logicOp);
             blend.blendEnable = VK_FALSE;
         }
     }
-    if (blend.blendEnable) {
-        auto bad = [](VkBlendFactor f) { return f > VK_BLEND_FACTOR_SRC_ALPHA_SATURATE; };
-        if (bad(blend.srcColorBlendFactor) || bad(blend.dstColorBlendFactor) || bad(blend.srcAlphaBlendFactor) || bad(blend.dstAlphaBlendFactor))
-            return reject("dual-source blend factors");
-        if (blend.colorBlendOp > VK_BLEND_OP_MAX || blend.alphaBlendOp > VK_BLEND_OP_MAX) return reject("advanced blend ops");
+    // each further attachment's own blend state (independent blending)
+    std::vector<VkPipelineColorBlendAttachmentState> extra_blend;
+    for (uint32_t k = 1; k < nca; k++) {
+        VkPipelineColorBlendAttachmentState b{};
+        b.colorWriteMask = 0xF;
+        if (ci.pColorBlendState && k < ci.pColorBlendState->attachmentCount) b = ci.pColorBlendState->pAttachments[k];
+        if (logic) b.blendEnable = VK_FALSE;
+        extra_blend.push_back(b);
     }
+    auto check_blend = [](const VkPipelineColorBlendAttachmentState& b) -> const char* {
+        if (!b.blendEnable) return nullptr;
+        auto bad = [](VkBlendFactor f) { return f > VK_BLEND_FACTOR_SRC_ALPHA_SATURATE; };
+        if (bad(b.srcColorBlendFactor) || bad(b.dstColorBlendFactor) || bad(b.srcAlphaBlendFactor) || bad(b.dstAlphaBlendFactor))
+            return "dual-source blend factors";
+        if (b.colorBlendOp > VK_BLEND_OP_MAX || b.alphaBlendOp > VK_BLEND_OP_MAX) return "advanced blend ops";
+        return nullptr;
+    };
+    if (const char* why = check_blend(blend)) return reject(why);
+    for (const auto& b : extra_blend)
+        if (const char* why = check_blend(b)) return reject(why);
 
     bool dyn_viewport = false, dyn_blend = false;
     if (ci.pDynamicState) {
@@ -438,34 +490,42 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
         src << "#define CPV_ST_" << sn[k] << "_WMASK " << so[k]->writeMask << "u\n";
         src << "#define CPV_ST_" << sn[k] << "_REF " << so[k]->reference << "u\n";
     }
-    src << "#define CPV_BLEND " << (blend.blendEnable ? 1 : 0) << "\n";
-    src << "#define CPV_SRC_COLOR " << static_cast<uint32_t>(blend.srcColorBlendFactor) << "\n";
-    src << "#define CPV_DST_COLOR " << static_cast<uint32_t>(blend.dstColorBlendFactor) << "\n";
-    src << "#define CPV_COLOR_OP " << static_cast<uint32_t>(blend.colorBlendOp) << "\n";
-    src << "#define CPV_SRC_ALPHA " << static_cast<uint32_t>(blend.srcAlphaBlendFactor) << "\n";
-    src << "#define CPV_DST_ALPHA " << static_cast<uint32_t>(blend.dstAlphaBlendFactor) << "\n";
-    src << "#define CPV_ALPHA_OP " << static_cast<uint32_t>(blend.alphaBlendOp) << "\n";
-    src << "#define CPV_WRITE_MASK " << (blend.colorWriteMask & 0xF) << "u\n";
+    // One colour attachment's macros: blend state, write mask, format and
+    // its layout (texel bytes, channels, bits per channel, kind 0 UNORM /
+    // 1 SNORM / 2 SFLOAT, red in byte 2).
+    auto colour_block = [](VkFormat f, const VkPipelineColorBlendAttachmentState& b) {
+        std::ostringstream o;
+        o << "#define CPV_BLEND " << (b.blendEnable ? 1 : 0) << "\n";
+        o << "#define CPV_SRC_COLOR " << static_cast<uint32_t>(b.srcColorBlendFactor) << "\n";
+        o << "#define CPV_DST_COLOR " << static_cast<uint32_t>(b.dstColorBlendFactor) << "\n";
+        o << "#define CPV_COLOR_OP " << static_cast<uint32_t>(b.colorBlendOp) << "\n";
+        o << "#define CPV_SRC_ALPHA " << static_cast<uint32_t>(b.srcAlphaBlendFactor) << "\n";
+        o << "#define CPV_DST_ALPHA " << static_cast<uint32_t>(b.dstAlphaBlendFactor) << "\n";
+        o << "#define CPV_ALPHA_OP " << static_cast<uint32_t>(b.alphaBlendOp) << "\n";
+        o << "#define CPV_WRITE_MASK " << (b.colorWriteMask & 0xF) << "u\n";
+        o << "#define CPV_COLOR_FORMAT " << static_cast<uint32_t>(f) << "\n";
+        ColourLayout cl;
+        if (f != VK_FORMAT_UNDEFINED) colour_layout(f, cl);
+        o << "#define CPV_CF_BYTES " << cl.bytes << "\n#define CPV_CF_CHANNELS " << cl.channels << "\n#define CPV_CF_BITS " << cl.bits
+          << "\n#define CPV_CF_KIND " << cl.kind << "\n#define CPV_CF_BGRA " << (cl.bgra ? 1 : 0) << "\n";
+        return o.str();
+    };
+    src << colour_block(cfmt, blend);
     src << "#define CPV_LOGIC " << (logic ? 1 : 0) << "\n";
     src << "#define CPV_LOGIC_OP " << logic_op << "\n";
-    src << "#define CPV_COLOR_FORMAT " << static_cast<uint32_t>(cfmt) << "\n";
-    {
-        // the colour attachment's layout: texel bytes, channels, bits per
-        // channel, kind (0 UNORM, 1 SNORM, 2 SFLOAT), red in byte 2
-        ColourLayout cl;
-        if (cfmt != VK_FORMAT_UNDEFINED) colour_layout(cfmt, cl);
-        src << "#define CPV_CF_BYTES " << cl.bytes << "\n#define CPV_CF_CHANNELS " << cl.channels << "\n#define CPV_CF_BITS " << cl.bits
-            << "\n#define CPV_CF_KIND " << cl.kind << "\n#define CPV_CF_BGRA " << (cl.bgra ? 1 : 0) << "\n";
-    }
+    src << "#define CPV_EXTRA_CA " << (nca > 1 ? nca - 1 : 0) << "\n";
     src << "#define CPV_DEPTH_FORMAT " << static_cast<uint32_t>(dfmt) << "\n";
     src << "#define CPV_ORIGIN_UPPER " << (fr.origin_upper_left ? 1 : 0) << "\n";
     // A fragment shader that reads neither FragCoord nor FrontFacing and only
     // flat inputs computes the same result for every fragment of a primitive:
     // it runs once per primitive at set-up.
-    bool fs_constant = !fr.reads_frag_coord && !fr.reads_front_facing;
+    // (With several colour attachments the fragment shader runs per
+    // fragment: a primitive record holds one colour.)
+    bool fs_constant = !fr.reads_frag_coord && !fr.reads_front_facing && nca <= 1;
     for (int k : fr.interp) fs_constant = fs_constant && k == 2;
     src << "#define CPV_FS_CONSTANT " << (fs_constant ? 1 : 0) << "\n";
     src << "#define CPV_FS_KILL " << (fr.has_kill ? 1 : 0) << "\n";
+    src << "#define CPV_VS_SAMPLES " << (vr.samples > 0 ? 1 : 0) << "\n";
     // Blending a per-primitive constant colour where each channel's result
     // depends only on that channel of the destination (no DST_ALPHA,
     // ONE_MINUS_DST_ALPHA or SRC_ALPHA_SATURATE colour factors): the result
@@ -483,15 +543,45 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
         if (fr.interp[i] != 0) src << "  case " << i << ": return " << fr.interp[i] << ";\n";
     src << "  default: return 0;\n  }\n}\n";
 
+    // Attachments 1 .. nca - 1: the fragment shader must declare an output
+    // for each used one (the reference looks the location up with
+    // std::map::at, LLVMRuntime/PipelineCompiler.cpp:1655-1659). Each is
+    // compiled from cpv_stage.cuh again in a nested namespace with its own
+    // colour macros, after the pipeline's own functions; the pipeline's
+    // cpv_load_extra / cpv_store_extra / cpv_write_extra call them.
+    std::ostringstream after;
+    if (nca > 1) {
+        static const char* const colour_macros[] = {"CPV_BLEND", "CPV_SRC_COLOR", "CPV_DST_COLOR", "CPV_COLOR_OP", "CPV_SRC_ALPHA", "CPV_DST_ALPHA",
+                                                    "CPV_ALPHA_OP", "CPV_WRITE_MASK", "CPV_COLOR_FORMAT", "CPV_CF_BYTES", "CPV_CF_CHANNELS",
+                                                    "CPV_CF_BITS", "CPV_CF_KIND", "CPV_CF_BGRA", "CPV_BLEND_TABLE", "CPV_EXTRA_CA"};
+        for (uint32_t k = 1; k < nca; k++) {
+            if (extra_fmt[k - 1] != VK_FORMAT_UNDEFINED && !((fr.outputs >> k) & 1u))
+                return reject("the fragment shader has no output for colour attachment " + std::to_string(k));
+            after << "namespace cpv_ca" << k << " {\n";
+            for (const char* m : colour_macros) after << "#undef " << m << "\n";
+            after << colour_block(extra_fmt[k - 1], extra_blend[k - 1]) << "#define CPV_BLEND_TABLE 0\n#define CPV_EXTRA_CA 0\n";
+            after << "#include \"cpv_stage.cuh\"\n}  // namespace cpv_ca" << k << "\n";
+        }
+        after << "__device__ __forceinline__ void cpv_load_extra(const uint8_t* const* c, uint64_t pix, CpvPixel& s) {\n";
+        for (uint32_t k = 1; k < nca; k++) after << "  s.extra[" << k - 1 << "] = cpv_ca" << k << "::cpv_load_colour(c[" << k - 1 << "], pix);\n";
+        after << "}\n__device__ __forceinline__ void cpv_store_extra(uint8_t* const* c, uint64_t pix, const CpvPixel& s) {\n";
+        for (uint32_t k = 1; k < nca; k++) after << "  cpv_ca" << k << "::cpv_store_colour(c[" << k - 1 << "], pix, s.extra[" << k - 1 << "]);\n";
+        after << "}\n__device__ __forceinline__ void cpv_write_extra(const float bc[4], const float* colour, CpvPixel& s) {\n";
+        for (uint32_t k = 1; k < nca; k++)
+            after << "  cpv_ca" << k << "::cpv_write_colour(bc, colour + " << 4 * k << ", s.extra[" << k - 1 << "]);\n";
+        after << "}\n";
+    }
+
     auto p = std::make_unique<Pipeline>();
     p->stage = src.str();
+    p->stage_after = after.str();
     p->nv = nv;
     p->prefers_deferred = prefers_deferred;
     p->samples = fr.samples > 0;
     p->tile_shift = tile_shift;
     p->blend_table = blend_table;
     p->fs_constant = fs_constant;
-    p->source = compose_module({p->stage}, {nv}, module_config(tile_shift, prefers_deferred, fs_constant, fr.samples > 0), false);
+    p->source = compose_module({p->stage}, {nv}, module_config(tile_shift, prefers_deferred, fs_constant, fr.samples > 0), false, {p->stage_after});
     // The key covers the generated source and the embedded kernel headers it
     // includes, so an on-disk cache never returns a cubin of older kernels.
     {

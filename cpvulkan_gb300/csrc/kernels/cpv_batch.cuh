@@ -36,8 +36,10 @@
  * set-up and raster kernels that follow (cpv_setup reads the slot instead of
  * shading the vertex again for each triangle and tile that uses it). */
 extern "C" __global__ void __launch_bounds__(CPV_BATCH_BLOCK) cpv_batch_vs(const __grid_constant__ CpvBatchParams B) {
-    cpv_lut8_init();  /* a vertex shader may sample images */
+#if CPV_ANY_VS_SAMPLES
+    cpv_lut8_init();  /* the vertex shader samples images */
     __syncthreads();
+#endif
     const uint32_t block = blockIdx.x;
     const uint32_t d = B.vs_block_draw[block];
     const CpvDrawParams& P = B.draws[d];
@@ -51,10 +53,19 @@ extern "C" __global__ void __launch_bounds__(CPV_BATCH_BLOCK) cpv_batch_vs(const
     cpv_dispatch(B.draw_pipeline[d], [&](auto S) { decltype(S)::vertex(P, P.vs_lo + v, P.first_instance + inst, local); });
 }
 
-extern "C" __global__ void __launch_bounds__(CPV_BATCH_BLOCK) cpv_batch_setup(const __grid_constant__ CpvBatchParams B) {
+/* register budget of the set-up: eight resident CTAs of 256 threads (32
+ * registers a thread). Its dependent loads (draw table, indices, vertex
+ * slots) leave it latency-bound: C4 set-up 11.8 ms at eight, 12.0 at six,
+ * 13.4 at five */
+#ifndef CPV_SETUP_MIN_BLOCKS
+#define CPV_SETUP_MIN_BLOCKS 8
+#endif
+extern "C" __global__ void __launch_bounds__(CPV_BATCH_BLOCK, CPV_SETUP_MIN_BLOCKS) cpv_batch_setup(const __grid_constant__ CpvBatchParams B) {
     __shared__ uint32_t warp_pairs[CPV_BATCH_BLOCK / 32];
-    cpv_lut8_init();  /* a vertex shader may sample images */
+#if CPV_ANY_VS_SAMPLES
+    cpv_lut8_init();  /* the vertex shader samples images */
     __syncthreads();
+#endif
     const uint32_t block = blockIdx.x;
     const uint32_t d = B.block_draw[block];
     const CpvDrawParams& P = B.draws[d];
@@ -117,22 +128,24 @@ struct CpvBatchSource {
         cpv_dispatch(pid, [&](auto S) { decltype(S)::template setup<true>(B.draws[d], local, t); });
         cpv_tri_tag(t, pid, d);
     }
-    __device__ __forceinline__ bool shade(const CpvTri& t, const float w[3], int32_t x, int32_t y, float colour[4], float& mapped,
+    __device__ __forceinline__ bool shade(const CpvTri& t, const float w[3], int32_t x, int32_t y, float* colour, float& mapped,
                                           const CpvPixel* early = nullptr) const {
         bool discard = false;
         const CpvDrawParams& P = B.draws[cpv_tri_draw(t)];
         cpv_dispatch(cpv_tri_pipeline(t), [&](auto S) { discard = decltype(S)::shade(P, t, w, x, y, colour, mapped, early); });
         return discard;
     }
-    __device__ __forceinline__ void rop(const CpvTri& t, const float colour[4], float mapped, CpvPixel& s) const {
+    __device__ __forceinline__ void rop(const CpvTri& t, const float* colour, float mapped, CpvPixel& s) const {
         const float* bc = B.draws[cpv_tri_draw(t)].blend_constants;
         const bool front = cpv_tri_front(t);
         cpv_dispatch(cpv_tri_pipeline(t), [&](auto S) { decltype(S)::rop(bc, front, colour, mapped, s); });
     }
     /* batched passes build no blend tables */
     __device__ __forceinline__ bool table_fragment(const CpvTri&, CpvPixel&) const { return false; }
-    __device__ __forceinline__ void load_pixel(uint64_t pix, CpvPixel& s) const { cpv_p0::Stage::load_pixel(B.color, B.depth, pix, s); }
-    __device__ __forceinline__ void store_pixel(uint64_t pix, const CpvPixel& s) const { cpv_p0::Stage::store_pixel(B.color, B.depth, pix, s); }
+    __device__ __forceinline__ void load_pixel(uint64_t pix, CpvPixel& s) const { cpv_p0::Stage::load_pixel(B.color, B.depth, pix, s, B.color_extra); }
+    __device__ __forceinline__ void store_pixel(uint64_t pix, const CpvPixel& s) const {
+        cpv_p0::Stage::store_pixel(B.color, B.depth, pix, s, B.color_extra);
+    }
 };
 
 /* Persistent raster: CTAs take tiles from B.tile_counter (reset to zero

@@ -24,6 +24,7 @@ typedef long long int64_t;
 #define CPV_MAX_TEX 4
 #define CPV_MAX_VARYINGS 16
 #define CPV_MAX_LEVELS 16
+#define CPV_MAX_CA 8 /* colour attachments per subpass (the reference's MAX_FRAGMENT_OUTPUT_ATTACHMENTS) */
 
 /* Status word bits written by kernels instead of trapping. */
 #define CPV_STATUS_LIST_OVERFLOW 0x1u
@@ -76,6 +77,7 @@ struct CpvDrawParams {
     /* attachments */
     uint8_t* color;
     uint8_t* depth;
+    uint8_t* color_extra[CPV_MAX_CA - 1]; /* colour attachments 1 .. of the subpass (null: unused) */
     uint32_t fb_width, fb_height;
     float viewport[6];
     float blend_constants[4];
@@ -125,6 +127,7 @@ struct CpvBatchParams {
     /* shared attachments and pixel-centre grid of the render pass */
     uint8_t* color;
     uint8_t* depth;
+    uint8_t* color_extra[CPV_MAX_CA - 1];
     uint32_t fb_width, fb_height;
     float vw, vh;
     uint32_t tiles_x, tiles_y;

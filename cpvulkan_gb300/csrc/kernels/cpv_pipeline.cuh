@@ -22,8 +22,10 @@
 #define CPV_PIPELINE_CUH
 
 extern "C" __global__ void __launch_bounds__(256) cpv_setup_rects(const __grid_constant__ CpvDrawParams P) {
-    cpv_lut8_init();  /* a vertex shader may sample images */
+#if CPV_ANY_VS_SAMPLES
+    cpv_lut8_init();  /* the vertex shader samples images */
     __syncthreads();
+#endif
     const uint64_t g = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (g >= P.total_prims) return;
     CpvTri t;
@@ -99,11 +101,11 @@ struct CpvPlainSource {
         }
         cpv_p0::Stage::setup<true>(P, g, t);
     }
-    __device__ __forceinline__ bool shade(const CpvTri& t, const float w[3], int32_t x, int32_t y, float colour[4], float& mapped,
+    __device__ __forceinline__ bool shade(const CpvTri& t, const float w[3], int32_t x, int32_t y, float* colour, float& mapped,
                                           const CpvPixel* early = nullptr) const {
         return cpv_p0::Stage::shade(P, t, w, x, y, colour, mapped, early);
     }
-    __device__ __forceinline__ void rop(const CpvTri& t, const float colour[4], float mapped, CpvPixel& s) const {
+    __device__ __forceinline__ void rop(const CpvTri& t, const float* colour, float mapped, CpvPixel& s) const {
         cpv_p0::Stage::rop(P.blend_constants, cpv_tri_front(t), colour, mapped, s, cpv_p0::Stage::table(P, t));
     }
     /* A covered fragment of a table-only pipeline: the table lookup is the
@@ -119,8 +121,10 @@ struct CpvPlainSource {
         }
         return false;
     }
-    __device__ __forceinline__ void load_pixel(uint64_t pix, CpvPixel& s) const { cpv_p0::Stage::load_pixel(P.color, P.depth, pix, s); }
-    __device__ __forceinline__ void store_pixel(uint64_t pix, const CpvPixel& s) const { cpv_p0::Stage::store_pixel(P.color, P.depth, pix, s); }
+    __device__ __forceinline__ void load_pixel(uint64_t pix, CpvPixel& s) const { cpv_p0::Stage::load_pixel(P.color, P.depth, pix, s, P.color_extra); }
+    __device__ __forceinline__ void store_pixel(uint64_t pix, const CpvPixel& s) const {
+        cpv_p0::Stage::store_pixel(P.color, P.depth, pix, s, P.color_extra);
+    }
 };
 
 /* Raster kernel: one CTA per screen tile (blockIdx.x = tile id).

@@ -22,13 +22,16 @@
 #define CPV_SCHEDULE 0 /* 0 immediate, 1 deferred, 2 sparse (see cpv_raster_tile) */
 #endif
 #define CPV_DEFERRED (CPV_SCHEDULE == 1)
+#if CPV_DEFERRED && CPV_NUM_CA > 1
+#error "the deferred schedule keeps one colour per recorded fragment: modules with several colour attachments use another"
+#endif
 #define CPV_SPARSE (CPV_SCHEDULE == 2)
 #define CPV_WARP_LISTS (CPV_SCHEDULE == 0) /* immediate: each warp walks only the primitives reaching its rows */
 #ifndef CPV_SLOT_DEPTH
 #define CPV_SLOT_DEPTH 16 /* sparse: fragments a pixel takes per batch before its fallback */
 #endif
 #ifndef CPV_SMALL_PX
-#define CPV_SMALL_PX 32 /* sparse: largest in-tile bounding box one thread rasterises */
+#define CPV_SMALL_PX 64 /* sparse: largest in-tile bounding box listed by the warp-spread tests (C4 raster 21.37 ms at 64, 21.65 at 32, 21.86 at 128) */
 #endif
 #ifndef CPV_RT_WARPS
 #define CPV_RT_WARPS 8
@@ -59,6 +62,14 @@
 #define CPV_BLOCK_H 4
 #ifndef CPV_ANY_LINES
 #define CPV_ANY_LINES 0 /* some pipeline of the module draws lines */
+#endif
+#ifndef CPV_NUM_CA
+#define CPV_NUM_CA 1 /* colour attachments of the module's subpass (up to 8; 1 also for a depth-only pass) */
+#endif
+/* fragment shader outputs: 4 floats per colour attachment */
+#define CPV_COLOUR_FLOATS (4 * CPV_NUM_CA)
+#ifndef CPV_ANY_VS_SAMPLES
+#define CPV_ANY_VS_SAMPLES 1 /* some pipeline's vertex shader samples images */
 #endif
 #define CPV_NV_ALLOC (CPV_NV_MAX > 0 ? CPV_NV_MAX : 1)
 #define CPV_NV_ROOM0 (CPV_ANY_FS_CONSTANT && CPV_NV_ALLOC < 4 ? 4 : CPV_NV_ALLOC)
@@ -336,6 +347,9 @@ struct CpvPixel {
     float depth;        /* decoded depth (D16: u16 / 65535) */
     uint32_t depth_raw; /* stored bits */
     uint32_t stencil;
+#if CPV_NUM_CA > 1
+    uint32_t extra[CPV_NUM_CA - 1]; /* texels of colour attachments 1 .. */
+#endif
 };
 
 /* Block-wide exclusive sum over CPV_RT_THREADS threads. */
@@ -450,10 +464,10 @@ __device__ __forceinline__ void cpv_list_small_warp(const CpvTri* tris, uint32_t
  * Source supplies:
  *   uint64_t count()                         primitives of this tile
  *   void setup(uint64_t i, CpvTri& t)        set up the i-th (or mark it dead)
- *   bool shade(const CpvTri&, const float w[3], int x, int y, float colour[4], float& mapped, const CpvPixel* early)
+ *   bool shade(const CpvTri&, const float w[3], int x, int y, float colour[CPV_COLOUR_FLOATS], float& mapped, const CpvPixel* early)
  *                                            (true: discarded, or failed the early depth
  *                                            test against *early when given)
- *   void rop(const CpvTri&, const float colour[4], float mapped, CpvPixel&)
+ *   void rop(const CpvTri&, const float colour[CPV_COLOUR_FLOATS], float mapped, CpvPixel&)
  *   bool table_fragment(const CpvTri&, CpvPixel&)  a covered fragment applied by a
  *                                            blend-table lookup alone (false: use shade + rop)
  *   void load_pixel(uint64_t pix, CpvPixel&) / store_pixel(uint64_t pix, const CpvPixel&)
@@ -619,7 +633,7 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
                         }
                         last = j;
                         const CpvTri& t = tris[j];
-                        float w[3], colour[4], mapped;
+                        float w[3], colour[CPV_COLOUR_FLOATS], mapped;
                         cpv_covers(t, xf[k], yf[k], w);
                         if (src.shade(t, w, px[k], py[k], colour, mapped, &st[k])) continue;
                         src.rop(t, colour, mapped, st[k]);
@@ -631,7 +645,7 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
                         if (!cpv_tri_live(t)) continue;
                         const int4 box = t.box;
                         if (px[k] < box.x || px[k] >= box.z || py[k] < box.y || py[k] >= box.w) continue;
-                        float w[3], colour[4], mapped;
+                        float w[3], colour[CPV_COLOUR_FLOATS], mapped;
                         if (!cpv_covers(t, xf[k], yf[k], w)) continue;
                         if (src.shade(t, w, px[k], py[k], colour, mapped, &st[k])) continue;
                         src.rop(t, colour, mapped, st[k]);
@@ -699,7 +713,7 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
                     /* the whole block is covered (one pixel a thread, all inside) */
                     const CpvTri& t = tris[j];
                     if (src.table_fragment(t, st[0])) continue;
-                    float w[3], colour[4], mapped;
+                    float w[3], colour[CPV_COLOUR_FLOATS], mapped;
                     cpv_covers(t, xf[0], yf[0], w);
                     if (src.shade(t, w, px[0], py[0], colour, mapped, &st[0])) continue;
                     src.rop(t, colour, mapped, st[0]);
@@ -719,7 +733,7 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
                     float w[3];
                     if (!cpv_covers(t, xf[k], yf[k], w)) continue;
                     if (src.table_fragment(t, st[k])) continue;
-                    float colour[4], mapped;
+                    float colour[CPV_COLOUR_FLOATS], mapped;
                     if (src.shade(t, w, px[k], py[k], colour, mapped, &st[k])) continue;
                     src.rop(t, colour, mapped, st[k]);
                 }
@@ -766,7 +780,7 @@ __device__ __forceinline__ void cpv_raster_tile(Source& src, uint32_t tx, uint32
                 const int32_t x = static_cast<int32_t>(tx * CPV_TILE + (owner % CPV_TILE));
                 const int32_t y = static_cast<int32_t>(ty * CPV_TILE + (owner / CPV_TILE) + k * CPV_ROWS_PER_PASS);
                 const float w[3] = {slot_f[5 * s + 0], slot_f[5 * s + 1], slot_f[5 * s + 2]};
-                float colour[4], mapped;
+                float colour[CPV_COLOUR_FLOATS], mapped;
                 const bool discard = src.shade(tris[j], w, x, y, colour, mapped);
                 slot_f[5 * s + 0] = colour[0];
                 slot_f[5 * s + 1] = colour[1];

@@ -11,7 +11,7 @@
  *   __device__ void cpv_vs_run(const CpvDrawParams&, uint32_t vertex_index,
  *                              uint32_t instance_index, float pos[4], float var[CPV_NV]);
  *   __device__ bool cpv_fs_run(const CpvDrawParams&, const float in[CPV_NV],
- *                              const float frag_coord[4], bool front, float colour[4]);
+ *                              const float frag_coord[4], bool front, float colour[4 * CPV_NUM_CA]);
  *   __device__ int  cpv_interp(int component);  // 0 perspective, 1 linear, 2 flat
  *
  * Vertex shading is recomputed where it is needed (set-up and raster) instead
@@ -57,7 +57,7 @@ __device__ __forceinline__ void cpv_shade_constant(const CpvDrawParams& P, const
 #pragma unroll
         for (int c = 0; c < CPV_NV_ALLOC; c++) in[c] = c < CPV_NV ? provoking[c] : 0.0f;
         const float frag_coord[4] = {0.0f, 0.0f, 0.0f, 1.0f};  /* not read by this shader */
-        float colour[4];
+        float colour[CPV_COLOUR_FLOATS];
         if (cpv_fs_run(P, in, frag_coord, front, colour)) live = false;
 #pragma unroll
         for (int c = 0; c < 4; c++) t.var[0][c] = colour[c];
@@ -425,6 +425,7 @@ __device__ __forceinline__ uint32_t cpv_cf_encode(float x) {
 #elif CPV_CF_KIND == 1
     const float v = roundf(__fmul_rn(fminf(fmaxf(x, -1.0f), 1.0f), CPV_CF_BITS == 8 ? 127.0f : 32767.0f));
     return static_cast<uint32_t>(static_cast<int32_t>(v)) & CPV_CF_MASK;
+
 #elif CPV_CF_BITS == 16
     return cpv_float_to_half(x);
 #else
@@ -432,16 +433,51 @@ __device__ __forceinline__ uint32_t cpv_cf_encode(float x) {
 #endif
 }
 
-__device__ __forceinline__ void cpv_load_pixel(const uint8_t* color, const uint8_t* depth, uint64_t pix, CpvPixel& s) {
+/* The colour texel of pixel `pix` of this attachment (0 without one). */
+__device__ __forceinline__ uint32_t cpv_load_colour(const uint8_t* color, uint64_t pix) {
 #if CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 1
-    s.colour = color[pix];
+    return color[pix];
 #elif CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 2
-    s.colour = reinterpret_cast<const uint16_t*>(color)[pix];
+    return reinterpret_cast<const uint16_t*>(color)[pix];
 #elif CPV_COLOR_FORMAT != 0
-    s.colour = reinterpret_cast<const uint32_t*>(color)[pix];
+    return reinterpret_cast<const uint32_t*>(color)[pix];
 #else
-    (void)color; /* a depth-only pass */
-    s.colour = 0u;
+    (void)color; (void)pix; /* a depth-only pass, or an unused attachment */
+    return 0u;
+#endif
+}
+
+__device__ __forceinline__ void cpv_store_colour(uint8_t* color, uint64_t pix, uint32_t texel) {
+#if CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 1
+    color[pix] = static_cast<uint8_t>(texel);
+#elif CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 2
+    reinterpret_cast<uint16_t*>(color)[pix] = static_cast<uint16_t>(texel);
+#elif CPV_COLOR_FORMAT != 0
+    reinterpret_cast<uint32_t*>(color)[pix] = texel;
+#else
+    (void)color; (void)pix; (void)texel;
+#endif
+}
+
+#ifndef CPV_EXTRA_CA
+#define CPV_EXTRA_CA 0 /* this pipeline's colour attachments after the first */
+#endif
+#if CPV_EXTRA_CA > 0
+/* The attachments after the first: each has its own format, blend state and
+ * write mask, compiled from this file again in a nested namespace
+ * (cpv_ca1 …); these are defined after those namespaces. */
+__device__ __forceinline__ void cpv_load_extra(const uint8_t* const* color, uint64_t pix, CpvPixel& s);
+__device__ __forceinline__ void cpv_store_extra(uint8_t* const* color, uint64_t pix, const CpvPixel& s);
+__device__ __forceinline__ void cpv_write_extra(const float blend_constants[4], const float* colour, CpvPixel& s);
+#endif
+
+__device__ __forceinline__ void cpv_load_pixel(const uint8_t* color, const uint8_t* depth, uint64_t pix, CpvPixel& s,
+                                               const uint8_t* const* extra = nullptr) {
+    s.colour = cpv_load_colour(color, pix);
+#if CPV_EXTRA_CA > 0
+    cpv_load_extra(extra, pix, s);
+#else
+    (void)extra;
 #endif
 #if CPV_DEPTH_FORMAT == 124
     s.depth_raw = reinterpret_cast<const uint16_t*>(depth)[pix];
@@ -464,15 +500,12 @@ __device__ __forceinline__ void cpv_load_pixel(const uint8_t* color, const uint8
 #endif
 }
 
-__device__ __forceinline__ void cpv_store_pixel(uint8_t* color, uint8_t* depth, uint64_t pix, const CpvPixel& s) {
-#if CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 1
-    color[pix] = static_cast<uint8_t>(s.colour);
-#elif CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 2
-    reinterpret_cast<uint16_t*>(color)[pix] = static_cast<uint16_t>(s.colour);
-#elif CPV_COLOR_FORMAT != 0
-    reinterpret_cast<uint32_t*>(color)[pix] = s.colour;
+__device__ __forceinline__ void cpv_store_pixel(uint8_t* color, uint8_t* depth, uint64_t pix, const CpvPixel& s, uint8_t* const* extra = nullptr) {
+    cpv_store_colour(color, pix, s.colour);
+#if CPV_EXTRA_CA > 0
+    cpv_store_extra(extra, pix, s);
 #else
-    (void)color;
+    (void)extra;
 #endif
 #if CPV_DEPTH_FORMAT == 124
     reinterpret_cast<uint16_t*>(depth)[pix] = static_cast<uint16_t>(s.depth_raw);
@@ -526,7 +559,7 @@ __device__ __forceinline__ void cpv_blend(const float s[4], const float d[4], co
  * depth mapping (:1300-1313) and the fragment shader. Returns true when the
  * shader discards, or when `early` (the pixel's current state) is given and
  * the fragment fails the early depth test. */
-__device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& t, const float wr[3], int32_t x, int32_t y, float colour[4],
+__device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& t, const float wr[3], int32_t x, int32_t y, float* colour,
                                           float& mapped, const CpvPixel* early = nullptr) {
     float in[CPV_NV_ALLOC];
 #if CPV_PRIM_KIND == 2
@@ -651,10 +684,56 @@ __device__ __forceinline__ uint32_t cpv_logic(uint32_t s, uint32_t d) {
     return r & 0xFFu;
 }
 
+/* The colour write of this attachment for a fragment that passed every
+ * test (LLVMRuntime/PipelineCompiler.cpp:1528-1727): logic op, else blend
+ * (CPVulkan/CommandBuffer.Draw.cpp:956-1262), else the colour; then the
+ * write mask and the format's encoder. `colour` is this attachment's output. */
+__device__ __forceinline__ void cpv_write_colour(const float blend_constants[4], const float colour[4], uint32_t& texel) {
+#if CPV_COLOR_FORMAT == 0
+    (void)blend_constants; (void)colour; (void)texel;
+#else
+#if CPV_LOGIC
+    /* 8-bit normalised formats only (pipeline creation rejects others) */
+    (void)blend_constants;
+    uint32_t logic = 0u;
+#pragma unroll
+    for (int i = 0; i < CPV_CF_CHANNELS; i++) {
+        const uint32_t d = (texel >> cpv_channel_shift(i)) & 0xFFu;
+        const uint32_t byte = ((CPV_WRITE_MASK >> i) & 1u) ? (cpv_logic(cpv_cf_encode(colour[i]), d) & 0xFFu) : d;
+        logic |= byte << cpv_channel_shift(i);
+    }
+    texel = logic;
+#else
+    float out[4];
+#if CPV_BLEND
+    /* the destination as the reference's decoder returns it: absent
+     * channels read (0, 0, 0, 1) */
+    float dst[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+        dst[i] = i < CPV_CF_CHANNELS ? cpv_cf_decode((texel >> cpv_channel_shift(i)) & CPV_CF_MASK) : (i == 3 ? 1.0f : 0.0f);
+    cpv_blend(colour, dst, blend_constants, out);
+#else
+    (void)blend_constants;
+#pragma unroll
+    for (int i = 0; i < 4; i++) out[i] = colour[i];
+#endif
+    /* the format's channels, each encoded or, outside the write mask, kept */
+    uint32_t packed = 0u;
+#pragma unroll
+    for (int i = 0; i < CPV_CF_CHANNELS; i++) {
+        const uint32_t field = ((CPV_WRITE_MASK >> i) & 1u) ? cpv_cf_encode(out[i]) : ((texel >> cpv_channel_shift(i)) & CPV_CF_MASK);
+        packed |= field << cpv_channel_shift(i);
+    }
+    texel = packed;
+#endif
+#endif
+}
+
 /* Order as the reference's fragment wrapper: current values → depth bounds
  * test → stencil test → depth test → depth / stencil write → colour write
  * (logic op or blend, write mask, encode). */
-__device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool front, const float colour[4], float mapped, CpvPixel& s,
+__device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool front, const float* colour, float mapped, CpvPixel& s,
                                         const uint8_t* table = nullptr) {
     const bool has_depth = CPV_DEPTH_FORMAT != 0;
 #if CPV_DEPTH_BOUNDS && CPV_DEPTH_FORMAT != 0
@@ -703,41 +782,10 @@ __device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool fro
 #else
         (void)table;
 #endif
-#if CPV_LOGIC
-        /* 8-bit normalised formats only (pipeline creation rejects others) */
-        (void)blend_constants;
-        uint32_t logic = 0u;
-#pragma unroll
-        for (int i = 0; i < CPV_CF_CHANNELS; i++) {
-            const uint32_t d = (s.colour >> cpv_channel_shift(i)) & 0xFFu;
-            const uint32_t byte = ((CPV_WRITE_MASK >> i) & 1u) ? (cpv_logic(cpv_cf_encode(colour[i]), d) & 0xFFu) : d;
-            logic |= byte << cpv_channel_shift(i);
-        }
-        s.colour = logic;
-        return;
+        cpv_write_colour(blend_constants, colour, s.colour);
+#if CPV_EXTRA_CA > 0
+        cpv_write_extra(blend_constants, colour, s);
 #endif
-        float out[4];
-#if CPV_BLEND
-        /* the destination as the reference's decoder returns it: absent
-         * channels read (0, 0, 0, 1) */
-        float dst[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-            dst[i] = i < CPV_CF_CHANNELS ? cpv_cf_decode((s.colour >> cpv_channel_shift(i)) & CPV_CF_MASK) : (i == 3 ? 1.0f : 0.0f);
-        cpv_blend(colour, dst, blend_constants, out);
-#else
-        (void)blend_constants;
-#pragma unroll
-        for (int i = 0; i < 4; i++) out[i] = colour[i];
-#endif
-        /* the format's channels, each encoded or, outside the write mask, kept */
-        uint32_t packed = 0u;
-#pragma unroll
-        for (int i = 0; i < CPV_CF_CHANNELS; i++) {
-            const uint32_t field = ((CPV_WRITE_MASK >> i) & 1u) ? cpv_cf_encode(out[i]) : ((s.colour >> cpv_channel_shift(i)) & CPV_CF_MASK);
-            packed |= field << cpv_channel_shift(i);
-        }
-        s.colour = packed;
     }
 }
 
@@ -793,11 +841,11 @@ struct Stage {
         (void)P; (void)vid; (void)instance; (void)slot;
 #endif
     }
-    static __device__ __forceinline__ bool shade(const CpvDrawParams& P, const CpvTri& t, const float w[3], int32_t x, int32_t y, float colour[4],
+    static __device__ __forceinline__ bool shade(const CpvDrawParams& P, const CpvTri& t, const float w[3], int32_t x, int32_t y, float* colour,
                                                  float& mapped, const CpvPixel* early = nullptr) {
         return cpv_shade(P, t, w, x, y, colour, mapped, early);
     }
-    static __device__ __forceinline__ void rop(const float blend_constants[4], bool front, const float colour[4], float mapped, CpvPixel& s,
+    static __device__ __forceinline__ void rop(const float blend_constants[4], bool front, const float* colour, float mapped, CpvPixel& s,
                                                const uint8_t* table = nullptr) {
         cpv_rop(blend_constants, front, colour, mapped, s, table);
     }
@@ -811,6 +859,11 @@ struct Stage {
         return nullptr;
 #endif
     }
-    static __device__ __forceinline__ void load_pixel(const uint8_t* c, const uint8_t* d, uint64_t pix, CpvPixel& s) { cpv_load_pixel(c, d, pix, s); }
-    static __device__ __forceinline__ void store_pixel(uint8_t* c, uint8_t* d, uint64_t pix, const CpvPixel& s) { cpv_store_pixel(c, d, pix, s); }
+    /* `extra`: the colour attachments after the first (unused without them) */
+    static __device__ __forceinline__ void load_pixel(const uint8_t* c, const uint8_t* d, uint64_t pix, CpvPixel& s, const uint8_t* const* extra) {
+        cpv_load_pixel(c, d, pix, s, extra);
+    }
+    static __device__ __forceinline__ void store_pixel(uint8_t* c, uint8_t* d, uint64_t pix, const CpvPixel& s, uint8_t* const* extra) {
+        cpv_store_pixel(c, d, pix, s, extra);
+    }
 };

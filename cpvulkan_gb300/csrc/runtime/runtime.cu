@@ -689,6 +689,7 @@ int BatchPlan::build(const Module& m, const BatchDraws& in, cudaStream_t stream)
     P_.total_blocks = static_cast<uint32_t>(blocks);
     P_.color = in.color;
     P_.depth = in.depth;
+    for (int k = 0; k < CPV_MAX_CA - 1; k++) P_.color_extra[k] = in.color_extra[k];
     P_.fb_width = in.fb_width;
     P_.fb_height = in.fb_height;
     P_.vw = in.vw;

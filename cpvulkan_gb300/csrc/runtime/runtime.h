@@ -130,6 +130,7 @@ struct BatchDraws {
     std::vector<uint8_t> triangles;  // per draw: the pipeline assembles triangles (the vertex stage applies)
     uint8_t* color = nullptr;
     uint8_t* depth = nullptr;
+    uint8_t* color_extra[CPV_MAX_CA - 1] = {};
     uint32_t fb_width = 0, fb_height = 0;
     float vw = 0.0f, vh = 0.0f;
 };

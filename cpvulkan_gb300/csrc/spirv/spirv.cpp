@@ -427,6 +427,7 @@ private:
     bool has_kill_ = false;
     uint32_t samples_ = 0;
     uint32_t instructions_ = 0;
+    uint32_t out_outputs_ = 0;  // FS output locations declared
 
     bool fail(const std::string& e) {
         if (err_.empty()) err_ = e;
@@ -967,11 +968,18 @@ bool Translator::emit_globals(const EntryPoint& ep, StageResult& out) {
                     }
                 } else {
                     if (is_builtin) return fail("unsupported fragment output builtin " + std::to_string(builtin));
-                    if (has_location && location == 0) {
+                    if (has_location) {
+                        // output L feeds colour attachment L of the subpass
+                        // (LLVMRuntime/PipelineCompiler.cpp:1415-1429, 1655-1667);
+                        // outputs beyond the module's attachments are dropped
+                        if (location >= 8) return fail("fragment output location beyond the 8 colour attachments");
                         const Type* t = type(tid);
                         if (!t || t->kind != TypeKind::Vector || t->count != 4 || !is_float_scalar(t->component))
-                            return fail("fragment output 0 must be a vec4");
-                        for (int i = 0; i < 4; i++) epi_ << "  cpv_colour[" << i << "] = " << var << ".v[" << i << "];\n";
+                            return fail("fragment output " + std::to_string(location) + " must be a vec4");
+                        if (location > 0) epi_ << "#if CPV_NUM_CA > " << location << "\n";
+                        for (int i = 0; i < 4; i++) epi_ << "  cpv_colour[" << 4 * location + i << "] = " << var << ".v[" << i << "];\n";
+                        if (location > 0) epi_ << "#endif\n";
+                        out_outputs_ |= 1u << location;
                     }
                 }
             }
@@ -1508,6 +1516,7 @@ bool Translator::run(const std::string& entry_name, StageResult& out, std::strin
     out.has_kill = has_kill_;
     out.samples = samples_;
     out.instructions = instructions_;
+    out.outputs = out_outputs_;
     const std::string ns = model_ == 0 ? "cpv_vs_ns" : "cpv_fs_ns";
     std::ostringstream s;
     s << "namespace " << ns << " {\n" << types_.str() << loaders_.str() << "}\n";

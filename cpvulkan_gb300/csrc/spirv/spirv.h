@@ -133,6 +133,7 @@ struct StageResult {
     uint32_t instructions = 0; // SPIR-V instructions of the entry function
     bool reads_frag_coord = false;    // FS: FragCoord is an input
     bool reads_front_facing = false;  // FS: FrontFacing is an input
+    uint32_t outputs = 0;             // FS: bit L set when an output is declared at location L (< 8)
 };
 
 // Translates the entry point of `m` for `model` (0 vertex, 4 fragment) into a

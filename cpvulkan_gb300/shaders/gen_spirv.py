@@ -468,6 +468,46 @@ def fetch_frag():
     return m.assemble(body)
 
 
+def mrt_frag():
+    """layout(location=0) in vec4 c; layout(location=L) out vec4 oL (L = 0..7);
+    void main() {
+        o0 = c;                                        o1 = vec4(1.0 - c.rgb, c.a);
+        o2 = c.zxyw;                                   o3 = c * 0.5;
+        o4 = c * c;                                    o5 = c * 2.0 - vec4(1.0);
+        o6 = vec4(c.x + c.y, c.y - c.z, c.z, 0.25);    o7 = c.wzyx; }
+    One output per colour attachment of a subpass of up to eight."""
+    m = Module(4)
+    v4, v3, f = m.vec(4), m.vec(3), m.float()
+    col = m.variable("Input", v4, "color")
+    m.decorate(col, "Location", 0)
+    outs = []
+    for k in range(8):
+        o = m.variable("Output", v4, "o%d" % k)
+        m.decorate(o, "Location", k)
+        outs.append(o)
+    one3 = m._const(("cc_one3",), "ConstantComposite", lambda: v3, lambda: [m.const_f(1.0)] * 3)
+    one4 = m._const(("cc_one4",), "ConstantComposite", lambda: v4, lambda: [m.const_f(1.0)] * 4)
+
+    def body(m):
+        c = m.load(v4, col)
+        m.store(outs[0], c)
+        rgb = m.op("VectorShuffle", v3, c, c, 0, 1, 2)
+        inv = m.op("FSub", v3, one3, rgb)
+        a = m.op("CompositeExtract", f, c, 3)
+        m.store(outs[1], m.op("CompositeConstruct", v4, inv, a))
+        m.store(outs[2], m.op("VectorShuffle", v4, c, c, 2, 0, 1, 3))
+        m.store(outs[3], m.op("VectorTimesScalar", v4, c, m.const_f(0.5)))
+        m.store(outs[4], m.op("FMul", v4, c, c))
+        m.store(outs[5], m.op("FSub", v4, m.op("VectorTimesScalar", v4, c, m.const_f(2.0)), one4))
+        x = m.op("CompositeExtract", f, c, 0)
+        y = m.op("CompositeExtract", f, c, 1)
+        z = m.op("CompositeExtract", f, c, 2)
+        m.store(outs[6], m.op("CompositeConstruct", v4, m.op("FAdd", f, x, y), m.op("FSub", f, y, z), z, m.const_f(0.25)))
+        m.store(outs[7], m.op("VectorShuffle", v4, c, c, 3, 2, 1, 0))
+        m.op_void("Return")
+    return m.assemble(body)
+
+
 PROGRAMS = {
     "cube": (cube_vert, lambda: colour_frag()),
     "texlit": (texlit_vert, texlit_frag),
@@ -477,6 +517,7 @@ PROGRAMS = {
     "nopersp": (cube_vert, lambda: colour_frag("NoPerspective")),
     "points": (points_vert, colour_frag),
     "fetch": (texlit_vert, fetch_frag),
+    "mrt": (cube_vert, mrt_frag),
 }
 
 

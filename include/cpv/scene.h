@@ -35,12 +35,23 @@ enum cpv_program {
     CPV_PROGRAM_POINTS = 6,      /* CUBE that also writes gl_PointSize = colour.a * 16                          */
     CPV_PROGRAM_FETCH = 7,       /* TEXLIT's vertex shader; FS: texelFetch at uv * (K * 8 + 8) with K a
                                     specialisation constant (default 3), bitCount, a copy between variables */
-    CPV_PROGRAM_COUNT = 8
+    CPV_PROGRAM_MRT = 8,         /* CUBE's vertex shader; FS: eight outputs (locations 0-7), each a different
+                                    function of the colour, one per colour attachment                         */
+    CPV_PROGRAM_COUNT = 9
 };
 
 #define CPV_SCENE_MAX_BINDINGS 4
 #define CPV_SCENE_MAX_ATTRIBUTES 8
 #define CPV_SCENE_MAX_PUSH 128
+#define CPV_SCENE_MAX_EXTRA_COLOR 7 /* colour attachments after the first */
+
+/* Blend state of one colour attachment after the first. */
+typedef struct cpv_scene_attachment_blend {
+    uint32_t blend_enable;
+    uint32_t src_color, dst_color, color_op;
+    uint32_t src_alpha, dst_alpha, alpha_op;
+    uint32_t color_write_mask; /* VkColorComponentFlags */
+} cpv_scene_attachment_blend;
 
 typedef struct cpv_scene_binding {
     uint32_t binding;
@@ -83,6 +94,7 @@ typedef struct cpv_scene_pipeline {
     uint32_t depth_bounds_test;              /* VkPipelineDepthStencilStateCreateInfo::depthBoundsTestEnable */
     float min_depth_bounds, max_depth_bounds;
     uint32_t spec_k;           /* non-zero: the fragment shader's specialisation constant 0 (a 32-bit int) */
+    cpv_scene_attachment_blend extra_blend[CPV_SCENE_MAX_EXTRA_COLOR]; /* colour attachments 1 .. */
 } cpv_scene_pipeline;
 
 typedef struct cpv_scene_draw {
@@ -136,6 +148,11 @@ typedef struct cpv_scene {
     const cpv_scene_pipeline* pipelines;
     uint32_t num_draws;
     const cpv_scene_draw* draws;
+
+    /* colour attachments after the first (same size; 0 formats: unused
+     * references), referenced by the subpass in order after it */
+    uint32_t extra_color_count;
+    uint32_t extra_color_formats[CPV_SCENE_MAX_EXTRA_COLOR];
 } cpv_scene;
 
 #ifdef __cplusplus

@@ -89,6 +89,9 @@ int cpvh_renderer_set_indirect_count(cpvh_renderer* r, uint32_t draw, uint32_t c
 
 /* Reads the attachments back (colour: width*height*4; depth: texel-sized). */
 int cpvh_readback(cpvh_renderer* r, uint8_t* color, uint8_t* depth);
+/* Colour attachment k (1 .. 7) of the scene's subpass after the last frame:
+ * width * height texels of its format (zeros for an unused reference). */
+int cpvh_readback_extra(cpvh_renderer* r, uint32_t k, uint8_t* out);
 
 /* Creates and destroys one of each host object kind the ICD places in an
  * application allocator (buffer, device memory, image, image view, render

@@ -360,6 +360,7 @@ ProgramInfo program_info(uint32_t program) {
     case CPV_PROGRAM_DISCARD: return {1, {4}, {INTERP_PERSPECTIVE}};
     case CPV_PROGRAM_NOPERSP: return {1, {4}, {INTERP_LINEAR}};
     case CPV_PROGRAM_POINTS: return {1, {4}, {INTERP_PERSPECTIVE}};
+    case CPV_PROGRAM_MRT: return {1, {4}, {INTERP_PERSPECTIVE}};
     default: return {0, {0}, {INTERP_PERSPECTIVE}};
     }
 }
@@ -388,7 +389,8 @@ void run_vs(uint32_t program, const float attr[8][4], const Resources& r, VsOut&
     case CPV_PROGRAM_CUBE:
     case CPV_PROGRAM_DISCARD:
     case CPV_PROGRAM_NOPERSP:
-    case CPV_PROGRAM_POINTS: {
+    case CPV_PROGRAM_POINTS:
+    case CPV_PROGRAM_MRT: {
         float m[16];
         for (int i = 0; i < 16; i++) m[i] = ubo_at(r, i);
         for (int i = 0; i < 4; i++) out.var[i] = attr[1][i];
@@ -428,9 +430,25 @@ void run_vs(uint32_t program, const float attr[8][4], const Resources& r, VsOut&
 }
 
 /* Returns true when the fragment is discarded (OpKill → return true,
- * LLVMRuntime/SPIRVCompiler.cpp:3308-3310, 3642-3651). */
-bool run_fs(uint32_t program, const float* in, const Resources& r, float colour[4], uint32_t spec_k) {
+ * LLVMRuntime/SPIRVCompiler.cpp:3308-3310, 3642-3651). colour holds 4
+ * floats per output location (locations 0-7); a program fills the
+ * locations it declares. */
+bool run_fs(uint32_t program, const float* in, const Resources& r, float* colour, uint32_t spec_k) {
     switch (program) {
+    case CPV_PROGRAM_MRT: {
+        /* gen_spirv.py mrt_frag: one SPIR-V operation per float operation */
+        const float* c = in;
+        for (int i = 0; i < 4; i++) colour[i] = c[i];
+        for (int i = 0; i < 3; i++) colour[4 + i] = 1.0f - c[i];
+        colour[7] = c[3];
+        colour[8] = c[2]; colour[9] = c[0]; colour[10] = c[1]; colour[11] = c[3];
+        for (int i = 0; i < 4; i++) colour[12 + i] = c[i] * 0.5f;
+        for (int i = 0; i < 4; i++) colour[16 + i] = c[i] * c[i];
+        for (int i = 0; i < 4; i++) colour[20 + i] = c[i] * 2.0f - 1.0f;
+        colour[24] = c[0] + c[1]; colour[25] = c[1] - c[2]; colour[26] = c[2]; colour[27] = 0.25f;
+        colour[28] = c[3]; colour[29] = c[2]; colour[30] = c[1]; colour[31] = c[0];
+        return false;
+    }
     case CPV_PROGRAM_CUBE:
     case CPV_PROGRAM_NOPERSP:
     case CPV_PROGRAM_FLATQUAD:
@@ -664,6 +682,8 @@ struct Frame {
     uint8_t* depth;
     uint32_t depth_size;
     uint32_t colour_size;  /* bytes per colour texel */
+    uint8_t* extra[CPV_SCENE_MAX_EXTRA_COLOR] = {};       /* colour attachments 1 .. (null: unused or not given) */
+    uint32_t extra_size[CPV_SCENE_MAX_EXTRA_COLOR] = {};  /* their bytes per texel */
     Resources res;
     cpv_oracle_stats* stats;
     /* Rows this frame writes: y % row_stride == row_index (1, 0: all rows).
@@ -875,7 +895,7 @@ uint8_t logic_op(uint32_t op, uint8_t s, uint8_t d) {
  * colour write mask keeps the stored byte of every channel it leaves out
  * (the reference aborts on a partial mask, PipelineCompiler.cpp:1693-1700;
  * this follows Vulkan 1.1, "Color Write Mask"). */
-void write_colour(uint8_t* texel, uint32_t fmt, const cpv_scene_pipeline& p, const float colour[4]) {
+void write_colour(uint8_t* texel, uint32_t fmt, const cpv_scene_pipeline& p, const cpv_scene_attachment_blend& b, const float colour[4]) {
     ColourFormat cf;
     if (!colour_format(fmt, cf)) return;
     uint8_t enc[4][4];
@@ -887,17 +907,22 @@ void write_colour(uint8_t* texel, uint32_t fmt, const cpv_scene_pipeline& p, con
         }
     } else {
         float out[4];
-        if (p.blend_enable) {
+        if (b.blend_enable) {
             float dst[4];
             get_colour(texel, fmt, dst);
-            blend(colour, dst, p.blend_constants, p.src_color, p.dst_color, p.color_op, p.src_alpha, p.dst_alpha, p.alpha_op, out);
+            blend(colour, dst, p.blend_constants, b.src_color, b.dst_color, b.color_op, b.src_alpha, b.dst_alpha, b.alpha_op, out);
         } else {
             for (int i = 0; i < 4; i++) out[i] = colour[i];
         }
         for (uint32_t i = 0; i < cf.channels; i++) encode_channel(out[i], cf, enc[i]);
     }
     for (uint32_t i = 0; i < cf.channels; i++)
-        if ((p.color_write_mask >> i) & 1u) std::memcpy(texel + cf.off[i], enc[i], cf.esize);
+        if ((b.color_write_mask >> i) & 1u) std::memcpy(texel + cf.off[i], enc[i], cf.esize);
+}
+
+/* The first colour attachment's blend state, from the pipeline's fields. */
+cpv_scene_attachment_blend first_blend(const cpv_scene_pipeline& p) {
+    return {p.blend_enable, p.src_color, p.dst_color, p.color_op, p.src_alpha, p.dst_alpha, p.alpha_op, p.color_write_mask};
 }
 
 /* Interpolation (CPVulkan/CommandBuffer.Draw.cpp:816-871). */
@@ -921,7 +946,7 @@ float interp_linear(const float v[3], const float w[3]) {
 void fragment(Frame& f, const cpv_scene_pipeline& p, uint32_t x, uint32_t y, float depth_mapped, bool front, const float* inputs) {
     const cpv_scene* s = f.s;
     f.stats->fragments++;
-    float colour[4];
+    float colour[32];
     if (run_fs(p.program, inputs, f.res, colour, p.spec_k)) return;
 
     const uint64_t pix = static_cast<uint64_t>(y) * s->width + x;
@@ -966,7 +991,13 @@ void fragment(Frame& f, const cpv_scene_pipeline& p, uint32_t x, uint32_t y, flo
     }
 
     if (stencil_result && depth_result) {
-        if (s->color_format) write_colour(f.colour + pix * f.colour_size, s->color_format, p, colour);
+        /* every colour attachment of the subpass, each with its output and
+         * blend state (CompileWriteFragment, PipelineCompiler.cpp:1415-1429) */
+        if (s->color_format) {
+            write_colour(f.colour + pix * f.colour_size, s->color_format, p, first_blend(p), colour);
+            for (uint32_t k = 0; k < s->extra_color_count; k++)
+                if (f.extra[k]) write_colour(f.extra[k] + pix * f.extra_size[k], s->extra_color_formats[k], p, p.extra_blend[k], colour + 4 * (k + 1));
+        }
         f.stats->fragments_written++;
     }
 }
@@ -1452,8 +1483,17 @@ void render_threaded(Frame& f, Shared& sh, uint32_t tid, uint32_t n, uint32_t en
 }
 
 /* Checks a scene and fills the parts of `f` and `tex` every render needs. */
-int prepare(const cpv_scene* scene, uint8_t* color, uint8_t* depth, Frame& f, Texture& tex) {
+int prepare(const cpv_scene* scene, uint8_t* color, uint8_t* depth, Frame& f, Texture& tex, uint8_t* const* extra = nullptr) {
     if (!scene || !color) return -1;
+    if (scene->extra_color_count > CPV_SCENE_MAX_EXTRA_COLOR) return -2;
+    for (uint32_t k = 0; k < scene->extra_color_count; k++) {
+        ColourFormat ecf{};
+        const uint32_t fmt = scene->extra_color_formats[k];
+        if (!fmt) continue;
+        if (!colour_format(fmt, ecf)) return -2;
+        f.extra[k] = extra ? extra[k] : nullptr;
+        f.extra_size[k] = ecf.bytes;
+    }
     ColourFormat cf{};
     if (scene->color_format != 0 && !colour_format(scene->color_format, cf)) return -2;
     if (scene->color_format == 0 && scene->depth_format == 0) return -2;
@@ -1496,8 +1536,12 @@ int prepare(const cpv_scene* scene, uint8_t* color, uint8_t* depth, Frame& f, Te
 void clear(const Frame& f) {
     const cpv_scene* scene = f.s;
     const uint64_t pixels = static_cast<uint64_t>(scene->width) * scene->height;
-    if (scene->color_format)  // a depth-only pass leaves `color` untouched
+    if (scene->color_format) {  // a depth-only pass leaves `color` untouched
         for (uint64_t i = 0; i < pixels; i++) set_colour(f.colour + i * f.colour_size, scene->color_format, scene->clear_color);
+        for (uint32_t k = 0; k < scene->extra_color_count; k++)
+            if (f.extra[k])
+                for (uint64_t i = 0; i < pixels; i++) set_colour(f.extra[k] + i * f.extra_size[k], scene->extra_color_formats[k], scene->clear_color);
+    }
     if (f.depth) {
         for (uint64_t i = 0; i < pixels; i++) {
             uint8_t* t = f.depth + i * f.depth_size;
@@ -1513,10 +1557,15 @@ extern "C" {
 
 int cpv_oracle_render(const cpv_scene* scene, uint8_t* color, uint8_t* depth, uint32_t do_clear, uint32_t draw_begin,
                       uint32_t draw_end, cpv_oracle_stats* stats) {
+    return cpv_oracle_render_extra(scene, color, nullptr, depth, do_clear, draw_begin, draw_end, stats);
+}
+
+int cpv_oracle_render_extra(const cpv_scene* scene, uint8_t* color, uint8_t* const* extra, uint8_t* depth, uint32_t do_clear,
+                            uint32_t draw_begin, uint32_t draw_end, cpv_oracle_stats* stats) {
     cpv_oracle_stats local{};
     Frame f{};
     Texture tex;
-    const int r = prepare(scene, color, depth, f, tex);
+    const int r = prepare(scene, color, depth, f, tex, extra);
     if (r != 0) return r;
     f.stats = stats ? stats : &local;
     if (do_clear) clear(f);

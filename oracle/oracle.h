@@ -49,6 +49,12 @@ typedef struct cpv_oracle_stats {
 int cpv_oracle_render(const cpv_scene* scene, uint8_t* color, uint8_t* depth, uint32_t do_clear,
                       uint32_t draw_begin, uint32_t draw_end, cpv_oracle_stats* stats);
 
+/* cpv_oracle_render with the scene's colour attachments after the first:
+ * extra[k] is attachment k + 1 (width*height texels of its format), null
+ * for an unused reference; extra may be null when the scene has none. */
+int cpv_oracle_render_extra(const cpv_scene* scene, uint8_t* color, uint8_t* const* extra, uint8_t* depth, uint32_t do_clear,
+                            uint32_t draw_begin, uint32_t draw_end, cpv_oracle_stats* stats);
+
 /* The same render on `threads` host threads (the reference renders on one;
  * this is the oracle's own parallel form, for full-size checks): the
  * assembly of each draw instance is made once, vertex shading and triangle

@@ -28,6 +28,8 @@ class Oracle:
         f, u32, vp = ctypes.c_float, ctypes.c_uint32, ctypes.c_void_p
         lib.cpv_oracle_render.restype = ctypes.c_int
         lib.cpv_oracle_render.argtypes = [vp, vp, vp, u32, u32, u32, ctypes.POINTER(Stats)]
+        lib.cpv_oracle_render_extra.restype = ctypes.c_int
+        lib.cpv_oracle_render_extra.argtypes = [vp, vp, vp, vp, u32, u32, u32, ctypes.POINTER(Stats)]
         lib.cpv_oracle_render_threaded.restype = ctypes.c_int
         lib.cpv_oracle_render_threaded.argtypes = [vp, vp, vp, u32, u32, u32, u32, ctypes.POINTER(Stats)]
         lib.cpv_oracle_edge.restype = f
@@ -68,6 +70,24 @@ class Oracle:
             raise RuntimeError("oracle rejected the scene (%d)" % r)
         return color, (depth if dsz else None), {k: getattr(st, k) for k, _ in Stats._fields_}
 
+
+    def render_extra(self, scene):
+        """Renders a scene with colour attachments after the first; returns
+        (color, [attachment 1, ...], depth or None, stats), each attachment
+        HxWxB uint8 in its format (zeros for an unused reference)."""
+        from cpvulkan_gb300 import colour_texel_bytes, depth_texel_bytes
+        h, w = scene.height, scene.width
+        color = np.zeros((h, w, colour_texel_bytes(scene.color_format)), np.uint8)
+        extras = [np.zeros((h, w, colour_texel_bytes(f)), np.uint8) for f in scene.extra_color_formats]
+        ptrs = (ctypes.c_void_p * 7)(*[(e.ctypes.data if f else None) for e, f in zip(extras, scene.extra_color_formats)])
+        dsz = depth_texel_bytes(scene.depth_format)
+        depth = np.zeros((h, w, dsz), np.uint8) if dsz else None
+        st = Stats()
+        r = self.lib.cpv_oracle_render_extra(scene.ptr, color.ctypes.data, ptrs, depth.ctypes.data if dsz else None, 1, 0, 0xFFFFFFFF,
+                                             ctypes.byref(st))
+        if r != 0:
+            raise RuntimeError("oracle rejected the scene (%d)" % r)
+        return color, extras, depth, {k: getattr(st, k) for k, _ in Stats._fields_}
 
     def render_threaded(self, scene, threads=None, draw_begin=0, draw_end=None, color=None, depth=None, clear=True):
         """render() on `threads` host threads (default: every usable core);

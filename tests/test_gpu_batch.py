@@ -101,15 +101,17 @@ def test_batched_program_variants(gpu_ctx, plain, monkeypatch):
 @pytest.mark.parametrize("seed", [6, 7])
 def test_tuned_batch_equals_plain(gpu_ctx, plain, monkeypatch, seed):
     """The tuner runs the pass once per candidate (tile 8/16/32, warps per
-    tile) on its first submission, restoring the attachments around each
-    run: the frames must still equal the per-draw path's, and the report
-    must name every candidate and the choice."""
+    tile, batch size, schedule and, for the sparse schedule, the per-pixel
+    fragment-list depth) on its first submission, restoring the attachments
+    around each run: the frames must still equal the per-draw path's, and
+    the report must name every candidate and the choice."""
     monkeypatch.setenv("CPV_AUTOTUNE", "1")
     scene = c.Scene(c.BATCH, seed, [32, 3000, 352, 208])
     ref = plain(gpu_ctx, scene)[0]
     runs = frames(gpu_ctx, scene, 3)
     report = c.batch_tuning()
-    assert report.count(" ms") == 7 and "chosen tile" in report, report
+    assert report.count(" ms") == 9 and "chosen tile" in report, report
+    assert "depth 16" in report and "depth 32" in report, report
     for got in runs:
         same(got, ref)
 

@@ -256,3 +256,49 @@ def test_colour_attachment_formats_batched(gpu_ctx, oracle, monkeypatch, fmt):
     scene = c.Scene(c.PROGRAM, 3, [c.PROGRAM_CUBE, 0x10 | 0x20, 64, 48, 24, 97, fmt])
     report, _ = check(gpu_ctx, oracle, scene)
     assert report["color_pixels_differing"] == 0, report
+
+
+def _pack(values):
+    """Bytes of a packed scene parameter (byte k = values[k])."""
+    out = 0
+    for k, v in enumerate(values):
+        out |= int(v) << (8 * k)
+    return out
+
+
+# Several colour attachments (the MRT program writes locations 0-7): the
+# formats of attachments 1 .. (0: an unused reference in the middle) and
+# each one's blend byte (bit 0 src-over, bit 1 additive colour with MAX
+# alpha, bits 4-7 a write mask), with the first attachment's variant.
+MRT_CASES = [
+    ([37], [0x01], 0x10),                                   # two RGBA8, the second blended
+    ([83, 100, 9], [0x02, 0x00, 0x00], 0x10 | 0x20),        # half, float, R8; the first blended too
+    ([38, 0, 77, 16, 70, 37, 44], [0x00, 0x00, 0x30, 0x01, 0x02, 0x90, 0x01], 0x18 | 0x100),  # eight, one unused; stencil
+    ([37, 9, 16], [0x00, 0x00, 0x10], 0x10 | 0x40000 | (6 << 20)),  # a logic op on every 8-bit attachment
+]
+
+
+@pytest.mark.parametrize("case", range(len(MRT_CASES)))
+@pytest.mark.parametrize("batched", [False, True])
+def test_colour_attachments(gpu_ctx, oracle, monkeypatch, case, batched):
+    """Up to eight colour attachments per subpass, each with its own format,
+    blend state and write mask, fed by the fragment shader's output at its
+    location (LLVMRuntime/PipelineCompiler.cpp:1415-1429): every attachment
+    equals the oracle's, per draw and batched."""
+    if batched:
+        monkeypatch.setenv("CPV_BATCH_MIN_DRAWS", "1")
+    fmts, blends, variant = MRT_CASES[case]
+    scene = c.Scene(c.PROGRAM, 3 + case, [c.PROGRAM_MRT, variant, 64, 48, 24, 0, 0, _pack(fmts), _pack(blends)])
+    r = c.Renderer(gpu_ctx, scene)
+    try:
+        r.render(1)
+        gc, gd = r.readback()
+        gx = [r.readback_extra(k + 1) for k in range(len(fmts))]
+    finally:
+        r.close()
+    rc, rx, rd, stats = oracle.render_extra(scene)
+    assert stats["fragments_written"] > 0
+    report = compare(scene, gc, gd, rc, rd)
+    assert report["color_pixels_differing"] == 0, report
+    for k, (g, o) in enumerate(zip(gx, rx)):
+        assert np.count_nonzero(np.any(g != o, axis=-1)) == 0, "attachment %d (format %d)" % (k + 1, fmts[k])

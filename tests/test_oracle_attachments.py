@@ -1,0 +1,51 @@
+"""The oracle's colour attachments after the first (CPU): each attachment
+receives the fragment shader's output at its location, through its own
+format, blend state and write mask."""
+import numpy as np
+
+import cpvulkan_gb300 as c
+
+
+def _pack(values):
+    out = 0
+    for k, v in enumerate(values):
+        out |= int(v) << (8 * k)
+    return out
+
+
+def test_first_attachment_equals_single_attachment_render(oracle):
+    # the MRT program's location 0 is the cube program's output
+    mrt = c.Scene(c.PROGRAM, 2, [c.PROGRAM_MRT, 0x10 | 0x20, 64, 48, 24, 0, 0, _pack([83, 9]), _pack([0x01, 0x00])])
+    cube = c.Scene(c.PROGRAM, 2, [c.PROGRAM_CUBE, 0x10 | 0x20, 64, 48, 24])
+    col, extras, dep, st = oracle.render_extra(mrt)
+    col0, dep0, st0 = oracle.render(cube)
+    assert np.array_equal(col, col0) and np.array_equal(dep, dep0)
+    assert st["fragments_written"] == st0["fragments_written"] > 0
+    assert [e.shape[-1] for e in extras] == [4, 1]
+
+
+def test_float_attachments_follow_their_outputs(oracle):
+    # every attachment R32_SFLOAT, no blending: location 1 holds 1 - c.r and
+    # location 3 c.r * 0.5 (exact in binary32), location 0 c.r
+    scene = c.Scene(c.PROGRAM, 5, [c.PROGRAM_MRT, 0x10, 64, 48, 24, 0, 100, _pack([100, 100, 100]), 0])
+    col, extras, _, st = oracle.render_extra(scene)
+    r0 = col.view(np.float32)[..., 0]
+    r1 = extras[0].view(np.float32)[..., 0]
+    r3 = extras[2].view(np.float32)[..., 0]
+    clear = np.float32(-0.3)
+    drawn = r0 != clear
+    assert drawn.any()
+    assert np.array_equal(r1[drawn], np.float32(1.0) - r0[drawn])
+    assert np.array_equal(r3[drawn], r0[drawn] * np.float32(0.5))
+    assert np.all(r1[~drawn] == clear) and np.all(r3[~drawn] == clear)
+
+
+def test_write_mask_and_unused_reference(oracle):
+    # attachment 2 unused (zeros), attachment 1 with a green-only write mask
+    # keeps the clear colour's other channels
+    scene = c.Scene(c.PROGRAM, 6, [c.PROGRAM_MRT, 0x10, 64, 48, 24, 0, 0, _pack([37, 0, 37]), _pack([0x20, 0x00, 0x00])])
+    col, extras, _, _ = oracle.render_extra(scene)
+    assert not extras[1].any()
+    m = extras[0]
+    assert np.all(m[..., [0, 2, 3]] == np.array([64, 191, 255], np.uint8))  # clear (0.25, 0.5, 0.75, 1) encoded, kept
+    assert (m[..., 1] != 128).any()  # green written somewhere

@@ -249,3 +249,23 @@ def test_logic_op_on_8bit_colour_formats_compiles(compile_ctx):
     for fmt in (9, 16, 38):
         ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [c.PROGRAM_CUBE, 0x40000 | (6 << 20), 32, 32, 4, 0, fmt]))
     assert len(glob.glob(str(dump / "pipeline_*.cu"))) == 3
+
+
+def test_colour_attachments_compile_and_reject(native, monkeypatch, tmp_path):
+    """A subpass of eight colour references (one unused) compiles per draw
+    and batched; a fragment shader without an output for a used attachment
+    is rejected at pipeline creation (the reference looks the location up
+    with std::map::at)."""
+    for k, v in {"CPV_COMPILE_ONLY": "1", "CPV_CACHE_DIR": str(tmp_path), "CPVH_RECORD_ONLY": "1", "CPV_AUTOTUNE": "0",
+                 "CPV_BATCH_MIN_DRAWS": "1"}.items():
+        monkeypatch.setenv(k, v)
+    fmts = 44 | (83 << 8) | (100 << 16) | (9 << 24) | (38 << 32) | (0 << 40) | (77 << 48)
+    ctx = c.Context()
+    try:
+        c.Renderer(ctx, c.Scene(c.PROGRAM, 1, [c.PROGRAM_MRT, 0x10, 32, 32, 4, 0, 0, fmts, 0x0201])).close()
+        assert "batched module compiled" in c.icd_last_error()
+        with pytest.raises(RuntimeError):
+            c.Renderer(ctx, c.Scene(c.PROGRAM, 1, [c.PROGRAM_CUBE, 0x10, 32, 32, 4, 0, 0, 37, 0]))
+        assert "no output for colour attachment 1" in c.icd_last_error()
+    finally:
+        ctx.close()
