@@ -20,7 +20,7 @@ MANIFEST_PATH = os.path.join(BUILD_DIR, "CPVulkan.json")
 # Scene configurations (include/cpv_harness.h).
 CUBE, HEIGHTFIELD, BLEND, BATCH, PROGRAM, SERVE = 1, 2, 3, 4, 5, 6
 # Shader programs (include/cpv/scene.h).
-PROGRAM_CUBE, PROGRAM_TEXLIT, PROGRAM_FLATQUAD, PROGRAM_MESHPC, PROGRAM_DISCARD, PROGRAM_NOPERSP, PROGRAM_POINTS, PROGRAM_FETCH, PROGRAM_MRT = range(9)
+PROGRAM_CUBE, PROGRAM_TEXLIT, PROGRAM_FLATQUAD, PROGRAM_MESHPC, PROGRAM_DISCARD, PROGRAM_NOPERSP, PROGRAM_POINTS, PROGRAM_FETCH, PROGRAM_MRT, PROGRAM_MRTI = range(10)
 
 VK_FORMAT_D16_UNORM = 124
 VK_FORMAT_D32_SFLOAT = 126
@@ -67,7 +67,7 @@ def colour_texel_bytes(fmt):
     """Bytes per texel of a colour attachment format (R8_UNORM 1; R8G8_UNORM
     and R16_UNORM 2; the 4-byte formats otherwise); a depth-only pass reads
     back zeros in the 4-byte layout."""
-    return {0: 4, 9: 1, 16: 2, 70: 2}.get(fmt, 4)
+    return {0: 4, 9: 1, 13: 1, 14: 1, 16: 2, 20: 2, 21: 2, 70: 2, 74: 2, 75: 2}.get(fmt, 4)
 
 
 _harness = None

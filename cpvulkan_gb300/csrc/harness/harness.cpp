@@ -271,7 +271,29 @@ void destroy_image(cpvh_context* c, ImageAlloc& i) {
 
 // Bytes per texel of a colour attachment format; 4 for a depth-only pass,
 // whose readback holds zeros in the RGBA8 layout.
-uint32_t colour_texel_size(uint32_t f) { return f == VK_FORMAT_R8_UNORM ? 1 : ((f == VK_FORMAT_R8G8_UNORM || f == VK_FORMAT_R16_UNORM) ? 2 : 4); }
+uint32_t colour_texel_size(uint32_t f) {
+    switch (f) {
+    case VK_FORMAT_R8_UNORM: case VK_FORMAT_R8_UINT: case VK_FORMAT_R8_SINT: return 1;
+    case VK_FORMAT_R8G8_UNORM: case VK_FORMAT_R16_UNORM: case VK_FORMAT_R8G8_UINT: case VK_FORMAT_R8G8_SINT: case VK_FORMAT_R16_UINT:
+    case VK_FORMAT_R16_SINT: return 2;
+    default: return 4;
+    }
+}
+// Integer colour formats: cleared with the integers round(clear_color * 100).
+bool integer_colour(uint32_t f) {
+    switch (f) {
+    case VK_FORMAT_R8_UINT: case VK_FORMAT_R8_SINT: case VK_FORMAT_R8G8_UINT: case VK_FORMAT_R8G8_SINT: case VK_FORMAT_R8G8B8A8_UINT:
+    case VK_FORMAT_R8G8B8A8_SINT: case VK_FORMAT_R16_UINT: case VK_FORMAT_R16_SINT: case VK_FORMAT_R16G16_UINT: case VK_FORMAT_R16G16_SINT:
+    case VK_FORMAT_R32_UINT: case VK_FORMAT_R32_SINT: return true;
+    default: return false;
+    }
+}
+void clear_value_for(uint32_t fmt, const float c[4], VkClearValue& v) {
+    for (int i = 0; i < 4; i++) {
+        if (integer_colour(fmt)) v.color.int32[i] = static_cast<int32_t>(std::lround(c[i] * 100.0f));
+        else v.color.float32[i] = c[i];
+    }
+}
 uint32_t depth_texel_size(uint32_t f) { return f == VK_FORMAT_D16_UNORM ? 2 : (f == VK_FORMAT_D32_SFLOAT ? 4 : (f == VK_FORMAT_D32_SFLOAT_S8_UINT ? 8 : 0)); }
 
 VkResult submit_and_wait(cpvh_renderer* r, VkCommandBuffer cmd) {
@@ -362,13 +384,9 @@ void record_frame(cpvh_renderer* r, VkCommandBuffer cmd) {
     // colour attachments (the same clear colour), depth
     uint32_t nclears = 0;
     if (s->color_format) {
-        for (int i = 0; i < 4; i++) clears[nclears].color.float32[i] = s->clear_color[i];
-        nclears++;
-        for (uint32_t k = 0; k < s->extra_color_count; k++) {
-            if (!s->extra_color_formats[k]) continue;
-            for (int i = 0; i < 4; i++) clears[nclears].color.float32[i] = s->clear_color[i];
-            nclears++;
-        }
+        clear_value_for(s->color_format, s->clear_color, clears[nclears++]);
+        for (uint32_t k = 0; k < s->extra_color_count; k++)
+            if (s->extra_color_formats[k]) clear_value_for(s->extra_color_formats[k], s->clear_color, clears[nclears++]);
     }
     if (s->depth_format) {
         clears[nclears].depthStencil.depth = s->clear_depth;

@@ -177,7 +177,17 @@ bool clear_texel(VkFormat fmt, const VkClearValue& cv, uint32_t& lo, uint32_t& h
         // float), at its bit offset; red in byte 2 for B8G8R8A8
         const int shift_bgra[4] = {16, 8, 0, 24};
         for (uint32_t ch = 0; ch < cl.channels; ch++) {
-            const uint32_t field = encode_channel_host(cv.color.float32[ch], cl);
+            uint32_t field;
+            if (cl.kind == 3) {  // UINT: the uint32 clear value, clamped to the channel's maximum
+                const uint32_t m = cl.bits >= 32 ? 0xFFFFFFFFu : ((1u << cl.bits) - 1u);
+                field = std::min(cv.color.uint32[ch], m);
+            } else if (cl.kind == 4) {  // SINT: the int32 clear value, clamped to the channel's range
+                const int32_t hi_v = cl.bits >= 32 ? INT32_MAX : ((1 << (cl.bits - 1)) - 1), lo_v = -hi_v - 1;
+                const int32_t v = std::max(std::min(cv.color.int32[ch], hi_v), lo_v);
+                field = static_cast<uint32_t>(v) & (cl.bits >= 32 ? 0xFFFFFFFFu : ((1u << cl.bits) - 1u));
+            } else {
+                field = encode_channel_host(cv.color.float32[ch], cl);
+            }
             lo |= field << (cl.bgra ? shift_bgra[ch] : static_cast<int>(cl.bits * ch));
         }
         return true;

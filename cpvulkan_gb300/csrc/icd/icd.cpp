@@ -25,13 +25,15 @@ namespace cpv::icd {
 
 uint32_t format_texel_size(VkFormat f) {
     switch (f) {
-    case VK_FORMAT_R8_UNORM: case VK_FORMAT_R8_UINT: case VK_FORMAT_S8_UINT: return 1;
-    case VK_FORMAT_R8G8_UNORM: case VK_FORMAT_D16_UNORM: case VK_FORMAT_R16_UNORM: case VK_FORMAT_R16_SFLOAT: return 2;
+    case VK_FORMAT_R8_UNORM: case VK_FORMAT_R8_UINT: case VK_FORMAT_R8_SINT: case VK_FORMAT_S8_UINT: return 1;
+    case VK_FORMAT_R8G8_UNORM: case VK_FORMAT_R8G8_UINT: case VK_FORMAT_R8G8_SINT: case VK_FORMAT_D16_UNORM: case VK_FORMAT_R16_UNORM:
+    case VK_FORMAT_R16_UINT: case VK_FORMAT_R16_SINT: case VK_FORMAT_R16_SFLOAT: return 2;
     case VK_FORMAT_D16_UNORM_S8_UINT: return 3;
     case VK_FORMAT_R8G8B8A8_UNORM: case VK_FORMAT_R8G8B8A8_SNORM: case VK_FORMAT_R8G8B8A8_UINT: case VK_FORMAT_R8G8B8A8_SINT:
     case VK_FORMAT_R8G8B8A8_SRGB: case VK_FORMAT_B8G8R8A8_UNORM: case VK_FORMAT_B8G8R8A8_SRGB: case VK_FORMAT_R32_UINT:
     case VK_FORMAT_R32_SINT: case VK_FORMAT_R32_SFLOAT: case VK_FORMAT_D32_SFLOAT: case VK_FORMAT_X8_D24_UNORM_PACK32:
-    case VK_FORMAT_D24_UNORM_S8_UINT: case VK_FORMAT_R16G16_UNORM: case VK_FORMAT_R16G16_SFLOAT:
+    case VK_FORMAT_D24_UNORM_S8_UINT: case VK_FORMAT_R16G16_UNORM: case VK_FORMAT_R16G16_SFLOAT: case VK_FORMAT_R16G16_UINT:
+    case VK_FORMAT_R16G16_SINT:
         return 4;
     case VK_FORMAT_R32G32_UINT: case VK_FORMAT_R32G32_SINT: case VK_FORMAT_R32G32_SFLOAT: case VK_FORMAT_D32_SFLOAT_S8_UINT: return 8;
     case VK_FORMAT_R32G32B32_UINT: case VK_FORMAT_R32G32B32_SINT: case VK_FORMAT_R32G32B32_SFLOAT: return 12;
@@ -51,6 +53,20 @@ bool colour_layout(VkFormat f, ColourLayout& out) {
     case VK_FORMAT_R16G16_UNORM: out = {4, 2, 16, 0, false}; return true;
     case VK_FORMAT_R16G16_SFLOAT: out = {4, 2, 16, 2, false}; return true;
     case VK_FORMAT_R32_SFLOAT: out = {4, 1, 32, 2, false}; return true;
+    // integer formats (kind 3 UINT, 4 SINT): the shader output's bits,
+    // clamped to the channel's range (LLVMRuntime/ImageCompiler.cpp:1121-1175)
+    case VK_FORMAT_R8_UINT: out = {1, 1, 8, 3, false}; return true;
+    case VK_FORMAT_R8_SINT: out = {1, 1, 8, 4, false}; return true;
+    case VK_FORMAT_R8G8_UINT: out = {2, 2, 8, 3, false}; return true;
+    case VK_FORMAT_R8G8_SINT: out = {2, 2, 8, 4, false}; return true;
+    case VK_FORMAT_R8G8B8A8_UINT: out = {4, 4, 8, 3, false}; return true;
+    case VK_FORMAT_R8G8B8A8_SINT: out = {4, 4, 8, 4, false}; return true;
+    case VK_FORMAT_R16_UINT: out = {2, 1, 16, 3, false}; return true;
+    case VK_FORMAT_R16_SINT: out = {2, 1, 16, 4, false}; return true;
+    case VK_FORMAT_R16G16_UINT: out = {4, 2, 16, 3, false}; return true;
+    case VK_FORMAT_R16G16_SINT: out = {4, 2, 16, 4, false}; return true;
+    case VK_FORMAT_R32_UINT: out = {4, 1, 32, 3, false}; return true;
+    case VK_FORMAT_R32_SINT: out = {4, 1, 32, 4, false}; return true;
     default: return false;
     }
 }
@@ -283,6 +299,10 @@ VKAPI_ATTR void VKAPI_CALL GetPhysicalDeviceFormatProperties(VkPhysicalDevice, V
         // computed in float and encoded to the format)
         p->linearTilingFeatures = p->optimalTilingFeatures = VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BIT | VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BLEND_BIT |
                                                              VK_FORMAT_FEATURE_TRANSFER_SRC_BIT | VK_FORMAT_FEATURE_TRANSFER_DST_BIT;
+        if (cl.kind >= 3) {  // integer formats are not blended
+            p->linearTilingFeatures &= ~VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BLEND_BIT;
+            p->optimalTilingFeatures &= ~VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BLEND_BIT;
+        }
     }
     if (f == VK_FORMAT_R8G8B8A8_UNORM || f == VK_FORMAT_B8G8R8A8_UNORM) {
         p->linearTilingFeatures = p->optimalTilingFeatures = VK_FORMAT_FEATURE_SAMPLED_IMAGE_BIT | VK_FORMAT_FEATURE_COLOR_ATTACHMENT_BIT |

@@ -377,9 +377,9 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
             // (LLVMRuntime/PipelineCompiler.cpp:1687-1690); formats of other
             // widths and float formats are rejected.
             ColourLayout cl;
-            if (!colour_layout(cfmt, cl) || cl.bits != 8 || cl.kind == 2) return reject("logic op on colour format " + std::to_string(cfmt));
+            if (!colour_layout(cfmt, cl) || cl.bits != 8 || cl.kind >= 2) return reject("logic op on colour format " + std::to_string(cfmt));
             for (VkFormat f : extra_fmt)
-                if (f != VK_FORMAT_UNDEFINED && (!colour_layout(f, cl) || cl.bits != 8 || cl.kind == 2))
+                if (f != VK_FORMAT_UNDEFINED && (!colour_layout(f, cl) || cl.bits != 8 || cl.kind >= 2))
                     return reject("logic op on colour format " + std::to_string(f));
             if (static_cast<uint32_t>(ci.pColorBlendState->logicOp) > VK_LOGIC_OP_SET) return reject("logic op " + std::to_string(ci.pColorBlendState->logicOp));
             logic = true;
@@ -396,6 +396,15 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
         if (logic) b.blendEnable = VK_FALSE;
         extra_blend.push_back(b);
     }
+    // integer attachments are not blended (Vulkan 1.1, "Blending": blending
+    // applies to floating-point and normalised formats only)
+    auto integer_format = [](VkFormat f) {
+        ColourLayout cl;
+        return f != VK_FORMAT_UNDEFINED && colour_layout(f, cl) && cl.kind >= 3;
+    };
+    if (integer_format(cfmt)) blend.blendEnable = VK_FALSE;
+    for (uint32_t k = 1; k < nca; k++)
+        if (integer_format(extra_fmt[k - 1])) extra_blend[k - 1].blendEnable = VK_FALSE;
     auto check_blend = [](const VkPipelineColorBlendAttachmentState& b) -> const char* {
         if (!b.blendEnable) return nullptr;
         auto bad = [](VkBlendFactor f) { return f > VK_BLEND_FACTOR_SRC_ALPHA_SATURATE; };

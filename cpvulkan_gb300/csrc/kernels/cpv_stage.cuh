@@ -408,6 +408,8 @@ __device__ __forceinline__ float cpv_cf_decode(uint32_t raw) {
     return cpv_decode_unorm16(raw);
 #elif CPV_CF_KIND == 1
     return cpv_decode_norm(raw, CPV_CF_BITS / 8, true);
+#elif CPV_CF_KIND >= 3
+    return __uint_as_float(raw); /* integer formats: not blended, never decoded to a value */
 #elif CPV_CF_BITS == 16
     return cpv_half_to_float(raw);
 #else
@@ -425,7 +427,20 @@ __device__ __forceinline__ uint32_t cpv_cf_encode(float x) {
 #elif CPV_CF_KIND == 1
     const float v = roundf(__fmul_rn(fminf(fmaxf(x, -1.0f), 1.0f), CPV_CF_BITS == 8 ? 127.0f : 32767.0f));
     return static_cast<uint32_t>(static_cast<int32_t>(v)) & CPV_CF_MASK;
-
+#elif CPV_CF_KIND == 3
+    /* UINT: the output's 32 bits as an unsigned integer, clamped to the
+     * channel's maximum (LLVMRuntime/ImageCompiler.cpp:1121-1144) */
+    const uint32_t u = __float_as_uint(x);
+    return CPV_CF_BITS >= 32 ? u : (u < CPV_CF_MASK ? u : CPV_CF_MASK);
+#elif CPV_CF_KIND == 4
+    /* SINT: as a signed integer, clamped to the channel's range (:1146-1175) */
+    int32_t v = static_cast<int32_t>(__float_as_uint(x));
+    if (CPV_CF_BITS < 32) {
+        const int32_t hi = static_cast<int32_t>(CPV_CF_MASK >> 1), lo = -hi - 1;
+        v = v > lo ? v : lo;
+        v = v < hi ? v : hi;
+    }
+    return static_cast<uint32_t>(v) & CPV_CF_MASK;
 #elif CPV_CF_BITS == 16
     return cpv_float_to_half(x);
 #else

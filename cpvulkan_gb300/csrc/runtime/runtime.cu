@@ -466,8 +466,10 @@ int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& s
     uint32_t direct = (G * tiles <= direct_limit) ? 1u : 0u;
     if (G > 0xFFFFFFFFull) return kErrInvalid;
     if (!direct) {
-        // Spans: one warp per ~256 primitives, at most 4096 spans.
-        uint64_t spans = (G + 255) / 256;
+        // Spans: one warp per ~CPV_SPAN_PRIMS primitives (default 256), at
+        // most 4096 spans; the (tiles x spans) count matrix grows with them.
+        static const uint32_t span_prims = std::max<uint32_t>(32u, env_u32("CPV_SPAN_PRIMS", 256u));
+        uint64_t spans = (G + span_prims - 1) / span_prims;
         if (spans > 4096) spans = 4096;
         if (spans < 1) spans = 1;
         const uint64_t bins = tiles * spans;

@@ -973,11 +973,19 @@ bool Translator::emit_globals(const EntryPoint& ep, StageResult& out) {
                         // (LLVMRuntime/PipelineCompiler.cpp:1415-1429, 1655-1667);
                         // outputs beyond the module's attachments are dropped
                         if (location >= 8) return fail("fragment output location beyond the 8 colour attachments");
+                        // a vec4, ivec4 or uvec4: an integer output's bits pass
+                        // unchanged (the attachment's encoder reads them as the
+                        // output's memory, :1528-1653)
                         const Type* t = type(tid);
-                        if (!t || t->kind != TypeKind::Vector || t->count != 4 || !is_float_scalar(t->component))
-                            return fail("fragment output " + std::to_string(location) + " must be a vec4");
+                        const Type* ct = t ? type(t->component) : nullptr;
+                        const bool int_out = ct && ct->kind == TypeKind::Int && ct->width == 32;
+                        if (!t || t->kind != TypeKind::Vector || t->count != 4 || !(is_float_scalar(t->component) || int_out))
+                            return fail("fragment output " + std::to_string(location) + " must be a vec4, ivec4 or uvec4");
                         if (location > 0) epi_ << "#if CPV_NUM_CA > " << location << "\n";
-                        for (int i = 0; i < 4; i++) epi_ << "  cpv_colour[" << 4 * location + i << "] = " << var << ".v[" << i << "];\n";
+                        for (int i = 0; i < 4; i++) {
+                            const std::string v = var + ".v[" + std::to_string(i) + "]";
+                            epi_ << "  cpv_colour[" << 4 * location + i << "] = " << (int_out ? "__uint_as_float((uint32_t)" + v + ")" : v) << ";\n";
+                        }
                         if (location > 0) epi_ << "#endif\n";
                         out_outputs_ |= 1u << location;
                     }

@@ -24,7 +24,7 @@ OP = dict(
     VectorTimesScalar=142, MatrixTimesVector=145, Dot=148, FOrdGreaterThan=186, SelectionMerge=247,
     Label=248, Branch=249, BranchConditional=250, Kill=252, Return=253, SpecConstant=50, SpecConstantOp=52,
     CopyMemory=63, ImageFetch=95, Image=100, ConvertFToS=110, ConvertSToF=111, IAdd=128, IMul=132, BitwiseXor=198,
-    BitCount=205,
+    BitCount=205, ConvertFToU=109, Bitcast=124,
 )
 DEC = dict(SpecId=1, Block=2, ColMajor=5, MatrixStride=7, BuiltIn=11, NoPerspective=13, Flat=14, Location=30, Binding=33,
            DescriptorSet=34, Offset=35)
@@ -99,6 +99,8 @@ class Module:
         return self._type(("struct", key), "TypeStruct", lambda: list(members))
 
     def ivec(self, n): return self._type(("ivec", n), "TypeVector", lambda: [self.int(), n])
+    def uint(self): return self._type(("uint",), "TypeInt", lambda: [32, 0])
+    def uvec(self, n): return self._type(("uvec", n), "TypeVector", lambda: [self.uint(), n])
 
     def image_2d(self):
         return self._type(("img2d",), "TypeImage", lambda: [self.float(), 1, 0, 0, 0, 1, 0])
@@ -508,6 +510,35 @@ def mrt_frag():
     return m.assemble(body)
 
 
+def mrti_frag():
+    """layout(location=0) in vec4 c;
+    layout(location=0) out vec4 o0; layout(location=1) out uvec4 o1;
+    layout(location=2) out ivec4 o2; layout(location=3) out uvec4 o3;
+    void main() { o0 = c; o1 = uvec4(c * 300.0); o2 = ivec4(c * 400.0 - vec4(200.0));
+                  o3 = floatBitsToUint(c); }
+    Integer outputs for integer colour attachments (values beyond an
+    8-bit channel's range clamp; o3 carries float bit patterns)."""
+    m = Module(4)
+    v4, u4, i4 = m.vec(4), m.uvec(4), m.ivec(4)
+    col = m.variable("Input", v4, "color")
+    m.decorate(col, "Location", 0)
+    outs = []
+    for k, t in enumerate((v4, u4, i4, u4)):
+        o = m.variable("Output", t, "o%d" % k)
+        m.decorate(o, "Location", k)
+        outs.append(o)
+    c200 = m._const(("cc_200",), "ConstantComposite", lambda: v4, lambda: [m.const_f(200.0)] * 4)
+
+    def body(m):
+        c = m.load(v4, col)
+        m.store(outs[0], c)
+        m.store(outs[1], m.op("ConvertFToU", u4, m.op("VectorTimesScalar", v4, c, m.const_f(300.0))))
+        m.store(outs[2], m.op("ConvertFToS", i4, m.op("FSub", v4, m.op("VectorTimesScalar", v4, c, m.const_f(400.0)), c200)))
+        m.store(outs[3], m.op("Bitcast", u4, c))
+        m.op_void("Return")
+    return m.assemble(body)
+
+
 PROGRAMS = {
     "cube": (cube_vert, lambda: colour_frag()),
     "texlit": (texlit_vert, texlit_frag),
@@ -518,6 +549,7 @@ PROGRAMS = {
     "points": (points_vert, colour_frag),
     "fetch": (texlit_vert, fetch_frag),
     "mrt": (cube_vert, mrt_frag),
+    "mrti": (cube_vert, mrti_frag),
 }
 
 

@@ -37,7 +37,9 @@ enum cpv_program {
                                     specialisation constant (default 3), bitCount, a copy between variables */
     CPV_PROGRAM_MRT = 8,         /* CUBE's vertex shader; FS: eight outputs (locations 0-7), each a different
                                     function of the colour, one per colour attachment                         */
-    CPV_PROGRAM_COUNT = 9
+    CPV_PROGRAM_MRTI = 9,        /* CUBE's vertex shader; FS: vec4 colour, uvec4(c * 300), ivec4(c * 400 - 200)
+                                    and floatBitsToUint(c) at locations 0-3 (integer attachments)            */
+    CPV_PROGRAM_COUNT = 10
 };
 
 #define CPV_SCENE_MAX_BINDINGS 4
@@ -150,7 +152,9 @@ typedef struct cpv_scene {
     const cpv_scene_draw* draws;
 
     /* colour attachments after the first (same size; 0 formats: unused
-     * references), referenced by the subpass in order after it */
+     * references), referenced by the subpass in order after it. An
+     * integer-format attachment is cleared with the integers
+     * round(clear_color * 100). */
     uint32_t extra_color_count;
     uint32_t extra_color_formats[CPV_SCENE_MAX_EXTRA_COLOR];
 } cpv_scene;

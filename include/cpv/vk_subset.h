@@ -162,7 +162,10 @@ typedef enum VkFormat {
     VK_FORMAT_UNDEFINED = 0,
     VK_FORMAT_R8_UNORM = 9,
     VK_FORMAT_R8_UINT = 13,
+    VK_FORMAT_R8_SINT = 14,
     VK_FORMAT_R8G8_UNORM = 16,
+    VK_FORMAT_R8G8_UINT = 20,
+    VK_FORMAT_R8G8_SINT = 21,
     VK_FORMAT_R8G8B8A8_UNORM = 37,
     VK_FORMAT_R8G8B8A8_SNORM = 38,
     VK_FORMAT_R8G8B8A8_UINT = 41,
@@ -171,8 +174,12 @@ typedef enum VkFormat {
     VK_FORMAT_B8G8R8A8_UNORM = 44,
     VK_FORMAT_B8G8R8A8_SRGB = 50,
     VK_FORMAT_R16_UNORM = 70,
+    VK_FORMAT_R16_UINT = 74,
+    VK_FORMAT_R16_SINT = 75,
     VK_FORMAT_R16_SFLOAT = 76,
     VK_FORMAT_R16G16_UNORM = 77,
+    VK_FORMAT_R16G16_UINT = 81,
+    VK_FORMAT_R16G16_SINT = 82,
     VK_FORMAT_R16G16_SFLOAT = 83,
     VK_FORMAT_R32_UINT = 98,
     VK_FORMAT_R32_SINT = 99,

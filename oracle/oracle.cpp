@@ -360,7 +360,8 @@ ProgramInfo program_info(uint32_t program) {
     case CPV_PROGRAM_DISCARD: return {1, {4}, {INTERP_PERSPECTIVE}};
     case CPV_PROGRAM_NOPERSP: return {1, {4}, {INTERP_LINEAR}};
     case CPV_PROGRAM_POINTS: return {1, {4}, {INTERP_PERSPECTIVE}};
-    case CPV_PROGRAM_MRT: return {1, {4}, {INTERP_PERSPECTIVE}};
+    case CPV_PROGRAM_MRT:
+    case CPV_PROGRAM_MRTI: return {1, {4}, {INTERP_PERSPECTIVE}};
     default: return {0, {0}, {INTERP_PERSPECTIVE}};
     }
 }
@@ -390,7 +391,8 @@ void run_vs(uint32_t program, const float attr[8][4], const Resources& r, VsOut&
     case CPV_PROGRAM_DISCARD:
     case CPV_PROGRAM_NOPERSP:
     case CPV_PROGRAM_POINTS:
-    case CPV_PROGRAM_MRT: {
+    case CPV_PROGRAM_MRT:
+    case CPV_PROGRAM_MRTI: {
         float m[16];
         for (int i = 0; i < 16; i++) m[i] = ubo_at(r, i);
         for (int i = 0; i < 4; i++) out.var[i] = attr[1][i];
@@ -447,6 +449,21 @@ bool run_fs(uint32_t program, const float* in, const Resources& r, float* colour
         for (int i = 0; i < 4; i++) colour[20 + i] = c[i] * 2.0f - 1.0f;
         colour[24] = c[0] + c[1]; colour[25] = c[1] - c[2]; colour[26] = c[2]; colour[27] = 0.25f;
         colour[28] = c[3]; colour[29] = c[2]; colour[30] = c[1]; colour[31] = c[0];
+        return false;
+    }
+    case CPV_PROGRAM_MRTI: {
+        /* gen_spirv.py mrti_frag: integer outputs keep their bits in the
+         * 32-bit output slots (OpConvertFToU / OpConvertFToS truncate) */
+        const float* c = in;
+        for (int i = 0; i < 4; i++) {
+            colour[i] = c[i];
+            const uint32_t u = static_cast<uint32_t>(c[i] * 300.0f);
+            const int32_t v = static_cast<int32_t>(c[i] * 400.0f - 200.0f);
+            std::memcpy(&colour[4 + i], &u, 4);
+            std::memcpy(&colour[8 + i], &v, 4);
+            colour[12 + i] = c[i];  /* OpBitcast: the same bits */
+        }
+        for (int i = 16; i < 32; i++) colour[i] = 0.0f;
         return false;
     }
     case CPV_PROGRAM_CUBE:
@@ -562,8 +579,37 @@ bool colour_format(uint32_t fmt, ColourFormat& cf) {
     case 77: cf = {4, 2, 2, 0, {0, 2, 0, 0}}; return true;   /* R16G16_UNORM */
     case 83: cf = {4, 2, 2, 2, {0, 2, 0, 0}}; return true;   /* R16G16_SFLOAT */
     case 100: cf = {4, 1, 4, 2, {0, 0, 0, 0}}; return true;  /* R32_SFLOAT */
+    /* integer formats: kind 3 UINT, 4 SINT */
+    case 13: cf = {1, 1, 1, 3, {0, 0, 0, 0}}; return true;   /* R8_UINT */
+    case 14: cf = {1, 1, 1, 4, {0, 0, 0, 0}}; return true;   /* R8_SINT */
+    case 20: cf = {2, 2, 1, 3, {0, 1, 0, 0}}; return true;   /* R8G8_UINT */
+    case 21: cf = {2, 2, 1, 4, {0, 1, 0, 0}}; return true;   /* R8G8_SINT */
+    case 41: cf = {4, 4, 1, 3, {0, 1, 2, 3}}; return true;   /* R8G8B8A8_UINT */
+    case 42: cf = {4, 4, 1, 4, {0, 1, 2, 3}}; return true;   /* R8G8B8A8_SINT */
+    case 74: cf = {2, 1, 2, 3, {0, 0, 0, 0}}; return true;   /* R16_UINT */
+    case 75: cf = {2, 1, 2, 4, {0, 0, 0, 0}}; return true;   /* R16_SINT */
+    case 81: cf = {4, 2, 2, 3, {0, 2, 0, 0}}; return true;   /* R16G16_UINT */
+    case 82: cf = {4, 2, 2, 4, {0, 2, 0, 0}}; return true;   /* R16G16_SINT */
+    case 98: cf = {4, 1, 4, 3, {0, 0, 0, 0}}; return true;   /* R32_UINT */
+    case 99: cf = {4, 1, 4, 4, {0, 0, 0, 0}}; return true;   /* R32_SINT */
     default: return false;
     }
+}
+
+/* An integer channel from a 32-bit integer value: UINT clamped to the
+ * channel's maximum, SINT to its range (LLVMRuntime/ImageCompiler.cpp:1121-1175). */
+uint32_t encode_integer(uint32_t bits, const ColourFormat& cf) {
+    const uint32_t width = 8 * cf.esize;
+    if (width >= 32) return bits;
+    if (cf.kind == 3) {
+        const uint32_t m = (1u << width) - 1u;
+        return bits < m ? bits : m;
+    }
+    const int32_t hi = (1 << (width - 1)) - 1, lo = -hi - 1;
+    int32_t v = static_cast<int32_t>(bits);
+    v = v > lo ? v : lo;
+    v = v < hi ? v : hi;
+    return static_cast<uint32_t>(v);
 }
 
 /* One stored channel → float: the reference's pixel decoder
@@ -597,7 +643,12 @@ float decode_channel(const uint8_t* p, const ColourFormat& cf) {
  * round-to-nearest-even narrowing; 32-bit floats unchanged. */
 void encode_channel(float x, const ColourFormat& cf, uint8_t* p) {
     uint32_t raw;
-    if (cf.kind == 0) {
+    if (cf.kind >= 3) {
+        /* an integer attachment reads the output's 32 bits as an integer */
+        uint32_t bits;
+        std::memcpy(&bits, &x, 4);
+        raw = encode_integer(bits, cf);
+    } else if (cf.kind == 0) {
         raw = encode_unorm(x, cf.esize == 1 ? 255.0f : 65535.0f);
     } else if (cf.kind == 1) {
         const float v = std::round(minnum(maxnum(x, -1.0f), 1.0f) * (cf.esize == 1 ? 127.0f : 32767.0f));
@@ -617,6 +668,23 @@ void set_colour(uint8_t* texel, uint32_t fmt, const float c[4]) {
     ColourFormat cf;
     if (!colour_format(fmt, cf)) return;
     for (uint32_t i = 0; i < cf.channels; i++) encode_channel(c[i], cf, texel + cf.off[i]);
+}
+
+/* The render pass's clear of one texel: an integer attachment is cleared
+ * with the integer values round(clear * 100) (the scene contract; the
+ * harness passes them as VkClearColorValue.int32), other formats with the
+ * clear colour through their encoder. */
+void clear_colour(uint8_t* texel, uint32_t fmt, const float c[4]) {
+    ColourFormat cf;
+    if (!colour_format(fmt, cf)) return;
+    if (cf.kind < 3) {
+        set_colour(texel, fmt, c);
+        return;
+    }
+    for (uint32_t i = 0; i < cf.channels; i++) {
+        const uint32_t raw = encode_integer(static_cast<uint32_t>(static_cast<int32_t>(std::lround(c[i] * 100.0f))), cf);
+        std::memcpy(texel + cf.off[i], &raw, cf.esize);
+    }
 }
 
 /* The texel as the reference decodes it; absent channels read 0, 0, 0, 1. */
@@ -907,7 +975,7 @@ void write_colour(uint8_t* texel, uint32_t fmt, const cpv_scene_pipeline& p, con
         }
     } else {
         float out[4];
-        if (b.blend_enable) {
+        if (b.blend_enable && cf.kind < 3) {  /* integer attachments are not blended (Vulkan 1.1, "Blending") */
             float dst[4];
             get_colour(texel, fmt, dst);
             blend(colour, dst, p.blend_constants, b.src_color, b.dst_color, b.color_op, b.src_alpha, b.dst_alpha, b.alpha_op, out);
@@ -1537,10 +1605,10 @@ void clear(const Frame& f) {
     const cpv_scene* scene = f.s;
     const uint64_t pixels = static_cast<uint64_t>(scene->width) * scene->height;
     if (scene->color_format) {  // a depth-only pass leaves `color` untouched
-        for (uint64_t i = 0; i < pixels; i++) set_colour(f.colour + i * f.colour_size, scene->color_format, scene->clear_color);
+        for (uint64_t i = 0; i < pixels; i++) clear_colour(f.colour + i * f.colour_size, scene->color_format, scene->clear_color);
         for (uint32_t k = 0; k < scene->extra_color_count; k++)
             if (f.extra[k])
-                for (uint64_t i = 0; i < pixels; i++) set_colour(f.extra[k] + i * f.extra_size[k], scene->extra_color_formats[k], scene->clear_color);
+                for (uint64_t i = 0; i < pixels; i++) clear_colour(f.extra[k] + i * f.extra_size[k], scene->extra_color_formats[k], scene->clear_color);
     }
     if (f.depth) {
         for (uint64_t i = 0; i < pixels; i++) {

@@ -302,3 +302,37 @@ def test_colour_attachments(gpu_ctx, oracle, monkeypatch, case, batched):
     assert report["color_pixels_differing"] == 0, report
     for k, (g, o) in enumerate(zip(gx, rx)):
         assert np.count_nonzero(np.any(g != o, axis=-1)) == 0, "attachment %d (format %d)" % (k + 1, fmts[k])
+
+
+# Integer colour attachments (UINT / SINT): the integer-output program's
+# vec4, uvec4(c * 300), ivec4(c * 400 - 200) and floatBitsToUint(c) into
+# integer formats of every width, clamped to each channel's range; blend
+# states on integer attachments are ignored (Vulkan: integer formats are not
+# blended); the render pass clears them with the integers round(clear * 100).
+INT_CASES = [
+    (37, [41, 42, 98], [0x00, 0x00, 0x00]),
+    (99, [81, 75, 13], [0x01, 0x02, 0x30]),
+    (42, [20, 82, 99], [0x00, 0x10, 0x00]),
+]
+
+
+@pytest.mark.parametrize("case", range(len(INT_CASES)))
+@pytest.mark.parametrize("batched", [False, True])
+def test_integer_colour_attachments(gpu_ctx, oracle, monkeypatch, case, batched):
+    if batched:
+        monkeypatch.setenv("CPV_BATCH_MIN_DRAWS", "1")
+    fmt0, fmts, blends = INT_CASES[case]
+    scene = c.Scene(c.PROGRAM, 7 + case, [c.PROGRAM_MRTI, 0x10, 64, 48, 24, 0, fmt0, _pack(fmts), _pack(blends)])
+    r = c.Renderer(gpu_ctx, scene)
+    try:
+        r.render(1)
+        gc, gd = r.readback()
+        gx = [r.readback_extra(k + 1) for k in range(len(fmts))]
+    finally:
+        r.close()
+    rc, rx, rd, stats = oracle.render_extra(scene)
+    assert stats["fragments_written"] > 0
+    assert np.count_nonzero(np.any(gc != rc, axis=-1)) == 0, "attachment 0 (format %d)" % fmt0
+    assert np.count_nonzero(np.any(gd != rd, axis=-1)) == 0
+    for k, (g, o) in enumerate(zip(gx, rx)):
+        assert np.count_nonzero(np.any(g != o, axis=-1)) == 0, "attachment %d (format %d)" % (k + 1, fmts[k])

@@ -49,3 +49,36 @@ def test_write_mask_and_unused_reference(oracle):
     m = extras[0]
     assert np.all(m[..., [0, 2, 3]] == np.array([64, 191, 255], np.uint8))  # clear (0.25, 0.5, 0.75, 1) encoded, kept
     assert (m[..., 1] != 128).any()  # green written somewhere
+
+
+def test_integer_attachments_hold_the_outputs_bits(oracle):
+    # R32_SFLOAT at location 0 (c.r), R32_UINT at location 1 (uint(c.r * 300))
+    # and location 3 (floatBitsToUint(c).r): exact relations between them
+    scene = c.Scene(c.PROGRAM, 3, [c.PROGRAM_MRTI, 0x10, 64, 48, 24, 0, 100, _pack([98, 99, 98]), 0])
+    col, extras, _, _ = oracle.render_extra(scene)
+    f0 = col.view(np.float32)[..., 0]
+    u1 = extras[0].view(np.uint32)[..., 0]
+    i2 = extras[1].view(np.int32)[..., 0]
+    u3 = extras[2].view(np.uint32)[..., 0]
+    drawn = f0 != np.float32(-0.3)
+    assert drawn.any()
+    assert np.array_equal(u3[drawn], col.view(np.uint32)[..., 0][drawn])
+    assert np.array_equal(u1[drawn], (f0[drawn] * np.float32(300.0)).astype(np.uint32))
+    assert np.array_equal(i2[drawn], (f0[drawn] * np.float32(400.0) - np.float32(200.0)).astype(np.int32))
+    # cleared pixels hold the integer clear: round(-0.3 * 100) = -30
+    assert np.all(i2[~drawn] == -30) and np.all(u1[~drawn] == np.uint32(2**32 - 30))
+
+
+def test_integer_channels_clamp(oracle):
+    # 8-bit UINT and SINT channels clamp uint(c * 300) to 255 and
+    # int(c * 400 - 200) to [-128, 127]
+    scene = c.Scene(c.PROGRAM, 4, [c.PROGRAM_MRTI, 0x10, 64, 48, 24, 0, 100, _pack([41, 42]), 0])
+    col, extras, _, _ = oracle.render_extra(scene)
+    f0 = col.view(np.float32)[..., 0]
+    drawn = f0 != np.float32(-0.3)
+    r1 = extras[0][..., 0][drawn].astype(np.int64)
+    r2 = extras[1][..., 0][drawn].view(np.int8).astype(np.int64)
+    want1 = np.minimum((f0[drawn] * np.float32(300.0)).astype(np.int64), 255)
+    want2 = np.clip((f0[drawn] * np.float32(400.0) - np.float32(200.0)).astype(np.int64), -128, 127)
+    assert np.array_equal(r1, want1) and np.array_equal(r2, want2)
+    assert (want1 == 255).any() and (want2 == 127).any() and (want2 == -128).any()

@@ -264,6 +264,10 @@ def test_colour_attachments_compile_and_reject(native, monkeypatch, tmp_path):
     try:
         c.Renderer(ctx, c.Scene(c.PROGRAM, 1, [c.PROGRAM_MRT, 0x10, 32, 32, 4, 0, 0, fmts, 0x0201])).close()
         assert "batched module compiled" in c.icd_last_error()
+        # integer outputs into integer formats of every width
+        ints = 41 | (42 << 8) | (98 << 16)
+        c.Renderer(ctx, c.Scene(c.PROGRAM, 1, [c.PROGRAM_MRTI, 0x10, 32, 32, 4, 0, 99, ints, 0x01])).close()
+        assert "batched module compiled" in c.icd_last_error()
         with pytest.raises(RuntimeError):
             c.Renderer(ctx, c.Scene(c.PROGRAM, 1, [c.PROGRAM_CUBE, 0x10, 32, 32, 4, 0, 0, 37, 0]))
         assert "no output for colour attachment 1" in c.icd_last_error()
