@@ -67,7 +67,8 @@ def colour_texel_bytes(fmt):
     """Bytes per texel of a colour attachment format (R8_UNORM 1; R8G8_UNORM
     and R16_UNORM 2; the 4-byte formats otherwise); a depth-only pass reads
     back zeros in the 4-byte layout."""
-    return {0: 4, 9: 1, 13: 1, 14: 1, 16: 2, 20: 2, 21: 2, 70: 2, 74: 2, 75: 2}.get(fmt, 4)
+    return {0: 4, 9: 1, 13: 1, 14: 1, 16: 2, 20: 2, 21: 2, 70: 2, 74: 2, 75: 2, 91: 8, 95: 8, 96: 8, 97: 8, 101: 8, 102: 8, 103: 8,
+            107: 16, 108: 16, 109: 16}.get(fmt, 4)
 
 
 _harness = None

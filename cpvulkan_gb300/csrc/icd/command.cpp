@@ -169,8 +169,10 @@ uint8_t* view_base(const ImageView* v, uint32_t& width, uint32_t& height) {
 // stencil byte in the second word of a D32S8 texel (ClearImage → SetPixel,
 // CPVulkan/CommandBuffer.Draw.cpp:117-149, 2398-2419). False for a format
 // without a clear encoding here.
-bool clear_texel(VkFormat fmt, const VkClearValue& cv, uint32_t& lo, uint32_t& hi) {
-    lo = hi = 0;
+bool clear_texel(VkFormat fmt, const VkClearValue& cv, uint32_t words[4]) {
+    for (int i = 0; i < 4; i++) words[i] = 0;
+    uint32_t& lo = words[0];
+    uint32_t& hi = words[1];
     ColourLayout cl;
     if (colour_layout(fmt, cl)) {
         // each channel through the format's encoder (UNORM, SNORM, half,
@@ -188,7 +190,9 @@ bool clear_texel(VkFormat fmt, const VkClearValue& cv, uint32_t& lo, uint32_t& h
             } else {
                 field = encode_channel_host(cv.color.float32[ch], cl);
             }
-            lo |= field << (cl.bgra ? shift_bgra[ch] : static_cast<int>(cl.bits * ch));
+            // channel ch in 32-bit word ch * bits / 32 (8- and 16-byte texels)
+            if (cl.bgra) lo |= field << shift_bgra[ch];
+            else words[(cl.bits * ch) >> 5] |= field << ((cl.bits * ch) & 31u);
         }
         return true;
     }
@@ -217,15 +221,17 @@ VkResult clear_rect(Queue* q, Image* img, uint32_t layer, uint32_t level, VkImag
     x0 = std::max(x0, 0);
     y0 = std::max(y0, 0);
     if (x1 <= x0 || y1 <= y0) return VK_SUCCESS;
-    uint32_t lo, hi;
-    if (!clear_texel(img->format, cv, lo, hi)) return VK_ERROR_DEVICE_LOST;
+    uint32_t words[4];
+    if (!clear_texel(img->format, cv, words)) return VK_ERROR_DEVICE_LOST;
     const bool depth = format_is_depth(img->format);
     const bool write_lo = !depth || (aspects & VK_IMAGE_ASPECT_DEPTH_BIT) != 0;
-    const bool write_hi = depth && (aspects & VK_IMAGE_ASPECT_STENCIL_BIT) != 0;
+    // the second word: a D32S8 texel's stencil, or an 8-byte colour texel's
+    const bool write_hi = depth ? (aspects & VK_IMAGE_ASPECT_STENCIL_BIT) != 0 : true;
     if (!write_lo && (img->texel != 8 || !write_hi)) return VK_SUCCESS;
     uint8_t* base = img->device_ptr() + static_cast<uint64_t>(layer) * img->layer_size + L.offset + static_cast<uint64_t>(y0) * L.stride +
                     static_cast<uint64_t>(x0) * img->texel;
-    return rt::fill_rect(q->stream, base, L.stride, static_cast<uint32_t>(x1 - x0), static_cast<uint32_t>(y1 - y0), img->texel, lo, hi, write_lo, write_hi) == rt::kOk
+    return rt::fill_rect(q->stream, base, L.stride, static_cast<uint32_t>(x1 - x0), static_cast<uint32_t>(y1 - y0), img->texel, words[0], words[1], write_lo,
+                         write_hi, words[2], words[3]) == rt::kOk
                ? VK_SUCCESS
                : VK_ERROR_DEVICE_LOST;
 }

@@ -35,7 +35,8 @@ uint32_t format_texel_size(VkFormat f) {
     case VK_FORMAT_D24_UNORM_S8_UINT: case VK_FORMAT_R16G16_UNORM: case VK_FORMAT_R16G16_SFLOAT: case VK_FORMAT_R16G16_UINT:
     case VK_FORMAT_R16G16_SINT:
         return 4;
-    case VK_FORMAT_R32G32_UINT: case VK_FORMAT_R32G32_SINT: case VK_FORMAT_R32G32_SFLOAT: case VK_FORMAT_D32_SFLOAT_S8_UINT: return 8;
+    case VK_FORMAT_R32G32_UINT: case VK_FORMAT_R32G32_SINT: case VK_FORMAT_R32G32_SFLOAT: case VK_FORMAT_D32_SFLOAT_S8_UINT:
+    case VK_FORMAT_R16G16B16A16_UNORM: case VK_FORMAT_R16G16B16A16_UINT: case VK_FORMAT_R16G16B16A16_SINT: case VK_FORMAT_R16G16B16A16_SFLOAT: return 8;
     case VK_FORMAT_R32G32B32_UINT: case VK_FORMAT_R32G32B32_SINT: case VK_FORMAT_R32G32B32_SFLOAT: return 12;
     case VK_FORMAT_R32G32B32A32_UINT: case VK_FORMAT_R32G32B32A32_SINT: case VK_FORMAT_R32G32B32A32_SFLOAT: return 16;
     default: return 0;
@@ -67,6 +68,17 @@ bool colour_layout(VkFormat f, ColourLayout& out) {
     case VK_FORMAT_R16G16_SINT: out = {4, 2, 16, 4, false}; return true;
     case VK_FORMAT_R32_UINT: out = {4, 1, 32, 3, false}; return true;
     case VK_FORMAT_R32_SINT: out = {4, 1, 32, 4, false}; return true;
+    // 8- and 16-byte texels: channel i in 32-bit word i * bits / 32
+    case VK_FORMAT_R16G16B16A16_UNORM: out = {8, 4, 16, 0, false}; return true;
+    case VK_FORMAT_R16G16B16A16_SFLOAT: out = {8, 4, 16, 2, false}; return true;
+    case VK_FORMAT_R16G16B16A16_UINT: out = {8, 4, 16, 3, false}; return true;
+    case VK_FORMAT_R16G16B16A16_SINT: out = {8, 4, 16, 4, false}; return true;
+    case VK_FORMAT_R32G32_SFLOAT: out = {8, 2, 32, 2, false}; return true;
+    case VK_FORMAT_R32G32_UINT: out = {8, 2, 32, 3, false}; return true;
+    case VK_FORMAT_R32G32_SINT: out = {8, 2, 32, 4, false}; return true;
+    case VK_FORMAT_R32G32B32A32_SFLOAT: out = {16, 4, 32, 2, false}; return true;
+    case VK_FORMAT_R32G32B32A32_UINT: out = {16, 4, 32, 3, false}; return true;
+    case VK_FORMAT_R32G32B32A32_SINT: out = {16, 4, 32, 4, false}; return true;
     default: return false;
     }
 }

@@ -116,6 +116,12 @@ std::string compose_module(const std::vector<std::string>& stages, const std::ve
         const size_t at = st.find("#define CPV_EXTRA_CA ");
         if (at != std::string::npos) num_ca = std::max<uint32_t>(num_ca, 1u + static_cast<uint32_t>(std::atoi(st.c_str() + at + 21)));
     }
+    // the widest first-attachment texel in 32-bit words
+    uint32_t colour_words = 1;
+    for (const std::string& st : stages) {
+        const size_t at = st.find("#define CPV_CF_BYTES ");
+        if (at != std::string::npos) colour_words = std::max<uint32_t>(colour_words, (static_cast<uint32_t>(std::atoi(st.c_str() + at + 21)) + 3u) / 4u);
+    }
     // the deferred schedule records one colour per fragment
     const uint32_t schedule = num_ca > 1 && mc.schedule == 1 ? 2u : mc.schedule;
     std::ostringstream src;
@@ -124,6 +130,7 @@ std::string compose_module(const std::vector<std::string>& stages, const std::ve
     src << "#define CPV_TILE_SHIFT " << mc.tile_shift << "\n";
     src << "#define CPV_SCHEDULE " << schedule << "\n";
     src << "#define CPV_NUM_CA " << num_ca << "\n";
+    src << "#define CPV_COLOUR_WORDS " << colour_words << "\n";
     src << "#define CPV_RT_WARPS " << mc.warps << "\n";
     src << "#define CPV_BATCH " << mc.batch << "\n";
     // Sparse schedule: fragments a pixel lists per batch before its
@@ -349,6 +356,9 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     for (uint32_t k = 1; k < nca; k++) {
         const VkFormat f = sub.colour[k] == VK_ATTACHMENT_UNUSED ? VK_FORMAT_UNDEFINED : pass->attachments[sub.colour[k]].format;
         if (f != VK_FORMAT_UNDEFINED && !supported_colour(f)) return reject("colour attachment format " + std::to_string(f));
+        ColourLayout ecl;
+        if (f != VK_FORMAT_UNDEFINED && colour_layout(f, ecl) && ecl.bytes > 4)
+            return reject("an 8- or 16-byte colour format after the first attachment");
         extra_fmt.push_back(f);
     }
     if (sub.colour.empty() && sub.depth == VK_ATTACHMENT_UNUSED) return reject("a colour or a depth attachment is required");
@@ -572,12 +582,12 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
             after << "#include \"cpv_stage.cuh\"\n}  // namespace cpv_ca" << k << "\n";
         }
         after << "__device__ __forceinline__ void cpv_load_extra(const uint8_t* const* c, uint64_t pix, CpvPixel& s) {\n";
-        for (uint32_t k = 1; k < nca; k++) after << "  s.extra[" << k - 1 << "] = cpv_ca" << k << "::cpv_load_colour(c[" << k - 1 << "], pix);\n";
+        for (uint32_t k = 1; k < nca; k++) after << "  cpv_ca" << k << "::cpv_load_colour(c[" << k - 1 << "], pix, &s.extra[" << k - 1 << "]);\n";
         after << "}\n__device__ __forceinline__ void cpv_store_extra(uint8_t* const* c, uint64_t pix, const CpvPixel& s) {\n";
-        for (uint32_t k = 1; k < nca; k++) after << "  cpv_ca" << k << "::cpv_store_colour(c[" << k - 1 << "], pix, s.extra[" << k - 1 << "]);\n";
+        for (uint32_t k = 1; k < nca; k++) after << "  cpv_ca" << k << "::cpv_store_colour(c[" << k - 1 << "], pix, &s.extra[" << k - 1 << "]);\n";
         after << "}\n__device__ __forceinline__ void cpv_write_extra(const float bc[4], const float* colour, CpvPixel& s) {\n";
         for (uint32_t k = 1; k < nca; k++)
-            after << "  cpv_ca" << k << "::cpv_write_colour(bc, colour + " << 4 * k << ", s.extra[" << k - 1 << "]);\n";
+            after << "  cpv_ca" << k << "::cpv_write_colour(bc, colour + " << 4 * k << ", &s.extra[" << k - 1 << "]);\n";
         after << "}\n";
     }
 

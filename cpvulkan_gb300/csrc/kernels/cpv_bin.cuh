@@ -441,12 +441,20 @@ extern "C" __global__ void __launch_bounds__(256) cpv_fill_u64(uint2* __restrict
         dst[i] = make_uint2(lo, hi);
 }
 
-/* Fill of a w x h texel rectangle whose rows start `pitch` bytes apart: a
- * 2-byte texel takes the low half of lo; 4- and 8-byte texels take lo in
- * their first word when write_lo, and an 8-byte (D32 + stencil) texel takes
- * hi in its second word when write_hi. */
+extern "C" __global__ void __launch_bounds__(256) cpv_fill_u128(uint4* __restrict__ dst, uint64_t count, uint4 value) {
+    for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        dst[i] = value;
+}
+
+/* Fill of a w x h texel rectangle whose rows start `pitch` bytes apart with
+ * the texel v (words x, y, z, w): a 2-byte texel takes the low half of v.x;
+ * 4- and 8-byte texels take v.x in their first word when write_lo, an
+ * 8-byte texel v.y in its second word when write_hi (a D32 + stencil
+ * texel's stencil, or an 8-byte colour texel's upper half), a 16-byte
+ * texel all four words. */
 extern "C" __global__ void __launch_bounds__(256) cpv_fill_rect(uint8_t* __restrict__ base, uint64_t pitch, uint32_t w, uint32_t h, uint32_t texel_bytes,
-                                                                uint32_t lo, uint32_t hi, uint32_t write_lo, uint32_t write_hi) {
+                                                                uint4 v, uint32_t write_lo, uint32_t write_hi) {
+    const uint32_t lo = v.x, hi = v.y;
     /* rows over blockIdx.y, texels of a row over x */
     for (uint32_t y = blockIdx.y; y < h; y += gridDim.y) {
         uint8_t* row = base + static_cast<uint64_t>(y) * pitch;
@@ -456,6 +464,8 @@ extern "C" __global__ void __launch_bounds__(256) cpv_fill_rect(uint8_t* __restr
                 *p = static_cast<uint8_t>(lo);
             } else if (texel_bytes == 2) {
                 *reinterpret_cast<uint16_t*>(p) = static_cast<uint16_t>(lo);
+            } else if (texel_bytes == 16) {
+                *reinterpret_cast<uint4*>(p) = v;
             } else {
                 if (write_lo) *reinterpret_cast<uint32_t*>(p) = lo;
                 if (texel_bytes == 8 && write_hi) *reinterpret_cast<uint32_t*>(p + 4) = hi;

@@ -342,8 +342,11 @@ __device__ __forceinline__ float cpv_blend_op(float s, float sf, float d, float 
 }
 
 /* Register-resident attachment state of one pixel. */
+#ifndef CPV_COLOUR_WORDS
+#define CPV_COLOUR_WORDS 1 /* 32-bit words of the module's widest first-attachment texel (8- and 16-byte formats: 2, 4) */
+#endif
 struct CpvPixel {
-    uint32_t colour;
+    uint32_t colour[CPV_COLOUR_WORDS];
     float depth;        /* decoded depth (D16: u16 / 65535) */
     uint32_t depth_raw; /* stored bits */
     uint32_t stencil;

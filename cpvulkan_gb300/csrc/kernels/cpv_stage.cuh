@@ -387,15 +387,27 @@ __device__ __forceinline__ void cpv_vertex_slot(const CpvDrawParams& P, uint32_t
 #endif
 #define CPV_CF_MASK (CPV_CF_BITS >= 32 ? 0xFFFFFFFFu : ((1u << (CPV_CF_BITS & 31)) - 1u))
 
-/* Bit offset of channel i in the colour attachment texel
- * (CPVulkanBase/Formats.cpp:248,255). */
+/* Where channel i of the colour attachment texel sits
+ * (CPVulkanBase/Formats.cpp:248,255): 32-bit word i * bits / 32 of the
+ * texel, at bit (i * bits) % 32; red in byte 2 for B8G8R8A8. */
+#define CPV_CF_WORDS ((CPV_CF_BYTES + 3) / 4)
 __device__ __forceinline__ int cpv_channel_shift(int i) {
 #if CPV_CF_BGRA
     return i == 0 ? 16 : (i == 1 ? 8 : (i == 2 ? 0 : 24));
 #else
-    return CPV_CF_BITS * i;
+    return (CPV_CF_BITS * i) & 31;
 #endif
 }
+__device__ __forceinline__ int cpv_channel_word(int i) {
+#if CPV_CF_BGRA
+    (void)i;
+    return 0;
+#else
+    return (CPV_CF_BITS * i) >> 5;
+#endif
+}
+/* Stored bits of channel i of a texel (CPV_CF_WORDS words). */
+__device__ __forceinline__ uint32_t cpv_channel_get(const uint32_t* t, int i) { return (t[cpv_channel_word(i)] >> cpv_channel_shift(i)) & CPV_CF_MASK; }
 
 /* Stored channel bits → float, the reference's pixel decoder
  * (LLVMRuntime/ImageCompiler.cpp:161-230): UNORM and SNORM over their
@@ -448,29 +460,44 @@ __device__ __forceinline__ uint32_t cpv_cf_encode(float x) {
 #endif
 }
 
-/* The colour texel of pixel `pix` of this attachment (0 without one). */
-__device__ __forceinline__ uint32_t cpv_load_colour(const uint8_t* color, uint64_t pix) {
+/* The colour texel of pixel `pix` of this attachment into t[0 ..
+ * CPV_CF_WORDS) (0 without one). */
+__device__ __forceinline__ void cpv_load_colour(const uint8_t* color, uint64_t pix, uint32_t* t) {
 #if CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 1
-    return color[pix];
+    t[0] = color[pix];
 #elif CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 2
-    return reinterpret_cast<const uint16_t*>(color)[pix];
+    t[0] = reinterpret_cast<const uint16_t*>(color)[pix];
+#elif CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 8
+    const uint2 v = reinterpret_cast<const uint2*>(color)[pix];
+    t[0] = v.x;
+    t[1] = v.y;
+#elif CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 16
+    const uint4 v = reinterpret_cast<const uint4*>(color)[pix];
+    t[0] = v.x;
+    t[1] = v.y;
+    t[2] = v.z;
+    t[3] = v.w;
 #elif CPV_COLOR_FORMAT != 0
-    return reinterpret_cast<const uint32_t*>(color)[pix];
+    t[0] = reinterpret_cast<const uint32_t*>(color)[pix];
 #else
     (void)color; (void)pix; /* a depth-only pass, or an unused attachment */
-    return 0u;
+    t[0] = 0u;
 #endif
 }
 
-__device__ __forceinline__ void cpv_store_colour(uint8_t* color, uint64_t pix, uint32_t texel) {
+__device__ __forceinline__ void cpv_store_colour(uint8_t* color, uint64_t pix, const uint32_t* t) {
 #if CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 1
-    color[pix] = static_cast<uint8_t>(texel);
+    color[pix] = static_cast<uint8_t>(t[0]);
 #elif CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 2
-    reinterpret_cast<uint16_t*>(color)[pix] = static_cast<uint16_t>(texel);
+    reinterpret_cast<uint16_t*>(color)[pix] = static_cast<uint16_t>(t[0]);
+#elif CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 8
+    reinterpret_cast<uint2*>(color)[pix] = make_uint2(t[0], t[1]);
+#elif CPV_COLOR_FORMAT != 0 && CPV_CF_BYTES == 16
+    reinterpret_cast<uint4*>(color)[pix] = make_uint4(t[0], t[1], t[2], t[3]);
 #elif CPV_COLOR_FORMAT != 0
-    reinterpret_cast<uint32_t*>(color)[pix] = texel;
+    reinterpret_cast<uint32_t*>(color)[pix] = t[0];
 #else
-    (void)color; (void)pix; (void)texel;
+    (void)color; (void)pix; (void)t;
 #endif
 }
 
@@ -488,7 +515,7 @@ __device__ __forceinline__ void cpv_write_extra(const float blend_constants[4], 
 
 __device__ __forceinline__ void cpv_load_pixel(const uint8_t* color, const uint8_t* depth, uint64_t pix, CpvPixel& s,
                                                const uint8_t* const* extra = nullptr) {
-    s.colour = cpv_load_colour(color, pix);
+    cpv_load_colour(color, pix, s.colour);
 #if CPV_EXTRA_CA > 0
     cpv_load_extra(extra, pix, s);
 #else
@@ -703,7 +730,7 @@ __device__ __forceinline__ uint32_t cpv_logic(uint32_t s, uint32_t d) {
  * test (LLVMRuntime/PipelineCompiler.cpp:1528-1727): logic op, else blend
  * (CPVulkan/CommandBuffer.Draw.cpp:956-1262), else the colour; then the
  * write mask and the format's encoder. `colour` is this attachment's output. */
-__device__ __forceinline__ void cpv_write_colour(const float blend_constants[4], const float colour[4], uint32_t& texel) {
+__device__ __forceinline__ void cpv_write_colour(const float blend_constants[4], const float colour[4], uint32_t* texel) {
 #if CPV_COLOR_FORMAT == 0
     (void)blend_constants; (void)colour; (void)texel;
 #else
@@ -713,11 +740,11 @@ __device__ __forceinline__ void cpv_write_colour(const float blend_constants[4],
     uint32_t logic = 0u;
 #pragma unroll
     for (int i = 0; i < CPV_CF_CHANNELS; i++) {
-        const uint32_t d = (texel >> cpv_channel_shift(i)) & 0xFFu;
+        const uint32_t d = (texel[0] >> cpv_channel_shift(i)) & 0xFFu;
         const uint32_t byte = ((CPV_WRITE_MASK >> i) & 1u) ? (cpv_logic(cpv_cf_encode(colour[i]), d) & 0xFFu) : d;
         logic |= byte << cpv_channel_shift(i);
     }
-    texel = logic;
+    texel[0] = logic;
 #else
     float out[4];
 #if CPV_BLEND
@@ -725,8 +752,7 @@ __device__ __forceinline__ void cpv_write_colour(const float blend_constants[4],
      * channels read (0, 0, 0, 1) */
     float dst[4];
 #pragma unroll
-    for (int i = 0; i < 4; i++)
-        dst[i] = i < CPV_CF_CHANNELS ? cpv_cf_decode((texel >> cpv_channel_shift(i)) & CPV_CF_MASK) : (i == 3 ? 1.0f : 0.0f);
+    for (int i = 0; i < 4; i++) dst[i] = i < CPV_CF_CHANNELS ? cpv_cf_decode(cpv_channel_get(texel, i)) : (i == 3 ? 1.0f : 0.0f);
     cpv_blend(colour, dst, blend_constants, out);
 #else
     (void)blend_constants;
@@ -734,13 +760,16 @@ __device__ __forceinline__ void cpv_write_colour(const float blend_constants[4],
     for (int i = 0; i < 4; i++) out[i] = colour[i];
 #endif
     /* the format's channels, each encoded or, outside the write mask, kept */
-    uint32_t packed = 0u;
+    uint32_t packed[CPV_CF_WORDS];
+#pragma unroll
+    for (int w = 0; w < CPV_CF_WORDS; w++) packed[w] = 0u;
 #pragma unroll
     for (int i = 0; i < CPV_CF_CHANNELS; i++) {
-        const uint32_t field = ((CPV_WRITE_MASK >> i) & 1u) ? cpv_cf_encode(out[i]) : ((texel >> cpv_channel_shift(i)) & CPV_CF_MASK);
-        packed |= field << cpv_channel_shift(i);
+        const uint32_t field = ((CPV_WRITE_MASK >> i) & 1u) ? cpv_cf_encode(out[i]) : cpv_channel_get(texel, i);
+        packed[cpv_channel_word(i)] |= field << cpv_channel_shift(i);
     }
-    texel = packed;
+#pragma unroll
+    for (int w = 0; w < CPV_CF_WORDS; w++) texel[w] = packed[w];
 #endif
 #endif
 }
@@ -788,10 +817,10 @@ __device__ __forceinline__ void cpv_rop(const float blend_constants[4], bool fro
             uint32_t packed = 0u;
 #pragma unroll
             for (int i = 0; i < 4; i++) {
-                const uint32_t d = (s.colour >> cpv_channel_shift(i)) & 0xFFu;
+                const uint32_t d = (s.colour[0] >> cpv_channel_shift(i)) & 0xFFu;
                 packed |= static_cast<uint32_t>(table[i * 256 + d]) << cpv_channel_shift(i);
             }
-            s.colour = packed;
+            s.colour[0] = packed;
             return;
         }
 #else
@@ -836,10 +865,10 @@ __device__ __forceinline__ void cpv_apply_table(const uint8_t* table, CpvPixel& 
     uint32_t packed = 0u;
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-        const uint32_t d = (s.colour >> cpv_channel_shift(i)) & 0xFFu;
+        const uint32_t d = (s.colour[0] >> cpv_channel_shift(i)) & 0xFFu;
         packed |= static_cast<uint32_t>(table[i * 256 + d]) << cpv_channel_shift(i);
     }
-    s.colour = packed;
+    s.colour[0] = packed;
 }
 
 /* The stage functions of this pipeline, as one type the module's

@@ -368,7 +368,7 @@ int scan_u32(cudaStream_t stream, const uint32_t* in, uint32_t* out, uint64_t n,
     return kOk;
 }
 
-int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, uint32_t lo, uint32_t hi) {
+int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, uint32_t lo, uint32_t hi, uint32_t w2, uint32_t w3) {
     if (!dst || texels == 0) return kOk;
     const unsigned grid = static_cast<unsigned>(texels / 256 + 1 < 152 * 16 ? texels / 256 + 1 : 152 * 16);
     switch (texel_bytes) {
@@ -384,6 +384,9 @@ int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, 
     case 8:
         cpv_fill_u64<<<grid, 256, 0, stream>>>(static_cast<uint2*>(dst), texels, lo, hi);
         break;
+    case 16:
+        cpv_fill_u128<<<grid, 256, 0, stream>>>(static_cast<uint4*>(dst), texels, make_uint4(lo, hi, w2, w3));
+        break;
     default:
         return kErrInvalid;
     }
@@ -393,15 +396,15 @@ int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, 
 }
 
 int fill_rect(cudaStream_t stream, uint8_t* base, uint64_t pitch, uint32_t w, uint32_t h, uint32_t texel_bytes, uint32_t lo, uint32_t hi, bool write_lo,
-              bool write_hi) {
+              bool write_hi, uint32_t w2, uint32_t w3) {
     if (!base || w == 0 || h == 0) return kOk;
-    if (texel_bytes != 1 && texel_bytes != 2 && texel_bytes != 4 && texel_bytes != 8) return kErrInvalid;
+    if (texel_bytes != 1 && texel_bytes != 2 && texel_bytes != 4 && texel_bytes != 8 && texel_bytes != 16) return kErrInvalid;
     if (reinterpret_cast<uintptr_t>(base) % texel_bytes != 0 || pitch % texel_bytes != 0 || pitch < static_cast<uint64_t>(w) * texel_bytes) return kErrInvalid;
     if (!write_lo && !(texel_bytes == 8 && write_hi)) return kOk;
     if (pitch == static_cast<uint64_t>(w) * texel_bytes && write_lo && (texel_bytes != 8 || write_hi))
-        return fill(stream, base, static_cast<uint64_t>(w) * h, texel_bytes, lo, hi);  // contiguous: one span
+        return fill(stream, base, static_cast<uint64_t>(w) * h, texel_bytes, lo, hi, w2, w3);  // contiguous: one span
     const dim3 grid((w + 255) / 256 < 8 ? (w + 255) / 256 : 8, h < 2048 ? h : 2048);
-    cpv_fill_rect<<<grid, 256, 0, stream>>>(base, pitch, w, h, texel_bytes, lo, hi, write_lo ? 1u : 0u, write_hi ? 1u : 0u);
+    cpv_fill_rect<<<grid, 256, 0, stream>>>(base, pitch, w, h, texel_bytes, make_uint4(lo, hi, w2, w3), write_lo ? 1u : 0u, write_hi ? 1u : 0u);
     count_launch();
     CPV_CUDA(cudaGetLastError());
     return kOk;

@@ -220,12 +220,12 @@ int blit(cudaStream_t stream, const CpvTexture& src, uint8_t* dst, uint32_t dst_
          const int32_t dst_region[4], uint32_t filter);
 
 // Attachment fill with an encoded texel (1, 2, 4 or 8 bytes).
-int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, uint32_t lo, uint32_t hi);
+int fill(cudaStream_t stream, void* dst, uint64_t texels, uint32_t texel_bytes, uint32_t lo, uint32_t hi, uint32_t w2 = 0, uint32_t w3 = 0);
 // Fill of a w x h rectangle of 2-, 4- or 8-byte texels whose rows start
 // `pitch` bytes apart (texel-aligned base and pitch); for 8-byte depth /
 // stencil texels write_lo / write_hi pick the depth and stencil words.
 int fill_rect(cudaStream_t stream, uint8_t* base, uint64_t pitch, uint32_t w, uint32_t h, uint32_t texel_bytes, uint32_t lo, uint32_t hi, bool write_lo,
-              bool write_hi);
+              bool write_hi, uint32_t w2 = 0, uint32_t w3 = 0);
 // Copies `bytes` from pinned host memory to HBM on `stream`: a kernel whose
 // SMs read the host memory directly (16-byte words, both pointers 16-byte
 // aligned), the unaligned remainder by cudaMemcpyAsync. CPV_H2D_KERNEL=0

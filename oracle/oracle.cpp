@@ -592,6 +592,17 @@ bool colour_format(uint32_t fmt, ColourFormat& cf) {
     case 82: cf = {4, 2, 2, 4, {0, 2, 0, 0}}; return true;   /* R16G16_SINT */
     case 98: cf = {4, 1, 4, 3, {0, 0, 0, 0}}; return true;   /* R32_UINT */
     case 99: cf = {4, 1, 4, 4, {0, 0, 0, 0}}; return true;   /* R32_SINT */
+    /* 8- and 16-byte texels */
+    case 91: cf = {8, 4, 2, 0, {0, 2, 4, 6}}; return true;   /* R16G16B16A16_UNORM */
+    case 95: cf = {8, 4, 2, 3, {0, 2, 4, 6}}; return true;   /* R16G16B16A16_UINT */
+    case 96: cf = {8, 4, 2, 4, {0, 2, 4, 6}}; return true;   /* R16G16B16A16_SINT */
+    case 97: cf = {8, 4, 2, 2, {0, 2, 4, 6}}; return true;   /* R16G16B16A16_SFLOAT */
+    case 101: cf = {8, 2, 4, 3, {0, 4, 0, 0}}; return true;  /* R32G32_UINT */
+    case 102: cf = {8, 2, 4, 4, {0, 4, 0, 0}}; return true;  /* R32G32_SINT */
+    case 103: cf = {8, 2, 4, 2, {0, 4, 0, 0}}; return true;  /* R32G32_SFLOAT */
+    case 107: cf = {16, 4, 4, 3, {0, 4, 8, 12}}; return true;  /* R32G32B32A32_UINT */
+    case 108: cf = {16, 4, 4, 4, {0, 4, 8, 12}}; return true;  /* R32G32B32A32_SINT */
+    case 109: cf = {16, 4, 4, 2, {0, 4, 8, 12}}; return true;  /* R32G32B32A32_SFLOAT */
     default: return false;
     }
 }

@@ -258,6 +258,29 @@ def test_colour_attachment_formats_batched(gpu_ctx, oracle, monkeypatch, fmt):
     assert report["color_pixels_differing"] == 0, report
 
 
+# 8- and 16-byte colour texels on the first attachment: R16G16B16A16
+# UNORM and SFLOAT, R32G32 and R32G32B32A32 SFLOAT, under the same variants
+# (opaque, blended, write mask with a logic op, wide lines, flat quads).
+WIDE_COLOUR_ATTACHMENTS = [91, 97, 103, 109]
+
+
+@pytest.mark.parametrize("fmt", WIDE_COLOUR_ATTACHMENTS)
+@pytest.mark.parametrize("program,variant", COLOUR_VARIANTS)
+def test_wide_colour_attachment_formats(gpu_ctx, oracle, fmt, program, variant):
+    scene = c.Scene(c.PROGRAM, 5, [program, variant, 64, 48, 24, 97, fmt])
+    report, stats = check(gpu_ctx, oracle, scene)
+    assert stats["fragments_written"] > 0
+    assert report["color_pixels_differing"] == 0, report
+
+
+@pytest.mark.parametrize("fmt", WIDE_COLOUR_ATTACHMENTS)
+def test_wide_colour_attachment_formats_batched(gpu_ctx, oracle, monkeypatch, fmt):
+    monkeypatch.setenv("CPV_BATCH_MIN_DRAWS", "1")
+    scene = c.Scene(c.PROGRAM, 6, [c.PROGRAM_CUBE, 0x10 | 0x20, 64, 48, 24, 97, fmt])
+    report, _ = check(gpu_ctx, oracle, scene)
+    assert report["color_pixels_differing"] == 0, report
+
+
 def _pack(values):
     """Bytes of a packed scene parameter (byte k = values[k])."""
     out = 0
@@ -336,3 +359,31 @@ def test_integer_colour_attachments(gpu_ctx, oracle, monkeypatch, case, batched)
     assert np.count_nonzero(np.any(gd != rd, axis=-1)) == 0
     for k, (g, o) in enumerate(zip(gx, rx)):
         assert np.count_nonzero(np.any(g != o, axis=-1)) == 0, "attachment %d (format %d)" % (k + 1, fmts[k])
+
+
+# Integer formats with 8- and 16-byte texels on the first attachment: the
+# MRTI program's location 0 output read as integers (16-bit channels
+# clamp, 32-bit channels keep the bits); few triangles, so the integer
+# clear stays visible.
+WIDE_INT_ATTACHMENTS = [95, 96, 101, 102, 107, 108]
+
+
+@pytest.mark.parametrize("fmt", WIDE_INT_ATTACHMENTS)
+@pytest.mark.parametrize("batched", [False, True])
+def test_wide_integer_colour_attachments(gpu_ctx, oracle, monkeypatch, fmt, batched):
+    if batched:
+        monkeypatch.setenv("CPV_BATCH_MIN_DRAWS", "1")
+    scene = c.Scene(c.PROGRAM, 9, [c.PROGRAM_MRTI, 0x10, 64, 48, 5, 0, fmt, _pack([98]), 0])
+    r = c.Renderer(gpu_ctx, scene)
+    try:
+        r.render(1)
+        gc, gd = r.readback()
+        g1 = r.readback_extra(1)
+    finally:
+        r.close()
+    rc, rx, rd, stats = oracle.render_extra(scene)
+    assert stats["fragments_written"] > 0
+    assert gc.shape[-1] == c.colour_texel_bytes(fmt)
+    assert np.count_nonzero(np.any(gc != rc, axis=-1)) == 0, "attachment 0 (format %d)" % fmt
+    assert np.count_nonzero(np.any(gd != rd, axis=-1)) == 0
+    assert np.count_nonzero(np.any(g1 != rx[0], axis=-1)) == 0

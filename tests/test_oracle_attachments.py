@@ -82,3 +82,52 @@ def test_integer_channels_clamp(oracle):
     want2 = np.clip((f0[drawn] * np.float32(400.0) - np.float32(200.0)).astype(np.int64), -128, 127)
     assert np.array_equal(r1, want1) and np.array_equal(r2, want2)
     assert (want1 == 255).any() and (want2 == 127).any() and (want2 == -128).any()
+
+
+def _render0(oracle, program, fmt, seed=7, tris=5):
+    scene = c.Scene(c.PROGRAM, seed, [program, 0x10, 64, 48, tris, 0, fmt, 0, 0])
+    col, _, _, st = oracle.render_extra(scene)
+    assert col.shape == (48, 64, c.colour_texel_bytes(fmt))
+    return col, st
+
+
+def test_wide_float_attachments_narrow_the_same_outputs(oracle):
+    # R32G32B32A32_SFLOAT holds the outputs as they are; R32G32_SFLOAT its
+    # first two channels; R16G16B16A16_SFLOAT them narrowed to binary16
+    # (round to nearest even) and R16G16B16A16_UNORM them clamped and scaled
+    f32, st = _render0(oracle, c.PROGRAM_CUBE, 109)
+    f32 = f32.view(np.float32)
+    g32, _ = _render0(oracle, c.PROGRAM_CUBE, 103)
+    h16, _ = _render0(oracle, c.PROGRAM_CUBE, 97)
+    u16, _ = _render0(oracle, c.PROGRAM_CUBE, 91)
+    assert st["fragments_written"] > 0
+    assert np.array_equal(g32.view(np.float32), f32[..., :2])
+    assert np.array_equal(h16.view(np.float16), f32.astype(np.float16))
+    drawn = np.any(f32 != f32[0, 0], axis=-1)
+    assert drawn.any() and not drawn.all()
+    from tests.parity import unorm
+    assert np.array_equal(u16.view(np.uint16)[drawn].astype(np.int64), unorm(f32[drawn], 16))
+
+
+def test_wide_integer_attachments_keep_or_clamp_the_bits(oracle):
+    # the MRTI program's location 0 is a float vector: 32-bit integer
+    # channels keep its bits, 16-bit UINT channels clamp them to 65535 and
+    # SINT ones to [-32768, 32767]; the clear (-0.3, 0.6, 1.7, 0.45) is
+    # stored as round(clear * 100)
+    raw, _ = _render0(oracle, c.PROGRAM_MRTI, 109)
+    f32, bits = raw.view(np.float32), raw.view(np.uint32)
+    u128, _ = _render0(oracle, c.PROGRAM_MRTI, 107)
+    s64, _ = _render0(oracle, c.PROGRAM_MRTI, 102)
+    u16, _ = _render0(oracle, c.PROGRAM_MRTI, 95)
+    s16, _ = _render0(oracle, c.PROGRAM_MRTI, 96)
+    clear = np.array([-0.3, 0.6, 1.7, 0.45], np.float32)
+    drawn = np.any(f32 != clear, axis=-1)
+    assert drawn.any() and not drawn.all()
+    assert np.array_equal(u128.view(np.uint32)[drawn], bits[drawn])
+    assert np.array_equal(s64.view(np.uint32)[drawn], bits[drawn][:, :2])
+    assert np.array_equal(u16.view(np.uint16)[drawn].astype(np.int64), np.minimum(bits[drawn].astype(np.int64), 65535))
+    s = bits[drawn].view(np.int32).astype(np.int64)
+    assert np.array_equal(s16.view(np.int16)[drawn].astype(np.int64), np.clip(s, -32768, 32767))
+    assert np.all(u128.view(np.int32)[~drawn] == [-30, 60, 170, 45]) and np.all(s16.view(np.int16)[~drawn] == [-30, 60, 170, 45])
+    assert np.all(u16.view(np.uint16)[~drawn] == [65535, 60, 170, 45])
+

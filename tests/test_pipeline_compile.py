@@ -218,7 +218,7 @@ def test_secondary_command_buffers_record_batched_pass(native, monkeypatch, tmp_
 
 
 COLOUR_ATTACHMENTS = [(9, 1, 1, 8, 0), (16, 2, 2, 8, 0), (38, 4, 4, 8, 1), (70, 2, 1, 16, 0), (77, 4, 2, 16, 0), (83, 4, 2, 16, 2),
-                      (100, 4, 1, 32, 2)]
+                      (100, 4, 1, 32, 2), (91, 8, 4, 16, 0), (97, 8, 4, 16, 2), (103, 8, 2, 32, 2), (109, 16, 4, 32, 2)]
 
 
 @pytest.mark.parametrize("fmt,nbytes,channels,bits,kind", COLOUR_ATTACHMENTS)
@@ -236,7 +236,7 @@ def test_colour_attachment_formats_compile(compile_ctx, fmt, nbytes, channels, b
     assert "#define CPV_BLEND_TABLE 0\n" in text
 
 
-@pytest.mark.parametrize("fmt", [70, 77, 83, 100])
+@pytest.mark.parametrize("fmt", [70, 77, 83, 100, 91, 109])
 def test_logic_op_on_wide_colour_format_rejected(compile_ctx, fmt):
     """A logic op is accepted on 8-bit normalised colour attachments only."""
     ctx, _ = compile_ctx
@@ -271,5 +271,11 @@ def test_colour_attachments_compile_and_reject(native, monkeypatch, tmp_path):
         with pytest.raises(RuntimeError):
             c.Renderer(ctx, c.Scene(c.PROGRAM, 1, [c.PROGRAM_CUBE, 0x10, 32, 32, 4, 0, 0, 37, 0]))
         assert "no output for colour attachment 1" in c.icd_last_error()
+        # 8- and 16-byte texels: the first attachment only
+        c.Renderer(ctx, c.Scene(c.PROGRAM, 1, [c.PROGRAM_MRTI, 0x10, 32, 32, 4, 0, 107, 98, 0])).close()
+        assert "batched module compiled" in c.icd_last_error()
+        with pytest.raises(RuntimeError):
+            c.Renderer(ctx, c.Scene(c.PROGRAM, 1, [c.PROGRAM_MRTI, 0x10, 32, 32, 4, 0, 98, 107, 0]))
+        assert "an 8- or 16-byte colour format after the first attachment" in c.icd_last_error()
     finally:
         ctx.close()
