@@ -318,6 +318,9 @@ SIDE_WORKLOADS = [
     ("blend", 3, [], {}, CONFIGS["blend"][2] + "; flat colour: per-primitive blend tables"),
     ("blend_general", 3, [], {"CPV_BLEND_TABLES": "0"}, CONFIGS["blend"][2] + "; blend computed per fragment (no tables)"),
     ("blend_interpolated", 3, [200000, 1920, 1080, 1], {}, CONFIGS["blend"][2] + "; a colour per corner, interpolated per fragment"),
+    ("heightfield_spec_lod", 2, [], {"CPV_SPEC_LOD": "1"},
+     CONFIGS["heightfield"][2] + "; labelled spec-LOD mode: implicit-LOD lambda from quad derivatives over the mip chain "
+     "(not the reference's lambda 0); compared with the oracle in the same mode"),
 ]
 
 
@@ -365,7 +368,8 @@ def roofline_of(name, scene, kernels, frag_written):
     peak, peak_kind = measured_peak()
     alg = algorithmic_bytes(name, scene, frag_written)
     achieved = alg / (kernels[dom]["ms_per_launch"] / 1000.0) / 1e9 if dom in kernels else None
-    base = name.split("_")[0]
+    # committed captures cover the workloads' default modes only
+    base = name if name.endswith("spec_lod") else name.split("_")[0]
     return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2) if achieved else None, "peak": peak, "peak_kind": peak_kind,
             "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None, "traffic": committed_traffic(dom, base),
             "algorithmic_bytes_per_launch": alg, "compute_side": limiter(base) if base != "cube" else
@@ -382,6 +386,7 @@ def measure_workload(ctx, h, icd, name, cfg, params, env, desc, min_seconds=1.5)
     os.environ.update(env)
     try:
         scene = c.Scene(cfg, 1, params)
+        scene.spec_lod = env.get("CPV_SPEC_LOD") == "1"
         r = c.Renderer(ctx, scene)
         try:
             timed_frames(h, r, 3)

@@ -48,7 +48,8 @@ class SceneHeader(ctypes.Structure):
                 ("index_data", vp), ("index_bytes", u64), ("index_type", u32), ("uniform_data", vp), ("uniform_bytes", u32),
                 ("texture_data", vp), ("texture_bytes", u64), ("texture_width", u32), ("texture_height", u32),
                 ("texture_levels", u32), ("texture_format", u32), ("sampler", SamplerDesc), ("num_pipelines", u32),
-                ("pipelines", vp), ("num_draws", u32), ("draws", vp), ("extra_color_count", u32), ("extra_color_formats", u32 * 7)]
+                ("pipelines", vp), ("num_draws", u32), ("draws", vp), ("extra_color_count", u32), ("extra_color_formats", u32 * 7),
+                ("spec_lod", u32)]
 
 
 class SceneDraw(ctypes.Structure):
@@ -156,6 +157,16 @@ class Scene:
     @property
     def draws(self):
         return SceneHeader.from_address(self.ptr).num_draws
+
+    @property
+    def spec_lod(self):
+        """1 when the oracle renders the scene in the quad-derivative LOD mode
+        (the ICD's CPV_SPEC_LOD=1); 0 for the reference's λ = 0."""
+        return SceneHeader.from_address(self.ptr).spec_lod
+
+    @spec_lod.setter
+    def spec_lod(self, value):
+        SceneHeader.from_address(self.ptr).spec_lod = 1 if value else 0
 
     def draw(self, i):
         """Draw i of the scene (a view of the harness's cpv_scene_draw)."""

@@ -677,7 +677,10 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
     s.depth_format = dfmts[dsel];
     s.clear_color[0] = 0.25f; s.clear_color[1] = 0.5f; s.clear_color[2] = 0.75f; s.clear_color[3] = 1.0f;
     if (attachment_format) { s.clear_color[0] = -0.3f; s.clear_color[1] = 0.6f; s.clear_color[2] = 1.7f; s.clear_color[3] = 0.45f; }
-    s.clear_depth = 0.75f;
+    // The textured and mesh programs view their geometry from afar (NDC
+    // depth near 1): their depth is cleared to 1 so a LESS test passes.
+    const bool far_geometry = program == CPV_PROGRAM_TEXLIT || program == CPV_PROGRAM_FETCH || program == CPV_PROGRAM_MESHPC;
+    s.clear_depth = far_geometry ? 1.0f : 0.75f;
     s.clear_stencil = 3;
     viewport_full(s);
     Rng rng(seed);
@@ -736,7 +739,7 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
         }
         if (b >> 4) eb.color_write_mask = b >> 4;
     }
-    if (const uint32_t bounds = (variant >> 28) & 3u) {  // depth bounds test (bits 28-29) against the stored depth (cleared to 0.75)
+    if (const uint32_t bounds = (variant >> 28) & 3u) {  // depth bounds test (bits 28-29) against the stored depth (cleared to 0.75 or 1)
         // 1: the whole range; 2: stored depth from 0.3 up; 3: above the clear depth, so nothing passes
         static const float range[4][2] = {{0.0f, 1.0f}, {0.0f, 1.0f}, {0.3f, 1.0f}, {0.8f, 1.0f}};
         p.depth_bounds_test = 1;

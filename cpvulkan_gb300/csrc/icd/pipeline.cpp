@@ -64,6 +64,7 @@ const char* const kStageMacros[] = {
     "CPV_DEPTH_BOUNDS", "CPV_MIN_DEPTH_BOUNDS", "CPV_MAX_DEPTH_BOUNDS",
     "CPV_COLOR_FORMAT", "CPV_DEPTH_FORMAT", "CPV_ORIGIN_UPPER", "CPV_FS_CONSTANT", "CPV_BLEND_TABLE", "CPV_LINE_WIDTH", "CPV_PRIM_KIND",
     "CPV_CF_BYTES", "CPV_CF_CHANNELS", "CPV_CF_BITS", "CPV_CF_KIND", "CPV_CF_BGRA", "CPV_FS_KILL", "CPV_EARLY_DEPTH", "CPV_VS_SAMPLES", "CPV_EXTRA_CA",
+    "CPV_LOD_SITES",
 };
 
 }  // namespace
@@ -463,7 +464,14 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     spirv::StageResult vr, fr;
     std::string err;
     if (!spirv::translate_stage(vs->module, 0, vs_entry, vs_spec, bindings, attributes, slots, vr, err)) return reject("vertex shader: " + err);
-    if (!spirv::translate_stage(fs->module, 4, fs_entry, fs_spec, {}, {}, slots, fr, err)) return reject("fragment shader: " + err);
+    // CPV_SPEC_LOD=1: the labelled quad-derivative LOD mode for implicit-LOD
+    // sampling in fragment shaders (Vulkan's λ from screen-space
+    // derivatives); otherwise λ is 0, as the reference computes it
+    // (CPVulkan/GlslFunctions.cpp:657-672).
+    const char* spec_lod_env = std::getenv("CPV_SPEC_LOD");
+    const bool spec_lod = spec_lod_env != nullptr && std::atoi(spec_lod_env) == 1;
+    if (!spirv::translate_stage(fs->module, 4, fs_entry, fs_spec, {}, {}, slots, fr, err, spec_lod)) return reject("fragment shader: " + err);
+    if (fr.lod_sites > 8) return reject("more than 8 implicit-LOD sampling instructions in a fragment shader under CPV_SPEC_LOD");
 
     const uint32_t nv = vr.num_floats > fr.num_floats ? vr.num_floats : fr.num_floats;
     const uint32_t tile_shift = tile_shift_for_pipeline();
@@ -545,6 +553,7 @@ VkResult create_graphics_pipeline(Device* dev, PipelineCache* cache, const VkGra
     src << "#define CPV_FS_CONSTANT " << (fs_constant ? 1 : 0) << "\n";
     src << "#define CPV_FS_KILL " << (fr.has_kill ? 1 : 0) << "\n";
     src << "#define CPV_VS_SAMPLES " << (vr.samples > 0 ? 1 : 0) << "\n";
+    src << "#define CPV_LOD_SITES " << fr.lod_sites << "\n";
     // Blending a per-primitive constant colour where each channel's result
     // depends only on that channel of the destination (no DST_ALPHA,
     // ONE_MINUS_DST_ALPHA or SRC_ALPHA_SATURATE colour factors): the result

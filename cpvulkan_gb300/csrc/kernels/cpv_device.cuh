@@ -451,6 +451,96 @@ __device__ __forceinline__ cvec<float, 4> cpv_sample(const CpvTexture& t, float 
 }
 
 /* ------------------------------------------------------------------------- */
+/* Quad-derivative LOD: the labelled "spec LOD" mode (Vulkan 1.1, "Scale      */
+/* Factor Operation, Level-of-Detail Operation and Image Level(s) Selection")*/
+/* ------------------------------------------------------------------------- */
+
+#define CPV_MAX_LOD_SITES 8
+
+/* A fragment's 2x2 quad for implicit-LOD sampling. The fragment shader runs
+ * first for the horizontal neighbour (mode 1: pixel (x ^ 1, y)) and the
+ * vertical one (mode 2: (x, y ^ 1)), each recording the coordinates it
+ * reaches at every implicit-LOD sampling instruction (site k) and sampling
+ * nothing, then for the fragment itself (mode 0), whose sites take fine
+ * derivatives within the quad: dP/dx = P(x | 1) - P(x & ~1), likewise in y.
+ * A site a neighbour did not reach (it discarded first) has derivative 0
+ * in that direction; a site inside a loop sees the neighbour's last value. */
+struct CpvQuadLod {
+    uint32_t mode;
+    uint32_t odd;      /* bit 0: x odd; bit 1: y odd */
+    uint32_t seen[2];  /* bit k: site k reached by neighbour 0 / 1 */
+    float u[2][CPV_MAX_LOD_SITES], v[2][CPV_MAX_LOD_SITES];
+};
+
+/* 0.5 * log2(r) for r = ρ², so that λ_base = log2(max(ρx, ρy)) needs no
+ * square root. Written from the series ln m = 2 atanh(s) = 2 (s + s³/3 +
+ * s⁵/5 + s⁷/7 + s⁹/9 + ...), s = (m - 1) / (m + 1), with the mantissa m
+ * reduced to [√½, √2] so |s| <= 0.1716 and the first omitted term is below
+ * 2⁻²⁸ of the sum; every step is one rounded binary32 operation, so a host
+ * restatement in the same order gives the same bits. r = 0 or NaN gives
+ * -∞ (no derivative: the least λ), r = +∞ gives +∞. */
+__device__ __forceinline__ float cpv_half_log2(float r) {
+    if (!(r > 0.0f)) return __uint_as_float(0xFF800000u);
+    if (r == __uint_as_float(0x7F800000u)) return r;
+    uint32_t b = __float_as_uint(r);
+    int32_t e = 0;
+    if (b < 0x00800000u) {
+        b = __float_as_uint(__fmul_rn(r, 16777216.0f));  /* subnormal: scale by 2^24 */
+        e = -24;
+    }
+    e += static_cast<int32_t>(b >> 23) - 127;
+    float m = __uint_as_float((b & 0x007FFFFFu) | 0x3F800000u);
+    if (m > 1.41421356f) {
+        m = __fmul_rn(m, 0.5f);
+        e += 1;
+    }
+    const float s = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
+    const float s2 = __fmul_rn(s, s);
+    float q = __fadd_rn(__fmul_rn(s2, 0.111111111f), 0.142857143f);
+    q = __fadd_rn(__fmul_rn(q, s2), 0.2f);
+    q = __fadd_rn(__fmul_rn(q, s2), 0.333333333f);
+    q = __fadd_rn(__fmul_rn(q, s2), 1.0f);
+    const float log2m = __fmul_rn(__fmul_rn(s, q), 2.88539008f);  /* 2 / ln 2 */
+    return __fmul_rn(__fadd_rn(static_cast<float>(e), log2m), 0.5f);
+}
+
+/* Implicit-LOD sampling at site k of a fragment shader compiled for the
+ * quad-derivative mode: records the coordinates in a neighbour's run
+ * (returning zeros), else samples with λ_base = log2(max(ρx, ρy)),
+ * ρ = |(du/d·, dv/d·)| scaled by the level-0 extent, through the same bias,
+ * clamp and level selection as explicit LOD. Without a quad (a shader run
+ * once per primitive: its coordinates do not vary) λ_base is -∞. */
+__device__ __forceinline__ cvec<float, 4> cpv_sample_quad(const CpvTexture& t, float u, float v, CpvQuadLod* q, uint32_t k) {
+    if (q != nullptr && q->mode != 0u) {
+        const uint32_t n = q->mode - 1u;
+        q->u[n][k] = u;
+        q->v[n][k] = v;
+        q->seen[n] |= 1u << k;
+        cvec<float, 4> r;
+        r.v[0] = r.v[1] = r.v[2] = r.v[3] = 0.0f;
+        return r;
+    }
+    float lambda = __uint_as_float(0xFF800000u);
+    if (q != nullptr && t.levels != 0u) {
+        const float w = __uint2float_rn(t.level_w[0]), h = __uint2float_rn(t.level_h[0]);
+        float r2[2];
+#pragma unroll
+        for (uint32_t n = 0; n < 2; n++) {
+            float du = 0.0f, dv = 0.0f;
+            if ((q->seen[n] >> k) & 1u) {
+                const bool odd = ((q->odd >> n) & 1u) != 0u;
+                du = odd ? __fsub_rn(u, q->u[n][k]) : __fsub_rn(q->u[n][k], u);
+                dv = odd ? __fsub_rn(v, q->v[n][k]) : __fsub_rn(q->v[n][k], v);
+            }
+            const float a = __fmul_rn(du, w), b = __fmul_rn(dv, h);
+            r2[n] = __fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b));
+        }
+        lambda = cpv_half_log2(r2[0] >= r2[1] ? r2[0] : r2[1]);
+    }
+    return cpv_sample(t, u, v, lambda);
+}
+
+/* ------------------------------------------------------------------------- */
 /* Input assembly                                                            */
 /* ------------------------------------------------------------------------- */
 

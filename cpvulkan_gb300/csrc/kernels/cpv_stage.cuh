@@ -595,27 +595,11 @@ __device__ __forceinline__ void cpv_blend(const float s[4], const float d[4], co
 #endif
 #define CPV_EARLY_DEPTH (CPV_PRIM_KIND == 0 && CPV_DEPTH_TEST && CPV_DEPTH_FORMAT != 0 && !(CPV_STENCIL_TEST && CPV_DEPTH_FORMAT == 130) && !CPV_FS_KILL)
 
-/* Shading of one covered pixel: barycentrics (w_k / area), screen-linear
- * depth, varyings (perspective Σ w·v/p ÷ Σ w/p, linear Σ w·v, or flat from
- * the provoking vertex; CPVulkan/CommandBuffer.Draw.cpp:816-954), viewport
- * depth mapping (:1300-1313) and the fragment shader. Returns true when the
- * shader discards, or when `early` (the pixel's current state) is given and
- * the fragment fails the early depth test. */
-__device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& t, const float wr[3], int32_t x, int32_t y, float* colour,
-                                          float& mapped, const CpvPixel* early = nullptr) {
-    float in[CPV_NV_ALLOC];
-#if CPV_PRIM_KIND == 2
-    /* a point's fragments take its vertex's outputs as they are and its NDC z
-     * (CPVulkan/CommandBuffer.Draw.cpp:1364-1374) */
-    (void)wr;
-    const float depth = t.za.x;
-#pragma unroll
-    for (int c = 0; c < CPV_NV; c++) in[c] = t.var[0][c];
-#elif CPV_PRIM_KIND == 1
-    /* line parameter t = dot(p - p0, d) / (|d| |d|) at the pixel centre,
-     * weights (1 - t, t), depth p0.z * t + p1.z * (1 - t) as the reference
-     * writes it (CPVulkan/CommandBuffer.Draw.cpp:1441-1486) */
-    (void)wr;
+/* The varyings of a line's fragment at pixel (x, y): line parameter
+ * t = dot(p - p0, d) / (|d| |d|) at the pixel centre, weights (1 - t, t),
+ * depth p0.z * t + p1.z * (1 - t) as the reference writes it
+ * (CPVulkan/CommandBuffer.Draw.cpp:1441-1486). Returns the NDC depth. */
+__device__ __forceinline__ float cpv_line_inputs(const CpvDrawParams& P, const CpvTri& t, int32_t x, int32_t y, float* in) {
     const float xf = cpv_pixel_ndc(x, P.viewport[2]), yf = cpv_pixel_ndc(y, P.viewport[3]);
     const float num = __fadd_rn(__fmul_rn(__fsub_rn(xf, t.var[2][0]), t.var[2][2]), __fmul_rn(__fsub_rn(yf, t.var[2][1]), t.var[2][3]));
     const float lt = __fdiv_rn(num, t.var[2][4]);
@@ -639,21 +623,18 @@ __device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& 
             in[c] = __fdiv_rn(n, d);
         }
     }
-#else
-    const float area = t.za.w;
-    float w[3];
-    w[0] = __fdiv_rn(wr[0], area);
-    w[1] = __fdiv_rn(wr[1], area);
-    w[2] = __fdiv_rn(wr[2], area);
-    const float depth = __fadd_rn(__fadd_rn(__fmul_rn(t.za.x, w[0]), __fmul_rn(t.za.y, w[1])), __fmul_rn(t.za.z, w[2]));
-#if CPV_EARLY_DEPTH
-    if (early) {
-        const float early_mapped = __fadd_rn(__fmul_rn(__fsub_rn(P.viewport[5], P.viewport[4]), depth), P.viewport[4]);
-        if (!cpv_fcompare(early_mapped, early->depth, CPV_DEPTH_OP)) return true;
-    }
-#else
-    (void)early;
-#endif
+    return depth;
+}
+
+/* A triangle's screen-linear NDC depth at barycentrics w (w_k / area). */
+__device__ __forceinline__ float cpv_tri_depth(const CpvTri& t, const float w[3]) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(t.za.x, w[0]), __fmul_rn(t.za.y, w[1])), __fmul_rn(t.za.z, w[2]));
+}
+
+/* A triangle's varyings at barycentrics w: perspective Σ w·v/p ÷ Σ w/p,
+ * linear Σ w·v, or flat from the provoking vertex
+ * (CPVulkan/CommandBuffer.Draw.cpp:816-954). */
+__device__ __forceinline__ void cpv_tri_inputs(const CpvTri& t, const float w[3], float* in) {
     const float pw[3] = {t.wf.x, t.wf.y, t.wf.z};
     const uint32_t pslot = cpv_tri_pslot(t);
 #pragma unroll
@@ -676,18 +657,101 @@ __device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& 
             in[c] = __fdiv_rn(num, den);
         }
     }
+}
+
+/* gl_FragCoord of pixel (x, y) at NDC depth `depth`. */
+__device__ __forceinline__ void cpv_frag_coord(const CpvDrawParams& P, int32_t x, int32_t y, float depth, float fc[4]) {
+#if CPV_ORIGIN_UPPER
+    (void)P;
+    fc[0] = static_cast<float>(x);
+#else
+    fc[0] = __fsub_rn(__fsub_rn(P.viewport[2], static_cast<float>(x)), 1.0f);
+#endif
+    fc[1] = static_cast<float>(y);
+    fc[2] = depth;
+    fc[3] = 1.0f;
+}
+
+#ifndef CPV_LOD_SITES
+#define CPV_LOD_SITES 0
+#endif
+
+#if CPV_LOD_SITES > 0 && !CPV_FS_CONSTANT
+/* The quad-derivative mode's helper runs: the fragment shader at the
+ * horizontal and the vertical neighbour of (x, y) within its 2x2 quad,
+ * whatever their coverage, with the varyings, depth and gl_FragCoord the
+ * primitive has there; they write nothing and only record their sampling
+ * coordinates in q. */
+__device__ __forceinline__ void cpv_quad_helpers(const CpvDrawParams& P, const CpvTri& t, int32_t x, int32_t y, CpvQuadLod& q) {
+    q.odd = static_cast<uint32_t>(x & 1) | (static_cast<uint32_t>(y & 1) << 1);
+    q.seen[0] = q.seen[1] = 0u;
+#pragma unroll
+    for (uint32_t n = 0; n < 2; n++) {
+        const int32_t nx = n == 0 ? (x ^ 1) : x, ny = n == 0 ? y : (y ^ 1);
+        float in[CPV_NV_ALLOC];
+#if CPV_PRIM_KIND == 2
+        const float depth = t.za.x;
+#pragma unroll
+        for (int c = 0; c < CPV_NV; c++) in[c] = t.var[0][c];
+#elif CPV_PRIM_KIND == 1
+        const float depth = cpv_line_inputs(P, t, nx, ny, in);
+#else
+        float w[3];
+        (void)cpv_covers(t, cpv_pixel_ndc(nx, P.viewport[2]), cpv_pixel_ndc(ny, P.viewport[3]), w);
+        const float area = t.za.w;
+#pragma unroll
+        for (int k = 0; k < 3; k++) w[k] = __fdiv_rn(w[k], area);
+        const float depth = cpv_tri_depth(t, w);
+        cpv_tri_inputs(t, w, in);
+#endif
+        float fc[4], scratch[CPV_COLOUR_FLOATS];
+        cpv_frag_coord(P, nx, ny, depth, fc);
+        q.mode = n + 1u;
+        (void)cpv_fs_run(P, in, fc, cpv_tri_front(t), scratch, &q);
+    }
+    q.mode = 0u;
+}
+#endif
+
+/* Shading of one covered pixel: barycentrics (w_k / area), screen-linear
+ * depth, varyings (cpv_tri_inputs, cpv_line_inputs; a point's fragments
+ * take its vertex's outputs as they are and its NDC z,
+ * CPVulkan/CommandBuffer.Draw.cpp:1364-1374), viewport depth mapping
+ * (:1300-1313) and the fragment shader. Returns true when the shader
+ * discards, or when `early` (the pixel's current state) is given and the
+ * fragment fails the early depth test. */
+__device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& t, const float wr[3], int32_t x, int32_t y, float* colour,
+                                          float& mapped, const CpvPixel* early = nullptr) {
+    float in[CPV_NV_ALLOC];
+#if CPV_PRIM_KIND == 2
+    (void)wr;
+    const float depth = t.za.x;
+#pragma unroll
+    for (int c = 0; c < CPV_NV; c++) in[c] = t.var[0][c];
+#elif CPV_PRIM_KIND == 1
+    (void)wr;
+    const float depth = cpv_line_inputs(P, t, x, y, in);
+#else
+    const float area = t.za.w;
+    float w[3];
+    w[0] = __fdiv_rn(wr[0], area);
+    w[1] = __fdiv_rn(wr[1], area);
+    w[2] = __fdiv_rn(wr[2], area);
+    const float depth = cpv_tri_depth(t, w);
+#if CPV_EARLY_DEPTH
+    if (early) {
+        const float early_mapped = __fadd_rn(__fmul_rn(__fsub_rn(P.viewport[5], P.viewport[4]), depth), P.viewport[4]);
+        if (!cpv_fcompare(early_mapped, early->depth, CPV_DEPTH_OP)) return true;
+    }
+#else
+    (void)early;
+#endif
+    cpv_tri_inputs(t, w, in);
 #endif /* CPV_PRIM_KIND */
     const float min_d = P.viewport[4], max_d = P.viewport[5];
     mapped = __fadd_rn(__fmul_rn(__fsub_rn(max_d, min_d), depth), min_d);
     float frag_coord[4];
-#if CPV_ORIGIN_UPPER
-    frag_coord[0] = static_cast<float>(x);
-#else
-    frag_coord[0] = __fsub_rn(__fsub_rn(P.viewport[2], static_cast<float>(x)), 1.0f);
-#endif
-    frag_coord[1] = static_cast<float>(y);
-    frag_coord[2] = depth;
-    frag_coord[3] = 1.0f;
+    cpv_frag_coord(P, x, y, depth, frag_coord);
 #if CPV_FS_CONSTANT
     /* shaded once at set-up (a discarding primitive is not live) */
     (void)in;
@@ -695,6 +759,10 @@ __device__ __forceinline__ bool cpv_shade(const CpvDrawParams& P, const CpvTri& 
 #pragma unroll
     for (int c = 0; c < 4; c++) colour[c] = t.var[0][c];
     return false;
+#elif CPV_LOD_SITES > 0
+    CpvQuadLod q;
+    cpv_quad_helpers(P, t, x, y, q);
+    return cpv_fs_run(P, in, frag_coord, cpv_tri_front(t), colour, &q);
 #else
     return cpv_fs_run(P, in, frag_coord, cpv_tri_front(t), colour);
 #endif

@@ -399,8 +399,8 @@ struct PtrInfo {
 class Translator {
 public:
     Translator(const Module& m, uint32_t model, const std::vector<SpecConstant>& spec, const std::vector<VertexBinding>& bindings,
-               const std::vector<VertexAttribute>& attributes, std::vector<ResourceSlot>& slots)
-        : m_(m), model_(model), spec_(spec), bindings_(bindings), attributes_(attributes), slots_(slots) {}
+               const std::vector<VertexAttribute>& attributes, std::vector<ResourceSlot>& slots, bool spec_lod)
+        : m_(m), model_(model), spec_(spec), bindings_(bindings), attributes_(attributes), slots_(slots), spec_lod_(spec_lod && model == 4) {}
 
     bool run(const std::string& entry_name, StageResult& out, std::string& error);
 
@@ -411,6 +411,7 @@ private:
     const std::vector<VertexBinding>& bindings_;
     const std::vector<VertexAttribute>& attributes_;
     std::vector<ResourceSlot>& slots_;
+    bool spec_lod_;  // FS: implicit-LOD sampling takes λ from quad derivatives
 
     std::ostringstream types_;    // struct/array definitions
     std::ostringstream loaders_;  // explicit-layout load helpers
@@ -426,6 +427,7 @@ private:
     std::string err_;
     bool has_kill_ = false;
     uint32_t samples_ = 0;
+    uint32_t lod_sites_ = 0;  // implicit-LOD sampling instructions (spec_lod_)
     uint32_t instructions_ = 0;
     uint32_t out_outputs_ = 0;  // FS output locations declared
 
@@ -1457,6 +1459,14 @@ bool Translator::emit_instruction(const Instruction& ins, const std::map<uint32_
             lod = value(w[5]);
         }
         samples_++;
+        if (ins.opcode == OpImageSampleImplicitLod && spec_lod_) {
+            // λ from the coordinates of the quad's neighbours at this
+            // instruction (one site per instruction)
+            body_ << "  " << R(w[1]) << " = cpv_sample_quad(P.tex[" << h->second << "], " << comp(w[3], 0) << ", " << comp(w[3], 1) << ", cpv_lod, "
+                  << lod_sites_ << ");\n";
+            lod_sites_++;
+            return true;
+        }
         body_ << "  " << R(w[1]) << " = cpv_sample(P.tex[" << h->second << "], " << comp(w[3], 0) << ", " << comp(w[3], 1) << ", " << lod << ");\n";
         return true;
     }
@@ -1523,6 +1533,7 @@ bool Translator::run(const std::string& entry_name, StageResult& out, std::strin
     }
     out.has_kill = has_kill_;
     out.samples = samples_;
+    out.lod_sites = lod_sites_;
     out.instructions = instructions_;
     out.outputs = out_outputs_;
     const std::string ns = model_ == 0 ? "cpv_vs_ns" : "cpv_fs_ns";
@@ -1536,8 +1547,9 @@ bool Translator::run(const std::string& entry_name, StageResult& out, std::strin
         s << "  cpv_pos[0] = cpv_pos[1] = cpv_pos[2] = 0.0f; cpv_pos[3] = 1.0f;\n";
     } else {
         s << "__device__ __forceinline__ bool cpv_fs_run(const CpvDrawParams& P, const float* cpv_in, const float* cpv_frag_coord, "
-             "bool cpv_front, float* cpv_colour) {\n";
+             "bool cpv_front, float* cpv_colour" << (spec_lod_ ? ", CpvQuadLod* cpv_lod = nullptr" : "") << ") {\n";
         s << "  using namespace " << ns << ";\n  (void)cpv_in; (void)cpv_frag_coord; (void)cpv_front;\n";
+        if (spec_lod_) s << "  (void)cpv_lod;\n";
         s << "  cpv_colour[0] = cpv_colour[1] = cpv_colour[2] = 0.0f; cpv_colour[3] = 1.0f;\n";
     }
     s << decls_.str() << pro_.str() << body_.str() << " cpv_epilogue:;\n" << epi_.str();
@@ -1551,8 +1563,8 @@ bool Translator::run(const std::string& entry_name, StageResult& out, std::strin
 
 bool translate_stage(const Module& m, uint32_t model, const std::string& entry, const std::vector<SpecConstant>& spec,
                      const std::vector<VertexBinding>& bindings, const std::vector<VertexAttribute>& attributes,
-                     std::vector<ResourceSlot>& slots, StageResult& out, std::string& error) {
-    Translator t(m, model, spec, bindings, attributes, slots);
+                     std::vector<ResourceSlot>& slots, StageResult& out, std::string& error, bool spec_lod) {
+    Translator t(m, model, spec, bindings, attributes, slots, spec_lod);
     return t.run(entry, out, error);
 }
 

@@ -130,6 +130,7 @@ struct StageResult {
     bool origin_upper_left = true;
     bool has_kill = false;
     uint32_t samples = 0;      // image sampling instructions emitted
+    uint32_t lod_sites = 0;    // FS with spec_lod: implicit-LOD sampling instructions (quad-derivative sites)
     uint32_t instructions = 0; // SPIR-V instructions of the entry function
     bool reads_frag_coord = false;    // FS: FragCoord is an input
     bool reads_front_facing = false;  // FS: FrontFacing is an input
@@ -138,9 +139,12 @@ struct StageResult {
 
 // Translates the entry point of `m` for `model` (0 vertex, 4 fragment) into a
 // device function named cpv_vs_run / cpv_fs_run. Resource slots are appended
-// to `slots` as new (set, binding) pairs are met.
+// to `slots` as new (set, binding) pairs are met. With spec_lod, a fragment
+// shader's implicit-LOD sampling takes λ from quad derivatives of its
+// coordinates (cpv_sample_quad) instead of the reference's λ = 0, and
+// cpv_fs_run takes the quad's context as a last argument.
 bool translate_stage(const Module& m, uint32_t model, const std::string& entry, const std::vector<SpecConstant>& spec,
                      const std::vector<VertexBinding>& bindings, const std::vector<VertexAttribute>& attributes,
-                     std::vector<ResourceSlot>& slots, StageResult& out, std::string& error);
+                     std::vector<ResourceSlot>& slots, StageResult& out, std::string& error, bool spec_lod = false);
 
 }  // namespace cpv::spirv

@@ -157,6 +157,11 @@ typedef struct cpv_scene {
      * round(clear_color * 100). */
     uint32_t extra_color_count;
     uint32_t extra_color_formats[CPV_SCENE_MAX_EXTRA_COLOR];
+
+    /* 1: implicit-LOD sampling in fragment shaders takes λ from quad
+     * derivatives (the ICD's CPV_SPEC_LOD=1 mode); 0: λ = 0 as the
+     * reference computes it. */
+    uint32_t spec_lod;
 } cpv_scene;
 
 #ifdef __cplusplus

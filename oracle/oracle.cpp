@@ -382,6 +382,67 @@ struct VsOut {
     float point_size; /* gl_PointSize (1 when the shader does not write it) */
 };
 
+/* The quad-derivative LOD mode (cpv_scene::spec_lod): the inputs the
+ * fragment's primitive has at its horizontal neighbour (x ^ 1, y) and its
+ * vertical one (x, y ^ 1) in the 2x2 quad, whatever their coverage, for
+ * fine derivatives dP/dx = P(x | 1) - P(x & ~1) (Vulkan 1.1, "Derivative
+ * Operations"). The GPU path runs the shader there and records its
+ * sampling coordinates (cpv_sample_quad); the restated programs sample at
+ * coordinates that are their inputs, so the inputs suffice. */
+struct Quad {
+    uint32_t odd;       /* bit 0: x odd; bit 1: y odd */
+    const float* in[2];
+};
+
+/* 0.5 * log2(r), the same binary32 steps as the GPU path's cpv_half_log2:
+ * the series ln m = 2 (s + s³/3 + s⁵/5 + s⁷/7 + s⁹/9), s = (m - 1) / (m + 1),
+ * on the mantissa reduced to [√½, √2]; 0 or NaN give -∞, +∞ gives +∞. */
+float half_log2(float r) {
+    if (!(r > 0.0f)) return -std::numeric_limits<float>::infinity();
+    if (r == std::numeric_limits<float>::infinity()) return r;
+    uint32_t b;
+    std::memcpy(&b, &r, 4);
+    int32_t e = 0;
+    if (b < 0x00800000u) {
+        const float scaled = r * 16777216.0f;
+        std::memcpy(&b, &scaled, 4);
+        e = -24;
+    }
+    e += static_cast<int32_t>(b >> 23) - 127;
+    const uint32_t mb = (b & 0x007FFFFFu) | 0x3F800000u;
+    float m;
+    std::memcpy(&m, &mb, 4);
+    if (m > 1.41421356f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float s2 = s * s;
+    float q = s2 * 0.111111111f + 0.142857143f;
+    q = q * s2 + 0.2f;
+    q = q * s2 + 0.333333333f;
+    q = q * s2 + 1.0f;
+    const float log2m = (s * q) * 2.88539008f;
+    return (static_cast<float>(e) + log2m) * 0.5f;
+}
+
+/* λ_base = log2(max(ρx, ρy)) of implicit-LOD sampling at (u, v), with
+ * ρ = |(du, dv)| scaled by the level-0 extent (Vulkan 1.1, "Scale Factor
+ * Operation"); the derivatives are the differences with the neighbours'
+ * coordinates (un[n], vn[n]), signed by the fragment's place in its quad. */
+float quad_lambda(const Texture& t, float u, float v, const float un[2], const float vn[2], uint32_t odd) {
+    const float w = static_cast<float>(t.level_w[0]), h = static_cast<float>(t.level_h[0]);
+    float r2[2];
+    for (uint32_t n = 0; n < 2; n++) {
+        const bool o = ((odd >> n) & 1u) != 0u;
+        const float du = o ? u - un[n] : un[n] - u;
+        const float dv = o ? v - vn[n] : vn[n] - v;
+        const float a = du * w, b = dv * h;
+        r2[n] = a * a + b * b;
+    }
+    return half_log2(r2[0] >= r2[1] ? r2[0] : r2[1]);
+}
+
 /* attr[location][4] holds each attribute as fetched (missing components
  * default to 0,0,0,1). */
 void run_vs(uint32_t program, const float attr[8][4], const Resources& r, VsOut& out) {
@@ -435,7 +496,7 @@ void run_vs(uint32_t program, const float attr[8][4], const Resources& r, VsOut&
  * LLVMRuntime/SPIRVCompiler.cpp:3308-3310, 3642-3651). colour holds 4
  * floats per output location (locations 0-7); a program fills the
  * locations it declares. */
-bool run_fs(uint32_t program, const float* in, const Resources& r, float* colour, uint32_t spec_k) {
+bool run_fs(uint32_t program, const float* in, const Resources& r, float* colour, uint32_t spec_k, const Quad* quad) {
     switch (program) {
     case CPV_PROGRAM_MRT: {
         /* gen_spirv.py mrt_frag: one SPIR-V operation per float operation */
@@ -478,7 +539,16 @@ bool run_fs(uint32_t program, const float* in, const Resources& r, float* colour
         return false;
     case CPV_PROGRAM_TEXLIT: {
         float c[4] = {0, 0, 0, 1};
-        if (r.texture && r.sampler) sample(*r.texture, *r.sampler, in[0], in[1], 0.0f, c);
+        if (r.texture && r.sampler) {
+            /* implicit LOD: λ 0 as the reference computes it
+             * (CPVulkan/GlslFunctions.cpp:657-672), or from the quad */
+            float lod = 0.0f;
+            if (quad && r.texture->levels != 0) {
+                const float un[2] = {quad->in[0][0], quad->in[1][0]}, vn[2] = {quad->in[0][1], quad->in[1][1]};
+                lod = quad_lambda(*r.texture, in[0], in[1], un, vn, quad->odd);
+            }
+            sample(*r.texture, *r.sampler, in[0], in[1], lod, c);
+        }
         float n[3];
         normalize3(in + 2, n);
         const float light[3] = {ubo_at(r, 16), ubo_at(r, 17), ubo_at(r, 18)};
@@ -1022,11 +1092,12 @@ float interp_linear(const float v[3], const float w[3]) {
 }
 
 /* Per-fragment operations (LLVMRuntime/PipelineCompiler.cpp:1020-1429). */
-void fragment(Frame& f, const cpv_scene_pipeline& p, uint32_t x, uint32_t y, float depth_mapped, bool front, const float* inputs) {
+void fragment(Frame& f, const cpv_scene_pipeline& p, uint32_t x, uint32_t y, float depth_mapped, bool front, const float* inputs,
+              const Quad* quad = nullptr) {
     const cpv_scene* s = f.s;
     f.stats->fragments++;
     float colour[32];
-    if (run_fs(p.program, inputs, f.res, colour, p.spec_k)) return;
+    if (run_fs(p.program, inputs, f.res, colour, p.spec_k, quad)) return;
 
     const uint64_t pix = static_cast<uint64_t>(y) * s->width + x;
     uint8_t* ds = f.depth ? f.depth + pix * f.depth_size : nullptr;
@@ -1167,6 +1238,19 @@ bool fragment_weights(const TriSetup& ts, float xf, float yf, float w[3], float&
     return true;
 }
 
+/* The weights of fragment_weights at any pixel centre, covered or not: a
+ * quad neighbour's barycentrics. */
+void helper_weights(const TriSetup& ts, float xf, float yf, float w[3]) {
+    static const int kFront[3][2] = {{1, 2}, {2, 0}, {0, 1}};
+    static const int kBack[3][2] = {{2, 1}, {0, 2}, {1, 0}};
+    const int (*e)[2] = ts.front ? kFront : kBack;
+    for (int k = 0; k < 3; k++) {
+        const float* a = ts.P[e[k][0]];
+        const float* b = ts.P[e[k][1]];
+        w[k] = edge(a[0], a[1], b[0], b[1], xf, yf) / ts.area;
+    }
+}
+
 /* The varyings of GetFragmentInput (SetDatum, CPVulkan/CommandBuffer.Draw.cpp:816-869,
  * 911-951): perspective, linear or the provoking vertex's value, per float
  * component in declaration order. */
@@ -1204,6 +1288,20 @@ void raster_triangle(Frame& f, const cpv_scene_pipeline& p, const ProgramInfo& i
             float inputs[kMaxVaryings];
             fragment_inputs(info, ts, vs, w, inputs);
             const float mapped = (max_d - min_d) * depth + min_d;
+            if (s->spec_lod) {
+                float nin[2][kMaxVaryings];
+                for (int n = 0; n < 2; n++) {
+                    const int64_t nx = n == 0 ? (x ^ 1) : x, ny = n == 0 ? y : (y ^ 1);
+                    const float nxf = (static_cast<float>(nx) / vw + half_x) * 2.0f - 1.0f;
+                    const float nyf = (static_cast<float>(ny) / vh + half_y) * 2.0f - 1.0f;
+                    float nw[3];
+                    helper_weights(ts, nxf, nyf, nw);
+                    fragment_inputs(info, ts, vs, nw, nin[n]);
+                }
+                const Quad quad = {static_cast<uint32_t>(x & 1) | (static_cast<uint32_t>(y & 1) << 1), {nin[0], nin[1]}};
+                fragment(f, p, static_cast<uint32_t>(x), static_cast<uint32_t>(y), mapped, ts.front, inputs, &quad);
+                continue;
+            }
             fragment(f, p, static_cast<uint32_t>(x), static_cast<uint32_t>(y), mapped, ts.front, inputs);
         }
     }
@@ -1249,7 +1347,9 @@ void rasterise_points(Frame& f, const cpv_scene_pipeline& p, const Assembled& as
                 const float pt = 0.5f + static_cast<float>(static_cast<int32_t>(y - sy)) / size;
                 if (!(ps >= 0 && pt >= 0 && ps <= 1 && pt <= 1)) continue;
                 const float mapped = (max_d - min_d) * p0[2] + min_d;
-                fragment(f, p, static_cast<uint32_t>(x), static_cast<uint32_t>(y), mapped, true, v.var);
+                /* a point's inputs are the same at its quad neighbours */
+                const Quad quad = {static_cast<uint32_t>(x & 1) | (static_cast<uint32_t>(y & 1) << 1), {v.var, v.var}};
+                fragment(f, p, static_cast<uint32_t>(x), static_cast<uint32_t>(y), mapped, true, v.var, s->spec_lod ? &quad : nullptr);
             }
         }
     }
@@ -1290,6 +1390,37 @@ void rasterise_lines(Frame& f, const cpv_scene_pipeline& p, const Assembled& as,
         const float c00[2] = {P[0][0] + ox, P[0][1] + oy}, c01[2] = {P[0][0] - ox, P[0][1] - oy};
         const float c10[2] = {P[1][0] + ox, P[1][1] + oy}, c11[2] = {P[1][0] - ox, P[1][1] - oy};
         const float dx = P[1][0] - P[0][0], dy = P[1][1] - P[0][1];
+        /* the line parameter, weights, varyings and depth at a pixel centre */
+        auto line_inputs = [&](float xf, float yf, float* inputs) {
+            const float num = (xf - P[0][0]) * dx + (yf - P[0][1]) * dy;
+            const float len = std::sqrt(dx * dx + dy * dy);
+            const float lt = num / (len * len);
+            const float wts[2] = {1.0f - lt, lt};
+            int comp = 0;
+            for (int in = 0; in < info.num_inputs; in++) {
+                for (int c = 0; c < info.input_size[in]; c++, comp++) {
+                    switch (info.input_interp[in]) {
+                    case INTERP_PERSPECTIVE: {
+                        float n = 0.0f, d = 0.0f;
+                        for (int k = 0; k < 2; k++) {
+                            n = n + wts[k] * v[k]->var[comp] / P[k][3];
+                            d = d + wts[k] / P[k][3];
+                        }
+                        inputs[comp] = n / d;
+                        break;
+                    }
+                    case INTERP_LINEAR: {
+                        float r = 0.0f;
+                        for (int k = 0; k < 2; k++) r = r + wts[k] * v[k]->var[comp];
+                        inputs[comp] = r;
+                        break;
+                    }
+                    case INTERP_FLAT: inputs[comp] = vs[provoking].var[comp]; break;
+                    }
+                }
+            }
+            return P[0][2] * lt + P[1][2] * (1.0f - lt);
+        };
         for (uint32_t y = f.row_index; static_cast<float>(y) < vh && y < s->height; y += f.row_stride) {
             const float yf = (static_cast<float>(y) / vh + half_y) * 2.0f - 1.0f;
             for (uint32_t x = 0; static_cast<float>(x) < vw && x < s->width; x++) {
@@ -1297,36 +1428,19 @@ void rasterise_lines(Frame& f, const cpv_scene_pipeline& p, const Assembled& as,
                 if (!(edge(c00[0], c00[1], c01[0], c01[1], xf, yf) >= 0 && edge(c11[0], c11[1], c10[0], c10[1], xf, yf) >= 0 &&
                       edge(c10[0], c10[1], c00[0], c00[1], xf, yf) >= 0 && edge(c01[0], c01[1], c11[0], c11[1], xf, yf) >= 0))
                     continue;
-                const float num = (xf - P[0][0]) * dx + (yf - P[0][1]) * dy;
-                const float len = std::sqrt(dx * dx + dy * dy);
-                const float lt = num / (len * len);
-                const float wts[2] = {1.0f - lt, lt};
                 float inputs[kMaxVaryings];
-                int comp = 0;
-                for (int in = 0; in < info.num_inputs; in++) {
-                    for (int c = 0; c < info.input_size[in]; c++, comp++) {
-                        switch (info.input_interp[in]) {
-                        case INTERP_PERSPECTIVE: {
-                            float n = 0.0f, d = 0.0f;
-                            for (int k = 0; k < 2; k++) {
-                                n = n + wts[k] * v[k]->var[comp] / P[k][3];
-                                d = d + wts[k] / P[k][3];
-                            }
-                            inputs[comp] = n / d;
-                            break;
-                        }
-                        case INTERP_LINEAR: {
-                            float r = 0.0f;
-                            for (int k = 0; k < 2; k++) r = r + wts[k] * v[k]->var[comp];
-                            inputs[comp] = r;
-                            break;
-                        }
-                        case INTERP_FLAT: inputs[comp] = vs[provoking].var[comp]; break;
-                        }
-                    }
-                }
-                const float depth = P[0][2] * lt + P[1][2] * (1.0f - lt);
+                const float depth = line_inputs(xf, yf, inputs);
                 const float mapped = (max_d - min_d) * depth + min_d;
+                if (s->spec_lod) {
+                    float nin[2][kMaxVaryings];
+                    for (int n = 0; n < 2; n++) {
+                        const uint32_t nx = n == 0 ? (x ^ 1u) : x, ny = n == 0 ? y : (y ^ 1u);
+                        line_inputs((static_cast<float>(nx) / vw + half_x) * 2.0f - 1.0f, (static_cast<float>(ny) / vh + half_y) * 2.0f - 1.0f, nin[n]);
+                    }
+                    const Quad quad = {(x & 1u) | ((y & 1u) << 1), {nin[0], nin[1]}};
+                    fragment(f, p, x, y, mapped, true, inputs, &quad);
+                    continue;
+                }
                 fragment(f, p, x, y, mapped, true, inputs);
             }
         }
@@ -1705,6 +1819,10 @@ int cpv_oracle_decode_attribute(uint32_t format, const uint8_t* bytes, float out
     out[3] = 1.0f;
     decode_attribute(bytes, comps, esize, kind, sgn, bgra, out);
     return comps;
+}
+
+void cpv_oracle_half_log2_n(const float* in, float* out, uint64_t n) {
+    for (uint64_t i = 0; i < n; i++) out[i] = half_log2(in[i]);
 }
 
 void cpv_oracle_edge_n(const float* in, float* out, uint64_t n) {

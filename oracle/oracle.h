@@ -95,6 +95,9 @@ void cpv_oracle_blit(const uint8_t* src, uint32_t src_w, uint32_t src_h, uint32_
  * provoking vertex in, covered, front, depth and 9 components out;
  * sample: 6 modes (mag, min, mipmap, address u, address v, border) and
  * u, v, λ in (no bias, no λ clamp), 4 floats out. */
+/* 0.5 * log2(r) as the quad-derivative LOD mode computes it (own series,
+ * the same binary32 steps as the GPU path). */
+void cpv_oracle_half_log2_n(const float* in, float* out, uint64_t n);
 void cpv_oracle_edge_n(const float* in, float* out, uint64_t n);
 void cpv_oracle_wrap_n(const int32_t* v, const int32_t* size, const uint32_t* mode, int32_t* out, uint64_t n);
 void cpv_oracle_blend_n(const float* src, const float* dst, const float* constant, const uint32_t* modes, float* out, uint64_t n);

@@ -86,6 +86,8 @@ DEPTH_ONLY = [
 def test_program_variants(gpu_ctx, oracle, program, variant, seed):
     scene = c.Scene(c.PROGRAM, seed, [program, variant, 64, 48, 24])
     report, stats = check(gpu_ctx, oracle, scene)
+    if (variant >> 28) & 3 != 3:  # depth bounds above the stored depth: nothing passes
+        assert stats["fragments_written"] > 0
     assert report["color_pixels_differing"] == 0, report
 
 
@@ -100,24 +102,28 @@ def test_cube_frames(gpu_ctx, oracle, frame):
 def test_heightfield_small(gpu_ctx, oracle):
     scene = c.Scene(c.HEIGHTFIELD, 1, [128, 480, 270])
     report, stats = check(gpu_ctx, oracle, scene)
+    assert stats["fragments_written"] > 0
     assert report["color_pixels_differing"] == 0, report
 
 
 def test_blend_small(gpu_ctx, oracle):
     scene = c.Scene(c.BLEND, 3, [2000, 640, 360])
     report, stats = check(gpu_ctx, oracle, scene)
+    assert stats["fragments_written"] > 0
     assert report["color_pixels_differing"] == 0, report
 
 
 def test_batch_small(gpu_ctx, oracle):
     scene = c.Scene(c.BATCH, 4, [48, 3000, 640, 360])
     report, stats = check(gpu_ctx, oracle, scene)
+    assert stats["fragments_written"] > 0
     assert report["color_pixels_differing"] == 0, report
 
 
 def test_serve_request(gpu_ctx, oracle):
     scene = c.Scene(c.SERVE, 5, [256, 5000, 3])
     report, stats = check(gpu_ctx, oracle, scene)
+    assert stats["fragments_written"] > 0
     assert report["color_pixels_differing"] == 0, report
 
 

@@ -279,3 +279,20 @@ def test_colour_attachments_compile_and_reject(native, monkeypatch, tmp_path):
         assert "an 8- or 16-byte colour format after the first attachment" in c.icd_last_error()
     finally:
         ctx.close()
+
+
+def test_spec_lod_module(compile_ctx, monkeypatch):
+    """CPV_SPEC_LOD=1 compiles a fragment shader's implicit-LOD sampling as
+    quad-derivative sites (cpv_sample_quad, CPV_LOD_SITES); without it the
+    module samples at the reference's λ 0 and has no site."""
+    ctx, dump = compile_ctx
+    scene = [c.PROGRAM_TEXLIT, 0x10, 32, 32, 4]
+    ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, scene))
+    (plain,) = glob.glob(str(dump / "pipeline_*.cu"))
+    monkeypatch.setenv("CPV_SPEC_LOD", "1")
+    ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, scene))
+    (spec,) = set(glob.glob(str(dump / "pipeline_*.cu"))) - {plain}
+    plain, spec = open(plain).read(), open(spec).read()
+    assert "#define CPV_LOD_SITES 0\n" in plain and "cpv_sample_quad(" not in plain
+    assert "#define CPV_LOD_SITES 1\n" in spec and "cpv_sample_quad(P.tex[0]" in spec and "cpv_lod, 0)" in spec
+
