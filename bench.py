@@ -307,7 +307,7 @@ def run_reference(args, world, rank, dist):
     print(json.dumps(line), flush=True)
 
 
-PLAIN_KERNELS = ("cpv_raster", "cpv_setup_rects", "cpv_span_count", "cpv_scan", "cpv_span_write", "cpv_blend_tables")
+PLAIN_KERNELS = ("cpv_raster", "cpv_setup_rects", "cpv_bins_zero", "cpv_span_count", "cpv_scan", "cpv_span_write", "cpv_blend_tables")
 BATCH_KERNELS = ("cpv_batch", "cpv_batch_vs", "cpv_batch_setup", "cpv_batch_bin", "cpv_batch_raster")
 
 # Workloads measured beside the headline frame in the default run:

@@ -5,23 +5,27 @@
  * Binning builds, for every screen tile, the list of primitive ids that
  * touch it, in API order — the per-pixel order the reference's serial loop
  * (CPVulkan/CommandBuffer.Draw.cpp:1526-1593) produces. Primitives are split
- * into S contiguous spans, one warp per span:
+ * into S contiguous spans, one warp per span, and the tiles are those of the
+ * union of the draw's tile rectangles (reduced by cpv_setup_rects into
+ * CpvDrawParams::tile_box), numbered row-major within it:
  *
  *   1. cpv_span_count: each warp counts, per tile, the primitives of its span
- *      that touch the tile → counts[tile * S + span].
- *   2. exclusive scan of counts in tile-major order → the write cursor of
- *      every (tile, span) pair; tile t's list is the contiguous range
+ *      that touch the tile → counts[tile * S + span] (counts start zero).
+ *   2. exclusive scan of counts in tile-major order (cpv_scan_dyn_reduce,
+ *      cpv_scan_dyn_apply, which zeroes the counts again) → the write cursor
+ *      of every (tile, span) pair; tile t's list is the contiguous range
  *      [cursor(t, 0), cursor(t + 1, 0)).
  *   3. cpv_span_write: each warp walks its span again in order and appends
  *      primitive ids at its cursors; within a warp, 32 (primitive, tile) pairs
  *      are placed per step with a match-any rank, so the order inside a span
  *      is the primitive order, and spans are laid out in span order.
  *
- * Everything is sized from host-known quantities (primitives, tiles, spans),
- * so a draw needs no host round trip and the whole sequence can be captured
- * in a CUDA graph. The list has a fixed capacity; a draw that would exceed
- * it records the overflow and the raster kernel falls back to scanning the
- * per-primitive rectangles (slower, same result).
+ * Grids are sized from host-known bounds (primitives, screen tiles, spans)
+ * and the union's size is read on the device, so a draw needs no host round
+ * trip and the whole sequence can be captured in a CUDA graph. The list has
+ * a fixed capacity; a draw that would exceed it records the overflow and
+ * the raster kernel falls back to scanning the per-primitive rectangles
+ * (slower, same result).
  */
 #ifndef CPV_BIN_CUH
 #define CPV_BIN_CUH
@@ -44,32 +48,44 @@ __device__ __forceinline__ void cpv_span_range(uint64_t total, uint32_t spans, u
     if (end > total) end = total;
 }
 
-/* counts[tile * spans + span] += primitives of the span touching the tile. */
+/* Zeroes the (union tiles x spans) count matrix (grid-stride over a fixed
+ * grid): for a matrix whose memory other buffers used since its last scan. */
+extern "C" __global__ void __launch_bounds__(256) cpv_bins_zero(uint32_t* __restrict__ counts, const uint32_t* __restrict__ box, uint32_t spans) {
+    const CpvTileBox b = cpv_tile_box(box);
+    const uint64_t n = static_cast<uint64_t>(b.w) * b.h * spans;
+    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) counts[i] = 0u;
+}
+
+/* counts[tile * spans + span] += primitives of the span touching the tile,
+ * tile numbered row-major within the union. */
 extern "C" __global__ void __launch_bounds__(256) cpv_span_count(const uint16_t* __restrict__ rects, uint64_t total, uint32_t spans,
-                                                                 uint32_t tiles_x, uint32_t* __restrict__ counts) {
+                                                                 const uint32_t* __restrict__ box, uint32_t* __restrict__ counts) {
     const uint32_t span = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31u;
     if (span >= spans) return;
+    const CpvTileBox b = cpv_tile_box(box);
     uint64_t begin, end;
     cpv_span_range(total, spans, span, begin, end);
     for (uint64_t g = begin + lane; g < end; g += 32u) {
         uint32_t x0, y0, x1, y1;
         cpv_rect_unpack(rects, g, x0, y0, x1, y1);
         for (uint32_t y = y0; y < y1; y++)
-            for (uint32_t x = x0; x < x1; x++) atomicAdd(&counts[(static_cast<uint64_t>(y) * tiles_x + x) * spans + span], 1u);
+            for (uint32_t x = x0; x < x1; x++) atomicAdd(&counts[(static_cast<uint64_t>(y - b.y0) * b.w + (x - b.x0)) * spans + span], 1u);
     }
 }
 
 /* Appends primitive ids in order. cursor = scanned counts (modified in place:
  * afterwards cursor[t * spans + s] is the end of (t, s)). */
 extern "C" __global__ void __launch_bounds__(256) cpv_span_write(const uint16_t* __restrict__ rects, uint64_t total, uint32_t spans,
-                                                                 uint32_t tiles_x, uint32_t* __restrict__ cursor,
+                                                                 const uint32_t* __restrict__ box, uint32_t* __restrict__ cursor,
                                                                  uint32_t* __restrict__ list, uint32_t capacity,
                                                                  const uint32_t* __restrict__ pair_total) {
     const uint32_t span = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31u;
     if (span >= spans) return;
     const bool overflow = *pair_total > capacity;
+    const CpvTileBox b = cpv_tile_box(box);
     uint64_t begin, end;
     cpv_span_range(total, spans, span, begin, end);
     const uint32_t lt_mask = (1u << lane) - 1u;
@@ -109,7 +125,7 @@ extern "C" __global__ void __launch_bounds__(256) cpv_span_write(const uint16_t*
             uint32_t tile = 0xFFFFFFFFu;
             if (valid) {
                 const uint32_t local = p - o_excl;
-                tile = (o_y0 + local / o_w) * tiles_x + (o_x0 + local % o_w);
+                tile = (o_y0 - b.y0 + local / o_w) * b.w + (o_x0 - b.x0 + local % o_w);
             }
             const uint32_t key = valid ? tile : (0x80000000u | lane);
             const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
@@ -198,6 +214,113 @@ extern "C" __global__ void __launch_bounds__(CPV_SCAN_THREADS) cpv_scan_add(uint
 /* total = last exclusive prefix + last input. */
 extern "C" __global__ void cpv_scan_total(const uint32_t* __restrict__ in, const uint32_t* __restrict__ out, uint64_t n, uint32_t* __restrict__ total) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *total = n ? out[n - 1] + in[n - 1] : 0u;
+}
+
+/* ---- exclusive scan of the (union tiles x spans) count matrix ----
+ * Its size n = union tiles x spans is known on the device only. Two
+ * launches over a fixed grid of G CTAs, CTA b owning the contiguous chunk
+ * [b * C, (b + 1) * C), C = ceil(n / G): (1) each CTA sums its chunk and the
+ * last CTA to finish scans the G sums (the counter at *done is reset for
+ * the next draw; no CTA waits on another), (2) each CTA scans its chunk
+ * from its scanned sum and zeroes the counts it read, so the matrix is
+ * zero again for the next draw. */
+
+__device__ __forceinline__ void cpv_dyn_chunk(uint32_t n, uint32_t& begin, uint32_t& end) {
+    const uint32_t per = (n + gridDim.x - 1u) / gridDim.x;
+    begin = per * blockIdx.x;
+    end = begin + per;
+    if (begin > n) begin = n;
+    if (end > n) end = n;
+}
+
+__device__ __forceinline__ uint32_t cpv_box_bins(const uint32_t* box, uint32_t spans) {
+    const CpvTileBox b = cpv_tile_box(box);
+    return b.w * b.h * spans;
+}
+
+/* 1: sums[b] = the total of CTA b's chunk; the last CTA replaces sums[0 ..
+ * G) by their exclusive scan and stores the pair total (G <= CPV_SCAN_BLOCK). */
+extern "C" __global__ void __launch_bounds__(CPV_SCAN_THREADS) cpv_scan_dyn_reduce(const uint32_t* __restrict__ in, const uint32_t* __restrict__ box,
+                                                                                  uint32_t spans, uint32_t* sums, uint32_t* done,
+                                                                                  uint32_t* __restrict__ total) {
+    uint32_t begin, end;
+    cpv_dyn_chunk(cpv_box_bins(box, spans), begin, end);
+    uint32_t s = 0;
+    /* CPV_SCAN_ITEMS independent loads in flight per thread and step */
+    for (uint32_t step = begin; step < end; step += CPV_SCAN_BLOCK) {
+#pragma unroll
+        for (int i = 0; i < CPV_SCAN_ITEMS; i++) {
+            const uint32_t k = step + static_cast<uint32_t>(i) * CPV_SCAN_THREADS + threadIdx.x;
+            s += k < end ? in[k] : 0u;
+        }
+    }
+    s = __reduce_add_sync(0xFFFFFFFFu, s);
+    __shared__ uint32_t warp_sums[CPV_SCAN_THREADS / 32];
+    __shared__ uint32_t last;
+    if ((threadIdx.x & 31u) == 0u) warp_sums[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0u) {
+        uint32_t t = 0;
+        for (int w = 0; w < CPV_SCAN_THREADS / 32; w++) t += warp_sums[w];
+        sums[blockIdx.x] = t;
+        __threadfence();
+        last = atomicAdd(done, 1u) == gridDim.x - 1u ? 1u : 0u;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const uint32_t count = gridDim.x;
+    const uint32_t base = threadIdx.x * CPV_SCAN_ITEMS;
+    uint32_t v[CPV_SCAN_ITEMS];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int i = 0; i < CPV_SCAN_ITEMS; i++) {
+        v[i] = base + i < count ? __ldcg(&sums[base + i]) : 0u;
+        sum += v[i];
+    }
+    uint32_t all;
+    uint32_t run = cpv_block_exclusive_scan(sum, all);
+#pragma unroll
+    for (int i = 0; i < CPV_SCAN_ITEMS; i++) {
+        if (base + i < count) sums[base + i] = run;
+        run += v[i];
+    }
+    if (threadIdx.x == 0u) {
+        *total = all;
+        *done = 0u;
+    }
+}
+
+/* 2: cursor = exclusive scan of counts, CTA b's chunk offset by sums[b]
+ * (CPV_SCAN_BLOCK elements per step, carried along the chunk); the counts
+ * read are zeroed. */
+extern "C" __global__ void __launch_bounds__(CPV_SCAN_THREADS) cpv_scan_dyn_apply(uint32_t* __restrict__ counts, uint32_t* __restrict__ cursor,
+                                                                                 const uint32_t* __restrict__ box, uint32_t spans,
+                                                                                 const uint32_t* __restrict__ sums) {
+    uint32_t begin, end;
+    cpv_dyn_chunk(cpv_box_bins(box, spans), begin, end);
+    uint32_t carry = sums[blockIdx.x];
+    for (uint32_t step = begin; step < end; step += CPV_SCAN_BLOCK) {
+        const uint32_t base = step + threadIdx.x * CPV_SCAN_ITEMS;
+        uint32_t v[CPV_SCAN_ITEMS];
+        uint32_t sum = 0;
+#pragma unroll
+        for (int i = 0; i < CPV_SCAN_ITEMS; i++) {
+            v[i] = base + i < end ? counts[base + i] : 0u;
+            sum += v[i];
+        }
+        uint32_t all;
+        uint32_t run = carry + cpv_block_exclusive_scan(sum, all);
+#pragma unroll
+        for (int i = 0; i < CPV_SCAN_ITEMS; i++) {
+            if (base + i < end) {
+                cursor[base + i] = run;
+                counts[base + i] = 0u;
+            }
+            run += v[i];
+        }
+        carry += all;
+    }
 }
 
 /* ---- batched binning: pairs, stable radix sort by tile, tile ranges ----

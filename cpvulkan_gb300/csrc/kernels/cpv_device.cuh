@@ -451,6 +451,46 @@ __device__ __forceinline__ cvec<float, 4> cpv_sample(const CpvTexture& t, float 
 }
 
 /* ------------------------------------------------------------------------- */
+/* Per-draw binning over the union of the draw's tile rectangles             */
+/* ------------------------------------------------------------------------- */
+
+/* The union of a draw's tile rectangles (CpvDrawParams::tile_box): its
+ * origin and extent in tiles; an empty union (no live primitive) has no
+ * tiles. */
+struct CpvTileBox {
+    uint32_t x0, y0, w, h;
+};
+__device__ __forceinline__ CpvTileBox cpv_tile_box(const uint32_t* box) {
+    CpvTileBox b;
+    b.x0 = 0xFFFFu - box[0];
+    b.y0 = 0xFFFFu - box[1];
+    const uint32_t x1 = box[2], y1 = box[3];
+    b.w = x1 > b.x0 ? x1 - b.x0 : 0u;
+    b.h = y1 > b.y0 ? y1 - b.y0 : 0u;
+    if (b.w == 0u || b.h == 0u) b.w = b.h = 0u;
+    return b;
+}
+
+/* Adds each thread's non-empty tile rectangle to the union: the CTA's
+ * maxima first (one atomic per word per CTA). Every thread of the CTA calls
+ * it. */
+__device__ __forceinline__ void cpv_tile_box_add(uint32_t* box, uint2 r) {
+    __shared__ uint32_t m[4];
+    if (threadIdx.x < 4u) m[threadIdx.x] = 0u;
+    __syncthreads();
+    const uint32_t x0 = r.x & 0xFFFFu, y0 = r.x >> 16, x1 = r.y & 0xFFFFu, y1 = r.y >> 16;
+    const bool any = x1 > x0 && y1 > y0;
+    const uint32_t v[4] = {any ? 0xFFFFu - x0 : 0u, any ? 0xFFFFu - y0 : 0u, any ? x1 : 0u, any ? y1 : 0u};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const uint32_t w = __reduce_max_sync(0xFFFFFFFFu, v[i]);
+        if ((threadIdx.x & 31u) == 0u && w) atomicMax(&m[i], w);
+    }
+    __syncthreads();
+    if (threadIdx.x < 4u && m[threadIdx.x]) atomicMax(&box[threadIdx.x], m[threadIdx.x]);
+}
+
+/* ------------------------------------------------------------------------- */
 /* Quad-derivative LOD: the labelled "spec LOD" mode (Vulkan 1.1, "Scale      */
 /* Factor Operation, Level-of-Detail Operation and Image Level(s) Selection")*/
 /* ------------------------------------------------------------------------- */

@@ -90,6 +90,10 @@ struct CpvDrawParams {
     const uint32_t* bin_list;   /* primitive ids, tile-major, primitive order within a tile */
     const uint32_t* pair_total; /* device word: pairs the draw needed */
     const uint16_t* rects;      /* per primitive tile rectangle (x0,y0,x1,y1), exclusive ends */
+    /* the union of the draw's tile rectangles, 4 device words kept as maxima
+     * of (0xFFFF - x0, 0xFFFF - y0, x1, y1) (zeroed before the draw): the
+     * (tiles x spans) matrix covers only its tiles, row-major */
+    uint32_t* tile_box;
     uint32_t spans;
     uint32_t list_capacity;
     uint32_t* status;

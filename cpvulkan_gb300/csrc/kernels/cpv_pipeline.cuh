@@ -27,10 +27,16 @@ extern "C" __global__ void __launch_bounds__(256) cpv_setup_rects(const __grid_c
     __syncthreads();
 #endif
     const uint64_t g = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (g >= P.total_prims) return;
-    CpvTri t;
-    cpv_p0::Stage::setup<false>(P, g, t);
-    reinterpret_cast<uint2*>(const_cast<uint16_t*>(P.rects))[g] = cpv_tile_rect(t, P.viewport[2], P.viewport[3]);
+    uint2 r = make_uint2(0u, 0u);
+    if (g < P.total_prims) {
+        CpvTri t;
+        cpv_p0::Stage::setup<false>(P, g, t);
+        r = cpv_tile_rect(t, P.viewport[2], P.viewport[3]);
+        reinterpret_cast<uint2*>(const_cast<uint16_t*>(P.rects))[g] = r;
+    }
+    /* the union of the draw's rectangles sizes its (tiles x spans) matrix
+     * (P.tile_box is the same for every CTA, so all or none call it) */
+    if (P.tile_box) cpv_tile_box_add(P.tile_box, r);
 }
 
 /* Blend tables (pipelines that blend a per-primitive constant colour): one
@@ -144,11 +150,15 @@ extern "C" __global__ void CPV_PLAIN_BOUNDS cpv_raster(const __grid_constant__ C
     uint64_t begin = 0, end = P.total_prims;
     bool scan_rects = false;
     if (!direct) {
+        /* tiles outside the union of the draw's rectangles have no primitive */
+        const CpvTileBox b = cpv_tile_box(P.tile_box);
+        if (tx - b.x0 >= b.w || ty - b.y0 >= b.h) return;
         if (*P.pair_total > P.list_capacity) {
             scan_rects = true;
         } else {
-            end = P.tile_end[static_cast<uint64_t>(tile) * P.spans + P.spans - 1u];
-            begin = tile == 0u ? 0u : P.tile_end[static_cast<uint64_t>(tile) * P.spans - 1u];
+            const uint64_t local = static_cast<uint64_t>(ty - b.y0) * b.w + (tx - b.x0);
+            end = P.tile_end[local * P.spans + P.spans - 1u];
+            begin = local == 0u ? 0u : P.tile_end[local * P.spans - 1u];
         }
     }
     if (begin >= end) return;

@@ -324,11 +324,11 @@ int Scratch::reserve_scan(uint64_t n) {
 
 int Scratch::ensure_words() {
     if (words_) return kOk;
-    if (cudaMalloc(reinterpret_cast<void**>(&words_), 64) != cudaSuccess) {
+    if (cudaMalloc(reinterpret_cast<void**>(&words_), kWordsBytes) != cudaSuccess) {
         cudaGetLastError();
         return kErrOutOfMemory;
     }
-    cudaMemset(words_, 0, 64);
+    cudaMemset(words_, 0, kWordsBytes);
     generation_++;
     return kOk;
 }
@@ -453,6 +453,58 @@ int blit(cudaStream_t stream, const CpvTexture& src, uint8_t* dst, uint32_t dst_
     return kOk;
 }
 
+static_assert(kWordsBytes >= 4ull * (kSumsWord + CPV_SCAN_BLOCK), "binning words hold a sum per scan element of a CTA");
+
+namespace {
+
+// CTAs of the per-draw binning kernels whose work is sized on the device,
+// for a count matrix of at most `bins` entries: one per CPV_SCAN_BLOCK
+// entries, at most one scanned CTA sum per scan element of a CTA (2048:
+// about 13 per SM, enough loads in flight for an image-sized matrix). Small
+// draws keep small grids, so draws of other queues run beside them.
+uint32_t bin_ctas(uint64_t bins) {
+    const uint64_t want = (bins + CPV_SCAN_BLOCK - 1) / CPV_SCAN_BLOCK;
+    return static_cast<uint32_t>(std::max<uint64_t>(1u, std::min<uint64_t>(CPV_SCAN_BLOCK, want)));
+}
+
+// The per-draw binning after cpv_setup_rects has written the rectangles and
+// their union (tile_box): count into the (union tiles x spans) matrix, scan
+// it (reduce-then-scan over bin_ctas() CTAs; its size is read on the device;
+// the scan leaves the counts zero again), write the lists. zero_first: the
+// counts' memory is not known to be zero (the fixed scratch moves it with
+// the draw's size). words: [0] pair total, [9] the reduce's CTA counter,
+// [kSumsWord ..] the CTA sums.
+void bin_draw(cudaStream_t stream, const uint16_t* rects, uint64_t G, uint64_t spans, uint64_t bins, const uint32_t* tile_box, uint32_t* counts,
+              uint32_t* cursor, uint32_t* list, uint32_t capacity, uint32_t* words, bool zero_first) {
+    const uint32_t ctas = bin_ctas(bins);
+    uint32_t* sums = words + kSumsWord;
+    const uint32_t sp = static_cast<uint32_t>(spans);
+    if (zero_first) {
+        const unsigned zero_grid = static_cast<unsigned>(std::min<uint64_t>(ctas, (bins + 255) / 256));
+        profile_begin(stream, "cpv_bins_zero");
+        cpv_bins_zero<<<zero_grid, 256, 0, stream>>>(counts, tile_box, sp);
+        profile_end(stream);
+        count_launch();
+    }
+    const unsigned warp_blocks = static_cast<unsigned>((spans * 32 + 255) / 256);
+    profile_begin(stream, "cpv_span_count");
+    cpv_span_count<<<warp_blocks, 256, 0, stream>>>(rects, G, sp, tile_box, counts);
+    profile_end(stream);
+    count_launch();
+    profile_begin(stream, "cpv_scan");
+    cpv_scan_dyn_reduce<<<ctas, CPV_SCAN_THREADS, 0, stream>>>(counts, tile_box, sp, sums, words + 9, words);
+    cpv_scan_dyn_apply<<<ctas, CPV_SCAN_THREADS, 0, stream>>>(counts, cursor, tile_box, sp, sums);
+    profile_end(stream);
+    count_launch();
+    count_launch();
+    profile_begin(stream, "cpv_span_write");
+    cpv_span_write<<<warp_blocks, 256, 0, stream>>>(rects, G, sp, tile_box, cursor, list, capacity, words);
+    profile_end(stream);
+    count_launch();
+}
+
+}  // namespace
+
 int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& sc) {
     if (P.total_prims == 0 || P.fb_width == 0 || P.fb_height == 0) return kOk;
     const uint32_t shift = m.tile_shift;
@@ -475,10 +527,17 @@ int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& s
         uint64_t spans = (G + span_prims - 1) / span_prims;
         if (spans > 4096) spans = 4096;
         if (spans < 1) spans = 1;
+        // the binning kernels index the (tiles x spans) matrix in 32 bits
+        while (spans > 1 && tiles * spans > 0x7FFFFFFFull) spans = (spans + 1) / 2;
+        if (tiles * spans > 0x7FFFFFFFull) return kErrInvalid;
         const uint64_t bins = tiles * spans;
         const uint32_t cap = env_u32("CPV_LIST_CAPACITY", 1u << 26);
         if ((r = sc.reserve_rects(G)) != kOk) return r;
+        const uint32_t* counts_before = sc.counts();
         if ((r = sc.reserve_bins(bins)) != kOk) return r;
+        // the count matrix is all zero between draws (each scan zeroes what
+        // it read); a new allocation starts it so
+        if (sc.counts() != counts_before) CPV_CUDA(cudaMemsetAsync(sc.counts(), 0, sc.counts_capacity() * sizeof(uint32_t), stream));
         if ((r = sc.reserve_list(cap)) != kOk) return r;
         P.rects = sc.rects();
         P.spans = static_cast<uint32_t>(spans);
@@ -486,7 +545,8 @@ int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& s
         P.pair_total = sc.words();
         P.tile_end = sc.cursor();
         P.bin_list = sc.list();
-        CPV_CUDA(cudaMemsetAsync(sc.counts(), 0, bins * sizeof(uint32_t), stream));
+        P.tile_box = sc.words() + 4;
+        CPV_CUDA(cudaMemsetAsync(P.tile_box, 0, 4 * sizeof(uint32_t), stream));
         {
             void* args[] = {&P};
             profile_begin(stream, "cpv_setup_rects");
@@ -494,19 +554,8 @@ int draw_plain(cudaStream_t stream, const Module& m, CpvDrawParams P, Scratch& s
             profile_end(stream);
             count_launch();
         }
-        const unsigned warp_blocks = static_cast<unsigned>((spans * 32 + 255) / 256);
-        profile_begin(stream, "cpv_span_count");
-        cpv_span_count<<<warp_blocks, 256, 0, stream>>>(sc.rects(), G, static_cast<uint32_t>(spans), P.tiles_x, sc.counts());
-        profile_end(stream);
-        count_launch();
-        profile_begin(stream, "cpv_scan");
-        if ((r = scan_u32(stream, sc.counts(), sc.cursor(), bins, sc.words(), sc)) != kOk) return r;
-        profile_end(stream);
-        profile_begin(stream, "cpv_span_write");
-        cpv_span_write<<<warp_blocks, 256, 0, stream>>>(sc.rects(), G, static_cast<uint32_t>(spans), P.tiles_x, sc.cursor(), sc.list(),
-                                                        sc.list_capacity(), sc.words());
-        profile_end(stream);
-        count_launch();
+        bin_draw(stream, sc.rects(), G, spans, bins, P.tile_box, sc.counts(), sc.cursor(), sc.list(), sc.list_capacity(), sc.words(), false);
+        CPV_CUDA(cudaGetLastError());
     }
     // Blend tables: 1 KiB per primitive, built once per draw, when the
     // pipeline blends a per-primitive constant colour (up to 4 GiB of them;
@@ -1016,7 +1065,7 @@ uint8_t* g_static_addr[kMaxStaticDevices] = {};
 uint64_t align256(uint64_t b) { return (b + 255u) & ~255ull; }
 
 struct StaticCarve {
-    uint64_t words = 0, rects = 0, counts = 0, cursor = 0, scan[8] = {}, list = 0, end = 0;
+    uint64_t words = 0, rects = 0, counts = 0, cursor = 0, list = 0, end = 0;
 };
 
 // Offsets of the binning buffers for `prims` primitives over `bins` tile·span
@@ -1025,20 +1074,13 @@ StaticCarve static_carve(uint64_t prims, uint64_t bins) {
     StaticCarve c;
     uint64_t o = 0;
     c.words = o;
-    o += 256;
+    o += kWordsBytes;
     c.rects = o;
     o += align256(prims * 8);
     c.counts = o;
     o += align256(bins * 4);
     c.cursor = o;
     o += align256(bins * 4);
-    uint64_t n = bins;
-    int level = 0;
-    while (n > CPV_SCAN_BLOCK && level < 8) {
-        n = (n + CPV_SCAN_BLOCK - 1) / CPV_SCAN_BLOCK;
-        c.scan[level++] = o;
-        o += align256(2 * n * 4);
-    }
     c.list = o;
     c.end = o;
     return c;
@@ -1063,28 +1105,6 @@ uint64_t static_spans(uint64_t prims, uint64_t tiles) {
     return spans;
 }
 
-int scan_level_static(cudaStream_t stream, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total, uint32_t* const* levels, int level) {
-    const uint64_t blocks = (n + CPV_SCAN_BLOCK - 1) / CPV_SCAN_BLOCK;
-    if (blocks <= 1) {
-        cpv_scan_blocks<<<1, CPV_SCAN_THREADS, 0, stream>>>(in, out, n, nullptr);
-        count_launch();
-    } else {
-        if (level >= 8 || !levels[level]) return kErrInvalid;
-        uint32_t* sums = levels[level];
-        uint32_t* sums_scanned = sums + blocks;
-        cpv_scan_blocks<<<static_cast<unsigned>(blocks), CPV_SCAN_THREADS, 0, stream>>>(in, out, n, sums);
-        count_launch();
-        const int r = scan_level_static(stream, sums, sums_scanned, blocks, nullptr, levels, level + 1);
-        if (r != kOk) return r;
-        cpv_scan_add<<<static_cast<unsigned>(blocks), CPV_SCAN_THREADS, 0, stream>>>(out, n, sums_scanned);
-        count_launch();
-    }
-    if (total) {
-        cpv_scan_total<<<1, 32, 0, stream>>>(in, out, n, total);
-        count_launch();
-    }
-    return kOk;
-}
 
 }  // namespace
 
@@ -1162,29 +1182,20 @@ int draw_plain_static(cudaStream_t stream, const Module& m, CpvDrawParams P) {
         uint32_t* counts = reinterpret_cast<uint32_t*>(base + c.counts);
         uint32_t* cursor = reinterpret_cast<uint32_t*>(base + c.cursor);
         uint32_t* list = reinterpret_cast<uint32_t*>(base + c.list);
-        uint32_t* levels[8] = {};
-        for (int l = 0; l < 8; l++) levels[l] = c.scan[l] ? reinterpret_cast<uint32_t*>(base + c.scan[l]) : nullptr;
         P.rects = rects;
         P.spans = static_cast<uint32_t>(spans);
         P.list_capacity = static_cast<uint32_t>(cap);
         P.pair_total = words;
         P.tile_end = cursor;
         P.bin_list = list;
-        CPV_CUDA(cudaMemsetAsync(counts, 0, bins * sizeof(uint32_t), stream));
+        P.tile_box = words + 4;
+        CPV_CUDA(cudaMemsetAsync(P.tile_box, 0, 4 * sizeof(uint32_t), stream));
         {
             void* args[] = {&P};
             CPV_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(m.setup_rects), dim3(static_cast<unsigned>((G + 255) / 256)), dim3(256), args, 0, stream));
             count_launch();
         }
-        const unsigned warp_blocks = static_cast<unsigned>((spans * 32 + 255) / 256);
-        cpv_span_count<<<warp_blocks, 256, 0, stream>>>(rects, G, static_cast<uint32_t>(spans), P.tiles_x, counts);
-        count_launch();
-        if ((r = scan_level_static(stream, counts, cursor, bins, words, levels, 0)) != kOk) {
-            set_last_error("static scratch scan levels exhausted");
-            return r;
-        }
-        cpv_span_write<<<warp_blocks, 256, 0, stream>>>(rects, G, static_cast<uint32_t>(spans), P.tiles_x, cursor, list, P.list_capacity, words);
-        count_launch();
+        bin_draw(stream, rects, G, spans, bins, P.tile_box, counts, cursor, list, P.list_capacity, words, true);
     }
     {
         void* args[] = {&P, &direct};

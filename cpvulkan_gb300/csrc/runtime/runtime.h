@@ -58,6 +58,12 @@ int compile(const std::string& source, const std::string& name, std::vector<uint
 int load(const std::vector<uint8_t>& cubin, uint32_t tile_shift, bool batched, Module& out, std::string& error);
 void unload(Module& m);
 
+// Device words of a queue's per-draw binning: [0] pair total, [1] status,
+// [4..7] the union of the draw's tile rectangles, [9] the scan's CTA
+// counter, [kSumsWord ..] one scanned sum per binning CTA (at most 2048).
+constexpr uint32_t kSumsWord = 16;
+constexpr uint64_t kWordsBytes = 4ull * (kSumsWord + 2048u);
+
 // Grow-only device scratch owned by one queue. Draws on that queue's stream
 // reuse it in stream order.
 class Scratch {
@@ -71,10 +77,11 @@ public:
     uint8_t* tables() const { return tables_; }
     uint16_t* rects() const { return rects_; }
     uint32_t* counts() const { return counts_; }
+    uint64_t counts_capacity() const { return counts_cap_; }
     uint32_t* cursor() const { return cursor_; }
     uint32_t* list() const { return list_; }
     uint32_t list_capacity() const { return static_cast<uint32_t>(list_cap_); }
-    uint32_t* words() const { return words_; }  // [0] pair total, [1] status
+    uint32_t* words() const { return words_; }  // kWordsBytes: see kSumsWord
     uint32_t* scan_level(int level) const { return scan_[level]; }
     int ensure_words();
     // Incremented whenever a buffer is (re)allocated: work captured in a CUDA
