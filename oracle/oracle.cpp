@@ -1821,6 +1821,18 @@ int cpv_oracle_decode_attribute(uint32_t format, const uint8_t* bytes, float out
     return comps;
 }
 
+void cpv_oracle_quad_lambda_n(const float* in, const uint32_t* odd, uint32_t width, uint32_t height, float* out, uint64_t n) {
+    Texture t;
+    t.levels = 1;
+    t.level_w[0] = width;
+    t.level_h[0] = height;
+    for (uint64_t i = 0; i < n; i++) {
+        const float* p = in + 6 * i;
+        const float un[2] = {p[2], p[4]}, vn[2] = {p[3], p[5]};
+        out[i] = quad_lambda(t, p[0], p[1], un, vn, odd[i]);
+    }
+}
+
 void cpv_oracle_half_log2_n(const float* in, float* out, uint64_t n) {
     for (uint64_t i = 0; i < n; i++) out[i] = half_log2(in[i]);
 }

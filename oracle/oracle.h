@@ -98,6 +98,10 @@ void cpv_oracle_blit(const uint8_t* src, uint32_t src_w, uint32_t src_h, uint32_
 /* 0.5 * log2(r) as the quad-derivative LOD mode computes it (own series,
  * the same binary32 steps as the GPU path). */
 void cpv_oracle_half_log2_n(const float* in, float* out, uint64_t n);
+/* λ_base of the quad-derivative LOD mode for n fragments: in[6 i ..] =
+ * (u, v, u and v at the horizontal neighbour, u and v at the vertical one),
+ * odd[i] bit 0 / bit 1 = x / y odd, on a width x height level 0. */
+void cpv_oracle_quad_lambda_n(const float* in, const uint32_t* odd, uint32_t width, uint32_t height, float* out, uint64_t n);
 void cpv_oracle_edge_n(const float* in, float* out, uint64_t n);
 void cpv_oracle_wrap_n(const int32_t* v, const int32_t* size, const uint32_t* mode, int32_t* out, uint64_t n);
 void cpv_oracle_blend_n(const float* src, const float* dst, const float* constant, const uint32_t* modes, float* out, uint64_t n);

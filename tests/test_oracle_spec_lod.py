@@ -39,6 +39,36 @@ def test_half_log2_series(oracle):
     assert list(special[:4]) == [-np.inf] * 4 and special[4] == np.inf
 
 
+def test_quad_lambda_follows_the_scale_factor_definition(oracle):
+    # Vulkan 1.1, "Scale Factor Operation": rho_x = |(du/dx * w, dv/dx * h)|,
+    # rho_y likewise, lambda_base = log2(max(rho_x, rho_y)); fine
+    # derivatives: P(x | 1) - P(x & ~1). numpy in binary64 against the oracle.
+    rng = np.random.default_rng(9)
+    n = 100000
+    u = rng.uniform(-2, 2, n).astype(np.float32)
+    v = rng.uniform(-2, 2, n).astype(np.float32)
+    scale = np.exp2(rng.uniform(-14, 2, (n, 4))).astype(np.float32) * rng.choice([-1, 1], (n, 4)).astype(np.float32)
+    ux, vx, uy, vy = u + scale[:, 0], v + scale[:, 1], u + scale[:, 2], v + scale[:, 3]
+    odd = rng.integers(0, 4, n).astype(np.uint32)
+    w, h = 1024, 512
+    packed = np.ascontiguousarray(np.stack([u, v, ux, vx, uy, vy], axis=1), np.float32)
+    out = np.empty(n, np.float32)
+    fn = oracle.lib.cpv_oracle_quad_lambda_n
+    fn.restype = None
+    fn(packed.ctypes.data_as(ctypes.c_void_p), odd.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint32(w), ctypes.c_uint32(h),
+       out.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint64(n))
+    sx = np.where(odd & 1, 1.0, -1.0)  # x odd: the neighbour is x - 1
+    sy = np.where(odd & 2, 1.0, -1.0)
+    f64 = np.float64
+    dudx, dvdx = sx * (u.astype(f64) - ux), sx * (v.astype(f64) - vx)
+    dudy, dvdy = sy * (u.astype(f64) - uy), sy * (v.astype(f64) - vy)
+    rho_x = np.hypot(dudx * w, dvdx * h)
+    rho_y = np.hypot(dudy * w, dvdy * h)
+    want = np.log2(np.maximum(rho_x, rho_y))
+    # binary32 differences and squares: a few ulps of rho, i.e. ~1e-6 in log2
+    assert np.max(np.abs(out.astype(f64) - want)) < 2e-5
+
+
 def _scene(variant=0x10, seed=1, lod_range=None):
     s = c.Scene(c.PROGRAM, seed, [c.PROGRAM_TEXLIT, variant, 64, 48, 24])
     if lod_range is not None:
