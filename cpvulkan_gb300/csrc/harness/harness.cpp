@@ -654,14 +654,32 @@ VkResult create_scene_pass(cpvh_context* c, const cpv_scene* s, VkRenderPass* ou
     return c->f.vkCreateRenderPass(c->device, &rpi, nullptr, out);
 }
 
+// A scene's descriptor set layout: binding 0 its uniform buffer; its
+// texture at binding 1 as a combined image sampler, a storage image, or a
+// sampled image with its sampler at binding 2 (cpv_scene::texture_binding).
+std::vector<VkDescriptorSetLayoutBinding> scene_bindings(const cpv_scene* s) {
+    std::vector<VkDescriptorSetLayoutBinding> lb;
+    if (s->uniform_bytes) lb.push_back({0, VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER, 1, VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
+    if (s->texture_data) {
+        switch (s->texture_binding) {
+        case CPV_TEXTURE_STORAGE: lb.push_back({1, VK_DESCRIPTOR_TYPE_STORAGE_IMAGE, 1, VK_SHADER_STAGE_FRAGMENT_BIT, nullptr}); break;
+        case CPV_TEXTURE_SEPARATE:
+            lb.push_back({1, VK_DESCRIPTOR_TYPE_SAMPLED_IMAGE, 1, VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
+            lb.push_back({2, VK_DESCRIPTOR_TYPE_SAMPLER, 1, VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
+            break;
+        default: lb.push_back({1, VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER, 1, VK_SHADER_STAGE_FRAGMENT_BIT, nullptr}); break;
+        }
+    }
+    return lb;
+}
+
 VkResult make_pass_and_layout(cpvh_context* c, const cpv_scene* s, bool with_sets, VkRenderPass& pass, VkDescriptorSetLayout& set_layout,
                               VkPipelineLayout& layout, bool two_subpasses = false) {
     const Fns& f = c->f;
     VkResult res = create_scene_pass(c, s, &pass, two_subpasses);
     if (res != VK_SUCCESS) return res;
     std::vector<VkDescriptorSetLayoutBinding> lb;
-    if (with_sets && s->uniform_bytes) lb.push_back({0, VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER, 1, VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
-    if (with_sets && s->texture_data) lb.push_back({1, VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER, 1, VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
+    if (with_sets) lb = scene_bindings(s);
     VkDescriptorSetLayoutCreateInfo dli{};
     dli.sType = VK_STRUCTURE_TYPE_DESCRIPTOR_SET_LAYOUT_CREATE_INFO;
     dli.bindingCount = static_cast<uint32_t>(lb.size());
@@ -872,8 +890,9 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
                        VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT | VK_IMAGE_USAGE_TRANSFER_SRC_BIT, VK_IMAGE_ASPECT_COLOR_BIT, r->extra[k]) != VK_SUCCESS)
             return fail("colour image " + std::to_string(k + 1));
     if (s->texture_data) {
+        const VkImageUsageFlags tex_usage = s->texture_binding == CPV_TEXTURE_STORAGE ? VK_IMAGE_USAGE_STORAGE_BIT : VK_IMAGE_USAGE_SAMPLED_BIT;
         if (make_image(c, static_cast<VkFormat>(s->texture_format), s->texture_width, s->texture_height, s->texture_levels,
-                       VK_IMAGE_USAGE_SAMPLED_BIT | VK_IMAGE_USAGE_TRANSFER_DST_BIT, VK_IMAGE_ASPECT_COLOR_BIT, r->texture) != VK_SUCCESS)
+                       tex_usage | VK_IMAGE_USAGE_TRANSFER_DST_BIT, VK_IMAGE_ASPECT_COLOR_BIT, r->texture) != VK_SUCCESS)
             return fail("texture image");
         VkSamplerCreateInfo sci{};
         sci.sType = VK_STRUCTURE_TYPE_SAMPLER_CREATE_INFO;
@@ -914,20 +933,20 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
     fbi.height = s->height;
     fbi.layers = 1;
     if (f.vkCreateFramebuffer(c->device, &fbi, nullptr, &r->fb) != VK_SUCCESS) return fail("framebuffer");
-    // Descriptors: binding 0 uniform buffer, binding 1 combined image sampler.
-    std::vector<VkDescriptorSetLayoutBinding> lb;
-    if (s->uniform_bytes) lb.push_back({0, VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER, 1, VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
-    if (s->texture_data) lb.push_back({1, VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER, 1, VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
+    // Descriptors: binding 0 uniform buffer, the texture at binding 1 (and
+    // its sampler at binding 2 when they are separate).
+    const std::vector<VkDescriptorSetLayoutBinding> lb = scene_bindings(s);
     VkDescriptorSetLayoutCreateInfo dli{};
     dli.sType = VK_STRUCTURE_TYPE_DESCRIPTOR_SET_LAYOUT_CREATE_INFO;
     dli.bindingCount = static_cast<uint32_t>(lb.size());
     dli.pBindings = lb.data();
     if (f.vkCreateDescriptorSetLayout(c->device, &dli, nullptr, &r->set_layout) != VK_SUCCESS) return fail("set layout");
-    VkDescriptorPoolSize ps[2] = {{VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER, 1}, {VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER, 1}};
+    VkDescriptorPoolSize ps[5] = {{VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER, 1}, {VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER, 1}, {VK_DESCRIPTOR_TYPE_STORAGE_IMAGE, 1},
+                                  {VK_DESCRIPTOR_TYPE_SAMPLED_IMAGE, 1}, {VK_DESCRIPTOR_TYPE_SAMPLER, 1}};
     VkDescriptorPoolCreateInfo dpi{};
     dpi.sType = VK_STRUCTURE_TYPE_DESCRIPTOR_POOL_CREATE_INFO;
     dpi.maxSets = 1;
-    dpi.poolSizeCount = 2;
+    dpi.poolSizeCount = 5;
     dpi.pPoolSizes = ps;
     if (f.vkCreateDescriptorPool(c->device, &dpi, nullptr, &r->pool) != VK_SUCCESS) return fail("descriptor pool");
     if (!lb.empty()) {
@@ -939,7 +958,10 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
         if (f.vkAllocateDescriptorSets(c->device, &dai, &r->set) != VK_SUCCESS) return fail("descriptor set");
         VkDescriptorBufferInfo dbi{r->uniform.buffer, 0, VK_WHOLE_SIZE};
         VkDescriptorImageInfo dii{r->sampler, r->texture.view, VK_IMAGE_LAYOUT_SHADER_READ_ONLY_OPTIMAL};
-        VkWriteDescriptorSet w[2]{};
+        if (s->texture_binding == CPV_TEXTURE_STORAGE) dii = {VK_NULL_HANDLE, r->texture.view, VK_IMAGE_LAYOUT_GENERAL};
+        if (s->texture_binding == CPV_TEXTURE_SEPARATE) dii.sampler = VK_NULL_HANDLE;
+        const VkDescriptorImageInfo sampler_info{r->sampler, VK_NULL_HANDLE, VK_IMAGE_LAYOUT_UNDEFINED};
+        VkWriteDescriptorSet w[3]{};
         uint32_t nw = 0;
         if (s->uniform_bytes) {
             w[nw].sType = VK_STRUCTURE_TYPE_WRITE_DESCRIPTOR_SET;
@@ -955,9 +977,20 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
             w[nw].dstSet = r->set;
             w[nw].dstBinding = 1;
             w[nw].descriptorCount = 1;
-            w[nw].descriptorType = VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER;
+            w[nw].descriptorType = s->texture_binding == CPV_TEXTURE_STORAGE    ? VK_DESCRIPTOR_TYPE_STORAGE_IMAGE
+                                   : s->texture_binding == CPV_TEXTURE_SEPARATE ? VK_DESCRIPTOR_TYPE_SAMPLED_IMAGE
+                                                                                : VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER;
             w[nw].pImageInfo = &dii;
             nw++;
+            if (s->texture_binding == CPV_TEXTURE_SEPARATE) {
+                w[nw].sType = VK_STRUCTURE_TYPE_WRITE_DESCRIPTOR_SET;
+                w[nw].dstSet = r->set;
+                w[nw].dstBinding = 2;
+                w[nw].descriptorCount = 1;
+                w[nw].descriptorType = VK_DESCRIPTOR_TYPE_SAMPLER;
+                w[nw].pImageInfo = &sampler_info;
+                nw++;
+            }
         }
         f.vkUpdateDescriptorSets(c->device, nw, w, 0, nullptr);
     }

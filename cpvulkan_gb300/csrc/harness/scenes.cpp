@@ -679,7 +679,9 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
     if (attachment_format) { s.clear_color[0] = -0.3f; s.clear_color[1] = 0.6f; s.clear_color[2] = 1.7f; s.clear_color[3] = 0.45f; }
     // The textured and mesh programs view their geometry from afar (NDC
     // depth near 1): their depth is cleared to 1 so a LESS test passes.
-    const bool far_geometry = program == CPV_PROGRAM_TEXLIT || program == CPV_PROGRAM_FETCH || program == CPV_PROGRAM_MESHPC;
+    const bool textured = program == CPV_PROGRAM_TEXLIT || program == CPV_PROGRAM_FETCH || program == CPV_PROGRAM_STORAGE ||
+                          program == CPV_PROGRAM_SEPARATE;
+    const bool far_geometry = textured || program == CPV_PROGRAM_MESHPC;
     s.clear_depth = far_geometry ? 1.0f : 0.75f;
     s.clear_stencil = 3;
     viewport_full(s);
@@ -806,7 +808,7 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
         p.num_attributes = 2;
         p.attributes[0] = {0, 0, VK_FORMAT_R32G32_SFLOAT, 0};
         p.attributes[1] = {1, 0, VK_FORMAT_R32G32B32A32_SFLOAT, 8};
-    } else if (program == CPV_PROGRAM_TEXLIT || program == CPV_PROGRAM_FETCH) {
+    } else if (textured) {
         const Mat4 proj = perspective(60.0 * M_PI / 180.0, static_cast<double>(width) / height, 0.1, 10.0);
         const Mat4 view = look_at({0, 1.2, -1.8}, {0, 0, 0.1}, {0, -1, 0});
         st.uniform.resize(80);
@@ -851,6 +853,8 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
         t.stencil_back = p.stencil_back;
         t.program = program;
         if (program == CPV_PROGRAM_FETCH) t.spec_k = colour_format;  // parameter 5: the specialisation constant (0: none)
+        if (program == CPV_PROGRAM_STORAGE) s.texture_binding = CPV_TEXTURE_STORAGE;
+        if (program == CPV_PROGRAM_SEPARATE) s.texture_binding = CPV_TEXTURE_SEPARATE;
         p = t;
     } else if (program == CPV_PROGRAM_MESHPC) {
         const double phase[3] = {1.0, 2.0, 3.0};

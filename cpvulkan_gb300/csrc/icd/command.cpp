@@ -297,7 +297,17 @@ VkResult build_draw(State& s, uint32_t count, uint32_t instances, uint32_t first
         if (it == s.sets[slot.set]->bindings.end() || it->second.empty()) continue;
         const Descriptor& d = it->second[0];
         if (slot.is_texture) {
-            fill_texture(P.tex[slot.slot], d.view, d.sampler);
+            // a texture joined by OpSampledImage takes its sampler from the
+            // sampler's own binding; a storage image has none
+            const Sampler* sampler = d.sampler;
+            if (slot.separate) {
+                sampler = nullptr;
+                if (slot.sampler_set < 8 && s.sets[slot.sampler_set]) {
+                    auto st = s.sets[slot.sampler_set]->bindings.find(slot.sampler_binding);
+                    if (st != s.sets[slot.sampler_set]->bindings.end() && !st->second.empty()) sampler = st->second[0].sampler;
+                }
+            }
+            fill_texture(P.tex[slot.slot], d.view, sampler);
         } else if (d.buffer && d.buffer->memory) {
             const uint64_t dyn = (d.type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC) ? dynamic_offset(s, slot.set, slot.binding) : 0;
             const uint64_t off = d.offset + dyn;

@@ -871,6 +871,13 @@ VKAPI_ATTR void VKAPI_CALL UpdateDescriptorSets(VkDevice, uint32_t nw, const VkW
                 d.view = reinterpret_cast<ImageView*>(w[i].pImageInfo[k].imageView);
                 if (w[i].pImageInfo[k].sampler) d.sampler = reinterpret_cast<Sampler*>(w[i].pImageInfo[k].sampler);
                 break;
+            case VK_DESCRIPTOR_TYPE_SAMPLED_IMAGE:
+            case VK_DESCRIPTOR_TYPE_STORAGE_IMAGE:
+                d.view = reinterpret_cast<ImageView*>(w[i].pImageInfo[k].imageView);
+                break;
+            case VK_DESCRIPTOR_TYPE_SAMPLER:
+                if (w[i].pImageInfo[k].sampler) d.sampler = reinterpret_cast<Sampler*>(w[i].pImageInfo[k].sampler);
+                break;
             default:
                 break;
             }

@@ -53,7 +53,7 @@ enum Op : uint16_t {
     OpShiftRightArithmetic = 195, OpShiftLeftLogical = 196, OpBitwiseOr = 197, OpBitwiseXor = 198,
     OpBitwiseAnd = 199, OpNot = 200, OpPhi = 245, OpLoopMerge = 246, OpSelectionMerge = 247, OpLabel = 248,
     OpBranch = 249, OpBranchConditional = 250, OpSwitch = 251, OpKill = 252, OpReturn = 253, OpReturnValue = 254,
-    OpUnreachable = 255, OpCopyMemory = 63, OpImageFetch = 95, OpImage = 100, OpBitCount = 205, OpSpecConstantOp = 52,
+    OpUnreachable = 255, OpCopyMemory = 63, OpImageFetch = 95, OpImage = 100, OpImageRead = 98, OpImageWrite = 99, OpBitCount = 205, OpSpecConstantOp = 52,
 };
 
 enum Dec : uint32_t {
@@ -223,7 +223,17 @@ bool parse(const uint32_t* words, size_t n, Module& m, std::string& error) {
             t.count = w[2];
             break;
         }
-        case OpTypeImage: if (!need(1)) return false; m.types[w[0]].kind = TypeKind::Image; break;
+        case OpTypeImage: {
+            if (!need(1)) return false;
+            Type& t = m.types[w[0]];
+            t.kind = TypeKind::Image;
+            if (w.size() >= 8) {
+                t.dim = w[2];
+                t.sampled = w[6];
+                t.image_format = w[7];
+            }
+            break;
+        }
         case OpTypeSampler: if (!need(1)) return false; m.types[w[0]].kind = TypeKind::Sampler; break;
         case OpTypeSampledImage: {
             if (!need(2)) return false;
@@ -388,12 +398,16 @@ bool parse(const uint32_t* words, size_t n, Module& m, std::string& error) {
 namespace {
 
 struct PtrInfo {
-    enum Kind { None, Lvalue, Explicit, Handle } kind = None;
+    // Handle: a combined image sampler (its texture slot); ImageVar /
+    // SamplerVar: a separate image or sampler binding, given a slot when an
+    // instruction uses it (OpSampledImage, OpImageRead, OpImageFetch)
+    enum Kind { None, Lvalue, Explicit, Handle, ImageVar, SamplerVar } kind = None;
     std::string lvalue;
     std::string base, bytes, offset;  // explicit layout: byte pointer, bytes available, offset expression
     uint32_t type = 0;                // pointee type
     uint32_t mstride = 16;            // matrix stride for matrix pointees
     uint32_t slot = 0;                // handle slot
+    uint32_t set = 0, binding = 0;    // ImageVar / SamplerVar descriptor
 };
 
 class Translator {
@@ -424,6 +438,8 @@ private:
     std::map<uint32_t, PtrInfo> ptrs_;
     std::map<uint32_t, uint32_t> value_type_;  // SSA id → type
     std::map<uint32_t, uint32_t> handles_;     // SSA id holding a sampled image → slot
+    std::map<uint32_t, PtrInfo> images_;       // SSA id holding a separate image → its binding
+    std::map<uint32_t, PtrInfo> samplers_;     // SSA id holding a sampler → its binding
     std::string err_;
     bool has_kill_ = false;
     uint32_t samples_ = 0;
@@ -470,7 +486,8 @@ private:
             emit_aggregate(id);
             return "S" + std::to_string(id);
         case TypeKind::SampledImage:
-        case TypeKind::Image: return "uint32_t";  /* handles: resolved at translation, never read */
+        case TypeKind::Image:
+        case TypeKind::Sampler: return "uint32_t";  /* handles: resolved at translation, never read */
         default:
             fail("unsupported type kind in shader");
             return "int";
@@ -696,7 +713,7 @@ private:
 
     uint32_t slot_for(uint32_t set, uint32_t binding, bool texture) {
         for (auto& s : slots_)
-            if (s.set == set && s.binding == binding && s.is_texture == texture) return s.slot;
+            if (s.set == set && s.binding == binding && s.is_texture == texture && !s.separate) return s.slot;
         uint32_t next = 0;
         for (auto& s : slots_)
             if (s.is_texture == texture) next++;
@@ -704,6 +721,26 @@ private:
         rs.set = set;
         rs.binding = binding;
         rs.is_texture = texture;
+        rs.slot = next;
+        slots_.push_back(rs);
+        return next;
+    }
+    // the texture slot of a (sampled image, sampler) pair joined by OpSampledImage
+    uint32_t slot_for_pair(const PtrInfo& image, const PtrInfo& sampler) {
+        for (auto& s : slots_)
+            if (s.is_texture && s.separate && s.set == image.set && s.binding == image.binding && s.sampler_set == sampler.set &&
+                s.sampler_binding == sampler.binding)
+                return s.slot;
+        uint32_t next = 0;
+        for (auto& s : slots_)
+            if (s.is_texture) next++;
+        ResourceSlot rs;
+        rs.set = image.set;
+        rs.binding = image.binding;
+        rs.is_texture = true;
+        rs.separate = true;
+        rs.sampler_set = sampler.set;
+        rs.sampler_binding = sampler.binding;
         rs.slot = next;
         slots_.push_back(rs);
         return next;
@@ -1017,13 +1054,25 @@ bool Translator::emit_globals(const EntryPoint& ep, StageResult& out) {
         }
         case SCUniformConstant: {
             const Type* t = type(tid);
-            if (!t || t->kind != TypeKind::SampledImage) return fail("only combined image samplers are supported as UniformConstant");
             uint32_t set = 0, binding = 0;
             m_.decoration(v.id, DecDescriptorSet, set);
             m_.decoration(v.id, DecBinding, binding);
-            info.kind = PtrInfo::Handle;
-            info.slot = slot_for(set, binding, true);
-            if (info.slot >= 4) return fail("more than 4 sampled images");
+            if (t && t->kind == TypeKind::SampledImage) {
+                info.kind = PtrInfo::Handle;
+                info.slot = slot_for(set, binding, true);
+                if (info.slot >= 4) return fail("more than 4 sampled images");
+            } else if (t && t->kind == TypeKind::Image) {
+                // a separate sampled image or a storage image
+                // (CPVulkan/CommandBuffer.Draw.cpp:368-377): 2D only
+                if (t->dim != 1) return fail("only 2D images are supported");
+                info.kind = PtrInfo::ImageVar;
+            } else if (t && t->kind == TypeKind::Sampler) {
+                info.kind = PtrInfo::SamplerVar;
+            } else {
+                return fail("unsupported UniformConstant variable");
+            }
+            info.set = set;
+            info.binding = binding;
             ptrs_[v.id] = info;
             break;
         }
@@ -1121,6 +1170,14 @@ bool Translator::emit_instruction(const Instruction& ins, const std::map<uint32_
         const PtrInfo& p = it->second;
         if (p.kind == PtrInfo::Handle) {
             handles_[w[1]] = p.slot;
+            return true;
+        }
+        if (p.kind == PtrInfo::ImageVar) {
+            images_[w[1]] = p;
+            return true;
+        }
+        if (p.kind == PtrInfo::SamplerVar) {
+            samplers_[w[1]] = p;
             return true;
         }
         if (p.kind == PtrInfo::Lvalue) body_ << "  " << R(w[1]) << " = " << p.lvalue << ";\n";
@@ -1415,8 +1472,40 @@ bool Translator::emit_instruction(const Instruction& ins, const std::map<uint32_
         }
     }
     // ---- images ----
-    case OpSampledImage:
-        return fail("separate images and samplers are not supported");
+    case OpSampledImage: {
+        // a sampled image from an image and a sampler in separate bindings
+        // (LLVMRuntime/SPIRVCompiler.cpp:2459-2466 passes both descriptors);
+        // each pair is a texture slot the ICD fills from both
+        auto im = images_.find(w[2]);
+        auto sm = samplers_.find(w[3]);
+        if (im == images_.end() || sm == samplers_.end()) return fail("OpSampledImage of an unknown image or sampler");
+        const Type* it = type(im->second.type);
+        if (it && it->sampled == 2) return fail("sampling a storage image");
+        const uint32_t slot = slot_for_pair(im->second, sm->second);
+        if (slot >= 4) return fail("more than 4 sampled images");
+        handles_[w[1]] = slot;
+        return true;
+    }
+    case OpImageRead: {
+        // imageLoad (CPVulkan/GlslFunctions.cpp:740-744): the reference's
+        // ImageFetch — level 0 of the view, zeros outside it; no image
+        // operands (LLVMRuntime/SPIRVCompiler.cpp:1655-1674)
+        if (w.size() > 4) return fail("image operands on OpImageRead");
+        auto im = images_.find(w[2]);
+        if (im == images_.end()) return fail("reading an unknown image");
+        const Type* it = type(im->second.type);
+        // the draw path's images are 8-bit RGBA: Rgba8 (4) or Unknown (0)
+        if (!it || it->sampled != 2 || (it->image_format != 4 && it->image_format != 0)) return fail("only rgba8 storage images can be read");
+        const uint32_t slot = slot_for(im->second.set, im->second.binding, true);
+        if (slot >= 4) return fail("more than 4 sampled images");
+        samples_++;
+        body_ << "  " << R(w[1]) << " = cpv_fetch(P.tex[" << slot << "], (int32_t)" << comp(w[3], 0) << ", (int32_t)" << comp(w[3], 1) << ");\n";
+        return true;
+    }
+    case OpImageWrite:
+        // fragments run concurrently here, and Vulkan leaves the order of
+        // their image stores undefined: no image writes from the draw path
+        return fail("image writes (imageStore) are not supported on the draw path");
     case OpImage: {
         // the image of a sampled image (LLVMRuntime/SPIRVCompiler.cpp:2480-2519)
         auto h = handles_.find(w[2]);
@@ -1427,10 +1516,19 @@ bool Translator::emit_instruction(const Instruction& ins, const std::map<uint32_
     case OpImageFetch: {
         // texelFetch (CPVulkan/GlslFunctions.cpp:674-742): level 0 whatever
         // the Lod operand, integer texel coordinates, zero outside the level
+        uint32_t slot = 0;
         auto h = handles_.find(w[2]);
-        if (h == handles_.end()) return fail("fetching from an unknown image");
+        auto im = images_.find(w[2]);
+        if (h != handles_.end()) {
+            slot = h->second;
+        } else if (im != images_.end()) {
+            slot = slot_for(im->second.set, im->second.binding, true);
+            if (slot >= 4) return fail("more than 4 sampled images");
+        } else {
+            return fail("fetching from an unknown image");
+        }
         samples_++;
-        body_ << "  " << R(w[1]) << " = cpv_fetch(P.tex[" << h->second << "], (int32_t)" << comp(w[3], 0) << ", (int32_t)" << comp(w[3], 1) << ");\n";
+        body_ << "  " << R(w[1]) << " = cpv_fetch(P.tex[" << slot << "], (int32_t)" << comp(w[3], 0) << ", (int32_t)" << comp(w[3], 1) << ");\n";
         return true;
     }
     case OpBitCount:

@@ -30,6 +30,7 @@ struct Type {
     uint32_t storage = 0;     // pointer storage class
     std::vector<uint32_t> members;  // struct members, function param types
     uint32_t result = 0;            // function return type
+    uint32_t dim = 0, sampled = 0, image_format = 0;  // image: Dim, Sampled (1 sampled, 2 storage), ImageFormat
 };
 
 struct Constant {
@@ -111,11 +112,16 @@ struct VertexBinding {
 
 // Descriptor slots: every (set, binding) a pipeline's shaders use is given a
 // dense slot in CpvDrawParams (ubo[] for uniform buffers, tex[] for combined
-// image samplers), shared by both stages.
+// image samplers, storage images read by OpImageRead, and each (sampled
+// image, sampler) pair an OpSampledImage joins), shared by both stages.
 struct ResourceSlot {
     uint32_t set = 0, binding = 0;
     bool is_texture = false;
     uint32_t slot = 0;
+    // a texture joined from a sampled image and a sampler in another binding
+    // (OpSampledImage): the sampler's (set, binding)
+    bool separate = false;
+    uint32_t sampler_set = 0, sampler_binding = 0;
 };
 
 struct SpecConstant {

@@ -27,7 +27,8 @@ HARNESS_LIB = os.path.join(BUILD, "libcpv_harness.so")
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function", "-I" + os.path.join(ROOT, "include"),
             "-I" + os.path.join(CUDA, "include")]
 
-PROGRAMS = ["cube", "texlit", "flatquad", "meshpc", "discard", "nopersp", "points", "fetch", "mrt", "mrti"]  # index = cpv_program
+PROGRAMS = ["cube", "texlit", "flatquad", "meshpc", "discard", "nopersp", "points", "fetch", "mrt", "mrti", "storage",
+            "separate"]  # index = cpv_program
 
 
 def _write_if_changed(path, text):

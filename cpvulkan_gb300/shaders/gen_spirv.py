@@ -24,7 +24,7 @@ OP = dict(
     VectorTimesScalar=142, MatrixTimesVector=145, Dot=148, FOrdGreaterThan=186, SelectionMerge=247,
     Label=248, Branch=249, BranchConditional=250, Kill=252, Return=253, SpecConstant=50, SpecConstantOp=52,
     CopyMemory=63, ImageFetch=95, Image=100, ConvertFToS=110, ConvertSToF=111, IAdd=128, IMul=132, BitwiseXor=198,
-    BitCount=205, ConvertFToU=109, Bitcast=124,
+    BitCount=205, ConvertFToU=109, Bitcast=124, TypeSampler=26, SampledImage=86, ImageRead=98,
 )
 DEC = dict(SpecId=1, Block=2, ColMajor=5, MatrixStride=7, BuiltIn=11, NoPerspective=13, Flat=14, Location=30, Binding=33,
            DescriptorSet=34, Offset=35)
@@ -108,6 +108,13 @@ class Module:
     def sampled_image_2d(self):
         img = self.image_2d()
         return self._type(("simg2d",), "TypeSampledImage", lambda: [img])
+
+    def storage_image_2d_rgba8(self):
+        # Sampled 2 (storage), ImageFormat Rgba8 (4)
+        return self._type(("stimg2d",), "TypeImage", lambda: [self.float(), 1, 0, 0, 0, 2, 4])
+
+    def sampler(self):
+        return self._type(("sampler",), "TypeSampler", lambda: [])
 
     def spec_const_int(self, default, spec_id):
         c = self._const(("sci", spec_id), "SpecConstant", self.int, lambda: [default & 0xFFFFFFFF])
@@ -470,6 +477,61 @@ def fetch_frag():
     return m.assemble(body)
 
 
+def storage_frag():
+    """layout(set=0,binding=1,rgba8) uniform readonly image2D img;
+    layout(location=0) in vec2 uv; layout(location=1) in vec3 n; layout(location=0) out vec4 o;
+    void main() { o = imageLoad(img, ivec2(uv * 64.0)); }"""
+    m = Module(4)
+    v2, v3, v4 = m.vec(2), m.vec(3), m.vec(4)
+    iv2 = m.ivec(2)
+    img = m.storage_image_2d_rgba8()
+    var = m.variable("UniformConstant", img, "img")
+    m.decorate(var, "DescriptorSet", 0)
+    m.decorate(var, "Binding", 1)
+    uv = m.variable("Input", v2, "uv"); m.decorate(uv, "Location", 0)
+    n = m.variable("Input", v3, "n"); m.decorate(n, "Location", 1)
+    out = m.variable("Output", v4, "o"); m.decorate(out, "Location", 0)
+
+    def body(m):
+        p = m.op("ConvertFToS", iv2, m.op("VectorTimesScalar", v2, m.load(v2, uv), m.const_f(64.0)))
+        m.store(out, m.op("ImageRead", v4, m.load(img, var), p))
+        m.op_void("Return")
+    return m.assemble(body)
+
+
+def separate_frag():
+    """texlit_frag with layout(set=0,binding=1) uniform texture2D t and
+    layout(set=0,binding=2) uniform sampler s, sampled as texture(sampler2D(t, s), uv)."""
+    m = Module(4)
+    v2, v3, v4, mat, f = m.vec(2), m.vec(3), m.vec(4), m.mat4(), m.float()
+    ubo = m.ubo_block("UBO", [mat, v4], [0, 64], binding=0)
+    img, smp, simg = m.image_2d(), m.sampler(), m.sampled_image_2d()
+    tv = m.variable("UniformConstant", img, "t")
+    m.decorate(tv, "DescriptorSet", 0)
+    m.decorate(tv, "Binding", 1)
+    sv = m.variable("UniformConstant", smp, "s")
+    m.decorate(sv, "DescriptorSet", 0)
+    m.decorate(sv, "Binding", 2)
+    uv = m.variable("Input", v2, "uv"); m.decorate(uv, "Location", 0)
+    n = m.variable("Input", v3, "n"); m.decorate(n, "Location", 1)
+    out = m.variable("Output", v4, "o"); m.decorate(out, "Location", 0)
+
+    def body(m):
+        si = m.op("SampledImage", simg, m.load(img, tv), m.load(smp, sv))
+        c = m.op("ImageSampleImplicitLod", v4, si, m.load(v2, uv))
+        nn = m.ext_inst(v3, "Normalize", m.load(v3, n))
+        light = m.load(v4, m.access("Uniform", v4, ubo, m.const_int(1)))
+        lxyz = m.op("VectorShuffle", v3, light, light, 0, 1, 2)
+        d = m.op("Dot", f, nn, lxyz)
+        l = m.ext_inst(f, "FMax", d, m.const_f(0.0))
+        cxyz = m.op("VectorShuffle", v3, c, c, 0, 1, 2)
+        rgb = m.op("VectorTimesScalar", v3, cxyz, l)
+        cw = m.op("CompositeExtract", f, c, 3)
+        m.store(out, m.op("CompositeConstruct", v4, rgb, cw))
+        m.op_void("Return")
+    return m.assemble(body)
+
+
 def mrt_frag():
     """layout(location=0) in vec4 c; layout(location=L) out vec4 oL (L = 0..7);
     void main() {
@@ -550,6 +612,8 @@ PROGRAMS = {
     "fetch": (texlit_vert, fetch_frag),
     "mrt": (cube_vert, mrt_frag),
     "mrti": (cube_vert, mrti_frag),
+    "storage": (texlit_vert, storage_frag),
+    "separate": (texlit_vert, separate_frag),
 }
 
 

@@ -39,7 +39,18 @@ enum cpv_program {
                                     function of the colour, one per colour attachment                         */
     CPV_PROGRAM_MRTI = 9,        /* CUBE's vertex shader; FS: vec4 colour, uvec4(c * 300), ivec4(c * 400 - 200)
                                     and floatBitsToUint(c) at locations 0-3 (integer attachments)            */
-    CPV_PROGRAM_COUNT = 10
+    CPV_PROGRAM_STORAGE = 10,    /* TEXLIT's vertex shader; FS: imageLoad of an rgba8 storage image at
+                                    ivec2(uv * 64) (OpImageRead)                                              */
+    CPV_PROGRAM_SEPARATE = 11,   /* TEXLIT with the texture and its sampler in separate bindings, joined by
+                                    sampler2D(t, s) (OpSampledImage)                                          */
+    CPV_PROGRAM_COUNT = 12
+};
+
+/* How a scene's texture is bound (cpv_scene::texture_binding). */
+enum cpv_texture_binding {
+    CPV_TEXTURE_COMBINED = 0,  /* binding 1: a combined image sampler                   */
+    CPV_TEXTURE_STORAGE = 1,   /* binding 1: a storage image (layout GENERAL)           */
+    CPV_TEXTURE_SEPARATE = 2   /* binding 1: a sampled image; binding 2: its sampler     */
 };
 
 #define CPV_SCENE_MAX_BINDINGS 4
@@ -162,6 +173,9 @@ typedef struct cpv_scene {
      * derivatives (the ICD's CPV_SPEC_LOD=1 mode); 0: λ = 0 as the
      * reference computes it. */
     uint32_t spec_lod;
+
+    /* cpv_texture_binding: the descriptors the texture is bound through */
+    uint32_t texture_binding;
 } cpv_scene;
 
 #ifdef __cplusplus

@@ -336,6 +336,7 @@ enum {
     VK_IMAGE_USAGE_TRANSFER_SRC_BIT = 0x1,
     VK_IMAGE_USAGE_TRANSFER_DST_BIT = 0x2,
     VK_IMAGE_USAGE_SAMPLED_BIT = 0x4,
+    VK_IMAGE_USAGE_STORAGE_BIT = 0x8,
     VK_IMAGE_USAGE_COLOR_ATTACHMENT_BIT = 0x10,
     VK_IMAGE_USAGE_DEPTH_STENCIL_ATTACHMENT_BIT = 0x20,
     VK_COMMAND_POOL_CREATE_RESET_COMMAND_BUFFER_BIT = 0x2,

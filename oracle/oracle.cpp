@@ -354,7 +354,9 @@ ProgramInfo program_info(uint32_t program) {
     switch (program) {
     case CPV_PROGRAM_CUBE: return {1, {4}, {INTERP_PERSPECTIVE}};
     case CPV_PROGRAM_TEXLIT:
-    case CPV_PROGRAM_FETCH: return {2, {2, 3}, {INTERP_PERSPECTIVE, INTERP_PERSPECTIVE}};
+    case CPV_PROGRAM_FETCH:
+    case CPV_PROGRAM_STORAGE:
+    case CPV_PROGRAM_SEPARATE: return {2, {2, 3}, {INTERP_PERSPECTIVE, INTERP_PERSPECTIVE}};
     case CPV_PROGRAM_FLATQUAD: return {1, {4}, {INTERP_FLAT}};
     case CPV_PROGRAM_MESHPC: return {1, {3}, {INTERP_PERSPECTIVE}};
     case CPV_PROGRAM_DISCARD: return {1, {4}, {INTERP_PERSPECTIVE}};
@@ -463,7 +465,9 @@ void run_vs(uint32_t program, const float attr[8][4], const Resources& r, VsOut&
         break;
     }
     case CPV_PROGRAM_TEXLIT:
-    case CPV_PROGRAM_FETCH: {
+    case CPV_PROGRAM_FETCH:
+    case CPV_PROGRAM_STORAGE:
+    case CPV_PROGRAM_SEPARATE: {
         float m[16];
         for (int i = 0; i < 16; i++) m[i] = ubo_at(r, i);
         out.var[0] = attr[1][0]; out.var[1] = attr[1][1];
@@ -537,7 +541,23 @@ bool run_fs(uint32_t program, const float* in, const Resources& r, float* colour
         if (in[0] > 0.5f) return true;
         for (int i = 0; i < 4; i++) colour[i] = in[i];
         return false;
-    case CPV_PROGRAM_TEXLIT: {
+    case CPV_PROGRAM_STORAGE: {
+        /* gen_spirv.py storage_frag: imageLoad at ivec2(uv * 64)
+         * (OpVectorTimesScalar, OpConvertFToS), the reference's ImageFetch
+         * (CPVulkan/GlslFunctions.cpp:740-744): level 0, zeros outside it */
+        const int32_t px = static_cast<int32_t>(in[0] * 64.0f);
+        const int32_t py = static_cast<int32_t>(in[1] * 64.0f);
+        float t[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (r.texture && r.texture->levels > 0 && px >= 0 && py >= 0 && px < static_cast<int32_t>(r.texture->level_w[0]) &&
+            py < static_cast<int32_t>(r.texture->level_h[0]))
+            get_texel(*r.texture, 0, px, py, 0, t);
+        for (int i = 0; i < 4; i++) colour[i] = t[i];
+        return false;
+    }
+    case CPV_PROGRAM_TEXLIT:
+    case CPV_PROGRAM_SEPARATE: {
+        /* SEPARATE samples the same texture through a sampler in its own
+         * binding (sampler2D(t, s)): the same arithmetic */
         float c[4] = {0, 0, 0, 1};
         if (r.texture && r.sampler) {
             /* implicit LOD: λ 0 as the reference computes it

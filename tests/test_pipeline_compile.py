@@ -296,3 +296,17 @@ def test_spec_lod_module(compile_ctx, monkeypatch):
     assert "#define CPV_LOD_SITES 0\n" in plain and "cpv_sample_quad(" not in plain
     assert "#define CPV_LOD_SITES 1\n" in spec and "cpv_sample_quad(P.tex[0]" in spec and "cpv_lod, 0)" in spec
 
+
+def test_image_binding_modules(compile_ctx):
+    """A storage image read by imageLoad compiles to a level-0 texel fetch
+    (cpv_fetch) and a sampled image joined with a sampler from another
+    binding to an ordinary texture sample, each in texture slot 0."""
+    ctx, dump = compile_ctx
+    ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [c.PROGRAM_STORAGE, 0x10, 32, 32, 4]))
+    (storage,) = glob.glob(str(dump / "pipeline_*.cu"))
+    ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [c.PROGRAM_SEPARATE, 0x10, 32, 32, 4]))
+    (separate,) = set(glob.glob(str(dump / "pipeline_*.cu"))) - {storage}
+    storage, separate = open(storage).read(), open(separate).read()
+    assert "cpv_fetch(P.tex[0]" in storage and "cpv_sample(" not in storage
+    assert "cpv_sample(P.tex[0]" in separate
+
