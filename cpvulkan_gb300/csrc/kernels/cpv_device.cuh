@@ -275,10 +275,50 @@ __device__ __forceinline__ float cpv_normalize(float x) { return signbit(x) ? 1.
         _Pragma("unroll") for (int i = 0; i < N; i++) r.v[i] = SCALAR(a.v[i], b.v[i]);     \
         return r;                                                                          \
     }
+/* NMin / NMax (CPVulkan/GlslFunctions.cpp:264-302): a NaN first operand
+ * gives the second, else std::min / std::max (so a NaN second operand
+ * gives the first). */
+__device__ __forceinline__ float cpv_nmin(float a, float b) { return isnan(a) ? b : cpv_std_min(a, b); }
+__device__ __forceinline__ float cpv_nmax(float a, float b) { return isnan(a) ? b : cpv_std_max(a, b); }
 CPV_VEC_FUNC2(cpv_glsl_fmax, cpv_std_max)
 CPV_VEC_FUNC2(cpv_glsl_fmin, cpv_std_min)
 CPV_VEC_FUNC2(cpv_glsl_pow, powf)
+CPV_VEC_FUNC2(cpv_glsl_nmin, cpv_nmin)
+CPV_VEC_FUNC2(cpv_glsl_nmax, cpv_nmax)
 #undef CPV_VEC_FUNC2
+
+/* NClamp: NMin(NMax(x, lo), hi) (CPVulkan/GlslFunctions.cpp:306-310). */
+__device__ __forceinline__ float cpv_glsl_nclamp(float v, float lo, float hi) { return cpv_nmin(cpv_nmax(v, lo), hi); }
+template <int N>
+__device__ __forceinline__ cvec<float, N> cpv_glsl_nclamp(const cvec<float, N>& v, const cvec<float, N>& lo, const cvec<float, N>& hi) {
+    cvec<float, N> r;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.v[i] = cpv_glsl_nclamp(v.v[i], lo.v[i], hi.v[i]);
+    return r;
+}
+
+/* Reflect → glm::reflect: I - N * dot(N, I) * 2, each component one
+ * rounded multiply, multiply and subtract (CPVulkan/GlslFunctions.cpp:184-188). */
+__device__ __forceinline__ float cpv_glsl_reflect(float i, float n) {
+    return __fsub_rn(i, __fmul_rn(__fmul_rn(n, __fmul_rn(n, i)), 2.0f));
+}
+template <int N>
+__device__ __forceinline__ cvec<float, N> cpv_glsl_reflect(const cvec<float, N>& i, const cvec<float, N>& n) {
+    const float d = cpv_dot(n, i);
+    cvec<float, N> r;
+#pragma unroll
+    for (int k = 0; k < N; k++) r.v[k] = __fsub_rn(i.v[k], __fmul_rn(__fmul_rn(n.v[k], d), 2.0f));
+    return r;
+}
+
+/* FindILsb / FindSMsb / FindUMsb on 32-bit integers (CPVulkan/GlslFunctions.cpp:190-262):
+ * -1 for no set bit; FindSMsb looks at ~v for negative v. */
+__device__ __forceinline__ int32_t cpv_find_ilsb(uint32_t v) { return v == 0u ? -1 : __ffs(static_cast<int>(v)) - 1; }
+__device__ __forceinline__ int32_t cpv_find_umsb(uint32_t v) { return v == 0u ? -1 : 31 - __clz(static_cast<int>(v)); }
+__device__ __forceinline__ int32_t cpv_find_smsb(int32_t v) {
+    if (v < 0) v = ~v;
+    return v == 0 ? -1 : 31 - __clz(v);
+}
 
 __device__ __forceinline__ float cpv_glsl_fclamp(float v, float lo, float hi) { return cpv_std_clamp(v, lo, hi); }
 template <int N>

@@ -1437,6 +1437,7 @@ bool Translator::emit_instruction(const Instruction& ins, const std::map<uint32_
         case 4: cw(w[1], w[0], a, [](auto& c) { return "fabsf(" + c[0] + ")"; }); return true;
         case 5: cw(w[1], w[0], a, [](auto& c) { return "abs(" + c[0] + ")"; }); return true;
         case 6: cw(w[1], w[0], a, [](auto& c) { return "(" + c[0] + " > 0.0f ? 1.0f : (" + c[0] + " < 0.0f ? -1.0f : 0.0f))"; }); return true;
+        case 7: cw(w[1], w[0], a, [](auto& c) { return "((0 < (" + c[0] + ")) - ((" + c[0] + ") < 0))"; }); return true;  // SSign
         case 8: cw(w[1], w[0], a, [](auto& c) { return "floorf(" + c[0] + ")"; }); return true;
         case 9: cw(w[1], w[0], a, [](auto& c) { return "ceilf(" + c[0] + ")"; }); return true;
         case 10: cw(w[1], w[0], a, [](auto& c) { return "__fsub_rn(" + c[0] + ", floorf(" + c[0] + "))"; }); return true;
@@ -1467,6 +1468,13 @@ bool Translator::emit_instruction(const Instruction& ins, const std::map<uint32_
             return true;
         }
         case 69: call("cpv_normalize"); return true;
+        case 71: call("cpv_glsl_reflect"); return true;
+        case 73: cw(w[1], w[0], a, [](auto& c) { return "cpv_find_ilsb((uint32_t)(" + c[0] + "))"; }); return true;
+        case 74: cw(w[1], w[0], a, [](auto& c) { return "cpv_find_smsb((int32_t)(" + c[0] + "))"; }); return true;
+        case 75: cw(w[1], w[0], a, [](auto& c) { return "cpv_find_umsb((uint32_t)(" + c[0] + "))"; }); return true;
+        case 79: call("cpv_glsl_nmin"); return true;
+        case 80: call("cpv_glsl_nmax"); return true;
+        case 81: call("cpv_glsl_nclamp"); return true;
         default:
             return fail("unsupported GLSL.std.450 instruction " + std::to_string(inst));
         }

@@ -24,13 +24,13 @@ OP = dict(
     VectorTimesScalar=142, MatrixTimesVector=145, Dot=148, FOrdGreaterThan=186, SelectionMerge=247,
     Label=248, Branch=249, BranchConditional=250, Kill=252, Return=253, SpecConstant=50, SpecConstantOp=52,
     CopyMemory=63, ImageFetch=95, Image=100, ConvertFToS=110, ConvertSToF=111, IAdd=128, IMul=132, BitwiseXor=198,
-    BitCount=205, ConvertFToU=109, Bitcast=124, TypeSampler=26, SampledImage=86, ImageRead=98,
+    BitCount=205, ConvertFToU=109, Bitcast=124, TypeSampler=26, SampledImage=86, ImageRead=98, ISub=130,
 )
 DEC = dict(SpecId=1, Block=2, ColMajor=5, MatrixStride=7, BuiltIn=11, NoPerspective=13, Flat=14, Location=30, Binding=33,
            DescriptorSet=34, Offset=35)
 SC = dict(UniformConstant=0, Input=1, Uniform=2, Output=3, Function=7, PushConstant=9)
 BUILTIN = dict(Position=0, PointSize=1, ClipDistance=3, CullDistance=4)
-GLSL = dict(FMax=40, Normalize=69)
+GLSL = dict(FMax=40, Normalize=69, SSign=7, Reflect=71, FindILsb=73, FindSMsb=74, FindUMsb=75, NMin=79, NMax=80, NClamp=81)
 
 
 def _str_words(s):
@@ -532,6 +532,44 @@ def separate_frag():
     return m.assemble(body)
 
 
+def mathx_frag():
+    """layout(location=0) in vec4 c; layout(location=0) out vec4 o;
+    void main() { float z = c.a - c.a; float nan = z / z;
+                  float r = nclamp(c.r * 3.0 - 1.0, 0.25, 0.75); r = nmin(nan, r); r = nmax(r, nan);
+                  int i = int(c.g * 1000.0) - 500; uint u = uint(c.b * 65535.0);
+                  int bits = findMSB(i) + findLSB(i) + sign(i);
+                  vec3 refl = reflect(c.rgb, vec3(0.6, 0.0, 0.8));
+                  o = vec4(r, float(bits) / 64.0, float(findMSB(u)) / 16.0, refl.x * 0.5 + 0.5); }
+    (GLSL.std.450 NMin, NMax, NClamp, FindSMsb, FindILsb, SSign, FindUMsb, Reflect.)"""
+    m = Module(4)
+    v3, v4, f, i, u = m.vec(3), m.vec(4), m.float(), m.int(), m.uint()
+    col = m.variable("Input", v4, "c")
+    m.decorate(col, "Location", 0)
+    out = m.variable("Output", v4, "o")
+    m.decorate(out, "Location", 0)
+
+    def body(m):
+        c = m.load(v4, col)
+        cr, cg, cb, ca = (m.op("CompositeExtract", f, c, k) for k in range(4))
+        z = m.op("FSub", f, ca, ca)
+        nan = m.op("FDiv", f, z, z)
+        r = m.ext_inst(f, "NClamp", m.op("FSub", f, m.op("FMul", f, cr, m.const_f(3.0)), m.const_f(1.0)), m.const_f(0.25), m.const_f(0.75))
+        r = m.ext_inst(f, "NMin", nan, r)
+        r = m.ext_inst(f, "NMax", r, nan)
+        iv = m.op("ISub", i, m.op("ConvertFToS", i, m.op("FMul", f, cg, m.const_f(1000.0))), m.const_int(500))
+        uv = m.op("ConvertFToU", u, m.op("FMul", f, cb, m.const_f(65535.0)))
+        bits = m.op("IAdd", i, m.op("IAdd", i, m.ext_inst(i, "FindSMsb", iv), m.ext_inst(i, "FindILsb", iv)), m.ext_inst(i, "SSign", iv))
+        g = m.op("FDiv", f, m.op("ConvertSToF", f, bits), m.const_f(64.0))
+        b = m.op("FDiv", f, m.op("ConvertSToF", f, m.ext_inst(i, "FindUMsb", uv)), m.const_f(16.0))
+        rgb = m.op("VectorShuffle", v3, c, c, 0, 1, 2)
+        nrm = m.op("CompositeConstruct", v3, m.const_f(0.6), m.const_f(0.0), m.const_f(0.8))
+        refl = m.ext_inst(v3, "Reflect", rgb, nrm)
+        a = m.op("FAdd", f, m.op("FMul", f, m.op("CompositeExtract", f, refl, 0), m.const_f(0.5)), m.const_f(0.5))
+        m.store(out, m.op("CompositeConstruct", v4, r, g, b, a))
+        m.op_void("Return")
+    return m.assemble(body)
+
+
 def mrt_frag():
     """layout(location=0) in vec4 c; layout(location=L) out vec4 oL (L = 0..7);
     void main() {
@@ -614,6 +652,7 @@ PROGRAMS = {
     "mrti": (cube_vert, mrti_frag),
     "storage": (texlit_vert, storage_frag),
     "separate": (texlit_vert, separate_frag),
+    "mathx": (cube_vert, mathx_frag),
 }
 
 

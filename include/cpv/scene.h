@@ -43,7 +43,9 @@ enum cpv_program {
                                     ivec2(uv * 64) (OpImageRead)                                              */
     CPV_PROGRAM_SEPARATE = 11,   /* TEXLIT with the texture and its sampler in separate bindings, joined by
                                     sampler2D(t, s) (OpSampledImage)                                          */
-    CPV_PROGRAM_COUNT = 12
+    CPV_PROGRAM_MATHX = 12,      /* CUBE's vertex shader; FS: GLSL.std.450 NMin/NMax/NClamp (with a NaN),
+                                    FindSMsb/FindILsb/SSign/FindUMsb on integers from the colour, Reflect    */
+    CPV_PROGRAM_COUNT = 13
 };
 
 /* How a scene's texture is bound (cpv_scene::texture_binding). */

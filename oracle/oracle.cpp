@@ -363,7 +363,8 @@ ProgramInfo program_info(uint32_t program) {
     case CPV_PROGRAM_NOPERSP: return {1, {4}, {INTERP_LINEAR}};
     case CPV_PROGRAM_POINTS: return {1, {4}, {INTERP_PERSPECTIVE}};
     case CPV_PROGRAM_MRT:
-    case CPV_PROGRAM_MRTI: return {1, {4}, {INTERP_PERSPECTIVE}};
+    case CPV_PROGRAM_MRTI:
+    case CPV_PROGRAM_MATHX: return {1, {4}, {INTERP_PERSPECTIVE}};
     default: return {0, {0}, {INTERP_PERSPECTIVE}};
     }
 }
@@ -455,7 +456,8 @@ void run_vs(uint32_t program, const float attr[8][4], const Resources& r, VsOut&
     case CPV_PROGRAM_NOPERSP:
     case CPV_PROGRAM_POINTS:
     case CPV_PROGRAM_MRT:
-    case CPV_PROGRAM_MRTI: {
+    case CPV_PROGRAM_MRTI:
+    case CPV_PROGRAM_MATHX: {
         float m[16];
         for (int i = 0; i < 16; i++) m[i] = ubo_at(r, i);
         for (int i = 0; i < 4; i++) out.var[i] = attr[1][i];
@@ -496,6 +498,22 @@ void run_vs(uint32_t program, const float attr[8][4], const Resources& r, VsOut&
     }
 }
 
+/* GLSL.std.450 functions the reference registers (CPVulkan/GlslFunctions.cpp:36-40,
+ * 190-310): NMin / NMax give the second operand for a NaN first one, else
+ * std::min / std::max; NClamp = NMin(NMax(x, lo), hi); FindILsb / FindUMsb /
+ * FindSMsb return -1 without a set bit, FindSMsb looks at ~v for v < 0;
+ * SSign = (0 < v) - (v < 0). */
+float glsl_nmin(float a, float b) { return std::isnan(a) ? b : std::min(a, b); }
+float glsl_nmax(float a, float b) { return std::isnan(a) ? b : std::max(a, b); }
+float glsl_nclamp(float x, float lo, float hi) { return glsl_nmin(glsl_nmax(x, lo), hi); }
+int32_t find_ilsb(uint32_t v) { return v == 0 ? -1 : __builtin_ctz(v); }
+int32_t find_umsb(uint32_t v) { return v == 0 ? -1 : 31 - __builtin_clz(v); }
+int32_t find_smsb(int32_t v) {
+    if (v < 0) v = ~v;
+    return v == 0 ? -1 : 31 - __builtin_clz(static_cast<uint32_t>(v));
+}
+int32_t ssign(int32_t v) { return (0 < v) - (v < 0); }
+
 /* Returns true when the fragment is discarded (OpKill → return true,
  * LLVMRuntime/SPIRVCompiler.cpp:3308-3310, 3642-3651). colour holds 4
  * floats per output location (locations 0-7); a program fills the
@@ -529,6 +547,27 @@ bool run_fs(uint32_t program, const float* in, const Resources& r, float* colour
             colour[12 + i] = c[i];  /* OpBitcast: the same bits */
         }
         for (int i = 16; i < 32; i++) colour[i] = 0.0f;
+        return false;
+    }
+    case CPV_PROGRAM_MATHX: {
+        /* gen_spirv.py mathx_frag, one operation per SPIR-V instruction */
+        const float* c = in;
+        const float z = c[3] - c[3];
+        const float nan = z / z;
+        float r = glsl_nclamp(c[0] * 3.0f - 1.0f, 0.25f, 0.75f);
+        r = glsl_nmin(nan, r);
+        r = glsl_nmax(r, nan);
+        const int32_t i = static_cast<int32_t>(c[1] * 1000.0f) - 500;  /* OpConvertFToS, OpISub */
+        const uint32_t u = static_cast<uint32_t>(c[2] * 65535.0f);       /* OpConvertFToU */
+        const int32_t bits = (find_smsb(i) + find_ilsb(static_cast<uint32_t>(i))) + ssign(i);
+        const float n[3] = {0.6f, 0.0f, 0.8f};
+        /* Reflect (glm::reflect): I - N * dot(N, I) * 2, dot left to right */
+        const float d = (n[0] * c[0] + n[1] * c[1]) + n[2] * c[2];
+        const float rx = c[0] - (n[0] * d) * 2.0f;
+        colour[0] = r;
+        colour[1] = static_cast<float>(bits) / 64.0f;
+        colour[2] = static_cast<float>(find_umsb(u)) / 16.0f;
+        colour[3] = rx * 0.5f + 0.5f;
         return false;
     }
     case CPV_PROGRAM_CUBE:

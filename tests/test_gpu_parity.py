@@ -423,3 +423,18 @@ def test_separate_sampler_equals_combined(gpu_ctx):
         b, _ = render_gpu(gpu_ctx, c.Scene(c.PROGRAM, 4, [c.PROGRAM_TEXLIT, variant, 64, 48, 24]))
         assert np.array_equal(a, b), hex(variant)
 
+
+# GLSL.std.450 instructions the reference registers beyond the programs
+# above (CPVulkan/GlslFunctions.cpp:36-40, 184-310): NMin / NMax / NClamp
+# with a NaN operand, FindSMsb / FindILsb / SSign / FindUMsb on integers
+# converted from the colour, Reflect.
+@pytest.mark.parametrize("variant", [0x10, 0x10 | 0x20, 0x8 | 0x2])
+@pytest.mark.parametrize("batched", [False, True])
+def test_glsl_builtins_program(gpu_ctx, oracle, monkeypatch, variant, batched):
+    if batched:
+        monkeypatch.setenv("CPV_BATCH_MIN_DRAWS", "1")
+    scene = c.Scene(c.PROGRAM, 5, [c.PROGRAM_MATHX, variant, 64, 48, 24])
+    report, stats = check(gpu_ctx, oracle, scene)
+    assert stats["fragments_written"] > 0
+    assert report["color_pixels_differing"] == 0, report
+

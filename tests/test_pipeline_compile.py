@@ -310,3 +310,15 @@ def test_image_binding_modules(compile_ctx):
     assert "cpv_fetch(P.tex[0]" in storage and "cpv_sample(" not in storage
     assert "cpv_sample(P.tex[0]" in separate
 
+
+def test_glsl_builtins_translate(compile_ctx):
+    """NMin, NMax, NClamp, FindSMsb, FindILsb, FindUMsb, SSign and Reflect
+    (GLSL.std.450 71-81, 7) translate to the device helpers that restate
+    the reference's definitions."""
+    ctx, dump = compile_ctx
+    ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [c.PROGRAM_MATHX, 0x10, 32, 32, 4]))
+    (path,) = glob.glob(str(dump / "pipeline_*.cu"))
+    text = open(path).read()
+    for fn in ("cpv_glsl_nclamp(", "cpv_glsl_nmin(", "cpv_glsl_nmax(", "cpv_find_smsb(", "cpv_find_ilsb(", "cpv_find_umsb(", "cpv_glsl_reflect("):
+        assert fn in text, fn
+
