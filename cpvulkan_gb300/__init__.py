@@ -21,7 +21,7 @@ MANIFEST_PATH = os.path.join(BUILD_DIR, "CPVulkan.json")
 CUBE, HEIGHTFIELD, BLEND, BATCH, PROGRAM, SERVE = 1, 2, 3, 4, 5, 6
 # Shader programs (include/cpv/scene.h).
 (PROGRAM_CUBE, PROGRAM_TEXLIT, PROGRAM_FLATQUAD, PROGRAM_MESHPC, PROGRAM_DISCARD, PROGRAM_NOPERSP, PROGRAM_POINTS, PROGRAM_FETCH, PROGRAM_MRT,
- PROGRAM_MRTI, PROGRAM_STORAGE, PROGRAM_SEPARATE, PROGRAM_MATHX) = range(13)
+ PROGRAM_MRTI, PROGRAM_STORAGE, PROGRAM_SEPARATE, PROGRAM_MATHX, PROGRAM_CALLS) = range(14)
 
 VK_FORMAT_D16_UNORM = 124
 VK_FORMAT_D32_SFLOAT = 126

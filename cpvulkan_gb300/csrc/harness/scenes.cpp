@@ -753,7 +753,8 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
     uint32_t vcount = 0;
     uint64_t colour_offset = 0;
     if (program == CPV_PROGRAM_CUBE || program == CPV_PROGRAM_DISCARD || program == CPV_PROGRAM_NOPERSP || program == CPV_PROGRAM_POINTS ||
-        program == CPV_PROGRAM_MRT || program == CPV_PROGRAM_MRTI || program == CPV_PROGRAM_MATHX) {
+        program == CPV_PROGRAM_MRT || program == CPV_PROGRAM_MRTI || program == CPV_PROGRAM_MATHX ||
+        program == CPV_PROGRAM_CALLS) {
         // Clip-space vertices with w in [0.5, 2] (positive, as the reference
         // requires), a shared-edge pair, and a zero-area triangle.
         st.uniform.resize(64);

@@ -446,6 +446,14 @@ private:
     uint32_t lod_sites_ = 0;  // implicit-LOD sampling instructions (spec_lod_)
     uint32_t instructions_ = 0;
     uint32_t out_outputs_ = 0;  // FS output locations declared
+    // Functions other than the entry point: each becomes a lambda inside the
+    // stage function (capturing the stage's variables by reference), defined
+    // callee first. While one is emitted, callee_ is it.
+    std::ostringstream funcs_;
+    const Function* callee_ = nullptr;
+    bool emit_callee(const Function& f);
+    bool order_callees(uint32_t fid, std::vector<uint32_t>& order, std::set<uint32_t>& seen, std::set<uint32_t>& stack);
+    std::string callee_default_return();
 
     bool fail(const std::string& e) {
         if (err_.empty()) err_ = e;
@@ -1593,22 +1601,132 @@ bool Translator::emit_instruction(const Instruction& ins, const std::map<uint32_
         return true;
     }
     case OpReturn:
-        body_ << "  goto cpv_epilogue;\n";
+        body_ << (callee_ ? "  return;\n" : "  goto cpv_epilogue;\n");
         return true;
     case OpKill:
         if (model_ != 4) return fail("OpKill outside a fragment shader");
         has_kill_ = true;
-        body_ << "  return true;\n";
+        // a discard inside a called function ends the whole invocation: the
+        // callers return too (cpv_killed, checked after every call)
+        if (callee_) body_ << "  cpv_killed = true;\n  return" << callee_default_return() << ";\n";
+        else body_ << "  return true;\n";
         return true;
     case OpUnreachable:
-        body_ << "  goto cpv_epilogue;\n";
+        if (callee_) body_ << "  return" << callee_default_return() << ";\n";
+        else body_ << "  goto cpv_epilogue;\n";
         return true;
     case OpReturnValue:
-    case OpFunctionCall:
-        return fail("function calls are not supported: inline the shader's functions");
+        if (!callee_) return fail("OpReturnValue in the entry point");
+        body_ << "  return " << value(w[0]) << ";\n";
+        return true;
+    case OpFunctionCall: {
+        // (LLVMRuntime/SPIRVCompiler.cpp translates every function; here each
+        // is a lambda of the stage function, called with its arguments: a
+        // pointer argument passes the variable it points at by reference)
+        std::string call = "f" + std::to_string(w[2]) + "(";
+        for (size_t k = 3; k < w.size(); k++) {
+            auto pit = ptrs_.find(w[k]);
+            if (pit != ptrs_.end()) {
+                if (pit->second.kind != PtrInfo::Lvalue) return fail("a function argument points at a uniform, image or input");
+                call += (k > 3 ? ", " : "") + pit->second.lvalue;
+            } else {
+                call += (k > 3 ? ", " : "") + value(w[k]);
+            }
+        }
+        call += ")";
+        const Type* rt = type(w[0]);
+        if (rt && rt->kind != TypeKind::Void) body_ << "  " << R(w[1]) << " = " << call << ";\n";
+        else body_ << "  " << call << ";\n";
+        if (model_ == 4 && has_kill_) {
+            if (callee_) body_ << "  if (cpv_killed) return" << callee_default_return() << ";\n";
+            else body_ << "  if (cpv_killed) return true;\n";
+        }
+        return true;
+    }
     default:
         return fail("unsupported SPIR-V opcode " + std::to_string(ins.opcode));
     }
+}
+
+std::string Translator::callee_default_return() {
+    const Type* rt = callee_ ? type(callee_->result_type) : nullptr;
+    if (!rt || rt->kind == TypeKind::Void) return "";
+    return " " + tn(callee_->result_type) + "{}";
+}
+
+// Functions reachable from `fid`, callees before their callers; recursion
+// (which SPIR-V shaders may not use) is rejected.
+bool Translator::order_callees(uint32_t fid, std::vector<uint32_t>& order, std::set<uint32_t>& seen, std::set<uint32_t>& stack) {
+    auto fit = m_.functions.find(fid);
+    if (fit == m_.functions.end()) return fail("call of an unknown function");
+    stack.insert(fid);
+    for (const Block& b : fit->second.blocks)
+        for (const Instruction& ins : b.body) {
+            if (ins.opcode != OpFunctionCall || ins.words.size() < 3) continue;
+            const uint32_t callee = ins.words[2];
+            if (stack.count(callee)) return fail("recursive function call");
+            if (seen.count(callee)) continue;
+            seen.insert(callee);
+            if (!order_callees(callee, order, seen, stack)) return false;
+            order.push_back(callee);
+        }
+    stack.erase(fid);
+    return true;
+}
+
+// A function other than the entry point as a lambda of the stage function:
+// value parameters by value, pointer parameters (to Function or Private
+// variables) as references to the caller's variable.
+bool Translator::emit_callee(const Function& f) {
+    std::ostringstream decls, pro, body;
+    std::swap(decls, decls_);
+    std::swap(pro, pro_);
+    std::swap(body, body_);
+    callee_ = &f;
+    std::string params;
+    bool ok = true;
+    for (size_t i = 0; i < f.params.size() && ok; i++) {
+        const uint32_t pid = f.params[i];
+        const Type* t = type(f.param_types[i]);
+        if (!t) {
+            ok = fail("bad function parameter type");
+            break;
+        }
+        if (i) params += ", ";
+        if (t->kind == TypeKind::Pointer) {
+            if (t->storage != SCFunction && t->storage != SCPrivate) {
+                ok = fail("a function parameter points at a uniform, image or input");
+                break;
+            }
+            PtrInfo info;
+            info.kind = PtrInfo::Lvalue;
+            info.lvalue = "v" + std::to_string(pid);
+            info.type = t->component;
+            ptrs_[pid] = info;
+            params += tn(t->component) + "& v" + std::to_string(pid);
+        } else {
+            if (t->kind == TypeKind::SampledImage || t->kind == TypeKind::Image || t->kind == TypeKind::Sampler) {
+                ok = fail("an image or sampler function parameter");
+                break;
+            }
+            value_type_[pid] = f.param_types[i];
+            params += tn(f.param_types[i]) + " r" + std::to_string(pid);
+        }
+    }
+    if (ok) ok = emit_function(f);
+    const Type* rt = type(f.result_type);
+    const bool has_value = rt && rt->kind != TypeKind::Void;
+    std::swap(decls, decls_);
+    std::swap(pro, pro_);
+    std::swap(body, body_);
+    if (ok) {
+        funcs_ << "  auto f" << f.id << " = [&](" << params << ") -> " << (has_value ? tn(f.result_type) : std::string("void")) << " {\n"
+               << decls.str() << pro.str() << body.str();
+        if (has_value) funcs_ << "  return " << tn(f.result_type) << "{};\n";
+        funcs_ << "  };\n";
+    }
+    callee_ = nullptr;
+    return ok && err_.empty();
 }
 
 bool Translator::run(const std::string& entry_name, StageResult& out, std::string& error) {
@@ -1633,7 +1751,11 @@ bool Translator::run(const std::string& entry_name, StageResult& out, std::strin
             }
         }
     }
-    if (!emit_globals(*ep, out) || !emit_function(fit->second)) {
+    std::vector<uint32_t> callees;
+    std::set<uint32_t> seen, stack;
+    bool ok = emit_globals(*ep, out) && order_callees(ep->function, callees, seen, stack);
+    for (size_t i = 0; ok && i < callees.size(); i++) ok = emit_callee(m_.functions.at(callees[i]));
+    if (!ok || !emit_function(fit->second)) {
         error = err_.empty() ? "translation failed" : err_;
         return false;
     }
@@ -1658,7 +1780,8 @@ bool Translator::run(const std::string& entry_name, StageResult& out, std::strin
         if (spec_lod_) s << "  (void)cpv_lod;\n";
         s << "  cpv_colour[0] = cpv_colour[1] = cpv_colour[2] = 0.0f; cpv_colour[3] = 1.0f;\n";
     }
-    s << decls_.str() << pro_.str() << body_.str() << " cpv_epilogue:;\n" << epi_.str();
+    if (!callees.empty() && model_ == 4) s << "  bool cpv_killed = false;\n  (void)cpv_killed;\n";
+    s << decls_.str() << pro_.str() << funcs_.str() << body_.str() << " cpv_epilogue:;\n" << epi_.str();
     if (model_ != 0) s << "  return false;\n";
     s << "}\n";
     out.code = s.str();

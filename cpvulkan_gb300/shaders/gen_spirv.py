@@ -25,6 +25,7 @@ OP = dict(
     Label=248, Branch=249, BranchConditional=250, Kill=252, Return=253, SpecConstant=50, SpecConstantOp=52,
     CopyMemory=63, ImageFetch=95, Image=100, ConvertFToS=110, ConvertSToF=111, IAdd=128, IMul=132, BitwiseXor=198,
     BitCount=205, ConvertFToU=109, Bitcast=124, TypeSampler=26, SampledImage=86, ImageRead=98, ISub=130,
+    FunctionParameter=55, FunctionCall=57, ReturnValue=254,
 )
 DEC = dict(SpecId=1, Block=2, ColMajor=5, MatrixStride=7, BuiltIn=11, NoPerspective=13, Flat=14, Location=30, Binding=33,
            DescriptorSet=34, Offset=35)
@@ -570,6 +571,63 @@ def mathx_frag():
     return m.assemble(body)
 
 
+def calls_frag():
+    """layout(location=0) in vec4 c; layout(location=0) out vec4 o;
+    float scale(inout vec4 v, float s) { v = v * s; return v.x + s; }
+    void check(vec4 v) { if (v.y > 0.45) discard; }
+    void main() { vec4 t = c; float k = scale(t, 0.5); check(t); o = vec4(t.xyz, k); }
+    (OpFunctionCall with a pointer and a value parameter, OpReturnValue, and a
+    discard inside a called function; the functions precede main.)"""
+    m = Module(4)
+    v3, v4, f, b = m.vec(3), m.vec(4), m.float(), m.bool()
+    col = m.variable("Input", v4, "c")
+    m.decorate(col, "Location", 0)
+    out = m.variable("Output", v4, "o")
+    m.decorate(out, "Location", 0)
+    pv4 = m.ptr("Function", v4)
+    fn_scale_t = m._type(("fn", f, pv4, f), "TypeFunction", lambda: [f, pv4, f])
+    fn_check_t = m._type(("fn", m.void(), v4), "TypeFunction", lambda: [m.void(), v4])
+
+    # float scale(inout vec4 v, float s)
+    scale = m.id()
+    m.body.append(m._ins("Function", [f, scale, 0, fn_scale_t]))
+    pv, ps = m.id(), m.id()
+    m.body.append(m._ins("FunctionParameter", [pv4, pv]))
+    m.body.append(m._ins("FunctionParameter", [f, ps]))
+    m.label()
+    mv = m.op("VectorTimesScalar", v4, m.load(v4, pv), ps)
+    m.store(pv, mv)
+    m.op_void("ReturnValue", m.op("FAdd", f, m.op("CompositeExtract", f, mv, 0), ps))
+    m.body.append(m._ins("FunctionEnd", []))
+
+    # void check(vec4 v)
+    check = m.id()
+    m.body.append(m._ins("Function", [m.void(), check, 0, fn_check_t]))
+    pc = m.id()
+    m.body.append(m._ins("FunctionParameter", [v4, pc]))
+    m.label()
+    cond = m.op("FOrdGreaterThan", b, m.op("CompositeExtract", f, pc, 1), m.const_f(0.45))
+    kill_lbl, merge_lbl = m.id(), m.id()
+    m.op_void("SelectionMerge", merge_lbl, 0)
+    m.op_void("BranchConditional", cond, kill_lbl, merge_lbl)
+    m.body.append(m._ins("Label", [kill_lbl]))
+    m.op_void("Kill")
+    m.body.append(m._ins("Label", [merge_lbl]))
+    m.op_void("Return")
+    m.body.append(m._ins("FunctionEnd", []))
+
+    def body(m):
+        t = m.local(v4)
+        m.store(t, m.load(v4, col))
+        k = m.op("FunctionCall", f, scale, t, m.const_f(0.5))
+        tv = m.load(v4, t)
+        m.op("FunctionCall", m.void(), check, tv)
+        xyz = m.op("VectorShuffle", v3, tv, tv, 0, 1, 2)
+        m.store(out, m.op("CompositeConstruct", v4, xyz, k))
+        m.op_void("Return")
+    return m.assemble(body)
+
+
 def mrt_frag():
     """layout(location=0) in vec4 c; layout(location=L) out vec4 oL (L = 0..7);
     void main() {
@@ -653,6 +711,7 @@ PROGRAMS = {
     "storage": (texlit_vert, storage_frag),
     "separate": (texlit_vert, separate_frag),
     "mathx": (cube_vert, mathx_frag),
+    "calls": (cube_vert, calls_frag),
 }
 
 

@@ -45,7 +45,9 @@ enum cpv_program {
                                     sampler2D(t, s) (OpSampledImage)                                          */
     CPV_PROGRAM_MATHX = 12,      /* CUBE's vertex shader; FS: GLSL.std.450 NMin/NMax/NClamp (with a NaN),
                                     FindSMsb/FindILsb/SSign/FindUMsb on integers from the colour, Reflect    */
-    CPV_PROGRAM_COUNT = 13
+    CPV_PROGRAM_CALLS = 13,      /* CUBE's vertex shader; FS: function calls (a pointer and a value parameter,
+                                    a return value, a discard inside a called function)                      */
+    CPV_PROGRAM_COUNT = 14
 };
 
 /* How a scene's texture is bound (cpv_scene::texture_binding). */

@@ -364,7 +364,8 @@ ProgramInfo program_info(uint32_t program) {
     case CPV_PROGRAM_POINTS: return {1, {4}, {INTERP_PERSPECTIVE}};
     case CPV_PROGRAM_MRT:
     case CPV_PROGRAM_MRTI:
-    case CPV_PROGRAM_MATHX: return {1, {4}, {INTERP_PERSPECTIVE}};
+    case CPV_PROGRAM_MATHX:
+    case CPV_PROGRAM_CALLS: return {1, {4}, {INTERP_PERSPECTIVE}};
     default: return {0, {0}, {INTERP_PERSPECTIVE}};
     }
 }
@@ -457,7 +458,8 @@ void run_vs(uint32_t program, const float attr[8][4], const Resources& r, VsOut&
     case CPV_PROGRAM_POINTS:
     case CPV_PROGRAM_MRT:
     case CPV_PROGRAM_MRTI:
-    case CPV_PROGRAM_MATHX: {
+    case CPV_PROGRAM_MATHX:
+    case CPV_PROGRAM_CALLS: {
         float m[16];
         for (int i = 0; i < 16; i++) m[i] = ubo_at(r, i);
         for (int i = 0; i < 4; i++) out.var[i] = attr[1][i];
@@ -547,6 +549,16 @@ bool run_fs(uint32_t program, const float* in, const Resources& r, float* colour
             colour[12 + i] = c[i];  /* OpBitcast: the same bits */
         }
         for (int i = 16; i < 32; i++) colour[i] = 0.0f;
+        return false;
+    }
+    case CPV_PROGRAM_CALLS: {
+        /* gen_spirv.py calls_frag: scale() multiplies the variable it is
+         * given by 0.5 and returns its x + 0.5; check() discards when y > 0.45 */
+        float t[4];
+        for (int i = 0; i < 4; i++) t[i] = in[i] * 0.5f;
+        const float k = t[0] + 0.5f;
+        if (t[1] > 0.45f) return true;
+        colour[0] = t[0]; colour[1] = t[1]; colour[2] = t[2]; colour[3] = k;
         return false;
     }
     case CPV_PROGRAM_MATHX: {

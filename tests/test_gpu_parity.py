@@ -438,3 +438,19 @@ def test_glsl_builtins_program(gpu_ctx, oracle, monkeypatch, variant, batched):
     assert stats["fragments_written"] > 0
     assert report["color_pixels_differing"] == 0, report
 
+
+# Function calls (OpFunctionCall): a function that scales the variable it
+# is given (a pointer parameter) and returns a value, and one that
+# discards; per draw, batched, and under the deferred schedule.
+@pytest.mark.parametrize("variant", [0x10, 0x10 | 0x20, 0x8 | 0x2])
+@pytest.mark.parametrize("mode", ["plain", "batched", "deferred"])
+def test_function_calls_program(gpu_ctx, oracle, monkeypatch, variant, mode):
+    if mode == "batched":
+        monkeypatch.setenv("CPV_BATCH_MIN_DRAWS", "1")
+    if mode == "deferred":
+        monkeypatch.setenv("CPV_SCHEDULE", "1")
+    scene = c.Scene(c.PROGRAM, 6, [c.PROGRAM_CALLS, variant, 64, 48, 24])
+    report, stats = check(gpu_ctx, oracle, scene)
+    assert 0 < stats["fragments_written"] < stats["fragments"]
+    assert report["color_pixels_differing"] == 0, report
+

@@ -322,3 +322,15 @@ def test_glsl_builtins_translate(compile_ctx):
     for fn in ("cpv_glsl_nclamp(", "cpv_glsl_nmin(", "cpv_glsl_nmax(", "cpv_find_smsb(", "cpv_find_ilsb(", "cpv_find_umsb(", "cpv_glsl_reflect("):
         assert fn in text, fn
 
+
+def test_function_calls_translate(compile_ctx):
+    """Functions other than the entry point become lambdas of the stage
+    function, callees first; a pointer parameter is a reference to the
+    caller's variable, and a discard inside one ends the invocation."""
+    ctx, dump = compile_ctx
+    ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [c.PROGRAM_CALLS, 0x10, 32, 32, 4]))
+    (path,) = glob.glob(str(dump / "pipeline_*.cu"))
+    text = open(path).read()
+    assert text.count("= [&](") == 2
+    assert "cvec<float, 4>& v" in text and "cpv_killed = true;" in text and "if (cpv_killed) return true;" in text
+
