@@ -21,7 +21,7 @@ MANIFEST_PATH = os.path.join(BUILD_DIR, "CPVulkan.json")
 CUBE, HEIGHTFIELD, BLEND, BATCH, PROGRAM, SERVE = 1, 2, 3, 4, 5, 6
 # Shader programs (include/cpv/scene.h).
 (PROGRAM_CUBE, PROGRAM_TEXLIT, PROGRAM_FLATQUAD, PROGRAM_MESHPC, PROGRAM_DISCARD, PROGRAM_NOPERSP, PROGRAM_POINTS, PROGRAM_FETCH, PROGRAM_MRT,
- PROGRAM_MRTI, PROGRAM_STORAGE, PROGRAM_SEPARATE, PROGRAM_MATHX, PROGRAM_CALLS) = range(14)
+ PROGRAM_MRTI, PROGRAM_STORAGE, PROGRAM_SEPARATE, PROGRAM_MATHX, PROGRAM_CALLS, PROGRAM_SSBO) = range(15)
 
 VK_FORMAT_D16_UNORM = 124
 VK_FORMAT_D32_SFLOAT = 126
@@ -50,7 +50,7 @@ class SceneHeader(ctypes.Structure):
                 ("texture_data", vp), ("texture_bytes", u64), ("texture_width", u32), ("texture_height", u32),
                 ("texture_levels", u32), ("texture_format", u32), ("sampler", SamplerDesc), ("num_pipelines", u32),
                 ("pipelines", vp), ("num_draws", u32), ("draws", vp), ("extra_color_count", u32), ("extra_color_formats", u32 * 7),
-                ("spec_lod", u32), ("texture_binding", u32)]
+                ("spec_lod", u32), ("texture_binding", u32), ("uniform_as_storage", u32)]
 
 
 class SceneDraw(ctypes.Structure):

@@ -660,6 +660,7 @@ VkResult create_scene_pass(cpvh_context* c, const cpv_scene* s, VkRenderPass* ou
 std::vector<VkDescriptorSetLayoutBinding> scene_bindings(const cpv_scene* s) {
     std::vector<VkDescriptorSetLayoutBinding> lb;
     if (s->uniform_bytes) lb.push_back({0, VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER, 1, VK_SHADER_STAGE_VERTEX_BIT | VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
+    if (s->uniform_bytes && s->uniform_as_storage) lb.push_back({3, VK_DESCRIPTOR_TYPE_STORAGE_BUFFER, 1, VK_SHADER_STAGE_FRAGMENT_BIT, nullptr});
     if (s->texture_data) {
         switch (s->texture_binding) {
         case CPV_TEXTURE_STORAGE: lb.push_back({1, VK_DESCRIPTOR_TYPE_STORAGE_IMAGE, 1, VK_SHADER_STAGE_FRAGMENT_BIT, nullptr}); break;
@@ -941,12 +942,12 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
     dli.bindingCount = static_cast<uint32_t>(lb.size());
     dli.pBindings = lb.data();
     if (f.vkCreateDescriptorSetLayout(c->device, &dli, nullptr, &r->set_layout) != VK_SUCCESS) return fail("set layout");
-    VkDescriptorPoolSize ps[5] = {{VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER, 1}, {VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER, 1}, {VK_DESCRIPTOR_TYPE_STORAGE_IMAGE, 1},
-                                  {VK_DESCRIPTOR_TYPE_SAMPLED_IMAGE, 1}, {VK_DESCRIPTOR_TYPE_SAMPLER, 1}};
+    VkDescriptorPoolSize ps[6] = {{VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER, 1}, {VK_DESCRIPTOR_TYPE_COMBINED_IMAGE_SAMPLER, 1}, {VK_DESCRIPTOR_TYPE_STORAGE_IMAGE, 1},
+                                  {VK_DESCRIPTOR_TYPE_SAMPLED_IMAGE, 1}, {VK_DESCRIPTOR_TYPE_SAMPLER, 1}, {VK_DESCRIPTOR_TYPE_STORAGE_BUFFER, 1}};
     VkDescriptorPoolCreateInfo dpi{};
     dpi.sType = VK_STRUCTURE_TYPE_DESCRIPTOR_POOL_CREATE_INFO;
     dpi.maxSets = 1;
-    dpi.poolSizeCount = 5;
+    dpi.poolSizeCount = 6;
     dpi.pPoolSizes = ps;
     if (f.vkCreateDescriptorPool(c->device, &dpi, nullptr, &r->pool) != VK_SUCCESS) return fail("descriptor pool");
     if (!lb.empty()) {
@@ -961,7 +962,7 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
         if (s->texture_binding == CPV_TEXTURE_STORAGE) dii = {VK_NULL_HANDLE, r->texture.view, VK_IMAGE_LAYOUT_GENERAL};
         if (s->texture_binding == CPV_TEXTURE_SEPARATE) dii.sampler = VK_NULL_HANDLE;
         const VkDescriptorImageInfo sampler_info{r->sampler, VK_NULL_HANDLE, VK_IMAGE_LAYOUT_UNDEFINED};
-        VkWriteDescriptorSet w[3]{};
+        VkWriteDescriptorSet w[4]{};
         uint32_t nw = 0;
         if (s->uniform_bytes) {
             w[nw].sType = VK_STRUCTURE_TYPE_WRITE_DESCRIPTOR_SET;
@@ -971,6 +972,15 @@ cpvh_renderer* cpvh_renderer_create(cpvh_context* c, const cpv_scene* s, char* e
             w[nw].descriptorType = VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER;
             w[nw].pBufferInfo = &dbi;
             nw++;
+            if (s->uniform_as_storage) {
+                w[nw].sType = VK_STRUCTURE_TYPE_WRITE_DESCRIPTOR_SET;
+                w[nw].dstSet = r->set;
+                w[nw].dstBinding = 3;
+                w[nw].descriptorCount = 1;
+                w[nw].descriptorType = VK_DESCRIPTOR_TYPE_STORAGE_BUFFER;
+                w[nw].pBufferInfo = &dbi;
+                nw++;
+            }
         }
         if (s->texture_data) {
             w[nw].sType = VK_STRUCTURE_TYPE_WRITE_DESCRIPTOR_SET;

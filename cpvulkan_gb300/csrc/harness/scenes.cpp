@@ -754,7 +754,8 @@ void build_program(Store& st, uint64_t seed, uint32_t program, uint32_t variant,
     uint64_t colour_offset = 0;
     if (program == CPV_PROGRAM_CUBE || program == CPV_PROGRAM_DISCARD || program == CPV_PROGRAM_NOPERSP || program == CPV_PROGRAM_POINTS ||
         program == CPV_PROGRAM_MRT || program == CPV_PROGRAM_MRTI || program == CPV_PROGRAM_MATHX ||
-        program == CPV_PROGRAM_CALLS) {
+        program == CPV_PROGRAM_CALLS || program == CPV_PROGRAM_SSBO) {
+        if (program == CPV_PROGRAM_SSBO) s.uniform_as_storage = 1;
         // Clip-space vertices with w in [0.5, 2] (positive, as the reference
         // requires), a shared-edge pair, and a zero-area triangle.
         st.uniform.resize(64);

@@ -309,7 +309,8 @@ VkResult build_draw(State& s, uint32_t count, uint32_t instances, uint32_t first
             }
             fill_texture(P.tex[slot.slot], d.view, sampler);
         } else if (d.buffer && d.buffer->memory) {
-            const uint64_t dyn = (d.type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC) ? dynamic_offset(s, slot.set, slot.binding) : 0;
+            const bool dynamic = d.type == VK_DESCRIPTOR_TYPE_UNIFORM_BUFFER_DYNAMIC || d.type == VK_DESCRIPTOR_TYPE_STORAGE_BUFFER_DYNAMIC;
+            const uint64_t dyn = dynamic ? dynamic_offset(s, slot.set, slot.binding) : 0;
             const uint64_t off = d.offset + dyn;
             uint64_t range = d.range == VK_WHOLE_SIZE ? (d.buffer->size > off ? d.buffer->size - off : 0) : d.range;
             if (off + range > d.buffer->size) range = d.buffer->size > off ? d.buffer->size - off : 0;

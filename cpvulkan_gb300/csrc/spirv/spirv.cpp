@@ -1041,8 +1041,14 @@ bool Translator::emit_globals(const EntryPoint& ep, StageResult& out) {
             break;
         }
         case SCUniform:
+        case SCStorageBuffer:
         case SCPushConstant: {
-            if (v.storage == SCUniform && m_.has_decoration(tid, DecBufferBlock)) return fail("storage buffers are not supported on the draw path");
+            // Storage buffers (StorageBuffer, or Uniform with BufferBlock) are
+            // read like uniform buffers, with explicit layout and bounds-checked
+            // loads (CPVulkan/CommandBuffer.Draw.cpp:379-395 binds both alike);
+            // stores through an explicit-layout pointer are rejected as writes
+            // to read-only memory: fragments run concurrently here and Vulkan
+            // leaves the order of their buffer writes undefined.
             info.kind = PtrInfo::Explicit;
             info.offset = "0ull";
             if (v.storage == SCPushConstant) {
@@ -1084,8 +1090,6 @@ bool Translator::emit_globals(const EntryPoint& ep, StageResult& out) {
             ptrs_[v.id] = info;
             break;
         }
-        case SCStorageBuffer:
-            return fail("storage buffers are not supported on the draw path");
         default:
             return fail("unsupported storage class " + std::to_string(v.storage));
         }
@@ -1226,7 +1230,8 @@ bool Translator::emit_instruction(const Instruction& ins, const std::map<uint32_
                     tid = t->members[k];
                     break;
                 }
-                case TypeKind::Array: {
+                case TypeKind::Array:
+                case TypeKind::RuntimeArray: {
                     uint32_t stride = 0;
                     if (!m_.decoration(tid, DecArrayStride, stride)) return fail("uniform array without ArrayStride");
                     p.offset = "(" + p.offset + " + (uint64_t)(" + value(ix) + ") * " + std::to_string(stride) + "ull)";

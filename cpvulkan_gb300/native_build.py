@@ -28,7 +28,7 @@ CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-un
             "-I" + os.path.join(CUDA, "include")]
 
 PROGRAMS = ["cube", "texlit", "flatquad", "meshpc", "discard", "nopersp", "points", "fetch", "mrt", "mrti", "storage",
-            "separate", "mathx", "calls"]  # index = cpv_program
+            "separate", "mathx", "calls", "ssbo"]  # index = cpv_program
 
 
 def _write_if_changed(path, text):

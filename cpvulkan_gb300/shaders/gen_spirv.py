@@ -25,10 +25,10 @@ OP = dict(
     Label=248, Branch=249, BranchConditional=250, Kill=252, Return=253, SpecConstant=50, SpecConstantOp=52,
     CopyMemory=63, ImageFetch=95, Image=100, ConvertFToS=110, ConvertSToF=111, IAdd=128, IMul=132, BitwiseXor=198,
     BitCount=205, ConvertFToU=109, Bitcast=124, TypeSampler=26, SampledImage=86, ImageRead=98, ISub=130,
-    FunctionParameter=55, FunctionCall=57, ReturnValue=254,
+    FunctionParameter=55, FunctionCall=57, ReturnValue=254, TypeRuntimeArray=29,
 )
 DEC = dict(SpecId=1, Block=2, ColMajor=5, MatrixStride=7, BuiltIn=11, NoPerspective=13, Flat=14, Location=30, Binding=33,
-           DescriptorSet=34, Offset=35)
+           DescriptorSet=34, Offset=35, BufferBlock=3, ArrayStride=6, NonWritable=24)
 SC = dict(UniformConstant=0, Input=1, Uniform=2, Output=3, Function=7, PushConstant=9)
 BUILTIN = dict(Position=0, PointSize=1, ClipDistance=3, CullDistance=4)
 GLSL = dict(FMax=40, Normalize=69, SSign=7, Reflect=71, FindILsb=73, FindSMsb=74, FindUMsb=75, NMin=79, NMax=80, NClamp=81)
@@ -628,6 +628,35 @@ def calls_frag():
     return m.assemble(body)
 
 
+def ssbo_frag():
+    """layout(std430, set=0, binding=3) readonly buffer Rows { vec4 rows[]; };
+    layout(location=0) in vec4 c; layout(location=0) out vec4 o;
+    void main() { o = c * rows[1]; }
+    (a storage buffer in SPIR-V 1.0 form: Uniform storage with BufferBlock,
+    a runtime array)"""
+    m = Module(4)
+    v4 = m.vec(4)
+    rarr = m._type(("rarr", v4), "TypeRuntimeArray", lambda: [v4])
+    m.decorate(rarr, "ArrayStride", 16)
+    st = m.struct("Rows", [rarr])
+    m.member_decorate(st, 0, "Offset", 0)
+    m.member_decorate(st, 0, "NonWritable")
+    m.decorate(st, "BufferBlock")
+    buf = m.variable("Uniform", st, "rows")
+    m.decorate(buf, "DescriptorSet", 0)
+    m.decorate(buf, "Binding", 3)
+    col = m.variable("Input", v4, "c")
+    m.decorate(col, "Location", 0)
+    out = m.variable("Output", v4, "o")
+    m.decorate(out, "Location", 0)
+
+    def body(m):
+        row = m.load(v4, m.access("Uniform", v4, buf, m.const_int(0), m.const_int(1)))
+        m.store(out, m.op("FMul", v4, m.load(v4, col), row))
+        m.op_void("Return")
+    return m.assemble(body)
+
+
 def mrt_frag():
     """layout(location=0) in vec4 c; layout(location=L) out vec4 oL (L = 0..7);
     void main() {
@@ -712,6 +741,7 @@ PROGRAMS = {
     "separate": (texlit_vert, separate_frag),
     "mathx": (cube_vert, mathx_frag),
     "calls": (cube_vert, calls_frag),
+    "ssbo": (cube_vert, ssbo_frag),
 }
 
 

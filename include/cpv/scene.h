@@ -47,7 +47,9 @@ enum cpv_program {
                                     FindSMsb/FindILsb/SSign/FindUMsb on integers from the colour, Reflect    */
     CPV_PROGRAM_CALLS = 13,      /* CUBE's vertex shader; FS: function calls (a pointer and a value parameter,
                                     a return value, a discard inside a called function)                      */
-    CPV_PROGRAM_COUNT = 14
+    CPV_PROGRAM_SSBO = 14,       /* CUBE's vertex shader; FS: colour × row 1 of a read-only storage buffer
+                                    (the uniform buffer bound again at binding 3, cpv_scene::uniform_as_storage) */
+    CPV_PROGRAM_COUNT = 15
 };
 
 /* How a scene's texture is bound (cpv_scene::texture_binding). */
@@ -180,6 +182,9 @@ typedef struct cpv_scene {
 
     /* cpv_texture_binding: the descriptors the texture is bound through */
     uint32_t texture_binding;
+
+    /* 1: the uniform buffer is also bound at binding 3 as a storage buffer */
+    uint32_t uniform_as_storage;
 } cpv_scene;
 
 #ifdef __cplusplus

@@ -365,7 +365,8 @@ ProgramInfo program_info(uint32_t program) {
     case CPV_PROGRAM_MRT:
     case CPV_PROGRAM_MRTI:
     case CPV_PROGRAM_MATHX:
-    case CPV_PROGRAM_CALLS: return {1, {4}, {INTERP_PERSPECTIVE}};
+    case CPV_PROGRAM_CALLS:
+    case CPV_PROGRAM_SSBO: return {1, {4}, {INTERP_PERSPECTIVE}};
     default: return {0, {0}, {INTERP_PERSPECTIVE}};
     }
 }
@@ -459,7 +460,8 @@ void run_vs(uint32_t program, const float attr[8][4], const Resources& r, VsOut&
     case CPV_PROGRAM_MRT:
     case CPV_PROGRAM_MRTI:
     case CPV_PROGRAM_MATHX:
-    case CPV_PROGRAM_CALLS: {
+    case CPV_PROGRAM_CALLS:
+    case CPV_PROGRAM_SSBO: {
         float m[16];
         for (int i = 0; i < 16; i++) m[i] = ubo_at(r, i);
         for (int i = 0; i < 4; i++) out.var[i] = attr[1][i];
@@ -551,6 +553,11 @@ bool run_fs(uint32_t program, const float* in, const Resources& r, float* colour
         for (int i = 16; i < 32; i++) colour[i] = 0.0f;
         return false;
     }
+    case CPV_PROGRAM_SSBO:
+        /* gen_spirv.py ssbo_frag: colour times row 1 (bytes 16-31) of the
+         * storage buffer, which is the uniform buffer bound again */
+        for (int i = 0; i < 4; i++) colour[i] = in[i] * ubo_at(r, 4 + i);
+        return false;
     case CPV_PROGRAM_CALLS: {
         /* gen_spirv.py calls_frag: scale() multiplies the variable it is
          * given by 0.5 and returns its x + 0.5; check() discards when y > 0.45 */

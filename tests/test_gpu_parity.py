@@ -454,3 +454,16 @@ def test_function_calls_program(gpu_ctx, oracle, monkeypatch, variant, mode):
     assert 0 < stats["fragments_written"] < stats["fragments"]
     assert report["color_pixels_differing"] == 0, report
 
+
+# A read-only storage buffer (Uniform storage with BufferBlock, a runtime
+# array; bound as STORAGE_BUFFER): the uniform buffer bound again at
+# binding 3, its row 1 multiplying the colour.
+@pytest.mark.parametrize("batched", [False, True])
+def test_storage_buffer_program(gpu_ctx, oracle, monkeypatch, batched):
+    if batched:
+        monkeypatch.setenv("CPV_BATCH_MIN_DRAWS", "1")
+    scene = c.Scene(c.PROGRAM, 7, [c.PROGRAM_SSBO, 0x10 | 0x20, 64, 48, 24])
+    report, stats = check(gpu_ctx, oracle, scene)
+    assert stats["fragments_written"] > 0
+    assert report["color_pixels_differing"] == 0, report
+

@@ -334,3 +334,14 @@ def test_function_calls_translate(compile_ctx):
     assert text.count("= [&](") == 2
     assert "cvec<float, 4>& v" in text and "cpv_killed = true;" in text and "if (cpv_killed) return true;" in text
 
+
+def test_storage_buffer_reads_translate(compile_ctx):
+    """A read-only storage buffer (BufferBlock, runtime array) is read with
+    the uniform buffers' bounds-checked explicit-layout loads, from its own
+    buffer slot."""
+    ctx, dump = compile_ctx
+    ctx.compile_pipelines(c.Scene(c.PROGRAM, 1, [c.PROGRAM_SSBO, 0x10, 32, 32, 4]))
+    (path,) = glob.glob(str(dump / "pipeline_*.cu"))
+    text = open(path).read()
+    assert "P.ubo[1], P.ubo_bytes[1]" in text
+
